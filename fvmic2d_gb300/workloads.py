@@ -1,0 +1,290 @@
+"""Seeded synthetic workloads for the marker-in-cell transfer path.
+
+No public dataset exists for this path; every input is generated here from a
+SplitMix64 stream so that the CPU oracle, the reference build and the GPU see
+identical arrays.  Marker placement follows fvmic2d's
+``distributeMarkersUniformInDomain`` (markers.c:342-400): a domain-uniform
+lattice of NMX*(NX-1) by NMY*(NY-1) markers, each jittered by U(-d/4, d/4) per
+axis, stored x-major (lattice column outer, row inner), so the initial array is
+not in cell order.  Cell centres follow ``getCellCenters`` (gridSpacing.c:150-157).
+
+Nodal inputs that the host Stokes / thermal solves would produce (vx, vy, p,
+strain rates, vorticity, nodal stresses and stress changes, the new
+temperature) are sampled from a prescribed divergence-free velocity field.
+"""
+from dataclasses import dataclass, field
+import math
+
+import numpy as np
+
+from .mic_types import MARKER_DTYPE, Materials, Options, BCs
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def splitmix64_uniform(seed, n, offset=0):
+    """n uniforms in [0,1) from SplitMix64 (Steele, Lea & Flood 2014), stream position offset.."""
+    with np.errstate(over="ignore"):
+        i = np.arange(offset + 1, offset + n + 1, dtype=np.uint64)
+        z = np.uint64(seed) + i * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def spacing_uniform(xmin, xmax, n):
+    """gridSpacingUniform (gridSpacing.c:8-17): running sum of a constant step."""
+    x = np.empty(n)
+    dx = (xmax - xmin) / (n - 1.0)
+    x[0] = xmin
+    acc = xmin
+    for i in range(1, n - 1):
+        acc = acc + dx
+        x[i] = acc
+    x[n - 1] = xmax
+    return x
+
+
+def cell_centers(x, L):
+    n = len(x)
+    xc = np.empty(n + 1)
+    xc[1:n] = (x[:-1] + x[1:]) / 2.0
+    xc[0] = -xc[1]
+    xc[n] = 2.0 * L - xc[n - 1]
+    return xc
+
+
+@dataclass
+class Grid:
+    NX: int
+    NY: int
+    LX: float
+    LY: float
+    x: np.ndarray
+    y: np.ndarray
+
+    def __post_init__(self):
+        self.x = np.ascontiguousarray(self.x, dtype=np.float64)
+        self.y = np.ascontiguousarray(self.y, dtype=np.float64)
+        self.xc = cell_centers(self.x, self.LX)
+        self.yc = cell_centers(self.y, self.LY)
+
+    @property
+    def ncells(self):
+        return (self.NX - 1) * (self.NY - 1)
+
+
+@dataclass
+class Workload:
+    name: str
+    grid: Grid
+    markers: np.ndarray
+    materials: Materials
+    options: Options
+    bcs: BCs
+    nodal: dict = field(default_factory=dict)
+    dt: float = 0.0            # displacement time step (stress update, subgrid stress)
+    dt_thermal: float = 0.0    # thermal time step (subgrid temperature, advection)
+    steps: int = 1
+    grain_size: np.ndarray = None  # per-marker grain size (composite creep workloads)
+
+
+def lattice_markers(grid, nmx, nmy, seed):
+    """Domain-uniform jittered lattice in x-major order (markers.c:369-395)."""
+    mdx = grid.LX / (nmx * (grid.NX - 1))
+    mdy = grid.LY / (nmy * (grid.NY - 1))
+    nk = int((grid.x[-1] - grid.x[0]) / mdx + 1e-9)
+    nl = int((grid.y[-1] - grid.y[0]) / mdy + 1e-9)
+    n = nk * nl
+    u = splitmix64_uniform(seed, 2 * n)
+    k = np.repeat(np.arange(nk, dtype=np.float64), nl)
+    l = np.tile(np.arange(nl, dtype=np.float64), nk)
+    m = np.zeros(n, dtype=MARKER_DTYPE)
+    m["X"] = grid.x[0] + mdx * (0.5 + k) + (-mdx / 4.0 + (mdx / 2.0) * u[0::2])
+    m["Y"] = grid.y[0] + mdy * (0.5 + l) + (-mdy / 4.0 + (mdy / 2.0) * u[1::2])
+    m["Mat"] = 0
+    m["cellX"] = -1
+    m["cellY"] = -1
+    return m
+
+
+def _materials(n):
+    mat = Materials()
+    mat.nMaterials = n
+    return mat
+
+
+def _free_slip():
+    b = BCs()
+    for side in (b.mechBCLeft, b.mechBCRight, b.mechBCTop, b.mechBCBottom):
+        for c in range(3):
+            side.type[c] = 1
+            side.value[c] = 0.0
+    return b
+
+
+def _eta_law(mat, m):
+    """computeRheology (viscosity.c:12-67) for hasEtaT in {0, 1, 5}, vectorised; clamp done by caller."""
+    eta = np.empty(len(m))
+    for k in range(mat.nMaterials):
+        sel = m["Mat"] == k
+        law = mat.hasEtaT[k]
+        if law == 0:
+            eta[sel] = mat.materialEta[k]
+        elif law == 1:
+            eta[sel] = mat.materialEta[k] * np.exp(mat.QonR[k] * (1.0 / m["T"][sel] - 1.0 / mat.Tref[k]))
+        elif law == 5:
+            eta[sel] = mat.materialEta[k] * np.exp(-mat.QonR[k] * m["T"][sel])
+        else:
+            raise ValueError("unsupported law in generator")
+    return eta
+
+
+def _velocity_fields(grid, vx_fn, vy_fn, dvx, dvy):
+    """Sample vx at (x[i], yc[j+1]), vy at (xc[i+1], y[j]) (markers.c:1978-1984, 2026-2029),
+    strain rates / vorticity at cell centres (xx, yy) and basic nodes (xy, wxy)."""
+    X, YC = np.meshgrid(grid.x, grid.yc[1:], indexing="xy")
+    XC, Y = np.meshgrid(grid.xc[1:], grid.y, indexing="xy")
+    vx = vx_fn(X, YC)
+    vy = vy_fn(XC, Y)
+    XCc, YCc = np.meshgrid(grid.xc[: grid.NX], grid.yc[: grid.NY], indexing="xy")
+    Xb, Yb = np.meshgrid(grid.x, grid.y, indexing="xy")
+    exx = dvx["x"](XCc, YCc)
+    eyy = dvy["y"](XCc, YCc)
+    exy = 0.5 * (dvx["y"](Xb, Yb) + dvy["x"](Xb, Yb))
+    wxy = 0.5 * (dvx["y"](Xb, Yb) - dvy["x"](Xb, Yb))
+    return vx, vy, exx, eyy, exy, wxy
+
+
+def convection_box(ncell=64, nm=4, seed=1, U=100.0):
+    """Unit-square thermal convection, viscosity exp(-ln(1000) T) (hasEtaT 5), free slip,
+    T0 = 1 - y + 0.01 cos(pi x) sin(pi y); 65x65 nodes and 65,536 markers at full size."""
+    NX = NY = ncell + 1
+    g = Grid(NX, NY, 1.0, 1.0, spacing_uniform(0.0, 1.0, NX), spacing_uniform(0.0, 1.0, NY))
+    m = lattice_markers(g, nm, nm, seed)
+    m["T"] = 1.0 - m["Y"] + 0.01 * np.cos(np.pi * m["X"]) * np.sin(np.pi * m["Y"])
+    mat = _materials(1)
+    mat.materialEta[0] = 1.0
+    mat.materialRho[0] = 1.0
+    mat.materialkThermal[0] = 1.0
+    mat.materialCp[0] = 1.0
+    mat.materialAlpha[0] = 1.0
+    mat.materialMu[0] = 1e20
+    mat.hasEtaT[0] = 5
+    mat.QonR[0] = math.log(1000.0)
+    mat.Tref[0] = 1.0
+    opt = Options(etamin=1e-3, etamax=1e3, fractionalEtamin=0.01, subgridStressDiffusivity=0.0,
+                  subgridTemperatureDiffusivity=1.0)
+    m["mu"] = mat.materialMu[0]
+    m["eta"] = _eta_law(mat, m)
+    pi = np.pi
+    vx_fn = lambda x, y: U * pi * np.sin(pi * x) * np.cos(pi * y)
+    vy_fn = lambda x, y: -U * pi * np.cos(pi * x) * np.sin(pi * y)
+    dvx = {"x": lambda x, y: U * pi * pi * np.cos(pi * x) * np.cos(pi * y),
+           "y": lambda x, y: -U * pi * pi * np.sin(pi * x) * np.sin(pi * y)}
+    dvy = {"x": lambda x, y: U * pi * pi * np.sin(pi * x) * np.sin(pi * y),
+           "y": lambda x, y: -U * pi * pi * np.cos(pi * x) * np.cos(pi * y)}
+    vx, vy, exx, eyy, exy, wxy = _velocity_fields(g, vx_fn, vy_fn, dvx, dvy)
+    ex_m = dvx["x"](m["X"], m["Y"])
+    m["exx"] = ex_m
+    m["eyy"] = -ex_m
+    m["exy"] = 0.0
+    m["sxx"] = 2.0 * m["eta"] * m["exx"]
+    m["syy"] = -m["sxx"]
+    XCc, YCc = np.meshgrid(g.xc[:NX], g.yc[:NY], indexing="xy")
+    Xb, Yb = np.meshgrid(g.x, g.y, indexing="xy")
+    Tn = 1.0 - Yb + 0.01 * np.cos(pi * Xb) * np.sin(pi * Yb)
+    eta_c = np.exp(-math.log(1000.0) * np.clip(1.0 - YCc, 0.0, 1.0))
+    nodal = {
+        "vx": vx, "vy": vy, "edotxx": exx, "edotyy": eyy, "edotxy": exy, "wxy": wxy,
+        "p": np.zeros((NY, NX)),
+        "soxx": 2.0 * eta_c * exx, "soyy": 2.0 * eta_c * eyy, "soxy": np.zeros((NY, NX)),
+        "thisT": Tn + 1e-3 * np.sin(pi * Xb) * np.sin(pi * Yb),
+    }
+    nodal["dsxx"] = 0.05 * nodal["soxx"]
+    nodal["dsyy"] = 0.05 * nodal["soyy"]
+    nodal["dsxy"] = 0.05 * exy
+    dt = 0.5 * (1.0 / ncell) / (U * pi)
+    return Workload("convection_box", g, m, mat, opt, _free_slip(), nodal, dt, dt, 10)
+
+
+def refined_top_y(LY, ny_cells, top_fraction=0.2):
+    """y gridlines with the top `top_fraction` of the box at about twice the resolution."""
+    n_top = max(1, min(ny_cells - 1, int(round(ny_cells * 2.0 * top_fraction / (1.0 + top_fraction)))))
+    n_bot = ny_cells - n_top
+    y_top = spacing_uniform(0.0, top_fraction * LY, n_top + 1)
+    y_bot = spacing_uniform(top_fraction * LY, LY, n_bot + 1)
+    return np.concatenate([y_top, y_bot[1:]])
+
+
+def vep_slab_box(nx_cells=1024, ny_cells=256, nm=4, seed=2):
+    """Visco-elasto-plastic two-material 4:1 box: dense slab rectangle (material 1, Mohr-Coulomb
+    yield C + F p) in a lighter Arrhenius mantle (material 0); eta clamped to [1e19, 1e23] Pa s,
+    shear modulus 1e10 Pa; y spacing about 2x finer in the top 20 %.  At full size
+    1025 x 257 nodes and 4,194,304 markers."""
+    NX, NY = nx_cells + 1, ny_cells + 1
+    LX, LY = 4.0e5, 1.0e5
+    g = Grid(NX, NY, LX, LY, spacing_uniform(0.0, LX, NX), refined_top_y(LY, ny_cells))
+    m = lattice_markers(g, nm, nm, seed)
+    u = splitmix64_uniform(seed + 1000, len(m))
+    X, Y = m["X"], m["Y"]
+    slab = (X > 0.35 * LX) & (X < 0.65 * LX) & (Y > 0.05 * LY) & (Y < 0.35 * LY)
+    m["Mat"] = np.where(slab, 1, 0)
+    Tgeo = 273.0 + 1300.0 * np.minimum(1.0, Y / (0.4 * LY))
+    m["T"] = np.where(slab, 273.0 + 0.5 * (Tgeo - 273.0), Tgeo) + 5.0 * (u - 0.5)
+    mat = _materials(2)
+    for k, (eta, rho) in enumerate([(1e21, 3300.0), (1e23, 3400.0)]):
+        mat.materialEta[k] = eta
+        mat.materialRho[k] = rho
+        mat.materialkThermal[k] = 3.0
+        mat.materialCp[k] = 1250.0
+        mat.materialAlpha[k] = 3e-5
+        mat.materialMu[k] = 1e10
+        mat.Tref[k] = 1573.0
+    mat.hasEtaT[0] = 1
+    mat.QonR[0] = 2.0e4
+    mat.hasEtaT[1] = 0
+    mat.hasPlasticity[1] = 1
+    mat.materialCohesion[1] = 2e7
+    mat.materialFriction[1] = 0.6
+    opt = Options(etamin=1e19, etamax=1e23, fractionalEtamin=0.1, subgridStressDiffusivity=1.0,
+                  subgridTemperatureDiffusivity=1.0)
+    edot, gdot = 1e-15, 4e-16
+    A = 0.3 * edot * LX * LY / np.pi
+    pi = np.pi
+    vx_fn = lambda x, y: edot * (x - LX / 2) + gdot * (y - LY / 2) + A * pi / LY * np.sin(pi * x / LX) * np.cos(pi * y / LY)
+    vy_fn = lambda x, y: -edot * (y - LY / 2) - A * pi / LX * np.cos(pi * x / LX) * np.sin(pi * y / LY)
+    dvx = {"x": lambda x, y: edot + A * pi * pi / (LX * LY) * np.cos(pi * x / LX) * np.cos(pi * y / LY),
+           "y": lambda x, y: gdot - A * pi * pi / (LY * LY) * np.sin(pi * x / LX) * np.sin(pi * y / LY)}
+    dvy = {"x": lambda x, y: A * pi * pi / (LX * LX) * np.sin(pi * x / LX) * np.sin(pi * y / LY),
+           "y": lambda x, y: -edot - A * pi * pi / (LX * LY) * np.cos(pi * x / LX) * np.cos(pi * y / LY)}
+    vx, vy, exx, eyy, exy, wxy = _velocity_fields(g, vx_fn, vy_fn, dvx, dvy)
+    m["mu"] = 1e10
+    m["eta"] = np.clip(_eta_law(mat, m), opt.etamin, opt.etamax)
+    m["exx"] = dvx["x"](X, Y)
+    m["eyy"] = dvy["y"](X, Y)
+    m["exy"] = 0.5 * (dvx["y"](X, Y) + dvy["x"](X, Y))
+    m["sxx"] = 2.0 * m["eta"] * m["exx"]
+    m["syy"] = 2.0 * m["eta"] * m["eyy"]
+    m["sxy"] = 2.0 * m["eta"] * m["exy"]
+    m["p"] = 3300.0 * 9.8 * Y
+    XCc, YCc = np.meshgrid(g.xc[:NX], g.yc[:NY], indexing="xy")
+    Xb, Yb = np.meshgrid(g.x, g.y, indexing="xy")
+    eta_ref = 1e21
+    nodal = {
+        "vx": vx, "vy": vy, "edotxx": exx, "edotyy": eyy, "edotxy": exy, "wxy": wxy,
+        "p": 3300.0 * 9.8 * YCc,
+        "soxx": 2.0 * eta_ref * exx, "soyy": 2.0 * eta_ref * eyy, "soxy": 2.0 * eta_ref * exy,
+        "thisT": 273.0 + 1300.0 * np.minimum(1.0, Yb / (0.4 * LY)) + 2.0 * np.sin(pi * Xb / LX) * np.sin(pi * Yb / LY),
+    }
+    nodal["dsxx"] = 0.05 * nodal["soxx"]
+    nodal["dsyy"] = 0.05 * nodal["soyy"]
+    nodal["dsxy"] = 0.05 * nodal["soxy"]
+    vmax = float(np.max(np.abs(vx))) + float(np.max(np.abs(vy)))
+    dmin = min(float(np.min(np.diff(g.x))), float(np.min(np.diff(g.y))))
+    dt = 0.5 * dmin / vmax
+    return Workload("vep_slab_box", g, m, mat, opt, _free_slip(), nodal, dt, dt, 20)
+
+
+WORKLOADS = {"convection_box": convection_box, "vep_slab_box": vep_slab_box}

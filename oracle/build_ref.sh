@@ -1,0 +1,34 @@
+#!/bin/sh
+# Builds oracle/_ref/libfvmic2d_ref.so from fvmic2d's OWN hot-path sources, compiled
+# in place (read-only) from the reference tree against the single-rank petsc_lite
+# stand-in.  Test infrastructure only: the library pins the project's C
+# restatement (oracle/mic_oracle.c) and generates the golden vectors under
+# tests/golden/.  Nothing is copied out of the reference tree.
+#
+# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default: /root/reference)
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-/root/reference}
+OUT="$HERE/_ref"
+if [ ! -f "$REF/markerProjection.c" ]; then
+  echo "reference sources not found under $REF; oracle/_ref not built" >&2
+  exit 3
+fi
+mkdir -p "$OUT"
+CC=${CC:-gcc}
+# -ffp-contract=off: no fused multiply-add, so results do not depend on the host ISA.
+CFLAGS="-O2 -fPIC -std=gnu99 -ffp-contract=off -fno-fast-math -w"
+INC="-I$HERE/petsc_lite/include -I$REF -I$HERE/../include"
+SRCS="markers.c markerProjection.c updateMarkerStrainPressure.c subgridStressChanges.c updateMarkerStress.c \
+subgridTemperatureChanges.c viscosity.c residual.c benchmarkInitialConditions.c gridSpacing.c profile.c"
+OBJS=""
+for s in $SRCS; do
+  o="$OUT/$(basename "$s" .c).o"
+  $CC $CFLAGS $INC -c "$REF/$s" -o "$o"
+  OBJS="$OBJS $o"
+done
+$CC $CFLAGS $INC -c "$HERE/petsc_lite/petsc_lite.c" -o "$OUT/petsc_lite.o"
+$CC $CFLAGS $INC -c "$HERE/ref_bridge.c" -o "$OUT/ref_bridge.o"
+$CC -shared -o "$OUT/libfvmic2d_ref.so" $OBJS "$OUT/petsc_lite.o" "$OUT/ref_bridge.o" -lm
+rm -f "$OUT"/*.o
+echo "built $OUT/libfvmic2d_ref.so"

@@ -1,0 +1,902 @@
+/*
+ * mic_oracle.c -- CPU restatement of fvmic2d's marker-in-cell transfer path.
+ * TEST INFRASTRUCTURE ONLY (see mic_oracle.h).  Reference citations are
+ * file:line in the fvmic2d tree.
+ *
+ * Single-rank DMDA semantics restated here: scatter-adds that land on a node
+ * index NX or NY (the ghost column/row of a ghosted, non-periodic DMDA) are
+ * dropped; a zero weight sum divides to zero (VecPointwiseDivide with a guarded
+ * divisor); ghost values are never read because boundary types other than
+ * prescribed (0) and free slip (1) are rejected.
+ */
+#include "mic_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct orc_ctx {
+  int NX, NY;
+  double LX, LY;
+  double *buf;
+  double *x, *y, *xc, *yc; /* ghost offset 2 */
+  mic_materials mat;
+  mic_options opt;
+  mic_bcs bcs;
+  double *nodal[MIC_NF_COUNT];
+  double *scratch;         /* per-marker scratch (subgrid temperature change) */
+  int64_t scratch_n;
+  double residuals[100];   /* residual.c:9-10 ring of stored residuals */
+};
+
+#define NODE(c, f, i, j) ((c)->nodal[f][(size_t)(j) * (size_t)(c)->NX + (size_t)(i)])
+
+orc_ctx *orc_create(int NX, int NY, double LX, double LY, const double *x, const double *y) {
+  if (NX < 3 || NY < 3) return NULL;
+  orc_ctx *c = (orc_ctx *)calloc(1, sizeof(orc_ctx));
+  if (!c) return NULL;
+  c->NX = NX;
+  c->NY = NY;
+  c->LX = LX;
+  c->LY = LY;
+  size_t nx4 = (size_t)NX + 4, ny4 = (size_t)NY + 4;
+  c->buf = (double *)malloc((2 * nx4 + 2 * ny4) * sizeof(double));
+  for (size_t k = 0; k < 2 * nx4 + 2 * ny4; ++k) c->buf[k] = NAN;
+  c->x = c->buf + 2;
+  c->xc = c->buf + nx4 + 2;
+  c->y = c->buf + 2 * nx4 + 2;
+  c->yc = c->buf + 2 * nx4 + ny4 + 2;
+  for (int i = 0; i < NX; ++i) c->x[i] = x[i];
+  for (int j = 0; j < NY; ++j) c->y[j] = y[j];
+  /* getCellCenters (gridSpacing.c:150-157) */
+  for (int i = 1; i < NX; ++i) c->xc[i] = (c->x[i - 1] + c->x[i]) / 2.0;
+  c->xc[0] = -c->xc[1];
+  c->xc[NX] = 2.0 * LX - c->xc[NX - 1];
+  for (int j = 1; j < NY; ++j) c->yc[j] = (c->y[j - 1] + c->y[j]) / 2.0;
+  c->yc[0] = -c->yc[1];
+  c->yc[NY] = 2.0 * LY - c->yc[NY - 1];
+  for (int f = 0; f < MIC_NF_COUNT; ++f) c->nodal[f] = (double *)calloc((size_t)NX * NY, sizeof(double));
+  for (int b = 0; b < 4; ++b) {
+    mic_bcinfo *s = &((mic_bcinfo *)&c->bcs)[b];
+    for (int k = 0; k < 3; ++k) s->type[k] = 1;
+  }
+  return c;
+}
+
+void orc_destroy(orc_ctx *c) {
+  if (!c) return;
+  for (int f = 0; f < MIC_NF_COUNT; ++f) free(c->nodal[f]);
+  free(c->scratch);
+  free(c->buf);
+  free(c);
+}
+
+void orc_get_grid(const orc_ctx *c, double *xc, double *yc) {
+  for (int i = 0; i <= c->NX; ++i) xc[i] = c->xc[i];
+  for (int j = 0; j <= c->NY; ++j) yc[j] = c->yc[j];
+}
+
+void orc_set_materials(orc_ctx *c, const mic_materials *m) { c->mat = *m; }
+void orc_set_options(orc_ctx *c, const mic_options *o) { c->opt = *o; }
+
+int orc_set_bcs(orc_ctx *c, const mic_bcs *b) {
+  /* markers.c:1986-2023 reads ghost velocities unless the top vx / left vy boundary is 0 or 1 */
+  if (b->mechBCTop.type[0] != 0 && b->mechBCTop.type[0] != 1) return ORC_ERR_BC;
+  if (b->mechBCLeft.type[1] != 0 && b->mechBCLeft.type[1] != 1) return ORC_ERR_BC;
+  c->bcs = *b;
+  return ORC_OK;
+}
+
+int orc_set_nodal(orc_ctx *c, int f, const double *v) {
+  if (f < 0 || f >= MIC_NF_COUNT) return ORC_ERR_ARG;
+  memcpy(c->nodal[f], v, sizeof(double) * (size_t)c->NX * c->NY);
+  return ORC_OK;
+}
+
+int orc_get_nodal(const orc_ctx *c, int f, double *v) {
+  if (f < 0 || f >= MIC_NF_COUNT) return ORC_ERR_ARG;
+  memcpy(v, c->nodal[f], sizeof(double) * (size_t)c->NX * c->NY);
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+/* cell location                                                              */
+
+/* Largest i in [0, n-2] with g[i] <= v, by bisection (markers.c:47-69). */
+static int bisect_cell(const double *g, int n, double v) {
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) / 2;
+    if (v >= g[mid])
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+/* findMarkerCell / findMarkerCells (markers.c:41-106) */
+int64_t orc_find_marker_cells(orc_ctx *c, mic_marker *mk, int64_t n, int *err) {
+  int64_t nout = 0;
+  *err = ORC_OK;
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->X >= 0.0 && p->Y >= 0.0 && p->X <= c->LX && p->Y <= c->LY) {
+      p->cellX = bisect_cell(c->x, c->NX, p->X);
+      p->cellY = bisect_cell(c->y, c->NY, p->Y);
+      if (p->cellX < 0 || p->cellX > c->NX - 2 || p->cellY < 0 || p->cellY > c->NY - 2) *err = ORC_ERR_CELL;
+    } else {
+      p->cellX = -1;
+      p->cellY = -1;
+    }
+    p->cpu = 0;
+    if (p->cellX == -1) nout++;
+  }
+  return nout;
+}
+
+/* main_subduction.c:255-264 */
+void orc_update_marker_rho(orc_ctx *c, mic_marker *mk, int64_t n) {
+  for (int64_t m = 0; m < n; ++m) {
+    if (mk[m].cellX == -1) continue;
+    int k = mk[m].Mat;
+    mk[m].rho = -c->mat.materialRho[k] * (c->mat.materialAlpha[k] * mk[m].T);
+    mk[m].rhodot = 0.0;
+  }
+}
+
+/* main_subduction.c:271-281 */
+double orc_max_marker_T(const orc_ctx *c, const mic_marker *mk, int64_t n) {
+  (void)c;
+  double t = 0.0;
+  for (int64_t m = 0; m < n; ++m)
+    if (mk[m].cellX != -1 && mk[m].T > t) t = mk[m].T;
+  return t;
+}
+
+/* main_subduction.c:437-448 */
+double orc_max_abs_sxx(const orc_ctx *c, const mic_marker *mk, int64_t n) {
+  (void)c;
+  double s = 0.0;
+  for (int64_t m = 0; m < n; ++m)
+    if (mk[m].cellX != -1 && fabs(mk[m].s.T11) > s) s = fabs(mk[m].s.T11);
+  return s;
+}
+
+/* ------------------------------------------------------------------------- */
+/* marker -> node projection                                                  */
+
+static double field_at(const mic_marker *m, int off) { return *(const double *)((const char *)m + off); }
+
+/* Staggered cell (findCellStag2D, markerProjection.c:252-269) and the fractional
+ * offsets of markerProjection.c:127-154. */
+static void stag_cell(const orc_ctx *c, const mic_marker *p, int stagx, int stagy, int *cx, int *cy, double *mdx,
+                      double *mdy) {
+  int i = p->cellX, j = p->cellY;
+  if (stagx == 1) {
+    if (p->X < c->xc[p->cellX + 1]) i--;
+  } else if (stagx == -1) {
+    if (p->X >= c->xc[p->cellX + 1]) i++;
+  }
+  if (stagy == 1) {
+    if (p->Y < c->yc[p->cellY + 1]) j--;
+  } else if (stagy == -1) {
+    if (p->Y >= c->yc[p->cellY + 1]) j++;
+  }
+  if (stagx == -1)
+    *mdx = (p->X - c->xc[i]) / (c->xc[i + 1] - c->xc[i]);
+  else if (stagx == 0)
+    *mdx = (p->X - c->x[i]) / (c->x[i + 1] - c->x[i]);
+  else
+    *mdx = (p->X - c->xc[i + 1]) / (c->xc[i + 2] - c->xc[i + 1]);
+  if (stagy == -1)
+    *mdy = (p->Y - c->yc[j]) / (c->yc[j + 1] - c->yc[j]);
+  else if (stagy == 0)
+    *mdy = (p->Y - c->y[j]) / (c->y[j + 1] - c->y[j]);
+  else
+    *mdy = (p->Y - c->yc[j + 1]) / (c->yc[j + 2] - c->yc[j + 1]);
+  *cx = i;
+  *cy = j;
+}
+
+/* accumulate into an interior node; node index NX or NY is a ghost of the DMDA and is dropped */
+static inline void acc2(double *nf, double *wt, int NX, int NY, int i, int j, double w, double v) {
+  if (i < 0 || j < 0 || i >= NX || j >= NY) return;
+  size_t k = (size_t)j * NX + i;
+  nf[k] += w * v;
+  wt[k] += w;
+}
+
+/* projectMarkerFieldToNodes (markerProjection.c:71-250) */
+int orc_project_marker_field(orc_ctx *c, const mic_marker *mk, int64_t n, int field_offset, const double *matprop,
+                             int out_field, int stagx, int stagy, int method) {
+  if (out_field < 0 || out_field >= MIC_NF_COUNT) return ORC_ERR_ARG;
+  if (stagx < -1 || stagx > 1 || stagy < -1 || stagy > 1) return ORC_ERR_ARG;
+  if (method != MIC_ARITHMETIC && method != MIC_ARITHMETIC_LOCAL && method != MIC_HARMONIC) return ORC_ERR_ARG;
+  const int NX = c->NX, NY = c->NY;
+  const size_t nn = (size_t)NX * NY;
+  double *nf = (double *)calloc(nn, sizeof(double));
+  double *wt = (double *)calloc(nn, sizeof(double));
+  for (int64_t m = 0; m < n; ++m) {
+    const mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    const double v = matprop ? matprop[p->Mat] : field_at(p, field_offset);
+    int i, j;
+    double mdx, mdy;
+    stag_cell(c, p, stagx, stagy, &i, &j, &mdx, &mdy);
+    if (method == MIC_ARITHMETIC) {
+      acc2(nf, wt, NX, NY, i, j, (1.0 - mdx) * (1.0 - mdy), v);
+      acc2(nf, wt, NX, NY, i + 1, j, mdx * (1.0 - mdy), v);
+      acc2(nf, wt, NX, NY, i, j + 1, (1.0 - mdx) * (mdy), v);
+      acc2(nf, wt, NX, NY, i + 1, j + 1, mdx * mdy, v);
+    } else if (method == MIC_ARITHMETIC_LOCAL) {
+      double w = 1.0;
+      if (mdx >= 0.5) {
+        i++;
+        w *= mdx;
+      } else {
+        w *= (1.0 - mdx);
+      }
+      if (mdy >= 0.5) {
+        j++;
+        w *= mdy;
+      } else {
+        w *= (1.0 - mdy);
+      }
+      acc2(nf, wt, NX, NY, i, j, w, v);
+    } else {
+      if (mdx >= 0.5) i++;
+      if (mdy >= 0.5) j++;
+      if (i < NX && j < NY) {
+        nf[(size_t)j * NX + i] += 1.0 / v;
+        wt[(size_t)j * NX + i] += 1.0;
+      }
+    }
+  }
+  double *out = c->nodal[out_field];
+  for (size_t k = 0; k < nn; ++k) {
+    double a = 0.0 + nf[k], b = 0.0 + wt[k];
+    if (method == MIC_HARMONIC)
+      out[k] = (a != 0.0) ? b / a : 0.0;
+    else
+      out[k] = (b != 0.0) ? a / b : 0.0;
+  }
+  free(nf);
+  free(wt);
+  return ORC_OK;
+}
+
+/* projectMarkersNodesAll2 (markerProjection.c:11-68) */
+int orc_project_markers_nodes_all2(orc_ctx *c, const mic_marker *mk, int64_t n) {
+  const int o_rho = (int)offsetof(mic_marker, rho), o_eta = (int)offsetof(mic_marker, eta);
+  const int o_T = (int)offsetof(mic_marker, T);
+  const int o_s11 = (int)offsetof(mic_marker, s.T11), o_s22 = (int)offsetof(mic_marker, s.T22);
+  const int o_s12 = (int)offsetof(mic_marker, s.T12);
+  int e = 0;
+  e |= orc_project_marker_field(c, mk, n, o_rho, NULL, MIC_NF_RHO, 0, 0, MIC_ARITHMETIC);
+  memset(c->nodal[MIC_NF_RHODOT], 0, sizeof(double) * (size_t)c->NX * c->NY);
+  e |= orc_project_marker_field(c, mk, n, o_eta, NULL, MIC_NF_ETAN, -1, -1, MIC_ARITHMETIC);
+  e |= orc_project_marker_field(c, mk, n, o_eta, NULL, MIC_NF_ETAS, 0, 0, MIC_ARITHMETIC);
+  for (size_t k = 0; k < (size_t)c->NX * c->NY; ++k) {
+    c->nodal[MIC_NF_MUS][k] = 1e99;
+    c->nodal[MIC_NF_MUN][k] = 1e99;
+  }
+  e |= orc_project_marker_field(c, mk, n, -1, c->mat.materialkThermal, MIC_NF_KTHERMAL, 0, 0, MIC_ARITHMETIC);
+  e |= orc_project_marker_field(c, mk, n, o_T, NULL, MIC_NF_LASTT, 0, 0, MIC_ARITHMETIC);
+  e |= orc_project_marker_field(c, mk, n, -1, c->mat.materialCp, MIC_NF_CP, 0, 0, MIC_ARITHMETIC);
+  e |= orc_project_marker_field(c, mk, n, o_s11, NULL, MIC_NF_SOXX, -1, -1, MIC_ARITHMETIC_LOCAL);
+  e |= orc_project_marker_field(c, mk, n, o_s22, NULL, MIC_NF_SOYY, -1, -1, MIC_ARITHMETIC_LOCAL);
+  e |= orc_project_marker_field(c, mk, n, o_s12, NULL, MIC_NF_SOXY, 0, 0, MIC_ARITHMETIC_LOCAL);
+  return e ? ORC_ERR_ARG : ORC_OK;
+}
+
+/* projectNodalFieldToMarkersS (markers.c:1670-1706): basic-node bilinear value */
+int orc_project_nodal_to_markers(orc_ctx *c, mic_marker *mk, int64_t n, int f, int field_offset) {
+  if (f < 0 || f >= MIC_NF_COUNT) return ORC_ERR_ARG;
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    int i = p->cellX, j = p->cellY;
+    double mdx = (p->X - c->x[i]) / (c->x[i + 1] - c->x[i]);
+    double mdy = (p->Y - c->y[j]) / (c->y[j + 1] - c->y[j]);
+    double val = NODE(c, f, i, j) * (1 - mdx) * (1 - mdy) + NODE(c, f, i, j + 1) * (1 - mdx) * mdy +
+                 NODE(c, f, i + 1, j) * (mdx) * (1 - mdy) + NODE(c, f, i + 1, j + 1) * mdx * mdy;
+    *(double *)((char *)p + field_offset) = val;
+  }
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+/* rheology                                                                   */
+
+/* computeRheology (viscosity.c:12-67) */
+int orc_compute_rheology(const orc_ctx *c, const mic_marker *p, double *eta, double *mu) {
+  const int k = p->Mat;
+  const mic_materials *M = &c->mat;
+  *mu = M->materialMu[k];
+  switch (M->hasEtaT[k]) {
+    case 1:
+      *eta = M->materialEta[k] * exp(M->QonR[k] * (1.0 / p->T - 1.0 / M->Tref[k]));
+      return ORC_OK;
+    case 2: {
+      double T0 = M->Tref[k];
+      *eta = M->materialEta[k] * exp(M->QonR[k] / T0 * (1.0 - (p->T - T0) / T0));
+      return ORC_OK;
+    }
+    case 3:
+      *eta = M->materialEta[k] * p->T;
+      return ORC_OK;
+    case 5:
+      *eta = M->materialEta[k] * exp(-M->QonR[k] * p->T);
+      return ORC_OK;
+    case 0:
+      *eta = M->materialEta[k];
+      return ORC_OK;
+    case 6: {
+      double depth = p->Y, dist = p->X, e = M->materialEta[k];
+      double edge = depth / tan(c->opt.slabAngle);
+      if (dist > edge && dist < (edge + c->opt.decoupleThickness) && depth > c->opt.minDecoupleDepth &&
+          depth < c->opt.maxDecoupleDepth)
+        e *= c->opt.decoupleEtaScaler;
+      *eta = e;
+      return ORC_OK;
+    }
+    default:
+      return ORC_ERR_LAW;
+  }
+}
+
+/* checkPlasticYielding (markers.c:1381-1505) */
+int orc_check_plastic_yielding(orc_ctx *c, mic_marker *mk, int64_t n, double dt, int *is_yielding) {
+  const mic_materials *M = &c->mat;
+  const double etamin = c->opt.etamin, etamax = c->opt.etamax, frac = c->opt.fractionalEtamin;
+  int err = ORC_OK;
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    const double eta_old = p->eta;
+    double etanew = eta_old;
+    /* visco-elastic stress forecast with the old viscosity (markers.c:1397-1402) */
+    const double X = p->eta / (p->mu * dt + p->eta);
+    const double sxx = p->s.T11 * X + 2 * p->eta * p->e.T11 * (1.0 - X);
+    const double syy = p->s.T22 * X + 2 * p->eta * p->e.T22 * (1.0 - X);
+    const double sxy = p->s.T12 * X + 2 * p->eta * p->e.T12 * (1.0 - X);
+    const double sii = sqrt(0.5 * (sxx * sxx + syy * syy) + sxy * sxy);
+    (void)sii;
+    double eta, mu;
+    if (orc_compute_rheology(c, p, &eta, &mu) != ORC_OK) err = ORC_ERR_LAW;
+    p->eta = eta;
+    p->mu = mu;
+    const int k = p->Mat;
+    const int plast = M->hasPlasticity[k];
+    if (!plast) continue;
+    double sy;
+    if (plast == 1) {
+      sy = M->materialCohesion[k] + M->materialFriction[k] * p->p;
+    } else if (plast == 2) {
+      /* linear strain weakening between gamma[0] and gamma[1] (markers.c:1426-1448) */
+      const double E = p->Eii;
+      double coh, fr;
+      if (E < M->gamma[k][0]) {
+        coh = M->C[k][0];
+        fr = sin(M->F[k][0] / 180.0 * M_PI);
+      } else if (E >= M->gamma[k][0] && E <= M->gamma[k][1]) {
+        const double dg = (E - M->gamma[k][0]) / (M->gamma[k][1] - M->gamma[k][0]);
+        coh = (M->C[k][1] - M->C[k][0]) * dg + M->C[k][0];
+        fr = (sin(M->F[k][1] / 180.0 * M_PI) - sin(M->F[k][0] / 180.0 * M_PI)) * dg + sin(M->F[k][0] / 180.0 * M_PI);
+      } else {
+        coh = M->C[k][1];
+        fr = sin(M->F[k][1] / 180.0 * M_PI);
+      }
+      sy = coh + fr * p->p;
+    } else {
+      sy = 0.0;
+    }
+    if (sy < 0.0) sy = 0.0;
+    if (sii > sy) {
+      const double exx = p->e.T11, eyy = p->e.T22, exy = p->e.T12;
+      const double eii = sqrt(0.5 * (exx * exx + eyy * eyy) + exy * exy);
+      etanew = sy / 2.0 / eii;
+      if (etanew / p->eta < frac) etanew = frac * p->eta;
+      if (etanew < etamin)
+        etanew = etamin;
+      else if (etanew > etamax)
+        etanew = etamax;
+      const double sio = sqrt(0.5 * (p->s.T11 * p->s.T11 + p->s.T22 * p->s.T22) + p->s.T12 * p->s.T12);
+      if (sio != 0.0) {
+        p->s.T11 *= sy / sio;
+        p->s.T22 *= sy / sio;
+        p->s.T12 *= sy / sio;
+      }
+      *is_yielding = 1;
+    }
+    /* plastic materials keep the pre-update viscosity unless they yield (markers.c:1397, 1493) */
+    p->eta = etanew;
+  }
+  return err;
+}
+
+/* limitViscosity / limitMarkerViscosity (viscosity.c:90-104): every marker, in domain or not */
+void orc_limit_viscosity(orc_ctx *c, mic_marker *mk, int64_t n) {
+  for (int64_t m = 0; m < n; ++m) {
+    if (mk[m].eta > c->opt.etamax)
+      mk[m].eta = c->opt.etamax;
+    else if (mk[m].eta < c->opt.etamin)
+      mk[m].eta = c->opt.etamin;
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* node -> marker                                                             */
+
+/* Pressure-cell (cell-centre) lookup with the bounds of updateMarkerStrainPressure.c:137-147:
+ * step right when X >= xc[cellX+1] (only while cellX < xlim), down when Y >= yc[cellY+1] (while
+ * cellY < NY-1), then clamp to the interior [1, NX-2] x [1, NY-2]. */
+static void centre_cell(const orc_ctx *c, const mic_marker *p, int xlim, int *cx, int *cy, double *mdx, double *mdy) {
+  int i = p->cellX, j = p->cellY;
+  if (i < xlim && p->X >= c->xc[i + 1]) i++;
+  if (j < c->NY - 1 && p->Y >= c->yc[j + 1]) j++;
+  if (j < 1)
+    j = 1;
+  else if (j > c->NY - 2)
+    j = c->NY - 2;
+  if (i < 1)
+    i = 1;
+  else if (i > c->NX - 2)
+    i = c->NX - 2;
+  *mdx = (p->X - c->xc[i]) / (c->xc[i + 1] - c->xc[i]);
+  *mdy = (p->Y - c->yc[j]) / (c->yc[j + 1] - c->yc[j]);
+  *cx = i;
+  *cy = j;
+}
+
+/* Basic cell clamped to [0, NX-2] x [0, NY-2] (updateMarkerStrainPressure.c:208-215). */
+static void basic_cell(const orc_ctx *c, const mic_marker *p, int *cx, int *cy, double *mdx, double *mdy) {
+  int i = p->cellX, j = p->cellY;
+  if (j < 0)
+    j = 0;
+  else if (j > c->NY - 2)
+    j = c->NY - 2;
+  if (i < 0)
+    i = 0;
+  else if (i > c->NX - 2)
+    i = c->NX - 2;
+  *mdx = (p->X - c->x[i]) / (c->x[i + 1] - c->x[i]);
+  *mdy = (p->Y - c->y[j]) / (c->y[j + 1] - c->y[j]);
+  *cx = i;
+  *cy = j;
+}
+
+/* Running bilinear sum in the order 00, 01, 10, 11 used by updateMarkerStrainPressure.c,
+ * subgridStressChanges.c and updateMarkerStress.c. */
+static inline double interp_run(const orc_ctx *c, int f, int i, int j, double mdx, double mdy) {
+  double s = 0.0;
+  s += (1.0 - mdx) * (1.0 - mdy) * NODE(c, f, i, j);
+  s += (1.0 - mdx) * mdy * NODE(c, f, i, j + 1);
+  s += mdx * (1.0 - mdy) * NODE(c, f, i + 1, j);
+  s += mdx * mdy * NODE(c, f, i + 1, j + 1);
+  return s;
+}
+
+/* updateMarkerStrainPressure (updateMarkerStrainPressure.c:131-339, non-TEXTURE branch) */
+int orc_update_marker_strain_pressure(orc_ctx *c, mic_marker *mk, int64_t n, double dt) {
+  int err = ORC_OK;
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    int i, j;
+    double mdx, mdy;
+    centre_cell(c, p, c->NX - 2, &i, &j, &mdx, &mdy);
+    p->p = interp_run(c, MIC_NF_P, i, j, mdx, mdy);
+    const double mexx = interp_run(c, MIC_NF_EDOTXX, i, j, mdx, mdy);
+    const double msxx = interp_run(c, MIC_NF_SOXX, i, j, mdx, mdy);
+    const double msyy = interp_run(c, MIC_NF_SOYY, i, j, mdx, mdy);
+    const double mdsxx = interp_run(c, MIC_NF_DSXX, i, j, mdx, mdy);
+    const double mdsyy = interp_run(c, MIC_NF_DSYY, i, j, mdx, mdy);
+    basic_cell(c, p, &i, &j, &mdx, &mdy);
+    p->wxy = interp_run(c, MIC_NF_WXY, i, j, mdx, mdy);
+    const double mexy = interp_run(c, MIC_NF_EDOTXY, i, j, mdx, mdy);
+    const double msxy = interp_run(c, MIC_NF_SOXY, i, j, mdx, mdy);
+    const double mdsxy = interp_run(c, MIC_NF_DSXY, i, j, mdx, mdy);
+    /* Gerya's method 1: viscous + elastic strain rate from nodal stress and stress change */
+    p->e.T11 = msxx / 2.0 / p->eta + mdsxx / 2.0 / dt / p->mu;
+    p->e.T22 = msyy / 2.0 / p->eta + mdsyy / 2.0 / dt / p->mu;
+    p->e.T12 = msxy / 2.0 / p->eta + mdsxy / 2.0 / dt / p->mu;
+    p->strainRateResidual = sqrt(pow(p->e.T11 - mexx, 2.0) + pow(p->e.T12 - mexy, 2.0));
+    if (isnan(p->strainRateResidual)) err = ORC_ERR_NAN;
+  }
+  return err;
+}
+
+/* updateGlobalStrainRateResidual (residual.c:12-51) */
+double orc_update_global_strain_rate_residual(orc_ctx *c, const mic_marker *mk, int64_t n, int iter) {
+  orc_project_marker_field(c, mk, n, (int)offsetof(mic_marker, strainRateResidual), NULL, MIC_NF_SRR, -1, -1,
+                           MIC_ARITHMETIC);
+  double *srr = c->nodal[MIC_NF_SRR];
+  for (int j = 0; j < c->NY; ++j)
+    for (int i = 0; i < c->NX; ++i) {
+      size_t k = (size_t)j * c->NX + i;
+      if (i > 0 && j > 0)
+        srr[k] *= (c->x[i] - c->x[i - 1]) * (c->y[j] - c->y[j - 1]);
+      else
+        srr[k] = 0.0;
+    }
+  double sum = 0.0;
+  for (size_t k = 0; k < (size_t)c->NX * c->NY; ++k) sum += srr[k];
+  sum /= (c->LX * c->LY);
+  c->residuals[iter % 100] = sum;
+  return sum;
+}
+
+/* subgridStressChanges (subgridStressChanges.c:5-318) */
+int orc_subgrid_stress_changes(orc_ctx *c, mic_marker *mk, int64_t n, double dt, double D) {
+  const int NX = c->NX, NY = c->NY;
+  const size_t nn = (size_t)NX * NY;
+  double *dxy = (double *)calloc(nn, sizeof(double)), *wxy = (double *)calloc(nn, sizeof(double));
+  double *dxx = (double *)calloc(nn, sizeof(double)), *dyy = (double *)calloc(nn, sizeof(double));
+  double *wn = (double *)calloc(nn, sizeof(double));
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    /* relaxation factor 1 - exp(-D dt mu / eta), exponent floored at -30 (subgridStressChanges.c:81-85) */
+    const double sdm = p->eta / p->mu;
+    double sdif = -D * dt / sdm;
+    if (sdif < -30.0) sdif = -30.0;
+    sdif = 1.0 - exp(sdif);
+    int i, j;
+    double mdx, mdy;
+    basic_cell(c, p, &i, &j, &mdx, &mdy);
+    double dsxy = interp_run(c, MIC_NF_SOXY, i, j, mdx, mdy) - p->s.T12;
+    dsxy *= sdif;
+    p->s.T12 += dsxy;
+    /* quadrant scatter of the shear change; a marker on a half line feeds both sides (134-175) */
+    i = p->cellX;
+    j = p->cellY;
+    mdx = (p->X - c->x[i]) / (c->x[i + 1] - c->x[i]);
+    mdy = (p->Y - c->y[j]) / (c->y[j + 1] - c->y[j]);
+    if (mdx <= 0.5 && mdy <= 0.5) {
+      size_t k = (size_t)j * NX + i;
+      dxy[k] = dxy[k] + (1.0 - mdx) * (1.0 - mdy) * dsxy;
+      wxy[k] = wxy[k] + (1.0 - mdx) * (1.0 - mdy);
+    }
+    if (mdx <= 0.5 && mdy >= 0.5) {
+      size_t k = (size_t)(j + 1) * NX + i;
+      dxy[k] = dxy[k] + (1.0 - mdx) * (mdy)*dsxy;
+      wxy[k] = wxy[k] + (1.0 - mdx) * (mdy);
+    }
+    if (mdx >= 0.5 && mdy <= 0.5) {
+      size_t k = (size_t)j * NX + i + 1;
+      dxy[k] = dxy[k] + (mdx) * (1.0 - mdy) * dsxy;
+      wxy[k] = wxy[k] + (mdx) * (1.0 - mdy);
+    }
+    if (mdx >= 0.5 && mdy >= 0.5) {
+      size_t k = (size_t)(j + 1) * NX + i + 1;
+      dxy[k] = dxy[k] + (mdx) * (mdy)*dsxy;
+      wxy[k] = wxy[k] + (mdx) * (mdy);
+    }
+    /* normal components at the pressure cell (178-210) */
+    centre_cell(c, p, NX - 1, &i, &j, &mdx, &mdy);
+    double dsxx = interp_run(c, MIC_NF_SOXX, i, j, mdx, mdy) - p->s.T11;
+    dsxx *= sdif;
+    p->s.T11 += dsxx;
+    double dsyy = interp_run(c, MIC_NF_SOYY, i, j, mdx, mdy) - p->s.T22;
+    dsyy *= sdif;
+    p->s.T22 += dsyy;
+    /* scatter to the cell's own centre node with a tent weight (222-233) */
+    i = p->cellX;
+    j = p->cellY;
+    mdy = (p->Y - c->y[j]) / (c->y[j + 1] - c->y[j]);
+    mdx = (p->X - c->x[i]) / (c->x[i + 1] - c->x[i]);
+    {
+      size_t k = (size_t)(j + 1) * NX + i + 1;
+      dxx[k] += (1.0 - fabs(0.5 - mdx)) * (1.0 - fabs(0.5 - mdy)) * dsxx;
+      dyy[k] += (1.0 - fabs(0.5 - mdx)) * (1.0 - fabs(0.5 - mdy)) * dsyy;
+      wn[k] += (1.0 - fabs(0.5 - mdx)) * (1.0 - fabs(0.5 - mdy));
+    }
+  }
+  /* divide by the weights and remove the subgrid part from the nodal stress changes (258-286) */
+  for (size_t k = 0; k < nn; ++k) {
+    double a = 0.0 + dxy[k], w = 0.0 + wxy[k];
+    double gxy = (w != 0.0) ? a / w : 0.0;
+    double wn_ = 0.0 + wn[k];
+    double gxx = (wn_ != 0.0) ? (0.0 + dxx[k]) / wn_ : 0.0;
+    double gyy = (wn_ != 0.0) ? (0.0 + dyy[k]) / wn_ : 0.0;
+    c->nodal[MIC_NF_DSXX][k] = c->nodal[MIC_NF_DSXX][k] + -1.0 * gxx;
+    c->nodal[MIC_NF_DSYY][k] = c->nodal[MIC_NF_DSYY][k] + -1.0 * gyy;
+    c->nodal[MIC_NF_DSXY][k] = c->nodal[MIC_NF_DSXY][k] + -1.0 * gxy;
+  }
+  free(dxy);
+  free(wxy);
+  free(dxx);
+  free(dyy);
+  free(wn);
+  return ORC_OK;
+}
+
+/* updateMarkerStress (updateMarkerStress.c:5-163) */
+int orc_update_marker_stress(orc_ctx *c, mic_marker *mk, int64_t n, int64_t *nan_count) {
+  int64_t nans = 0;
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    int i, j;
+    double mdx, mdy;
+    centre_cell(c, p, c->NX - 2, &i, &j, &mdx, &mdy);
+    const double mdsxx = interp_run(c, MIC_NF_DSXX, i, j, mdx, mdy);
+    const double mdsyy = interp_run(c, MIC_NF_DSYY, i, j, mdx, mdy);
+    p->s.T11 += mdsxx;
+    p->s.T22 += mdsyy;
+    basic_cell(c, p, &i, &j, &mdx, &mdy);
+    const double mdsxy = interp_run(c, MIC_NF_DSXY, i, j, mdx, mdy);
+    p->s.T12 += mdsxy;
+    if (isnan(mdsxy)) nans++;
+  }
+  if (nan_count) *nan_count = nans;
+  return ORC_OK;
+}
+
+/* subgridTemperatureChanges (subgridTemperatureChanges.c:5-124) with the marker-to-node
+ * projection of the subgrid change (projectMarkersNodesFromScalar, markers.c:1507-1594). */
+int orc_subgrid_temperature_changes(orc_ctx *c, mic_marker *mk, int64_t n, double dt) {
+  const int NX = c->NX, NY = c->NY;
+  const size_t nn = (size_t)NX * NY;
+  const double D = c->opt.subgridTemperatureDiffusivity;
+  if (c->scratch_n < n) {
+    free(c->scratch);
+    c->scratch = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    c->scratch_n = n;
+  }
+  double *dTsub = c->scratch;
+  const double *Tn = c->nodal[MIC_NF_LASTT], *rn = c->nodal[MIC_NF_RHO];
+  const double *cpn = c->nodal[MIC_NF_CP], *kn = c->nodal[MIC_NF_KTHERMAL];
+  for (int64_t m = 0; m < n; ++m) {
+    const mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    const int i = p->cellX, j = p->cellY;
+    const size_t k00 = (size_t)j * NX + i, k10 = k00 + 1, k01 = k00 + NX, k11 = k01 + 1;
+    const double dx = c->x[i + 1] - c->x[i], dy = c->y[j + 1] - c->y[j];
+    const double mdx = (p->X - c->x[i]) / dx, mdy = (p->Y - c->y[j]) / dy;
+    const double Tm = Tn[k00] * (1.0 - mdx) * (1.0 - mdy) + Tn[k10] * mdx * (1.0 - mdy) +
+                      Tn[k01] * (1.0 - mdx) * (mdy) + Tn[k11] * mdx * mdy;
+    const double rhom = c->mat.materialRho[0] + rn[k00] * (1.0 - mdx) * (1.0 - mdy) + rn[k10] * (mdx) * (1.0 - mdy) +
+                        rn[k01] * (1.0 - mdx) * (mdy) + rn[k11] * mdx * mdy;
+    const double cpm = cpn[k00] * (1.0 - mdx) * (1.0 - mdy) + cpn[k10] * (mdx) * (1.0 - mdy) +
+                       cpn[k01] * (1.0 - mdx) * (mdy) + cpn[k11] * mdx * mdy;
+    const double km = kn[k00] * (1.0 - mdx) * (1.0 - mdy) + kn[k10] * (mdx) * (1.0 - mdy) +
+                      kn[k01] * (1.0 - mdx) * (mdy) + kn[k11] * mdx * mdy;
+    /* diffusion time of one cell, Gerya's eq. 10.16 */
+    const double tdiff = cpm * rhom / km / (2.0 / (dx * dx) + 2.0 / (dy * dy));
+    dTsub[m] = (Tm - p->T) * (1.0 - exp(-D * dt / tdiff));
+  }
+  /* project the subgrid change onto basic nodes */
+  double *nf = (double *)calloc(nn, sizeof(double)), *wt = (double *)calloc(nn, sizeof(double));
+  for (int64_t m = 0; m < n; ++m) {
+    const mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    const int i = p->cellX, j = p->cellY;
+    const double dx = c->x[i + 1] - c->x[i], dy = c->y[j + 1] - c->y[j];
+    const double mdx = (p->X - c->x[i]) / dx, mdy = (p->Y - c->y[j]) / dy;
+    const size_t k00 = (size_t)j * NX + i;
+    double w = (1.0 - mdx) * (1.0 - mdy);
+    wt[k00] += w;
+    nf[k00] += w * dTsub[m];
+    w = mdx * (1.0 - mdy);
+    wt[k00 + 1] += w;
+    nf[k00 + 1] += w * dTsub[m];
+    w = (1.0 - mdx) * mdy;
+    wt[k00 + NX] += w;
+    nf[k00 + NX] += w * dTsub[m];
+    w = mdx * mdy;
+    wt[k00 + NX + 1] += w;
+    nf[k00 + NX + 1] += w * dTsub[m];
+  }
+  /* remaining nodal change: thisT - lastT - projected subgrid change (VecAXPBYPCZ, alpha = 1) */
+  const double *thisT = c->nodal[MIC_NF_THIST];
+  for (size_t k = 0; k < nn; ++k) {
+    double w = 0.0 + wt[k];
+    double proj = (w != 0.0) ? (0.0 + nf[k]) / w : 0.0;
+    nf[k] = thisT[k] + -1.0 * Tn[k] + -1.0 * proj;
+  }
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    const int i = p->cellX, j = p->cellY;
+    const double dx = c->x[i + 1] - c->x[i], dy = c->y[j + 1] - c->y[j];
+    const double mdx = (p->X - c->x[i]) / dx, mdy = (p->Y - c->y[j]) / dy;
+    const size_t k00 = (size_t)j * NX + i;
+    const double dtm = (nf[k00] * (1.0 - mdy) * (1.0 - mdx) + nf[k00 + NX] * mdy * (1.0 - mdx) +
+                        nf[k00 + 1] * (1.0 - mdy) * mdx + nf[k00 + NX + 1] * mdy * mdx) +
+                       dTsub[m];
+    p->T += dtm;
+    p->Tdot = dtm / dt;
+  }
+  free(nf);
+  free(wt);
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+/* advection                                                                  */
+
+/* advectMarkersRK (markers.c:1865-2250), non-periodic grid, non-JAUMANN stress rotation */
+int orc_advect_markers_rk(orc_ctx *c, mic_marker *mk, int64_t n, double dt) {
+  const int NX = c->NX, NY = c->NY;
+  const double *vx = c->nodal[MIC_NF_VX], *vy = c->nodal[MIC_NF_VY], *wz = c->nodal[MIC_NF_WXY];
+  const mic_bcinfo *top = &c->bcs.mechBCTop, *left = &c->bcs.mechBCLeft;
+#define VXN(i, j) vx[(size_t)(j) * NX + (i)]
+#define VYN(i, j) vy[(size_t)(j) * NX + (i)]
+#define WZN(i, j) wz[(size_t)(j) * NX + (i)]
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    double xcur = p->X, ycur = p->Y;
+    double mvx[4], mvy[4], mwz[4];
+    for (int s = 0; s < 4; ++s) {
+      /* walk from the stored cell to the cell holding the stage position (1928-1944) */
+      int i = p->cellX, j = p->cellY;
+      if (xcur > c->x[i + 1]) {
+        while (xcur > c->x[i + 1] && i < NX - 2) i++;
+      } else if (xcur < c->x[i]) {
+        while (xcur < c->x[i] && i > 0) i--;
+      }
+      if (ycur > c->y[j + 1]) {
+        while (ycur > c->y[j + 1] && j < NY - 2) j++;
+      } else if (ycur < c->y[j]) {
+        while (ycur < c->y[j] && j > 0) j--;
+      }
+      /* staggered vx cell (x[i], yc[j+1]) and vy cell (xc[i+1], y[j]) (1946-1974) */
+      int vxX = i, vxY = j, vyX = i, vyY = j;
+      if (vxY > -1 && ycur < c->yc[vxY + 1]) vxY--;
+      if (vyX > -1 && xcur < c->xc[vyX + 1]) vyX--;
+      if (vxX < 0)
+        vxX = 0;
+      else if (vxX > NX - 2)
+        vxX = NX - 2;
+      if (vyX < -1)
+        vyX = -1;
+      else if (vyX > NX - 2)
+        vyX = NX - 2;
+      if (vxY < -1)
+        vxY = -1;
+      else if (vxY > NY - 2)
+        vxY = NY - 2;
+      if (vyY < 0)
+        vyY = 0;
+      else if (vyY > NY - 2)
+        vyY = NY - 2;
+      double ax = xcur - c->x[vxX];
+      double ay = ycur - c->yc[vxY + 1];
+      double hx = c->x[vxX + 1] - c->x[vxX];
+      double hy = c->yc[vxY + 2] - c->yc[vxY + 1];
+      double vul, vur;
+      if (vxY == -1 && top->type[0] == 0) { /* prescribed velocity on the top wall (1986-1991) */
+        vul = 2.0 * top->value[0] - VXN(vxX, vxY + 1);
+        vur = 2.0 * top->value[0] - VXN(vxX + 1, vxY + 1);
+      } else if (vxY == -1) { /* free slip */
+        vul = VXN(vxX, vxY + 1);
+        vur = VXN(vxX + 1, vxY + 1);
+      } else {
+        vul = VXN(vxX, vxY);
+        vur = VXN(vxX + 1, vxY);
+      }
+      double vll = VXN(vxX, vxY + 1), vlr = VXN(vxX + 1, vxY + 1);
+      mvx[s] = vul * (1.0 - ax / hx) * (1.0 - ay / hy);
+      mvx[s] += vur * (ax / hx) * (1.0 - ay / hy);
+      mvx[s] += vll * (1.0 - ax / hx) * (ay / hy);
+      mvx[s] += vlr * (ax * ay) / hx / hy;
+      double wur = VYN(vyX + 1, vyY), wlr = VYN(vyX + 1, vyY + 1), wul, wll;
+      if (vyX == -1 && left->type[1] == 0) { /* prescribed velocity on the left wall (2009-2023) */
+        wul = 2.0 * left->value[1] - VYN(vyX + 1, vyY);
+        wll = 2.0 * left->value[1] - VYN(vyX + 1, vyY + 1);
+      } else if (vyX == -1) {
+        wul = VYN(vyX + 1, vyY);
+        wll = VYN(vyX + 1, vyY + 1);
+      } else {
+        wul = VYN(vyX, vyY);
+        wll = VYN(vyX, vyY + 1);
+      }
+      ax = xcur - c->xc[vyX + 1];
+      ay = ycur - c->y[vyY];
+      hx = c->xc[vyX + 2] - c->xc[vyX + 1];
+      hy = c->y[vyY + 1] - c->y[vyY];
+      mvy[s] = wul * (1.0 - ax / hx) * (1.0 - ay / hy);
+      mvy[s] += wur * (ax / hx) * (1.0 - ay / hy);
+      mvy[s] += wll * (1.0 - ax / hx) * (ay / hy);
+      mvy[s] += wlr * (ax * ay) / hx / hy;
+      /* vorticity at basic nodes of the walked cell (2089-2094) */
+      const double mdx = (xcur - c->x[i]) / (c->x[i + 1] - c->x[i]);
+      const double mdy = (ycur - c->y[j]) / (c->y[j + 1] - c->y[j]);
+      mwz[s] = (1.0 - mdx) * (1.0 - mdy) * WZN(i, j);
+      mwz[s] += (mdx) * (1.0 - mdy) * WZN(i + 1, j);
+      mwz[s] += (1.0 - mdx) * (mdy)*WZN(i, j + 1);
+      mwz[s] += (mdx) * (mdy)*WZN(i + 1, j + 1);
+      if (s < 2) {
+        xcur = p->X + dt / 2 * mvx[s];
+        ycur = p->Y + dt / 2 * mvy[s];
+      } else if (s == 2) {
+        xcur = p->X + dt * mvx[s];
+        ycur = p->Y + dt * mvy[s];
+      }
+    }
+    p->VX = (mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]) / 6;
+    p->VY = (mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]) / 6;
+    p->wxy = (mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]) / 6.0;
+    p->X += dt * p->VX;
+    p->Y += dt * p->VY;
+    /* finite rotation of the stress tensor by -wxy dt (2158-2164) */
+    const double s11 = p->s.T11, s22 = p->s.T22, s12 = p->s.T12;
+    const double th = -p->wxy * dt;
+    p->s.T11 = s11 * pow(cos(th), 2.0) + s22 * pow(sin(th), 2.0) - s12 * sin(2.0 * th);
+    p->s.T22 = s11 * pow(sin(th), 2.0) + s22 * pow(cos(th), 2.0) + s12 * sin(2.0 * th);
+    p->s.T12 = 0.5 * (s11 - s22) * sin(2.0 * th) + s12 * cos(2.0 * th);
+    p->Eii += dt * sqrt(0.5 * (p->e.T11 * p->e.T11 + p->e.T22 * p->e.T22) + p->e.T12 * p->e.T12);
+  }
+#undef VXN
+#undef VYN
+#undef WZN
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+int orc_step(orc_ctx *c, mic_marker *mk, int64_t n, double dt_disp, double dt_thermal, int do_subgrid_stress,
+             double *residual) {
+  int err = ORC_OK, e;
+  orc_find_marker_cells(c, mk, n, &e);
+  if (e) return e;
+  orc_update_marker_rho(c, mk, n);
+  orc_project_markers_nodes_all2(c, mk, n);
+  (void)orc_max_marker_T(c, mk, n);
+  int yielding = 0;
+  if ((e = orc_check_plastic_yielding(c, mk, n, dt_disp, &yielding))) return e;
+  orc_limit_viscosity(c, mk, n);
+  orc_project_markers_nodes_all2(c, mk, n);
+  if ((e = orc_update_marker_strain_pressure(c, mk, n, dt_disp))) err = e;
+  double r = orc_update_global_strain_rate_residual(c, mk, n, 0);
+  if (residual) *residual = r;
+  if (do_subgrid_stress) orc_subgrid_stress_changes(c, mk, n, dt_disp, c->opt.subgridStressDiffusivity);
+  orc_update_marker_stress(c, mk, n, NULL);
+  orc_subgrid_temperature_changes(c, mk, n, dt_thermal);
+  orc_advect_markers_rk(c, mk, n, dt_thermal);
+  (void)orc_max_abs_sxx(c, mk, n);
+  return err;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Goldsby & Kohlstedt (2001) composite ice creep, as in viscosity.c:106-179    */
+double orc_gk_viscosity(double s, double T, double d, double P) {
+  const double R = 8.3144621;
+  if (P < 1.0) P = 1.0;
+  const double b = 4.52e-10, Vm = 1.97e-5, Qv = 59.4 * 1000.0, delta = 2.0 * b, Qb = 49 * 1000.0;
+  const double D0v = 9.10e-4, D0b = 5.8e-4;
+  const double Dv = D0v * exp(-Qv / (R * T));
+  const double Db = D0b * exp(-Qb / (R * T));
+  double ediff = 42.0 * Vm / (R * T * d * d) * (Dv + M_PI * delta / d * Db);
+  if (s < 1e0) return 0.5 / ediff;
+  ediff *= s;
+  double A, nn, Q;
+  const double V = -13e-6;
+  if (T < 255) {
+    A = 3.9e-3;
+    nn = 1.8;
+    Q = 49 * 1000.0;
+  } else {
+    A = 3.0e26;
+    nn = 1.8;
+    Q = 192 * 1000.0;
+  }
+  const double egbs = A * pow(s / 1e6, nn) / pow(d, 1.4) * exp((-Q + P * V) / (R * T));
+  if (T < 258) {
+    A = 4.0e5;
+    nn = 4.0;
+    Q = 60 * 1000.0;
+  } else {
+    A = 6.0e28;
+    nn = 4.0;
+    Q = 180 * 1000.0;
+  }
+  const double edisl = A * pow(s / 1e6, nn) * exp((-Q + P * V) / (R * T));
+  const double ebs = 5.5e7 * pow(s / 1e6, 2.4) * exp((-60.0 * 1000.0 + P * V) / (R * T));
+  const double etot = ediff + 1.0 / (1.0 / ebs + 1.0 / egbs) + edisl;
+  return s / 2.0 / etot;
+}

@@ -1,0 +1,2 @@
+/* single-rank stand-in header; see petsc_lite.h */
+#include "petsc_lite.h"

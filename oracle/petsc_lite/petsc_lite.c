@@ -1,0 +1,315 @@
+/* petsc_lite.c -- implementation of the single-rank PETSc/MPI stand-in described
+ * in include/petsc_lite.h.  TEST INFRASTRUCTURE ONLY (oracle pinning). */
+#include "petsc_lite.h"
+#include <stdarg.h>
+#include <time.h>
+
+struct _p_DM {
+  PetscInt NX, NY;
+};
+
+struct _p_Vec {
+  DM dm;
+  int is_local;          /* 1: (NX+4)*(NY+4) ghosted layout, 0: NX*NY */
+  PetscInt n;
+  PetscScalar *data;
+  PetscScalar **rows;    /* row pointers handed out by DMDAVecGetArray */
+};
+
+static int g_quiet = 1;
+void plite_set_quiet(int quiet) { g_quiet = quiet; }
+
+PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da) {
+  *da = (DM)calloc(1, sizeof(struct _p_DM));
+  if (!*da) return 1;
+  (*da)->NX = NX;
+  (*da)->NY = NY;
+  return 0;
+}
+
+PetscErrorCode plite_DMDestroy(DM *da) {
+  free(*da);
+  *da = NULL;
+  return 0;
+}
+
+PetscErrorCode DMDAGetCorners(DM da, PetscInt *x, PetscInt *y, PetscInt *z, PetscInt *m, PetscInt *n,
+                              PetscInt *p) {
+  if (x) *x = 0;
+  if (y) *y = 0;
+  if (z) *z = 0;
+  if (m) *m = da->NX;
+  if (n) *n = da->NY;
+  if (p) *p = 1;
+  return 0;
+}
+
+static PetscErrorCode vec_new(DM da, int is_local, Vec *v) {
+  Vec w = (Vec)calloc(1, sizeof(struct _p_Vec));
+  if (!w) return 1;
+  w->dm = da;
+  w->is_local = is_local;
+  w->n = is_local ? (da->NX + 4) * (da->NY + 4) : da->NX * da->NY;
+  w->data = (PetscScalar *)calloc((size_t)w->n, sizeof(PetscScalar));
+  if (!w->data) { free(w); return 1; }
+  *v = w;
+  return 0;
+}
+
+PetscErrorCode DMCreateGlobalVector(DM da, Vec *v) { return vec_new(da, 0, v); }
+PetscErrorCode DMCreateLocalVector(DM da, Vec *v) { return vec_new(da, 1, v); }
+PetscErrorCode DMGetGlobalVector(DM da, Vec *v) { return vec_new(da, 0, v); }
+PetscErrorCode DMGetLocalVector(DM da, Vec *v) { return vec_new(da, 1, v); }
+PetscErrorCode DMRestoreGlobalVector(DM da, Vec *v) { (void)da; return VecDestroy(v); }
+PetscErrorCode DMRestoreLocalVector(DM da, Vec *v) { (void)da; return VecDestroy(v); }
+
+PetscErrorCode VecDuplicate(Vec a, Vec *b) { return vec_new(a->dm, a->is_local, b); }
+
+PetscErrorCode VecDestroy(Vec *v) {
+  if (!v || !*v) return 0;
+  free((*v)->data);
+  free((*v)->rows);
+  free(*v);
+  *v = NULL;
+  return 0;
+}
+
+PetscErrorCode VecGetArray(Vec v, PetscScalar **a) { *a = v->data; return 0; }
+PetscErrorCode VecRestoreArray(Vec v, PetscScalar **a) { (void)v; *a = NULL; return 0; }
+PetscErrorCode VecGetSize(Vec v, PetscInt *n) { *n = v->n; return 0; }
+
+PetscErrorCode VecZeroEntries(Vec v) {
+  memset(v->data, 0, (size_t)v->n * sizeof(PetscScalar));
+  return 0;
+}
+
+PetscErrorCode VecSet(Vec v, PetscScalar a) {
+  for (PetscInt i = 0; i < v->n; ++i) v->data[i] = a;
+  return 0;
+}
+
+PetscErrorCode VecCopy(Vec x, Vec y) {
+  if (x->n != y->n) return 60;
+  memcpy(y->data, x->data, (size_t)x->n * sizeof(PetscScalar));
+  return 0;
+}
+
+/* y = y + alpha*x */
+PetscErrorCode VecAXPY(Vec y, PetscScalar alpha, Vec x) {
+  if (x->n != y->n) return 60;
+  for (PetscInt i = 0; i < y->n; ++i) y->data[i] = y->data[i] + alpha * x->data[i];
+  return 0;
+}
+
+/* z = alpha*x + beta*y + gamma*z, with PETSc's alpha==1 shortcut: z = x + beta*y + gamma*z */
+PetscErrorCode VecAXPBYPCZ(Vec z, PetscScalar alpha, PetscScalar beta, PetscScalar gamma, Vec x, Vec y) {
+  if (x->n != z->n || y->n != z->n) return 60;
+  PetscScalar *zz = z->data;
+  const PetscScalar *xx = x->data, *yy = y->data;
+  if (alpha == 1.0) {
+    for (PetscInt i = 0; i < z->n; ++i) zz[i] = xx[i] + beta * yy[i] + gamma * zz[i];
+  } else if (gamma == 1.0) {
+    for (PetscInt i = 0; i < z->n; ++i) zz[i] = alpha * xx[i] + beta * yy[i] + zz[i];
+  } else if (gamma == 0.0) {
+    for (PetscInt i = 0; i < z->n; ++i) zz[i] = alpha * xx[i] + beta * yy[i];
+  } else {
+    for (PetscInt i = 0; i < z->n; ++i) zz[i] = alpha * xx[i] + beta * yy[i] + gamma * zz[i];
+  }
+  return 0;
+}
+
+/* w = x ./ y, zero where y == 0 */
+PetscErrorCode VecPointwiseDivide(Vec w, Vec x, Vec y) {
+  if (x->n != w->n || y->n != w->n) return 60;
+  for (PetscInt i = 0; i < w->n; ++i) {
+    PetscScalar d = y->data[i];
+    w->data[i] = (d != 0.0) ? x->data[i] / d : 0.0;
+  }
+  return 0;
+}
+
+PetscErrorCode VecSum(Vec v, PetscScalar *s) {
+  PetscScalar acc = 0.0;
+  for (PetscInt i = 0; i < v->n; ++i) acc += v->data[i];
+  *s = acc;
+  return 0;
+}
+
+PetscErrorCode VecView(Vec v, PetscViewer vw) { (void)v; (void)vw; return 0; }
+
+PetscErrorCode DMGlobalToLocalBegin(DM da, Vec g, InsertMode mode, Vec l) {
+  (void)mode;
+  if (g->is_local || !l->is_local) return 62;
+  const PetscInt NX = da->NX, NY = da->NY, W = NX + 4;
+  for (PetscInt j = 0; j < NY; ++j)
+    memcpy(l->data + (size_t)(j + 2) * W + 2, g->data + (size_t)j * NX, (size_t)NX * sizeof(PetscScalar));
+  return 0;
+}
+PetscErrorCode DMGlobalToLocalEnd(DM da, Vec g, InsertMode mode, Vec l) { (void)da; (void)g; (void)mode; (void)l; return 0; }
+
+PetscErrorCode DMLocalToGlobalBegin(DM da, Vec l, InsertMode mode, Vec g) {
+  if (g->is_local || !l->is_local) return 62;
+  const PetscInt NX = da->NX, NY = da->NY, W = NX + 4;
+  for (PetscInt j = 0; j < NY; ++j) {
+    const PetscScalar *src = l->data + (size_t)(j + 2) * W + 2;
+    PetscScalar *dst = g->data + (size_t)j * NX;
+    if (mode == ADD_VALUES) {
+      for (PetscInt i = 0; i < NX; ++i) dst[i] = dst[i] + src[i];
+    } else {
+      memcpy(dst, src, (size_t)NX * sizeof(PetscScalar));
+    }
+  }
+  return 0;
+}
+PetscErrorCode DMLocalToGlobalEnd(DM da, Vec l, InsertMode mode, Vec g) { (void)da; (void)l; (void)mode; (void)g; return 0; }
+
+PetscErrorCode DMDAVecGetArray(DM da, Vec v, void *array) {
+  const PetscInt NX = da->NX, NY = da->NY;
+  const int g = v->is_local ? 2 : 0;
+  const PetscInt W = NX + 2 * g, H = NY + 2 * g;
+  if (!v->rows) {
+    v->rows = (PetscScalar **)malloc((size_t)H * sizeof(PetscScalar *));
+    if (!v->rows) return 1;
+  }
+  for (PetscInt r = 0; r < H; ++r) v->rows[r] = v->data + (size_t)r * W + g;
+  *(PetscScalar ***)array = v->rows + g;
+  return 0;
+}
+PetscErrorCode DMDAVecRestoreArray(DM da, Vec v, void *array) { (void)da; (void)v; *(PetscScalar ***)array = NULL; return 0; }
+PetscErrorCode DMDAVecGetArrayDOF(DM da, Vec v, void *array) { (void)da; (void)v; (void)array; return 63; }
+PetscErrorCode DMDAVecRestoreArrayDOF(DM da, Vec v, void *array) { (void)da; (void)v; (void)array; return 63; }
+
+/* ---- logging stages: exclusive wall time attributed to the top of the stack ---- */
+#define PLITE_MAX_STAGES 64
+#define PLITE_STACK 64
+static int g_nstages = 0;
+static double g_stage_sec[PLITE_MAX_STAGES];
+static int g_stack[PLITE_STACK];
+static int g_depth = 0;
+static double g_last = 0.0;
+
+static double now_sec(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+PetscErrorCode PetscLogStageRegister(const char *name, PetscLogStage *s) {
+  (void)name;
+  if (g_nstages >= PLITE_MAX_STAGES) return 1;
+  *s = g_nstages++;
+  return 0;
+}
+
+static void charge_top(void) {
+  double t = now_sec();
+  if (g_depth > 0) g_stage_sec[g_stack[g_depth - 1]] += t - g_last;
+  g_last = t;
+}
+
+PetscErrorCode PetscLogStagePush(PetscLogStage s) {
+  charge_top();
+  if (g_depth < PLITE_STACK) g_stack[g_depth++] = s;
+  return 0;
+}
+
+PetscErrorCode PetscLogStagePop(void) {
+  charge_top();
+  if (g_depth > 0) g_depth--;
+  return 0;
+}
+
+double plite_stage_seconds(int stage) {
+  return (stage >= 0 && stage < PLITE_MAX_STAGES) ? g_stage_sec[stage] : 0.0;
+}
+
+void plite_stage_reset(void) {
+  memset(g_stage_sec, 0, sizeof(g_stage_sec));
+  g_depth = 0;
+  g_last = now_sec();
+}
+
+PetscErrorCode PetscPrintf(MPI_Comm c, const char *fmt, ...) {
+  (void)c;
+  if (g_quiet) return 0;
+  va_list ap;
+  va_start(ap, fmt);
+  vfprintf(stderr, fmt, ap);
+  va_end(ap);
+  return 0;
+}
+PetscErrorCode PetscSynchronizedPrintf(MPI_Comm c, const char *fmt, ...) {
+  (void)c;
+  if (g_quiet) return 0;
+  va_list ap;
+  va_start(ap, fmt);
+  vfprintf(stderr, fmt, ap);
+  va_end(ap);
+  return 0;
+}
+PetscErrorCode PetscSynchronizedFlush(MPI_Comm c, ...) { (void)c; return 0; }
+
+/* ---- random numbers: drand48-style uniform on [lo, hi) ---- */
+struct _p_PetscRandom {
+  double lo, hi;
+  unsigned short state[3];
+};
+
+PetscErrorCode PetscRandomCreate(MPI_Comm c, PetscRandom *r) {
+  (void)c;
+  *r = (PetscRandom)calloc(1, sizeof(struct _p_PetscRandom));
+  if (!*r) return 1;
+  (*r)->lo = 0.0;
+  (*r)->hi = 1.0;
+  return 0;
+}
+PetscErrorCode PetscRandomSetType(PetscRandom r, PetscRandomType t) { (void)r; (void)t; return 0; }
+PetscErrorCode PetscRandomSetSeed(PetscRandom r, unsigned long seed) {
+  r->state[0] = 0x330E;
+  r->state[1] = (unsigned short)(seed & 0xFFFF);
+  r->state[2] = (unsigned short)((seed >> 16) & 0xFFFF);
+  return 0;
+}
+PetscErrorCode PetscRandomSeed(PetscRandom r) { (void)r; return 0; }
+PetscErrorCode PetscRandomSetInterval(PetscRandom r, PetscScalar lo, PetscScalar hi) {
+  r->lo = lo;
+  r->hi = hi;
+  return 0;
+}
+PetscErrorCode PetscRandomGetValue(PetscRandom r, PetscScalar *v) {
+  *v = r->lo + (r->hi - r->lo) * erand48(r->state);
+  return 0;
+}
+PetscErrorCode PetscRandomDestroy(PetscRandom *r) {
+  free(*r);
+  *r = NULL;
+  return 0;
+}
+
+int MPI_Comm_rank(MPI_Comm c, int *r) { (void)c; *r = 0; return 0; }
+int MPI_Comm_size(MPI_Comm c, int *s) { (void)c; *s = 1; return 0; }
+
+static size_t mpi_type_size(MPI_Datatype t) {
+  switch (t) {
+    case MPI_INT: return sizeof(int);
+    case MPI_DOUBLE: return sizeof(double);
+    default: return 1;
+  }
+}
+
+int MPI_Allreduce(const void *s, void *r, int count, MPI_Datatype t, MPI_Op op, MPI_Comm c) {
+  (void)op;
+  (void)c;
+  if (s != r) memmove(r, s, (size_t)count * mpi_type_size(t));
+  return 0;
+}
+
+int MPI_Sendrecv(const void *sb, int sc, MPI_Datatype st, int dest, int stag, void *rb, int rc, MPI_Datatype rt,
+                 int src, int rtag, MPI_Comm c, MPI_Status *status) {
+  (void)dest; (void)stag; (void)src; (void)rtag; (void)c; (void)status;
+  size_t n = (size_t)sc * mpi_type_size(st);
+  size_t m = (size_t)rc * mpi_type_size(rt);
+  if (n > m) n = m;
+  if (n) memmove(rb, sb, n);
+  return 0;
+}

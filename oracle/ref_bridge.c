@@ -1,0 +1,266 @@
+/*
+ * ref_bridge.c -- ctypes-friendly wrappers that drive fvmic2d's OWN hot-path
+ * functions (compiled unmodified from the reference tree against petsc_lite)
+ * on caller-provided grids, markers and nodal fields.
+ *
+ * TEST INFRASTRUCTURE ONLY.  It is linked into oracle/_ref/libfvmic2d_ref.so
+ * by oracle/build_ref.sh; the library is used to pin the project's C
+ * restatement (oracle/mic_oracle.c) and to generate golden vectors.
+ *
+ * Nothing here re-implements reference arithmetic except the three marker
+ * loops that live inline in main_subduction.c (density update, main:255-264;
+ * maximum temperature, main:271-289; maximum |sxx|, main:437-448), restated as
+ * small loops because main() itself cannot be linked.
+ */
+#include "fdcode.h"
+#include "markers.h"
+#include "markerProjection.h"
+#include "viscosity.h"
+#include "updateMarkerStrainPressure.h"
+#include "subgridStressChanges.h"
+#include "updateMarkerStress.h"
+#include "subgridTemperatureChanges.h"
+#include "residual.h"
+#include "profile.h"
+#include "gridSpacing.h"
+#include "mic_types.h"
+
+PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da);
+PetscErrorCode plite_DMDestroy(DM *da);
+PetscScalar goldsbyKohlstedt(PetscScalar, PetscScalar, PetscScalar, PetscScalar);
+
+_Static_assert(sizeof(Marker) == sizeof(mic_marker), "marker layout");
+_Static_assert(offsetof(Marker, cellX) == offsetof(mic_marker, cellX), "marker layout");
+_Static_assert(offsetof(Marker, isYielding) == offsetof(mic_marker, isYielding), "marker layout");
+_Static_assert(sizeof(Materials) == sizeof(mic_materials), "materials layout");
+_Static_assert(offsetof(Materials, Tref) == offsetof(mic_materials, Tref), "materials layout");
+_Static_assert(sizeof(BoundaryValues) == sizeof(mic_bcs), "bc layout");
+
+typedef struct {
+  GridData grid;
+  NodalFields nf;
+  Materials mat;
+  Options opt;
+  BoundaryValues bv;
+  MarkerSet ms;
+  Vec thisT;
+  Vec srr;
+  double *gbuf;
+} refp;
+
+static int g_logging = 0;
+
+static Vec *field_vec(refp *p, int id) {
+  switch (id) {
+    case MIC_NF_RHO: return &p->nf.rho;
+    case MIC_NF_RHODOT: return &p->nf.rhodot;
+    case MIC_NF_ETAS: return &p->nf.etaS;
+    case MIC_NF_ETAN: return &p->nf.etaN;
+    case MIC_NF_THIST: return &p->thisT;
+    case MIC_NF_LASTT: return &p->nf.lastT;
+    case MIC_NF_KTHERMAL: return &p->nf.kThermal;
+    case MIC_NF_CP: return &p->nf.Cp;
+    case MIC_NF_EDOTXX: return &p->nf.edotxx;
+    case MIC_NF_EDOTXY: return &p->nf.edotxy;
+    case MIC_NF_EDOTYY: return &p->nf.edotyy;
+    case MIC_NF_SOXX: return &p->nf.soxx;
+    case MIC_NF_SOXY: return &p->nf.soxy;
+    case MIC_NF_SOYY: return &p->nf.soyy;
+    case MIC_NF_DSXX: return &p->nf.dsxx;
+    case MIC_NF_DSYY: return &p->nf.dsyy;
+    case MIC_NF_DSXY: return &p->nf.dsxy;
+    case MIC_NF_MUS: return &p->nf.muS;
+    case MIC_NF_MUN: return &p->nf.muN;
+    case MIC_NF_VX: return &p->nf.vx;
+    case MIC_NF_VY: return &p->nf.vy;
+    case MIC_NF_P: return &p->nf.p;
+    case MIC_NF_WXY: return &p->nf.wxy;
+    case MIC_NF_SRR: return &p->srr;
+    default: return NULL;
+  }
+}
+
+/* x[NX], y[NY]: basic gridlines.  Cell centres follow getCellCenters (gridSpacing.c:150-157).
+ * Ghost entries that the reference leaves uninitialised are set to NaN so that any read shows. */
+refp *ref_create(int NX, int NY, double LX, double LY, const double *x, const double *y) {
+  if (!g_logging) {
+    initializeLogging();
+    g_logging = 1;
+  }
+  refp *p = (refp *)calloc(1, sizeof(refp));
+  if (!p) return NULL;
+  size_t nx4 = (size_t)NX + 4, ny4 = (size_t)NY + 4;
+  p->gbuf = (double *)malloc((2 * nx4 + 2 * ny4) * sizeof(double));
+  for (size_t i = 0; i < 2 * nx4 + 2 * ny4; ++i) p->gbuf[i] = NAN;
+  p->grid.x = p->gbuf + 2;
+  p->grid.xc = p->gbuf + nx4 + 2;
+  p->grid.y = p->gbuf + 2 * nx4 + 2;
+  p->grid.yc = p->gbuf + 2 * nx4 + ny4 + 2;
+  for (int i = 0; i < NX; ++i) p->grid.x[i] = x[i];
+  for (int j = 0; j < NY; ++j) p->grid.y[j] = y[j];
+  p->grid.NX = NX;
+  p->grid.NY = NY;
+  p->grid.LX = LX;
+  p->grid.LY = LY;
+  p->grid.xperiodic = 0;
+  p->grid.yperiodic = 0;
+  getCellCenters(p->grid.x, p->grid.xc, LX, NX);
+  getCellCenters(p->grid.y, p->grid.yc, LY, NY);
+  plite_DMDACreate(NX, NY, &p->grid.da);
+  for (int id = 0; id < MIC_NF_COUNT; ++id) DMCreateGlobalVector(p->grid.da, field_vec(p, id));
+  return p;
+}
+
+void ref_destroy(refp *p) {
+  if (!p) return;
+  for (int id = 0; id < MIC_NF_COUNT; ++id) VecDestroy(field_vec(p, id));
+  plite_DMDestroy(&p->grid.da);
+  free(p->gbuf);
+  free(p);
+}
+
+void ref_get_grid(refp *p, double *xc, double *yc) {
+  for (int i = 0; i <= p->grid.NX; ++i) xc[i] = p->grid.xc[i];
+  for (int j = 0; j <= p->grid.NY; ++j) yc[j] = p->grid.yc[j];
+}
+
+void ref_set_materials(refp *p, const mic_materials *m) { memcpy(&p->mat, m, sizeof(Materials)); }
+void ref_set_bcs(refp *p, const mic_bcs *b) { memcpy(&p->bv, b, sizeof(BoundaryValues)); }
+void ref_set_options(refp *p, const mic_options *o) {
+  p->opt.etamin = o->etamin;
+  p->opt.etamax = o->etamax;
+  p->opt.fractionalEtamin = o->fractionalEtamin;
+  p->opt.subgridStressDiffusivity = o->subgridStressDiffusivity;
+  p->opt.subgridTemperatureDiffusivity = o->subgridTemperatureDiffusivity;
+  p->opt.slabAngle = o->slabAngle;
+  p->opt.decoupleThickness = o->decoupleThickness;
+  p->opt.minDecoupleDepth = o->minDecoupleDepth;
+  p->opt.maxDecoupleDepth = o->maxDecoupleDepth;
+  p->opt.decoupleEtaScaler = o->decoupleEtaScaler;
+}
+
+/* markers stay owned by the caller (a numpy structured array with the Marker layout) */
+void ref_set_markers(refp *p, mic_marker *m, int n) {
+  p->ms.markers = (Marker *)m;
+  p->ms.nMark = n;
+  p->ms.maxMark = n;
+  p->ms.nOut = 0;
+}
+
+int ref_set_nodal(refp *p, int id, const double *v) {
+  Vec *f = field_vec(p, id);
+  if (!f) return 1;
+  PetscScalar *a;
+  VecGetArray(*f, &a);
+  memcpy(a, v, sizeof(double) * (size_t)p->grid.NX * (size_t)p->grid.NY);
+  return 0;
+}
+
+int ref_get_nodal(refp *p, int id, double *v) {
+  Vec *f = field_vec(p, id);
+  if (!f) return 1;
+  PetscScalar *a;
+  VecGetArray(*f, &a);
+  memcpy(v, a, sizeof(double) * (size_t)p->grid.NX * (size_t)p->grid.NY);
+  return 0;
+}
+
+int ref_findMarkerCells(refp *p) {
+  findMarkerCells(&p->ms, &p->grid);
+  return p->ms.nOut;
+}
+
+/* main_subduction.c:255-264 */
+void ref_updateMarkerRho(refp *p) {
+  Marker *mk = p->ms.markers;
+  for (int m = 0; m < p->ms.nMark; ++m) {
+    if (mk[m].cellX != -1) {
+      mk[m].rho = -p->mat.materialRho[mk[m].Mat] * (p->mat.materialAlpha[mk[m].Mat] * mk[m].T);
+      mk[m].rhodot = 0.0;
+    }
+  }
+}
+
+/* main_subduction.c:271-281 */
+double ref_maxMarkerT(refp *p) {
+  double maxT = 0.0;
+  Marker *mk = p->ms.markers;
+  for (int m = 0; m < p->ms.nMark; ++m)
+    if (mk[m].cellX != -1 && mk[m].T > maxT) maxT = mk[m].T;
+  return maxT;
+}
+
+/* main_subduction.c:437-448 */
+double ref_maxAbsSxx(refp *p) {
+  double sxxmax = 0.0;
+  Marker *mk = p->ms.markers;
+  for (int m = 0; m < p->ms.nMark; ++m)
+    if (mk[m].cellX != -1 && fabs(mk[m].s.T11) > sxxmax) sxxmax = fabs(mk[m].s.T11);
+  return sxxmax;
+}
+
+int ref_projectMarkersNodesAll2(refp *p) {
+  return projectMarkersNodesAll2(&p->ms, &p->grid, &p->nf, &p->mat, &p->opt);
+}
+
+/* field_offset: byte offset of a double inside Marker, or -1 with matprop != NULL */
+int ref_projectMarkerFieldToNodes(refp *p, int field_offset, double *matprop, int out_id, int stagx, int stagy,
+                                  int method) {
+  PetscScalar *mf = NULL;
+  if (field_offset >= 0) mf = (PetscScalar *)((char *)p->ms.markers + field_offset);
+  return projectMarkerFieldToNodes(&p->grid, &p->ms, matprop, mf, *field_vec(p, out_id), stagx, stagy,
+                                   (PROJECTION_METHOD)method);
+}
+
+int ref_projectNodalFieldToMarkersS(refp *p, int nodal_id, int field_offset) {
+  return projectNodalFieldToMarkersS(&p->nf, *field_vec(p, nodal_id), &p->ms,
+                                     (PetscScalar *)((char *)p->ms.markers + field_offset), &p->grid);
+}
+
+int ref_checkPlasticYielding(refp *p, double dt, double t) {
+  PetscInt isYielding = 0;
+  checkPlasticYielding(&p->grid, &p->ms, &p->mat, dt, &isYielding, &p->opt, t);
+  return isYielding;
+}
+
+void ref_limitViscosity(refp *p) { limitViscosity(&p->ms, &p->opt, &p->mat); }
+void ref_updateViscosity(refp *p) { updateViscosity(&p->ms, &p->opt, &p->mat); }
+
+int ref_updateMarkerStrainPressure(refp *p, double dt) {
+  return updateMarkerStrainPressure(&p->grid, &p->nf, &p->ms, &p->mat, &p->opt, dt);
+}
+
+double ref_updateGlobalStrainRateResidual(refp *p, int iter) {
+  updateGlobalStrainRateResidual(&p->grid, &p->ms, iter);
+  return getGlobalStrainRateResidual(iter);
+}
+
+int ref_checkConvergence(double atol, double rtol, int iter) { return checkConvergence(atol, rtol, iter); }
+
+int ref_subgridStressChanges(refp *p, double dt, double D) {
+  return subgridStressChanges(&p->grid, &p->nf, &p->ms, &p->mat, dt, D);
+}
+
+int ref_updateMarkerStress(refp *p) { return updateMarkerStress(&p->grid, &p->nf, &p->ms, &p->mat); }
+
+int ref_subgridTemperatureChanges(refp *p, double dt) {
+  return subgridTemperatureChanges(p->thisT, &p->grid, &p->nf, &p->ms, &p->mat, dt, &p->opt);
+}
+
+int ref_advectMarkersRK(refp *p, double dt) { return advectMarkersRK(&p->ms, &p->nf, &p->grid, &p->opt, &p->bv, dt); }
+
+double ref_goldsbyKohlstedt(double s, double T, double d, double P) { return goldsbyKohlstedt(s, T, d, P); }
+
+void ref_goldsbyKohlstedt_many(const double *s, const double *T, const double *d, const double *P, double *eta, int n) {
+  for (int i = 0; i < n; ++i) eta[i] = goldsbyKohlstedt(s[i], T[i], d[i], P[i]);
+}
+
+/* Per-stage CPU time, profile.h:5-22 numbering. */
+double ref_stage_seconds(int stage) {
+  extern double plite_stage_seconds(int);
+  return plite_stage_seconds(stage);
+}
+void ref_stage_reset(void) {
+  extern void plite_stage_reset(void);
+  plite_stage_reset();
+}

@@ -1,0 +1,181 @@
+"""ctypes driver for oracle/_ref/libfvmic2d_ref.so: fvmic2d's own hot-path C compiled
+against petsc_lite (oracle/build_ref.sh).  TEST INFRASTRUCTURE ONLY: pins the C
+restatement (oracle/mic_oracle.c) and generates tests/golden/ fixtures.  The
+library only exists where the reference tree is present (never on the GPU machine)."""
+import ctypes
+import os
+
+import numpy as np
+
+from fvmic2d_gb300.mic_types import NF, MARKER_DTYPE, MARKER_F64_OFFSETS
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libfvmic2d_ref.so")
+
+_lib = None
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+def available():
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not available():
+            raise RuntimeError("oracle/_ref/libfvmic2d_ref.so missing: run oracle/build_ref.sh where the reference tree exists")
+        L = ctypes.CDLL(LIB_PATH)
+        sig = {
+            "ref_create": (_P, [_I, _I, _D, _D, _DP, _DP]),
+            "ref_destroy": (None, [_P]),
+            "ref_get_grid": (None, [_P, _DP, _DP]),
+            "ref_set_materials": (None, [_P, _P]),
+            "ref_set_bcs": (None, [_P, _P]),
+            "ref_set_options": (None, [_P, _P]),
+            "ref_set_markers": (None, [_P, _P, _I]),
+            "ref_set_nodal": (_I, [_P, _I, _DP]),
+            "ref_get_nodal": (_I, [_P, _I, _DP]),
+            "ref_findMarkerCells": (_I, [_P]),
+            "ref_updateMarkerRho": (None, [_P]),
+            "ref_maxMarkerT": (_D, [_P]),
+            "ref_maxAbsSxx": (_D, [_P]),
+            "ref_projectMarkersNodesAll2": (_I, [_P]),
+            "ref_projectMarkerFieldToNodes": (_I, [_P, _I, _DP, _I, _I, _I, _I]),
+            "ref_projectNodalFieldToMarkersS": (_I, [_P, _I, _I]),
+            "ref_checkPlasticYielding": (_I, [_P, _D, _D]),
+            "ref_limitViscosity": (None, [_P]),
+            "ref_updateViscosity": (None, [_P]),
+            "ref_updateMarkerStrainPressure": (_I, [_P, _D]),
+            "ref_updateGlobalStrainRateResidual": (_D, [_P, _I]),
+            "ref_checkConvergence": (_I, [_D, _D, _I]),
+            "ref_subgridStressChanges": (_I, [_P, _D, _D]),
+            "ref_updateMarkerStress": (_I, [_P]),
+            "ref_subgridTemperatureChanges": (_I, [_P, _D]),
+            "ref_advectMarkersRK": (_I, [_P, _D]),
+            "ref_goldsbyKohlstedt": (_D, [_D, _D, _D, _D]),
+            "ref_goldsbyKohlstedt_many": (None, [_DP, _DP, _DP, _DP, _DP, _I]),
+            "ref_stage_seconds": (_D, [_I]),
+            "ref_stage_reset": (None, []),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+class RefProblem:
+    """One reference problem: grid + nodal Vecs + material/option tables + a marker array
+    that stays owned by this object (the reference functions mutate it in place)."""
+
+    def __init__(self, wl, markers=None):
+        L = lib()
+        g = wl.grid
+        self.wl = wl
+        self.NX, self.NY = g.NX, g.NY
+        self.h = L.ref_create(g.NX, g.NY, g.LX, g.LY, _dp(g.x), _dp(g.y))
+        self.materials = wl.materials
+        self.options = wl.options
+        self.bcs = wl.bcs
+        L.ref_set_materials(self.h, ctypes.byref(self.materials))
+        L.ref_set_options(self.h, ctypes.byref(self.options))
+        L.ref_set_bcs(self.h, ctypes.byref(self.bcs))
+        self.markers = np.array(wl.markers if markers is None else markers, dtype=MARKER_DTYPE, copy=True)
+        L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        for name, arr in wl.nodal.items():
+            self.set_nodal(name, arr)
+
+    def close(self):
+        if self.h:
+            lib().ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def grid_centres(self):
+        xc = np.empty(self.NX + 1)
+        yc = np.empty(self.NY + 1)
+        lib().ref_get_grid(self.h, _dp(xc), _dp(yc))
+        return xc, yc
+
+    def set_nodal(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.NY, self.NX)
+        assert lib().ref_set_nodal(self.h, NF[name], _dp(a)) == 0
+
+    def get_nodal(self, name):
+        a = np.empty((self.NY, self.NX))
+        assert lib().ref_get_nodal(self.h, NF[name], _dp(a)) == 0
+        return a
+
+    # --- reference entry points -------------------------------------------------
+    def findMarkerCells(self):
+        return lib().ref_findMarkerCells(self.h)
+
+    def updateMarkerRho(self):
+        lib().ref_updateMarkerRho(self.h)
+
+    def maxMarkerT(self):
+        return lib().ref_maxMarkerT(self.h)
+
+    def maxAbsSxx(self):
+        return lib().ref_maxAbsSxx(self.h)
+
+    def projectMarkersNodesAll2(self):
+        return lib().ref_projectMarkersNodesAll2(self.h)
+
+    def projectMarkerFieldToNodes(self, field, out, stagx, stagy, method, matprop=None):
+        off = -1 if field is None else MARKER_F64_OFFSETS[field]
+        mp = None
+        if matprop is not None:
+            self._mp = np.ascontiguousarray(matprop, dtype=np.float64)
+            mp = _dp(self._mp)
+        return lib().ref_projectMarkerFieldToNodes(self.h, off, mp, NF[out], stagx, stagy, method)
+
+    def projectNodalFieldToMarkersS(self, nodal, field):
+        return lib().ref_projectNodalFieldToMarkersS(self.h, NF[nodal], MARKER_F64_OFFSETS[field])
+
+    def checkPlasticYielding(self, dt, t=0.0):
+        return lib().ref_checkPlasticYielding(self.h, dt, t)
+
+    def limitViscosity(self):
+        lib().ref_limitViscosity(self.h)
+
+    def updateMarkerStrainPressure(self, dt):
+        return lib().ref_updateMarkerStrainPressure(self.h, dt)
+
+    def updateGlobalStrainRateResidual(self, it=0):
+        return lib().ref_updateGlobalStrainRateResidual(self.h, it)
+
+    def subgridStressChanges(self, dt, D):
+        return lib().ref_subgridStressChanges(self.h, dt, D)
+
+    def updateMarkerStress(self):
+        return lib().ref_updateMarkerStress(self.h)
+
+    def subgridTemperatureChanges(self, dt):
+        return lib().ref_subgridTemperatureChanges(self.h, dt)
+
+    def advectMarkersRK(self, dt):
+        return lib().ref_advectMarkersRK(self.h, dt)
+
+
+def goldsby_kohlstedt(s, T, d, P):
+    """Vectorised viscosity.c:106-179 (returns effective viscosity)."""
+    s, T, d, P = (np.ascontiguousarray(np.broadcast_to(a, np.broadcast(s, T, d, P).shape), dtype=np.float64).ravel()
+                  for a in (s, T, d, P))
+    out = np.empty_like(s)
+    lib().ref_goldsbyKohlstedt_many(_dp(s), _dp(T), _dp(d), _dp(P), _dp(out), len(s))
+    return out
