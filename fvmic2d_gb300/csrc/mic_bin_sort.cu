@@ -1,0 +1,332 @@
+// mic_bin_sort.cu -- K1: cell location (findMarkerCells, markers.c:41-106) and the stable
+// counting sort that orders the device marker columns by cell.
+//
+// Cell location uses integer compares on the IEEE bit patterns of X, Y and the gridlines
+// (valid because every compared value is non-negative): the same answer as the reference's
+// bisection, with no FP64 instructions on a GPU whose FP64 rate is 1/60 of FP32.
+//
+// Sorting: key = cellY*(NX-1) + cellX, out-of-domain markers get key (NX-1)*(NY-1).  An
+// LSD radix sort with 8-bit digits (stable by construction) orders (key, index) pairs:
+// per 4096-marker tile a digit histogram, one exclusive scan over the digit-major
+// histogram matrix, then a scatter in which each tile ranks its items per digit with warp
+// match/ballot in index order.  Ties keep the current device order, so the result equals
+// a CPU stable sort of the current order.  cell_start[] brackets each cell's markers.
+#include "mic_internal.cuh"
+
+using namespace mic;
+
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kItemsPerThread = 16;
+constexpr int kTile = kSortThreads * kItemsPerThread;  // 4096
+constexpr int kRadixBits = 8;
+constexpr int kBuckets = 1 << kRadixBits;
+
+// Largest i in [0, n-2] with g[i] <= v (markers.c:47-69), on bit patterns.
+__device__ __forceinline__ int bisect_bits(const long long *__restrict__ g, int n, long long v) {
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (v >= __ldg(g + mid))
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_find_cells(Params P, const double *__restrict__ X, const double *__restrict__ Y,
+                             int *__restrict__ cellX, int *__restrict__ cellY, int *__restrict__ cpu,
+                             int *__restrict__ key, int64_t n, Status *st) {
+  __shared__ unsigned long long s_out;
+  if (threadIdx.x == 0) s_out = 0;
+  __syncthreads();
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m < n) {
+    const long long bx = __double_as_longlong(X[m]);
+    const long long by = __double_as_longlong(Y[m]);
+    const long long ux = (bx == (long long)0x8000000000000000ULL) ? 0LL : bx;
+    const long long uy = (by == (long long)0x8000000000000000ULL) ? 0LL : by;
+    const long long blx = __double_as_longlong(P.LX), bly = __double_as_longlong(P.LY);
+    // X >= 0 && Y >= 0 && X <= LX && Y <= LY; NaN fails every test
+    const bool in = ux >= 0 && uy >= 0 && ux <= blx && uy <= bly;
+    int cx = -1, cy = -1, k = (P.NX - 1) * (P.NY - 1);
+    if (in) {
+      cx = bisect_bits(P.xbits, P.NX, ux);
+      cy = bisect_bits(P.ybits, P.NY, uy);
+      k = cy * (P.NX - 1) + cx;
+    } else {
+      atomicAdd(&s_out, 1ULL);
+    }
+    cellX[m] = cx;
+    cellY[m] = cy;
+    cpu[m] = 0;
+    key[m] = k;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_out) atomicAdd(&st->n_out, s_out);
+}
+
+__global__ void k_radix_hist(const int *__restrict__ key, int64_t n, int shift, int *__restrict__ hist,
+                             int ntiles) {
+  __shared__ int cnt[kBuckets];
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) cnt[b] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+#pragma unroll 4
+  for (int r = 0; r < kItemsPerThread; ++r) {
+    const int64_t idx = base + (int64_t)r * kSortThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&cnt[(key[idx] >> shift) & (kBuckets - 1)], 1);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) hist[(size_t)b * ntiles + blockIdx.x] = cnt[b];
+}
+
+// In-place exclusive scan of an int array of length len, in blocks of 2048; block totals go
+// to aux[] and are scanned by the same routine recursively from the host.
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 8;
+constexpr int kScanBlock = kScanThreads * kScanPer;
+
+__global__ void k_scan_block(int *__restrict__ data, int64_t len, int *__restrict__ block_sums) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  const int64_t base = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanPer;
+  int v[kScanPer];
+  int sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    v[k] = (base + k < len) ? data[base + k] : 0;
+    sum += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = (lane < kScanThreads / 32) ? warp_tot[lane] : 0;
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < kScanThreads / 32) warp_tot[lane] = wi - w;
+    if (lane == kScanThreads / 32 - 1 && block_sums) block_sums[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  int run = warp_tot[warp] + incl - sum;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    if (base + k < len) data[base + k] = run;
+    run += v[k];
+  }
+}
+
+__global__ void k_scan_add(int *__restrict__ data, int64_t len, const int *__restrict__ block_offsets) {
+  const int64_t base = (int64_t)blockIdx.x * kScanBlock;
+  const int add = block_offsets[blockIdx.x];
+  for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x)
+    if (base + k < len) data[base + k] += add;
+}
+
+__global__ void k_radix_scatter(const int *__restrict__ key_in, const int *__restrict__ val_in, int use_iota,
+                                int *__restrict__ key_out, int *__restrict__ val_out, int64_t n, int shift,
+                                const int *__restrict__ hist, int ntiles) {
+  __shared__ int tile_off[kBuckets];
+  __shared__ int run[kBuckets];
+  __shared__ int wcnt[kSortThreads / 32][kBuckets];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) {
+    tile_off[b] = hist[(size_t)b * ntiles + blockIdx.x];
+    run[b] = 0;
+  }
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+  for (int r = 0; r < kItemsPerThread; ++r) {
+    for (int t = threadIdx.x; t < (kSortThreads / 32) * kBuckets; t += blockDim.x) (&wcnt[0][0])[t] = 0;
+    __syncthreads();
+    const int64_t idx = base + (int64_t)r * kSortThreads + threadIdx.x;
+    const bool valid = idx < n;
+    int k = 0, v = 0, d = kBuckets;  // invalid items form their own group and are never written
+    if (valid) {
+      k = key_in[idx];
+      v = use_iota ? (int)idx : val_in[idx];
+      d = (k >> shift) & (kBuckets - 1);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    // per digit: exclusive prefix over the warps of this round, then advance the running count
+    for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) {
+      int acc = run[b];
+#pragma unroll
+      for (int w = 0; w < kSortThreads / 32; ++w) {
+        int c = wcnt[w][b];
+        wcnt[w][b] = acc;
+        acc += c;
+      }
+      run[b] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+      const int pos = tile_off[d] + wcnt[warp][d] + rank;
+      key_out[pos] = k;
+      val_out[pos] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// cell_start[c] = first sorted position with key >= c, for c in [0, ncells+1]
+__global__ void k_cell_start(const int *__restrict__ skey, int64_t n, int ncells, int *__restrict__ cs) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k > n) return;
+  const int hi = (k < n) ? skey[k] : ncells + 1;
+  const int lo = (k == 0) ? -1 : skey[k - 1];
+  for (int c = lo + 1; c <= hi; ++c) cs[c] = (int)k;
+}
+
+struct GatherCols {
+  const double *src_f[C_F64_COUNT];
+  double *dst_f[C_F64_COUNT];
+  const int *src_i[C_I32_COUNT];
+  int *dst_i[C_I32_COUNT];
+};
+
+__global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int p = perm[k];
+#pragma unroll
+  for (int c = 0; c < C_F64_COUNT; ++c) g.dst_f[c][k] = g.src_f[c][p];
+#pragma unroll
+  for (int c = 0; c < C_I32_COUNT; ++c) g.dst_i[c][k] = g.src_i[c][p];
+}
+
+// aux: free space for the block totals of this level and all coarser levels
+int scan_exclusive(mic_ctx *ctx, int *data, int64_t len, int *aux) {
+  const int64_t nb = (len + kScanBlock - 1) / kScanBlock;
+  if (nb <= 1) {
+    k_scan_block<<<1, kScanThreads, 0, ctx->stream>>>(data, len, nullptr);
+    return cudaGetLastError() == cudaSuccess ? MIC_OK : MIC_ERR_CUDA;
+  }
+  int *sums = aux;
+  k_scan_block<<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(data, len, sums);
+  int e = scan_exclusive(ctx, sums, nb, aux + nb + 1);
+  if (e) return e;
+  k_scan_add<<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(data, len, sums);
+  return cudaGetLastError() == cudaSuccess ? MIC_OK : MIC_ERR_CUDA;
+}
+
+int ensure_sort_scratch(mic_ctx *ctx, int ntiles) {
+  const int64_t need = (int64_t)kBuckets * ntiles;
+  if (ctx->hist_cap >= need) return MIC_OK;
+  cudaFree(ctx->hist);
+  cudaFree(ctx->scan_aux);
+  ctx->hist = nullptr;
+  ctx->scan_aux = nullptr;
+  ctx->hist_cap = 0;
+  if (cudaMalloc((void **)&ctx->hist, sizeof(int) * need) != cudaSuccess) return MIC_ERR_NOMEM;
+  int64_t aux = 0, l = need;
+  while (l > 1) {
+    l = (l + kScanBlock - 1) / kScanBlock;
+    aux += l + 1;
+  }
+  if (cudaMalloc((void **)&ctx->scan_aux, sizeof(int) * (aux + 16)) != cudaSuccess) return MIC_ERR_NOMEM;
+  ctx->hist_cap = (int)need;
+  return MIC_OK;
+}
+
+}  // namespace
+
+// Bins every marker, sorts the columns by cell (stable) and rebuilds cell_start.
+int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
+  const int64_t n = ctx->n;
+  cudaMemsetAsync(&ctx->d_status->n_out, 0, sizeof(unsigned long long), ctx->stream);
+  if (n == 0) {
+    MIC_CUDA_TRY(cudaMemsetAsync(ctx->cell_start, 0, sizeof(int) * ((size_t)ctx->ncells + 2), ctx->stream));
+    ctx->sorted = 1;
+    if (n_out) *n_out = 0;
+    return MIC_OK;
+  }
+  k_find_cells<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y], ctx->i32[C_CELLX],
+                                                        ctx->i32[C_CELLY], ctx->i32[C_CPU], ctx->key, n,
+                                                        ctx->d_status);
+  MIC_CUDA_TRY(cudaGetLastError());
+  const int ntiles = (int)((n + kTile - 1) / kTile);
+  int e = ensure_sort_scratch(ctx, ntiles);
+  if (e) return e;
+  int bits = 1;
+  while ((1LL << bits) <= (long long)ctx->ncells) ++bits;
+  const int passes = (bits + kRadixBits - 1) / kRadixBits;
+  int *kin = ctx->key, *kout = ctx->key_alt, *vin = ctx->perm, *vout = ctx->perm_alt;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = p * kRadixBits;
+    k_radix_hist<<<ntiles, kSortThreads, 0, ctx->stream>>>(kin, n, shift, ctx->hist, ntiles);
+    MIC_CUDA_TRY(cudaGetLastError());
+    e = scan_exclusive(ctx, ctx->hist, (int64_t)kBuckets * ntiles, ctx->scan_aux);
+    if (e) return e;
+    k_radix_scatter<<<ntiles, kSortThreads, 0, ctx->stream>>>(kin, vin, p == 0, kout, vout, n, shift, ctx->hist,
+                                                              ntiles);
+    MIC_CUDA_TRY(cudaGetLastError());
+    int *t = kin;
+    kin = kout;
+    kout = t;
+    t = vin;
+    vin = vout;
+    vout = t;
+  }
+  // kin / vin now hold the sorted keys and the permutation
+  k_cell_start<<<grid_for(n + 1), kBlock, 0, ctx->stream>>>(kin, n, ctx->ncells, ctx->cell_start);
+  MIC_CUDA_TRY(cudaGetLastError());
+  GatherCols g;
+  for (int c = 0; c < C_F64_COUNT; ++c) {
+    g.src_f[c] = ctx->f64[c];
+    g.dst_f[c] = ctx->f64_alt[c];
+  }
+  for (int c = 0; c < C_I32_COUNT; ++c) {
+    g.src_i[c] = ctx->i32[c];
+    g.dst_i[c] = ctx->i32_alt[c];
+  }
+  k_reorder<<<grid_for(n), kBlock, 0, ctx->stream>>>(g, vin, n);
+  MIC_CUDA_TRY(cudaGetLastError());
+  for (int c = 0; c < C_F64_COUNT; ++c) {
+    double *t = ctx->f64[c];
+    ctx->f64[c] = ctx->f64_alt[c];
+    ctx->f64_alt[c] = t;
+  }
+  for (int c = 0; c < C_I32_COUNT; ++c) {
+    int *t = ctx->i32[c];
+    ctx->i32[c] = ctx->i32_alt[c];
+    ctx->i32_alt[c] = t;
+  }
+  ctx->sorted = 1;
+  ctx->geo_valid = 0;
+  if (n_out) {
+    MIC_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, ctx->stream));
+    MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *n_out = (int64_t)ctx->h_status->n_out;
+  }
+  return MIC_OK;
+}
+
+int mic_ensure_sorted(mic_ctx *ctx) {
+  if (ctx->sorted) return MIC_OK;
+  return mic_bin_and_sort(ctx, nullptr);
+}
+
+extern "C" int mic_find_marker_cells(mic_ctx *ctx, int64_t *n_out) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int64_t no = 0;
+  int e = mic_bin_and_sort(ctx, &no);
+  if (n_out) *n_out = no;
+  return e;
+}

@@ -1,0 +1,441 @@
+// mic_context.cu -- context lifecycle, host<->device transfers and status for the C ABI.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "mic_internal.cuh"
+
+using namespace mic;
+
+extern "C" int mic_version(void) { return 100; }
+
+extern "C" const char *mic_error_string(int code) {
+  switch (code) {
+    case MIC_OK: return "ok";
+    case MIC_ERR_ARG: return "invalid argument";
+    case MIC_ERR_CUDA: return "CUDA runtime error";
+    case MIC_ERR_NOMEM: return "out of memory";
+    case MIC_ERR_CELL: return "impossible marker cell index";
+    case MIC_ERR_NAN: return "NaN strain-rate residual";
+    case MIC_ERR_LAW: return "undefined viscosity law";
+    case MIC_ERR_BC: return "unsupported boundary condition";
+    case MIC_ERR_CAPACITY: return "marker capacity exceeded";
+    case MIC_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown error";
+  }
+}
+
+int mic_fail_cuda(mic_ctx *ctx, cudaError_t e) {
+  if (ctx) ctx->last_error = (int)e;
+  fprintf(stderr, "mic_gb300: CUDA error %d (%s)\n", (int)e, cudaGetErrorString(e));
+  return MIC_ERR_CUDA;
+}
+
+void mic_invalidate_sort(mic_ctx *ctx) {
+  ctx->sorted = 0;
+  ctx->geo_valid = 0;
+}
+
+// ---- AoS <-> SoA ----------------------------------------------------------------
+
+struct ColPtrs {
+  double *f[C_F64_COUNT];
+  int *i[C_I32_COUNT];
+};
+
+// byte offsets of the f64 columns inside mic_marker, in F64Col order
+__constant__ int c_f64_off[C_F64_COUNT];
+__constant__ int c_i32_off[C_I32_COUNT - 1];  // all but C_ID
+
+static const int h_f64_off[C_F64_COUNT] = {
+    (int)offsetof(mic_marker, X),     (int)offsetof(mic_marker, Y),     (int)offsetof(mic_marker, VX),
+    (int)offsetof(mic_marker, VY),    (int)offsetof(mic_marker, T),     (int)offsetof(mic_marker, Tdot),
+    (int)offsetof(mic_marker, s.T11), (int)offsetof(mic_marker, s.T22), (int)offsetof(mic_marker, s.T12),
+    (int)offsetof(mic_marker, eta),   (int)offsetof(mic_marker, mu),    (int)offsetof(mic_marker, rho),
+    (int)offsetof(mic_marker, rhodot), (int)offsetof(mic_marker, p),    (int)offsetof(mic_marker, e.T11),
+    (int)offsetof(mic_marker, e.T22), (int)offsetof(mic_marker, e.T12), (int)offsetof(mic_marker, E.T11),
+    (int)offsetof(mic_marker, E.T22), (int)offsetof(mic_marker, E.T12), (int)offsetof(mic_marker, Eii),
+    (int)offsetof(mic_marker, wxy),   (int)offsetof(mic_marker, strainRateResidual)};
+static const int h_i32_off[C_I32_COUNT - 1] = {(int)offsetof(mic_marker, Mat), (int)offsetof(mic_marker, cellX),
+                                               (int)offsetof(mic_marker, cellY), (int)offsetof(mic_marker, cpu),
+                                               (int)offsetof(mic_marker, isYielding)};
+
+static_assert(sizeof(mic_marker) == 216, "fvmic2d Marker is 216 bytes");
+static_assert(offsetof(mic_marker, cellX) == 184, "fvmic2d Marker layout");
+
+int mic_f64_column_of_offset(int off) {
+  for (int c = 0; c < C_F64_COUNT; ++c)
+    if (h_f64_off[c] == off) return c;
+  return -1;
+}
+
+__global__ void k_aos_to_soa(const unsigned char *__restrict__ aos, ColPtrs cols, int64_t n) {
+  int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const unsigned char *r = aos + m * (int64_t)sizeof(mic_marker);
+#pragma unroll
+  for (int c = 0; c < C_F64_COUNT; ++c) cols.f[c][m] = *reinterpret_cast<const double *>(r + c_f64_off[c]);
+#pragma unroll
+  for (int c = 0; c < C_I32_COUNT - 1; ++c) cols.i[c][m] = *reinterpret_cast<const int *>(r + c_i32_off[c]);
+  cols.i[C_ID][m] = (int)m;
+}
+
+__global__ void k_soa_to_aos(unsigned char *__restrict__ aos, ColPtrs cols, int64_t n) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int m = cols.i[C_ID][k];
+  if (m < 0 || m >= n) return;
+  unsigned char *r = aos + (int64_t)m * (int64_t)sizeof(mic_marker);
+  memset(r, 0, sizeof(mic_marker));
+#pragma unroll
+  for (int c = 0; c < C_F64_COUNT; ++c) *reinterpret_cast<double *>(r + c_f64_off[c]) = cols.f[c][k];
+#pragma unroll
+  for (int c = 0; c < C_I32_COUNT - 1; ++c) *reinterpret_cast<int *>(r + c_i32_off[c]) = cols.i[c][k];
+}
+
+static ColPtrs cur_cols(mic_ctx *ctx) {
+  ColPtrs p;
+  for (int c = 0; c < C_F64_COUNT; ++c) p.f[c] = ctx->f64[c];
+  for (int c = 0; c < C_I32_COUNT; ++c) p.i[c] = ctx->i32[c];
+  return p;
+}
+
+// ---- lifecycle --------------------------------------------------------------------
+
+static void free_ctx(mic_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  for (int c = 0; c < C_F64_COUNT; ++c) {
+    cudaFree(ctx->f64[c]);
+    cudaFree(ctx->f64_alt[c]);
+  }
+  for (int c = 0; c < C_I32_COUNT; ++c) {
+    cudaFree(ctx->i32[c]);
+    cudaFree(ctx->i32_alt[c]);
+  }
+  for (int f = 0; f < MIC_NF_COUNT; ++f) cudaFree(ctx->nodal[f]);
+  for (int f = 0; f < 6; ++f) cudaFree(ctx->node_scr[f]);
+  cudaFree(ctx->grid_buf);
+  cudaFree(ctx->bits_buf);
+  cudaFree(ctx->key);
+  cudaFree(ctx->key_alt);
+  cudaFree(ctx->perm);
+  cudaFree(ctx->perm_alt);
+  cudaFree(ctx->cell_start);
+  cudaFree(ctx->hist);
+  cudaFree(ctx->scan_aux);
+  for (int g = 0; g < 4; ++g) cudaFree(ctx->geo[g]);
+  cudaFree(ctx->geo_flags);
+  cudaFree(ctx->scr0);
+  cudaFree(ctx->scr1);
+  cudaFree(ctx->scr2);
+  cudaFree(ctx->red_buf);
+  cudaFree(ctx->d_status);
+  cudaFree(ctx->stage_aos);
+  if (ctx->h_status) cudaFreeHost(ctx->h_status);
+  if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  free(ctx->h_x);
+  delete ctx;
+}
+
+#define ALLOC(ptr, bytes)                                                            \
+  do {                                                                               \
+    if (cudaMalloc((void **)&(ptr), (size_t)(bytes)) != cudaSuccess) {              \
+      free_ctx(ctx);                                                                 \
+      return MIC_ERR_NOMEM;                                                          \
+    }                                                                                \
+  } while (0)
+
+extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int NY, double LX, double LY,
+                          const double *x, const double *y, int64_t max_markers) {
+  if (!out || !x || !y || NX < 3 || NY < 3 || max_markers < 0 || max_markers > (int64_t)0x7FFFFFFF - 4096)
+    return MIC_ERR_ARG;
+  if ((int64_t)(NX - 1) * (NY - 1) >= (int64_t)0x7FFFFFF0) return MIC_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return MIC_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return MIC_ERR_ARG;
+  for (int i = 1; i < NX; ++i)
+    if (!(x[i] > x[i - 1])) return MIC_ERR_ARG;
+  for (int j = 1; j < NY; ++j)
+    if (!(y[j] > y[j - 1])) return MIC_ERR_ARG;
+  if (!(x[0] >= 0.0) || !(y[0] >= 0.0)) return MIC_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MIC_ERR_CUDA;
+  mic_ctx *ctx = new (std::nothrow) mic_ctx();
+  if (!ctx) return MIC_ERR_NOMEM;
+  memset((void *)ctx, 0, sizeof(*ctx));
+  ctx->device = device;
+  if (stream) {
+    ctx->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ctx;
+      return MIC_ERR_CUDA;
+    }
+    ctx->owns_stream = 1;
+  }
+  // host grid copies with fvmic2d's ghost offset of 2; cell centres as in getCellCenters
+  const size_t nx4 = (size_t)NX + 4, ny4 = (size_t)NY + 4;
+  ctx->h_x = (double *)malloc(sizeof(double) * (2 * nx4 + 2 * ny4));
+  if (!ctx->h_x) {
+    free_ctx(ctx);
+    return MIC_ERR_NOMEM;
+  }
+  for (size_t k = 0; k < 2 * nx4 + 2 * ny4; ++k) ctx->h_x[k] = 0.0;
+  double *hx = ctx->h_x + 2, *hxc = ctx->h_x + nx4 + 2, *hy = ctx->h_x + 2 * nx4 + 2,
+         *hyc = ctx->h_x + 2 * nx4 + ny4 + 2;
+  for (int i = 0; i < NX; ++i) hx[i] = x[i];
+  for (int j = 0; j < NY; ++j) hy[j] = y[j];
+  for (int i = 1; i < NX; ++i) hxc[i] = (hx[i - 1] + hx[i]) / 2.0;
+  hxc[0] = -hxc[1];
+  hxc[NX] = 2.0 * LX - hxc[NX - 1];
+  for (int j = 1; j < NY; ++j) hyc[j] = (hy[j - 1] + hy[j]) / 2.0;
+  hyc[0] = -hyc[1];
+  hyc[NY] = 2.0 * LY - hyc[NY - 1];
+  ctx->h_xc = hxc;
+  ctx->h_y = hy;
+  ctx->h_yc = hyc;
+  ALLOC(ctx->grid_buf, sizeof(double) * (2 * nx4 + 2 * ny4));
+  if (cudaMemcpy(ctx->grid_buf, ctx->h_x, sizeof(double) * (2 * nx4 + 2 * ny4), cudaMemcpyHostToDevice) !=
+      cudaSuccess) {
+    free_ctx(ctx);
+    return MIC_ERR_CUDA;
+  }
+  ALLOC(ctx->bits_buf, sizeof(long long) * (nx4 + ny4));
+  {
+    long long *hb = (long long *)malloc(sizeof(long long) * (nx4 + ny4));
+    for (int i = 0; i < NX; ++i) memcpy(&hb[i], &hx[i], 8);
+    for (int j = 0; j < NY; ++j) memcpy(&hb[nx4 + j], &hy[j], 8);
+    cudaMemcpy(ctx->bits_buf, hb, sizeof(long long) * (nx4 + ny4), cudaMemcpyHostToDevice);
+    free(hb);
+  }
+  ctx->P.NX = NX;
+  ctx->P.NY = NY;
+  ctx->P.LX = LX;
+  ctx->P.LY = LY;
+  ctx->P.x = ctx->grid_buf + 2;
+  ctx->P.xc = ctx->grid_buf + nx4 + 2;
+  ctx->P.y = ctx->grid_buf + 2 * nx4 + 2;
+  ctx->P.yc = ctx->grid_buf + 2 * nx4 + ny4 + 2;
+  ctx->P.xbits = ctx->bits_buf;
+  ctx->P.ybits = ctx->bits_buf + nx4;
+  const int64_t cap = max_markers > 0 ? max_markers : 1;
+  ctx->cap = cap;
+  for (int c = 0; c < C_F64_COUNT; ++c) {
+    ALLOC(ctx->f64[c], sizeof(double) * cap);
+    ALLOC(ctx->f64_alt[c], sizeof(double) * cap);
+  }
+  for (int c = 0; c < C_I32_COUNT; ++c) {
+    ALLOC(ctx->i32[c], sizeof(int) * cap);
+    ALLOC(ctx->i32_alt[c], sizeof(int) * cap);
+  }
+  const size_t nn = (size_t)NX * NY;
+  for (int f = 0; f < MIC_NF_COUNT; ++f) {
+    ALLOC(ctx->nodal[f], sizeof(double) * nn);
+    cudaMemset(ctx->nodal[f], 0, sizeof(double) * nn);
+  }
+  for (int f = 0; f < 6; ++f) ALLOC(ctx->node_scr[f], sizeof(double) * nn);
+  ctx->ncells = (NX - 1) * (NY - 1);
+  ALLOC(ctx->key, sizeof(int) * cap);
+  ALLOC(ctx->key_alt, sizeof(int) * cap);
+  ALLOC(ctx->perm, sizeof(int) * cap);
+  ALLOC(ctx->perm_alt, sizeof(int) * cap);
+  ALLOC(ctx->cell_start, sizeof(int) * ((size_t)ctx->ncells + 2));
+  for (int g = 0; g < 4; ++g) ALLOC(ctx->geo[g], sizeof(double) * cap);
+  ALLOC(ctx->geo_flags, sizeof(int) * cap);
+  ALLOC(ctx->scr0, sizeof(double) * cap);
+  ALLOC(ctx->scr1, sizeof(double) * cap);
+  ALLOC(ctx->scr2, sizeof(double) * cap);
+  ctx->red_cap = 4096;
+  ALLOC(ctx->red_buf, sizeof(double) * ctx->red_cap);
+  ALLOC(ctx->d_status, sizeof(Status));
+  cudaMemset(ctx->d_status, 0, sizeof(Status));
+  if (cudaHostAlloc((void **)&ctx->h_status, sizeof(Status), cudaHostAllocDefault) != cudaSuccess) {
+    free_ctx(ctx);
+    return MIC_ERR_NOMEM;
+  }
+  memset(ctx->h_status, 0, sizeof(Status));
+  cudaMemcpyToSymbol(c_f64_off, h_f64_off, sizeof(h_f64_off));
+  cudaMemcpyToSymbol(c_i32_off, h_i32_off, sizeof(h_i32_off));
+  for (int b = 0; b < 4; ++b) {
+    mic_bcinfo *s = &((mic_bcinfo *)&ctx->bcs)[b];
+    for (int k = 0; k < 3; ++k) s->type[k] = 1;
+  }
+  ctx->mat.nMaterials = 1;
+  ctx->opt.etamin = 0.0;
+  ctx->opt.etamax = 1e300;
+  ctx->n = 0;
+  ctx->sorted = 0;
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    free_ctx(ctx);
+    return MIC_ERR_CUDA;
+  }
+  *out = ctx;
+  return MIC_OK;
+}
+
+extern "C" int mic_destroy(mic_ctx *ctx) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_ctx(ctx);
+  return MIC_OK;
+}
+
+extern "C" int mic_set_materials(mic_ctx *ctx, const mic_materials *m) {
+  if (!ctx || !m || m->nMaterials < 1 || m->nMaterials > MIC_MAXMAT) return MIC_ERR_ARG;
+  ctx->mat = *m;
+  return MIC_OK;
+}
+
+extern "C" int mic_set_options(mic_ctx *ctx, const mic_options *o) {
+  if (!ctx || !o) return MIC_ERR_ARG;
+  ctx->opt = *o;
+  return MIC_OK;
+}
+
+extern "C" int mic_set_bcs(mic_ctx *ctx, const mic_bcs *b) {
+  if (!ctx || !b) return MIC_ERR_ARG;
+  if (b->mechBCTop.type[0] != 0 && b->mechBCTop.type[0] != 1) return MIC_ERR_BC;
+  if (b->mechBCLeft.type[1] != 0 && b->mechBCLeft.type[1] != 1) return MIC_ERR_BC;
+  ctx->bcs = *b;
+  return MIC_OK;
+}
+
+extern "C" int mic_get_grid_centres(mic_ctx *ctx, double *xc, double *yc) {
+  if (!ctx) return MIC_ERR_ARG;
+  if (xc)
+    for (int i = 0; i <= ctx->P.NX; ++i) xc[i] = ctx->h_xc[i];
+  if (yc)
+    for (int j = 0; j <= ctx->P.NY; ++j) yc[j] = ctx->h_yc[j];
+  return MIC_OK;
+}
+
+static int ensure_stage(mic_ctx *ctx, int64_t n) {
+  if (ctx->stage_cap >= n) return MIC_OK;
+  cudaFree(ctx->stage_aos);
+  ctx->stage_aos = nullptr;
+  ctx->stage_cap = 0;
+  if (cudaMalloc((void **)&ctx->stage_aos, (size_t)n * sizeof(mic_marker)) != cudaSuccess) return MIC_ERR_NOMEM;
+  ctx->stage_cap = n;
+  return MIC_OK;
+}
+
+extern "C" int mic_markers_upload(mic_ctx *ctx, const mic_marker *host, int64_t n) {
+  if (!ctx || (n > 0 && !host) || n < 0) return MIC_ERR_ARG;
+  if (n > ctx->cap) return MIC_ERR_CAPACITY;
+  cudaSetDevice(ctx->device);
+  int e = ensure_stage(ctx, n > 0 ? n : 1);
+  if (e) return e;
+  if (n > 0) {
+    MIC_CUDA_TRY(cudaMemcpyAsync(ctx->stage_aos, host, (size_t)n * sizeof(mic_marker), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    k_aos_to_soa<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->stage_aos, cur_cols(ctx), n);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  ctx->n = n;
+  mic_invalidate_sort(ctx);
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_markers_download(mic_ctx *ctx, mic_marker *host, int64_t n) {
+  if (!ctx || (n > 0 && !host) || n != ctx->n) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (n == 0) return MIC_OK;
+  int e = ensure_stage(ctx, n);
+  if (e) return e;
+  k_soa_to_aos<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->stage_aos, cur_cols(ctx), n);
+  MIC_CUDA_TRY(cudaGetLastError());
+  MIC_CUDA_TRY(cudaMemcpyAsync(host, ctx->stage_aos, (size_t)n * sizeof(mic_marker), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_markers_count(mic_ctx *ctx, int64_t *n) {
+  if (!ctx || !n) return MIC_ERR_ARG;
+  *n = ctx->n;
+  return MIC_OK;
+}
+
+extern "C" int mic_nodal_upload(mic_ctx *ctx, int f, const double *host) {
+  if (!ctx || !host || f < 0 || f >= MIC_NF_COUNT) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  MIC_CUDA_TRY(cudaMemcpyAsync(ctx->nodal[f], host, sizeof(double) * (size_t)ctx->P.NX * ctx->P.NY,
+                               cudaMemcpyHostToDevice, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_nodal_download(mic_ctx *ctx, int f, double *host) {
+  if (!ctx || !host || f < 0 || f >= MIC_NF_COUNT) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  MIC_CUDA_TRY(cudaMemcpyAsync(host, ctx->nodal[f], sizeof(double) * (size_t)ctx->P.NX * ctx->P.NY,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_nodal_device_ptr(mic_ctx *ctx, int f, double **dev) {
+  if (!ctx || !dev || f < 0 || f >= MIC_NF_COUNT) return MIC_ERR_ARG;
+  *dev = ctx->nodal[f];
+  return MIC_OK;
+}
+
+extern "C" int mic_synchronize(mic_ctx *ctx) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_get_stream(mic_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return MIC_ERR_ARG;
+  *stream = (void *)ctx->stream;
+  return MIC_OK;
+}
+
+extern "C" int mic_get_status(mic_ctx *ctx, mic_status *st) {
+  if (!ctx || !st) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  MIC_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  st->bad_cell = ctx->h_status->bad_cell;
+  st->nan_residual = ctx->h_status->nan_residual;
+  st->nan_dsxy = ctx->h_status->nan_dsxy;
+  st->bad_law = ctx->h_status->bad_law;
+  st->n_out = ctx->h_status->n_out;
+  st->is_yielding = ctx->h_status->is_yielding;
+  return MIC_OK;
+}
+
+extern "C" int mic_debug_sorted_ids(mic_ctx *ctx, int32_t *ids) {
+  if (!ctx || !ids) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->n == 0) return MIC_OK;
+  MIC_CUDA_TRY(cudaMemcpyAsync(ids, ctx->i32[C_ID], sizeof(int) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_debug_cell_start(mic_ctx *ctx, int32_t *cs) {
+  if (!ctx || !cs) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  MIC_CUDA_TRY(cudaMemcpyAsync(cs, ctx->cell_start, sizeof(int) * ((size_t)ctx->ncells + 2), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_host_alloc(void **ptr, int64_t bytes) {
+  if (!ptr || bytes <= 0) return MIC_ERR_ARG;
+  if (cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) return MIC_ERR_NOMEM;
+  return MIC_OK;
+}
+
+extern "C" int mic_host_free(void *ptr) {
+  if (!ptr) return MIC_ERR_ARG;
+  cudaFreeHost(ptr);
+  return MIC_OK;
+}

@@ -1,0 +1,141 @@
+// mic_internal.cuh -- device context and helpers shared by the GB300 marker-in-cell kernels.
+//
+// Markers live on the device as structure-of-arrays columns, physically ordered by
+// cell after every binning (stable counting sort by linear cell id, out-of-domain
+// markers last).  Column `id` keeps each marker's index in the caller's array so
+// that host transfers restore the caller's order.
+//
+// Nodal fields are NX*NY doubles, x fastest, one device array per field id of
+// include/mic_types.h.  Grid arrays x, y, xc, yc keep fvmic2d's two ghost entries
+// on each side (gridGenerator.c:123-130); the device copies point at entry 0.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mic_gb300.h"
+#include "mic_types.h"
+
+namespace mic {
+
+// double-valued marker columns, in mic_marker field order
+enum F64Col {
+  C_X = 0, C_Y, C_VX, C_VY, C_T, C_TDOT, C_SXX, C_SYY, C_SXY, C_ETA, C_MU, C_RHO, C_RHODOT, C_P,
+  C_EXX, C_EYY, C_EXY, C_EXX_TOT, C_EYY_TOT, C_EXY_TOT, C_EII, C_WXY, C_SRR, C_F64_COUNT
+};
+// int-valued marker columns
+enum I32Col { C_MAT = 0, C_CELLX, C_CELLY, C_CPU, C_ISYIELD, C_ID, C_I32_COUNT };
+
+// device status word (counts of events the reference aborts or prints on)
+struct Status {
+  unsigned long long bad_cell;      // impossible cell index (markers.c:74-77)
+  unsigned long long nan_residual;  // NaN strain-rate residual (updateMarkerStrainPressure.c:302-306)
+  unsigned long long nan_dsxy;      // NaN interpolated dsxy (updateMarkerStress.c:136-142)
+  unsigned long long bad_law;       // unknown viscosity law (viscosity.c:60-62)
+  unsigned long long n_out;         // out-of-domain markers after the last binning
+  int is_yielding;                  // any marker yielded in the last checkPlasticYielding
+  int pad;
+};
+
+struct Params {  // everything a kernel needs besides the marker columns; passed by value
+  int NX, NY;
+  double LX, LY;
+  const double *x, *y, *xc, *yc;  // point at index 0 (ghost entries at -2, -1 exist)
+  const long long *xbits, *ybits; // bit patterns of x[0..NX-1], y[0..NY-1] for integer compares
+};
+
+}  // namespace mic
+
+struct mic_ctx {
+  int device;
+  cudaStream_t stream;
+  int owns_stream;
+  mic::Params P;
+  double *grid_buf;  // device: x, xc, y, yc with ghosts
+  long long *bits_buf;
+  double *h_x, *h_y, *h_xc, *h_yc;  // host copies (with ghosts)
+  mic_materials mat;
+  mic_options opt;
+  mic_bcs bcs;
+  int64_t n, cap;
+  double *f64[mic::C_F64_COUNT];
+  int *i32[mic::C_I32_COUNT];
+  double *f64_alt[mic::C_F64_COUNT];
+  int *i32_alt[mic::C_I32_COUNT];
+  double *nodal[MIC_NF_COUNT];
+  // binning / sort scratch
+  int ncells;
+  int *key, *key_alt, *perm, *perm_alt;
+  int *cell_start;     // ncells + 2 entries
+  int *hist;           // radix histograms (digit-major per tile)
+  int hist_cap;
+  int *scan_aux;
+  int sorted;          // columns are in cell order for the current positions
+  // per-marker projection geometry for the current positions and order (see mic_project.cu)
+  double *geo[4];      // mdx0, mdy0 (basic cell), mdx1, mdy1 (cell-centre stagger -1,-1)
+  int *geo_flags;      // bit0 qx, bit1 qy, bit2 mdx0>=.5, bit3 mdy0>=.5, bit4 mdx1>=.5, bit5 mdy1>=.5
+  int geo_valid;
+  // per-marker scratch
+  double *scr0, *scr1, *scr2;
+  double *node_scr[6];  // nodal scratch (NX*NY each)
+  double *red_buf;     // reduction partials
+  int red_cap;
+  mic::Status *d_status;
+  mic::Status *h_status;  // pinned mirror
+  unsigned char *stage_aos;  // device staging for AoS transfers
+  int64_t stage_cap;
+  double residuals[100];
+  int last_error;
+};
+
+// ---- helpers -------------------------------------------------------------------------
+
+#define MIC_CUDA_TRY(expr)                                  \
+  do {                                                      \
+    cudaError_t _e = (expr);                                \
+    if (_e != cudaSuccess) return mic_fail_cuda(ctx, _e);   \
+  } while (0)
+
+int mic_fail_cuda(mic_ctx *ctx, cudaError_t e);
+int mic_ensure_sorted(mic_ctx *ctx);  // bins + sorts if positions changed since the last sort
+void mic_invalidate_sort(mic_ctx *ctx);
+int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out);
+int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry
+int mic_f64_column_of_offset(int byte_offset);
+
+namespace mic {
+
+constexpr int kBlock = 256;
+
+inline unsigned grid_for(int64_t n, int block = kBlock) {
+  int64_t g = (n + block - 1) / block;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+// Bit pattern of a non-negative double, canonicalising -0.0 to +0.0, so that for
+// non-negative finite values a >= b  <=>  bits(a) >= bits(b) as signed integers.
+__device__ __forceinline__ long long nonneg_bits(double v) {
+  long long b = __double_as_longlong(v);
+  return (b == (long long)0x8000000000000000ULL) ? 0LL : b;
+}
+
+// Order-preserving map of any non-NaN double to a signed integer key.
+__device__ __forceinline__ long long ordered_bits(double v) {
+  long long b = __double_as_longlong(v);
+  return b >= 0 ? b : (long long)(0x8000000000000000ULL) - b;
+}
+
+// Running bilinear sum in the order 00, 01, 10, 11 of updateMarkerStrainPressure.c:152-158,
+// subgridStressChanges.c:97-102 and updateMarkerStress.c:84-93.
+__device__ __forceinline__ double interp_run(const double *__restrict__ f, int NX, int i, int j, double mdx,
+                                             double mdy) {
+  const size_t k = (size_t)j * NX + i;
+  double s = 0.0;
+  s += (1.0 - mdx) * (1.0 - mdy) * __ldg(f + k);
+  s += (1.0 - mdx) * mdy * __ldg(f + k + NX);
+  s += mdx * (1.0 - mdy) * __ldg(f + k + 1);
+  s += mdx * mdy * __ldg(f + k + NX + 1);
+  return s;
+}
+
+}  // namespace mic

@@ -1,0 +1,992 @@
+// mic_marker_passes.cu -- K3..K5: the per-marker passes of the marker path and the
+// deterministic node gathers of the subgrid corrections.
+//
+// Every marker kernel runs one thread per marker over the cell-sorted columns and skips
+// markers outside the domain (cellX == -1), like the reference loops.  Floating-point
+// expressions keep the reference's evaluation order; built without FMA contraction
+// (-fmad=false) the results match the reference bit for bit except where a CUDA
+// transcendental (exp, sin, cos, tan) differs from the host libm in the last place.
+#include <cmath>
+#include <cstring>
+
+#include "mic_internal.cuh"
+
+using namespace mic;
+
+int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out);
+
+namespace {
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Interpolation cell at cell centres (updateMarkerStrainPressure.c:137-150, updateMarkerStress.c:66-80,
+// subgridStressChanges.c:179-190): staggered cell clamped to the interior [1, NX-2] x [1, NY-2].
+// Where the clamp leaves the staggered cell unchanged the offsets are the projection geometry.
+__device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, int fl, double gx1, double gy1,
+                                              double x, double y, int &i, int &j, double &mdx, double &mdy) {
+  const int sx = cx + (fl & 1), sy = cy + ((fl >> 1) & 1);
+  i = clampi(sx, 1, P.NX - 2);
+  j = clampi(sy, 1, P.NY - 2);
+  mdx = (i == sx) ? gx1 : (x - P.xc[i]) / (P.xc[i + 1] - P.xc[i]);
+  mdy = (j == sy) ? gy1 : (y - P.yc[j]) / (P.yc[j + 1] - P.yc[j]);
+}
+
+// computeRheology (viscosity.c:12-67); returns false for an undefined law
+__device__ __forceinline__ bool rheology(const mic_materials &M, const mic_options &O, int k, double T, double X,
+                                         double Y, double &eta, double &mu) {
+  mu = M.materialMu[k];
+  switch (M.hasEtaT[k]) {
+    case 1: eta = M.materialEta[k] * exp(M.QonR[k] * (1.0 / T - 1.0 / M.Tref[k])); return true;
+    case 2: {
+      const double T0 = M.Tref[k];
+      eta = M.materialEta[k] * exp(M.QonR[k] / T0 * (1.0 - (T - T0) / T0));
+      return true;
+    }
+    case 3: eta = M.materialEta[k] * T; return true;
+    case 5: eta = M.materialEta[k] * exp(-M.QonR[k] * T); return true;
+    case 0: eta = M.materialEta[k]; return true;
+    case 6: {
+      double e = M.materialEta[k];
+      const double edge = Y / tan(O.slabAngle);
+      if (X > edge && X < (edge + O.decoupleThickness) && Y > O.minDecoupleDepth && Y < O.maxDecoupleDepth)
+        e *= O.decoupleEtaScaler;
+      eta = e;
+      return true;
+    }
+    default: return false;
+  }
+}
+
+struct YieldCols {
+  const int *cellX, *mat;
+  const double *X, *Y, *T, *p, *Eii, *exx, *eyy, *exy;
+  double *eta, *mu, *sxx, *syy, *sxy;
+};
+
+// checkPlasticYielding (markers.c:1381-1505)
+__global__ void k_yield(YieldCols c, mic_materials M, mic_options O, double dt, int64_t n, Status *st) {
+  __shared__ int s_yield, s_bad;
+  if (threadIdx.x == 0) s_yield = s_bad = 0;
+  __syncthreads();
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m < n && c.cellX[m] != -1) {
+    const double eta_old = c.eta[m], mu_old = c.mu[m];
+    double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+    const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
+    // visco-elastic forecast with the old viscosity and modulus (markers.c:1397-1402)
+    const double Xf = eta_old / (mu_old * dt + eta_old);
+    const double fxx = s11 * Xf + 2 * eta_old * e11 * (1.0 - Xf);
+    const double fyy = s22 * Xf + 2 * eta_old * e22 * (1.0 - Xf);
+    const double fxy = s12 * Xf + 2 * eta_old * e12 * (1.0 - Xf);
+    const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
+    const int k = c.mat[m];
+    double eta, mu;
+    if (!rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu)) {
+      eta = eta_old;
+      mu = mu_old;
+      s_bad = 1;
+      atomicAdd(&st->bad_law, 1ULL);
+    }
+    const int plast = M.hasPlasticity[k];
+    if (plast) {
+      double sy;
+      if (plast == 1) {
+        sy = M.materialCohesion[k] + M.materialFriction[k] * c.p[m];
+      } else if (plast == 2) {  // strain weakening (markers.c:1426-1448)
+        const double E = c.Eii[m];
+        double coh, fr;
+        if (E < M.gamma[k][0]) {
+          coh = M.C[k][0];
+          fr = sin(M.F[k][0] / 180.0 * M_PI);
+        } else if (E >= M.gamma[k][0] && E <= M.gamma[k][1]) {
+          const double dg = (E - M.gamma[k][0]) / (M.gamma[k][1] - M.gamma[k][0]);
+          coh = (M.C[k][1] - M.C[k][0]) * dg + M.C[k][0];
+          fr = (sin(M.F[k][1] / 180.0 * M_PI) - sin(M.F[k][0] / 180.0 * M_PI)) * dg + sin(M.F[k][0] / 180.0 * M_PI);
+        } else {
+          coh = M.C[k][1];
+          fr = sin(M.F[k][1] / 180.0 * M_PI);
+        }
+        sy = coh + fr * c.p[m];
+      } else {
+        sy = 0.0;
+      }
+      if (sy < 0.0) sy = 0.0;
+      double etanew = eta_old;  // plastic materials keep the old viscosity unless they yield
+      if (sii > sy) {
+        const double eii = sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+        etanew = sy / 2.0 / eii;
+        if (etanew / eta < O.fractionalEtamin) etanew = O.fractionalEtamin * eta;
+        if (etanew < O.etamin)
+          etanew = O.etamin;
+        else if (etanew > O.etamax)
+          etanew = O.etamax;
+        const double sio = sqrt(0.5 * (s11 * s11 + s22 * s22) + s12 * s12);
+        if (sio != 0.0) {
+          s11 *= sy / sio;
+          s22 *= sy / sio;
+          s12 *= sy / sio;
+          c.sxx[m] = s11;
+          c.syy[m] = s22;
+          c.sxy[m] = s12;
+        }
+        s_yield = 1;
+      }
+      eta = etanew;
+    }
+    c.eta[m] = eta;
+    c.mu[m] = mu;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
+  (void)s_bad;
+}
+
+// updateViscosity (viscosity.c:77-88): rheology from the current marker stress
+__global__ void k_update_viscosity(YieldCols c, mic_materials M, mic_options O, int64_t n, Status *st) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n || c.cellX[m] == -1) return;
+  double eta, mu;
+  if (!rheology(M, O, c.mat[m], c.T[m], c.X[m], c.Y[m], eta, mu)) {
+    atomicAdd(&st->bad_law, 1ULL);
+    return;
+  }
+  c.eta[m] = eta;
+  c.mu[m] = mu;
+}
+
+// limitViscosity (viscosity.c:90-104): every marker
+__global__ void k_limit_viscosity(double *eta, double etamin, double etamax, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const double e = eta[m];
+  if (e > etamax)
+    eta[m] = etamax;
+  else if (e < etamin)
+    eta[m] = etamin;
+}
+
+// density update inline in main_subduction.c:255-264
+__global__ void k_update_rho(const int *cellX, const int *mat, const double *T, double *rho, double *rhodot,
+                             mic_materials M, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n || cellX[m] == -1) return;
+  const int k = mat[m];
+  rho[m] = -M.materialRho[k] * (M.materialAlpha[k] * T[m]);
+  rhodot[m] = 0.0;
+}
+
+struct Geo {
+  const double *gx0, *gy0, *gx1, *gy1;
+  const int *flags;
+};
+
+struct Nodal {
+  const double *p, *exx, *exy, *soxx, *soyy, *soxy, *dsxx, *dsyy, *dsxy, *wxy;
+};
+
+struct StrainCols {
+  const int *cellX, *cellY;
+  const double *X, *Y, *eta, *mu;
+  double *p, *exx, *eyy, *exy, *wxy, *srr;
+};
+
+// updateMarkerStrainPressure (updateMarkerStrainPressure.c:131-306, non-TEXTURE branch)
+__global__ void k_strain_pressure(Params P, StrainCols c, Geo g, Nodal nd, double dt, int64_t n, Status *st) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int cx = c.cellX[m], cy = c.cellY[m];
+  if (cx == -1) return;
+  const double x = c.X[m], y = c.Y[m];
+  int i, j;
+  double mdx, mdy;
+  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], x, y, i, j, mdx, mdy);
+  const int NX = P.NX;
+  c.p[m] = interp_run(nd.p, NX, i, j, mdx, mdy);
+  const double mexx = interp_run(nd.exx, NX, i, j, mdx, mdy);
+  const double msxx = interp_run(nd.soxx, NX, i, j, mdx, mdy);
+  const double msyy = interp_run(nd.soyy, NX, i, j, mdx, mdy);
+  const double mdsxx = interp_run(nd.dsxx, NX, i, j, mdx, mdy);
+  const double mdsyy = interp_run(nd.dsyy, NX, i, j, mdx, mdy);
+  const double bx = g.gx0[m], by = g.gy0[m];
+  c.wxy[m] = interp_run(nd.wxy, NX, cx, cy, bx, by);
+  const double mexy = interp_run(nd.exy, NX, cx, cy, bx, by);
+  const double msxy = interp_run(nd.soxy, NX, cx, cy, bx, by);
+  const double mdsxy = interp_run(nd.dsxy, NX, cx, cy, bx, by);
+  const double eta = c.eta[m], mu = c.mu[m];
+  const double e11 = msxx / 2.0 / eta + mdsxx / 2.0 / dt / mu;
+  const double e22 = msyy / 2.0 / eta + mdsyy / 2.0 / dt / mu;
+  const double e12 = msxy / 2.0 / eta + mdsxy / 2.0 / dt / mu;
+  c.exx[m] = e11;
+  c.eyy[m] = e22;
+  c.exy[m] = e12;
+  const double a = e11 - mexx, b = e12 - mexy;
+  const double r = sqrt(a * a + b * b);  // pow(., 2.0) of the reference: the correctly rounded square
+  c.srr[m] = r;
+  if (isnan(r)) atomicAdd(&st->nan_residual, 1ULL);
+}
+
+// area weighting of the projected residual (residual.c:23-38) and per-block partial sums
+__global__ void k_residual_weight(Params P, double *srr, double *partial) {
+  __shared__ double sh[kBlock];
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (q < (int64_t)P.NX * P.NY) {
+    const int i = (int)(q % P.NX), j = (int)(q / P.NX);
+    double s = srr[q];
+    if (i > 0 && j > 0)
+      s *= (P.x[i] - P.x[i - 1]) * (P.y[j] - P.y[j - 1]);
+    else
+      s = 0.0;
+    srr[q] = s;
+    v = s;
+  }
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_sum_partials(const double *partial, int np, double *out) {
+  __shared__ double sh[1024];
+  double v = 0.0;
+  for (int k = threadIdx.x; k < np; k += blockDim.x) v += partial[k];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+struct SubgridCols {
+  const int *cellX, *cellY;
+  const double *X, *Y, *eta, *mu;
+  double *sxx, *syy, *sxy;
+  double *dxy, *dxx, *dyy;  // per-marker stress changes (scratch)
+};
+
+// subgridStressChanges, marker part (subgridStressChanges.c:79-221)
+__global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal nd, double dt, double D,
+                                         int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int cx = c.cellX[m], cy = c.cellY[m];
+  if (cx == -1) return;
+  const double sdm = c.eta[m] / c.mu[m];
+  double sdif = -D * dt / sdm;
+  if (sdif < -30.0) sdif = -30.0;
+  sdif = 1.0 - exp(sdif);
+  double dsxy = interp_run(nd.soxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]) - c.sxy[m];
+  dsxy *= sdif;
+  c.sxy[m] = c.sxy[m] + dsxy;
+  int i, j;
+  double mdx, mdy;
+  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], i, j, mdx, mdy);
+  double dsxx = interp_run(nd.soxx, P.NX, i, j, mdx, mdy) - c.sxx[m];
+  dsxx *= sdif;
+  c.sxx[m] = c.sxx[m] + dsxx;
+  double dsyy = interp_run(nd.soyy, P.NX, i, j, mdx, mdy) - c.syy[m];
+  dsyy *= sdif;
+  c.syy[m] = c.syy[m] + dsyy;
+  c.dxy[m] = dsxy;
+  c.dxx[m] = dsxx;
+  c.dyy[m] = dsyy;
+}
+
+// subgridStressChanges, node part (134-175 quadrant scatter, 227-233 centre scatter, 258-286
+// divide and subtract) as a gather in marker order.
+__global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const int *__restrict__ cellX,
+                                                              const double *__restrict__ gx0,
+                                                              const double *__restrict__ gy0,
+                                                              const double *__restrict__ dxy,
+                                                              const double *__restrict__ dxx,
+                                                              const double *__restrict__ dyy,
+                                                              const int *__restrict__ cs, double *dsxx, double *dsyy,
+                                                              double *dsxy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= P.NX || j >= P.NY) return;
+  const int NC = P.NX - 1;
+  const long long half = 0x3FE0000000000000LL;
+  double sxy = 0.0, wxy = 0.0;
+  const int cy0 = max(j - 1, 0), cy1 = min(j, P.NY - 2);
+  const int cx0 = max(i - 1, 0), cx1 = min(i, P.NX - 2);
+  for (int cy = cy0; cy <= cy1; ++cy) {
+    const int mb = cs[cy * NC + cx0], me = cs[cy * NC + cx1 + 1];
+    const int oy = j - cy;
+    for (int m = mb; m < me; ++m) {
+      const int ox = i - cellX[m];
+      const double mx = gx0[m], my = gy0[m];
+      const long long bx = nonneg_bits(mx), by = nonneg_bits(my);
+      const bool inx = ox ? (bx >= half) : (bx <= half);
+      const bool iny = oy ? (by >= half) : (by <= half);
+      if (inx && iny) {
+        const double w = (ox ? mx : (1.0 - mx)) * (oy ? my : (1.0 - my));
+        sxy = sxy + w * dxy[m];
+        wxy = wxy + w;
+      }
+    }
+  }
+  double sxx = 0.0, syy = 0.0, wn = 0.0;
+  if (i >= 1 && j >= 1) {
+    const int c = (j - 1) * NC + (i - 1);
+    for (int m = cs[c]; m < cs[c + 1]; ++m) {
+      const double w = (1.0 - fabs(0.5 - gx0[m])) * (1.0 - fabs(0.5 - gy0[m]));
+      sxx += w * dxx[m];
+      syy += w * dyy[m];
+      wn += w;
+    }
+  }
+  const size_t q = (size_t)j * P.NX + i;
+  const double W = 0.0 + wxy, Wn = 0.0 + wn;
+  const double gxy = (W != 0.0) ? (0.0 + sxy) / W : 0.0;
+  const double gxx = (Wn != 0.0) ? (0.0 + sxx) / Wn : 0.0;
+  const double gyy = (Wn != 0.0) ? (0.0 + syy) / Wn : 0.0;
+  dsxx[q] = dsxx[q] + -1.0 * gxx;
+  dsyy[q] = dsyy[q] + -1.0 * gyy;
+  dsxy[q] = dsxy[q] + -1.0 * gxy;
+}
+
+struct StressCols {
+  const int *cellX, *cellY;
+  const double *X, *Y;
+  double *sxx, *syy, *sxy;
+};
+
+// updateMarkerStress (updateMarkerStress.c:60-144)
+__global__ void k_update_marker_stress(Params P, StressCols c, Geo g, Nodal nd, int64_t n, Status *st) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int cx = c.cellX[m], cy = c.cellY[m];
+  if (cx == -1) return;
+  int i, j;
+  double mdx, mdy;
+  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], i, j, mdx, mdy);
+  const double mdsxx = interp_run(nd.dsxx, P.NX, i, j, mdx, mdy);
+  const double mdsyy = interp_run(nd.dsyy, P.NX, i, j, mdx, mdy);
+  c.sxx[m] = c.sxx[m] + mdsxx;
+  c.syy[m] = c.syy[m] + mdsyy;
+  const double mdsxy = interp_run(nd.dsxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]);
+  c.sxy[m] = c.sxy[m] + mdsxy;
+  if (isnan(mdsxy)) atomicAdd(&st->nan_dsxy, 1ULL);
+}
+
+struct SubTCols {
+  const int *cellX, *cellY;
+  double *T, *Tdot;
+  double *dTsub;
+};
+
+// subgridTemperatureChanges, first marker loop (subgridTemperatureChanges.c:45-70)
+__global__ void k_subgridT_markers(Params P, SubTCols c, Geo g, const double *__restrict__ Tn,
+                                   const double *__restrict__ rn, const double *__restrict__ cpn,
+                                   const double *__restrict__ kn, double rho0, double D, double dt, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int i = c.cellX[m], j = c.cellY[m];
+  if (i == -1) return;
+  const int NX = P.NX;
+  const size_t k00 = (size_t)j * NX + i, k10 = k00 + 1, k01 = k00 + NX, k11 = k01 + 1;
+  const double dx = P.x[i + 1] - P.x[i], dy = P.y[j + 1] - P.y[j];
+  const double mdx = g.gx0[m], mdy = g.gy0[m];
+  const double Tm = Tn[k00] * (1.0 - mdx) * (1.0 - mdy) + Tn[k10] * mdx * (1.0 - mdy) +
+                    Tn[k01] * (1.0 - mdx) * (mdy) + Tn[k11] * mdx * mdy;
+  const double rhom = rho0 + rn[k00] * (1.0 - mdx) * (1.0 - mdy) + rn[k10] * (mdx) * (1.0 - mdy) +
+                      rn[k01] * (1.0 - mdx) * (mdy) + rn[k11] * mdx * mdy;
+  const double cpm = cpn[k00] * (1.0 - mdx) * (1.0 - mdy) + cpn[k10] * (mdx) * (1.0 - mdy) +
+                     cpn[k01] * (1.0 - mdx) * (mdy) + cpn[k11] * mdx * mdy;
+  const double km = kn[k00] * (1.0 - mdx) * (1.0 - mdy) + kn[k10] * (mdx) * (1.0 - mdy) +
+                    kn[k01] * (1.0 - mdx) * (mdy) + kn[k11] * mdx * mdy;
+  const double tdiff = cpm * rhom / km / (2.0 / (dx * dx) + 2.0 / (dy * dy));
+  c.dTsub[m] = (Tm - c.T[m]) * (1.0 - exp(-D * dt / tdiff));
+}
+
+// nodal remainder thisT - lastT - projected subgrid change (VecAXPBYPCZ with alpha = 1)
+__global__ void k_subgridT_nodes(const double *thisT, const double *lastT, const double *proj, double *dT,
+                                 int64_t nn) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= nn) return;
+  dT[q] = thisT[q] + -1.0 * lastT[q] + -1.0 * proj[q];
+}
+
+// subgridTemperatureChanges, second marker loop (subgridTemperatureChanges.c:87-103)
+__global__ void k_subgridT_apply(Params P, SubTCols c, Geo g, const double *__restrict__ dT, double dt, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int i = c.cellX[m], j = c.cellY[m];
+  if (i == -1) return;
+  const size_t k00 = (size_t)j * P.NX + i;
+  const double mdx = g.gx0[m], mdy = g.gy0[m];
+  const double dtm = (dT[k00] * (1.0 - mdy) * (1.0 - mdx) + dT[k00 + P.NX] * mdy * (1.0 - mdx) +
+                      dT[k00 + 1] * (1.0 - mdy) * mdx + dT[k00 + P.NX + 1] * mdy * mdx) +
+                     c.dTsub[m];
+  c.T[m] = c.T[m] + dtm;
+  c.Tdot[m] = dtm / dt;
+}
+
+struct AdvectCols {
+  const int *cellX, *cellY;
+  double *X, *Y, *VX, *VY, *wxy, *sxx, *syy, *sxy, *Eii;
+  const double *exx, *eyy, *exy;
+};
+
+// advectMarkersRK (markers.c:1865-2250), non-periodic grid, non-JAUMANN rotation
+__global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, const double *__restrict__ vy,
+                         const double *__restrict__ wz, mic_bcinfo top, mic_bcinfo left, double dt, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int ci = c.cellX[m], cj = c.cellY[m];
+  if (ci == -1) return;
+  const int NX = P.NX, NY = P.NY;
+  const double X0 = c.X[m], Y0 = c.Y[m];
+  double xcur = X0, ycur = Y0;
+  double mvx[4], mvy[4], mwz[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    int i = ci, j = cj;
+    if (xcur > P.x[i + 1]) {
+      while (xcur > P.x[i + 1] && i < NX - 2) i++;
+    } else if (xcur < P.x[i]) {
+      while (xcur < P.x[i] && i > 0) i--;
+    }
+    if (ycur > P.y[j + 1]) {
+      while (ycur > P.y[j + 1] && j < NY - 2) j++;
+    } else if (ycur < P.y[j]) {
+      while (ycur < P.y[j] && j > 0) j--;
+    }
+    int vxX = i, vxY = j, vyX = i, vyY = j;
+    if (vxY > -1 && ycur < P.yc[vxY + 1]) vxY--;
+    if (vyX > -1 && xcur < P.xc[vyX + 1]) vyX--;
+    vxX = clampi(vxX, 0, NX - 2);
+    vyX = clampi(vyX, -1, NX - 2);
+    vxY = clampi(vxY, -1, NY - 2);
+    vyY = clampi(vyY, 0, NY - 2);
+    double ax = xcur - P.x[vxX];
+    double ay = ycur - P.yc[vxY + 1];
+    double hx = P.x[vxX + 1] - P.x[vxX];
+    double hy = P.yc[vxY + 2] - P.yc[vxY + 1];
+    const size_t r1 = (size_t)(vxY + 1) * NX;
+    double vul, vur;
+    if (vxY == -1 && top.type[0] == 0) {
+      vul = 2.0 * top.value[0] - vx[r1 + vxX];
+      vur = 2.0 * top.value[0] - vx[r1 + vxX + 1];
+    } else if (vxY == -1) {
+      vul = vx[r1 + vxX];
+      vur = vx[r1 + vxX + 1];
+    } else {
+      vul = vx[r1 - NX + vxX];
+      vur = vx[r1 - NX + vxX + 1];
+    }
+    const double vll = vx[r1 + vxX], vlr = vx[r1 + vxX + 1];
+    double t = vul * (1.0 - ax / hx) * (1.0 - ay / hy);
+    t += vur * (ax / hx) * (1.0 - ay / hy);
+    t += vll * (1.0 - ax / hx) * (ay / hy);
+    t += vlr * (ax * ay) / hx / hy;
+    mvx[s] = t;
+    const size_t q0 = (size_t)vyY * NX, q1 = q0 + NX;
+    const double wur = vy[q0 + vyX + 1], wlr = vy[q1 + vyX + 1];
+    double wul, wll;
+    if (vyX == -1 && left.type[1] == 0) {
+      wul = 2.0 * left.value[1] - vy[q0 + vyX + 1];
+      wll = 2.0 * left.value[1] - vy[q1 + vyX + 1];
+    } else if (vyX == -1) {
+      wul = vy[q0 + vyX + 1];
+      wll = vy[q1 + vyX + 1];
+    } else {
+      wul = vy[q0 + vyX];
+      wll = vy[q1 + vyX];
+    }
+    ax = xcur - P.xc[vyX + 1];
+    ay = ycur - P.y[vyY];
+    hx = P.xc[vyX + 2] - P.xc[vyX + 1];
+    hy = P.y[vyY + 1] - P.y[vyY];
+    t = wul * (1.0 - ax / hx) * (1.0 - ay / hy);
+    t += wur * (ax / hx) * (1.0 - ay / hy);
+    t += wll * (1.0 - ax / hx) * (ay / hy);
+    t += wlr * (ax * ay) / hx / hy;
+    mvy[s] = t;
+    const double mdx = (xcur - P.x[i]) / (P.x[i + 1] - P.x[i]);
+    const double mdy = (ycur - P.y[j]) / (P.y[j + 1] - P.y[j]);
+    const size_t w0 = (size_t)j * NX + i;
+    t = (1.0 - mdx) * (1.0 - mdy) * wz[w0];
+    t += (mdx) * (1.0 - mdy) * wz[w0 + 1];
+    t += (1.0 - mdx) * (mdy)*wz[w0 + NX];
+    t += (mdx) * (mdy)*wz[w0 + NX + 1];
+    mwz[s] = t;
+    if (s < 2) {
+      xcur = X0 + dt / 2 * mvx[s];
+      ycur = Y0 + dt / 2 * mvy[s];
+    } else if (s == 2) {
+      xcur = X0 + dt * mvx[s];
+      ycur = Y0 + dt * mvy[s];
+    }
+  }
+  const double VX = (mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]) / 6;
+  const double VY = (mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]) / 6;
+  const double w = (mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]) / 6.0;
+  c.VX[m] = VX;
+  c.VY[m] = VY;
+  c.wxy[m] = w;
+  c.X[m] = X0 + dt * VX;
+  c.Y[m] = Y0 + dt * VY;
+  const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+  const double th = -w * dt;
+  const double ct = cos(th), st_ = sin(th), s2 = sin(2.0 * th), c2 = cos(2.0 * th);
+  c.sxx[m] = s11 * (ct * ct) + s22 * (st_ * st_) - s12 * s2;
+  c.syy[m] = s11 * (st_ * st_) + s22 * (ct * ct) + s12 * s2;
+  c.sxy[m] = 0.5 * (s11 - s22) * s2 + s12 * c2;
+  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
+  c.Eii[m] = c.Eii[m] + dt * sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+}
+
+// max over in-domain markers of v (or |v|), starting from 0 (main_subduction.c:271-281, 437-448)
+__global__ void k_max(const int *cellX, const double *v, int absval, int64_t n, unsigned long long *out) {
+  __shared__ long long sh[kBlock];
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  long long b = 0;  // bits of 0.0
+  if (m < n && cellX[m] != -1) {
+    double x = v[m];
+    if (absval) x = fabs(x);
+    if (x > 0.0) b = __double_as_longlong(x);
+  }
+  sh[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] = max(sh[threadIdx.x], sh[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && sh[0] > 0) atomicMax(out, (unsigned long long)sh[0]);
+}
+
+// projectNodalFieldToMarkersS (markers.c:1670-1706)
+__global__ void k_nodal_to_markers(Params P, const int *cellX, const int *cellY, Geo g, const double *f,
+                                   double *dst, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int i = cellX[m], j = cellY[m];
+  if (i == -1) return;
+  const double mdx = g.gx0[m], mdy = g.gy0[m];
+  const size_t k = (size_t)j * P.NX + i;
+  dst[m] = f[k] * (1 - mdx) * (1 - mdy) + f[k + P.NX] * (1 - mdx) * mdy + f[k + 1] * (mdx) * (1 - mdy) +
+           f[k + P.NX + 1] * mdx * mdy;
+}
+
+Geo geo_of(mic_ctx *ctx) {
+  Geo g;
+  g.gx0 = ctx->geo[0];
+  g.gy0 = ctx->geo[1];
+  g.gx1 = ctx->geo[2];
+  g.gy1 = ctx->geo[3];
+  g.flags = ctx->geo_flags;
+  return g;
+}
+
+Nodal nodal_of(mic_ctx *ctx) {
+  Nodal d;
+  d.p = ctx->nodal[MIC_NF_P];
+  d.exx = ctx->nodal[MIC_NF_EDOTXX];
+  d.exy = ctx->nodal[MIC_NF_EDOTXY];
+  d.soxx = ctx->nodal[MIC_NF_SOXX];
+  d.soyy = ctx->nodal[MIC_NF_SOYY];
+  d.soxy = ctx->nodal[MIC_NF_SOXY];
+  d.dsxx = ctx->nodal[MIC_NF_DSXX];
+  d.dsyy = ctx->nodal[MIC_NF_DSYY];
+  d.dsxy = ctx->nodal[MIC_NF_DSXY];
+  d.wxy = ctx->nodal[MIC_NF_WXY];
+  return d;
+}
+
+YieldCols yield_cols(mic_ctx *ctx) {
+  YieldCols c;
+  c.cellX = ctx->i32[C_CELLX];
+  c.mat = ctx->i32[C_MAT];
+  c.X = ctx->f64[C_X];
+  c.Y = ctx->f64[C_Y];
+  c.T = ctx->f64[C_T];
+  c.p = ctx->f64[C_P];
+  c.Eii = ctx->f64[C_EII];
+  c.exx = ctx->f64[C_EXX];
+  c.eyy = ctx->f64[C_EYY];
+  c.exy = ctx->f64[C_EXY];
+  c.eta = ctx->f64[C_ETA];
+  c.mu = ctx->f64[C_MU];
+  c.sxx = ctx->f64[C_SXX];
+  c.syy = ctx->f64[C_SYY];
+  c.sxy = ctx->f64[C_SXY];
+  return c;
+}
+
+int read_status(mic_ctx *ctx) {
+  MIC_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+int run_max(mic_ctx *ctx, int col, int absval, double *out) {
+  unsigned long long *d = reinterpret_cast<unsigned long long *>(ctx->red_buf + 8);
+  MIC_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
+  if (ctx->n > 0) {
+    k_max<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->f64[col], absval, ctx->n, d);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  if (out) {
+    unsigned long long h = 0;
+    MIC_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    double v;
+    memcpy(&v, &h, sizeof(v));
+    *out = v;
+  }
+  return MIC_OK;
+}
+
+}  // namespace
+
+#define CHECK_CTX()                 \
+  if (!ctx) return MIC_ERR_ARG;     \
+  cudaSetDevice(ctx->device)
+
+extern "C" int mic_update_marker_rho(mic_ctx *ctx) {
+  CHECK_CTX();
+  int e = mic_ensure_sorted(ctx);
+  if (e) return e;
+  if (ctx->n == 0) return MIC_OK;
+  k_update_rho<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
+                                                             ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n);
+  MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
+
+extern "C" int mic_max_marker_T(mic_ctx *ctx, double *maxT) {
+  CHECK_CTX();
+  int e = mic_ensure_sorted(ctx);
+  if (e) return e;
+  return run_max(ctx, C_T, 0, maxT);
+}
+
+extern "C" int mic_max_abs_sxx(mic_ctx *ctx, double *v) {
+  CHECK_CTX();
+  return run_max(ctx, C_SXX, 1, v);
+}
+
+static int yield_launch(mic_ctx *ctx, double dt) {
+  int e = mic_ensure_sorted(ctx);
+  if (e) return e;
+  MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->is_yielding, 0, sizeof(int), ctx->stream));
+  MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->bad_law, 0, sizeof(unsigned long long), ctx->stream));
+  if (ctx->n > 0) {
+    k_yield<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, dt, ctx->n,
+                                                          ctx->d_status);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  return MIC_OK;
+}
+
+extern "C" int mic_check_plastic_yielding(mic_ctx *ctx, double dt, int *is_yielding, double elapsed_time) {
+  CHECK_CTX();
+  (void)elapsed_time;  // only read by the SANDBOX build of the reference
+  int e = yield_launch(ctx, dt);
+  if (e) return e;
+  if ((e = read_status(ctx))) return e;
+  if (is_yielding) *is_yielding = ctx->h_status->is_yielding;
+  return ctx->h_status->bad_law ? MIC_ERR_LAW : MIC_OK;
+}
+
+extern "C" int mic_update_viscosity(mic_ctx *ctx) {
+  CHECK_CTX();
+  int e = mic_ensure_sorted(ctx);
+  if (e) return e;
+  MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->bad_law, 0, sizeof(unsigned long long), ctx->stream));
+  if (ctx->n > 0) {
+    k_update_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->n,
+                                                                     ctx->d_status);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  if ((e = read_status(ctx))) return e;
+  return ctx->h_status->bad_law ? MIC_ERR_LAW : MIC_OK;
+}
+
+extern "C" int mic_limit_viscosity(mic_ctx *ctx) {
+  CHECK_CTX();
+  if (ctx->n == 0) return MIC_OK;
+  k_limit_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->f64[C_ETA], ctx->opt.etamin,
+                                                                  ctx->opt.etamax, ctx->n);
+  MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
+
+static int strain_launch(mic_ctx *ctx, double dt) {
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->nan_residual, 0, sizeof(unsigned long long), ctx->stream));
+  if (ctx->n == 0) return MIC_OK;
+  StrainCols c;
+  c.cellX = ctx->i32[C_CELLX];
+  c.cellY = ctx->i32[C_CELLY];
+  c.X = ctx->f64[C_X];
+  c.Y = ctx->f64[C_Y];
+  c.eta = ctx->f64[C_ETA];
+  c.mu = ctx->f64[C_MU];
+  c.p = ctx->f64[C_P];
+  c.exx = ctx->f64[C_EXX];
+  c.eyy = ctx->f64[C_EYY];
+  c.exy = ctx->f64[C_EXY];
+  c.wxy = ctx->f64[C_WXY];
+  c.srr = ctx->f64[C_SRR];
+  k_strain_pressure<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n,
+                                                                  ctx->d_status);
+  MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
+
+extern "C" int mic_update_marker_strain_pressure(mic_ctx *ctx, double dt) {
+  CHECK_CTX();
+  int e = strain_launch(ctx, dt);
+  if (e) return e;
+  if ((e = read_status(ctx))) return e;
+  return ctx->h_status->nan_residual ? MIC_ERR_NAN : MIC_OK;
+}
+
+static int residual_launch(mic_ctx *ctx, int iter, double *res_dev) {
+  int e = mic_project_scalar(ctx, ctx->f64[C_SRR], -1, ctx->nodal[MIC_NF_SRR]);
+  if (e) return e;
+  const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
+  const int nb = (int)grid_for(nn);
+  double *partial = ctx->node_scr[5];  // NX*NY >= number of blocks
+  k_residual_weight<<<nb, kBlock, 0, ctx->stream>>>(ctx->P, ctx->nodal[MIC_NF_SRR], partial);
+  MIC_CUDA_TRY(cudaGetLastError());
+  k_sum_partials<<<1, 1024, 0, ctx->stream>>>(partial, nb, res_dev);
+  MIC_CUDA_TRY(cudaGetLastError());
+  (void)iter;
+  return MIC_OK;
+}
+
+extern "C" int mic_update_global_strain_rate_residual(mic_ctx *ctx, int iter, double *residual) {
+  CHECK_CTX();
+  if (iter < 0) return MIC_ERR_ARG;
+  double *d = ctx->red_buf + 16;
+  int e = residual_launch(ctx, iter, d);
+  if (e) return e;
+  double s = 0.0;
+  MIC_CUDA_TRY(cudaMemcpyAsync(&s, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  s /= (ctx->P.LX * ctx->P.LY);
+  ctx->residuals[iter % 100] = s;
+  if (residual) *residual = s;
+  return MIC_OK;
+}
+
+// checkConvergence (residual.c:53-69)
+extern "C" int mic_check_convergence(mic_ctx *ctx, double atol, double rtol, int iter, int *converged) {
+  if (!ctx || !converged || iter < 0) return MIC_ERR_ARG;
+  const double r = ctx->residuals[iter % 100];
+  if (r < atol) {
+    *converged = 1;
+    return MIC_OK;
+  }
+  if (iter > 0) {
+    const double last = ctx->residuals[(iter - 1) % 100];
+    if (fabs((r - last) / last) < rtol) {
+      *converged = 2;
+      return MIC_OK;
+    }
+  }
+  *converged = 0;
+  return MIC_OK;
+}
+
+extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
+  CHECK_CTX();
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  if (ctx->n > 0) {
+    SubgridCols c;
+    c.cellX = ctx->i32[C_CELLX];
+    c.cellY = ctx->i32[C_CELLY];
+    c.X = ctx->f64[C_X];
+    c.Y = ctx->f64[C_Y];
+    c.eta = ctx->f64[C_ETA];
+    c.mu = ctx->f64[C_MU];
+    c.sxx = ctx->f64[C_SXX];
+    c.syy = ctx->f64[C_SYY];
+    c.sxy = ctx->f64[C_SXY];
+    c.dxy = ctx->scr0;
+    c.dxx = ctx->scr1;
+    c.dyy = ctx->scr2;
+    k_subgrid_stress_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
+                                                                           D, ctx->n);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  dim3 grid((ctx->P.NX + 127) / 128, ctx->P.NY);
+  k_subgrid_stress_nodes<<<grid, 128, 0, ctx->stream>>>(ctx->P, ctx->i32[C_CELLX], ctx->geo[0], ctx->geo[1],
+                                                        ctx->scr0, ctx->scr1, ctx->scr2, ctx->cell_start,
+                                                        ctx->nodal[MIC_NF_DSXX], ctx->nodal[MIC_NF_DSYY],
+                                                        ctx->nodal[MIC_NF_DSXY]);
+  MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
+
+static int stress_launch(mic_ctx *ctx) {
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->nan_dsxy, 0, sizeof(unsigned long long), ctx->stream));
+  if (ctx->n == 0) return MIC_OK;
+  StressCols c;
+  c.cellX = ctx->i32[C_CELLX];
+  c.cellY = ctx->i32[C_CELLY];
+  c.X = ctx->f64[C_X];
+  c.Y = ctx->f64[C_Y];
+  c.sxx = ctx->f64[C_SXX];
+  c.syy = ctx->f64[C_SYY];
+  c.sxy = ctx->f64[C_SXY];
+  k_update_marker_stress<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), ctx->n,
+                                                                       ctx->d_status);
+  MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
+
+extern "C" int mic_update_marker_stress(mic_ctx *ctx) {
+  CHECK_CTX();
+  return stress_launch(ctx);
+}
+
+extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
+  CHECK_CTX();
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  SubTCols c;
+  c.cellX = ctx->i32[C_CELLX];
+  c.cellY = ctx->i32[C_CELLY];
+  c.T = ctx->f64[C_T];
+  c.Tdot = ctx->f64[C_TDOT];
+  c.dTsub = ctx->scr0;
+  if (ctx->n > 0) {
+    k_subgridT_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(
+        ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_LASTT], ctx->nodal[MIC_NF_RHO], ctx->nodal[MIC_NF_CP],
+        ctx->nodal[MIC_NF_KTHERMAL], ctx->mat.materialRho[0], ctx->opt.subgridTemperatureDiffusivity, dt, ctx->n);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  if ((e = mic_project_scalar(ctx, ctx->scr0, 0, ctx->node_scr[0]))) return e;
+  const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
+  k_subgridT_nodes<<<grid_for(nn), kBlock, 0, ctx->stream>>>(ctx->nodal[MIC_NF_THIST], ctx->nodal[MIC_NF_LASTT],
+                                                             ctx->node_scr[0], ctx->node_scr[1], nn);
+  MIC_CUDA_TRY(cudaGetLastError());
+  if (ctx->n > 0) {
+    k_subgridT_apply<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->node_scr[1], dt,
+                                                                   ctx->n);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  return MIC_OK;
+}
+
+extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
+  CHECK_CTX();
+  int e = mic_ensure_sorted(ctx);
+  if (e) return e;
+  if (ctx->n > 0) {
+    AdvectCols c;
+    c.cellX = ctx->i32[C_CELLX];
+    c.cellY = ctx->i32[C_CELLY];
+    c.X = ctx->f64[C_X];
+    c.Y = ctx->f64[C_Y];
+    c.VX = ctx->f64[C_VX];
+    c.VY = ctx->f64[C_VY];
+    c.wxy = ctx->f64[C_WXY];
+    c.sxx = ctx->f64[C_SXX];
+    c.syy = ctx->f64[C_SYY];
+    c.sxy = ctx->f64[C_SXY];
+    c.Eii = ctx->f64[C_EII];
+    c.exx = ctx->f64[C_EXX];
+    c.eyy = ctx->f64[C_EYY];
+    c.exy = ctx->f64[C_EXY];
+    k_advect<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY],
+                                                           ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
+                                                           ctx->bcs.mechBCLeft, dt, ctx->n);
+    MIC_CUDA_TRY(cudaGetLastError());
+  }
+  // positions moved: cells, order and geometry are stale until the next binning
+  ctx->sorted = 0;
+  ctx->geo_valid = 0;
+  return MIC_OK;
+}
+
+extern "C" int mic_project_nodal_field_to_markers(mic_ctx *ctx, int f, int off) {
+  CHECK_CTX();
+  if (f < 0 || f >= MIC_NF_COUNT) return MIC_ERR_ARG;
+  const int col = mic_f64_column_of_offset(off);
+  if (col < 0) return MIC_ERR_ARG;
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  if (ctx->n == 0) return MIC_OK;
+  k_nodal_to_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->i32[C_CELLX], ctx->i32[C_CELLY],
+                                                                   geo_of(ctx), ctx->nodal[f], ctx->f64[col], ctx->n);
+  MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
+
+// ---- step drivers ------------------------------------------------------------------
+
+extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yielding, double *max_T) {
+  CHECK_CTX();
+  int e;
+  // findMarkerCells (main:243, 247, 252): positions do not change between the three calls on
+  // one rank without density control, so one binning gives all three results
+  if ((e = mic_bin_and_sort(ctx, nullptr))) return e;
+  if ((e = mic_update_marker_rho(ctx))) return e;
+  if ((e = mic_project_markers_nodes_all2(ctx))) return e;
+  if ((e = run_max(ctx, C_T, 0, nullptr))) return e;
+  if ((e = yield_launch(ctx, dt_disp))) return e;
+  if ((e = mic_limit_viscosity(ctx))) return e;
+  if ((e = mic_project_markers_nodes_all2(ctx))) return e;
+  if (is_yielding || max_T) {
+    if ((e = read_status(ctx))) return e;
+    if (is_yielding) *is_yielding = ctx->h_status->is_yielding;
+    if (max_T) {
+      unsigned long long h = 0;
+      MIC_CUDA_TRY(cudaMemcpyAsync(&h, ctx->red_buf + 8, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+      MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+      memcpy(max_T, &h, sizeof(double));
+    }
+  }
+  return MIC_OK;
+}
+
+extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_stress, double *residual) {
+  CHECK_CTX();
+  int e;
+  if ((e = strain_launch(ctx, dt_disp))) return e;
+  double *d = ctx->red_buf + 16;
+  if ((e = residual_launch(ctx, 0, d))) return e;
+  if (subgrid_stress && ctx->opt.subgridStressDiffusivity > 0.0)
+    if ((e = mic_subgrid_stress_changes(ctx, dt_disp, ctx->opt.subgridStressDiffusivity))) return e;
+  if ((e = stress_launch(ctx))) return e;
+  if (residual) {
+    double s = 0.0;
+    MIC_CUDA_TRY(cudaMemcpyAsync(&s, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    s /= (ctx->P.LX * ctx->P.LY);
+    ctx->residuals[0] = s;
+    *residual = s;
+  }
+  return MIC_OK;
+}
+
+extern "C" int mic_step_post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx) {
+  CHECK_CTX();
+  int e;
+  if ((e = mic_subgrid_temperature_changes(ctx, dt_thermal))) return e;
+  if ((e = mic_advect_markers_rk(ctx, dt_thermal))) return e;
+  return run_max(ctx, C_SXX, 1, max_abs_sxx);
+}
+
+extern "C" int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, double *residual) {
+  CHECK_CTX();
+  int e;
+  if ((e = mic_step_pre_stokes(ctx, dt_disp, nullptr, nullptr))) return e;
+  if ((e = mic_step_post_stokes(ctx, dt_disp, subgrid_stress, residual))) return e;
+  return mic_step_post_thermal(ctx, dt_thermal, nullptr);
+}

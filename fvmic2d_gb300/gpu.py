@@ -1,0 +1,279 @@
+"""Python host side of the GB300 marker path: ctypes over the C ABI of libmic_gb300.so.
+
+``MicProblem`` mirrors fvmic2d's entry points (findMarkerCells,
+projectMarkersNodesAll2, checkPlasticYielding, ...) with the reference's argument
+meaning, so a test can drive the same sequence through the reference build, the CPU
+oracle and the GPU.  There is no CPU fallback: a missing library or GPU raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .mic_types import MARKER_DTYPE, MARKER_F64_OFFSETS, NF
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+
+SIGNATURES = {
+    "mic_version": (_I, []),
+    "mic_error_string": (ctypes.c_char_p, [_I]),
+    "mic_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _I, _D, _D, _DP, _DP, _I64]),
+    "mic_destroy": (_I, [_P]),
+    "mic_set_materials": (_I, [_P, _P]),
+    "mic_set_options": (_I, [_P, _P]),
+    "mic_set_bcs": (_I, [_P, _P]),
+    "mic_get_grid_centres": (_I, [_P, _DP, _DP]),
+    "mic_markers_upload": (_I, [_P, _P, _I64]),
+    "mic_markers_download": (_I, [_P, _P, _I64]),
+    "mic_markers_count": (_I, [_P, _I64P]),
+    "mic_nodal_upload": (_I, [_P, _I, _DP]),
+    "mic_nodal_download": (_I, [_P, _I, _DP]),
+    "mic_nodal_device_ptr": (_I, [_P, _I, ctypes.POINTER(_DP)]),
+    "mic_find_marker_cells": (_I, [_P, _I64P]),
+    "mic_update_marker_rho": (_I, [_P]),
+    "mic_max_marker_T": (_I, [_P, _DP]),
+    "mic_project_markers_nodes_all2": (_I, [_P]),
+    "mic_project_marker_field_to_nodes": (_I, [_P, _I, _DP, _I, _I, _I, _I]),
+    "mic_project_nodal_field_to_markers": (_I, [_P, _I, _I]),
+    "mic_check_plastic_yielding": (_I, [_P, _D, _IP, _D]),
+    "mic_update_viscosity": (_I, [_P]),
+    "mic_limit_viscosity": (_I, [_P]),
+    "mic_update_marker_strain_pressure": (_I, [_P, _D]),
+    "mic_update_global_strain_rate_residual": (_I, [_P, _I, _DP]),
+    "mic_check_convergence": (_I, [_P, _D, _D, _I, _IP]),
+    "mic_subgrid_stress_changes": (_I, [_P, _D, _D]),
+    "mic_update_marker_stress": (_I, [_P]),
+    "mic_subgrid_temperature_changes": (_I, [_P, _D]),
+    "mic_advect_markers_rk": (_I, [_P, _D]),
+    "mic_max_abs_sxx": (_I, [_P, _DP]),
+    "mic_step_pre_stokes": (_I, [_P, _D, _IP, _DP]),
+    "mic_step_post_stokes": (_I, [_P, _D, _I, _DP]),
+    "mic_step_post_thermal": (_I, [_P, _D, _DP]),
+    "mic_step": (_I, [_P, _D, _D, _I, _DP]),
+    "mic_synchronize": (_I, [_P]),
+    "mic_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
+    "mic_get_status": (_I, [_P, _P]),
+    "mic_debug_sorted_ids": (_I, [_P, _P]),
+    "mic_debug_cell_start": (_I, [_P, _P]),
+    "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
+    "mic_host_free": (_I, [_P]),
+}
+
+_libs = {}
+
+
+class MicError(RuntimeError):
+    def __init__(self, code, what):
+        self.code = code
+        super().__init__("%s failed: %s (code %d)" % (what, load().mic_error_string(code).decode(), code))
+
+
+def library_path(exact=False):
+    return os.path.join(HERE, "libmic_gb300_exact.so" if exact else "libmic_gb300.so")
+
+
+def load(exact=False):
+    """Load the CUDA library; raises if it was not built (there is no fallback)."""
+    key = bool(exact)
+    if key not in _libs:
+        path = library_path(exact)
+        if not os.path.exists(path):
+            raise RuntimeError("%s is missing: run __graft_entry__.build() (nvcc, sm_103a)" % path)
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _libs[key] = L
+    return _libs[key]
+
+
+class Status(ctypes.Structure):
+    _fields_ = [("bad_cell", ctypes.c_uint64), ("nan_residual", ctypes.c_uint64), ("nan_dsxy", ctypes.c_uint64),
+                ("bad_law", ctypes.c_uint64), ("n_out", ctypes.c_uint64), ("is_yielding", ctypes.c_int32)]
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+class MicProblem:
+    """A device context holding one grid, its nodal fields and a marker set."""
+
+    def __init__(self, wl, markers=None, exact=False, device=0, capacity=None, stream=None):
+        self.L = L = load(exact)
+        g = wl.grid
+        self.wl = wl
+        self.NX, self.NY = g.NX, g.NY
+        mk = wl.markers if markers is None else markers
+        cap = len(mk) if capacity is None else capacity
+        h = _P()
+        self._check(L.mic_create(ctypes.byref(h), device, stream, g.NX, g.NY, g.LX, g.LY, _dp(g.x), _dp(g.y), cap),
+                    "mic_create")
+        self.h = h
+        self.materials, self.options, self.bcs = wl.materials, wl.options, wl.bcs
+        self._check(L.mic_set_materials(self.h, ctypes.byref(self.materials)), "mic_set_materials")
+        self._check(L.mic_set_options(self.h, ctypes.byref(self.options)), "mic_set_options")
+        self._check(L.mic_set_bcs(self.h, ctypes.byref(self.bcs)), "mic_set_bcs")
+        self.upload_markers(mk)
+        for name, arr in wl.nodal.items():
+            self.set_nodal(name, arr)
+
+    def _check(self, code, what):
+        if code != 0:
+            raise MicError(code, what)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mic_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- transfers -----------------------------------------------------------
+    def upload_markers(self, mk):
+        mk = np.ascontiguousarray(mk, dtype=MARKER_DTYPE)
+        self.n = len(mk)
+        self._check(self.L.mic_markers_upload(self.h, mk.ctypes.data, self.n), "mic_markers_upload")
+
+    @property
+    def markers(self):
+        out = np.zeros(self.n, dtype=MARKER_DTYPE)
+        self._check(self.L.mic_markers_download(self.h, out.ctypes.data, self.n), "mic_markers_download")
+        return out
+
+    def set_nodal(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.NY, self.NX)
+        self._check(self.L.mic_nodal_upload(self.h, NF[name], _dp(a)), "mic_nodal_upload")
+
+    def get_nodal(self, name):
+        a = np.empty((self.NY, self.NX))
+        self._check(self.L.mic_nodal_download(self.h, NF[name], _dp(a)), "mic_nodal_download")
+        return a
+
+    def grid_centres(self):
+        xc = np.empty(self.NX + 1)
+        yc = np.empty(self.NY + 1)
+        self._check(self.L.mic_get_grid_centres(self.h, _dp(xc), _dp(yc)), "mic_get_grid_centres")
+        return xc, yc
+
+    def status(self):
+        s = Status()
+        self._check(self.L.mic_get_status(self.h, ctypes.byref(s)), "mic_get_status")
+        return s
+
+    def sorted_ids(self):
+        ids = np.empty(self.n, dtype=np.int32)
+        self._check(self.L.mic_debug_sorted_ids(self.h, ids.ctypes.data), "mic_debug_sorted_ids")
+        return ids
+
+    def cell_start(self):
+        cs = np.empty((self.NX - 1) * (self.NY - 1) + 2, dtype=np.int32)
+        self._check(self.L.mic_debug_cell_start(self.h, cs.ctypes.data), "mic_debug_cell_start")
+        return cs
+
+    def synchronize(self):
+        self._check(self.L.mic_synchronize(self.h), "mic_synchronize")
+
+    def stream(self):
+        s = _P()
+        self._check(self.L.mic_get_stream(self.h, ctypes.byref(s)), "mic_get_stream")
+        return s.value
+
+    # ---- fvmic2d entry points --------------------------------------------------
+    def findMarkerCells(self):
+        n = ctypes.c_int64(0)
+        self._check(self.L.mic_find_marker_cells(self.h, ctypes.byref(n)), "findMarkerCells")
+        return n.value
+
+    def updateMarkerRho(self):
+        self._check(self.L.mic_update_marker_rho(self.h), "updateMarkerRho")
+
+    def maxMarkerT(self):
+        v = ctypes.c_double(0.0)
+        self._check(self.L.mic_max_marker_T(self.h, ctypes.byref(v)), "maxMarkerT")
+        return v.value
+
+    def maxAbsSxx(self):
+        v = ctypes.c_double(0.0)
+        self._check(self.L.mic_max_abs_sxx(self.h, ctypes.byref(v)), "maxAbsSxx")
+        return v.value
+
+    def projectMarkersNodesAll2(self):
+        self._check(self.L.mic_project_markers_nodes_all2(self.h), "projectMarkersNodesAll2")
+        return 0
+
+    def projectMarkerFieldToNodes(self, field, out, stagx, stagy, method, matprop=None):
+        off = -1 if field is None else MARKER_F64_OFFSETS[field]
+        mp = None
+        if matprop is not None:
+            self._mp = np.zeros(8)
+            self._mp[: len(matprop)] = matprop
+            mp = _dp(self._mp)
+        self._check(self.L.mic_project_marker_field_to_nodes(self.h, off, mp, NF[out], stagx, stagy, method),
+                    "projectMarkerFieldToNodes")
+        return 0
+
+    def projectNodalFieldToMarkersS(self, nodal, field):
+        self._check(self.L.mic_project_nodal_field_to_markers(self.h, NF[nodal], MARKER_F64_OFFSETS[field]),
+                    "projectNodalFieldToMarkersS")
+        return 0
+
+    def checkPlasticYielding(self, dt, t=0.0):
+        y = ctypes.c_int(0)
+        self._check(self.L.mic_check_plastic_yielding(self.h, dt, ctypes.byref(y), t), "checkPlasticYielding")
+        return y.value
+
+    def updateViscosity(self):
+        self._check(self.L.mic_update_viscosity(self.h), "updateViscosity")
+
+    def limitViscosity(self):
+        self._check(self.L.mic_limit_viscosity(self.h), "limitViscosity")
+
+    def updateMarkerStrainPressure(self, dt):
+        self._check(self.L.mic_update_marker_strain_pressure(self.h, dt), "updateMarkerStrainPressure")
+        return 0
+
+    def updateGlobalStrainRateResidual(self, it=0):
+        r = ctypes.c_double(0.0)
+        self._check(self.L.mic_update_global_strain_rate_residual(self.h, it, ctypes.byref(r)),
+                    "updateGlobalStrainRateResidual")
+        return r.value
+
+    def checkConvergence(self, atol, rtol, it):
+        c = ctypes.c_int(0)
+        self._check(self.L.mic_check_convergence(self.h, atol, rtol, it, ctypes.byref(c)), "checkConvergence")
+        return c.value
+
+    def subgridStressChanges(self, dt, D):
+        self._check(self.L.mic_subgrid_stress_changes(self.h, dt, D), "subgridStressChanges")
+        return 0
+
+    def updateMarkerStress(self):
+        self._check(self.L.mic_update_marker_stress(self.h), "updateMarkerStress")
+        return 0
+
+    def subgridTemperatureChanges(self, dt):
+        self._check(self.L.mic_subgrid_temperature_changes(self.h, dt), "subgridTemperatureChanges")
+        return 0
+
+    def advectMarkersRK(self, dt):
+        self._check(self.L.mic_advect_markers_rk(self.h, dt), "advectMarkersRK")
+        return 0
+
+    def step(self, dt_disp, dt_thermal, subgrid_stress=True):
+        r = ctypes.c_double(0.0)
+        self._check(self.L.mic_step(self.h, dt_disp, dt_thermal, int(subgrid_stress), ctypes.byref(r)), "mic_step")
+        return 0, r.value

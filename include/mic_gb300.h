@@ -1,0 +1,150 @@
+/*
+ * mic_gb300.h -- C ABI of the GB300 marker-in-cell transfer library (libmic_gb300.so).
+ *
+ * The library replaces fvmic2d's marker-side routines -- the work between and
+ * around the host Stokes and thermal solves -- with CUDA kernels for sm_103a.
+ * Every entry point takes plain pointers and sizes; markers use the reference's
+ * 216-byte record (mic_marker == fdcode.h Marker), nodal fields the NX*NY
+ * global-vector layout ([j][i] = j*NX + i).  See INTEGRATION.md for the
+ * reference-side binding.
+ *
+ * State model: a context owns one grid, the device copies of every nodal field
+ * and up to `max_markers` markers kept on the device as columns.  Markers are
+ * re-ordered by cell on the device after binning; mic_markers_download always
+ * returns them in the caller's original order.  Calls on a context are
+ * serialised on the context's stream; entry points that return host values
+ * synchronise that stream.  All functions return 0 (MIC_OK) or an error code;
+ * none aborts the process (the reference aborts, see the codes below).
+ */
+#ifndef MIC_GB300_H
+#define MIC_GB300_H
+
+#include <stdint.h>
+#include "mic_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mic_ctx mic_ctx;
+
+enum {
+  MIC_OK = 0,
+  MIC_ERR_ARG = 1,        /* invalid argument (bad field id, stagger, method, size) */
+  MIC_ERR_CUDA = 2,       /* CUDA runtime error (context left usable where CUDA allows) */
+  MIC_ERR_NOMEM = 3,      /* device or host allocation failed */
+  MIC_ERR_CELL = 4,       /* impossible cell index; markers.c:74-77 aborts */
+  MIC_ERR_NAN = 5,        /* NaN strain-rate residual; updateMarkerStrainPressure.c:302-306 aborts */
+  MIC_ERR_LAW = 6,        /* undefined viscosity law; viscosity.c:60-62 aborts */
+  MIC_ERR_BC = 7,         /* boundary type whose ghost values the path would read (periodic) */
+  MIC_ERR_CAPACITY = 8,   /* more markers than the context was created for; markers.c:771-774 aborts */
+  MIC_ERR_NO_DEVICE = 9   /* no CUDA device: there is no CPU fallback */
+};
+
+typedef struct {
+  uint64_t bad_cell;      /* markers with an impossible cell index in the last binning */
+  uint64_t nan_residual;  /* markers with a NaN strain-rate residual */
+  uint64_t nan_dsxy;      /* markers whose interpolated dsxy was NaN (the reference only prints) */
+  uint64_t bad_law;       /* markers whose material has an undefined viscosity law */
+  uint64_t n_out;         /* out-of-domain markers after the last binning */
+  int32_t is_yielding;    /* any marker yielded in the last checkPlasticYielding */
+} mic_status;
+
+int mic_version(void);
+const char *mic_error_string(int code);
+
+/* ---- lifecycle: replaces GridData / NodalFields setup and allocateMarkers (markers.c:15-27) ---- */
+/* x[NX], y[NY] are the basic gridlines; cell centres follow getCellCenters (gridSpacing.c:150-157).
+ * stream: a cudaStream_t to run on, or NULL for a stream owned by the context. */
+int mic_create(mic_ctx **out, int device, void *stream, int NX, int NY, double LX, double LY, const double *x,
+               const double *y, int64_t max_markers);
+/* destroyMarkers (markers.c:29-39) + nodal field / grid teardown */
+int mic_destroy(mic_ctx *ctx);
+int mic_set_materials(mic_ctx *ctx, const mic_materials *materials);
+int mic_set_options(mic_ctx *ctx, const mic_options *options);
+/* BoundaryValues read by advectMarkersRK (markers.c:1986-2023); periodic walls are rejected */
+int mic_set_bcs(mic_ctx *ctx, const mic_bcs *bcs);
+int mic_get_grid_centres(mic_ctx *ctx, double *xc, double *yc); /* NX+1, NY+1 entries */
+
+/* ---- markers: host AoS records <-> device columns ---- */
+int mic_markers_upload(mic_ctx *ctx, const mic_marker *host, int64_t n);
+int mic_markers_download(mic_ctx *ctx, mic_marker *host, int64_t n);
+int mic_markers_count(mic_ctx *ctx, int64_t *n);
+
+/* ---- nodal fields (MIC_NF_* ids) ---- */
+int mic_nodal_upload(mic_ctx *ctx, int field, const double *host);
+int mic_nodal_download(mic_ctx *ctx, int field, double *host);
+int mic_nodal_device_ptr(mic_ctx *ctx, int field, double **device_ptr);
+
+/* ---- the marker path; each entry point replaces the reference function cited ---- */
+/* findMarkerCells (markers.c:85-106; markers.h:15) plus the stable counting sort by cell
+ * that orders the device columns; *n_out = markers outside the domain (MarkerSet.nOut). */
+int mic_find_marker_cells(mic_ctx *ctx, int64_t *n_out);
+/* density update inline in main_subduction.c:255-264 */
+int mic_update_marker_rho(mic_ctx *ctx);
+/* maximum marker temperature, main_subduction.c:271-289 */
+int mic_max_marker_T(mic_ctx *ctx, double *max_T);
+/* projectMarkersNodesAll2 (markerProjection.c:11-68; markerProjection.h:11) */
+int mic_project_markers_nodes_all2(mic_ctx *ctx);
+/* projectMarkerFieldToNodes (markerProjection.c:71-250; markerProjection.h:10).  The marker
+ * field is named by its byte offset inside the record (the reference passes &markers[0].field
+ * and strides by sizeof(Marker)); pass material_property (MIC_MAXMAT values) instead to
+ * project a per-material constant, as with materialkThermal / materialCp. */
+int mic_project_marker_field_to_nodes(mic_ctx *ctx, int marker_field_offset, const double *material_property,
+                                      int out_field, int stagx, int stagy, int method);
+/* projectNodalFieldToMarkersS (markers.c:1670-1706; markers.h:21) */
+int mic_project_nodal_field_to_markers(mic_ctx *ctx, int nodal_field, int marker_field_offset);
+/* checkPlasticYielding (markers.c:1381-1505; markers.h:14) with computeRheology
+ * (viscosity.c:12-67) */
+int mic_check_plastic_yielding(mic_ctx *ctx, double dt, int *is_yielding, double elapsed_time);
+/* updateViscosity (viscosity.c:77-88; viscosity.h:2) */
+int mic_update_viscosity(mic_ctx *ctx);
+/* limitViscosity (viscosity.c:90-104; viscosity.h:3) */
+int mic_limit_viscosity(mic_ctx *ctx);
+/* updateMarkerStrainPressure (updateMarkerStrainPressure.c:9-399; updateMarkerStrainPressure.h:1) */
+int mic_update_marker_strain_pressure(mic_ctx *ctx, double dt);
+/* updateGlobalStrainRateResidual (residual.c:12-51; residual.h:4) */
+int mic_update_global_strain_rate_residual(mic_ctx *ctx, int iter, double *residual);
+/* checkConvergence (residual.c:53-69; residual.h:5) over the stored residuals */
+int mic_check_convergence(mic_ctx *ctx, double atol, double rtol, int iter, int *converged);
+/* subgridStressChanges (subgridStressChanges.c:5-318; subgridStressChanges.h:1) */
+int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double diffusivity);
+/* updateMarkerStress (updateMarkerStress.c:5-163; updateMarkerStress.h:1) */
+int mic_update_marker_stress(mic_ctx *ctx);
+/* subgridTemperatureChanges (subgridTemperatureChanges.c:5-124; subgridTemperatureChanges.h:2);
+ * the new temperature (the reference's thisT argument) is nodal field MIC_NF_THIST */
+int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt);
+/* advectMarkersRK (markers.c:1865-2250; markers.h:20) */
+int mic_advect_markers_rk(mic_ctx *ctx, double dt);
+/* maximum |sxx| over in-domain markers, main_subduction.c:437-448 */
+int mic_max_abs_sxx(mic_ctx *ctx, double *max_abs_sxx);
+
+/* ---- one time step of the marker path, in main_subduction.c order (main:243-448) ----
+ * pre_stokes:   findMarkerCells, density update, projectMarkersNodesAll2, max T,
+ *               checkPlasticYielding, limitViscosity, projectMarkersNodesAll2
+ * post_stokes:  updateMarkerStrainPressure, updateGlobalStrainRateResidual,
+ *               subgridStressChanges (when subgrid_stress != 0), updateMarkerStress
+ * post_thermal: subgridTemperatureChanges, advectMarkersRK, max |sxx|
+ * mic_step runs all three with the nodal inputs already on the device. */
+int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yielding, double *max_T);
+int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_stress, double *residual);
+int mic_step_post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx);
+int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, double *residual);
+
+/* ---- plumbing ---- */
+int mic_synchronize(mic_ctx *ctx);
+int mic_get_stream(mic_ctx *ctx, void **stream);
+int mic_get_status(mic_ctx *ctx, mic_status *status);
+/* device order of the caller's marker indices and the per-cell start offsets
+ * ((NX-1)*(NY-1)+2 entries; the last two bracket the out-of-domain markers) */
+int mic_debug_sorted_ids(mic_ctx *ctx, int32_t *ids);
+int mic_debug_cell_start(mic_ctx *ctx, int32_t *cell_start);
+/* pinned host memory for fast transfers */
+int mic_host_alloc(void **ptr, int64_t bytes);
+int mic_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -900,3 +900,17 @@ double orc_gk_viscosity(double s, double T, double d, double P) {
   const double etot = ediff + 1.0 / (1.0 / ebs + 1.0 / egbs) + edisl;
   return s / 2.0 / etot;
 }
+
+/* sizes of the boundary structs as this compiler lays them out (checked against the
+ * ctypes mirrors by the tests) */
+int64_t orc_sizeof(int which) {
+  switch (which) {
+    case 0: return (int64_t)sizeof(mic_marker);
+    case 1: return (int64_t)sizeof(mic_materials);
+    case 2: return (int64_t)sizeof(mic_bcs);
+    case 3: return (int64_t)sizeof(mic_options);
+    case 4: return (int64_t)offsetof(mic_marker, cellX);
+    case 5: return (int64_t)offsetof(mic_materials, Tref);
+    default: return -1;
+  }
+}

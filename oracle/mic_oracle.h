@@ -71,6 +71,8 @@ int orc_step(orc_ctx *c, mic_marker *mk, int64_t n, double dt_disp, double dt_th
  * returns the effective viscosity at stress s, temperature T, grain size d, pressure P. */
 double orc_gk_viscosity(double s, double T, double d, double P);
 
+int64_t orc_sizeof(int which);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,7 @@ def lib():
             "orc_advect_markers_rk": (_I, [_P, _P, _I64, _D]),
             "orc_step": (_I, [_P, _P, _I64, _D, _D, _I, _DP]),
             "orc_gk_viscosity": (_D, [_D, _D, _D, _D]),
+            "orc_sizeof": (_I64, [_I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

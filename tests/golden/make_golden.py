@@ -1,0 +1,170 @@
+"""Generate the golden vectors in this directory from fvmic2d's OWN hot-path C.
+
+The reference sources are compiled against the single-rank petsc_lite stand-in by
+oracle/build_ref.sh (needs the reference tree, so this runs only where it exists).
+Each fixture records seeded inputs and the reference's outputs after every entry
+point of one marker-path step, so the CPU oracle and the GPU kernels can be
+checked against the reference anywhere, including machines without the tree.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from fvmic2d_gb300 import workloads as W  # noqa: E402
+from fvmic2d_gb300.mic_types import PROJECTED_FIELDS  # noqa: E402
+from oracle import build as obuild  # noqa: E402
+from oracle import refpy  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def edge_case_workload():
+    """Small VEP box whose markers include the reference's corner cases: markers exactly on
+    gridlines and cell centres (0.5 ties), at X = LX and Y = LY (cell NX-2 / NY-2,
+    markers.c:49-59), outside the domain and NaN (cellX = -1), and one material per
+    viscosity law and plasticity mode."""
+    wl = W.vep_slab_box(nx_cells=12, ny_cells=6, nm=2, seed=7)
+    g = wl.grid
+    m = wl.markers
+    extra = np.zeros(24, dtype=m.dtype)
+    pts = [
+        (g.x[3], g.y[2]), (g.x[5], g.yc[3]), (g.xc[4], g.y[4]), (g.xc[6], g.yc[2]),  # gridlines / centres
+        (g.LX, g.y[3]), (g.x[2], g.LY), (g.LX, g.LY), (0.0, 0.0), (-0.0, g.yc[1]),
+        (0.5 * (g.x[7] + g.x[8]), 0.5 * (g.y[1] + g.y[2])),  # exact 0.5 offsets
+        (-1.0, g.yc[2]), (g.LX * 1.0000001, g.yc[2]), (g.xc[3], -5.0), (np.nan, g.yc[2]),
+    ]
+    for k, (x, y) in enumerate(pts):
+        extra[k]["X"], extra[k]["Y"] = x, y
+    rng_u = W.splitmix64_uniform(99, 2 * 24)
+    for k in range(len(pts), len(extra)):
+        extra[k]["X"] = rng_u[2 * k] * g.LX
+        extra[k]["Y"] = rng_u[2 * k + 1] * g.LY
+    for f in ("T", "eta", "mu", "sxx", "syy", "sxy", "exx", "eyy", "exy", "p", "Eii"):
+        extra[f] = np.resize(m[f], len(extra))
+    extra["Mat"] = np.arange(len(extra)) % 6
+    m = np.concatenate([m, extra])
+    m["Mat"][: len(m) - len(extra)] = np.arange(len(m) - len(extra)) % 6
+    m["Eii"] = np.linspace(0.0, 2.0, len(m))
+    mat = wl.materials
+    mat.nMaterials = 6
+    laws = [0, 1, 2, 3, 5, 6]
+    for k in range(6):
+        mat.materialEta[k] = [1e21, 1e21, 1e22, 1e18, 1e22, 1e21][k]
+        mat.materialRho[k] = 3300.0 + 10 * k
+        mat.materialkThermal[k] = 3.0 + 0.1 * k
+        mat.materialCp[k] = 1250.0 - 5 * k
+        mat.materialAlpha[k] = 3e-5
+        mat.materialMu[k] = 1e10
+        mat.hasEtaT[k] = laws[k]
+        mat.QonR[k] = 2.0e4 if k != 4 else 1e-3
+        mat.Tref[k] = 1573.0
+    mat.hasPlasticity[1] = 1
+    mat.materialCohesion[1] = 1e7
+    mat.materialFriction[1] = 0.6
+    mat.hasPlasticity[2] = 2  # strain weakening between gamma0 and gamma1
+    mat.gamma[2][0], mat.gamma[2][1] = 0.5, 1.5
+    mat.C[2][0], mat.C[2][1] = 2e7, 1e6
+    mat.F[2][0], mat.F[2][1] = 30.0, 10.0
+    mat.hasPlasticity[3] = 3  # unknown mode: yield stress 0
+    opt = wl.options
+    opt.slabAngle = 0.7
+    opt.decoupleThickness = 3e4
+    opt.minDecoupleDepth = 1e4
+    opt.maxDecoupleDepth = 6e4
+    opt.decoupleEtaScaler = 0.1
+    wl.markers = m
+    # prescribed-velocity walls exercise the ghost-velocity branches of advectMarkersRK
+    wl.bcs.mechBCTop.type[0] = 0
+    wl.bcs.mechBCTop.value[0] = 1e-10
+    wl.bcs.mechBCLeft.type[1] = 0
+    wl.bcs.mechBCLeft.value[1] = -2e-10
+    wl.name = "edge_cases"
+    return wl
+
+
+def record(wl, steps=2):
+    """Run `steps` reference steps; store inputs and the state after every entry point."""
+    p = refpy.RefProblem(wl)
+    out = {"x": wl.grid.x, "y": wl.grid.y, "LX": wl.grid.LX, "LY": wl.grid.LY,
+           "markers_in": wl.markers.copy(), "dt": wl.dt, "dt_thermal": wl.dt_thermal}
+    for name, arr in wl.nodal.items():
+        out["nodal_in_" + name] = np.asarray(arr, dtype=np.float64)
+    D = wl.options.subgridStressDiffusivity
+    for s in range(steps):
+        pre = "s%d_" % s
+        out[pre + "nout"] = p.findMarkerCells()
+        out[pre + "after_find"] = p.markers.copy()
+        p.updateMarkerRho()
+        p.projectMarkersNodesAll2()
+        for f in PROJECTED_FIELDS:
+            out[pre + "proj1_" + f] = p.get_nodal(f)
+        out[pre + "maxT"] = p.maxMarkerT()
+        out[pre + "yield"] = p.checkPlasticYielding(wl.dt)
+        out[pre + "after_yield"] = p.markers.copy()
+        p.limitViscosity()
+        p.projectMarkersNodesAll2()
+        for f in PROJECTED_FIELDS:
+            out[pre + "proj2_" + f] = p.get_nodal(f)
+        p.updateMarkerStrainPressure(wl.dt)
+        out[pre + "after_strain"] = p.markers.copy()
+        out[pre + "residual"] = p.updateGlobalStrainRateResidual(0)
+        if D > 0:
+            p.subgridStressChanges(wl.dt, D)
+            out[pre + "after_subgrid_stress"] = p.markers.copy()
+            for f in ("dsxx", "dsyy", "dsxy"):
+                out[pre + "ds_" + f] = p.get_nodal(f)
+        p.updateMarkerStress()
+        out[pre + "after_stress"] = p.markers.copy()
+        p.subgridTemperatureChanges(wl.dt_thermal)
+        out[pre + "after_subgrid_T"] = p.markers.copy()
+        p.advectMarkersRK(wl.dt_thermal)
+        out[pre + "after_advect"] = p.markers.copy()
+        out[pre + "maxSxx"] = p.maxAbsSxx()
+    p.close()
+    return out
+
+
+def tables(wl):
+    m, o, b = wl.materials, wl.options, wl.bcs
+    return {"materials_bytes": np.frombuffer(bytes(m), dtype=np.uint8),
+            "options_bytes": np.frombuffer(bytes(o), dtype=np.uint8),
+            "bcs_bytes": np.frombuffer(bytes(b), dtype=np.uint8)}
+
+
+def creep_table():
+    """viscosity.c:106-179 on a grid over the composite-creep workload ranges, including the
+    T = 255 K and 258 K parameter switches and the s < 1 Pa early return."""
+    s = np.concatenate([[0.0, 0.5, 0.999999, 1.0, 1.000001], np.logspace(0, 8, 23)])
+    T = np.array([100.0, 180.0, 254.999, 255.0, 257.0, 258.0, 265.0, 273.0])
+    d = np.array([1e-4, 1e-3, 1e-2, 1e-1])
+    P = np.array([0.0, 0.5, 1.0, 1e6, 1e8])
+    S, TT, DD, PP = np.meshgrid(s, T, d, P, indexing="ij")
+    eta = refpy.goldsby_kohlstedt(S.ravel(), TT.ravel(), DD.ravel(), PP.ravel())
+    return {"s": S.ravel(), "T": TT.ravel(), "d": DD.ravel(), "P": PP.ravel(), "eta": eta}
+
+
+def main():
+    if obuild.build_ref() is None:
+        raise SystemExit("reference tree not found; golden vectors can only be generated where it exists")
+    cases = {
+        "convection_box_8": W.convection_box(ncell=8, nm=4, seed=1),
+        "vep_slab_box_16x4": W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2),
+        "edge_cases": edge_case_workload(),
+    }
+    for name, wl in cases.items():
+        rec = record(wl, steps=2)
+        rec.update(tables(wl))
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), **rec)
+        print("wrote", name, len(wl.markers), "markers")
+    np.savez_compressed(os.path.join(OUT, "goldsby_kohlstedt.npz"), **creep_table())
+    print("wrote goldsby_kohlstedt")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,209 @@
+"""Pins the CPU oracle (oracle/mic_oracle.c) to fvmic2d itself.
+
+1. Against the committed golden vectors (tests/golden/*.npz), produced by the
+   reference's own hot-path C: runs anywhere.
+2. Directly against the reference build (oracle/_ref), only where the reference tree
+   was available to build it.
+Both comparisons are bit-exact: the oracle follows the reference's marker order and
+expression order, and both are compiled without FMA contraction.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from fvmic2d_gb300 import workloads as W
+from fvmic2d_gb300.mic_types import MARKER_DTYPE, PROJECTED_FIELDS, Materials, Options, BCs
+from oracle import oraclepy, refpy
+from tests.helpers import compare_markers, exact
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["convection_box_8", "vep_slab_box_16x4", "edge_cases"]
+
+
+def as_markers(a):
+    out = np.zeros(len(a), dtype=MARKER_DTYPE)
+    for n in MARKER_DTYPE.names:
+        out[n] = a[n]
+    return out
+
+
+def load_case(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    x, y = z["x"], z["y"]
+    g = W.Grid(len(x), len(y), float(z["LX"]), float(z["LY"]), x, y)
+    mat = Materials.from_buffer_copy(z["materials_bytes"].tobytes())
+    opt = Options.from_buffer_copy(z["options_bytes"].tobytes())
+    bcs = BCs.from_buffer_copy(z["bcs_bytes"].tobytes())
+    nodal = {k[len("nodal_in_"):]: z[k] for k in z.files if k.startswith("nodal_in_")}
+    wl = W.Workload(name, g, as_markers(z["markers_in"]), mat, opt, bcs, nodal,
+                    float(z["dt"]), float(z["dt_thermal"]), 2)
+    return wl, z
+
+
+def run_sequence(P, wl, z, steps=2, check=None):
+    """Drive the recorded entry-point sequence on P, calling check(tag, P) after each."""
+    D = wl.options.subgridStressDiffusivity
+    for s in range(steps):
+        pre = "s%d_" % s
+        nout = P.findMarkerCells()
+        check(pre + "after_find", P, nout=nout)
+        P.updateMarkerRho()
+        P.projectMarkersNodesAll2()
+        check(pre + "proj1", P)
+        check(pre + "maxT", P, value=P.maxMarkerT())
+        y = P.checkPlasticYielding(wl.dt)
+        check(pre + "yield", P, value=y)
+        check(pre + "after_yield", P)
+        P.limitViscosity()
+        P.projectMarkersNodesAll2()
+        check(pre + "proj2", P)
+        P.updateMarkerStrainPressure(wl.dt)
+        check(pre + "after_strain", P)
+        check(pre + "residual", P, value=P.updateGlobalStrainRateResidual(0))
+        if D > 0:
+            P.subgridStressChanges(wl.dt, D)
+            check(pre + "after_subgrid_stress", P)
+        P.updateMarkerStress()
+        check(pre + "after_stress", P)
+        P.subgridTemperatureChanges(wl.dt_thermal)
+        check(pre + "after_subgrid_T", P)
+        P.advectMarkersRK(wl.dt_thermal)
+        check(pre + "after_advect", P)
+        check(pre + "maxSxx", P, value=P.maxAbsSxx())
+
+
+def golden_checker(z, fails):
+    def check(tag, P, nout=None, value=None):
+        if tag.endswith("after_find"):
+            if int(z[tag[:3] + "nout"]) != nout:
+                fails.append("%s nOut %s vs %s" % (tag, nout, z[tag[:3] + "nout"]))
+        if tag.endswith(("proj1", "proj2")):
+            for f in PROJECTED_FIELDS:
+                ok, msg = exact(P.get_nodal(f), z[tag + "_" + f])
+                if not ok:
+                    fails.append("%s %s: %s" % (tag, f, msg))
+            return
+        if tag.endswith("after_subgrid_stress"):
+            for f in ("dsxx", "dsyy", "dsxy"):
+                ok, msg = exact(P.get_nodal(f), z[tag[:3] + "ds_" + f])
+                if not ok:
+                    fails.append("%s ds %s: %s" % (tag, f, msg))
+        if value is not None:
+            if not (value == float(z[tag]) or (np.isnan(value) and np.isnan(float(z[tag])))):
+                fails.append("%s value %r vs %r" % (tag, value, float(z[tag])))
+            return
+        want = as_markers(z[tag])
+        for msg in compare_markers(P.markers, want):
+            fails.append("%s %s" % (tag, msg))
+    return check
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_golden(name):
+    wl, z = load_case(name)
+    P = oraclepy.OracleProblem(wl)
+    fails = []
+    run_sequence(P, wl, z, check=golden_checker(z, fails))
+    assert not fails, "\n".join(fails[:20])
+
+
+def test_goldsby_kohlstedt_matches_golden():
+    z = np.load(os.path.join(GOLDEN, "goldsby_kohlstedt.npz"))
+    got = oraclepy.gk_viscosity(z["s"], z["T"], z["d"], z["P"])
+    ok, msg = exact(got, z["eta"])
+    assert ok, msg
+
+
+def test_boundary_struct_layouts():
+    L = oraclepy.lib()
+    assert L.orc_sizeof(0) == MARKER_DTYPE.itemsize == 216
+    assert L.orc_sizeof(4) == MARKER_DTYPE.fields["cellX"][1] == 184
+    assert L.orc_sizeof(1) == ctypes.sizeof(Materials)
+    assert L.orc_sizeof(5) == Materials.Tref.offset
+    assert L.orc_sizeof(2) == ctypes.sizeof(BCs)
+    assert L.orc_sizeof(3) == ctypes.sizeof(Options)
+
+
+needs_ref = pytest.mark.skipif(not refpy.available(), reason="reference build (oracle/_ref) not present")
+
+
+@needs_ref
+@pytest.mark.parametrize("make", [
+    lambda: W.convection_box(ncell=16, nm=4, seed=11),
+    lambda: W.vep_slab_box(nx_cells=48, ny_cells=12, nm=4, seed=12),
+])
+def test_oracle_matches_reference_build(make):
+    wl = make()
+    R = refpy.RefProblem(wl)
+    O = oraclepy.OracleProblem(wl)
+    D = wl.options.subgridStressDiffusivity
+    for _ in range(3):
+        for P in (R, O):
+            P.findMarkerCells()
+            P.updateMarkerRho()
+            P.projectMarkersNodesAll2()
+        for f in PROJECTED_FIELDS:
+            ok, msg = exact(O.get_nodal(f), R.get_nodal(f))
+            assert ok, f + " " + msg
+        assert O.checkPlasticYielding(wl.dt) == R.checkPlasticYielding(wl.dt)
+        for P in (R, O):
+            P.limitViscosity()
+            P.projectMarkersNodesAll2()
+            P.updateMarkerStrainPressure(wl.dt)
+        assert O.updateGlobalStrainRateResidual(0) == R.updateGlobalStrainRateResidual(0)
+        for P in (R, O):
+            if D > 0:
+                P.subgridStressChanges(wl.dt, D)
+            P.updateMarkerStress()
+            P.subgridTemperatureChanges(wl.dt_thermal)
+            P.advectMarkersRK(wl.dt_thermal)
+        fails = compare_markers(O.markers, R.markers)
+        assert not fails, fails
+        assert O.maxAbsSxx() == R.maxAbsSxx()
+
+
+@needs_ref
+def test_generic_projection_matches_reference_build():
+    """projectMarkerFieldToNodes for every stagger and method (markerProjection.c:71-250)."""
+    wl = W.vep_slab_box(nx_cells=20, ny_cells=8, nm=3, seed=5)
+    R = refpy.RefProblem(wl)
+    O = oraclepy.OracleProblem(wl)
+    R.findMarkerCells()
+    O.findMarkerCells()
+    for sx in (-1, 0, 1):
+        for sy in (-1, 0, 1):
+            for method in (0, 1, 2):
+                R.projectMarkerFieldToNodes("eta", "srr", sx, sy, method)
+                O.projectMarkerFieldToNodes("eta", "srr", sx, sy, method)
+                ok, msg = exact(O.get_nodal("srr"), R.get_nodal("srr"))
+                assert ok, (sx, sy, method, msg)
+    mp = np.array([3.0, 4.5] + [0.0] * 6)
+    R.projectMarkerFieldToNodes(None, "kThermal", 0, 0, 0, matprop=mp)
+    O.projectMarkerFieldToNodes(None, "kThermal", 0, 0, 0, matprop=mp)
+    ok, msg = exact(O.get_nodal("kThermal"), R.get_nodal("kThermal"))
+    assert ok, msg
+
+
+@needs_ref
+def test_nodal_to_markers_matches_reference_build():
+    wl = W.convection_box(ncell=12, nm=3, seed=3)
+    R = refpy.RefProblem(wl)
+    O = oraclepy.OracleProblem(wl)
+    for P in (R, O):
+        P.findMarkerCells()
+        P.projectNodalFieldToMarkersS("thisT", "T")
+    fails = compare_markers(O.markers, R.markers)
+    assert not fails, fails
+
+
+@needs_ref
+def test_goldsby_kohlstedt_matches_reference_build():
+    u = W.splitmix64_uniform(3, 4000)
+    s = 10 ** (u[0::4] * 9 - 1)
+    T = 100 + 173 * u[1::4]
+    d = 10 ** (-4 + 3 * u[2::4])
+    P = 1e8 * u[3::4]
+    ok, msg = exact(oraclepy.gk_viscosity(s, T, d, P), refpy.goldsby_kohlstedt(s, T, d, P))
+    assert ok, msg
