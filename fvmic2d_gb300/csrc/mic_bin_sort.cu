@@ -214,14 +214,23 @@ __global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n)
 int scan_exclusive(mic_ctx *ctx, int *data, int64_t len, int *aux) {
   const int64_t nb = (len + kScanBlock - 1) / kScanBlock;
   if (nb <= 1) {
-    k_scan_block<<<1, kScanThreads, 0, ctx->stream>>>(data, len, nullptr);
+    {
+      MIC_KERNEL(ctx, "k_scan_block");
+      k_scan_block<<<1, kScanThreads, 0, ctx->stream>>>(data, len, nullptr);
+    }
     return cudaGetLastError() == cudaSuccess ? MIC_OK : MIC_ERR_CUDA;
   }
   int *sums = aux;
-  k_scan_block<<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(data, len, sums);
+  {
+    MIC_KERNEL(ctx, "k_scan_block");
+    k_scan_block<<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(data, len, sums);
+  }
   int e = scan_exclusive(ctx, sums, nb, aux + nb + 1);
   if (e) return e;
-  k_scan_add<<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(data, len, sums);
+  {
+    MIC_KERNEL(ctx, "k_scan_add");
+    k_scan_add<<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(data, len, sums);
+  }
   return cudaGetLastError() == cudaSuccess ? MIC_OK : MIC_ERR_CUDA;
 }
 
@@ -256,9 +265,12 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
     if (n_out) *n_out = 0;
     return MIC_OK;
   }
-  k_find_cells<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y], ctx->i32[C_CELLX],
-                                                        ctx->i32[C_CELLY], ctx->i32[C_CPU], ctx->key, n,
-                                                        ctx->d_status);
+  {
+    MIC_KERNEL(ctx, "k_find_cells");
+    k_find_cells<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y], ctx->i32[C_CELLX],
+                                                          ctx->i32[C_CELLY], ctx->i32[C_CPU], ctx->key, n,
+                                                          ctx->d_status);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   const int ntiles = (int)((n + kTile - 1) / kTile);
   int e = ensure_sort_scratch(ctx, ntiles);
@@ -269,12 +281,18 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   int *kin = ctx->key, *kout = ctx->key_alt, *vin = ctx->perm, *vout = ctx->perm_alt;
   for (int p = 0; p < passes; ++p) {
     const int shift = p * kRadixBits;
-    k_radix_hist<<<ntiles, kSortThreads, 0, ctx->stream>>>(kin, n, shift, ctx->hist, ntiles);
+    {
+      MIC_KERNEL(ctx, "k_radix_hist");
+      k_radix_hist<<<ntiles, kSortThreads, 0, ctx->stream>>>(kin, n, shift, ctx->hist, ntiles);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
     e = scan_exclusive(ctx, ctx->hist, (int64_t)kBuckets * ntiles, ctx->scan_aux);
     if (e) return e;
-    k_radix_scatter<<<ntiles, kSortThreads, 0, ctx->stream>>>(kin, vin, p == 0, kout, vout, n, shift, ctx->hist,
-                                                              ntiles);
+    {
+      MIC_KERNEL(ctx, "k_radix_scatter");
+      k_radix_scatter<<<ntiles, kSortThreads, 0, ctx->stream>>>(kin, vin, p == 0, kout, vout, n, shift, ctx->hist,
+                                                                ntiles);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
     int *t = kin;
     kin = kout;
@@ -284,7 +302,10 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
     vout = t;
   }
   // kin / vin now hold the sorted keys and the permutation
-  k_cell_start<<<grid_for(n + 1), kBlock, 0, ctx->stream>>>(kin, n, ctx->ncells, ctx->cell_start);
+  {
+    MIC_KERNEL(ctx, "k_cell_start");
+    k_cell_start<<<grid_for(n + 1), kBlock, 0, ctx->stream>>>(kin, n, ctx->ncells, ctx->cell_start);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   GatherCols g;
   for (int c = 0; c < C_F64_COUNT; ++c) {
@@ -295,7 +316,10 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
     g.src_i[c] = ctx->i32[c];
     g.dst_i[c] = ctx->i32_alt[c];
   }
-  k_reorder<<<grid_for(n), kBlock, 0, ctx->stream>>>(g, vin, n);
+  {
+    MIC_KERNEL(ctx, "k_reorder");
+    k_reorder<<<grid_for(n), kBlock, 0, ctx->stream>>>(g, vin, n);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   for (int c = 0; c < C_F64_COUNT; ++c) {
     double *t = ctx->f64[c];

@@ -103,9 +103,12 @@ static ColPtrs cur_cols(mic_ctx *ctx) {
 
 // ---- lifecycle --------------------------------------------------------------------
 
+static void prof_free(mic_ctx *ctx);
+
 static void free_ctx(mic_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
+  prof_free(ctx);
   for (int c = 0; c < C_F64_COUNT; ++c) {
     cudaFree(ctx->f64[c]);
     cudaFree(ctx->f64_alt[c]);
@@ -330,7 +333,10 @@ extern "C" int mic_markers_upload(mic_ctx *ctx, const mic_marker *host, int64_t 
   if (n > 0) {
     MIC_CUDA_TRY(cudaMemcpyAsync(ctx->stage_aos, host, (size_t)n * sizeof(mic_marker), cudaMemcpyHostToDevice,
                                  ctx->stream));
-    k_aos_to_soa<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->stage_aos, cur_cols(ctx), n);
+    {
+      MIC_KERNEL(ctx, "k_aos_to_soa");
+      k_aos_to_soa<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->stage_aos, cur_cols(ctx), n);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   ctx->n = n;
@@ -345,7 +351,10 @@ extern "C" int mic_markers_download(mic_ctx *ctx, mic_marker *host, int64_t n) {
   if (n == 0) return MIC_OK;
   int e = ensure_stage(ctx, n);
   if (e) return e;
-  k_soa_to_aos<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->stage_aos, cur_cols(ctx), n);
+  {
+    MIC_KERNEL(ctx, "k_soa_to_aos");
+    k_soa_to_aos<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->stage_aos, cur_cols(ctx), n);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   MIC_CUDA_TRY(cudaMemcpyAsync(host, ctx->stage_aos, (size_t)n * sizeof(mic_marker), cudaMemcpyDeviceToHost,
                                ctx->stream));
@@ -437,5 +446,95 @@ extern "C" int mic_host_alloc(void **ptr, int64_t bytes) {
 extern "C" int mic_host_free(void *ptr) {
   if (!ptr) return MIC_ERR_ARG;
   cudaFreeHost(ptr);
+  return MIC_OK;
+}
+
+// ---- launch accounting and per-launch timing ------------------------------------------
+
+void mic_prof_begin(mic_ctx *ctx, const char *name) {
+  ctx->launches++;
+  if (!ctx->prof_on || ctx->prof_n >= ctx->prof_cap) return;
+  ctx->prof_name[ctx->prof_n] = name;
+  cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n], ctx->stream);
+}
+
+void mic_prof_end(mic_ctx *ctx) {
+  if (!ctx->prof_on || ctx->prof_n >= ctx->prof_cap) return;
+  cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n + 1], ctx->stream);
+  ctx->prof_n++;
+}
+
+static void prof_free(mic_ctx *ctx) {
+  for (int k = 0; k < 2 * ctx->prof_cap; ++k) cudaEventDestroy(ctx->prof_ev[k]);
+  free(ctx->prof_ev);
+  free(ctx->prof_name);
+  ctx->prof_ev = nullptr;
+  ctx->prof_name = nullptr;
+  ctx->prof_cap = ctx->prof_n = 0;
+}
+
+// Enables (capacity > 0) or disables (0) per-launch timing; enabling clears the records.
+extern "C" int mic_profile_enable(mic_ctx *ctx, int capacity) {
+  if (!ctx || capacity < 0) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (capacity == 0) {
+    ctx->prof_on = 0;
+    return MIC_OK;
+  }
+  if (capacity != ctx->prof_cap) {
+    prof_free(ctx);
+    ctx->prof_ev = (cudaEvent_t *)calloc(2 * (size_t)capacity, sizeof(cudaEvent_t));
+    ctx->prof_name = (const char **)calloc((size_t)capacity, sizeof(char *));
+    if (!ctx->prof_ev || !ctx->prof_name) return MIC_ERR_NOMEM;
+    for (int k = 0; k < 2 * capacity; ++k) MIC_CUDA_TRY(cudaEventCreate(&ctx->prof_ev[k]));
+    ctx->prof_cap = capacity;
+  }
+  ctx->prof_n = 0;
+  ctx->prof_on = 1;
+  return MIC_OK;
+}
+
+// Aggregates the recorded launches by kernel name: returns the number of distinct kernels
+// and, for k < max, their names (NUL-terminated, 48 bytes each), total ms and launch counts.
+extern "C" int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64_t *counts,
+                                int *nkernels) {
+  if (!ctx || !nkernels) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  const char *uniq[128];
+  double tot[128];
+  int64_t cnt[128];
+  int nu = 0;
+  for (int r = 0; r < ctx->prof_n; ++r) {
+    float ms = 0.f;
+    MIC_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->prof_ev[2 * r], ctx->prof_ev[2 * r + 1]));
+    int u = 0;
+    while (u < nu && strcmp(uniq[u], ctx->prof_name[r]) != 0) ++u;
+    if (u == nu) {
+      if (nu == 128) continue;
+      uniq[nu] = ctx->prof_name[r];
+      tot[nu] = 0.0;
+      cnt[nu] = 0;
+      ++nu;
+    }
+    tot[u] += ms;
+    cnt[u] += 1;
+  }
+  for (int u = 0; u < nu && u < max; ++u) {
+    if (names) {
+      strncpy(names + 48 * u, uniq[u], 47);
+      names[48 * u + 47] = 0;
+    }
+    if (total_ms) total_ms[u] = tot[u];
+    if (counts) counts[u] = cnt[u];
+  }
+  *nkernels = nu;
+  return MIC_OK;
+}
+
+extern "C" int mic_launch_count(mic_ctx *ctx, int64_t *n) {
+  if (!ctx || !n) return MIC_ERR_ARG;
+  *n = ctx->launches;
   return MIC_OK;
 }

@@ -86,7 +86,25 @@ struct mic_ctx {
   int64_t stage_cap;
   double residuals[100];
   int last_error;
+  // launch accounting and optional per-launch CUDA-event timing
+  long long launches;
+  int prof_on;
+  int prof_n, prof_cap;
+  const char **prof_name;
+  cudaEvent_t *prof_ev;  // 2 per record
 };
+
+void mic_prof_begin(mic_ctx *ctx, const char *name);
+void mic_prof_end(mic_ctx *ctx);
+
+namespace mic {
+struct ProfScope {  // brackets one kernel launch: counts it and, when enabled, times it
+  mic_ctx *c;
+  ProfScope(mic_ctx *ctx, const char *name) : c(ctx) { mic_prof_begin(ctx, name); }
+  ~ProfScope() { mic_prof_end(c); }
+};
+}  // namespace mic
+#define MIC_KERNEL(ctx, name) mic::ProfScope _mic_prof_scope(ctx, name)
 
 // ---- helpers -------------------------------------------------------------------------
 

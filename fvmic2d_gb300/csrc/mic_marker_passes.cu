@@ -630,7 +630,10 @@ int run_max(mic_ctx *ctx, int col, int absval, double *out) {
   unsigned long long *d = reinterpret_cast<unsigned long long *>(ctx->red_buf + 8);
   MIC_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
   if (ctx->n > 0) {
-    k_max<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->f64[col], absval, ctx->n, d);
+    {
+      MIC_KERNEL(ctx, "k_max");
+      k_max<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->f64[col], absval, ctx->n, d);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   if (out) {
@@ -655,8 +658,11 @@ extern "C" int mic_update_marker_rho(mic_ctx *ctx) {
   int e = mic_ensure_sorted(ctx);
   if (e) return e;
   if (ctx->n == 0) return MIC_OK;
-  k_update_rho<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
-                                                             ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n);
+  {
+    MIC_KERNEL(ctx, "k_update_rho");
+    k_update_rho<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
+                                                               ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
@@ -679,8 +685,11 @@ static int yield_launch(mic_ctx *ctx, double dt) {
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->is_yielding, 0, sizeof(int), ctx->stream));
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->bad_law, 0, sizeof(unsigned long long), ctx->stream));
   if (ctx->n > 0) {
-    k_yield<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, dt, ctx->n,
-                                                          ctx->d_status);
+    {
+      MIC_KERNEL(ctx, "k_yield");
+      k_yield<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, dt, ctx->n,
+                                                            ctx->d_status);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   return MIC_OK;
@@ -702,8 +711,11 @@ extern "C" int mic_update_viscosity(mic_ctx *ctx) {
   if (e) return e;
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->bad_law, 0, sizeof(unsigned long long), ctx->stream));
   if (ctx->n > 0) {
-    k_update_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->n,
-                                                                     ctx->d_status);
+    {
+      MIC_KERNEL(ctx, "k_update_viscosity");
+      k_update_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->n,
+                                                                       ctx->d_status);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   if ((e = read_status(ctx))) return e;
@@ -713,8 +725,11 @@ extern "C" int mic_update_viscosity(mic_ctx *ctx) {
 extern "C" int mic_limit_viscosity(mic_ctx *ctx) {
   CHECK_CTX();
   if (ctx->n == 0) return MIC_OK;
-  k_limit_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->f64[C_ETA], ctx->opt.etamin,
-                                                                  ctx->opt.etamax, ctx->n);
+  {
+    MIC_KERNEL(ctx, "k_limit_viscosity");
+    k_limit_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->f64[C_ETA], ctx->opt.etamin,
+                                                                    ctx->opt.etamax, ctx->n);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
@@ -737,8 +752,11 @@ static int strain_launch(mic_ctx *ctx, double dt) {
   c.exy = ctx->f64[C_EXY];
   c.wxy = ctx->f64[C_WXY];
   c.srr = ctx->f64[C_SRR];
-  k_strain_pressure<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n,
-                                                                  ctx->d_status);
+  {
+    MIC_KERNEL(ctx, "k_strain_pressure");
+    k_strain_pressure<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n,
+                                                                    ctx->d_status);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
@@ -757,9 +775,15 @@ static int residual_launch(mic_ctx *ctx, int iter, double *res_dev) {
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
   const int nb = (int)grid_for(nn);
   double *partial = ctx->node_scr[5];  // NX*NY >= number of blocks
-  k_residual_weight<<<nb, kBlock, 0, ctx->stream>>>(ctx->P, ctx->nodal[MIC_NF_SRR], partial);
+  {
+    MIC_KERNEL(ctx, "k_residual_weight");
+    k_residual_weight<<<nb, kBlock, 0, ctx->stream>>>(ctx->P, ctx->nodal[MIC_NF_SRR], partial);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
-  k_sum_partials<<<1, 1024, 0, ctx->stream>>>(partial, nb, res_dev);
+  {
+    MIC_KERNEL(ctx, "k_sum_partials");
+    k_sum_partials<<<1, 1024, 0, ctx->stream>>>(partial, nb, res_dev);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   (void)iter;
   return MIC_OK;
@@ -817,15 +841,21 @@ extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
     c.dxy = ctx->scr0;
     c.dxx = ctx->scr1;
     c.dyy = ctx->scr2;
-    k_subgrid_stress_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
-                                                                           D, ctx->n);
+    {
+      MIC_KERNEL(ctx, "k_subgrid_stress_markers");
+      k_subgrid_stress_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
+                                                                             D, ctx->n);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   dim3 grid((ctx->P.NX + 127) / 128, ctx->P.NY);
-  k_subgrid_stress_nodes<<<grid, 128, 0, ctx->stream>>>(ctx->P, ctx->i32[C_CELLX], ctx->geo[0], ctx->geo[1],
-                                                        ctx->scr0, ctx->scr1, ctx->scr2, ctx->cell_start,
-                                                        ctx->nodal[MIC_NF_DSXX], ctx->nodal[MIC_NF_DSYY],
-                                                        ctx->nodal[MIC_NF_DSXY]);
+  {
+    MIC_KERNEL(ctx, "k_subgrid_stress_nodes");
+    k_subgrid_stress_nodes<<<grid, 128, 0, ctx->stream>>>(ctx->P, ctx->i32[C_CELLX], ctx->geo[0], ctx->geo[1],
+                                                          ctx->scr0, ctx->scr1, ctx->scr2, ctx->cell_start,
+                                                          ctx->nodal[MIC_NF_DSXX], ctx->nodal[MIC_NF_DSYY],
+                                                          ctx->nodal[MIC_NF_DSXY]);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
@@ -843,8 +873,11 @@ static int stress_launch(mic_ctx *ctx) {
   c.sxx = ctx->f64[C_SXX];
   c.syy = ctx->f64[C_SYY];
   c.sxy = ctx->f64[C_SXY];
-  k_update_marker_stress<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), ctx->n,
-                                                                       ctx->d_status);
+  {
+    MIC_KERNEL(ctx, "k_update_marker_stress");
+    k_update_marker_stress<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), ctx->n,
+                                                                         ctx->d_status);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
@@ -865,19 +898,28 @@ extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
   c.Tdot = ctx->f64[C_TDOT];
   c.dTsub = ctx->scr0;
   if (ctx->n > 0) {
-    k_subgridT_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(
-        ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_LASTT], ctx->nodal[MIC_NF_RHO], ctx->nodal[MIC_NF_CP],
-        ctx->nodal[MIC_NF_KTHERMAL], ctx->mat.materialRho[0], ctx->opt.subgridTemperatureDiffusivity, dt, ctx->n);
+    {
+      MIC_KERNEL(ctx, "k_subgridT_markers");
+      k_subgridT_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(
+          ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_LASTT], ctx->nodal[MIC_NF_RHO], ctx->nodal[MIC_NF_CP],
+          ctx->nodal[MIC_NF_KTHERMAL], ctx->mat.materialRho[0], ctx->opt.subgridTemperatureDiffusivity, dt, ctx->n);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   if ((e = mic_project_scalar(ctx, ctx->scr0, 0, ctx->node_scr[0]))) return e;
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
-  k_subgridT_nodes<<<grid_for(nn), kBlock, 0, ctx->stream>>>(ctx->nodal[MIC_NF_THIST], ctx->nodal[MIC_NF_LASTT],
-                                                             ctx->node_scr[0], ctx->node_scr[1], nn);
+  {
+    MIC_KERNEL(ctx, "k_subgridT_nodes");
+    k_subgridT_nodes<<<grid_for(nn), kBlock, 0, ctx->stream>>>(ctx->nodal[MIC_NF_THIST], ctx->nodal[MIC_NF_LASTT],
+                                                               ctx->node_scr[0], ctx->node_scr[1], nn);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   if (ctx->n > 0) {
-    k_subgridT_apply<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->node_scr[1], dt,
-                                                                   ctx->n);
+    {
+      MIC_KERNEL(ctx, "k_subgridT_apply");
+      k_subgridT_apply<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->node_scr[1], dt,
+                                                                     ctx->n);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   return MIC_OK;
@@ -903,9 +945,12 @@ extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
     c.exx = ctx->f64[C_EXX];
     c.eyy = ctx->f64[C_EYY];
     c.exy = ctx->f64[C_EXY];
-    k_advect<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY],
-                                                           ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
-                                                           ctx->bcs.mechBCLeft, dt, ctx->n);
+    {
+      MIC_KERNEL(ctx, "k_advect");
+      k_advect<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY],
+                                                             ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
+                                                             ctx->bcs.mechBCLeft, dt, ctx->n);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   // positions moved: cells, order and geometry are stale until the next binning
@@ -922,8 +967,11 @@ extern "C" int mic_project_nodal_field_to_markers(mic_ctx *ctx, int f, int off) 
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   if (ctx->n == 0) return MIC_OK;
-  k_nodal_to_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->i32[C_CELLX], ctx->i32[C_CELLY],
-                                                                   geo_of(ctx), ctx->nodal[f], ctx->f64[col], ctx->n);
+  {
+    MIC_KERNEL(ctx, "k_nodal_to_markers");
+    k_nodal_to_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->i32[C_CELLX], ctx->i32[C_CELLY],
+                                                                     geo_of(ctx), ctx->nodal[f], ctx->f64[col], ctx->n);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }

@@ -258,10 +258,13 @@ int mic_ensure_geometry(mic_ctx *ctx) {
   if (e) return e;
   if (ctx->geo_valid) return MIC_OK;
   if (ctx->n > 0) {
-    k_geometry<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y],
-                                                             ctx->i32[C_CELLX], ctx->i32[C_CELLY], ctx->geo[0],
-                                                             ctx->geo[1], ctx->geo[2], ctx->geo[3],
-                                                             ctx->geo_flags, ctx->n);
+    {
+      MIC_KERNEL(ctx, "k_geometry");
+      k_geometry<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y],
+                                                               ctx->i32[C_CELLX], ctx->i32[C_CELLY], ctx->geo[0],
+                                                               ctx->geo[1], ctx->geo[2], ctx->geo[3],
+                                                               ctx->geo_flags, ctx->n);
+    }
     MIC_CUDA_TRY(cudaGetLastError());
   }
   ctx->geo_valid = 1;
@@ -273,11 +276,17 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   if (stag == 0)
-    k_project_geo_arith<0><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(
-        ctx->P, v, ctx->i32[C_CELLX], ctx->geo[0], ctx->geo[1], ctx->geo_flags, ctx->cell_start, out);
+    {
+      MIC_KERNEL(ctx, "k_project_geo_arith");
+      k_project_geo_arith<0><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(
+          ctx->P, v, ctx->i32[C_CELLX], ctx->geo[0], ctx->geo[1], ctx->geo_flags, ctx->cell_start, out);
+    }
   else
-    k_project_geo_arith<-1><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(
-        ctx->P, v, ctx->i32[C_CELLX], ctx->geo[2], ctx->geo[3], ctx->geo_flags, ctx->cell_start, out);
+    {
+      MIC_KERNEL(ctx, "k_project_geo_arith");
+      k_project_geo_arith<-1><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(
+          ctx->P, v, ctx->i32[C_CELLX], ctx->geo[2], ctx->geo[3], ctx->geo_flags, ctx->cell_start, out);
+    }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
@@ -314,7 +323,10 @@ extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
   o.soxx = ctx->nodal[MIC_NF_SOXX];
   o.soyy = ctx->nodal[MIC_NF_SOYY];
   o.soxy = ctx->nodal[MIC_NF_SOXY];
-  k_project_all2<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, mv, ctx->cell_start, ctx->mat, o);
+  {
+    MIC_KERNEL(ctx, "k_project_all2");
+    k_project_all2<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, mv, ctx->cell_start, ctx->mat, o);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
@@ -337,9 +349,12 @@ extern "C" int mic_project_marker_field_to_nodes(mic_ctx *ctx, int off, const do
     mp = ctx->red_buf;  // MIC_MAXMAT values
     MIC_CUDA_TRY(cudaMemcpyAsync(mp, matprop, sizeof(double) * MIC_MAXMAT, cudaMemcpyHostToDevice, ctx->stream));
   }
-  k_project_generic<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(
-      ctx->P, ctx->f64[C_X], ctx->f64[C_Y], ctx->i32[C_CELLX], col >= 0 ? ctx->f64[col] : nullptr, ctx->i32[C_MAT],
-      mp, stagx, stagy, method, ctx->cell_start, ctx->nodal[out_field]);
+  {
+    MIC_KERNEL(ctx, "k_project_generic");
+    k_project_generic<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(
+        ctx->P, ctx->f64[C_X], ctx->f64[C_Y], ctx->i32[C_CELLX], col >= 0 ? ctx->f64[col] : nullptr, ctx->i32[C_MAT],
+        mp, stagx, stagy, method, ctx->cell_start, ctx->nodal[out_field]);
+  }
   MIC_CUDA_TRY(cudaGetLastError());
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return MIC_OK;

@@ -63,6 +63,9 @@ SIGNATURES = {
     "mic_get_status": (_I, [_P, _P]),
     "mic_debug_sorted_ids": (_I, [_P, _P]),
     "mic_debug_cell_start": (_I, [_P, _P]),
+    "mic_launch_count": (_I, [_P, _I64P]),
+    "mic_profile_enable": (_I, [_P, _I]),
+    "mic_profile_read": (_I, [_P, _I, _P, _DP, _I64P, _IP]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -183,6 +186,29 @@ class MicProblem:
         cs = np.empty((self.NX - 1) * (self.NY - 1) + 2, dtype=np.int32)
         self._check(self.L.mic_debug_cell_start(self.h, cs.ctypes.data), "mic_debug_cell_start")
         return cs
+
+    def launch_count(self):
+        n = ctypes.c_int64(0)
+        self._check(self.L.mic_launch_count(self.h, ctypes.byref(n)), "mic_launch_count")
+        return n.value
+
+    def profile_enable(self, capacity):
+        self._check(self.L.mic_profile_enable(self.h, capacity), "mic_profile_enable")
+
+    def profile_read(self):
+        """{kernel name: (total ms, launches)} over the records since profile_enable."""
+        cap = 128
+        names = ctypes.create_string_buffer(48 * cap)
+        tot = np.zeros(cap)
+        cnt = np.zeros(cap, dtype=np.int64)
+        nk = ctypes.c_int(0)
+        self._check(self.L.mic_profile_read(self.h, cap, names, _dp(tot), cnt.ctypes.data_as(_I64P),
+                                             ctypes.byref(nk)), "mic_profile_read")
+        out = {}
+        for u in range(min(nk.value, cap)):
+            nm = names.raw[48 * u: 48 * u + 48].split(b"\0", 1)[0].decode()
+            out[nm] = (float(tot[u]), int(cnt[u]))
+        return out
 
     def synchronize(self):
         self._check(self.L.mic_synchronize(self.h), "mic_synchronize")

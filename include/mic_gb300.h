@@ -139,6 +139,12 @@ int mic_get_status(mic_ctx *ctx, mic_status *status);
  * ((NX-1)*(NY-1)+2 entries; the last two bracket the out-of-domain markers) */
 int mic_debug_sorted_ids(mic_ctx *ctx, int32_t *ids);
 int mic_debug_cell_start(mic_ctx *ctx, int32_t *cell_start);
+/* kernel launches issued by this context so far */
+int mic_launch_count(mic_ctx *ctx, int64_t *launches);
+/* per-launch CUDA-event timing on the context stream: enable with a record capacity (0 turns it
+ * off); read aggregates by kernel name (names: max * 48 bytes) */
+int mic_profile_enable(mic_ctx *ctx, int capacity);
+int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64_t *counts, int *nkernels);
 /* pinned host memory for fast transfers */
 int mic_host_alloc(void **ptr, int64_t bytes);
 int mic_host_free(void *ptr);
