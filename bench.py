@@ -1,0 +1,407 @@
+"""Benchmark: markers/s per step of the marker-in-cell transfer path on GB300.
+
+Workload (default): the visco-elasto-plastic two-material 4:1 box, 1025 x 257 nodes,
+4,194,304 markers, FP64 -- the path's headline configuration.  A step is one pass of
+fvmic2d's marker path in main_subduction.c order (bin + stable sort, density update,
+projectMarkersNodesAll2, max T, checkPlasticYielding, limitViscosity,
+projectMarkersNodesAll2, updateMarkerStrainPressure, updateGlobalStrainRateResidual,
+subgridStressChanges, updateMarkerStress, subgridTemperatureChanges, advectMarkersRK,
+max |sxx|), with the host Stokes/thermal solves outside the timed region; their nodal
+outputs are synthetic inputs held on the device.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One JSON line on rank 0.  Under torchrun (N > 1) every rank runs an independent replica
+on its own GPU (the path shards only across independent problems); value = all markers
+processed / max-over-ranks time.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "markers/s per step (project+advect+rheology), plain vs surrogate @1e-6 rel err"
+WORKLOAD_DESC = ("vep_slab_box: 1025x257 staggered grid (2x refined top 20%), 16 markers/cell, "
+                 "4,194,304 markers, two materials, Mohr-Coulomb yield, FP64")
+
+# Host-solve outputs that cross the boundary each step in the drop-in model (markers stay
+# resident on the device): nodal inputs up, projected nodal fields down.
+E2E_UP = ["vx", "vy", "p", "edotxx", "edotyy", "edotxy", "wxy", "soxx", "soyy", "soxy", "dsxx", "dsyy", "dsxy",
+          "thisT"]
+E2E_DOWN = ["rho", "etaN", "etaS", "kThermal", "lastT", "Cp", "soxx", "soyy", "soxy"]
+
+# Algorithmic bytes per marker of the whole step (compulsory marker-state traffic of the five
+# dependency-forced passes) and per node (44 nodal-array touches of 8 bytes).
+STEP_BYTES_PER_MARKER = 436
+STEP_BYTES_PER_NODE = 352
+
+# Per-kernel algorithmic bytes: each kernel's own inputs read once and outputs written once
+# (marker columns per marker, nodal arrays per node).  Indexing and scratch re-reads are not
+# credited.
+KERNEL_BYTES = {
+    # X, Y read; cellX, cellY, key, cpu written
+    "k_find_cells": (16 + 16, 0),
+    # cellX, flags, 4 offsets, eta, rho, T, sxx, syy, sxy, Mat read; 12 nodal fields written
+    "k_project_all2": (4 + 4 + 32 + 48 + 4, 96),
+    # cellX, cellY, X, Y, s3, e3, Eii read; X, Y, VX, VY, wxy, s3, Eii written; vx, vy, wxy read
+    "k_advect": (8 + 16 + 24 + 24 + 8 + 16 + 16 + 8 + 24 + 8, 24),
+    # cellX, cellY, flags, 4 offsets, X, Y, eta, mu read; p, e3, wxy, srr written; 10 nodal read
+    "k_strain_pressure": (8 + 4 + 32 + 16 + 16 + 8 + 24 + 8 + 8, 80),
+    # cellX, Mat, X, Y, T, p, Eii, e3, eta, mu, s3 read; eta, mu, s3 written
+    "k_yield": (8 + 16 + 8 + 8 + 8 + 24 + 16 + 24 + 16 + 24, 0),
+    # all 29 marker columns read and written
+    "k_reorder": (2 * (23 * 8 + 6 * 4) + 4, 0),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="vep_slab_box")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-cores", type=int, default=0, help="host processes for the CPU legs (0 = all)")
+    return ap.parse_args()
+
+
+def make_workload(name):
+    from fvmic2d_gb300 import workloads as W
+
+    return W.WORKLOADS[name]()
+
+
+# ---------------------------------------------------------------------------------------
+# CPU legs: the CPU restatement of the reference path (oracle/liboracle.so), one process per
+# core, each running whole steps of the full workload (spawned before any GPU work).
+
+
+def _cpu_worker(args):
+    name, steps, warmup, barrier = args
+    sys.path.insert(0, ROOT)
+    from oracle import oraclepy
+
+    wl = make_workload(name)
+    P = oraclepy.OracleProblem(wl)
+    for _ in range(warmup):
+        P.step(wl.dt, wl.dt_thermal)
+    barrier.wait()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        e, _ = P.step(wl.dt, wl.dt_thermal)
+        if e:
+            raise RuntimeError("oracle step failed with %d" % e)
+    t1 = time.perf_counter()
+    return len(wl.markers), t1 - t0
+
+
+def cpu_throughput(name, cores, steps, warmup):
+    """Aggregate markers/s of `cores` concurrent single-threaded replicas."""
+    from oracle import build as obuild
+
+    obuild.build_oracle()
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as man:
+        barrier = man.Barrier(cores)
+        with ctx.Pool(cores) as pool:
+            res = pool.map(_cpu_worker, [(name, steps, warmup, barrier)] * cores)
+    n = sum(r[0] for r in res) * steps
+    t = max(r[1] for r in res)
+    return n / t, t / steps * 1e3
+
+
+def host_cores(requested):
+    n = os.cpu_count() or 1
+    return max(1, min(n, requested)) if requested else n
+
+
+# ---------------------------------------------------------------------------------------
+# clocks during the timed region
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    p = [s.strip() for s in line.split(",")]
+                    if len(p) >= 9:
+                        rows.append(p)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        loaded = [s for s in sm if s >= 0.5 * (max(sm) if sm else 0)]
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------------
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def base_config(wl, args, world):
+    return {"workload": WORKLOAD_DESC if args.workload == "vep_slab_box" else args.workload,
+            "markers_per_replica": int(len(wl.markers)), "nodes": [wl.grid.NX, wl.grid.NY],
+            "parallelism": "replicas x%d (independent problems, no collective)" % world,
+            "l2": "inputs larger than L2 (marker state %.2f GB per replica)" % (len(wl.markers) * 208 / 1e9),
+            "timed": "bin+sort, rho, project x2, max T, yield, limit, strain/pressure, residual, subgrid stress, "
+                     "stress update, subgrid T, RK4 advection, max |sxx|; host solves excluded"}
+
+
+def run_reference_arm(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    cores = host_cores(args.cpu_cores)
+    rate, ms = cpu_throughput(args.workload, cores, args.steps, args.warmup)
+    wl = make_workload(args.workload)
+    line = {"metric": METRIC, "value": rate, "unit": "markers/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+            "config": base_config(wl, args, 1), "impl": "reference",
+            "cpu_baseline": {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
+                             "sample": "%d concurrent single-threaded replicas x %d steps of the full workload "
+                                       "(CPU restatement of the reference path; the reference tree is not on "
+                                       "this host)" % (cores, args.steps)},
+            "e2e": {"value": rate, "unit": "markers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    world, rank, local, pg = dist_setup(args)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # bounded sample: one step per replica on all host cores, spawned before any GPU work
+        cores = host_cores(args.cpu_cores)
+        rate, ms = cpu_throughput(args.workload, cores, 1, 0)
+        rate1, ms1 = cpu_throughput(args.workload, 1, 1, 0)
+        cpu = {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
+               "sample": "1 step of the full workload per replica, %d concurrent replicas "
+                         "(single replica: %.3g markers/s, %.0f ms/step)" % (cores, rate1, ms1)}
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from fvmic2d_gb300 import gpu
+    from fvmic2d_gb300.mic_types import NF
+
+    torch.cuda.set_device(local)
+    wl = make_workload(args.workload)
+    G = gpu.MicProblem(wl, device=local)
+    L, h = G.L, G.h
+    stream = torch.cuda.ExternalStream(G.stream(), device=local)
+    n = len(wl.markers)
+    nodes = wl.grid.NX * wl.grid.NY
+    sub = 1 if wl.options.subgridStressDiffusivity > 0 else 0
+
+    def step():
+        e = L.mic_step(h, wl.dt, wl.dt_thermal, sub, None)
+        if e:
+            raise gpu.MicError(e, "mic_step")
+
+    for _ in range(args.warmup):
+        step()
+    G.synchronize()
+    cap = max(64, 40 * args.steps)
+    G.profile_enable(cap)
+    launches0 = G.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(pg)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        barrier(pg)
+    launches = G.launch_count() - launches0
+    prof = G.profile_read()
+    G.profile_enable(0)
+    ms_total = ev0.elapsed_time(ev1)
+    t_max = max_over_ranks(pg, ms_total)
+    markers_all = sum_over_ranks(pg, float(n * args.steps))
+    value = markers_all / (t_max * 1e-3)
+    ms_step = t_max / args.steps
+
+    # ---- end to end through the C ABI with pinned host buffers --------------------------
+    def pinned(nbytes):
+        p = ctypes.c_void_p()
+        assert L.mic_host_alloc(ctypes.byref(p), nbytes) == 0
+        return p
+
+    up_bufs, down_bufs = [], []
+    for name in E2E_UP:
+        p = pinned(nodes * 8)
+        a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_double)), shape=(nodes,))
+        a[:] = np.asarray(wl.nodal[name], dtype=np.float64).ravel()
+        up_bufs.append((NF[name], p, a))
+    for name in E2E_DOWN:
+        p = pinned(nodes * 8)
+        a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_double)), shape=(nodes,))
+        down_bufs.append((NF[name], p, a))
+    res = ctypes.c_double(0.0)
+    DP = ctypes.POINTER(ctypes.c_double)
+
+    def e2e_step():
+        for fid, p, _ in up_bufs:
+            assert L.mic_nodal_upload(h, fid, ctypes.cast(p, DP)) == 0
+        assert L.mic_step(h, wl.dt, wl.dt_thermal, sub, ctypes.byref(res)) == 0
+        for fid, p, _ in down_bufs:
+            assert L.mic_nodal_download(h, fid, ctypes.cast(p, DP)) == 0
+
+    e2e_steps = max(3, min(args.steps, 50))
+    e2e_step()
+    G.synchronize()
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    G.synchronize()
+    t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_value = sum_over_ranks(pg, float(n * e2e_steps)) / t_e2e
+    for _, p, _ in up_bufs + down_bufs:
+        L.mic_host_free(p)
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel (live CUDA-event timing over the timed region) ------
+    import json as _json
+
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        hbm_peak = float(_json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    else:
+        hbm_peak, peak_src = 6800.0, "fallback"
+    kern = sorted(prof.items(), key=lambda kv: -kv[1][0])
+    top_name, (top_ms, top_cnt) = kern[0]
+    per_marker, per_node = KERNEL_BYTES.get(top_name, (0, 0))
+    algo = per_marker * n + per_node * nodes
+    dur = top_ms / max(top_cnt, 1)
+    achieved = algo / (dur * 1e-3) / 1e9
+    step_bytes = STEP_BYTES_PER_MARKER * n + STEP_BYTES_PER_NODE * nodes
+    step_gbs = step_bytes / (ms_step * 1e-3) / 1e9
+    prof_total = sum(v[0] for v in prof.values())
+    line = {
+        "metric": METRIC, "value": value, "unit": "markers/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+        "config": base_config(wl, args, world),
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_value, "unit": "markers/s",
+                "h2d_bytes_per_step": len(E2E_UP) * nodes * 8, "d2h_bytes_per_step": len(E2E_DOWN) * nodes * 8 + 8,
+                "model": "markers resident on the device; host-solve nodal fields up and projected nodal fields "
+                         "down every step through mic_nodal_upload/mic_step/mic_nodal_download"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": algo, "ms_per_launch": dur},
+        "step_roofline": {"algorithmic_bytes_per_step": step_bytes, "achieved_gbs": step_gbs,
+                          "frac": step_gbs / hbm_peak},
+        "kernel_share": {k: round(v[0] / prof_total, 4) for k, v in kern[:12]},
+        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kern[:12]},
+        "surrogate": None,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -287,4 +287,10 @@ def vep_slab_box(nx_cells=1024, ny_cells=256, nm=4, seed=2):
     return Workload("vep_slab_box", g, m, mat, opt, _free_slip(), nodal, dt, dt, 20)
 
 
-WORKLOADS = {"convection_box": convection_box, "vep_slab_box": vep_slab_box}
+WORKLOADS = {
+    "convection_box": convection_box,
+    "vep_slab_box": vep_slab_box,
+    # 513 x 129 nodes, 1,048,576 markers (about 220 MB of marker state, larger than L2):
+    # the small case used for detailed profiles
+    "vep_slab_box_1m": lambda: vep_slab_box(nx_cells=512, ny_cells=128),
+}
