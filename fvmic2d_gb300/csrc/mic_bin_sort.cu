@@ -354,3 +354,164 @@ extern "C" int mic_find_marker_cells(mic_ctx *ctx, int64_t *n_out) {
   if (n_out) *n_out = no;
   return e;
 }
+
+// ---- binning and stable sort for callers that cannot allocate ------------------------
+//
+// Some callers of this code cannot call cudaMalloc: a host that has finished its
+// start-up and forbids device allocation afterwards (fixed-memory production runs),
+// code that runs between the capture calls of a stream it does not own, or a plug-in
+// whose host application owns the allocator.  mic_bin_sort_noalloc serves them: the
+// caller passes device pointers for its inputs and outputs, and the sort's scratch (keys,
+// the second value buffer, the digit histograms and the scan's block totals) lives in the
+// file-scope device array below, reserved once when the library loads on a device and
+// held until the process exits.  Every call shares that array, so calls whose work
+// overlaps on the GPU (different streams, or different host threads on one device) race
+// and must be ordered by the caller.
+
+#include <mutex>
+
+namespace {
+
+constexpr int64_t kNoallocMaxMarkers = MIC_NOALLOC_MAX_MARKERS;
+constexpr int64_t kNoallocMaxCells = MIC_NOALLOC_MAX_CELLS;
+constexpr int64_t kNoallocTiles = (kNoallocMaxMarkers + kTile - 1) / kTile;
+constexpr int64_t kNoallocHist = (int64_t)kBuckets * kNoallocTiles;
+// block totals of every scan level of the histogram matrix, with one spare entry per level
+constexpr int64_t kNoallocAux = (kNoallocHist + kScanBlock - 1) / kScanBlock + 64;
+// layout (in 4-byte words): key | key_alt | val_alt | hist | aux, then one 8-byte counter
+constexpr int64_t kOffKey = 0;
+constexpr int64_t kOffKeyAlt = kOffKey + kNoallocMaxMarkers;
+constexpr int64_t kOffValAlt = kOffKeyAlt + kNoallocMaxMarkers;
+constexpr int64_t kOffHist = kOffValAlt + kNoallocMaxMarkers;
+constexpr int64_t kOffAux = kOffHist + kNoallocHist;
+constexpr int64_t kWords = (kOffAux + kNoallocAux + 63) / 64 * 64;
+constexpr size_t kNoallocBytes = (size_t)kWords * 4 + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+// host-side: device address of g_noalloc_scratch per device (the symbol itself is only a
+// host stand-in and must never be handed to a kernel)
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[64];
+
+__global__ void k_find_cells_grid(const double *__restrict__ X, const double *__restrict__ Y,
+                                  const double *__restrict__ xg, const double *__restrict__ yg, int NX, int NY,
+                                  double LX, double LY, int *__restrict__ cellX, int *__restrict__ cellY,
+                                  int *__restrict__ key, int64_t n, unsigned long long *n_out) {
+  __shared__ unsigned long long s_out;
+  if (threadIdx.x == 0) s_out = 0;
+  __syncthreads();
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m < n) {
+    const long long ux = nonneg_bits(X[m]), uy = nonneg_bits(Y[m]);
+    const bool in = ux >= 0 && uy >= 0 && ux <= __double_as_longlong(LX) && uy <= __double_as_longlong(LY);
+    int cx = -1, cy = -1, k = (NX - 1) * (NY - 1);
+    if (in) {
+      int lo = 0, hi = NX - 1;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (ux >= nonneg_bits(xg[mid])) lo = mid; else hi = mid;
+      }
+      cx = lo;
+      lo = 0;
+      hi = NY - 1;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (uy >= nonneg_bits(yg[mid])) lo = mid; else hi = mid;
+      }
+      cy = lo;
+      k = cy * (NX - 1) + cx;
+    } else {
+      atomicAdd(&s_out, 1ULL);
+    }
+    cellX[m] = cx;
+    cellY[m] = cy;
+    key[m] = k;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_out) atomicAdd(n_out, s_out);
+}
+
+int noalloc_scratch(int device, unsigned char **out) {
+  if (device < 0 || device >= 64) return MIC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    unsigned char *p = nullptr;
+    if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return MIC_ERR_CUDA;
+    }
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return MIC_OK;
+}
+
+}  // namespace
+
+extern "C" int mic_bin_sort_noalloc(const double *X, const double *Y, int64_t n, const double *x, const double *y,
+                                    int NX, int NY, double LX, double LY, int32_t *cellX, int32_t *cellY,
+                                    int32_t *perm, int32_t *cell_start, void *stream, int64_t *n_out) {
+  if (n < 0 || NX < 3 || NY < 3 || !x || !y || !cell_start) return MIC_ERR_ARG;
+  if (n > 0 && (!X || !Y || !cellX || !cellY || !perm)) return MIC_ERR_ARG;
+  if (n > kNoallocMaxMarkers) return MIC_ERR_CAPACITY;
+  const int64_t ncells = (int64_t)(NX - 1) * (NY - 1);
+  if (ncells > kNoallocMaxCells) return MIC_ERR_CAPACITY;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return MIC_ERR_NO_DEVICE;
+  unsigned char *base = nullptr;
+  int e = noalloc_scratch(device, &base);
+  if (e) return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  int *words = reinterpret_cast<int *>(base);
+  int *key = words + kOffKey, *key_alt = words + kOffKeyAlt, *val_alt = words + kOffValAlt;
+  int *hist = words + kOffHist, *aux = words + kOffAux;
+  unsigned long long *d_out = reinterpret_cast<unsigned long long *>(base + (size_t)kWords * 4);
+  // the counter keeps the previous call's value: clear it
+  if (cudaMemsetAsync(d_out, 0, sizeof(unsigned long long), s) != cudaSuccess) return MIC_ERR_CUDA;
+  if (n > 0) {
+    k_find_cells_grid<<<grid_for(n), kBlock, 0, s>>>(X, Y, x, y, NX, NY, LX, LY, cellX, cellY, key, n, d_out);
+    if (cudaGetLastError() != cudaSuccess) return MIC_ERR_CUDA;
+    const int ntiles = (int)((n + kTile - 1) / kTile);
+    int bits = 1;
+    while ((1LL << bits) <= ncells) ++bits;
+    const int passes = (bits + kRadixBits - 1) / kRadixBits;
+    // the last pass must write the caller's perm[]: pick the ping-pong order accordingly
+    int *vbuf[2] = {(passes & 1) ? perm : val_alt, (passes & 1) ? val_alt : perm};
+    int *kbuf[2] = {key_alt, key};
+    int *kin = key, *vin = nullptr;
+    for (int p = 0; p < passes; ++p) {
+      int *kout = kbuf[p & 1], *vout = vbuf[p & 1];
+      k_radix_hist<<<ntiles, kSortThreads, 0, s>>>(kin, n, p * kRadixBits, hist, ntiles);
+      if (cudaGetLastError() != cudaSuccess) return MIC_ERR_CUDA;
+      // every bucket of every tile is written by k_radix_hist, so nothing stale survives
+      const int64_t len = (int64_t)kBuckets * ntiles;
+      const int64_t nb = (len + kScanBlock - 1) / kScanBlock;
+      if (nb <= 1) {
+        k_scan_block<<<1, kScanThreads, 0, s>>>(hist, len, nullptr);
+      } else {
+        // two levels suffice: nb <= kScanBlock for the largest histogram matrix
+        k_scan_block<<<(unsigned)nb, kScanThreads, 0, s>>>(hist, len, aux);
+        k_scan_block<<<1, kScanThreads, 0, s>>>(aux, nb, nullptr);
+        k_scan_add<<<(unsigned)nb, kScanThreads, 0, s>>>(hist, len, aux);
+      }
+      k_radix_scatter<<<ntiles, kSortThreads, 0, s>>>(kin, vin, p == 0, kout, vout, n, p * kRadixBits, hist,
+                                                       ntiles);
+      if (cudaGetLastError() != cudaSuccess) return MIC_ERR_CUDA;
+      kin = kout;
+      vin = vout;
+    }
+    k_cell_start<<<grid_for(n + 1), kBlock, 0, s>>>(kin, n, (int)ncells, cell_start);
+  } else {
+    if (cudaMemsetAsync(cell_start, 0, sizeof(int32_t) * (size_t)(ncells + 2), s) != cudaSuccess)
+      return MIC_ERR_CUDA;
+  }
+  if (cudaGetLastError() != cudaSuccess) return MIC_ERR_CUDA;
+  if (n_out) {
+    unsigned long long h = 0;
+    if (cudaMemcpyAsync(&h, d_out, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MIC_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return MIC_ERR_CUDA;
+    *n_out = (int64_t)h;
+  }
+  return MIC_OK;
+}

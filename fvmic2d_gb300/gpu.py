@@ -66,11 +66,15 @@ SIGNATURES = {
     "mic_launch_count": (_I, [_P, _I64P]),
     "mic_profile_enable": (_I, [_P, _I]),
     "mic_profile_read": (_I, [_P, _I, _P, _DP, _I64P, _IP]),
+    "mic_bin_sort_noalloc": (_I, [_P, _P, _I64, _P, _P, _I, _I, _D, _D, _P, _P, _P, _P, _P, _I64P]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
 
 _libs = {}
+
+NOALLOC_MAX_MARKERS = 1048576  # MIC_NOALLOC_MAX_MARKERS
+NOALLOC_MAX_CELLS = 1048576    # MIC_NOALLOC_MAX_CELLS
 
 
 class MicError(RuntimeError):

@@ -145,6 +145,30 @@ int mic_launch_count(mic_ctx *ctx, int64_t *launches);
  * off); read aggregates by kernel name (names: max * 48 bytes) */
 int mic_profile_enable(mic_ctx *ctx, int capacity);
 int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64_t *counts, int *nkernels);
+/* ---- binning without allocation ----
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc -- a host that
+ * forbids device allocation once it has started, or a plug-in whose application owns the
+ * allocator -- this bins markers and returns their stable cell order without allocating
+ * anything: the caller passes device pointers for every input and output, and the sort's
+ * scratch lives in a fixed device array inside the library, reserved when the library is
+ * loaded on a device and kept until the process exits.
+ *   X, Y [n]          marker positions (device), any order
+ *   x [NX], y [NY]    basic gridlines (device), increasing, x[0] >= 0, y[0] >= 0
+ *   cellX, cellY [n]  out: findMarkerCells' cells (markers.c:41-106), -1 outside the domain
+ *   perm [n]          out: perm[k] = index of the marker at sorted position k (stable by cell)
+ *   cell_start [(NX-1)*(NY-1)+2]  out: first sorted position of each cell; the last two
+ *                     entries bracket the out-of-domain markers
+ *   stream            cudaStream_t to run on (NULL: the legacy default stream)
+ *   n_out             optional host pointer: markers outside the domain (synchronises stream)
+ * Limits: n <= MIC_NOALLOC_MAX_MARKERS and (NX-1)*(NY-1) <= MIC_NOALLOC_MAX_CELLS, else
+ * MIC_ERR_CAPACITY.  The first call on a device looks up the array's device address, so make
+ * that first call before capturing a stream.  All calls share the one array: calls that overlap
+ * on the GPU race and must be ordered by the caller. */
+#define MIC_NOALLOC_MAX_MARKERS 1048576
+#define MIC_NOALLOC_MAX_CELLS 1048576
+int mic_bin_sort_noalloc(const double *X, const double *Y, int64_t n, const double *x, const double *y, int NX,
+                         int NY, double LX, double LY, int32_t *cellX, int32_t *cellY, int32_t *perm,
+                         int32_t *cell_start, void *stream, int64_t *n_out);
 /* pinned host memory for fast transfers */
 int mic_host_alloc(void **ptr, int64_t bytes);
 int mic_host_free(void *ptr);
