@@ -5,8 +5,11 @@
 // (valid because every compared value is non-negative): the same answer as the reference's
 // bisection, with no FP64 instructions on a GPU whose FP64 rate is 1/60 of FP32.
 //
-// Sorting: key = cellY*(NX-1) + cellX, out-of-domain markers get key (NX-1)*(NY-1).  An
-// LSD radix sort with 8-bit digits (stable by construction) orders (key, index) pairs:
+// Sorting: key = 4*(cellY*(NX-1) + cellX) + 2*qy + qx, where (qx, qy) is the marker's quadrant
+// of its cell (X >= xc[cellX+1], Y >= yc[cellY+1]: the stagger test of findCellStag2D); out-of-
+// domain markers get key 4*(NX-1)*(NY-1).  Cells stay contiguous and inside a cell the markers
+// of each quadrant are contiguous, so every staggered (cell-centre) cell's markers are four
+// runs.  An LSD radix sort with 8-bit digits (stable by construction) orders (key, index) pairs:
 // per 4096-marker tile a digit histogram, one exclusive scan over the digit-major
 // histogram matrix, then a scatter in which each tile ranks its items per digit with warp
 // match/ballot in index order.  Ties keep the current device order, so the result equals
@@ -51,11 +54,12 @@ __global__ void k_find_cells(Params P, const double *__restrict__ X, const doubl
     const long long blx = __double_as_longlong(P.LX), bly = __double_as_longlong(P.LY);
     // X >= 0 && Y >= 0 && X <= LX && Y <= LY; NaN fails every test
     const bool in = ux >= 0 && uy >= 0 && ux <= blx && uy <= bly;
-    int cx = -1, cy = -1, k = (P.NX - 1) * (P.NY - 1);
+    int cx = -1, cy = -1, k = 4 * (P.NX - 1) * (P.NY - 1);
     if (in) {
       cx = bisect_bits(P.xbits, P.NX, ux);
       cy = bisect_bits(P.ybits, P.NY, uy);
-      k = cy * (P.NX - 1) + cx;
+      const int qx = ux >= nonneg_bits(P.xc[cx + 1]), qy = uy >= nonneg_bits(P.yc[cy + 1]);
+      k = 4 * (cy * (P.NX - 1) + cx) + 2 * qy + qx;
     } else {
       atomicAdd(&s_out, 1ULL);
     }
@@ -184,13 +188,18 @@ __global__ void k_radix_scatter(const int *__restrict__ key_in, const int *__res
   }
 }
 
-// cell_start[c] = first sorted position with key >= c, for c in [0, ncells+1]
-__global__ void k_cell_start(const int *__restrict__ skey, int64_t n, int ncells, int *__restrict__ cs) {
+// From the sorted (cell, quadrant) keys: qs[q] = first sorted position with key >= q for
+// q in [0, 4*ncells+4] (when qs is given) and cs[c] = qs[4c] for c in [0, ncells+1].
+__global__ void k_cell_start(const int *__restrict__ skey, int64_t n, int ncells, int *__restrict__ cs,
+                             int *__restrict__ qs) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k > n) return;
-  const int hi = (k < n) ? skey[k] : ncells + 1;
+  const int hi = (k < n) ? skey[k] : 4 * ncells + 4;
   const int lo = (k == 0) ? -1 : skey[k - 1];
-  for (int c = lo + 1; c <= hi; ++c) cs[c] = (int)k;
+  for (int q = lo + 1; q <= hi; ++q) {
+    if (qs) qs[q] = (int)k;
+    if ((q & 3) == 0) cs[q >> 2] = (int)k;
+  }
 }
 
 struct GatherCols {
@@ -261,6 +270,7 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   cudaMemsetAsync(&ctx->d_status->n_out, 0, sizeof(unsigned long long), ctx->stream);
   if (n == 0) {
     MIC_CUDA_TRY(cudaMemsetAsync(ctx->cell_start, 0, sizeof(int) * ((size_t)ctx->ncells + 2), ctx->stream));
+    MIC_CUDA_TRY(cudaMemsetAsync(ctx->quad_start, 0, sizeof(int) * (4 * (size_t)ctx->ncells + 5), ctx->stream));
     ctx->sorted = 1;
     if (n_out) *n_out = 0;
     return MIC_OK;
@@ -276,7 +286,7 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   int e = ensure_sort_scratch(ctx, ntiles);
   if (e) return e;
   int bits = 1;
-  while ((1LL << bits) <= (long long)ctx->ncells) ++bits;
+  while ((1LL << bits) <= 4LL * ctx->ncells) ++bits;
   const int passes = (bits + kRadixBits - 1) / kRadixBits;
   int *kin = ctx->key, *kout = ctx->key_alt, *vin = ctx->perm, *vout = ctx->perm_alt;
   for (int p = 0; p < passes; ++p) {
@@ -304,7 +314,8 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   // kin / vin now hold the sorted keys and the permutation
   {
     MIC_KERNEL(ctx, "k_cell_start");
-    k_cell_start<<<grid_for(n + 1), kBlock, 0, ctx->stream>>>(kin, n, ctx->ncells, ctx->cell_start);
+    k_cell_start<<<grid_for(n + 1), kBlock, 0, ctx->stream>>>(kin, n, ctx->ncells, ctx->cell_start,
+                                                             ctx->quad_start);
   }
   MIC_CUDA_TRY(cudaGetLastError());
   GatherCols g;
@@ -405,7 +416,7 @@ __global__ void k_find_cells_grid(const double *__restrict__ X, const double *__
   if (m < n) {
     const long long ux = nonneg_bits(X[m]), uy = nonneg_bits(Y[m]);
     const bool in = ux >= 0 && uy >= 0 && ux <= __double_as_longlong(LX) && uy <= __double_as_longlong(LY);
-    int cx = -1, cy = -1, k = (NX - 1) * (NY - 1);
+    int cx = -1, cy = -1, k = 4 * (NX - 1) * (NY - 1);
     if (in) {
       int lo = 0, hi = NX - 1;
       while (hi - lo > 1) {
@@ -420,7 +431,10 @@ __global__ void k_find_cells_grid(const double *__restrict__ X, const double *__
         if (uy >= nonneg_bits(yg[mid])) lo = mid; else hi = mid;
       }
       cy = lo;
-      k = cy * (NX - 1) + cx;
+      // quadrant of the cell: the same test as the context binning (cell centres from x, y)
+      const int qx = ux >= nonneg_bits((xg[cx] + xg[cx + 1]) / 2.0);
+      const int qy = uy >= nonneg_bits((yg[cy] + yg[cy + 1]) / 2.0);
+      k = 4 * (cy * (NX - 1) + cx) + 2 * qy + qx;
     } else {
       atomicAdd(&s_out, 1ULL);
     }
@@ -474,7 +488,7 @@ extern "C" int mic_bin_sort_noalloc(const double *X, const double *Y, int64_t n,
     if (cudaGetLastError() != cudaSuccess) return MIC_ERR_CUDA;
     const int ntiles = (int)((n + kTile - 1) / kTile);
     int bits = 1;
-    while ((1LL << bits) <= ncells) ++bits;
+    while ((1LL << bits) <= 4 * ncells) ++bits;
     const int passes = (bits + kRadixBits - 1) / kRadixBits;
     // the last pass must write the caller's perm[]: pick the ping-pong order accordingly
     int *vbuf[2] = {(passes & 1) ? perm : val_alt, (passes & 1) ? val_alt : perm};
@@ -501,7 +515,7 @@ extern "C" int mic_bin_sort_noalloc(const double *X, const double *Y, int64_t n,
       kin = kout;
       vin = vout;
     }
-    k_cell_start<<<grid_for(n + 1), kBlock, 0, s>>>(kin, n, (int)ncells, cell_start);
+    k_cell_start<<<grid_for(n + 1), kBlock, 0, s>>>(kin, n, (int)ncells, cell_start, nullptr);
   } else {
     if (cudaMemsetAsync(cell_start, 0, sizeof(int32_t) * (size_t)(ncells + 2), s) != cudaSuccess)
       return MIC_ERR_CUDA;

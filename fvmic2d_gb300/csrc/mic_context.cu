@@ -121,11 +121,15 @@ static void free_ctx(mic_ctx *ctx) {
   for (int f = 0; f < 6; ++f) cudaFree(ctx->node_scr[f]);
   cudaFree(ctx->grid_buf);
   cudaFree(ctx->bits_buf);
+  cudaFree(ctx->spacing_buf);
   cudaFree(ctx->key);
   cudaFree(ctx->key_alt);
   cudaFree(ctx->perm);
   cudaFree(ctx->perm_alt);
   cudaFree(ctx->cell_start);
+  cudaFree(ctx->quad_start);
+  cudaFree(ctx->part_b);
+  cudaFree(ctx->part_c);
   cudaFree(ctx->hist);
   cudaFree(ctx->scan_aux);
   for (int g = 0; g < 4; ++g) cudaFree(ctx->geo[g]);
@@ -222,6 +226,41 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ctx->P.yc = ctx->grid_buf + 2 * nx4 + ny4 + 2;
   ctx->P.xbits = ctx->bits_buf;
   ctx->P.ybits = ctx->bits_buf + nx4;
+  {
+    // spacing tables: 8 arrays of nx4 / ny4 entries (hx, ix, hxc, ixc sized nx4; hy, iy, hyc, iyc ny4)
+    const size_t tot = 4 * nx4 + 4 * ny4;
+    ALLOC(ctx->spacing_buf, sizeof(double) * tot);
+    double *h = (double *)calloc(tot, sizeof(double));
+    double *hx_ = h, *ix_ = h + nx4, *hxc_ = h + 2 * nx4, *ixc_ = h + 3 * nx4;
+    double *hy_ = h + 4 * nx4, *iy_ = hy_ + ny4, *hyc_ = hy_ + 2 * ny4, *iyc_ = hy_ + 3 * ny4;
+    for (int i = 0; i + 1 < NX; ++i) {
+      hx_[i] = hx[i + 1] - hx[i];
+      ix_[i] = 1.0 / hx_[i];
+    }
+    for (int i = 0; i < NX; ++i) {
+      hxc_[i] = hxc[i + 1] - hxc[i];
+      ixc_[i] = 1.0 / hxc_[i];
+    }
+    for (int j = 0; j + 1 < NY; ++j) {
+      hy_[j] = hy[j + 1] - hy[j];
+      iy_[j] = 1.0 / hy_[j];
+    }
+    for (int j = 0; j < NY; ++j) {
+      hyc_[j] = hyc[j + 1] - hyc[j];
+      iyc_[j] = 1.0 / hyc_[j];
+    }
+    cudaMemcpy(ctx->spacing_buf, h, sizeof(double) * tot, cudaMemcpyHostToDevice);
+    free(h);
+    const double *d = ctx->spacing_buf;
+    ctx->P.hx = d;
+    ctx->P.ix = d + nx4;
+    ctx->P.hxc = d + 2 * nx4;
+    ctx->P.ixc = d + 3 * nx4;
+    ctx->P.hy = d + 4 * nx4;
+    ctx->P.iy = d + 4 * nx4 + ny4;
+    ctx->P.hyc = d + 4 * nx4 + 2 * ny4;
+    ctx->P.iyc = d + 4 * nx4 + 3 * ny4;
+  }
   const int64_t cap = max_markers > 0 ? max_markers : 1;
   ctx->cap = cap;
   for (int c = 0; c < C_F64_COUNT; ++c) {
@@ -244,6 +283,9 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ALLOC(ctx->perm, sizeof(int) * cap);
   ALLOC(ctx->perm_alt, sizeof(int) * cap);
   ALLOC(ctx->cell_start, sizeof(int) * ((size_t)ctx->ncells + 2));
+  ALLOC(ctx->quad_start, sizeof(int) * (4 * (size_t)ctx->ncells + 5));
+  ALLOC(ctx->part_b, sizeof(double) * 32 * (size_t)ctx->ncells);
+  ALLOC(ctx->part_c, sizeof(double) * 20 * nn);
   for (int g = 0; g < 4; ++g) ALLOC(ctx->geo[g], sizeof(double) * cap);
   ALLOC(ctx->geo_flags, sizeof(int) * cap);
   ALLOC(ctx->scr0, sizeof(double) * cap);

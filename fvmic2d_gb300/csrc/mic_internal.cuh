@@ -42,6 +42,9 @@ struct Params {  // everything a kernel needs besides the marker columns; passed
   double LX, LY;
   const double *x, *y, *xc, *yc;  // point at index 0 (ghost entries at -2, -1 exist)
   const long long *xbits, *ybits; // bit patterns of x[0..NX-1], y[0..NY-1] for integer compares
+  // cell spacings h[i] = g[i+1] - g[i] (the reference's own differences) and their correctly
+  // rounded reciprocals, for basic lines (i in [0, N-2]) and cell centres (i in [0, N-1])
+  const double *hx, *ix, *hy, *iy, *hxc, *ixc, *hyc, *iyc;
 };
 
 }  // namespace mic
@@ -52,6 +55,7 @@ struct mic_ctx {
   int owns_stream;
   mic::Params P;
   double *grid_buf;  // device: x, xc, y, yc with ghosts
+  double *spacing_buf;  // device: hx, ix, hy, iy, hxc, ixc, hyc, iyc
   long long *bits_buf;
   double *h_x, *h_y, *h_xc, *h_yc;  // host copies (with ghosts)
   mic_materials mat;
@@ -67,6 +71,8 @@ struct mic_ctx {
   int ncells;
   int *key, *key_alt, *perm, *perm_alt;
   int *cell_start;     // ncells + 2 entries
+  int *quad_start;     // 4*ncells + 5 entries: runs of each (cell, quadrant)
+  double *part_b, *part_c;  // per-cell corner partial sums of the projections (product build)
   int *hist;           // radix histograms (digit-major per tile)
   int hist_cap;
   int *scan_aux;
@@ -141,6 +147,21 @@ __device__ __forceinline__ long long nonneg_bits(double v) {
 __device__ __forceinline__ long long ordered_bits(double v) {
   long long b = __double_as_longlong(v);
   return b >= 0 ? b : (long long)(0x8000000000000000ULL) - b;
+}
+
+// num / den for a grid-spacing divisor den whose correctly rounded reciprocal is inv.  The
+// FMA-free parity build divides.  The product build multiplies by the reciprocal and corrects
+// the quotient with one residual step (Markstein): q = num*inv, e = num - q*den (exact with
+// FMA), q + e*inv -- the correctly rounded quotient, for a third of a division's FP64 work.
+__device__ __forceinline__ double div_sp(double num, double den, double inv) {
+#ifdef MIC_EXACT
+  (void)inv;
+  return num / den;
+#else
+  const double q = num * inv;
+  const double e = fma(-q, den, num);
+  return fma(e, inv, q);
+#endif
 }
 
 // Running bilinear sum in the order 00, 01, 10, 11 of updateMarkerStrainPressure.c:152-158,

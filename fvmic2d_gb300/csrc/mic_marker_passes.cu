@@ -19,6 +19,30 @@ namespace {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// Bilinear value of corners (00, 10, 01, 11) at fractions (tx, ty) in lerp form: three
+// subtractions and three FMAs (product build only).
+__device__ __forceinline__ double lerp2(double f00, double f10, double f01, double f11, double tx, double ty) {
+  const double a = fma(tx, f10 - f00, f00);
+  const double b = fma(tx, f11 - f01, f01);
+  return fma(ty, b - a, a);
+}
+
+// cos, sin, sin 2t, cos 2t of the rotation angle t of markers.c:2158-2164.  Per-step rotations
+// are small: for |t| <= 2^-6 truncated Taylor series (to t^7 / t^8, remainder below 2^-60
+// relative) and the double-angle identities replace four transcendental calls; larger angles
+// use sincos.
+__device__ __forceinline__ void small_angle_rotation(double t, double &c, double &s, double &s2, double &c2) {
+  if (fabs(t) <= 0.015625) {
+    const double t2 = t * t;
+    s = t * fma(t2, fma(t2, fma(t2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), 1.0);
+    c = fma(t2, fma(t2, fma(t2, fma(t2, 1.0 / 40320.0, -1.0 / 720.0), 1.0 / 24.0), -0.5), 1.0);
+  } else {
+    sincos(t, &s, &c);
+  }
+  s2 = 2.0 * s * c;
+  c2 = (c - s) * (c + s);
+}
+
 // Interpolation cell at cell centres (updateMarkerStrainPressure.c:137-150, updateMarkerStress.c:66-80,
 // subgridStressChanges.c:179-190): staggered cell clamped to the interior [1, NX-2] x [1, NY-2].
 // Where the clamp leaves the staggered cell unchanged the offsets are the projection geometry.
@@ -27,8 +51,8 @@ __device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, i
   const int sx = cx + (fl & 1), sy = cy + ((fl >> 1) & 1);
   i = clampi(sx, 1, P.NX - 2);
   j = clampi(sy, 1, P.NY - 2);
-  mdx = (i == sx) ? gx1 : (x - P.xc[i]) / (P.xc[i + 1] - P.xc[i]);
-  mdy = (j == sy) ? gy1 : (y - P.yc[j]) / (P.yc[j + 1] - P.yc[j]);
+  mdx = (i == sx) ? gx1 : div_sp(x - P.xc[i], P.hxc[i], P.ixc[i]);
+  mdy = (j == sy) ? gy1 : div_sp(y - P.yc[j], P.hyc[j], P.iyc[j]);
 }
 
 // computeRheology (viscosity.c:12-67); returns false for an undefined law
@@ -213,9 +237,17 @@ __global__ void k_strain_pressure(Params P, StrainCols c, Geo g, Nodal nd, doubl
   const double msxy = interp_run(nd.soxy, NX, cx, cy, bx, by);
   const double mdsxy = interp_run(nd.dsxy, NX, cx, cy, bx, by);
   const double eta = c.eta[m], mu = c.mu[m];
+#ifdef MIC_EXACT
   const double e11 = msxx / 2.0 / eta + mdsxx / 2.0 / dt / mu;
   const double e22 = msyy / 2.0 / eta + mdsyy / 2.0 / dt / mu;
   const double e12 = msxy / 2.0 / eta + mdsxy / 2.0 / dt / mu;
+#else
+  // two divisions instead of nine: 1/(2 eta) and 1/(2 dt mu) shared by the three components
+  const double ie = 0.5 / eta, idm = 0.5 / (dt * mu);
+  const double e11 = fma(mdsxx, idm, msxx * ie);
+  const double e22 = fma(mdsyy, idm, msyy * ie);
+  const double e12 = fma(mdsxy, idm, msxy * ie);
+#endif
   c.exx[m] = e11;
   c.eyy[m] = e22;
   c.exy[m] = e12;
@@ -276,8 +308,12 @@ __global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal n
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
+#ifdef MIC_EXACT
   const double sdm = c.eta[m] / c.mu[m];
   double sdif = -D * dt / sdm;
+#else
+  double sdif = -D * dt * c.mu[m] / c.eta[m];
+#endif
   if (sdif < -30.0) sdif = -30.0;
   sdif = 1.0 - exp(sdif);
   double dsxy = interp_run(nd.soxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]) - c.sxy[m];
@@ -401,8 +437,17 @@ __global__ void k_subgridT_markers(Params P, SubTCols c, Geo g, const double *__
                      cpn[k01] * (1.0 - mdx) * (mdy) + cpn[k11] * mdx * mdy;
   const double km = kn[k00] * (1.0 - mdx) * (1.0 - mdy) + kn[k10] * (mdx) * (1.0 - mdy) +
                     kn[k01] * (1.0 - mdx) * (mdy) + kn[k11] * mdx * mdy;
+#ifdef MIC_EXACT
   const double tdiff = cpm * rhom / km / (2.0 / (dx * dx) + 2.0 / (dy * dy));
   c.dTsub[m] = (Tm - c.T[m]) * (1.0 - exp(-D * dt / tdiff));
+#else
+  (void)dx;
+  (void)dy;
+  // -D dt / tdiff with 1/dx^2, 1/dy^2 from the reciprocal tables: one division
+  const double ixx = P.ix[i], iyy = P.iy[j];
+  const double arg = -D * dt * km * (2.0 * (ixx * ixx + iyy * iyy)) / (cpm * rhom);
+  c.dTsub[m] = (Tm - c.T[m]) * (1.0 - exp(arg));
+#endif
 }
 
 // nodal remainder thisT - lastT - projected subgrid change (VecAXPBYPCZ with alpha = 1)
@@ -467,8 +512,13 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     vyY = clampi(vyY, 0, NY - 2);
     double ax = xcur - P.x[vxX];
     double ay = ycur - P.yc[vxY + 1];
+#ifdef MIC_EXACT
     double hx = P.x[vxX + 1] - P.x[vxX];
     double hy = P.yc[vxY + 2] - P.yc[vxY + 1];
+#else
+    const double tx = div_sp(ax, P.hx[vxX], P.ix[vxX]);
+    const double ty = div_sp(ay, P.hyc[vxY + 1], P.iyc[vxY + 1]);
+#endif
     const size_t r1 = (size_t)(vxY + 1) * NX;
     double vul, vur;
     if (vxY == -1 && top.type[0] == 0) {
@@ -482,10 +532,14 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
       vur = vx[r1 - NX + vxX + 1];
     }
     const double vll = vx[r1 + vxX], vlr = vx[r1 + vxX + 1];
+#ifdef MIC_EXACT
     double t = vul * (1.0 - ax / hx) * (1.0 - ay / hy);
     t += vur * (ax / hx) * (1.0 - ay / hy);
     t += vll * (1.0 - ax / hx) * (ay / hy);
     t += vlr * (ax * ay) / hx / hy;
+#else
+    double t = lerp2(vul, vur, vll, vlr, tx, ty);
+#endif
     mvx[s] = t;
     const size_t q0 = (size_t)vyY * NX, q1 = q0 + NX;
     const double wur = vy[q0 + vyX + 1], wlr = vy[q1 + vyX + 1];
@@ -502,20 +556,28 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     }
     ax = xcur - P.xc[vyX + 1];
     ay = ycur - P.y[vyY];
+#ifdef MIC_EXACT
     hx = P.xc[vyX + 2] - P.xc[vyX + 1];
     hy = P.y[vyY + 1] - P.y[vyY];
     t = wul * (1.0 - ax / hx) * (1.0 - ay / hy);
     t += wur * (ax / hx) * (1.0 - ay / hy);
     t += wll * (1.0 - ax / hx) * (ay / hy);
     t += wlr * (ax * ay) / hx / hy;
+#else
+    t = lerp2(wul, wur, wll, wlr, div_sp(ax, P.hxc[vyX + 1], P.ixc[vyX + 1]), div_sp(ay, P.hy[vyY], P.iy[vyY]));
+#endif
     mvy[s] = t;
-    const double mdx = (xcur - P.x[i]) / (P.x[i + 1] - P.x[i]);
-    const double mdy = (ycur - P.y[j]) / (P.y[j + 1] - P.y[j]);
+    const double mdx = div_sp(xcur - P.x[i], P.hx[i], P.ix[i]);
+    const double mdy = div_sp(ycur - P.y[j], P.hy[j], P.iy[j]);
     const size_t w0 = (size_t)j * NX + i;
+#ifdef MIC_EXACT
     t = (1.0 - mdx) * (1.0 - mdy) * wz[w0];
     t += (mdx) * (1.0 - mdy) * wz[w0 + 1];
     t += (1.0 - mdx) * (mdy)*wz[w0 + NX];
     t += (mdx) * (mdy)*wz[w0 + NX + 1];
+#else
+    t = lerp2(wz[w0], wz[w0 + 1], wz[w0 + NX], wz[w0 + NX + 1], mdx, mdy);
+#endif
     mwz[s] = t;
     if (s < 2) {
       xcur = X0 + dt / 2 * mvx[s];
@@ -535,7 +597,12 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
   c.Y[m] = Y0 + dt * VY;
   const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
   const double th = -w * dt;
+#ifdef MIC_EXACT
   const double ct = cos(th), st_ = sin(th), s2 = sin(2.0 * th), c2 = cos(2.0 * th);
+#else
+  double ct, st_, s2, c2;
+  small_angle_rotation(th, ct, st_, s2, c2);
+#endif
   c.sxx[m] = s11 * (ct * ct) + s22 * (st_ * st_) - s12 * s2;
   c.syy[m] = s11 * (st_ * st_) + s22 * (ct * ct) + s12 * s2;
   c.sxy[m] = 0.5 * (s11 - s22) * s2 + s12 * c2;

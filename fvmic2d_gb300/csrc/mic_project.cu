@@ -33,14 +33,14 @@ __global__ void k_geometry(Params P, const double *__restrict__ X, const double 
   }
   const double x = X[m], y = Y[m];
   // basic cell (markerProjection.c:131-146, stagger 0)
-  const double mdx0 = (x - P.x[cx]) / (P.x[cx + 1] - P.x[cx]);
-  const double mdy0 = (y - P.y[cy]) / (P.y[cy + 1] - P.y[cy]);
+  const double mdx0 = div_sp(x - P.x[cx], P.hx[cx], P.ix[cx]);
+  const double mdy0 = div_sp(y - P.y[cy], P.hy[cy], P.iy[cy]);
   // cell-centre cell (findCellStag2D stagger -1, markerProjection.c:260-267, 128-143)
   const int qx = nonneg_bits(x) >= nonneg_bits(P.xc[cx + 1]);
   const int qy = nonneg_bits(y) >= nonneg_bits(P.yc[cy + 1]);
   const int sx = cx + qx, sy = cy + qy;
-  const double mdx1 = (x - P.xc[sx]) / (P.xc[sx + 1] - P.xc[sx]);
-  const double mdy1 = (y - P.yc[sy]) / (P.yc[sy + 1] - P.yc[sy]);
+  const double mdx1 = div_sp(x - P.xc[sx], P.hxc[sx], P.ixc[sx]);
+  const double mdy1 = div_sp(y - P.yc[sy], P.hyc[sy], P.iyc[sy]);
   const long long half = 0x3FE0000000000000LL;  // bits of 0.5; all offsets here are >= 0
   int f = qx | (qy << 1);
   f |= (nonneg_bits(mdx0) >= half) << 2;
@@ -251,6 +251,244 @@ __global__ void __launch_bounds__(128) k_project_generic(Params P, const double 
 
 inline dim3 node_grid(const Params &P) { return dim3((P.NX + 127) / 128, P.NY); }
 
+#ifndef MIC_EXACT
+// ---- product build: divergence-free projection through per-cell corner partials ------
+//
+// One thread per cell runs over the cell's markers, whose quadrant runs are contiguous
+// after the (cell, quadrant) sort, and accumulates each marker's weight into all four
+// corners of its (basic or staggered) cell: every lane of a warp does useful FP64 work
+// on every iteration, instead of one thread per node testing, and mostly discarding, the
+// markers of nine cells.  A node kernel then adds the four cell partials that meet at
+// each node in a fixed order and divides.  Summation order differs from the reference's
+// sequential loop (rounding at the last place); the order is fixed, so results are
+// reproducible run to run.  Corner k = ox + 2*oy; quadrant q = qx + 2*qy.
+
+struct PartialView {
+  const double *T, *eta, *rho, *sxx, *syy, *sxy, *scalar;
+  const int *mat;
+  const double *gx0, *gy0, *gx1, *gy1;
+  const int *flags;
+};
+
+// ALL2: rho, etaS, k, T, Cp, weight per corner (24) + nearest-node sxy, weight (8) = 32 sums.
+// !ALL2: scalar, weight per corner = 8 sums.  part[acc * ncells + cell].
+template <bool ALL2>
+__global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v, const int *__restrict__ qs,
+                                                         mic_materials mat, double *__restrict__ part) {
+  const int ncells = (P.NX - 1) * (P.NY - 1);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  constexpr int NA = ALL2 ? 6 : 2;
+  double acc[4][NA], loc[4][2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+#pragma unroll
+    for (int f = 0; f < NA; ++f) acc[k][f] = 0.0;
+    loc[k][0] = loc[k][1] = 0.0;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int mb = qs[4 * c + q], me = qs[4 * c + q + 1];
+    for (int m = mb; m < me; ++m) {
+      const double mx = v.gx0[m], my = v.gy0[m];
+      const double a = 1.0 - mx, b = 1.0 - my;
+      const double w[4] = {a * b, mx * b, a * my, mx * my};
+      if (ALL2) {
+        const double r = v.rho[m], e = v.eta[m], t = v.T[m];
+        const int mt = v.mat[m];
+        const double kk = mat.materialkThermal[mt], cp = mat.materialCp[mt];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          acc[k][0] = fma(w[k], r, acc[k][0]);
+          acc[k][1] = fma(w[k], e, acc[k][1]);
+          acc[k][2] = fma(w[k], kk, acc[k][2]);
+          acc[k][3] = fma(w[k], t, acc[k][3]);
+          acc[k][4] = fma(w[k], cp, acc[k][4]);
+          acc[k][5] += w[k];
+        }
+        // nearest basic node: (mdx0 >= .5, mdy0 >= .5), the quadrant's own corner but for
+        // markers a rounding away from the midline
+        const int fl = v.flags[m];
+        const int corner = ((fl >> 2) & 1) | (((fl >> 3) & 1) << 1);
+        const double sxy = v.sxy[m];
+        if (corner == q) {
+          loc[q][0] = fma(w[q], sxy, loc[q][0]);
+          loc[q][1] += w[q];
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (k == corner) {
+              loc[k][0] = fma(w[k], sxy, loc[k][0]);
+              loc[k][1] += w[k];
+            }
+        }
+      } else {
+        const double s = v.scalar[m];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          acc[k][0] = fma(w[k], s, acc[k][0]);
+          acc[k][1] += w[k];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+#pragma unroll
+    for (int f = 0; f < NA; ++f) part[(size_t)(k * NA + f) * ncells + c] = acc[k][f];
+    if (ALL2) {
+      part[(size_t)(24 + 2 * k) * ncells + c] = loc[k][0];
+      part[(size_t)(25 + 2 * k) * ncells + c] = loc[k][1];
+    }
+  }
+}
+
+// Staggered (cell-centre) cell s = (sx, sy), sx in [0, NX-1]: its markers are quadrant 3 of
+// basic cell (sx-1, sy-1), quadrant 2 of (sx, sy-1), quadrant 1 of (sx-1, sy) and quadrant 0 of
+// (sx, sy).  ALL2: etaN, weight per corner (8) + nearest-node sxx, syy, weight (12) = 20 sums;
+// !ALL2: scalar, weight per corner = 8.  part[acc * NX*NY + s].
+template <bool ALL2>
+__global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v, const int *__restrict__ qs,
+                                                          double *__restrict__ part) {
+  const int sx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int sy = blockIdx.y;
+  if (sx >= P.NX || sy >= P.NY) return;
+  const int NC = P.NX - 1;
+  const size_t ns = (size_t)P.NX * P.NY, s = (size_t)sy * P.NX + sx;
+  double acc[4][2], loc[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    acc[k][0] = acc[k][1] = 0.0;
+    loc[k][0] = loc[k][1] = loc[k][2] = 0.0;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int dx = r & 1, dy = r >> 1;         // basic cell (sx-1+dx, sy-1+dy) ...
+    const int cx = sx - 1 + dx, cy = sy - 1 + dy;
+    const int q = (1 - dx) + 2 * (1 - dy);      // ... contributes its quadrant q
+    if (cx < 0 || cx > P.NX - 2 || cy < 0 || cy > P.NY - 2) continue;
+    const int qq = 4 * (cy * NC + cx) + q;
+    const int mb = qs[qq], me = qs[qq + 1];
+    for (int m = mb; m < me; ++m) {
+      const double mx = v.gx1[m], my = v.gy1[m];
+      const double a = 1.0 - mx, b = 1.0 - my;
+      const double w[4] = {a * b, mx * b, a * my, mx * my};
+      const double e = ALL2 ? v.eta[m] : v.scalar[m];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        acc[k][0] = fma(w[k], e, acc[k][0]);
+        acc[k][1] += w[k];
+      }
+      if (ALL2) {
+        // nearest cell centre (mdx1 >= .5, mdy1 >= .5): on a uniform grid always the basic
+        // cell's own centre, corner 3 - q
+        const int fl = v.flags[m];
+        const int corner = ((fl >> 4) & 1) | (((fl >> 5) & 1) << 1);
+        const double a1 = v.sxx[m], a2 = v.syy[m];
+        if (corner == 3 - q) {
+          loc[3 - q][0] = fma(w[3 - q], a1, loc[3 - q][0]);
+          loc[3 - q][1] = fma(w[3 - q], a2, loc[3 - q][1]);
+          loc[3 - q][2] += w[3 - q];
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (k == corner) {
+              loc[k][0] = fma(w[k], a1, loc[k][0]);
+              loc[k][1] = fma(w[k], a2, loc[k][1]);
+              loc[k][2] += w[k];
+            }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    part[(size_t)(2 * k) * ns + s] = acc[k][0];
+    part[(size_t)(2 * k + 1) * ns + s] = acc[k][1];
+    if (ALL2) {
+      part[(size_t)(8 + 3 * k) * ns + s] = loc[k][0];
+      part[(size_t)(9 + 3 * k) * ns + s] = loc[k][1];
+      part[(size_t)(10 + 3 * k) * ns + s] = loc[k][2];
+    }
+  }
+}
+
+// Node (i, j): basic sums from cells (i-1,j-1) corner 3, (i,j-1) corner 2, (i-1,j) corner 1,
+// (i,j) corner 0; centre sums from staggered cells with the same offsets.
+__device__ __forceinline__ double guarded(double a, double w) { return (w != 0.0) ? a / w : 0.0; }
+
+__global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__restrict__ pb,
+                                                       const double *__restrict__ pc, All2Out o) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= P.NX || j >= P.NY) return;
+  const int NC = P.NX - 1, ncells = NC * (P.NY - 1);
+  const size_t ns = (size_t)P.NX * P.NY;
+  double b[8] = {0, 0, 0, 0, 0, 0, 0, 0}, c[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int dx = r & 1, dy = r >> 1;
+    const int cx = i - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
+    if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
+      const size_t cc = (size_t)cy * NC + cx;
+#pragma unroll
+      for (int f = 0; f < 6; ++f) b[f] += pb[(size_t)(k * 6 + f) * ncells + cc];
+      b[6] += pb[(size_t)(24 + 2 * k) * ncells + cc];
+      b[7] += pb[(size_t)(25 + 2 * k) * ncells + cc];
+    }
+    if (cx >= 0 && cy >= 0) {  // staggered cells exist for sx in [0, NX-1]
+      const size_t ss = (size_t)cy * P.NX + cx;
+      c[0] += pc[(size_t)(2 * k) * ns + ss];
+      c[1] += pc[(size_t)(2 * k + 1) * ns + ss];
+      c[2] += pc[(size_t)(8 + 3 * k) * ns + ss];
+      c[3] += pc[(size_t)(9 + 3 * k) * ns + ss];
+      c[4] += pc[(size_t)(10 + 3 * k) * ns + ss];
+    }
+  }
+  const size_t q = (size_t)j * P.NX + i;
+  o.rho[q] = guarded(b[0], b[5]);
+  o.etaS[q] = guarded(b[1], b[5]);
+  o.k[q] = guarded(b[2], b[5]);
+  o.lastT[q] = guarded(b[3], b[5]);
+  o.Cp[q] = guarded(b[4], b[5]);
+  o.soxy[q] = guarded(b[6], b[7]);
+  o.etaN[q] = guarded(c[0], c[1]);
+  o.soxx[q] = guarded(c[2], c[4]);
+  o.soyy[q] = guarded(c[3], c[4]);
+  o.rhodot[q] = 0.0;
+  o.muS[q] = 1e99;
+  o.muN[q] = 1e99;
+}
+
+template <int STAG>
+__global__ void __launch_bounds__(128) k_combine_scalar(Params P, const double *__restrict__ part,
+                                                         double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= P.NX || j >= P.NY) return;
+  const int NC = P.NX - 1, ncells = NC * (P.NY - 1);
+  const size_t ns = (size_t)P.NX * P.NY;
+  double a = 0.0, w = 0.0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int dx = r & 1, dy = r >> 1;
+    const int cx = i - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
+    if (STAG == 0) {
+      if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
+        const size_t cc = (size_t)cy * NC + cx;
+        a += part[(size_t)(2 * k) * ncells + cc];
+        w += part[(size_t)(2 * k + 1) * ncells + cc];
+      }
+    } else if (cx >= 0 && cy >= 0) {
+      const size_t ss = (size_t)cy * P.NX + cx;
+      a += part[(size_t)(2 * k) * ns + ss];
+      w += part[(size_t)(2 * k + 1) * ns + ss];
+    }
+  }
+  out[(size_t)j * P.NX + i] = guarded(a, w);
+}
+#endif  // !MIC_EXACT
+
 }  // namespace
 
 int mic_ensure_geometry(mic_ctx *ctx) {
@@ -275,6 +513,40 @@ int mic_ensure_geometry(mic_ctx *ctx) {
 int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
+#ifndef MIC_EXACT
+  {
+    PartialView pv = {};
+    pv.scalar = v;
+    pv.gx0 = ctx->geo[0];
+    pv.gy0 = ctx->geo[1];
+    pv.gx1 = ctx->geo[2];
+    pv.gy1 = ctx->geo[3];
+    pv.flags = ctx->geo_flags;
+    if (stag == 0) {
+      {
+        MIC_KERNEL(ctx, "k_partials_basic<scalar>");
+        k_partials_basic<false><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
+                                                                                     ctx->mat, ctx->part_b);
+      }
+      {
+        MIC_KERNEL(ctx, "k_combine_scalar<0>");
+        k_combine_scalar<0><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, out);
+      }
+    } else {
+      {
+        MIC_KERNEL(ctx, "k_partials_centre<scalar>");
+        k_partials_centre<false><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
+                                                                            ctx->part_c);
+      }
+      {
+        MIC_KERNEL(ctx, "k_combine_scalar<-1>");
+        k_combine_scalar<-1><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_c, out);
+      }
+    }
+    MIC_CUDA_TRY(cudaGetLastError());
+    return MIC_OK;
+  }
+#endif
   if (stag == 0)
     {
       MIC_KERNEL(ctx, "k_project_geo_arith");
@@ -323,10 +595,39 @@ extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
   o.soxx = ctx->nodal[MIC_NF_SOXX];
   o.soyy = ctx->nodal[MIC_NF_SOYY];
   o.soxy = ctx->nodal[MIC_NF_SOXY];
+#ifdef MIC_EXACT
   {
     MIC_KERNEL(ctx, "k_project_all2");
     k_project_all2<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, mv, ctx->cell_start, ctx->mat, o);
   }
+#else
+  PartialView pv = {};
+  pv.T = mv.T;
+  pv.eta = mv.eta;
+  pv.rho = mv.rho;
+  pv.sxx = mv.sxx;
+  pv.syy = mv.syy;
+  pv.sxy = mv.sxy;
+  pv.mat = mv.mat;
+  pv.gx0 = mv.gx0;
+  pv.gy0 = mv.gy0;
+  pv.gx1 = mv.gx1;
+  pv.gy1 = mv.gy1;
+  pv.flags = mv.flags;
+  {
+    MIC_KERNEL(ctx, "k_partials_basic");
+    k_partials_basic<true><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
+                                                                                ctx->mat, ctx->part_b);
+  }
+  {
+    MIC_KERNEL(ctx, "k_partials_centre");
+    k_partials_centre<true><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
+  }
+  {
+    MIC_KERNEL(ctx, "k_combine_all2");
+    k_combine_all2<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
+  }
+#endif
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }

@@ -25,6 +25,19 @@ def cell_keys(markers, NX, NY):
     return np.where(markers["cellX"] < 0, (NX - 1) * (NY - 1), k)
 
 
+def sort_keys(markers, grid):
+    """The binning's sort key: 4 * cell + quadrant (qx = X >= xc[cellX+1], qy = Y >= yc[cellY+1]),
+    out-of-domain markers last."""
+    inside = markers["cellX"] >= 0
+    cx = np.where(inside, markers["cellX"], 0).astype(np.int64)
+    cy = np.where(inside, markers["cellY"], 0).astype(np.int64)
+    with np.errstate(invalid="ignore"):
+        qx = (markers["X"] >= grid.xc[cx + 1]).astype(np.int64)
+        qy = (markers["Y"] >= grid.yc[cy + 1]).astype(np.int64)
+    k = 4 * (cy * (grid.NX - 1) + cx) + 2 * qy + qx
+    return np.where(inside, k, 4 * grid.ncells)
+
+
 def transcendental_free(wl):
     """Same workload with every exp/sin/cos argument made exactly zero: constant viscosity
     laws, no subgrid diffusion, zero vorticity."""
@@ -71,7 +84,7 @@ def test_find_cells_and_sort_match_stable_sort(name):
         assert ok, f + " " + msg
     keys = cell_keys(want, wl.grid.NX, wl.grid.NY)
     ids = G.sorted_ids()
-    np.testing.assert_array_equal(ids, np.argsort(keys, kind="stable"))
+    np.testing.assert_array_equal(ids, np.argsort(sort_keys(want, wl.grid), kind="stable"))
     cs = G.cell_start()
     counts = np.bincount(keys, minlength=wl.grid.ncells + 1)
     np.testing.assert_array_equal(cs, np.concatenate([[0], np.cumsum(counts)]))
@@ -87,7 +100,7 @@ def test_second_binning_is_stable_in_device_order():
     G.findMarkerCells()
     ids1 = G.sorted_ids()
     mk = G.markers
-    keys_prev_order = cell_keys(mk, wl.grid.NX, wl.grid.NY)[ids0]
+    keys_prev_order = sort_keys(mk, wl.grid)[ids0]
     np.testing.assert_array_equal(ids1, ids0[np.argsort(keys_prev_order, kind="stable")])
 
 
@@ -108,8 +121,7 @@ def test_sort_many_cells_and_ragged_counts():
     got = G.markers
     for f in ("cellX", "cellY"):
         np.testing.assert_array_equal(got[f], O.markers[f])
-    keys = cell_keys(O.markers, wl.grid.NX, wl.grid.NY)
-    np.testing.assert_array_equal(G.sorted_ids(), np.argsort(keys, kind="stable"))
+    np.testing.assert_array_equal(G.sorted_ids(), np.argsort(sort_keys(O.markers, wl.grid), kind="stable"))
 
 
 def test_empty_marker_set():
@@ -329,7 +341,7 @@ def test_full_size_vep_box_step_matches_oracle():
     ids = G.sorted_ids()
     assert np.array_equal(np.sort(ids), np.arange(len(ids)))
     mk = G.markers
-    keys = cell_keys(mk, wl.grid.NX, wl.grid.NY)[ids]
+    keys = sort_keys(mk, wl.grid)[ids]
     assert np.all(np.diff(keys) >= 0)
     cs = G.cell_start()
     assert cs[0] == 0 and cs[-1] == len(ids) and np.all(np.diff(cs) >= 0)
