@@ -17,6 +17,8 @@
 #include <string.h>
 
 struct orc_ctx {
+  const double *grain;     /* per-marker grain size for the composite creep law (law 7) */
+  int64_t ngrain;
   int NX, NY;
   double LX, LY;
   double *buf;
@@ -28,6 +30,7 @@ struct orc_ctx {
   double *scratch;         /* per-marker scratch (subgrid temperature change) */
   int64_t scratch_n;
   double residuals[100];   /* residual.c:9-10 ring of stored residuals */
+  const mic_marker *mk_base; /* marker array of the current call (indexes the grain sizes) */
 };
 
 #define NODE(c, f, i, j) ((c)->nodal[f][(size_t)(j) * (size_t)(c)->NX + (size_t)(i)])
@@ -342,6 +345,19 @@ int orc_compute_rheology(const orc_ctx *c, const mic_marker *p, double *eta, dou
       *eta = e;
       return ORC_OK;
     }
+    case 7: {
+      /* composite ice creep: the stress at which the Goldsby-Kohlstedt strain rate
+       * (viscosity.c:106-179) equals the marker's strain-rate invariant */
+      const int64_t m = p - c->mk_base;
+      if (!c->grain || m < 0 || m >= c->ngrain) return ORC_ERR_LAW;
+      const double e2 = 0.5 * (p->e.T11 * p->e.T11 + p->e.T22 * p->e.T22) + p->e.T12 * p->e.T12;
+      const double edot = sqrt(e2);
+      double sst;
+      int it;
+      orc_creep_stress(edot, p->T, c->grain[m], p->p, 1e-14, &sst, &it);
+      *eta = (edot > 0.0) ? sst / (2.0 * edot) : orc_gk_viscosity(0.0, p->T, c->grain[m], p->p);
+      return ORC_OK;
+    }
     default:
       return ORC_ERR_LAW;
   }
@@ -350,6 +366,7 @@ int orc_compute_rheology(const orc_ctx *c, const mic_marker *p, double *eta, dou
 /* checkPlasticYielding (markers.c:1381-1505) */
 int orc_check_plastic_yielding(orc_ctx *c, mic_marker *mk, int64_t n, double dt, int *is_yielding) {
   const mic_materials *M = &c->mat;
+  c->mk_base = mk;
   const double etamin = c->opt.etamin, etamax = c->opt.etamax, frac = c->opt.fractionalEtamin;
   int err = ORC_OK;
   for (int64_t m = 0; m < n; ++m) {
@@ -913,4 +930,67 @@ int64_t orc_sizeof(int which) {
     case 5: return (int64_t)offsetof(mic_materials, Tref);
     default: return -1;
   }
+}
+
+void orc_set_grain(orc_ctx *c, const double *d, int64_t n) {
+  c->grain = d;
+  c->ngrain = n;
+}
+
+/* Strain rate of the Goldsby-Kohlstedt law at stress s: s / (2 eta(s)) with eta from
+ * viscosity.c:106-179 exactly as the reference evaluates it. */
+double orc_gk_strain_rate(double s, double T, double d, double P) {
+  return s / 2.0 / orc_gk_viscosity(s, T, d, P);
+}
+
+/* Stress s* >= 0 with gk_strain_rate(s*) = edot, to relative residual rtol: safeguarded
+ * secant on ln(strain rate) against ln(s), which is nearly linear (local exponent 1 to 4),
+ * inside a bracket that always holds the root; bisection when the secant step leaves it.
+ * Below 1 Pa the law is linear diffusion creep and the root is edot / C. */
+int orc_creep_stress(double edot, double T, double d, double P, double rtol, double *s_out, int *iters) {
+  *iters = 0;
+  if (!(edot > 0.0)) {
+    *s_out = 0.0;
+    return ORC_OK;
+  }
+  const double C = 0.5 / orc_gk_viscosity(0.5, T, d, P); /* linear coefficient, eta = 0.5 / C */
+  double s_lin = edot / C;
+  if (s_lin < 1.0) {
+    *s_out = s_lin;
+    return ORC_OK;
+  }
+  const double le = log(edot);
+  double ulo = 0.0, flo = log(orc_gk_strain_rate(1.0, T, d, P)) - le;
+  if (flo >= 0.0) { /* the rate jumps past edot at s = 1 Pa: the root is the jump point */
+    *s_out = 1.0;
+    return ORC_OK;
+  }
+  double uhi = log(s_lin), fhi = log(orc_gk_strain_rate(s_lin, T, d, P)) - le;
+  while (fhi < 0.0 && *iters < 200) { /* only reached if the linear estimate undershoots */
+    ulo = uhi;
+    flo = fhi;
+    uhi += 2.0;
+    fhi = log(orc_gk_strain_rate(exp(uhi), T, d, P)) - le;
+    (*iters)++;
+  }
+  double u = uhi, f = fhi;
+  for (int it = 0; it < 200; ++it) {
+    (*iters)++;
+    if (fabs(f) <= rtol) break;
+    double un = (flo != fhi) ? uhi - fhi * (uhi - ulo) / (fhi - flo) : 0.5 * (ulo + uhi);
+    if (!(un > ulo && un < uhi)) un = 0.5 * (ulo + uhi);
+    const double fn = log(orc_gk_strain_rate(exp(un), T, d, P)) - le;
+    if (fn > 0.0) {
+      uhi = un;
+      fhi = fn;
+    } else {
+      ulo = un;
+      flo = fn;
+    }
+    u = un;
+    f = fn;
+    if (uhi - ulo <= 1e-15 * fabs(uhi)) break;
+  }
+  *s_out = exp(u);
+  return ORC_OK;
 }

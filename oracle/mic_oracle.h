@@ -73,6 +73,12 @@ double orc_gk_viscosity(double s, double T, double d, double P);
 
 int64_t orc_sizeof(int which);
 
+/* Composite ice creep (material law 7, new): per-marker grain sizes, the strain rate of the
+ * Goldsby-Kohlstedt law and the stress at which it equals a given strain rate. */
+void orc_set_grain(orc_ctx *c, const double *d, int64_t n);
+double orc_gk_strain_rate(double s, double T, double d, double P);
+int orc_creep_stress(double edot, double T, double d, double P, double rtol, double *s_out, int *iters);
+
 #ifdef __cplusplus
 }
 #endif
