@@ -45,10 +45,10 @@ struct ColPtrs {
 };
 
 // byte offsets of the f64 columns inside mic_marker, in F64Col order
-__constant__ int c_f64_off[C_F64_COUNT];
+__constant__ int c_f64_off[C_AOS_F64];
 __constant__ int c_i32_off[C_I32_COUNT - 1];  // all but C_ID
 
-static const int h_f64_off[C_F64_COUNT] = {
+static const int h_f64_off[C_AOS_F64] = {
     (int)offsetof(mic_marker, X),     (int)offsetof(mic_marker, Y),     (int)offsetof(mic_marker, VX),
     (int)offsetof(mic_marker, VY),    (int)offsetof(mic_marker, T),     (int)offsetof(mic_marker, Tdot),
     (int)offsetof(mic_marker, s.T11), (int)offsetof(mic_marker, s.T22), (int)offsetof(mic_marker, s.T12),
@@ -65,7 +65,7 @@ static_assert(sizeof(mic_marker) == 216, "fvmic2d Marker is 216 bytes");
 static_assert(offsetof(mic_marker, cellX) == 184, "fvmic2d Marker layout");
 
 int mic_f64_column_of_offset(int off) {
-  for (int c = 0; c < C_F64_COUNT; ++c)
+  for (int c = 0; c < C_AOS_F64; ++c)
     if (h_f64_off[c] == off) return c;
   return -1;
 }
@@ -75,10 +75,11 @@ __global__ void k_aos_to_soa(const unsigned char *__restrict__ aos, ColPtrs cols
   if (m >= n) return;
   const unsigned char *r = aos + m * (int64_t)sizeof(mic_marker);
 #pragma unroll
-  for (int c = 0; c < C_F64_COUNT; ++c) cols.f[c][m] = *reinterpret_cast<const double *>(r + c_f64_off[c]);
+  for (int c = 0; c < C_AOS_F64; ++c) cols.f[c][m] = *reinterpret_cast<const double *>(r + c_f64_off[c]);
 #pragma unroll
   for (int c = 0; c < C_I32_COUNT - 1; ++c) cols.i[c][m] = *reinterpret_cast<const int *>(r + c_i32_off[c]);
   cols.i[C_ID][m] = (int)m;
+  cols.f[C_GRAIN][m] = 1e-3;  // default grain size until mic_markers_set_grain_size
 }
 
 __global__ void k_soa_to_aos(unsigned char *__restrict__ aos, ColPtrs cols, int64_t n) {
@@ -89,7 +90,7 @@ __global__ void k_soa_to_aos(unsigned char *__restrict__ aos, ColPtrs cols, int6
   unsigned char *r = aos + (int64_t)m * (int64_t)sizeof(mic_marker);
   memset(r, 0, sizeof(mic_marker));
 #pragma unroll
-  for (int c = 0; c < C_F64_COUNT; ++c) *reinterpret_cast<double *>(r + c_f64_off[c]) = cols.f[c][k];
+  for (int c = 0; c < C_AOS_F64; ++c) *reinterpret_cast<double *>(r + c_f64_off[c]) = cols.f[c][k];
 #pragma unroll
   for (int c = 0; c < C_I32_COUNT - 1; ++c) *reinterpret_cast<int *>(r + c_i32_off[c]) = cols.i[c][k];
 }
@@ -139,6 +140,9 @@ static void free_ctx(mic_ctx *ctx) {
   cudaFree(ctx->scr2);
   cudaFree(ctx->red_buf);
   cudaFree(ctx->d_status);
+  cudaFree(ctx->d_creep);
+  cudaFree(ctx->mlp);
+  cudaFree(ctx->train_buf);
   cudaFree(ctx->stage_aos);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -293,6 +297,8 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ALLOC(ctx->scr2, sizeof(double) * cap);
   ctx->red_cap = 4096;
   ALLOC(ctx->red_buf, sizeof(double) * ctx->red_cap);
+  ALLOC(ctx->d_creep, sizeof(CreepCounters));
+  cudaMemset(ctx->d_creep, 0, sizeof(CreepCounters));
   ALLOC(ctx->d_status, sizeof(Status));
   cudaMemset(ctx->d_status, 0, sizeof(Status));
   if (cudaHostAlloc((void **)&ctx->h_status, sizeof(Status), cudaHostAllocDefault) != cudaSuccess) {
@@ -307,6 +313,12 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
     for (int k = 0; k < 3; ++k) s->type[k] = 1;
   }
   ctx->mat.nMaterials = 1;
+  ctx->creep.mode = 0;
+  ctx->creep.polish_iters = 2;
+  ctx->creep.maxit = 60;
+  ctx->creep.tol = 2e-14;
+  ctx->creep.polish_tol = 1e-7;
+  ctx->creep.mlp = nullptr;
   ctx->opt.etamin = 0.0;
   ctx->opt.etamax = 1e300;
   ctx->n = 0;
@@ -578,5 +590,23 @@ extern "C" int mic_profile_read(mic_ctx *ctx, int max, char *names, double *tota
 extern "C" int mic_launch_count(mic_ctx *ctx, int64_t *n) {
   if (!ctx || !n) return MIC_ERR_ARG;
   *n = ctx->launches;
+  return MIC_OK;
+}
+
+// dst[k] = src[id[k]]: a caller-order per-marker array into device (cell-sorted) order
+__global__ void k_gather_by_id(const double *__restrict__ src, const int *__restrict__ id, double *__restrict__ dst,
+                               int64_t n) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  dst[k] = src[id[k]];
+}
+
+int mic_gather_by_id(mic_ctx *ctx, const double *src, double *dst) {
+  if (ctx->n == 0) return MIC_OK;
+  {
+    MIC_KERNEL(ctx, "k_gather_by_id");
+    k_gather_by_id<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(src, ctx->i32[C_ID], dst, ctx->n);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }

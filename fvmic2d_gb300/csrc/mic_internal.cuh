@@ -21,7 +21,10 @@ namespace mic {
 // double-valued marker columns, in mic_marker field order
 enum F64Col {
   C_X = 0, C_Y, C_VX, C_VY, C_T, C_TDOT, C_SXX, C_SYY, C_SXY, C_ETA, C_MU, C_RHO, C_RHODOT, C_P,
-  C_EXX, C_EYY, C_EXY, C_EXX_TOT, C_EYY_TOT, C_EXY_TOT, C_EII, C_WXY, C_SRR, C_F64_COUNT
+  C_EXX, C_EYY, C_EXY, C_EXX_TOT, C_EYY_TOT, C_EXY_TOT, C_EII, C_WXY, C_SRR,
+  C_AOS_F64,              // columns above mirror mic_marker fields; those below are device-only
+  C_GRAIN = C_AOS_F64,    // grain size for the composite creep law (law 7), metres
+  C_F64_COUNT
 };
 // int-valued marker columns
 enum I32Col { C_MAT = 0, C_CELLX, C_CELLY, C_CPU, C_ISYIELD, C_ID, C_I32_COUNT };
@@ -35,6 +38,21 @@ struct Status {
   unsigned long long n_out;         // out-of-domain markers after the last binning
   int is_yielding;                  // any marker yielded in the last checkPlasticYielding
   int pad;
+};
+
+// Composite creep (law 7) settings and per-pass counters
+struct CreepConfig {
+  int mode;             // 0: exact Newton; 1: surrogate guess + polish + exact fallback
+  int polish_iters;     // Newton steps after the surrogate guess
+  int maxit;            // iteration cap of the exact solve
+  double tol;           // exact solve: |rate/edot - 1| <= tol
+  double polish_tol;    // surrogate path: residual above this after polishing -> exact fallback
+  const float *mlp;     // surrogate network parameters (device), see mic_creep.cu
+};
+
+struct CreepCounters {
+  unsigned long long markers, iterations, fallbacks;
+  unsigned long long max_res_bits;  // bits of the largest |rate/edot - 1| (non-negative double)
 };
 
 struct Params {  // everything a kernel needs besides the marker columns; passed by value
@@ -61,6 +79,11 @@ struct mic_ctx {
   mic_materials mat;
   mic_options opt;
   mic_bcs bcs;
+  mic::CreepConfig creep;
+  mic::CreepCounters *d_creep;  // device counters of the last rheology pass
+  float *mlp;                   // device surrogate parameters
+  float *train_buf;             // training scratch (grown on demand)
+  int64_t train_cap;
   int64_t n, cap;
   double *f64[mic::C_F64_COUNT];
   int *i32[mic::C_I32_COUNT];

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "mic_creep.cuh"
 #include "mic_internal.cuh"
 
 using namespace mic;
@@ -55,11 +56,35 @@ __device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, i
   mdy = (j == sy) ? gy1 : div_sp(y - P.yc[j], P.hyc[j], P.iyc[j]);
 }
 
-// computeRheology (viscosity.c:12-67); returns false for an undefined law
+// Inputs of the composite creep law (law 7): the marker's strain-rate invariant, grain size
+// and pressure; iteration count and residual of its stress solve come back in it.
+struct CreepIn {
+  double e11, e22, e12, grain, p;
+  int iters;
+  double res;
+};
+
+// Law 7 (new): composite ice creep, eta = s* / (2 edot_II) with s* the stress at which the
+// Goldsby-Kohlstedt strain rate (viscosity.c:106-179) equals the marker's strain-rate
+// invariant; at zero strain rate the law's diffusion viscosity 0.5 / C (viscosity.c:130-133).
+__device__ __forceinline__ double creep_viscosity_exact(const CreepConfig &cfg, double T, CreepIn &ci) {
+  const double edot = sqrt(0.5 * (ci.e11 * ci.e11 + ci.e22 * ci.e22) + ci.e12 * ci.e12);
+  const CreepCoef k = creep_coef(T, ci.grain, ci.p);
+  if (!(edot > 0.0)) return 0.5 / k.C;
+  const double s = creep_stress_exact(k, edot, cfg.tol, cfg.maxit, &ci.iters, &ci.res);
+  return s / (2.0 * edot);
+}
+
+// computeRheology (viscosity.c:12-67) plus law 7; returns false for an undefined law
 __device__ __forceinline__ bool rheology(const mic_materials &M, const mic_options &O, int k, double T, double X,
-                                         double Y, double &eta, double &mu) {
+                                         double Y, double &eta, double &mu, const CreepConfig *cfg = nullptr,
+                                         CreepIn *ci = nullptr) {
   mu = M.materialMu[k];
   switch (M.hasEtaT[k]) {
+    case 7:
+      if (!cfg || !ci) return false;
+      eta = creep_viscosity_exact(*cfg, T, *ci);
+      return true;
     case 1: eta = M.materialEta[k] * exp(M.QonR[k] * (1.0 / T - 1.0 / M.Tref[k])); return true;
     case 2: {
       const double T0 = M.Tref[k];
@@ -83,16 +108,38 @@ __device__ __forceinline__ bool rheology(const mic_materials &M, const mic_optio
 
 struct YieldCols {
   const int *cellX, *mat;
-  const double *X, *Y, *T, *p, *Eii, *exx, *eyy, *exy;
+  const double *X, *Y, *T, *p, *Eii, *exx, *eyy, *exy, *grain;
   double *eta, *mu, *sxx, *syy, *sxy;
 };
 
+// per-warp reduction of the creep counters into the device totals
+__device__ __forceinline__ void creep_count(CreepCounters *cc, int active, int iters, double res, int fallback) {
+  const unsigned full = 0xffffffffu;
+  int a = active, it = iters, fb = fallback;
+  long long rb = active ? nonneg_bits(fabs(res)) : 0;
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(full, a, o);
+    it += __shfl_down_sync(full, it, o);
+    fb += __shfl_down_sync(full, fb, o);
+    rb = max(rb, __shfl_down_sync(full, rb, o));
+  }
+  if ((threadIdx.x & 31) == 0 && a) {
+    atomicAdd(&cc->markers, (unsigned long long)a);
+    atomicAdd(&cc->iterations, (unsigned long long)it);
+    if (fb) atomicAdd(&cc->fallbacks, (unsigned long long)fb);
+    atomicMax(&cc->max_res_bits, (unsigned long long)rb);
+  }
+}
+
 // checkPlasticYielding (markers.c:1381-1505)
-__global__ void k_yield(YieldCols c, mic_materials M, mic_options O, double dt, int64_t n, Status *st) {
+__global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig cfg, double dt, int64_t n,
+                        Status *st, CreepCounters *cc) {
   __shared__ int s_yield, s_bad;
   if (threadIdx.x == 0) s_yield = s_bad = 0;
   __syncthreads();
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int creep_active = 0, creep_iters = 0;
+  double creep_res = 0.0;
   if (m < n && c.cellX[m] != -1) {
     const double eta_old = c.eta[m], mu_old = c.mu[m];
     double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
@@ -105,11 +152,17 @@ __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, double dt, 
     const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
     const int k = c.mat[m];
     double eta, mu;
-    if (!rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu)) {
+    CreepIn ci = {e11, e22, e12, c.grain[m], c.p[m], 0, 0.0};
+    if (!rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)) {
       eta = eta_old;
       mu = mu_old;
       s_bad = 1;
       atomicAdd(&st->bad_law, 1ULL);
+    }
+    if (M.hasEtaT[k] == 7) {
+      creep_active = 1;
+      creep_iters = ci.iters;
+      creep_res = ci.res;
     }
     const int plast = M.hasPlasticity[k];
     if (plast) {
@@ -160,17 +213,20 @@ __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, double dt, 
     c.eta[m] = eta;
     c.mu[m] = mu;
   }
+  creep_count(cc, creep_active, creep_iters, creep_res, 0);
   __syncthreads();
   if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
   (void)s_bad;
 }
 
 // updateViscosity (viscosity.c:77-88): rheology from the current marker stress
-__global__ void k_update_viscosity(YieldCols c, mic_materials M, mic_options O, int64_t n, Status *st) {
+__global__ void k_update_viscosity(YieldCols c, mic_materials M, mic_options O, CreepConfig cfg, int64_t n,
+                                   Status *st) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n || c.cellX[m] == -1) return;
   double eta, mu;
-  if (!rheology(M, O, c.mat[m], c.T[m], c.X[m], c.Y[m], eta, mu)) {
+  CreepIn ci = {c.exx[m], c.eyy[m], c.exy[m], c.grain[m], c.p[m], 0, 0.0};
+  if (!rheology(M, O, c.mat[m], c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)) {
     atomicAdd(&st->bad_law, 1ULL);
     return;
   }
@@ -679,6 +735,7 @@ YieldCols yield_cols(mic_ctx *ctx) {
   c.exx = ctx->f64[C_EXX];
   c.eyy = ctx->f64[C_EYY];
   c.exy = ctx->f64[C_EXY];
+  c.grain = ctx->f64[C_GRAIN];
   c.eta = ctx->f64[C_ETA];
   c.mu = ctx->f64[C_MU];
   c.sxx = ctx->f64[C_SXX];
@@ -751,11 +808,12 @@ static int yield_launch(mic_ctx *ctx, double dt) {
   if (e) return e;
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->is_yielding, 0, sizeof(int), ctx->stream));
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->bad_law, 0, sizeof(unsigned long long), ctx->stream));
+  MIC_CUDA_TRY(cudaMemsetAsync(ctx->d_creep, 0, sizeof(CreepCounters), ctx->stream));
   if (ctx->n > 0) {
     {
       MIC_KERNEL(ctx, "k_yield");
-      k_yield<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, dt, ctx->n,
-                                                            ctx->d_status);
+      k_yield<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep, dt,
+                                                            ctx->n, ctx->d_status, ctx->d_creep);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }
@@ -780,8 +838,8 @@ extern "C" int mic_update_viscosity(mic_ctx *ctx) {
   if (ctx->n > 0) {
     {
       MIC_KERNEL(ctx, "k_update_viscosity");
-      k_update_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->n,
-                                                                       ctx->d_status);
+      k_update_viscosity<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt,
+                                                                       ctx->creep, ctx->n, ctx->d_status);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }

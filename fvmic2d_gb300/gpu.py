@@ -67,6 +67,15 @@ SIGNATURES = {
     "mic_profile_enable": (_I, [_P, _I]),
     "mic_profile_read": (_I, [_P, _I, _P, _DP, _I64P, _IP]),
     "mic_bin_sort_noalloc": (_I, [_P, _P, _I64, _P, _P, _I, _I, _D, _D, _P, _P, _P, _P, _P, _I64P]),
+    "mic_creep_configure": (_I, [_P, _I, _D, _I, _I, _D]),
+    "mic_markers_set_grain_size": (_I, [_P, _DP, _I64]),
+    "mic_creep_param_count": (_I, []),
+    "mic_creep_set_mlp": (_I, [_P, _P, _I]),
+    "mic_creep_get_mlp": (_I, [_P, _P, _I]),
+    "mic_creep_train": (_I, [_P, _I64, _I, _I, ctypes.c_float, ctypes.c_uint64, _P]),
+    "mic_creep_mlp_grad": (_I, [_P, _P, _P, _P, _I, _P, _P]),
+    "mic_creep_solve_batch": (_I, [_P, _DP, _DP, _DP, _DP, _I64, _I, _DP, _P, _DP, _P]),
+    "mic_creep_stats": (_I, [_P, _I64P, _I64P, _I64P, _DP]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -213,6 +222,59 @@ class MicProblem:
             nm = names.raw[48 * u: 48 * u + 48].split(b"\0", 1)[0].decode()
             out[nm] = (float(tot[u]), int(cnt[u]))
         return out
+
+    # ---- composite creep closure (law 7) ----------------------------------------
+    def set_grain_size(self, d):
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        self._check(self.L.mic_markers_set_grain_size(self.h, _dp(d), len(d)), "mic_markers_set_grain_size")
+
+    def creep_configure(self, mode=0, tol=2e-14, maxit=60, polish_iters=2, polish_tol=1e-7):
+        self._check(self.L.mic_creep_configure(self.h, mode, tol, maxit, polish_iters, polish_tol),
+                    "mic_creep_configure")
+
+    def creep_train(self, nsamples=1 << 20, batch=4096, steps=2000, lr=3e-3, seed=1):
+        hist = np.zeros(steps, dtype=np.float32)
+        self._check(self.L.mic_creep_train(self.h, nsamples, batch, steps, lr, seed, hist.ctypes.data),
+                    "mic_creep_train")
+        return hist
+
+    def creep_params(self):
+        n = self.L.mic_creep_param_count()
+        p = np.zeros(n, dtype=np.float32)
+        self._check(self.L.mic_creep_get_mlp(self.h, p.ctypes.data, n), "mic_creep_get_mlp")
+        return p
+
+    def creep_set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self.L.mic_creep_set_mlp(self.h, p.ctypes.data, len(p)), "mic_creep_set_mlp")
+
+    def creep_grad(self, params, feats, targets):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        feats = np.ascontiguousarray(feats, dtype=np.float32)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.zeros(len(params) - 2, dtype=np.float32)
+        loss = ctypes.c_float(0.0)
+        self._check(self.L.mic_creep_mlp_grad(self.h, params.ctypes.data, feats.ctypes.data, targets.ctypes.data,
+                                              len(targets), g.ctypes.data, ctypes.byref(loss)), "mic_creep_mlp_grad")
+        return g, loss.value
+
+    def creep_solve(self, edot, T, d, P, mode=0):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in np.broadcast_arrays(edot, T, d, P)]
+        n = len(arrs[0])
+        s = np.zeros(n)
+        it = np.zeros(n, dtype=np.int32)
+        res = np.zeros(n)
+        fb = np.zeros(n, dtype=np.int32)
+        self._check(self.L.mic_creep_solve_batch(self.h, *[_dp(a) for a in arrs], n, mode, _dp(s), it.ctypes.data,
+                                                 _dp(res), fb.ctypes.data), "mic_creep_solve_batch")
+        return s, it, res, fb
+
+    def creep_stats(self):
+        a, b, c = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        r = ctypes.c_double(0.0)
+        self._check(self.L.mic_creep_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                           ctypes.byref(r)), "mic_creep_stats")
+        return {"markers": a.value, "iterations": b.value, "fallbacks": c.value, "max_residual": r.value}
 
     def synchronize(self):
         self._check(self.L.mic_synchronize(self.h), "mic_synchronize")

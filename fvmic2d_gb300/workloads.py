@@ -287,10 +287,73 @@ def vep_slab_box(nx_cells=1024, ny_cells=256, nm=4, seed=2):
     return Workload("vep_slab_box", g, m, mat, opt, _free_slip(), nodal, dt, dt, 20)
 
 
+def ice_creep_box(nx_cells=1024, ny_cells=1024, nm=4, seed=3):
+    """Composite ice creep (material law 7): per-marker strain-rate invariant
+    10^U[-18,-10] 1/s, T ~ U[100, 273] K, grain size 10^U[-4,-1] m, pressure U[0, 1e8] Pa;
+    1025 x 1025 nodes and 16,777,216 markers at full size."""
+    NX, NY = nx_cells + 1, ny_cells + 1
+    L = 1.0e5
+    g = Grid(NX, NY, L, L, spacing_uniform(0.0, L, NX), spacing_uniform(0.0, L, NY))
+    m = lattice_markers(g, nm, nm, seed)
+    n = len(m)
+    u = splitmix64_uniform(seed + 7, 5 * n)
+    edot = 10.0 ** (-18.0 + 8.0 * u[0::5])
+    phi = 2.0 * np.pi * u[4::5]
+    m["exx"] = edot * np.cos(phi)
+    m["eyy"] = -m["exx"]
+    m["exy"] = edot * np.sin(phi)
+    m["T"] = 100.0 + 173.0 * u[1::5]
+    grain = 10.0 ** (-4.0 + 3.0 * u[2::5])
+    m["p"] = 1e8 * u[3::5]
+    mat = _materials(1)
+    mat.materialEta[0] = 1e14
+    mat.materialRho[0] = 917.0
+    mat.materialkThermal[0] = 2.1
+    mat.materialCp[0] = 2000.0
+    mat.materialAlpha[0] = 1.6e-4
+    mat.materialMu[0] = 3.5e9
+    mat.hasEtaT[0] = 7
+    opt = Options(etamin=1e8, etamax=1e22, fractionalEtamin=0.01, subgridStressDiffusivity=1.0,
+                  subgridTemperatureDiffusivity=1.0)
+    m["mu"] = 3.5e9
+    m["eta"] = 1e14
+    m["sxx"] = 2.0 * m["eta"] * m["exx"]
+    m["syy"] = 2.0 * m["eta"] * m["eyy"]
+    m["sxy"] = 2.0 * m["eta"] * m["exy"]
+    U = 1e-9
+    pi = np.pi
+    vx_fn = lambda x, y: U * np.sin(pi * x / L) * np.cos(pi * y / L)
+    vy_fn = lambda x, y: -U * np.cos(pi * x / L) * np.sin(pi * y / L)
+    dvx = {"x": lambda x, y: U * pi / L * np.cos(pi * x / L) * np.cos(pi * y / L),
+           "y": lambda x, y: -U * pi / L * np.sin(pi * x / L) * np.sin(pi * y / L)}
+    dvy = {"x": lambda x, y: U * pi / L * np.sin(pi * x / L) * np.sin(pi * y / L),
+           "y": lambda x, y: -U * pi / L * np.cos(pi * x / L) * np.cos(pi * y / L)}
+    vx, vy, exx, eyy, exy, wxy = _velocity_fields(g, vx_fn, vy_fn, dvx, dvy)
+    XCc, YCc = np.meshgrid(g.xc[:NX], g.yc[:NY], indexing="xy")
+    Xb, Yb = np.meshgrid(g.x, g.y, indexing="xy")
+    eta_ref = 1e14
+    nodal = {
+        "vx": vx, "vy": vy, "edotxx": exx, "edotyy": eyy, "edotxy": exy, "wxy": wxy,
+        "p": 1e8 * YCc / L,
+        "soxx": 2.0 * eta_ref * exx, "soyy": 2.0 * eta_ref * eyy, "soxy": 2.0 * eta_ref * exy,
+        "thisT": 100.0 + 173.0 * Yb / L,
+    }
+    nodal["dsxx"] = 0.05 * nodal["soxx"]
+    nodal["dsyy"] = 0.05 * nodal["soyy"]
+    nodal["dsxy"] = 0.05 * nodal["soxy"]
+    dt = 0.5 * (L / nx_cells) / (2 * U)
+    wl = Workload("ice_creep_box", g, m, mat, opt, _free_slip(), nodal, dt, dt, 10)
+    wl.grain_size = grain
+    return wl
+
+
 WORKLOADS = {
     "convection_box": convection_box,
     "vep_slab_box": vep_slab_box,
     # 513 x 129 nodes, 1,048,576 markers (about 220 MB of marker state, larger than L2):
     # the small case used for detailed profiles
     "vep_slab_box_1m": lambda: vep_slab_box(nx_cells=512, ny_cells=128),
+    "ice_creep_box": ice_creep_box,
+    # 513 x 513 nodes, 4,194,304 markers
+    "ice_creep_box_4m": lambda: ice_creep_box(nx_cells=512, ny_cells=512),
 }

@@ -131,6 +131,34 @@ int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_stress, doubl
 int mic_step_post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx);
 int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, double *residual);
 
+/* ---- composite ice creep closure (material law 7; no reference counterpart) ----
+ * fvmic2d evaluates the Goldsby-Kohlstedt law forwards only (goldsbyKohlstedt, viscosity.c:
+ * 106-179, stress -> strain rate).  Law 7 inverts it per marker: the viscosity is s* / (2 edot_II)
+ * where s* is the stress at which the law's strain rate equals the marker's strain-rate
+ * invariant (grain size from mic_markers_set_grain_size, pressure and temperature from the
+ * marker).  mode 0 solves exactly (FP64 Newton to |rate/edot - 1| <= tol); mode 1 starts from
+ * the trained surrogate (4 -> 64 -> 64 -> 1 MLP, hidden layer on the tensor cores in BF16 with
+ * FP32 accumulation), takes polish_iters FP64 Newton steps and finishes with the exact solve for
+ * markers still above polish_tol. */
+int mic_creep_configure(mic_ctx *ctx, int mode, double tol, int maxit, int polish_iters, double polish_tol);
+int mic_markers_set_grain_size(mic_ctx *ctx, const double *grain_size, int64_t n); /* caller order */
+int mic_creep_param_count(void);
+int mic_creep_set_mlp(mic_ctx *ctx, const float *params, int n);
+int mic_creep_get_mlp(mic_ctx *ctx, float *params, int n);
+/* train the surrogate on the GPU from nsamples exact solves (Adam, cosine decay, batch % 128 == 0) */
+int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int steps, float lr, unsigned long long seed,
+                    float *loss_history);
+/* mean-squared-loss gradient of the training kernels at params over n samples (n % 128 == 0) */
+int mic_creep_mlp_grad(mic_ctx *ctx, const float *params, const float *features, const float *targets, int n,
+                       float *grad, float *loss);
+/* batch solve from host arrays: mode 0 exact, 1 surrogate (CUDA-core inference), 2 surrogate
+ * (tensor-core inference); outputs may be NULL except stress */
+int mic_creep_solve_batch(mic_ctx *ctx, const double *edot, const double *T, const double *d, const double *P,
+                          int64_t n, int mode, double *stress, int32_t *iterations, double *residual,
+                          int32_t *fallback);
+/* counters of the last checkPlasticYielding pass over law-7 markers */
+int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iterations, int64_t *fallbacks, double *max_residual);
+
 /* ---- plumbing ---- */
 int mic_synchronize(mic_ctx *ctx);
 int mic_get_stream(mic_ctx *ctx, void **stream);

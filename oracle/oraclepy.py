@@ -51,6 +51,9 @@ def lib():
             "orc_step": (_I, [_P, _P, _I64, _D, _D, _I, _DP]),
             "orc_gk_viscosity": (_D, [_D, _D, _D, _D]),
             "orc_sizeof": (_I64, [_I]),
+            "orc_set_grain": (None, [_P, _DP, _I64]),
+            "orc_gk_strain_rate": (_D, [_D, _D, _D, _D]),
+            "orc_creep_stress": (_I, [_D, _D, _D, _D, _D, _DP, _IP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -115,6 +118,10 @@ class OracleProblem:
         a = np.empty((self.NY, self.NX))
         assert lib().orc_get_nodal(self.h, NF[name], _dp(a)) == 0
         return a
+
+    def set_grain_size(self, d):
+        self._grain = np.ascontiguousarray(d, dtype=np.float64)
+        lib().orc_set_grain(self.h, _dp(self._grain), len(self._grain))
 
     def findMarkerCells(self):
         err = ctypes.c_int(0)
@@ -184,3 +191,23 @@ def gk_viscosity(s, T, d, P):
     f = lib().orc_gk_viscosity
     return np.array([f(float(a), float(b), float(c), float(e)) for a, b, c, e in
                      np.broadcast(np.asarray(s), np.asarray(T), np.asarray(d), np.asarray(P))])
+
+
+def gk_strain_rate(s, T, d, P):
+    """Strain rate of the reference law at stress s (viscosity.c:106-179, s / (2 eta))."""
+    f = lib().orc_gk_strain_rate
+    return np.array([f(float(a), float(b), float(c), float(e)) for a, b, c, e in
+                     np.broadcast(np.asarray(s), np.asarray(T), np.asarray(d), np.asarray(P))])
+
+
+def creep_stress(edot, T, d, P, rtol=1e-14):
+    """Stress at which the reference law's strain rate equals edot (oracle solve)."""
+    f = lib().orc_creep_stress
+    out, its = [], []
+    for a, b, c, e in np.broadcast(np.asarray(edot), np.asarray(T), np.asarray(d), np.asarray(P)):
+        sv = ctypes.c_double(0.0)
+        it = ctypes.c_int(0)
+        f(float(a), float(b), float(c), float(e), rtol, ctypes.byref(sv), ctypes.byref(it))
+        out.append(sv.value)
+        its.append(it.value)
+    return np.array(out), np.array(its)

@@ -1,0 +1,101 @@
+"""GPU checks of the composite ice creep closure (law 7): exact solve, training gradients,
+the trained surrogate with FP64 polish and exact fallback, and law 7 inside the marker pass."""
+import numpy as np
+import pytest
+
+from fvmic2d_gb300 import gpu, workloads as W
+from oracle import mlp_oracle as M
+from oracle import oraclepy
+from tests.helpers import close
+from tests.test_creep_oracle import creep_samples
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    wl = W.ice_creep_box(nx_cells=16, ny_cells=16, nm=2, seed=4)
+    G = gpu.MicProblem(wl)
+    G.set_grain_size(wl.grain_size)
+    return G, wl
+
+
+def test_exact_solve_matches_oracle_and_reference_law(ctx):
+    G, _ = ctx
+    edot, T, d, P = creep_samples(20000, 21)
+    edot = np.concatenate([edot, [1e-18, 1e-10, 3e-14, 3e-14, 3e-14, 3e-14, 1e-12, 0.0]])
+    T = np.concatenate([T, [100.0, 273.0, 254.999, 255.0, 257.999, 258.0, 200.0, 200.0]])
+    d = np.concatenate([d, [1e-4, 1e-1, 1e-3, 1e-3, 1e-3, 1e-3, 1e-2, 1e-3]])
+    P = np.concatenate([P, [0.0, 1e8, 5e7, 5e7, 5e7, 5e7, 0.3, 1e5]])
+    s, it, res, _ = G.creep_solve(edot, T, d, P, mode=0)
+    sub = slice(0, None, 7)  # the oracle solve is a Python loop: check every 7th sample
+    s_o, _ = oraclepy.creep_stress(edot[sub], T[sub], d[sub], P[sub])
+    ok, msg = close(s[sub], s_o, 1e-12)
+    assert ok, msg
+    pos = edot > 0
+    rate = oraclepy.gk_strain_rate(s[pos][::3], T[pos][::3], d[pos][::3], P[pos][::3])
+    rel = np.abs(rate / edot[pos][::3] - 1.0)
+    jump = s[pos][::3] == 1.0
+    assert np.all(rel[~jump] <= 1e-13), rel[~jump].max()
+    assert it.max() < 60 and s[-1] == 0.0
+
+
+def test_training_gradient_matches_fp64_oracle(ctx):
+    G, _ = ctx
+    rng = np.random.default_rng(9)
+    p = np.zeros(M.N_PARAMS, dtype=np.float32)
+    p[:M.N_TRAIN] = rng.normal(0, 0.3, M.N_TRAIN)
+    p[M.OFF_NORM], p[M.OFF_NORM + 1] = 5.0, 1.5
+    X = rng.uniform(-1, 1, (512, 4)).astype(np.float32)
+    t = rng.normal(5.0, 1.5, 512).astype(np.float32)
+    g, loss = G.creep_grad(p, X, t)
+    loss_o, g_o = M.loss_and_grad(p.astype(np.float64), X.astype(np.float64), t.astype(np.float64))
+    assert abs(loss - loss_o) <= 1e-4 * loss_o
+    assert np.linalg.norm(g - g_o) <= 1e-4 * np.linalg.norm(g_o)
+    # every parameter block individually
+    for a, b in [(M.OFF_W1, M.OFF_B1), (M.OFF_B1, M.OFF_W2), (M.OFF_W2, M.OFF_B2), (M.OFF_B2, M.OFF_W3),
+                 (M.OFF_W3, M.OFF_B3), (M.OFF_B3, M.OFF_NORM)]:
+        assert np.linalg.norm(g[a:b] - g_o[a:b]) <= 2e-4 * np.linalg.norm(g_o[a:b]) + 1e-7
+
+
+@pytest.fixture(scope="module")
+def trained(ctx):
+    G, _ = ctx
+    hist = G.creep_train(nsamples=1 << 20, batch=4096, steps=3000, lr=3e-3, seed=1)
+    return G, hist
+
+
+def test_training_converges(trained):
+    _, hist = trained
+    assert hist[-50:].mean() < 0.02 * hist[:50].mean()
+
+
+def test_surrogate_polish_meets_tolerance_and_saves_iterations(trained):
+    """What the trained network gains: the same stresses (<= 1e-6 relative to the exact
+    solve, checked here) from fewer FP64 Newton iterations."""
+    G, _ = trained
+    edot, T, d, P = creep_samples(200000, 77)
+    s_exact, it_exact, _, _ = G.creep_solve(edot, T, d, P, mode=0)
+    G.creep_configure(mode=0, polish_iters=2, polish_tol=1e-7)
+    s_sur, it_sur, res, fb = G.creep_solve(edot, T, d, P, mode=1)
+    rel = np.abs(s_sur / s_exact - 1.0)
+    assert rel.max() <= 1e-6, rel.max()
+    assert fb.mean() < 0.05, fb.mean()
+    assert it_sur.mean() < it_exact.mean(), (it_sur.mean(), it_exact.mean())
+
+
+def test_law7_marker_pass_matches_oracle():
+    wl = W.ice_creep_box(nx_cells=24, ny_cells=24, nm=3, seed=5)
+    G = gpu.MicProblem(wl)
+    G.set_grain_size(wl.grain_size)
+    O = oraclepy.OracleProblem(wl)
+    O.set_grain_size(wl.grain_size)
+    G.findMarkerCells()
+    O.findMarkerCells()
+    G.checkPlasticYielding(wl.dt)
+    O.checkPlasticYielding(wl.dt)
+    ok, msg = close(G.markers["eta"], O.markers["eta"], 1e-12)
+    assert ok, msg
+    st = G.creep_stats()
+    assert st["markers"] == len(wl.markers) and st["fallbacks"] == 0
+    assert st["max_residual"] <= 1e-13
