@@ -314,7 +314,7 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   }
   ctx->mat.nMaterials = 1;
   ctx->creep.mode = 0;
-  ctx->creep.polish_iters = 2;
+  ctx->creep.polish_iters = 3;
   ctx->creep.maxit = 60;
   ctx->creep.tol = 2e-14;
   ctx->creep.polish_tol = 1e-7;

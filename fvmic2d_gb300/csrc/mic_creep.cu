@@ -19,65 +19,21 @@ using namespace mic;
 
 namespace {
 
-// ---- network layout ------------------------------------------------------------------
-constexpr int kH = 64;
-constexpr int kOffW1 = 0;                // W1[64][4]
-constexpr int kOffB1 = kOffW1 + kH * 4;  // b1[64]
-constexpr int kOffW2 = kOffB1 + kH;      // W2[64][64], row = output neuron
-constexpr int kOffB2 = kOffW2 + kH * kH;
-constexpr int kOffW3 = kOffB2 + kH;      // w3[64]
-constexpr int kOffB3 = kOffW3 + kH;      // b3
-constexpr int kOffNorm = kOffB3 + 1;     // out_mu, out_sigma
-constexpr int kNParams = kOffNorm + 2;   // 4547
-constexpr int kNTrain = kOffNorm;        // trained parameters (normalisation excluded)
-
-// input normalisation over the composite-creep workload ranges
-__device__ __forceinline__ void creep_features(double edot, double T, double d, double P, float f[4]) {
-  f[0] = (float)((log10(edot) + 14.0) * 0.25);
-  f[1] = (float)((T - 186.5) / 86.5);
-  f[2] = (float)((log10(d) + 2.5) / 1.5);
-  f[3] = (float)(P * 2e-8 - 1.0);
-}
-
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
-__device__ __forceinline__ float dsilu(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
-  return s * (1.0f + z * (1.0f - s));
-}
-
-// FP32 forward pass on CUDA cores (reference path; W2 read from w2s, a shared-memory copy)
-__device__ __forceinline__ float mlp_forward(const float *__restrict__ p, const float *__restrict__ w2s,
-                                             const float f[4]) {
-  float h1[kH];
-#pragma unroll
-  for (int n = 0; n < kH; ++n) {
-    float z = p[kOffB1 + n];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) z = fmaf(p[kOffW1 + 4 * n + i], f[i], z);
-    h1[n] = silu(z);
-  }
-  float y = p[kOffB3];
-  for (int n = 0; n < kH; ++n) {
-    float z = p[kOffB2 + n];
-#pragma unroll 16
-    for (int k = 0; k < kH; ++k) z = fmaf(w2s[n * kH + k], h1[k], z);
-    y = fmaf(p[kOffW3 + n], silu(z), y);
-  }
-  return y;
-}
-
 // ---- exact batch solve and training pairs -----------------------------------------------
 
 __global__ void k_creep_exact_batch(const double *edot, const double *T, const double *d, const double *P, int64_t n,
-                                    CreepConfig cfg, double *s_out, int *it_out, double *res_out) {
+                                    CreepConfig cfg, double *s_out, int *it_out, double *res_out, CreepCounters *cc) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (m >= n) return;
-  const CreepCoef k = creep_coef(T[m], d[m], P[m]);
-  int it;
-  double res;
-  s_out[m] = creep_stress_exact(k, edot[m], cfg.tol, cfg.maxit, &it, &res);
-  if (it_out) it_out[m] = it;
-  if (res_out) res_out[m] = res;
+  int it = 0, active = 0;
+  double res = 0.0;
+  if (m < n) {
+    const CreepCoef k = creep_coef(T[m], d[m], P[m]);
+    s_out[m] = creep_stress_exact(k, edot[m], cfg.tol, cfg.maxit, &it, &res);
+    if (it_out) it_out[m] = it;
+    if (res_out) res_out[m] = res;
+    active = edot[m] > 0.0;
+  }
+  creep_count(cc, active, it, res, 0);
 }
 
 __device__ __forceinline__ double splitmix_u01(unsigned long long seed, unsigned long long i) {
@@ -89,7 +45,8 @@ __device__ __forceinline__ double splitmix_u01(unsigned long long seed, unsigned
 }
 
 // inputs drawn from the workload's distribution: log10 edot ~ U[-18,-10], T ~ U[100,273] K,
-// log10 d ~ U[-4,-1] m, P ~ U[0, 1e8] Pa; target = log10 of the exact stress
+// log10 d ~ U[-4,-1] m, P ~ U[0, 1e8] Pa; features of their coefficients, target = ln x* - m
+// from the exact root of the composite law
 __global__ void k_creep_samples(unsigned long long seed, int64_t n, CreepConfig cfg, float *feat, float *target) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
@@ -100,12 +57,12 @@ __global__ void k_creep_samples(unsigned long long seed, int64_t n, CreepConfig 
   const CreepCoef k = creep_coef(T, d, P);
   int it;
   double res;
-  const double s = creep_stress_exact(k, edot, cfg.tol, cfg.maxit, &it, &res);
+  const double u = creep_root_u(k, edot, cfg.tol, cfg.maxit, &it, &res);
   float f[4];
-  creep_features(edot, T, d, P, f);
+  const float mref = creep_features(k, edot, f);
 #pragma unroll
   for (int i = 0; i < 4; ++i) feat[4 * m + i] = f[i];
-  target[m] = (float)log10(s);
+  target[m] = (float)(u - kLn1e6 - (double)mref);
 }
 
 // ---- training: per-block forward/backward with deterministic partial gradients -------
@@ -257,43 +214,44 @@ __global__ void k_epoch_order(int *idx, int64_t n, unsigned long long a, unsigne
 __global__ void __launch_bounds__(128) k_creep_surrogate_batch_fp32(const double *edot, const double *T,
                                                                      const double *d, const double *P, int64_t n,
                                                                      CreepConfig cfg, double *s_out, int *it_out,
-                                                                     double *res_out, int *fb_out) {
+                                                                     double *res_out, int *fb_out,
+                                                                     CreepCounters *cc) {
   __shared__ float w2s[kH * kH];
   for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = cfg.mlp[kOffW2 + q];
   __syncthreads();
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (m >= n) return;
-  const double e = edot[m];
-  const CreepCoef k = creep_coef(T[m], d[m], P[m]);
-  int it = 0, fb = 0;
-  double res = 0.0, s;
-  if (!(e > 0.0)) {
-    s = 0.0;
-  } else if (e / k.C < 1.0) {
-    s = e / k.C;
-  } else {
-    float f[4];
-    creep_features(e, T[m], d[m], P[m], f);
-    const float y = mlp_forward(cfg.mlp, w2s, f);
-    double u = ((double)y * cfg.mlp[kOffNorm + 1] + cfg.mlp[kOffNorm]) * 2.302585092994046;
-    double ulo = -1e308, uhi = 1e308;
-    it = creep_newton(k, e, u, ulo, uhi, cfg.polish_tol, cfg.polish_iters, res);
-    if (!(fabs(res) <= cfg.polish_tol)) {
-      fb = 1;
-      int it2 = 0;
-      double r2;
-      s = creep_stress_exact(k, e, cfg.tol, cfg.maxit, &it2, &r2);
-      it += it2;
-      res = r2;
-    } else {
-      s = exp(u);
-      if (s < 1.0) s = 1.0;
+  int it = 0, fb = 0, active = 0;
+  double res = 0.0;
+  if (m < n) {
+    const double e = edot[m];
+    const CreepCoef k = creep_coef(T[m], d[m], P[m]);
+    double u0 = 0.0;
+    if (e > 0.0 && e / k.C >= 1.0) {  // the network is consulted on the non-linear branch only
+      float f[4];
+      const float mref = creep_features(k, e, f);
+      u0 = creep_guess_u(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
     }
+    s_out[m] = creep_stress_from_guess(k, e, u0, cfg.tol, cfg.maxit, cfg.polish_iters, cfg.polish_tol, &it, &res,
+                                       &fb);
+    if (it_out) it_out[m] = it;
+    if (res_out) res_out[m] = res;
+    if (fb_out) fb_out[m] = fb;
+    active = e > 0.0;
   }
-  s_out[m] = s;
-  if (it_out) it_out[m] = it;
-  if (res_out) res_out[m] = res;
-  if (fb_out) fb_out[m] = fb;
+  creep_count(cc, active, it, res, fb);
+}
+
+__global__ void __launch_bounds__(128) k_mlp_infer_fp32(const float *__restrict__ feat, int64_t n,
+                                                         const float *__restrict__ p, float *y_out) {
+  __shared__ float w2s[kH * kH];
+  for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = p[kOffW2 + q];
+  __syncthreads();
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  float f[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) f[i] = feat[4 * m + i];
+  y_out[m] = mlp_forward(p, w2s, f);
 }
 
 // He-style uniform initialisation from SplitMix64 (deterministic)
@@ -338,10 +296,10 @@ extern "C" int mic_creep_param_count(void) { return kNParams; }
 
 extern "C" int mic_creep_configure(mic_ctx *ctx, int mode, double tol, int maxit, int polish_iters,
                                    double polish_tol) {
-  if (!ctx || mode < 0 || mode > 1 || !(tol > 0.0) || maxit < 1 || maxit > 1000 || polish_iters < 0 ||
+  if (!ctx || mode < 0 || mode > 2 || !(tol > 0.0) || maxit < 1 || maxit > 1000 || polish_iters < 0 ||
       polish_iters > 50 || !(polish_tol > 0.0))
     return MIC_ERR_ARG;
-  if (mode == 1 && !ctx->mlp) return MIC_ERR_ARG;
+  if (mode >= 1 && !ctx->mlp) return MIC_ERR_ARG;
   ctx->creep.mode = mode;
   ctx->creep.tol = tol;
   ctx->creep.maxit = maxit;
@@ -357,7 +315,6 @@ extern "C" int mic_markers_set_grain_size(mic_ctx *ctx, const double *d, int64_t
   // grain sizes arrive in the caller's order; the columns are in device order: scatter by id
   double *tmp = ctx->scr0;
   MIC_CUDA_TRY(cudaMemcpyAsync(tmp, d, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-  extern int mic_gather_by_id(mic_ctx *, const double *, double *);
   int e = mic_gather_by_id(ctx, tmp, ctx->f64[C_GRAIN]);
   if (e) return e;
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -404,16 +361,16 @@ extern "C" int mic_creep_solve_batch(mic_ctx *ctx, const double *edot, const dou
   MIC_CUDA_TRY(cudaMemcpyAsync(dd, d, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   MIC_CUDA_TRY(cudaMemcpyAsync(dP, P, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   MIC_CUDA_TRY(cudaMemsetAsync(df, 0, sizeof(int) * n, ctx->stream));
+  MIC_CUDA_TRY(cudaMemsetAsync(ctx->d_creep, 0, sizeof(CreepCounters), ctx->stream));
   if (mode == 0) {
     MIC_KERNEL(ctx, "k_creep_exact_batch");
-    k_creep_exact_batch<<<grid_for(n), kBlock, 0, ctx->stream>>>(de, dT, dd, dP, n, ctx->creep, ds, di, dr);
+    k_creep_exact_batch<<<grid_for(n), kBlock, 0, ctx->stream>>>(de, dT, dd, dP, n, ctx->creep, ds, di, dr,
+                                                                 ctx->d_creep);
   } else if (mode == 1) {
     MIC_KERNEL(ctx, "k_creep_surrogate_batch_fp32");
     k_creep_surrogate_batch_fp32<<<grid_for(n, 128), 128, 0, ctx->stream>>>(de, dT, dd, dP, n, ctx->creep, ds, di,
-                                                                           dr, df);
+                                                                           dr, df, ctx->d_creep);
   } else {
-    extern int mic_creep_surrogate_tc_launch(mic_ctx *, const double *, const double *, const double *,
-                                             const double *, int64_t, double *, int *, double *, int *);
     e = mic_creep_surrogate_tc_launch(ctx, de, dT, dd, dP, n, ds, di, dr, df);
     if (e) return e;
   }
@@ -426,6 +383,29 @@ extern "C" int mic_creep_solve_batch(mic_ctx *ctx, const double *edot, const dou
   return MIC_OK;
 }
 
+// Network outputs y[n] for features feat[n][4] (host arrays) with the context's parameters:
+// mode 1 on the CUDA cores in FP32, mode 2 with the hidden layer on the tensor cores.
+extern "C" int mic_creep_mlp_infer(mic_ctx *ctx, const float *feat, int64_t n, int mode, float *y) {
+  if (!ctx || !feat || !y || n < 0 || mode < 1 || mode > 2 || !ctx->mlp) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (n == 0) return MIC_OK;
+  int e = ensure_train(ctx, 5 * n);
+  if (e) return e;
+  float *df = ctx->train_buf, *dy = df + 4 * n;
+  MIC_CUDA_TRY(cudaMemcpyAsync(df, feat, sizeof(float) * 4 * n, cudaMemcpyHostToDevice, ctx->stream));
+  MIC_CUDA_TRY(cudaMemsetAsync(ctx->d_creep, 0, sizeof(CreepCounters), ctx->stream));
+  if (mode == 1) {
+    MIC_KERNEL(ctx, "k_mlp_infer_fp32");
+    k_mlp_infer_fp32<<<grid_for(n, 128), 128, 0, ctx->stream>>>(df, n, ctx->mlp, dy);
+  } else if ((e = mic_mlp_infer_tc_launch(ctx, df, n, dy))) {
+    return e;
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  MIC_CUDA_TRY(cudaMemcpyAsync(y, dy, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
 // Gradient of the mean squared loss over n samples (n a multiple of 128) at the given
 // parameters, from the training kernels: grad[kNParams-2] (normalisation excluded), *loss.
 extern "C" int mic_creep_mlp_grad(mic_ctx *ctx, const float *params, const float *feat, const float *target,
@@ -433,7 +413,8 @@ extern "C" int mic_creep_mlp_grad(mic_ctx *ctx, const float *params, const float
   if (!ctx || !params || !feat || !target || !grad || n <= 0 || n % kTB) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   const int nblocks = n / kTB;
-  const int64_t need = (int64_t)kNParams + 5 * (int64_t)n + (int64_t)nblocks * kNTrain + nblocks + kNTrain + 8;
+  // params, features (4n), targets (n), sample order (n ints), partials, loss partials, gradient, loss
+  const int64_t need = (int64_t)kNParams + 6 * (int64_t)n + (int64_t)nblocks * kNTrain + nblocks + kNTrain + 8;
   int e = ensure_train(ctx, need);
   if (e) return e;
   float *p = ctx->train_buf, *fe = p + kNParams, *tg = fe + 4 * (int64_t)n;
@@ -481,7 +462,8 @@ extern "C" int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int st
   int e = ensure_mlp(ctx);
   if (e) return e;
   const int nblocks = batch / kTB;
-  const int64_t need = 5 * nsamples + (int64_t)nblocks * kNTrain + nblocks + 2 * (int64_t)kNTrain + steps + 16;
+  // features (4n), targets (n), sample order (n ints), partials, loss partials, Adam moments, losses
+  const int64_t need = 6 * nsamples + (int64_t)nblocks * kNTrain + nblocks + 2 * (int64_t)kNTrain + steps + 16;
   if ((e = ensure_train(ctx, need))) return e;
   float *fe = ctx->train_buf, *tg = fe + 4 * nsamples;
   int *ix = reinterpret_cast<int *>(tg + nsamples);
@@ -547,7 +529,7 @@ extern "C" int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int st
 
 // creep counters of the last rheology pass
 extern "C" int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iterations, int64_t *fallbacks,
-                               double *max_residual) {
+                               double *max_residual, int64_t *tc_timeouts) {
   if (!ctx) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   CreepCounters h;
@@ -557,5 +539,6 @@ extern "C" int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iteratio
   if (iterations) *iterations = (int64_t)h.iterations;
   if (fallbacks) *fallbacks = (int64_t)h.fallbacks;
   if (max_residual) memcpy(max_residual, &h.max_res_bits, sizeof(double));
+  if (tc_timeouts) *tc_timeouts = (int64_t)h.tc_timeouts;
   return MIC_OK;
 }

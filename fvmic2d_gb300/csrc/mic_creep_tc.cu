@@ -1,9 +1,98 @@
-// mic_creep_tc.cu -- tensor-core inference of the creep surrogate (placeholder until the
-// tcgen05 kernel lands): routes to an error so callers cannot silently run a CUDA-core path.
-#include "mic_internal.cuh"
+// mic_creep_tc.cu -- batch solve of the composite creep law with the surrogate guess from the
+// tensor cores (mic_creep_tc.cuh), FP64 Newton polish and exact fallback.
+//
+// Persistent blocks of 128 threads walk the batch in tiles of 128 samples; each block stages
+// the network once, holds 64 TMEM columns for its lifetime and frees them on exit.  At most
+// four blocks fit on an SM (about 51 KB of shared memory each), so the 512 TMEM columns of an
+// SM are never over-subscribed and an allocation never waits on another block.
+#include "mic_creep_tc.cuh"
 
-int mic_creep_surrogate_tc_launch(mic_ctx *ctx, const double *, const double *, const double *, const double *,
-                                  int64_t, double *, int *, double *, int *) {
-  (void)ctx;
-  return MIC_ERR_ARG;
+using namespace mic;
+
+namespace {
+
+__global__ void __launch_bounds__(tc::kTile) k_creep_surrogate_batch_tc(const double *__restrict__ edot,
+                                                                         const double *__restrict__ T,
+                                                                         const double *__restrict__ d,
+                                                                         const double *__restrict__ P, int64_t n,
+                                                                         CreepConfig cfg, double *s_out, int *it_out,
+                                                                         double *res_out, int *fb_out,
+                                                                         CreepCounters *cc) {
+  extern __shared__ unsigned char dyn[];
+  tc::Block B;
+  tc::setup(B, dyn, cfg.mlp);
+  const int64_t ntiles = (n + tc::kTile - 1) / tc::kTile;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t m = tile * tc::kTile + threadIdx.x;
+    const bool valid = m < n;
+    double e = 0.0;
+    float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
+    CreepCoef k = {1.0, 1.0, 1.0, 1.0};
+    if (valid) {
+      e = edot[m];
+      k = creep_coef(T[m], d[m], P[m]);
+      if (e > 0.0) mref = creep_features(k, e, f);
+    }
+    const float y = tc::guess(B, f, &cc->tc_timeouts);
+    int it = 0, fb = 0;
+    double res = 0.0;
+    if (valid) {
+      const double s = creep_stress_from_guess(k, e, creep_guess_u(cfg.mlp, y, mref), cfg.tol, cfg.maxit,
+                                               cfg.polish_iters, cfg.polish_tol, &it, &res, &fb);
+      s_out[m] = s;
+      if (it_out) it_out[m] = it;
+      if (res_out) res_out[m] = res;
+      if (fb_out) fb_out[m] = fb;
+    }
+    creep_count(cc, valid && e > 0.0, it, res, fb);
+  }
+  tc::teardown(B);
+}
+
+// network outputs for given features (n x 4, row-major) on the tensor-core path
+__global__ void __launch_bounds__(tc::kTile) k_mlp_infer_tc(const float *__restrict__ feat, int64_t n,
+                                                             const float *__restrict__ p, float *y_out,
+                                                             CreepCounters *cc) {
+  extern __shared__ unsigned char dyn[];
+  tc::Block B;
+  tc::setup(B, dyn, p);
+  const int64_t ntiles = (n + tc::kTile - 1) / tc::kTile;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t m = tile * tc::kTile + threadIdx.x;
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+    if (m < n)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) f[i] = feat[4 * m + i];
+    const float y = tc::guess(B, f, &cc->tc_timeouts);
+    if (m < n) y_out[m] = y;
+  }
+  tc::teardown(B);
+}
+
+}  // namespace
+
+int mic_mlp_infer_tc_launch(mic_ctx *ctx, const float *feat, int64_t n, float *y) {
+  MIC_CUDA_TRY(cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem));
+  MIC_KERNEL(ctx, "k_mlp_infer_tc");
+  k_mlp_infer_tc<<<mic_creep_tc_blocks(ctx, n), tc::kTile, tc::kDynSmem, ctx->stream>>>(feat, n, ctx->mlp, y,
+                                                                                         ctx->d_creep);
+  return MIC_OK;
+}
+
+int mic_creep_tc_blocks(mic_ctx *ctx, int64_t n) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  const int64_t tiles = (n + tc::kTile - 1) / tc::kTile;
+  const int64_t cap = 4 * (int64_t)(sms > 0 ? sms : 1);
+  return (int)(tiles < cap ? (tiles > 0 ? tiles : 1) : cap);
+}
+
+int mic_creep_surrogate_tc_launch(mic_ctx *ctx, const double *edot, const double *T, const double *d,
+                                  const double *P, int64_t n, double *s, int *it, double *res, int *fb) {
+  MIC_CUDA_TRY(cudaFuncSetAttribute(k_creep_surrogate_batch_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)tc::kDynSmem));
+  MIC_KERNEL(ctx, "k_creep_surrogate_batch_tc");
+  k_creep_surrogate_batch_tc<<<mic_creep_tc_blocks(ctx, n), tc::kTile, tc::kDynSmem, ctx->stream>>>(
+      edot, T, d, P, n, ctx->creep, s, it, res, fb, ctx->d_creep);
+  return MIC_OK;
 }

@@ -53,6 +53,7 @@ struct CreepConfig {
 struct CreepCounters {
   unsigned long long markers, iterations, fallbacks;
   unsigned long long max_res_bits;  // bits of the largest |rate/edot - 1| (non-negative double)
+  unsigned long long tc_timeouts;   // tensor-core tiles whose completion wait ran out
 };
 
 struct Params {  // everything a kernel needs besides the marker columns; passed by value
@@ -149,6 +150,15 @@ void mic_invalidate_sort(mic_ctx *ctx);
 int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out);
 int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry
 int mic_f64_column_of_offset(int byte_offset);
+// scatter a caller-order per-marker array into device (column) order through the id column
+int mic_gather_by_id(mic_ctx *ctx, const double *src, double *dst);
+// persistent block count of the tensor-core creep kernels for n markers (mic_creep_tc.cu)
+int mic_creep_tc_blocks(mic_ctx *ctx, int64_t n);
+// network outputs for device features (n x 4) on the tensor cores (mic_creep_tc.cu)
+int mic_mlp_infer_tc_launch(mic_ctx *ctx, const float *feat, int64_t n, float *y);
+// tensor-core creep surrogate over a device batch (mic_creep_tc.cu)
+int mic_creep_surrogate_tc_launch(mic_ctx *ctx, const double *edot, const double *T, const double *d,
+                                  const double *P, int64_t n, double *s, int *it, double *res, int *fb);
 
 namespace mic {
 

@@ -10,6 +10,7 @@
 #include <cstring>
 
 #include "mic_creep.cuh"
+#include "mic_creep_tc.cuh"
 #include "mic_internal.cuh"
 
 using namespace mic;
@@ -56,22 +57,29 @@ __device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, i
   mdy = (j == sy) ? gy1 : div_sp(y - P.yc[j], P.hyc[j], P.iyc[j]);
 }
 
-// Inputs of the composite creep law (law 7): the marker's strain-rate invariant, grain size
-// and pressure; iteration count and residual of its stress solve come back in it.
+// Inputs of the composite creep law (law 7): the marker's strain-rate invariant, grain size,
+// pressure and (surrogate modes) the network's ln s* guess; iteration count, residual and
+// fallback flag of its stress solve come back in it.
 struct CreepIn {
   double e11, e22, e12, grain, p;
-  int iters;
+  double u_guess;
+  int iters, fb;
   double res;
+  int have_k;    // coefficients below already evaluated for this marker
+  CreepCoef k;
 };
 
 // Law 7 (new): composite ice creep, eta = s* / (2 edot_II) with s* the stress at which the
 // Goldsby-Kohlstedt strain rate (viscosity.c:106-179) equals the marker's strain-rate
 // invariant; at zero strain rate the law's diffusion viscosity 0.5 / C (viscosity.c:130-133).
-__device__ __forceinline__ double creep_viscosity_exact(const CreepConfig &cfg, double T, CreepIn &ci) {
+__device__ __forceinline__ double creep_viscosity(const CreepConfig &cfg, double T, CreepIn &ci) {
   const double edot = sqrt(0.5 * (ci.e11 * ci.e11 + ci.e22 * ci.e22) + ci.e12 * ci.e12);
-  const CreepCoef k = creep_coef(T, ci.grain, ci.p);
+  const CreepCoef k = ci.have_k ? ci.k : creep_coef(T, ci.grain, ci.p);
   if (!(edot > 0.0)) return 0.5 / k.C;
-  const double s = creep_stress_exact(k, edot, cfg.tol, cfg.maxit, &ci.iters, &ci.res);
+  const double s = (cfg.mode == 0) ? creep_stress_exact(k, edot, cfg.tol, cfg.maxit, &ci.iters, &ci.res)
+                                   : creep_stress_from_guess(k, edot, ci.u_guess, cfg.tol, cfg.maxit,
+                                                             cfg.polish_iters, cfg.polish_tol, &ci.iters, &ci.res,
+                                                             &ci.fb);
   return s / (2.0 * edot);
 }
 
@@ -83,7 +91,7 @@ __device__ __forceinline__ bool rheology(const mic_materials &M, const mic_optio
   switch (M.hasEtaT[k]) {
     case 7:
       if (!cfg || !ci) return false;
-      eta = creep_viscosity_exact(*cfg, T, *ci);
+      eta = creep_viscosity(*cfg, T, *ci);
       return true;
     case 1: eta = M.materialEta[k] * exp(M.QonR[k] * (1.0 / T - 1.0 / M.Tref[k])); return true;
     case 2: {
@@ -112,111 +120,154 @@ struct YieldCols {
   double *eta, *mu, *sxx, *syy, *sxy;
 };
 
-// per-warp reduction of the creep counters into the device totals
-__device__ __forceinline__ void creep_count(CreepCounters *cc, int active, int iters, double res, int fallback) {
-  const unsigned full = 0xffffffffu;
-  int a = active, it = iters, fb = fallback;
-  long long rb = active ? nonneg_bits(fabs(res)) : 0;
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(full, a, o);
-    it += __shfl_down_sync(full, it, o);
-    fb += __shfl_down_sync(full, fb, o);
-    rb = max(rb, __shfl_down_sync(full, rb, o));
+// One marker of checkPlasticYielding (markers.c:1381-1505).  u_guess: the surrogate's ln s*
+// guess for a law-7 marker (surrogate modes).  Returns whether the marker yielded.
+__device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_materials &M, const mic_options &O,
+                                             const CreepConfig &cfg, double dt, int64_t m, double u_guess,
+                                             const CreepCoef *kc, Status *st, CreepIn &ci, int &creep_active) {
+  bool yielded = false;
+  const double eta_old = c.eta[m], mu_old = c.mu[m];
+  double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
+  // visco-elastic forecast with the old viscosity and modulus (markers.c:1397-1402)
+  const double Xf = eta_old / (mu_old * dt + eta_old);
+  const double fxx = s11 * Xf + 2 * eta_old * e11 * (1.0 - Xf);
+  const double fyy = s22 * Xf + 2 * eta_old * e22 * (1.0 - Xf);
+  const double fxy = s12 * Xf + 2 * eta_old * e12 * (1.0 - Xf);
+  const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
+  const int k = c.mat[m];
+  double eta, mu;
+  ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], u_guess, 0, 0, 0.0, kc != nullptr, {}};
+  if (kc) ci.k = *kc;
+  if (!rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)) {
+    eta = eta_old;
+    mu = mu_old;
+    atomicAdd(&st->bad_law, 1ULL);
   }
-  if ((threadIdx.x & 31) == 0 && a) {
-    atomicAdd(&cc->markers, (unsigned long long)a);
-    atomicAdd(&cc->iterations, (unsigned long long)it);
-    if (fb) atomicAdd(&cc->fallbacks, (unsigned long long)fb);
-    atomicMax(&cc->max_res_bits, (unsigned long long)rb);
+  creep_active = M.hasEtaT[k] == 7;
+  const int plast = M.hasPlasticity[k];
+  if (plast) {
+    double sy;
+    if (plast == 1) {
+      sy = M.materialCohesion[k] + M.materialFriction[k] * c.p[m];
+    } else if (plast == 2) {  // strain weakening (markers.c:1426-1448)
+      const double E = c.Eii[m];
+      double coh, fr;
+      if (E < M.gamma[k][0]) {
+        coh = M.C[k][0];
+        fr = sin(M.F[k][0] / 180.0 * M_PI);
+      } else if (E >= M.gamma[k][0] && E <= M.gamma[k][1]) {
+        const double dg = (E - M.gamma[k][0]) / (M.gamma[k][1] - M.gamma[k][0]);
+        coh = (M.C[k][1] - M.C[k][0]) * dg + M.C[k][0];
+        fr = (sin(M.F[k][1] / 180.0 * M_PI) - sin(M.F[k][0] / 180.0 * M_PI)) * dg + sin(M.F[k][0] / 180.0 * M_PI);
+      } else {
+        coh = M.C[k][1];
+        fr = sin(M.F[k][1] / 180.0 * M_PI);
+      }
+      sy = coh + fr * c.p[m];
+    } else {
+      sy = 0.0;
+    }
+    if (sy < 0.0) sy = 0.0;
+    double etanew = eta_old;  // plastic materials keep the old viscosity unless they yield
+    if (sii > sy) {
+      const double eii = sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+      etanew = sy / 2.0 / eii;
+      if (etanew / eta < O.fractionalEtamin) etanew = O.fractionalEtamin * eta;
+      if (etanew < O.etamin)
+        etanew = O.etamin;
+      else if (etanew > O.etamax)
+        etanew = O.etamax;
+      const double sio = sqrt(0.5 * (s11 * s11 + s22 * s22) + s12 * s12);
+      if (sio != 0.0) {
+        s11 *= sy / sio;
+        s22 *= sy / sio;
+        s12 *= sy / sio;
+        c.sxx[m] = s11;
+        c.syy[m] = s22;
+        c.sxy[m] = s12;
+      }
+      yielded = true;
+    }
+    eta = etanew;
   }
+  c.eta[m] = eta;
+  c.mu[m] = mu;
+  return yielded;
 }
 
-// checkPlasticYielding (markers.c:1381-1505)
+// coefficients and surrogate features of marker m when it follows law 7 with a positive strain
+// rate (false otherwise); *mref receives the features' reference
+__device__ __forceinline__ bool creep_marker_features(const YieldCols &c, const mic_materials &M, int64_t m,
+                                                      CreepCoef &k, float f[4], float *mref) {
+  if (M.hasEtaT[c.mat[m]] != 7) return false;
+  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
+  const double edot = sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+  k = creep_coef(c.T[m], c.grain[m], c.p[m]);
+  if (!(edot > 0.0)) {
+    *mref = 0.f;
+    f[0] = f[1] = f[2] = f[3] = 0.f;
+    return true;
+  }
+  *mref = creep_features(k, edot, f);
+  return true;
+}
+
+// checkPlasticYielding, one thread per marker.  MODE 0: exact creep solve; MODE 1: surrogate
+// guess on the CUDA cores (FP32), polish and fallback.
+template <int MODE>
 __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig cfg, double dt, int64_t n,
                         Status *st, CreepCounters *cc) {
-  __shared__ int s_yield, s_bad;
-  if (threadIdx.x == 0) s_yield = s_bad = 0;
+  __shared__ int s_yield;
+  __shared__ float w2s[MODE == 1 ? kH * kH : 1];
+  if (threadIdx.x == 0) s_yield = 0;
+  if (MODE == 1)
+    for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = cfg.mlp[kOffW2 + q];
   __syncthreads();
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int creep_active = 0, creep_iters = 0;
-  double creep_res = 0.0;
+  int creep_active = 0;
+  CreepIn ci = {};
   if (m < n && c.cellX[m] != -1) {
-    const double eta_old = c.eta[m], mu_old = c.mu[m];
-    double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
-    const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
-    // visco-elastic forecast with the old viscosity and modulus (markers.c:1397-1402)
-    const double Xf = eta_old / (mu_old * dt + eta_old);
-    const double fxx = s11 * Xf + 2 * eta_old * e11 * (1.0 - Xf);
-    const double fyy = s22 * Xf + 2 * eta_old * e22 * (1.0 - Xf);
-    const double fxy = s12 * Xf + 2 * eta_old * e12 * (1.0 - Xf);
-    const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
-    const int k = c.mat[m];
-    double eta, mu;
-    CreepIn ci = {e11, e22, e12, c.grain[m], c.p[m], 0, 0.0};
-    if (!rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)) {
-      eta = eta_old;
-      mu = mu_old;
-      s_bad = 1;
-      atomicAdd(&st->bad_law, 1ULL);
-    }
-    if (M.hasEtaT[k] == 7) {
-      creep_active = 1;
-      creep_iters = ci.iters;
-      creep_res = ci.res;
-    }
-    const int plast = M.hasPlasticity[k];
-    if (plast) {
-      double sy;
-      if (plast == 1) {
-        sy = M.materialCohesion[k] + M.materialFriction[k] * c.p[m];
-      } else if (plast == 2) {  // strain weakening (markers.c:1426-1448)
-        const double E = c.Eii[m];
-        double coh, fr;
-        if (E < M.gamma[k][0]) {
-          coh = M.C[k][0];
-          fr = sin(M.F[k][0] / 180.0 * M_PI);
-        } else if (E >= M.gamma[k][0] && E <= M.gamma[k][1]) {
-          const double dg = (E - M.gamma[k][0]) / (M.gamma[k][1] - M.gamma[k][0]);
-          coh = (M.C[k][1] - M.C[k][0]) * dg + M.C[k][0];
-          fr = (sin(M.F[k][1] / 180.0 * M_PI) - sin(M.F[k][0] / 180.0 * M_PI)) * dg + sin(M.F[k][0] / 180.0 * M_PI);
-        } else {
-          coh = M.C[k][1];
-          fr = sin(M.F[k][1] / 180.0 * M_PI);
-        }
-        sy = coh + fr * c.p[m];
-      } else {
-        sy = 0.0;
-      }
-      if (sy < 0.0) sy = 0.0;
-      double etanew = eta_old;  // plastic materials keep the old viscosity unless they yield
-      if (sii > sy) {
-        const double eii = sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
-        etanew = sy / 2.0 / eii;
-        if (etanew / eta < O.fractionalEtamin) etanew = O.fractionalEtamin * eta;
-        if (etanew < O.etamin)
-          etanew = O.etamin;
-        else if (etanew > O.etamax)
-          etanew = O.etamax;
-        const double sio = sqrt(0.5 * (s11 * s11 + s22 * s22) + s12 * s12);
-        if (sio != 0.0) {
-          s11 *= sy / sio;
-          s22 *= sy / sio;
-          s12 *= sy / sio;
-          c.sxx[m] = s11;
-          c.syy[m] = s22;
-          c.sxy[m] = s12;
-        }
-        s_yield = 1;
-      }
-      eta = etanew;
-    }
-    c.eta[m] = eta;
-    c.mu[m] = mu;
+    double u = 0.0;
+    float f[4], mref;
+    CreepCoef k;
+    const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, f, &mref);
+    if (law7) u = creep_guess_u(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
+    if (yield_marker(c, M, O, cfg, dt, m, u, law7 ? &k : nullptr, st, ci, creep_active)) s_yield = 1;
   }
-  creep_count(cc, creep_active, creep_iters, creep_res, 0);
+  creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   __syncthreads();
   if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
-  (void)s_bad;
+}
+
+// checkPlasticYielding with the surrogate's hidden layer on the tensor cores: persistent
+// blocks of 128 threads, one 128-marker tile per round (mic_creep_tc.cuh).
+__global__ void __launch_bounds__(tc::kTile) k_yield_tc(YieldCols c, mic_materials M, mic_options O,
+                                                        CreepConfig cfg, double dt, int64_t n, Status *st,
+                                                        CreepCounters *cc) {
+  extern __shared__ unsigned char dyn[];
+  __shared__ int s_yield;
+  if (threadIdx.x == 0) s_yield = 0;
+  tc::Block B;
+  tc::setup(B, dyn, cfg.mlp);
+  const int64_t ntiles = (n + tc::kTile - 1) / tc::kTile;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t m = tile * tc::kTile + threadIdx.x;
+    const bool live = m < n && c.cellX[m] != -1;
+    float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
+    CreepCoef k;
+    const bool law7 = live && creep_marker_features(c, M, m, k, f, &mref);
+    const float y = tc::guess(B, f, &cc->tc_timeouts);
+    int creep_active = 0;
+    CreepIn ci = {};
+    if (live && yield_marker(c, M, O, cfg, dt, m, creep_guess_u(cfg.mlp, y, mref), law7 ? &k : nullptr, st, ci,
+                             creep_active))
+      s_yield = 1;
+    creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
+  }
+  tc::teardown(B);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
 }
 
 // updateViscosity (viscosity.c:77-88): rheology from the current marker stress
@@ -225,8 +276,10 @@ __global__ void k_update_viscosity(YieldCols c, mic_materials M, mic_options O, 
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n || c.cellX[m] == -1) return;
   double eta, mu;
-  CreepIn ci = {c.exx[m], c.eyy[m], c.exy[m], c.grain[m], c.p[m], 0, 0.0};
-  if (!rheology(M, O, c.mat[m], c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)) {
+  CreepIn ci = {c.exx[m], c.eyy[m], c.exy[m], c.grain[m], c.p[m], 0.0, 0, 0, 0.0, 0, {}};
+  CreepConfig exact = cfg;  // no surrogate guess on this pass: exact solve
+  exact.mode = 0;
+  if (!rheology(M, O, c.mat[m], c.T[m], c.X[m], c.Y[m], eta, mu, &exact, &ci)) {
     atomicAdd(&st->bad_law, 1ULL);
     return;
   }
@@ -810,10 +863,21 @@ static int yield_launch(mic_ctx *ctx, double dt) {
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->bad_law, 0, sizeof(unsigned long long), ctx->stream));
   MIC_CUDA_TRY(cudaMemsetAsync(ctx->d_creep, 0, sizeof(CreepCounters), ctx->stream));
   if (ctx->n > 0) {
-    {
+    const int mode = ctx->creep.mlp ? ctx->creep.mode : 0;
+    if (mode == 0) {
       MIC_KERNEL(ctx, "k_yield");
-      k_yield<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep, dt,
-                                                            ctx->n, ctx->d_status, ctx->d_creep);
+      k_yield<0><<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
+                                                               dt, ctx->n, ctx->d_status, ctx->d_creep);
+    } else if (mode == 1) {
+      MIC_KERNEL(ctx, "k_yield_surrogate_fp32");
+      k_yield<1><<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
+                                                                 dt, ctx->n, ctx->d_status, ctx->d_creep);
+    } else {
+      MIC_CUDA_TRY(cudaFuncSetAttribute(k_yield_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)tc::kDynSmem));
+      MIC_KERNEL(ctx, "k_yield_tc");
+      k_yield_tc<<<mic_creep_tc_blocks(ctx, ctx->n), tc::kTile, tc::kDynSmem, ctx->stream>>>(
+          yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep, dt, ctx->n, ctx->d_status, ctx->d_creep);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }

@@ -75,7 +75,8 @@ SIGNATURES = {
     "mic_creep_train": (_I, [_P, _I64, _I, _I, ctypes.c_float, ctypes.c_uint64, _P]),
     "mic_creep_mlp_grad": (_I, [_P, _P, _P, _P, _I, _P, _P]),
     "mic_creep_solve_batch": (_I, [_P, _DP, _DP, _DP, _DP, _I64, _I, _DP, _P, _DP, _P]),
-    "mic_creep_stats": (_I, [_P, _I64P, _I64P, _I64P, _DP]),
+    "mic_creep_mlp_infer": (_I, [_P, _P, _I64, _I, _P]),
+    "mic_creep_stats": (_I, [_P, _I64P, _I64P, _I64P, _DP, _I64P]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -228,11 +229,11 @@ class MicProblem:
         d = np.ascontiguousarray(d, dtype=np.float64)
         self._check(self.L.mic_markers_set_grain_size(self.h, _dp(d), len(d)), "mic_markers_set_grain_size")
 
-    def creep_configure(self, mode=0, tol=2e-14, maxit=60, polish_iters=2, polish_tol=1e-7):
+    def creep_configure(self, mode=0, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7):
         self._check(self.L.mic_creep_configure(self.h, mode, tol, maxit, polish_iters, polish_tol),
                     "mic_creep_configure")
 
-    def creep_train(self, nsamples=1 << 20, batch=4096, steps=2000, lr=3e-3, seed=1):
+    def creep_train(self, nsamples=1 << 21, batch=4096, steps=10000, lr=3e-3, seed=1):
         hist = np.zeros(steps, dtype=np.float32)
         self._check(self.L.mic_creep_train(self.h, nsamples, batch, steps, lr, seed, hist.ctypes.data),
                     "mic_creep_train")
@@ -269,12 +270,21 @@ class MicProblem:
                                                  _dp(res), fb.ctypes.data), "mic_creep_solve_batch")
         return s, it, res, fb
 
+    def creep_infer(self, feat, mode):
+        """Network outputs for normalised features (n x 4): mode 1 FP32 CUDA cores, 2 tensor cores."""
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        y = np.zeros(len(feat), dtype=np.float32)
+        self._check(self.L.mic_creep_mlp_infer(self.h, feat.ctypes.data, len(feat), mode, y.ctypes.data),
+                    "mic_creep_mlp_infer")
+        return y
+
     def creep_stats(self):
-        a, b, c = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        a, b, c, t = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
         r = ctypes.c_double(0.0)
         self._check(self.L.mic_creep_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
-                                           ctypes.byref(r)), "mic_creep_stats")
-        return {"markers": a.value, "iterations": b.value, "fallbacks": c.value, "max_residual": r.value}
+                                           ctypes.byref(r), ctypes.byref(t)), "mic_creep_stats")
+        return {"markers": a.value, "iterations": b.value, "fallbacks": c.value, "max_residual": r.value,
+                "tc_timeouts": t.value}
 
     def synchronize(self):
         self._check(self.L.mic_synchronize(self.h), "mic_synchronize")

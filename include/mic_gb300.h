@@ -136,10 +136,11 @@ int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress
  * 106-179, stress -> strain rate).  Law 7 inverts it per marker: the viscosity is s* / (2 edot_II)
  * where s* is the stress at which the law's strain rate equals the marker's strain-rate
  * invariant (grain size from mic_markers_set_grain_size, pressure and temperature from the
- * marker).  mode 0 solves exactly (FP64 Newton to |rate/edot - 1| <= tol); mode 1 starts from
- * the trained surrogate (4 -> 64 -> 64 -> 1 MLP, hidden layer on the tensor cores in BF16 with
- * FP32 accumulation), takes polish_iters FP64 Newton steps and finishes with the exact solve for
- * markers still above polish_tol. */
+ * marker).  mode 0 solves exactly (FP64 Newton to |rate/edot - 1| <= tol); modes 1 and 2 start
+ * from the trained surrogate (4 -> 64 -> 64 -> 1 MLP; mode 1 on the CUDA cores in FP32, mode 2
+ * with the hidden layer on the tensor cores in split BF16 with FP32 accumulation), take up to
+ * polish_iters FP64 Newton steps and finish with the exact solve for markers still above
+ * polish_tol.  With polish_tol = tol the surrogate modes converge to the same root as mode 0. */
 int mic_creep_configure(mic_ctx *ctx, int mode, double tol, int maxit, int polish_iters, double polish_tol);
 int mic_markers_set_grain_size(mic_ctx *ctx, const double *grain_size, int64_t n); /* caller order */
 int mic_creep_param_count(void);
@@ -156,8 +157,14 @@ int mic_creep_mlp_grad(mic_ctx *ctx, const float *params, const float *features,
 int mic_creep_solve_batch(mic_ctx *ctx, const double *edot, const double *T, const double *d, const double *P,
                           int64_t n, int mode, double *stress, int32_t *iterations, double *residual,
                           int32_t *fallback);
-/* counters of the last checkPlasticYielding pass over law-7 markers */
-int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iterations, int64_t *fallbacks, double *max_residual);
+/* surrogate network outputs y[n] for normalised features feat[n][4] (host arrays) with the
+ * context's parameters: mode 1 FP32 on the CUDA cores, mode 2 hidden layer on the tensor cores */
+int mic_creep_mlp_infer(mic_ctx *ctx, const float *feat, int64_t n, int mode, float *y);
+/* counters of the last law-7 pass (checkPlasticYielding or a batch solve): markers solved, Newton
+ * iterations, exact fallbacks, largest final |rate/edot - 1|, tensor-core tiles whose completion
+ * wait ran out (their markers took the exact solve) */
+int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iterations, int64_t *fallbacks, double *max_residual,
+                    int64_t *tc_timeouts);
 
 /* ---- plumbing ---- */
 int mic_synchronize(mic_ctx *ctx);

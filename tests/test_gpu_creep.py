@@ -58,10 +58,41 @@ def test_training_gradient_matches_fp64_oracle(ctx):
         assert np.linalg.norm(g[a:b] - g_o[a:b]) <= 2e-4 * np.linalg.norm(g_o[a:b]) + 1e-7
 
 
+def _random_params(seed):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(M.N_PARAMS, dtype=np.float32)
+    p[M.OFF_W1:M.OFF_B1] = rng.uniform(-1.2, 1.2, M.OFF_B1 - M.OFF_W1)
+    p[M.OFF_B1:M.OFF_W2] = rng.uniform(-0.5, 0.5, M.H)
+    p[M.OFF_W2:M.OFF_B2] = rng.uniform(-0.3, 0.3, M.H * M.H)
+    p[M.OFF_B2:M.OFF_W3] = rng.uniform(-0.5, 0.5, M.H)
+    p[M.OFF_W3:M.OFF_B3] = rng.uniform(-0.3, 0.3, M.H)
+    p[M.OFF_B3], p[M.OFF_NORM], p[M.OFF_NORM + 1] = 0.1, 5.0, 1.5
+    return p
+
+
+@pytest.mark.parametrize("n", [1, 127, 1000, 128 * 4 * 152 * 2 + 7])
+def test_tensor_core_network_matches_fp64_forward(ctx, n):
+    """The tcgen05 path (split-BF16 hidden layer, FP32 accumulation in tensor memory) against the
+    FP64 NumPy forward pass and the FP32 CUDA-core path; ragged tile counts and more tiles than
+    persistent blocks."""
+    G, _ = ctx
+    p = _random_params(n)
+    G.creep_set_params(p)
+    X = np.random.default_rng(n + 1).uniform(-1, 1, (n, 4)).astype(np.float32)
+    y64, (_, h1, z2, h2) = M.forward(p.astype(np.float64), X.astype(np.float64))
+    # error scale: magnitude of the terms summed in the hidden and output layers
+    scale = 1.0 + np.abs(h2) @ np.abs(p[M.OFF_W3:M.OFF_B3].astype(np.float64))
+    y1 = G.creep_infer(X, mode=1)
+    y2 = G.creep_infer(X, mode=2)
+    assert G.creep_stats()["tc_timeouts"] == 0
+    assert np.all(np.abs(y1 - y64) <= 2e-6 * scale), np.abs(y1 - y64).max()
+    assert np.all(np.abs(y2 - y64) <= 2e-5 * scale), np.abs(y2 - y64).max()
+
+
 @pytest.fixture(scope="module")
 def trained(ctx):
     G, _ = ctx
-    hist = G.creep_train(nsamples=1 << 20, batch=4096, steps=3000, lr=3e-3, seed=1)
+    hist = G.creep_train(nsamples=1 << 21, batch=4096, steps=10000, lr=3e-3, seed=1)
     return G, hist
 
 
@@ -71,23 +102,47 @@ def test_training_converges(trained):
 
 
 def test_surrogate_polish_meets_tolerance_and_saves_iterations(trained):
-    """What the trained network gains: the same stresses (<= 1e-6 relative to the exact
-    solve, checked here) from fewer FP64 Newton iterations."""
+    """What the trained network gains: stresses within 1e-6 of the exact solve (the polish
+    tolerance 1e-7 on the rate residual) from under 60% of its FP64 Newton iterations, with
+    almost no exact fallbacks, on both inference paths."""
     G, _ = trained
     edot, T, d, P = creep_samples(200000, 77)
+    G.creep_configure(mode=0, tol=2e-14, polish_iters=3, polish_tol=1e-7)
     s_exact, it_exact, _, _ = G.creep_solve(edot, T, d, P, mode=0)
-    G.creep_configure(mode=0, polish_iters=2, polish_tol=1e-7)
-    s_sur, it_sur, res, fb = G.creep_solve(edot, T, d, P, mode=1)
-    rel = np.abs(s_sur / s_exact - 1.0)
-    assert rel.max() <= 1e-6, rel.max()
-    assert fb.mean() < 0.05, fb.mean()
-    assert it_sur.mean() < it_exact.mean(), (it_sur.mean(), it_exact.mean())
+    for mode in (1, 2):
+        s_sur, it_sur, res, fb = G.creep_solve(edot, T, d, P, mode=mode)
+        rel = np.abs(s_sur / s_exact - 1.0)
+        assert rel.max() <= 1e-6, (mode, rel.max())
+        assert fb.mean() < 0.01, (mode, fb.mean())
+        assert it_sur.mean() < 0.6 * it_exact.mean(), (mode, it_sur.mean(), it_exact.mean())
+        assert np.all(np.abs(res) <= 1e-7)
 
 
-def test_law7_marker_pass_matches_oracle():
+def test_surrogate_modes_converge_to_the_exact_root(trained):
+    """With the polish tolerance at the exact tolerance, both surrogate paths return the exact
+    solve's stress (<= 1e-12 relative) from fewer FP64 Newton iterations."""
+    G, _ = trained
+    edot, T, d, P = creep_samples(300001, 78)
+    G.creep_configure(mode=0, tol=2e-14, polish_iters=6, polish_tol=2e-14)
+    s0, it0, _, _ = G.creep_solve(edot, T, d, P, mode=0)
+    for mode in (1, 2):
+        s, it, res, fb = G.creep_solve(edot, T, d, P, mode=mode)
+        ok, msg = close(s, s0, 1e-12)
+        assert ok, (mode, msg)
+        st = G.creep_stats()
+        assert st["tc_timeouts"] == 0 and st["max_residual"] <= 2e-14
+        assert fb.mean() < 0.01, (mode, fb.mean())
+        assert it.mean() < 0.8 * it0.mean(), (mode, it.mean(), it0.mean())
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_law7_marker_pass_matches_oracle(trained, mode):
     wl = W.ice_creep_box(nx_cells=24, ny_cells=24, nm=3, seed=5)
     G = gpu.MicProblem(wl)
     G.set_grain_size(wl.grain_size)
+    if mode:
+        G.creep_set_params(trained[0].creep_params())
+    G.creep_configure(mode=mode, tol=2e-14, polish_iters=6, polish_tol=2e-14)
     O = oraclepy.OracleProblem(wl)
     O.set_grain_size(wl.grain_size)
     G.findMarkerCells()
@@ -97,5 +152,6 @@ def test_law7_marker_pass_matches_oracle():
     ok, msg = close(G.markers["eta"], O.markers["eta"], 1e-12)
     assert ok, msg
     st = G.creep_stats()
-    assert st["markers"] == len(wl.markers) and st["fallbacks"] == 0
-    assert st["max_residual"] <= 1e-13
+    assert st["markers"] == len(wl.markers) and st["tc_timeouts"] == 0
+    assert st["fallbacks"] <= 0.01 * len(wl.markers)
+    assert st["max_residual"] <= 2e-14
