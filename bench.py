@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="vep_slab_box")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the composite-creep surrogate leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-cores", type=int, default=0, help="host processes for the CPU legs (0 = all)")
     return ap.parse_args()
@@ -388,11 +389,74 @@ def run_ours(args):
                           "frac": step_gbs / hbm_peak},
         "kernel_share": {k: round(v[0] / prof_total, 4) for k, v in kern[:12]},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kern[:12]},
-        "surrogate": None,
+        "surrogate": surrogate_leg(args, local) if not args.no_surrogate else None,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+
+
+def surrogate_leg(args, local):
+    """The composite ice creep workload (law 7) stepped with the exact creep solve and with the
+    trained surrogate (CUDA-core and tensor-core inference), plus the surrogate's stress error
+    against the exact solve on a sample of the same input distribution."""
+    import numpy as np
+    import torch
+
+    from fvmic2d_gb300 import gpu
+    from fvmic2d_gb300 import workloads as W
+
+    wl = W.ice_creep_box()
+    G = gpu.MicProblem(wl, device=local)
+    G.set_grain_size(wl.grain_size)
+    L, h = G.L, G.h
+    stream = torch.cuda.ExternalStream(G.stream(), device=local)
+    n = len(wl.markers)
+    t0 = time.perf_counter()
+    hist = G.creep_train()
+    train_s = time.perf_counter() - t0
+    steps = max(3, min(args.steps, 20))
+    out = {"workload": "ice_creep_box: 1025x1025 uniform nodes, 16 markers/cell (%d markers), composite ice "
+                       "creep (law 7) with per-marker log10 edot ~ U[-18,-10], T ~ U[100,273] K, log10 d ~ "
+                       "U[-4,-1] m, P ~ U[0,1e8] Pa; markers larger than L2" % n,
+           "steps": steps, "train_seconds": round(train_s, 3), "train_loss_final": float(hist[-200:].mean()),
+           "polish": {"iters": 3, "tol": 1e-7}}
+    for label, mode in (("plain", 0), ("surrogate_fp32", 1), ("surrogate_tc", 2)):
+        G.creep_configure(mode=mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
+        for _ in range(3):
+            assert L.mic_step(h, wl.dt, wl.dt_thermal, 1, None) == 0
+        G.synchronize()
+        G.profile_enable(64 * steps)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            assert L.mic_step(h, wl.dt, wl.dt_thermal, 1, None) == 0
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        prof = G.profile_read()
+        G.profile_enable(0)
+        st = G.creep_stats()
+        yk = [k for k in prof if k.startswith("k_yield")]
+        out[label] = {"value": n / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
+                      "yield_kernel": yk[0] if yk else None,
+                      "yield_ms_per_step": prof[yk[0]][0] / steps if yk else None,
+                      "newton_iters_per_marker": st["iterations"] / max(st["markers"], 1),
+                      "fallbacks_per_step": st["fallbacks"], "tc_timeouts": st["tc_timeouts"],
+                      "max_residual": st["max_residual"]}
+    out["speedup_tc_vs_plain"] = out["surrogate_tc"]["value"] / out["plain"]["value"]
+    # stress error of the surrogate path against the exact solve, same input distribution
+    m = 1 << 20
+    u = W.splitmix64_uniform(11, 4 * m)
+    edot, T, d, P = 10 ** (-18 + 8 * u[0::4]), 100 + 173 * u[1::4], 10 ** (-4 + 3 * u[2::4]), 1e8 * u[3::4]
+    G.creep_configure(mode=0, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
+    s0, _, _, _ = G.creep_solve(edot, T, d, P, mode=0)
+    s2, _, _, fb = G.creep_solve(edot, T, d, P, mode=2)
+    rel = np.abs(s2 / s0 - 1.0)
+    out["stress_rel_err"] = {"max": float(rel.max()), "median": float(np.median(rel)),
+                             "fallbacks": int(fb.sum()), "sample": "%d solves, tensor-core surrogate vs exact" % m}
+    return out
 
 
 def main():

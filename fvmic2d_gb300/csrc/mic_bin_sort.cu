@@ -207,6 +207,7 @@ struct GatherCols {
   double *dst_f[C_F64_COUNT];
   const int *src_i[C_I32_COUNT];
   int *dst_i[C_I32_COUNT];
+  int nf;  // double columns moved: the device-only grain column only once grain sizes were set
 };
 
 __global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n) {
@@ -214,7 +215,8 @@ __global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n)
   if (k >= n) return;
   const int p = perm[k];
 #pragma unroll
-  for (int c = 0; c < C_F64_COUNT; ++c) g.dst_f[c][k] = g.src_f[c][p];
+  for (int c = 0; c < C_F64_COUNT; ++c)
+    if (c < g.nf) g.dst_f[c][k] = g.src_f[c][p];
 #pragma unroll
   for (int c = 0; c < C_I32_COUNT; ++c) g.dst_i[c][k] = g.src_i[c][p];
 }
@@ -319,6 +321,7 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   }
   MIC_CUDA_TRY(cudaGetLastError());
   GatherCols g;
+  g.nf = ctx->has_grain ? C_F64_COUNT : C_AOS_F64;
   for (int c = 0; c < C_F64_COUNT; ++c) {
     g.src_f[c] = ctx->f64[c];
     g.dst_f[c] = ctx->f64_alt[c];
@@ -332,7 +335,7 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
     k_reorder<<<grid_for(n), kBlock, 0, ctx->stream>>>(g, vin, n);
   }
   MIC_CUDA_TRY(cudaGetLastError());
-  for (int c = 0; c < C_F64_COUNT; ++c) {
+  for (int c = 0; c < g.nf; ++c) {
     double *t = ctx->f64[c];
     ctx->f64[c] = ctx->f64_alt[c];
     ctx->f64_alt[c] = t;

@@ -394,6 +394,7 @@ extern "C" int mic_markers_upload(mic_ctx *ctx, const mic_marker *host, int64_t 
     MIC_CUDA_TRY(cudaGetLastError());
   }
   ctx->n = n;
+  ctx->has_grain = 0;  // grain column back to its uniform default
   mic_invalidate_sort(ctx);
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return MIC_OK;

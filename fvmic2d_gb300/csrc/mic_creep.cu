@@ -317,6 +317,7 @@ extern "C" int mic_markers_set_grain_size(mic_ctx *ctx, const double *d, int64_t
   MIC_CUDA_TRY(cudaMemcpyAsync(tmp, d, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   int e = mic_gather_by_id(ctx, tmp, ctx->f64[C_GRAIN]);
   if (e) return e;
+  ctx->has_grain = 1;
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return MIC_OK;
 }

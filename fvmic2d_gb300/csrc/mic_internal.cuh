@@ -86,6 +86,7 @@ struct mic_ctx {
   float *train_buf;             // training scratch (grown on demand)
   int64_t train_cap;
   int64_t n, cap;
+  int has_grain;  // per-marker grain sizes were set: the grain column moves with the sorts
   double *f64[mic::C_F64_COUNT];
   int *i32[mic::C_I32_COUNT];
   double *f64_alt[mic::C_F64_COUNT];
