@@ -58,6 +58,9 @@ KERNEL_BYTES = {
     "k_strain_pressure": (8 + 4 + 32 + 16 + 16 + 8 + 24 + 8 + 8, 80),
     # cellX, Mat, X, Y, T, p, Eii, e3, eta, mu, s3 read; eta, mu, s3 written
     "k_yield": (8 + 16 + 8 + 8 + 8 + 24 + 16 + 24 + 16 + 24, 0),
+    # law-7 variants read the grain size as well
+    "k_yield_surrogate_fp32": (8 + 16 + 8 + 8 + 8 + 24 + 16 + 24 + 16 + 24 + 8, 0),
+    "k_yield_tc": (8 + 16 + 8 + 8 + 8 + 24 + 16 + 24 + 16 + 24 + 8, 0),
     # all 29 marker columns read and written
     "k_reorder": (2 * (23 * 8 + 6 * 4) + 4, 0),
 }
@@ -71,6 +74,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="vep_slab_box")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the composite-creep surrogate leg")
+    ap.add_argument("--creep-mode", type=int, default=0, choices=[0, 1, 2],
+                    help="law-7 solve of the main leg: 0 exact, 1 FP32 surrogate, 2 tensor-core surrogate")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-cores", type=int, default=0, help="host processes for the CPU legs (0 = all)")
     return ap.parse_args()
@@ -273,6 +278,11 @@ def run_ours(args):
     torch.cuda.set_device(local)
     wl = make_workload(args.workload)
     G = gpu.MicProblem(wl, device=local)
+    if getattr(wl, "grain_size", None) is not None:
+        G.set_grain_size(wl.grain_size)
+    if args.creep_mode:
+        G.creep_train()
+        G.creep_configure(mode=args.creep_mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
     L, h = G.L, G.h
     stream = torch.cuda.ExternalStream(G.stream(), device=local)
     n = len(wl.markers)
