@@ -221,6 +221,16 @@ __global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n)
   for (int c = 0; c < C_I32_COUNT; ++c) g.dst_i[c][k] = g.src_i[c][p];
 }
 
+// perm[k] = device slot of caller marker k (k < n); slots from n on stay in place
+__global__ void k_restore_perm(const int *__restrict__ id, int64_t n, int64_t cap, int *__restrict__ perm) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= cap) return;
+  if (s < n)
+    perm[id[s]] = (int)s;
+  else
+    perm[s] = (int)s;
+}
+
 // aux: free space for the block totals of this level and all coarser levels
 int scan_exclusive(mic_ctx *ctx, int *data, int64_t len, int *aux) {
   const int64_t nb = (len + kScanBlock - 1) / kScanBlock;
@@ -352,6 +362,44 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
     MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     *n_out = (int64_t)ctx->h_status->n_out;
   }
+  return MIC_OK;
+}
+
+// Columns [0, n) back to the caller's marker order (slot k holds caller marker k); slots
+// [n, cap) keep their contents.  The next pass bins and sorts again.
+int mic_restore_caller_order(mic_ctx *ctx) {
+  const int64_t cap = ctx->cap;
+  if (cap == 0) return MIC_OK;
+  {
+    MIC_KERNEL(ctx, "k_restore_perm");
+    k_restore_perm<<<grid_for(cap), kBlock, 0, ctx->stream>>>(ctx->i32[C_ID], ctx->n, cap, ctx->perm);
+  }
+  GatherCols g;
+  g.nf = ctx->has_grain ? C_F64_COUNT : C_AOS_F64;
+  for (int c = 0; c < C_F64_COUNT; ++c) {
+    g.src_f[c] = ctx->f64[c];
+    g.dst_f[c] = ctx->f64_alt[c];
+  }
+  for (int c = 0; c < C_I32_COUNT; ++c) {
+    g.src_i[c] = ctx->i32[c];
+    g.dst_i[c] = ctx->i32_alt[c];
+  }
+  {
+    MIC_KERNEL(ctx, "k_reorder");
+    k_reorder<<<grid_for(cap), kBlock, 0, ctx->stream>>>(g, ctx->perm, cap);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  for (int c = 0; c < g.nf; ++c) {
+    double *t = ctx->f64[c];
+    ctx->f64[c] = ctx->f64_alt[c];
+    ctx->f64_alt[c] = t;
+  }
+  for (int c = 0; c < C_I32_COUNT; ++c) {
+    int *t = ctx->i32[c];
+    ctx->i32[c] = ctx->i32_alt[c];
+    ctx->i32_alt[c] = t;
+  }
+  mic_invalidate_sort(ctx);
   return MIC_OK;
 }
 

@@ -267,13 +267,15 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   }
   const int64_t cap = max_markers > 0 ? max_markers : 1;
   ctx->cap = cap;
-  for (int c = 0; c < C_F64_COUNT; ++c) {
+  for (int c = 0; c < C_F64_COUNT; ++c) {  // zeroed: fields no routine has written read as 0
     ALLOC(ctx->f64[c], sizeof(double) * cap);
     ALLOC(ctx->f64_alt[c], sizeof(double) * cap);
+    cudaMemset(ctx->f64[c], 0, sizeof(double) * cap);
   }
   for (int c = 0; c < C_I32_COUNT; ++c) {
     ALLOC(ctx->i32[c], sizeof(int) * cap);
     ALLOC(ctx->i32_alt[c], sizeof(int) * cap);
+    cudaMemset(ctx->i32[c], 0, sizeof(int) * cap);
   }
   const size_t nn = (size_t)NX * NY;
   for (int f = 0; f < MIC_NF_COUNT; ++f) {
@@ -342,12 +344,14 @@ extern "C" int mic_destroy(mic_ctx *ctx) {
 extern "C" int mic_set_materials(mic_ctx *ctx, const mic_materials *m) {
   if (!ctx || !m || m->nMaterials < 1 || m->nMaterials > MIC_MAXMAT) return MIC_ERR_ARG;
   ctx->mat = *m;
+  ctx->gen++;
   return MIC_OK;
 }
 
 extern "C" int mic_set_options(mic_ctx *ctx, const mic_options *o) {
   if (!ctx || !o) return MIC_ERR_ARG;
   ctx->opt = *o;
+  ctx->gen++;
   return MIC_OK;
 }
 
@@ -356,6 +360,7 @@ extern "C" int mic_set_bcs(mic_ctx *ctx, const mic_bcs *b) {
   if (b->mechBCTop.type[0] != 0 && b->mechBCTop.type[0] != 1) return MIC_ERR_BC;
   if (b->mechBCLeft.type[1] != 0 && b->mechBCLeft.type[1] != 1) return MIC_ERR_BC;
   ctx->bcs = *b;
+  ctx->gen++;
   return MIC_OK;
 }
 
@@ -394,6 +399,7 @@ extern "C" int mic_markers_upload(mic_ctx *ctx, const mic_marker *host, int64_t 
     MIC_CUDA_TRY(cudaGetLastError());
   }
   ctx->n = n;
+  ctx->gen++;
   ctx->has_grain = 0;  // grain column back to its uniform default
   mic_invalidate_sort(ctx);
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -609,5 +615,140 @@ int mic_gather_by_id(mic_ctx *ctx, const double *src, double *dst) {
     k_gather_by_id<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(src, ctx->i32[C_ID], dst, ctx->n);
   }
   MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
+
+// ---- marker lifecycle: resetMarkers, distributeMarkersUniformInDomain, field fills ----------
+
+// resetMarker (markers.c:255-330) on every slot of the capacity; mu, cellX, cellY, cpu and the
+// strain-rate residual are left as they are, as in the reference
+__global__ void k_reset_markers(ColPtrs c, int64_t cap) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= cap) return;
+  c.f[C_X][m] = -1.0;
+  c.f[C_Y][m] = -1.0;
+  const int zero[] = {C_VX, C_VY, C_T, C_TDOT, C_SXX, C_SYY, C_SXY, C_ETA, C_RHO, C_RHODOT, C_P,
+                      C_EXX, C_EYY, C_EXY, C_EXX_TOT, C_EYY_TOT, C_EXY_TOT, C_EII, C_WXY};
+#pragma unroll
+  for (int q = 0; q < (int)(sizeof(zero) / sizeof(zero[0])); ++q) c.f[zero[q]][m] = 0.0;
+  c.f[C_GRAIN][m] = 1e-3;
+  c.i[C_MAT][m] = -1;
+  c.i[C_ISYIELD][m] = 0;
+}
+
+// The single-rank PETSc random stream of distributeMarkersUniformInDomain: 48-bit state
+// X <- (0x5DEECE66D X + 11) mod 2^48 from (seed << 16) | 0x330E, value u = X / 2^48 after each
+// step.  k steps at once: the affine map x -> A x + C composed k times (binary powers).
+__device__ __forceinline__ unsigned long long lcg48_after(unsigned long long x0, unsigned long long k) {
+  unsigned long long A = 0x5DEECE66DULL, C = 0xBULL, m = 1ULL, a = 0ULL;
+  while (k) {
+    if (k & 1ULL) {
+      m = A * m;
+      a = A * a + C;
+    }
+    C = A * C + C;
+    A = A * A;
+    k >>= 1;
+  }
+  return (m * x0 + a) & 0xFFFFFFFFFFFFULL;
+}
+
+// PetscRandomGetValue on [lo, hi) after `calls` earlier values; the reference's expression
+// order, without contraction
+__device__ __forceinline__ double stream_value(unsigned long long x0, unsigned long long calls, double lo,
+                                               double hi) {
+  const double u = (double)lcg48_after(x0, calls + 1) * (1.0 / 281474976710656.0);
+  return __dadd_rn(lo, __dmul_rn(__dsub_rn(hi, lo), u));
+}
+
+// distributeMarkersUniformInDomain (markers.c:342-400): marker idx = k * nyl + l at
+// x0 + mdx (0.5 + k) + U(-mdx/4, mdx/4), y0 + mdy (0.5 + l) + U(-mdy/4, mdy/4), two values per
+// marker from the stream in marker order
+__global__ void k_distribute(ColPtrs c, int64_t n, int nyl, double x0, double y0, double mdx, double mdy,
+                             unsigned long long state0) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int64_t k = idx / nyl, l = idx % nyl;
+  const double tx = stream_value(state0, 2ULL * (unsigned long long)idx, -mdx / 4.0, mdx / 4.0);
+  const double ty = stream_value(state0, 2ULL * (unsigned long long)idx + 1ULL, -mdy / 4.0, mdy / 4.0);
+  c.f[C_X][idx] = __dadd_rn(__dadd_rn(x0, __dmul_rn(mdx, 0.5 + (double)k)), tx);
+  c.f[C_Y][idx] = __dadd_rn(__dadd_rn(y0, __dmul_rn(mdy, 0.5 + (double)l)), ty);
+  c.i[C_ID][idx] = (int)idx;
+}
+
+__global__ void k_fill_f64(double *col, double v, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m < n) col[m] = v;
+}
+
+__global__ void k_fill_i32(int *col, int v, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m < n) col[m] = v;
+}
+
+extern "C" int mic_reset_markers(mic_ctx *ctx) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->cap > 0) {
+    MIC_KERNEL(ctx, "k_reset_markers");
+    k_reset_markers<<<grid_for(ctx->cap), kBlock, 0, ctx->stream>>>(cur_cols(ctx), ctx->cap);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  ctx->has_grain = 0;
+  ctx->gen++;
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_distribute_markers_uniform_in_domain(mic_ctx *ctx, int NMX, int NMY, unsigned long seed,
+                                                        int64_t *n_placed) {
+  if (!ctx || NMX < 1 || NMY < 1) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const int NX = ctx->P.NX, NY = ctx->P.NY;
+  const double *hx = ctx->h_x + 2;
+  const size_t nx4 = (size_t)NX + 4;
+  const double *hy = ctx->h_x + 2 * nx4 + 2;
+  // markers.c:367-375, one rank owning the whole grid
+  const double mdx = ctx->P.LX / (NMX * (NX - 1));
+  const double mdy = ctx->P.LY / (NMY * (NY - 1));
+  const int nxl = (int)((hx[NX - 1] - hx[0]) / mdx);
+  const int nyl = (int)((hy[NY - 1] - hy[0]) / mdy);
+  const int64_t n = (int64_t)(nxl > 0 ? nxl : 0) * (int64_t)(nyl > 0 ? nyl : 0);
+  if (n > ctx->cap) return MIC_ERR_CAPACITY;
+  int e;
+  // the reference writes X, Y into array slots 0..n-1 and leaves every other field as it was
+  if (ctx->n > 0 && (e = mic_restore_caller_order(ctx))) return e;
+  if (n > 0) {
+    const unsigned long long state0 = ((unsigned long long)(seed & 0xFFFFFFFFUL) << 16) | 0x330EULL;
+    MIC_KERNEL(ctx, "k_distribute");
+    k_distribute<<<grid_for(n), kBlock, 0, ctx->stream>>>(cur_cols(ctx), n, nyl, hx[0], hy[0], mdx, mdy, state0);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  ctx->n = n;
+  ctx->gen++;
+  mic_invalidate_sort(ctx);
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (n_placed) *n_placed = n;
+  return MIC_OK;
+}
+
+extern "C" int mic_markers_fill(mic_ctx *ctx, int field_offset, double value) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const int fc = mic_f64_column_of_offset(field_offset);
+  int ic = -1;
+  for (int c = 0; c < C_I32_COUNT - 1; ++c)
+    if (h_i32_off[c] == field_offset) ic = c;
+  if (fc < 0 && ic < 0) return MIC_ERR_ARG;
+  if (ctx->n > 0) {
+    MIC_KERNEL(ctx, "k_fill");
+    if (fc >= 0)
+      k_fill_f64<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->f64[fc], value, ctx->n);
+    else
+      k_fill_i32<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[ic], (int)value, ctx->n);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  if (ic == C_CELLX || ic == C_CELLY || fc == C_X || fc == C_Y) mic_invalidate_sort(ctx);
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return MIC_OK;
 }

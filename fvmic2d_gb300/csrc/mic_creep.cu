@@ -283,6 +283,7 @@ int ensure_mlp(mic_ctx *ctx) {
   if (ctx->mlp) return MIC_OK;
   if (cudaMalloc((void **)&ctx->mlp, sizeof(float) * kNParams) != cudaSuccess) return MIC_ERR_NOMEM;
   ctx->creep.mlp = ctx->mlp;
+  ctx->gen++;
   return MIC_OK;
 }
 
@@ -305,6 +306,7 @@ extern "C" int mic_creep_configure(mic_ctx *ctx, int mode, double tol, int maxit
   ctx->creep.maxit = maxit;
   ctx->creep.polish_iters = polish_iters;
   ctx->creep.polish_tol = polish_tol;
+  ctx->gen++;
   return MIC_OK;
 }
 
@@ -318,6 +320,7 @@ extern "C" int mic_markers_set_grain_size(mic_ctx *ctx, const double *d, int64_t
   int e = mic_gather_by_id(ctx, tmp, ctx->f64[C_GRAIN]);
   if (e) return e;
   ctx->has_grain = 1;
+  ctx->gen++;
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return MIC_OK;
 }
@@ -525,6 +528,7 @@ extern "C" int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int st
   }
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   ctx->creep.mlp = ctx->mlp;
+  ctx->gen++;
   return MIC_OK;
 }
 

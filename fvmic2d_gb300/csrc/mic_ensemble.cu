@@ -1,0 +1,237 @@
+// mic_ensemble.cu -- many independent marker-in-cell problems stepped together on one GPU.
+//
+// Members are ordinary contexts, each with its own stream.  One ensemble step forks from the
+// ensemble stream to every member stream (events), issues each member's whole step (the same
+// launches as mic_step without a residual read, so nothing waits on the host) and joins back.
+// Small members then overlap on the GPU instead of running one after another.
+//
+// With graphs on, the fork / members / join sequence is captured once into CUDA graphs and each
+// later step is a single graph launch.  A step's launches read the marker columns from one
+// buffer of each double-buffered pair and leave them in the other (the binning's reorder), so
+// the sequence alternates between two layouts: two graphs are captured, one per layout, and
+// replays alternate between them while the host keeps each member's column pointers in step.
+// A graph is re-captured when a member's settings change (materials, options, boundary values,
+// creep configuration, marker count: the member's generation counter) or the time steps do.
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "mic_internal.cuh"
+
+struct mic_ensemble {
+  int device;
+  int n;
+  std::vector<mic_ctx *> m;
+  cudaStream_t stream;
+  cudaEvent_t fork;
+  std::vector<cudaEvent_t> join;
+  // captured steps
+  int have_graph;
+  cudaGraphExec_t exec[2];
+  int parity;
+  std::vector<double> key_dt;  // dt_disp and dt_thermal per member at capture
+  std::vector<long long> key_gen;
+  int key_sub;
+  long long graph_kernels[2];  // kernel launches inside each graph
+  long long launches;          // kernel launches issued through this ensemble
+};
+
+namespace {
+
+int fail(cudaError_t e) {
+  mic_fail_cuda(nullptr, e);
+  return MIC_ERR_CUDA;
+}
+
+// fork, every member's step, join: all asynchronous on the ensemble stream's timeline
+int issue(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub) {
+  cudaError_t ce = cudaEventRecord(E->fork, E->stream);
+  if (ce != cudaSuccess) return fail(ce);
+  for (int i = 0; i < E->n; ++i) {
+    mic_ctx *c = E->m[i];
+    if ((ce = cudaStreamWaitEvent(c->stream, E->fork, 0)) != cudaSuccess) return fail(ce);
+    const long long l0 = c->launches;
+    const int e = mic_step(c, dt_disp[i], dt_thermal[i], sub, nullptr);
+    if (e) return e;
+    E->launches += c->launches - l0;
+    if ((ce = cudaEventRecord(E->join[i], c->stream)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaStreamWaitEvent(E->stream, E->join[i], 0)) != cudaSuccess) return fail(ce);
+  }
+  return MIC_OK;
+}
+
+void drop_graphs(mic_ensemble *E) {
+  for (int q = 0; q < 2; ++q)
+    if (E->have_graph) cudaGraphExecDestroy(E->exec[q]);
+  E->have_graph = 0;
+}
+
+bool graph_current(const mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub) {
+  if (!E->have_graph || E->key_sub != sub) return false;
+  for (int i = 0; i < E->n; ++i) {
+    if (E->key_dt[2 * i] != dt_disp[i] || E->key_dt[2 * i + 1] != dt_thermal[i]) return false;
+    if (E->key_gen[i] != E->m[i]->gen) return false;
+  }
+  return true;
+}
+
+// the host side of a replayed step: the binning swapped each member's column buffers
+void replayed(mic_ensemble *E) {
+  for (int i = 0; i < E->n; ++i) {
+    mic_ctx *c = E->m[i];
+    if (c->n == 0) continue;
+    const int nf = c->has_grain ? mic::C_F64_COUNT : mic::C_AOS_F64;
+    for (int k = 0; k < nf; ++k) {
+      double *t = c->f64[k];
+      c->f64[k] = c->f64_alt[k];
+      c->f64_alt[k] = t;
+    }
+    for (int k = 0; k < mic::C_I32_COUNT; ++k) {
+      int *t = c->i32[k];
+      c->i32[k] = c->i32_alt[k];
+      c->i32_alt[k] = t;
+    }
+    mic_invalidate_sort(c);
+  }
+}
+
+int capture(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub) {
+  drop_graphs(E);
+  for (int q = 0; q < 2; ++q) {
+    std::vector<int> prof(E->n);
+    for (int i = 0; i < E->n; ++i) {  // no per-launch timing events inside a graph
+      prof[i] = E->m[i]->prof_on;
+      E->m[i]->prof_on = 0;
+    }
+    cudaError_t ce = cudaStreamBeginCapture(E->stream, cudaStreamCaptureModeRelaxed);
+    if (ce != cudaSuccess) return fail(ce);
+    const long long l0 = E->launches;
+    int e = issue(E, dt_disp, dt_thermal, sub);
+    cudaGraph_t g = nullptr;
+    ce = cudaStreamEndCapture(E->stream, &g);
+    for (int i = 0; i < E->n; ++i) E->m[i]->prof_on = prof[i];
+    E->graph_kernels[q] = E->launches - l0;
+    E->launches = l0;
+    if (e) {
+      if (g) cudaGraphDestroy(g);
+      if (q == 1) cudaGraphExecDestroy(E->exec[0]);
+      return e;
+    }
+    if (ce != cudaSuccess) return fail(ce);
+    ce = cudaGraphInstantiate(&E->exec[q], g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      if (q == 1) cudaGraphExecDestroy(E->exec[0]);
+      return fail(ce);
+    }
+  }
+  // two captured steps swapped every member's buffers twice: the host view is unchanged
+  E->have_graph = 1;
+  E->parity = 0;
+  E->key_sub = sub;
+  E->key_dt.assign(2 * E->n, 0.0);
+  E->key_gen.assign(E->n, 0);
+  for (int i = 0; i < E->n; ++i) {
+    E->key_dt[2 * i] = dt_disp[i];
+    E->key_dt[2 * i + 1] = dt_thermal[i];
+    E->key_gen[i] = E->m[i]->gen;
+  }
+  return MIC_OK;
+}
+
+}  // namespace
+
+extern "C" int mic_ensemble_create(mic_ensemble **out, mic_ctx *const *members, int n_members) {
+  if (!out || !members || n_members < 1) return MIC_ERR_ARG;
+  for (int i = 0; i < n_members; ++i)
+    if (!members[i] || members[i]->device != members[0]->device) return MIC_ERR_ARG;
+  for (int i = 0; i < n_members; ++i)
+    for (int j = 0; j < i; ++j)
+      if (members[i] == members[j] || members[i]->stream == members[j]->stream) return MIC_ERR_ARG;
+  mic_ensemble *E = new (std::nothrow) mic_ensemble();
+  if (!E) return MIC_ERR_NOMEM;
+  E->device = members[0]->device;
+  E->n = n_members;
+  E->m.assign(members, members + n_members);
+  E->join.assign(n_members, nullptr);
+  cudaSetDevice(E->device);
+  bool ok = cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&E->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; ok && i < n_members; ++i)
+    ok = cudaEventCreateWithFlags(&E->join[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    delete E;
+    return MIC_ERR_CUDA;
+  }
+  *out = E;
+  return MIC_OK;
+}
+
+extern "C" int mic_ensemble_destroy(mic_ensemble *E) {
+  if (!E) return MIC_ERR_ARG;
+  cudaSetDevice(E->device);
+  cudaStreamSynchronize(E->stream);
+  drop_graphs(E);
+  for (auto ev : E->join)
+    if (ev) cudaEventDestroy(ev);
+  cudaEventDestroy(E->fork);
+  cudaStreamDestroy(E->stream);
+  delete E;
+  return MIC_OK;
+}
+
+// One step of every member (dt_disp[i], dt_thermal[i]; subgrid stress changes on or off).
+// Asynchronous: returns once the work is queued; mic_ensemble_synchronize waits for it.  With
+// use_graph, the first call (and any call after a member's settings or the time steps changed)
+// runs the step directly and captures the graphs the following calls launch.
+extern "C" int mic_ensemble_step(mic_ensemble *E, const double *dt_disp, const double *dt_thermal,
+                                 int subgrid_stress, int use_graph) {
+  if (!E || !dt_disp || !dt_thermal) return MIC_ERR_ARG;
+  cudaSetDevice(E->device);
+  if (!use_graph) {
+    drop_graphs(E);
+    return issue(E, dt_disp, dt_thermal, subgrid_stress);
+  }
+  if (graph_current(E, dt_disp, dt_thermal, subgrid_stress)) {
+    // the graph runs after whatever the caller queued on member streams (nodal uploads), and
+    // member streams see its results
+    cudaError_t ce;
+    for (int i = 0; i < E->n; ++i) {
+      if ((ce = cudaEventRecord(E->join[i], E->m[i]->stream)) != cudaSuccess) return fail(ce);
+      if ((ce = cudaStreamWaitEvent(E->stream, E->join[i], 0)) != cudaSuccess) return fail(ce);
+    }
+    if ((ce = cudaGraphLaunch(E->exec[E->parity], E->stream)) != cudaSuccess) return fail(ce);
+    if ((ce = cudaEventRecord(E->fork, E->stream)) != cudaSuccess) return fail(ce);
+    for (int i = 0; i < E->n; ++i)
+      if ((ce = cudaStreamWaitEvent(E->m[i]->stream, E->fork, 0)) != cudaSuccess) return fail(ce);
+    E->launches += E->graph_kernels[E->parity];
+    replayed(E);
+    E->parity ^= 1;
+    return MIC_OK;
+  }
+  int e = issue(E, dt_disp, dt_thermal, subgrid_stress);  // this call's step, run directly
+  if (e) return e;
+  cudaError_t ce = cudaStreamSynchronize(E->stream);  // scratch sized, nothing in flight
+  if (ce != cudaSuccess) return fail(ce);
+  return capture(E, dt_disp, dt_thermal, subgrid_stress);
+}
+
+extern "C" int mic_ensemble_synchronize(mic_ensemble *E) {
+  if (!E) return MIC_ERR_ARG;
+  cudaSetDevice(E->device);
+  cudaError_t ce = cudaStreamSynchronize(E->stream);
+  return ce == cudaSuccess ? MIC_OK : fail(ce);
+}
+
+extern "C" int mic_ensemble_launch_count(mic_ensemble *E, int64_t *launches, int64_t *graph_kernels) {
+  if (!E) return MIC_ERR_ARG;
+  if (launches) *launches = E->launches;
+  if (graph_kernels) *graph_kernels = E->have_graph ? E->graph_kernels[0] : 0;
+  return MIC_OK;
+}
+
+extern "C" int mic_ensemble_get_stream(mic_ensemble *E, void **stream) {
+  if (!E || !stream) return MIC_ERR_ARG;
+  *stream = (void *)E->stream;
+  return MIC_OK;
+}

@@ -87,6 +87,7 @@ struct mic_ctx {
   int64_t train_cap;
   int64_t n, cap;
   int has_grain;  // per-marker grain sizes were set: the grain column moves with the sorts
+  long long gen;  // bumped by every setter that changes what a step launches (captured graphs)
   double *f64[mic::C_F64_COUNT];
   int *i32[mic::C_I32_COUNT];
   double *f64_alt[mic::C_F64_COUNT];
@@ -151,6 +152,8 @@ void mic_invalidate_sort(mic_ctx *ctx);
 int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out);
 int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry
 int mic_f64_column_of_offset(int byte_offset);
+// columns [0, n) back to caller order, slots from n on kept (mic_bin_sort.cu)
+int mic_restore_caller_order(mic_ctx *ctx);
 // scatter a caller-order per-marker array into device (column) order through the id column
 int mic_gather_by_id(mic_ctx *ctx, const double *src, double *dst);
 // persistent block count of the tensor-core creep kernels for n markers (mic_creep_tc.cu)

@@ -77,6 +77,15 @@ SIGNATURES = {
     "mic_creep_solve_batch": (_I, [_P, _DP, _DP, _DP, _DP, _I64, _I, _DP, _P, _DP, _P]),
     "mic_creep_mlp_infer": (_I, [_P, _P, _I64, _I, _P]),
     "mic_creep_stats": (_I, [_P, _I64P, _I64P, _I64P, _DP, _I64P]),
+    "mic_reset_markers": (_I, [_P]),
+    "mic_distribute_markers_uniform_in_domain": (_I, [_P, _I, _I, ctypes.c_ulong, _I64P]),
+    "mic_markers_fill": (_I, [_P, _I, _D]),
+    "mic_ensemble_create": (_I, [ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
+    "mic_ensemble_destroy": (_I, [_P]),
+    "mic_ensemble_step": (_I, [_P, _DP, _DP, _I, _I]),
+    "mic_ensemble_synchronize": (_I, [_P]),
+    "mic_ensemble_launch_count": (_I, [_P, _I64P, _I64P]),
+    "mic_ensemble_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -158,6 +167,22 @@ class MicProblem:
             self.close()
         except Exception:
             pass
+
+    # ---- marker lifecycle (markers.c:255-400) ---------------------------------
+    def resetMarkers(self):
+        self._check(self.L.mic_reset_markers(self.h), "mic_reset_markers")
+
+    def distributeMarkersUniformInDomain(self, NMX, NMY, seed=0):
+        n = ctypes.c_int64(0)
+        self._check(self.L.mic_distribute_markers_uniform_in_domain(self.h, NMX, NMY, seed, ctypes.byref(n)),
+                    "mic_distribute_markers_uniform_in_domain")
+        self.n = n.value
+        return self.n
+
+    def fill(self, field, value):
+        """Set one marker field (a MARKER_DTYPE name) to value on every marker."""
+        off = MARKER_DTYPE.fields[field][1]
+        self._check(self.L.mic_markers_fill(self.h, off, float(value)), "mic_markers_fill")
 
     # ---- transfers -----------------------------------------------------------
     def upload_markers(self, mk):
@@ -379,3 +404,67 @@ class MicProblem:
         r = ctypes.c_double(0.0)
         self._check(self.L.mic_step(self.h, dt_disp, dt_thermal, int(subgrid_stress), ctypes.byref(r)), "mic_step")
         return 0, r.value
+
+
+def initialize_markers(P, NMX, NMY, seed=0, mat=0, T_field="lastT"):
+    """The reference's marker set-up on the device (main_subduction.c:175-202): resetMarkers,
+    distributeMarkersUniformInDomain, material id, cells, temperature from a nodal field
+    (projectNodalFieldToMarkersS) and viscosity from it (updateViscosity)."""
+    P.resetMarkers()
+    n = P.distributeMarkersUniformInDomain(NMX, NMY, seed)
+    P.fill("Mat", mat)
+    P.findMarkerCells()
+    P.projectNodalFieldToMarkersS(T_field, "T")
+    P.updateViscosity()
+    return n
+
+
+class MicEnsemble:
+    """Independent problems stepped together (mic_ensemble_*): members are MicProblem objects,
+    each on its own context stream."""
+
+    def __init__(self, members):
+        self.members = list(members)
+        self.L = self.members[0].L
+        arr = (_P * len(self.members))(*[m.h for m in self.members])
+        h = _P()
+        code = self.L.mic_ensemble_create(ctypes.byref(h), arr, len(self.members))
+        if code:
+            raise MicError(code, "mic_ensemble_create")
+        self.h = h
+
+    def step(self, dt_disp=None, dt_thermal=None, subgrid_stress=1, graph=True):
+        n = len(self.members)
+        dd = np.ascontiguousarray(dt_disp if dt_disp is not None else [m.wl.dt for m in self.members], dtype=np.float64)
+        dth = np.ascontiguousarray(dt_thermal if dt_thermal is not None else [m.wl.dt_thermal for m in self.members],
+                                   dtype=np.float64)
+        assert len(dd) == n and len(dth) == n
+        code = self.L.mic_ensemble_step(self.h, _dp(dd), _dp(dth), subgrid_stress, 1 if graph else 0)
+        if code:
+            raise MicError(code, "mic_ensemble_step")
+
+    def synchronize(self):
+        code = self.L.mic_ensemble_synchronize(self.h)
+        if code:
+            raise MicError(code, "mic_ensemble_synchronize")
+
+    def launch_count(self):
+        a, b = ctypes.c_int64(0), ctypes.c_int64(0)
+        self.L.mic_ensemble_launch_count(self.h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def stream(self):
+        s = _P()
+        self.L.mic_ensemble_get_stream(self.h, ctypes.byref(s))
+        return s.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mic_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

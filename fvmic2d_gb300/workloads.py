@@ -347,6 +347,73 @@ def ice_creep_box(nx_cells=1024, ny_cells=1024, nm=4, seed=3):
     return wl
 
 
+def convection_member(nx_cells, ny_cells, nmx, nmy, Ra, contrast, seed):
+    """One ensemble member: thermal convection in a box of aspect nx_cells:ny_cells (height 1),
+    viscosity exp(-ln(contrast) T) (hasEtaT 5), free slip, T0 = 1 - y + 0.01 cos(pi x) sin(pi y);
+    prescribed cellular flow with speed 100 (Ra / 1e4)^(2/3).  No host markers: the member's
+    markers are laid out on the device (resetMarkers, distributeMarkersUniformInDomain with
+    nmx x nmy per cell and this seed, Mat 0, T from the nodal field, viscosity from T)."""
+    NX, NY = nx_cells + 1, ny_cells + 1
+    LX = float(nx_cells) / float(ny_cells)
+    g = Grid(NX, NY, LX, 1.0, spacing_uniform(0.0, LX, NX), spacing_uniform(0.0, 1.0, NY))
+    mat = _materials(1)
+    mat.materialEta[0] = 1.0
+    mat.materialRho[0] = 1.0
+    mat.materialkThermal[0] = 1.0
+    mat.materialCp[0] = 1.0
+    mat.materialAlpha[0] = 1.0
+    mat.materialMu[0] = 1e20
+    mat.hasEtaT[0] = 5
+    mat.QonR[0] = math.log(contrast)
+    mat.Tref[0] = 1.0
+    opt = Options(etamin=1.0 / contrast, etamax=contrast, fractionalEtamin=0.01, subgridStressDiffusivity=0.0,
+                  subgridTemperatureDiffusivity=1.0)
+    U = 100.0 * (Ra / 1e4) ** (2.0 / 3.0)
+    pi = np.pi
+    vx_fn = lambda x, y: U * pi * np.sin(pi * x / LX) * np.cos(pi * y)
+    vy_fn = lambda x, y: -U * pi / LX * np.cos(pi * x / LX) * np.sin(pi * y)
+    dvx = {"x": lambda x, y: U * pi * pi / LX * np.cos(pi * x / LX) * np.cos(pi * y),
+           "y": lambda x, y: -U * pi * pi * np.sin(pi * x / LX) * np.sin(pi * y)}
+    dvy = {"x": lambda x, y: U * pi * pi / LX ** 2 * np.sin(pi * x / LX) * np.sin(pi * y),
+           "y": lambda x, y: -U * pi * pi / LX * np.cos(pi * x / LX) * np.cos(pi * y)}
+    vx, vy, exx, eyy, exy, wxy = _velocity_fields(g, vx_fn, vy_fn, dvx, dvy)
+    XCc, YCc = np.meshgrid(g.xc[:NX], g.yc[:NY], indexing="xy")
+    Xb, Yb = np.meshgrid(g.x, g.y, indexing="xy")
+    Tn = 1.0 - Yb + 0.01 * np.cos(pi * Xb / LX) * np.sin(pi * Yb)
+    eta_c = np.exp(-math.log(contrast) * np.clip(1.0 - YCc, 0.0, 1.0))
+    nodal = {
+        "vx": vx, "vy": vy, "edotxx": exx, "edotyy": eyy, "edotxy": exy, "wxy": wxy,
+        "p": np.zeros((NY, NX)),
+        "soxx": 2.0 * eta_c * exx, "soyy": 2.0 * eta_c * eyy, "soxy": np.zeros((NY, NX)),
+        "thisT": Tn + 1e-3 * np.sin(pi * Xb / LX) * np.sin(pi * Yb), "lastT": Tn,
+    }
+    nodal["dsxx"] = 0.05 * nodal["soxx"]
+    nodal["dsyy"] = 0.05 * nodal["soyy"]
+    nodal["dsxy"] = 0.05 * exy
+    dt = 0.5 * (1.0 / ny_cells) / (U * pi)
+    wl = Workload("convection_member", g, np.zeros(0, dtype=MARKER_DTYPE), mat, opt, _free_slip(), nodal, dt, dt,
+                  10)
+    wl.nm = (nmx, nmy)
+    wl.seed = seed
+    wl.capacity = nmx * nmy * nx_cells * ny_cells
+    return wl
+
+
+def convection_ensemble(n_members=64, seed=4):
+    """Ensemble of independent convection runs: square grids drawn from {64^2, 128^2, 256^2,
+    512^2} cells, 9, 16 or 25 markers per cell (3x3, 4x4, 5x5), Ra log-uniform in [1e4, 1e7],
+    viscosity contrast log-uniform in [1e1, 1e5]; all draws from SplitMix64(seed)."""
+    u = splitmix64_uniform(seed, 4 * n_members)
+    members = []
+    for i in range(n_members):
+        ncell = (64, 128, 256, 512)[min(3, int(u[4 * i] * 4))]
+        nm = (3, 4, 5)[min(2, int(u[4 * i + 1] * 3))]
+        Ra = 10 ** (4 + 3 * u[4 * i + 2])
+        contrast = 10 ** (1 + 4 * u[4 * i + 3])
+        members.append(convection_member(ncell, ncell, nm, nm, Ra, contrast, seed * 1000 + i))
+    return members
+
+
 WORKLOADS = {
     "convection_box": convection_box,
     "vep_slab_box": vep_slab_box,

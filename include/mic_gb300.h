@@ -180,6 +180,39 @@ int mic_launch_count(mic_ctx *ctx, int64_t *launches);
  * off); read aggregates by kernel name (names: max * 48 bytes) */
 int mic_profile_enable(mic_ctx *ctx, int capacity);
 int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64_t *counts, int *nkernels);
+/* ---- marker lifecycle (markers.c:15-39, 255-400) ----
+ * resetMarkers: every slot of the capacity gets resetMarker's values (X = Y = -1, Mat = -1, the
+ * kinematic, thermal, stress, strain and density fields 0; mu, cellX, cellY, cpu and the
+ * strain-rate residual untouched).  The marker count is unchanged. */
+int mic_reset_markers(mic_ctx *ctx);
+/* distributeMarkersUniformInDomain on one rank: NMX x NMY markers per basic cell of the
+ * domain-wide lattice (mdx = LX / (NMX (NX-1)), marker k*nyl + l at x0 + mdx (0.5 + k) plus a
+ * U(-mdx/4, mdx/4) jitter, likewise in y), jitter drawn in marker order from the 48-bit stream
+ * the reference's PETSc random object is seeded with (seed 0 reproduces the reference).  Sets
+ * the marker count (*n_placed); other fields keep their values (call mic_reset_markers first). */
+int mic_distribute_markers_uniform_in_domain(mic_ctx *ctx, int NMX, int NMY, unsigned long seed, int64_t *n_placed);
+/* set one marker field, addressed as offsetof(mic_marker, field), to value for every marker
+ * (integer fields take (int)value) -- the per-marker initial-condition loops of the host code */
+int mic_markers_fill(mic_ctx *ctx, int field_offset, double value);
+
+/* ---- ensembles ----
+ * No counterpart in the reference (one problem per run).  Independent problems, each a context
+ * with its own stream, stepped together: mic_ensemble_step forks every member's mic_step
+ * (no residual read) onto its stream and joins them, so small members overlap on the GPU.  With
+ * use_graph the whole ensemble step is captured as CUDA graphs on the first call and replayed as
+ * one launch afterwards (re-captured when a member's settings, marker count or the time steps
+ * change).  Asynchronous: mic_ensemble_synchronize waits; member streams are ordered after each
+ * step.  Members stay owned by the caller and must outlive the ensemble. */
+typedef struct mic_ensemble mic_ensemble;
+int mic_ensemble_create(mic_ensemble **out, mic_ctx *const *members, int n_members);
+int mic_ensemble_destroy(mic_ensemble *ens);
+int mic_ensemble_step(mic_ensemble *ens, const double *dt_disp, const double *dt_thermal, int subgrid_stress,
+                      int use_graph);
+int mic_ensemble_synchronize(mic_ensemble *ens);
+/* kernels issued through the ensemble so far, and kernels inside one captured step */
+int mic_ensemble_launch_count(mic_ensemble *ens, int64_t *launches, int64_t *graph_kernels);
+int mic_ensemble_get_stream(mic_ensemble *ens, void **stream);
+
 /* ---- binning without allocation ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc -- a host that
  * forbids device allocation once it has started, or a plug-in whose application owns the

@@ -994,3 +994,63 @@ int orc_creep_stress(double edot, double T, double d, double P, double rtol, dou
   *s_out = exp(u);
   return ORC_OK;
 }
+
+/* ---- marker lifecycle -------------------------------------------------------------- */
+
+/* resetMarker (markers.c:255-330): the fields the reference zeroes; mu, cellX, cellY, cpu and
+ * strainRateResidual are left as they are. */
+void orc_reset_markers(mic_marker *mk, int64_t n) {
+  for (int64_t m = 0; m < n; ++m) {
+    mic_marker *p = &mk[m];
+    p->X = -1;
+    p->Y = -1;
+    p->VX = 0;
+    p->VY = 0;
+    p->p = 0.0;
+    p->Mat = -1;
+    p->T = 0.0;
+    p->Tdot = 0.0;
+    p->eta = 0.0;
+    p->s.T11 = p->s.T22 = p->s.T12 = 0.0;
+    p->e.T11 = p->e.T22 = p->e.T12 = 0.0;
+    p->rho = 0.0;
+    p->rhodot = 0.0;
+    p->E.T11 = p->E.T22 = p->E.T12 = 0.0;
+    p->Eii = 0.0;
+    p->wxy = 0.0;
+    p->isYielding = 0;
+  }
+}
+
+/* The random stream of the single-rank PETSc stand-in: PetscRandomSetSeed(r, s) sets the 48-bit
+ * state to (s << 16) | 0x330E, and each value is lo + (hi - lo) * u with u = X / 2^48 after the
+ * LCG step X <- (0x5DEECE66D X + 11) mod 2^48 (the erand48 recurrence). */
+static double orc_rand48(uint64_t *state, double lo, double hi) {
+  *state = (0x5DEECE66DULL * *state + 0xBULL) & 0xFFFFFFFFFFFFULL;
+  const double u = (double)*state / 281474976710656.0;
+  return lo + (hi - lo) * u;
+}
+
+/* distributeMarkersUniformInDomain (markers.c:342-400), one rank: NMX x NMY markers per basic
+ * cell on the domain-wide lattice, each jittered by U(-mdx/4, mdx/4) x U(-mdy/4, mdy/4) from the
+ * stream seeded with `seed` (the reference seeds 0).  Returns the number of markers placed
+ * (-1 if more than cap). */
+int64_t orc_distribute_uniform(const orc_ctx *c, mic_marker *mk, int64_t cap, int NMX, int NMY, unsigned long seed) {
+  const double mdx = c->LX / (NMX * (c->NX - 1));
+  const double mdy = c->LY / (NMY * (c->NY - 1));
+  const int nxl = (int)((c->x[c->NX - 1] - c->x[0]) / mdx);
+  const int nyl = (int)((c->y[c->NY - 1] - c->y[0]) / mdy);
+  if ((int64_t)nxl * nyl > cap) return -1;
+  uint64_t state = ((uint64_t)(seed & 0xFFFFFFFFUL) << 16) | 0x330EULL;
+  int64_t idx = 0;
+  for (int k = 0; k < nxl; ++k) {
+    for (int l = 0; l < nyl; ++l) {
+      double tmp = orc_rand48(&state, -mdx / 4.0, mdx / 4.0);
+      mk[idx].X = c->x[0] + mdx * (0.5 + (double)k) + tmp;
+      tmp = orc_rand48(&state, -mdy / 4.0, mdy / 4.0);
+      mk[idx].Y = c->y[0] + mdy * (0.5 + (double)l) + tmp;
+      ++idx;
+    }
+  }
+  return idx;
+}

@@ -79,6 +79,11 @@ void orc_set_grain(orc_ctx *c, const double *d, int64_t n);
 double orc_gk_strain_rate(double s, double T, double d, double P);
 int orc_creep_stress(double edot, double T, double d, double P, double rtol, double *s_out, int *iters);
 
+/* marker lifecycle: resetMarker (markers.c:255-330) and distributeMarkersUniformInDomain
+ * (markers.c:342-400) with the stand-in's seeded erand48 stream */
+void orc_reset_markers(mic_marker *mk, int64_t n);
+int64_t orc_distribute_uniform(const orc_ctx *c, mic_marker *mk, int64_t cap, int NMX, int NMY, unsigned long seed);
+
 #ifdef __cplusplus
 }
 #endif

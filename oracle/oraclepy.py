@@ -54,6 +54,8 @@ def lib():
             "orc_set_grain": (None, [_P, _DP, _I64]),
             "orc_gk_strain_rate": (_D, [_D, _D, _D, _D]),
             "orc_creep_stress": (_I, [_D, _D, _D, _D, _D, _DP, _IP]),
+            "orc_reset_markers": (None, [_P, _I64]),
+            "orc_distribute_uniform": (_I64, [_P, _P, _I64, _I, _I, ctypes.c_ulong]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -103,6 +105,18 @@ class OracleProblem:
     @property
     def n(self):
         return len(self.markers)
+
+    def distribute_uniform(self, NMX, NMY, seed=0, cap=None):
+        """resetMarkers + distributeMarkersUniformInDomain into a fresh array of capacity cap."""
+        L = lib()
+        cap = cap or NMX * NMY * (self.NX - 1) * (self.NY - 1) + 16
+        mk = np.zeros(cap, dtype=MARKER_DTYPE)
+        L.orc_reset_markers(mk.ctypes.data, cap)
+        n = L.orc_distribute_uniform(self.h, mk.ctypes.data, cap, NMX, NMY, seed)
+        if n < 0:
+            raise ValueError("capacity exceeded")
+        self.markers = mk[:n].copy()
+        return mk, n
 
     def grid_centres(self):
         xc = np.empty(self.NX + 1)

@@ -264,3 +264,21 @@ void ref_stage_reset(void) {
   extern void plite_stage_reset(void);
   plite_stage_reset();
 }
+
+/* resetMarkers + distributeMarkersUniformInDomain (markers.c:332-400) on a caller-owned array of
+ * capacity cap; returns the reference's nMark.  The PETSc random stream is the stand-in's. */
+int ref_resetMarkers(refp *p, mic_marker *m, int cap) {
+  p->ms.markers = (Marker *)m;
+  p->ms.maxMark = cap;
+  resetMarkers(&p->ms, &p->opt);
+  return 0;
+}
+
+int ref_distributeMarkersUniformInDomain(refp *p, mic_marker *m, int cap, int NMX, int NMY) {
+  p->ms.markers = (Marker *)m;
+  p->ms.maxMark = cap;
+  p->opt.NMX = NMX;
+  p->opt.NMY = NMY;
+  if (distributeMarkersUniformInDomain(&p->ms, &p->opt, &p->grid)) return -1;
+  return p->ms.nMark;
+}

@@ -58,6 +58,8 @@ def lib():
             "ref_advectMarkersRK": (_I, [_P, _D]),
             "ref_goldsbyKohlstedt": (_D, [_D, _D, _D, _D]),
             "ref_goldsbyKohlstedt_many": (None, [_DP, _DP, _DP, _DP, _DP, _I]),
+            "ref_resetMarkers": (_I, [_P, _P, _I]),
+            "ref_distributeMarkersUniformInDomain": (_I, [_P, _P, _I, _I, _I]),
             "ref_stage_seconds": (_D, [_I]),
             "ref_stage_reset": (None, []),
         }
@@ -93,6 +95,16 @@ class RefProblem:
         L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         for name, arr in wl.nodal.items():
             self.set_nodal(name, arr)
+
+    def distribute_uniform(self, NMX, NMY, cap=None):
+        """The reference's resetMarkers + distributeMarkersUniformInDomain (seed 0)."""
+        L = lib()
+        cap = cap or NMX * NMY * (self.wl.grid.NX - 1) * (self.wl.grid.NY - 1) + 16
+        mk = np.zeros(cap, dtype=self.markers.dtype)
+        L.ref_resetMarkers(self.h, mk.ctypes.data, cap)
+        n = L.ref_distributeMarkersUniformInDomain(self.h, mk.ctypes.data, cap, NMX, NMY)
+        L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        return mk, n
 
     def close(self):
         if self.h:

@@ -149,9 +149,30 @@ def creep_table():
     return {"s": S.ravel(), "T": TT.ravel(), "d": DD.ravel(), "P": PP.ravel(), "eta": eta}
 
 
+def lifecycle_table():
+    """resetMarkers + distributeMarkersUniformInDomain (markers.c:332-400) on a uniform and a
+    refined grid at two marker densities: the reference's marker arrays (capacity included)."""
+    out = {}
+    for tag, wl in (("uniform", W.convection_box(ncell=8, nm=4, seed=1)),
+                    ("refined", W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2))):
+        R = refpy.RefProblem(wl)
+        for NMX, NMY in ((4, 4), (3, 5)):
+            mk, n = R.distribute_uniform(NMX, NMY)
+            key = "%s_%dx%d" % (tag, NMX, NMY)
+            out[key + "_markers"] = mk.view(np.uint8).reshape(len(mk), -1)
+            out[key + "_n"] = np.int64(n)
+        out[tag + "_x"], out[tag + "_y"] = wl.grid.x, wl.grid.y
+        out[tag + "_L"] = np.array([wl.grid.LX, wl.grid.LY])
+    return out
+
+
 def main():
     if obuild.build_ref() is None:
         raise SystemExit("reference tree not found; golden vectors can only be generated where it exists")
+    np.savez_compressed(os.path.join(OUT, "marker_lifecycle.npz"), **lifecycle_table())
+    print("wrote marker_lifecycle")
+    if sys.argv[1:] == ["lifecycle"]:
+        return
     cases = {
         "convection_box_8": W.convection_box(ncell=8, nm=4, seed=1),
         "vep_slab_box_16x4": W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2),

@@ -1,0 +1,101 @@
+"""GPU checks of the marker lifecycle (resetMarkers, distributeMarkersUniformInDomain) against
+the oracle, and of ensembles: stepping members together -- on their own streams or as captured
+CUDA graphs -- gives exactly what stepping each member alone gives."""
+import numpy as np
+import pytest
+
+from fvmic2d_gb300 import gpu, workloads as W
+from fvmic2d_gb300.mic_types import MARKER_DTYPE
+from oracle import oraclepy
+
+pytestmark = pytest.mark.gpu
+
+
+def _bytes(a):
+    return np.ascontiguousarray(a).view(np.uint8).reshape(len(a), -1)
+
+
+@pytest.mark.parametrize("case", ["uniform", "refined"])
+@pytest.mark.parametrize("nm,seed", [((4, 4), 0), ((3, 5), 0), ((5, 2), 12345)])
+def test_distribute_matches_oracle(case, nm, seed):
+    wl = W.convection_box(ncell=8, nm=4, seed=1) if case == "uniform" else W.vep_slab_box(16, 4, nm=4, seed=2)
+    cap = nm[0] * nm[1] * (wl.grid.NX - 1) * (wl.grid.NY - 1) + 40
+    G = gpu.MicProblem(wl, markers=np.zeros(0, dtype=MARKER_DTYPE), capacity=cap)
+    G.resetMarkers()
+    n = G.distributeMarkersUniformInDomain(nm[0], nm[1], seed)
+    O = oraclepy.OracleProblem(wl, markers=np.zeros(0, dtype=MARKER_DTYPE))
+    mk, no = O.distribute_uniform(nm[0], nm[1], seed=seed, cap=cap)
+    assert n == no
+    assert np.array_equal(_bytes(G.markers), _bytes(mk[:n]))
+
+
+def test_distribute_keeps_other_fields_in_caller_order():
+    """Without a reset the reference overwrites X, Y only: the other fields of array slot k stay
+    -- also after the device has binned and reordered the markers."""
+    wl = W.vep_slab_box(16, 4, nm=4, seed=2)
+    G = gpu.MicProblem(wl)
+    G.findMarkerCells()
+    G.projectMarkersNodesAll2()  # columns now in cell order
+    n = G.distributeMarkersUniformInDomain(3, 3, 7)
+    O = oraclepy.OracleProblem(wl)
+    mk = O.markers.copy()
+    o = oraclepy.lib().orc_distribute_uniform(O.h, mk.ctypes.data, len(mk), 3, 3, 7)
+    assert n == o
+    got = G.markers
+    G.findMarkerCells()
+    exp = mk[:n].copy()
+    for f in ("X", "Y", "T", "eta", "Mat", "p"):
+        assert np.array_equal(got[f], exp[f]), f
+
+
+def _members(seed):
+    specs = [(16, 3, 1e4, 10.0), (32, 4, 3e5, 1e3), (24, 5, 1e7, 1e5), (16, 4, 2e6, 50.0)]
+    return [W.convection_member(c, c, m, m, Ra, k, seed + i) for i, (c, m, Ra, k) in enumerate(specs)]
+
+
+def _setup(wls):
+    out = []
+    for wl in wls:
+        P = gpu.MicProblem(wl, capacity=wl.capacity)
+        gpu.initialize_markers(P, *wl.nm, seed=wl.seed)
+        out.append(P)
+    return out
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_ensemble_matches_members_stepped_alone(graph):
+    wls = _members(40)
+    A = _setup(wls)
+    B = _setup(wls)
+    E = gpu.MicEnsemble(A)
+    dts = np.array([wl.dt for wl in wls])
+
+    def compare():
+        E.synchronize()
+        for a, b in zip(A, B):
+            assert a.n == b.n
+            assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
+            for f in ("rho", "etaN", "etaS", "lastT"):
+                assert np.array_equal(a.get_nodal(f), b.get_nodal(f)), f
+
+    for step in range(4):
+        E.step(dts, dts, subgrid_stress=1, graph=graph)
+        for b, dt in zip(B, dts):
+            b.step(dt, dt, True)
+        if step in (0, 3):
+            compare()
+    # new time steps and a changed member force a fresh capture
+    dts = dts * 0.75
+    A[1].wl.materials.QonR[0] *= 1.5
+    for P in (A[1], B[1]):
+        P._check(P.L.mic_set_materials(P.h, gpu.ctypes.byref(A[1].wl.materials)), "mic_set_materials")
+    for step in range(3):
+        E.step(dts, dts, subgrid_stress=1, graph=graph)
+        for b, dt in zip(B, dts):
+            b.step(dt, dt, True)
+    compare()
+    launches, per_graph = E.launch_count()
+    assert launches > 0
+    if graph:
+        assert per_graph >= 25 * len(A)
+    E.close()

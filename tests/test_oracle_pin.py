@@ -207,3 +207,38 @@ def test_goldsby_kohlstedt_matches_reference_build():
     P = 1e8 * u[3::4]
     ok, msg = exact(oraclepy.gk_viscosity(s, T, d, P), refpy.goldsby_kohlstedt(s, T, d, P))
     assert ok, msg
+
+
+def _lifecycle_grid(z, tag):
+    x, y = z[tag + "_x"], z[tag + "_y"]
+    LX, LY = z[tag + "_L"]
+    return W.Grid(len(x), len(y), float(LX), float(LY), x, y)
+
+
+def test_marker_lifecycle_matches_golden():
+    """resetMarkers + distributeMarkersUniformInDomain restated in the oracle: every byte of the
+    reference's marker array (capacity included) and its marker count."""
+    z = np.load(os.path.join(GOLDEN, "marker_lifecycle.npz"))
+    for tag in ("uniform", "refined"):
+        g = _lifecycle_grid(z, tag)
+        wl = W.Workload("lifecycle", g, np.zeros(0, dtype=MARKER_DTYPE), Materials(), Options(), BCs(), {},
+                        1.0, 1.0, 1)
+        O = oraclepy.OracleProblem(wl)
+        for NMX, NMY in ((4, 4), (3, 5)):
+            key = "%s_%dx%d" % (tag, NMX, NMY)
+            ref = z[key + "_markers"]
+            mk, n = O.distribute_uniform(NMX, NMY, seed=0, cap=len(ref))
+            assert n == int(z[key + "_n"])
+            assert np.array_equal(mk.view(np.uint8).reshape(len(mk), -1), ref), key
+
+
+@needs_ref
+def test_marker_lifecycle_matches_reference_build():
+    for wl in (W.convection_box(ncell=8, nm=4, seed=1), W.vep_slab_box(nx_cells=32, ny_cells=8, nm=4, seed=2)):
+        R = refpy.RefProblem(wl)
+        O = oraclepy.OracleProblem(wl)
+        for NMX, NMY in ((4, 4), (2, 7), (5, 3)):
+            mr, nr = R.distribute_uniform(NMX, NMY)
+            mo, no = O.distribute_uniform(NMX, NMY, seed=0, cap=len(mr))
+            assert nr == no
+            assert np.array_equal(mr.view(np.uint8), mo.view(np.uint8))
