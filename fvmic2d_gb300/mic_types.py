@@ -109,3 +109,12 @@ NF_COUNT = len(NF)
 PROJECTED_FIELDS = ["rho", "rhodot", "etaN", "etaS", "muS", "muN", "kThermal", "lastT", "Cp", "soxx", "soyy", "soxy"]
 
 ARITHMETIC, ARITHMETIC_LOCAL, HARMONIC = 0, 1, 2
+
+
+class DensityOptions(ctypes.Structure):
+    """mic_density_options: checkMarkerDensity settings (markers per cell at set-up, per
+    quarter-cell bounds) and the subduction-benchmark parameters of the inflow markers it makes."""
+    _fields_ = [("NMX", ctypes.c_int32), ("NMY", ctypes.c_int32), ("minMarkers", ctypes.c_int32),
+                ("maxMarkers", ctypes.c_int32), ("slabAngle", ctypes.c_double), ("slabAge", ctypes.c_double),
+                ("overridingPlateThickness", ctypes.c_double), ("rootThickness", ctypes.c_double),
+                ("rootCenter", ctypes.c_double), ("rootWidth", ctypes.c_double)]

@@ -414,6 +414,53 @@ def convection_ensemble(n_members=64, seed=4):
     return members
 
 
+def density_case(nx_cells=32, ny_cells=8, seed=6):
+    """A marker set for checkMarkerDensity (markers.c:455-781): the refined VEP box at 4x4
+    markers per cell (4 per quarter cell) with quarter cells emptied (including some in the first
+    cell column, where the reference creates slab-inflow markers, and in the last column below
+    the overriding plate, where it creates mantle-inflow markers) and quarter cells overfilled
+    with markers moved in from elsewhere.  Returns (workload, density options) for
+    minMarkers = 1 (the reference default), maxMarkers = 6 and NMX = NMY = 8 (its quarter-cell
+    target ceil(NMX (NX-1)/2 dx/LX) with dx half a cell width is NMX/4 per axis)."""
+    from .mic_types import DensityOptions
+
+    wl = vep_slab_box(nx_cells=nx_cells, ny_cells=ny_cells, nm=4, seed=seed)
+    g, m = wl.grid, wl.markers
+    u = splitmix64_uniform(seed + 100, 4096)
+    xc = cell_centers(g.x, g.LX)
+    yc = cell_centers(g.y, g.LY)
+
+    def quarter(i, j):  # bounds of basic quarter cell (i, j) as the reference computes them
+        xmin = g.x[i // 2] if i % 2 == 0 else xc[(i + 1) // 2]
+        xmax = xc[i // 2 + 1] if i % 2 == 0 else g.x[(i + 1) // 2]
+        ymin = g.y[j // 2] if j % 2 == 0 else yc[(j + 1) // 2]
+        ymax = yc[j // 2 + 1] if j % 2 == 0 else g.y[(j + 1) // 2]
+        return xmin, xmax, ymin, ymax
+
+    def inside(b):
+        return (m["X"] >= b[0]) & (m["X"] < b[1]) & (m["Y"] >= b[2]) & (m["Y"] < b[3])
+
+    nqx, nqy = 2 * nx_cells, 2 * ny_cells
+    empty = [(0, 1), (1, nqy - 2), (5, 3), (nqx - 1, nqy - 1), (nqx - 2, nqy - 3), (nqx // 2, nqy // 2),
+             (nqx // 2 + 1, nqy // 2)]
+    for (i, j) in empty:
+        m["X"][inside(quarter(i, j))] = -1.0  # leave the domain: out-of-domain markers
+    full = [(3, 4), (nqx // 3, 2), (nqx - 5, nqy // 2 + 1)]
+    donors = np.flatnonzero(m["X"] > 0)[::7]
+    k = 0
+    for n_extra, (i, j) in zip((5, 9, 3), full):
+        b = quarter(i, j)
+        for e in range(n_extra):
+            d = donors[k]
+            m["X"][d] = b[0] + (b[1] - b[0]) * (0.05 + 0.9 * u[2 * k])
+            m["Y"][d] = b[2] + (b[3] - b[2]) * (0.05 + 0.9 * u[2 * k + 1])
+            k += 1
+    dopt = DensityOptions(NMX=8, NMY=8, minMarkers=1, maxMarkers=6, slabAngle=0.5, slabAge=50.0,
+                          overridingPlateThickness=0.3 * g.LY, rootThickness=0.05 * g.LY, rootCenter=0.9 * g.LX,
+                          rootWidth=0.2 * g.LX)
+    return wl, dopt
+
+
 WORKLOADS = {
     "convection_box": convection_box,
     "vep_slab_box": vep_slab_box,

@@ -46,6 +46,16 @@ typedef struct {
   int32_t isYielding;
 } mic_marker;
 
+/* Marker density control settings (fdcode.h:158-159, 193-204 Options fields read by
+ * checkMarkerDensity and by the inflow markers it creates, benchmarkInitialConditions.c). */
+typedef struct {
+  int32_t NMX, NMY;               /* markers per cell at set-up */
+  int32_t minMarkers, maxMarkers; /* per basic quarter cell */
+  double slabAngle;               /* radians */
+  double slabAge;                 /* Myr */
+  double overridingPlateThickness, rootThickness, rootCenter, rootWidth;
+} mic_density_options;
+
 /* Material table; same layout as fdcode.h:74-95. */
 typedef struct {
   int32_t nMaterials;

@@ -1054,3 +1054,213 @@ int64_t orc_distribute_uniform(const orc_ctx *c, mic_marker *mk, int64_t cap, in
   }
   return idx;
 }
+
+/* ---- marker density control: checkMarkerDensity (markers.c:455-781) ------------------- */
+
+/* the C library's drand48 recurrence on an explicit state (the stream the reference's
+ * drand48() calls and its PETSCRAND48 object share) */
+static double orc_drand48(uint64_t *state) {
+  *state = (0x5DEECE66DULL * *state + 0xBULL) & 0xFFFFFFFFFFFFULL;
+  return (double)*state / 281474976710656.0;
+}
+
+uint64_t orc_srand48_state(long seed) { return ((uint64_t)(seed & 0xFFFFFFFFL) << 16) | 0x330EULL; }
+
+/* benchmarkInitialConditions.c:80-91, 124-134, 72-75 */
+static double orc_plate_depth(double x, const mic_density_options *d) {
+  if (fabs(x - d->rootCenter) < d->rootWidth)
+    return d->overridingPlateThickness + d->rootThickness * pow(cos(M_PI * (x - d->rootCenter) / d->rootWidth / 2.0), 2.0);
+  return d->overridingPlateThickness;
+}
+static double orc_slab_inflow_temperature(double x, double y, double angle, double age) {
+  const double Ts = 273, T0 = 1623, kappa = 0.7272e-6, s_in_year = 3.15576e7;
+  const double slab_age_s = age * 1.0e6 * s_in_year;
+  return Ts + (T0 - Ts) * erf((y - x * tan(angle)) / (2.0 * sqrt(kappa * slab_age_s)));
+}
+
+/* new_slab_marker / new_inflow_marker (benchmarkInitialConditions.c:44-66) + findMarkerCell;
+ * the reference leaves cpu and strainRateResidual of such markers uninitialised: 0 here */
+static void orc_new_inflow_marker(const orc_ctx *c, mic_marker *p, double x, double y, double T) {
+  memset(p, 0, sizeof(*p));
+  orc_reset_markers(p, 1);
+  p->X = x;
+  p->Y = y;
+  p->Mat = 0;
+  p->T = T;
+  double eta, mu;
+  orc_compute_rheology(c, p, &eta, &mu);
+  p->eta = eta;
+  p->mu = mu;
+  if (p->X >= 0.0 && p->Y >= 0.0 && p->X <= c->LX && p->Y <= c->LY) {
+    p->cellX = bisect_cell(c->x, c->NX, p->X);
+    p->cellY = bisect_cell(c->y, c->NY, p->Y);
+  } else {
+    p->cellX = p->cellY = -1;
+  }
+}
+
+/* Returns the new marker count, or -1 where the reference aborts (a quarter cell that would
+ * get a non-positive number of markers; more markers than cap), -2 for a removal from a
+ * quarter cell with no marker inside its bounds.  *state is the drand48 stream. */
+int64_t orc_check_marker_density(orc_ctx *c, mic_marker *mk, int64_t n, int64_t cap, const mic_density_options *d,
+                                 uint64_t *state, int64_t *n_added, int64_t *n_removed) {
+  const int NX = c->NX, NY = c->NY, m = NX - 1, nn = NY - 1;
+  const int nq = 4 * m * nn;
+  const int64_t nMark = n;
+  int64_t *cnt = (int64_t *)calloc((size_t)nq, sizeof(int64_t));
+  int64_t *isout = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
+  int64_t nOut = 0, ret = 0;
+  *n_added = *n_removed = 0;
+  for (int64_t m1 = 0; m1 < n; ++m1) {
+    if (mk[m1].cellX != -1) {
+      int cx = mk[m1].cellX, cy = mk[m1].cellY;
+      cx = 2 * cx + (mk[m1].X >= c->xc[cx + 1] ? 1 : 0);
+      cy = 2 * cy + (mk[m1].Y >= c->yc[cy + 1] ? 1 : 0);
+      cnt[cx + cy * 2 * m] += 1;
+    } else {
+      isout[nOut++] = m1;
+    }
+  }
+  int64_t maxQC = 0;
+  for (int q = 0; q < nq; ++q)
+    if (cnt[q] > maxQC) maxQC = cnt[q];
+  int64_t nAdd = 0, nRemove = 0;
+  for (int j = 0; j < 2 * nn; ++j) {
+    for (int i = 0; i < 2 * m; ++i) {
+      const int q = i + 2 * m * j;
+      if (cnt[q] < d->minMarkers) {
+        double dy = c->y[j / 2 + 1] - c->y[j / 2];
+        double dx = c->x[i / 2 + 1] - c->x[i / 2];
+        dx /= 2.0;
+        dy /= 2.0;
+        const int64_t mynmx = (int64_t)ceil(d->NMX * (NX - 1) / 2.0 * dx / c->LX);
+        const int64_t mynmy = (int64_t)ceil(d->NMY * (NY - 1) / 2.0 * dy / c->LY);
+        const int64_t mynadd = mynmx * mynmy - cnt[q];
+        if (mynadd <= 0) {
+          ret = -1;
+          goto done;
+        }
+        nAdd += mynadd;
+        cnt[q] = mynadd;
+      } else if (cnt[q] > d->maxMarkers) {
+        const int64_t t = cnt[q] - d->maxMarkers;
+        nRemove += t;
+        cnt[q] = -t;
+      } else {
+        cnt[q] = 0;
+      }
+    }
+  }
+  if (nRemove > 0) {
+    int64_t *idx = (int64_t *)malloc(sizeof(int64_t) * (size_t)(maxQC + 1));
+    double *rnd = (double *)malloc(sizeof(double) * (size_t)(maxQC + 1));
+    isout = (int64_t *)realloc(isout, sizeof(int64_t) * (size_t)(n + nRemove + 1));
+    for (int j = 0; j < 2 * nn && ret == 0; ++j) {
+      const double ymin = !(j % 2) ? c->y[j / 2] : c->yc[(j + 1) / 2];
+      const double ymax = !(j % 2) ? c->yc[j / 2 + 1] : c->y[(j + 1) / 2];
+      for (int i = 0; i < 2 * m; ++i) {
+        const double xmin = !(i % 2) ? c->x[i / 2] : c->xc[(i + 1) / 2];
+        const double xmax = !(i % 2) ? c->xc[i / 2 + 1] : c->x[(i + 1) / 2];
+        const int q = 2 * m * j + i;
+        if (cnt[q] >= 0) continue;
+        const int64_t toRemove = -cnt[q];
+        int64_t nCell = 0;
+        for (int64_t im = 0; im < n; ++im)
+          if (mk[im].X >= xmin && mk[im].X < xmax && mk[im].Y >= ymin && mk[im].Y < ymax) {
+            if (nCell > maxQC) break;
+            idx[nCell++] = im;
+          }
+        if (nCell == 0 || nCell > maxQC) {
+          ret = -2;
+          break;
+        }
+        for (int64_t k = 0; k < nCell; ++k) rnd[k] = orc_drand48(state);
+        for (int64_t r = 0; r < toRemove; ++r) {
+          double minv = 1.0;
+          int64_t minidx = 0;
+          for (int64_t k = 0; k < nCell; ++k)
+            if (rnd[k] < minv) {
+              minv = rnd[k];
+              minidx = k;
+            }
+          rnd[minidx] = 1.0;
+          mic_marker *p = &mk[idx[minidx]];
+          p->X = -1.0;
+          p->Y = -1.0;
+          p->cellX = -1;
+          p->cellY = -1;
+          isout[nOut++] = idx[minidx];
+        }
+      }
+    }
+    free(idx);
+    free(rnd);
+    if (ret) goto done;
+    *n_removed = nRemove;
+  }
+  if (nAdd > 0 && (nAdd + n - nOut) < cap) {
+    double *nx = (double *)malloc(sizeof(double) * (size_t)nAdd), *ny = (double *)malloc(sizeof(double) * (size_t)nAdd);
+    int64_t iMark = 0;
+    for (int j = 0; j < 2 * nn; ++j) {
+      for (int i = 0; i < 2 * m; ++i) {
+        const int q = 2 * m * j + i;
+        for (int64_t k = 0; k < cnt[q]; ++k) {
+          const double xlo = !(i % 2) ? c->x[i / 2] : c->xc[(i + 1) / 2];
+          const double xhi = !(i % 2) ? c->xc[i / 2 + 1] : c->x[(i + 1) / 2];
+          nx[iMark] = xlo + (xhi - xlo) * orc_drand48(state);
+          const double ylo = !(j % 2) ? c->y[j / 2] : c->yc[(j + 1) / 2];
+          const double yhi = !(j % 2) ? c->yc[j / 2 + 1] : c->y[(j + 1) / 2];
+          ny[iMark] = ylo + (yhi - ylo) * orc_drand48(state);
+          ++iMark;
+        }
+      }
+    }
+    for (int64_t a = 0; a < nAdd; ++a) {
+      int64_t id;
+      if (nOut > 0) {
+        id = isout[nOut - 1];
+        nOut--;
+      } else {
+        id = n;
+        n++;
+      }
+      if (nx[a] < c->x[1]) {
+        orc_new_inflow_marker(c, &mk[id], nx[a], ny[a], orc_slab_inflow_temperature(nx[a], ny[a], d->slabAngle, d->slabAge));
+      } else if (nx[a] >= c->x[NX - 2] && ny[a] >= orc_plate_depth(c->LX, d)) {
+        orc_new_inflow_marker(c, &mk[id], nx[a], ny[a], 1573.0);
+      } else {
+        double mindist = c->LX * c->LY;
+        int64_t minidx = -1;
+        for (int64_t m1 = 0; m1 < nMark; ++m1) {
+          if (m1 != id && mk[m1].cellX != -1) {
+            if (fabs(mk[m1].X - nx[a]) <= (c->x[mk[m1].cellX + 1] - c->x[mk[m1].cellX]) &&
+                fabs(mk[m1].Y - ny[a]) <= (c->y[mk[m1].cellY + 1] - c->y[mk[m1].cellY])) {
+              const double x1 = mk[m1].X - nx[a], y1 = mk[m1].Y - ny[a];
+              const double r1 = sqrt(x1 * x1 + y1 * y1);
+              if (r1 < mindist) {
+                mindist = r1;
+                minidx = m1;
+              }
+            }
+          }
+        }
+        if (minidx != -1) {
+          mk[id] = mk[minidx];
+          mk[id].X = nx[a];
+          mk[id].Y = ny[a];
+        }
+      }
+    }
+    free(nx);
+    free(ny);
+    *n_added = nAdd;
+  } else if ((nAdd + n - nOut) > cap) {
+    ret = -1;
+    goto done;
+  }
+  ret = n;
+done:
+  free(cnt);
+  free(isout);
+  return ret;
+}

@@ -84,6 +84,12 @@ int orc_creep_stress(double edot, double T, double d, double P, double rtol, dou
 void orc_reset_markers(mic_marker *mk, int64_t n);
 int64_t orc_distribute_uniform(const orc_ctx *c, mic_marker *mk, int64_t cap, int NMX, int NMY, unsigned long seed);
 
+/* checkMarkerDensity (markers.c:455-781) on an array of capacity cap; *state is the 48-bit
+ * drand48 stream (orc_srand48_state(seed) = srand48(seed)) */
+uint64_t orc_srand48_state(long seed);
+int64_t orc_check_marker_density(orc_ctx *c, mic_marker *mk, int64_t n, int64_t cap, const mic_density_options *d,
+                                 uint64_t *state, int64_t *n_added, int64_t *n_removed);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,9 @@ def lib():
             "orc_gk_strain_rate": (_D, [_D, _D, _D, _D]),
             "orc_creep_stress": (_I, [_D, _D, _D, _D, _D, _DP, _IP]),
             "orc_reset_markers": (None, [_P, _I64]),
+            "orc_srand48_state": (ctypes.c_uint64, [ctypes.c_long]),
+            "orc_check_marker_density": (_I64, [_P, _P, _I64, _I64, _P, ctypes.POINTER(ctypes.c_uint64), _I64P,
+                                                 _I64P]),
             "orc_distribute_uniform": (_I64, [_P, _P, _I64, _I, _I, ctypes.c_ulong]),
         }
         for name, (res, args) in sig.items():
@@ -117,6 +120,21 @@ class OracleProblem:
             raise ValueError("capacity exceeded")
         self.markers = mk[:n].copy()
         return mk, n
+
+    def checkMarkerDensity(self, dopt, cap, state=None, seed=1):
+        """checkMarkerDensity on a copy of the markers grown to capacity cap; returns
+        (markers[:n_new], n_added, n_removed, rng state after)."""
+        L = lib()
+        mk = np.zeros(cap, dtype=MARKER_DTYPE)
+        mk[:len(self.markers)] = self.markers
+        st = ctypes.c_uint64(L.orc_srand48_state(seed) if state is None else state)
+        na, nr = ctypes.c_int64(0), ctypes.c_int64(0)
+        n = L.orc_check_marker_density(self.h, mk.ctypes.data, len(self.markers), cap, ctypes.byref(dopt),
+                                       ctypes.byref(st), ctypes.byref(na), ctypes.byref(nr))
+        if n < 0:
+            raise RuntimeError("orc_check_marker_density failed with %d" % n)
+        self.markers = mk[:n].copy()
+        return self.markers, na.value, nr.value, st.value
 
     def grid_centres(self):
         xc = np.empty(self.NX + 1)

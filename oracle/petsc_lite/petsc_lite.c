@@ -2,6 +2,8 @@
  * in include/petsc_lite.h.  TEST INFRASTRUCTURE ONLY (oracle pinning). */
 #include "petsc_lite.h"
 #include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
 #include <time.h>
 
 struct _p_DM {
@@ -249,10 +251,17 @@ PetscErrorCode PetscSynchronizedPrintf(MPI_Comm c, const char *fmt, ...) {
 }
 PetscErrorCode PetscSynchronizedFlush(MPI_Comm c, ...) { (void)c; return 0; }
 
-/* ---- random numbers: drand48-style uniform on [lo, hi) ---- */
+/* ---- random numbers ----
+ * PETSCRAND48 objects draw from the C library's global drand48 stream, which PetscRandomSeed
+ * seeds with srand48(seed) -- the documented behaviour of PETSc's rand48 type; the reference's
+ * own drand48() calls (markers.c:651) share that stream.  Every other type gets a private
+ * erand48 stream whose 48-bit state PetscRandomSetSeed sets to (seed << 16) | 0x330E.  Values
+ * are lo + (hi - lo) * u with u uniform on [0, 1). */
 struct _p_PetscRandom {
   double lo, hi;
   unsigned short state[3];
+  unsigned long seed;
+  int rand48;
 };
 
 PetscErrorCode PetscRandomCreate(MPI_Comm c, PetscRandom *r) {
@@ -263,21 +272,29 @@ PetscErrorCode PetscRandomCreate(MPI_Comm c, PetscRandom *r) {
   (*r)->hi = 1.0;
   return 0;
 }
-PetscErrorCode PetscRandomSetType(PetscRandom r, PetscRandomType t) { (void)r; (void)t; return 0; }
+PetscErrorCode PetscRandomSetType(PetscRandom r, PetscRandomType t) {
+  r->rand48 = t && strcmp(t, PETSCRAND48) == 0;
+  return 0;
+}
 PetscErrorCode PetscRandomSetSeed(PetscRandom r, unsigned long seed) {
+  r->seed = seed;
   r->state[0] = 0x330E;
   r->state[1] = (unsigned short)(seed & 0xFFFF);
   r->state[2] = (unsigned short)((seed >> 16) & 0xFFFF);
   return 0;
 }
-PetscErrorCode PetscRandomSeed(PetscRandom r) { (void)r; return 0; }
+PetscErrorCode PetscRandomSeed(PetscRandom r) {
+  if (r->rand48) srand48((long)r->seed);
+  return 0;
+}
 PetscErrorCode PetscRandomSetInterval(PetscRandom r, PetscScalar lo, PetscScalar hi) {
   r->lo = lo;
   r->hi = hi;
   return 0;
 }
 PetscErrorCode PetscRandomGetValue(PetscRandom r, PetscScalar *v) {
-  *v = r->lo + (r->hi - r->lo) * erand48(r->state);
+  const double u = r->rand48 ? drand48() : erand48(r->state);
+  *v = r->lo + (r->hi - r->lo) * u;
   return 0;
 }
 PetscErrorCode PetscRandomDestroy(PetscRandom *r) {

@@ -282,3 +282,46 @@ int ref_distributeMarkersUniformInDomain(refp *p, mic_marker *m, int cap, int NM
   if (distributeMarkersUniformInDomain(&p->ms, &p->opt, &p->grid)) return -1;
   return p->ms.nMark;
 }
+
+/* checkMarkerDensity (markers.c:455-781) on the caller's marker array (capacity cap, nMark
+ * markers, cells current).  The PETSc random object is the reference's (PETSCRAND48, seeded
+ * with srand48(seed) before the call when seed >= 0; seed < 0 continues the current global
+ * drand48 stream).  Returns the new nMark; *rng_state receives the drand48 state afterwards. */
+int ref_checkMarkerDensity(refp *p, mic_marker *m, int n, int cap, int NMX, int NMY, int minMarkers,
+                           int maxMarkers, const double *slab, long seed, unsigned short *rng_state) {
+  p->ms.markers = (Marker *)m;
+  p->ms.nMark = n;
+  p->ms.maxMark = cap;
+  p->opt.NMX = NMX;
+  p->opt.NMY = NMY;
+  p->opt.minMarkers = minMarkers;
+  p->opt.maxMarkers = maxMarkers;
+  /* slab: slabAngle, slabAge, overridingPlateThickness, rootThickness, rootCenter, rootWidth */
+  p->opt.slabAngle = slab[0];
+  p->opt.slabAge = slab[1];
+  p->opt.overridingPlateThickness = slab[2];
+  p->opt.rootThickness = slab[3];
+  p->opt.rootCenter = slab[4];
+  p->opt.rootWidth = slab[5];
+  static Problem prob;
+  memset(&prob, 0, sizeof(prob));
+  prob.materials = p->mat;
+  PetscRandom r;
+  PetscRandomCreate(PETSC_COMM_WORLD, &r);
+  PetscRandomSetType(r, PETSCRAND48);
+  if (seed >= 0) {
+    PetscRandomSetSeed(r, (unsigned long)seed);
+    PetscRandomSeed(r);
+  }
+  int e = checkMarkerDensity(&prob, &p->ms, &p->grid, &p->opt, r);
+  PetscRandomDestroy(&r);
+  if (rng_state) {
+    unsigned short *st = seed48((unsigned short[3]){0, 0, 0}); /* read the state back ... */
+    rng_state[0] = st[0];
+    rng_state[1] = st[1];
+    rng_state[2] = st[2];
+    seed48(rng_state); /* ... and restore it */
+  }
+  if (e) return -1;
+  return p->ms.nMark;
+}

@@ -59,6 +59,8 @@ def lib():
             "ref_goldsbyKohlstedt": (_D, [_D, _D, _D, _D]),
             "ref_goldsbyKohlstedt_many": (None, [_DP, _DP, _DP, _DP, _DP, _I]),
             "ref_resetMarkers": (_I, [_P, _P, _I]),
+            "ref_checkMarkerDensity": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _DP, ctypes.c_long,
+                                            ctypes.POINTER(ctypes.c_ushort)]),
             "ref_distributeMarkersUniformInDomain": (_I, [_P, _P, _I, _I, _I]),
             "ref_stage_seconds": (_D, [_I]),
             "ref_stage_reset": (None, []),
@@ -95,6 +97,25 @@ class RefProblem:
         L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         for name, arr in wl.nodal.items():
             self.set_nodal(name, arr)
+
+    def checkMarkerDensity(self, dopt, cap, seed=1):
+        """The reference's checkMarkerDensity (PETSCRAND48 object seeded with srand48(seed)) on a
+        copy of the markers grown to capacity cap; returns (markers[:n_new], 48-bit state)."""
+        L = lib()
+        mk = np.zeros(cap, dtype=self.markers.dtype)
+        mk[:len(self.markers)] = self.markers
+        slab = np.array([dopt.slabAngle, dopt.slabAge, dopt.overridingPlateThickness, dopt.rootThickness,
+                         dopt.rootCenter, dopt.rootWidth])
+        st = (ctypes.c_ushort * 3)()
+        n = L.ref_checkMarkerDensity(self.h, mk.ctypes.data, len(self.markers), cap, dopt.NMX, dopt.NMY,
+                                     dopt.minMarkers, dopt.maxMarkers, _dp(slab), seed, st)
+        L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        if n < 0:
+            raise RuntimeError("checkMarkerDensity failed")
+        self.markers = mk[:n].copy()
+        L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        state = int(st[0]) | (int(st[1]) << 16) | (int(st[2]) << 32)
+        return self.markers, state
 
     def distribute_uniform(self, NMX, NMY, cap=None):
         """The reference's resetMarkers + distributeMarkersUniformInDomain (seed 0)."""

@@ -159,19 +159,64 @@ def lifecycle_table():
         for NMX, NMY in ((4, 4), (3, 5)):
             mk, n = R.distribute_uniform(NMX, NMY)
             key = "%s_%dx%d" % (tag, NMX, NMY)
-            out[key + "_markers"] = mk.view(np.uint8).reshape(len(mk), -1)
+            out[key + "_markers"] = _fields_only(mk).view(np.uint8).reshape(len(mk), -1)
             out[key + "_n"] = np.int64(n)
         out[tag + "_x"], out[tag + "_y"] = wl.grid.x, wl.grid.y
         out[tag + "_L"] = np.array([wl.grid.LX, wl.grid.LY])
     return out
 
 
+def _fields_only(a):
+    """the same markers with padding bytes zeroed (numpy leaves them arbitrary on copies)"""
+    out = np.zeros(len(a), dtype=a.dtype)
+    for f in a.dtype.names:
+        out[f] = a[f]
+    return out
+
+
+def density_table():
+    """checkMarkerDensity (markers.c:455-781) on the density case at two seeds: markers before
+    (cells current) and after, capacity, and the drand48 state after.  The reference leaves cpu
+    and strainRateResidual of the inflow markers it creates uninitialised; they are zeroed here."""
+    out = {}
+    for seed in (1, 77):
+        wl, dopt = W.density_case()
+        R = refpy.RefProblem(wl)
+        R.findMarkerCells()
+        before = R.markers.copy()
+        cap = len(before) + 400
+        after, state = R.checkMarkerDensity(dopt, cap, seed=seed)
+        new = np.ones(len(after), dtype=bool)
+        new[:len(before)] = ~np.all(after[:len(before)].view(np.uint8).reshape(len(before), -1) ==
+                                    before.view(np.uint8).reshape(len(before), -1), axis=1)
+        g, d = wl.grid, dopt
+        plate = d.overridingPlateThickness + (d.rootThickness * np.cos(np.pi * (g.LX - d.rootCenter) / d.rootWidth / 2) ** 2
+                                              if abs(g.LX - d.rootCenter) < d.rootWidth else 0.0)
+        special = new & ((after["X"] < g.x[1]) | ((after["X"] >= g.x[-2]) & (after["Y"] >= plate)))
+        after = after.copy()
+        after["cpu"][special] = 0
+        after["srr"][special] = 0.0
+        key = "seed%d" % seed
+        before, after = _fields_only(before), _fields_only(after)
+        out[key + "_before"] = before.view(np.uint8).reshape(len(before), -1)
+        out[key + "_after"] = after.view(np.uint8).reshape(len(after), -1)
+        out[key + "_special"] = special
+        out[key + "_cap"] = np.int64(cap)
+        out[key + "_state"] = np.uint64(state)
+    out["options_bytes"] = np.frombuffer(bytes(dopt), dtype=np.uint8)
+    return out
+
+
 def main():
     if obuild.build_ref() is None:
         raise SystemExit("reference tree not found; golden vectors can only be generated where it exists")
-    np.savez_compressed(os.path.join(OUT, "marker_lifecycle.npz"), **lifecycle_table())
-    print("wrote marker_lifecycle")
-    if sys.argv[1:] == ["lifecycle"]:
+    if sys.argv[1:] in ([], ["lifecycle"]):
+        np.savez_compressed(os.path.join(OUT, "marker_lifecycle.npz"), **lifecycle_table())
+        print("wrote marker_lifecycle")
+    if sys.argv[1:] in ([], ["density"]):
+        np.savez_compressed(os.path.join(OUT, "marker_density.npz"), **density_table())
+        print("wrote marker_density")
+    if sys.argv[1:]:
         return
     cases = {
         "convection_box_8": W.convection_box(ncell=8, nm=4, seed=1),

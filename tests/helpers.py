@@ -57,3 +57,15 @@ def compare_markers(got, want, fields=None, rtol=None, skip=()):
         if not ok:
             fails.append("%s: %s" % (f, msg))
     return fails
+
+
+def same_fields(a, b):
+    """Every field of two marker arrays bit-identical (padding ignored, NaN compared by bits)."""
+    if len(a) != len(b):
+        return False, "lengths %d vs %d" % (len(a), len(b))
+    for f in a.dtype.names:
+        x, y = np.ascontiguousarray(a[f]), np.ascontiguousarray(b[f])
+        if not np.array_equal(x.view(np.uint8), y.view(np.uint8)):
+            rows = np.flatnonzero(x != y)
+            return False, "field %s differs at %s" % (f, rows[:8])
+    return True, ""

@@ -16,7 +16,7 @@ import pytest
 from fvmic2d_gb300 import workloads as W
 from fvmic2d_gb300.mic_types import MARKER_DTYPE, PROJECTED_FIELDS, Materials, Options, BCs
 from oracle import oraclepy, refpy
-from tests.helpers import compare_markers, exact
+from tests.helpers import compare_markers, exact, same_fields
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["convection_box_8", "vep_slab_box_16x4", "edge_cases"]
@@ -229,7 +229,8 @@ def test_marker_lifecycle_matches_golden():
             ref = z[key + "_markers"]
             mk, n = O.distribute_uniform(NMX, NMY, seed=0, cap=len(ref))
             assert n == int(z[key + "_n"])
-            assert np.array_equal(mk.view(np.uint8).reshape(len(mk), -1), ref), key
+            ok, msg = same_fields(mk, ref.view(MARKER_DTYPE).ravel())
+            assert ok, (key, msg)
 
 
 @needs_ref
@@ -241,4 +242,47 @@ def test_marker_lifecycle_matches_reference_build():
             mr, nr = R.distribute_uniform(NMX, NMY)
             mo, no = O.distribute_uniform(NMX, NMY, seed=0, cap=len(mr))
             assert nr == no
-            assert np.array_equal(mr.view(np.uint8), mo.view(np.uint8))
+            ok, msg = same_fields(mr, mo)
+            assert ok, msg
+
+
+def _density_from_golden(z, seed):
+    from fvmic2d_gb300.mic_types import DensityOptions
+
+    wl, _ = W.density_case()
+    before = z["seed%d_before" % seed].view(MARKER_DTYPE).ravel()
+    dopt = DensityOptions.from_buffer_copy(z["options_bytes"].tobytes())
+    return wl, before, dopt
+
+
+@pytest.mark.parametrize("seed", [1, 77])
+def test_marker_density_matches_golden(seed):
+    """checkMarkerDensity restated: quarter-cell counts, drand48 removal, new positions, slot
+    recycling, nearest-neighbour copies and inflow markers -- byte for byte, and the stream
+    state afterwards."""
+    z = np.load(os.path.join(GOLDEN, "marker_density.npz"))
+    wl, before, dopt = _density_from_golden(z, seed)
+    O = oraclepy.OracleProblem(wl, markers=before)
+    after, n_added, n_removed, state = O.checkMarkerDensity(dopt, int(z["seed%d_cap" % seed]), seed=seed)
+    ref = z["seed%d_after" % seed].view(MARKER_DTYPE).ravel()
+    assert n_added > 0 and n_removed > 0
+    ok, msg = same_fields(after, ref)
+    assert ok, msg
+    assert state == int(z["seed%d_state" % seed])
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [3, 1234])
+def test_marker_density_matches_reference_build(seed):
+    wl, dopt = W.density_case(seed=seed % 50 + 6)
+    R = refpy.RefProblem(wl)
+    O = oraclepy.OracleProblem(wl)
+    R.findMarkerCells()
+    O.findMarkerCells()
+    cap = len(wl.markers) + 400
+    mr, sr = R.checkMarkerDensity(dopt, cap, seed=seed)
+    mo, _, _, so = O.checkMarkerDensity(dopt, cap, seed=seed)
+    assert len(mr) == len(mo) and sr == so
+    fields = [f for f in MARKER_DTYPE.names if f not in ("cpu", "srr")]
+    for f in fields:
+        assert np.array_equal(mr[f], mo[f]) or np.array_equal(np.isnan(mr[f]), np.isnan(mo[f])), f
