@@ -365,6 +365,18 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   return MIC_OK;
 }
 
+// exclusive prefix sum of data[0, len) in place; aux: mic_scan_aux_ints(len) ints of scratch
+int mic_scan_exclusive(mic_ctx *ctx, int *data, int64_t len, int *aux) { return scan_exclusive(ctx, data, len, aux); }
+
+int64_t mic_scan_aux_ints(int64_t len) {
+  int64_t aux = 0, l = len;
+  while (l > 1) {
+    l = (l + kScanBlock - 1) / kScanBlock;
+    aux += l + 1;
+  }
+  return aux + 16;
+}
+
 // Columns [0, n) back to the caller's marker order (slot k holds caller marker k); slots
 // [n, cap) keep their contents.  The next pass bins and sorts again.
 int mic_restore_caller_order(mic_ctx *ctx) {

@@ -22,6 +22,7 @@ extern "C" const char *mic_error_string(int code) {
     case MIC_ERR_BC: return "unsupported boundary condition";
     case MIC_ERR_CAPACITY: return "marker capacity exceeded";
     case MIC_ERR_NO_DEVICE: return "no CUDA device";
+    case MIC_ERR_DENSITY: return "marker density control cannot proceed";
     default: return "unknown error";
   }
 }
@@ -143,6 +144,8 @@ static void free_ctx(mic_ctx *ctx) {
   cudaFree(ctx->d_creep);
   cudaFree(ctx->mlp);
   cudaFree(ctx->train_buf);
+  cudaFree(ctx->dens_buf);
+  cudaFree(ctx->dens_add);
   cudaFree(ctx->stage_aos);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -315,6 +318,7 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
     for (int k = 0; k < 3; ++k) s->type[k] = 1;
   }
   ctx->mat.nMaterials = 1;
+  ctx->rng48 = (1ULL << 16) | 0x330EULL;  // srand48(1), the seed of the reference's main
   ctx->creep.mode = 0;
   ctx->creep.polish_iters = 3;
   ctx->creep.maxit = 60;
@@ -325,7 +329,7 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ctx->opt.etamax = 1e300;
   ctx->n = 0;
   ctx->sorted = 0;
-  if (cudaDeviceSynchronize() != cudaSuccess) {
+  if (cudaDeviceSynchronize() != cudaSuccess || mic_reset_markers(ctx) != MIC_OK) {  // allocateMarkers resets
     free_ctx(ctx);
     return MIC_ERR_CUDA;
   }
@@ -750,5 +754,11 @@ extern "C" int mic_markers_fill(mic_ctx *ctx, int field_offset, double value) {
   MIC_CUDA_TRY(cudaGetLastError());
   if (ic == C_CELLX || ic == C_CELLY || fc == C_X || fc == C_Y) mic_invalidate_sort(ctx);
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_marker_count(mic_ctx *ctx, int64_t *n) {
+  if (!ctx || !n) return MIC_ERR_ARG;
+  *n = ctx->n;
   return MIC_OK;
 }

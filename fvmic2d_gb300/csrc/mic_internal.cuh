@@ -88,6 +88,9 @@ struct mic_ctx {
   int64_t n, cap;
   int has_grain;  // per-marker grain sizes were set: the grain column moves with the sorts
   long long gen;  // bumped by every setter that changes what a step launches (captured graphs)
+  unsigned long long rng48;  // drand48 stream of marker density control (48-bit state)
+  void *dens_buf, *dens_add;  // density-control scratch (grown on demand)
+  size_t dens_bytes, dens_add_bytes;
   double *f64[mic::C_F64_COUNT];
   int *i32[mic::C_I32_COUNT];
   double *f64_alt[mic::C_F64_COUNT];
@@ -152,6 +155,9 @@ void mic_invalidate_sort(mic_ctx *ctx);
 int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out);
 int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry
 int mic_f64_column_of_offset(int byte_offset);
+// exclusive prefix sum in place on the context stream, and the scratch it needs (mic_bin_sort.cu)
+int mic_scan_exclusive(mic_ctx *ctx, int *data, int64_t len, int *aux);
+int64_t mic_scan_aux_ints(int64_t len);
 // columns [0, n) back to caller order, slots from n on kept (mic_bin_sort.cu)
 int mic_restore_caller_order(mic_ctx *ctx);
 // scatter a caller-order per-marker array into device (column) order through the id column

@@ -12,6 +12,7 @@
 #include "mic_creep.cuh"
 #include "mic_creep_tc.cuh"
 #include "mic_internal.cuh"
+#include "mic_rheology.cuh"
 
 using namespace mic;
 
@@ -55,63 +56,6 @@ __device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, i
   j = clampi(sy, 1, P.NY - 2);
   mdx = (i == sx) ? gx1 : div_sp(x - P.xc[i], P.hxc[i], P.ixc[i]);
   mdy = (j == sy) ? gy1 : div_sp(y - P.yc[j], P.hyc[j], P.iyc[j]);
-}
-
-// Inputs of the composite creep law (law 7): the marker's strain-rate invariant, grain size,
-// pressure and (surrogate modes) the network's ln s* guess; iteration count, residual and
-// fallback flag of its stress solve come back in it.
-struct CreepIn {
-  double e11, e22, e12, grain, p;
-  double u_guess;
-  int iters, fb;
-  double res;
-  int have_k;    // coefficients below already evaluated for this marker
-  CreepCoef k;
-};
-
-// Law 7 (new): composite ice creep, eta = s* / (2 edot_II) with s* the stress at which the
-// Goldsby-Kohlstedt strain rate (viscosity.c:106-179) equals the marker's strain-rate
-// invariant; at zero strain rate the law's diffusion viscosity 0.5 / C (viscosity.c:130-133).
-__device__ __forceinline__ double creep_viscosity(const CreepConfig &cfg, double T, CreepIn &ci) {
-  const double edot = sqrt(0.5 * (ci.e11 * ci.e11 + ci.e22 * ci.e22) + ci.e12 * ci.e12);
-  const CreepCoef k = ci.have_k ? ci.k : creep_coef(T, ci.grain, ci.p);
-  if (!(edot > 0.0)) return 0.5 / k.C;
-  const double s = (cfg.mode == 0) ? creep_stress_exact(k, edot, cfg.tol, cfg.maxit, &ci.iters, &ci.res)
-                                   : creep_stress_from_guess(k, edot, ci.u_guess, cfg.tol, cfg.maxit,
-                                                             cfg.polish_iters, cfg.polish_tol, &ci.iters, &ci.res,
-                                                             &ci.fb);
-  return s / (2.0 * edot);
-}
-
-// computeRheology (viscosity.c:12-67) plus law 7; returns false for an undefined law
-__device__ __forceinline__ bool rheology(const mic_materials &M, const mic_options &O, int k, double T, double X,
-                                         double Y, double &eta, double &mu, const CreepConfig *cfg = nullptr,
-                                         CreepIn *ci = nullptr) {
-  mu = M.materialMu[k];
-  switch (M.hasEtaT[k]) {
-    case 7:
-      if (!cfg || !ci) return false;
-      eta = creep_viscosity(*cfg, T, *ci);
-      return true;
-    case 1: eta = M.materialEta[k] * exp(M.QonR[k] * (1.0 / T - 1.0 / M.Tref[k])); return true;
-    case 2: {
-      const double T0 = M.Tref[k];
-      eta = M.materialEta[k] * exp(M.QonR[k] / T0 * (1.0 - (T - T0) / T0));
-      return true;
-    }
-    case 3: eta = M.materialEta[k] * T; return true;
-    case 5: eta = M.materialEta[k] * exp(-M.QonR[k] * T); return true;
-    case 0: eta = M.materialEta[k]; return true;
-    case 6: {
-      double e = M.materialEta[k];
-      const double edge = Y / tan(O.slabAngle);
-      if (X > edge && X < (edge + O.decoupleThickness) && Y > O.minDecoupleDepth && Y < O.maxDecoupleDepth)
-        e *= O.decoupleEtaScaler;
-      eta = e;
-      return true;
-    }
-    default: return false;
-  }
 }
 
 struct YieldCols {

@@ -78,6 +78,7 @@ SIGNATURES = {
     "mic_creep_mlp_infer": (_I, [_P, _P, _I64, _I, _P]),
     "mic_creep_stats": (_I, [_P, _I64P, _I64P, _I64P, _DP, _I64P]),
     "mic_reset_markers": (_I, [_P]),
+    "mic_marker_count": (_I, [_P, _I64P]),
     "mic_distribute_markers_uniform_in_domain": (_I, [_P, _I, _I, ctypes.c_ulong, _I64P]),
     "mic_markers_fill": (_I, [_P, _I, _D]),
     "mic_ensemble_create": (_I, [ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
@@ -86,6 +87,9 @@ SIGNATURES = {
     "mic_ensemble_synchronize": (_I, [_P]),
     "mic_ensemble_launch_count": (_I, [_P, _I64P, _I64P]),
     "mic_ensemble_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
+    "mic_check_marker_density": (_I, [_P, _P, _I64P, _I64P]),
+    "mic_density_seed": (_I, [_P, ctypes.c_long]),
+    "mic_density_rng_state": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -178,6 +182,27 @@ class MicProblem:
                     "mic_distribute_markers_uniform_in_domain")
         self.n = n.value
         return self.n
+
+    def checkMarkerDensity(self, dopt):
+        """markers.c:455-781 on the device; returns (n_added, n_removed)."""
+        a, r = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self.L.mic_check_marker_density(self.h, ctypes.byref(dopt), ctypes.byref(a), ctypes.byref(r)),
+                    "mic_check_marker_density")
+        self.n = self._count()
+        return a.value, r.value
+
+    def _count(self):
+        n = ctypes.c_int64(0)
+        self._check(self.L.mic_marker_count(self.h, ctypes.byref(n)), "mic_marker_count")
+        return n.value
+
+    def density_seed(self, seed):
+        self._check(self.L.mic_density_seed(self.h, seed), "mic_density_seed")
+
+    def density_state(self):
+        v = ctypes.c_uint64(0)
+        self._check(self.L.mic_density_rng_state(self.h, ctypes.byref(v), None), "mic_density_rng_state")
+        return v.value
 
     def fill(self, field, value):
         """Set one marker field (a MARKER_DTYPE name) to value on every marker."""

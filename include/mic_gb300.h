@@ -38,7 +38,10 @@ enum {
   MIC_ERR_LAW = 6,        /* undefined viscosity law; viscosity.c:60-62 aborts */
   MIC_ERR_BC = 7,         /* boundary type whose ghost values the path would read (periodic) */
   MIC_ERR_CAPACITY = 8,   /* more markers than the context was created for; markers.c:771-774 aborts */
-  MIC_ERR_NO_DEVICE = 9   /* no CUDA device: there is no CPU fallback */
+  MIC_ERR_NO_DEVICE = 9,  /* no CUDA device: there is no CPU fallback */
+  MIC_ERR_DENSITY = 10    /* density control: a quarter cell would get a non-positive number of
+                           * markers (markers.c:590-593 aborts), an overfull quarter cell with no
+                           * marker inside its bounds, or more than 2048 markers in one */
 };
 
 typedef struct {
@@ -185,6 +188,8 @@ int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64
  * kinematic, thermal, stress, strain and density fields 0; mu, cellX, cellY, cpu and the
  * strain-rate residual untouched).  The marker count is unchanged. */
 int mic_reset_markers(mic_ctx *ctx);
+/* current number of markers (MarkerSet.nMark) */
+int mic_marker_count(mic_ctx *ctx, int64_t *n);
 /* distributeMarkersUniformInDomain on one rank: NMX x NMY markers per basic cell of the
  * domain-wide lattice (mdx = LX / (NMX (NX-1)), marker k*nyl + l at x0 + mdx (0.5 + k) plus a
  * U(-mdx/4, mdx/4) jitter, likewise in y), jitter drawn in marker order from the 48-bit stream
@@ -194,6 +199,23 @@ int mic_distribute_markers_uniform_in_domain(mic_ctx *ctx, int NMX, int NMY, uns
 /* set one marker field, addressed as offsetof(mic_marker, field), to value for every marker
  * (integer fields take (int)value) -- the per-marker initial-condition loops of the host code */
 int mic_markers_fill(mic_ctx *ctx, int field_offset, double value);
+
+/* ---- marker density control ----
+ * checkMarkerDensity (markers.c:455-781): bins the markers if their positions changed (the
+ * findMarkerCells the reference calls first, main:247), counts markers per basic quarter cell,
+ * removes random markers (drand48) from quarter cells above maxMarkers, adds markers at random
+ * positions (the reference's PETSCRAND48 object, which shares the drand48 stream) to quarter
+ * cells below minMarkers, recycling out-of-domain slots last-in first-out before appending, and
+ * gives each new marker its nearest neighbour's properties -- or, left of x[1] and right of
+ * x[NX-2] below the overriding plate, those of a subduction inflow marker
+ * (benchmarkInitialConditions.c:44-66; cpu and strainRateResidual, which the reference leaves
+ * uninitialised there, are 0).  MIC_ERR_CAPACITY where the reference aborts on a full marker
+ * array.  The marker count changes; *n_added / *n_removed report what was done. */
+int mic_check_marker_density(mic_ctx *ctx, const mic_density_options *options, int64_t *n_added, int64_t *n_removed);
+/* the drand48 stream density control draws from: srand48(seed) (the reference seeds 1, the
+ * default), or read / replace the 48-bit state */
+int mic_density_seed(mic_ctx *ctx, long seed);
+int mic_density_rng_state(mic_ctx *ctx, uint64_t *get, const uint64_t *set);
 
 /* ---- ensembles ----
  * No counterpart in the reference (one problem per run).  Independent problems, each a context
