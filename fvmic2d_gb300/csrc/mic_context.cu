@@ -215,12 +215,20 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
     free_ctx(ctx);
     return MIC_ERR_CUDA;
   }
-  ALLOC(ctx->bits_buf, sizeof(long long) * (nx4 + ny4));
+  ALLOC(ctx->bits_buf, sizeof(long long) * 2 * (nx4 + ny4));
   {
-    long long *hb = (long long *)malloc(sizeof(long long) * (nx4 + ny4));
-    for (int i = 0; i < NX; ++i) memcpy(&hb[i], &hx[i], 8);
-    for (int j = 0; j < NY; ++j) memcpy(&hb[nx4 + j], &hy[j], 8);
-    cudaMemcpy(ctx->bits_buf, hb, sizeof(long long) * (nx4 + ny4), cudaMemcpyHostToDevice);
+    // raw bits of the (non-negative) grid lines; order-preserving images of the cell centres
+    auto ordered = [](double v) {
+      long long b;
+      memcpy(&b, &v, 8);
+      return b >= 0 ? b : (long long)(0x8000000000000000ULL) - b;
+    };
+    long long *hb = (long long *)calloc(2 * (nx4 + ny4), sizeof(long long));
+    for (int i = 0; i < NX; ++i) hb[i] = ordered(hx[i]);  // -0.0 -> bits of +0.0
+    for (int j = 0; j < NY; ++j) hb[nx4 + j] = ordered(hy[j]);
+    for (int i = 0; i <= NX; ++i) hb[nx4 + ny4 + i] = ordered(hxc[i]);
+    for (int j = 0; j <= NY; ++j) hb[2 * nx4 + ny4 + j] = ordered(hyc[j]);
+    cudaMemcpy(ctx->bits_buf, hb, sizeof(long long) * 2 * (nx4 + ny4), cudaMemcpyHostToDevice);
     free(hb);
   }
   ctx->P.NX = NX;
@@ -233,6 +241,8 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ctx->P.yc = ctx->grid_buf + 2 * nx4 + ny4 + 2;
   ctx->P.xbits = ctx->bits_buf;
   ctx->P.ybits = ctx->bits_buf + nx4;
+  ctx->P.xcbits = ctx->bits_buf + nx4 + ny4;
+  ctx->P.ycbits = ctx->bits_buf + 2 * nx4 + ny4;
   {
     // spacing tables: 8 arrays of nx4 / ny4 entries (hx, ix, hxc, ixc sized nx4; hy, iy, hyc, iyc ny4)
     const size_t tot = 4 * nx4 + 4 * ny4;

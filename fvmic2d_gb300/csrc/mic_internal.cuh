@@ -61,6 +61,7 @@ struct Params {  // everything a kernel needs besides the marker columns; passed
   double LX, LY;
   const double *x, *y, *xc, *yc;  // point at index 0 (ghost entries at -2, -1 exist)
   const long long *xbits, *ybits; // bit patterns of x[0..NX-1], y[0..NY-1] for integer compares
+  const long long *xcbits, *ycbits;  // ordered_bits of xc[0..NX], yc[0..NY] (xc[0], yc[0] < 0)
   // cell spacings h[i] = g[i+1] - g[i] (the reference's own differences) and their correctly
   // rounded reciprocals, for basic lines (i in [0, N-2]) and cell centres (i in [0, N-1])
   const double *hx, *ix, *hy, *iy, *hxc, *ixc, *hyc, *iyc;
@@ -190,6 +191,22 @@ __device__ __forceinline__ long long nonneg_bits(double v) {
 __device__ __forceinline__ long long ordered_bits(double v) {
   long long b = __double_as_longlong(v);
   return b >= 0 ? b : (long long)(0x8000000000000000ULL) - b;
+}
+
+// true for a NaN bit pattern (integer test: no FP64 instruction)
+__device__ __forceinline__ bool nan_bits(long long b) {
+  return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
+}
+
+// a / 6 from the correctly rounded reciprocal, corrected by one residual step (Markstein)
+__device__ __forceinline__ double div6(double a) {
+#ifdef MIC_EXACT
+  return a / 6;
+#else
+  const double inv6 = 0.16666666666666666;
+  const double q = a * inv6;
+  return fma(fma(-q, 6.0, a), inv6, q);
+#endif
 }
 
 // num / den for a grid-spacing divisor den whose correctly rounded reciprocal is inv.  The

@@ -545,31 +545,46 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
   double mvx[4], mvy[4], mwz[4];
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
+    // cell walk from the stored cell (markers.c:1928-1944) and the staggered-cell tests, all on
+    // order-preserving integer images of the coordinates: same decisions as the FP64 compares
+    // (a NaN coordinate compares false everywhere, as in the reference), none on the FP64 pipe
+    const long long bx = ordered_bits(xcur), by = ordered_bits(ycur);
+    const bool okx = !nan_bits(__double_as_longlong(xcur)), oky = !nan_bits(__double_as_longlong(ycur));
     int i = ci, j = cj;
-    if (xcur > P.x[i + 1]) {
-      while (xcur > P.x[i + 1] && i < NX - 2) i++;
-    } else if (xcur < P.x[i]) {
-      while (xcur < P.x[i] && i > 0) i--;
+    if (okx) {
+      if (bx > P.xbits[i + 1]) {
+        while (bx > P.xbits[i + 1] && i < NX - 2) i++;
+      } else if (bx < P.xbits[i]) {
+        while (bx < P.xbits[i] && i > 0) i--;
+      }
     }
-    if (ycur > P.y[j + 1]) {
-      while (ycur > P.y[j + 1] && j < NY - 2) j++;
-    } else if (ycur < P.y[j]) {
-      while (ycur < P.y[j] && j > 0) j--;
+    if (oky) {
+      if (by > P.ybits[j + 1]) {
+        while (by > P.ybits[j + 1] && j < NY - 2) j++;
+      } else if (by < P.ybits[j]) {
+        while (by < P.ybits[j] && j > 0) j--;
+      }
     }
     int vxX = i, vxY = j, vyX = i, vyY = j;
-    if (vxY > -1 && ycur < P.yc[vxY + 1]) vxY--;
-    if (vyX > -1 && xcur < P.xc[vyX + 1]) vyX--;
+    if (vxY > -1 && oky && by < P.ycbits[vxY + 1]) vxY--;
+    if (vyX > -1 && okx && bx < P.xcbits[vyX + 1]) vyX--;
     vxX = clampi(vxX, 0, NX - 2);
     vyX = clampi(vyX, -1, NX - 2);
     vxY = clampi(vxY, -1, NY - 2);
     vyY = clampi(vyY, 0, NY - 2);
+#ifndef MIC_EXACT
+    // vx sits on the basic x lines and vy on the basic y lines: with vxX == i and vyY == j (the
+    // walk keeps i, j inside the clamps) their fractions there are the basic cell's mdx, mdy
+    const double mdx = div_sp(xcur - P.x[i], P.hx[i], P.ix[i]);
+    const double mdy = div_sp(ycur - P.y[j], P.hy[j], P.iy[j]);
+#endif
     double ax = xcur - P.x[vxX];
     double ay = ycur - P.yc[vxY + 1];
 #ifdef MIC_EXACT
     double hx = P.x[vxX + 1] - P.x[vxX];
     double hy = P.yc[vxY + 2] - P.yc[vxY + 1];
 #else
-    const double tx = div_sp(ax, P.hx[vxX], P.ix[vxX]);
+    const double tx = mdx;
     const double ty = div_sp(ay, P.hyc[vxY + 1], P.iyc[vxY + 1]);
 #endif
     const size_t r1 = (size_t)(vxY + 1) * NX;
@@ -591,6 +606,7 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     t += vll * (1.0 - ax / hx) * (ay / hy);
     t += vlr * (ax * ay) / hx / hy;
 #else
+    (void)ax;
     double t = lerp2(vul, vur, vll, vlr, tx, ty);
 #endif
     mvx[s] = t;
@@ -607,9 +623,9 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
       wul = vy[q0 + vyX];
       wll = vy[q1 + vyX];
     }
+#ifdef MIC_EXACT
     ax = xcur - P.xc[vyX + 1];
     ay = ycur - P.y[vyY];
-#ifdef MIC_EXACT
     hx = P.xc[vyX + 2] - P.xc[vyX + 1];
     hy = P.y[vyY + 1] - P.y[vyY];
     t = wul * (1.0 - ax / hx) * (1.0 - ay / hy);
@@ -617,13 +633,13 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     t += wll * (1.0 - ax / hx) * (ay / hy);
     t += wlr * (ax * ay) / hx / hy;
 #else
-    t = lerp2(wul, wur, wll, wlr, div_sp(ax, P.hxc[vyX + 1], P.ixc[vyX + 1]), div_sp(ay, P.hy[vyY], P.iy[vyY]));
+    t = lerp2(wul, wur, wll, wlr, div_sp(xcur - P.xc[vyX + 1], P.hxc[vyX + 1], P.ixc[vyX + 1]), mdy);
 #endif
     mvy[s] = t;
-    const double mdx = div_sp(xcur - P.x[i], P.hx[i], P.ix[i]);
-    const double mdy = div_sp(ycur - P.y[j], P.hy[j], P.iy[j]);
     const size_t w0 = (size_t)j * NX + i;
 #ifdef MIC_EXACT
+    const double mdx = div_sp(xcur - P.x[i], P.hx[i], P.ix[i]);
+    const double mdy = div_sp(ycur - P.y[j], P.hy[j], P.iy[j]);
     t = (1.0 - mdx) * (1.0 - mdy) * wz[w0];
     t += (mdx) * (1.0 - mdy) * wz[w0 + 1];
     t += (1.0 - mdx) * (mdy)*wz[w0 + NX];
@@ -640,9 +656,9 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
       ycur = Y0 + dt * mvy[s];
     }
   }
-  const double VX = (mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]) / 6;
-  const double VY = (mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]) / 6;
-  const double w = (mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]) / 6.0;
+  const double VX = div6(mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]);
+  const double VY = div6(mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]);
+  const double w = div6(mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]);
   c.VX[m] = VX;
   c.VY[m] = VY;
   c.wxy[m] = w;
