@@ -66,6 +66,17 @@ KERNEL_BYTES = {
 }
 
 
+# DRAM bytes per marker of one launch from an ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum) of the 1,048,576-marker box, scaled to a full launch by markers
+# processed (profiles/k_advect_vep_slab_box_1m_full.md).  Reads match the algorithmic reads;
+# at the small size part of the written bytes is still in L2 when the kernel ends.
+KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (85691904 + 23738624) / 1048576}
+# FP64 flops per marker (DFMA counted twice) from the same capture: the kernels of this path
+# are bound by the FP64 pipe (2 DFMA per SM per clock on GB300), not by HBM.
+KERNEL_FP64_FLOPS_PER_MARKER = {"k_advect": 328.8}
+FP64_PEAK_TFLOPS = 2 * 2 * 152 * 2.07e9 / 1e12  # 2 DFMA/SM/clk x 2 flops x 152 SMs x 2.07 GHz
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -394,8 +405,17 @@ def run_ours(args):
                          "down every step through mic_nodal_upload/mic_step/mic_nodal_download"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_src,
-                     "algorithmic_bytes_per_launch": algo, "ms_per_launch": dur},
+                     "frac": achieved / hbm_peak,
+                     "traffic": (KERNEL_TRAFFIC_PER_MARKER[top_name] * n if top_name in KERNEL_TRAFFIC_PER_MARKER
+                                 else None),
+                     "traffic_note": "ncu dram bytes of the 1,048,576-marker case scaled by markers processed",
+                     "peak_source": peak_src, "algorithmic_bytes_per_launch": algo, "ms_per_launch": dur},
+        "fp64_roofline": ({"kernel": top_name, "flops_per_marker": KERNEL_FP64_FLOPS_PER_MARKER[top_name],
+                           "achieved": KERNEL_FP64_FLOPS_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e12,
+                           "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                           "frac": KERNEL_FP64_FLOPS_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
+                           "note": "the bound that applies: FP64 pipe, 2 DFMA/SM/clk; flops per marker from ncu"}
+                          if top_name in KERNEL_FP64_FLOPS_PER_MARKER else None),
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes, "achieved_gbs": step_gbs,
                           "frac": step_gbs / hbm_peak},
         "kernel_share": {k: round(v[0] / prof_total, 4) for k, v in kern[:12]},
