@@ -422,6 +422,7 @@ def run_ours(args):
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kern[:12]},
         "surrogate": surrogate_leg(args, local) if not args.no_surrogate else None,
         "ensemble": ensemble_leg(args, local) if not args.no_ensemble else None,
+        "ice_ensemble": ice_ensemble_leg(args, local) if not args.no_ensemble else None,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
@@ -544,6 +545,66 @@ def ensemble_leg(args, local):
         out[label] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
                       "kernels_per_step": (l1 - l0) / steps}
     out["speedup_graph_vs_sequential"] = out["graph"]["value"] / out["sequential"]["value"]
+    E.close()
+    for P in members:
+        P.close()
+    return out
+
+
+def ice_ensemble_leg(args, local):
+    """Mixed ensemble with the learned closure: 256 independent ice-creep VEP boxes (grids from
+    128^2 to 1024 x 256 cells, 16 markers per cell, law 7 with per-marker grain sizes,
+    Drucker-Prager yield), stepped as captured graphs with the exact creep solve and with the
+    tensor-core surrogate (one network trained once, shared by all members)."""
+    import torch
+
+    from fvmic2d_gb300 import gpu
+    from fvmic2d_gb300 import workloads as W
+
+    wls = W.ice_ensemble()
+    members = []
+    for wl in wls:
+        P = gpu.MicProblem(wl, device=local, capacity=wl.capacity)
+        gpu.initialize_markers(P, *wl.nm, seed=wl.seed)
+        P.set_grain_size(W.ice_grain_sizes(P.n, wl.seed))
+        members.append(P)
+    n_total = sum(P.n for P in members)
+    t0 = time.perf_counter()
+    members[0].creep_train()
+    train_s = time.perf_counter() - t0
+    params = members[0].creep_params()
+    for P in members[1:]:
+        P.creep_set_params(params)
+    E = gpu.MicEnsemble(members)
+    es = torch.cuda.ExternalStream(E.stream(), device=local)
+    dts = [wl.dt for wl in wls]
+    steps = max(3, min(args.steps, 10))
+    out = {"workload": "ice_ensemble: 256 independent ice-creep VEP boxes (law 7, Drucker-Prager yield, "
+                       "shear modulus 3.5 GPa), grids drawn from {128^2, 256x64, 128x256, 192^2, 1024x256} cells "
+                       "(SplitMix64 seed 5), 16 markers per cell, per-marker log10 grain size ~ U[-4,-1] m",
+           "members": len(members), "markers": int(n_total), "steps": steps, "train_seconds": round(train_s, 3)}
+    for label, mode in (("plain", 0), ("surrogate_tc", 2)):
+        for P in members:
+            P.creep_configure(mode=mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
+        for _ in range(2):
+            E.step(dts, dts, 1, True)
+        E.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(es)
+        for _ in range(steps):
+            E.step(dts, dts, 1, True)
+        ev1.record(es)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        st = [P.creep_stats() for P in members]
+        mk = sum(x["markers"] for x in st)
+        out[label] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
+                      "newton_iters_per_marker": sum(x["iterations"] for x in st) / max(mk, 1),
+                      "fallbacks_per_step": sum(x["fallbacks"] for x in st),
+                      "max_residual": max(x["max_residual"] for x in st),
+                      "tc_timeouts": sum(x["tc_timeouts"] for x in st)}
+    out["speedup_surrogate_vs_plain"] = out["surrogate_tc"]["value"] / out["plain"]["value"]
     E.close()
     for P in members:
         P.close()

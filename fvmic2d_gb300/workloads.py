@@ -414,6 +414,80 @@ def convection_ensemble(n_members=64, seed=4):
     return members
 
 
+def ice_member(nx_cells, ny_cells, seed, nm=4):
+    """One member of the mixed ice ensemble: the composite-creep (law 7) visco-elasto-plastic
+    box of ice_creep_box on an nx_cells x ny_cells grid (100 km wide, aspect as given), with
+    Drucker-Prager yield (cohesion 1 MPa, friction 0.6) and shear modulus 3.5 GPa.  No host
+    markers: nm x nm markers per cell are laid out on the device; grain sizes (log10 d ~
+    U[-4,-1] m, SplitMix64) follow in distribution order."""
+    NX, NY = nx_cells + 1, ny_cells + 1
+    LX = 1.0e5
+    LY = LX * ny_cells / nx_cells
+    g = Grid(NX, NY, LX, LY, spacing_uniform(0.0, LX, NX), spacing_uniform(0.0, LY, NY))
+    mat = _materials(1)
+    mat.materialEta[0] = 1e14
+    mat.materialRho[0] = 917.0
+    mat.materialkThermal[0] = 2.1
+    mat.materialCp[0] = 2000.0
+    mat.materialAlpha[0] = 1.6e-4
+    mat.materialMu[0] = 3.5e9
+    mat.hasEtaT[0] = 7
+    mat.hasPlasticity[0] = 1
+    mat.materialCohesion[0] = 1e6
+    mat.materialFriction[0] = 0.6
+    opt = Options(etamin=1e8, etamax=1e22, fractionalEtamin=0.01, subgridStressDiffusivity=1.0,
+                  subgridTemperatureDiffusivity=1.0)
+    U = 1e-9
+    pi = np.pi
+    vx_fn = lambda x, y: U * np.sin(pi * x / LX) * np.cos(pi * y / LY)
+    vy_fn = lambda x, y: -U * LY / LX * np.cos(pi * x / LX) * np.sin(pi * y / LY)
+    dvx = {"x": lambda x, y: U * pi / LX * np.cos(pi * x / LX) * np.cos(pi * y / LY),
+           "y": lambda x, y: -U * pi / LY * np.sin(pi * x / LX) * np.sin(pi * y / LY)}
+    dvy = {"x": lambda x, y: U * pi * LY / LX ** 2 * np.sin(pi * x / LX) * np.sin(pi * y / LY),
+           "y": lambda x, y: -U * pi / LX * np.cos(pi * x / LX) * np.cos(pi * y / LY)}
+    vx, vy, exx, eyy, exy, wxy = _velocity_fields(g, vx_fn, vy_fn, dvx, dvy)
+    XCc, YCc = np.meshgrid(g.xc[:NX], g.yc[:NY], indexing="xy")
+    Xb, Yb = np.meshgrid(g.x, g.y, indexing="xy")
+    eta_ref = 1e14
+    nodal = {
+        "vx": vx, "vy": vy, "edotxx": exx, "edotyy": eyy, "edotxy": exy, "wxy": wxy,
+        "p": 1e8 * YCc / LY,
+        "soxx": 2.0 * eta_ref * exx, "soyy": 2.0 * eta_ref * eyy, "soxy": 2.0 * eta_ref * exy,
+        "thisT": 100.0 + 173.0 * Yb / LY, "lastT": 100.0 + 173.0 * Yb / LY,
+    }
+    nodal["dsxx"] = 0.05 * nodal["soxx"]
+    nodal["dsyy"] = 0.05 * nodal["soyy"]
+    nodal["dsxy"] = 0.05 * nodal["soxy"]
+    dt = 0.5 * (LX / nx_cells) / (2 * U)
+    wl = Workload("ice_member", g, np.zeros(0, dtype=MARKER_DTYPE), mat, opt, _free_slip(), nodal, dt, dt, 10)
+    wl.nm = (nm, nm)
+    wl.seed = seed
+    wl.capacity = nm * nm * nx_cells * ny_cells
+    return wl
+
+
+def ice_grain_sizes(n, seed):
+    return 10.0 ** (-4.0 + 3.0 * splitmix64_uniform(seed + 17, n))
+
+
+# mixed member grids (cells) and their draw probabilities: most members small, a few at the
+# 1024 x 256 size of the VEP box
+ICE_GRIDS = [(128, 128), (256, 64), (128, 256), (192, 192), (1024, 256)]
+ICE_GRID_P = [0.55, 0.25, 0.12, 0.075, 0.005]
+
+
+def ice_ensemble(n_members=256, seed=5):
+    """Ensemble of independent ice-creep VEP boxes on mixed grids from 128^2 to 1024 x 256 cells,
+    16 markers per cell (SplitMix64 seed 5): about 80-90 million markers."""
+    u = splitmix64_uniform(seed, n_members)
+    cum = np.cumsum(ICE_GRID_P)
+    out = []
+    for i in range(n_members):
+        nx, ny = ICE_GRIDS[min(len(ICE_GRIDS) - 1, int(np.searchsorted(cum, u[i], side="right")))]
+        out.append(ice_member(nx, ny, seed * 1000 + i))
+    return out
+
+
 def density_case(nx_cells=32, ny_cells=8, seed=6):
     """A marker set for checkMarkerDensity (markers.c:455-781): the refined VEP box at 4x4
     markers per cell (4 per quarter cell) with quarter cells emptied (including some in the first
