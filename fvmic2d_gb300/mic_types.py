@@ -99,7 +99,7 @@ NF = {
         [
             "rho", "rhodot", "etaS", "etaN", "thisT", "lastT", "kThermal", "Cp",
             "edotxx", "edotxy", "edotyy", "soxx", "soxy", "soyy", "dsxx", "dsyy", "dsxy",
-            "muS", "muN", "vx", "vy", "p", "wxy", "srr",
+            "muS", "muN", "vx", "vy", "p", "wxy", "srr", "eii", "sii", "heating",
         ]
     )
 }

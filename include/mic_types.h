@@ -122,6 +122,9 @@ enum {
   MIC_NF_P,
   MIC_NF_WXY,
   MIC_NF_SRR,       /* strain-rate residual projected to cell centres (residual.c:20) */
+  MIC_NF_EII,       /* strain-rate second invariant at basic nodes (nodalStressStrain.c) */
+  MIC_NF_SII,       /* stress second invariant at basic nodes */
+  MIC_NF_HEATING,   /* shear heating at basic nodes (the nodalHeating argument) */
   MIC_NF_COUNT
 };
 

@@ -1264,3 +1264,157 @@ done:
   free(isout);
   return ret;
 }
+
+/* ---- grid routines between the solves ------------------------------------------------ */
+
+#define NF(c, f, i, j) ((c)->nodal[f][(size_t)(j) * (size_t)(c)->NX + (size_t)(i)])
+
+/* nodalStressStrain (nodalStressStrain.c:6-486), one rank, non-periodic x.  The reference's
+ * vector operations (X = etaN ./ (etaN + dt muN) with the zero-divisor guard, X1 = etaN (2 - 2X),
+ * s_new = X1 e + X s_old, ds = s_new - s_old) are restated elementwise in their order. */
+void orc_nodal_stress_strain(orc_ctx *c, double dt) {
+  const int NX = c->NX, NY = c->NY;
+  double *exx = c->nodal[MIC_NF_EDOTXX], *eyy = c->nodal[MIC_NF_EDOTYY];
+  for (int ix = 0; ix < NX; ++ix) {
+    for (int jy = 0; jy < NY; ++jy) {
+      const size_t k = (size_t)jy * NX + ix;
+      if (ix == 0 || jy == 0) {
+        exx[k] = 0.0;
+        eyy[k] = 0.0;
+      } else {
+        const double dx = c->x[ix] - c->x[ix - 1];
+        const double dy = c->y[jy] - c->y[jy - 1];
+        const double divv = (NF(c, MIC_NF_VX, ix, jy - 1) - NF(c, MIC_NF_VX, ix - 1, jy - 1)) / dx +
+                            (NF(c, MIC_NF_VY, ix - 1, jy) - NF(c, MIC_NF_VY, ix - 1, jy - 1)) / dy;
+        exx[k] = (NF(c, MIC_NF_VX, ix, jy - 1) - NF(c, MIC_NF_VX, ix - 1, jy - 1)) / dx - divv / 3.0;
+        eyy[k] = (NF(c, MIC_NF_VY, ix - 1, jy) - NF(c, MIC_NF_VY, ix - 1, jy - 1)) / dy - divv / 3.0;
+      }
+    }
+  }
+  const size_t nn = (size_t)NX * NY;
+  for (size_t k = 0; k < nn; ++k) {  /* cell-centred stresses */
+    const double eta = c->nodal[MIC_NF_ETAN][k], mu = c->nodal[MIC_NF_MUN][k];
+    const double den = eta + dt * mu;
+    const double X = den != 0.0 ? eta / den : 0.0;
+    const double X1 = eta * (-2.0 * X + 2.0);
+    const int so[2] = {MIC_NF_SOXX, MIC_NF_SOYY}, ds[2] = {MIC_NF_DSXX, MIC_NF_DSYY};
+    const double *e[2] = {exx, eyy};
+    for (int q = 0; q < 2; ++q) {
+      const double et = X1 * e[q][k];
+      double st = X * c->nodal[so[q]][k];
+      st = st + 1.0 * et;
+      c->nodal[ds[q]][k] = st + -1.0 * c->nodal[so[q]][k];
+      c->nodal[so[q]][k] = st;
+    }
+  }
+  for (int jy = 0; jy < NY; ++jy) {  /* basic nodes: vorticity and shear strain rate */
+    for (int ix = 0; ix < NX; ++ix) {
+      double vxm, vym, vxp, vyp;
+      if (ix == 0)
+        vym = (c->bcs.mechBCLeft.type[1] == 0) ? 2.0 * c->bcs.mechBCLeft.value[1] - NF(c, MIC_NF_VY, ix, jy)
+                                               : NF(c, MIC_NF_VY, ix, jy);
+      else
+        vym = NF(c, MIC_NF_VY, ix - 1, jy);
+      vyp = NF(c, MIC_NF_VY, ix, jy);
+      if (jy == 0)
+        vxm = (c->bcs.mechBCTop.type[0] == 0) ? 2.0 * c->bcs.mechBCTop.value[0] - NF(c, MIC_NF_VX, ix, jy)
+                                              : NF(c, MIC_NF_VX, ix, jy);
+      else
+        vxm = NF(c, MIC_NF_VX, ix, jy - 1);
+      vxp = NF(c, MIC_NF_VX, ix, jy);
+      const double dx = c->xc[ix + 1] - c->xc[ix];
+      const double dy = c->yc[jy + 1] - c->yc[jy];
+      NF(c, MIC_NF_WXY, ix, jy) = 0.5 * ((vxp - vxm) / dy - (vyp - vym) / dx);
+      NF(c, MIC_NF_EDOTXY, ix, jy) = 0.5 * ((vxp - vxm) / dy + (vyp - vym) / dx);
+    }
+  }
+  for (size_t k = 0; k < nn; ++k) {  /* basic-node shear stress */
+    const double eta = c->nodal[MIC_NF_ETAS][k], mu = c->nodal[MIC_NF_MUS][k];
+    const double den = eta + dt * mu;
+    const double X = den != 0.0 ? eta / den : 0.0;
+    const double X1 = eta * (-2.0 * X + 2.0);
+    const double et = X1 * c->nodal[MIC_NF_EDOTXY][k];
+    double st = X * c->nodal[MIC_NF_SOXY][k];
+    st = st + 1.0 * et;
+    c->nodal[MIC_NF_DSXY][k] = st + -1.0 * c->nodal[MIC_NF_SOXY][k];
+    c->nodal[MIC_NF_SOXY][k] = st;
+  }
+  double *hs_out = c->nodal[MIC_NF_HEATING], *eii = c->nodal[MIC_NF_EII], *sii = c->nodal[MIC_NF_SII];
+  memset(hs_out, 0, sizeof(double) * nn);
+  memset(eii, 0, sizeof(double) * nn);
+  memset(sii, 0, sizeof(double) * nn);
+  const double *sxx = c->nodal[MIC_NF_SOXX], *syy = c->nodal[MIC_NF_SOYY], *sxy = c->nodal[MIC_NF_SOXY];
+  const double *eN = c->nodal[MIC_NF_ETAN], *eS = c->nodal[MIC_NF_ETAS], *exy = c->nodal[MIC_NF_EDOTXY];
+  for (int jy = 1; jy < NY - 1; ++jy) {
+    for (int ix = 1; ix < NX - 1; ++ix) {
+      const size_t a = (size_t)jy * NX + ix, b = a + NX, r = a + 1, d = b + 1;
+      double hs = (sxx[a] * sxx[a] / eN[a] + sxx[b] * sxx[b] / eN[b] + sxx[r] * sxx[r] / eN[r] + sxx[d] * sxx[d] / eN[d]) / 8.0;
+      hs += (syy[a] * syy[a] / eN[a] + syy[b] * syy[b] / eN[b] + syy[r] * syy[r] / eN[r] + syy[d] * syy[d] / eN[d]) / 8.0;
+      hs += sxy[a] * sxy[a] / eS[a];
+      hs_out[a] += hs;
+      eii[a] = sqrt((exx[a] * exx[a] + exx[b] * exx[b] + exx[r] * exx[r] + exx[d] * exx[d]) / 8.0 +
+                    (eyy[a] * eyy[a] + eyy[b] * eyy[b] + eyy[r] * eyy[r] + eyy[d] * eyy[d]) / 8.0 + exy[a] * exy[a]);
+      sii[a] = sqrt((sxx[a] * sxx[a] + sxx[b] * sxx[b] + sxx[r] * sxx[r] + sxx[d] * sxx[d]) / 8.0 +
+                    (syy[a] * syy[a] + syy[b] * syy[b] + syy[r] * syy[r] + syy[d] * syy[d]) / 8.0 + sxy[a] * sxy[a]);
+    }
+  }
+}
+
+/* limitDisplacementTimestep (limitTimestep.c:6-133): the smallest of dt, factor times the
+ * time to cross the smaller adjacent cell at each nodal vx / vy, 1% of rho / rhodot per node,
+ * and 0.01 / max |rhodot| */
+double orc_limit_displacement_timestep(const orc_ctx *c, double dt, double factor) {
+  const int NX = c->NX, NY = c->NY;
+  const double *vx = c->nodal[MIC_NF_VX], *vy = c->nodal[MIC_NF_VY];
+  const double *rho = c->nodal[MIC_NF_RHO], *rhodot = c->nodal[MIC_NF_RHODOT];
+  for (int ix = 0; ix < NX; ++ix) {
+    for (int jy = 0; jy < NY; ++jy) {
+      const size_t k = (size_t)jy * NX + ix;
+      double dx, dy, dt1;
+      const double dx1 = c->x[ix + 1] - c->x[ix], dx2 = c->x[ix] - c->x[ix - 1];
+      if (ix == 0) dx = dx1;
+      else if (ix == NX - 1) dx = dx2;
+      else dx = (dx1 <= dx2) ? dx1 : dx2;
+      dt1 = (vx[k] != 0.0) ? dx / (fabs(vx[k])) * factor : dt;
+      if (dt > dt1) dt = dt1;
+      const double dy1 = c->y[jy + 1] - c->y[jy], dy2 = c->y[jy] - c->y[jy - 1];
+      if (jy == 0) dy = dy1;
+      else if (jy == NY - 1) dy = dy2;
+      else dy = (dy1 <= dy2) ? dy1 : dy2;
+      dt1 = (vy[k] != 0.0) ? dy / (fabs(vy[k])) * factor : dt;
+      if (dt > dt1) dt = dt1;
+      if (rhodot[k] != 0.0) dt1 = fabs(0.01 * rho[k] / rhodot[k]);
+      if (dt > dt1) dt = dt1;
+    }
+  }
+  double mx = -INFINITY, mn = INFINITY;
+  for (size_t k = 0; k < (size_t)NX * NY; ++k) {
+    if (rhodot[k] > mx) mx = rhodot[k];
+    if (rhodot[k] < mn) mn = rhodot[k];
+  }
+  mx = fabs(mx);
+  mn = fabs(mn);
+  if (mn > mx) mx = mn;
+  if (mx * dt > 0.01) dt = 0.01 / mx;
+  return dt;
+}
+
+/* retrieveSolutions (retrieveSolutions.c:4-82): vx, vy, p from S[(j NX + i) 3 + {0,1,2}],
+ * pressure scaled by Kcont, minus the dx-weighted mean of row 1 (i >= 1) on every j, i >= 1 */
+void orc_retrieve_solutions(orc_ctx *c, const double *S, double Kcont) {
+  const int NX = c->NX, NY = c->NY;
+  for (int j = 0; j < NY; ++j)
+    for (int i = 0; i < NX; ++i) {
+      const size_t k = (size_t)j * NX + i;
+      c->nodal[MIC_NF_P][k] = S[3 * k + 2] * Kcont;
+      c->nodal[MIC_NF_VX][k] = S[3 * k + 0];
+      c->nodal[MIC_NF_VY][k] = S[3 * k + 1];
+    }
+  double pm = 0.0;
+  for (int i = 1; i < NX; ++i) {
+    const double dx = c->x[i] - c->x[i - 1];
+    pm += NF(c, MIC_NF_P, i, 1) * dx / c->LX;
+  }
+  for (int j = 1; j < NY; ++j)
+    for (int i = 1; i < NX; ++i) NF(c, MIC_NF_P, i, j) -= pm;
+}

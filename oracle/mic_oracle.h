@@ -87,6 +87,11 @@ int64_t orc_distribute_uniform(const orc_ctx *c, mic_marker *mk, int64_t cap, in
 /* checkMarkerDensity (markers.c:455-781) on an array of capacity cap; *state is the 48-bit
  * drand48 stream (orc_srand48_state(seed) = srand48(seed)) */
 uint64_t orc_srand48_state(long seed);
+/* grid routines between the solves: nodalStressStrain, limitDisplacementTimestep,
+ * retrieveSolutions (S: [(j NX + i) 3 + {vx, vy, p}]) */
+void orc_nodal_stress_strain(orc_ctx *c, double dt);
+double orc_limit_displacement_timestep(const orc_ctx *c, double dt, double factor);
+void orc_retrieve_solutions(orc_ctx *c, const double *S, double Kcont);
 int64_t orc_check_marker_density(orc_ctx *c, mic_marker *mk, int64_t n, int64_t cap, const mic_density_options *d,
                                  uint64_t *state, int64_t *n_added, int64_t *n_removed);
 

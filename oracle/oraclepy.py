@@ -56,6 +56,9 @@ def lib():
             "orc_creep_stress": (_I, [_D, _D, _D, _D, _D, _DP, _IP]),
             "orc_reset_markers": (None, [_P, _I64]),
             "orc_srand48_state": (ctypes.c_uint64, [ctypes.c_long]),
+            "orc_nodal_stress_strain": (None, [_P, _D]),
+            "orc_limit_displacement_timestep": (_D, [_P, _D, _D]),
+            "orc_retrieve_solutions": (None, [_P, _DP, _D]),
             "orc_check_marker_density": (_I64, [_P, _P, _I64, _I64, _P, ctypes.POINTER(ctypes.c_uint64), _I64P,
                                                  _I64P]),
             "orc_distribute_uniform": (_I64, [_P, _P, _I64, _I, _I, ctypes.c_ulong]),
@@ -120,6 +123,16 @@ class OracleProblem:
             raise ValueError("capacity exceeded")
         self.markers = mk[:n].copy()
         return mk, n
+
+    def nodalStressStrain(self, dt, gy=0.0):
+        lib().orc_nodal_stress_strain(self.h, dt)
+
+    def limitDisplacementTimestep(self, dt, factor):
+        return lib().orc_limit_displacement_timestep(self.h, dt, factor)
+
+    def retrieveSolutions(self, S, Kcont):
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        lib().orc_retrieve_solutions(self.h, _dp(S), Kcont)
 
     def checkMarkerDensity(self, dopt, cap, state=None, seed=1):
         """checkMarkerDensity on a copy of the markers grown to capacity cap; returns

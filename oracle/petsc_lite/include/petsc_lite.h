@@ -8,7 +8,8 @@
  * oracle) and the GPU kernels can be pinned against the reference's arithmetic.
  *
  * Semantics fixed here (they decide the reference's results on one rank):
- *  - One DMDA: NX x NY nodes, dof 1, stencil width 2, DMDA_STENCIL_BOX, boundary
+ *  - The DMDA: NX x NY nodes, dof 1 (dof 3 for the Stokes solution, values interleaved per
+ *    node), stencil width 2, DMDA_STENCIL_BOX, boundary
  *    DM_BOUNDARY_GHOSTED in x and y (fvmic2d nodalFields.c:19-20).  Periodic x
  *    is not modelled: the harness rejects it.
  *  - Global vectors hold NX*NY values, x fastest ([j][i]); local vectors hold
@@ -19,6 +20,7 @@
  *  - VecPointwiseDivide(w,x,y) gives w[i] = x[i]/y[i] when y[i] != 0 and 0
  *    otherwise (the zero-divisor guard of current PETSc releases).
  *  - Fresh vectors (DMCreate*Vector, DMGet*Vector, VecDuplicate) are zeroed.
+ *  - VecMax / VecMin skip NaN entries (their comparisons are false).
  *  - MPI: one rank; MPI_Allreduce copies.
  */
 #ifndef PETSC_LITE_H
@@ -88,6 +90,7 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 
 /* DMDA / Vec (single rank) */
 PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da);
+PetscErrorCode plite_DMDACreateDOF(PetscInt NX, PetscInt NY, PetscInt dof, DM *da);
 PetscErrorCode plite_DMDestroy(DM *da);
 PetscErrorCode DMDAGetCorners(DM, PetscInt *, PetscInt *, PetscInt *, PetscInt *, PetscInt *, PetscInt *);
 PetscErrorCode DMCreateGlobalVector(DM, Vec *);
@@ -117,6 +120,13 @@ PetscErrorCode VecView(Vec, PetscViewer);
 PetscErrorCode VecGetArray(Vec, PetscScalar **);
 PetscErrorCode VecRestoreArray(Vec, PetscScalar **);
 PetscErrorCode VecGetSize(Vec, PetscInt *);
+PetscErrorCode VecScale(Vec, PetscScalar);
+PetscErrorCode VecShift(Vec, PetscScalar);
+PetscErrorCode VecPointwiseMult(Vec, Vec, Vec);
+PetscErrorCode VecAYPX(Vec, PetscScalar, Vec);
+PetscErrorCode VecMax(Vec, PetscInt *, PetscReal *);
+PetscErrorCode VecMin(Vec, PetscInt *, PetscReal *);
+PetscErrorCode VecStrideScale(Vec, PetscInt, PetscScalar);
 
 /* logging: stages accumulate wall time per stage id (used for the CPU breakdown) */
 PetscErrorCode PetscLogStageRegister(const char *, PetscLogStage *);

@@ -8,6 +8,7 @@
 
 struct _p_DM {
   PetscInt NX, NY;
+  PetscInt dof;          /* values per node: 1, or 3 for the Stokes solution DMDA (vx, vy, p) */
 };
 
 struct _p_Vec {
@@ -26,7 +27,14 @@ PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da) {
   if (!*da) return 1;
   (*da)->NX = NX;
   (*da)->NY = NY;
+  (*da)->dof = 1;
   return 0;
+}
+
+PetscErrorCode plite_DMDACreateDOF(PetscInt NX, PetscInt NY, PetscInt dof, DM *da) {
+  PetscErrorCode e = plite_DMDACreate(NX, NY, da);
+  if (!e) (*da)->dof = dof;
+  return e;
 }
 
 PetscErrorCode plite_DMDestroy(DM *da) {
@@ -51,7 +59,7 @@ static PetscErrorCode vec_new(DM da, int is_local, Vec *v) {
   if (!w) return 1;
   w->dm = da;
   w->is_local = is_local;
-  w->n = is_local ? (da->NX + 4) * (da->NY + 4) : da->NX * da->NY;
+  w->n = (is_local ? (da->NX + 4) * (da->NY + 4) : da->NX * da->NY) * da->dof;
   w->data = (PetscScalar *)calloc((size_t)w->n, sizeof(PetscScalar));
   if (!w->data) { free(w); return 1; }
   *v = w;
@@ -178,8 +186,81 @@ PetscErrorCode DMDAVecGetArray(DM da, Vec v, void *array) {
   return 0;
 }
 PetscErrorCode DMDAVecRestoreArray(DM da, Vec v, void *array) { (void)da; (void)v; *(PetscScalar ***)array = NULL; return 0; }
-PetscErrorCode DMDAVecGetArrayDOF(DM da, Vec v, void *array) { (void)da; (void)v; (void)array; return 63; }
-PetscErrorCode DMDAVecRestoreArrayDOF(DM da, Vec v, void *array) { (void)da; (void)v; (void)array; return 63; }
+/* [j][i][dof] view of a global vector of a multi-dof DMDA (dof interleaved per node) */
+PetscErrorCode DMDAVecGetArrayDOF(DM da, Vec v, void *array) {
+  if (v->is_local) return 63;
+  const PetscInt NX = da->NX, NY = da->NY, dof = da->dof;
+  PetscScalar ***a = (PetscScalar ***)malloc((size_t)NY * sizeof(PetscScalar **));
+  PetscScalar **cells = (PetscScalar **)malloc((size_t)NY * NX * sizeof(PetscScalar *));
+  if (!a || !cells) return 1;
+  for (PetscInt j = 0; j < NY; ++j) {
+    a[j] = cells + (size_t)j * NX;
+    for (PetscInt i = 0; i < NX; ++i) a[j][i] = v->data + ((size_t)j * NX + i) * dof;
+  }
+  *(PetscScalar ****)array = a;
+  return 0;
+}
+PetscErrorCode DMDAVecRestoreArrayDOF(DM da, Vec v, void *array) {
+  (void)da;
+  (void)v;
+  PetscScalar ***a = *(PetscScalar ****)array;
+  if (a) {
+    free(a[0]);
+    free(a);
+  }
+  *(PetscScalar ****)array = NULL;
+  return 0;
+}
+
+/* elementwise operations, as PETSc documents them (no fused multiply-add: the stand-in is
+ * compiled with -ffp-contract=off) */
+PetscErrorCode VecScale(Vec x, PetscScalar a) {
+  for (PetscInt k = 0; k < x->n; ++k) x->data[k] = a * x->data[k];
+  return 0;
+}
+PetscErrorCode VecShift(Vec x, PetscScalar a) {
+  for (PetscInt k = 0; k < x->n; ++k) x->data[k] = x->data[k] + a;
+  return 0;
+}
+PetscErrorCode VecPointwiseMult(Vec w, Vec x, Vec y) {
+  for (PetscInt k = 0; k < w->n; ++k) w->data[k] = x->data[k] * y->data[k];
+  return 0;
+}
+PetscErrorCode VecAYPX(Vec y, PetscScalar beta, Vec x) {  /* y = x + beta y */
+  for (PetscInt k = 0; k < y->n; ++k) y->data[k] = x->data[k] + beta * y->data[k];
+  return 0;
+}
+/* largest / smallest entry; NaN entries never win (comparisons with NaN are false) */
+PetscErrorCode VecMax(Vec x, PetscInt *idx, PetscReal *v) {
+  PetscReal m = -INFINITY;
+  PetscInt at = -1;
+  for (PetscInt k = 0; k < x->n; ++k)
+    if (x->data[k] > m) {
+      m = x->data[k];
+      at = k;
+    }
+  if (idx) *idx = at;
+  *v = m;
+  return 0;
+}
+PetscErrorCode VecMin(Vec x, PetscInt *idx, PetscReal *v) {
+  PetscReal m = INFINITY;
+  PetscInt at = -1;
+  for (PetscInt k = 0; k < x->n; ++k)
+    if (x->data[k] < m) {
+      m = x->data[k];
+      at = k;
+    }
+  if (idx) *idx = at;
+  *v = m;
+  return 0;
+}
+/* scale component `field` of a dof-interleaved vector */
+PetscErrorCode VecStrideScale(Vec v, PetscInt field, PetscScalar a) {
+  const PetscInt dof = v->dm->dof;
+  for (PetscInt k = field; k < v->n; k += dof) v->data[k] = v->data[k] * a;
+  return 0;
+}
 
 /* ---- logging stages: exclusive wall time attributed to the top of the stack ---- */
 #define PLITE_MAX_STAGES 64

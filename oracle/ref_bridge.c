@@ -23,6 +23,9 @@
 #include "residual.h"
 #include "profile.h"
 #include "gridSpacing.h"
+#include "nodalStressStrain.h"
+#include "limitTimestep.h"
+#include "retrieveSolutions.h"
 #include "mic_types.h"
 
 PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da);
@@ -45,6 +48,7 @@ typedef struct {
   MarkerSet ms;
   Vec thisT;
   Vec srr;
+  Vec heat;
   double *gbuf;
 } refp;
 
@@ -76,6 +80,9 @@ static Vec *field_vec(refp *p, int id) {
     case MIC_NF_P: return &p->nf.p;
     case MIC_NF_WXY: return &p->nf.wxy;
     case MIC_NF_SRR: return &p->srr;
+    case MIC_NF_EII: return &p->nf.eii;
+    case MIC_NF_SII: return &p->nf.sii;
+    case MIC_NF_HEATING: return &p->heat;
     default: return NULL;
   }
 }
@@ -107,6 +114,7 @@ refp *ref_create(int NX, int NY, double LX, double LY, const double *x, const do
   getCellCenters(p->grid.x, p->grid.xc, LX, NX);
   getCellCenters(p->grid.y, p->grid.yc, LY, NY);
   plite_DMDACreate(NX, NY, &p->grid.da);
+  plite_DMDACreateDOF(NX, NY, 3, &p->grid.vda);
   for (int id = 0; id < MIC_NF_COUNT; ++id) DMCreateGlobalVector(p->grid.da, field_vec(p, id));
   return p;
 }
@@ -115,6 +123,7 @@ void ref_destroy(refp *p) {
   if (!p) return;
   for (int id = 0; id < MIC_NF_COUNT; ++id) VecDestroy(field_vec(p, id));
   plite_DMDestroy(&p->grid.da);
+  plite_DMDestroy(&p->grid.vda);
   free(p->gbuf);
   free(p);
 }
@@ -324,4 +333,32 @@ int ref_checkMarkerDensity(refp *p, mic_marker *m, int n, int cap, int NMX, int 
   }
   if (e) return -1;
   return p->ms.nMark;
+}
+
+/* nodalStressStrain (nodalStressStrain.c:6): new nodal strain rates, vorticity, stresses and
+ * stress changes from vx, vy, etaN/S, muN/S, soxx/yy/xy; shear heating into MIC_NF_HEATING */
+int ref_nodalStressStrain(refp *p, double dt, double gy) {
+  return nodalStressStrain(&p->grid, &p->nf, &p->opt, &p->bv, dt, p->heat, gy);
+}
+
+/* limitDisplacementTimestep (limitTimestep.c:6) starting from dt */
+double ref_limitDisplacementTimestep(refp *p, double dt, double factor) {
+  p->opt.displacementStepLimit = factor;
+  PetscScalar d = dt;
+  limitDisplacementTimestep(&p->grid, &p->nf, &d, &p->opt);
+  return d;
+}
+
+/* retrieveSolutions (retrieveSolutions.c:4) from a solution vector S[(j NX + i) 3 + dof]
+ * (copied; the reference scales the pressure entries of S in place) */
+int ref_retrieveSolutions(refp *p, const double *S, double Kcont) {
+  Vec v;
+  DMCreateGlobalVector(p->grid.vda, &v);
+  PetscScalar *a;
+  VecGetArray(v, &a);
+  memcpy(a, S, sizeof(double) * 3 * (size_t)p->grid.NX * (size_t)p->grid.NY);
+  PetscInt nan = 0;
+  int e = retrieveSolutions(&p->grid, &p->nf, v, Kcont, &nan);
+  VecDestroy(&v);
+  return e ? -1 : nan;
 }

@@ -62,6 +62,9 @@ def lib():
             "ref_checkMarkerDensity": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _DP, ctypes.c_long,
                                             ctypes.POINTER(ctypes.c_ushort)]),
             "ref_distributeMarkersUniformInDomain": (_I, [_P, _P, _I, _I, _I]),
+            "ref_nodalStressStrain": (_I, [_P, _D, _D]),
+            "ref_limitDisplacementTimestep": (_D, [_P, _D, _D]),
+            "ref_retrieveSolutions": (_I, [_P, _DP, _D]),
             "ref_stage_seconds": (_D, [_I]),
             "ref_stage_reset": (None, []),
         }
@@ -97,6 +100,16 @@ class RefProblem:
         L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         for name, arr in wl.nodal.items():
             self.set_nodal(name, arr)
+
+    def nodalStressStrain(self, dt, gy=0.0):
+        return lib().ref_nodalStressStrain(self.h, dt, gy)
+
+    def limitDisplacementTimestep(self, dt, factor):
+        return lib().ref_limitDisplacementTimestep(self.h, dt, factor)
+
+    def retrieveSolutions(self, S, Kcont):
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        return lib().ref_retrieveSolutions(self.h, _dp(S), Kcont)
 
     def checkMarkerDensity(self, dopt, cap, seed=1):
         """The reference's checkMarkerDensity (PETSCRAND48 object seeded with srand48(seed)) on a

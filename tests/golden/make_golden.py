@@ -207,6 +207,30 @@ def density_table():
     return out
 
 
+def grid_table():
+    """nodalStressStrain, limitDisplacementTimestep and retrieveSolutions of the reference on
+    the grid cases of tests/test_oracle_pin.py (inputs and outputs)."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from tests.test_oracle_pin import GRID_OUT, grid_case
+
+    out = {}
+    for kind, seed in (("free_slip", 5), ("prescribed", 8)):
+        wl, S = grid_case(kind, seed)
+        R = refpy.RefProblem(wl)
+        for name, arr in wl.nodal.items():
+            out["%s_in_%s" % (kind, name)] = np.asarray(arr, dtype=np.float64)
+        out[kind + "_bcs"] = np.frombuffer(bytes(wl.bcs), dtype=np.uint8)
+        R.nodalStressStrain(3.0e11)
+        for name in GRID_OUT:
+            out["%s_out_%s" % (kind, name)] = R.get_nodal(name)
+        out[kind + "_dt"] = np.array([R.limitDisplacementTimestep(1e14, 0.5), R.limitDisplacementTimestep(1e30, 0.1)])
+        out[kind + "_S"] = S
+        R.retrieveSolutions(S, 1e20)
+        for name in ("vx", "vy", "p"):
+            out["%s_ret_%s" % (kind, name)] = R.get_nodal(name)
+    return out
+
+
 def main():
     if obuild.build_ref() is None:
         raise SystemExit("reference tree not found; golden vectors can only be generated where it exists")
@@ -216,6 +240,9 @@ def main():
     if sys.argv[1:] in ([], ["density"]):
         np.savez_compressed(os.path.join(OUT, "marker_density.npz"), **density_table())
         print("wrote marker_density")
+    if sys.argv[1:] in ([], ["grid"]):
+        np.savez_compressed(os.path.join(OUT, "grid_routines.npz"), **grid_table())
+        print("wrote grid_routines")
     if sys.argv[1:]:
         return
     cases = {

@@ -286,3 +286,67 @@ def test_marker_density_matches_reference_build(seed):
     fields = [f for f in MARKER_DTYPE.names if f not in ("cpu", "srr")]
     for f in fields:
         assert np.array_equal(mr[f], mo[f]) or np.array_equal(np.isnan(mr[f]), np.isnan(mo[f])), f
+
+
+def grid_case(kind, seed):
+    """A refined-grid box with random nodal solver fields: the inputs of the grid routines
+    between the solves (nodalStressStrain, limitDisplacementTimestep, retrieveSolutions)."""
+    wl = W.vep_slab_box(nx_cells=24, ny_cells=10, nm=2, seed=seed)
+    NX, NY = wl.grid.NX, wl.grid.NY
+    u = W.splitmix64_uniform(seed + 31, 16 * NX * NY).reshape(16, NY, NX)
+    f = {"vx": (u[0] - 0.5) * 1e-9, "vy": (u[1] - 0.5) * 1e-9, "etaN": 10 ** (19 + 4 * u[2]),
+         "etaS": 10 ** (19 + 4 * u[3]), "muN": 1e10 * (0.5 + u[4]), "muS": 1e10 * (0.5 + u[5]),
+         "soxx": (u[6] - 0.5) * 1e7, "soyy": (u[7] - 0.5) * 1e7, "soxy": (u[8] - 0.5) * 1e7,
+         "rho": 3300 * (u[9] - 0.5) * 1e-2, "rhodot": (u[10] - 0.5) * 1e-15}
+    f["rhodot"][u[11] < 0.3] = 0.0
+    f["vx"][u[12] < 0.05] = 0.0
+    f["etaN"][0, 3] = 0.0  # a zero divisor for the guarded divide
+    f["muN"][0, 3] = 0.0
+    if kind == "prescribed":
+        wl.bcs.mechBCTop.type[0] = 0
+        wl.bcs.mechBCTop.value[0] = 2e-10
+        wl.bcs.mechBCLeft.type[1] = 0
+        wl.bcs.mechBCLeft.value[1] = -1e-10
+    wl.nodal.update(f)
+    S = np.stack([(u[13] - 0.5) * 1e-9, (u[14] - 0.5) * 1e-9, (u[15] - 0.5) * 1e3], axis=-1).ravel()
+    return wl, S
+
+
+GRID_OUT = ["edotxx", "edotyy", "edotxy", "wxy", "soxx", "soyy", "soxy", "dsxx", "dsyy", "dsxy", "eii", "sii",
+            "heating"]
+
+
+@needs_ref
+@pytest.mark.parametrize("kind", ["free_slip", "prescribed"])
+def test_grid_routines_match_reference_build(kind):
+    wl, S = grid_case(kind, 5 if kind == "free_slip" else 8)
+    R, O = refpy.RefProblem(wl), oraclepy.OracleProblem(wl)
+    for P in (R, O):
+        P.nodalStressStrain(3.0e11)
+    for name in GRID_OUT:
+        ok, msg = exact(O.get_nodal(name), R.get_nodal(name))
+        assert ok, (name, msg)
+    assert O.limitDisplacementTimestep(1e14, 0.5) == R.limitDisplacementTimestep(1e14, 0.5)
+    assert O.limitDisplacementTimestep(1e30, 0.1) == R.limitDisplacementTimestep(1e30, 0.1)
+    assert R.retrieveSolutions(S, 1e20) == 0
+    O.retrieveSolutions(S, 1e20)
+    for name in ("vx", "vy", "p"):
+        ok, msg = exact(O.get_nodal(name), R.get_nodal(name))
+        assert ok, (name, msg)
+
+
+@pytest.mark.parametrize("kind", ["free_slip", "prescribed"])
+def test_grid_routines_match_golden(kind):
+    z = np.load(os.path.join(GOLDEN, "grid_routines.npz"))
+    wl, S = grid_case(kind, 5 if kind == "free_slip" else 8)
+    O = oraclepy.OracleProblem(wl)
+    O.nodalStressStrain(3.0e11)
+    for name in GRID_OUT:
+        ok, msg = exact(O.get_nodal(name), z["%s_out_%s" % (kind, name)])
+        assert ok, (name, msg)
+    dts = [O.limitDisplacementTimestep(1e14, 0.5), O.limitDisplacementTimestep(1e30, 0.1)]
+    assert np.array_equal(np.array(dts), z[kind + "_dt"])
+    O.retrieveSolutions(z[kind + "_S"], 1e20)
+    for name in ("vx", "vy", "p"):
+        ok, msg = exact(O.get_nodal(name), z["%s_ret_%s" % (kind, name)])
+        assert ok, (name, msg)
