@@ -146,6 +146,7 @@ static void free_ctx(mic_ctx *ctx) {
   cudaFree(ctx->train_buf);
   cudaFree(ctx->dens_buf);
   cudaFree(ctx->dens_add);
+  cudaFree(ctx->solution);
   cudaFree(ctx->stage_aos);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -88,6 +88,9 @@ SIGNATURES = {
     "mic_ensemble_launch_count": (_I, [_P, _I64P, _I64P]),
     "mic_ensemble_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "mic_check_marker_density": (_I, [_P, _P, _I64P, _I64P]),
+    "mic_nodal_stress_strain": (_I, [_P, _D, _D]),
+    "mic_limit_displacement_timestep": (_I, [_P, _D, _DP]),
+    "mic_retrieve_solutions": (_I, [_P, _DP, _D, _IP]),
     "mic_density_seed": (_I, [_P, ctypes.c_long]),
     "mic_density_rng_state": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
@@ -182,6 +185,21 @@ class MicProblem:
                     "mic_distribute_markers_uniform_in_domain")
         self.n = n.value
         return self.n
+
+    def nodalStressStrain(self, dt, gy=0.0):
+        self._check(self.L.mic_nodal_stress_strain(self.h, dt, gy), "mic_nodal_stress_strain")
+
+    def limitDisplacementTimestep(self, dt, factor):
+        d = ctypes.c_double(dt)
+        self._check(self.L.mic_limit_displacement_timestep(self.h, factor, ctypes.byref(d)),
+                    "mic_limit_displacement_timestep")
+        return d.value
+
+    def retrieveSolutions(self, S, Kcont):
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        nan = ctypes.c_int(0)
+        self._check(self.L.mic_retrieve_solutions(self.h, _dp(S), Kcont, ctypes.byref(nan)), "mic_retrieve_solutions")
+        return nan.value
 
     def checkMarkerDensity(self, dopt):
         """markers.c:455-781 on the device; returns (n_added, n_removed)."""

@@ -200,6 +200,23 @@ int mic_distribute_markers_uniform_in_domain(mic_ctx *ctx, int NMX, int NMY, uns
  * (integer fields take (int)value) -- the per-marker initial-condition loops of the host code */
 int mic_markers_fill(mic_ctx *ctx, int field_offset, double value);
 
+/* ---- grid routines between the solves ----
+ * nodalStressStrain (nodalStressStrain.c:6): from vx, vy (MIC_NF_VX/VY), etaN/S, muN/S and the
+ * old stresses: deviatoric strain rates (edotxx, edotyy at cell centres, edotxy at basic nodes),
+ * vorticity wxy, visco-elastic stress update (soxx, soyy, soxy) and stress changes (dsxx, dsyy,
+ * dsxy), shear heating (MIC_NF_HEATING) and the invariants MIC_NF_EII / MIC_NF_SII at interior
+ * basic nodes.  Walls from mic_set_bcs.  gy is the reference's unused gravity argument. */
+int mic_nodal_stress_strain(mic_ctx *ctx, double dt, double gy);
+/* limitDisplacementTimestep (limitTimestep.c:6): *dt = min(*dt, factor times the crossing time of
+ * the smaller adjacent cell at every nodal vx, vy, 1% of rho / rhodot), then 0.01 / max |rhodot|
+ * (factor = Options.displacementStepLimit) */
+int mic_limit_displacement_timestep(mic_ctx *ctx, double factor, double *dt);
+/* retrieveSolutions (retrieveSolutions.c:4): vx, vy, p from the solver's vector S
+ * ([(j NX + i) 3 + {0 vx, 1 vy, 2 p}], host memory), p scaled by Kcont, minus the dx-weighted
+ * mean of row 1 on every j, i >= 1.  The reference also scales the pressure entries of S in
+ * place; here S is only read.  *foundnan = 0 (the reference checks only in its TEXTURE build). */
+int mic_retrieve_solutions(mic_ctx *ctx, const double *S, double Kcont, int *foundnan);
+
 /* ---- marker density control ----
  * checkMarkerDensity (markers.c:455-781): bins the markers if their positions changed (the
  * findMarkerCells the reference calls first, main:247), counts markers per basic quarter cell,

@@ -335,10 +335,21 @@ def test_grid_routines_match_reference_build(kind):
         assert ok, (name, msg)
 
 
+def grid_case_from_golden(z, kind):
+    """the grid case with the inputs stored in the golden file (regenerating them would depend on
+    the host's libm: NumPy's power differs in the last place between machines)"""
+    wl, _ = grid_case(kind, 5 if kind == "free_slip" else 8)
+    for k in z.files:
+        if k.startswith(kind + "_in_"):
+            wl.nodal[k[len(kind + "_in_"):]] = z[k]
+    wl.bcs = BCs.from_buffer_copy(z[kind + "_bcs"].tobytes())
+    return wl, z[kind + "_S"]
+
+
 @pytest.mark.parametrize("kind", ["free_slip", "prescribed"])
 def test_grid_routines_match_golden(kind):
     z = np.load(os.path.join(GOLDEN, "grid_routines.npz"))
-    wl, S = grid_case(kind, 5 if kind == "free_slip" else 8)
+    wl, S = grid_case_from_golden(z, kind)
     O = oraclepy.OracleProblem(wl)
     O.nodalStressStrain(3.0e11)
     for name in GRID_OUT:
