@@ -23,6 +23,7 @@ extern "C" const char *mic_error_string(int code) {
     case MIC_ERR_CAPACITY: return "marker capacity exceeded";
     case MIC_ERR_NO_DEVICE: return "no CUDA device";
     case MIC_ERR_DENSITY: return "marker density control cannot proceed";
+    case MIC_ERR_IO: return "checkpoint file could not be read or written";
     default: return "unknown error";
   }
 }
@@ -147,6 +148,7 @@ static void free_ctx(mic_ctx *ctx) {
   cudaFree(ctx->dens_buf);
   cudaFree(ctx->dens_add);
   cudaFree(ctx->solution);
+  cudaFree(ctx->io_buf);
   cudaFree(ctx->stage_aos);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);

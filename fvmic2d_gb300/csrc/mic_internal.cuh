@@ -92,6 +92,8 @@ struct mic_ctx {
   unsigned long long rng48;  // drand48 stream of marker density control (48-bit state)
   void *dens_buf, *dens_add;  // density-control scratch (grown on demand)
   double *solution;           // Stokes solution (3 NX NY, dof-interleaved) for retrieveSolutions
+  void *io_buf;               // checkpoint packing scratch (grown on demand)
+  size_t io_bytes;
   size_t dens_bytes, dens_add_bytes;
   double *f64[mic::C_F64_COUNT];
   int *i32[mic::C_I32_COUNT];

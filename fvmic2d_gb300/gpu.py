@@ -89,6 +89,8 @@ SIGNATURES = {
     "mic_ensemble_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "mic_check_marker_density": (_I, [_P, _P, _I64P, _I64P]),
     "mic_nodal_stress_strain": (_I, [_P, _D, _D]),
+    "mic_save_markers_binary": (_I, [_P, ctypes.c_char_p, _D]),
+    "mic_restart_from_markers": (_I, [_P, ctypes.c_char_p, _DP]),
     "mic_limit_displacement_timestep": (_I, [_P, _D, _DP]),
     "mic_retrieve_solutions": (_I, [_P, _DP, _D, _IP]),
     "mic_density_seed": (_I, [_P, ctypes.c_long]),
@@ -185,6 +187,16 @@ class MicProblem:
                     "mic_distribute_markers_uniform_in_domain")
         self.n = n.value
         return self.n
+
+    def saveMarkersBinary(self, path, elapsed_time):
+        self._check(self.L.mic_save_markers_binary(self.h, os.fsencode(path), elapsed_time), "mic_save_markers_binary")
+
+    def restartFromMarkers(self, path):
+        t = ctypes.c_double(0.0)
+        self._check(self.L.mic_restart_from_markers(self.h, os.fsencode(path), ctypes.byref(t)),
+                    "mic_restart_from_markers")
+        self.n = self._count()
+        return t.value
 
     def nodalStressStrain(self, dt, gy=0.0):
         self._check(self.L.mic_nodal_stress_strain(self.h, dt, gy), "mic_nodal_stress_strain")

@@ -39,9 +39,10 @@ enum {
   MIC_ERR_BC = 7,         /* boundary type whose ghost values the path would read (periodic) */
   MIC_ERR_CAPACITY = 8,   /* more markers than the context was created for; markers.c:771-774 aborts */
   MIC_ERR_NO_DEVICE = 9,  /* no CUDA device: there is no CPU fallback */
-  MIC_ERR_DENSITY = 10    /* density control: a quarter cell would get a non-positive number of
+  MIC_ERR_DENSITY = 10,   /* density control: a quarter cell would get a non-positive number of
                            * markers (markers.c:590-593 aborts), an overfull quarter cell with no
                            * marker inside its bounds, or more than 2048 markers in one */
+  MIC_ERR_IO = 11         /* checkpoint file could not be opened, read or written */
 };
 
 typedef struct {
@@ -216,6 +217,17 @@ int mic_limit_displacement_timestep(mic_ctx *ctx, double factor, double *dt);
  * mean of row 1 on every j, i >= 1.  The reference also scales the pressure entries of S in
  * place; here S is only read.  *foundnan = 0 (the reference checks only in its TEXTURE build). */
 int mic_retrieve_solutions(mic_ctx *ctx, const double *S, double Kcont, int *foundnan);
+
+/* ---- marker checkpoints (io.c:299-402, restart.c:8-125) ----
+ * The reference's field-major binary format: int32 count of in-domain markers, float64 elapsed
+ * time, then cpu, cellX, cellY (int32), X, Y, VX, VY (float64), Mat (int32), T, Tdot, eta, mu,
+ * e11, e12, Eii, s11, s22, s12, p, rho, rhodot (float64), each over the markers with cellX != -1
+ * in the caller's order.  The reference names the file output/Markers.<iMonte>.<iTime>; here the
+ * caller passes the path.  Restart resets the marker set (as allocateMarkers does), fills the
+ * file's markers in file order and bins them (findMarkerCells); MIC_ERR_CAPACITY when the file
+ * holds more markers than the context. */
+int mic_save_markers_binary(mic_ctx *ctx, const char *path, double elapsed_time);
+int mic_restart_from_markers(mic_ctx *ctx, const char *path, double *elapsed_time);
 
 /* ---- marker density control ----
  * checkMarkerDensity (markers.c:455-781): bins the markers if their positions changed (the

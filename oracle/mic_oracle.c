@@ -1418,3 +1418,61 @@ void orc_retrieve_solutions(orc_ctx *c, const double *S, double Kcont) {
   for (int j = 1; j < NY; ++j)
     for (int i = 1; i < NX; ++i) NF(c, MIC_NF_P, i, j) -= pm;
 }
+
+/* ---- marker checkpoint: saveMarkersBinary (io.c:299-402) / restartFromMarkers (restart.c:8-125) */
+
+#include <stdio.h>
+
+/* fields of the file after the header (int32 count, float64 elapsed time), each over the
+ * in-domain markers in array order: kind 'i' int32, 'd' float64, at the given record offset */
+typedef struct { char kind; int off; } orc_io_field;
+static const orc_io_field ORC_IO_FIELDS[] = {
+    {'i', offsetof(mic_marker, cpu)},   {'i', offsetof(mic_marker, cellX)}, {'i', offsetof(mic_marker, cellY)},
+    {'d', offsetof(mic_marker, X)},     {'d', offsetof(mic_marker, Y)},     {'d', offsetof(mic_marker, VX)},
+    {'d', offsetof(mic_marker, VY)},    {'i', offsetof(mic_marker, Mat)},   {'d', offsetof(mic_marker, T)},
+    {'d', offsetof(mic_marker, Tdot)},  {'d', offsetof(mic_marker, eta)},   {'d', offsetof(mic_marker, mu)},
+    {'d', offsetof(mic_marker, e.T11)}, {'d', offsetof(mic_marker, e.T12)}, {'d', offsetof(mic_marker, Eii)},
+    {'d', offsetof(mic_marker, s.T11)}, {'d', offsetof(mic_marker, s.T22)}, {'d', offsetof(mic_marker, s.T12)},
+    {'d', offsetof(mic_marker, p)},     {'d', offsetof(mic_marker, rho)},   {'d', offsetof(mic_marker, rhodot)}};
+#define ORC_IO_NFIELDS ((int)(sizeof(ORC_IO_FIELDS) / sizeof(ORC_IO_FIELDS[0])))
+
+int orc_save_markers_binary(const char *path, const mic_marker *mk, int64_t n, double elapsed) {
+  FILE *f = fopen(path, "wb");
+  if (!f) return -1;
+  int32_t cnt = 0;
+  for (int64_t m = 0; m < n; ++m) cnt += mk[m].cellX != -1;
+  fwrite(&cnt, sizeof(int32_t), 1, f);
+  fwrite(&elapsed, sizeof(double), 1, f);
+  for (int k = 0; k < ORC_IO_NFIELDS; ++k)
+    for (int64_t m = 0; m < n; ++m) {
+      if (mk[m].cellX == -1) continue;
+      const char *rec = (const char *)&mk[m] + ORC_IO_FIELDS[k].off;
+      fwrite(rec, ORC_IO_FIELDS[k].kind == 'i' ? 4 : 8, 1, f);
+    }
+  return fclose(f) == 0 ? 0 : -1;
+}
+
+/* reads into mk (capacity cap, reset first as allocateMarkers does), then finds cells;
+ * returns the marker count or -1 */
+int64_t orc_restart_from_markers(orc_ctx *c, const char *path, mic_marker *mk, int64_t cap, double *elapsed) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return -1;
+  int32_t cnt = 0;
+  if (fread(&cnt, sizeof(int32_t), 1, f) != 1 || fread(elapsed, sizeof(double), 1, f) != 1 || cnt < 0 || cnt > cap) {
+    fclose(f);
+    return -1;
+  }
+  orc_reset_markers(mk, cap);
+  for (int k = 0; k < ORC_IO_NFIELDS; ++k)
+    for (int32_t m = 0; m < cnt; ++m) {
+      char *rec = (char *)&mk[m] + ORC_IO_FIELDS[k].off;
+      if (fread(rec, ORC_IO_FIELDS[k].kind == 'i' ? 4 : 8, 1, f) != 1) {
+        fclose(f);
+        return -1;
+      }
+    }
+  fclose(f);
+  int err = 0;
+  orc_find_marker_cells(c, mk, cnt, &err);
+  return err ? -1 : cnt;
+}

@@ -4,6 +4,7 @@ TEST INFRASTRUCTURE ONLY (tests/, __graft_entry__.smoke(), bench.py's CPU-baseli
 leg).  The interface mirrors oracle/refpy.RefProblem so that a test can run the
 same sequence through the reference build and through the restatement."""
 import ctypes
+import os
 
 import numpy as np
 
@@ -57,6 +58,8 @@ def lib():
             "orc_reset_markers": (None, [_P, _I64]),
             "orc_srand48_state": (ctypes.c_uint64, [ctypes.c_long]),
             "orc_nodal_stress_strain": (None, [_P, _D]),
+            "orc_save_markers_binary": (_I, [ctypes.c_char_p, _P, _I64, _D]),
+            "orc_restart_from_markers": (_I64, [_P, ctypes.c_char_p, _P, _I64, _DP]),
             "orc_limit_displacement_timestep": (_D, [_P, _D, _D]),
             "orc_retrieve_solutions": (None, [_P, _DP, _D]),
             "orc_check_marker_density": (_I64, [_P, _P, _I64, _I64, _P, ctypes.POINTER(ctypes.c_uint64), _I64P,
@@ -123,6 +126,20 @@ class OracleProblem:
             raise ValueError("capacity exceeded")
         self.markers = mk[:n].copy()
         return mk, n
+
+    def saveMarkersBinary(self, path, elapsed_time):
+        if lib().orc_save_markers_binary(os.fsencode(path), self.markers.ctypes.data, len(self.markers),
+                                         elapsed_time):
+            raise IOError(path)
+
+    def restartFromMarkers(self, path, cap):
+        mk = np.zeros(cap, dtype=MARKER_DTYPE)
+        t = ctypes.c_double(0.0)
+        n = lib().orc_restart_from_markers(self.h, os.fsencode(path), mk.ctypes.data, cap, ctypes.byref(t))
+        if n < 0:
+            raise IOError(path)
+        self.markers = mk[:n].copy()
+        return t.value
 
     def nodalStressStrain(self, dt, gy=0.0):
         lib().orc_nodal_stress_strain(self.h, dt)

@@ -155,5 +155,41 @@ int MPI_Comm_size(MPI_Comm, int *);
 int MPI_Allreduce(const void *, void *, int, MPI_Datatype, MPI_Op, MPI_Comm);
 int MPI_Sendrecv(const void *, int, MPI_Datatype, int, int, void *, int, MPI_Datatype, int, int,
                  MPI_Comm, MPI_Status *);
+/* one rank: gathers copy, broadcasts do nothing, point-to-point is never reached */
+int MPI_Allgather(const void *, int, MPI_Datatype, void *, int, MPI_Datatype, MPI_Comm);
+int MPI_Gather(const void *, int, MPI_Datatype, void *, int, MPI_Datatype, int, MPI_Comm);
+int MPI_Bcast(void *, int, MPI_Datatype, int, MPI_Comm);
+int MPI_Send(const void *, int, MPI_Datatype, int, int, MPI_Comm);
+int MPI_Recv(void *, int, MPI_Datatype, int, int, MPI_Comm, MPI_Status *);
+typedef int MPI_Info;
+#define MPI_MODE_CREATE 1
+
+/* Viewers, bags, object names and options: io.c's nodal-field and options writers use them;
+ * the marker writer (saveMarkersBinary) does not.  These stand-ins do nothing and report an
+ * error where output would be produced. */
+typedef enum {
+  PETSC_VIEWER_DEFAULT = 0, PETSC_VIEWER_ASCII_MATLAB, PETSC_VIEWER_BINARY_MATLAB, PETSC_VIEWER_ASCII_VTK,
+  PETSC_VIEWER_VTK_VTS, PETSC_VIEWER_NATIVE
+} PetscViewerFormat;
+typedef enum { FILE_MODE_READ = 0, FILE_MODE_WRITE = 1, FILE_MODE_APPEND = 2 } PetscFileMode;
+typedef const char *PetscViewerType;
+#define PETSCVIEWERBINARY "binary"
+#define PETSCVIEWERASCII "ascii"
+#define PETSCVIEWERVTK "vtk"
+typedef void *PetscObject;
+PetscErrorCode PetscViewerASCIIOpen(MPI_Comm, const char *, PetscViewer *);
+PetscErrorCode PetscViewerBinaryOpen(MPI_Comm, const char *, PetscFileMode, PetscViewer *);
+PetscErrorCode PetscViewerMatlabOpen(MPI_Comm, const char *, PetscFileMode, PetscViewer *);
+PetscErrorCode PetscViewerCreate(MPI_Comm, PetscViewer *);
+PetscErrorCode PetscViewerSetType(PetscViewer, PetscViewerType);
+PetscErrorCode PetscViewerFileSetMode(PetscViewer, PetscFileMode);
+PetscErrorCode PetscViewerFileSetName(PetscViewer, const char *);
+PetscErrorCode PetscViewerSetFormat(PetscViewer, PetscViewerFormat);
+PetscErrorCode PetscViewerMatlabPutArray(PetscViewer, int, int, const PetscScalar *, const char *);
+PetscErrorCode PetscViewerDestroy(PetscViewer *);
+PetscErrorCode PetscObjectSetName(PetscObject, const char *);
+PetscErrorCode DMView(DM, PetscViewer);
+PetscErrorCode DMGetCoordinates(DM, Vec *);
+PetscErrorCode PetscOptionsGetBool(const char *, const char *, PetscBool *, PetscBool *);  /* PETSc 3.5 form */
 
 #endif

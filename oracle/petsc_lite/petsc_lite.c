@@ -411,3 +411,71 @@ int MPI_Sendrecv(const void *sb, int sc, MPI_Datatype st, int dest, int stag, vo
   if (n) memmove(rb, sb, n);
   return 0;
 }
+
+/* ---- one-rank collectives and point-to-point ---- */
+int MPI_Allgather(const void *s, int sc, MPI_Datatype st, void *r, int rc, MPI_Datatype rt, MPI_Comm c) {
+  (void)rc; (void)rt; (void)c;
+  memcpy(r, s, (size_t)sc * mpi_type_size(st));
+  return 0;
+}
+int MPI_Gather(const void *s, int sc, MPI_Datatype st, void *r, int rc, MPI_Datatype rt, int root, MPI_Comm c) {
+  (void)rc; (void)rt; (void)root; (void)c;
+  memcpy(r, s, (size_t)sc * mpi_type_size(st));
+  return 0;
+}
+int MPI_Bcast(void *b, int n, MPI_Datatype t, int root, MPI_Comm c) { (void)b; (void)n; (void)t; (void)root; (void)c; return 0; }
+int MPI_Send(const void *b, int n, MPI_Datatype t, int d, int tag, MPI_Comm c) {
+  (void)b; (void)n; (void)t; (void)d; (void)tag; (void)c;
+  return 1;  /* no other rank */
+}
+int MPI_Recv(void *b, int n, MPI_Datatype t, int s, int tag, MPI_Comm c, MPI_Status *st) {
+  (void)b; (void)n; (void)t; (void)s; (void)tag; (void)c; (void)st;
+  return 1;
+}
+
+/* ---- viewers, bags, names, options: inert ---- */
+PetscErrorCode PetscViewerASCIIOpen(MPI_Comm c, const char *n, PetscViewer *v) { (void)c; (void)n; *v = NULL; return 0; }
+PetscErrorCode PetscViewerBinaryOpen(MPI_Comm c, const char *n, PetscFileMode m, PetscViewer *v) {
+  (void)c; (void)n; (void)m; *v = NULL; return 0;
+}
+PetscErrorCode PetscViewerMatlabOpen(MPI_Comm c, const char *n, PetscFileMode m, PetscViewer *v) {
+  (void)c; (void)n; (void)m; *v = NULL; return 0;
+}
+PetscErrorCode PetscViewerCreate(MPI_Comm c, PetscViewer *v) { (void)c; *v = NULL; return 0; }
+PetscErrorCode PetscViewerSetType(PetscViewer v, PetscViewerType t) { (void)v; (void)t; return 0; }
+PetscErrorCode PetscViewerFileSetMode(PetscViewer v, PetscFileMode m) { (void)v; (void)m; return 0; }
+PetscErrorCode PetscViewerFileSetName(PetscViewer v, const char *n) { (void)v; (void)n; return 0; }
+PetscErrorCode PetscViewerSetFormat(PetscViewer v, PetscViewerFormat f) { (void)v; (void)f; return 0; }
+PetscErrorCode PetscViewerMatlabPutArray(PetscViewer v, int m, int n, const PetscScalar *a, const char *nm) {
+  (void)v; (void)m; (void)n; (void)a; (void)nm; return 0;
+}
+PetscErrorCode PetscViewerDestroy(PetscViewer *v) { if (v) *v = NULL; return 0; }
+PetscErrorCode PetscObjectSetName(PetscObject o, const char *n) { (void)o; (void)n; return 0; }
+PetscErrorCode DMView(DM d, PetscViewer v) { (void)d; (void)v; return 0; }
+PetscErrorCode DMGetCoordinates(DM d, Vec *c) { (void)d; *c = NULL; return 1; }  /* no coordinates kept */
+PetscErrorCode PetscOptionsGetBool(const char *pre, const char *name, PetscBool *v, PetscBool *set) {
+  (void)pre; (void)name; (void)v;
+  if (set) *set = PETSC_FALSE;
+  return 0;
+}
+
+#include "petscbag.h"
+struct _p_PetscBag { void *data; };
+PetscErrorCode PetscBagCreate(MPI_Comm c, size_t sz, PetscBag *b) {
+  (void)c;
+  *b = (PetscBag)calloc(1, sizeof(struct _p_PetscBag));
+  if (!*b) return 1;
+  (*b)->data = calloc(1, sz ? sz : 1);
+  return (*b)->data ? 0 : 1;
+}
+PetscErrorCode PetscBagGetData(PetscBag b, void **d) { *d = b->data; return 0; }
+PetscErrorCode PetscBagRegisterScalar(PetscBag b, void *a, PetscScalar v, const char *n, const char *h) {
+  (void)b; (void)n; (void)h;
+  *(PetscScalar *)a = v;
+  return 0;
+}
+PetscErrorCode PetscBagView(PetscBag b, PetscViewer v) { (void)b; (void)v; return 0; }
+PetscErrorCode PetscBagDestroy(PetscBag *b) {
+  if (*b) { free((*b)->data); free(*b); *b = NULL; }
+  return 0;
+}

@@ -26,6 +26,8 @@
 #include "nodalStressStrain.h"
 #include "limitTimestep.h"
 #include "retrieveSolutions.h"
+#include "io.h"
+#include "restart.h"
 #include "mic_types.h"
 
 PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da);
@@ -361,4 +363,33 @@ int ref_retrieveSolutions(refp *p, const double *S, double Kcont) {
   int e = retrieveSolutions(&p->grid, &p->nf, v, Kcont, &nan);
   VecDestroy(&v);
   return e ? -1 : nan;
+}
+
+/* saveMarkersBinary (io.c:299) of the caller's markers: writes output/Markers.<iMonte>.<iTime>
+ * under the current directory; nOut from the markers' cells */
+int ref_saveMarkersBinary(refp *p, mic_marker *m, int n, int iMonte, int iTime, double elapsed) {
+  p->ms.markers = (Marker *)m;
+  p->ms.nMark = n;
+  p->ms.maxMark = n;
+  int nout = 0;
+  for (int k = 0; k < n; ++k) nout += m[k].cellX == -1;
+  p->ms.nOut = nout;
+  return saveMarkersBinary(&p->ms, iMonte, iTime, elapsed);
+}
+
+/* restartFromMarkers (restart.c:8): reads output/Markers.<iMonte>.<iTime>, allocates with
+ * maxMarkFactor, bins; copies up to cap markers out; returns nMark (or -1) */
+int ref_restartFromMarkers(refp *p, int iMonte, int iTime, double maxMarkFactor, mic_marker *out, int cap,
+                           double *elapsed) {
+  MarkerSet ms;
+  memset(&ms, 0, sizeof(ms));
+  p->opt.maxMarkFactor = maxMarkFactor;
+  PetscScalar t = 0.0;
+  if (restartFromMarkers(&ms, &p->grid, &p->mat, &p->opt, iMonte, iTime, &t)) return -1;
+  *elapsed = t;
+  const int n = ms.nMark < cap ? ms.nMark : cap;
+  memcpy(out, ms.markers, sizeof(Marker) * (size_t)n);
+  const int total = ms.nMark;
+  free(ms.markers);
+  return total;
 }

@@ -63,6 +63,8 @@ def lib():
                                             ctypes.POINTER(ctypes.c_ushort)]),
             "ref_distributeMarkersUniformInDomain": (_I, [_P, _P, _I, _I, _I]),
             "ref_nodalStressStrain": (_I, [_P, _D, _D]),
+            "ref_saveMarkersBinary": (_I, [_P, _P, _I, _I, _I, _D]),
+            "ref_restartFromMarkers": (_I, [_P, _I, _I, _D, _P, _I, _DP]),
             "ref_limitDisplacementTimestep": (_D, [_P, _D, _D]),
             "ref_retrieveSolutions": (_I, [_P, _DP, _D]),
             "ref_stage_seconds": (_D, [_I]),
@@ -100,6 +102,24 @@ class RefProblem:
         L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         for name, arr in wl.nodal.items():
             self.set_nodal(name, arr)
+
+    def saveMarkersBinary(self, iMonte, iTime, elapsed_time):
+        """writes output/Markers.<iMonte>.<iTime> under the current directory"""
+        L = lib()
+        e = L.ref_saveMarkersBinary(self.h, self.markers.ctypes.data, len(self.markers), iMonte, iTime, elapsed_time)
+        L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        return e
+
+    def restartFromMarkers(self, iMonte, iTime, cap, maxMarkFactor=1.0):
+        L = lib()
+        mk = np.zeros(cap, dtype=self.markers.dtype)
+        t = ctypes.c_double(0.0)
+        n = L.ref_restartFromMarkers(self.h, iMonte, iTime, maxMarkFactor, mk.ctypes.data, cap, ctypes.byref(t))
+        if n < 0:
+            raise IOError("restartFromMarkers failed")
+        self.markers = mk[:n].copy()
+        L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        return t.value
 
     def nodalStressStrain(self, dt, gy=0.0):
         return lib().ref_nodalStressStrain(self.h, dt, gy)

@@ -231,6 +231,40 @@ def grid_table():
     return out
 
 
+def checkpoint_case():
+    """the VEP box after a step, with some markers pushed out of the domain"""
+    wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2)
+    m = wl.markers
+    m["X"][::37] = -1.0
+    m["Y"][5::41] = wl.grid.LY * 1.5
+    return wl
+
+
+def checkpoint_table():
+    """saveMarkersBinary / restartFromMarkers (io.c:299, restart.c:8) of the reference: input
+    markers (cells found), the file's bytes, and the markers restarted from it."""
+    import tempfile
+
+    wl = checkpoint_case()
+    R = refpy.RefProblem(wl)
+    R.findMarkerCells()
+    before = _fields_only(R.markers)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        try:
+            os.mkdir("output")
+            R.saveMarkersBinary(0, 7, 1.25e13)
+            raw = np.fromfile(os.path.join("output", "Markers.0.7"), dtype=np.uint8)
+            t = R.restartFromMarkers(0, 7, len(before) + 10)
+        finally:
+            os.chdir(cwd)
+    after = _fields_only(R.markers)
+    after["srr"] = 0.0  # never read from the file; the reference leaves it as allocated
+    return {"markers_in": before.view(np.uint8).reshape(len(before), -1), "file_bytes": raw,
+            "restart": after.view(np.uint8).reshape(len(after), -1), "elapsed": np.float64(t)}
+
+
 def main():
     if obuild.build_ref() is None:
         raise SystemExit("reference tree not found; golden vectors can only be generated where it exists")
@@ -240,6 +274,9 @@ def main():
     if sys.argv[1:] in ([], ["density"]):
         np.savez_compressed(os.path.join(OUT, "marker_density.npz"), **density_table())
         print("wrote marker_density")
+    if sys.argv[1:] in ([], ["checkpoint"]):
+        np.savez_compressed(os.path.join(OUT, "marker_checkpoint.npz"), **checkpoint_table())
+        print("wrote marker_checkpoint")
     if sys.argv[1:] in ([], ["grid"]):
         np.savez_compressed(os.path.join(OUT, "grid_routines.npz"), **grid_table())
         print("wrote grid_routines")

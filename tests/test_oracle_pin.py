@@ -361,3 +361,38 @@ def test_grid_routines_match_golden(kind):
     for name in ("vx", "vy", "p"):
         ok, msg = exact(O.get_nodal(name), z["%s_ret_%s" % (kind, name)])
         assert ok, (name, msg)
+
+
+def test_checkpoint_matches_golden(tmp_path):
+    """the reference's marker file format, byte for byte, and the restart from it"""
+    z = np.load(os.path.join(GOLDEN, "marker_checkpoint.npz"))
+    wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2)
+    before = z["markers_in"].view(MARKER_DTYPE).ravel()
+    O = oraclepy.OracleProblem(wl, markers=before)
+    path = str(tmp_path / "Markers.0.7")
+    O.saveMarkersBinary(path, 1.25e13)
+    assert np.array_equal(np.fromfile(path, dtype=np.uint8), z["file_bytes"])
+    t = O.restartFromMarkers(path, len(before) + 10)
+    assert t == float(z["elapsed"])
+    ok, msg = same_fields(O.markers, z["restart"].view(MARKER_DTYPE).ravel())
+    assert ok, msg
+
+
+@needs_ref
+def test_checkpoint_matches_reference_build(tmp_path, monkeypatch):
+    wl = W.convection_box(ncell=8, nm=4, seed=1)
+    wl.markers["X"][3::29] = -0.5
+    R, O = refpy.RefProblem(wl), oraclepy.OracleProblem(wl)
+    R.findMarkerCells()
+    O.findMarkerCells()
+    monkeypatch.chdir(tmp_path)
+    os.mkdir("output")
+    R.saveMarkersBinary(2, 11, 3.5)
+    O.saveMarkersBinary(str(tmp_path / "mine"), 3.5)
+    assert np.array_equal(np.fromfile("output/Markers.2.11", dtype=np.uint8), np.fromfile("mine", dtype=np.uint8))
+    R.restartFromMarkers(2, 11, len(wl.markers))
+    O.restartFromMarkers(str(tmp_path / "mine"), len(wl.markers))
+    a, b = R.markers.copy(), O.markers.copy()
+    a["srr"] = b["srr"] = 0.0
+    ok, msg = same_fields(a, b)
+    assert ok, msg
