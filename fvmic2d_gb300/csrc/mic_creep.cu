@@ -548,3 +548,20 @@ extern "C" int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iteratio
   if (tc_timeouts) *tc_timeouts = (int64_t)h.tc_timeouts;
   return MIC_OK;
 }
+
+// ---- the survey's names for the closure's exports ----------------------------------------------
+
+// exact composite-creep Newton solve of a host batch (mic_creep_solve_batch, mode 0)
+extern "C" int mic_creep_newton(mic_ctx *ctx, const double *edot, const double *T, const double *d,
+                                const double *P, int64_t n, double *stress, int32_t *iterations, double *residual) {
+  return mic_creep_solve_batch(ctx, edot, T, d, P, n, 0, stress, iterations, residual, nullptr);
+}
+
+extern "C" int mic_surrogate_train(mic_ctx *ctx, int64_t nsamples, int batch, int steps, float lr,
+                                   unsigned long long seed, float *loss_hist) {
+  return mic_creep_train(ctx, nsamples, batch, steps, lr, seed, loss_hist);
+}
+
+extern "C" int mic_surrogate_infer(mic_ctx *ctx, const float *feat, int64_t n, int mode, float *y) {
+  return mic_creep_mlp_infer(ctx, feat, n, mode, y);
+}

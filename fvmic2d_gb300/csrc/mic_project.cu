@@ -660,3 +660,20 @@ extern "C" int mic_project_marker_field_to_nodes(mic_ctx *ctx, int off, const do
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return MIC_OK;
 }
+
+// projectMarkersNodesFromScalar (markers.c:1507-1594): a per-marker array in the caller's order
+// projected onto the basic nodes (the bilinear weights of each marker's basic cell), divided by
+// the weights; zero where nothing contributes
+extern "C" int mic_project_markers_nodes_from_scalar(mic_ctx *ctx, const double *values, int out_field) {
+  if (!ctx || (!values && ctx->n > 0) || out_field < 0 || out_field >= MIC_NF_COUNT) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int e = mic_ensure_sorted(ctx);
+  if (e) return e;
+  if (ctx->n > 0) {
+    MIC_CUDA_TRY(cudaMemcpyAsync(ctx->scr1, values, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->stream));
+    if ((e = mic_gather_by_id(ctx, ctx->scr1, ctx->scr2))) return e;
+  }
+  if ((e = mic_project_scalar(ctx, ctx->scr2, 0, ctx->nodal[out_field]))) return e;
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}

@@ -89,6 +89,10 @@ SIGNATURES = {
     "mic_ensemble_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "mic_check_marker_density": (_I, [_P, _P, _I64P, _I64P]),
     "mic_nodal_stress_strain": (_I, [_P, _D, _D]),
+    "mic_project_markers_nodes_from_scalar": (_I, [_P, _DP, _I]),
+    "mic_creep_newton": (_I, [_P, _DP, _DP, _DP, _DP, _I64, _DP, _P, _DP]),
+    "mic_surrogate_train": (_I, [_P, _I64, _I, _I, ctypes.c_float, ctypes.c_uint64, _P]),
+    "mic_surrogate_infer": (_I, [_P, _P, _I64, _I, _P]),
     "mic_save_markers_binary": (_I, [_P, ctypes.c_char_p, _D]),
     "mic_restart_from_markers": (_I, [_P, ctypes.c_char_p, _DP]),
     "mic_limit_displacement_timestep": (_I, [_P, _D, _DP]),
@@ -187,6 +191,12 @@ class MicProblem:
                     "mic_distribute_markers_uniform_in_domain")
         self.n = n.value
         return self.n
+
+    def projectMarkersNodesFromScalar(self, values, nodal):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self.L.mic_project_markers_nodes_from_scalar(self.h, _dp(v), NF[nodal]),
+                    "mic_project_markers_nodes_from_scalar")
+        return 0
 
     def saveMarkersBinary(self, path, elapsed_time):
         self._check(self.L.mic_save_markers_binary(self.h, os.fsencode(path), elapsed_time), "mic_save_markers_binary")

@@ -164,6 +164,13 @@ int mic_creep_solve_batch(mic_ctx *ctx, const double *edot, const double *T, con
 /* surrogate network outputs y[n] for normalised features feat[n][4] (host arrays) with the
  * context's parameters: mode 1 FP32 on the CUDA cores, mode 2 hidden layer on the tensor cores */
 int mic_creep_mlp_infer(mic_ctx *ctx, const float *feat, int64_t n, int mode, float *y);
+/* the same entry points under the names of the reference-side plan: exact Newton batch solve
+ * (mic_creep_solve_batch, mode 0), surrogate training and inference */
+int mic_creep_newton(mic_ctx *ctx, const double *edot, const double *T, const double *d, const double *P, int64_t n,
+                     double *stress, int32_t *iterations, double *residual);
+int mic_surrogate_train(mic_ctx *ctx, int64_t nsamples, int batch, int steps, float lr, unsigned long long seed,
+                        float *loss_hist);
+int mic_surrogate_infer(mic_ctx *ctx, const float *feat, int64_t n, int mode, float *y);
 /* counters of the last law-7 pass (checkPlasticYielding or a batch solve): markers solved, Newton
  * iterations, exact fallbacks, largest final |rate/edot - 1|, tensor-core tiles whose completion
  * wait ran out (their markers took the exact solve) */
@@ -200,6 +207,10 @@ int mic_distribute_markers_uniform_in_domain(mic_ctx *ctx, int NMX, int NMY, uns
 /* set one marker field, addressed as offsetof(mic_marker, field), to value for every marker
  * (integer fields take (int)value) -- the per-marker initial-condition loops of the host code */
 int mic_markers_fill(mic_ctx *ctx, int field_offset, double value);
+
+/* projectMarkersNodesFromScalar (markers.c:1507): a per-marker array (caller order, n values)
+ * projected onto the basic nodes and divided by the weights, into nodal field out_field */
+int mic_project_markers_nodes_from_scalar(mic_ctx *ctx, const double *values, int out_field);
 
 /* ---- grid routines between the solves ----
  * nodalStressStrain (nodalStressStrain.c:6): from vx, vy (MIC_NF_VX/VY), etaN/S, muN/S and the

@@ -1476,3 +1476,41 @@ int64_t orc_restart_from_markers(orc_ctx *c, const char *path, mic_marker *mk, i
   orc_find_marker_cells(c, mk, cnt, &err);
   return err ? -1 : cnt;
 }
+
+/* projectMarkersNodesFromScalar (markers.c:1507-1594): a per-marker array (caller order)
+ * projected bilinearly onto the basic nodes of each marker's cell, divided by the weights
+ * (zero where no marker contributes) */
+int orc_project_from_scalar(orc_ctx *c, const mic_marker *mk, int64_t n, const double *v, int field) {
+  if (field < 0 || field >= MIC_NF_COUNT) return ORC_ERR_ARG;
+  const int NX = c->NX;
+  const size_t nn = (size_t)c->NX * c->NY;
+  double *nf = (double *)calloc(nn, sizeof(double)), *wt = (double *)calloc(nn, sizeof(double));
+  for (int64_t m = 0; m < n; ++m) {
+    const mic_marker *p = &mk[m];
+    if (p->cellX == -1) continue;
+    const int i = p->cellX, j = p->cellY;
+    const double dx = c->x[i + 1] - c->x[i], dy = c->y[j + 1] - c->y[j];
+    const double mdx = (p->X - c->x[i]) / dx, mdy = (p->Y - c->y[j]) / dy;
+    const size_t k00 = (size_t)j * NX + i;
+    double w = (1.0 - mdx) * (1.0 - mdy);
+    wt[k00] += w;
+    nf[k00] += w * v[m];
+    w = mdx * (1.0 - mdy);
+    wt[k00 + 1] += w;
+    nf[k00 + 1] += w * v[m];
+    w = (1.0 - mdx) * mdy;
+    wt[k00 + NX] += w;
+    nf[k00 + NX] += w * v[m];
+    w = mdx * mdy;
+    wt[k00 + NX + 1] += w;
+    nf[k00 + NX + 1] += w * v[m];
+  }
+  double *out = c->nodal[field];
+  for (size_t k = 0; k < nn; ++k) {
+    const double w = 0.0 + wt[k];
+    out[k] = (w != 0.0) ? (0.0 + nf[k]) / w : 0.0;
+  }
+  free(nf);
+  free(wt);
+  return ORC_OK;
+}

@@ -95,6 +95,7 @@ void orc_retrieve_solutions(orc_ctx *c, const double *S, double Kcont);
 /* marker checkpoint in the reference's field-major binary format (io.c:299, restart.c:8) */
 int orc_save_markers_binary(const char *path, const mic_marker *mk, int64_t n, double elapsed);
 int64_t orc_restart_from_markers(orc_ctx *c, const char *path, mic_marker *mk, int64_t cap, double *elapsed);
+int orc_project_from_scalar(orc_ctx *c, const mic_marker *mk, int64_t n, const double *v, int field);
 int64_t orc_check_marker_density(orc_ctx *c, mic_marker *mk, int64_t n, int64_t cap, const mic_density_options *d,
                                  uint64_t *state, int64_t *n_added, int64_t *n_removed);
 

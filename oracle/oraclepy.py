@@ -58,6 +58,7 @@ def lib():
             "orc_reset_markers": (None, [_P, _I64]),
             "orc_srand48_state": (ctypes.c_uint64, [ctypes.c_long]),
             "orc_nodal_stress_strain": (None, [_P, _D]),
+            "orc_project_from_scalar": (_I, [_P, _P, _I64, _DP, _I]),
             "orc_save_markers_binary": (_I, [ctypes.c_char_p, _P, _I64, _D]),
             "orc_restart_from_markers": (_I64, [_P, ctypes.c_char_p, _P, _I64, _DP]),
             "orc_limit_displacement_timestep": (_D, [_P, _D, _D]),
@@ -140,6 +141,10 @@ class OracleProblem:
             raise IOError(path)
         self.markers = mk[:n].copy()
         return t.value
+
+    def projectMarkersNodesFromScalar(self, values, nodal):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        return lib().orc_project_from_scalar(self.h, self._m, self.n, _dp(v), NF[nodal])
 
     def nodalStressStrain(self, dt, gy=0.0):
         lib().orc_nodal_stress_strain(self.h, dt)

@@ -393,3 +393,10 @@ int ref_restartFromMarkers(refp *p, int iMonte, int iTime, double maxMarkFactor,
   free(ms.markers);
   return total;
 }
+
+/* projectMarkersNodesFromScalar (markers.c:1507) of a per-marker array into a nodal field */
+int ref_projectMarkersNodesFromScalar(refp *p, double *values, int out_id) {
+  Vec *f = field_vec(p, out_id);
+  if (!f) return -1;
+  return projectMarkersNodesFromScalar(&p->ms, &p->grid, values, *f);
+}

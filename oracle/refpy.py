@@ -63,6 +63,7 @@ def lib():
                                             ctypes.POINTER(ctypes.c_ushort)]),
             "ref_distributeMarkersUniformInDomain": (_I, [_P, _P, _I, _I, _I]),
             "ref_nodalStressStrain": (_I, [_P, _D, _D]),
+            "ref_projectMarkersNodesFromScalar": (_I, [_P, _DP, _I]),
             "ref_saveMarkersBinary": (_I, [_P, _P, _I, _I, _I, _D]),
             "ref_restartFromMarkers": (_I, [_P, _I, _I, _D, _P, _I, _DP]),
             "ref_limitDisplacementTimestep": (_D, [_P, _D, _D]),
@@ -120,6 +121,10 @@ class RefProblem:
         self.markers = mk[:n].copy()
         L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         return t.value
+
+    def projectMarkersNodesFromScalar(self, values, nodal):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        return lib().ref_projectMarkersNodesFromScalar(self.h, _dp(v), NF[nodal])
 
     def nodalStressStrain(self, dt, gy=0.0):
         return lib().ref_nodalStressStrain(self.h, dt, gy)

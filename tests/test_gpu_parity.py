@@ -362,3 +362,28 @@ def test_constant_field_reproduction_and_partition_of_unity():
         v = G.get_nodal(f)
         nz = v != 0.0
         assert np.all(np.abs(v[nz] - 3.0e21) <= 1e-14 * 3.0e21)
+
+
+def test_project_from_scalar_matches_oracle():
+    """projectMarkersNodesFromScalar (markers.c:1507) of a per-marker array in caller order"""
+    wl = W.vep_slab_box(nx_cells=32, ny_cells=8, nm=4, seed=3)
+    G, O = gpu.MicProblem(wl), oraclepy.OracleProblem(wl)
+    G.findMarkerCells()
+    O.findMarkerCells()
+    v = W.splitmix64_uniform(43, len(wl.markers)) - 0.3
+    G.projectMarkersNodesFromScalar(v, "lastT")
+    O.projectMarkersNodesFromScalar(v, "lastT")
+    ok, msg = close(G.get_nodal("lastT"), O.get_nodal("lastT"), RTOL)
+    assert ok, msg
+
+
+def test_survey_named_exports():
+    wl = W.ice_creep_box(nx_cells=8, ny_cells=8, nm=2, seed=4)
+    G = gpu.MicProblem(wl)
+    L = G.L
+    e = np.array([1e-14, 3e-12]); T = np.array([200.0, 250.0]); d = np.array([1e-3, 1e-2]); P = np.array([1e6, 2e7])
+    s = np.zeros(2); it = np.zeros(2, dtype=np.int32); r = np.zeros(2)
+    assert L.mic_creep_newton(G.h, *[x.ctypes.data_as(gpu._DP) for x in (e, T, d, P)], 2,
+                              s.ctypes.data_as(gpu._DP), it.ctypes.data, r.ctypes.data_as(gpu._DP)) == 0
+    s2, _, _, _ = G.creep_solve(e, T, d, P, mode=0)
+    assert np.array_equal(s, s2)

@@ -396,3 +396,16 @@ def test_checkpoint_matches_reference_build(tmp_path, monkeypatch):
     a["srr"] = b["srr"] = 0.0
     ok, msg = same_fields(a, b)
     assert ok, msg
+
+
+@needs_ref
+def test_project_from_scalar_matches_reference_build():
+    wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2)
+    R, O = refpy.RefProblem(wl), oraclepy.OracleProblem(wl)
+    R.findMarkerCells()
+    O.findMarkerCells()
+    v = W.splitmix64_uniform(41, len(wl.markers)) - 0.3
+    R.projectMarkersNodesFromScalar(v, "lastT")
+    O.projectMarkersNodesFromScalar(v, "lastT")
+    ok, msg = exact(O.get_nodal("lastT"), R.get_nodal("lastT"))
+    assert ok, msg
