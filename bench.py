@@ -373,6 +373,25 @@ def run_ours(args):
     for _, p, _ in up_bufs + down_bufs:
         L.mic_host_free(p)
 
+    # ---- density control (checkMarkerDensity, called every step by the reference) after the
+    # timed steps moved the markers; the reference's default bounds (1 and 100 per quarter cell)
+    from fvmic2d_gb300.mic_types import DensityOptions
+
+    dens = None
+    if rank == 0:  # after the end-to-end run: the marker count may change
+        dopt = DensityOptions(NMX=4, NMY=4, minMarkers=1, maxMarkers=100)
+        G.synchronize()
+        t0 = time.perf_counter()
+        reps = 5
+        tot_add = tot_rem = 0
+        for _ in range(reps):
+            a, r_ = G.checkMarkerDensity(dopt)
+            tot_add += a
+            tot_rem += r_
+        dens = {"ms_per_call": (time.perf_counter() - t0) * 1e3 / reps, "markers_added": tot_add,
+                "markers_removed": tot_rem, "calls": reps,
+                "note": "host wall time per call, including its host synchronisations"}
+
     if rank != 0:
         return
     # ---- roofline of the dominant kernel (live CUDA-event timing over the timed region) ------
@@ -420,6 +439,7 @@ def run_ours(args):
                           "frac": step_gbs / hbm_peak},
         "kernel_share": {k: round(v[0] / prof_total, 4) for k, v in kern[:12]},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kern[:12]},
+        "density_control": dens,
         "surrogate": surrogate_leg(args, local) if not args.no_surrogate else None,
         "ensemble": ensemble_leg(args, local) if not args.no_ensemble else None,
         "ice_ensemble": ice_ensemble_leg(args, local) if not args.no_ensemble else None,

@@ -16,8 +16,12 @@
 //   positions one thread per quarter cell, values by skip-ahead, recycled or appended slot;
 //   neighbours one warp per new marker over the static candidate set (markers that were in the
 //             domain before the call and not removed);
-//   fill      one warp, in order: the only order-dependent part -- a recycled slot filled by an
-//             earlier new marker becomes a candidate for later ones (per-cell lists).
+//   fill      the only order-dependent part -- a recycled slot filled by an earlier new marker
+//             becomes a candidate for later ones.  Decisions for all new markers at once from
+//             estimated facts about the earlier ones, roots of the chains of copies by pointer
+//             jumping, repeated until the estimates reproduce themselves; then one copy per slot.
+//             A slot recycled twice (the reference's over-removal case), or no fixed point within
+//             64 rounds, falls back to one warp walking the new markers in order.
 // The drand48 stream (the reference's drand48() calls and its PETSCRAND48 object share it) is a
 // 48-bit state kept in the context.
 #include <cmath>
@@ -227,6 +231,7 @@ __global__ void __launch_bounds__(256) k_density_remove(Params P, const int *__r
   for (int e = threadIdx.x; e < toRemove; e += blockDim.x) {
     // all candidates gone: the reference's search falls back to the first one
     const int k = e < N ? (int)(pick[e] & 0xFFFF) : 0;
+    if (e >= N) err[1] = 1;  // a slot listed twice: only the in-order fill gives the reference's result
     const int slot = (int)(cand[k] & 0xFFFFFFFFULL);
     isout[out0 + qrem[r] + e] = (int)(cand[k] >> 32);
     c.f[C_X][slot] = -1.0;
@@ -323,6 +328,196 @@ __global__ void k_density_nn(Params P, const int *__restrict__ cell_start, DCols
   }
 }
 
+// new_slab_marker / new_inflow_marker (benchmarkInitialConditions.c:44-66) + findMarkerCell into
+// slot; cpu and the strain-rate residual, which the reference leaves uninitialised, are 0
+__device__ void build_inflow_marker(const Params &P, const mic_materials &M, const mic_options &O,
+                                    const CreepConfig &cfg, const DCols &c, int nf, const mic_density_options &d,
+                                    int kind, double xv, double yv, int slot) {
+  for (int f = 0; f < nf; ++f) c.f[f][slot] = 0.0;
+  if (nf > C_GRAIN) c.f[C_GRAIN][slot] = 1e-3;
+  for (int f = 0; f < C_I32_COUNT; ++f)
+    if (f != C_ID) c.i[f][slot] = 0;
+  double T;
+  if (kind == 1) {  // slab_inflow_temperature (benchmarkInitialConditions.c:124-134)
+    const double slab_age_s = d.slabAge * 1.0e6 * 3.15576e7;
+    T = 273.0 + (1623.0 - 273.0) * erf((yv - xv * tan(d.slabAngle)) / (2.0 * sqrt(0.7272e-6 * slab_age_s)));
+  } else {
+    T = 1573.0;  // mantle_temperature
+  }
+  c.f[C_X][slot] = xv;
+  c.f[C_Y][slot] = yv;
+  c.f[C_T][slot] = T;
+  c.i[C_MAT][slot] = 0;
+  double eta, mu;
+  CreepIn ci = {0.0, 0.0, 0.0, 1e-3, 0.0, 0.0, 0, 0, 0.0, 0, {}};
+  CreepConfig exact = cfg;
+  exact.mode = 0;
+  if (rheology(M, O, 0, T, xv, yv, eta, mu, &exact, &ci)) {
+    c.f[C_ETA][slot] = eta;
+    c.f[C_MU][slot] = mu;
+  }
+  const bool in = xv >= 0.0 && yv >= 0.0 && xv <= P.LX && yv <= P.LY;
+  c.i[C_CELLX][slot] = in ? bisect(P.x, P.NX, xv) : -1;
+  c.i[C_CELLY][slot] = in ? bisect(P.y, P.NY, yv) : -1;
+}
+
+// cell holding a (clamped) position
+__device__ __forceinline__ int pos_cell(const Params &P, double xv, double yv) {
+  return bisect(P.y, P.NY, fmin(fmax(yv, P.y[0]), P.y[P.NY - 1])) * (P.NX - 1) +
+         bisect(P.x, P.NX, fmin(fmax(xv, P.x[0]), P.x[P.NX - 1]));
+}
+
+// ---- parallel fill ------------------------------------------------------------------------
+// Taken in order, new marker t copies the nearest of the static candidates and of the recycled
+// slots that earlier new markers t' < t filled inside its window.  A copy keeps its source's cell
+// until the next binning, so the window test of a later marker against t' uses the cell of t''s
+// root: the static or inflow marker at the start of its chain of copies.  Three facts about t'
+// enter later decisions: whether it was filled, its root's cell and its position (known).  The
+// facts are estimated for every t' at once, every decision is taken from the estimates, roots are
+// found by pointer jumping and the facts recomputed.  Decisions look only backwards, so estimates
+// that reproduce themselves give the in-order result (by induction over t); each slot then takes
+// its root's columns and its own position.
+
+__global__ void k_density_bucket(Params P, const double *__restrict__ nx, const double *__restrict__ ny, int nrec,
+                                 int *tcell, int *ccount) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrec) return;
+  const int cell = pos_cell(P, nx[t], ny[t]);
+  tcell[t] = cell;
+  atomicAdd(&ccount[cell], 1);
+}
+
+__global__ void k_density_scatter(const int *__restrict__ tcell, const int *__restrict__ cstart, int nrec, int *cfill,
+                                  int *clist) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrec) return;
+  const int cell = tcell[t];
+  clist[cstart[cell] + atomicAdd(&cfill[cell], 1)] = t;
+}
+
+// first estimates: every new marker filled, its root in its own cell
+__global__ void k_density_guess(Params P, const double *__restrict__ nx, const double *__restrict__ ny, int nadd,
+                                int *ewrote, int *ecx, int *ecy) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nadd) return;
+  ewrote[t] = 1;
+  ecx[t] = bisect(P.x, P.NX, fmin(fmax(nx[t], P.x[0]), P.x[P.NX - 1]));
+  ecy[t] = bisect(P.y, P.NY, fmin(fmax(ny[t], P.y[0]), P.y[P.NY - 1]));
+}
+
+// markers.c:740-760 for new marker t against the recycled slots of earlier new markers, with the
+// estimated facts; the static candidates' best is already known
+__global__ void k_density_decide(Params P, const double *__restrict__ nx, const double *__restrict__ ny,
+                                 const int *__restrict__ kind, const int *__restrict__ tid,
+                                 const double *__restrict__ best_r, const int *__restrict__ best_id,
+                                 const int *__restrict__ cstart, const int *__restrict__ clist, int nadd, double wmax,
+                                 double hmax, const int *__restrict__ ewrote, const int *__restrict__ ecx,
+                                 const int *__restrict__ ecy, int *src, int *ptr) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nadd) return;
+  int bt = -1;
+  if (kind[t] == 0) {
+    const int id = tid[t];
+    const double xv = nx[t], yv = ny[t];
+    double br = best_r[t];
+    int bid = best_id[t];
+    int cx0, cx1, cy0, cy1;
+    window(P.x, P.NX, xv, wmax, cx0, cx1);
+    window(P.y, P.NY, yv, hmax, cy0, cy1);
+    for (int cy = cy0; cy <= cy1; ++cy)
+      for (int cx = cx0; cx <= cx1; ++cx) {
+        const int cell = cy * (P.NX - 1) + cx;
+        for (int e = cstart[cell]; e < cstart[cell + 1]; ++e) {
+          const int t2 = clist[e];
+          if (t2 >= t || !ewrote[t2]) continue;
+          const int id2 = tid[t2];
+          const int mx = ecx[t2], my = ecy[t2];
+          if (id2 == id || mx == -1) continue;
+          const double xm = nx[t2], ym = ny[t2];
+          if (fabs(xm - xv) <= (P.x[mx + 1] - P.x[mx]) && fabs(ym - yv) <= (P.y[my + 1] - P.y[my])) {
+            const double x1 = xm - xv, y1 = ym - yv;
+            const double r1 = sqrt(__dadd_rn(__dmul_rn(x1, x1), __dmul_rn(y1, y1)));
+            if (better(r1, id2, br, bid)) {
+              br = r1;
+              bid = id2;
+              bt = t2;
+            }
+          }
+        }
+      }
+  }
+  src[t] = bt;
+  ptr[t] = bt >= 0 ? bt : t;
+}
+
+__global__ void k_density_jump(const int *__restrict__ in, int *out, int nadd) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nadd) out[t] = in[in[t]];
+}
+
+// the facts the decisions imply: filled, root cell, root slot; any change from the estimates
+// means another round
+__global__ void k_density_facts(Params P, DCols c, const double *__restrict__ nx, const double *__restrict__ ny,
+                                const int *__restrict__ kind, const int *__restrict__ tslot,
+                                const int *__restrict__ best_slot, const int *__restrict__ src,
+                                const int *__restrict__ root, int nadd, int *ewrote, int *ecx, int *ecy, int *rslot,
+                                int *changed) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nadd) return;
+  const int r = root[t];
+  int w = 0, cx = -1, cy = -1, rs = -1;
+  if (kind[r] != 0) {  // inflow marker: findMarkerCell of its own position
+    const double xv = nx[r], yv = ny[r];
+    const bool in = xv >= 0.0 && yv >= 0.0 && xv <= P.LX && yv <= P.LY;
+    w = 1;
+    cx = in ? bisect(P.x, P.NX, xv) : -1;
+    cy = in ? bisect(P.y, P.NY, yv) : -1;
+    rs = tslot[r];
+  } else if (best_slot[r] >= 0) {
+    rs = best_slot[r];
+    w = 1;
+    cx = c.i[C_CELLX][rs];
+    cy = c.i[C_CELLY][rs];
+  }
+  if (src[t] >= 0) w = 1;
+  rslot[t] = rs;
+  if (w != ewrote[t] || cx != ecx[t] || cy != ecy[t]) {
+    ewrote[t] = w;
+    ecx[t] = cx;
+    ecy[t] = cy;
+    *changed = 1;
+  }
+}
+
+__global__ void k_density_build(Params P, mic_materials M, mic_options O, CreepConfig cfg, DCols c, int nf,
+                                mic_density_options d, const double *__restrict__ nx, const double *__restrict__ ny,
+                                const int *__restrict__ kind, const int *__restrict__ tid,
+                                const int *__restrict__ tslot, int nadd, int64_t nmark) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nadd || kind[t] == 0) return;
+  build_inflow_marker(P, M, O, cfg, c, nf, d, kind[t], nx[t], ny[t], tslot[t]);
+  if (tid[t] >= nmark) c.i[C_ID][tslot[t]] = tid[t];
+}
+
+// markers[idx] = markers[minidx] with the new position (markers.c:761-764); the source's columns
+// are its root's
+__global__ void k_density_copy(DCols c, int nf, const double *__restrict__ nx, const double *__restrict__ ny,
+                               const int *__restrict__ kind, const int *__restrict__ tid,
+                               const int *__restrict__ tslot, const int *__restrict__ ewrote,
+                               const int *__restrict__ rslot, int nadd, int64_t nmark) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nadd || kind[t] != 0) return;
+  const int slot = tslot[t], rs = rslot[t];
+  if (ewrote[t] && rs >= 0) {
+    for (int f = 0; f < nf; ++f) c.f[f][slot] = c.f[f][rs];
+    for (int f = 0; f < C_I32_COUNT; ++f)
+      if (f != C_ID) c.i[f][slot] = c.i[f][rs];
+    c.f[C_X][slot] = nx[t];
+    c.f[C_Y][slot] = ny[t];
+  }
+  if (tid[t] >= nmark) c.i[C_ID][slot] = tid[t];
+}
+
 // one warp, new markers in order (markers.c:720-765)
 __global__ void k_density_fill(Params P, mic_materials M, mic_options O, CreepConfig cfg, DCols c, int nf,
                                mic_density_options d, const double *__restrict__ nx, const double *__restrict__ ny,
@@ -337,34 +532,7 @@ __global__ void k_density_fill(Params P, mic_materials M, mic_options O, CreepCo
     const double xv = nx[t], yv = ny[t];
     bool wrote = false;
     if (kind[t] != 0) {
-      if (lane == 0) {  // new_slab_marker / new_inflow_marker (benchmarkInitialConditions.c:44-66)
-        for (int f = 0; f < nf; ++f) c.f[f][slot] = 0.0;
-        if (nf > C_GRAIN) c.f[C_GRAIN][slot] = 1e-3;
-        for (int f = 0; f < C_I32_COUNT; ++f)
-          if (f != C_ID) c.i[f][slot] = 0;
-        double T;
-        if (kind[t] == 1) {  // slab_inflow_temperature (benchmarkInitialConditions.c:124-134)
-          const double slab_age_s = d.slabAge * 1.0e6 * 3.15576e7;
-          T = 273.0 + (1623.0 - 273.0) * erf((yv - xv * tan(d.slabAngle)) / (2.0 * sqrt(0.7272e-6 * slab_age_s)));
-        } else {
-          T = 1573.0;  // mantle_temperature
-        }
-        c.f[C_X][slot] = xv;
-        c.f[C_Y][slot] = yv;
-        c.f[C_T][slot] = T;
-        c.i[C_MAT][slot] = 0;
-        double eta, mu;
-        CreepIn ci = {0.0, 0.0, 0.0, 1e-3, 0.0, 0.0, 0, 0, 0.0, 0, {}};
-        CreepConfig exact = cfg;
-        exact.mode = 0;
-        if (rheology(M, O, 0, T, xv, yv, eta, mu, &exact, &ci)) {
-          c.f[C_ETA][slot] = eta;
-          c.f[C_MU][slot] = mu;
-        }
-        const bool in = xv >= 0.0 && yv >= 0.0 && xv <= P.LX && yv <= P.LY;
-        c.i[C_CELLX][slot] = in ? bisect(P.x, P.NX, xv) : -1;
-        c.i[C_CELLY][slot] = in ? bisect(P.y, P.NY, yv) : -1;
-      }
+      if (lane == 0) build_inflow_marker(P, M, O, cfg, c, nf, d, kind[t], xv, yv, slot);
       wrote = true;
     } else {
       double br = best_r[t];
@@ -416,8 +584,7 @@ __global__ void k_density_fill(Params P, mic_materials M, mic_options O, CreepCo
     if (lane == 0) {
       if (id >= nmark) c.i[C_ID][slot] = id;  // appended slot
       if (wrote && id < nmark) {  // a recycled slot joins the candidates of later new markers
-        const int cell = bisect(P.y, P.NY, fmin(fmax(yv, P.y[0]), P.y[P.NY - 1])) * (P.NX - 1) +
-                         bisect(P.x, P.NX, fmin(fmax(xv, P.x[0]), P.x[P.NX - 1]));
+        const int cell = pos_cell(P, xv, yv);
         next[t] = heads[cell];
         heads[cell] = t;
       }
@@ -471,12 +638,19 @@ extern "C" int mic_density_rng_state(mic_ctx *ctx, uint64_t *get, const uint64_t
   return MIC_OK;
 }
 
+extern "C" int mic_density_fill_rounds(mic_ctx *ctx, int *rounds) {
+  if (!ctx || !rounds) return MIC_ERR_ARG;
+  *rounds = ctx->density_rounds;
+  return MIC_OK;
+}
+
 extern "C" int mic_check_marker_density(mic_ctx *ctx, const mic_density_options *d, int64_t *n_added,
                                         int64_t *n_removed) {
   if (!ctx || !d || d->NMX < 1 || d->NMY < 1) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   if (n_added) *n_added = 0;
   if (n_removed) *n_removed = 0;
+  ctx->density_rounds = 0;
   int e = mic_ensure_sorted(ctx);  // cells of the current positions (findMarkerCells, main:247)
   if (e) return e;
   const int NX = ctx->P.NX, NY = ctx->P.NY;
@@ -501,7 +675,7 @@ extern "C" int mic_check_marker_density(mic_ctx *ctx, const mic_density_options 
   Totals *tot = carve<Totals>(p, 1);
   int *err = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(tot) + 128);
   int *heads = carve<int>(p, ctx->ncells);
-  MIC_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  MIC_CUDA_TRY(cudaMemsetAsync(err, 0, 2 * sizeof(int), ctx->stream));
   DCols c;
   for (int k = 0; k < C_F64_COUNT; ++k) c.f[k] = ctx->f64[k];
   for (int k = 0; k < C_I32_COUNT; ++k) c.i[k] = ctx->i32[k];
@@ -534,11 +708,11 @@ extern "C" int mic_check_marker_density(mic_ctx *ctx, const mic_density_options 
   }
   MIC_CUDA_TRY(cudaGetLastError());
   Totals h;
-  int herr = 0;
+  int herr[2] = {0, 0};
   MIC_CUDA_TRY(cudaMemcpyAsync(&h, tot, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
-  MIC_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaMemcpyAsync(herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  if (herr) return MIC_ERR_DENSITY;
+  if (herr[0]) return MIC_ERR_DENSITY;
   // ---- removal ----
   const unsigned long long s0 = ctx->rng48;
   if (h.nrem > 0) {
@@ -548,9 +722,9 @@ extern "C" int mic_check_marker_density(mic_ctx *ctx, const mic_density_options 
                                                              h.nout, isout, err);
     }
     MIC_CUDA_TRY(cudaGetLastError());
-    MIC_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MIC_CUDA_TRY(cudaMemcpyAsync(herr, err, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    if (herr) return MIC_ERR_DENSITY;
+    if (herr[0]) return MIC_ERR_DENSITY;
     if (n_removed) *n_removed = h.nrem;
   }
   const unsigned long long s1 = lcg48_skip(s0, (unsigned long long)h.ndraw);
@@ -563,14 +737,25 @@ extern "C" int mic_check_marker_density(mic_ctx *ctx, const mic_density_options 
     return MIC_OK;
   }
   // ---- additions ----
+  const int64_t nrec = nadd < nout ? nadd : nout;  // new markers that take recycled slots
+  const int64_t ncl = ctx->ncells;
   size_t need2 = 0;
   need2 += 3 * (((nadd * sizeof(double)) + 255) / 256) * 256;   // nx ny best_r
-  need2 += 6 * (((nadd * sizeof(int)) + 255) / 256) * 256;      // kind tid tslot best_id best_slot next
+  need2 += 14 * (((nadd * sizeof(int)) + 255) / 256) * 256;     // kind tid tslot best_id best_slot next tcell
+                                                                // ewrote ecx ecy src ptrA ptrB rslot
+  need2 += (((nrec > 0 ? nrec : 1) * sizeof(int) + 255) / 256) * 256;  // clist
+  need2 += 2 * ((((ncl + 1) * sizeof(int)) + 255) / 256) * 256;  // cstart cfill
+  need2 += 256;                                                 // round flag
   if ((e = ensure_buf(&ctx->dens_add, &ctx->dens_add_bytes, need2))) return e;
   p = (unsigned char *)ctx->dens_add;
   double *nx = carve<double>(p, nadd), *ny = carve<double>(p, nadd), *best_r = carve<double>(p, nadd);
   int *kind = carve<int>(p, nadd), *tid = carve<int>(p, nadd), *tslot = carve<int>(p, nadd);
   int *best_id = carve<int>(p, nadd), *best_slot = carve<int>(p, nadd), *next = carve<int>(p, nadd);
+  int *tcell = carve<int>(p, nadd), *ewrote = carve<int>(p, nadd), *ecx = carve<int>(p, nadd);
+  int *ecy = carve<int>(p, nadd), *src = carve<int>(p, nadd), *ptrA = carve<int>(p, nadd);
+  int *ptrB = carve<int>(p, nadd), *rslot = carve<int>(p, nadd);
+  int *clist = carve<int>(p, nrec > 0 ? nrec : 1), *cstart = carve<int>(p, ncl + 1), *cfill = carve<int>(p, ncl + 1);
+  int *flags = carve<int>(p, 64);
   // plate_depth(LX) (benchmarkInitialConditions.c:80-91)
   double plate = d->overridingPlateThickness;
   if (fabs(ctx->P.LX - d->rootCenter) < d->rootWidth)
@@ -595,12 +780,72 @@ extern "C" int mic_check_marker_density(mic_ctx *ctx, const mic_density_options 
                                                                      (int)nadd, wmax, hmax, ctx->P.LX * ctx->P.LY,
                                                                      best_r, best_id, best_slot);
   }
-  MIC_CUDA_TRY(cudaMemsetAsync(heads, 0xFF, sizeof(int) * ctx->ncells, ctx->stream));
-  {
+  const int nf = ctx->has_grain ? C_F64_COUNT : C_AOS_F64;
+  bool parallel = herr[1] == 0;
+  int rounds = 0;
+  if (parallel) {
+    MIC_CUDA_TRY(cudaMemsetAsync(cstart, 0, sizeof(int) * (ncl + 1), ctx->stream));
+    MIC_CUDA_TRY(cudaMemsetAsync(cfill, 0, sizeof(int) * (ncl + 1), ctx->stream));
+    if (nrec > 0) {
+      {
+        MIC_KERNEL(ctx, "k_density_bucket");
+        k_density_bucket<<<grid_for(nrec), kBlock, 0, ctx->stream>>>(ctx->P, nx, ny, (int)nrec, tcell, cstart);
+      }
+      if ((e = mic_scan_exclusive(ctx, cstart, ncl + 1, aux))) return e;
+      MIC_KERNEL(ctx, "k_density_scatter");
+      k_density_scatter<<<grid_for(nrec), kBlock, 0, ctx->stream>>>(tcell, cstart, (int)nrec, cfill, clist);
+    }
+    {
+      MIC_KERNEL(ctx, "k_density_guess");
+      k_density_guess<<<grid_for(nadd), kBlock, 0, ctx->stream>>>(ctx->P, nx, ny, (int)nadd, ewrote, ecx, ecy);
+    }
+    int jumps = 1;
+    while ((1LL << jumps) < nadd + 1) ++jumps;
+    constexpr int kMaxRounds = 64;
+    int changed = 1;
+    while (changed && rounds < kMaxRounds) {
+      ++rounds;
+      MIC_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int), ctx->stream));
+      {
+        MIC_KERNEL(ctx, "k_density_decide");
+        k_density_decide<<<grid_for(nadd), kBlock, 0, ctx->stream>>>(ctx->P, nx, ny, kind, tid, best_r, best_id,
+                                                                     cstart, clist, (int)nadd, wmax, hmax, ewrote,
+                                                                     ecx, ecy, src, ptrA);
+      }
+      int *pin = ptrA, *pout = ptrB;
+      for (int k = 0; k < jumps; ++k) {
+        MIC_KERNEL(ctx, "k_density_jump");
+        k_density_jump<<<grid_for(nadd), kBlock, 0, ctx->stream>>>(pin, pout, (int)nadd);
+        int *tmp = pin;
+        pin = pout;
+        pout = tmp;
+      }
+      {
+        MIC_KERNEL(ctx, "k_density_facts");
+        k_density_facts<<<grid_for(nadd), kBlock, 0, ctx->stream>>>(ctx->P, c, nx, ny, kind, tslot, best_slot, src,
+                                                                    pin, (int)nadd, ewrote, ecx, ecy, rslot, flags);
+      }
+      MIC_CUDA_TRY(cudaGetLastError());
+      MIC_CUDA_TRY(cudaMemcpyAsync(&changed, flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    }
+    parallel = changed == 0;
+  }
+  ctx->density_rounds = parallel ? rounds : (herr[1] ? -1 : -rounds);
+  if (parallel) {
+    {
+      MIC_KERNEL(ctx, "k_density_build");
+      k_density_build<<<grid_for(nadd), kBlock, 0, ctx->stream>>>(ctx->P, ctx->mat, ctx->opt, ctx->creep, c, nf, *d,
+                                                                  nx, ny, kind, tid, tslot, (int)nadd, n);
+    }
+    MIC_KERNEL(ctx, "k_density_copy");
+    k_density_copy<<<grid_for(nadd), kBlock, 0, ctx->stream>>>(c, nf, nx, ny, kind, tid, tslot, ewrote, rslot,
+                                                               (int)nadd, n);
+  } else {  // a slot recycled twice, or no fixed point within the round limit: in order
+    MIC_CUDA_TRY(cudaMemsetAsync(heads, 0xFF, sizeof(int) * ctx->ncells, ctx->stream));
     MIC_KERNEL(ctx, "k_density_fill");
-    k_density_fill<<<1, 32, 0, ctx->stream>>>(ctx->P, ctx->mat, ctx->opt, ctx->creep, c,
-                                              ctx->has_grain ? C_F64_COUNT : C_AOS_F64, *d, nx, ny, kind, tid, tslot,
-                                              best_r, best_id, best_slot, (int)nadd, n, wmax, hmax, heads, next);
+    k_density_fill<<<1, 32, 0, ctx->stream>>>(ctx->P, ctx->mat, ctx->opt, ctx->creep, c, nf, *d, nx, ny, kind, tid,
+                                              tslot, best_r, best_id, best_slot, (int)nadd, n, wmax, hmax, heads, next);
   }
   MIC_CUDA_TRY(cudaGetLastError());
   ctx->n = n + (nadd > nout ? nadd - nout : 0);

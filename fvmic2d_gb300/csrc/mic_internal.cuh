@@ -90,6 +90,7 @@ struct mic_ctx {
   int has_grain;  // per-marker grain sizes were set: the grain column moves with the sorts
   long long gen;  // bumped by every setter that changes what a step launches (captured graphs)
   unsigned long long rng48;  // drand48 stream of marker density control (48-bit state)
+  int density_rounds;        // rounds of the last parallel fill; negative: the in-order fill ran
   void *dens_buf, *dens_add;  // density-control scratch (grown on demand)
   double *solution;           // Stokes solution (3 NX NY, dof-interleaved) for retrieveSolutions
   void *io_buf;               // checkpoint packing scratch (grown on demand)

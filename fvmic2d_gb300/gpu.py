@@ -99,6 +99,7 @@ SIGNATURES = {
     "mic_retrieve_solutions": (_I, [_P, _DP, _D, _IP]),
     "mic_density_seed": (_I, [_P, ctypes.c_long]),
     "mic_density_rng_state": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+    "mic_density_fill_rounds": (_I, [_P, _IP]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -242,6 +243,12 @@ class MicProblem:
     def density_state(self):
         v = ctypes.c_uint64(0)
         self._check(self.L.mic_density_rng_state(self.h, ctypes.byref(v), None), "mic_density_rng_state")
+        return v.value
+
+    def density_fill_rounds(self):
+        """rounds the last checkMarkerDensity took to settle the copies (negative: in-order fill)"""
+        v = ctypes.c_int(0)
+        self._check(self.L.mic_density_fill_rounds(self.h, ctypes.byref(v)), "mic_density_fill_rounds")
         return v.value
 
     def fill(self, field, value):

@@ -118,3 +118,13 @@ class DensityOptions(ctypes.Structure):
                 ("maxMarkers", ctypes.c_int32), ("slabAngle", ctypes.c_double), ("slabAge", ctypes.c_double),
                 ("overridingPlateThickness", ctypes.c_double), ("rootThickness", ctypes.c_double),
                 ("rootCenter", ctypes.c_double), ("rootWidth", ctypes.c_double)]
+
+
+class SubductionOptions(ctypes.Structure):
+    """mic_subduction_options: the Options fields the Stokes and thermal assemblies read
+    (gravity, imposed slab velocity, slab / overriding-plate geometry, top thermal boundary)."""
+    _fields_ = [("gx", ctypes.c_double), ("gy", ctypes.c_double), ("slabVelocity", ctypes.c_double),
+                ("slabAngle", ctypes.c_double), ("slabAge", ctypes.c_double),
+                ("overridingPlateThickness", ctypes.c_double), ("rootThickness", ctypes.c_double),
+                ("rootCenter", ctypes.c_double), ("rootWidth", ctypes.c_double),
+                ("thermalBCTopType", ctypes.c_int32), ("thermalBCTopValue", ctypes.c_double)]

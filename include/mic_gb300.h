@@ -256,6 +256,11 @@ int mic_check_marker_density(mic_ctx *ctx, const mic_density_options *options, i
  * default), or read / replace the 48-bit state */
 int mic_density_seed(mic_ctx *ctx, long seed);
 int mic_density_rng_state(mic_ctx *ctx, uint64_t *get, const uint64_t *set);
+/* rounds the last mic_check_marker_density took to settle which marker each new marker copies:
+ * 0 nothing added; -1 a slot was recycled twice (the reference's over-asked removal), so the new
+ * markers were filled one at a time in order; below -1 no fixed point within that many rounds,
+ * filled in order too */
+int mic_density_fill_rounds(mic_ctx *ctx, int *rounds);
 
 /* ---- ensembles ----
  * No counterpart in the reference (one problem per run).  Independent problems, each a context

@@ -56,6 +56,19 @@ typedef struct {
   double overridingPlateThickness, rootThickness, rootCenter, rootWidth;
 } mic_density_options;
 
+/* Options fields read by the Stokes and thermal assemblies (vep_system.c:12-726,
+ * formThermalSystem.c:6-249, enforceThermalBC.c:5-38; fdcode.h:155-211) and the slab / plate
+ * geometry they share with the inflow markers (benchmarkInitialConditions.c:75-145). */
+typedef struct {
+  double gx, gy;                   /* gravity components */
+  double slabVelocity;             /* imposed slab speed, m/s */
+  double slabAngle;                /* radians */
+  double slabAge;                  /* Myr */
+  double overridingPlateThickness, rootThickness, rootCenter, rootWidth;
+  int32_t thermalBCTopType;        /* thermalBCTop.type[0]: 0 fixed temperature, 1 fixed gradient */
+  double thermalBCTopValue;        /* thermalBCTop.value[0] */
+} mic_subduction_options;
+
 /* Material table; same layout as fdcode.h:74-95. */
 typedef struct {
   int32_t nMaterials;

@@ -192,4 +192,35 @@ PetscErrorCode DMView(DM, PetscViewer);
 PetscErrorCode DMGetCoordinates(DM, Vec *);
 PetscErrorCode PetscOptionsGetBool(const char *, const char *, PetscBool *, PetscBool *);  /* PETSc 3.5 form */
 
+/* Mat (one rank, AIJ semantics): rows of (column, value) entries.  MatSetValue(s) with
+ * INSERT_VALUES replaces an existing entry and ADD_VALUES adds to it; rows or columns with a
+ * negative index are skipped, which is how PETSc drops the ghost points of a ghosted DMDA
+ * (their local-to-global index is -1).  Assembly does nothing.  VecSetValue(s) follow the same
+ * rules on global vectors. */
+typedef enum { MAT_FINAL_ASSEMBLY = 0, MAT_FLUSH_ASSEMBLY = 1 } MatAssemblyType;
+typedef enum { DIFFERENT_NONZERO_PATTERN, SUBSET_NONZERO_PATTERN, SAME_NONZERO_PATTERN } MatStructure;
+PetscErrorCode plite_MatCreate(PetscInt nrows, Mat *A);
+PetscErrorCode MatDestroy(Mat *A);
+PetscErrorCode MatZeroEntries(Mat A);
+PetscErrorCode MatSetValues(Mat A, PetscInt m, const PetscInt *rows, PetscInt n, const PetscInt *cols,
+                            const PetscScalar *v, InsertMode mode);
+PetscErrorCode MatSetValue(Mat A, PetscInt row, PetscInt col, PetscScalar v, InsertMode mode);
+PetscErrorCode MatAssemblyBegin(Mat A, MatAssemblyType t);
+PetscErrorCode MatAssemblyEnd(Mat A, MatAssemblyType t);
+PetscErrorCode MatCopy(Mat A, Mat B, MatStructure s);
+/* CSR copy, columns ascending within a row; the arrays are malloc'd; returns the entry count */
+PetscInt plite_MatGetCSR(Mat A, PetscInt **rowptr, PetscInt **cols, PetscScalar **vals);
+PetscErrorCode VecSetValues(Vec v, PetscInt n, const PetscInt *idx, const PetscScalar *y, InsertMode mode);
+PetscErrorCode VecSetValue(Vec v, PetscInt i, PetscScalar y, InsertMode mode);
+PetscErrorCode VecAssemblyBegin(Vec v);
+PetscErrorCode VecAssemblyEnd(Vec v);
+/* local-to-global map of the ghosted node layout ((NX+4) x (NY+4), offset 2): the node index
+ * j NX + i inside the domain, -1 on the ghost points */
+typedef struct _p_ISLocalToGlobalMapping *ISLocalToGlobalMapping;
+PetscErrorCode DMGetLocalToGlobalMapping(DM da, ISLocalToGlobalMapping *map);
+PetscErrorCode ISLocalToGlobalMappingGetIndices(ISLocalToGlobalMapping map, const PetscInt **idx);
+PetscErrorCode ISLocalToGlobalMappingRestoreIndices(ISLocalToGlobalMapping map, const PetscInt **idx);
+PetscErrorCode DMDAGetGhostCorners(DM da, PetscInt *x, PetscInt *y, PetscInt *z, PetscInt *m, PetscInt *n,
+                                   PetscInt *p);
+
 #endif

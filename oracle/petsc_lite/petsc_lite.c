@@ -6,9 +6,14 @@
 #include <string.h>
 #include <time.h>
 
+struct _p_ISLocalToGlobalMapping {
+  PetscInt *idx;
+};
+
 struct _p_DM {
   PetscInt NX, NY;
   PetscInt dof;          /* values per node: 1, or 3 for the Stokes solution DMDA (vx, vy, p) */
+  struct _p_ISLocalToGlobalMapping *ltog;  /* built on first request */
 };
 
 struct _p_Vec {
@@ -38,6 +43,10 @@ PetscErrorCode plite_DMDACreateDOF(PetscInt NX, PetscInt NY, PetscInt dof, DM *d
 }
 
 PetscErrorCode plite_DMDestroy(DM *da) {
+  if (*da && (*da)->ltog) {
+    free((*da)->ltog->idx);
+    free((*da)->ltog);
+  }
   free(*da);
   *da = NULL;
   return 0;
@@ -477,5 +486,181 @@ PetscErrorCode PetscBagRegisterScalar(PetscBag b, void *a, PetscScalar v, const 
 PetscErrorCode PetscBagView(PetscBag b, PetscViewer v) { (void)b; (void)v; return 0; }
 PetscErrorCode PetscBagDestroy(PetscBag *b) {
   if (*b) { free((*b)->data); free(*b); *b = NULL; }
+  return 0;
+}
+
+/* ---- Mat ------------------------------------------------------------------------------ */
+typedef struct {
+  PetscInt n, cap;
+  PetscInt *col;
+  PetscScalar *val;
+} MatRow;
+
+struct _p_Mat {
+  PetscInt nrows;
+  MatRow *rows;
+};
+
+PetscErrorCode plite_MatCreate(PetscInt nrows, Mat *A) {
+  Mat m = (Mat)calloc(1, sizeof(struct _p_Mat));
+  if (!m) return 1;
+  m->nrows = nrows;
+  m->rows = (MatRow *)calloc((size_t)(nrows > 0 ? nrows : 1), sizeof(MatRow));
+  if (!m->rows) { free(m); return 1; }
+  *A = m;
+  return 0;
+}
+
+PetscErrorCode MatDestroy(Mat *A) {
+  if (!A || !*A) return 0;
+  for (PetscInt r = 0; r < (*A)->nrows; ++r) {
+    free((*A)->rows[r].col);
+    free((*A)->rows[r].val);
+  }
+  free((*A)->rows);
+  free(*A);
+  *A = NULL;
+  return 0;
+}
+
+/* PETSc keeps the nonzero pattern and zeroes the values */
+PetscErrorCode MatZeroEntries(Mat A) {
+  for (PetscInt r = 0; r < A->nrows; ++r)
+    for (PetscInt k = 0; k < A->rows[r].n; ++k) A->rows[r].val[k] = 0.0;
+  return 0;
+}
+
+static PetscErrorCode mat_set(Mat A, PetscInt r, PetscInt c, PetscScalar v, InsertMode mode) {
+  if (r < 0 || c < 0) return 0;
+  if (r >= A->nrows || c >= A->nrows) return 63;  /* PETSC_ERR_ARG_OUTOFRANGE */
+  MatRow *row = &A->rows[r];
+  for (PetscInt k = 0; k < row->n; ++k)
+    if (row->col[k] == c) {
+      row->val[k] = mode == ADD_VALUES ? row->val[k] + v : v;
+      return 0;
+    }
+  if (row->n == row->cap) {
+    PetscInt nc = row->cap ? 2 * row->cap : 8;
+    PetscInt *ci = (PetscInt *)realloc(row->col, (size_t)nc * sizeof(PetscInt));
+    if (!ci) return 55;
+    row->col = ci;
+    PetscScalar *vv = (PetscScalar *)realloc(row->val, (size_t)nc * sizeof(PetscScalar));
+    if (!vv) return 55;
+    row->val = vv;
+    row->cap = nc;
+  }
+  row->col[row->n] = c;
+  row->val[row->n] = v;  /* a new entry: INSERT and ADD both give v */
+  row->n++;
+  return 0;
+}
+
+PetscErrorCode MatSetValues(Mat A, PetscInt m, const PetscInt *rows, PetscInt n, const PetscInt *cols,
+                            const PetscScalar *v, InsertMode mode) {
+  for (PetscInt i = 0; i < m; ++i)
+    for (PetscInt j = 0; j < n; ++j) {
+      PetscErrorCode e = mat_set(A, rows[i], cols[j], v[i * n + j], mode);
+      if (e) return e;
+    }
+  return 0;
+}
+
+PetscErrorCode MatSetValue(Mat A, PetscInt row, PetscInt col, PetscScalar v, InsertMode mode) {
+  return mat_set(A, row, col, v, mode);
+}
+
+PetscErrorCode MatAssemblyBegin(Mat A, MatAssemblyType t) { (void)A; (void)t; return 0; }
+PetscErrorCode MatAssemblyEnd(Mat A, MatAssemblyType t) { (void)A; (void)t; return 0; }
+
+PetscErrorCode MatCopy(Mat A, Mat B, MatStructure s) {
+  (void)s;
+  if (A->nrows != B->nrows) return 60;
+  for (PetscInt r = 0; r < A->nrows; ++r)
+    for (PetscInt k = 0; k < A->rows[r].n; ++k) {
+      PetscErrorCode e = mat_set(B, r, A->rows[r].col[k], A->rows[r].val[k], INSERT_VALUES);
+      if (e) return e;
+    }
+  return 0;
+}
+
+PetscInt plite_MatGetCSR(Mat A, PetscInt **rowptr, PetscInt **cols, PetscScalar **vals) {
+  PetscInt nnz = 0;
+  for (PetscInt r = 0; r < A->nrows; ++r) nnz += A->rows[r].n;
+  *rowptr = (PetscInt *)malloc((size_t)(A->nrows + 1) * sizeof(PetscInt));
+  *cols = (PetscInt *)malloc((size_t)(nnz ? nnz : 1) * sizeof(PetscInt));
+  *vals = (PetscScalar *)malloc((size_t)(nnz ? nnz : 1) * sizeof(PetscScalar));
+  PetscInt at = 0;
+  for (PetscInt r = 0; r < A->nrows; ++r) {
+    (*rowptr)[r] = at;
+    const MatRow *row = &A->rows[r];
+    for (PetscInt k = 0; k < row->n; ++k) {  /* insertion sort by column */
+      PetscInt c = row->col[k];
+      PetscScalar v = row->val[k];
+      PetscInt q = at;
+      while (q > (*rowptr)[r] && (*cols)[q - 1] > c) {
+        (*cols)[q] = (*cols)[q - 1];
+        (*vals)[q] = (*vals)[q - 1];
+        --q;
+      }
+      (*cols)[q] = c;
+      (*vals)[q] = v;
+      ++at;
+    }
+  }
+  (*rowptr)[A->nrows] = at;
+  return nnz;
+}
+
+PetscErrorCode VecSetValues(Vec v, PetscInt n, const PetscInt *idx, const PetscScalar *y, InsertMode mode) {
+  for (PetscInt k = 0; k < n; ++k) {
+    PetscInt i = idx[k];
+    if (i < 0) continue;
+    if (i >= v->n) return 63;
+    v->data[i] = mode == ADD_VALUES ? v->data[i] + y[k] : y[k];
+  }
+  return 0;
+}
+
+PetscErrorCode VecSetValue(Vec v, PetscInt i, PetscScalar y, InsertMode mode) { return VecSetValues(v, 1, &i, &y, mode); }
+PetscErrorCode VecAssemblyBegin(Vec v) { (void)v; return 0; }
+PetscErrorCode VecAssemblyEnd(Vec v) { (void)v; return 0; }
+
+PetscErrorCode DMGetLocalToGlobalMapping(DM da, ISLocalToGlobalMapping *map) {
+  if (!da->ltog) {
+    const PetscInt mg = da->NX + 4, ng = da->NY + 4;
+    ISLocalToGlobalMapping m = (ISLocalToGlobalMapping)calloc(1, sizeof(*m));
+    if (!m) return 55;
+    m->idx = (PetscInt *)malloc((size_t)mg * ng * sizeof(PetscInt));
+    if (!m->idx) { free(m); return 55; }
+    for (PetscInt jl = 0; jl < ng; ++jl)
+      for (PetscInt il = 0; il < mg; ++il) {
+        const PetscInt i = il - 2, j = jl - 2;
+        m->idx[il + mg * jl] = (i >= 0 && i < da->NX && j >= 0 && j < da->NY) ? j * da->NX + i : -1;
+      }
+    da->ltog = m;
+  }
+  *map = da->ltog;
+  return 0;
+}
+
+PetscErrorCode ISLocalToGlobalMappingGetIndices(ISLocalToGlobalMapping map, const PetscInt **idx) {
+  *idx = map->idx;
+  return 0;
+}
+
+PetscErrorCode ISLocalToGlobalMappingRestoreIndices(ISLocalToGlobalMapping map, const PetscInt **idx) {
+  (void)map;
+  *idx = NULL;
+  return 0;
+}
+
+PetscErrorCode DMDAGetGhostCorners(DM da, PetscInt *x, PetscInt *y, PetscInt *z, PetscInt *m, PetscInt *n,
+                                   PetscInt *p) {
+  if (x) *x = -2;
+  if (y) *y = -2;
+  if (z) *z = 0;
+  if (m) *m = da->NX + 4;
+  if (n) *n = da->NY + 4;
+  if (p) *p = 1;
   return 0;
 }

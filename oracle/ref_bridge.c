@@ -28,6 +28,8 @@
 #include "retrieveSolutions.h"
 #include "io.h"
 #include "restart.h"
+#include "vep_system.h"
+#include "thermalSystem.h"
 #include "mic_types.h"
 
 PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da);
@@ -399,4 +401,96 @@ int ref_projectMarkersNodesFromScalar(refp *p, double *values, int out_id) {
   Vec *f = field_vec(p, out_id);
   if (!f) return -1;
   return projectMarkersNodesFromScalar(&p->ms, &p->grid, values, *f);
+}
+
+/* ---- the two linear systems (vep_system.c:12, formThermalSystem.c:6, enforceThermalBC.c:5) ---- */
+
+PetscErrorCode plite_DMDACreateDOF(PetscInt NX, PetscInt NY, PetscInt dof, DM *da);
+
+static void set_subduction(refp *p, const mic_subduction_options *so) {
+  p->opt.gx = so->gx;
+  p->opt.gy = so->gy;
+  p->opt.slabVelocity = so->slabVelocity;
+  p->opt.slabAngle = so->slabAngle;
+  p->opt.slabAge = so->slabAge;
+  p->opt.overridingPlateThickness = so->overridingPlateThickness;
+  p->opt.rootThickness = so->rootThickness;
+  p->opt.rootCenter = so->rootCenter;
+  p->opt.rootWidth = so->rootWidth;
+  p->opt.thermalBCTop.type[0] = so->thermalBCTopType;
+  p->opt.thermalBCTop.value[0] = so->thermalBCTopValue;
+}
+
+typedef struct {
+  PetscInt n, nnz;
+  PetscInt *rowptr, *cols;
+  PetscScalar *vals, *rhs;
+} ref_system;
+
+static ref_system g_sys[2];  /* 0: Stokes, 1: thermal (the last assembly of each) */
+
+static void keep_system(int which, Mat A, Vec rhs) {
+  ref_system *s = &g_sys[which];
+  free(s->rowptr);
+  free(s->cols);
+  free(s->vals);
+  free(s->rhs);
+  s->nnz = plite_MatGetCSR(A, &s->rowptr, &s->cols, &s->vals);
+  VecGetSize(rhs, &s->n);
+  s->rhs = (PetscScalar *)malloc(sizeof(PetscScalar) * (size_t)s->n);
+  PetscScalar *a;
+  VecGetArray(rhs, &a);
+  memcpy(s->rhs, a, sizeof(PetscScalar) * (size_t)s->n);
+}
+
+/* formVEPSystem on the nodal fields with gy = so->gy and P = NULL (no preconditioner matrix) */
+int ref_formVEPSystem(refp *p, const mic_subduction_options *so, double dt, double *Kbond, double *Kcont) {
+  set_subduction(p, so);
+  Mat A;
+  Vec rhs;
+  plite_MatCreate(3 * p->grid.NX * p->grid.NY, &A);
+  DMCreateGlobalVector(p->grid.vda, &rhs);
+  int e = formVEPSystem(&p->nf, &p->grid, A, NULL, rhs, Kbond, Kcont, so->gy, dt, &p->opt, &p->bv);
+  if (!e) keep_system(0, A, rhs);
+  MatDestroy(&A);
+  VecDestroy(&rhs);
+  return e;
+}
+
+/* enforceThermalBCs1 on lastT (main_subduction.c:383) */
+int ref_enforceThermalBCs1(refp *p, const mic_subduction_options *so) {
+  set_subduction(p, so);
+  return enforceThermalBCs1(&p->grid, &p->opt, &p->nf);
+}
+
+/* formThermalSystem with the right-hand side starting as a copy of the heating field
+ * (main_subduction.c:381, VecCopy(nodal_heating, rhs)) */
+int ref_formThermalSystem(refp *p, const mic_subduction_options *so, double dt, int doSteady) {
+  set_subduction(p, so);
+  Problem pr;
+  memset(&pr, 0, sizeof(pr));
+  pr.materials = p->mat;
+  Mat A;
+  Vec rhs;
+  plite_MatCreate(p->grid.NX * p->grid.NY, &A);
+  DMCreateGlobalVector(p->grid.da, &rhs);
+  VecCopy(p->heat, rhs);
+  int e = formThermalSystem(&pr, &p->grid, &p->nf, A, rhs, dt, &p->opt, doSteady);
+  if (!e) keep_system(1, A, rhs);
+  MatDestroy(&A);
+  VecDestroy(&rhs);
+  return e;
+}
+
+long ref_system_nnz(int which, long *nrows) {
+  if (nrows) *nrows = g_sys[which].n;
+  return g_sys[which].nnz;
+}
+
+void ref_system_get(int which, int *rowptr, int *cols, double *vals, double *rhs) {
+  const ref_system *s = &g_sys[which];
+  memcpy(rowptr, s->rowptr, sizeof(int) * (size_t)(s->n + 1));
+  memcpy(cols, s->cols, sizeof(int) * (size_t)s->nnz);
+  memcpy(vals, s->vals, sizeof(double) * (size_t)s->nnz);
+  memcpy(rhs, s->rhs, sizeof(double) * (size_t)s->n);
 }

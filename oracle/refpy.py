@@ -68,6 +68,11 @@ def lib():
             "ref_restartFromMarkers": (_I, [_P, _I, _I, _D, _P, _I, _DP]),
             "ref_limitDisplacementTimestep": (_D, [_P, _D, _D]),
             "ref_retrieveSolutions": (_I, [_P, _DP, _D]),
+            "ref_formVEPSystem": (_I, [_P, _P, _D, _DP, _DP]),
+            "ref_enforceThermalBCs1": (_I, [_P, _P]),
+            "ref_formThermalSystem": (_I, [_P, _P, _D, _I]),
+            "ref_system_nnz": (ctypes.c_long, [_I, ctypes.POINTER(ctypes.c_long)]),
+            "ref_system_get": (None, [_I, _P, _P, _DP, _DP]),
             "ref_stage_seconds": (_D, [_I]),
             "ref_stage_reset": (None, []),
         }
@@ -135,6 +140,40 @@ class RefProblem:
     def retrieveSolutions(self, S, Kcont):
         S = np.ascontiguousarray(S, dtype=np.float64)
         return lib().ref_retrieveSolutions(self.h, _dp(S), Kcont)
+
+    def _system(self, which):
+        L = lib()
+        nrows = ctypes.c_long(0)
+        nnz = L.ref_system_nnz(which, ctypes.byref(nrows))
+        rowptr = np.zeros(nrows.value + 1, dtype=np.int32)
+        cols = np.zeros(max(nnz, 1), dtype=np.int32)
+        vals = np.zeros(max(nnz, 1), dtype=np.float64)
+        rhs = np.zeros(nrows.value, dtype=np.float64)
+        L.ref_system_get(which, rowptr.ctypes.data, cols.ctypes.data, _dp(vals), _dp(rhs))
+        return rowptr, cols[:nnz], vals[:nnz], rhs
+
+    def formVEPSystem(self, sopt, dt):
+        """formVEPSystem (vep_system.c:12) on the nodal fields: (rowptr, cols, vals, rhs, Kbond,
+        Kcont), the matrix as CSR with ascending columns, rows in the reference's ordering
+        3 (j NX + i) + dof"""
+        kb, kc = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        e = lib().ref_formVEPSystem(self.h, ctypes.byref(sopt), dt, ctypes.byref(kb), ctypes.byref(kc))
+        if e:
+            raise RuntimeError("formVEPSystem failed: %d" % e)
+        return self._system(0) + (kb.value, kc.value)
+
+    def enforceThermalBCs1(self, sopt):
+        e = lib().ref_enforceThermalBCs1(self.h, ctypes.byref(sopt))
+        if e:
+            raise RuntimeError("enforceThermalBCs1 failed: %d" % e)
+
+    def formThermalSystem(self, sopt, dt, doSteady=0):
+        """formThermalSystem (formThermalSystem.c:6) with the right-hand side starting as the
+        heating field: (rowptr, cols, vals, rhs)"""
+        e = lib().ref_formThermalSystem(self.h, ctypes.byref(sopt), dt, doSteady)
+        if e:
+            raise RuntimeError("formThermalSystem failed: %d" % e)
+        return self._system(1)
 
     def checkMarkerDensity(self, dopt, cap, seed=1):
         """The reference's checkMarkerDensity (PETSCRAND48 object seeded with srand48(seed)) on a

@@ -69,6 +69,9 @@ def test_density_over_several_calls_matches_oracle():
         added, removed = G.checkMarkerDensity(dopt)
         mo, ao, ro, state = O.checkMarkerDensity(dopt, cap, state=state, seed=5)
         assert (added, removed) == (ao, ro)
+        # markers pushed onto x = LX by the drift sit in the last quarter cell's count but
+        # outside its removal bounds: the reference's over-asked removal, filled in order (-1)
+        assert added == 0 or G.density_fill_rounds() != 0
         got = G.markers
         # inflow markers take T from erf and eta from exp (last-place differences from the host
         # libm) and later new markers may copy them: T, eta, mu within 1e-12, the rest exact
@@ -80,6 +83,38 @@ def test_density_over_several_calls_matches_oracle():
         G.upload_markers(moved)
         O.markers = moved.copy()
         O.findMarkerCells()
+
+
+@pytest.mark.parametrize("band", ["top", "block"])
+def test_density_emptied_region_matches_oracle(band):
+    """A region emptied of markers (they left through the boundary): every quarter cell in it
+    takes new markers into recycled slots, each copying the previous new one, in long chains of
+    copies that start at the region's edge; the parallel fill settles them and matches the
+    in-order result of the oracle."""
+    wl, dopt = W.density_case(nx_cells=64, ny_cells=16, seed=3)
+    g = wl.grid
+    m = wl.markers
+    if band == "top":
+        gone = m["Y"] < g.y[3]
+    else:
+        gone = (m["X"] > g.x[10]) & (m["X"] < g.x[40]) & (m["Y"] > g.y[4]) & (m["Y"] < g.y[12])
+    m["X"][gone] = -1.0
+    m["Y"][gone] = -1.0
+    wl = W.Workload(wl.name, g, m, wl.materials, wl.options, wl.bcs, {}, 1, 1, 1)
+    cap = len(m) + 4096
+    G = gpu.MicProblem(wl, capacity=cap)
+    O = oraclepy.OracleProblem(wl)
+    O.findMarkerCells()
+    G.density_seed(11)
+    added, removed = G.checkMarkerDensity(dopt)
+    rounds = G.density_fill_rounds()
+    mo, ao, ro, state = O.checkMarkerDensity(dopt, cap, seed=11)
+    assert (added, removed) == (ao, ro)
+    assert added >= int(gone.sum()) // 2
+    assert rounds > 0  # the parallel fill settled (no in-order fallback)
+    ok, msg = _split_compare(G.markers, mo, np.ones(len(mo), dtype=bool))
+    assert ok, msg
+    assert G.density_state() == state
 
 
 def test_density_nothing_to_do_and_capacity():
