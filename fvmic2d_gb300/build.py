@@ -16,7 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["mic_context.cu", "mic_bin_sort.cu", "mic_project.cu", "mic_marker_passes.cu", "mic_creep.cu",
-           "mic_creep_tc.cu", "mic_ensemble.cu", "mic_density.cu", "mic_grid.cu", "mic_io.cu"]
+           "mic_creep_tc.cu", "mic_ensemble.cu", "mic_density.cu", "mic_grid.cu", "mic_io.cu", "mic_systems.cu",
+           "mic_band_lu.cu", "mic_timestep.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 VARIANTS = {"libmic_gb300.so": ["-fmad=true"], "libmic_gb300_exact.so": ["-fmad=false", "-DMIC_EXACT=1"]}
 
@@ -47,7 +48,7 @@ def _stale(target, inputs):
 
 def _compile(args):
     src, obj, flags = args
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v",
            *flags, "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -149,6 +149,14 @@ static void free_ctx(mic_ctx *ctx) {
   cudaFree(ctx->dens_add);
   cudaFree(ctx->solution);
   cudaFree(ctx->io_buf);
+  for (int w = 0; w < 2; ++w) {
+    cudaFree(ctx->sys[w].cnt);
+    cudaFree(ctx->sys[w].col);
+    cudaFree(ctx->sys[w].val);
+    cudaFree(ctx->sys[w].rhs);
+  }
+  cudaFree(ctx->sys_scratch);
+  cudaFree(ctx->lu_buf);
   cudaFree(ctx->stage_aos);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -247,13 +247,15 @@ extern "C" int mic_limit_displacement_timestep(mic_ctx *ctx, double factor, doub
 }
 
 extern "C" int mic_retrieve_solutions(mic_ctx *ctx, const double *S, double Kcont, int *foundnan) {
-  if (!ctx || !S) return MIC_ERR_ARG;
+  if (!ctx || (!S && !ctx->solution)) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
   if (!ctx->solution) {
     if (cudaMalloc((void **)&ctx->solution, sizeof(double) * 3 * nn) != cudaSuccess) return MIC_ERR_NOMEM;
   }
-  MIC_CUDA_TRY(cudaMemcpyAsync(ctx->solution, S, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, ctx->stream));
+  // S = NULL: the solution mic_linear_solve left on the device
+  if (S)
+    MIC_CUDA_TRY(cudaMemcpyAsync(ctx->solution, S, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, ctx->stream));
   double *pm = ctx->red_buf + 28;
   {
     MIC_KERNEL(ctx, "k_retrieve");

@@ -69,6 +69,19 @@ struct Params {  // everything a kernel needs besides the marker columns; passed
 
 }  // namespace mic
 
+// one assembled linear system: rows of at most `width` (column, value) entries, the right-hand
+// side, and the banded factorisation state
+struct mic_system_store {
+  int64_t n;
+  int width;
+  int *cnt, *col;
+  double *val, *rhs;
+  double Kbond, Kcont;
+  int factored;
+  int kl, ku;       // band widths of the last factorisation
+  int zero_pivot;   // first zero pivot of the last factorisation (-1: none)
+};
+
 struct mic_ctx {
   int device;
   cudaStream_t stream;
@@ -94,6 +107,11 @@ struct mic_ctx {
   void *dens_buf, *dens_add;  // density-control scratch (grown on demand)
   double *solution;           // Stokes solution (3 NX NY, dof-interleaved) for retrieveSolutions
   void *io_buf;               // checkpoint packing scratch (grown on demand)
+  mic_system_store sys[2];    // assembled systems: 0 Stokes (vep_system.c), 1 thermal
+  void *sys_scratch;          // assembly scratch: geometry tables, scaled viscosities
+  size_t sys_scratch_bytes;
+  void *lu_buf;               // banded factorisation storage (grown on demand)
+  size_t lu_bytes;
   size_t io_bytes;
   size_t dens_bytes, dens_add_bytes;
   double *f64[mic::C_F64_COUNT];

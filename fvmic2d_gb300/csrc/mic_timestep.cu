@@ -1,0 +1,146 @@
+// mic_timestep.cu -- one time step of fvmic2d's subduction model (main_subduction.c:227-460)
+// on the device, without PETSc: marker density control, the plasticity iterations around the
+// Stokes solve, the sub-grid stress and stress updates, the thermal solve (repeated with a
+// shorter step when the temperature changes too much) and the marker advection.  Every stage is
+// the library's own entry point for the reference routine of the same name; the linear systems
+// are assembled and solved on the device (mic_systems.cu, mic_band_lu.cu).  Nodal fields and
+// markers stay on the device; only scalars (time steps, flags, maxima) come back to the host,
+// where main_subduction's control flow runs.
+#include <cmath>
+
+#include "mic_internal.cuh"
+
+using namespace mic;
+
+namespace {
+
+// VecNorm(thisT - lastT, NORM_INFINITY) (main:387-390), NaN entries skipped
+__global__ void k_temp_change(const double *__restrict__ thisT, const double *__restrict__ lastT, int64_t nn,
+                              double *part) {
+  __shared__ double sm[256];
+  double m = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nn; k += (int64_t)gridDim.x * blockDim.x) {
+    const double d = fabs(thisT[k] - lastT[k]);
+    if (d > m) m = d;
+  }
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s && sm[threadIdx.x + s] > sm[threadIdx.x]) sm[threadIdx.x] = sm[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+int max_temp_change(mic_ctx *ctx, double *out) {
+  const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
+  constexpr int kParts = 64;
+  double *part = ctx->red_buf;  // reduction scratch of the context (at least 64 entries)
+  {
+    MIC_KERNEL(ctx, "k_temp_change");
+    k_temp_change<<<kParts, 256, 0, ctx->stream>>>(ctx->nodal[MIC_NF_THIST], ctx->nodal[MIC_NF_LASTT], nn, part);
+  }
+  double h[kParts];
+  MIC_CUDA_TRY(cudaMemcpyAsync(h, part, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  double m = 0.0;
+  for (double v : h)
+    if (v > m) m = v;
+  *out = m;
+  return MIC_OK;
+}
+
+// main:381-384 / 396-399: heating into the right-hand side, boundary values of lastT, assembly,
+// solve (the solution is thisT)
+int thermal_solve(mic_ctx *ctx, const mic_timestep_options &o, double dt) {
+  int e = mic_enforce_thermal_bcs(ctx, &o.sub);
+  if (!e) e = mic_form_thermal_system(ctx, &o.sub, dt, 0);
+  if (!e) e = mic_linear_solve(ctx, 1);
+  return e;
+}
+
+}  // namespace
+
+#define MIC_TRY(x)           \
+  do {                       \
+    const int _e = (x);      \
+    if (_e) return _e;       \
+  } while (0)
+
+extern "C" int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options *o, double elapsed_time,
+                                       mic_timestep_report *rep) {
+  if (!ctx || !o || !rep) return MIC_ERR_ARG;
+  if (ctx->red_cap < 64) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  *rep = mic_timestep_report{};
+  int64_t n = 0;
+  // main:241-250: cells, density control, cells
+  MIC_TRY(mic_find_marker_cells(ctx, &n));
+  if (o->densityControl) {
+    MIC_TRY(mic_check_marker_density(ctx, &o->density, &rep->markers_added, &rep->markers_removed));
+    MIC_TRY(mic_find_marker_cells(ctx, &n));
+  }
+  // main:255-268: marker density anomaly, projection
+  MIC_TRY(mic_update_marker_rho(ctx));
+  MIC_TRY(mic_project_markers_nodes_all2(ctx));
+  // main:271-289: melting check
+  MIC_TRY(mic_max_marker_T(ctx, &rep->max_T));
+  if (rep->max_T > 9999.0) {  // TBREAK
+    rep->stopped = 1;
+    return MIC_OK;
+  }
+  // main:292-362: plasticity iterations
+  double displacementdt = o->dtMax;
+  int isYielding = 1, converged = 0, iPlastic = 0;
+  const double gy = o->sub.gy;
+  while ((o->firstStep && iPlastic < 1) || ((isYielding || !converged) && iPlastic < o->maxNumPlasticity)) {
+    isYielding = 0;
+    converged = 0;
+    MIC_TRY(mic_check_plastic_yielding(ctx, displacementdt, &isYielding, elapsed_time));
+    MIC_TRY(mic_limit_viscosity(ctx));
+    MIC_TRY(mic_project_markers_nodes_all2(ctx));
+    MIC_TRY(mic_form_vep_system(ctx, &o->sub, displacementdt, &rep->Kbond, &rep->Kcont));
+    MIC_TRY(mic_linear_solve(ctx, 0));
+    int fn = 0;
+    MIC_TRY(mic_retrieve_solutions(ctx, nullptr, rep->Kcont, &fn));
+    if (fn) return MIC_ERR_NAN;
+    MIC_TRY(mic_nodal_stress_strain(ctx, displacementdt, gy));
+    MIC_TRY(mic_update_marker_strain_pressure(ctx, displacementdt));
+    MIC_TRY(mic_update_global_strain_rate_residual(ctx, iPlastic, &rep->residual));
+    MIC_TRY(mic_check_convergence(ctx, 1e-16, 1e-1, iPlastic, &converged));
+    const double lastdt = displacementdt;
+    MIC_TRY(mic_limit_displacement_timestep(ctx, o->displacementStepLimit, &displacementdt));
+    if (displacementdt != lastdt) converged = 0;
+    ++iPlastic;
+  }
+  rep->plastic_iterations = iPlastic;
+  rep->is_yielding = isYielding;
+  rep->converged = converged;
+  rep->displacement_dt = displacementdt;
+  double dt = displacementdt;
+  // main:369-376: sub-grid stress diffusion, stress update, heating
+  if (ctx->opt.subgridStressDiffusivity > 0.0)
+    MIC_TRY(mic_subgrid_stress_changes(ctx, displacementdt, ctx->opt.subgridStressDiffusivity));
+  MIC_TRY(mic_update_marker_stress(ctx));
+  if (!o->shearHeating)
+    MIC_CUDA_TRY(cudaMemsetAsync(ctx->nodal[MIC_NF_HEATING], 0, sizeof(double) * ctx->P.NX * ctx->P.NY,
+                                 ctx->stream));
+  // main:379-403: thermal solve, repeated with a shorter step for a too large change
+  MIC_TRY(thermal_solve(ctx, *o, dt));
+  double dTmax = 0.0;
+  MIC_TRY(max_temp_change(ctx, &dTmax));
+  if (dTmax > o->maxTempChange) {
+    dt = dt * o->maxTempChange / dTmax;
+    MIC_TRY(thermal_solve(ctx, *o, dt));
+    rep->thermal_resolves = 1;
+    MIC_TRY(max_temp_change(ctx, &dTmax));
+  }
+  rep->max_temp_change = dTmax;
+  rep->dt = dt;
+  // main:409, 435: sub-grid temperature changes with the new temperature, advection
+  MIC_TRY(mic_subgrid_temperature_changes(ctx, dt));
+  MIC_TRY(mic_advect_markers_rk(ctx, dt));
+  MIC_TRY(mic_max_abs_sxx(ctx, &rep->max_abs_sxx));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}

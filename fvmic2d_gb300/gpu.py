@@ -100,6 +100,15 @@ SIGNATURES = {
     "mic_density_seed": (_I, [_P, ctypes.c_long]),
     "mic_density_rng_state": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "mic_density_fill_rounds": (_I, [_P, _IP]),
+    "mic_form_vep_system": (_I, [_P, _P, _D, _DP, _DP]),
+    "mic_enforce_thermal_bcs": (_I, [_P, _P]),
+    "mic_form_thermal_system": (_I, [_P, _P, _D, _I]),
+    "mic_system_size": (_I, [_P, _I, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "mic_system_get": (_I, [_P, _I, _P, _P, _DP, _DP]),
+    "mic_linear_solve": (_I, [_P, _I]),
+    "mic_solution_get": (_I, [_P, _I, _DP]),
+    "mic_system_band": (_I, [_P, _I, _IP, _IP]),
+    "mic_subduction_timestep": (_I, [_P, _P, _D, _P]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -219,10 +228,69 @@ class MicProblem:
         return d.value
 
     def retrieveSolutions(self, S, Kcont):
-        S = np.ascontiguousarray(S, dtype=np.float64)
+        """S: the solver's vector (host), or None for the solution mic_linear_solve left on the
+        device"""
         nan = ctypes.c_int(0)
+        if S is None:
+            self._check(self.L.mic_retrieve_solutions(self.h, None, Kcont, ctypes.byref(nan)),
+                        "mic_retrieve_solutions")
+            return nan.value
+        S = np.ascontiguousarray(S, dtype=np.float64)
         self._check(self.L.mic_retrieve_solutions(self.h, _dp(S), Kcont, ctypes.byref(nan)), "mic_retrieve_solutions")
         return nan.value
+
+    STOKES, THERMAL = 0, 1
+
+    def formVEPSystem(self, sopt, dt):
+        """formVEPSystem (vep_system.c:12) on the device; returns (Kbond, Kcont)"""
+        kb, kc = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        self._check(self.L.mic_form_vep_system(self.h, ctypes.byref(sopt), dt, ctypes.byref(kb), ctypes.byref(kc)),
+                    "mic_form_vep_system")
+        return kb.value, kc.value
+
+    def enforceThermalBCs1(self, sopt):
+        self._check(self.L.mic_enforce_thermal_bcs(self.h, ctypes.byref(sopt)), "mic_enforce_thermal_bcs")
+
+    def formThermalSystem(self, sopt, dt, doSteady=0):
+        self._check(self.L.mic_form_thermal_system(self.h, ctypes.byref(sopt), dt, doSteady),
+                    "mic_form_thermal_system")
+
+    def system(self, which):
+        """the assembled system as (rowptr, cols, vals, rhs), columns ascending"""
+        nr, nnz = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self.L.mic_system_size(self.h, which, ctypes.byref(nr), ctypes.byref(nnz)), "mic_system_size")
+        rp = np.zeros(nr.value + 1, dtype=np.int32)
+        c = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        v = np.zeros(max(nnz.value, 1))
+        rhs = np.zeros(nr.value)
+        self._check(self.L.mic_system_get(self.h, which, rp.ctypes.data, c.ctypes.data, _dp(v), _dp(rhs)),
+                    "mic_system_get")
+        return rp, c[:nnz.value], v[:nnz.value], rhs
+
+    def linear_solve(self, which):
+        """direct solve of an assembled system on the device (kspLinearSolve, preonly + LU)"""
+        self._check(self.L.mic_linear_solve(self.h, which), "mic_linear_solve")
+
+    def solution(self, which):
+        nn = self.NX * self.NY
+        out = np.zeros(3 * nn if which == self.STOKES else nn)
+        self._check(self.L.mic_solution_get(self.h, which, _dp(out)), "mic_solution_get")
+        return out
+
+    def subductionTimestep(self, topt, elapsed_time=0.0):
+        """one time step of main_subduction.c on the device; returns the report as a dict"""
+        from .mic_types import TimestepReport
+
+        rep = TimestepReport()
+        self._check(self.L.mic_subduction_timestep(self.h, ctypes.byref(topt), elapsed_time, ctypes.byref(rep)),
+                    "mic_subduction_timestep")
+        self.n = self._count()
+        return rep.as_dict()
+
+    def system_band(self, which):
+        kl, ku = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(self.L.mic_system_band(self.h, which, ctypes.byref(kl), ctypes.byref(ku)), "mic_system_band")
+        return kl.value, ku.value
 
     def checkMarkerDensity(self, dopt):
         """markers.c:455-781 on the device; returns (n_added, n_removed)."""

@@ -128,3 +128,23 @@ class SubductionOptions(ctypes.Structure):
                 ("overridingPlateThickness", ctypes.c_double), ("rootThickness", ctypes.c_double),
                 ("rootCenter", ctypes.c_double), ("rootWidth", ctypes.c_double),
                 ("thermalBCTopType", ctypes.c_int32), ("thermalBCTopValue", ctypes.c_double)]
+
+
+class TimestepOptions(ctypes.Structure):
+    """mic_timestep_options: one time step of main_subduction.c on the device"""
+    _fields_ = [("dtMax", ctypes.c_double), ("displacementStepLimit", ctypes.c_double),
+                ("maxTempChange", ctypes.c_double), ("maxNumPlasticity", ctypes.c_int32),
+                ("shearHeating", ctypes.c_int32), ("firstStep", ctypes.c_int32), ("densityControl", ctypes.c_int32),
+                ("density", DensityOptions), ("sub", SubductionOptions)]
+
+
+class TimestepReport(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("displacement_dt", ctypes.c_double), ("Kbond", ctypes.c_double),
+                ("Kcont", ctypes.c_double), ("max_T", ctypes.c_double), ("residual", ctypes.c_double),
+                ("max_temp_change", ctypes.c_double), ("max_abs_sxx", ctypes.c_double),
+                ("plastic_iterations", ctypes.c_int32), ("is_yielding", ctypes.c_int32),
+                ("converged", ctypes.c_int32), ("thermal_resolves", ctypes.c_int32), ("stopped", ctypes.c_int32),
+                ("markers_added", ctypes.c_int64), ("markers_removed", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}

@@ -42,7 +42,8 @@ enum {
   MIC_ERR_DENSITY = 10,   /* density control: a quarter cell would get a non-positive number of
                            * markers (markers.c:590-593 aborts), an overfull quarter cell with no
                            * marker inside its bounds, or more than 2048 markers in one */
-  MIC_ERR_IO = 11         /* checkpoint file could not be opened, read or written */
+  MIC_ERR_IO = 11,        /* checkpoint file could not be opened, read or written */
+  MIC_ERR_SOLVE = 12      /* direct solve: zero pivot (singular matrix) or a band too wide */
 };
 
 typedef struct {
@@ -226,7 +227,8 @@ int mic_limit_displacement_timestep(mic_ctx *ctx, double factor, double *dt);
 /* retrieveSolutions (retrieveSolutions.c:4): vx, vy, p from the solver's vector S
  * ([(j NX + i) 3 + {0 vx, 1 vy, 2 p}], host memory), p scaled by Kcont, minus the dx-weighted
  * mean of row 1 on every j, i >= 1.  The reference also scales the pressure entries of S in
- * place; here S is only read.  *foundnan = 0 (the reference checks only in its TEXTURE build). */
+ * place; here S is only read.  S = NULL takes the solution mic_linear_solve left on the device.
+ * *foundnan = 0 (the reference checks only in its TEXTURE build). */
 int mic_retrieve_solutions(mic_ctx *ctx, const double *S, double Kcont, int *foundnan);
 
 /* ---- marker checkpoints (io.c:299-402, restart.c:8-125) ----
@@ -261,6 +263,46 @@ int mic_density_rng_state(mic_ctx *ctx, uint64_t *get, const uint64_t *set);
  * markers were filled one at a time in order; below -1 no fixed point within that many rounds,
  * filled in order too */
 int mic_density_fill_rounds(mic_ctx *ctx, int *rounds);
+
+/* ---- the linear systems of a time step ----
+ * Assembly on the device from the context's nodal arrays, rows in the reference's ordering
+ * (3 (j NX + i) + dof, dof 0 vx, 1 vy, 2 p, for Stokes; j NX + i for temperature), every entry
+ * bit-identical to the reference's: the Stokes system (formVEPSystem, vep_system.c:12-726;
+ * the caller's P matrix is not built: the reference's solve uses the system matrix itself),
+ * the thermal boundary values of lastT (enforceThermalBCs1, enforceThermalBC.c:5-38) and the
+ * thermal system, whose right-hand side starts as the heating field (MIC_NF_HEATING), as
+ * main_subduction.c:381 copies nodal_heating into it (formThermalSystem,
+ * formThermalSystem.c:6-249).  The slab / plate geometry is benchmarkInitialConditions.c's. */
+int mic_form_vep_system(mic_ctx *ctx, const mic_subduction_options *options, double dt, double *Kbond,
+                        double *Kcont);
+int mic_enforce_thermal_bcs(mic_ctx *ctx, const mic_subduction_options *options);
+int mic_form_thermal_system(mic_ctx *ctx, const mic_subduction_options *options, double dt, int doSteady);
+/* which: 0 Stokes, 1 thermal.  Size, and a copy as CSR with ascending columns. */
+int mic_system_size(mic_ctx *ctx, int which, int64_t *nrows, int64_t *nnz);
+int mic_system_get(mic_ctx *ctx, int which, int32_t *rowptr, int32_t *cols, double *vals, double *rhs);
+/* kspLinearSolve (kspLinearSolve.c:13) as the reference's option files run it (preonly + LU,
+ * option_files/run_mumps.petscopt): a direct solve on the device, banded LU with partial
+ * pivoting.  The Stokes solution stays on the device for mic_retrieve_solutions(ctx, NULL, ...);
+ * the temperature goes to MIC_NF_THIST.  MIC_ERR_SOLVE for a zero pivot. */
+int mic_linear_solve(mic_ctx *ctx, int which);
+int mic_solution_get(mic_ctx *ctx, int which, double *out);
+/* band widths (lower, upper) the last solve of a system factorised */
+int mic_system_band(mic_ctx *ctx, int which, int *kl, int *ku);
+
+/* One time step of main_subduction.c (227-460) without PETSc, everything on the device:
+ * findMarkerCells, checkMarkerDensity (when options->densityControl), the marker density
+ * anomaly, projection and melting check, then plasticity iterations (checkPlasticYielding,
+ * limitViscosity, projection, the Stokes system and its direct solve, retrieveSolutions,
+ * nodalStressStrain, updateMarkerStrainPressure, the strain-rate residual and convergence test,
+ * limitDisplacementTimestep), subgridStressChanges (when the options' diffusivity is positive),
+ * updateMarkerStress, the thermal system and its solve (again with a shorter step when the
+ * largest nodal change exceeds maxTempChange), subgridTemperatureChanges and advectMarkersRK.
+ * elapsed_time is the model time before the step (checkPlasticYielding's t); the caller adds
+ * report->dt.  A step whose markers are above the reference's TBREAK (9999 K) stops after the
+ * projection with report->stopped = 1, as main goes to the next Monte-Carlo run.  The
+ * Options.staticVelocity and adiabaticHeating paths are not provided. */
+int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options *options, double elapsed_time,
+                            mic_timestep_report *report);
 
 /* ---- ensembles ----
  * No counterpart in the reference (one problem per run).  Independent problems, each a context

@@ -69,6 +69,34 @@ typedef struct {
   double thermalBCTopValue;        /* thermalBCTop.value[0] */
 } mic_subduction_options;
 
+/* One time step of main_subduction.c (227-460) on the device: the Options fields it reads
+ * besides the marker path's (fdcode.h:155-211) and the two sets above. */
+typedef struct {
+  double dtMax;                  /* first time step tried (main:242) */
+  double displacementStepLimit;  /* limitDisplacementTimestep's factor */
+  double maxTempChange;          /* largest nodal temperature change before the step shrinks (main:392) */
+  int32_t maxNumPlasticity;      /* plasticity iterations at most */
+  int32_t shearHeating;          /* 0: the nodal heating is zeroed before the thermal solve (main:372) */
+  int32_t firstStep;             /* iTime == 0: one plasticity iteration even when converged (main:294) */
+  int32_t densityControl;        /* run checkMarkerDensity (main:250) with `density` */
+  mic_density_options density;
+  mic_subduction_options sub;
+} mic_timestep_options;
+
+/* What the step did. */
+typedef struct {
+  double dt;                /* time step taken (the thermal one, main:371 and 393) */
+  double displacement_dt;   /* the last plasticity iteration's displacement time step */
+  double Kbond, Kcont;      /* scalings of the last Stokes system */
+  double max_T;             /* largest marker temperature before the step (main:271-289) */
+  double residual;          /* last global strain-rate residual (residual.c) */
+  double max_temp_change;   /* largest nodal change of the accepted thermal solve */
+  double max_abs_sxx;       /* main:437-448 */
+  int32_t plastic_iterations, is_yielding, converged, thermal_resolves;
+  int32_t stopped;          /* 1: max_T above 9999 (TBREAK), nothing after the projection ran */
+  int64_t markers_added, markers_removed;
+} mic_timestep_report;
+
 /* Material table; same layout as fdcode.h:74-95. */
 typedef struct {
   int32_t nMaterials;

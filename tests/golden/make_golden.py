@@ -231,6 +231,28 @@ def grid_table():
     return out
 
 
+def systems_table():
+    """formVEPSystem, enforceThermalBCs1 and formThermalSystem of the reference on the systems
+    cases of tests/test_oracle_pin.py: inputs, the matrices as CSR, right-hand sides, Kbond and
+    Kcont, and lastT after the boundary values."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from tests.test_oracle_pin import SYSTEM_IN, SYSTEM_KINDS, reference_systems, systems_case
+
+    out = {}
+    for kind in SYSTEM_KINDS:
+        wl, so, dt = systems_case(kind)
+        for name in SYSTEM_IN:
+            out["%s_in_%s" % (kind, name)] = np.asarray(wl.nodal[name], dtype=np.float64)
+        (rp, c, v, rhs, kb, kc), lastT, (trp, tc, tv, trhs) = reference_systems(wl, so, dt)
+        for name, a in (("rowptr", rp), ("cols", c), ("vals", v), ("rhs", rhs)):
+            out["%s_stokes_%s" % (kind, name)] = a
+        out[kind + "_K"] = np.array([kb, kc])
+        out[kind + "_lastT"] = lastT
+        for name, a in (("rowptr", trp), ("cols", tc), ("vals", tv), ("rhs", trhs)):
+            out["%s_thermal_%s" % (kind, name)] = a
+    return out
+
+
 def checkpoint_case():
     """the VEP box after a step, with some markers pushed out of the domain"""
     wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2)
@@ -277,6 +299,9 @@ def main():
     if sys.argv[1:] in ([], ["checkpoint"]):
         np.savez_compressed(os.path.join(OUT, "marker_checkpoint.npz"), **checkpoint_table())
         print("wrote marker_checkpoint")
+    if sys.argv[1:] in ([], ["systems"]):
+        np.savez_compressed(os.path.join(OUT, "linear_systems.npz"), **systems_table())
+        print("wrote linear_systems")
     if sys.argv[1:] in ([], ["grid"]):
         np.savez_compressed(os.path.join(OUT, "grid_routines.npz"), **grid_table())
         print("wrote grid_routines")

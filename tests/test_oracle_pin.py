@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from fvmic2d_gb300 import workloads as W
-from fvmic2d_gb300.mic_types import MARKER_DTYPE, PROJECTED_FIELDS, Materials, Options, BCs
+from fvmic2d_gb300.mic_types import MARKER_DTYPE, PROJECTED_FIELDS, Materials, Options, BCs, SubductionOptions
 from oracle import oraclepy, refpy
 from tests.helpers import compare_markers, exact, same_fields
 
@@ -361,6 +361,107 @@ def test_grid_routines_match_golden(kind):
     for name in ("vx", "vy", "p"):
         ok, msg = exact(O.get_nodal(name), z["%s_ret_%s" % (kind, name)])
         assert ok, (name, msg)
+
+
+SYSTEM_KINDS = {"fixed_top": 5, "gradient_top": 9}
+
+
+def systems_case(kind, seed=None):
+    """The Stokes and thermal assemblies' inputs: the refined box with random nodal fields
+    (viscosities over four decades, finite shear moduli so that the visco-elastic factor
+    matters, densities, conductivities, heat capacities, temperatures, a horizontal velocity
+    that is negative on part of the right wall) and subduction options (the overriding plate's
+    root kept away from the right wall, whose geometry the reference reads from its ghost
+    coordinates otherwise).  Returns (workload, options, dt)."""
+    seed = SYSTEM_KINDS[kind] if seed is None else seed
+    wl = W.vep_slab_box(nx_cells=24, ny_cells=10, nm=2, seed=seed)
+    g = wl.grid
+    NX, NY = g.NX, g.NY
+    u = W.splitmix64_uniform(seed + 77, 16 * NX * NY).reshape(16, NY, NX)
+    f = {"etaN": 10 ** (19 + 4 * u[0]), "etaS": 10 ** (19 + 4 * u[1]), "muN": 1e10 * (0.5 + u[2]),
+         "muS": 1e10 * (0.5 + u[3]), "rho": 3300 * (u[4] - 0.5) * 1e-2, "rhodot": (u[5] - 0.5) * 1e-15,
+         "kThermal": 2.0 + 2.0 * u[6], "Cp": 1000.0 + 250.0 * u[7], "lastT": 273.0 + 1300.0 * u[8],
+         "vx": (u[9] - 0.4) * 1e-9, "heating": u[10] * 1e-6}
+    f["muN"][u[11] < 0.1] = 1e99  # the projection's placeholder where no marker reached
+    wl.nodal.update(f)
+    top = 0 if kind == "fixed_top" else 1
+    # slab angle and plate thickness leave no pressure cells cut off between the slab and the
+    # plate (such a pocket makes the reference's matrix singular: its pressures only appear in one
+    # gradient between them)
+    so = SubductionOptions(gx=0.0 if top == 0 else 0.3, gy=10.0, slabVelocity=0.05 / 3.15576e7,
+                           slabAngle=0.8 if top == 0 else 0.3, slabAge=50.0,
+                           overridingPlateThickness=(0.3 if top == 0 else 0.2) * g.LY, rootThickness=0.05 * g.LY,
+                           rootCenter=0.5 * g.LX, rootWidth=0.2 * g.LX, thermalBCTopType=top,
+                           thermalBCTopValue=273.0)
+    dt = 3.0e11 if top == 0 else 7.0e10
+    return wl, so, dt
+
+
+SYSTEM_IN = ["etaN", "etaS", "muN", "muS", "rho", "rhodot", "kThermal", "Cp", "lastT", "vx", "heating"]
+
+
+def systems_case_from_golden(z, kind):
+    """the systems case with the nodal inputs stored in the golden file"""
+    wl, so, dt = systems_case(kind)
+    for name in SYSTEM_IN:
+        wl.nodal[name] = z["%s_in_%s" % (kind, name)]
+    return wl, so, dt
+
+
+def reference_systems(wl, so, dt):
+    """formVEPSystem, enforceThermalBCs1 and formThermalSystem of the reference build"""
+    R = refpy.RefProblem(wl)
+    sto = R.formVEPSystem(so, dt)
+    R.enforceThermalBCs1(so)
+    lastT = R.get_nodal("lastT")
+    th = R.formThermalSystem(so, dt)
+    return sto, lastT, th
+
+
+@needs_ref
+@pytest.mark.parametrize("kind", list(SYSTEM_KINDS))
+def test_systems_reference_build_matches_golden(kind):
+    """the golden systems are what the reference build assembles from the stored inputs"""
+    z = np.load(os.path.join(GOLDEN, "linear_systems.npz"))
+    wl, so, dt = systems_case_from_golden(z, kind)
+    (rp, c, v, rhs, kb, kc), lastT, (trp, tc, tv, trhs) = reference_systems(wl, so, dt)
+    for name, a in (("rowptr", rp), ("cols", c), ("vals", v), ("rhs", rhs)):
+        assert np.array_equal(a, z["%s_stokes_%s" % (kind, name)]), name
+    assert (kb, kc) == tuple(z[kind + "_K"])
+    assert np.array_equal(lastT, z[kind + "_lastT"])
+    for name, a in (("rowptr", trp), ("cols", tc), ("vals", tv), ("rhs", trhs)):
+        assert np.array_equal(a, z["%s_thermal_%s" % (kind, name)]), name
+
+
+def test_systems_golden_are_consistent():
+    """the stored systems: square CSR with ascending columns, a diagonal or a coupling in every
+    row, no NaN; the Stokes matrix is nonsingular (one pressure fixed) and the thermal one an
+    M-matrix row by row"""
+    z = np.load(os.path.join(GOLDEN, "linear_systems.npz"))
+    for kind in SYSTEM_KINDS:
+        wl, so, dt = systems_case_from_golden(z, kind)
+        nn = wl.grid.NX * wl.grid.NY
+        for sysname, n in (("stokes", 3 * nn), ("thermal", nn)):
+            rp = z["%s_%s_rowptr" % (kind, sysname)]
+            c = z["%s_%s_cols" % (kind, sysname)]
+            v = z["%s_%s_vals" % (kind, sysname)]
+            assert len(rp) == n + 1 and rp[-1] == len(c) == len(v)
+            assert np.all(np.diff(rp) > 0)
+            for r in range(n):
+                assert np.all(np.diff(c[rp[r]:rp[r + 1]]) > 0)
+            assert not np.isnan(v).any()
+        rp, c, v = (z["%s_stokes_%s" % (kind, k)] for k in ("rowptr", "cols", "vals"))
+        dense = np.zeros((3 * nn, 3 * nn))
+        dense[np.repeat(np.arange(3 * nn), np.diff(rp)), c] = v
+        sv = np.linalg.svd(dense, compute_uv=False)
+        assert sv[-1] > 1e-14 * sv[0]  # nonsingular: the solves have one answer
+        tv, trp, tc = z[kind + "_thermal_vals"], z[kind + "_thermal_rowptr"], z[kind + "_thermal_cols"]
+        for r in range(nn):
+            seg = slice(trp[r], trp[r + 1])
+            d = tv[seg][tc[seg] == r]
+            off = tv[seg][tc[seg] != r]
+            if len(off) and kind == "fixed_top":
+                assert d[0] > 0 and np.all(off <= 0) and d[0] >= -off.sum()
 
 
 def test_checkpoint_matches_golden(tmp_path):
