@@ -253,6 +253,24 @@ def systems_table():
     return out
 
 
+def timestep_table():
+    """one time step of main_subduction.c through the reference's routines (host LU solves):
+    markers before and after, the step's scalars and the final nodal velocity, pressure and
+    temperature"""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from tests.timestep_case import reference_timestep, timestep_case
+
+    wl, topt = timestep_case()
+    before = np.array(wl.markers, copy=True)
+    mk, rep, nodal = reference_timestep(wl, topt, elapsed=0.0)
+    out = {"before": before.view(np.uint8), "after": mk.view(np.uint8)}
+    for k, v in rep.items():
+        out["rep_" + k] = np.array(v)
+    for k, v in nodal.items():
+        out["nodal_" + k] = v
+    return out
+
+
 def checkpoint_case():
     """the VEP box after a step, with some markers pushed out of the domain"""
     wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2)
@@ -299,6 +317,9 @@ def main():
     if sys.argv[1:] in ([], ["checkpoint"]):
         np.savez_compressed(os.path.join(OUT, "marker_checkpoint.npz"), **checkpoint_table())
         print("wrote marker_checkpoint")
+    if sys.argv[1:] in ([], ["timestep"]):
+        np.savez_compressed(os.path.join(OUT, "subduction_step.npz"), **timestep_table())
+        print("wrote subduction_step")
     if sys.argv[1:] in ([], ["systems"]):
         np.savez_compressed(os.path.join(OUT, "linear_systems.npz"), **systems_table())
         print("wrote linear_systems")

@@ -1,0 +1,95 @@
+"""One time step of main_subduction.c (227-460) as a case: the workload, the step options, and
+the reference's own routines called in main's order with host sparse LU solves standing in for
+MUMPS (test infrastructure: generates and checks tests/golden/subduction_step.npz)."""
+import contextlib
+import os
+
+import numpy as np
+
+from fvmic2d_gb300 import workloads as W
+from fvmic2d_gb300.mic_types import DensityOptions, TimestepOptions
+from tests.test_oracle_pin import systems_case
+
+
+def timestep_case(seed=4):
+    """the refined VEP box with 4 x 4 markers per cell, subduction boundary geometry (slab at
+    0.8 rad below a plate 0.3 LY thick) and the step settings"""
+    wl = W.vep_slab_box(nx_cells=24, ny_cells=10, nm=4, seed=seed)
+    _, so, _ = systems_case("fixed_top")
+    g = wl.grid
+    so.overridingPlateThickness = 0.3 * g.LY
+    so.rootCenter = 0.5 * g.LX
+    so.rootWidth = 0.2 * g.LX
+    so.rootThickness = 0.05 * g.LY
+    topt = TimestepOptions(dtMax=3.0e11, displacementStepLimit=0.5, maxTempChange=50.0, maxNumPlasticity=4,
+                           shearHeating=1, firstStep=1, densityControl=0,
+                           density=DensityOptions(NMX=4, NMY=4, minMarkers=1, maxMarkers=100), sub=so)
+    return wl, topt
+
+
+def _spsolve(rp, c, v, rhs):
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+
+    n = len(rp) - 1
+    return spl.spsolve(sp.csr_matrix((v, c, rp), shape=(n, n)).tocsc(), rhs)
+
+
+def reference_timestep(wl, topt, elapsed=0.0):
+    """main_subduction.c:241-438 with the reference build's routines; returns (markers after the
+    step, report dict, nodal fields dict)"""
+    from oracle import refpy
+
+    so = topt.sub
+    with open(os.devnull, "w") as devnull, contextlib.redirect_stdout(devnull):
+        R = refpy.RefProblem(wl)
+        R.findMarkerCells()
+        R.updateMarkerRho()
+        R.projectMarkersNodesAll2()
+        rep = {"max_T": R.maxMarkerT()}
+        ddt = topt.dtMax
+        is_y, conv, it = 1, 0, 0
+        kb = kc = res = 0.0
+        while (topt.firstStep and it < 1) or ((is_y or not conv) and it < topt.maxNumPlasticity):
+            is_y = R.checkPlasticYielding(ddt, elapsed)
+            R.limitViscosity()
+            R.projectMarkersNodesAll2()
+            rp, c, v, rhs, kb, kc = R.formVEPSystem(so, ddt)
+            R.retrieveSolutions(_spsolve(rp, c, v, rhs), kc)
+            R.nodalStressStrain(ddt, so.gy)
+            R.updateMarkerStrainPressure(ddt)
+            res = R.updateGlobalStrainRateResidual(it)
+            conv = refpy.lib().ref_checkConvergence(1e-16, 1e-1, it)
+            last = ddt
+            ddt = R.limitDisplacementTimestep(ddt, topt.displacementStepLimit)
+            if ddt != last:
+                conv = 0
+            it += 1
+        rep.update(plastic_iterations=it, is_yielding=is_y, converged=conv, displacement_dt=ddt, Kbond=kb,
+                   Kcont=kc, residual=res)
+        dt = ddt
+        if wl.options.subgridStressDiffusivity > 0.0:
+            R.subgridStressChanges(ddt, wl.options.subgridStressDiffusivity)
+        R.updateMarkerStress()
+        if not topt.shearHeating:
+            R.set_nodal("heating", np.zeros((R.NY, R.NX)))
+
+        def thermal(dt):
+            R.enforceThermalBCs1(so)
+            rp, c, v, rhs = R.formThermalSystem(so, dt)
+            T = _spsolve(rp, c, v, rhs)
+            R.set_nodal("thisT", T.reshape(R.NY, R.NX))
+            return np.max(np.abs(T - R.get_nodal("lastT").ravel()))
+
+        dTmax = thermal(dt)
+        rep["thermal_resolves"] = 0
+        if dTmax > topt.maxTempChange:
+            dt = dt * topt.maxTempChange / dTmax
+            dTmax = thermal(dt)
+            rep["thermal_resolves"] = 1
+        rep.update(dt=dt, max_temp_change=dTmax)
+        R.subgridTemperatureChanges(dt)
+        R.advectMarkersRK(dt)
+        rep["max_abs_sxx"] = R.maxAbsSxx()
+        nodal = {f: R.get_nodal(f) for f in ("vx", "vy", "p", "thisT", "lastT", "etaS", "etaN", "heating")}
+    return R.markers.copy(), rep, nodal
