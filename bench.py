@@ -88,6 +88,7 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the convection-ensemble leg")
     ap.add_argument("--creep-mode", type=int, default=0, choices=[0, 1, 2],
                     help="law-7 solve of the main leg: 0 exact, 1 FP32 surrogate, 2 tensor-core surrogate")
+    ap.add_argument("--no-systems", action="store_true", help="skip the linear-systems / whole-time-step leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-cores", type=int, default=0, help="host processes for the CPU legs (0 = all)")
     return ap.parse_args()
@@ -443,6 +444,7 @@ def run_ours(args):
         "surrogate": surrogate_leg(args, local) if not args.no_surrogate else None,
         "ensemble": ensemble_leg(args, local) if not args.no_ensemble else None,
         "ice_ensemble": ice_ensemble_leg(args, local) if not args.no_ensemble else None,
+        "systems": systems_leg(args, local) if not args.no_systems else None,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
@@ -628,6 +630,82 @@ def ice_ensemble_leg(args, local):
     E.close()
     for P in members:
         P.close()
+    return out
+
+
+def systems_leg(args, local):
+    """The solves between the marker passes, on the device: the Stokes (formVEPSystem) and thermal
+    (formThermalSystem) assembly and the direct solve (banded LU; the reference runs MUMPS LU) of
+    the subduction box at 129 x 33 and 513 x 129 nodes, beside a host sparse LU (SuperLU) of the
+    same matrices; then whole time steps (mic_subduction_timestep) of the 129 x 33 box with 16
+    markers per cell."""
+    import numpy as np
+    import torch
+
+    from fvmic2d_gb300 import gpu
+    from fvmic2d_gb300 import workloads as W
+
+    out = {"workload": "subduction_box: refined VEP box, slab at 0.8 rad below a 0.3 LY plate, 5 cm/yr inflow"}
+    try:
+        import scipy.sparse as sps
+        import scipy.sparse.linalg as spl
+    except ImportError:
+        sps = None
+    for ncx, ncy in ((128, 32), (512, 128)):
+        wl, topt = W.subduction_box(nx_cells=ncx, ny_cells=ncy, nm=2)
+        G = gpu.MicProblem(wl, device=local)
+        G.findMarkerCells()
+        G.updateMarkerRho()
+        G.projectMarkersNodesAll2()
+        st = torch.cuda.ExternalStream(G.stream(), device=local)
+        rec = {"nodes": [wl.grid.NX, wl.grid.NY]}
+        for which, name in ((G.STOKES, "stokes"), (G.THERMAL, "thermal")):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            if which == G.STOKES:
+                G.formVEPSystem(topt.sub, topt.dtMax)
+                G.linear_solve(which)  # warm-up
+                G.synchronize()
+                ev[0].record(st)
+                G.formVEPSystem(topt.sub, topt.dtMax)
+            else:
+                G.enforceThermalBCs1(topt.sub)
+                G.formThermalSystem(topt.sub, topt.dtMax)
+                G.linear_solve(which)
+                G.synchronize()
+                ev[0].record(st)
+                G.formThermalSystem(topt.sub, topt.dtMax)
+            ev[1].record(st)
+            G.linear_solve(which)
+            ev[2].record(st)
+            ev[2].synchronize()
+            kl, ku = G.system_band(which)
+            rp, c, v, rhs = G.system(which)
+            r = {"unknowns": int(len(rhs)), "band": [kl, ku], "assembly_ms": ev[0].elapsed_time(ev[1]),
+                 "solve_ms": ev[1].elapsed_time(ev[2])}
+            if sps is not None:
+                A = sps.csr_matrix((v, c, rp), shape=(len(rhs), len(rhs))).tocsc()
+                t0 = time.perf_counter()
+                xr = spl.spsolve(A, rhs)
+                r["host_superlu_ms"] = (time.perf_counter() - t0) * 1e3
+                x = G.solution(which)
+                r["rel_diff_vs_superlu"] = float(np.max(np.abs(x - xr)) / np.max(np.abs(xr)))
+            rec[name] = r
+        G.close()
+        out["%dx%d" % (wl.grid.NX, wl.grid.NY)] = rec
+    wl, topt = W.subduction_box(nx_cells=128, ny_cells=32, nm=4)
+    G = gpu.MicProblem(wl, device=local)
+    G.subductionTimestep(topt, 0.0)  # warm-up step
+    topt.firstStep = 0
+    steps = 3
+    t0 = time.perf_counter()
+    reps = [G.subductionTimestep(topt, 0.0) for _ in range(steps)]
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    out["timestep"] = {"nodes": [wl.grid.NX, wl.grid.NY], "markers": int(G.n), "steps": steps,
+                       "ms_per_step": ms, "plastic_iterations": [r["plastic_iterations"] for r in reps],
+                       "dt": [r["dt"] for r in reps],
+                       "note": "host wall time of mic_subduction_timestep: density control off, every "
+                               "plasticity iteration assembles and solves the Stokes system on the device"}
+    G.close()
     return out
 
 

@@ -9,13 +9,15 @@
 // side.  The matrix goes into row-band storage, row i holding columns i-kl .. i+kl+ku (the extra
 // kl for the fill that row interchanges bring), W = 2 kl + ku + 1 values per row.
 //
-// Factorisation, right-looking in panels of NB columns:
-//   panel  one CTA: the panel's (NB + kl) x NB block in shared memory, column by column: pivot
-//          row (largest |value|, first on ties), interchange (whole rows, the right-hand side
+// Factorisation, right-looking in panels of NB columns (32, 16 or 8: the widest whose window of
+// NB + kl rows fits one CTA at one row per thread):
+//   panel  one CTA, each window row in one thread's registers, column by column: pivot row
+//          (largest |value|, first on ties), interchange (whole panel rows, the right-hand side
 //          too), multipliers, rank-1 update of the panel; the forward substitution of the
-//          right-hand side rides along (it is one more column);
-//   trsm   U12 = L11^-1 A12 for the columns right of the panel, one thread per column;
-//   update A22 -= L21 U12 over the band window, 64 x 64 tiles.
+//          right-hand side rides along (it is one more column); the trailing columns of the rows
+//          whose position changed follow once per panel, as a gather;
+//   trsm   U12 = L11^-1 A12 for the columns right of the panel, a warp per column;
+//   update A22 -= L21 U12 over the band window, 32 x 32 tiles.
 // Interchanges inside a panel move whole panel rows, multipliers included, so that the panel's
 // L is in final row order for the deferred trsm and update; interchanges can carry multipliers
 // outside the band, so the panel's L goes to a dense (NB + kl) x NB buffer rather than back into
@@ -73,42 +75,58 @@ __global__ void k_band_gather(const double *__restrict__ x, int64_t n, int dof, 
   if (r < n) out[r] = x[bmap(r, dof, NX, NY, transpose)];
 }
 
-constexpr int kPanelThreads = 1024;
-
-template <int NB>
-__global__ void __launch_bounds__(kPanelThreads) k_band_panel(double *band, int64_t n, int kl, int ku, int W,
-                                                             int64_t k0, int *piv, double *b, int *info,
-                                                             double *Lbuf) {
-  extern __shared__ double sp[];  // [R][NB]
-  __shared__ double red_v[32];
-  __shared__ int red_i[32];
-  __shared__ int s_p;
-  __shared__ double s_bj;
+// One panel: columns k0 .. k1-1 and the window rows k0 .. k0+R-1 (R <= 1024).  Thread r holds
+// window row r in registers (its NB panel columns and its right-hand side entry), fully unrolled
+// over the panel's columns, so a column step is: the pivot search over the column (integer images
+// of |a|: ordered for non-negative doubles, NaN skipped, off the FP64 pipe), the pivot row and
+// the row it displaces published in shared memory, one reciprocal, and every row below forming
+// its multiplier and updating itself against the broadcast pivot row.  Interchanges move whole
+// panel rows (multipliers included, so that L ends in final row order for the deferred trsm and
+// update) and the right-hand side; the trailing columns of the rows whose position changed
+// follow once at the end, as a gather.
+template <int NB, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_band_panel(double *band, int64_t n, int kl, int ku, int W, int64_t k0,
+                                                    int *piv, double *b, int *info, double *Lbuf, double *Tbuf) {
+  __shared__ double sA[NB + 1];  // the pivot row (new row jj) and its right-hand side
+  __shared__ double sB[NB + 1];  // row jj, which moves to the pivot's position
+  __shared__ long long red_v[MAXT / 32];
+  __shared__ int red_i[MAXT / 32];
+  __shared__ int who[MAXT];      // the window row now at each position
+  __shared__ int s_piv[NB];
+  __shared__ double s_rcp;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int64_t k1 = min(k0 + NB, n);
   const int nbc = (int)(k1 - k0);
   const int R = (int)(min(n, k1 + kl) - k0);
-  for (int idx = tid; idx < R * NB; idx += blockDim.x) {
-    const int r = idx / NB, c = idx % NB;
-    const int off = c - r + kl;
-    sp[idx] = (c < nbc && off >= 0 && off < W) ? band[(k0 + r) * (int64_t)W + off] : 0.0;
+  const bool own = tid < R;
+  double row[NB];
+  double brow = 0.0;
+#pragma unroll
+  for (int c = 0; c < NB; ++c) {
+    const int off = c - tid + kl;
+    row[c] = (own && c < nbc && off >= 0 && off < W) ? band[(k0 + tid) * (int64_t)W + off] : 0.0;
+  }
+  if (own) {
+    brow = b[k0 + tid];
+    who[tid] = tid;
   }
   __syncthreads();
-  for (int jj = 0; jj < nbc; ++jj) {
-    const int64_t j = k0 + jj;
-    const int rmax = (int)(min(n - 1, j + kl) - k0);
+#pragma unroll
+  for (int jj = 0; jj < NB; ++jj) {
+    if (jj >= nbc) break;
+    const int rmax = (int)(min(n - 1, k0 + jj + kl) - k0);
     // pivot: largest |a|, the first of equal ones (LAPACK's idamax)
-    double bv = -1.0;
+    long long bv = -1;
     int bi = INT_MAX;
-    for (int r = jj + tid; r <= rmax; r += blockDim.x) {
-      const double a = fabs(sp[r * NB + jj]);
-      if (a > bv) {
+    if (own && tid >= jj && tid <= rmax) {
+      const long long a = __double_as_longlong(row[jj]) & 0x7fffffffffffffffLL;
+      if (a <= 0x7ff0000000000000LL) {
         bv = a;
-        bi = r;
+        bi = tid;
       }
     }
     for (int o = 16; o > 0; o >>= 1) {
-      const double v2 = __shfl_down_sync(0xffffffffu, bv, o);
+      const long long v2 = __shfl_down_sync(0xffffffffu, bv, o);
       const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
       if (v2 > bv || (v2 == bv && i2 < bi)) {
         bv = v2;
@@ -120,81 +138,94 @@ __global__ void __launch_bounds__(kPanelThreads) k_band_panel(double *band, int6
       red_i[warp] = bi;
     }
     __syncthreads();
-    if (warp == 0) {
-      bv = lane < nwarps ? red_v[lane] : -1.0;
-      bi = lane < nwarps ? red_i[lane] : INT_MAX;
-      for (int o = 16; o > 0; o >>= 1) {
-        const double v2 = __shfl_down_sync(0xffffffffu, bv, o);
-        const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
-        if (v2 > bv || (v2 == bv && i2 < bi)) {
-          bv = v2;
-          bi = i2;
-        }
+    bv = red_v[0];
+    bi = red_i[0];
+    for (int w = 1; w < nwarps; ++w)
+      if (red_v[w] > bv || (red_v[w] == bv && red_i[w] < bi)) {
+        bv = red_v[w];
+        bi = red_i[w];
       }
-      if (lane == 0) s_p = (bi >= jj && bi <= rmax) ? bi : jj;  // all NaN: keep the diagonal
+    const int p = (bi >= jj && bi <= rmax) ? bi : jj;  // all NaN: keep the diagonal
+    if (tid == p) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c) sA[c] = row[c];
+      sA[NB] = brow;
+      s_rcp = row[jj] != 0.0 ? 1.0 / row[jj] : 0.0;  // the column's one division
+    }
+    if (tid == jj && p != jj) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c) sB[c] = row[c];
+      sB[NB] = brow;
+    }
+    if (tid == 0) {
+      s_piv[jj] = p;
+      const int w2 = who[jj];
+      who[jj] = who[p];
+      who[p] = w2;
     }
     __syncthreads();
-    const int p = s_p;
-    if (p != jj) {
-      // whole panel rows: the multipliers of earlier columns move with their rows, so that the
-      // panel's L is in final row order for the deferred update
-      for (int c = tid; c < NB; c += blockDim.x) {
-        const double t = sp[jj * NB + c];
-        sp[jj * NB + c] = sp[p * NB + c];
-        sp[p * NB + c] = t;
-      }
-      const int64_t q = k0 + p;
-      const int64_t cend = min(n - 1, j + kl + ku);
-      for (int64_t c = k1 + tid; c <= cend; c += blockDim.x) {
-        double *a = band + j * W + (c - j + kl);
-        double *bq = band + q * W + (c - q + kl);
-        const double t = *a;
-        *a = *bq;
-        *bq = t;
-      }
-      if (tid == 0) {
-        const double t = b[j];
-        b[j] = b[q];
-        b[q] = t;
-      }
+    const double rcp = s_rcp;
+    if (tid == jj) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c) row[c] = sA[c];
+      brow = sA[NB];
+    } else if (tid == p) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c) row[c] = sB[c];
+      brow = sB[NB];
     }
-    if (tid == 0) piv[j] = (int)(k0 + p);
-    __syncthreads();
-    if (tid == 0) s_bj = b[j];
-    const double d = sp[jj * NB + jj];
-    if (d == 0.0 && tid == 0) atomicMin(info, (int)j);
-    __syncthreads();
-    const double bj = s_bj;
-    if (d != 0.0) {
-      for (int r = jj + 1 + tid; r <= rmax; r += blockDim.x) {
-        const double l = sp[r * NB + jj] / d;
-        sp[r * NB + jj] = l;
-        b[k0 + r] -= l * bj;
-      }
+    if (rcp == 0.0) {
+      if (tid == 0) atomicMin(info, (int)(k0 + jj));
+      continue;
     }
-    __syncthreads();
-    const int ncol = nbc - 1 - jj, nrow = rmax - jj;
-    for (int idx = tid; idx < nrow * ncol; idx += blockDim.x) {
-      const int r = jj + 1 + idx / ncol, c = jj + 1 + idx % ncol;
-      sp[r * NB + c] -= sp[r * NB + jj] * sp[jj * NB + c];
+    if (own && tid > jj && tid <= rmax) {
+      const double l = row[jj] * rcp;  // LAPACK's scaling by the pivot's reciprocal
+      row[jj] = l;
+#pragma unroll
+      for (int c = jj + 1; c < NB; ++c) row[c] -= l * sA[c];
+      brow -= l * sA[NB];
     }
-    __syncthreads();
   }
-  // U of the panel rows back into the band; the whole panel (L11 and L21, which row
-  // interchanges can carry outside the band) to the dense panel buffer
-  for (int idx = tid; idx < R * NB; idx += blockDim.x) {
-    const int r = idx / NB, c = idx % NB;
-    const int off = c - r + kl;
-    if (c < nbc && c >= r && off < W) band[(k0 + r) * (int64_t)W + off] = sp[idx];
-    Lbuf[idx] = sp[idx];
+  // U of the panel rows back into the band; the whole panel (L11 and L21, which interchanges can
+  // carry outside the band) to the dense panel buffer; the right-hand side; the pivots
+  if (own) {
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      const int off = c - tid + kl;
+      if (c < nbc && c >= tid && off < W) band[(k0 + tid) * (int64_t)W + off] = row[c];
+      Lbuf[(int64_t)tid * NB + c] = row[c];
+    }
+    b[k0 + tid] = brow;
+  }
+  __syncthreads();
+  for (int jj = tid; jj < nbc; jj += blockDim.x) piv[k0 + jj] = (int)(k0 + s_piv[jj]);
+  // trailing columns of the moved rows: position i takes those of window row who[i] (a row's
+  // storage ends at column (its index) + kl + ku; beyond it the moved row is zero)
+  if (k1 < n) {
+    for (int i = warp; i < R; i += nwarps) {
+      if (who[i] == i) continue;
+      const int64_t gi = k0 + i;
+      const int64_t cend = min(n - 1, gi + kl + ku);
+      for (int64_t c = k1 + lane; c <= cend; c += 32) Tbuf[(int64_t)i * W + (c - k1)] = band[gi * W + (c - gi + kl)];
+    }
+    __syncthreads();
+    for (int i = warp; i < R; i += nwarps) {
+      const int o = who[i];
+      if (o == i) continue;
+      const int64_t gi = k0 + i, go = k0 + o;
+      const int64_t cend = min(n - 1, gi + kl + ku);
+      for (int64_t c = k1 + lane; c <= cend; c += 32)
+        band[gi * W + (c - gi + kl)] = c <= go + kl + ku ? Tbuf[(int64_t)o * W + (c - k1)] : 0.0;
+    }
   }
 }
 
-// U12 = L11^-1 A12: columns k1 .. k1 + ncols - 1, one thread each
+// U12 = L11^-1 A12: columns k1 .. k1 + ncols - 1, a warp per column (lane ii holds row ii), so the
+// columns spread over all SMs
 template <int NB>
-__global__ void k_band_trsm(double *band, int64_t n, int kl, int W, int64_t k0, int ncols,
-                            const double *__restrict__ Lbuf) {
-  __shared__ double L[NB][NB];
+__global__ void __launch_bounds__(256) k_band_trsm(double *band, int64_t n, int kl, int W, int64_t k0, int ncols,
+                                                  const double *__restrict__ Lbuf) {
+  __shared__ double L[NB][NB + 1];
   const int64_t k1 = min(k0 + NB, n);
   const int nbc = (int)(k1 - k0);
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
@@ -202,70 +233,63 @@ __global__ void k_band_trsm(double *band, int64_t n, int kl, int W, int64_t k0, 
     L[ii][jj] = (ii > jj && ii < nbc) ? Lbuf[idx] : 0.0;
   }
   __syncthreads();
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (t >= ncols) return;
   const int64_t c = k1 + t;
-  double u[NB];
+  const int64_t off = c - (k0 + lane) + kl;
+  const bool mine = lane < nbc && off < W;
+  double u = mine ? band[(k0 + lane) * W + off] : 0.0;
 #pragma unroll
-  for (int ii = 0; ii < NB; ++ii) {
-    const int64_t off = c - (k0 + ii) + kl;
-    u[ii] = (ii < nbc && off < W) ? band[(k0 + ii) * W + off] : 0.0;
+  for (int jj = 0; jj < NB; ++jj) {
+    const double uj = __shfl_sync(0xffffffffu, u, jj);
+    if (lane > jj && lane < NB) u -= L[lane < NB ? lane : 0][jj] * uj;
   }
-#pragma unroll
-  for (int jj = 0; jj < NB; ++jj)
-#pragma unroll
-    for (int ii = jj + 1; ii < NB; ++ii) u[ii] -= L[ii][jj] * u[jj];
-#pragma unroll
-  for (int ii = 0; ii < NB; ++ii) {
-    const int64_t off = c - (k0 + ii) + kl;
-    if (ii < nbc && off < W) band[(k0 + ii) * W + off] = u[ii];
-  }
+  if (mine) band[(k0 + lane) * W + off] = u;
 }
 
-// A22 -= L21 U12 over rows k1 .. k1 + nrows - 1 and columns k1 .. k1 + ncols - 1
+// A22 -= L21 U12 over rows k1 .. k1 + nrows - 1 and columns k1 .. k1 + ncols - 1, 32 x 32 tiles
+// (the FP64 pipe is the bound: small tiles spread one panel's update over all SMs)
+constexpr int kTile = 32;
 template <int NB>
 __global__ void __launch_bounds__(256) k_band_update(double *band, int64_t n, int kl, int W, int64_t k0, int nrows,
                                                     int ncols, const double *__restrict__ Lbuf) {
-  __shared__ double Lt[64][NB + 1];
-  __shared__ double Ut[NB][64];
+  __shared__ double Lt[kTile][NB + 1];
+  __shared__ double Ut[NB][kTile + 1];
   const int64_t k1 = min(k0 + NB, n);
   const int nbc = (int)(k1 - k0);
-  const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
-  for (int idx = threadIdx.x; idx < 64 * NB; idx += blockDim.x) {
+  const int r0 = blockIdx.y * kTile, c0 = blockIdx.x * kTile;
+  for (int idx = threadIdx.x; idx < kTile * NB; idx += blockDim.x) {
     const int i = idx / NB, jj = idx % NB;
-    const int64_t rl = (k1 - k0) + r0 + i;  // row in the panel buffer
+    const int64_t rl = nbc + r0 + i;  // row in the panel buffer
     Lt[i][jj] = (r0 + i < nrows && jj < nbc) ? Lbuf[rl * NB + jj] : 0.0;
   }
-  for (int idx = threadIdx.x; idx < 64 * NB; idx += blockDim.x) {
-    const int jj = idx / 64, t = idx % 64;
+  for (int idx = threadIdx.x; idx < kTile * NB; idx += blockDim.x) {
+    const int jj = idx / kTile, t = idx % kTile;
     const int64_t c = k1 + c0 + t;
     const int64_t off = c - (k0 + jj) + kl;
     Ut[jj][t] = (c0 + t < ncols && jj < nbc && off < W) ? band[(k0 + jj) * W + off] : 0.0;
   }
   __syncthreads();
-  const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
-  double acc[4][4] = {};
-#pragma unroll
+  const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;  // rows ti, ti+16; columns tj, tj+16
+  double acc[2][2] = {};
+#pragma unroll 8
   for (int jj = 0; jj < NB; ++jj) {
-    double a[4], bb[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      a[u] = Lt[ti * 4 + u][jj];
-      bb[u] = Ut[jj][tj * 4 + u];
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * bb[v];
+    const double a0 = Lt[ti][jj], a1 = Lt[ti + 16][jj];
+    const double b0 = Ut[jj][tj], b1 = Ut[jj][tj + 16];
+    acc[0][0] += a0 * b0;
+    acc[0][1] += a0 * b1;
+    acc[1][0] += a1 * b0;
+    acc[1][1] += a1 * b1;
   }
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const int i = r0 + ti * 4 + u;
+  for (int u = 0; u < 2; ++u) {
+    const int i = r0 + ti + 16 * u;
     if (i >= nrows) continue;
     const int64_t r = k1 + i;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int t = c0 + tj * 4 + v;
+    for (int v = 0; v < 2; ++v) {
+      const int t = c0 + tj + 16 * v;
       if (t >= ncols) continue;
       const int64_t off = (k1 + t) - r + kl;
       if (off >= 0 && off < W) band[r * W + off] -= acc[u][v];
@@ -273,10 +297,12 @@ __global__ void __launch_bounds__(256) k_band_update(double *band, int64_t n, in
   }
 }
 
-// U x = y, 32 rows at a time from the bottom
+// U x = y, 32 rows at a time from the bottom: a warp per row for the part from solved unknowns,
+// the 32 x 32 diagonal block staged in shared memory, one warp for the triangle
 __global__ void __launch_bounds__(1024) k_band_back(const double *__restrict__ band, int64_t n, int kl, int ku,
                                                    int W, const double *__restrict__ y, double *x) {
   __shared__ double acc[32];
+  __shared__ double Ud[32][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t j1 = n; j1 > 0; j1 -= 32) {
     const int64_t j0 = j1 - 32 > 0 ? j1 - 32 : 0;
@@ -285,26 +311,25 @@ __global__ void __launch_bounds__(1024) k_band_back(const double *__restrict__ b
       const int64_t i = j0 + warp;
       const int64_t cend = min(n - 1, i + kl + ku);
       double s = 0.0;
+#pragma unroll 4
       for (int64_t c = j1 + lane; c <= cend; c += 32) s += band[i * W + (c - i + kl)] * x[c];
       for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
       if (lane == 0) acc[warp] = y[i] - s;
+      const int64_t off = (j0 + lane) - i + kl;  // row `warp` of the diagonal block, column `lane`
+      Ud[warp][lane] = (lane >= warp && lane < nr && off < W) ? band[i * W + off] : 0.0;
     }
     __syncthreads();
     if (warp == 0) {
       double a = lane < nr ? acc[lane] : 0.0;
-      const int64_t i = j0 + lane;
+      const double dl = lane < nr ? Ud[lane][lane] : 1.0;  // each lane divides once, at its turn
       for (int t = nr - 1; t >= 0; --t) {
         double xt = 0.0;
-        if (lane == t) {
-          xt = a / band[i * W + kl];
-          x[i] = xt;
-        }
+        if (lane == t) xt = a / dl;
         xt = __shfl_sync(0xffffffffu, xt, t);
-        if (lane < t) {
-          const int64_t off = (j0 + t) - i + kl;
-          if (off < W) a -= band[i * W + off] * xt;
-        }
+        if (lane < t) a -= Ud[lane][t] * xt;
+        if (lane == t) a = xt;
       }
+      if (lane < nr) x[j0 + lane] = a;
     }
     __syncthreads();
   }
@@ -320,27 +345,27 @@ int ensure_lu(mic_ctx *ctx, size_t need) {
   return MIC_OK;
 }
 
-template <int NB>
+template <int NB, int MAXT>
 int factor_solve(mic_ctx *ctx, double *band, int64_t n, int kl, int ku, int W, int *piv, double *b, int *info,
-                 double *Lbuf) {
-  const size_t smem = sizeof(double) * (size_t)(NB + kl) * NB;
-  MIC_CUDA_TRY(cudaFuncSetAttribute(k_band_panel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                 double *Lbuf, double *Tbuf) {
   for (int64_t k0 = 0; k0 < n; k0 += NB) {
     const int64_t k1 = std::min<int64_t>(k0 + NB, n);
+    const int R = (int)(std::min<int64_t>(n, k1 + kl) - k0);
     {
       MIC_KERNEL(ctx, "k_band_panel");
-      k_band_panel<NB><<<1, kPanelThreads, smem, ctx->stream>>>(band, n, kl, ku, W, k0, piv, b, info, Lbuf);
+      k_band_panel<NB, MAXT><<<1, (R + 31) / 32 * 32, 0, ctx->stream>>>(band, n, kl, ku, W, k0, piv, b, info, Lbuf,
+                                                                        Tbuf);
     }
     if (k1 >= n) break;
     const int ncols = (int)(std::min<int64_t>(n - 1, k1 - 1 + kl + ku) - k1 + 1);
     const int nrows = (int)(std::min<int64_t>(n - 1, k1 - 1 + kl) - k1 + 1);
     if (ncols > 0) {
       MIC_KERNEL(ctx, "k_band_trsm");
-      k_band_trsm<NB><<<(ncols + 127) / 128, 128, 0, ctx->stream>>>(band, n, kl, W, k0, ncols, Lbuf);
+      k_band_trsm<NB><<<(ncols + 7) / 8, 256, 0, ctx->stream>>>(band, n, kl, W, k0, ncols, Lbuf);
     }
     if (ncols > 0 && nrows > 0) {
       MIC_KERNEL(ctx, "k_band_update");
-      dim3 g((ncols + 63) / 64, (nrows + 63) / 64);
+      dim3 g((ncols + kTile - 1) / kTile, (nrows + kTile - 1) / kTile);
       k_band_update<NB><<<g, 256, 0, ctx->stream>>>(band, n, kl, W, k0, nrows, ncols, Lbuf);
     }
   }
@@ -380,17 +405,21 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   const int kl = hbw[0], ku = hbw[1];
   const int W = 2 * kl + ku + 1;
-  const size_t kSmemMax = 200 * 1024;
+  // panel width: the window's NB + kl rows are one thread each (at most 1024); 32 columns in
+  // registers while the window fits 512 threads, else 16, else 8
   int nb = 0;
-  for (int cand : {32, 16, 8})
-    if (sizeof(double) * (size_t)(cand + kl) * cand <= kSmemMax) {
-      nb = cand;
-      break;
-    }
-  if (!nb) return MIC_ERR_SOLVE;  // band wider than a panel in shared memory
+  if (32 + kl <= 512)
+    nb = 32;
+  else if (16 + kl <= 1024)
+    nb = 16;
+  else if (8 + kl <= 1024)
+    nb = 8;
+  if (!nb) return MIC_ERR_SOLVE;  // band wider than one panel window
   const size_t lbuf = (size_t)(nb + kl) * nb;
+  const size_t tbuf = (size_t)(nb + kl) * W;
   const size_t need = 256 + (((size_t)n * W * sizeof(double) + 255) / 256) * 256 +
-                      3 * (((size_t)n * 8 + 255) / 256) * 256 + ((lbuf * 8 + 255) / 256) * 256 + 256;
+                      3 * (((size_t)n * 8 + 255) / 256) * 256 + ((lbuf * 8 + 255) / 256) * 256 +
+                      ((tbuf * 8 + 255) / 256) * 256 + 256;
   int e = ensure_lu(ctx, need);
   if (e) return e;
   unsigned char *p = static_cast<unsigned char *>(ctx->lu_buf);
@@ -400,6 +429,7 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
   double *x = carve<double>(p, n);
   int *piv = carve<int>(p, n);
   double *Lbuf = carve<double>(p, lbuf);
+  double *Tbuf = carve<double>(p, tbuf);
   MIC_CUDA_TRY(cudaMemsetAsync(band, 0, sizeof(double) * (size_t)n * W, ctx->stream));
   const int big = INT_MAX;
   MIC_CUDA_TRY(cudaMemcpyAsync(info, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
@@ -409,11 +439,11 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
                                                             transpose, kl, W, band, b);
   }
   if (nb == 32)
-    e = factor_solve<32>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf);
+    e = factor_solve<32, 512>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, Tbuf);
   else if (nb == 16)
-    e = factor_solve<16>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf);
+    e = factor_solve<16, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, Tbuf);
   else
-    e = factor_solve<8>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf);
+    e = factor_solve<8, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, Tbuf);
   if (e) return e;
   {
     MIC_KERNEL(ctx, "k_band_back");

@@ -535,6 +535,25 @@ def density_case(nx_cells=32, ny_cells=8, seed=6):
     return wl, dopt
 
 
+def subduction_box(nx_cells=128, ny_cells=32, nm=4, seed=4):
+    """The refined VEP box as a self-consistent subduction model: markers nm x nm per cell, a slab
+    dipping at 0.8 rad entering from the left at 5 cm/yr below an overriding plate 0.3 LY thick
+    (with a root 0.05 LY deep centred at LX/2), gravity 10 m/s^2, top at 273 K.  Returns
+    (workload, mic_timestep_options) for mic_subduction_timestep: first step, at most 4
+    plasticity iterations, displacement limit half a cell, temperature change limit 50 K."""
+    from .mic_types import DensityOptions, SubductionOptions, TimestepOptions
+
+    wl = vep_slab_box(nx_cells=nx_cells, ny_cells=ny_cells, nm=nm, seed=seed)
+    g = wl.grid
+    so = SubductionOptions(gx=0.0, gy=10.0, slabVelocity=0.05 / 3.15576e7, slabAngle=0.8, slabAge=50.0,
+                           overridingPlateThickness=0.3 * g.LY, rootThickness=0.05 * g.LY, rootCenter=0.5 * g.LX,
+                           rootWidth=0.2 * g.LX, thermalBCTopType=0, thermalBCTopValue=273.0)
+    topt = TimestepOptions(dtMax=3.0e11, displacementStepLimit=0.5, maxTempChange=50.0, maxNumPlasticity=4,
+                           shearHeating=1, firstStep=1, densityControl=0,
+                           density=DensityOptions(NMX=nm, NMY=nm, minMarkers=1, maxMarkers=100), sub=so)
+    return wl, topt
+
+
 WORKLOADS = {
     "convection_box": convection_box,
     "vep_slab_box": vep_slab_box,
