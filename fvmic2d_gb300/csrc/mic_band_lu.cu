@@ -14,9 +14,9 @@
 //   panel  one CTA, each window row in one thread's registers, column by column: pivot row
 //          (largest |value|, first on ties), interchange (whole panel rows, the right-hand side
 //          too), multipliers, rank-1 update of the panel; the forward substitution of the
-//          right-hand side rides along (it is one more column); the trailing columns of the rows
-//          whose position changed follow once per panel, as a gather;
-//   trsm   U12 = L11^-1 A12 for the columns right of the panel, a warp per column;
+//          right-hand side rides along (it is one more column);
+//   trsm   the trailing columns of the rows whose position changed follow them (a gather), then
+//          U12 = L11^-1 A12 for the columns right of the panel, a warp per column;
 //   update A22 -= L21 U12 over the band window, 32 x 32 tiles.
 // Interchanges inside a panel move whole panel rows, multipliers included, so that the panel's
 // L is in final row order for the deferred trsm and update; interchanges can carry multipliers
@@ -83,10 +83,10 @@ __global__ void k_band_gather(const double *__restrict__ x, int64_t n, int dof, 
 // its multiplier and updating itself against the broadcast pivot row.  Interchanges move whole
 // panel rows (multipliers included, so that L ends in final row order for the deferred trsm and
 // update) and the right-hand side; the trailing columns of the rows whose position changed
-// follow once at the end, as a gather.
+// follow in the trsm (the list of moved rows goes to `moved`).
 template <int NB, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_band_panel(double *band, int64_t n, int kl, int ku, int W, int64_t k0,
-                                                    int *piv, double *b, int *info, double *Lbuf, double *Tbuf) {
+                                                    int *piv, double *b, int *info, double *Lbuf, int *moved) {
   __shared__ double sA[NB + 1];  // the pivot row (new row jj) and its right-hand side
   __shared__ double sB[NB + 1];  // row jj, which moves to the pivot's position
   __shared__ long long red_v[MAXT / 32];
@@ -94,6 +94,7 @@ __global__ void __launch_bounds__(MAXT) k_band_panel(double *band, int64_t n, in
   __shared__ int who[MAXT];      // the window row now at each position
   __shared__ int s_piv[NB];
   __shared__ double s_rcp;
+  __shared__ int s_nchg;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int64_t k1 = min(k0 + NB, n);
   const int nbc = (int)(k1 - k0);
@@ -199,44 +200,63 @@ __global__ void __launch_bounds__(MAXT) k_band_panel(double *band, int64_t n, in
   }
   __syncthreads();
   for (int jj = tid; jj < nbc; jj += blockDim.x) piv[k0 + jj] = (int)(k0 + s_piv[jj]);
-  // trailing columns of the moved rows: position i takes those of window row who[i] (a row's
-  // storage ends at column (its index) + kl + ku; beyond it the moved row is zero)
-  if (k1 < n) {
-    for (int i = warp; i < R; i += nwarps) {
-      if (who[i] == i) continue;
-      const int64_t gi = k0 + i;
-      const int64_t cend = min(n - 1, gi + kl + ku);
-      for (int64_t c = k1 + lane; c <= cend; c += 32) Tbuf[(int64_t)i * W + (c - k1)] = band[gi * W + (c - gi + kl)];
-    }
-    __syncthreads();
-    for (int i = warp; i < R; i += nwarps) {
-      const int o = who[i];
-      if (o == i) continue;
-      const int64_t gi = k0 + i, go = k0 + o;
-      const int64_t cend = min(n - 1, gi + kl + ku);
-      for (int64_t c = k1 + lane; c <= cend; c += 32)
-        band[gi * W + (c - gi + kl)] = c <= go + kl + ku ? Tbuf[(int64_t)o * W + (c - k1)] : 0.0;
-    }
+  // the positions whose row changed and the window row each now holds, for the trsm's gather
+  if (tid == 0) s_nchg = 0;
+  __syncthreads();
+  if (own && who[tid] != tid) {
+    const int q = atomicAdd(&s_nchg, 1);
+    moved[1 + 2 * q] = tid;
+    moved[2 + 2 * q] = who[tid];
   }
+  __syncthreads();
+  if (tid == 0) moved[0] = s_nchg;
 }
 
 // U12 = L11^-1 A12: columns k1 .. k1 + ncols - 1, a warp per column (lane ii holds row ii), so the
-// columns spread over all SMs
+// columns spread over all SMs.  First the column's entries of the rows the panel moved follow
+// them: every nonzero an interchange at step j moves lies in columns j .. j + kl + ku, inside this
+// range, so the gather is complete here; each warp reads all the moved entries of its column
+// before it writes any.
 template <int NB>
-__global__ void __launch_bounds__(256) k_band_trsm(double *band, int64_t n, int kl, int W, int64_t k0, int ncols,
-                                                  const double *__restrict__ Lbuf) {
+__global__ void __launch_bounds__(256) k_band_trsm(double *band, int64_t n, int kl, int ku, int W, int64_t k0,
+                                                  int ncols, const double *__restrict__ Lbuf,
+                                                  const int *__restrict__ moved) {
   __shared__ double L[NB][NB + 1];
+  __shared__ int mv[4 * NB + 1];
   const int64_t k1 = min(k0 + NB, n);
   const int nbc = (int)(k1 - k0);
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int ii = idx / NB, jj = idx % NB;
     L[ii][jj] = (ii > jj && ii < nbc) ? Lbuf[idx] : 0.0;
   }
+  const int nm = moved[0];  // at most 2 NB rows change position
+  for (int idx = threadIdx.x; idx < 2 * nm; idx += blockDim.x) mv[idx] = moved[1 + idx];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (t >= ncols) return;
   const int64_t c = k1 + t;
+  constexpr int PERM = (2 * NB + 31) / 32;
+  double v[PERM];
+#pragma unroll
+  for (int q = 0; q < PERM; ++q) {
+    const int e = lane + 32 * q;
+    v[q] = 0.0;
+    if (e < nm) {
+      const int64_t go = k0 + mv[2 * e + 1];
+      if (c <= go + kl + ku) v[q] = band[go * W + (c - go + kl)];
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < PERM; ++q) {
+    const int e = lane + 32 * q;
+    if (e < nm) {
+      const int64_t gi = k0 + mv[2 * e];
+      if (c <= gi + kl + ku) band[gi * W + (c - gi + kl)] = v[q];
+    }
+  }
+  __syncwarp();
   const int64_t off = c - (k0 + lane) + kl;
   const bool mine = lane < nbc && off < W;
   double u = mine ? band[(k0 + lane) * W + off] : 0.0;
@@ -321,10 +341,10 @@ __global__ void __launch_bounds__(1024) k_band_back(const double *__restrict__ b
     __syncthreads();
     if (warp == 0) {
       double a = lane < nr ? acc[lane] : 0.0;
-      const double dl = lane < nr ? Ud[lane][lane] : 1.0;  // each lane divides once, at its turn
+      const double rd = 1.0 / (lane < nr ? Ud[lane][lane] : 1.0);  // all lanes' divisions at once
       for (int t = nr - 1; t >= 0; --t) {
         double xt = 0.0;
-        if (lane == t) xt = a / dl;
+        if (lane == t) xt = a * rd;
         xt = __shfl_sync(0xffffffffu, xt, t);
         if (lane < t) a -= Ud[lane][t] * xt;
         if (lane == t) a = xt;
@@ -347,21 +367,21 @@ int ensure_lu(mic_ctx *ctx, size_t need) {
 
 template <int NB, int MAXT>
 int factor_solve(mic_ctx *ctx, double *band, int64_t n, int kl, int ku, int W, int *piv, double *b, int *info,
-                 double *Lbuf, double *Tbuf) {
+                 double *Lbuf, int *moved) {
   for (int64_t k0 = 0; k0 < n; k0 += NB) {
     const int64_t k1 = std::min<int64_t>(k0 + NB, n);
     const int R = (int)(std::min<int64_t>(n, k1 + kl) - k0);
     {
       MIC_KERNEL(ctx, "k_band_panel");
       k_band_panel<NB, MAXT><<<1, (R + 31) / 32 * 32, 0, ctx->stream>>>(band, n, kl, ku, W, k0, piv, b, info, Lbuf,
-                                                                        Tbuf);
+                                                                        moved);
     }
     if (k1 >= n) break;
     const int ncols = (int)(std::min<int64_t>(n - 1, k1 - 1 + kl + ku) - k1 + 1);
     const int nrows = (int)(std::min<int64_t>(n - 1, k1 - 1 + kl) - k1 + 1);
     if (ncols > 0) {
       MIC_KERNEL(ctx, "k_band_trsm");
-      k_band_trsm<NB><<<(ncols + 7) / 8, 256, 0, ctx->stream>>>(band, n, kl, W, k0, ncols, Lbuf);
+      k_band_trsm<NB><<<(ncols + 7) / 8, 256, 0, ctx->stream>>>(band, n, kl, ku, W, k0, ncols, Lbuf, moved);
     }
     if (ncols > 0 && nrows > 0) {
       MIC_KERNEL(ctx, "k_band_update");
@@ -416,10 +436,10 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
     nb = 8;
   if (!nb) return MIC_ERR_SOLVE;  // band wider than one panel window
   const size_t lbuf = (size_t)(nb + kl) * nb;
-  const size_t tbuf = (size_t)(nb + kl) * W;
+  const size_t mbuf = 1 + 4 * 32;  // count, then (position, window row) pairs, at most 2 NB
   const size_t need = 256 + (((size_t)n * W * sizeof(double) + 255) / 256) * 256 +
                       3 * (((size_t)n * 8 + 255) / 256) * 256 + ((lbuf * 8 + 255) / 256) * 256 +
-                      ((tbuf * 8 + 255) / 256) * 256 + 256;
+                      ((mbuf * 4 + 255) / 256) * 256 + 256;
   int e = ensure_lu(ctx, need);
   if (e) return e;
   unsigned char *p = static_cast<unsigned char *>(ctx->lu_buf);
@@ -429,7 +449,7 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
   double *x = carve<double>(p, n);
   int *piv = carve<int>(p, n);
   double *Lbuf = carve<double>(p, lbuf);
-  double *Tbuf = carve<double>(p, tbuf);
+  int *moved = carve<int>(p, mbuf);
   MIC_CUDA_TRY(cudaMemsetAsync(band, 0, sizeof(double) * (size_t)n * W, ctx->stream));
   const int big = INT_MAX;
   MIC_CUDA_TRY(cudaMemcpyAsync(info, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
@@ -439,11 +459,11 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
                                                             transpose, kl, W, band, b);
   }
   if (nb == 32)
-    e = factor_solve<32, 512>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, Tbuf);
+    e = factor_solve<32, 512>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, moved);
   else if (nb == 16)
-    e = factor_solve<16, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, Tbuf);
+    e = factor_solve<16, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, moved);
   else
-    e = factor_solve<8, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, Tbuf);
+    e = factor_solve<8, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, moved);
   if (e) return e;
   {
     MIC_KERNEL(ctx, "k_band_back");
