@@ -89,6 +89,8 @@ def parse():
     ap.add_argument("--creep-mode", type=int, default=0, choices=[0, 1, 2],
                     help="law-7 solve of the main leg: 0 exact, 1 FP32 surrogate, 2 tensor-core surrogate")
     ap.add_argument("--no-systems", action="store_true", help="skip the linear-systems / whole-time-step leg")
+    ap.add_argument("--only-systems", action="store_true",
+                    help="run only the linear-systems / whole-time-step leg and print it (for profiling the solver)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-cores", type=int, default=0, help="host processes for the CPU legs (0 = all)")
     return ap.parse_args()
@@ -271,6 +273,13 @@ def run_reference_arm(args):
 
 def run_ours(args):
     world, rank, local, pg = dist_setup(args)
+    if args.only_systems:
+        if rank == 0:
+            import torch
+
+            torch.cuda.set_device(local)
+            print(json.dumps({"systems": systems_leg(args, local)}), flush=True)
+        return
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # bounded sample: one step per replica on all host cores, spawned before any GPU work

@@ -260,14 +260,22 @@ def timestep_table():
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     from tests.timestep_case import reference_timestep, timestep_case
 
+    from tests.timestep_case import timestep_density_case
+
+    out = {}
     wl, topt = timestep_case()
-    before = np.array(wl.markers, copy=True)
-    mk, rep, nodal = reference_timestep(wl, topt, elapsed=0.0)
-    out = {"before": before.view(np.uint8), "after": mk.view(np.uint8)}
-    for k, v in rep.items():
-        out["rep_" + k] = np.array(v)
-    for k, v in nodal.items():
-        out["nodal_" + k] = v
+    cases = [("", wl, topt, None)]
+    wl2, topt2, cap2 = timestep_density_case()
+    cases.append(("dens_", wl2, topt2, cap2))
+    for pre, w, t, cap in cases:
+        before = np.array(w.markers, copy=True)
+        mk, rep, nodal = reference_timestep(w, t, elapsed=0.0, capacity=cap)
+        out[pre + "before"] = before.view(np.uint8)
+        out[pre + "after"] = mk.view(np.uint8)
+        for k, v in rep.items():
+            out[pre + "rep_" + k] = np.array(v)
+        for k, v in nodal.items():
+            out[pre + "nodal_" + k] = v
     return out
 
 

@@ -10,7 +10,7 @@ import pytest
 
 from fvmic2d_gb300 import gpu
 from fvmic2d_gb300.mic_types import MARKER_DTYPE
-from tests.timestep_case import timestep_case
+from tests.timestep_case import timestep_case, timestep_density_case
 
 pytestmark = pytest.mark.gpu
 
@@ -28,18 +28,28 @@ def _fields(m):
 
 
 @pytest.mark.parametrize("build", ["exact", "product"])
-def test_timestep_matches_reference(build):
+@pytest.mark.parametrize("case", ["plain", "density"])
+def test_timestep_matches_reference(build, case):
+    """plain: no density control; density: checkMarkerDensity inside the step fills an emptied
+    block of the wedge and the first cell column (subduction-inflow markers) before the solves"""
     z = np.load(os.path.join(GOLDEN, "subduction_step.npz"))
-    wl, topt = timestep_case()
-    wl.markers = z["before"].view(MARKER_DTYPE).copy()
-    ref = z["after"].view(MARKER_DTYPE)
-    G = gpu.MicProblem(wl, exact=(build == "exact"))
+    pre = "" if case == "plain" else "dens_"
+    if case == "plain":
+        wl, topt = timestep_case()
+        cap = None
+    else:
+        wl, topt, cap = timestep_density_case()
+    wl.markers = z[pre + "before"].view(MARKER_DTYPE).copy()
+    ref = z[pre + "after"].view(MARKER_DTYPE)
+    G = gpu.MicProblem(wl, exact=(build == "exact"), capacity=cap)
     rep = G.subductionTimestep(topt, 0.0)
     assert rep["stopped"] == 0
+    assert rep["markers_added"] == int(z[pre + "rep_markers_added"])
     for k in ("plastic_iterations", "is_yielding", "converged", "thermal_resolves"):
-        assert rep[k] == int(z["rep_" + k]), k
+        assert rep[k] == int(z[pre + "rep_" + k]), k
     for k in ("dt", "displacement_dt", "Kbond", "Kcont", "max_T", "max_temp_change", "max_abs_sxx"):
-        assert abs(rep[k] - float(z["rep_" + k])) <= 1e-9 * abs(float(z["rep_" + k])), (k, rep[k], z["rep_" + k])
+        ref_v = float(z[pre + "rep_" + k])
+        assert abs(rep[k] - ref_v) <= 1e-9 * abs(ref_v), (k, rep[k], ref_v)
     got = G.markers
     assert len(got) == len(ref)
     gf, rf = _fields(got), _fields(ref)
@@ -50,5 +60,19 @@ def test_timestep_matches_reference(build):
         worst[k] = err
         assert err <= tol, (k, err, worst)
     for f in ("vx", "vy", "thisT"):
-        a, b = G.get_nodal(f), z["nodal_" + f]
+        a, b = G.get_nodal(f), z[pre + "nodal_" + f]
         assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(b)), f
+
+
+def test_timestep_stops_above_melting():
+    """a marker above the reference's TBREAK (9999 K) ends the step after the projection, as main
+    goes on to the next Monte-Carlo run: nothing is solved or advected"""
+    wl, topt = timestep_case()
+    wl.markers["T"][17] = 1.2e4
+    G = gpu.MicProblem(wl)
+    rep = G.subductionTimestep(topt, 0.0)
+    assert rep["stopped"] == 1 and rep["max_T"] == 1.2e4
+    assert rep["plastic_iterations"] == 0 and rep["dt"] == 0.0
+    got = G.markers
+    for f in ("X", "Y", "T", "sxx", "eta"):
+        assert np.array_equal(got[f], wl.markers[f]), f

@@ -27,6 +27,23 @@ def timestep_case(seed=4):
     return wl, topt
 
 
+def timestep_density_case(seed=6):
+    """the same box with density control in the step (main_subduction.c:250): markers emptied
+    from a block of cells inside the wedge and from the first cell column (the reference then adds
+    subduction-inflow markers there), drand48 stream at srand48(1), main's seed"""
+    wl, topt = timestep_case(seed=seed)
+    g, m = wl.grid, wl.markers
+    gone = ((m["X"] > g.x[12]) & (m["X"] < g.x[15]) & (m["Y"] > g.y[5]) & (m["Y"] < g.y[7])) | (m["X"] < g.x[1])
+    m["X"][gone] = -1.0
+    m["Y"][gone] = -1.0
+    so = topt.sub
+    topt.densityControl = 1
+    topt.density = DensityOptions(NMX=4, NMY=4, minMarkers=1, maxMarkers=100, slabAngle=so.slabAngle,
+                                  slabAge=so.slabAge, overridingPlateThickness=so.overridingPlateThickness,
+                                  rootThickness=so.rootThickness, rootCenter=so.rootCenter, rootWidth=so.rootWidth)
+    return wl, topt, len(m) + 4096
+
+
 def _spsolve(rp, c, v, rhs):
     import scipy.sparse as sp
     import scipy.sparse.linalg as spl
@@ -35,7 +52,7 @@ def _spsolve(rp, c, v, rhs):
     return spl.spsolve(sp.csr_matrix((v, c, rp), shape=(n, n)).tocsc(), rhs)
 
 
-def reference_timestep(wl, topt, elapsed=0.0):
+def reference_timestep(wl, topt, elapsed=0.0, capacity=None):
     """main_subduction.c:241-438 with the reference build's routines; returns (markers after the
     step, report dict, nodal fields dict)"""
     from oracle import refpy
@@ -44,9 +61,16 @@ def reference_timestep(wl, topt, elapsed=0.0):
     with open(os.devnull, "w") as devnull, contextlib.redirect_stdout(devnull):
         R = refpy.RefProblem(wl)
         R.findMarkerCells()
+        added = 0
+        if topt.densityControl:
+            n0 = len(R.markers)
+            out0 = int(np.sum(R.markers["cellX"] == -1))
+            R.checkMarkerDensity(topt.density, capacity, seed=1)
+            R.findMarkerCells()
+            added = len(R.markers) - n0 + out0 - int(np.sum(R.markers["cellX"] == -1))
         R.updateMarkerRho()
         R.projectMarkersNodesAll2()
-        rep = {"max_T": R.maxMarkerT()}
+        rep = {"max_T": R.maxMarkerT(), "markers_added": added}
         ddt = topt.dtMax
         is_y, conv, it = 1, 0, 0
         kb = kc = res = 0.0
