@@ -9,8 +9,8 @@
 // side.  The matrix goes into row-band storage, row i holding columns i-kl .. i+kl+ku (the extra
 // kl for the fill that row interchanges bring), W = 2 kl + ku + 1 values per row.
 //
-// Factorisation, right-looking in panels of NB columns (32, 16 or 8: the widest whose window of
-// NB + kl rows fits one CTA at one row per thread):
+// Factorisation, right-looking in panels of NB columns (16, or 8 when the window of NB + kl rows
+// would not fit one CTA at one row per thread):
 //   panel  one CTA, each window row in one thread's registers, column by column: pivot row
 //          (largest |value|, first on ties), interchange (whole panel rows, the right-hand side
 //          too), multipliers, rank-1 update of the panel; the forward substitution of the
@@ -425,12 +425,11 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   const int kl = hbw[0], ku = hbw[1];
   const int W = 2 * kl + ku + 1;
-  // panel width: the window's NB + kl rows are one thread each (at most 1024); 32 columns in
-  // registers while the window fits 512 threads, else 16, else 8
+  // panel width: the window's NB + kl rows are one thread each (at most 1024).  16 columns: 32
+  // halved the panel's launches but doubled its unrolled code and its per-column FP64 work, and
+  // was slower at every size measured (band 65 to 392)
   int nb = 0;
-  if (32 + kl <= 512)
-    nb = 32;
-  else if (16 + kl <= 1024)
+  if (16 + kl <= 1024)
     nb = 16;
   else if (8 + kl <= 1024)
     nb = 8;
