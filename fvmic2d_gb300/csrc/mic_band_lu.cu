@@ -17,7 +17,8 @@
 //          right-hand side rides along (it is one more column);
 //   trsm   the trailing columns of the rows whose position changed follow them (a gather), then
 //          U12 = L11^-1 A12 for the columns right of the panel, a warp per column;
-//   update A22 -= L21 U12 over the band window, 32 x 32 tiles.
+//   update A22 -= L21 U12 over the band window, 32 x 32 tiles: the next panel's columns on the
+//          main stream, the rest on a side stream, overlapping the next panel.
 // Interchanges inside a panel move whole panel rows, multipliers included, so that the panel's
 // L is in final row order for the deferred trsm and update; interchanges can carry multipliers
 // outside the band, so the panel's L goes to a dense (NB + kl) x NB buffer rather than back into
@@ -268,12 +269,13 @@ __global__ void __launch_bounds__(256) k_band_trsm(double *band, int64_t n, int 
   if (mine) band[(k0 + lane) * W + off] = u;
 }
 
-// A22 -= L21 U12 over rows k1 .. k1 + nrows - 1 and columns k1 .. k1 + ncols - 1, 32 x 32 tiles
+// A22 -= L21 U12 over rows k1 .. k1 + nrows - 1 and columns k1 + coff .. k1 + coff + ncols - 1,
+// 32 x 32 tiles
 // (the FP64 pipe is the bound: small tiles spread one panel's update over all SMs)
 constexpr int kTile = 32;
 template <int NB>
 __global__ void __launch_bounds__(256) k_band_update(double *band, int64_t n, int kl, int W, int64_t k0, int nrows,
-                                                    int ncols, const double *__restrict__ Lbuf) {
+                                                    int coff, int ncols, const double *__restrict__ Lbuf) {
   __shared__ double Lt[kTile][NB + 1];
   __shared__ double Ut[NB][kTile + 1];
   const int64_t k1 = min(k0 + NB, n);
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(256) k_band_update(double *band, int64_t n, in
   }
   for (int idx = threadIdx.x; idx < kTile * NB; idx += blockDim.x) {
     const int jj = idx / kTile, t = idx % kTile;
-    const int64_t c = k1 + c0 + t;
+    const int64_t c = k1 + coff + c0 + t;
     const int64_t off = c - (k0 + jj) + kl;
     Ut[jj][t] = (c0 + t < ncols && jj < nbc && off < W) ? band[(k0 + jj) * W + off] : 0.0;
   }
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(256) k_band_update(double *band, int64_t n, in
     for (int v = 0; v < 2; ++v) {
       const int t = c0 + tj + 16 * v;
       if (t >= ncols) continue;
-      const int64_t off = (k1 + t) - r + kl;
+      const int64_t off = (k1 + coff + t) - r + kl;
       if (off >= 0 && off < W) band[r * W + off] -= acc[u][v];
     }
   }
@@ -365,12 +367,22 @@ int ensure_lu(mic_ctx *ctx, size_t need) {
   return MIC_OK;
 }
 
+// The update of panel k splits in two: its first NB columns (the next panel's) on the main
+// stream, the rest on the side stream, where it runs while panel k+1 factors (the panel touches
+// only its own columns; the trailing columns of its interchanged rows move in its trsm, which
+// waits for the side stream).  The dense panel buffer alternates between two halves, so that
+// panel k+1 does not overwrite the L21 the side stream is still reading.
 template <int NB, int MAXT>
 int factor_solve(mic_ctx *ctx, double *band, int64_t n, int kl, int ku, int W, int *piv, double *b, int *info,
-                 double *Lbuf, int *moved) {
-  for (int64_t k0 = 0; k0 < n; k0 += NB) {
+                 double *Lbuf2, size_t lhalf, int *moved) {
+  cudaStream_t side = ctx->lu_side;
+  cudaEvent_t ev_trsm = ctx->lu_ev[0], ev_far = ctx->lu_ev[1];
+  bool far_pending = false;
+  int parity = 0;
+  for (int64_t k0 = 0; k0 < n; k0 += NB, parity ^= 1) {
     const int64_t k1 = std::min<int64_t>(k0 + NB, n);
     const int R = (int)(std::min<int64_t>(n, k1 + kl) - k0);
+    double *Lbuf = Lbuf2 + parity * lhalf;
     {
       MIC_KERNEL(ctx, "k_band_panel");
       k_band_panel<NB, MAXT><<<1, (R + 31) / 32 * 32, 0, ctx->stream>>>(band, n, kl, ku, W, k0, piv, b, info, Lbuf,
@@ -379,16 +391,31 @@ int factor_solve(mic_ctx *ctx, double *band, int64_t n, int kl, int ku, int W, i
     if (k1 >= n) break;
     const int ncols = (int)(std::min<int64_t>(n - 1, k1 - 1 + kl + ku) - k1 + 1);
     const int nrows = (int)(std::min<int64_t>(n - 1, k1 - 1 + kl) - k1 + 1);
+    if (far_pending) MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ev_far, 0));
+    far_pending = false;
     if (ncols > 0) {
       MIC_KERNEL(ctx, "k_band_trsm");
       k_band_trsm<NB><<<(ncols + 7) / 8, 256, 0, ctx->stream>>>(band, n, kl, ku, W, k0, ncols, Lbuf, moved);
     }
     if (ncols > 0 && nrows > 0) {
-      MIC_KERNEL(ctx, "k_band_update");
-      dim3 g((ncols + kTile - 1) / kTile, (nrows + kTile - 1) / kTile);
-      k_band_update<NB><<<g, 256, 0, ctx->stream>>>(band, n, kl, W, k0, nrows, ncols, Lbuf);
+      const int nnear = std::min(NB, ncols), nfar = ncols - nnear;
+      if (nfar > 0) MIC_CUDA_TRY(cudaEventRecord(ev_trsm, ctx->stream));
+      {
+        MIC_KERNEL(ctx, "k_band_update");
+        dim3 g((nnear + kTile - 1) / kTile, (nrows + kTile - 1) / kTile);
+        k_band_update<NB><<<g, 256, 0, ctx->stream>>>(band, n, kl, W, k0, nrows, 0, nnear, Lbuf);
+      }
+      if (nfar > 0) {
+        MIC_CUDA_TRY(cudaStreamWaitEvent(side, ev_trsm, 0));
+        dim3 g((nfar + kTile - 1) / kTile, (nrows + kTile - 1) / kTile);
+        k_band_update<NB><<<g, 256, 0, side>>>(band, n, kl, W, k0, nrows, nnear, nfar, Lbuf);
+        ++ctx->launches;
+        MIC_CUDA_TRY(cudaEventRecord(ev_far, side));
+        far_pending = true;
+      }
     }
   }
+  if (far_pending) MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ev_far, 0));
   return MIC_OK;
 }
 
@@ -434,20 +461,25 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
   else if (8 + kl <= 1024)
     nb = 8;
   if (!nb) return MIC_ERR_SOLVE;  // band wider than one panel window
-  const size_t lbuf = (size_t)(nb + kl) * nb;
+  const size_t lbuf = (((size_t)(nb + kl) * nb + 31) / 32) * 32;  // one half of the panel buffer
   const size_t mbuf = 1 + 4 * 32;  // count, then (position, window row) pairs, at most 2 NB
   const size_t need = 256 + (((size_t)n * W * sizeof(double) + 255) / 256) * 256 +
-                      3 * (((size_t)n * 8 + 255) / 256) * 256 + ((lbuf * 8 + 255) / 256) * 256 +
+                      3 * (((size_t)n * 8 + 255) / 256) * 256 + ((2 * lbuf * 8 + 255) / 256) * 256 +
                       ((mbuf * 4 + 255) / 256) * 256 + 256;
   int e = ensure_lu(ctx, need);
   if (e) return e;
+  if (!ctx->lu_side) {
+    MIC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->lu_side, cudaStreamNonBlocking));
+    MIC_CUDA_TRY(cudaEventCreateWithFlags(&ctx->lu_ev[0], cudaEventDisableTiming));
+    MIC_CUDA_TRY(cudaEventCreateWithFlags(&ctx->lu_ev[1], cudaEventDisableTiming));
+  }
   unsigned char *p = static_cast<unsigned char *>(ctx->lu_buf);
   int *info = carve<int>(p, 64);
   double *band = carve<double>(p, (size_t)n * W);
   double *b = carve<double>(p, n);
   double *x = carve<double>(p, n);
   int *piv = carve<int>(p, n);
-  double *Lbuf = carve<double>(p, lbuf);
+  double *Lbuf = carve<double>(p, 2 * lbuf);
   int *moved = carve<int>(p, mbuf);
   MIC_CUDA_TRY(cudaMemsetAsync(band, 0, sizeof(double) * (size_t)n * W, ctx->stream));
   const int big = INT_MAX;
@@ -457,13 +489,49 @@ extern "C" int mic_linear_solve(mic_ctx *ctx, int which) {
     k_band_scatter<<<grid_for(n), kBlock, 0, ctx->stream>>>(S.cnt, S.col, S.val, S.rhs, S.width, n, dof, NX, NY,
                                                             transpose, kl, W, band, b);
   }
-  if (nb == 32)
-    e = factor_solve<32, 512>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, moved);
-  else if (nb == 16)
-    e = factor_solve<16, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, moved);
-  else
-    e = factor_solve<8, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, moved);
-  if (e) return e;
+  auto factor = [&]() -> int {
+    if (nb == 32) return factor_solve<32, 512>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, lbuf, moved);
+    if (nb == 16) return factor_solve<16, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, lbuf, moved);
+    return factor_solve<8, 1024>(ctx, band, n, kl, ku, W, piv, b, info, Lbuf, lbuf, moved);
+  };
+  // The factorisation is 3-4 launches and two stream hand-offs per panel, the same sequence for
+  // every solve of a system of this shape (the band comes from the grid's stencil): captured once
+  // as a graph and replayed, so host launch cost stops gating the panels.  Not while launches are
+  // being timed one by one, and not beyond 20,000 panels (instantiation cost).
+  const bool graphable = !ctx->prof_on && (n + nb - 1) / nb <= 20000;
+  if (graphable && S.lu_exec && S.lu_key_buf == ctx->lu_buf && S.lu_key_n == n && S.lu_key_kl == kl &&
+      S.lu_key_ku == ku && S.lu_key_nb == nb) {
+    MIC_CUDA_TRY(cudaGraphLaunch(S.lu_exec, ctx->stream));
+    ctx->launches += S.lu_nodes;
+  } else if (graphable && cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+    const long long l0 = ctx->launches;
+    e = factor();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (e || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return e ? e : mic_fail_cuda(ctx, ce);
+    }
+    if (S.lu_exec) cudaGraphExecDestroy(S.lu_exec);
+    S.lu_exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&S.lu_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      S.lu_exec = nullptr;
+      return mic_fail_cuda(ctx, ie);
+    }
+    S.lu_nodes = ctx->launches - l0;
+    S.lu_key_buf = ctx->lu_buf;
+    S.lu_key_n = n;
+    S.lu_key_kl = kl;
+    S.lu_key_ku = ku;
+    S.lu_key_nb = nb;
+    MIC_CUDA_TRY(cudaGraphLaunch(S.lu_exec, ctx->stream));
+  } else {
+    cudaGetLastError();  // a stream that cannot be captured: launch directly
+    e = factor();
+    if (e) return e;
+  }
   {
     MIC_KERNEL(ctx, "k_band_back");
     k_band_back<<<1, 1024, 0, ctx->stream>>>(band, n, kl, ku, W, b, x);

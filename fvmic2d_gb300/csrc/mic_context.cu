@@ -24,6 +24,7 @@ extern "C" const char *mic_error_string(int code) {
     case MIC_ERR_NO_DEVICE: return "no CUDA device";
     case MIC_ERR_DENSITY: return "marker density control cannot proceed";
     case MIC_ERR_IO: return "checkpoint file could not be read or written";
+    case MIC_ERR_SOLVE: return "direct solve failed (zero pivot, or a band too wide)";
     default: return "unknown error";
   }
 }
@@ -150,6 +151,7 @@ static void free_ctx(mic_ctx *ctx) {
   cudaFree(ctx->solution);
   cudaFree(ctx->io_buf);
   for (int w = 0; w < 2; ++w) {
+    if (ctx->sys[w].lu_exec) cudaGraphExecDestroy(ctx->sys[w].lu_exec);
     cudaFree(ctx->sys[w].cnt);
     cudaFree(ctx->sys[w].col);
     cudaFree(ctx->sys[w].val);
@@ -157,6 +159,11 @@ static void free_ctx(mic_ctx *ctx) {
   }
   cudaFree(ctx->sys_scratch);
   cudaFree(ctx->lu_buf);
+  if (ctx->lu_side) {
+    cudaStreamDestroy(ctx->lu_side);
+    cudaEventDestroy(ctx->lu_ev[0]);
+    cudaEventDestroy(ctx->lu_ev[1]);
+  }
   cudaFree(ctx->stage_aos);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -80,6 +80,12 @@ struct mic_system_store {
   int factored;
   int kl, ku;       // band widths of the last factorisation
   int zero_pivot;   // first zero pivot of the last factorisation (-1: none)
+  // the factorisation's launches captured as a graph, valid for this buffer, size, band, panel
+  cudaGraphExec_t lu_exec;
+  const void *lu_key_buf;
+  int64_t lu_key_n;
+  int lu_key_kl, lu_key_ku, lu_key_nb;
+  long long lu_nodes;
 };
 
 struct mic_ctx {
@@ -112,6 +118,8 @@ struct mic_ctx {
   size_t sys_scratch_bytes;
   void *lu_buf;               // banded factorisation storage (grown on demand)
   size_t lu_bytes;
+  cudaStream_t lu_side;       // second stream of the factorisation: the far part of each update
+  cudaEvent_t lu_ev[2];       // its two hand-offs (trsm done, far update done)
   size_t io_bytes;
   size_t dens_bytes, dens_add_bytes;
   double *f64[mic::C_F64_COUNT];

@@ -491,6 +491,7 @@ int ensure_system(mic_ctx *ctx, int which, int64_t n) {
   cudaFree(S.col);
   cudaFree(S.val);
   cudaFree(S.rhs);
+  if (S.lu_exec) cudaGraphExecDestroy(S.lu_exec);
   S = mic_system_store{};
   if (cudaMalloc(&S.cnt, sizeof(int) * n) != cudaSuccess || cudaMalloc(&S.col, sizeof(int) * n * kMaxEnt) != cudaSuccess ||
       cudaMalloc(&S.val, sizeof(double) * n * kMaxEnt) != cudaSuccess ||
