@@ -128,3 +128,30 @@ def test_solve_larger_grid_residual():
     A = sp.csr_matrix((v, c, rp), shape=(len(rhs), len(rhs)))
     assert np.all(np.isfinite(x))
     assert np.max(np.abs(A @ x - rhs)) <= 1e-11 * np.max(np.abs(A).sum(axis=1)) * np.max(np.abs(x))
+
+
+def test_repeated_solves_replay_the_same_factorisation():
+    """The first solve of a system captures its factorisation as a CUDA graph; later solves of the
+    same shape replay it.  Stokes and thermal solves alternate over one shared factorisation
+    buffer: every replay gives the first solve's answer bit for bit, and the launch counter counts
+    the replayed kernels."""
+    z = _golden()
+    G, so, dt = _problem(z, "fixed_top")
+    G.formVEPSystem(so, dt)
+    G.enforceThermalBCs1(so)
+    G.formThermalSystem(so, dt)
+    first = {}
+    launches = []
+    for rnd in range(3):
+        for which in (G.STOKES, G.THERMAL):
+            l0 = G.launch_count()
+            G.linear_solve(which)
+            launches.append((which, G.launch_count() - l0))
+            x = G.solution(which)
+            if rnd == 0:
+                first[which] = x
+            else:
+                assert np.array_equal(x, first[which]), (rnd, which)
+    for which in (G.STOKES, G.THERMAL):
+        counts = [c for w, c in launches if w == which]
+        assert counts[0] > 10 and len(set(counts)) == 1, counts
