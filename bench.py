@@ -715,6 +715,32 @@ def systems_leg(args, local):
                        "note": "host wall time of mic_subduction_timestep: density control off, every "
                                "plasticity iteration assembles and solves the Stokes system on the device"}
     G.close()
+    # Monte-Carlo members (fvmic2d's iMonte loop runs them one after another): 16 independent
+    # 129 x 33 boxes with different slab angles, one step each, one member at a time and all of
+    # them from host threads side by side (mic_subduction_timestep_many)
+    members = []
+    for k in range(16):
+        wl, topt = W.subduction_box(nx_cells=128, ny_cells=32, nm=4, seed=10 + k)
+        topt.sub.slabAngle = 0.6 + 0.02 * k
+        members.append((gpu.MicProblem(wl, device=local), topt))
+    probs = [P for P, _ in members]
+    topts = [t for _, t in members]
+    gpu.subduction_timestep_many(probs, topts)  # warm-up step: buffers, captured factorisations
+    for t in topts:
+        t.firstStep = 0
+    t0 = time.perf_counter()
+    for P, t in members:
+        P.subductionTimestep(t, 0.0)
+    seq_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    gpu.subduction_timestep_many(probs, topts)
+    par_ms = (time.perf_counter() - t0) * 1e3
+    out["monte_carlo"] = {"members": len(members), "markers": int(sum(P.n for P in probs)),
+                          "one_at_a_time_ms_per_step": seq_ms, "side_by_side_ms_per_step": par_ms,
+                          "speedup": seq_ms / par_ms,
+                          "note": "host wall time of one step of every member"}
+    for P in probs:
+        P.close()
     return out
 
 

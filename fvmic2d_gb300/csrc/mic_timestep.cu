@@ -6,7 +6,11 @@
 // are assembled and solved on the device (mic_systems.cu, mic_band_lu.cu).  Nodal fields and
 // markers stay on the device; only scalars (time steps, flags, maxima) come back to the host,
 // where main_subduction's control flow runs.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <thread>
+#include <vector>
 
 #include "mic_internal.cuh"
 
@@ -143,4 +147,34 @@ extern "C" int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options 
   MIC_TRY(mic_max_abs_sxx(ctx, &rep->max_abs_sxx));
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return MIC_OK;
+}
+
+// Monte-Carlo members side by side.  fvmic2d's main runs its realisations one after another
+// (the iMonte loop, main_subduction.c); here independent contexts step together, one host
+// thread per member at a time, so that their sequential parts (the solver's panel chains, the
+// host decisions between passes) overlap on the GPU instead of queueing behind each other.
+extern "C" int mic_subduction_timestep_many(mic_ctx *const *ctxs, int n, const mic_timestep_options *options,
+                                            const double *elapsed_time, mic_timestep_report *reports,
+                                            int *codes, int max_threads) {
+  if (!ctxs || n < 0 || !options || !reports) return MIC_ERR_ARG;
+  for (int k = 0; k < n; ++k)
+    if (!ctxs[k]) return MIC_ERR_ARG;
+  int nt = max_threads > 0 ? max_threads : (int)std::thread::hardware_concurrency();
+  nt = std::max(1, std::min(nt, n));
+  std::atomic<int> next(0);
+  std::vector<int> rc(n, MIC_OK);
+  auto work = [&]() {
+    for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1))
+      rc[k] = mic_subduction_timestep(ctxs[k], &options[k], elapsed_time ? elapsed_time[k] : 0.0, &reports[k]);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto &th : pool) th.join();
+  int first = MIC_OK;
+  for (int k = 0; k < n; ++k) {
+    if (codes) codes[k] = rc[k];
+    if (rc[k] && !first) first = rc[k];
+  }
+  return first;
 }

@@ -109,6 +109,7 @@ SIGNATURES = {
     "mic_solution_get": (_I, [_P, _I, _DP]),
     "mic_system_band": (_I, [_P, _I, _IP, _IP]),
     "mic_subduction_timestep": (_I, [_P, _P, _D, _P]),
+    "mic_subduction_timestep_many": (_I, [_P, _I, _P, _DP, _P, _IP, _I]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
 }
@@ -608,3 +609,23 @@ class MicEnsemble:
             self.close()
         except Exception:
             pass
+
+
+def subduction_timestep_many(problems, topts, elapsed=None, max_threads=0):
+    """One mic_subduction_timestep on every problem at once (independent Monte-Carlo members, each
+    on its own stream, stepped from host threads side by side).  Returns the reports as dicts."""
+    from .mic_types import TimestepOptions, TimestepReport
+
+    n = len(problems)
+    L = problems[0].L
+    hs = (ctypes.c_void_p * n)(*[P.h for P in problems])
+    opts = (TimestepOptions * n)(*topts)
+    reps = (TimestepReport * n)()
+    codes = (ctypes.c_int * n)()
+    el = np.ascontiguousarray(np.zeros(n) if elapsed is None else elapsed, dtype=np.float64)
+    e = L.mic_subduction_timestep_many(hs, n, opts, _dp(el), reps, codes, max_threads)
+    for P in problems:
+        P.n = P._count()
+    if e:
+        raise MicError(e, "mic_subduction_timestep_many (member codes %s)" % list(codes))
+    return [r.as_dict() for r in reps]

@@ -303,6 +303,16 @@ int mic_system_band(mic_ctx *ctx, int which, int *kl, int *ku);
  * Options.staticVelocity and adiabaticHeating paths are not provided. */
 int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options *options, double elapsed_time,
                             mic_timestep_report *report);
+/* No counterpart in the reference, whose main runs its Monte-Carlo realisations one after another
+ * (iMonte): one mic_subduction_timestep on each of n independent contexts (each created with its
+ * own stream), members on up to max_threads host threads at once (0: the host's core count), so
+ * that their sequential parts overlap on the GPU.  options, elapsed_time (NULL: 0), reports and
+ * codes (NULL allowed) have one entry per member; returns the first member's non-zero code.
+ * Create every member before the call: mic_create's synchronous copies would disturb the
+ * members' graph captures. */
+int mic_subduction_timestep_many(mic_ctx *const *ctxs, int n, const mic_timestep_options *options,
+                                 const double *elapsed_time, mic_timestep_report *reports, int *codes,
+                                 int max_threads);
 
 /* ---- ensembles ----
  * No counterpart in the reference (one problem per run).  Independent problems, each a context

@@ -76,3 +76,41 @@ def test_timestep_stops_above_melting():
     got = G.markers
     for f in ("X", "Y", "T", "sxx", "eta"):
         assert np.array_equal(got[f], wl.markers[f]), f
+
+
+def _members(k_seeds=(4, 5, 6)):
+    from fvmic2d_gb300 import workloads as W
+
+    out = []
+    for k, seed in enumerate(k_seeds):
+        wl, topt = W.subduction_box(nx_cells=32, ny_cells=8, nm=4, seed=seed)
+        topt.sub.slabAngle = 0.7 + 0.05 * k  # members differ in geometry as well as markers
+        out.append((wl, topt))
+    return out
+
+
+def test_members_stepped_together_match_members_stepped_alone():
+    """mic_subduction_timestep_many steps independent Monte-Carlo members from host threads side
+    by side; each member's result is the one it gets stepped alone, bit for bit, over two steps"""
+    alone, together = [], []
+    for wl, topt in _members():
+        alone.append((gpu.MicProblem(wl), topt))
+        together.append(gpu.MicProblem(wl))
+    rep_alone = []
+    for step in range(2):
+        for P, topt in alone:
+            topt.firstStep = 1 if step == 0 else 0
+            rep_alone.append(P.subductionTimestep(topt, 0.0))
+    rep_many = []
+    topts = [t for _, t in alone]
+    for step in range(2):
+        for t in topts:
+            t.firstStep = 1 if step == 0 else 0
+        rep_many += gpu.subduction_timestep_many(together, topts)
+    assert rep_many == rep_alone
+    for (P, _), Q in zip(alone, together):
+        a, b = P.markers, Q.markers
+        for f in ("X", "Y", "T", "sxx", "syy", "sxy", "eta", "p", "Eii"):
+            assert np.array_equal(a[f], b[f]), f
+        for f in ("vx", "vy", "p", "thisT"):
+            assert np.array_equal(P.get_nodal(f), Q.get_nodal(f)), f
