@@ -16,7 +16,6 @@
 
 using namespace mic;
 
-int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out);
 
 namespace {
 

@@ -36,6 +36,27 @@ __global__ void k_temp_change(const double *__restrict__ thisT, const double *__
   if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
 }
 
+// adiabaticHeating (adiabaticHeating.c:24-43): each marker's alpha T VY rho gy, in the binned
+// column order (out-of-domain markers are in no cell and contribute nothing)
+__global__ void k_adiabatic_values(const int *__restrict__ cellX, const int *__restrict__ mat,
+                                   const double *__restrict__ T, const double *__restrict__ VY, mic_materials M,
+                                   double gy, int64_t n, double *v) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  if (cellX[m] == -1) {
+    v[m] = 0.0;
+    return;
+  }
+  const int mt = mat[m];
+  v[m] = M.materialAlpha[mt] * T[m] * VY[m] * M.materialRho[mt] * gy;
+}
+
+// VecAXPY(nodal_heating, 1.0, ha) (main_subduction.c:377)
+__global__ void k_add_heating(double *heat, const double *__restrict__ ha, int64_t nn) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < nn) heat[k] = heat[k] + 1.0 * ha[k];
+}
+
 int max_temp_change(mic_ctx *ctx, double *out) {
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
   constexpr int kParts = 64;
@@ -64,6 +85,27 @@ int thermal_solve(mic_ctx *ctx, const mic_timestep_options &o, double dt) {
 }
 
 }  // namespace
+
+extern "C" int mic_adiabatic_heating(mic_ctx *ctx, double gy) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int e = mic_ensure_sorted(ctx);
+  if (e) return e;
+  const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
+  if (ctx->n > 0) {
+    MIC_KERNEL(ctx, "k_adiabatic_values");
+    k_adiabatic_values<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
+                                                                     ctx->f64[C_VY], ctx->mat, gy, ctx->n, ctx->scr1);
+  }
+  // the markers' basic-node projection, weights (1 - mdx)(1 - mdy) etc., divided by their sum
+  if ((e = mic_project_scalar(ctx, ctx->scr1, 0, ctx->node_scr[5]))) return e;
+  {
+    MIC_KERNEL(ctx, "k_add_heating");
+    k_add_heating<<<grid_for(nn), kBlock, 0, ctx->stream>>>(ctx->nodal[MIC_NF_HEATING], ctx->node_scr[5], nn);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  return MIC_OK;
+}
 
 #define MIC_TRY(x)           \
   do {                       \
@@ -129,6 +171,7 @@ extern "C" int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options 
   if (!o->shearHeating)
     MIC_CUDA_TRY(cudaMemsetAsync(ctx->nodal[MIC_NF_HEATING], 0, sizeof(double) * ctx->P.NX * ctx->P.NY,
                                  ctx->stream));
+  if (o->adiabaticHeating) MIC_TRY(mic_adiabatic_heating(ctx, o->sub.gy));
   // main:379-403: thermal solve, repeated with a shorter step for a too large change
   MIC_TRY(thermal_solve(ctx, *o, dt));
   double dTmax = 0.0;

@@ -109,6 +109,7 @@ SIGNATURES = {
     "mic_solution_get": (_I, [_P, _I, _DP]),
     "mic_system_band": (_I, [_P, _I, _IP, _IP]),
     "mic_subduction_timestep": (_I, [_P, _P, _D, _P]),
+    "mic_adiabatic_heating": (_I, [_P, _D]),
     "mic_subduction_timestep_many": (_I, [_P, _I, _P, _DP, _P, _IP, _I]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
@@ -277,6 +278,10 @@ class MicProblem:
         out = np.zeros(3 * nn if which == self.STOKES else nn)
         self._check(self.L.mic_solution_get(self.h, which, _dp(out)), "mic_solution_get")
         return out
+
+    def adiabaticHeating(self, gy):
+        """adiabaticHeating (adiabaticHeating.c:7) added to the heating field (main:377)"""
+        self._check(self.L.mic_adiabatic_heating(self.h, gy), "mic_adiabatic_heating")
 
     def subductionTimestep(self, topt, elapsed_time=0.0):
         """one time step of main_subduction.c on the device; returns the report as a dict"""

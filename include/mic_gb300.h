@@ -300,9 +300,13 @@ int mic_system_band(mic_ctx *ctx, int which, int *kl, int *ku);
  * elapsed_time is the model time before the step (checkPlasticYielding's t); the caller adds
  * report->dt.  A step whose markers are above the reference's TBREAK (9999 K) stops after the
  * projection with report->stopped = 1, as main goes to the next Monte-Carlo run.  The
- * Options.staticVelocity and adiabaticHeating paths are not provided. */
+ * Options.staticVelocity path (reusing an earlier Stokes solution) is not provided. */
 int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options *options, double elapsed_time,
                             mic_timestep_report *report);
+/* adiabaticHeating (adiabaticHeating.c:7): every in-domain marker's alpha T VY rho gy projected to
+ * the basic nodes (weights (1 - mdx)(1 - mdy), ..., divided by their sum), added to
+ * MIC_NF_HEATING as main_subduction.c:377 adds it (VecAXPY(nodal_heating, 1.0, ha)) */
+int mic_adiabatic_heating(mic_ctx *ctx, double gy);
 /* No counterpart in the reference, whose main runs its Monte-Carlo realisations one after another
  * (iMonte): one mic_subduction_timestep on each of n independent contexts (each created with its
  * own stream), members on up to max_threads host threads at once (0: the host's core count), so

@@ -81,6 +81,7 @@ typedef struct {
   int32_t densityControl;        /* run checkMarkerDensity (main:250) with `density` */
   mic_density_options density;
   mic_subduction_options sub;
+  int32_t adiabaticHeating;      /* add adiabatic heating to the nodal heating (main:374-378) */
 } mic_timestep_options;
 
 /* What the step did. */

@@ -29,6 +29,7 @@
 #include "io.h"
 #include "restart.h"
 #include "vep_system.h"
+#include "adiabaticHeating.h"
 #include "thermalSystem.h"
 #include "mic_types.h"
 
@@ -120,12 +121,14 @@ refp *ref_create(int NX, int NY, double LX, double LY, const double *x, const do
   plite_DMDACreate(NX, NY, &p->grid.da);
   plite_DMDACreateDOF(NX, NY, 3, &p->grid.vda);
   for (int id = 0; id < MIC_NF_COUNT; ++id) DMCreateGlobalVector(p->grid.da, field_vec(p, id));
+  DMCreateGlobalVector(p->grid.da, &p->nf.ha);
   return p;
 }
 
 void ref_destroy(refp *p) {
   if (!p) return;
   for (int id = 0; id < MIC_NF_COUNT; ++id) VecDestroy(field_vec(p, id));
+  VecDestroy(&p->nf.ha);
   plite_DMDestroy(&p->grid.da);
   plite_DMDestroy(&p->grid.vda);
   free(p->gbuf);
@@ -493,4 +496,13 @@ void ref_system_get(int which, int *rowptr, int *cols, double *vals, double *rhs
   memcpy(cols, s->cols, sizeof(int) * (size_t)s->nnz);
   memcpy(vals, s->vals, sizeof(double) * (size_t)s->nnz);
   memcpy(rhs, s->rhs, sizeof(double) * (size_t)s->n);
+}
+
+/* adiabaticHeating (adiabaticHeating.c:7) with gy, then main's VecAXPY(nodal_heating, 1.0, ha)
+ * (main_subduction.c:377) */
+int ref_adiabaticHeating(refp *p, double gy) {
+  p->opt.gy = gy;
+  int e = adiabaticHeating(&p->grid, &p->ms, &p->nf, &p->mat, &p->opt);
+  if (!e) e = VecAXPY(p->heat, 1.0, p->nf.ha);
+  return e;
 }

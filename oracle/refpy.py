@@ -69,6 +69,7 @@ def lib():
             "ref_limitDisplacementTimestep": (_D, [_P, _D, _D]),
             "ref_retrieveSolutions": (_I, [_P, _DP, _D]),
             "ref_formVEPSystem": (_I, [_P, _P, _D, _DP, _DP]),
+            "ref_adiabaticHeating": (_I, [_P, _D]),
             "ref_enforceThermalBCs1": (_I, [_P, _P]),
             "ref_formThermalSystem": (_I, [_P, _P, _D, _I]),
             "ref_system_nnz": (ctypes.c_long, [_I, ctypes.POINTER(ctypes.c_long)]),
@@ -161,6 +162,12 @@ class RefProblem:
         if e:
             raise RuntimeError("formVEPSystem failed: %d" % e)
         return self._system(0) + (kb.value, kc.value)
+
+    def adiabaticHeating(self, gy):
+        """adiabaticHeating (adiabaticHeating.c:7) added to the heating field as main adds it"""
+        e = lib().ref_adiabaticHeating(self.h, gy)
+        if e:
+            raise RuntimeError("adiabaticHeating failed: %d" % e)
 
     def enforceThermalBCs1(self, sopt):
         e = lib().ref_enforceThermalBCs1(self.h, ctypes.byref(sopt))

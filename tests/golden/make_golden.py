@@ -267,6 +267,10 @@ def timestep_table():
     cases = [("", wl, topt, None)]
     wl2, topt2, cap2 = timestep_density_case()
     cases.append(("dens_", wl2, topt2, cap2))
+    from tests.timestep_case import timestep_adiabatic_case
+
+    wl3, topt3 = timestep_adiabatic_case()
+    cases.append(("adiab_", wl3, topt3, None))
     for pre, w, t, cap in cases:
         before = np.array(w.markers, copy=True)
         mk, rep, nodal = reference_timestep(w, t, elapsed=0.0, capacity=cap)
@@ -277,6 +281,19 @@ def timestep_table():
         for k, v in nodal.items():
             out[pre + "nodal_" + k] = v
     return out
+
+
+def adiabatic_table():
+    """adiabaticHeating of the reference plus main's addition to the heating field"""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from tests.test_oracle_pin import adiabatic_case
+
+    wl, gy = adiabatic_case()
+    R = refpy.RefProblem(wl)
+    R.findMarkerCells()
+    R.adiabaticHeating(gy)
+    return {"before": np.array(wl.markers, copy=True).view(np.uint8), "heat_in": wl.nodal["heating"],
+            "heat_out": R.get_nodal("heating")}
 
 
 def checkpoint_case():
@@ -328,6 +345,9 @@ def main():
     if sys.argv[1:] in ([], ["timestep"]):
         np.savez_compressed(os.path.join(OUT, "subduction_step.npz"), **timestep_table())
         print("wrote subduction_step")
+    if sys.argv[1:] in ([], ["adiabatic"]):
+        np.savez_compressed(os.path.join(OUT, "adiabatic_heating.npz"), **adiabatic_table())
+        print("wrote adiabatic_heating")
     if sys.argv[1:] in ([], ["systems"]):
         np.savez_compressed(os.path.join(OUT, "linear_systems.npz"), **systems_table())
         print("wrote linear_systems")

@@ -10,7 +10,7 @@ import pytest
 
 from fvmic2d_gb300 import gpu
 from fvmic2d_gb300.mic_types import MARKER_DTYPE
-from tests.timestep_case import timestep_case, timestep_density_case
+from tests.timestep_case import timestep_adiabatic_case, timestep_case, timestep_density_case
 
 pytestmark = pytest.mark.gpu
 
@@ -28,17 +28,20 @@ def _fields(m):
 
 
 @pytest.mark.parametrize("build", ["exact", "product"])
-@pytest.mark.parametrize("case", ["plain", "density"])
+@pytest.mark.parametrize("case", ["plain", "density", "adiabatic"])
 def test_timestep_matches_reference(build, case):
     """plain: no density control; density: checkMarkerDensity inside the step fills an emptied
-    block of the wedge and the first cell column (subduction-inflow markers) before the solves"""
+    block of the wedge and the first cell column (subduction-inflow markers) before the solves;
+    adiabatic: adiabatic heating added to the shear heating before the thermal solve"""
     z = np.load(os.path.join(GOLDEN, "subduction_step.npz"))
-    pre = "" if case == "plain" else "dens_"
+    pre = {"plain": "", "density": "dens_", "adiabatic": "adiab_"}[case]
+    cap = None
     if case == "plain":
         wl, topt = timestep_case()
-        cap = None
-    else:
+    elif case == "density":
         wl, topt, cap = timestep_density_case()
+    else:
+        wl, topt = timestep_adiabatic_case()
     wl.markers = z[pre + "before"].view(MARKER_DTYPE).copy()
     ref = z[pre + "after"].view(MARKER_DTYPE)
     G = gpu.MicProblem(wl, exact=(build == "exact"), capacity=cap)
@@ -114,3 +117,20 @@ def test_members_stepped_together_match_members_stepped_alone():
             assert np.array_equal(a[f], b[f]), f
         for f in ("vx", "vy", "p", "thisT"):
             assert np.array_equal(P.get_nodal(f), Q.get_nodal(f)), f
+
+
+@pytest.mark.parametrize("build", ["exact", "product"])
+def test_adiabatic_heating_matches_reference(build):
+    """adiabaticHeating (adiabaticHeating.c:7) plus main's addition to the heating field: the
+    projection sums in another order than the reference's marker loop (and multiplies the weight
+    factors in another order), so the added heating agrees to 1e-12 of its largest value"""
+    from tests.test_oracle_pin import adiabatic_case
+
+    z = np.load(os.path.join(GOLDEN, "adiabatic_heating.npz"))
+    wl, gy = adiabatic_case()
+    wl.markers = z["before"].view(MARKER_DTYPE).copy()
+    wl.nodal["heating"] = z["heat_in"]
+    G = gpu.MicProblem(wl, exact=(build == "exact"))
+    G.adiabaticHeating(gy)
+    added, ref = G.get_nodal("heating") - z["heat_in"], z["heat_out"] - z["heat_in"]
+    assert np.max(np.abs(added - ref)) <= 1e-12 * np.max(np.abs(ref))

@@ -464,6 +464,30 @@ def test_systems_golden_are_consistent():
                 assert d[0] > 0 and np.all(off <= 0) and d[0] >= -off.sum()
 
 
+def adiabatic_case(seed=12):
+    """adiabaticHeating's inputs: the refined box with a random vertical marker velocity
+    (markers' VY, as the last advection left it) and a random heating field to add to"""
+    wl = W.vep_slab_box(nx_cells=24, ny_cells=10, nm=4, seed=seed)
+    g, m = wl.grid, wl.markers
+    u = W.splitmix64_uniform(seed + 5, len(m) + g.NX * g.NY)
+    m["VY"] = (u[:len(m)] - 0.5) * 2e-9
+    m["X"][::97] = -1.0  # some markers out of the domain: they contribute nothing
+    wl.nodal["heating"] = (u[len(m):].reshape(g.NY, g.NX) - 0.5) * 1e-6
+    return wl, 10.0
+
+
+@needs_ref
+def test_adiabatic_heating_reference_build_matches_golden():
+    z = np.load(os.path.join(GOLDEN, "adiabatic_heating.npz"))
+    wl, gy = adiabatic_case()
+    wl.markers = z["before"].view(MARKER_DTYPE).copy()
+    wl.nodal["heating"] = z["heat_in"]
+    R = refpy.RefProblem(wl)
+    R.findMarkerCells()
+    R.adiabaticHeating(gy)
+    assert np.array_equal(R.get_nodal("heating"), z["heat_out"])
+
+
 def test_checkpoint_matches_golden(tmp_path):
     """the reference's marker file format, byte for byte, and the restart from it"""
     z = np.load(os.path.join(GOLDEN, "marker_checkpoint.npz"))

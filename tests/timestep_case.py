@@ -44,6 +44,16 @@ def timestep_density_case(seed=6):
     return wl, topt, len(m) + 4096
 
 
+def timestep_adiabatic_case(seed=7):
+    """the box with adiabatic heating on (main_subduction.c:374-378) and the markers moving
+    vertically, as a previous advection would have left them"""
+    wl, topt = timestep_case(seed=seed)
+    m = wl.markers
+    m["VY"] = (W.splitmix64_uniform(seed + 50, len(m)) - 0.5) * 2e-9
+    topt.adiabaticHeating = 1
+    return wl, topt
+
+
 def _spsolve(rp, c, v, rhs):
     import scipy.sparse as sp
     import scipy.sparse.linalg as spl
@@ -97,6 +107,8 @@ def reference_timestep(wl, topt, elapsed=0.0, capacity=None):
         R.updateMarkerStress()
         if not topt.shearHeating:
             R.set_nodal("heating", np.zeros((R.NY, R.NX)))
+        if topt.adiabaticHeating:
+            R.adiabaticHeating(so.gy)
 
         def thermal(dt):
             R.enforceThermalBCs1(so)
