@@ -145,8 +145,13 @@ extern "C" int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options 
     MIC_TRY(mic_check_plastic_yielding(ctx, displacementdt, &isYielding, elapsed_time));
     MIC_TRY(mic_limit_viscosity(ctx));
     MIC_TRY(mic_project_markers_nodes_all2(ctx));
-    MIC_TRY(mic_form_vep_system(ctx, &o->sub, displacementdt, &rep->Kbond, &rep->Kcont));
-    MIC_TRY(mic_linear_solve(ctx, 0));
+    if (!o->staticVelocity || !ctx->sys[0].factored || !ctx->solution) {
+      MIC_TRY(mic_form_vep_system(ctx, &o->sub, displacementdt, &rep->Kbond, &rep->Kcont));
+      MIC_TRY(mic_linear_solve(ctx, 0));
+    } else {  // main:315-317: the steady solution again, with the Kcont of its assembly
+      rep->Kbond = ctx->sys[0].Kbond;
+      rep->Kcont = ctx->sys[0].Kcont;
+    }
     int fn = 0;
     MIC_TRY(mic_retrieve_solutions(ctx, nullptr, rep->Kcont, &fn));
     if (fn) return MIC_ERR_NAN;

@@ -135,7 +135,8 @@ class TimestepOptions(ctypes.Structure):
     _fields_ = [("dtMax", ctypes.c_double), ("displacementStepLimit", ctypes.c_double),
                 ("maxTempChange", ctypes.c_double), ("maxNumPlasticity", ctypes.c_int32),
                 ("shearHeating", ctypes.c_int32), ("firstStep", ctypes.c_int32), ("densityControl", ctypes.c_int32),
-                ("density", DensityOptions), ("sub", SubductionOptions), ("adiabaticHeating", ctypes.c_int32)]
+                ("density", DensityOptions), ("sub", SubductionOptions), ("adiabaticHeating", ctypes.c_int32),
+                ("staticVelocity", ctypes.c_int32)]
 
 
 class TimestepReport(ctypes.Structure):

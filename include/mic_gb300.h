@@ -299,8 +299,9 @@ int mic_system_band(mic_ctx *ctx, int which, int *kl, int *ku);
  * largest nodal change exceeds maxTempChange), subgridTemperatureChanges and advectMarkersRK.
  * elapsed_time is the model time before the step (checkPlasticYielding's t); the caller adds
  * report->dt.  A step whose markers are above the reference's TBREAK (9999 K) stops after the
- * projection with report->stopped = 1, as main goes to the next Monte-Carlo run.  The
- * Options.staticVelocity path (reusing an earlier Stokes solution) is not provided. */
+ * projection with report->stopped = 1, as main goes to the next Monte-Carlo run.  With
+ * options->staticVelocity the Stokes system is assembled and solved once per context (the run's
+ * first step, main:306-318) and its solution reused afterwards. */
 int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options *options, double elapsed_time,
                             mic_timestep_report *report);
 /* adiabaticHeating (adiabaticHeating.c:7): every in-domain marker's alpha T VY rho gy projected to

@@ -82,6 +82,7 @@ typedef struct {
   mic_density_options density;
   mic_subduction_options sub;
   int32_t adiabaticHeating;      /* add adiabatic heating to the nodal heating (main:374-378) */
+  int32_t staticVelocity;        /* reuse the run's first Stokes solution (main:306-318) */
 } mic_timestep_options;
 
 /* What the step did. */

@@ -134,3 +134,32 @@ def test_adiabatic_heating_matches_reference(build):
     G.adiabaticHeating(gy)
     added, ref = G.get_nodal("heating") - z["heat_in"], z["heat_out"] - z["heat_in"]
     assert np.max(np.abs(added - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_static_velocity_reuses_the_first_solution():
+    """Options.staticVelocity (main_subduction.c:306-318): the run's first step solves the Stokes
+    system; later steps reuse that solution (same velocities, same Kcont) while the markers still
+    go through their plasticity iterations and move"""
+    wl, topt = timestep_case()
+    topt.staticVelocity = 1
+    G = gpu.MicProblem(wl)
+    r1 = G.subductionTimestep(topt, 0.0)
+    v1 = {f: G.get_nodal(f) for f in ("vx", "vy", "p")}
+    x1 = G.markers["X"].copy()
+    l0 = G.launch_count()
+    topt.firstStep = 0
+    r2 = G.subductionTimestep(topt, r1["dt"])
+    for f in ("vx", "vy", "p"):
+        assert np.array_equal(G.get_nodal(f), v1[f]), f
+    assert (r2["Kbond"], r2["Kcont"]) == (r1["Kbond"], r1["Kcont"])
+    assert r2["plastic_iterations"] >= 1
+    assert not np.array_equal(G.markers["X"], x1)
+    l_static = G.launch_count() - l0
+    # the same two steps without staticVelocity: the second step solves again, with more launches
+    wl2, topt2 = timestep_case()
+    H = gpu.MicProblem(wl2)
+    H.subductionTimestep(topt2, 0.0)
+    topt2.firstStep = 0
+    l1 = H.launch_count()
+    H.subductionTimestep(topt2, r1["dt"])
+    assert l_static < H.launch_count() - l1
