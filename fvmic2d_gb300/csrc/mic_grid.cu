@@ -275,3 +275,88 @@ extern "C" int mic_retrieve_solutions(mic_ctx *ctx, const double *S, double Kcon
   if (foundnan) *foundnan = 0;  // the reference checks for NaN only in its TEXTURE build
   return MIC_OK;
 }
+
+// ---- diagnostics of main's time loop (post.c) -------------------------------------------------
+
+namespace {
+
+// nusseltNumber (post.c:5-46): the surface heat flux integral, summed in the reference's order by
+// one thread (NX - 1 terms), every operation an IEEE intrinsic
+__global__ void k_nusselt(Params P, const double *__restrict__ T, double dTbc, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int NX = P.NX;
+  const double dz = S(P.y[1], P.y[0]);
+  double integrand = 0.0;
+  for (int ix = 0; ix < NX - 1; ++ix) {
+    const double dT = D(S(A(S(T[NX + ix], T[ix]), T[NX + ix + 1]), T[ix + 1]), 2.0);
+    const double dx = S(P.x[ix + 1], P.x[ix]);
+    integrand = A(integrand, M(D(dT, dz), dx));
+  }
+  out[0] = M(D(D(P.LY, P.LX), dTbc), integrand);
+}
+
+// rmsVelocity (post.c:49-92): one term per cell, summed by a fixed tree (the reference sums the
+// cells in order; the two agree to rounding)
+__global__ void k_vrms_partial(Params P, const double *__restrict__ vx, const double *__restrict__ vy,
+                               double *part) {
+  __shared__ double sm[256];
+  const int NX = P.NX, nc = (P.NX - 1) * (P.NY - 1);
+  double acc = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const int ix = c % (NX - 1), jy = c / (NX - 1);
+    const int64_t k = (int64_t)jy * NX + ix;
+    const double dx = S(P.x[ix + 1], P.x[ix]), dy = S(P.y[jy + 1], P.y[jy]);
+    const double vx2 = D(A(M(vx[k], vx[k]), M(vx[k + 1], vx[k + 1])), 2.0);
+    const double vy2 = D(A(M(vy[k], vy[k]), M(vy[k + NX], vy[k + NX])), 2.0);
+    acc = A(acc, M(M(A(vx2, vy2), dx), dy));
+  }
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] = A(sm[threadIdx.x], sm[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+__global__ void k_vrms_final(Params P, const double *__restrict__ part, int nparts, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s = A(s, part[b]);
+  out[0] = __dsqrt_rn(D(s, M(P.LX, P.LY)));
+}
+
+}  // namespace
+
+extern "C" int mic_nusselt_number(mic_ctx *ctx, double bottom_T, double top_T, double *Nu) {
+  if (!ctx || !Nu) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  double *d = ctx->red_buf + 40;
+  {
+    MIC_KERNEL(ctx, "k_nusselt");
+    k_nusselt<<<1, 32, 0, ctx->stream>>>(ctx->P, ctx->nodal[MIC_NF_THIST], bottom_T - top_T, d);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  MIC_CUDA_TRY(cudaMemcpyAsync(Nu, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_rms_velocity(mic_ctx *ctx, double *vrms) {
+  if (!ctx || !vrms) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  constexpr int kParts = 64;
+  double *part = ctx->red_buf + 64, *d = ctx->red_buf + 41;
+  {
+    MIC_KERNEL(ctx, "k_vrms_partial");
+    k_vrms_partial<<<kParts, 256, 0, ctx->stream>>>(ctx->P, ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], part);
+  }
+  {
+    MIC_KERNEL(ctx, "k_vrms_final");
+    k_vrms_final<<<1, 32, 0, ctx->stream>>>(ctx->P, part, kParts, d);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  MIC_CUDA_TRY(cudaMemcpyAsync(vrms, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}

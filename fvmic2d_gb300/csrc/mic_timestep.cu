@@ -189,8 +189,11 @@ extern "C" int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options 
   }
   rep->max_temp_change = dTmax;
   rep->dt = dt;
-  // main:409, 435: sub-grid temperature changes with the new temperature, advection
+  // main:409, 435: sub-grid temperature changes with the new temperature, the diagnostics,
+  // advection
   MIC_TRY(mic_subgrid_temperature_changes(ctx, dt));
+  MIC_TRY(mic_nusselt_number(ctx, o->thermalBCBottomValue, o->sub.thermalBCTopValue, &rep->nusselt));
+  MIC_TRY(mic_rms_velocity(ctx, &rep->vrms));
   MIC_TRY(mic_advect_markers_rk(ctx, dt));
   MIC_TRY(mic_max_abs_sxx(ctx, &rep->max_abs_sxx));
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

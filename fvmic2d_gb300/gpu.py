@@ -110,6 +110,8 @@ SIGNATURES = {
     "mic_system_band": (_I, [_P, _I, _IP, _IP]),
     "mic_subduction_timestep": (_I, [_P, _P, _D, _P]),
     "mic_adiabatic_heating": (_I, [_P, _D]),
+    "mic_nusselt_number": (_I, [_P, _D, _D, _DP]),
+    "mic_rms_velocity": (_I, [_P, _DP]),
     "mic_subduction_timestep_many": (_I, [_P, _I, _P, _DP, _P, _IP, _I]),
     "mic_host_alloc": (_I, [ctypes.POINTER(_P), _I64]),
     "mic_host_free": (_I, [_P]),
@@ -282,6 +284,16 @@ class MicProblem:
     def adiabaticHeating(self, gy):
         """adiabaticHeating (adiabaticHeating.c:7) added to the heating field (main:377)"""
         self._check(self.L.mic_adiabatic_heating(self.h, gy), "mic_adiabatic_heating")
+
+    def nusseltNumber(self, bottom_T, top_T):
+        v = ctypes.c_double(0.0)
+        self._check(self.L.mic_nusselt_number(self.h, bottom_T, top_T, ctypes.byref(v)), "mic_nusselt_number")
+        return v.value
+
+    def rmsVelocity(self):
+        v = ctypes.c_double(0.0)
+        self._check(self.L.mic_rms_velocity(self.h, ctypes.byref(v)), "mic_rms_velocity")
+        return v.value
 
     def subductionTimestep(self, topt, elapsed_time=0.0):
         """one time step of main_subduction.c on the device; returns the report as a dict"""

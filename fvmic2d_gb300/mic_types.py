@@ -136,7 +136,7 @@ class TimestepOptions(ctypes.Structure):
                 ("maxTempChange", ctypes.c_double), ("maxNumPlasticity", ctypes.c_int32),
                 ("shearHeating", ctypes.c_int32), ("firstStep", ctypes.c_int32), ("densityControl", ctypes.c_int32),
                 ("density", DensityOptions), ("sub", SubductionOptions), ("adiabaticHeating", ctypes.c_int32),
-                ("staticVelocity", ctypes.c_int32)]
+                ("staticVelocity", ctypes.c_int32), ("thermalBCBottomValue", ctypes.c_double)]
 
 
 class TimestepReport(ctypes.Structure):
@@ -145,7 +145,8 @@ class TimestepReport(ctypes.Structure):
                 ("max_temp_change", ctypes.c_double), ("max_abs_sxx", ctypes.c_double),
                 ("plastic_iterations", ctypes.c_int32), ("is_yielding", ctypes.c_int32),
                 ("converged", ctypes.c_int32), ("thermal_resolves", ctypes.c_int32), ("stopped", ctypes.c_int32),
-                ("markers_added", ctypes.c_int64), ("markers_removed", ctypes.c_int64)]
+                ("markers_added", ctypes.c_int64), ("markers_removed", ctypes.c_int64),
+                ("nusselt", ctypes.c_double), ("vrms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

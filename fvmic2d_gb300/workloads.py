@@ -550,7 +550,8 @@ def subduction_box(nx_cells=128, ny_cells=32, nm=4, seed=4):
                            rootWidth=0.2 * g.LX, thermalBCTopType=0, thermalBCTopValue=273.0)
     topt = TimestepOptions(dtMax=3.0e11, displacementStepLimit=0.5, maxTempChange=50.0, maxNumPlasticity=4,
                            shearHeating=1, firstStep=1, densityControl=0,
-                           density=DensityOptions(NMX=nm, NMY=nm, minMarkers=1, maxMarkers=100), sub=so)
+                           density=DensityOptions(NMX=nm, NMY=nm, minMarkers=1, maxMarkers=100), sub=so,
+                           thermalBCBottomValue=1573.0)
     return wl, topt
 
 

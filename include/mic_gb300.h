@@ -308,6 +308,12 @@ int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options *options, d
  * the basic nodes (weights (1 - mdx)(1 - mdy), ..., divided by their sum), added to
  * MIC_NF_HEATING as main_subduction.c:377 adds it (VecAXPY(nodal_heating, 1.0, ha)) */
 int mic_adiabatic_heating(mic_ctx *ctx, double gy);
+/* main's per-step diagnostics (main_subduction.c:413-416): nusseltNumber (post.c:5) of the new
+ * temperature MIC_NF_THIST with the boundary temperatures (thermalBCBottom.value[0],
+ * thermalBCTop.value[0]), bit-identical; rmsVelocity (post.c:49) of the nodal vx, vy, summed by a
+ * fixed tree instead of the reference's cell order (rounding differences only) */
+int mic_nusselt_number(mic_ctx *ctx, double bottom_T, double top_T, double *Nu);
+int mic_rms_velocity(mic_ctx *ctx, double *vrms);
 /* No counterpart in the reference, whose main runs its Monte-Carlo realisations one after another
  * (iMonte): one mic_subduction_timestep on each of n independent contexts (each created with its
  * own stream), members on up to max_threads host threads at once (0: the host's core count), so

@@ -83,6 +83,7 @@ typedef struct {
   mic_subduction_options sub;
   int32_t adiabaticHeating;      /* add adiabatic heating to the nodal heating (main:374-378) */
   int32_t staticVelocity;        /* reuse the run's first Stokes solution (main:306-318) */
+  double thermalBCBottomValue;   /* thermalBCBottom.value[0], for the Nusselt number (post.c:10) */
 } mic_timestep_options;
 
 /* What the step did. */
@@ -97,6 +98,7 @@ typedef struct {
   int32_t plastic_iterations, is_yielding, converged, thermal_resolves;
   int32_t stopped;          /* 1: max_T above 9999 (TBREAK), nothing after the projection ran */
   int64_t markers_added, markers_removed;
+  double nusselt, vrms;     /* main's diagnostics after the thermal solve (post.c) */
 } mic_timestep_report;
 
 /* Material table; same layout as fdcode.h:74-95. */

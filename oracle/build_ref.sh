@@ -22,7 +22,7 @@ INC="-I$HERE/petsc_lite/include -I$REF -I$HERE/../include"
 SRCS="markers.c markerProjection.c updateMarkerStrainPressure.c subgridStressChanges.c updateMarkerStress.c \
 subgridTemperatureChanges.c viscosity.c residual.c benchmarkInitialConditions.c gridSpacing.c profile.c \
 nodalStressStrain.c limitTimestep.c retrieveSolutions.c io.c restart.c vep_system.c formThermalSystem.c \
-enforceThermalBC.c adiabaticHeating.c"
+enforceThermalBC.c adiabaticHeating.c post.c"
 OBJS=""
 for s in $SRCS; do
   o="$OUT/$(basename "$s" .c).o"

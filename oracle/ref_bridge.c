@@ -30,6 +30,7 @@
 #include "restart.h"
 #include "vep_system.h"
 #include "adiabaticHeating.h"
+#include "post.h"
 #include "thermalSystem.h"
 #include "mic_types.h"
 
@@ -505,4 +506,20 @@ int ref_adiabaticHeating(refp *p, double gy) {
   int e = adiabaticHeating(&p->grid, &p->ms, &p->nf, &p->mat, &p->opt);
   if (!e) e = VecAXPY(p->heat, 1.0, p->nf.ha);
   return e;
+}
+
+/* nusseltNumber (post.c:5) of thisT with the bottom and top boundary temperatures */
+double ref_nusseltNumber(refp *p, double bottom, double top) {
+  p->opt.thermalBCBottom.value[0] = bottom;
+  p->opt.thermalBCTop.value[0] = top;
+  PetscScalar Nu = 0.0;
+  nusseltNumber(&p->grid, &p->opt, p->thisT, &Nu);
+  return Nu;
+}
+
+/* rmsVelocity (post.c:49) of the nodal vx, vy */
+double ref_rmsVelocity(refp *p) {
+  PetscScalar v = 0.0;
+  rmsVelocity(&p->grid, &p->nf, &v);
+  return v;
 }

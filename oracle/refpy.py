@@ -70,6 +70,8 @@ def lib():
             "ref_retrieveSolutions": (_I, [_P, _DP, _D]),
             "ref_formVEPSystem": (_I, [_P, _P, _D, _DP, _DP]),
             "ref_adiabaticHeating": (_I, [_P, _D]),
+            "ref_nusseltNumber": (_D, [_P, _D, _D]),
+            "ref_rmsVelocity": (_D, [_P]),
             "ref_enforceThermalBCs1": (_I, [_P, _P]),
             "ref_formThermalSystem": (_I, [_P, _P, _D, _I]),
             "ref_system_nnz": (ctypes.c_long, [_I, ctypes.POINTER(ctypes.c_long)]),
@@ -168,6 +170,12 @@ class RefProblem:
         e = lib().ref_adiabaticHeating(self.h, gy)
         if e:
             raise RuntimeError("adiabaticHeating failed: %d" % e)
+
+    def nusseltNumber(self, bottom, top):
+        return lib().ref_nusseltNumber(self.h, bottom, top)
+
+    def rmsVelocity(self):
+        return lib().ref_rmsVelocity(self.h)
 
     def enforceThermalBCs1(self, sopt):
         e = lib().ref_enforceThermalBCs1(self.h, ctypes.byref(sopt))

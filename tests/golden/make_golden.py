@@ -296,6 +296,19 @@ def adiabatic_table():
             "heat_out": R.get_nodal("heating")}
 
 
+def diagnostics_table():
+    """nusseltNumber and rmsVelocity (post.c) of the reference on the diagnostics case"""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from tests.test_oracle_pin import diagnostics_case
+
+    wl, bottom, top = diagnostics_case()
+    R = refpy.RefProblem(wl)
+    out = {"in_" + f: np.asarray(wl.nodal[f], dtype=np.float64) for f in ("thisT", "vx", "vy")}
+    out["nusselt"] = np.array(R.nusseltNumber(bottom, top))
+    out["vrms"] = np.array(R.rmsVelocity())
+    return out
+
+
 def checkpoint_case():
     """the VEP box after a step, with some markers pushed out of the domain"""
     wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2)
@@ -345,6 +358,9 @@ def main():
     if sys.argv[1:] in ([], ["timestep"]):
         np.savez_compressed(os.path.join(OUT, "subduction_step.npz"), **timestep_table())
         print("wrote subduction_step")
+    if sys.argv[1:] in ([], ["diagnostics"]):
+        np.savez_compressed(os.path.join(OUT, "post_diagnostics.npz"), **diagnostics_table())
+        print("wrote post_diagnostics")
     if sys.argv[1:] in ([], ["adiabatic"]):
         np.savez_compressed(os.path.join(OUT, "adiabatic_heating.npz"), **adiabatic_table())
         print("wrote adiabatic_heating")

@@ -50,7 +50,8 @@ def test_timestep_matches_reference(build, case):
     assert rep["markers_added"] == int(z[pre + "rep_markers_added"])
     for k in ("plastic_iterations", "is_yielding", "converged", "thermal_resolves"):
         assert rep[k] == int(z[pre + "rep_" + k]), k
-    for k in ("dt", "displacement_dt", "Kbond", "Kcont", "max_T", "max_temp_change", "max_abs_sxx"):
+    for k in ("dt", "displacement_dt", "Kbond", "Kcont", "max_T", "max_temp_change", "max_abs_sxx", "nusselt",
+              "vrms"):
         ref_v = float(z[pre + "rep_" + k])
         assert abs(rep[k] - ref_v) <= 1e-9 * abs(ref_v), (k, rep[k], ref_v)
     got = G.markers
@@ -163,3 +164,18 @@ def test_static_velocity_reuses_the_first_solution():
     l1 = H.launch_count()
     H.subductionTimestep(topt2, r1["dt"])
     assert l_static < H.launch_count() - l1
+
+
+def test_diagnostics_match_reference():
+    """nusseltNumber (bit-identical: one thread sums in the reference's order) and rmsVelocity
+    (a tree sum of the same terms: rounding only) against the reference's post.c"""
+    from tests.test_oracle_pin import diagnostics_case
+
+    z = np.load(os.path.join(GOLDEN, "post_diagnostics.npz"))
+    wl, bottom, top = diagnostics_case()
+    for f in ("thisT", "vx", "vy"):
+        wl.nodal[f] = z["in_" + f]
+    G = gpu.MicProblem(wl)
+    assert G.nusseltNumber(bottom, top) == float(z["nusselt"])
+    v = float(z["vrms"])
+    assert abs(G.rmsVelocity() - v) <= 1e-14 * v

@@ -488,6 +488,27 @@ def test_adiabatic_heating_reference_build_matches_golden():
     assert np.array_equal(R.get_nodal("heating"), z["heat_out"])
 
 
+def diagnostics_case(seed=13):
+    """post.c's inputs: the refined box with random nodal temperature (the new one, thisT) and
+    velocities; bottom and top boundary temperatures"""
+    wl = W.vep_slab_box(nx_cells=24, ny_cells=10, nm=2, seed=seed)
+    g = wl.grid
+    u = W.splitmix64_uniform(seed + 9, 3 * g.NX * g.NY).reshape(3, g.NY, g.NX)
+    wl.nodal.update({"thisT": 273.0 + 1300.0 * u[0], "vx": (u[1] - 0.5) * 1e-9, "vy": (u[2] - 0.5) * 1e-9})
+    return wl, 1573.0, 273.0
+
+
+@needs_ref
+def test_diagnostics_reference_build_matches_golden():
+    z = np.load(os.path.join(GOLDEN, "post_diagnostics.npz"))
+    wl, bottom, top = diagnostics_case()
+    for f in ("thisT", "vx", "vy"):
+        wl.nodal[f] = z["in_" + f]
+    R = refpy.RefProblem(wl)
+    assert R.nusseltNumber(bottom, top) == float(z["nusselt"])
+    assert R.rmsVelocity() == float(z["vrms"])
+
+
 def test_checkpoint_matches_golden(tmp_path):
     """the reference's marker file format, byte for byte, and the restart from it"""
     z = np.load(os.path.join(GOLDEN, "marker_checkpoint.npz"))

@@ -23,7 +23,8 @@ def timestep_case(seed=4):
     so.rootThickness = 0.05 * g.LY
     topt = TimestepOptions(dtMax=3.0e11, displacementStepLimit=0.5, maxTempChange=50.0, maxNumPlasticity=4,
                            shearHeating=1, firstStep=1, densityControl=0,
-                           density=DensityOptions(NMX=4, NMY=4, minMarkers=1, maxMarkers=100), sub=so)
+                           density=DensityOptions(NMX=4, NMY=4, minMarkers=1, maxMarkers=100), sub=so,
+                           thermalBCBottomValue=1573.0)
     return wl, topt
 
 
@@ -125,6 +126,8 @@ def reference_timestep(wl, topt, elapsed=0.0, capacity=None):
             rep["thermal_resolves"] = 1
         rep.update(dt=dt, max_temp_change=dTmax)
         R.subgridTemperatureChanges(dt)
+        rep["nusselt"] = R.nusseltNumber(topt.thermalBCBottomValue, so.thermalBCTopValue)
+        rep["vrms"] = R.rmsVelocity()
         R.advectMarkersRK(dt)
         rep["max_abs_sxx"] = R.maxAbsSxx()
         nodal = {f: R.get_nodal(f) for f in ("vx", "vy", "p", "thisT", "lastT", "etaS", "etaN", "heating")}
