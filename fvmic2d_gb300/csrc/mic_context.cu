@@ -387,6 +387,12 @@ extern "C" int mic_set_options(mic_ctx *ctx, const mic_options *o) {
   return MIC_OK;
 }
 
+extern "C" int mic_get_bcs(mic_ctx *ctx, mic_bcs *bcs) {
+  if (!ctx || !bcs) return MIC_ERR_ARG;
+  *bcs = ctx->bcs;
+  return MIC_OK;
+}
+
 extern "C" int mic_set_bcs(mic_ctx *ctx, const mic_bcs *b) {
   if (!ctx || !b) return MIC_ERR_ARG;
   if (b->mechBCTop.type[0] != 0 && b->mechBCTop.type[0] != 1) return MIC_ERR_BC;

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "mic_internal.cuh"
+#include "mic_rheology.cuh"
 
 using namespace mic;
 
@@ -504,7 +505,81 @@ int ensure_system(mic_ctx *ctx, int which, int64_t n) {
 
 Rows rows_of(const mic_system_store &S) { return Rows{S.cnt, S.col, S.val, S.rhs}; }
 
+// initialConditionsVanKeken (benchmarkInitialConditions.c:8-33) for one marker: temperature by
+// region (slab: the half-space cooling profile; overriding plate: the linear geotherm; wedge:
+// mantle temperature), material 0, density anomaly, viscosity and shear modulus
+__global__ void k_van_keken(mic_materials M, mic_options O, CreepConfig cfg, double tanA, double slabAge,
+                            double plate, double rootT, double rootC, double rootW, double *X, double *Y, double *T,
+                            double *rho, double *rhodot, double *eta, double *mu, int *mat, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const double x = X[m], y = Y[m];
+  const double sd = x * tanA;  // slab_depth
+  double pd = plate;           // plate_depth
+  if (fabs(x - rootC) < rootW) {
+    const double c = cos(M_PI * (x - rootC) / rootW / 2.0);
+    pd = plate + rootT * (c * c);
+  }
+  double t;
+  if (y >= sd) {
+    const double slab_age_s = slabAge * 1.0e6 * 3.15576e7;
+    t = 273.0 + (1623.0 - 273.0) * erf((y - sd) / (2.0 * sqrt(0.7272e-6 * slab_age_s)));
+  } else if (y <= pd) {
+    t = y / pd * (1573.0 - 273.0) + 273.0;
+  } else {
+    t = 1573.0;
+  }
+  T[m] = t;
+  mat[m] = 0;
+  rhodot[m] = 0.0;
+  rho[m] = -M.materialRho[0] * (M.materialAlpha[0] * t);
+  double e, u;
+  CreepIn ci = {0.0, 0.0, 0.0, 1e-3, 0.0, 0.0, 0, 0, 0.0, 0, {}};
+  CreepConfig exact = cfg;
+  exact.mode = 0;
+  if (rheology(M, O, 0, t, x, y, e, u, &exact, &ci)) {  // updateMarkerViscosity(m, ..., 0.0)
+    eta[m] = e;
+    mu[m] = u;
+  }
+}
+
 }  // namespace
+
+extern "C" int mic_reset_nodal_fields(mic_ctx *ctx) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const size_t bytes = sizeof(double) * ctx->P.NX * ctx->P.NY;
+  for (int f = 0; f < MIC_NF_COUNT; ++f) MIC_CUDA_TRY(cudaMemsetAsync(ctx->nodal[f], 0, bytes, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+extern "C" int mic_initial_conditions_van_keken(mic_ctx *ctx, const mic_subduction_options *o) {
+  if (!ctx || !o) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->n > 0) {
+    MIC_KERNEL(ctx, "k_van_keken");
+    k_van_keken<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(
+        ctx->mat, ctx->opt, ctx->creep, std::tan(o->slabAngle), o->slabAge, o->overridingPlateThickness,
+        o->rootThickness, o->rootCenter, o->rootWidth, ctx->f64[C_X], ctx->f64[C_Y], ctx->f64[C_T], ctx->f64[C_RHO],
+        ctx->f64[C_RHODOT], ctx->f64[C_ETA], ctx->f64[C_MU], ctx->i32[C_MAT], ctx->n);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  // boundary conditions for the prescribed slab velocity (benchmarkInitialConditions.c:36-46)
+  mic_bcs b = ctx->bcs;
+  b.mechBCLeft.type[0] = 0;
+  b.mechBCLeft.type[1] = 0;
+  b.mechBCLeft.value[0] = o->slabVelocity * std::cos(o->slabAngle);
+  b.mechBCLeft.value[1] = o->slabVelocity * std::sin(o->slabAngle);
+  b.mechBCTop.type[0] = 0;
+  b.mechBCTop.value[0] = 0.0;
+  b.mechBCTop.type[1] = 0;
+  b.mechBCTop.value[1] = 0.0;
+  int e = mic_set_bcs(ctx, &b);
+  if (e) return e;
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
 
 extern "C" int mic_form_vep_system(mic_ctx *ctx, const mic_subduction_options *o, double dt, double *Kbond,
                                    double *Kcont) {

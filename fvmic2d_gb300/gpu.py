@@ -30,6 +30,7 @@ SIGNATURES = {
     "mic_set_materials": (_I, [_P, _P]),
     "mic_set_options": (_I, [_P, _P]),
     "mic_set_bcs": (_I, [_P, _P]),
+    "mic_get_bcs": (_I, [_P, _P]),
     "mic_get_grid_centres": (_I, [_P, _DP, _DP]),
     "mic_markers_upload": (_I, [_P, _P, _I64]),
     "mic_markers_download": (_I, [_P, _P, _I64]),
@@ -110,6 +111,8 @@ SIGNATURES = {
     "mic_system_band": (_I, [_P, _I, _IP, _IP]),
     "mic_subduction_timestep": (_I, [_P, _P, _D, _P]),
     "mic_adiabatic_heating": (_I, [_P, _D]),
+    "mic_reset_nodal_fields": (_I, [_P]),
+    "mic_initial_conditions_van_keken": (_I, [_P, _P]),
     "mic_nusselt_number": (_I, [_P, _D, _D, _DP]),
     "mic_rms_velocity": (_I, [_P, _DP]),
     "mic_subduction_timestep_many": (_I, [_P, _I, _P, _DP, _P, _IP, _I]),
@@ -284,6 +287,23 @@ class MicProblem:
     def adiabaticHeating(self, gy):
         """adiabaticHeating (adiabaticHeating.c:7) added to the heating field (main:377)"""
         self._check(self.L.mic_adiabatic_heating(self.h, gy), "mic_adiabatic_heating")
+
+    def get_bcs(self):
+        """the context's boundary conditions (mic_bcs)"""
+        from .mic_types import BCs
+
+        b = BCs()
+        self._check(self.L.mic_get_bcs(self.h, ctypes.byref(b)), "mic_get_bcs")
+        return b
+
+    def resetNodalFields(self):
+        self._check(self.L.mic_reset_nodal_fields(self.h), "mic_reset_nodal_fields")
+
+    def initialConditionsVanKeken(self, sopt):
+        """initialConditionsVanKeken (benchmarkInitialConditions.c:8) on the device; the left and
+        top boundary conditions change as the reference changes them"""
+        self._check(self.L.mic_initial_conditions_van_keken(self.h, ctypes.byref(sopt)),
+                    "mic_initial_conditions_van_keken")
 
     def nusseltNumber(self, bottom_T, top_T):
         v = ctypes.c_double(0.0)

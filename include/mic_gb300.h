@@ -69,6 +69,7 @@ int mic_set_materials(mic_ctx *ctx, const mic_materials *materials);
 int mic_set_options(mic_ctx *ctx, const mic_options *options);
 /* BoundaryValues read by advectMarkersRK (markers.c:1986-2023); periodic walls are rejected */
 int mic_set_bcs(mic_ctx *ctx, const mic_bcs *bcs);
+int mic_get_bcs(mic_ctx *ctx, mic_bcs *bcs); /* the context's boundary conditions */
 int mic_get_grid_centres(mic_ctx *ctx, double *xc, double *yc); /* NX+1, NY+1 entries */
 
 /* ---- markers: host AoS records <-> device columns ---- */
@@ -313,6 +314,13 @@ int mic_adiabatic_heating(mic_ctx *ctx, double gy);
  * thermalBCTop.value[0]), bit-identical; rmsVelocity (post.c:49) of the nodal vx, vy, summed by a
  * fixed tree instead of the reference's cell order (rounding differences only) */
 int mic_nusselt_number(mic_ctx *ctx, double bottom_T, double top_T, double *Nu);
+/* set-up of main (main_subduction.c:176-183): resetNodalFields (nodalFields.c:155) zeroes every
+ * nodal field; initialConditionsVanKeken (benchmarkInitialConditions.c:8) gives every marker the
+ * subduction benchmark's temperature (slab inflow profile, plate geotherm or mantle), material 0,
+ * rho, rhodot = 0 and its viscosity, and sets the left (slab velocity) and top (no slip) boundary
+ * conditions, as the reference sets them in its Options */
+int mic_reset_nodal_fields(mic_ctx *ctx);
+int mic_initial_conditions_van_keken(mic_ctx *ctx, const mic_subduction_options *options);
 int mic_rms_velocity(mic_ctx *ctx, double *vrms);
 /* No counterpart in the reference, whose main runs its Monte-Carlo realisations one after another
  * (iMonte): one mic_subduction_timestep on each of n independent contexts (each created with its

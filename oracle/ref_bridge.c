@@ -523,3 +523,18 @@ double ref_rmsVelocity(refp *p) {
   rmsVelocity(&p->grid, &p->nf, &v);
   return v;
 }
+
+/* initialConditionsVanKeken (benchmarkInitialConditions.c:8) on the caller's markers; the
+ * boundary conditions it sets in Options come back in bcs */
+int ref_initialConditionsVanKeken(refp *p, mic_marker *m, int n, const mic_subduction_options *so, mic_bcs *bcs) {
+  set_subduction(p, so);
+  p->ms.markers = (Marker *)m;
+  p->ms.nMark = n;
+  p->ms.maxMark = n;
+  int e = initialConditionsVanKeken(&p->ms, &p->opt, &p->mat, &p->grid);
+  bcs->mechBCLeft = *(const mic_bcinfo *)&p->opt.mechBCLeft;
+  bcs->mechBCRight = *(const mic_bcinfo *)&p->opt.mechBCRight;
+  bcs->mechBCTop = *(const mic_bcinfo *)&p->opt.mechBCTop;
+  bcs->mechBCBottom = *(const mic_bcinfo *)&p->opt.mechBCBottom;
+  return e;
+}

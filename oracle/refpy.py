@@ -70,6 +70,7 @@ def lib():
             "ref_retrieveSolutions": (_I, [_P, _DP, _D]),
             "ref_formVEPSystem": (_I, [_P, _P, _D, _DP, _DP]),
             "ref_adiabaticHeating": (_I, [_P, _D]),
+            "ref_initialConditionsVanKeken": (_I, [_P, _P, _I, _P, _P]),
             "ref_nusseltNumber": (_D, [_P, _D, _D]),
             "ref_rmsVelocity": (_D, [_P]),
             "ref_enforceThermalBCs1": (_I, [_P, _P]),
@@ -176,6 +177,18 @@ class RefProblem:
 
     def rmsVelocity(self):
         return lib().ref_rmsVelocity(self.h)
+
+    def initialConditionsVanKeken(self, sopt):
+        """initialConditionsVanKeken on this problem's markers; returns the BCs it sets"""
+        from fvmic2d_gb300.mic_types import BCs
+
+        b = BCs()
+        e = lib().ref_initialConditionsVanKeken(self.h, self.markers.ctypes.data, len(self.markers),
+                                                ctypes.byref(sopt), ctypes.byref(b))
+        lib().ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        if e:
+            raise RuntimeError("initialConditionsVanKeken failed: %d" % e)
+        return b
 
     def enforceThermalBCs1(self, sopt):
         e = lib().ref_enforceThermalBCs1(self.h, ctypes.byref(sopt))

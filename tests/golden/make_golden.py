@@ -309,6 +309,19 @@ def diagnostics_table():
     return out
 
 
+def van_keken_table():
+    """initialConditionsVanKeken of the reference: markers before and after, the BCs it sets"""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from tests.test_oracle_pin import van_keken_case
+
+    wl, so = van_keken_case()
+    before = np.array(wl.markers, copy=True)
+    R = refpy.RefProblem(wl)
+    b = R.initialConditionsVanKeken(so)
+    return {"before": before.view(np.uint8), "after": R.markers.view(np.uint8),
+            "bcs": np.frombuffer(bytes(b), dtype=np.uint8)}
+
+
 def checkpoint_case():
     """the VEP box after a step, with some markers pushed out of the domain"""
     wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=2)
@@ -358,6 +371,9 @@ def main():
     if sys.argv[1:] in ([], ["timestep"]):
         np.savez_compressed(os.path.join(OUT, "subduction_step.npz"), **timestep_table())
         print("wrote subduction_step")
+    if sys.argv[1:] in ([], ["vankeken"]):
+        np.savez_compressed(os.path.join(OUT, "van_keken.npz"), **van_keken_table())
+        print("wrote van_keken")
     if sys.argv[1:] in ([], ["diagnostics"]):
         np.savez_compressed(os.path.join(OUT, "post_diagnostics.npz"), **diagnostics_table())
         print("wrote post_diagnostics")

@@ -179,3 +179,32 @@ def test_diagnostics_match_reference():
     assert G.nusseltNumber(bottom, top) == float(z["nusselt"])
     v = float(z["vrms"])
     assert abs(G.rmsVelocity() - v) <= 1e-14 * v
+
+
+@pytest.mark.parametrize("build", ["exact", "product"])
+def test_van_keken_initial_conditions_match_reference(build):
+    """initialConditionsVanKeken (benchmarkInitialConditions.c:8): material, rhodot and the
+    boundary conditions' types exact; temperature, density, viscosity and shear modulus within
+    1e-12 (CUDA's erf, cos and exp against the host C library's)"""
+    from fvmic2d_gb300.mic_types import BCs
+    from tests.test_oracle_pin import van_keken_case
+
+    z = np.load(os.path.join(GOLDEN, "van_keken.npz"))
+    wl, so = van_keken_case()
+    wl.markers = z["before"].view(MARKER_DTYPE).copy()
+    ref = z["after"].view(MARKER_DTYPE)
+    G = gpu.MicProblem(wl, exact=(build == "exact"))
+    G.initialConditionsVanKeken(so)
+    got = G.markers
+    assert np.array_equal(got["Mat"], ref["Mat"]) and np.array_equal(got["rhodot"], ref["rhodot"])
+    for f in ("T", "rho", "eta", "mu"):
+        a, b = got[f], ref[f]
+        assert np.all(np.abs(a - b) <= 1e-12 * np.abs(b)), f
+    for f in ("X", "Y", "sxx", "p"):
+        assert np.array_equal(got[f], ref[f]), f
+    rb = BCs.from_buffer_copy(z["bcs"].tobytes())
+    gb = G.get_bcs()
+    for side in ("mechBCLeft", "mechBCTop"):  # the entries the routine sets: x and y of both
+        g, r = getattr(gb, side), getattr(rb, side)
+        assert list(g.type)[:2] == list(r.type)[:2], side
+        assert np.allclose(list(g.value)[:2], list(r.value)[:2], rtol=1e-15, atol=0), side

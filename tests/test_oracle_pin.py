@@ -509,6 +509,26 @@ def test_diagnostics_reference_build_matches_golden():
     assert R.rmsVelocity() == float(z["vrms"])
 
 
+def van_keken_case(seed=14):
+    """initialConditionsVanKeken's inputs: markers spread over the refined box (some outside it),
+    the subduction geometry with the plate's root inside the box"""
+    wl = W.vep_slab_box(nx_cells=24, ny_cells=10, nm=4, seed=seed)
+    wl.markers["X"][::53] = -1.0
+    _, so, _ = systems_case("fixed_top")
+    return wl, so
+
+
+@needs_ref
+def test_van_keken_reference_build_matches_golden():
+    z = np.load(os.path.join(GOLDEN, "van_keken.npz"))
+    wl, so = van_keken_case()
+    R = refpy.RefProblem(wl, markers=z["before"].view(MARKER_DTYPE))
+    b = R.initialConditionsVanKeken(so)
+    assert bytes(b) == z["bcs"].tobytes()
+    ok, msg = same_fields(R.markers, z["after"].view(MARKER_DTYPE))
+    assert ok, msg
+
+
 def test_checkpoint_matches_golden(tmp_path):
     """the reference's marker file format, byte for byte, and the restart from it"""
     z = np.load(os.path.join(GOLDEN, "marker_checkpoint.npz"))
