@@ -283,6 +283,23 @@ def timestep_table():
     return out
 
 
+def run_table():
+    """main_subduction.c's set-up and first two time steps through the reference's routines (host
+    LU solves) on the small subduction box: markers after set-up and after each step, the step
+    reports"""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from tests.timestep_case import reference_run, run_case
+
+    wl, topt, nmx, nmy, steps = run_case()
+    setup, mks, reps = reference_run(wl, topt, nmx, nmy, steps)
+    out = {"setup": setup.view(np.uint8)}
+    for i, (mk, rep) in enumerate(zip(mks, reps)):
+        out["step%d" % i] = mk.view(np.uint8)
+        for k, v in rep.items():
+            out["rep%d_%s" % (i, k)] = np.array(v)
+    return out
+
+
 def adiabatic_table():
     """adiabaticHeating of the reference plus main's addition to the heating field"""
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
@@ -371,6 +388,9 @@ def main():
     if sys.argv[1:] in ([], ["timestep"]):
         np.savez_compressed(os.path.join(OUT, "subduction_step.npz"), **timestep_table())
         print("wrote subduction_step")
+    if sys.argv[1:] in ([], ["run"]):
+        np.savez_compressed(os.path.join(OUT, "subduction_run.npz"), **run_table())
+        print("wrote subduction_run")
     if sys.argv[1:] in ([], ["vankeken"]):
         np.savez_compressed(os.path.join(OUT, "van_keken.npz"), **van_keken_table())
         print("wrote van_keken")

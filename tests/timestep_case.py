@@ -7,7 +7,7 @@ import os
 import numpy as np
 
 from fvmic2d_gb300 import workloads as W
-from fvmic2d_gb300.mic_types import DensityOptions, TimestepOptions
+from fvmic2d_gb300.mic_types import NF, DensityOptions, TimestepOptions
 from tests.test_oracle_pin import systems_case
 
 
@@ -68,9 +68,16 @@ def reference_timestep(wl, topt, elapsed=0.0, capacity=None):
     step, report dict, nodal fields dict)"""
     from oracle import refpy
 
+    R = refpy.RefProblem(wl)
+    return reference_step(R, topt, elapsed, capacity)
+
+
+def reference_step(R, topt, elapsed=0.0, capacity=None):
+    """one pass of main's time loop on an existing reference problem"""
+    from oracle import refpy
+
     so = topt.sub
     with open(os.devnull, "w") as devnull, contextlib.redirect_stdout(devnull):
-        R = refpy.RefProblem(wl)
         R.findMarkerCells()
         added = 0
         if topt.densityControl:
@@ -103,8 +110,8 @@ def reference_timestep(wl, topt, elapsed=0.0, capacity=None):
         rep.update(plastic_iterations=it, is_yielding=is_y, converged=conv, displacement_dt=ddt, Kbond=kb,
                    Kcont=kc, residual=res)
         dt = ddt
-        if wl.options.subgridStressDiffusivity > 0.0:
-            R.subgridStressChanges(ddt, wl.options.subgridStressDiffusivity)
+        if R.wl.options.subgridStressDiffusivity > 0.0:
+            R.subgridStressChanges(ddt, R.wl.options.subgridStressDiffusivity)
         R.updateMarkerStress()
         if not topt.shearHeating:
             R.set_nodal("heating", np.zeros((R.NY, R.NX)))
@@ -132,3 +139,46 @@ def reference_timestep(wl, topt, elapsed=0.0, capacity=None):
         rep["max_abs_sxx"] = R.maxAbsSxx()
         nodal = {f: R.get_nodal(f) for f in ("vx", "vy", "p", "thisT", "lastT", "etaS", "etaN", "heating")}
     return R.markers.copy(), rep, nodal
+
+
+def reference_run(wl, topt, NMX, NMY, steps):
+    """main_subduction.c from set-up (176-202) through `steps` passes of the time loop, with the
+    reference build's routines and host sparse LU solves; density control off.  Returns the
+    markers after set-up, the markers after every step and the step reports."""
+    import ctypes
+
+    from oracle import refpy
+
+    so = topt.sub
+    with open(os.devnull, "w") as devnull, contextlib.redirect_stdout(devnull):
+        R = refpy.RefProblem(wl)
+        for f in NF:  # resetNodalFields (nodalFields.c:155); the Vecs it leaves are zero from creation
+            R.set_nodal(f, np.zeros((R.NY, R.NX)))
+        mk, n = R.distribute_uniform(NMX, NMY)
+        R.markers = mk[:n].copy()
+        refpy.lib().ref_set_markers(R.h, R.markers.ctypes.data, len(R.markers))
+        bcs = R.initialConditionsVanKeken(so)
+        refpy.lib().ref_set_bcs(R.h, ctypes.byref(bcs))  # updateBoundaryConditions (updateBCs.c:9)
+        R.findMarkerCells()
+        R.projectMarkersNodesAll2()
+        R.projectMarkersNodesAll2()
+        R.enforceThermalBCs1(so)
+        R.projectNodalFieldToMarkersS("lastT", "T")
+        R.findMarkerCells()
+    setup = R.markers.copy()
+    out, reps, elapsed = [], [], 0.0
+    for it in range(steps):
+        topt.firstStep = 1 if it == 0 else 0
+        mk, rep, _ = reference_step(R, topt, elapsed)
+        elapsed += rep["dt"]
+        out.append(mk)
+        reps.append(rep)
+    return setup, out, reps
+
+
+def run_case():
+    """the whole program on a small grid: the subduction box of 32 x 8 cells, 4 x 4 markers per
+    cell at set-up, two steps, density control off"""
+    wl, topt = W.subduction_box(nx_cells=32, ny_cells=8, nm=4, seed=4)
+    topt.densityControl = 0
+    return wl, topt, 4, 4, 2
