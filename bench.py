@@ -70,11 +70,15 @@ KERNEL_BYTES = {
 # dram__bytes_write.sum) of the 1,048,576-marker box, scaled to a full launch by markers
 # processed (profiles/k_advect_vep_slab_box_1m_full.md).  Reads match the algorithmic reads;
 # at the small size part of the written bytes is still in L2 when the kernel ends.
-KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (85691904 + 23738624) / 1048576}
-# FP64 flops per marker (DFMA counted twice) from the same capture: the kernels of this path
-# are bound by the FP64 pipe (2 DFMA per SM per clock on GB300), not by HBM.
-KERNEL_FP64_FLOPS_PER_MARKER = {"k_advect": 328.8}
+KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (85659904 + 23770112) / 1048576}
+# FP64 work per marker from the same capture (per-cycle DFMA / DADD / DMUL thread instructions x
+# elapsed cycles / markers: 73.9 / 70.9 / 37.0): flops with DFMA counted twice, and FP64
+# instructions.  The kernels of this path are bound by the FP64 pipe, which issues 2 FP64
+# instructions (DFMA, DADD or DMUL alike) per SM per clock on GB300, not by HBM.
+KERNEL_FP64_FLOPS_PER_MARKER = {"k_advect": 255.8}
+KERNEL_FP64_INST_PER_MARKER = {"k_advect": 181.9}
 FP64_PEAK_TFLOPS = 2 * 2 * 152 * 2.07e9 / 1e12  # 2 DFMA/SM/clk x 2 flops x 152 SMs x 2.07 GHz
+FP64_PEAK_GINST = 2 * 152 * 2.07  # FP64 instructions per second, in G
 
 
 def parse():
@@ -443,7 +447,10 @@ def run_ours(args):
                            "achieved": KERNEL_FP64_FLOPS_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e12,
                            "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
                            "frac": KERNEL_FP64_FLOPS_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
-                           "note": "the bound that applies: FP64 pipe, 2 DFMA/SM/clk; flops per marker from ncu"}
+                           "inst_per_marker": KERNEL_FP64_INST_PER_MARKER[top_name],
+                           "issue_frac": KERNEL_FP64_INST_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e9 / FP64_PEAK_GINST,
+                           "note": "the bound that applies: FP64 pipe, 2 FP64 instructions/SM/clk; flops and "
+                                   "instructions per marker from ncu; issue_frac = FP64 instructions issued / peak"}
                           if top_name in KERNEL_FP64_FLOPS_PER_MARKER else None),
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes, "achieved_gbs": step_gbs,
                           "frac": step_gbs / hbm_peak},

@@ -574,8 +574,10 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
 #ifndef MIC_EXACT
     // vx sits on the basic x lines and vy on the basic y lines: with vxX == i and vyY == j (the
     // walk keeps i, j inside the clamps) their fractions there are the basic cell's mdx, mdy
-    const double mdx = div_sp(xcur - P.x[i], P.hx[i], P.ix[i]);
-    const double mdy = div_sp(ycur - P.y[j], P.hy[j], P.iy[j]);
+    // fractions here only weight interpolations (every cell decision above is on integer images),
+    // so one multiply by the tabulated reciprocal, within an ulp of the quotient, stands in for it
+    const double mdx = (xcur - P.x[i]) * P.ix[i];
+    const double mdy = (ycur - P.y[j]) * P.iy[j];
 #endif
     double ax = xcur - P.x[vxX];
     double ay = ycur - P.yc[vxY + 1];
@@ -584,7 +586,7 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     double hy = P.yc[vxY + 2] - P.yc[vxY + 1];
 #else
     const double tx = mdx;
-    const double ty = div_sp(ay, P.hyc[vxY + 1], P.iyc[vxY + 1]);
+    const double ty = ay * P.iyc[vxY + 1];
 #endif
     const size_t r1 = (size_t)(vxY + 1) * NX;
     double vul, vur;
@@ -632,7 +634,7 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     t += wll * (1.0 - ax / hx) * (ay / hy);
     t += wlr * (ax * ay) / hx / hy;
 #else
-    t = lerp2(wul, wur, wll, wlr, div_sp(xcur - P.xc[vyX + 1], P.hxc[vyX + 1], P.ixc[vyX + 1]), mdy);
+    t = lerp2(wul, wur, wll, wlr, (xcur - P.xc[vyX + 1]) * P.ixc[vyX + 1], mdy);
 #endif
     mvy[s] = t;
     const size_t w0 = (size_t)j * NX + i;
@@ -655,9 +657,16 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
       ycur = Y0 + dt * mvy[s];
     }
   }
+#ifdef MIC_EXACT
   const double VX = div6(mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]);
   const double VY = div6(mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]);
   const double w = div6(mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]);
+#else
+  const double inv6 = 0.16666666666666666;
+  const double VX = (mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]) * inv6;
+  const double VY = (mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]) * inv6;
+  const double w = (mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]) * inv6;
+#endif
   c.VX[m] = VX;
   c.VY[m] = VY;
   c.wxy[m] = w;
