@@ -192,14 +192,21 @@ __global__ void k_radix_scatter(const int *__restrict__ key_in, const int *__res
 // q in [0, 4*ncells+4] (when qs is given) and cs[c] = qs[4c] for c in [0, ncells+1].
 __global__ void k_cell_start(const int *__restrict__ skey, int64_t n, int ncells, int *__restrict__ cs,
                              int *__restrict__ qs) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k > n) return;
-  const int hi = (k < n) ? skey[k] : 4 * ncells + 4;
-  const int lo = (k == 0) ? -1 : skey[k - 1];
-  for (int q = lo + 1; q <= hi; ++q) {
-    if (qs) qs[q] = (int)k;
-    if ((q & 3) == 0) cs[q >> 2] = (int)k;
+  // one thread per (cell, quadrant) key q in [0, 4 ncells + 4]: the run of key q starts at the
+  // first sorted position whose key is >= q (n when there is none), found by binary search, so
+  // empty stretches of cells cost nothing extra.  cs[c] = qs[4c].
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q > 4LL * ncells + 4) return;
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (skey[mid] < q)
+      lo = mid + 1;
+    else
+      hi = mid;
   }
+  if (qs) qs[q] = (int)lo;
+  if ((q & 3) == 0) cs[q >> 2] = (int)lo;
 }
 
 struct GatherCols {
@@ -326,8 +333,8 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   // kin / vin now hold the sorted keys and the permutation
   {
     MIC_KERNEL(ctx, "k_cell_start");
-    k_cell_start<<<grid_for(n + 1), kBlock, 0, ctx->stream>>>(kin, n, ctx->ncells, ctx->cell_start,
-                                                             ctx->quad_start);
+    k_cell_start<<<grid_for(4LL * ctx->ncells + 5), kBlock, 0, ctx->stream>>>(kin, n, ctx->ncells,
+                                                                              ctx->cell_start, ctx->quad_start);
   }
   MIC_CUDA_TRY(cudaGetLastError());
   GatherCols g;
@@ -578,7 +585,7 @@ extern "C" int mic_bin_sort_noalloc(const double *X, const double *Y, int64_t n,
       kin = kout;
       vin = vout;
     }
-    k_cell_start<<<grid_for(n + 1), kBlock, 0, s>>>(kin, n, (int)ncells, cell_start, nullptr);
+    k_cell_start<<<grid_for(4LL * ncells + 5), kBlock, 0, s>>>(kin, n, (int)ncells, cell_start, nullptr);
   } else {
     if (cudaMemsetAsync(cell_start, 0, sizeof(int32_t) * (size_t)(ncells + 2), s) != cudaSuccess)
       return MIC_ERR_CUDA;

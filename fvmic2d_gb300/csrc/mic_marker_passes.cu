@@ -439,6 +439,102 @@ __global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const in
   dsxy[q] = dsxy[q] + -1.0 * gxy;
 }
 
+#ifndef MIC_EXACT
+// Product build: the same sums through per-cell partials.  One thread per basic cell walks the
+// cell's markers once.  Each marker adds its dsxy to the corner node(s) its quadrant tests pick
+// (both tests of subgridStressChanges.c:134-175 are inclusive, so a marker on a midline feeds two
+// or four corners) in per-thread shared slots, and its dsxx, dsyy to the cell centre
+// (227-233).  k_subgrid_combine then adds the four cells meeting at each node in a fixed order
+// and divides.  Sums run in marker order within a cell; the cross-cell order differs from the
+// reference's single loop (rounding at the last place), and is fixed, so runs reproduce.
+// part[acc * ncells + cell]: corner k sxy at 2k, weight at 2k+1; centre sxx, syy, weight at 8..10.
+__global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double *__restrict__ gx0,
+                                                          const double *__restrict__ gy0,
+                                                          const double *__restrict__ dxy,
+                                                          const double *__restrict__ dxx,
+                                                          const double *__restrict__ dyy,
+                                                          const int *__restrict__ cs, double *__restrict__ part) {
+  __shared__ double sloc[8][128];
+  const int ncells = (P.NX - 1) * (P.NY - 1);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) sloc[k][t] = 0.0;
+  const long long half = 0x3FE0000000000000LL;
+  double sxx = 0.0, syy = 0.0, wn = 0.0;
+  const int mb = cs[c], me = cs[c + 1];
+  for (int m = mb; m < me; ++m) {
+    const double mx = gx0[m], my = gy0[m];
+    const long long bx = nonneg_bits(mx), by = nonneg_bits(my);
+    const int ox = bx > half, oy = by > half;  // the one corner off the midlines
+    const double d = dxy[m];
+    {
+      const double w = (ox ? mx : (1.0 - mx)) * (oy ? my : (1.0 - my));
+      double *L = &sloc[2 * (ox + 2 * oy)][t];
+      L[0] = L[0] + w * d;
+      L[128] = L[128] + w;
+    }
+    if (bx == half || by == half) {  // on a midline: the other corners whose tests hold too
+      for (int k = 0; k < 4; ++k) {
+        const int kx = k & 1, ky = k >> 1;
+        if ((kx == ox && ky == oy) || (kx != ox && bx != half) || (ky != oy && by != half)) continue;
+        const double w = (kx ? mx : (1.0 - mx)) * (ky ? my : (1.0 - my));
+        double *L = &sloc[2 * k][t];
+        L[0] = L[0] + w * d;
+        L[128] = L[128] + w;
+      }
+    }
+    const double wc = (1.0 - fabs(0.5 - mx)) * (1.0 - fabs(0.5 - my));
+    sxx += wc * dxx[m];
+    syy += wc * dyy[m];
+    wn += wc;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) part[(size_t)k * ncells + c] = sloc[k][t];
+  part[(size_t)8 * ncells + c] = sxx;
+  part[(size_t)9 * ncells + c] = syy;
+  part[(size_t)10 * ncells + c] = wn;
+}
+
+// Node (i, j): dsxy sums of cells (i-1,j-1) corner 3, (i,j-1) corner 2, (i-1,j) corner 1, (i,j)
+// corner 0; dsxx, dsyy from cell (i-1, j-1)'s centre; guarded divides and the subtraction of
+// subgridStressChanges.c:258-286.
+__global__ void __launch_bounds__(128) k_subgrid_combine(Params P, const double *__restrict__ part, double *dsxx,
+                                                         double *dsyy, double *dsxy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= P.NX || j >= P.NY) return;
+  const int NC = P.NX - 1, ncells = NC * (P.NY - 1);
+  double sxy = 0.0, wxy = 0.0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int dx = r & 1, dy = r >> 1;
+    const int cx = i - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
+    if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
+      const size_t cc = (size_t)cy * NC + cx;
+      sxy += part[(size_t)(2 * k) * ncells + cc];
+      wxy += part[(size_t)(2 * k + 1) * ncells + cc];
+    }
+  }
+  double sxx = 0.0, syy = 0.0, wn = 0.0;
+  if (i >= 1 && j >= 1 && i <= P.NX - 1 && j <= P.NY - 1) {
+    const size_t cc = (size_t)(j - 1) * NC + (i - 1);
+    sxx = part[(size_t)8 * ncells + cc];
+    syy = part[(size_t)9 * ncells + cc];
+    wn = part[(size_t)10 * ncells + cc];
+  }
+  const size_t q = (size_t)j * P.NX + i;
+  const double W = 0.0 + wxy, Wn = 0.0 + wn;
+  const double gxy = (W != 0.0) ? (0.0 + sxy) / W : 0.0;
+  const double gxx = (Wn != 0.0) ? (0.0 + sxx) / Wn : 0.0;
+  const double gyy = (Wn != 0.0) ? (0.0 + syy) / Wn : 0.0;
+  dsxx[q] = dsxx[q] + -1.0 * gxx;
+  dsyy[q] = dsyy[q] + -1.0 * gyy;
+  dsxy[q] = dsxy[q] + -1.0 * gxy;
+}
+#endif
+
 struct StressCols {
   const int *cellX, *cellY;
   const double *X, *Y;
@@ -1006,6 +1102,7 @@ extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
     MIC_CUDA_TRY(cudaGetLastError());
   }
   dim3 grid((ctx->P.NX + 127) / 128, ctx->P.NY);
+#ifdef MIC_EXACT
   {
     MIC_KERNEL(ctx, "k_subgrid_stress_nodes");
     k_subgrid_stress_nodes<<<grid, 128, 0, ctx->stream>>>(ctx->P, ctx->i32[C_CELLX], ctx->geo[0], ctx->geo[1],
@@ -1013,6 +1110,21 @@ extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
                                                           ctx->nodal[MIC_NF_DSXX], ctx->nodal[MIC_NF_DSYY],
                                                           ctx->nodal[MIC_NF_DSXY]);
   }
+#else
+  if (ctx->n > 0) {
+    MIC_KERNEL(ctx, "k_subgrid_partials");
+    k_subgrid_partials<<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(
+        ctx->P, ctx->geo[0], ctx->geo[1], ctx->scr0, ctx->scr1, ctx->scr2, ctx->cell_start, ctx->part_b);
+  } else {
+    MIC_CUDA_TRY(cudaMemsetAsync(ctx->part_b, 0, sizeof(double) * 11 * (size_t)ctx->ncells, ctx->stream));
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  {
+    MIC_KERNEL(ctx, "k_subgrid_combine");
+    k_subgrid_combine<<<grid, 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->nodal[MIC_NF_DSXX],
+                                                     ctx->nodal[MIC_NF_DSYY], ctx->nodal[MIC_NF_DSXY]);
+  }
+#endif
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }

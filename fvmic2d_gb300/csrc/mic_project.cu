@@ -272,63 +272,61 @@ struct PartialView {
 
 // ALL2: rho, etaS, k, T, Cp, weight per corner (24) + nearest-node sxy, weight (8) = 32 sums.
 // !ALL2: scalar, weight per corner = 8 sums.  part[acc * ncells + cell].
+//
+// One loop over the cell's markers (its four quadrant runs back to back, the same order as
+// quadrant by quadrant): a warp's lanes then wait for the longest cell of the warp once, not
+// for the longest run of each quadrant four times.  The nearest-node sums go to a per-thread
+// shared-memory slot picked by the marker's corner, so the loop has no corner branches.
 template <bool ALL2>
 __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v, const int *__restrict__ qs,
                                                          mic_materials mat, double *__restrict__ part) {
+  __shared__ double sloc[ALL2 ? 8 : 1][128];
   const int ncells = (P.NX - 1) * (P.NY - 1);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   constexpr int NA = ALL2 ? 6 : 2;
-  double acc[4][NA], loc[4][2];
+  const int t = threadIdx.x;
+  double acc[4][NA];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
 #pragma unroll
     for (int f = 0; f < NA; ++f) acc[k][f] = 0.0;
-    loc[k][0] = loc[k][1] = 0.0;
   }
+  if (ALL2) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int mb = qs[4 * c + q], me = qs[4 * c + q + 1];
-    for (int m = mb; m < me; ++m) {
-      const double mx = v.gx0[m], my = v.gy0[m];
-      const double a = 1.0 - mx, b = 1.0 - my;
-      const double w[4] = {a * b, mx * b, a * my, mx * my};
-      if (ALL2) {
-        const double r = v.rho[m], e = v.eta[m], t = v.T[m];
-        const int mt = v.mat[m];
-        const double kk = mat.materialkThermal[mt], cp = mat.materialCp[mt];
+    for (int k = 0; k < 8; ++k) sloc[k][t] = 0.0;
+  }
+  const int mb = qs[4 * c], me = qs[4 * c + 4];
+  for (int m = mb; m < me; ++m) {
+    const double mx = v.gx0[m], my = v.gy0[m];
+    const double a = 1.0 - mx, b = 1.0 - my;
+    const double w[4] = {a * b, mx * b, a * my, mx * my};
+    if (ALL2) {
+      const double r = v.rho[m], e = v.eta[m], tt = v.T[m];
+      const int mt = v.mat[m];
+      const double kk = mat.materialkThermal[mt], cp = mat.materialCp[mt];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          acc[k][0] = fma(w[k], r, acc[k][0]);
-          acc[k][1] = fma(w[k], e, acc[k][1]);
-          acc[k][2] = fma(w[k], kk, acc[k][2]);
-          acc[k][3] = fma(w[k], t, acc[k][3]);
-          acc[k][4] = fma(w[k], cp, acc[k][4]);
-          acc[k][5] += w[k];
-        }
-        // nearest basic node: (mdx0 >= .5, mdy0 >= .5), the quadrant's own corner but for
-        // markers a rounding away from the midline
-        const int fl = v.flags[m];
-        const int corner = ((fl >> 2) & 1) | (((fl >> 3) & 1) << 1);
-        const double sxy = v.sxy[m];
-        if (corner == q) {
-          loc[q][0] = fma(w[q], sxy, loc[q][0]);
-          loc[q][1] += w[q];
-        } else {
+      for (int k = 0; k < 4; ++k) {
+        acc[k][0] = fma(w[k], r, acc[k][0]);
+        acc[k][1] = fma(w[k], e, acc[k][1]);
+        acc[k][2] = fma(w[k], kk, acc[k][2]);
+        acc[k][3] = fma(w[k], tt, acc[k][3]);
+        acc[k][4] = fma(w[k], cp, acc[k][4]);
+        acc[k][5] += w[k];
+      }
+      // nearest basic node (mdx0 >= .5, mdy0 >= .5): the weight of that corner, as w[corner]
+      const int fl = v.flags[m];
+      const int corner = ((fl >> 2) & 1) | (((fl >> 3) & 1) << 1);
+      const double wc = __dmul_rn((corner & 1) ? mx : a, (corner & 2) ? my : b);
+      double *L = &sloc[2 * corner][t];
+      L[0] = fma(wc, v.sxy[m], L[0]);
+      L[128] = __dadd_rn(L[128], wc);
+    } else {
+      const double sc = v.scalar[m];
 #pragma unroll
-          for (int k = 0; k < 4; ++k)
-            if (k == corner) {
-              loc[k][0] = fma(w[k], sxy, loc[k][0]);
-              loc[k][1] += w[k];
-            }
-        }
-      } else {
-        const double s = v.scalar[m];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          acc[k][0] = fma(w[k], s, acc[k][0]);
-          acc[k][1] += w[k];
-        }
+      for (int k = 0; k < 4; ++k) {
+        acc[k][0] = fma(w[k], sc, acc[k][0]);
+        acc[k][1] += w[k];
       }
     }
   }
@@ -337,8 +335,8 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
 #pragma unroll
     for (int f = 0; f < NA; ++f) part[(size_t)(k * NA + f) * ncells + c] = acc[k][f];
     if (ALL2) {
-      part[(size_t)(24 + 2 * k) * ncells + c] = loc[k][0];
-      part[(size_t)(25 + 2 * k) * ncells + c] = loc[k][1];
+      part[(size_t)(24 + 2 * k) * ncells + c] = sloc[2 * k][t];
+      part[(size_t)(25 + 2 * k) * ncells + c] = sloc[2 * k + 1][t];
     }
   }
 }
@@ -347,58 +345,62 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
 // basic cell (sx-1, sy-1), quadrant 2 of (sx, sy-1), quadrant 1 of (sx-1, sy) and quadrant 0 of
 // (sx, sy).  ALL2: etaN, weight per corner (8) + nearest-node sxx, syy, weight (12) = 20 sums;
 // !ALL2: scalar, weight per corner = 8.  part[acc * NX*NY + s].
+//
+// The four runs are walked as one sequence (run 0's markers, then run 1's, ...) by one loop,
+// for the same reason as in k_partials_basic; the nearest-centre sums use per-thread shared
+// slots.
 template <bool ALL2>
 __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v, const int *__restrict__ qs,
                                                           double *__restrict__ part) {
+  __shared__ double sloc[ALL2 ? 12 : 1][128];
   const int sx = blockIdx.x * blockDim.x + threadIdx.x;
   const int sy = blockIdx.y;
   if (sx >= P.NX || sy >= P.NY) return;
   const int NC = P.NX - 1;
+  const int t = threadIdx.x;
   const size_t ns = (size_t)P.NX * P.NY, s = (size_t)sy * P.NX + sx;
-  double acc[4][2], loc[4][3];
+  double acc[4][2];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    acc[k][0] = acc[k][1] = 0.0;
-    loc[k][0] = loc[k][1] = loc[k][2] = 0.0;
+  for (int k = 0; k < 4; ++k) acc[k][0] = acc[k][1] = 0.0;
+  if (ALL2) {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) sloc[k][t] = 0.0;
   }
+  int rb[4], rn[4];  // run starts and lengths; a run outside the grid is empty
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int dx = r & 1, dy = r >> 1;         // basic cell (sx-1+dx, sy-1+dy) ...
     const int cx = sx - 1 + dx, cy = sy - 1 + dy;
     const int q = (1 - dx) + 2 * (1 - dy);      // ... contributes its quadrant q
-    if (cx < 0 || cx > P.NX - 2 || cy < 0 || cy > P.NY - 2) continue;
-    const int qq = 4 * (cy * NC + cx) + q;
-    const int mb = qs[qq], me = qs[qq + 1];
-    for (int m = mb; m < me; ++m) {
-      const double mx = v.gx1[m], my = v.gy1[m];
-      const double a = 1.0 - mx, b = 1.0 - my;
-      const double w[4] = {a * b, mx * b, a * my, mx * my};
-      const double e = ALL2 ? v.eta[m] : v.scalar[m];
+    rb[r] = 0;
+    rn[r] = 0;
+    if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
+      const int qq = 4 * (cy * NC + cx) + q;
+      rb[r] = qs[qq];
+      rn[r] = qs[qq + 1] - qs[qq];
+    }
+  }
+  const int e1 = rn[0], e2 = e1 + rn[1], e3 = e2 + rn[2], total = e3 + rn[3];
+  for (int u = 0; u < total; ++u) {
+    const int m = (u < e1) ? rb[0] + u : (u < e2) ? rb[1] + (u - e1) : (u < e3) ? rb[2] + (u - e2) : rb[3] + (u - e3);
+    const double mx = v.gx1[m], my = v.gy1[m];
+    const double a = 1.0 - mx, b = 1.0 - my;
+    const double w[4] = {a * b, mx * b, a * my, mx * my};
+    const double e = ALL2 ? v.eta[m] : v.scalar[m];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        acc[k][0] = fma(w[k], e, acc[k][0]);
-        acc[k][1] += w[k];
-      }
-      if (ALL2) {
-        // nearest cell centre (mdx1 >= .5, mdy1 >= .5): on a uniform grid always the basic
-        // cell's own centre, corner 3 - q
-        const int fl = v.flags[m];
-        const int corner = ((fl >> 4) & 1) | (((fl >> 5) & 1) << 1);
-        const double a1 = v.sxx[m], a2 = v.syy[m];
-        if (corner == 3 - q) {
-          loc[3 - q][0] = fma(w[3 - q], a1, loc[3 - q][0]);
-          loc[3 - q][1] = fma(w[3 - q], a2, loc[3 - q][1]);
-          loc[3 - q][2] += w[3 - q];
-        } else {
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            if (k == corner) {
-              loc[k][0] = fma(w[k], a1, loc[k][0]);
-              loc[k][1] = fma(w[k], a2, loc[k][1]);
-              loc[k][2] += w[k];
-            }
-        }
-      }
+    for (int k = 0; k < 4; ++k) {
+      acc[k][0] = fma(w[k], e, acc[k][0]);
+      acc[k][1] += w[k];
+    }
+    if (ALL2) {
+      // nearest cell centre (mdx1 >= .5, mdy1 >= .5), weight as w[corner]
+      const int fl = v.flags[m];
+      const int corner = ((fl >> 4) & 1) | (((fl >> 5) & 1) << 1);
+      const double wc = __dmul_rn((corner & 1) ? mx : a, (corner & 2) ? my : b);
+      double *L = &sloc[3 * corner][t];
+      L[0] = fma(wc, v.sxx[m], L[0]);
+      L[128] = fma(wc, v.syy[m], L[128]);
+      L[256] = __dadd_rn(L[256], wc);
     }
   }
 #pragma unroll
@@ -406,9 +408,9 @@ __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v
     part[(size_t)(2 * k) * ns + s] = acc[k][0];
     part[(size_t)(2 * k + 1) * ns + s] = acc[k][1];
     if (ALL2) {
-      part[(size_t)(8 + 3 * k) * ns + s] = loc[k][0];
-      part[(size_t)(9 + 3 * k) * ns + s] = loc[k][1];
-      part[(size_t)(10 + 3 * k) * ns + s] = loc[k][2];
+      part[(size_t)(8 + 3 * k) * ns + s] = sloc[3 * k][t];
+      part[(size_t)(9 + 3 * k) * ns + s] = sloc[3 * k + 1][t];
+      part[(size_t)(10 + 3 * k) * ns + s] = sloc[3 * k + 2][t];
     }
   }
 }
