@@ -138,6 +138,8 @@ static void free_ctx(mic_ctx *ctx) {
   cudaFree(ctx->scan_aux);
   for (int g = 0; g < 4; ++g) cudaFree(ctx->geo[g]);
   cudaFree(ctx->geo_flags);
+  cudaFree(ctx->wgt[0]);
+  cudaFree(ctx->wgt[1]);
   cudaFree(ctx->scr0);
   cudaFree(ctx->scr1);
   cudaFree(ctx->scr2);
@@ -325,6 +327,10 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ALLOC(ctx->part_c, sizeof(double) * 20 * nn);
   for (int g = 0; g < 4; ++g) ALLOC(ctx->geo[g], sizeof(double) * cap);
   ALLOC(ctx->geo_flags, sizeof(int) * cap);
+#ifndef MIC_EXACT
+  ALLOC(ctx->wgt[0], 4 * sizeof(double) * cap);
+  ALLOC(ctx->wgt[1], 4 * sizeof(double) * cap);
+#endif
   ALLOC(ctx->scr0, sizeof(double) * cap);
   ALLOC(ctx->scr1, sizeof(double) * cap);
   ALLOC(ctx->scr2, sizeof(double) * cap);

@@ -140,6 +140,8 @@ struct mic_ctx {
   // per-marker projection geometry for the current positions and order (see mic_project.cu)
   double *geo[4];      // mdx0, mdy0 (basic cell), mdx1, mdy1 (cell-centre stagger -1,-1)
   int *geo_flags;      // bit0 qx, bit1 qy, bit2 mdx0>=.5, bit3 mdy0>=.5, bit4 mdx1>=.5, bit5 mdy1>=.5
+  double *wgt[2];      // bilinear corner weights (product build), 4 per marker in corner order
+                       // 00, 10, 01, 11: [0] of the basic cell, [1] of the cell-centre cell
   int geo_valid;
   // per-marker scratch
   double *scr0, *scr1, *scr2;
@@ -215,6 +217,29 @@ inline unsigned grid_for(int64_t n, int block = kBlock) {
 
 // Bit pattern of a non-negative double, canonicalising -0.0 to +0.0, so that for
 // non-negative finite values a >= b  <=>  bits(a) >= bits(b) as signed integers.
+// Bilinear weights (1-mdx)(1-mdy), mdx(1-mdy), (1-mdx)mdy, mdx mdy, formed as the reference's
+// interpolations form them.
+struct W4 {
+  double w00, w10, w01, w11;
+};
+__device__ __forceinline__ W4 make_w4(double mdx, double mdy) {
+  const double a = 1.0 - mdx, b = 1.0 - mdy;
+  return W4{a * b, mdx * b, a * mdy, mdx * mdy};
+}
+__device__ __forceinline__ W4 load_w4(const double *__restrict__ w, int64_t m) {
+  const double2 lo = __ldg(reinterpret_cast<const double2 *>(w + 4 * m));
+  const double2 hi = __ldg(reinterpret_cast<const double2 *>(w + 4 * m) + 1);
+  return W4{lo.x, lo.y, hi.x, hi.y};
+}
+// weight of corner k = ox + 2 oy (selects, no FP64 work)
+__device__ __forceinline__ double w4_at(const W4 &w, int k) {
+  return (k & 2) ? ((k & 1) ? w.w11 : w.w01) : ((k & 1) ? w.w10 : w.w00);
+}
+__device__ __forceinline__ void store_w4(double *w, int64_t m, const W4 &v) {
+  reinterpret_cast<double2 *>(w + 4 * m)[0] = make_double2(v.w00, v.w10);
+  reinterpret_cast<double2 *>(w + 4 * m)[1] = make_double2(v.w01, v.w11);
+}
+
 __device__ __forceinline__ long long nonneg_bits(double v) {
   long long b = __double_as_longlong(v);
   return (b == (long long)0x8000000000000000ULL) ? 0LL : b;
@@ -259,6 +284,16 @@ __device__ __forceinline__ double div_sp(double num, double den, double inv) {
 
 // Running bilinear sum in the order 00, 01, 10, 11 of updateMarkerStrainPressure.c:152-158,
 // subgridStressChanges.c:97-102 and updateMarkerStress.c:84-93.
+// The same running sum with the weights given.
+__device__ __forceinline__ double interp_w(const double *__restrict__ f, int NX, int i, int j, const W4 &w) {
+  const size_t k = (size_t)j * NX + i;
+  double s = w.w00 * __ldg(f + k);
+  s = fma(w.w01, __ldg(f + k + NX), s);
+  s = fma(w.w10, __ldg(f + k + 1), s);
+  s = fma(w.w11, __ldg(f + k + NX + 1), s);
+  return s;
+}
+
 __device__ __forceinline__ double interp_run(const double *__restrict__ f, int NX, int i, int j, double mdx,
                                              double mdy) {
   const size_t k = (size_t)j * NX + i;

@@ -74,9 +74,16 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   // visco-elastic forecast with the old viscosity and modulus (markers.c:1397-1402)
   const double Xf = eta_old / (mu_old * dt + eta_old);
+#ifdef MIC_EXACT
   const double fxx = s11 * Xf + 2 * eta_old * e11 * (1.0 - Xf);
   const double fyy = s22 * Xf + 2 * eta_old * e22 * (1.0 - Xf);
   const double fxy = s12 * Xf + 2 * eta_old * e12 * (1.0 - Xf);
+#else
+  const double ve = 2 * eta_old * (1.0 - Xf);  // shared by the three components
+  const double fxx = fma(s11, Xf, ve * e11);
+  const double fyy = fma(s22, Xf, ve * e22);
+  const double fxy = fma(s12, Xf, ve * e12);
+#endif
   const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
   const int k = c.mat[m];
   double eta, mu;
@@ -254,7 +261,24 @@ __global__ void k_update_rho(const int *cellX, const int *mat, const double *T, 
 struct Geo {
   const double *gx0, *gy0, *gx1, *gy1;
   const int *flags;
+  const double *w0, *w1;  // stored corner weights (product build)
 };
+
+#ifndef MIC_EXACT
+// Centre-cell weights of marker m: the stored ones, unless the interior clamp of centre_interp
+// moved the cell (then formed from the offsets, as centre_interp forms them).
+__device__ __forceinline__ W4 centre_w(const Params &P, const Geo &g, int64_t m, int cx, int cy,
+                                       const double *__restrict__ X, const double *__restrict__ Y, int &i, int &j) {
+  const int fl = g.flags[m];
+  const int sx = cx + (fl & 1), sy = cy + ((fl >> 1) & 1);
+  i = clampi(sx, 1, P.NX - 2);
+  j = clampi(sy, 1, P.NY - 2);
+  if (i == sx && j == sy) return load_w4(g.w1, m);
+  const double mdx = (i == sx) ? g.gx1[m] : div_sp(X[m] - P.xc[i], P.hxc[i], P.ixc[i]);
+  const double mdy = (j == sy) ? g.gy1[m] : div_sp(Y[m] - P.yc[j], P.hyc[j], P.iyc[j]);
+  return make_w4(mdx, mdy);
+}
+#endif
 
 struct Nodal {
   const double *p, *exx, *exy, *soxx, *soyy, *soxy, *dsxx, *dsyy, *dsxy, *wxy;
@@ -272,11 +296,12 @@ __global__ void k_strain_pressure(Params P, StrainCols c, Geo g, Nodal nd, doubl
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
-  const double x = c.X[m], y = c.Y[m];
   int i, j;
+  const int NX = P.NX;
+#ifdef MIC_EXACT
+  const double x = c.X[m], y = c.Y[m];
   double mdx, mdy;
   centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], x, y, i, j, mdx, mdy);
-  const int NX = P.NX;
   c.p[m] = interp_run(nd.p, NX, i, j, mdx, mdy);
   const double mexx = interp_run(nd.exx, NX, i, j, mdx, mdy);
   const double msxx = interp_run(nd.soxx, NX, i, j, mdx, mdy);
@@ -288,14 +313,39 @@ __global__ void k_strain_pressure(Params P, StrainCols c, Geo g, Nodal nd, doubl
   const double mexy = interp_run(nd.exy, NX, cx, cy, bx, by);
   const double msxy = interp_run(nd.soxy, NX, cx, cy, bx, by);
   const double mdsxy = interp_run(nd.dsxy, NX, cx, cy, bx, by);
+#else
+  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
+  c.p[m] = interp_w(nd.p, NX, i, j, wc);
+  const double mexx = interp_w(nd.exx, NX, i, j, wc);
+  const double msxx = interp_w(nd.soxx, NX, i, j, wc);
+  const double msyy = interp_w(nd.soyy, NX, i, j, wc);
+  const double mdsxx = interp_w(nd.dsxx, NX, i, j, wc);
+  const double mdsyy = interp_w(nd.dsyy, NX, i, j, wc);
+  const W4 wb = load_w4(g.w0, m);
+  c.wxy[m] = interp_w(nd.wxy, NX, cx, cy, wb);
+  const double mexy = interp_w(nd.exy, NX, cx, cy, wb);
+  const double msxy = interp_w(nd.soxy, NX, cx, cy, wb);
+  const double mdsxy = interp_w(nd.dsxy, NX, cx, cy, wb);
+#endif
   const double eta = c.eta[m], mu = c.mu[m];
 #ifdef MIC_EXACT
   const double e11 = msxx / 2.0 / eta + mdsxx / 2.0 / dt / mu;
   const double e22 = msyy / 2.0 / eta + mdsyy / 2.0 / dt / mu;
   const double e12 = msxy / 2.0 / eta + mdsxy / 2.0 / dt / mu;
 #else
-  // two divisions instead of nine: 1/(2 eta) and 1/(2 dt mu) shared by the three components
-  const double ie = 0.5 / eta, idm = 0.5 / (dt * mu);
+  // one division instead of nine: 1/(2 eta) and 1/(2 dt mu) from 1/(eta dt mu), shared by the
+  // three components (within a few ulp of the reference's quotients)
+  const double dtmu = dt * mu, den = eta * dtmu;
+  double ie, idm;
+  const unsigned ex = (unsigned)(__double_as_longlong(den) >> 52) & 0x7ffu;  // den >= 0
+  if (ex > 64u && ex < 1984u) {  // far from under- and overflow (an integer test)
+    const double inv = 0.5 / den;
+    ie = dtmu * inv;
+    idm = eta * inv;
+  } else {
+    ie = 0.5 / eta;
+    idm = 0.5 / dtmu;
+  }
   const double e11 = fma(mdsxx, idm, msxx * ie);
   const double e22 = fma(mdsyy, idm, msyy * ie);
   const double e12 = fma(mdsxy, idm, msxy * ie);
@@ -368,16 +418,28 @@ __global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal n
 #endif
   if (sdif < -30.0) sdif = -30.0;
   sdif = 1.0 - exp(sdif);
+#ifdef MIC_EXACT
   double dsxy = interp_run(nd.soxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]) - c.sxy[m];
+#else
+  double dsxy = interp_w(nd.soxy, P.NX, cx, cy, load_w4(g.w0, m)) - c.sxy[m];
+#endif
   dsxy *= sdif;
   c.sxy[m] = c.sxy[m] + dsxy;
   int i, j;
+#ifdef MIC_EXACT
   double mdx, mdy;
   centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], i, j, mdx, mdy);
   double dsxx = interp_run(nd.soxx, P.NX, i, j, mdx, mdy) - c.sxx[m];
   dsxx *= sdif;
   c.sxx[m] = c.sxx[m] + dsxx;
   double dsyy = interp_run(nd.soyy, P.NX, i, j, mdx, mdy) - c.syy[m];
+#else
+  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
+  double dsxx = interp_w(nd.soxx, P.NX, i, j, wc) - c.sxx[m];
+  dsxx *= sdif;
+  c.sxx[m] = c.sxx[m] + dsxx;
+  double dsyy = interp_w(nd.soyy, P.NX, i, j, wc) - c.syy[m];
+#endif
   dsyy *= sdif;
   c.syy[m] = c.syy[m] + dsyy;
   c.dxy[m] = dsxy;
@@ -450,6 +512,7 @@ __global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const in
 // part[acc * ncells + cell]: corner k sxy at 2k, weight at 2k+1; centre sxx, syy, weight at 8..10.
 __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double *__restrict__ gx0,
                                                           const double *__restrict__ gy0,
+                                                          const double *__restrict__ wb,
                                                           const double *__restrict__ dxy,
                                                           const double *__restrict__ dxx,
                                                           const double *__restrict__ dyy,
@@ -469,8 +532,9 @@ __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double
     const long long bx = nonneg_bits(mx), by = nonneg_bits(my);
     const int ox = bx > half, oy = by > half;  // the one corner off the midlines
     const double d = dxy[m];
+    const W4 ww = load_w4(wb, m);  // (kx ? mx : 1 - mx) (ky ? my : 1 - my) for corner kx + 2 ky
     {
-      const double w = (ox ? mx : (1.0 - mx)) * (oy ? my : (1.0 - my));
+      const double w = w4_at(ww, ox + 2 * oy);
       double *L = &sloc[2 * (ox + 2 * oy)][t];
       L[0] = L[0] + w * d;
       L[128] = L[128] + w;
@@ -479,7 +543,7 @@ __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double
       for (int k = 0; k < 4; ++k) {
         const int kx = k & 1, ky = k >> 1;
         if ((kx == ox && ky == oy) || (kx != ox && bx != half) || (ky != oy && by != half)) continue;
-        const double w = (kx ? mx : (1.0 - mx)) * (ky ? my : (1.0 - my));
+        const double w = w4_at(ww, k);
         double *L = &sloc[2 * k][t];
         L[0] = L[0] + w * d;
         L[128] = L[128] + w;
@@ -548,13 +612,23 @@ __global__ void k_update_marker_stress(Params P, StressCols c, Geo g, Nodal nd, 
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
   int i, j;
+#ifdef MIC_EXACT
   double mdx, mdy;
   centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], i, j, mdx, mdy);
   const double mdsxx = interp_run(nd.dsxx, P.NX, i, j, mdx, mdy);
   const double mdsyy = interp_run(nd.dsyy, P.NX, i, j, mdx, mdy);
+#else
+  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
+  const double mdsxx = interp_w(nd.dsxx, P.NX, i, j, wc);
+  const double mdsyy = interp_w(nd.dsyy, P.NX, i, j, wc);
+#endif
   c.sxx[m] = c.sxx[m] + mdsxx;
   c.syy[m] = c.syy[m] + mdsyy;
+#ifdef MIC_EXACT
   const double mdsxy = interp_run(nd.dsxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]);
+#else
+  const double mdsxy = interp_w(nd.dsxy, P.NX, cx, cy, load_w4(g.w0, m));
+#endif
   c.sxy[m] = c.sxy[m] + mdsxy;
   if (isnan(mdsxy)) atomicAdd(&st->nan_dsxy, 1ULL);
 }
@@ -575,8 +649,9 @@ __global__ void k_subgridT_markers(Params P, SubTCols c, Geo g, const double *__
   if (i == -1) return;
   const int NX = P.NX;
   const size_t k00 = (size_t)j * NX + i, k10 = k00 + 1, k01 = k00 + NX, k11 = k01 + 1;
-  const double dx = P.x[i + 1] - P.x[i], dy = P.y[j + 1] - P.y[j];
   const double mdx = g.gx0[m], mdy = g.gy0[m];
+#ifdef MIC_EXACT
+  const double dx = P.x[i + 1] - P.x[i], dy = P.y[j + 1] - P.y[j];
   const double Tm = Tn[k00] * (1.0 - mdx) * (1.0 - mdy) + Tn[k10] * mdx * (1.0 - mdy) +
                     Tn[k01] * (1.0 - mdx) * (mdy) + Tn[k11] * mdx * mdy;
   const double rhom = rho0 + rn[k00] * (1.0 - mdx) * (1.0 - mdy) + rn[k10] * (mdx) * (1.0 - mdy) +
@@ -585,12 +660,22 @@ __global__ void k_subgridT_markers(Params P, SubTCols c, Geo g, const double *__
                      cpn[k01] * (1.0 - mdx) * (mdy) + cpn[k11] * mdx * mdy;
   const double km = kn[k00] * (1.0 - mdx) * (1.0 - mdy) + kn[k10] * (mdx) * (1.0 - mdy) +
                     kn[k01] * (1.0 - mdx) * (mdy) + kn[k11] * mdx * mdy;
+#else
+  // the stored corner weights, shared by the four fields (the reference multiplies each value
+  // by both factors in turn; the products agree to rounding)
+  (void)k01;
+  (void)k10;
+  (void)k11;
+  const W4 w = load_w4(g.w0, m);
+  const double Tm = interp_w(Tn, NX, i, j, w);
+  const double rhom = rho0 + interp_w(rn, NX, i, j, w);
+  const double cpm = interp_w(cpn, NX, i, j, w);
+  const double km = interp_w(kn, NX, i, j, w);
+#endif
 #ifdef MIC_EXACT
   const double tdiff = cpm * rhom / km / (2.0 / (dx * dx) + 2.0 / (dy * dy));
   c.dTsub[m] = (Tm - c.T[m]) * (1.0 - exp(-D * dt / tdiff));
 #else
-  (void)dx;
-  (void)dy;
   // -D dt / tdiff with 1/dx^2, 1/dy^2 from the reciprocal tables: one division
   const double ixx = P.ix[i], iyy = P.iy[j];
   const double arg = -D * dt * km * (2.0 * (ixx * ixx + iyy * iyy)) / (cpm * rhom);
@@ -614,9 +699,16 @@ __global__ void k_subgridT_apply(Params P, SubTCols c, Geo g, const double *__re
   if (i == -1) return;
   const size_t k00 = (size_t)j * P.NX + i;
   const double mdx = g.gx0[m], mdy = g.gy0[m];
+#ifdef MIC_EXACT
   const double dtm = (dT[k00] * (1.0 - mdy) * (1.0 - mdx) + dT[k00 + P.NX] * mdy * (1.0 - mdx) +
                       dT[k00 + 1] * (1.0 - mdy) * mdx + dT[k00 + P.NX + 1] * mdy * mdx) +
                      c.dTsub[m];
+#else
+  (void)k00;
+  (void)mdx;
+  (void)mdy;
+  const double dtm = interp_w(dT, P.NX, i, j, load_w4(g.w0, m)) + c.dTsub[m];
+#endif
   c.T[m] = c.T[m] + dtm;
   c.Tdot[m] = dtm / dt;
 }
@@ -822,6 +914,8 @@ Geo geo_of(mic_ctx *ctx) {
   g.gx1 = ctx->geo[2];
   g.gy1 = ctx->geo[3];
   g.flags = ctx->geo_flags;
+  g.w0 = ctx->wgt[0];
+  g.w1 = ctx->wgt[1];
   return g;
 }
 
@@ -1114,7 +1208,8 @@ extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
   if (ctx->n > 0) {
     MIC_KERNEL(ctx, "k_subgrid_partials");
     k_subgrid_partials<<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(
-        ctx->P, ctx->geo[0], ctx->geo[1], ctx->scr0, ctx->scr1, ctx->scr2, ctx->cell_start, ctx->part_b);
+        ctx->P, ctx->geo[0], ctx->geo[1], ctx->wgt[0], ctx->scr0, ctx->scr1, ctx->scr2, ctx->cell_start,
+        ctx->part_b);
   } else {
     MIC_CUDA_TRY(cudaMemsetAsync(ctx->part_b, 0, sizeof(double) * 11 * (size_t)ctx->ncells, ctx->stream));
   }

@@ -23,7 +23,7 @@ namespace {
 __global__ void k_geometry(Params P, const double *__restrict__ X, const double *__restrict__ Y,
                            const int *__restrict__ cellX, const int *__restrict__ cellY, double *__restrict__ gx0,
                            double *__restrict__ gy0, double *__restrict__ gx1, double *__restrict__ gy1,
-                           int *__restrict__ flags, int64_t n) {
+                           int *__restrict__ flags, double *__restrict__ w0, double *__restrict__ w1, int64_t n) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
   const int cx = cellX[m], cy = cellY[m];
@@ -52,6 +52,10 @@ __global__ void k_geometry(Params P, const double *__restrict__ X, const double 
   gx1[m] = mdx1;
   gy1[m] = mdy1;
   flags[m] = f;
+  if (w0) {  // the weights every later interpolation and projection of the step uses
+    store_w4(w0, m, make_w4(mdx0, mdy0));
+    store_w4(w1, m, make_w4(mdx1, mdy1));
+  }
 }
 
 struct All2Out {
@@ -268,6 +272,7 @@ struct PartialView {
   const int *mat;
   const double *gx0, *gy0, *gx1, *gy1;
   const int *flags;
+  const double *w0, *w1;  // stored corner weights of the basic and the cell-centre cell
 };
 
 // ALL2: rho, etaS, k, T, Cp, weight per corner (24) + nearest-node sxy, weight (8) = 32 sums.
@@ -298,9 +303,8 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
   }
   const int mb = qs[4 * c], me = qs[4 * c + 4];
   for (int m = mb; m < me; ++m) {
-    const double mx = v.gx0[m], my = v.gy0[m];
-    const double a = 1.0 - mx, b = 1.0 - my;
-    const double w[4] = {a * b, mx * b, a * my, mx * my};
+    const W4 ww = load_w4(v.w0, m);
+    const double w[4] = {ww.w00, ww.w10, ww.w01, ww.w11};
     if (ALL2) {
       const double r = v.rho[m], e = v.eta[m], tt = v.T[m];
       const int mt = v.mat[m];
@@ -317,7 +321,7 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
       // nearest basic node (mdx0 >= .5, mdy0 >= .5): the weight of that corner, as w[corner]
       const int fl = v.flags[m];
       const int corner = ((fl >> 2) & 1) | (((fl >> 3) & 1) << 1);
-      const double wc = __dmul_rn((corner & 1) ? mx : a, (corner & 2) ? my : b);
+      const double wc = w4_at(ww, corner);
       double *L = &sloc[2 * corner][t];
       L[0] = fma(wc, v.sxy[m], L[0]);
       L[128] = __dadd_rn(L[128], wc);
@@ -383,9 +387,8 @@ __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v
   const int e1 = rn[0], e2 = e1 + rn[1], e3 = e2 + rn[2], total = e3 + rn[3];
   for (int u = 0; u < total; ++u) {
     const int m = (u < e1) ? rb[0] + u : (u < e2) ? rb[1] + (u - e1) : (u < e3) ? rb[2] + (u - e2) : rb[3] + (u - e3);
-    const double mx = v.gx1[m], my = v.gy1[m];
-    const double a = 1.0 - mx, b = 1.0 - my;
-    const double w[4] = {a * b, mx * b, a * my, mx * my};
+    const W4 ww = load_w4(v.w1, m);
+    const double w[4] = {ww.w00, ww.w10, ww.w01, ww.w11};
     const double e = ALL2 ? v.eta[m] : v.scalar[m];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -396,7 +399,7 @@ __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v
       // nearest cell centre (mdx1 >= .5, mdy1 >= .5), weight as w[corner]
       const int fl = v.flags[m];
       const int corner = ((fl >> 4) & 1) | (((fl >> 5) & 1) << 1);
-      const double wc = __dmul_rn((corner & 1) ? mx : a, (corner & 2) ? my : b);
+      const double wc = w4_at(ww, corner);
       double *L = &sloc[3 * corner][t];
       L[0] = fma(wc, v.sxx[m], L[0]);
       L[128] = fma(wc, v.syy[m], L[128]);
@@ -503,7 +506,7 @@ int mic_ensure_geometry(mic_ctx *ctx) {
       k_geometry<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y],
                                                                ctx->i32[C_CELLX], ctx->i32[C_CELLY], ctx->geo[0],
                                                                ctx->geo[1], ctx->geo[2], ctx->geo[3],
-                                                               ctx->geo_flags, ctx->n);
+                                                               ctx->geo_flags, ctx->wgt[0], ctx->wgt[1], ctx->n);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }
@@ -524,6 +527,8 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out) {
     pv.gx1 = ctx->geo[2];
     pv.gy1 = ctx->geo[3];
     pv.flags = ctx->geo_flags;
+    pv.w0 = ctx->wgt[0];
+    pv.w1 = ctx->wgt[1];
     if (stag == 0) {
       {
         MIC_KERNEL(ctx, "k_partials_basic<scalar>");
@@ -616,6 +621,8 @@ extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
   pv.gx1 = mv.gx1;
   pv.gy1 = mv.gy1;
   pv.flags = mv.flags;
+  pv.w0 = ctx->wgt[0];
+  pv.w1 = ctx->wgt[1];
   {
     MIC_KERNEL(ctx, "k_partials_basic");
     k_partials_basic<true><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
