@@ -217,15 +217,32 @@ struct GatherCols {
   int nf;  // double columns moved: the device-only grain column only once grain sizes were set
 };
 
-__global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n) {
+// The gather of every column into the sorted order.  GEO: also the projection geometry of each
+// marker, from the position and cell just gathered: this kernel is bound by HBM and the
+// geometry by the FP64 pipe, so together they cost little more than the gather alone.
+template <bool GEO>
+__global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n, Params P, GeoOut go) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int p = perm[k];
+  double x = 0.0, y = 0.0;
+  int cx = -1, cy = -1;
 #pragma unroll
   for (int c = 0; c < C_F64_COUNT; ++c)
-    if (c < g.nf) g.dst_f[c][k] = g.src_f[c][p];
+    if (c < g.nf) {
+      const double v = g.src_f[c][p];
+      g.dst_f[c][k] = v;
+      if (c == C_X) x = v;
+      if (c == C_Y) y = v;
+    }
 #pragma unroll
-  for (int c = 0; c < C_I32_COUNT; ++c) g.dst_i[c][k] = g.src_i[c][p];
+  for (int c = 0; c < C_I32_COUNT; ++c) {
+    const int v = g.src_i[c][p];
+    g.dst_i[c][k] = v;
+    if (c == C_CELLX) cx = v;
+    if (c == C_CELLY) cy = v;
+  }
+  if (GEO) geometry_marker(P, x, y, cx, cy, go, k);
 }
 
 // perm[k] = device slot of caller marker k (k < n); slots from n on stay in place
@@ -349,7 +366,7 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   }
   {
     MIC_KERNEL(ctx, "k_reorder");
-    k_reorder<<<grid_for(n), kBlock, 0, ctx->stream>>>(g, vin, n);
+    k_reorder<true><<<grid_for(n), kBlock, 0, ctx->stream>>>(g, vin, n, ctx->P, geo_out(ctx));
   }
   MIC_CUDA_TRY(cudaGetLastError());
   for (int c = 0; c < g.nf; ++c) {
@@ -363,7 +380,7 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
     ctx->i32_alt[c] = t;
   }
   ctx->sorted = 1;
-  ctx->geo_valid = 0;
+  ctx->geo_valid = 1;  // computed by the gather
   if (n_out) {
     MIC_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, ctx->stream));
     MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -405,7 +422,7 @@ int mic_restore_caller_order(mic_ctx *ctx) {
   }
   {
     MIC_KERNEL(ctx, "k_reorder");
-    k_reorder<<<grid_for(cap), kBlock, 0, ctx->stream>>>(g, ctx->perm, cap);
+    k_reorder<false><<<grid_for(cap), kBlock, 0, ctx->stream>>>(g, ctx->perm, cap, ctx->P, GeoOut{});
   }
   MIC_CUDA_TRY(cudaGetLastError());
   for (int c = 0; c < g.nf; ++c) {

@@ -305,4 +305,49 @@ __device__ __forceinline__ double interp_run(const double *__restrict__ f, int N
   return s;
 }
 
+// Per-marker projection geometry of one binning: the fractional offsets of the marker in its
+// basic cell and in its cell-centre cell (the divisions of markerProjection.c:127-154, correctly
+// rounded), the quadrant / nearest-node bits, and (product build) the two cells' corner weights.
+struct GeoOut {
+  double *gx0, *gy0, *gx1, *gy1;
+  int *flags;  // bit0 qx, bit1 qy, bit2 mdx0>=.5, bit3 mdy0>=.5, bit4 mdx1>=.5, bit5 mdy1>=.5
+  double *w0, *w1;
+};
+
+__device__ __forceinline__ void geometry_marker(const Params &P, double x, double y, int cx, int cy, const GeoOut &o,
+                                                int64_t m) {
+  if (cx < 0) {
+    o.flags[m] = 0;
+    return;
+  }
+  // basic cell (markerProjection.c:131-146, stagger 0)
+  const double mdx0 = div_sp(x - P.x[cx], P.hx[cx], P.ix[cx]);
+  const double mdy0 = div_sp(y - P.y[cy], P.hy[cy], P.iy[cy]);
+  // cell-centre cell (findCellStag2D stagger -1, markerProjection.c:260-267, 128-143)
+  const int qx = nonneg_bits(x) >= nonneg_bits(P.xc[cx + 1]);
+  const int qy = nonneg_bits(y) >= nonneg_bits(P.yc[cy + 1]);
+  const int sx = cx + qx, sy = cy + qy;
+  const double mdx1 = div_sp(x - P.xc[sx], P.hxc[sx], P.ixc[sx]);
+  const double mdy1 = div_sp(y - P.yc[sy], P.hyc[sy], P.iyc[sy]);
+  const long long half = 0x3FE0000000000000LL;  // bits of 0.5; all offsets here are >= 0
+  int f = qx | (qy << 1);
+  f |= (nonneg_bits(mdx0) >= half) << 2;
+  f |= (nonneg_bits(mdy0) >= half) << 3;
+  f |= (nonneg_bits(mdx1) >= half) << 4;
+  f |= (nonneg_bits(mdy1) >= half) << 5;
+  o.gx0[m] = mdx0;
+  o.gy0[m] = mdy0;
+  o.gx1[m] = mdx1;
+  o.gy1[m] = mdy1;
+  o.flags[m] = f;
+  if (o.w0) {  // the weights every later interpolation and projection of the step uses
+    store_w4(o.w0, m, make_w4(mdx0, mdy0));
+    store_w4(o.w1, m, make_w4(mdx1, mdy1));
+  }
+}
+
+inline GeoOut geo_out(mic_ctx *ctx) {
+  return GeoOut{ctx->geo[0], ctx->geo[1], ctx->geo[2], ctx->geo[3], ctx->geo_flags, ctx->wgt[0], ctx->wgt[1]};
+}
+
 }  // namespace mic

@@ -720,7 +720,7 @@ struct AdvectCols {
 };
 
 // advectMarkersRK (markers.c:1865-2250), non-periodic grid, non-JAUMANN rotation
-__global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, const double *__restrict__ vy,
+__global__ void k_advect(Params P, AdvectCols c, Geo g, const double *__restrict__ vx, const double *__restrict__ vy,
                          const double *__restrict__ wz, mic_bcinfo top, mic_bcinfo left, double dt, int64_t n) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
@@ -763,9 +763,12 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     // vx sits on the basic x lines and vy on the basic y lines: with vxX == i and vyY == j (the
     // walk keeps i, j inside the clamps) their fractions there are the basic cell's mdx, mdy
     // fractions here only weight interpolations (every cell decision above is on integer images),
-    // so one multiply by the tabulated reciprocal, within an ulp of the quotient, stands in for it
-    const double mdx = (xcur - P.x[i]) * P.ix[i];
-    const double mdy = (ycur - P.y[j]) * P.iy[j];
+    // so one multiply by the tabulated reciprocal, within an ulp of the quotient, stands in for it.
+    // The first stage samples at the marker itself, in its stored cell: its fractions are the
+    // binning geometry's (basic cell; the vx cell's y and the vy cell's x fractions are those of
+    // the cell-centre cell, whose stagger tests are the same).
+    const double mdx = (s == 0) ? g.gx0[m] : (xcur - P.x[i]) * P.ix[i];
+    const double mdy = (s == 0) ? g.gy0[m] : (ycur - P.y[j]) * P.iy[j];
 #endif
     double ax = xcur - P.x[vxX];
     double ay = ycur - P.yc[vxY + 1];
@@ -774,7 +777,7 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     double hy = P.yc[vxY + 2] - P.yc[vxY + 1];
 #else
     const double tx = mdx;
-    const double ty = ay * P.iyc[vxY + 1];
+    const double ty = (s == 0) ? g.gy1[m] : ay * P.iyc[vxY + 1];
 #endif
     const size_t r1 = (size_t)(vxY + 1) * NX;
     double vul, vur;
@@ -822,7 +825,7 @@ __global__ void k_advect(Params P, AdvectCols c, const double *__restrict__ vx, 
     t += wll * (1.0 - ax / hx) * (ay / hy);
     t += wlr * (ax * ay) / hx / hy;
 #else
-    t = lerp2(wul, wur, wll, wlr, (xcur - P.xc[vyX + 1]) * P.ixc[vyX + 1], mdy);
+    t = lerp2(wul, wur, wll, wlr, (s == 0) ? g.gx1[m] : (xcur - P.xc[vyX + 1]) * P.ixc[vyX + 1], mdy);
 #endif
     mvy[s] = t;
     const size_t w0 = (size_t)j * NX + i;
@@ -1291,7 +1294,7 @@ extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
 
 extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
   CHECK_CTX();
-  int e = mic_ensure_sorted(ctx);
+  int e = mic_ensure_geometry(ctx);
   if (e) return e;
   if (ctx->n > 0) {
     AdvectCols c;
@@ -1311,7 +1314,8 @@ extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
     c.exy = ctx->f64[C_EXY];
     {
       MIC_KERNEL(ctx, "k_advect");
-      k_advect<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY],
+      k_advect<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX],
+                                                             ctx->nodal[MIC_NF_VY],
                                                              ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
                                                              ctx->bcs.mechBCLeft, dt, ctx->n);
     }

@@ -21,41 +21,10 @@ using namespace mic;
 namespace {
 
 __global__ void k_geometry(Params P, const double *__restrict__ X, const double *__restrict__ Y,
-                           const int *__restrict__ cellX, const int *__restrict__ cellY, double *__restrict__ gx0,
-                           double *__restrict__ gy0, double *__restrict__ gx1, double *__restrict__ gy1,
-                           int *__restrict__ flags, double *__restrict__ w0, double *__restrict__ w1, int64_t n) {
+                           const int *__restrict__ cellX, const int *__restrict__ cellY, GeoOut o, int64_t n) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
-  const int cx = cellX[m], cy = cellY[m];
-  if (cx < 0) {
-    flags[m] = 0;
-    return;
-  }
-  const double x = X[m], y = Y[m];
-  // basic cell (markerProjection.c:131-146, stagger 0)
-  const double mdx0 = div_sp(x - P.x[cx], P.hx[cx], P.ix[cx]);
-  const double mdy0 = div_sp(y - P.y[cy], P.hy[cy], P.iy[cy]);
-  // cell-centre cell (findCellStag2D stagger -1, markerProjection.c:260-267, 128-143)
-  const int qx = nonneg_bits(x) >= nonneg_bits(P.xc[cx + 1]);
-  const int qy = nonneg_bits(y) >= nonneg_bits(P.yc[cy + 1]);
-  const int sx = cx + qx, sy = cy + qy;
-  const double mdx1 = div_sp(x - P.xc[sx], P.hxc[sx], P.ixc[sx]);
-  const double mdy1 = div_sp(y - P.yc[sy], P.hyc[sy], P.iyc[sy]);
-  const long long half = 0x3FE0000000000000LL;  // bits of 0.5; all offsets here are >= 0
-  int f = qx | (qy << 1);
-  f |= (nonneg_bits(mdx0) >= half) << 2;
-  f |= (nonneg_bits(mdy0) >= half) << 3;
-  f |= (nonneg_bits(mdx1) >= half) << 4;
-  f |= (nonneg_bits(mdy1) >= half) << 5;
-  gx0[m] = mdx0;
-  gy0[m] = mdy0;
-  gx1[m] = mdx1;
-  gy1[m] = mdy1;
-  flags[m] = f;
-  if (w0) {  // the weights every later interpolation and projection of the step uses
-    store_w4(w0, m, make_w4(mdx0, mdy0));
-    store_w4(w1, m, make_w4(mdx1, mdy1));
-  }
+  geometry_marker(P, X[m], Y[m], cellX[m], cellY[m], o, m);
 }
 
 struct All2Out {
@@ -504,9 +473,8 @@ int mic_ensure_geometry(mic_ctx *ctx) {
     {
       MIC_KERNEL(ctx, "k_geometry");
       k_geometry<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y],
-                                                               ctx->i32[C_CELLX], ctx->i32[C_CELLY], ctx->geo[0],
-                                                               ctx->geo[1], ctx->geo[2], ctx->geo[3],
-                                                               ctx->geo_flags, ctx->wgt[0], ctx->wgt[1], ctx->n);
+                                                               ctx->i32[C_CELLX], ctx->i32[C_CELLY], geo_out(ctx),
+                                                               ctx->n);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }
