@@ -64,7 +64,9 @@ struct YieldCols {
 };
 
 // One marker of checkPlasticYielding (markers.c:1381-1505).  u_guess: the surrogate's ln s*
-// guess for a law-7 marker (surrogate modes).  Returns whether the marker yielded.
+// guess for a law-7 marker (surrogate modes).  Returns whether the marker yielded.  CREEP false:
+// no material uses law 7, and its solver is left out (fewer registers, more resident warps).
+template <bool CREEP = true>
 __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_materials &M, const mic_options &O,
                                              const CreepConfig &cfg, double dt, int64_t m, double u_guess,
                                              const CreepCoef *kc, Status *st, CreepIn &ci, int &creep_active) {
@@ -89,7 +91,8 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
   double eta, mu;
   ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], u_guess, 0, 0, 0.0, kc != nullptr, {}};
   if (kc) ci.k = *kc;
-  if (!rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)) {
+  if (!(CREEP ? rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)
+              : rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu))) {
     eta = eta_old;
     mu = mu_old;
     atomicAdd(&st->bad_law, 1ULL);
@@ -164,7 +167,7 @@ __device__ __forceinline__ bool creep_marker_features(const YieldCols &c, const 
 }
 
 // checkPlasticYielding, one thread per marker.  MODE 0: exact creep solve; MODE 1: surrogate
-// guess on the CUDA cores (FP32), polish and fallback.
+// guess on the CUDA cores (FP32), polish and fallback; MODE 2: no material uses law 7.
 template <int MODE>
 __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig cfg, double dt, int64_t n,
                         Status *st, CreepCounters *cc) {
@@ -183,9 +186,9 @@ __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig
     CreepCoef k;
     const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, f, &mref);
     if (law7) u = creep_guess_u(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
-    if (yield_marker(c, M, O, cfg, dt, m, u, law7 ? &k : nullptr, st, ci, creep_active)) s_yield = 1;
+    if (yield_marker<MODE != 2>(c, M, O, cfg, dt, m, u, law7 ? &k : nullptr, st, ci, creep_active)) s_yield = 1;
   }
-  creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
+  if (MODE != 2) creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   __syncthreads();
   if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
 }
@@ -527,6 +530,7 @@ __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double
   const long long half = 0x3FE0000000000000LL;
   double sxx = 0.0, syy = 0.0, wn = 0.0;
   const int mb = cs[c], me = cs[c + 1];
+#pragma unroll 4
   for (int m = mb; m < me; ++m) {
     const double mx = gx0[m], my = gy0[m];
     const long long bx = nonneg_bits(mx), by = nonneg_bits(my);
@@ -1025,7 +1029,13 @@ static int yield_launch(mic_ctx *ctx, double dt) {
   MIC_CUDA_TRY(cudaMemsetAsync(ctx->d_creep, 0, sizeof(CreepCounters), ctx->stream));
   if (ctx->n > 0) {
     const int mode = ctx->creep.mlp ? ctx->creep.mode : 0;
-    if (mode == 0) {
+    bool law7 = false;
+    for (int k = 0; k < MIC_MAXMAT; ++k) law7 = law7 || ctx->mat.hasEtaT[k] == 7;
+    if (!law7) {
+      MIC_KERNEL(ctx, "k_yield");
+      k_yield<2><<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
+                                                               dt, ctx->n, ctx->d_status, ctx->d_creep);
+    } else if (mode == 0) {
       MIC_KERNEL(ctx, "k_yield");
       k_yield<0><<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
                                                                dt, ctx->n, ctx->d_status, ctx->d_creep);
