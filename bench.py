@@ -96,6 +96,7 @@ def parse():
     ap.add_argument("--only-systems", action="store_true",
                     help="run only the linear-systems / whole-time-step leg and print it (for profiling the solver)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no mic_autotune)")
     ap.add_argument("--cpu-cores", type=int, default=0, help="host processes for the CPU legs (0 = all)")
     return ap.parse_args()
 
@@ -323,6 +324,8 @@ def run_ours(args):
     for _ in range(args.warmup):
         step()
     G.synchronize()
+    # launch shapes measured on this workload (state restored afterwards; outside the timing)
+    tuning = G.autotune(wl.dt, wl.dt_thermal, subgrid_stress=sub, steps=2) if not args.no_autotune else None
     launches0 = G.launch_count()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -441,6 +444,7 @@ def run_ours(args):
                 "model": "markers resident on the device; host-solve nodal fields up and projected nodal fields "
                          "down every step through mic_nodal_upload/mic_step/mic_nodal_download"},
         "gpu_launches": launches,
+        "launch_tuning": tuning,
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,
                      "traffic": (KERNEL_TRAFFIC_PER_MARKER[top_name] * n if top_name in KERNEL_TRAFFIC_PER_MARKER

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["mic_context.cu", "mic_bin_sort.cu", "mic_project.cu", "mic_marker_passes.cu", "mic_creep.cu",
            "mic_creep_tc.cu", "mic_ensemble.cu", "mic_density.cu", "mic_grid.cu", "mic_io.cu", "mic_systems.cu",
-           "mic_band_lu.cu", "mic_timestep.cu"]
+           "mic_band_lu.cu", "mic_timestep.cu", "mic_autotune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 VARIANTS = {"libmic_gb300.so": ["-fmad=true"], "libmic_gb300_exact.so": ["-fmad=false", "-DMIC_EXACT=1"]}
 

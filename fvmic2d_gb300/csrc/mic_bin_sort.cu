@@ -313,7 +313,7 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   }
   {
     MIC_KERNEL(ctx, "k_find_cells");
-    k_find_cells<<<grid_for(n), kBlock, 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y], ctx->i32[C_CELLX],
+    k_find_cells<<<grid_for(n, tuned_block(ctx, TU_FIND_CELLS)), tuned_block(ctx, TU_FIND_CELLS), 0, ctx->stream>>>(ctx->P, ctx->f64[C_X], ctx->f64[C_Y], ctx->i32[C_CELLX],
                                                           ctx->i32[C_CELLY], ctx->i32[C_CPU], ctx->key, n,
                                                           ctx->d_status);
   }
@@ -366,7 +366,8 @@ int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out) {
   }
   {
     MIC_KERNEL(ctx, "k_reorder");
-    k_reorder<true><<<grid_for(n), kBlock, 0, ctx->stream>>>(g, vin, n, ctx->P, geo_out(ctx));
+    k_reorder<true><<<grid_for(n, tuned_block(ctx, TU_REORDER)), tuned_block(ctx, TU_REORDER), 0, ctx->stream>>>(
+        g, vin, n, ctx->P, geo_out(ctx));
   }
   MIC_CUDA_TRY(cudaGetLastError());
   for (int c = 0; c < g.nf; ++c) {

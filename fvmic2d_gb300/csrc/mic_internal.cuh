@@ -156,6 +156,7 @@ struct mic_ctx {
   int last_error;
   // launch accounting and optional per-launch CUDA-event timing
   long long launches;
+  int tune_bs[16];  // launch block size per tuned kernel (TuneId); 0 = kBlock
   int prof_on;
   int prof_n, prof_cap;
   const char **prof_name;
@@ -210,7 +211,28 @@ namespace mic {
 
 constexpr int kBlock = 256;
 
-inline unsigned grid_for(int64_t n, int block = kBlock) {
+// Marker-parallel kernels whose block size mic_autotune picks (each uses at most 96 registers,
+// so every candidate up to 512 threads fits an SM's register file).
+enum TuneId {
+  TU_ADVECT = 0,
+  TU_STRAIN,
+  TU_YIELD,
+  TU_SUBGRID_STRESS,
+  TU_UPDATE_STRESS,
+  TU_SUBGRID_T,
+  TU_SUBGRID_T_APPLY,
+  TU_REORDER,
+  TU_FIND_CELLS,
+  TU_UPDATE_RHO,
+  TU_COUNT
+};
+
+inline unsigned grid_for(int64_t n, int block = kBlock);
+inline int tuned_block(const mic_ctx *ctx, int id) {
+  const int b = ctx->tune_bs[id];
+  return b > 0 ? b : kBlock;
+}
+inline unsigned grid_for(int64_t n, int block) {
   int64_t g = (n + block - 1) / block;
   return (unsigned)(g < 1 ? 1 : g);
 }

@@ -1002,7 +1002,7 @@ extern "C" int mic_update_marker_rho(mic_ctx *ctx) {
   if (ctx->n == 0) return MIC_OK;
   {
     MIC_KERNEL(ctx, "k_update_rho");
-    k_update_rho<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
+    k_update_rho<<<grid_for(ctx->n, tuned_block(ctx, TU_UPDATE_RHO)), tuned_block(ctx, TU_UPDATE_RHO), 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
                                                                ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n);
   }
   MIC_CUDA_TRY(cudaGetLastError());
@@ -1033,11 +1033,11 @@ static int yield_launch(mic_ctx *ctx, double dt) {
     for (int k = 0; k < MIC_MAXMAT; ++k) law7 = law7 || ctx->mat.hasEtaT[k] == 7;
     if (!law7) {
       MIC_KERNEL(ctx, "k_yield");
-      k_yield<2><<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
+      k_yield<2><<<grid_for(ctx->n, tuned_block(ctx, TU_YIELD)), tuned_block(ctx, TU_YIELD), 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
                                                                dt, ctx->n, ctx->d_status, ctx->d_creep);
     } else if (mode == 0) {
       MIC_KERNEL(ctx, "k_yield");
-      k_yield<0><<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
+      k_yield<0><<<grid_for(ctx->n, tuned_block(ctx, TU_YIELD)), tuned_block(ctx, TU_YIELD), 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
                                                                dt, ctx->n, ctx->d_status, ctx->d_creep);
     } else if (mode == 1) {
       MIC_KERNEL(ctx, "k_yield_surrogate_fp32");
@@ -1114,7 +1114,7 @@ static int strain_launch(mic_ctx *ctx, double dt) {
   c.srr = ctx->f64[C_SRR];
   {
     MIC_KERNEL(ctx, "k_strain_pressure");
-    k_strain_pressure<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n,
+    k_strain_pressure<<<grid_for(ctx->n, tuned_block(ctx, TU_STRAIN)), tuned_block(ctx, TU_STRAIN), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n,
                                                                     ctx->d_status);
   }
   MIC_CUDA_TRY(cudaGetLastError());
@@ -1203,7 +1203,7 @@ extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
     c.dyy = ctx->scr2;
     {
       MIC_KERNEL(ctx, "k_subgrid_stress_markers");
-      k_subgrid_stress_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
+      k_subgrid_stress_markers<<<grid_for(ctx->n, tuned_block(ctx, TU_SUBGRID_STRESS)), tuned_block(ctx, TU_SUBGRID_STRESS), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
                                                                              D, ctx->n);
     }
     MIC_CUDA_TRY(cudaGetLastError());
@@ -1252,7 +1252,7 @@ static int stress_launch(mic_ctx *ctx) {
   c.sxy = ctx->f64[C_SXY];
   {
     MIC_KERNEL(ctx, "k_update_marker_stress");
-    k_update_marker_stress<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), ctx->n,
+    k_update_marker_stress<<<grid_for(ctx->n, tuned_block(ctx, TU_UPDATE_STRESS)), tuned_block(ctx, TU_UPDATE_STRESS), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), ctx->n,
                                                                          ctx->d_status);
   }
   MIC_CUDA_TRY(cudaGetLastError());
@@ -1277,7 +1277,7 @@ extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
   if (ctx->n > 0) {
     {
       MIC_KERNEL(ctx, "k_subgridT_markers");
-      k_subgridT_markers<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(
+      k_subgridT_markers<<<grid_for(ctx->n, tuned_block(ctx, TU_SUBGRID_T)), tuned_block(ctx, TU_SUBGRID_T), 0, ctx->stream>>>(
           ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_LASTT], ctx->nodal[MIC_NF_RHO], ctx->nodal[MIC_NF_CP],
           ctx->nodal[MIC_NF_KTHERMAL], ctx->mat.materialRho[0], ctx->opt.subgridTemperatureDiffusivity, dt, ctx->n);
     }
@@ -1294,7 +1294,7 @@ extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
   if (ctx->n > 0) {
     {
       MIC_KERNEL(ctx, "k_subgridT_apply");
-      k_subgridT_apply<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->node_scr[1], dt,
+      k_subgridT_apply<<<grid_for(ctx->n, tuned_block(ctx, TU_SUBGRID_T_APPLY)), tuned_block(ctx, TU_SUBGRID_T_APPLY), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->node_scr[1], dt,
                                                                      ctx->n);
     }
     MIC_CUDA_TRY(cudaGetLastError());
@@ -1324,7 +1324,7 @@ extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
     c.exy = ctx->f64[C_EXY];
     {
       MIC_KERNEL(ctx, "k_advect");
-      k_advect<<<grid_for(ctx->n), kBlock, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX],
+      k_advect<<<grid_for(ctx->n, tuned_block(ctx, TU_ADVECT)), tuned_block(ctx, TU_ADVECT), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX],
                                                              ctx->nodal[MIC_NF_VY],
                                                              ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
                                                              ctx->bcs.mechBCLeft, dt, ctx->n);

@@ -67,6 +67,9 @@ SIGNATURES = {
     "mic_launch_count": (_I, [_P, _I64P]),
     "mic_profile_enable": (_I, [_P, _I]),
     "mic_profile_read": (_I, [_P, _I, _P, _DP, _I64P, _IP]),
+    "mic_autotune": (_I, [_P, _D, _D, _I, _I, _IP]),
+    "mic_get_tuning": (_I, [_P, _IP, _I]),
+    "mic_set_tuning": (_I, [_P, _IP, _I]),
     "mic_bin_sort_noalloc": (_I, [_P, _P, _I64, _P, _P, _I, _I, _D, _D, _P, _P, _P, _P, _P, _I64P]),
     "mic_creep_configure": (_I, [_P, _I, _D, _I, _I, _D]),
     "mic_markers_set_grain_size": (_I, [_P, _DP, _I64]),
@@ -159,6 +162,11 @@ class Status(ctypes.Structure):
 
 def _dp(a):
     return a.ctypes.data_as(_DP)
+
+
+# kernels whose launch block size mic_autotune picks, in the library's MIC_TUNE_* order
+TUNE_KERNELS = ["k_advect", "k_strain_pressure", "k_yield", "k_subgrid_stress_markers", "k_update_marker_stress",
+                "k_subgridT_markers", "k_subgridT_apply", "k_reorder", "k_find_cells", "k_update_rho"]
 
 
 class MicProblem:
@@ -408,6 +416,25 @@ class MicProblem:
         n = ctypes.c_int64(0)
         self._check(self.L.mic_launch_count(self.h, ctypes.byref(n)), "mic_launch_count")
         return n.value
+
+    def autotune(self, dt_disp, dt_thermal, subgrid_stress=1, steps=2):
+        """mic_autotune: per-kernel block sizes measured on this workload; state left unchanged.
+        Returns {kernel: block size}."""
+        out = (ctypes.c_int * len(TUNE_KERNELS))()
+        self._check(self.L.mic_autotune(self.h, dt_disp, dt_thermal, int(subgrid_stress), steps, out),
+                    "mic_autotune")
+        return dict(zip(TUNE_KERNELS, list(out)))
+
+    def tuning(self):
+        out = (ctypes.c_int * len(TUNE_KERNELS))()
+        self._check(self.L.mic_get_tuning(self.h, out, len(TUNE_KERNELS)), "mic_get_tuning")
+        return dict(zip(TUNE_KERNELS, list(out)))
+
+    def set_tuning(self, blocks):
+        """blocks: {kernel: size} (sizes 0, 128, 256 or 512; 0 = default) or a list in kernel order"""
+        vals = [int(blocks.get(k, 0)) for k in TUNE_KERNELS] if isinstance(blocks, dict) else [int(b) for b in blocks]
+        arr = (ctypes.c_int * len(vals))(*vals)
+        self._check(self.L.mic_set_tuning(self.h, arr, len(vals)), "mic_set_tuning")
 
     def profile_enable(self, capacity):
         self._check(self.L.mic_profile_enable(self.h, capacity), "mic_profile_enable")

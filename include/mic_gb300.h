@@ -192,6 +192,30 @@ int mic_launch_count(mic_ctx *ctx, int64_t *launches);
 /* per-launch CUDA-event timing on the context stream: enable with a record capacity (0 turns it
  * off); read aggregates by kernel name (names: max * 48 bytes) */
 int mic_profile_enable(mic_ctx *ctx, int capacity);
+/* Launch shapes (new; the reference has no counterpart).  The marker-parallel kernels of a step
+ * each launch with one block size.  mic_autotune measures 128, 256 and 512 threads for each on
+ * this context's workload: it saves the marker columns and nodal fields, runs for every candidate
+ * one untimed and `steps` timed mic_step calls (dt_disp, dt_thermal, subgrid_stress as mic_step)
+ * from the saved state, keeps per kernel the fastest size, and puts the saved state back, so the
+ * simulation is where it was.  chosen (MIC_TUNE_COUNT ints, may be NULL) receives the sizes.
+ * Results of a step do not depend on the sizes.  mic_get_tuning / mic_set_tuning read and set
+ * them (0 = the default, 256), e.g. to reuse one tuning for many contexts of one workload. */
+enum {
+  MIC_TUNE_ADVECT = 0,
+  MIC_TUNE_STRAIN,
+  MIC_TUNE_YIELD,
+  MIC_TUNE_SUBGRID_STRESS,
+  MIC_TUNE_UPDATE_STRESS,
+  MIC_TUNE_SUBGRID_T,
+  MIC_TUNE_SUBGRID_T_APPLY,
+  MIC_TUNE_REORDER,
+  MIC_TUNE_FIND_CELLS,
+  MIC_TUNE_UPDATE_RHO,
+  MIC_TUNE_COUNT
+};
+int mic_autotune(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, int steps, int *chosen);
+int mic_get_tuning(mic_ctx *ctx, int *block, int count);
+int mic_set_tuning(mic_ctx *ctx, const int *block, int count);
 int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64_t *counts, int *nkernels);
 /* ---- marker lifecycle (markers.c:15-39, 255-400) ----
  * resetMarkers: every slot of the capacity gets resetMarker's values (X = Y = -1, Mat = -1, the
