@@ -591,6 +591,28 @@ def ensemble_leg(args, local):
         out[label] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
                       "kernels_per_step": (l1 - l0) / steps}
     out["speedup_graph_vs_sequential"] = out["graph"]["value"] / out["sequential"]["value"]
+    # members' launch shapes and the issue order of their steps from mic_ensemble_autotune (state
+    # restored by it), then the captured steps timed again
+    E.synchronize()
+    t_tune = time.perf_counter()
+    order = E.autotune(dts, dts, 1, steps=2)
+    t_tune = time.perf_counter() - t_tune
+    sizes = [members[i].n for i in order]
+    for _ in range(3):
+        E.step(dts, dts, 1, True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(es)
+    for _ in range(steps):
+        E.step(dts, dts, 1, True)
+    ev1.record(es)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    out["graph_tuned"] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
+                          "tune_seconds": t_tune,
+                          "order": ("largest first" if sizes == sorted(sizes, reverse=True) else
+                                    "smallest first" if sizes == sorted(sizes) else "as given"),
+                          "member_blocks_k_advect": sorted(set(P.tuning()["k_advect"] for P in members))}
     E.close()
     for P in members:
         P.close()

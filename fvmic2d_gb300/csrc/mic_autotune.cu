@@ -9,6 +9,7 @@
 // simulation where it was; the choices stay in the context (mic_get_tuning / mic_set_tuning
 // carry them to another context of the same workload).
 #include <cstring>
+#include <new>
 #include <vector>
 
 #include "mic_internal.cuh"
@@ -83,6 +84,25 @@ int tuned_times(mic_ctx *ctx, double *t) {
 }
 
 }  // namespace
+
+// saved marker columns and nodal fields of a context (ensemble tuning)
+int mic_state_save(mic_ctx *ctx, void **handle) {
+  Snapshot *s = new (std::nothrow) Snapshot;
+  if (!s) return MIC_ERR_NOMEM;
+  const int e = snapshot_take(ctx, *s);
+  if (e) {
+    delete s;
+    return e;
+  }
+  *handle = s;
+  return MIC_OK;
+}
+int mic_state_restore(mic_ctx *ctx, void *handle) { return snapshot_restore(ctx, *(Snapshot *)handle); }
+void mic_state_free(void *handle) {
+  if (!handle) return;
+  snapshot_free(*(Snapshot *)handle);
+  delete (Snapshot *)handle;
+}
 
 extern "C" int mic_autotune(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, int steps,
                             int *chosen) {

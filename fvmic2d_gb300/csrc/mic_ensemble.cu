@@ -12,6 +12,7 @@
 // replays alternate between them while the host keeps each member's column pointers in step.
 // A graph is re-captured when a member's settings change (materials, options, boundary values,
 // creep configuration, marker count: the member's generation counter) or the time steps do.
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -34,6 +35,7 @@ struct mic_ensemble {
   int key_sub;
   long long graph_kernels[2];  // kernel launches inside each graph
   long long launches;          // kernel launches issued through this ensemble
+  std::vector<int> order;      // members in the order their steps are issued (and captured)
 };
 
 namespace {
@@ -47,7 +49,8 @@ int fail(cudaError_t e) {
 int issue(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub) {
   cudaError_t ce = cudaEventRecord(E->fork, E->stream);
   if (ce != cudaSuccess) return fail(ce);
-  for (int i = 0; i < E->n; ++i) {
+  for (int k = 0; k < E->n; ++k) {
+    const int i = E->order[k];
     mic_ctx *c = E->m[i];
     if ((ce = cudaStreamWaitEvent(c->stream, E->fork, 0)) != cudaSuccess) return fail(ce);
     const long long l0 = c->launches;
@@ -154,6 +157,8 @@ extern "C" int mic_ensemble_create(mic_ensemble **out, mic_ctx *const *members, 
   E->n = n_members;
   E->m.assign(members, members + n_members);
   E->join.assign(n_members, nullptr);
+  E->order.resize(n_members);
+  for (int i = 0; i < n_members; ++i) E->order[i] = i;
   cudaSetDevice(E->device);
   bool ok = cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&E->fork, cudaEventDisableTiming) == cudaSuccess;
@@ -233,5 +238,69 @@ extern "C" int mic_ensemble_launch_count(mic_ensemble *E, int64_t *launches, int
 extern "C" int mic_ensemble_get_stream(mic_ensemble *E, void **stream) {
   if (!E || !stream) return MIC_ERR_ARG;
   *stream = (void *)E->stream;
+  return MIC_OK;
+}
+
+// Launch shapes and the member schedule, measured on the ensemble's own members: each member's
+// kernels get their block sizes from mic_autotune (member by member), then the order in which
+// the members' steps are issued into the step (and its captured graphs) is chosen among: as
+// given, largest member first, smallest first, by timing `steps` pairs of graph replays of each
+// from the same saved state.  Every member's state is put back at the end.  order_out (n ints,
+// may be NULL) receives the chosen order.
+extern "C" int mic_ensemble_autotune(mic_ensemble *E, const double *dt_disp, const double *dt_thermal,
+                                     int subgrid_stress, int steps, int *order_out) {
+  if (!E || !dt_disp || !dt_thermal || steps < 0) return MIC_ERR_ARG;
+  cudaSetDevice(E->device);
+  if (steps == 0) steps = 1;
+  int e = MIC_OK;
+  for (int i = 0; i < E->n && !e; ++i) e = mic_autotune(E->m[i], dt_disp[i], dt_thermal[i], subgrid_stress, 1, nullptr);
+  if (e) return e;
+  std::vector<void *> saved(E->n, nullptr);
+  for (int i = 0; i < E->n && !e; ++i) e = mic_state_save(E->m[i], &saved[i]);
+  std::vector<std::vector<int>> cand(3, E->order);
+  for (int i = 0; i < E->n; ++i) cand[0][i] = i;
+  cand[1] = cand[0];
+  std::stable_sort(cand[1].begin(), cand[1].end(), [&](int a, int b) { return E->m[a]->n > E->m[b]->n; });
+  cand[2] = cand[0];
+  std::stable_sort(cand[2].begin(), cand[2].end(), [&](int a, int b) { return E->m[a]->n < E->m[b]->n; });
+  const std::vector<int> before = E->order;
+  int best = -1;
+  float best_ms = 0.f;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (!e && (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)) e = MIC_ERR_CUDA;
+  for (int c = 0; c < (int)cand.size() && !e; ++c) {
+    E->order = cand[c];
+    drop_graphs(E);
+    for (int i = 0; i < E->n && !e; ++i) e = mic_state_restore(E->m[i], saved[i]);
+    if (e) break;
+    for (int w = 0; w < 3 && !e; ++w) e = mic_ensemble_step(E, dt_disp, dt_thermal, subgrid_stress, 1);  // capture
+    if (e) break;
+    if (cudaEventRecord(t0, E->stream) != cudaSuccess) e = MIC_ERR_CUDA;
+    for (int s = 0; s < 2 * steps && !e; ++s) e = mic_ensemble_step(E, dt_disp, dt_thermal, subgrid_stress, 1);
+    if (e) break;
+    float ms = 0.f;
+    if (cudaEventRecord(t1, E->stream) != cudaSuccess || cudaEventSynchronize(t1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) {
+      e = MIC_ERR_CUDA;
+      break;
+    }
+    if (best < 0 || ms < best_ms) {
+      best = c;
+      best_ms = ms;
+    }
+  }
+  if (t0) cudaEventDestroy(t0);
+  if (t1) cudaEventDestroy(t1);
+  drop_graphs(E);
+  E->order = (!e && best >= 0) ? cand[best] : before;
+  int e2 = MIC_OK;
+  for (int i = 0; i < E->n; ++i) {
+    if (saved[i] && !e2) e2 = mic_state_restore(E->m[i], saved[i]);
+    if (cudaStreamSynchronize(E->m[i]->stream) != cudaSuccess && !e2) e2 = MIC_ERR_CUDA;
+    mic_state_free(saved[i]);
+  }
+  if (e || e2) return e ? e : e2;
+  if (order_out)
+    for (int k = 0; k < E->n; ++k) order_out[k] = E->order[k];
   return MIC_OK;
 }

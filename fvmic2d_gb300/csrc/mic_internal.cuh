@@ -191,6 +191,10 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out);
 void mic_invalidate_sort(mic_ctx *ctx);
 int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out);
 int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry
+// copies of a context's marker columns and nodal fields, put back by mic_state_restore
+int mic_state_save(mic_ctx *ctx, void **handle);
+int mic_state_restore(mic_ctx *ctx, void *handle);
+void mic_state_free(void *handle);
 int mic_f64_column_of_offset(int byte_offset);
 // exclusive prefix sum in place on the context stream, and the scratch it needs (mic_bin_sort.cu)
 int mic_scan_exclusive(mic_ctx *ctx, int *data, int64_t len, int *aux);

@@ -88,6 +88,7 @@ SIGNATURES = {
     "mic_ensemble_create": (_I, [ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
     "mic_ensemble_destroy": (_I, [_P]),
     "mic_ensemble_step": (_I, [_P, _DP, _DP, _I, _I]),
+    "mic_ensemble_autotune": (_I, [_P, _DP, _DP, _I, _I, _IP]),
     "mic_ensemble_synchronize": (_I, [_P]),
     "mic_ensemble_launch_count": (_I, [_P, _I64P, _I64P]),
     "mic_ensemble_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
@@ -637,6 +638,19 @@ class MicEnsemble:
         if code:
             raise MicError(code, "mic_ensemble_create")
         self.h = h
+
+    def autotune(self, dt_disp=None, dt_thermal=None, subgrid_stress=1, steps=2):
+        """mic_ensemble_autotune: members' launch shapes and the issue order of their steps;
+        member states left unchanged.  Returns the order."""
+        n = len(self.members)
+        dd = np.ascontiguousarray(dt_disp if dt_disp is not None else [m.wl.dt for m in self.members], dtype=np.float64)
+        dth = np.ascontiguousarray(dt_thermal if dt_thermal is not None else [m.wl.dt_thermal for m in self.members],
+                                   dtype=np.float64)
+        out = (ctypes.c_int * n)()
+        code = self.L.mic_ensemble_autotune(self.h, _dp(dd), _dp(dth), subgrid_stress, steps, out)
+        if code:
+            raise MicError(code, "mic_ensemble_autotune")
+        return list(out)
 
     def step(self, dt_disp=None, dt_thermal=None, subgrid_stress=1, graph=True):
         n = len(self.members)

@@ -371,6 +371,12 @@ int mic_ensemble_destroy(mic_ensemble *ens);
 int mic_ensemble_step(mic_ensemble *ens, const double *dt_disp, const double *dt_thermal, int subgrid_stress,
                       int use_graph);
 int mic_ensemble_synchronize(mic_ensemble *ens);
+/* Launch shapes and member schedule measured on the ensemble (new): mic_autotune on every member,
+ * then the order in which member steps are issued (as given, largest first, smallest first) that
+ * gives the fastest captured step, timed over 2 x steps graph replays from saved member states.
+ * Every member's state is restored; order_out (n_members ints, may be NULL) receives the order. */
+int mic_ensemble_autotune(mic_ensemble *ens, const double *dt_disp, const double *dt_thermal, int subgrid_stress,
+                          int steps, int *order_out);
 /* kernels issued through the ensemble so far, and kernels inside one captured step */
 int mic_ensemble_launch_count(mic_ensemble *ens, int64_t *launches, int64_t *graph_kernels);
 int mic_ensemble_get_stream(mic_ensemble *ens, void **stream);

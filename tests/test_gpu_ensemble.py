@@ -99,3 +99,31 @@ def test_ensemble_matches_members_stepped_alone(graph):
     if graph:
         assert per_graph >= 25 * len(A)
     E.close()
+
+
+def test_ensemble_autotune_keeps_states_and_results():
+    """mic_ensemble_autotune tunes every member and picks an issue order by timing graph replays
+    from saved states: the members' states are those from before the call, and stepping on gives
+    the members' results stepped alone, bit for bit"""
+    wls = _members(40)
+    A = _setup(wls)
+    B = _setup(wls)
+    E = gpu.MicEnsemble(A)
+    dts = np.array([wl.dt for wl in wls])
+    E.step(dts, dts, subgrid_stress=1, graph=True)
+    for b, dt in zip(B, dts):
+        b.step(dt, dt, True)
+    E.synchronize()
+    before = [_bytes(a.markers) for a in A]
+    order = E.autotune(dts, dts, subgrid_stress=1, steps=1)
+    assert sorted(order) == list(range(len(A)))
+    for a, m in zip(A, before):
+        assert np.array_equal(_bytes(a.markers), m)
+    for _ in range(3):
+        E.step(dts, dts, subgrid_stress=1, graph=True)
+        for b, dt in zip(B, dts):
+            b.step(dt, dt, True)
+    E.synchronize()
+    for a, b in zip(A, B):
+        assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
+        assert np.array_equal(a.get_nodal("lastT"), b.get_nodal("lastT"))
