@@ -71,10 +71,10 @@ __device__ __forceinline__ void creep_rate_p(const CreepCoef &k, double p, doubl
   const double p2 = p * p, p4 = p2 * p2, p5 = p4 * p, p8 = p4 * p4, p9 = p8 * p, p12 = p8 * p4;
   const double p20 = p12 * p8;
   const double td = k.C * 1e6 * p5, tg = k.G * p9, tb = k.B * p12, tl = k.D * p20;
-  const double sum = tg + tb;
-  const double tc = tg * tb / sum;  // (1/tb + 1/tg)^-1
+  const double isum = 1.0 / (tg + tb);  // one division for the series term and its derivative
+  const double tc = tg * tb * isum;      // (1/tb + 1/tg)^-1
   f = td + tc + tl;
-  df = td + tc * (2.4 * tg + 1.8 * tb) / sum + 4.0 * tl;
+  df = td + tc * (2.4 * tg + 1.8 * tb) * isum + 4.0 * tl;
 }
 
 // ln r for the Newton function, with the series near 1 (no log call in the final iterations)
@@ -92,11 +92,12 @@ __device__ __forceinline__ int creep_newton(const CreepCoef &k, double edot, dou
                                             double tol, int maxit, double &res) {
   int it = 0;
   res = 1.0;
+  const double iedot = 1.0 / edot;  // once per marker, not per iteration
   for (; it < maxit; ++it) {
     const double p = exp(0.2 * (u - kLn1e6));
     double f, df;
     creep_rate_p(k, p, f, df);
-    const double r = f / edot;
+    const double r = f * iedot;
     res = r - 1.0;
     if (fabs(res) <= tol) break;
     if (res > 0.0)
