@@ -346,12 +346,15 @@ def run_ours(args):
     ms_total = ev0.elapsed_time(ev1)
     # the same steps again with an event pair around every launch, for the per-kernel durations
     # (kept out of the headline timing above: the extra event records ride on the stream)
-    G.profile_enable(max(64, 40 * args.steps))
+    G.profile_enable(max(64, 64 * args.steps))  # room for every launch (44 per step)
     for _ in range(args.steps):
         step()
     G.synchronize()
     prof = G.profile_read()
     G.profile_enable(0)
+    recorded = sum(v[1] for v in prof.values())
+    if recorded != launches:  # a truncated record would understate every per-step figure
+        raise RuntimeError("per-launch profile holds %d of %d launches" % (recorded, launches))
     t_max = max_over_ranks(pg, ms_total)
     markers_all = sum_over_ranks(pg, float(n * args.steps))
     value = markers_all / (t_max * 1e-3)
