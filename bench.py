@@ -377,14 +377,15 @@ def run_ours(args):
         a = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_double)), shape=(nodes,))
         down_bufs.append((NF[name], p, a))
     res = ctypes.c_double(0.0)
-    DP = ctypes.POINTER(ctypes.c_double)
+    up_f = (ctypes.c_int * len(up_bufs))(*[fid for fid, _, _ in up_bufs])
+    up_p = (ctypes.c_void_p * len(up_bufs))(*[p.value for _, p, _ in up_bufs])
+    dn_f = (ctypes.c_int * len(down_bufs))(*[fid for fid, _, _ in down_bufs])
+    dn_p = (ctypes.c_void_p * len(down_bufs))(*[p.value for _, p, _ in down_bufs])
 
     def e2e_step():
-        for fid, p, _ in up_bufs:
-            assert L.mic_nodal_upload(h, fid, ctypes.cast(p, DP)) == 0
+        assert L.mic_nodal_upload_many(h, up_f, up_p, len(up_bufs)) == 0
         assert L.mic_step(h, wl.dt, wl.dt_thermal, sub, ctypes.byref(res)) == 0
-        for fid, p, _ in down_bufs:
-            assert L.mic_nodal_download(h, fid, ctypes.cast(p, DP)) == 0
+        assert L.mic_nodal_download_many(h, dn_f, dn_p, len(down_bufs)) == 0
 
     e2e_steps = max(3, min(args.steps, 50))
     e2e_step()
@@ -447,7 +448,8 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "markers/s",
                 "h2d_bytes_per_step": len(E2E_UP) * nodes * 8, "d2h_bytes_per_step": len(E2E_DOWN) * nodes * 8 + 8,
                 "model": "markers resident on the device; host-solve nodal fields up and projected nodal fields "
-                         "down every step through mic_nodal_upload/mic_step/mic_nodal_download"},
+                         "down every step from/to pinned host buffers through mic_nodal_upload_many / mic_step / "
+                         "mic_nodal_download_many"},
         "gpu_launches": launches,
         "launch_tuning": tuning,
         "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

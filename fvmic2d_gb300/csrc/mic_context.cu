@@ -491,6 +491,84 @@ extern "C" int mic_nodal_download(mic_ctx *ctx, int f, double *host) {
   return MIC_OK;
 }
 
+// ---- batched nodal transfers --------------------------------------------------------
+//
+// Several fields in one call with one synchronization.  When every host buffer is pinned (so the
+// device can address it: on Grace-Blackwell over the coherent NVLink-C2C link), one kernel moves
+// all of them, element by element, instead of one copy per field; otherwise one asynchronous copy
+// per field.
+constexpr int kMaxBatch = 32;
+struct NodalBatch {
+  const double *src[kMaxBatch];
+  double *dst[kMaxBatch];
+};
+
+__global__ void k_nodal_batch(NodalBatch b, int count, int64_t nn) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nn * count) return;
+  const int f = (int)(t / nn);
+  const int64_t q = t - (int64_t)f * nn;
+  b.dst[f][q] = b.src[f][q];
+}
+
+namespace {
+
+// the device address of a host buffer the device can access directly, else null
+const void *device_view(const void *host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();  // an unregistered pointer: not an error for the caller
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return a.devicePointer;
+}
+
+int nodal_batch(mic_ctx *ctx, const int *fields, const double *const *host_in, double *const *host_out, int count) {
+  if (!ctx || !fields || count < 0 || count > kMaxBatch || (!host_in && !host_out)) return MIC_ERR_ARG;
+  for (int k = 0; k < count; ++k) {
+    if (fields[k] < 0 || fields[k] >= MIC_NF_COUNT) return MIC_ERR_ARG;
+    if (host_in ? !host_in[k] : !host_out[k]) return MIC_ERR_ARG;
+  }
+  if (count == 0) return MIC_OK;
+  cudaSetDevice(ctx->device);
+  const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
+  NodalBatch b;
+  bool direct = true;
+  for (int k = 0; k < count && direct; ++k) {
+    const void *v = device_view(host_in ? (const void *)host_in[k] : (const void *)host_out[k]);
+    if (!v) {
+      direct = false;
+      break;
+    }
+    b.src[k] = host_in ? (const double *)v : ctx->nodal[fields[k]];
+    b.dst[k] = host_in ? ctx->nodal[fields[k]] : (double *)v;
+  }
+  if (direct) {
+    MIC_KERNEL(ctx, host_in ? "k_nodal_batch_up" : "k_nodal_batch_down");
+    k_nodal_batch<<<grid_for(nn * count), kBlock, 0, ctx->stream>>>(b, count, nn);
+  } else {
+    for (int k = 0; k < count; ++k)
+      MIC_CUDA_TRY(host_in ? cudaMemcpyAsync(ctx->nodal[fields[k]], host_in[k], sizeof(double) * nn,
+                                             cudaMemcpyHostToDevice, ctx->stream)
+                           : cudaMemcpyAsync(host_out[k], ctx->nodal[fields[k]], sizeof(double) * nn,
+                                             cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return MIC_OK;
+}
+
+}  // namespace
+
+extern "C" int mic_nodal_upload_many(mic_ctx *ctx, const int *fields, const double *const *host, int count) {
+  return nodal_batch(ctx, fields, host, nullptr, count);
+}
+
+extern "C" int mic_nodal_download_many(mic_ctx *ctx, const int *fields, double *const *host, int count) {
+  return nodal_batch(ctx, fields, nullptr, host, count);
+}
+
 extern "C" int mic_nodal_device_ptr(mic_ctx *ctx, int f, double **dev) {
   if (!ctx || !dev || f < 0 || f >= MIC_NF_COUNT) return MIC_ERR_ARG;
   *dev = ctx->nodal[f];

@@ -36,6 +36,8 @@ SIGNATURES = {
     "mic_markers_download": (_I, [_P, _P, _I64]),
     "mic_markers_count": (_I, [_P, _I64P]),
     "mic_nodal_upload": (_I, [_P, _I, _DP]),
+    "mic_nodal_upload_many": (_I, [_P, _IP, _P, _I]),
+    "mic_nodal_download_many": (_I, [_P, _IP, _P, _I]),
     "mic_nodal_download": (_I, [_P, _I, _DP]),
     "mic_nodal_device_ptr": (_I, [_P, _I, ctypes.POINTER(_DP)]),
     "mic_find_marker_cells": (_I, [_P, _I64P]),

@@ -80,6 +80,12 @@ int mic_markers_count(mic_ctx *ctx, int64_t *n);
 /* ---- nodal fields (MIC_NF_* ids) ---- */
 int mic_nodal_upload(mic_ctx *ctx, int field, const double *host);
 int mic_nodal_download(mic_ctx *ctx, int field, double *host);
+/* Several nodal fields in one call (new): fields[k] to or from host[k], count <= 32, one
+ * synchronization.  When every host buffer is pinned (mic_host_alloc, or registered) a single
+ * kernel moves all of them through the device's view of host memory (coherent NVLink-C2C on
+ * Grace-Blackwell); otherwise one copy per field. */
+int mic_nodal_upload_many(mic_ctx *ctx, const int *fields, const double *const *host, int count);
+int mic_nodal_download_many(mic_ctx *ctx, const int *fields, double *const *host, int count);
 int mic_nodal_device_ptr(mic_ctx *ctx, int field, double **device_ptr);
 
 /* ---- the marker path; each entry point replaces the reference function cited ---- */
