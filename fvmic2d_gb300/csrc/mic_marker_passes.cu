@@ -21,8 +21,9 @@ namespace {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+#ifndef MIC_EXACT  // product-build helpers
 // Bilinear value of corners (00, 10, 01, 11) at fractions (tx, ty) in lerp form: three
-// subtractions and three FMAs (product build only).
+// subtractions and three FMAs.
 __device__ __forceinline__ double lerp2(double f00, double f10, double f01, double f11, double tx, double ty) {
   const double a = fma(tx, f10 - f00, f00);
   const double b = fma(tx, f11 - f01, f01);
@@ -44,7 +45,9 @@ __device__ __forceinline__ void small_angle_rotation(double t, double &c, double
   s2 = 2.0 * s * c;
   c2 = (c - s) * (c + s);
 }
+#endif
 
+#ifdef MIC_EXACT
 // Interpolation cell at cell centres (updateMarkerStrainPressure.c:137-150, updateMarkerStress.c:66-80,
 // subgridStressChanges.c:179-190): staggered cell clamped to the interior [1, NX-2] x [1, NY-2].
 // Where the clamp leaves the staggered cell unchanged the offsets are the projection geometry.
@@ -56,6 +59,7 @@ __device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, i
   mdx = (i == sx) ? gx1 : div_sp(x - P.xc[i], P.hxc[i], P.ixc[i]);
   mdy = (j == sy) ? gy1 : div_sp(y - P.yc[j], P.hyc[j], P.iyc[j]);
 }
+#endif
 
 struct YieldCols {
   const int *cellX, *mat;
@@ -450,6 +454,7 @@ __global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal n
   c.dyy[m] = dsyy;
 }
 
+#ifdef MIC_EXACT
 // subgridStressChanges, node part (134-175 quadrant scatter, 227-233 centre scatter, 258-286
 // divide and subtract) as a gather in marker order.
 __global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const int *__restrict__ cellX,
@@ -503,6 +508,7 @@ __global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const in
   dsyy[q] = dsyy[q] + -1.0 * gyy;
   dsxy[q] = dsxy[q] + -1.0 * gxy;
 }
+#endif
 
 #ifndef MIC_EXACT
 // Product build: the same sums through per-cell partials.  One thread per basic cell walks the
@@ -652,9 +658,9 @@ __global__ void k_subgridT_markers(Params P, SubTCols c, Geo g, const double *__
   const int i = c.cellX[m], j = c.cellY[m];
   if (i == -1) return;
   const int NX = P.NX;
+#ifdef MIC_EXACT
   const size_t k00 = (size_t)j * NX + i, k10 = k00 + 1, k01 = k00 + NX, k11 = k01 + 1;
   const double mdx = g.gx0[m], mdy = g.gy0[m];
-#ifdef MIC_EXACT
   const double dx = P.x[i + 1] - P.x[i], dy = P.y[j + 1] - P.y[j];
   const double Tm = Tn[k00] * (1.0 - mdx) * (1.0 - mdy) + Tn[k10] * mdx * (1.0 - mdy) +
                     Tn[k01] * (1.0 - mdx) * (mdy) + Tn[k11] * mdx * mdy;
@@ -667,9 +673,6 @@ __global__ void k_subgridT_markers(Params P, SubTCols c, Geo g, const double *__
 #else
   // the stored corner weights, shared by the four fields (the reference multiplies each value
   // by both factors in turn; the products agree to rounding)
-  (void)k01;
-  (void)k10;
-  (void)k11;
   const W4 w = load_w4(g.w0, m);
   const double Tm = interp_w(Tn, NX, i, j, w);
   const double rhom = rho0 + interp_w(rn, NX, i, j, w);
@@ -701,16 +704,13 @@ __global__ void k_subgridT_apply(Params P, SubTCols c, Geo g, const double *__re
   if (m >= n) return;
   const int i = c.cellX[m], j = c.cellY[m];
   if (i == -1) return;
+#ifdef MIC_EXACT
   const size_t k00 = (size_t)j * P.NX + i;
   const double mdx = g.gx0[m], mdy = g.gy0[m];
-#ifdef MIC_EXACT
   const double dtm = (dT[k00] * (1.0 - mdy) * (1.0 - mdx) + dT[k00 + P.NX] * mdy * (1.0 - mdx) +
                       dT[k00 + 1] * (1.0 - mdy) * mdx + dT[k00 + P.NX + 1] * mdy * mdx) +
                      c.dTsub[m];
 #else
-  (void)k00;
-  (void)mdx;
-  (void)mdy;
   const double dtm = interp_w(dT, P.NX, i, j, load_w4(g.w0, m)) + c.dTsub[m];
 #endif
   c.T[m] = c.T[m] + dtm;
@@ -774,9 +774,9 @@ __global__ void k_advect(Params P, AdvectCols c, Geo g, const double *__restrict
     const double mdx = (s == 0) ? g.gx0[m] : (xcur - P.x[i]) * P.ix[i];
     const double mdy = (s == 0) ? g.gy0[m] : (ycur - P.y[j]) * P.iy[j];
 #endif
-    double ax = xcur - P.x[vxX];
     double ay = ycur - P.yc[vxY + 1];
 #ifdef MIC_EXACT
+    double ax = xcur - P.x[vxX];
     double hx = P.x[vxX + 1] - P.x[vxX];
     double hy = P.yc[vxY + 2] - P.yc[vxY + 1];
 #else
@@ -802,7 +802,6 @@ __global__ void k_advect(Params P, AdvectCols c, Geo g, const double *__restrict
     t += vll * (1.0 - ax / hx) * (ay / hy);
     t += vlr * (ax * ay) / hx / hy;
 #else
-    (void)ax;
     double t = lerp2(vul, vur, vll, vlr, tx, ty);
 #endif
     mvx[s] = t;

@@ -38,6 +38,7 @@ struct MarkerView {
   const int *flags;
 };
 
+#ifdef MIC_EXACT  // the product build projects through per-cell partials (below)
 // One thread per node (i, j): basic-node sums (rho, etaS, k, T, Cp with ARITHMETIC weights;
 // soxy with the nearest-node ARITHMETIC_LOCAL weight) and cell-centre sums (etaN ARITHMETIC;
 // soxx, soyy ARITHMETIC_LOCAL) in the marker order of markerProjection.c:115-229.
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(128) k_project_all2(Params P, MarkerView mv, c
   o.muS[q] = 1e99;
   o.muN[q] = 1e99;
 }
+#endif
 
 // Single-field ARITHMETIC projection reusing the step geometry: STAG 0 -> basic nodes
 // (projectMarkersNodesFromScalar, markers.c:1507-1594, and stagger (0,0)); STAG -1 ->
