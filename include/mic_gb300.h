@@ -198,6 +198,7 @@ int mic_launch_count(mic_ctx *ctx, int64_t *launches);
 /* per-launch CUDA-event timing on the context stream: enable with a record capacity (0 turns it
  * off); read aggregates by kernel name (names: max * 48 bytes) */
 int mic_profile_enable(mic_ctx *ctx, int capacity);
+int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64_t *counts, int *nkernels);
 /* Launch shapes (new; the reference has no counterpart).  The marker-parallel kernels of a step
  * each launch with one block size.  mic_autotune measures 128, 256 and 512 threads for each on
  * this context's workload: it saves the marker columns and nodal fields, runs for every candidate
@@ -222,7 +223,6 @@ enum {
 int mic_autotune(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, int steps, int *chosen);
 int mic_get_tuning(mic_ctx *ctx, int *block, int count);
 int mic_set_tuning(mic_ctx *ctx, const int *block, int count);
-int mic_profile_read(mic_ctx *ctx, int max, char *names, double *total_ms, int64_t *counts, int *nkernels);
 /* ---- marker lifecycle (markers.c:15-39, 255-400) ----
  * resetMarkers: every slot of the capacity gets resetMarker's values (X = Y = -1, Mat = -1, the
  * kinematic, thermal, stress, strain and density fields 0; mu, cellX, cellY, cpu and the
