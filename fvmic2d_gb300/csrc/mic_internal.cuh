@@ -191,6 +191,9 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out);
 void mic_invalidate_sort(mic_ctx *ctx);
 int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out);
 int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry
+// projectMarkersNodesAll2 again after a full pass on unchanged positions, densities, temperatures
+// and materials (only viscosities and stresses changed): the product build re-forms only those
+int mic_project_all2_viscous(mic_ctx *ctx);
 // copies of a context's marker columns and nodal fields, put back by mic_state_restore
 int mic_state_save(mic_ctx *ctx, void **handle);
 int mic_state_restore(mic_ctx *ctx, void *handle);

@@ -1366,7 +1366,8 @@ extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yieldin
   if ((e = run_max(ctx, C_T, 0, nullptr))) return e;
   if ((e = yield_launch(ctx, dt_disp))) return e;
   if ((e = mic_limit_viscosity(ctx))) return e;
-  if ((e = mic_project_markers_nodes_all2(ctx))) return e;
+  // the second projection (main:303): yielding and the limit changed viscosities and stresses only
+  if ((e = mic_project_all2_viscous(ctx))) return e;
   if (is_yielding || max_T) {
     if ((e = read_status(ctx))) return e;
     if (is_yielding) *is_yielding = ctx->h_status->is_yielding;

@@ -247,13 +247,15 @@ struct PartialView {
 };
 
 // ALL2: rho, etaS, k, T, Cp, weight per corner (24) + nearest-node sxy, weight (8) = 32 sums.
-// !ALL2: scalar, weight per corner = 8 sums.  part[acc * ncells + cell].
+// !ALL2: scalar, weight per corner = 8 sums.  part[acc * ncells + cell].  VISC (with ALL2): only
+// the sums whose marker inputs yielding and the viscosity limit change (etaS per corner, the
+// nearest-node sxy and its weight); the other slots keep the previous ALL2 pass's sums.
 //
 // One loop over the cell's markers (its four quadrant runs back to back, the same order as
 // quadrant by quadrant): a warp's lanes then wait for the longest cell of the warp once, not
 // for the longest run of each quadrant four times.  The nearest-node sums go to a per-thread
 // shared-memory slot picked by the marker's corner, so the loop has no corner branches.
-template <bool ALL2>
+template <bool ALL2, bool VISC = false>
 __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v, const int *__restrict__ qs,
                                                          mic_materials mat, double *__restrict__ part) {
   __shared__ double sloc[ALL2 ? 8 : 1][128];
@@ -276,7 +278,11 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
   for (int m = mb; m < me; ++m) {
     const W4 ww = load_w4(v.w0, m);
     const double w[4] = {ww.w00, ww.w10, ww.w01, ww.w11};
-    if (ALL2) {
+    if (ALL2 && VISC) {
+      const double e = v.eta[m];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[k][1] = fma(w[k], e, acc[k][1]);
+    } else if (ALL2) {
       const double r = v.rho[m], e = v.eta[m], tt = v.T[m];
       const int mt = v.mat[m];
       const double kk = mat.materialkThermal[mt], cp = mat.materialCp[mt];
@@ -289,6 +295,8 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
         acc[k][4] = fma(w[k], cp, acc[k][4]);
         acc[k][5] += w[k];
       }
+    }
+    if (ALL2) {
       // nearest basic node (mdx0 >= .5, mdy0 >= .5): the weight of that corner, as w[corner]
       const int fl = v.flags[m];
       const int corner = ((fl >> 2) & 1) | (((fl >> 3) & 1) << 1);
@@ -308,7 +316,8 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
 #pragma unroll
-    for (int f = 0; f < NA; ++f) part[(size_t)(k * NA + f) * ncells + c] = acc[k][f];
+    for (int f = 0; f < NA; ++f)
+      if (!VISC || f == 1) part[(size_t)(k * NA + f) * ncells + c] = acc[k][f];
     if (ALL2) {
       part[(size_t)(24 + 2 * k) * ncells + c] = sloc[2 * k][t];
       part[(size_t)(25 + 2 * k) * ncells + c] = sloc[2 * k + 1][t];
@@ -393,6 +402,9 @@ __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v
 // (i,j) corner 0; centre sums from staggered cells with the same offsets.
 __device__ __forceinline__ double guarded(double a, double w) { return (w != 0.0) ? a / w : 0.0; }
 
+// VISC: only the viscosity and stress fields (etaS, soxy, etaN, soxx, soyy); rho, k, T, Cp and
+// the constants keep the values of the previous full pass.
+template <bool VISC>
 __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__restrict__ pb,
                                                        const double *__restrict__ pc, All2Out o) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -408,7 +420,8 @@ __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__
     if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
       const size_t cc = (size_t)cy * NC + cx;
 #pragma unroll
-      for (int f = 0; f < 6; ++f) b[f] += pb[(size_t)(k * 6 + f) * ncells + cc];
+      for (int f = 0; f < 6; ++f)
+        if (!VISC || f == 1 || f == 5) b[f] += pb[(size_t)(k * 6 + f) * ncells + cc];
       b[6] += pb[(size_t)(24 + 2 * k) * ncells + cc];
       b[7] += pb[(size_t)(25 + 2 * k) * ncells + cc];
     }
@@ -422,18 +435,20 @@ __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__
     }
   }
   const size_t q = (size_t)j * P.NX + i;
-  o.rho[q] = guarded(b[0], b[5]);
   o.etaS[q] = guarded(b[1], b[5]);
-  o.k[q] = guarded(b[2], b[5]);
-  o.lastT[q] = guarded(b[3], b[5]);
-  o.Cp[q] = guarded(b[4], b[5]);
   o.soxy[q] = guarded(b[6], b[7]);
   o.etaN[q] = guarded(c[0], c[1]);
   o.soxx[q] = guarded(c[2], c[4]);
   o.soyy[q] = guarded(c[3], c[4]);
-  o.rhodot[q] = 0.0;
-  o.muS[q] = 1e99;
-  o.muN[q] = 1e99;
+  if (!VISC) {
+    o.rho[q] = guarded(b[0], b[5]);
+    o.k[q] = guarded(b[2], b[5]);
+    o.lastT[q] = guarded(b[3], b[5]);
+    o.Cp[q] = guarded(b[4], b[5]);
+    o.rhodot[q] = 0.0;
+    o.muS[q] = 1e99;
+    o.muN[q] = 1e99;
+  }
 }
 
 template <int STAG>
@@ -540,8 +555,10 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out) {
   return MIC_OK;
 }
 
-extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
-  if (!ctx) return MIC_ERR_ARG;
+// visc: the second projection of a step (main:303), after yielding and the viscosity limit changed
+// only viscosities and stresses: the product build then forms only those sums and keeps the
+// first projection's rho, k, T, Cp (same inputs, same order, so the same values)
+static int project_all2(mic_ctx *ctx, bool visc) {
   cudaSetDevice(ctx->device);
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
@@ -573,6 +590,7 @@ extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
   o.soyy = ctx->nodal[MIC_NF_SOYY];
   o.soxy = ctx->nodal[MIC_NF_SOXY];
 #ifdef MIC_EXACT
+  (void)visc;  // the exact build gathers every field in reference order each time
   {
     MIC_KERNEL(ctx, "k_project_all2");
     k_project_all2<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, mv, ctx->cell_start, ctx->mat, o);
@@ -593,7 +611,11 @@ extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
   pv.flags = mv.flags;
   pv.w0 = ctx->wgt[0];
   pv.w1 = ctx->wgt[1];
-  {
+  if (visc) {
+    MIC_KERNEL(ctx, "k_partials_basic<visc>");
+    k_partials_basic<true, true><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
+                                                                                      ctx->mat, ctx->part_b);
+  } else {
     MIC_KERNEL(ctx, "k_partials_basic");
     k_partials_basic<true><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
                                                                                 ctx->mat, ctx->part_b);
@@ -602,14 +624,24 @@ extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
     MIC_KERNEL(ctx, "k_partials_centre");
     k_partials_centre<true><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
   }
-  {
+  if (visc) {
+    MIC_KERNEL(ctx, "k_combine_all2<visc>");
+    k_combine_all2<true><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
+  } else {
     MIC_KERNEL(ctx, "k_combine_all2");
-    k_combine_all2<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
+    k_combine_all2<false><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
   }
 #endif
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
 }
+
+extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
+  if (!ctx) return MIC_ERR_ARG;
+  return project_all2(ctx, false);
+}
+
+int mic_project_all2_viscous(mic_ctx *ctx) { return project_all2(ctx, true); }
 
 extern "C" int mic_project_marker_field_to_nodes(mic_ctx *ctx, int off, const double *matprop, int out_field,
                                                  int stagx, int stagy, int method) {
