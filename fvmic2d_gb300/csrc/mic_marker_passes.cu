@@ -295,6 +295,8 @@ struct StrainCols {
   const int *cellX, *cellY;
   const double *X, *Y, *eta, *mu;
   double *p, *exx, *eyy, *exy, *wxy, *srr;
+  double *kxx, *kyy, *kxy;  // product build, when not null: the interpolated soxx, soyy, soxy kept
+                            // for the sub-grid stress pass that follows in the same step
 };
 
 // updateMarkerStrainPressure (updateMarkerStrainPressure.c:131-306, non-TEXTURE branch)
@@ -360,6 +362,13 @@ __global__ void k_strain_pressure(Params P, StrainCols c, Geo g, Nodal nd, doubl
   c.exx[m] = e11;
   c.eyy[m] = e22;
   c.exy[m] = e12;
+#ifndef MIC_EXACT
+  if (c.kxx) {
+    c.kxx[m] = msxx;
+    c.kyy[m] = msyy;
+    c.kxy[m] = msxy;
+  }
+#endif
   const double a = e11 - mexx, b = e12 - mexy;
   const double r = sqrt(a * a + b * b);  // pow(., 2.0) of the reference: the correctly rounded square
   c.srr[m] = r;
@@ -411,8 +420,10 @@ struct SubgridCols {
 };
 
 // subgridStressChanges, marker part (subgridStressChanges.c:79-221)
+// reuse (product build): dxx, dyy, dxy hold the nodal soxx, soyy, soxy interpolated at the
+// marker by k_strain_pressure of this step (same nodes, weights and order: the same values)
 __global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal nd, double dt, double D,
-                                         int64_t n) {
+                                         int64_t n, int reuse) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
@@ -426,9 +437,10 @@ __global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal n
   if (sdif < -30.0) sdif = -30.0;
   sdif = 1.0 - exp(sdif);
 #ifdef MIC_EXACT
+  (void)reuse;
   double dsxy = interp_run(nd.soxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]) - c.sxy[m];
 #else
-  double dsxy = interp_w(nd.soxy, P.NX, cx, cy, load_w4(g.w0, m)) - c.sxy[m];
+  double dsxy = (reuse ? c.dxy[m] : interp_w(nd.soxy, P.NX, cx, cy, load_w4(g.w0, m))) - c.sxy[m];
 #endif
   dsxy *= sdif;
   c.sxy[m] = c.sxy[m] + dsxy;
@@ -441,11 +453,19 @@ __global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal n
   c.sxx[m] = c.sxx[m] + dsxx;
   double dsyy = interp_run(nd.soyy, P.NX, i, j, mdx, mdy) - c.syy[m];
 #else
-  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
-  double dsxx = interp_w(nd.soxx, P.NX, i, j, wc) - c.sxx[m];
+  double msxx, msyy;
+  if (reuse) {
+    msxx = c.dxx[m];
+    msyy = c.dyy[m];
+  } else {
+    const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
+    msxx = interp_w(nd.soxx, P.NX, i, j, wc);
+    msyy = interp_w(nd.soyy, P.NX, i, j, wc);
+  }
+  double dsxx = msxx - c.sxx[m];
   dsxx *= sdif;
   c.sxx[m] = c.sxx[m] + dsxx;
-  double dsyy = interp_w(nd.soyy, P.NX, i, j, wc) - c.syy[m];
+  double dsyy = msyy - c.syy[m];
 #endif
   dsyy *= sdif;
   c.syy[m] = c.syy[m] + dsyy;
@@ -724,8 +744,11 @@ struct AdvectCols {
 };
 
 // advectMarkersRK (markers.c:1865-2250), non-periodic grid, non-JAUMANN rotation
-__global__ void k_advect(Params P, AdvectCols c, Geo g, const double *__restrict__ vx, const double *__restrict__ vy,
-                         const double *__restrict__ wz, mic_bcinfo top, mic_bcinfo left, double dt, int64_t n) {
+// wz_known (product build): the marker's wxy column holds the vorticity k_strain_pressure of this
+// step interpolated at the marker (the first stage's value: same nodes, weights and order)
+__global__ void __launch_bounds__(512, 2) k_advect(Params P, AdvectCols c, Geo g, const double *__restrict__ vx, const double *__restrict__ vy,
+                                                   const double *__restrict__ wz, mic_bcinfo top, mic_bcinfo left,
+                                                   double dt, int64_t n, int wz_known) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
   const int ci = c.cellX[m], cj = c.cellY[m];
@@ -840,7 +863,10 @@ __global__ void k_advect(Params P, AdvectCols c, Geo g, const double *__restrict
     t += (1.0 - mdx) * (mdy)*wz[w0 + NX];
     t += (mdx) * (mdy)*wz[w0 + NX + 1];
 #else
-    t = lerp2(wz[w0], wz[w0 + 1], wz[w0 + NX], wz[w0 + NX + 1], mdx, mdy);
+    if (s == 0)  // at the marker itself: the bilinear form of the stored weights
+      t = wz_known ? c.wxy[m] : interp_w(wz, NX, i, j, load_w4(g.w0, m));
+    else
+      t = lerp2(wz[w0], wz[w0 + 1], wz[w0 + NX], wz[w0 + NX + 1], mdx, mdy);
 #endif
     mwz[s] = t;
     if (s < 2) {
@@ -1093,7 +1119,8 @@ extern "C" int mic_limit_viscosity(mic_ctx *ctx) {
   return MIC_OK;
 }
 
-static int strain_launch(mic_ctx *ctx, double dt) {
+// keep: store the interpolated old stresses for a sub-grid stress pass that follows in this step
+static int strain_launch(mic_ctx *ctx, double dt, bool keep = false) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->nan_residual, 0, sizeof(unsigned long long), ctx->stream));
@@ -1111,6 +1138,9 @@ static int strain_launch(mic_ctx *ctx, double dt) {
   c.exy = ctx->f64[C_EXY];
   c.wxy = ctx->f64[C_WXY];
   c.srr = ctx->f64[C_SRR];
+  c.kxy = keep ? ctx->scr0 : nullptr;
+  c.kxx = keep ? ctx->scr1 : nullptr;
+  c.kyy = keep ? ctx->scr2 : nullptr;
   {
     MIC_KERNEL(ctx, "k_strain_pressure");
     k_strain_pressure<<<grid_for(ctx->n, tuned_block(ctx, TU_STRAIN)), tuned_block(ctx, TU_STRAIN), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n,
@@ -1182,8 +1212,8 @@ extern "C" int mic_check_convergence(mic_ctx *ctx, double atol, double rtol, int
   return MIC_OK;
 }
 
-extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
-  CHECK_CTX();
+// reuse: k_strain_pressure of this step kept the interpolated old stresses in the scratch columns
+static int subgrid_launch(mic_ctx *ctx, double dt, double D, bool reuse) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   if (ctx->n > 0) {
@@ -1202,8 +1232,9 @@ extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
     c.dyy = ctx->scr2;
     {
       MIC_KERNEL(ctx, "k_subgrid_stress_markers");
-      k_subgrid_stress_markers<<<grid_for(ctx->n, tuned_block(ctx, TU_SUBGRID_STRESS)), tuned_block(ctx, TU_SUBGRID_STRESS), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
-                                                                             D, ctx->n);
+      const int B = tuned_block(ctx, TU_SUBGRID_STRESS);
+      k_subgrid_stress_markers<<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
+                                                                           D, ctx->n, reuse ? 1 : 0);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }
@@ -1234,6 +1265,11 @@ extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
 #endif
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
+}
+
+extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
+  CHECK_CTX();
+  return subgrid_launch(ctx, dt, D, false);
 }
 
 static int stress_launch(mic_ctx *ctx) {
@@ -1301,8 +1337,7 @@ extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
   return MIC_OK;
 }
 
-extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
-  CHECK_CTX();
+static int advect_launch(mic_ctx *ctx, double dt, bool wz_known) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   if (ctx->n > 0) {
@@ -1326,7 +1361,7 @@ extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
       k_advect<<<grid_for(ctx->n, tuned_block(ctx, TU_ADVECT)), tuned_block(ctx, TU_ADVECT), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX],
                                                              ctx->nodal[MIC_NF_VY],
                                                              ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
-                                                             ctx->bcs.mechBCLeft, dt, ctx->n);
+                                                             ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }
@@ -1334,6 +1369,11 @@ extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
   ctx->sorted = 0;
   ctx->geo_valid = 0;
   return MIC_OK;
+}
+
+extern "C" int mic_advect_markers_rk(mic_ctx *ctx, double dt) {
+  CHECK_CTX();
+  return advect_launch(ctx, dt, false);
 }
 
 extern "C" int mic_project_nodal_field_to_markers(mic_ctx *ctx, int f, int off) {
@@ -1384,11 +1424,16 @@ extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yieldin
 extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_stress, double *residual) {
   CHECK_CTX();
   int e;
-  if ((e = strain_launch(ctx, dt_disp))) return e;
+  const bool sub = subgrid_stress && ctx->opt.subgridStressDiffusivity > 0.0;
+#ifdef MIC_EXACT
+  const bool keep = false;
+#else
+  const bool keep = sub && ctx->n > 0;
+#endif
+  if ((e = strain_launch(ctx, dt_disp, keep))) return e;
   double *d = ctx->red_buf + 16;
-  if ((e = residual_launch(ctx, 0, d))) return e;
-  if (subgrid_stress && ctx->opt.subgridStressDiffusivity > 0.0)
-    if ((e = mic_subgrid_stress_changes(ctx, dt_disp, ctx->opt.subgridStressDiffusivity))) return e;
+  if ((e = residual_launch(ctx, 0, d))) return e;  // leaves the scratch columns alone
+  if (sub && (e = subgrid_launch(ctx, dt_disp, ctx->opt.subgridStressDiffusivity, keep))) return e;
   if ((e = stress_launch(ctx))) return e;
   if (residual) {
     double s = 0.0;
@@ -1401,12 +1446,18 @@ extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_st
   return MIC_OK;
 }
 
-extern "C" int mic_step_post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx) {
-  CHECK_CTX();
+// wz_known: the marker vorticity is this step's k_strain_pressure value on the nodal wxy the
+// advection reads (true inside mic_step; a caller between the calls may replace nodal fields)
+static int post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx, bool wz_known) {
   int e;
   if ((e = mic_subgrid_temperature_changes(ctx, dt_thermal))) return e;
-  if ((e = mic_advect_markers_rk(ctx, dt_thermal))) return e;
+  if ((e = advect_launch(ctx, dt_thermal, wz_known))) return e;
   return run_max(ctx, C_SXX, 1, max_abs_sxx);
+}
+
+extern "C" int mic_step_post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx) {
+  CHECK_CTX();
+  return post_thermal(ctx, dt_thermal, max_abs_sxx, false);
 }
 
 extern "C" int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, double *residual) {
@@ -1414,5 +1465,9 @@ extern "C" int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int sub
   int e;
   if ((e = mic_step_pre_stokes(ctx, dt_disp, nullptr, nullptr))) return e;
   if ((e = mic_step_post_stokes(ctx, dt_disp, subgrid_stress, residual))) return e;
-  return mic_step_post_thermal(ctx, dt_thermal, nullptr);
+#ifdef MIC_EXACT
+  return post_thermal(ctx, dt_thermal, nullptr, false);
+#else
+  return post_thermal(ctx, dt_thermal, nullptr, ctx->n > 0);
+#endif
 }
