@@ -256,13 +256,32 @@ __global__ void k_limit_viscosity(double *eta, double etamin, double etamax, int
 }
 
 // density update inline in main_subduction.c:255-264
+// MAXT: also the maximum marker temperature of main:271-281 (in-domain markers, from 0; the bit
+// patterns of non-negative doubles order as the values), one atomic per block into *maxT
+template <bool MAXT>
 __global__ void k_update_rho(const int *cellX, const int *mat, const double *T, double *rho, double *rhodot,
-                             mic_materials M, int64_t n) {
+                             mic_materials M, int64_t n, unsigned long long *maxT) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (m >= n || cellX[m] == -1) return;
-  const int k = mat[m];
-  rho[m] = -M.materialRho[k] * (M.materialAlpha[k] * T[m]);
-  rhodot[m] = 0.0;
+  long long b = 0;  // bits of 0.0
+  if (m < n && cellX[m] != -1) {
+    const int k = mat[m];
+    const double t = T[m];
+    rho[m] = -M.materialRho[k] * (M.materialAlpha[k] * t);
+    rhodot[m] = 0.0;
+    if (MAXT && t > 0.0) b = __double_as_longlong(t);
+  }
+  if (MAXT) {
+    __shared__ long long wmax[32];
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wmax[warp] = b;
+    __syncthreads();
+    if (warp == 0) {
+      b = lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0;
+      for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+      if (lane == 0 && b > 0) atomicMax(maxT, (unsigned long long)b);
+    }
+  }
 }
 
 struct Geo {
@@ -621,8 +640,9 @@ __global__ void __launch_bounds__(128) k_subgrid_combine(Params P, const double 
   const size_t q = (size_t)j * P.NX + i;
   const double W = 0.0 + wxy, Wn = 0.0 + wn;
   const double gxy = (W != 0.0) ? (0.0 + sxy) / W : 0.0;
-  const double gxx = (Wn != 0.0) ? (0.0 + sxx) / Wn : 0.0;
-  const double gyy = (Wn != 0.0) ? (0.0 + syy) / Wn : 0.0;
+  const double rn = (Wn != 0.0) ? 1.0 / Wn : 0.0;  // one division for the two centre sums
+  const double gxx = (0.0 + sxx) * rn;
+  const double gyy = (0.0 + syy) * rn;
   dsxx[q] = dsxx[q] + -1.0 * gxx;
   dsyy[q] = dsyy[q] + -1.0 * gyy;
   dsxy[q] = dsxy[q] + -1.0 * gxy;
@@ -1020,18 +1040,31 @@ int run_max(mic_ctx *ctx, int col, int absval, double *out) {
   if (!ctx) return MIC_ERR_ARG;     \
   cudaSetDevice(ctx->device)
 
-extern "C" int mic_update_marker_rho(mic_ctx *ctx) {
-  CHECK_CTX();
+// with_max: the step's maximum marker temperature into the reduction slot as well (run_max's)
+static int update_rho(mic_ctx *ctx, bool with_max) {
   int e = mic_ensure_sorted(ctx);
   if (e) return e;
+  unsigned long long *d = reinterpret_cast<unsigned long long *>(ctx->red_buf + 8);
+  if (with_max) MIC_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
   if (ctx->n == 0) return MIC_OK;
+  const int B = tuned_block(ctx, TU_UPDATE_RHO);
   {
     MIC_KERNEL(ctx, "k_update_rho");
-    k_update_rho<<<grid_for(ctx->n, tuned_block(ctx, TU_UPDATE_RHO)), tuned_block(ctx, TU_UPDATE_RHO), 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
-                                                               ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n);
+    if (with_max)
+      k_update_rho<true><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
+                                                                    ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n, d);
+    else
+      k_update_rho<false><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
+                                                                     ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n,
+                                                                     nullptr);
   }
   MIC_CUDA_TRY(cudaGetLastError());
   return MIC_OK;
+}
+
+extern "C" int mic_update_marker_rho(mic_ctx *ctx) {
+  CHECK_CTX();
+  return update_rho(ctx, false);
 }
 
 extern "C" int mic_max_marker_T(mic_ctx *ctx, double *maxT) {
@@ -1401,9 +1434,10 @@ extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yieldin
   // findMarkerCells (main:243, 247, 252): positions do not change between the three calls on
   // one rank without density control, so one binning gives all three results
   if ((e = mic_bin_and_sort(ctx, nullptr))) return e;
-  if ((e = mic_update_marker_rho(ctx))) return e;
+  // the density update also finds the maximum temperature (main:271-281; the projection between
+  // changes no marker temperature)
+  if ((e = update_rho(ctx, true))) return e;
   if ((e = mic_project_markers_nodes_all2(ctx))) return e;
-  if ((e = run_max(ctx, C_T, 0, nullptr))) return e;
   if ((e = yield_launch(ctx, dt_disp))) return e;
   if ((e = mic_limit_viscosity(ctx))) return e;
   // the second projection (main:303): yielding and the limit changed viscosities and stresses only

@@ -401,6 +401,8 @@ __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v
 // Node (i, j): basic sums from cells (i-1,j-1) corner 3, (i,j-1) corner 2, (i-1,j) corner 1,
 // (i,j) corner 0; centre sums from staggered cells with the same offsets.
 __device__ __forceinline__ double guarded(double a, double w) { return (w != 0.0) ? a / w : 0.0; }
+// 1/w for several sums over one weight (one division; each product within an ulp of the quotient)
+__device__ __forceinline__ double guarded_rcp(double w) { return (w != 0.0) ? 1.0 / w : 0.0; }
 
 // VISC: only the viscosity and stress fields (etaS, soxy, etaN, soxx, soyy); rho, k, T, Cp and
 // the constants keep the values of the previous full pass.
@@ -435,16 +437,17 @@ __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__
     }
   }
   const size_t q = (size_t)j * P.NX + i;
-  o.etaS[q] = guarded(b[1], b[5]);
+  const double r0 = guarded_rcp(b[5]), r2 = guarded_rcp(c[4]);  // shared weight sums
+  o.etaS[q] = b[1] * r0;
   o.soxy[q] = guarded(b[6], b[7]);
   o.etaN[q] = guarded(c[0], c[1]);
-  o.soxx[q] = guarded(c[2], c[4]);
-  o.soyy[q] = guarded(c[3], c[4]);
+  o.soxx[q] = c[2] * r2;
+  o.soyy[q] = c[3] * r2;
   if (!VISC) {
-    o.rho[q] = guarded(b[0], b[5]);
-    o.k[q] = guarded(b[2], b[5]);
-    o.lastT[q] = guarded(b[3], b[5]);
-    o.Cp[q] = guarded(b[4], b[5]);
+    o.rho[q] = b[0] * r0;
+    o.k[q] = b[2] * r0;
+    o.lastT[q] = b[3] * r0;
+    o.Cp[q] = b[4] * r0;
     o.rhodot[q] = 0.0;
     o.muS[q] = 1e99;
     o.muN[q] = 1e99;

@@ -387,3 +387,30 @@ def test_survey_named_exports():
                               s.ctypes.data_as(gpu._DP), it.ctypes.data, r.ctypes.data_as(gpu._DP)) == 0
     s2, _, _, _ = G.creep_solve(e, T, d, P, mode=0)
     assert np.array_equal(s, s2)
+
+
+def test_step_split_reports_max_temperature_and_yielding():
+    """mic_step_pre_stokes's maximum marker temperature (formed with the density update) is the
+    entry point's (mic_max_marker_T) and numpy's over the in-domain markers, some pushed out of
+    the domain with the hottest temperatures; its yield flag is checkPlasticYielding's"""
+    import ctypes
+
+    wl = W.vep_slab_box(nx_cells=32, ny_cells=8, nm=4, seed=57)
+    m = wl.markers
+    m["T"] = m["T"] + np.linspace(0.0, 50.0, len(m))
+    out = np.arange(len(m)) % 97 == 0
+    m["X"][out] = -1.0  # out of the domain, hottest markers among them
+    m["T"][out] = 5.0e3
+    A = gpu.MicProblem(wl)
+    B = gpu.MicProblem(wl)
+    isy = ctypes.c_int(-1)
+    mt = ctypes.c_double(-1.0)
+    assert A.L.mic_step_pre_stokes(A.h, wl.dt, ctypes.byref(isy), ctypes.byref(mt)) == 0
+    B.findMarkerCells()
+    B.updateMarkerRho()
+    B.projectMarkersNodesAll2()
+    ref_t = B.maxMarkerT()
+    ref_y = B.checkPlasticYielding(wl.dt)
+    inside = ~out
+    assert mt.value == ref_t == float(np.max(m["T"][inside]))
+    assert isy.value == ref_y
