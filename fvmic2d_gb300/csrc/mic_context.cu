@@ -166,6 +166,9 @@ static void free_ctx(mic_ctx *ctx) {
     cudaEventDestroy(ctx->lu_ev[0]);
     cudaEventDestroy(ctx->lu_ev[1]);
   }
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
+  for (int k = 0; k < 2; ++k)
+    if (ctx->aux_ev[k]) cudaEventDestroy(ctx->aux_ev[k]);
   cudaFree(ctx->stage_aos);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -207,6 +210,12 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
       return MIC_ERR_CUDA;
     }
     ctx->owns_stream = 1;
+  }
+  if (cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->aux_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->aux_ev[1], cudaEventDisableTiming) != cudaSuccess) {
+    free_ctx(ctx);
+    return MIC_ERR_CUDA;
   }
   // host grid copies with fvmic2d's ghost offset of 2; cell centres as in getCellCenters
   const size_t nx4 = (size_t)NX + 4, ny4 = (size_t)NY + 4;
@@ -634,16 +643,16 @@ extern "C" int mic_host_free(void *ptr) {
 
 // ---- launch accounting and per-launch timing ------------------------------------------
 
-void mic_prof_begin(mic_ctx *ctx, const char *name) {
+void mic_prof_begin(mic_ctx *ctx, const char *name, cudaStream_t s) {
   ctx->launches++;
   if (!ctx->prof_on || ctx->prof_n >= ctx->prof_cap) return;
   ctx->prof_name[ctx->prof_n] = name;
-  cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n], ctx->stream);
+  cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n], s);
 }
 
-void mic_prof_end(mic_ctx *ctx) {
+void mic_prof_end(mic_ctx *ctx, cudaStream_t s) {
   if (!ctx->prof_on || ctx->prof_n >= ctx->prof_cap) return;
-  cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n + 1], ctx->stream);
+  cudaEventRecord(ctx->prof_ev[2 * ctx->prof_n + 1], s);
   ctx->prof_n++;
 }
 

@@ -120,6 +120,8 @@ struct mic_ctx {
   size_t lu_bytes;
   cudaStream_t lu_side;       // second stream of the factorisation: the far part of each update
   cudaEvent_t lu_ev[2];       // its two hand-offs (trsm done, far update done)
+  cudaStream_t aux;           // second stream of a projection: its cell-centre partial sums run
+  cudaEvent_t aux_ev[2];      // beside the basic-cell ones (fork, join)
   size_t io_bytes;
   size_t dens_bytes, dens_add_bytes;
   double *f64[mic::C_F64_COUNT];
@@ -163,17 +165,19 @@ struct mic_ctx {
   cudaEvent_t *prof_ev;  // 2 per record
 };
 
-void mic_prof_begin(mic_ctx *ctx, const char *name);
-void mic_prof_end(mic_ctx *ctx);
+void mic_prof_begin(mic_ctx *ctx, const char *name, cudaStream_t s);
+void mic_prof_end(mic_ctx *ctx, cudaStream_t s);
 
 namespace mic {
 struct ProfScope {  // brackets one kernel launch: counts it and, when enabled, times it
   mic_ctx *c;
-  ProfScope(mic_ctx *ctx, const char *name) : c(ctx) { mic_prof_begin(ctx, name); }
-  ~ProfScope() { mic_prof_end(c); }
+  cudaStream_t s;
+  ProfScope(mic_ctx *ctx, const char *name, cudaStream_t st) : c(ctx), s(st) { mic_prof_begin(ctx, name, st); }
+  ~ProfScope() { mic_prof_end(c, s); }
 };
 }  // namespace mic
-#define MIC_KERNEL(ctx, name) mic::ProfScope _mic_prof_scope(ctx, name)
+#define MIC_KERNEL(ctx, name) mic::ProfScope _mic_prof_scope(ctx, name, (ctx)->stream)
+#define MIC_KERNEL_ON(ctx, name, st) mic::ProfScope _mic_prof_scope(ctx, name, st)
 
 // ---- helpers -------------------------------------------------------------------------
 

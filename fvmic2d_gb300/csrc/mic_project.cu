@@ -614,6 +614,15 @@ static int project_all2(mic_ctx *ctx, bool visc) {
   pv.flags = mv.flags;
   pv.w0 = ctx->wgt[0];
   pv.w1 = ctx->wgt[1];
+  // the cell-centre sums on the second stream, beside the basic-cell sums: both only read the
+  // markers and each runs at a fraction of the SMs' warp slots
+  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
+  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
+  {
+    MIC_KERNEL_ON(ctx, "k_partials_centre", ctx->aux);
+    k_partials_centre<true><<<node_grid(ctx->P), 128, 0, ctx->aux>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
+  }
+  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
   if (visc) {
     MIC_KERNEL(ctx, "k_partials_basic<visc>");
     k_partials_basic<true, true><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
@@ -623,10 +632,7 @@ static int project_all2(mic_ctx *ctx, bool visc) {
     k_partials_basic<true><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
                                                                                 ctx->mat, ctx->part_b);
   }
-  {
-    MIC_KERNEL(ctx, "k_partials_centre");
-    k_partials_centre<true><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
-  }
+  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));  // the cell-centre sums
   if (visc) {
     MIC_KERNEL(ctx, "k_combine_all2<visc>");
     k_combine_all2<true><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
