@@ -191,7 +191,7 @@ int mic_fail_cuda(mic_ctx *ctx, cudaError_t e);
 int mic_ensure_sorted(mic_ctx *ctx);  // bins + sorts if positions changed since the last sort
 // ARITHMETIC projection of a marker value column (binned order) to basic nodes (stag 0) or cell
 // centres (stag -1), divided by the weights
-int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out);
+int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out, cudaStream_t s = nullptr);
 void mic_invalidate_sort(mic_ctx *ctx);
 int mic_bin_and_sort(mic_ctx *ctx, int64_t *n_out);
 int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry

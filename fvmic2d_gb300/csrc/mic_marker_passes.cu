@@ -1191,20 +1191,21 @@ extern "C" int mic_update_marker_strain_pressure(mic_ctx *ctx, double dt) {
   return ctx->h_status->nan_residual ? MIC_ERR_NAN : MIC_OK;
 }
 
-static int residual_launch(mic_ctx *ctx, int iter, double *res_dev) {
-  int e = mic_project_scalar(ctx, ctx->f64[C_SRR], -1, ctx->nodal[MIC_NF_SRR]);
+static int residual_launch(mic_ctx *ctx, int iter, double *res_dev, cudaStream_t st = nullptr) {
+  const cudaStream_t s = st ? st : ctx->stream;
+  int e = mic_project_scalar(ctx, ctx->f64[C_SRR], -1, ctx->nodal[MIC_NF_SRR], s);
   if (e) return e;
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
   const int nb = (int)grid_for(nn);
   double *partial = ctx->node_scr[5];  // NX*NY >= number of blocks
   {
-    MIC_KERNEL(ctx, "k_residual_weight");
-    k_residual_weight<<<nb, kBlock, 0, ctx->stream>>>(ctx->P, ctx->nodal[MIC_NF_SRR], partial);
+    MIC_KERNEL_ON(ctx, "k_residual_weight", s);
+    k_residual_weight<<<nb, kBlock, 0, s>>>(ctx->P, ctx->nodal[MIC_NF_SRR], partial);
   }
   MIC_CUDA_TRY(cudaGetLastError());
   {
-    MIC_KERNEL(ctx, "k_sum_partials");
-    k_sum_partials<<<1, 1024, 0, ctx->stream>>>(partial, nb, res_dev);
+    MIC_KERNEL_ON(ctx, "k_sum_partials", s);
+    k_sum_partials<<<1, 1024, 0, s>>>(partial, nb, res_dev);
   }
   MIC_CUDA_TRY(cudaGetLastError());
   (void)iter;
@@ -1466,9 +1467,22 @@ extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_st
 #endif
   if ((e = strain_launch(ctx, dt_disp, keep))) return e;
   double *d = ctx->red_buf + 16;
-  if ((e = residual_launch(ctx, 0, d))) return e;  // leaves the scratch columns alone
+#ifdef MIC_EXACT
+  if ((e = residual_launch(ctx, 0, d))) return e;
+#else
+  // the residual (a cell-centre projection of srr and its area-weighted sum) shares no buffer with
+  // the sub-grid stress and stress-update passes: it runs on the second stream beside them
+  if ((e = mic_ensure_geometry(ctx))) return e;
+  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
+  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
+  if ((e = residual_launch(ctx, 0, d, ctx->aux))) return e;  // leaves the scratch columns alone
+  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
+#endif
   if (sub && (e = subgrid_launch(ctx, dt_disp, ctx->opt.subgridStressDiffusivity, keep))) return e;
   if ((e = stress_launch(ctx))) return e;
+#ifndef MIC_EXACT
+  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
+#endif
   if (residual) {
     double s = 0.0;
     MIC_CUDA_TRY(cudaMemcpyAsync(&s, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

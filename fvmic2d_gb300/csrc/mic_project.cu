@@ -503,11 +503,12 @@ int mic_ensure_geometry(mic_ctx *ctx) {
 }
 
 // Single-field ARITHMETIC projection of a sorted per-marker array (stagger 0 or -1).
-int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out) {
+int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out, cudaStream_t st) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
 #ifndef MIC_EXACT
   {
+    const cudaStream_t s = st ? st : ctx->stream;
     PartialView pv = {};
     pv.scalar = v;
     pv.gx0 = ctx->geo[0];
@@ -519,28 +520,29 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out) {
     pv.w1 = ctx->wgt[1];
     if (stag == 0) {
       {
-        MIC_KERNEL(ctx, "k_partials_basic<scalar>");
-        k_partials_basic<false><<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
-                                                                                     ctx->mat, ctx->part_b);
+        MIC_KERNEL_ON(ctx, "k_partials_basic<scalar>", s);
+        k_partials_basic<false><<<grid_for(ctx->ncells, 128), 128, 0, s>>>(ctx->P, pv, ctx->quad_start, ctx->mat,
+                                                                           ctx->part_b);
       }
       {
-        MIC_KERNEL(ctx, "k_combine_scalar<0>");
-        k_combine_scalar<0><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, out);
+        MIC_KERNEL_ON(ctx, "k_combine_scalar<0>", s);
+        k_combine_scalar<0><<<node_grid(ctx->P), 128, 0, s>>>(ctx->P, ctx->part_b, out);
       }
     } else {
       {
-        MIC_KERNEL(ctx, "k_partials_centre<scalar>");
-        k_partials_centre<false><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, pv, ctx->quad_start,
-                                                                            ctx->part_c);
+        MIC_KERNEL_ON(ctx, "k_partials_centre<scalar>", s);
+        k_partials_centre<false><<<node_grid(ctx->P), 128, 0, s>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
       }
       {
-        MIC_KERNEL(ctx, "k_combine_scalar<-1>");
-        k_combine_scalar<-1><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_c, out);
+        MIC_KERNEL_ON(ctx, "k_combine_scalar<-1>", s);
+        k_combine_scalar<-1><<<node_grid(ctx->P), 128, 0, s>>>(ctx->P, ctx->part_c, out);
       }
     }
     MIC_CUDA_TRY(cudaGetLastError());
     return MIC_OK;
   }
+#else
+  (void)st;  // the exact build projects on the context's stream
 #endif
   if (stag == 0)
     {
