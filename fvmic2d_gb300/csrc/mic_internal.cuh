@@ -198,6 +198,10 @@ int mic_ensure_geometry(mic_ctx *ctx);  // sorted columns + projection geometry
 // projectMarkersNodesAll2 again after a full pass on unchanged positions, densities, temperatures
 // and materials (only viscosities and stresses changed): the product build re-forms only those
 int mic_project_all2_viscous(mic_ctx *ctx);
+// the step's first projectMarkersNodesAll2 when mic_project_all2_viscous follows before any of
+// its viscosity or stress fields is read: the product build forms only rho, k, T, Cp (and the
+// weights the viscous pass divides by), on stream s; the exact build projects everything
+int mic_project_all2_first(mic_ctx *ctx, cudaStream_t s);
 // copies of a context's marker columns and nodal fields, put back by mic_state_restore
 int mic_state_save(mic_ctx *ctx, void **handle);
 int mic_state_restore(mic_ctx *ctx, void *handle);

@@ -1438,11 +1438,27 @@ extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yieldin
   // the density update also finds the maximum temperature (main:271-281; the projection between
   // changes no marker temperature)
   if ((e = update_rho(ctx, true))) return e;
+#ifdef MIC_EXACT
   if ((e = mic_project_markers_nodes_all2(ctx))) return e;
   if ((e = yield_launch(ctx, dt_disp))) return e;
   if ((e = mic_limit_viscosity(ctx))) return e;
-  // the second projection (main:303): yielding and the limit changed viscosities and stresses only
   if ((e = mic_project_all2_viscous(ctx))) return e;
+#else
+  // The first projection (main:268) and the yield pass touch disjoint marker columns (rho, T,
+  // materials against viscosity, modulus and stresses), and the first projection's viscosity and
+  // stress fields are replaced by the second (main:303) before anything reads them: so it forms
+  // only rho, k, T and Cp, on the second stream, beside the yield pass and the viscosity limit.
+  if ((e = mic_ensure_geometry(ctx))) return e;
+  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
+  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
+  if ((e = mic_project_all2_first(ctx, ctx->aux))) return e;
+  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
+  if ((e = yield_launch(ctx, dt_disp))) return e;
+  if ((e = mic_limit_viscosity(ctx))) return e;
+  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
+  // the second projection: yielding and the limit changed viscosities and stresses only
+  if ((e = mic_project_all2_viscous(ctx))) return e;
+#endif
   if (is_yielding || max_T) {
     if ((e = read_status(ctx))) return e;
     if (is_yielding) *is_yielding = ctx->h_status->is_yielding;

@@ -249,16 +249,18 @@ struct PartialView {
 // ALL2: rho, etaS, k, T, Cp, weight per corner (24) + nearest-node sxy, weight (8) = 32 sums.
 // !ALL2: scalar, weight per corner = 8 sums.  part[acc * ncells + cell].  VISC (with ALL2): only
 // the sums whose marker inputs yielding and the viscosity limit change (etaS per corner, the
-// nearest-node sxy and its weight); the other slots keep the previous ALL2 pass's sums.
+// nearest-node sxy and its weight); the other slots keep the previous ALL2 pass's sums.  FIRST
+// (with ALL2): only the others (rho, k, T, Cp and the weight per corner), for a projection whose
+// viscosity and stress fields a VISC pass replaces before they are read.
 //
 // One loop over the cell's markers (its four quadrant runs back to back, the same order as
 // quadrant by quadrant): a warp's lanes then wait for the longest cell of the warp once, not
 // for the longest run of each quadrant four times.  The nearest-node sums go to a per-thread
 // shared-memory slot picked by the marker's corner, so the loop has no corner branches.
-template <bool ALL2, bool VISC = false>
+template <bool ALL2, bool VISC = false, bool FIRST = false>
 __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v, const int *__restrict__ qs,
                                                          mic_materials mat, double *__restrict__ part) {
-  __shared__ double sloc[ALL2 ? 8 : 1][128];
+  __shared__ double sloc[(ALL2 && !FIRST) ? 8 : 1][128];
   const int ncells = (P.NX - 1) * (P.NY - 1);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
@@ -270,7 +272,7 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
 #pragma unroll
     for (int f = 0; f < NA; ++f) acc[k][f] = 0.0;
   }
-  if (ALL2) {
+  if (ALL2 && !FIRST) {
 #pragma unroll
     for (int k = 0; k < 8; ++k) sloc[k][t] = 0.0;
   }
@@ -283,20 +285,21 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
 #pragma unroll
       for (int k = 0; k < 4; ++k) acc[k][1] = fma(w[k], e, acc[k][1]);
     } else if (ALL2) {
-      const double r = v.rho[m], e = v.eta[m], tt = v.T[m];
+      const double r = v.rho[m], tt = v.T[m];
+      const double e = FIRST ? 0.0 : v.eta[m];
       const int mt = v.mat[m];
       const double kk = mat.materialkThermal[mt], cp = mat.materialCp[mt];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         acc[k][0] = fma(w[k], r, acc[k][0]);
-        acc[k][1] = fma(w[k], e, acc[k][1]);
+        if (!FIRST) acc[k][1] = fma(w[k], e, acc[k][1]);
         acc[k][2] = fma(w[k], kk, acc[k][2]);
         acc[k][3] = fma(w[k], tt, acc[k][3]);
         acc[k][4] = fma(w[k], cp, acc[k][4]);
         acc[k][5] += w[k];
       }
     }
-    if (ALL2) {
+    if (ALL2 && !FIRST) {
       // nearest basic node (mdx0 >= .5, mdy0 >= .5): the weight of that corner, as w[corner]
       const int fl = v.flags[m];
       const int corner = ((fl >> 2) & 1) | (((fl >> 3) & 1) << 1);
@@ -304,7 +307,7 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
       double *L = &sloc[2 * corner][t];
       L[0] = fma(wc, v.sxy[m], L[0]);
       L[128] = __dadd_rn(L[128], wc);
-    } else {
+    } else if (!ALL2) {
       const double sc = v.scalar[m];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
@@ -317,8 +320,8 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
   for (int k = 0; k < 4; ++k) {
 #pragma unroll
     for (int f = 0; f < NA; ++f)
-      if (!VISC || f == 1) part[(size_t)(k * NA + f) * ncells + c] = acc[k][f];
-    if (ALL2) {
+      if ((!VISC || f == 1) && (!FIRST || f != 1)) part[(size_t)(k * NA + f) * ncells + c] = acc[k][f];
+    if (ALL2 && !FIRST) {
       part[(size_t)(24 + 2 * k) * ncells + c] = sloc[2 * k][t];
       part[(size_t)(25 + 2 * k) * ncells + c] = sloc[2 * k + 1][t];
     }
@@ -404,11 +407,13 @@ __device__ __forceinline__ double guarded(double a, double w) { return (w != 0.0
 // 1/w for several sums over one weight (one division; each product within an ulp of the quotient)
 __device__ __forceinline__ double guarded_rcp(double w) { return (w != 0.0) ? 1.0 / w : 0.0; }
 
-// VISC: only the viscosity and stress fields (etaS, soxy, etaN, soxx, soyy); rho, k, T, Cp and
-// the constants keep the values of the previous full pass.
-template <bool VISC>
+// MODE 0 every field; 1 (VISC) only the viscosity and stress fields (etaS, soxy, etaN, soxx,
+// soyy), rho, k, T, Cp and the constants keeping the previous full pass's values; 2 (FIRST) only
+// the others, from basic-cell sums alone (pc unused).
+template <int MODE>
 __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__restrict__ pb,
                                                        const double *__restrict__ pc, All2Out o) {
+  constexpr bool VISC = MODE == 1, FIRST = MODE == 2;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= P.NX || j >= P.NY) return;
@@ -423,11 +428,13 @@ __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__
       const size_t cc = (size_t)cy * NC + cx;
 #pragma unroll
       for (int f = 0; f < 6; ++f)
-        if (!VISC || f == 1 || f == 5) b[f] += pb[(size_t)(k * 6 + f) * ncells + cc];
-      b[6] += pb[(size_t)(24 + 2 * k) * ncells + cc];
-      b[7] += pb[(size_t)(25 + 2 * k) * ncells + cc];
+        if ((!VISC || f == 1 || f == 5) && (!FIRST || f != 1)) b[f] += pb[(size_t)(k * 6 + f) * ncells + cc];
+      if (!FIRST) {
+        b[6] += pb[(size_t)(24 + 2 * k) * ncells + cc];
+        b[7] += pb[(size_t)(25 + 2 * k) * ncells + cc];
+      }
     }
-    if (cx >= 0 && cy >= 0) {  // staggered cells exist for sx in [0, NX-1]
+    if (!FIRST && cx >= 0 && cy >= 0) {  // staggered cells exist for sx in [0, NX-1]
       const size_t ss = (size_t)cy * P.NX + cx;
       c[0] += pc[(size_t)(2 * k) * ns + ss];
       c[1] += pc[(size_t)(2 * k + 1) * ns + ss];
@@ -437,12 +444,15 @@ __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__
     }
   }
   const size_t q = (size_t)j * P.NX + i;
-  const double r0 = guarded_rcp(b[5]), r2 = guarded_rcp(c[4]);  // shared weight sums
-  o.etaS[q] = b[1] * r0;
-  o.soxy[q] = guarded(b[6], b[7]);
-  o.etaN[q] = guarded(c[0], c[1]);
-  o.soxx[q] = c[2] * r2;
-  o.soyy[q] = c[3] * r2;
+  const double r0 = guarded_rcp(b[5]);  // shared weight sums
+  if (!FIRST) {
+    const double r2 = guarded_rcp(c[4]);
+    o.etaS[q] = b[1] * r0;
+    o.soxy[q] = guarded(b[6], b[7]);
+    o.etaN[q] = guarded(c[0], c[1]);
+    o.soxx[q] = c[2] * r2;
+    o.soyy[q] = c[3] * r2;
+  }
   if (!VISC) {
     o.rho[q] = b[0] * r0;
     o.k[q] = b[2] * r0;
@@ -560,10 +570,13 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out, cud
   return MIC_OK;
 }
 
-// visc: the second projection of a step (main:303), after yielding and the viscosity limit changed
-// only viscosities and stresses: the product build then forms only those sums and keeps the
-// first projection's rho, k, T, Cp (same inputs, same order, so the same values)
-static int project_all2(mic_ctx *ctx, bool visc) {
+// mode 0: every field.  1 (visc): the second projection of a step (main:303), after yielding and
+// the viscosity limit changed only viscosities and stresses: the product build then forms only
+// those sums and keeps the first projection's rho, k, T, Cp (same inputs, same order, so the
+// same values).  2 (first, product build, on stream st): the step's first projection (main:268)
+// when a visc pass follows before its viscosity and stress fields are read: only rho, k, T, Cp.
+static int project_all2(mic_ctx *ctx, int mode, cudaStream_t st = nullptr) {
+  const bool visc = mode == 1;
   cudaSetDevice(ctx->device);
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
@@ -596,6 +609,7 @@ static int project_all2(mic_ctx *ctx, bool visc) {
   o.soxy = ctx->nodal[MIC_NF_SOXY];
 #ifdef MIC_EXACT
   (void)visc;  // the exact build gathers every field in reference order each time
+  (void)st;
   {
     MIC_KERNEL(ctx, "k_project_all2");
     k_project_all2<<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, mv, ctx->cell_start, ctx->mat, o);
@@ -616,6 +630,20 @@ static int project_all2(mic_ctx *ctx, bool visc) {
   pv.flags = mv.flags;
   pv.w0 = ctx->wgt[0];
   pv.w1 = ctx->wgt[1];
+  if (mode == 2) {
+    const cudaStream_t s = st ? st : ctx->stream;
+    {
+      MIC_KERNEL_ON(ctx, "k_partials_basic<first>", s);
+      k_partials_basic<true, false, true><<<grid_for(ctx->ncells, 128), 128, 0, s>>>(ctx->P, pv, ctx->quad_start,
+                                                                                     ctx->mat, ctx->part_b);
+    }
+    {
+      MIC_KERNEL_ON(ctx, "k_combine_all2<first>", s);
+      k_combine_all2<2><<<node_grid(ctx->P), 128, 0, s>>>(ctx->P, ctx->part_b, ctx->part_c, o);
+    }
+    MIC_CUDA_TRY(cudaGetLastError());
+    return MIC_OK;
+  }
   // the cell-centre sums on the second stream, beside the basic-cell sums: both only read the
   // markers and each runs at a fraction of the SMs' warp slots
   MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
@@ -637,10 +665,10 @@ static int project_all2(mic_ctx *ctx, bool visc) {
   MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));  // the cell-centre sums
   if (visc) {
     MIC_KERNEL(ctx, "k_combine_all2<visc>");
-    k_combine_all2<true><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
+    k_combine_all2<1><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
   } else {
     MIC_KERNEL(ctx, "k_combine_all2");
-    k_combine_all2<false><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
+    k_combine_all2<0><<<node_grid(ctx->P), 128, 0, ctx->stream>>>(ctx->P, ctx->part_b, ctx->part_c, o);
   }
 #endif
   MIC_CUDA_TRY(cudaGetLastError());
@@ -649,10 +677,19 @@ static int project_all2(mic_ctx *ctx, bool visc) {
 
 extern "C" int mic_project_markers_nodes_all2(mic_ctx *ctx) {
   if (!ctx) return MIC_ERR_ARG;
-  return project_all2(ctx, false);
+  return project_all2(ctx, 0);
 }
 
-int mic_project_all2_viscous(mic_ctx *ctx) { return project_all2(ctx, true); }
+int mic_project_all2_viscous(mic_ctx *ctx) { return project_all2(ctx, 1); }
+
+int mic_project_all2_first(mic_ctx *ctx, cudaStream_t s) {
+#ifdef MIC_EXACT
+  (void)s;
+  return project_all2(ctx, 0);
+#else
+  return project_all2(ctx, 2, s);
+#endif
+}
 
 extern "C" int mic_project_marker_field_to_nodes(mic_ctx *ctx, int off, const double *matprop, int out_field,
                                                  int stagx, int stagy, int method) {
