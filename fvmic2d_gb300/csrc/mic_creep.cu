@@ -549,7 +549,7 @@ extern "C" int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iteratio
   return MIC_OK;
 }
 
-// ---- the survey's names for the closure's exports ----------------------------------------------
+// ---- the closure's exports under their short names (exact solve, training, inference) --------
 
 // exact composite-creep Newton solve of a host batch (mic_creep_solve_batch, mode 0)
 extern "C" int mic_creep_newton(mic_ctx *ctx, const double *edot, const double *T, const double *d,

@@ -377,7 +377,8 @@ def test_project_from_scalar_matches_oracle():
     assert ok, msg
 
 
-def test_survey_named_exports():
+def test_short_named_creep_exports():
+    """mic_creep_newton is mic_creep_solve_batch's exact mode, bit for bit"""
     wl = W.ice_creep_box(nx_cells=8, ny_cells=8, nm=2, seed=4)
     G = gpu.MicProblem(wl)
     L = G.L
