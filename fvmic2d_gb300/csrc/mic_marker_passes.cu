@@ -766,13 +766,12 @@ struct AdvectCols {
 // advectMarkersRK (markers.c:1865-2250), non-periodic grid, non-JAUMANN rotation
 // wz_known (product build): the marker's wxy column holds the vorticity k_strain_pressure of this
 // step interpolated at the marker (the first stage's value: same nodes, weights and order)
-__global__ void __launch_bounds__(512, 2) k_advect(Params P, AdvectCols c, Geo g, const double *__restrict__ vx, const double *__restrict__ vy,
-                                                   const double *__restrict__ wz, mic_bcinfo top, mic_bcinfo left,
-                                                   double dt, int64_t n, int wz_known) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (m >= n) return;
-  const int ci = c.cellX[m], cj = c.cellY[m];
-  if (ci == -1) return;
+// one in-domain marker m in stored cell (ci, cj); returns its rotated sxx
+__device__ __forceinline__ double advect_marker(const Params &P, const AdvectCols &c, const Geo &g,
+                                                const double *__restrict__ vx, const double *__restrict__ vy,
+                                                const double *__restrict__ wz, const mic_bcinfo &top,
+                                                const mic_bcinfo &left, double dt, int64_t m, int ci, int cj,
+                                                int wz_known) {
   const int NX = P.NX, NY = P.NY;
   const double X0 = c.X[m], Y0 = c.Y[m];
   double xcur = X0, ycur = Y0;
@@ -920,11 +919,43 @@ __global__ void __launch_bounds__(512, 2) k_advect(Params P, AdvectCols c, Geo g
   double ct, st_, s2, c2;
   small_angle_rotation(th, ct, st_, s2, c2);
 #endif
-  c.sxx[m] = s11 * (ct * ct) + s22 * (st_ * st_) - s12 * s2;
+  const double nsxx = s11 * (ct * ct) + s22 * (st_ * st_) - s12 * s2;
+  c.sxx[m] = nsxx;
   c.syy[m] = s11 * (st_ * st_) + s22 * (ct * ct) + s12 * s2;
   c.sxy[m] = 0.5 * (s11 - s22) * s2 + s12 * c2;
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   c.Eii[m] = c.Eii[m] + dt * sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+  return nsxx;
+}
+
+// MAXS: also max |sxx| over the in-domain markers after the rotation (main_subduction.c:437-448,
+// from 0, bit patterns of non-negative doubles), one atomic per block into *maxs
+template <bool MAXS>
+__global__ void __launch_bounds__(512, 2) k_advect(Params P, AdvectCols c, Geo g, const double *__restrict__ vx,
+                                                   const double *__restrict__ vy, const double *__restrict__ wz,
+                                                   mic_bcinfo top, mic_bcinfo left, double dt, int64_t n,
+                                                   int wz_known, unsigned long long *maxs) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  long long b = 0;  // bits of 0.0
+  if (m < n) {
+    const int ci = c.cellX[m], cj = c.cellY[m];
+    if (ci != -1) {
+      const double a = fabs(advect_marker(P, c, g, vx, vy, wz, top, left, dt, m, ci, cj, wz_known));
+      if (MAXS && a > 0.0) b = __double_as_longlong(a);
+    }
+  }
+  if (MAXS) {
+    __shared__ long long wmax[32];
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wmax[warp] = b;
+    __syncthreads();
+    if (warp == 0) {
+      b = lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0;
+      for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+      if (lane == 0 && b > 0) atomicMax(maxs, (unsigned long long)b);
+    }
+  }
 }
 
 // max over in-domain markers of v (or |v|), starting from 0 (main_subduction.c:271-281, 437-448)
@@ -1371,9 +1402,12 @@ extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
   return MIC_OK;
 }
 
-static int advect_launch(mic_ctx *ctx, double dt, bool wz_known) {
+// with_max: max |sxx| after the rotation into the reduction slot as well (run_max's)
+static int advect_launch(mic_ctx *ctx, double dt, bool wz_known, bool with_max = false) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
+  unsigned long long *d = reinterpret_cast<unsigned long long *>(ctx->red_buf + 8);
+  if (with_max) MIC_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
   if (ctx->n > 0) {
     AdvectCols c;
     c.cellX = ctx->i32[C_CELLX];
@@ -1392,10 +1426,15 @@ static int advect_launch(mic_ctx *ctx, double dt, bool wz_known) {
     c.exy = ctx->f64[C_EXY];
     {
       MIC_KERNEL(ctx, "k_advect");
-      k_advect<<<grid_for(ctx->n, tuned_block(ctx, TU_ADVECT)), tuned_block(ctx, TU_ADVECT), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX],
-                                                             ctx->nodal[MIC_NF_VY],
-                                                             ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
-                                                             ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0);
+      const int B = tuned_block(ctx, TU_ADVECT);
+      if (with_max)
+        k_advect<true><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(
+            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY],
+            ctx->bcs.mechBCTop, ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0, d);
+      else
+        k_advect<false><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(
+            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY],
+            ctx->bcs.mechBCTop, ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0, nullptr);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }
@@ -1515,8 +1554,15 @@ extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_st
 static int post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx, bool wz_known) {
   int e;
   if ((e = mic_subgrid_temperature_changes(ctx, dt_thermal))) return e;
-  if ((e = advect_launch(ctx, dt_thermal, wz_known))) return e;
-  return run_max(ctx, C_SXX, 1, max_abs_sxx);
+  // the advection also forms max |sxx| of the rotated stresses (main:437-448)
+  if ((e = advect_launch(ctx, dt_thermal, wz_known, true))) return e;
+  if (max_abs_sxx) {
+    unsigned long long h = 0;
+    MIC_CUDA_TRY(cudaMemcpyAsync(&h, ctx->red_buf + 8, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    memcpy(max_abs_sxx, &h, sizeof(double));
+  }
+  return MIC_OK;
 }
 
 extern "C" int mic_step_post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx) {

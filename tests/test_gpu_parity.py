@@ -415,3 +415,17 @@ def test_step_split_reports_max_temperature_and_yielding():
     inside = ~out
     assert mt.value == ref_t == float(np.max(m["T"][inside]))
     assert isy.value == ref_y
+    # the rest of the step: max |sxx| formed by the advection equals mic_max_abs_sxx's
+    B.limitViscosity()
+    B.projectMarkersNodesAll2()
+    assert A.L.mic_step_post_stokes(A.h, wl.dt, 1, None) == 0
+    B.updateMarkerStrainPressure(wl.dt)
+    B.updateGlobalStrainRateResidual(0)
+    B.subgridStressChanges(wl.dt, wl.options.subgridStressDiffusivity)
+    B.updateMarkerStress()
+    mx = ctypes.c_double(-1.0)
+    assert A.L.mic_step_post_thermal(A.h, wl.dt_thermal, ctypes.byref(mx)) == 0
+    B.subgridTemperatureChanges(wl.dt_thermal)
+    B.advectMarkersRK(wl.dt_thermal)
+    assert mx.value == B.maxAbsSxx() > 0.0
+    assert not compare_markers(A.markers, B.markers)
