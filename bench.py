@@ -72,13 +72,13 @@ KERNEL_BYTES = {
 # the 32 B/marker of stored offsets the first RK4 stage loads instead of forming them (bytes for
 # FP64 instructions); at the small size part of the written bytes is still in L2 when the kernel
 # ends.
-KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (127414016 + 31936000) / 1048576}
+KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (127373312 + 32452608) / 1048576}
 # FP64 work per marker from the same capture (per-cycle DFMA / DADD / DMUL thread instructions x
-# elapsed cycles / markers: 68.0 / 60.0 / 33.0): flops with DFMA counted twice, and the FP64
-# arithmetic instructions (the three summed, 161.0).  The kernels of this path are bound by the
+# elapsed cycles / markers: 67.9 / 60.9 / 32.9): flops with DFMA counted twice, and the FP64
+# arithmetic instructions (the three summed, 161.7).  The kernels of this path are bound by the
 # FP64 pipe, which issues 2 FP64 instructions per SM per clock on GB300, not by HBM.
-KERNEL_FP64_FLOPS_PER_MARKER = {"k_advect": 228.9}
-KERNEL_FP64_INST_PER_MARKER = {"k_advect": 161.0}
+KERNEL_FP64_FLOPS_PER_MARKER = {"k_advect": 229.6}
+KERNEL_FP64_INST_PER_MARKER = {"k_advect": 161.7}
 FP64_PEAK_TFLOPS = 2 * 2 * 152 * 2.07e9 / 1e12  # 2 DFMA/SM/clk x 2 flops x 152 SMs x 2.07 GHz
 FP64_PEAK_GINST = 2 * 152 * 2.07  # FP64 instructions per second, in G
 
