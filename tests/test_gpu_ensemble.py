@@ -127,3 +127,26 @@ def test_ensemble_autotune_keeps_states_and_results():
     for a, b in zip(A, B):
         assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
         assert np.array_equal(a.get_nodal("lastT"), b.get_nodal("lastT"))
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_plastic_members_match_members_stepped_alone(graph):
+    """Visco-elasto-plastic members (yielding, so the step's viscosity-only second projection
+    and its first projection beside the yield pass on each member's second stream both matter),
+    of different sizes, stepped together as captured graphs or on streams: each member's markers
+    and nodal fields are what stepping it alone gives, bit for bit"""
+    wls = [W.vep_slab_box(nx_cells=nx, ny_cells=ny, nm=4, seed=s)
+           for nx, ny, s in ((32, 8, 71), (48, 12, 72), (24, 6, 73))]
+    A = [gpu.MicProblem(wl) for wl in wls]
+    B = [gpu.MicProblem(wl) for wl in wls]
+    E = gpu.MicEnsemble(A)
+    dts = np.array([wl.dt for wl in wls])
+    for _ in range(3):
+        E.step(dts, dts, subgrid_stress=1, graph=graph)
+        for b, wl in zip(B, wls):
+            b.step(wl.dt, wl.dt)
+    E.synchronize()
+    for a, b in zip(A, B):
+        assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
+        for f in ("rho", "etaN", "etaS", "soxx", "soxy", "lastT", "kThermal", "dsxx"):
+            assert np.array_equal(a.get_nodal(f), b.get_nodal(f)), f
