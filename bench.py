@@ -1,19 +1,24 @@
 """Benchmark: markers/s per step of the marker-in-cell transfer path on GB300.
 
-Workload (default): the visco-elasto-plastic two-material 4:1 box, 1025 x 257 nodes,
-4,194,304 markers, FP64 -- the path's headline configuration.  A step is one pass of
-fvmic2d's marker path in main_subduction.c order (bin + stable sort, density update,
-projectMarkersNodesAll2, max T, checkPlasticYielding, limitViscosity,
-projectMarkersNodesAll2, updateMarkerStrainPressure, updateGlobalStrainRateResidual,
-subgridStressChanges, updateMarkerStress, subgridTemperatureChanges, advectMarkersRK,
-max |sxx|), with the host Stokes/thermal solves outside the timed region; their nodal
-outputs are synthetic inputs held on the device.
+Workload (default): the composite ice creep box, 1025 x 1025 nodes, 16,777,216 markers, material
+law 7 (the Goldsby-Kohlstedt law of viscosity.c:106-179 inverted per marker), FP64 -- the
+configuration the metric is quoted on.  A step is one pass of fvmic2d's marker path in
+main_subduction.c order (bin + stable sort, density update, projectMarkersNodesAll2, max T,
+checkPlasticYielding, limitViscosity, projectMarkersNodesAll2, updateMarkerStrainPressure,
+updateGlobalStrainRateResidual, subgridStressChanges, updateMarkerStress,
+subgridTemperatureChanges, advectMarkersRK, max |sxx|), with the host Stokes/thermal solves
+outside the timed region; their nodal outputs are synthetic inputs held on the device.  The
+law-7 stress solve runs two ways on the same context: the plain exact solve, and the trained
+surrogate with the hidden layer on the tensor cores, FP64 polish and exact fallback.  `value` is
+the surrogate path's markers/s; the plain path's sits beside it under `plain`.  The
+visco-elasto-plastic box (1025 x 257 nodes, 4,194,304 markers) and the ensembles ride along as
+extra legs.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 
-One JSON line on rank 0.  Under torchrun (N > 1) every rank runs an independent replica
-on its own GPU (the path shards only across independent problems); value = all markers
-processed / max-over-ranks time.
+One JSON line on rank 0.  Under torchrun (N > 1) every rank runs an independent replica on its
+own GPU (the path shards only across independent problems); value = all markers processed /
+max-over-ranks time.
 """
 import argparse
 import json
@@ -30,8 +35,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "markers/s per step (project+advect+rheology), plain vs surrogate @1e-6 rel err"
-WORKLOAD_DESC = ("vep_slab_box: 1025x257 staggered grid (2x refined top 20%), 16 markers/cell, "
-                 "4,194,304 markers, two materials, Mohr-Coulomb yield, FP64")
+WORKLOAD_DESC = {
+    "ice_creep_box": ("ice_creep_box: 1025x1025 uniform nodes, 16 markers/cell, 16,777,216 markers, composite ice "
+                      "creep (law 7) with per-marker log10 edot ~ U[-18,-10] 1/s, T ~ U[100,273] K, log10 grain size "
+                      "~ U[-4,-1] m, P ~ U[0,1e8] Pa (SplitMix64 seed 3); MLP 4->64->64->1, BF16 hidden layer on the "
+                      "tensor cores with FP32 accumulation, FP64 polish to |rate/edot - 1| <= 1e-7, exact fallback; FP64"),
+    "vep_slab_box": ("vep_slab_box: 1025x257 staggered grid (2x refined top 20%), 16 markers/cell, "
+                     "4,194,304 markers, two materials, Mohr-Coulomb yield, FP64"),
+}
+# the bounded sample of each workload that the host-core baseline steps: the same generator and
+# per-marker distributions on a smaller grid
+CPU_SAMPLE = {"ice_creep_box": "ice_creep_box_sample", "vep_slab_box": "vep_slab_box_sample",
+              "ice_creep_box_4m": "ice_creep_box_sample", "vep_slab_box_1m": "vep_slab_box_sample"}
+CPU_SAMPLE_DESC = {"ice_creep_box_sample": "129x129 nodes, 262,144 markers",
+                   "vep_slab_box_sample": "257x65 nodes, 262,144 markers"}
+# law-7 settings of the timed paths: exact solve to |rate/edot - 1| <= 2e-14; surrogate polish to
+# 1e-7 (stress within 1e-7 of the exact root) in at most 3 steps, else the exact solve
+CREEP_TOL, CREEP_MAXIT, POLISH_ITERS, POLISH_TOL = 2e-14, 60, 3, 1e-7
 
 # Host-solve outputs that cross the boundary each step in the drop-in model (markers stay
 # resident on the device): nodal inputs up, projected nodal fields down.
@@ -86,14 +106,13 @@ FP64_PEAK_GINST = 2 * 152 * 2.07  # FP64 instructions per second, in G
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="vep_slab_box")
-    ap.add_argument("--no-surrogate", action="store_true", help="skip the composite-creep surrogate leg")
-    ap.add_argument("--no-ensemble", action="store_true", help="skip the convection-ensemble leg")
-    ap.add_argument("--creep-mode", type=int, default=0, choices=[0, 1, 2],
-                    help="law-7 solve of the main leg: 0 exact, 1 FP32 surrogate, 2 tensor-core surrogate")
+    ap.add_argument("--workload", default="ice_creep_box")
+    ap.add_argument("--no-legs", action="store_true", help="main workload only (no VEP, ensemble, systems legs)")
+    ap.add_argument("--no-vep", action="store_true", help="skip the visco-elasto-plastic box leg")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble legs")
     ap.add_argument("--no-systems", action="store_true", help="skip the linear-systems / whole-time-step leg")
     ap.add_argument("--only-systems", action="store_true",
                     help="run only the linear-systems / whole-time-step leg and print it (for profiling the solver)")
@@ -110,8 +129,9 @@ def make_workload(name):
 
 
 # ---------------------------------------------------------------------------------------
-# CPU legs: the CPU restatement of the reference path (oracle/liboracle.so), one process per
-# core, each running whole steps of the full workload (spawned before any GPU work).
+# CPU legs: the CPU restatement of the reference path (oracle/liboracle.so, gcc -O2
+# -ffp-contract=off), one process per core, each stepping its own replica of a bounded sample of
+# the workload (spawned before any GPU work).
 
 
 def _cpu_worker(args):
@@ -121,6 +141,8 @@ def _cpu_worker(args):
 
     wl = make_workload(name)
     P = oraclepy.OracleProblem(wl)
+    if getattr(wl, "grain_size", None) is not None:
+        P.set_grain_size(wl.grain_size)
     for _ in range(warmup):
         P.step(wl.dt, wl.dt_thermal)
     barrier.wait()
@@ -151,6 +173,22 @@ def cpu_throughput(name, cores, steps, warmup):
 def host_cores(requested):
     n = os.cpu_count() or 1
     return max(1, min(n, requested)) if requested else n
+
+
+def cpu_sample(name):
+    """the workload the host-core baseline steps for `name` (itself when it has no smaller sample)"""
+    return CPU_SAMPLE.get(name, name)
+
+
+def cpu_sample_text(name, cores, steps, rate1=None, ms1=None):
+    sample = cpu_sample(name)
+    what = ("%s (%s; the full workload's generator and per-marker distributions on a smaller grid)"
+            % (sample, CPU_SAMPLE_DESC[sample]) if sample in CPU_SAMPLE_DESC else "the full workload " + sample)
+    txt = ("%d step(s) per replica of %s, %d concurrent single-threaded replicas; CPU restatement of the reference "
+           "path, gcc -O2 -ffp-contract=off (the reference tree is not on this host)" % (steps, what, cores))
+    if rate1 is not None:
+        txt += "; single replica: %.4g markers/s, %.0f ms/step" % (rate1, ms1)
+    return txt
 
 
 # ---------------------------------------------------------------------------------------
@@ -251,71 +289,50 @@ def sum_over_ranks(pg, v):
     return float(t.item())
 
 
-def base_config(wl, args, world):
-    return {"workload": WORKLOAD_DESC if args.workload == "vep_slab_box" else args.workload,
+def base_config(wl, name, world):
+    return {"workload": WORKLOAD_DESC.get(name, name),
             "markers_per_replica": int(len(wl.markers)), "nodes": [wl.grid.NX, wl.grid.NY],
             "parallelism": "replicas x%d (independent problems, no collective)" % world,
             "l2": "inputs larger than L2 (marker state %.2f GB per replica)" % (len(wl.markers) * 208 / 1e9),
-            "timed": "bin+sort, rho, project x2, max T, yield, limit, strain/pressure, residual, subgrid stress, "
-                     "stress update, subgrid T, RK4 advection, max |sxx|; host solves excluded"}
+            "timed": "bin+sort, rho, project x2, max T, yield (law-7 stress solve), limit, strain/pressure, residual, "
+                     "subgrid stress, stress update, subgrid T, RK4 advection, max |sxx|; host solves excluded"}
 
 
 def run_reference_arm(args):
+    """The reference's CPU path on the host cores: the C restatement (pinned bit for bit to the
+    reference's own sources, which are not on this host), one single-threaded replica per core,
+    each stepping a bounded sample of the workload for warmup + steps steps."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
     cores = host_cores(args.cpu_cores)
-    rate, ms = cpu_throughput(args.workload, cores, args.steps, args.warmup)
+    rate, ms = cpu_throughput(cpu_sample(args.workload), cores, args.steps, args.warmup)
     wl = make_workload(args.workload)
     line = {"metric": METRIC, "value": rate, "unit": "markers/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-            "config": base_config(wl, args, 1), "impl": "reference",
+            "config": base_config(wl, args.workload, 1), "impl": "reference",
             "cpu_baseline": {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
-                             "sample": "%d concurrent single-threaded replicas x %d steps of the full workload "
-                                       "(CPU restatement of the reference path; the reference tree is not on "
-                                       "this host)" % (cores, args.steps)},
+                             "sample": cpu_sample_text(args.workload, cores, args.steps)},
             "e2e": {"value": rate, "unit": "markers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args):
-    world, rank, local, pg = dist_setup(args)
-    if args.only_systems:
-        if rank == 0:
-            import torch
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return float(json.load(open(path))["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback"
 
-            torch.cuda.set_device(local)
-            print(json.dumps({"systems": systems_leg(args, local)}), flush=True)
-        return
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        # bounded sample: one step per replica on all host cores, spawned before any GPU work
-        cores = host_cores(args.cpu_cores)
-        rate, ms = cpu_throughput(args.workload, cores, 1, 0)
-        rate1, ms1 = cpu_throughput(args.workload, 1, 1, 0)
-        cpu = {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
-               "sample": "1 step of the full workload per replica, %d concurrent replicas "
-                         "(single replica: %.3g markers/s, %.0f ms/step)" % (cores, rate1, ms1)}
-    import ctypes
 
-    import numpy as np
+def timed_steps(G, wl, args, pg, label):
+    """warmup, launch shapes, then `steps` steps between CUDA events on the context's stream, and
+    the same steps again with an event pair around every launch for the per-kernel durations"""
     import torch
 
     from fvmic2d_gb300 import gpu
-    from fvmic2d_gb300.mic_types import NF
 
-    torch.cuda.set_device(local)
-    wl = make_workload(args.workload)
-    G = gpu.MicProblem(wl, device=local)
-    if getattr(wl, "grain_size", None) is not None:
-        G.set_grain_size(wl.grain_size)
-    if args.creep_mode:
-        G.creep_train()
-        G.creep_configure(mode=args.creep_mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
     L, h = G.L, G.h
-    stream = torch.cuda.ExternalStream(G.stream(), device=local)
-    n = len(wl.markers)
-    nodes = wl.grid.NX * wl.grid.NY
+    stream = torch.cuda.ExternalStream(G.stream(), device=G.device)
     sub = 1 if wl.options.subgridStressDiffusivity > 0 else 0
 
     def step():
@@ -331,7 +348,7 @@ def run_ours(args):
     launches0 = G.launch_count()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    with ClockSampler(G.device) as clk:
         torch.cuda.synchronize()
         barrier(pg)
         torch.cuda.synchronize()
@@ -344,8 +361,6 @@ def run_ours(args):
         barrier(pg)
     launches = G.launch_count() - launches0
     ms_total = ev0.elapsed_time(ev1)
-    # the same steps again with an event pair around every launch, for the per-kernel durations
-    # (kept out of the headline timing above: the extra event records ride on the stream)
     G.profile_enable(max(64, 64 * args.steps))  # room for every launch (44 per step)
     for _ in range(args.steps):
         step()
@@ -354,13 +369,58 @@ def run_ours(args):
     G.profile_enable(0)
     recorded = sum(v[1] for v in prof.values())
     if recorded != launches:  # a truncated record would understate every per-step figure
-        raise RuntimeError("per-launch profile holds %d of %d launches" % (recorded, launches))
+        raise RuntimeError("per-launch profile holds %d of %d launches (%s)" % (recorded, launches, label))
+    n = G.n
     t_max = max_over_ranks(pg, ms_total)
-    markers_all = sum_over_ranks(pg, float(n * args.steps))
-    value = markers_all / (t_max * 1e-3)
-    ms_step = t_max / args.steps
+    value = sum_over_ranks(pg, float(n * args.steps)) / (t_max * 1e-3)
+    out = {"value": value, "unit": "markers/s", "ms_per_step": t_max / args.steps, "gpu_launches": launches,
+           "launch_tuning": tuning, "clocks": clk.summary()}
+    return out, prof
 
-    # ---- end to end through the C ABI with pinned host buffers --------------------------
+
+def roofline(prof, n, nodes, steps, hbm_peak, peak_src):
+    """HBM roofline of the step's dominant kernel (live CUDA-event duration), with its FP64 issue
+    rate where ncu measured its FP64 instructions per marker"""
+    kern = sorted(prof.items(), key=lambda kv: -kv[1][0])
+    top_name, (top_ms, top_cnt) = kern[0]
+    per_marker, per_node = KERNEL_BYTES.get(top_name, (0, 0))
+    algo = per_marker * n + per_node * nodes
+    dur = top_ms / max(top_cnt, 1)
+    achieved = algo / (dur * 1e-3) / 1e9
+    prof_total = sum(v[0] for v in prof.values())
+    roof = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak,
+            "traffic": (KERNEL_TRAFFIC_PER_MARKER[top_name] * n if top_name in KERNEL_TRAFFIC_PER_MARKER else None),
+            "traffic_note": "ncu dram bytes of a smaller capture of the same kernel, scaled by markers processed",
+            "peak_source": peak_src, "algorithmic_bytes_per_launch": algo, "ms_per_launch": dur}
+    fp64 = None
+    if top_name in KERNEL_FP64_INST_PER_MARKER:
+        ipm = KERNEL_FP64_INST_PER_MARKER[top_name]
+        fpm = KERNEL_FP64_FLOPS_PER_MARKER[top_name]
+        fp64 = {"kernel": top_name, "flops_per_marker": fpm, "achieved": fpm * n / (dur * 1e-3) / 1e12,
+                "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": fpm * n / (dur * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
+                "inst_per_marker": ipm, "issue_frac": ipm * n / (dur * 1e-3) / 1e9 / FP64_PEAK_GINST,
+                "note": "the bound that applies: FP64 pipe, 2 FP64 instructions/SM/clk; flops and instructions per "
+                        "marker from ncu; issue_frac = FP64 instructions issued / peak"}
+    shares = {k: round(v[0] / prof_total, 4) for k, v in kern[:12]}
+    per_step = {k: round(v[0] / steps, 4) for k, v in kern[:12]}
+    return roof, fp64, shares, per_step
+
+
+def e2e_run(G, wl, steps, pg):
+    """the same step end to end through the C ABI with pinned host buffers: the host-solve nodal
+    fields up and the projected nodal fields down every step"""
+    import ctypes
+
+    import numpy as np
+
+    from fvmic2d_gb300.mic_types import NF
+
+    L, h = G.L, G.h
+    nodes = wl.grid.NX * wl.grid.NY
+    n = G.n
+    sub = 1 if wl.options.subgridStressDiffusivity > 0 else 0
+
     def pinned(nbytes):
         p = ctypes.c_void_p()
         assert L.mic_host_alloc(ctypes.byref(p), nbytes) == 0
@@ -387,7 +447,7 @@ def run_ours(args):
         assert L.mic_step(h, wl.dt, wl.dt_thermal, sub, ctypes.byref(res)) == 0
         assert L.mic_nodal_download_many(h, dn_f, dn_p, len(down_bufs)) == 0
 
-    e2e_steps = max(3, min(args.steps, 50))
+    e2e_steps = max(3, min(steps, 50))
     e2e_step()
     G.synchronize()
     barrier(pg)
@@ -396,16 +456,114 @@ def run_ours(args):
         e2e_step()
     G.synchronize()
     t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
-    e2e_value = sum_over_ranks(pg, float(n * e2e_steps)) / t_e2e
+    value = sum_over_ranks(pg, float(n * e2e_steps)) / t_e2e
     for _, p, _ in up_bufs + down_bufs:
         L.mic_host_free(p)
+    return {"value": value, "unit": "markers/s", "h2d_bytes_per_step": len(E2E_UP) * nodes * 8,
+            "d2h_bytes_per_step": len(E2E_DOWN) * nodes * 8 + 8,
+            "model": "markers resident on the device; host-solve nodal fields up and projected nodal fields down "
+                     "every step from/to pinned host buffers through mic_nodal_upload_many / mic_step / "
+                     "mic_nodal_download_many"}
 
-    # ---- density control (checkMarkerDensity, called every step by the reference) after the
-    # timed steps moved the markers; the reference's default bounds (1 and 100 per quarter cell)
-    from fvmic2d_gb300.mic_types import DensityOptions
 
-    dens = None
-    if rank == 0:  # after the end-to-end run: the marker count may change
+def surrogate_error_in_step(G, wl):
+    """The surrogate's stress error on the stepped workload, judged by the exact solve: the
+    law-7 viscosity of every marker from the same marker state by checkPlasticYielding with the
+    exact solve and with the surrogate (eta = s* / (2 edot), so the relative viscosity error is the
+    relative stress error; the ice has no plastic yield, so the pass leaves everything but eta and
+    mu as it found it)"""
+    import numpy as np
+
+    G.creep_configure(mode=0, tol=CREEP_TOL, maxit=CREEP_MAXIT, polish_iters=POLISH_ITERS, polish_tol=POLISH_TOL)
+    G.checkPlasticYielding(wl.dt)
+    eta0 = G.markers["eta"]
+    G.creep_configure(mode=2, tol=CREEP_TOL, maxit=CREEP_MAXIT, polish_iters=POLISH_ITERS, polish_tol=POLISH_TOL)
+    G.checkPlasticYielding(wl.dt)
+    st = G.creep_stats()
+    eta2 = G.markers["eta"]
+    ok = np.isfinite(eta0) & (eta0 > 0)
+    rel = np.abs(eta2[ok] / eta0[ok] - 1.0)
+    return {"max": float(rel.max()), "median": float(np.median(rel)), "markers": int(ok.sum()),
+            "fallbacks": st["fallbacks"], "max_residual": st["max_residual"], "tc_timeouts": st["tc_timeouts"],
+            "sample": "every marker of the workload after the timed steps: surrogate vs exact solve from the same "
+                      "state (one checkPlasticYielding pass each)"}
+
+
+def surrogate_error_batch(G):
+    """the same comparison on 1,048,576 fresh samples of the workload's input distribution"""
+    import numpy as np
+
+    from fvmic2d_gb300 import workloads as W
+
+    m = 1 << 20
+    u = W.splitmix64_uniform(11, 4 * m)
+    edot, T, d, P = 10 ** (-18 + 8 * u[0::4]), 100 + 173 * u[1::4], 10 ** (-4 + 3 * u[2::4]), 1e8 * u[3::4]
+    G.creep_configure(mode=0, tol=CREEP_TOL, maxit=CREEP_MAXIT, polish_iters=POLISH_ITERS, polish_tol=POLISH_TOL)
+    s0, it0, _, _ = G.creep_solve(edot, T, d, P, mode=0)
+    s2, it2, _, fb = G.creep_solve(edot, T, d, P, mode=2)
+    rel = np.abs(s2 / s0 - 1.0)
+    return {"max": float(rel.max()), "median": float(np.median(rel)), "fallbacks": int(fb.sum()),
+            "iters_exact": float(it0.mean()), "iters_surrogate": float(it2.mean()),
+            "sample": "%d solves, tensor-core surrogate vs exact" % m}
+
+
+def measure_workload(args, name, local, pg, world, cpu=None, with_e2e=True, with_density=True):
+    """One marker-path workload timed on one context: for law 7 the exact solve ("plain") and the
+    tensor-core surrogate, the surrogate being the headline; otherwise the plain path."""
+    import torch
+
+    from fvmic2d_gb300 import gpu
+
+    wl = make_workload(name)
+    G = gpu.MicProblem(wl, device=local)
+    G.device = local
+    law7 = getattr(wl, "grain_size", None) is not None
+    out = {}
+    if law7:
+        G.set_grain_size(wl.grain_size)
+        t0 = time.perf_counter()
+        hist = G.creep_train()
+        torch.cuda.synchronize()
+        out["train"] = {"seconds": round(time.perf_counter() - t0, 3), "loss_final": float(hist[-200:].mean()),
+                        "loss_first": float(hist[:50].mean()),
+                        "note": "surrogate trained on the GPU (2,097,152 exact solves, 10,000 Adam steps), "
+                                "outside the timed region"}
+    modes = [("plain", 0), ("surrogate_tc", 2)] if law7 else [("plain", 0)]
+    hbm_peak, peak_src = read_peaks()
+    n, nodes = G.n, wl.grid.NX * wl.grid.NY
+    for label, mode in modes:
+        if law7:
+            G.creep_configure(mode=mode, tol=CREEP_TOL, maxit=CREEP_MAXIT, polish_iters=POLISH_ITERS,
+                              polish_tol=POLISH_TOL)
+        rec, prof = timed_steps(G, wl, args, pg, label)
+        roof, fp64, shares, per_step = roofline(prof, n, nodes, args.steps, hbm_peak, peak_src)
+        rec.update({"roofline": roof, "fp64_roofline": fp64, "kernel_share": shares, "kernel_ms_per_step": per_step})
+        if law7:
+            st = G.creep_stats()
+            yk = [k for k in prof if k.startswith("k_yield")]
+            rec.update({"yield_kernel": yk[0] if yk else None,
+                        "yield_ms_per_step": prof[yk[0]][0] / args.steps if yk else None,
+                        "newton_iters_per_marker": st["iterations"] / max(st["markers"], 1),
+                        "fallbacks_per_step": st["fallbacks"], "tc_timeouts": st["tc_timeouts"],
+                        "max_residual": st["max_residual"]})
+        step_bytes = STEP_BYTES_PER_MARKER * n + STEP_BYTES_PER_NODE * nodes + (8 * n if law7 else 0)
+        gbs = step_bytes / (rec["ms_per_step"] * 1e-3) / 1e9
+        rec["step_roofline"] = {"algorithmic_bytes_per_step": step_bytes, "achieved_gbs": gbs, "frac": gbs / hbm_peak}
+        out[label] = rec
+    head = out["surrogate_tc" if law7 else "plain"]
+    if law7:
+        out["speedup_surrogate_vs_plain"] = head["value"] / out["plain"]["value"]
+        out["yield_speedup_surrogate_vs_plain"] = out["plain"]["yield_ms_per_step"] / head["yield_ms_per_step"]
+    if with_e2e:
+        out["e2e"] = e2e_run(G, wl, args.steps, pg)  # in the headline mode (the last configured)
+    if law7:
+        out["stress_rel_err"] = surrogate_error_in_step(G, wl)
+        out["stress_rel_err_batch"] = surrogate_error_batch(G)
+    if with_density and int(os.environ.get("RANK", "0")) == 0:
+        # checkMarkerDensity (called every step by the reference) after the steps moved the
+        # markers, with the reference's default bounds (1 and 100 per quarter cell)
+        from fvmic2d_gb300.mic_types import DensityOptions
+
         dopt = DensityOptions(NMX=4, NMY=4, minMarkers=1, maxMarkers=100)
         G.synchronize()
         t0 = time.perf_counter()
@@ -415,134 +573,83 @@ def run_ours(args):
             a, r_ = G.checkMarkerDensity(dopt)
             tot_add += a
             tot_rem += r_
-        dens = {"ms_per_call": (time.perf_counter() - t0) * 1e3 / reps, "markers_added": tot_add,
-                "markers_removed": tot_rem, "calls": reps,
-                "note": "host wall time per call, including its host synchronisations"}
-
-    if rank != 0:
-        return
-    # ---- roofline of the dominant kernel (live CUDA-event timing over the timed region) ------
-    import json as _json
-
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        hbm_peak = float(_json.load(open(peaks_path))["hbm_gbs"])
-        peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
-    else:
-        hbm_peak, peak_src = 6800.0, "fallback"
-    kern = sorted(prof.items(), key=lambda kv: -kv[1][0])
-    top_name, (top_ms, top_cnt) = kern[0]
-    per_marker, per_node = KERNEL_BYTES.get(top_name, (0, 0))
-    algo = per_marker * n + per_node * nodes
-    dur = top_ms / max(top_cnt, 1)
-    achieved = algo / (dur * 1e-3) / 1e9
-    step_bytes = STEP_BYTES_PER_MARKER * n + STEP_BYTES_PER_NODE * nodes
-    step_gbs = step_bytes / (ms_step * 1e-3) / 1e9
-    prof_total = sum(v[0] for v in prof.values())
-    line = {
-        "metric": METRIC, "value": value, "unit": "markers/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-        "config": base_config(wl, args, world),
-        "clocks": clk.summary(),
-        "e2e": {"value": e2e_value, "unit": "markers/s",
-                "h2d_bytes_per_step": len(E2E_UP) * nodes * 8, "d2h_bytes_per_step": len(E2E_DOWN) * nodes * 8 + 8,
-                "model": "markers resident on the device; host-solve nodal fields up and projected nodal fields "
-                         "down every step from/to pinned host buffers through mic_nodal_upload_many / mic_step / "
-                         "mic_nodal_download_many"},
-        "gpu_launches": launches,
-        "launch_tuning": tuning,
-        "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak,
-                     "traffic": (KERNEL_TRAFFIC_PER_MARKER[top_name] * n if top_name in KERNEL_TRAFFIC_PER_MARKER
-                                 else None),
-                     "traffic_note": "ncu dram bytes of the 1,048,576-marker case scaled by markers processed",
-                     "peak_source": peak_src, "algorithmic_bytes_per_launch": algo, "ms_per_launch": dur},
-        "fp64_roofline": ({"kernel": top_name, "flops_per_marker": KERNEL_FP64_FLOPS_PER_MARKER[top_name],
-                           "achieved": KERNEL_FP64_FLOPS_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e12,
-                           "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                           "frac": KERNEL_FP64_FLOPS_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
-                           "inst_per_marker": KERNEL_FP64_INST_PER_MARKER[top_name],
-                           "issue_frac": KERNEL_FP64_INST_PER_MARKER[top_name] * n / (dur * 1e-3) / 1e9 / FP64_PEAK_GINST,
-                           "note": "the bound that applies: FP64 pipe, 2 FP64 instructions/SM/clk; flops and "
-                                   "instructions per marker from ncu; issue_frac = FP64 instructions issued / peak"}
-                          if top_name in KERNEL_FP64_FLOPS_PER_MARKER else None),
-        "step_roofline": {"algorithmic_bytes_per_step": step_bytes, "achieved_gbs": step_gbs,
-                          "frac": step_gbs / hbm_peak},
-        "kernel_share": {k: round(v[0] / prof_total, 4) for k, v in kern[:12]},
-        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kern[:12]},
-        "density_control": dens,
-        "surrogate": surrogate_leg(args, local) if not args.no_surrogate else None,
-        "ensemble": ensemble_leg(args, local) if not args.no_ensemble else None,
-        "ice_ensemble": ice_ensemble_leg(args, local) if not args.no_ensemble else None,
-        "systems": systems_leg(args, local) if not args.no_systems else None,
-    }
+        out["density_control"] = {"ms_per_call": (time.perf_counter() - t0) * 1e3 / reps, "markers_added": tot_add,
+                                  "markers_removed": tot_rem, "calls": reps,
+                                  "note": "host wall time per call, including its host synchronisations"}
+    out["config"] = base_config(wl, name, world)
     if cpu is not None:
-        line["cpu_baseline"] = cpu
-    print(json.dumps(line), flush=True)
+        out["cpu_baseline"] = cpu
+    G.close()
+    return out, head
 
 
-def surrogate_leg(args, local):
-    """The composite ice creep workload (law 7) stepped with the exact creep solve and with the
-    trained surrogate (CUDA-core and tensor-core inference), plus the surrogate's stress error
-    against the exact solve on a sample of the same input distribution."""
-    import numpy as np
+def run_ours(args):
+    world, rank, local, pg = dist_setup(args)
+    if args.only_systems:
+        if rank == 0:
+            import torch
+
+            torch.cuda.set_device(local)
+            print(json.dumps({"systems": systems_leg(args, local)}), flush=True)
+        return
+    cpu = cpu_vep = None
+    legs = not args.no_legs
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # bounded samples: one step per replica on all host cores, and on one core, spawned before
+        # any GPU work
+        cores = host_cores(args.cpu_cores)
+        rate, ms = cpu_throughput(cpu_sample(args.workload), cores, 1, 0)
+        rate1, ms1 = cpu_throughput(cpu_sample(args.workload), 1, 1, 0)
+        cpu = {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
+               "sample": cpu_sample_text(args.workload, cores, 1, rate1, ms1), "value_1core": rate1}
+        if legs and not args.no_vep and args.workload != "vep_slab_box":
+            rate, ms = cpu_throughput(cpu_sample("vep_slab_box"), cores, 1, 0)
+            cpu_vep = {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
+                       "sample": cpu_sample_text("vep_slab_box", cores, 1)}
     import torch
 
-    from fvmic2d_gb300 import gpu
-    from fvmic2d_gb300 import workloads as W
-
-    wl = W.ice_creep_box()
-    G = gpu.MicProblem(wl, device=local)
-    G.set_grain_size(wl.grain_size)
-    L, h = G.L, G.h
-    stream = torch.cuda.ExternalStream(G.stream(), device=local)
-    n = len(wl.markers)
-    t0 = time.perf_counter()
-    hist = G.creep_train()
-    train_s = time.perf_counter() - t0
-    steps = max(3, min(args.steps, 20))
-    out = {"workload": "ice_creep_box: 1025x1025 uniform nodes, 16 markers/cell (%d markers), composite ice "
-                       "creep (law 7) with per-marker log10 edot ~ U[-18,-10], T ~ U[100,273] K, log10 d ~ "
-                       "U[-4,-1] m, P ~ U[0,1e8] Pa; markers larger than L2" % n,
-           "steps": steps, "train_seconds": round(train_s, 3), "train_loss_final": float(hist[-200:].mean()),
-           "polish": {"iters": 3, "tol": 1e-7}}
-    for label, mode in (("plain", 0), ("surrogate_fp32", 1), ("surrogate_tc", 2)):
-        G.creep_configure(mode=mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
-        for _ in range(3):
-            assert L.mic_step(h, wl.dt, wl.dt_thermal, 1, None) == 0
-        G.synchronize()
-        G.profile_enable(64 * steps)
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(steps):
-            assert L.mic_step(h, wl.dt, wl.dt_thermal, 1, None) == 0
-        ev1.record(stream)
-        ev1.synchronize()
-        ms = ev0.elapsed_time(ev1) / steps
-        prof = G.profile_read()
-        G.profile_enable(0)
-        st = G.creep_stats()
-        yk = [k for k in prof if k.startswith("k_yield")]
-        out[label] = {"value": n / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
-                      "yield_kernel": yk[0] if yk else None,
-                      "yield_ms_per_step": prof[yk[0]][0] / steps if yk else None,
-                      "newton_iters_per_marker": st["iterations"] / max(st["markers"], 1),
-                      "fallbacks_per_step": st["fallbacks"], "tc_timeouts": st["tc_timeouts"],
-                      "max_residual": st["max_residual"]}
-    out["speedup_tc_vs_plain"] = out["surrogate_tc"]["value"] / out["plain"]["value"]
-    # stress error of the surrogate path against the exact solve, same input distribution
-    m = 1 << 20
-    u = W.splitmix64_uniform(11, 4 * m)
-    edot, T, d, P = 10 ** (-18 + 8 * u[0::4]), 100 + 173 * u[1::4], 10 ** (-4 + 3 * u[2::4]), 1e8 * u[3::4]
-    G.creep_configure(mode=0, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
-    s0, _, _, _ = G.creep_solve(edot, T, d, P, mode=0)
-    s2, _, _, fb = G.creep_solve(edot, T, d, P, mode=2)
-    rel = np.abs(s2 / s0 - 1.0)
-    out["stress_rel_err"] = {"max": float(rel.max()), "median": float(np.median(rel)),
-                             "fallbacks": int(fb.sum()), "sample": "%d solves, tensor-core surrogate vs exact" % m}
-    return out
+    torch.cuda.set_device(local)
+    main, head = measure_workload(args, args.workload, local, pg, world)
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": head["value"], "unit": "markers/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+        "config": main.pop("config"),
+        "clocks": head["clocks"],
+        "e2e": main.pop("e2e"),
+        "gpu_launches": head["gpu_launches"],
+        "roofline": head["roofline"],
+        "fp64_roofline": head["fp64_roofline"],
+        "step_roofline": head["step_roofline"],
+        "kernel_share": head["kernel_share"],
+        "kernel_ms_per_step": head["kernel_ms_per_step"],
+    }
+    if "surrogate_tc" in main:
+        line["config"]["path"] = "surrogate_tc (value); plain exact solve under plain"
+        line["plain"] = {k: main["plain"][k] for k in ("value", "unit", "ms_per_step", "yield_kernel",
+                                                       "yield_ms_per_step", "newton_iters_per_marker",
+                                                       "fallbacks_per_step", "roofline", "fp64_roofline",
+                                                       "kernel_ms_per_step", "clocks")}
+        line["surrogate"] = {k: head[k] for k in ("yield_kernel", "yield_ms_per_step", "newton_iters_per_marker",
+                                                  "fallbacks_per_step", "tc_timeouts", "max_residual")}
+        for k in ("speedup_surrogate_vs_plain", "yield_speedup_surrogate_vs_plain", "stress_rel_err",
+                  "stress_rel_err_batch", "train"):
+            line[k] = main[k]
+    line["density_control"] = main.get("density_control")
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if legs and not args.no_vep and args.workload != "vep_slab_box":
+        vep, vhead = measure_workload(args, "vep_slab_box", local, None, 1, cpu=cpu_vep, with_density=False)
+        vep["plain"].pop("launch_tuning", None)
+        line["vep_slab_box"] = vep
+    if legs and not args.no_ensemble:
+        line["ensemble"] = ensemble_leg(args, local)
+        line["ice_ensemble"] = ice_ensemble_leg(args, local)
+    if legs and not args.no_systems:
+        line["systems"] = systems_leg(args, local)
+    print(json.dumps(line), flush=True)
 
 
 def ensemble_leg(args, local):

@@ -56,6 +56,7 @@ int snapshot_take(mic_ctx *ctx, Snapshot &s) {
 }
 
 int snapshot_restore(mic_ctx *ctx, const Snapshot &s) {
+  if (ctx->n != s.n) ctx->gen++;  // launch grids follow the marker count
   ctx->n = s.n;
   const size_t nn = (size_t)ctx->P.NX * ctx->P.NY;
   for (int c = 0; c < (int)s.bufs.size(); ++c) {
@@ -142,6 +143,7 @@ extern "C" int mic_autotune(mic_ctx *ctx, double dt_disp, double dt_thermal, int
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess && !e2) e2 = MIC_ERR_CUDA;
   snapshot_free(snap);
   mic_profile_enable(ctx, prof_was);
+  ctx->gen++;  // launch shapes (and, through the restores, buffers) changed: captured graphs are stale
   if (e || e2) {
     memcpy(ctx->tune_bs, saved, sizeof(saved));
     return e ? e : e2;
@@ -163,5 +165,6 @@ extern "C" int mic_set_tuning(mic_ctx *ctx, const int *block, int count) {
   for (int id = 0; id < count && id < TU_COUNT; ++id)
     if (block[id] != 0 && block[id] != 128 && block[id] != 256 && block[id] != 512) return MIC_ERR_ARG;
   for (int id = 0; id < count && id < TU_COUNT; ++id) ctx->tune_bs[id] = block[id];
+  ctx->gen++;  // captured graphs hold the old launch shapes
   return MIC_OK;
 }

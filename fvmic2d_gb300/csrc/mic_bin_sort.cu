@@ -488,10 +488,41 @@ constexpr size_t kNoallocBytes = (size_t)kWords * 4 + 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
-// host-side: device address of g_noalloc_scratch per device (the symbol itself is only a
-// host stand-in and must never be handed to a kernel)
+// host-side: device address of g_noalloc_scratch per CUDA context (the symbol itself is only a
+// host stand-in and must never be handed to a kernel).  The cache is keyed on the context's
+// process-unique id, not on the device ordinal: after cudaDeviceReset, or under another context
+// of the same device, the address is looked up again instead of reusing a stale one.
 std::mutex g_noalloc_mu;
-unsigned char *g_noalloc_ptr[64];
+constexpr int kNoallocCache = 64;
+unsigned long long g_noalloc_ctx[kNoallocCache];  // context ids (0 = empty slot)
+unsigned char *g_noalloc_ptr[kNoallocCache];
+int g_noalloc_next;  // next slot to fill (round robin once all are used)
+
+// the current context's id through the driver entry points (no link against libcuda); 0 when
+// they are unavailable, and then the address is looked up on every call
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+    cudaGetLastError();
+  });
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 __global__ void k_find_cells_grid(const double *__restrict__ X, const double *__restrict__ Y,
                                   const double *__restrict__ xg, const double *__restrict__ yg, int NX, int NY,
@@ -534,18 +565,31 @@ __global__ void k_find_cells_grid(const double *__restrict__ X, const double *__
   if (threadIdx.x == 0 && s_out) atomicAdd(n_out, s_out);
 }
 
-int noalloc_scratch(int device, unsigned char **out) {
-  if (device < 0 || device >= 64) return MIC_ERR_ARG;
+// Device address of the scratch array in the current context.  The first call in a context
+// (on each device, with that device current) looks it up with cudaGetSymbolAddress, which also
+// makes the runtime set the context up; later calls in the same context reuse it.
+int noalloc_scratch(unsigned char **out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[device]) {
-    unsigned char *p = nullptr;
-    if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p) {
-      cudaGetLastError();
-      return MIC_ERR_CUDA;
-    }
-    g_noalloc_ptr[device] = p;
+  const unsigned long long id = current_context_id();
+  if (id)
+    for (int k = 0; k < kNoallocCache; ++k)
+      if (g_noalloc_ctx[k] == id) {
+        *out = g_noalloc_ptr[k];
+        return MIC_OK;
+      }
+  unsigned char *p = nullptr;
+  if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+    cudaGetLastError();
+    return MIC_ERR_CUDA;
   }
-  *out = g_noalloc_ptr[device];
+  // the lookup may have created the context: take its id now
+  const unsigned long long id2 = id ? id : current_context_id();
+  if (id2) {
+    g_noalloc_ctx[g_noalloc_next] = id2;
+    g_noalloc_ptr[g_noalloc_next] = p;
+    g_noalloc_next = (g_noalloc_next + 1) % kNoallocCache;
+  }
+  *out = p;
   return MIC_OK;
 }
 
@@ -562,7 +606,7 @@ extern "C" int mic_bin_sort_noalloc(const double *X, const double *Y, int64_t n,
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) return MIC_ERR_NO_DEVICE;
   unsigned char *base = nullptr;
-  int e = noalloc_scratch(device, &base);
+  int e = noalloc_scratch(&base);
   if (e) return e;
   cudaStream_t s = (cudaStream_t)stream;
   int *words = reinterpret_cast<int *>(base);

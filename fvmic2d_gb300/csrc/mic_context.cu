@@ -82,7 +82,7 @@ __global__ void k_aos_to_soa(const unsigned char *__restrict__ aos, ColPtrs cols
 #pragma unroll
   for (int c = 0; c < C_I32_COUNT - 1; ++c) cols.i[c][m] = *reinterpret_cast<const int *>(r + c_i32_off[c]);
   cols.i[C_ID][m] = (int)m;
-  cols.f[C_GRAIN][m] = 1e-3;  // default grain size until mic_markers_set_grain_size
+  cols.f[C_GRAIN][m] = kGrainArgDefault;  // default grain size until mic_markers_set_grain_size
 }
 
 __global__ void k_soa_to_aos(unsigned char *__restrict__ aos, ColPtrs cols, int64_t n) {
@@ -368,6 +368,7 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ctx->creep.tol = 2e-14;
   ctx->creep.polish_tol = 1e-7;
   ctx->creep.mlp = nullptr;
+  ctx->creep.tc_wait_limit = 1 << 20;  // try_wait rounds on a tensor-core tile (mic_creep_tc.cuh)
   ctx->opt.etamin = 0.0;
   ctx->opt.etamax = 1e300;
   ctx->n = 0;
@@ -620,6 +621,37 @@ extern "C" int mic_debug_sorted_ids(mic_ctx *ctx, int32_t *ids) {
   return MIC_OK;
 }
 
+namespace {
+// quotients by the path the kernels use for fractions of a grid spacing: inv = 1 / den
+// (correctly rounded), then div_sp(num, den, inv)
+__global__ void k_debug_div_sp(const double *num, const double *den, int64_t n, double *q) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const double d = den[m];
+  q[m] = div_sp(num[m], d, 1.0 / d);
+}
+}  // namespace
+
+// num[k] / den[k] (host arrays) as the kernels divide by a grid spacing (test access)
+extern "C" int mic_debug_div_sp(mic_ctx *ctx, const double *num, const double *den, int64_t n, double *quot) {
+  if (!ctx || n < 0 || (n > 0 && (!num || !den || !quot))) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (n == 0) return MIC_OK;
+  double *d = nullptr;
+  if (cudaMalloc((void **)&d, sizeof(double) * 3 * (size_t)n) != cudaSuccess) return MIC_ERR_NOMEM;
+  cudaError_t ce = cudaMemcpyAsync(d, num, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(d + n, den, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (ce == cudaSuccess) {
+    MIC_KERNEL(ctx, "k_debug_div_sp");
+    k_debug_div_sp<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(d, d + n, n, d + 2 * n);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(quot, d + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  return ce == cudaSuccess ? MIC_OK : MIC_ERR_CUDA;
+}
+
 extern "C" int mic_debug_cell_start(mic_ctx *ctx, int32_t *cs) {
   if (!ctx || !cs) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
@@ -762,7 +794,7 @@ __global__ void k_reset_markers(ColPtrs c, int64_t cap) {
                       C_EXX, C_EYY, C_EXY, C_EXX_TOT, C_EYY_TOT, C_EXY_TOT, C_EII, C_WXY};
 #pragma unroll
   for (int q = 0; q < (int)(sizeof(zero) / sizeof(zero[0])); ++q) c.f[zero[q]][m] = 0.0;
-  c.f[C_GRAIN][m] = 1e-3;
+  c.f[C_GRAIN][m] = kGrainArgDefault;
   c.i[C_MAT][m] = -1;
   c.i[C_ISYIELD][m] = 0;
 }

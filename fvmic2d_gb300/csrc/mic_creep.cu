@@ -27,7 +27,7 @@ __global__ void k_creep_exact_batch(const double *edot, const double *T, const d
   int it = 0, active = 0;
   double res = 0.0;
   if (m < n) {
-    const CreepCoef k = creep_coef(T[m], d[m], P[m]);
+    const CreepCoef k = creep_coef(T[m], grain_arg(d[m]), P[m]);
     s_out[m] = creep_stress_exact(k, edot[m], cfg.tol, cfg.maxit, &it, &res);
     if (it_out) it_out[m] = it;
     if (res_out) res_out[m] = res;
@@ -55,7 +55,7 @@ __global__ void k_creep_samples(unsigned long long seed, int64_t n, CreepConfig 
   const double T = 100.0 + 173.0 * splitmix_u01(seed, 4 * m + 1);
   const double d = pow(10.0, -4.0 + 3.0 * splitmix_u01(seed, 4 * m + 2));
   const double P = 1e8 * splitmix_u01(seed, 4 * m + 3);
-  const CreepCoef k = creep_coef(T, d, P);
+  const CreepCoef k = creep_coef(T, grain_arg(d), P);
   int it;
   double res;
   const double u = creep_root_u(k, edot, cfg.tol, cfg.maxit, &it, &res);
@@ -225,14 +225,14 @@ __global__ void __launch_bounds__(128) k_creep_surrogate_batch_fp32(const double
   double res = 0.0;
   if (m < n) {
     const double e = edot[m];
-    const CreepCoef k = creep_coef(T[m], d[m], P[m]);
-    double u0 = 0.0;
+    const CreepCoef k = creep_coef(T[m], grain_arg(d[m]), P[m]);
+    float lx0 = 0.f;
     if (e > 0.0 && e / k.C >= 1.0) {  // the network is consulted on the non-linear branch only
       float f[4];
       const float mref = creep_features(k, e, f);
-      u0 = creep_guess_u(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
+      lx0 = creep_guess_lx(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
     }
-    s_out[m] = creep_stress_from_guess(k, e, u0, cfg.tol, cfg.maxit, cfg.polish_iters, cfg.polish_tol, &it, &res,
+    s_out[m] = creep_stress_from_guess(k, e, lx0, cfg.tol, cfg.maxit, cfg.polish_iters, cfg.polish_tol, &it, &res,
                                        &fb);
     if (it_out) it_out[m] = it;
     if (res_out) res_out[m] = res;
@@ -292,6 +292,12 @@ size_t fwdbwd_smem() { return sizeof(float) * (kH * kH + 4 * kTB * kH + kTB * 4 
 
 }  // namespace
 
+// grain sizes -> the grain argument the creep coefficients take (grain_arg), in place
+__global__ void k_grain_arg(double *g, int64_t n) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m < n) g[m] = grain_arg(g[m]);
+}
+
 // ---- C ABI ---------------------------------------------------------------------------
 
 extern "C" int mic_creep_param_count(void) { return kNParams; }
@@ -311,6 +317,27 @@ extern "C" int mic_creep_configure(mic_ctx *ctx, int mode, double tol, int maxit
   return MIC_OK;
 }
 
+// Limit of the bounded wait on each tensor-core tile's completion barrier (try_wait rounds;
+// default 2^20).  A tile whose wait runs out makes its block stop using the tensor cores; its
+// markers take the exact solve, and mic_creep_tc_stats counts it.
+extern "C" int mic_creep_set_tc_wait_limit(mic_ctx *ctx, int rounds) {
+  if (!ctx || rounds < 0) return MIC_ERR_ARG;
+  ctx->creep.tc_wait_limit = rounds;
+  ctx->gen++;
+  return MIC_OK;
+}
+
+extern "C" int mic_creep_tc_stats(mic_ctx *ctx, int64_t *tile_timeouts, int64_t *drain_timeouts) {
+  if (!ctx) return MIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  CreepCounters h;
+  MIC_CUDA_TRY(cudaMemcpyAsync(&h, ctx->d_creep, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (tile_timeouts) *tile_timeouts = (int64_t)h.tc_timeouts;
+  if (drain_timeouts) *drain_timeouts = (int64_t)h.tc_drain_timeouts;
+  return MIC_OK;
+}
+
 extern "C" int mic_markers_set_grain_size(mic_ctx *ctx, const double *d, int64_t n) {
   if (!ctx || !d || n != ctx->n) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
@@ -320,6 +347,8 @@ extern "C" int mic_markers_set_grain_size(mic_ctx *ctx, const double *d, int64_t
   MIC_CUDA_TRY(cudaMemcpyAsync(tmp, d, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   int e = mic_gather_by_id(ctx, tmp, ctx->f64[C_GRAIN]);
   if (e) return e;
+  MIC_KERNEL(ctx, "k_grain_arg");
+  k_grain_arg<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(ctx->f64[C_GRAIN], n);
   ctx->has_grain = 1;
   ctx->gen++;
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

@@ -8,11 +8,21 @@
 // D (dislocation creep) that depend on T, grain size d and pressure P only.  Law 7 needs the
 // inverse: the stress s* at which rate(s*) equals the marker's strain-rate invariant.
 //
-// Exact solve: Newton on g(u) = ln rate(e^u) - ln edot, u = ln s.  g is increasing with
-// slope between 1 and 4 and nearly linear, so Newton converges in a few steps; it starts from
-// min(edot / C, 1e6 (edot / D)^(1/4)) -- each term alone reaching edot bounds s* from above --
-// and keeps a bracket.  Powers of x come from one exp per iteration: p = x^0.2 gives
-// x^1.8 = p^9, x^2.4 = p^12, x^4 = p^20, s = 1e6 p^5.
+// All powers of x come from p = x^0.2: x^1.8 = p^9, x^2.4 = p^12, x^4 = p^20, s = 1e6 p^5.
+//
+// Exact solve: the root of g(u) = ln rate(e^u) - ln edot, u = ln s.  g is increasing with
+// slope between 1 and 4 and nearly linear.  The start is min(edot / C, 1e6 (edot / D)^(1/4))
+// -- each term alone reaching edot bounds s* from above -- and a bracket is kept.
+//   FMA-free parity build: Newton in u, one FP64 exp per iteration (the reference's arithmetic
+//   throughout, for the bitwise comparisons of that build).
+//   Product build: the iterate is p itself.  Each iteration evaluates the residual
+//   rate(p) / edot - 1 exactly in FP64 (powers of p by multiplication, one division), and the
+//   step -- a Halley step on g, third order -- is formed on the FP32 pipe from FP32 copies of
+//   the terms; p moves by the factor exp(0.2 du), an FP64 polynomial for small steps.  Only the
+//   residual decides convergence, so rounding in the step changes how fast the iterates
+//   approach the root, never which root is accepted.  The FP64 pipe, the bound of this
+//   solve on GB300 (2 FP64 instructions per SM per clock), then carries no transcendental
+//   inside the loop.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,13 +38,26 @@ struct CreepCoef {
   double D;     // dislocation: rate = D x^4
 };
 
-// viscosity.c:109-173: constants of the law at (T, d, P), with P clamped below at 1 Pa.  The
-// FMA-free parity build evaluates each Arrhenius factor as the reference writes it.  The product
-// build factors exp((-Q + P V) / RT) = exp(-Q / RT) exp(P V / RT) and shares the factors whose
-// activation energies coincide (grain-boundary diffusion and cold GBS: 49 kJ; basal slip and
-// cold dislocation creep: 60 kJ): four exponentials instead of five plus pow for cold ice,
-// agreeing with the reference's form to a few ulp.
-__device__ __forceinline__ CreepCoef creep_coef(double T, double d, double P) {
+// The per-marker grain column holds what creep_coef takes: the grain size d in the FMA-free
+// parity build, d^-0.2 in the product build (1/d = g^5 and d^-1.4 = g^7 then cost multiplies,
+// where d itself would cost a division, a log2 and an exp2 per marker and step).
+__device__ __forceinline__ double grain_arg(double d) {
+#ifdef MIC_EXACT
+  return d;
+#else
+  return exp2(-0.2 * log2(d));
+#endif
+}
+constexpr double kGrainDefault = 1e-3;  // metres, until mic_markers_set_grain_size
+
+// viscosity.c:109-173: constants of the law at (T, grain argument g, P), with P clamped below at
+// 1 Pa.  The FMA-free parity build evaluates each Arrhenius factor as the reference writes it.
+// The product build factors exp((-Q + P V) / RT) = exp(-Q / RT) exp(P V / RT); the activation
+// energies 49, 60, 180 and 192 kJ/mol are whole kJ/mol, so their factors are integer powers of
+// c = exp(-1 kJ/mol / RT) by repeated squaring (relative error about Q/kJ ulp, below 5e-14),
+// and only c, the 59.4 kJ/mol volume diffusion and the pressure factor take an exp: three
+// exponentials instead of six (both temperature branches of a warp run) plus log2 and exp2.
+__device__ __forceinline__ CreepCoef creep_coef(double T, double g, double P) {
   const double R = 8.3144621;
   if (P < 1.0) P = 1.0;
   const double RT = R * T;
@@ -42,6 +65,7 @@ __device__ __forceinline__ CreepCoef creep_coef(double T, double d, double P) {
   const double V = -13e-6;
   CreepCoef k;
 #ifdef MIC_EXACT
+  const double d = g;
   const double Dv = 9.10e-4 * exp(-59.4e3 / RT);
   const double Db = 5.8e-4 * exp(-49.0e3 / RT);
   k.C = 42.0 * Vm / (RT * d * d) * (Dv + M_PI * delta / d * Db);
@@ -52,14 +76,19 @@ __device__ __forceinline__ CreepCoef creep_coef(double T, double d, double P) {
   k.B = 5.5e7 * exp((-60.0e3 + P * V) / RT);
 #else
   const double iRT = 1.0 / RT;
-  const double e49 = exp(-49.0e3 * iRT), e60 = exp(-60.0e3 * iRT), eP = exp(P * V * iRT);
+  const double c1 = exp(-1.0e3 * iRT);
+  const double c2 = c1 * c1, c4 = c2 * c2, c8 = c4 * c4, c16 = c8 * c8, c32 = c16 * c16, c64 = c32 * c32,
+               c128 = c64 * c64;
+  const double e49 = (c32 * c16) * c1, e60 = (c32 * c16) * (c8 * c4);
+  const double e180 = (c128 * c32) * (c16 * c4), e192 = c128 * c64;
+  const double eP = exp(P * V * iRT);
   const double Dv = 9.10e-4 * exp(-59.4e3 * iRT);
   const double Db = 5.8e-4 * e49;
-  const double id = 1.0 / d;
+  const double g2 = g * g, id = (g2 * g2) * g;  // 1/d
   k.C = 42.0 * Vm * iRT * id * id * (Dv + M_PI * delta * id * Db);
-  const double eg = (T < 255.0) ? 3.9e-3 * e49 : 3.0e26 * exp(-192.0e3 * iRT);
-  const double ed = (T < 258.0) ? 4.0e5 * e60 : 6.0e28 * exp(-180.0e3 * iRT);
-  k.G = eg * eP * exp2(-1.4 * log2(d));
+  const double eg = (T < 255.0) ? 3.9e-3 * e49 : 3.0e26 * e192;
+  const double ed = (T < 258.0) ? 4.0e5 * e60 : 6.0e28 * e180;
+  k.G = eg * eP * (id * g2);  // d^-1.4
   k.D = ed * eP;
   k.B = 5.5e7 * e60 * eP;
 #endif
@@ -125,9 +154,10 @@ __device__ __forceinline__ double creep_root_u(const CreepCoef &k, double edot, 
   return u;
 }
 
-// Exact stress at strain rate edot (law 7): returns s*, iterations in *iters.
-__device__ __forceinline__ double creep_stress_exact(const CreepCoef &k, double edot, double tol, int maxit,
-                                                     int *iters, double *res_out) {
+// Exact stress at strain rate edot (law 7), FMA-free parity build: returns s*, iterations in
+// *iters.
+__device__ __forceinline__ double creep_stress_exact_u(const CreepCoef &k, double edot, double tol, int maxit,
+                                                       int *iters, double *res_out) {
   *iters = 0;
   *res_out = 0.0;
   if (!(edot > 0.0)) return 0.0;
@@ -136,6 +166,147 @@ __device__ __forceinline__ double creep_stress_exact(const CreepCoef &k, double 
   const double s = exp(creep_root_u(k, edot, tol, maxit, iters, res_out));
   // the rate jumps at s = 1 Pa where the non-linear terms switch on; a root in the jump is 1 Pa
   return s < 1.0 ? 1.0 : s;
+}
+
+// natural log of a positive normal double to FP32 accuracy: exponent from frexp, __logf of the
+// mantissa (no FP64 transcendental; also the range of every double, which FP32 lacks)
+__device__ __forceinline__ float ln_f(double v) {
+  int e;
+  const double mant = frexp(v, &e);  // [0.5, 1)
+  return (float)e * 0.693147181f + __logf((float)mant);
+}
+
+#ifndef MIC_EXACT
+// ---- product-build solve: the iterate is p = (s / 1e6)^0.2 ----------------------------------
+
+// rate(p) / edot = a p^5 + (1 / (g p^9) + 1 / (b p^12))^-1 + d p^20: the coefficients divided by
+// edot once per marker, so no iteration divides by it
+struct CreepTerms {
+  double a, g, b, d;
+};
+__device__ __forceinline__ CreepTerms creep_terms(const CreepCoef &k, double iedot) {
+  return {k.C * 1e6 * iedot, k.G * iedot, k.B * iedot, k.D * iedot};
+}
+
+// one evaluation at p: the residual r - 1 (exact FP64), the three terms of r (diffusion, the
+// series of basal slip and grain-boundary sliding, dislocation), w = tg / (tg + tb), and p^5
+struct CreepEval {
+  double res, td, tc, tl, w, p5;
+};
+__device__ __forceinline__ void creep_eval(const CreepTerms &q, double p, CreepEval &e) {
+  const double p2 = p * p, p4 = p2 * p2, p8 = p4 * p4;
+  const double p12 = p8 * p4;
+  const double tg = q.g * (p8 * p), tb = q.b * p12;
+  e.p5 = p4 * p;
+  e.w = tg / (tg + tb);
+  e.td = q.a * e.p5;
+  e.tc = tb * e.w;  // (1/tg + 1/tb)^-1
+  e.tl = q.d * (p12 * p8);
+  e.res = (e.td + e.tc + e.tl) - 1.0;
+}
+
+// Halley step in u = ln s for g(u) = ln r from one evaluation.  With r' and r'' the u-derivatives
+// of r (term slopes 1, mc = 1.8 + 0.6 w for the series, 4; the series' log has curvature
+// -0.36 w (1 - w)), g' = r'/r, g'' = r''/r - g'^2, and du = -2 g g' / (2 g'^2 - g g'').
+// Far from the root (|r - 1| >= 2^-16) it runs on the FP32 pipe: its rounding (about 1e-7 of
+// the step) only perturbs the next iterate.  Near the root, g, g' and the final quotient are
+// FP64 (the step then decides the last digits), the small Halley correction stays FP32.
+__device__ __forceinline__ double creep_step(const CreepEval &e) {
+  const float td = (float)e.td, tc = (float)e.tc, tl = (float)e.tl, w = (float)e.w;
+  const float mc = fmaf(0.6f, w, 1.8f);
+  const float r1f = fmaf(tc, mc, fmaf(4.0f, tl, td));
+  const float r2f = fmaf(tc, fmaf(mc, mc, -0.36f * w * (1.0f - w)), fmaf(16.0f, tl, td));
+  if (fabs(e.res) >= 0x1p-16) {
+    const float r = td + tc + tl;
+    if (!(r > 1e-30f && r < 1e30f)) {
+      // terms beyond FP32 range (an iterate far from the root): a step of -g / 4, which the
+      // slope bound g' <= 4 keeps on the root's side
+      return -0.25 * (double)ln_f(e.res + 1.0);
+    }
+    const float ir = 1.0f / r;
+    const float g = fabsf((float)e.res) < 0.5f ? log1pf((float)e.res) : __logf(r);
+    const float g1 = r1f * ir, g2 = fmaf(-g1, g1, r2f * ir);
+    const float den = fmaf(-g, g2, 2.0f * g1 * g1);
+    // Halley where its correction is moderate, Newton otherwise
+    return (double)(den > g1 * g1 ? -2.0f * g * g1 / den : -g / g1);
+  }
+  const double t = e.res;
+  const double g = t * fma(t, fma(t, fma(t, -0.25, 1.0 / 3.0), -0.5), 1.0);  // ln(1 + t), |t| < 2^-16
+  const double r1 = fma(e.tc, fma(0.6, e.w, 1.8), fma(4.0, e.tl, e.td));
+  // r = 1 + t within 2^-16, so the correction g g'' / (2 g'^2) is formed with r = 1
+  const float h = 1.0f - (float)g * (r2f - r1f * r1f) / (2.0f * r1f * r1f);
+  return -(g * (1.0 + t)) / (r1 * (double)h);
+}
+
+// exp(0.2 du), the factor that moves p by a step du in u: Taylor polynomial in FP64 for
+// |0.2 du| < 2^-5 (truncation below 7e-15), else FP32 (large steps are far from the root)
+__device__ __forceinline__ double creep_p_factor(double du) {
+  const double a = 0.2 * du;
+  if (fabs(a) < 0.03125) {
+    double t = fma(a, 1.0 / 720.0, 1.0 / 120.0);
+    t = fma(a, t, 1.0 / 24.0);
+    t = fma(a, t, 1.0 / 6.0);
+    t = fma(a, t, 0.5);
+    t = fma(a, t, 1.0);
+    return fma(a, t, 1.0);
+  }
+  return (double)__expf((float)fmin(fmax(a, -80.0), 80.0));
+}
+
+// Steps from p until |r - 1| <= tol or maxit steps were taken; [plo, phi] brackets the root
+// (plo may be 0, phi infinite) and a step leaving it bisects in ln p instead.  Returns the
+// steps taken; res and p5 belong to the final p.
+__device__ __forceinline__ int creep_iterate(const CreepTerms &q, double &p, double plo, double phi, double tol,
+                                             int maxit, double &res, double &p5) {
+  CreepEval e;
+  int it = 0;
+  for (;; ++it) {
+    creep_eval(q, p, e);
+    if (fabs(e.res) <= tol || it >= maxit) break;
+    if (e.res > 0.0)
+      phi = fmin(phi, p);
+    else
+      plo = fmax(plo, p);
+    double pn = p * creep_p_factor(creep_step(e));
+    if (!(pn > plo && pn < phi)) pn = (plo > 0.0) ? sqrt(plo * phi) : phi * 0.67032004603563930;  // e^-0.4
+    p = pn;
+  }
+  res = e.res;
+  p5 = e.p5;
+  return it;
+}
+
+// the exact solve from the upper bound min(x_lin, x_dis) (as p, FP32 logs, raised by 1e-4 so
+// that their rounding cannot put it below the root); s >= 1 Pa branch
+__device__ __forceinline__ double creep_solve_terms(const CreepTerms &q, double tol, int maxit, int *iters,
+                                                    double *res_out) {
+  const float lp = fminf(-0.2f * ln_f(q.a), -0.05f * ln_f(q.d));
+  double p = (double)__expf(lp) * 1.0001, res, p5;
+  *iters = creep_iterate(q, p, 0.0, INFINITY, tol, maxit, res, p5);
+  *res_out = res;
+  const double s = 1e6 * p5;
+  // the rate jumps at s = 1 Pa where the non-linear terms switch on; a root in the jump is 1 Pa
+  return s < 1.0 ? 1.0 : s;
+}
+#endif
+
+// Exact stress at strain rate edot (law 7) given 1 / edot: returns s*, iterations in *iters.
+__device__ __forceinline__ double creep_stress_exact(const CreepCoef &k, double edot, double iedot, double tol,
+                                                     int maxit, int *iters, double *res_out) {
+#ifdef MIC_EXACT
+  (void)iedot;
+  return creep_stress_exact_u(k, edot, tol, maxit, iters, res_out);
+#else
+  *iters = 0;
+  *res_out = 0.0;
+  if (!(edot > 0.0)) return 0.0;
+  if (edot < k.C) return edot / k.C;  // linear diffusion branch, s = edot / C < 1 Pa (viscosity.c:130-133)
+  return creep_solve_terms(creep_terms(k, iedot), tol, maxit, iters, res_out);
+#endif
+}
+__device__ __forceinline__ double creep_stress_exact(const CreepCoef &k, double edot, double tol, int maxit,
+                                                     int *iters, double *res_out) {
+  return creep_stress_exact(k, edot, edot > 0.0 ? 1.0 / edot : 0.0, tol, maxit, iters, res_out);
 }
 
 // ---- surrogate network ------------------------------------------------------------------
@@ -161,14 +332,6 @@ constexpr int kOffNorm = kOffB3 + 1;     // out_mu, out_sigma
 constexpr int kNParams = kOffNorm + 2;   // 4547
 constexpr int kNTrain = kOffNorm;        // trained parameters (normalisation excluded)
 constexpr float kFeatClamp = 12.0f;
-
-// natural log of a positive normal double to FP32 accuracy: exponent from frexp, __logf of the
-// mantissa (the features need no more, and no FP64 transcendental is spent on them)
-__device__ __forceinline__ float ln_f(double v) {
-  int e;
-  const double mant = frexp(v, &e);  // [0.5, 1)
-  return (float)e * 0.693147181f + __logf((float)mant);
-}
 
 // features of (coefficients, edot > 0); returns the reference m (ln x units)
 __device__ __forceinline__ float creep_features(const CreepCoef &k, double edot, float f[4]) {
@@ -212,20 +375,22 @@ __device__ __forceinline__ float mlp_forward(const float *__restrict__ p, const 
 }
 
 
-// Stress from a surrogate guess u0 (ln s): Newton polish until |rate/edot - 1| <= polish_tol
-// within polish_iters steps, else the exact solve from its own start (*fb = 1).  The zero-rate
-// and linear-diffusion cases are those of creep_stress_exact.
-__device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, double edot, double u0, double tol,
-                                                          int maxit, int polish_iters, double polish_tol,
+// Stress from a surrogate guess lx0 = ln(s / 1e6): polish steps until |rate/edot - 1| <=
+// polish_tol within polish_iters steps, else the exact solve from its own start (*fb = 1).  The
+// zero-rate and linear-diffusion cases are those of creep_stress_exact.
+__device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, double edot, double iedot, float lx0,
+                                                          double tol, int maxit, int polish_iters, double polish_tol,
                                                           int *iters, double *res_out, int *fb) {
   *iters = 0;
   *res_out = 0.0;
   *fb = 0;
   if (!(edot > 0.0)) return 0.0;
+#ifdef MIC_EXACT
+  (void)iedot;
   const double s_lin = edot / k.C;
   if (s_lin < 1.0) return s_lin;
-  if (isfinite(u0)) {
-    double u = u0, ulo = -1e308, uhi = 1e308, res;
+  if (isfinite(lx0)) {
+    double u = (double)lx0 + kLn1e6, ulo = -1e308, uhi = 1e308, res;
     *iters = creep_newton(k, edot, u, ulo, uhi, polish_tol, polish_iters, res);
     if (fabs(res) <= polish_tol) {
       *res_out = res;
@@ -235,9 +400,33 @@ __device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, do
   }
   *fb = 1;
   int it2;
-  const double s = creep_stress_exact(k, edot, tol, maxit, &it2, res_out);
+  const double s = creep_stress_exact_u(k, edot, tol, maxit, &it2, res_out);
   *iters += it2;
   return s;
+#else
+  if (edot < k.C) return edot / k.C;
+  const CreepTerms q = creep_terms(k, iedot);
+  if (isfinite(lx0)) {
+    double p = (double)__expf(0.2f * lx0), res, p5;
+    *iters = creep_iterate(q, p, 0.0, INFINITY, polish_tol, polish_iters, res, p5);
+    if (fabs(res) <= polish_tol) {
+      *res_out = res;
+      const double s = 1e6 * p5;
+      return s < 1.0 ? 1.0 : s;
+    }
+  }
+  *fb = 1;
+  int it2;
+  const double s = creep_solve_terms(q, tol, maxit, &it2, res_out);
+  *iters += it2;
+  return s;
+#endif
+}
+__device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, double edot, float lx0, double tol,
+                                                          int maxit, int polish_iters, double polish_tol,
+                                                          int *iters, double *res_out, int *fb) {
+  return creep_stress_from_guess(k, edot, edot > 0.0 ? 1.0 / edot : 0.0, lx0, tol, maxit, polish_iters, polish_tol,
+                                 iters, res_out, fb);
 }
 
 // per-warp reduction of the creep counters into the device totals (all lanes of the warp)
@@ -259,8 +448,8 @@ __device__ __forceinline__ void creep_count(CreepCounters *cc, int active, int i
   }
 }
 
-// network output and reference m -> ln s guess
-__device__ __forceinline__ double creep_guess_u(const float *__restrict__ p, float y, float m) {
-  return kLn1e6 + (double)m + ((double)y * p[kOffNorm + 1] + p[kOffNorm]);
+// network output and reference m -> guess of ln x* = ln(s* / 1e6)
+__device__ __forceinline__ float creep_guess_lx(const float *__restrict__ p, float y, float m) {
+  return m + fmaf(y, p[kOffNorm + 1], p[kOffNorm]);
 }
 }  // namespace mic

@@ -30,14 +30,14 @@ __global__ void __launch_bounds__(tc::kTile) k_creep_surrogate_batch_tc(const do
     CreepCoef k = {1.0, 1.0, 1.0, 1.0};
     if (valid) {
       e = edot[m];
-      k = creep_coef(T[m], d[m], P[m]);
+      k = creep_coef(T[m], grain_arg(d[m]), P[m]);
       if (e > 0.0) mref = creep_features(k, e, f);
     }
-    const float y = tc::guess(B, f, &cc->tc_timeouts);
+    const float y = tc::guess(B, f, cfg.tc_wait_limit, &cc->tc_timeouts);
     int it = 0, fb = 0;
     double res = 0.0;
     if (valid) {
-      const double s = creep_stress_from_guess(k, e, creep_guess_u(cfg.mlp, y, mref), cfg.tol, cfg.maxit,
+      const double s = creep_stress_from_guess(k, e, creep_guess_lx(cfg.mlp, y, mref), cfg.tol, cfg.maxit,
                                                cfg.polish_iters, cfg.polish_tol, &it, &res, &fb);
       s_out[m] = s;
       if (it_out) it_out[m] = it;
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(tc::kTile) k_creep_surrogate_batch_tc(const do
     }
     creep_count(cc, valid && e > 0.0, it, res, fb);
   }
-  tc::teardown(B);
+  tc::teardown(B, &cc->tc_drain_timeouts);
 }
 
 // network outputs for given features (n x 4, row-major) on the tensor-core path
@@ -63,10 +63,10 @@ __global__ void __launch_bounds__(tc::kTile) k_mlp_infer_tc(const float *__restr
     if (m < n)
 #pragma unroll
       for (int i = 0; i < 4; ++i) f[i] = feat[4 * m + i];
-    const float y = tc::guess(B, f, &cc->tc_timeouts);
+    const float y = tc::guess(B, f, tc::kWaitLimit, &cc->tc_timeouts);
     if (m < n) y_out[m] = y;
   }
-  tc::teardown(B);
+  tc::teardown(B, &cc->tc_drain_timeouts);
 }
 
 }  // namespace

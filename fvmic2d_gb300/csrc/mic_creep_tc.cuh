@@ -13,8 +13,9 @@
 // so the stride between core matrices along K (leading byte offset) is 128 bytes and along the
 // rows (stride byte offset) 1024 bytes.  The MMA over k in [16j, 16j+16) starts at +256 j.
 //
-// Every wait on the MMA's completion barrier is bounded; a block whose wait runs out stops
-// using the tensor cores, reports it, and its markers take the exact solve.
+// Every wait on the MMA's completion barrier is bounded (the limit is a context setting,
+// mic_creep_set_tc_wait_limit); a block whose wait runs out stops using the tensor cores,
+// reports it, and its markers take the exact solve.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -132,7 +133,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-constexpr int kWaitLimit = 1 << 20;  // try_wait rounds before a block gives up on the MMA
+constexpr int kWaitLimit = 1 << 20;  // default try_wait rounds before a block gives up on the MMA
+constexpr int kDrainLimit = 1 << 22;  // try_wait rounds of the final drain before TMEM is freed
 
 // Per-block state of the tensor-core surrogate.
 struct Block {
@@ -191,8 +193,9 @@ __device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float 
 
 // All kTile threads, block-uniform: network output y for this thread's features (NaN when the
 // block has stopped using the tensor path).  `active` threads carry real features; the others
-// feed zeros and ignore the result.
-__device__ __forceinline__ float guess(Block &B, const float f[4], unsigned long long *timeouts) {
+// feed zeros and ignore the result.  wait_limit: try_wait rounds on the MMA's completion before
+// the block gives up (the context's setting, default kWaitLimit).
+__device__ __forceinline__ float guess(Block &B, const float f[4], int wait_limit, unsigned long long *timeouts) {
   const int t = threadIdx.x;
   const float *sp = reinterpret_cast<const float *>(B.base + Smem::small);
   if (B.ok) {
@@ -237,7 +240,7 @@ __device__ __forceinline__ float guess(Block &B, const float f[4], unsigned long
     }
     mma_commit(B.sbase + Smem::bar);
   }
-  const bool done = mbar_wait(B.sbase + Smem::bar, B.phase, kWaitLimit);
+  const bool done = mbar_wait(B.sbase + Smem::bar, B.phase, wait_limit);
   if (!__syncthreads_and(done)) {  // block-uniform give-up: never touch the accumulator again
     B.ok = 0;
     B.pending = 1;
@@ -265,9 +268,18 @@ __device__ __forceinline__ float guess(Block &B, const float f[4], unsigned long
 }
 
 // All kTile threads at the end: drain (bounded) a committed MMA whose completion was not
-// observed, then free TMEM (warp 0).
-__device__ __forceinline__ void teardown(Block &B) {
-  if (B.pending) mbar_wait(B.sbase + Smem::bar, B.phase, kWaitLimit);
+// observed, then free TMEM (warp 0).  The drain waits on the same barrier phase the give-up
+// abandoned: the MMA chain writes only this block's TMEM columns and arrives on the barrier when
+// it is done, so once the phase completes nothing is in flight and the columns can be freed.
+// A drain that runs out as well (the tensor pipe never signalled) is counted in
+// *drain_timeouts and the columns are freed regardless, since a CTA must release its TMEM
+// before it exits; a nonzero count means the accumulator may have been overwritten after the
+// free and the pass's tensor-core results are void (its markers took the exact solve).
+__device__ __forceinline__ void teardown(Block &B, unsigned long long *drain_timeouts) {
+  if (B.pending) {
+    const bool drained = mbar_wait(B.sbase + Smem::bar, B.phase, kDrainLimit);
+    if (!__syncthreads_and(drained) && threadIdx.x == 0) atomicAdd(drain_timeouts, 1ULL);
+  }
   fence_before_sync();
   __syncthreads();
   fence_after_sync();

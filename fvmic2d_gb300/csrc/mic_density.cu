@@ -334,7 +334,7 @@ __device__ void build_inflow_marker(const Params &P, const mic_materials &M, con
                                     const CreepConfig &cfg, const DCols &c, int nf, const mic_density_options &d,
                                     int kind, double xv, double yv, int slot) {
   for (int f = 0; f < nf; ++f) c.f[f][slot] = 0.0;
-  if (nf > C_GRAIN) c.f[C_GRAIN][slot] = 1e-3;
+  if (nf > C_GRAIN) c.f[C_GRAIN][slot] = kGrainArgDefault;
   for (int f = 0; f < C_I32_COUNT; ++f)
     if (f != C_ID) c.i[f][slot] = 0;
   double T;
@@ -349,7 +349,7 @@ __device__ void build_inflow_marker(const Params &P, const mic_materials &M, con
   c.f[C_T][slot] = T;
   c.i[C_MAT][slot] = 0;
   double eta, mu;
-  CreepIn ci = {0.0, 0.0, 0.0, 1e-3, 0.0, 0.0, 0, 0, 0.0, 0, {}};
+  CreepIn ci = {0.0, 0.0, 0.0, kGrainArgDefault, 0.0, 0.0f, 0, 0, 0.0, 0, {}, 0.0};
   CreepConfig exact = cfg;
   exact.mode = 0;
   if (rheology(M, O, 0, T, xv, yv, eta, mu, &exact, &ci)) {

@@ -11,7 +11,9 @@
 // the sequence alternates between two layouts: two graphs are captured, one per layout, and
 // replays alternate between them while the host keeps each member's column pointers in step.
 // A graph is re-captured when a member's settings change (materials, options, boundary values,
-// creep configuration, marker count: the member's generation counter) or the time steps do.
+// creep configuration, launch shapes, marker count: the member's generation counter), when the
+// time steps do, or when a member's column buffers are not where the graph expects them (the
+// member was stepped, tuned or restored outside the ensemble since the last replay).
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -32,6 +34,7 @@ struct mic_ensemble {
   int parity;
   std::vector<double> key_dt;  // dt_disp and dt_thermal per member at capture
   std::vector<long long> key_gen;
+  std::vector<const void *> key_cols;  // per member and graph: the f64 column buffer it reads first
   int key_sub;
   long long graph_kernels[2];  // kernel launches inside each graph
   long long launches;          // kernel launches issued through this ensemble
@@ -74,6 +77,7 @@ bool graph_current(const mic_ensemble *E, const double *dt_disp, const double *d
   for (int i = 0; i < E->n; ++i) {
     if (E->key_dt[2 * i] != dt_disp[i] || E->key_dt[2 * i + 1] != dt_thermal[i]) return false;
     if (E->key_gen[i] != E->m[i]->gen) return false;
+    if (E->key_cols[2 * i + E->parity] != (const void *)E->m[i]->f64[0]) return false;
   }
   return true;
 }
@@ -100,7 +104,9 @@ void replayed(mic_ensemble *E) {
 
 int capture(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub) {
   drop_graphs(E);
+  E->key_cols.assign(2 * E->n, nullptr);
   for (int q = 0; q < 2; ++q) {
+    for (int i = 0; i < E->n; ++i) E->key_cols[2 * i + q] = E->m[i]->f64[0];
     std::vector<int> prof(E->n);
     for (int i = 0; i < E->n; ++i) {  // no per-launch timing events inside a graph
       prof[i] = E->m[i]->prof_on;

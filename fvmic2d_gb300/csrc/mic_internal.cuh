@@ -23,9 +23,16 @@ enum F64Col {
   C_X = 0, C_Y, C_VX, C_VY, C_T, C_TDOT, C_SXX, C_SYY, C_SXY, C_ETA, C_MU, C_RHO, C_RHODOT, C_P,
   C_EXX, C_EYY, C_EXY, C_EXX_TOT, C_EYY_TOT, C_EXY_TOT, C_EII, C_WXY, C_SRR,
   C_AOS_F64,              // columns above mirror mic_marker fields; those below are device-only
-  C_GRAIN = C_AOS_F64,    // grain size for the composite creep law (law 7), metres
+  C_GRAIN = C_AOS_F64,    // grain argument of the composite creep law (law 7): grain_arg(d)
   C_F64_COUNT
 };
+// grain argument of the default grain size d = 1 mm (until mic_markers_set_grain_size): d itself
+// in the FMA-free parity build, d^-0.2 = 10^0.6 in the product build (mic_creep.cuh, grain_arg)
+#ifdef MIC_EXACT
+constexpr double kGrainArgDefault = 1e-3;
+#else
+constexpr double kGrainArgDefault = 3.9810717055349727;
+#endif
 // int-valued marker columns
 enum I32Col { C_MAT = 0, C_CELLX, C_CELLY, C_CPU, C_ISYIELD, C_ID, C_I32_COUNT };
 
@@ -48,12 +55,14 @@ struct CreepConfig {
   double tol;           // exact solve: |rate/edot - 1| <= tol
   double polish_tol;    // surrogate path: residual above this after polishing -> exact fallback
   const float *mlp;     // surrogate network parameters (device), see mic_creep.cu
+  int tc_wait_limit;    // try_wait rounds on a tensor-core tile's completion before giving up
 };
 
 struct CreepCounters {
   unsigned long long markers, iterations, fallbacks;
   unsigned long long max_res_bits;  // bits of the largest |rate/edot - 1| (non-negative double)
   unsigned long long tc_timeouts;   // tensor-core tiles whose completion wait ran out
+  unsigned long long tc_drain_timeouts;  // blocks whose final drain ran out before TMEM was freed
 };
 
 struct Params {  // everything a kernel needs besides the marker columns; passed by value

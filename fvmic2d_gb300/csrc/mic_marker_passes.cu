@@ -67,13 +67,16 @@ struct YieldCols {
   double *eta, *mu, *sxx, *syy, *sxy;
 };
 
-// One marker of checkPlasticYielding (markers.c:1381-1505).  u_guess: the surrogate's ln s*
-// guess for a law-7 marker (surrogate modes).  Returns whether the marker yielded.  CREEP false:
-// no material uses law 7, and its solver is left out (fewer registers, more resident warps).
+// One marker of checkPlasticYielding (markers.c:1381-1505).  lx_guess: the surrogate's guess of
+// ln(s* / 1e6) for a law-7 marker (surrogate modes); kc, kedot: its creep coefficients and
+// strain-rate invariant when already evaluated.  Returns whether the marker yielded.  CREEP
+// false: no material uses law 7, and its solver is left out (fewer registers, more resident
+// warps).
 template <bool CREEP = true>
 __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_materials &M, const mic_options &O,
-                                             const CreepConfig &cfg, double dt, int64_t m, double u_guess,
-                                             const CreepCoef *kc, Status *st, CreepIn &ci, int &creep_active) {
+                                             const CreepConfig &cfg, double dt, int64_t m, float lx_guess,
+                                             const CreepCoef *kc, double kedot, Status *st, CreepIn &ci,
+                                             int &creep_active) {
   bool yielded = false;
   const double eta_old = c.eta[m], mu_old = c.mu[m];
   double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
@@ -93,7 +96,7 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
   const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
   const int k = c.mat[m];
   double eta, mu;
-  ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], u_guess, 0, 0, 0.0, kc != nullptr, {}};
+  ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], lx_guess, 0, 0, 0.0, kc != nullptr, {}, kedot};
   if (kc) ci.k = *kc;
   if (!(CREEP ? rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)
               : rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu))) {
@@ -153,13 +156,12 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
   return yielded;
 }
 
-// coefficients and surrogate features of marker m when it follows law 7 with a positive strain
-// rate (false otherwise); *mref receives the features' reference
+// coefficients, strain-rate invariant and surrogate features of marker m when it follows law 7
+// (false otherwise); *mref receives the features' reference
 __device__ __forceinline__ bool creep_marker_features(const YieldCols &c, const mic_materials &M, int64_t m,
-                                                      CreepCoef &k, float f[4], float *mref) {
+                                                      CreepCoef &k, double &edot, float f[4], float *mref) {
   if (M.hasEtaT[c.mat[m]] != 7) return false;
-  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
-  const double edot = sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+  edot = strain_rate_invariant(c.exx[m], c.eyy[m], c.exy[m]);
   k = creep_coef(c.T[m], c.grain[m], c.p[m]);
   if (!(edot > 0.0)) {
     *mref = 0.f;
@@ -185,12 +187,13 @@ __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig
   int creep_active = 0;
   CreepIn ci = {};
   if (m < n && c.cellX[m] != -1) {
-    double u = 0.0;
-    float f[4], mref;
+    float lx = 0.f, f[4], mref;
+    double edot = 0.0;
     CreepCoef k;
-    const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, f, &mref);
-    if (law7) u = creep_guess_u(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
-    if (yield_marker<MODE != 2>(c, M, O, cfg, dt, m, u, law7 ? &k : nullptr, st, ci, creep_active)) s_yield = 1;
+    const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, edot, f, &mref);
+    if (law7) lx = creep_guess_lx(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
+    if (yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, st, ci, creep_active))
+      s_yield = 1;
   }
   if (MODE != 2) creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   __syncthreads();
@@ -212,17 +215,18 @@ __global__ void __launch_bounds__(tc::kTile) k_yield_tc(YieldCols c, mic_materia
     const int64_t m = tile * tc::kTile + threadIdx.x;
     const bool live = m < n && c.cellX[m] != -1;
     float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
+    double edot = 0.0;
     CreepCoef k;
-    const bool law7 = live && creep_marker_features(c, M, m, k, f, &mref);
-    const float y = tc::guess(B, f, &cc->tc_timeouts);
+    const bool law7 = live && creep_marker_features(c, M, m, k, edot, f, &mref);
+    const float y = tc::guess(B, f, cfg.tc_wait_limit, &cc->tc_timeouts);
     int creep_active = 0;
     CreepIn ci = {};
-    if (live && yield_marker(c, M, O, cfg, dt, m, creep_guess_u(cfg.mlp, y, mref), law7 ? &k : nullptr, st, ci,
-                             creep_active))
+    if (live && yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 ? &k : nullptr, edot, st,
+                             ci, creep_active))
       s_yield = 1;
     creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   }
-  tc::teardown(B);
+  tc::teardown(B, &cc->tc_drain_timeouts);
   __syncthreads();
   if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
 }
@@ -233,7 +237,7 @@ __global__ void k_update_viscosity(YieldCols c, mic_materials M, mic_options O, 
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n || c.cellX[m] == -1) return;
   double eta, mu;
-  CreepIn ci = {c.exx[m], c.eyy[m], c.exy[m], c.grain[m], c.p[m], 0.0, 0, 0, 0.0, 0, {}};
+  CreepIn ci = {c.exx[m], c.eyy[m], c.exy[m], c.grain[m], c.p[m], 0.0f, 0, 0, 0.0, 0, {}, 0.0};
   CreepConfig exact = cfg;  // no surrogate guess on this pass: exact solve
   exact.mode = 0;
   if (!rheology(M, O, c.mat[m], c.T[m], c.X[m], c.Y[m], eta, mu, &exact, &ci)) {

@@ -9,30 +9,44 @@
 
 namespace mic {
 
-// Inputs of the composite creep law (law 7): the marker's strain-rate invariant, grain size,
-// pressure and (surrogate modes) the network's ln s* guess; iteration count, residual and
-// fallback flag of its stress solve come back in it.
+// Inputs of the composite creep law (law 7): the marker's strain rate, grain argument (the
+// grain column: see grain_arg), pressure and (surrogate modes) the network's guess of
+// ln(s* / 1e6); iteration count, residual and fallback flag of its stress solve come back in it.
 struct CreepIn {
   double e11, e22, e12, grain, p;
-  double u_guess;
+  float lx_guess;
   int iters, fb;
   double res;
-  int have_k;    // coefficients below already evaluated for this marker
+  int have_k;    // k and edot below already evaluated for this marker
   CreepCoef k;
+  double edot;   // strain-rate invariant sqrt(0.5 (e11^2 + e22^2) + e12^2)
 };
+
+__device__ __forceinline__ double strain_rate_invariant(double e11, double e22, double e12) {
+  return sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+}
 
 // Law 7 (new): composite ice creep, eta = s* / (2 edot_II) with s* the stress at which the
 // Goldsby-Kohlstedt strain rate (viscosity.c:106-179) equals the marker's strain-rate
 // invariant; at zero strain rate the law's diffusion viscosity 0.5 / C (viscosity.c:130-133).
 __device__ __forceinline__ double creep_viscosity(const CreepConfig &cfg, double T, CreepIn &ci) {
-  const double edot = sqrt(0.5 * (ci.e11 * ci.e11 + ci.e22 * ci.e22) + ci.e12 * ci.e12);
+  const double edot = ci.have_k ? ci.edot : strain_rate_invariant(ci.e11, ci.e22, ci.e12);
   const CreepCoef k = ci.have_k ? ci.k : creep_coef(T, ci.grain, ci.p);
   if (!(edot > 0.0)) return 0.5 / k.C;
-  const double s = (cfg.mode == 0) ? creep_stress_exact(k, edot, cfg.tol, cfg.maxit, &ci.iters, &ci.res)
-                                   : creep_stress_from_guess(k, edot, ci.u_guess, cfg.tol, cfg.maxit,
+#ifdef MIC_EXACT
+  const double iedot = 0.0;  // unused: the parity build divides as the reference does
+#else
+  const double iedot = 1.0 / edot;  // once per marker: the solve and the viscosity share it
+#endif
+  const double s = (cfg.mode == 0) ? creep_stress_exact(k, edot, iedot, cfg.tol, cfg.maxit, &ci.iters, &ci.res)
+                                   : creep_stress_from_guess(k, edot, iedot, ci.lx_guess, cfg.tol, cfg.maxit,
                                                              cfg.polish_iters, cfg.polish_tol, &ci.iters, &ci.res,
                                                              &ci.fb);
+#ifdef MIC_EXACT
   return s / (2.0 * edot);
+#else
+  return s * (0.5 * iedot);
+#endif
 }
 
 // computeRheology (viscosity.c:12-67) plus law 7; returns false for an undefined law

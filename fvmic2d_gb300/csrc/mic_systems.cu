@@ -534,7 +534,7 @@ __global__ void k_van_keken(mic_materials M, mic_options O, CreepConfig cfg, dou
   rhodot[m] = 0.0;
   rho[m] = -M.materialRho[0] * (M.materialAlpha[0] * t);
   double e, u;
-  CreepIn ci = {0.0, 0.0, 0.0, 1e-3, 0.0, 0.0, 0, 0, 0.0, 0, {}};
+  CreepIn ci = {0.0, 0.0, 0.0, kGrainArgDefault, 0.0, 0.0f, 0, 0, 0.0, 0, {}, 0.0};
   CreepConfig exact = cfg;
   exact.mode = 0;
   if (rheology(M, O, 0, t, x, y, e, u, &exact, &ci)) {  // updateMarkerViscosity(m, ..., 0.0)

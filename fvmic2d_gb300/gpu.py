@@ -66,6 +66,7 @@ SIGNATURES = {
     "mic_get_status": (_I, [_P, _P]),
     "mic_debug_sorted_ids": (_I, [_P, _P]),
     "mic_debug_cell_start": (_I, [_P, _P]),
+    "mic_debug_div_sp": (_I, [_P, _P, _P, _I64, _P]),
     "mic_launch_count": (_I, [_P, _I64P]),
     "mic_profile_enable": (_I, [_P, _I]),
     "mic_profile_read": (_I, [_P, _I, _P, _DP, _I64P, _IP]),
@@ -83,6 +84,8 @@ SIGNATURES = {
     "mic_creep_solve_batch": (_I, [_P, _DP, _DP, _DP, _DP, _I64, _I, _DP, _P, _DP, _P]),
     "mic_creep_mlp_infer": (_I, [_P, _P, _I64, _I, _P]),
     "mic_creep_stats": (_I, [_P, _I64P, _I64P, _I64P, _DP, _I64P]),
+    "mic_creep_set_tc_wait_limit": (_I, [_P, _I]),
+    "mic_creep_tc_stats": (_I, [_P, _I64P, _I64P]),
     "mic_reset_markers": (_I, [_P]),
     "mic_marker_count": (_I, [_P, _I64P]),
     "mic_distribute_markers_uniform_in_domain": (_I, [_P, _I, _I, ctypes.c_ulong, _I64P]),
@@ -415,6 +418,15 @@ class MicProblem:
         self._check(self.L.mic_debug_cell_start(self.h, cs.ctypes.data), "mic_debug_cell_start")
         return cs
 
+    def debug_div_sp(self, num, den):
+        """num / den by the kernels' grid-spacing division (mic_debug_div_sp)"""
+        num = np.ascontiguousarray(num, dtype=np.float64)
+        den = np.ascontiguousarray(den, dtype=np.float64)
+        q = np.zeros(len(num))
+        self._check(self.L.mic_debug_div_sp(self.h, num.ctypes.data, den.ctypes.data, len(num), q.ctypes.data),
+                    "mic_debug_div_sp")
+        return q
+
     def launch_count(self):
         n = ctypes.c_int64(0)
         self._check(self.L.mic_launch_count(self.h, ctypes.byref(n)), "mic_launch_count")
@@ -518,6 +530,15 @@ class MicProblem:
                                            ctypes.byref(r), ctypes.byref(t)), "mic_creep_stats")
         return {"markers": a.value, "iterations": b.value, "fallbacks": c.value, "max_residual": r.value,
                 "tc_timeouts": t.value}
+
+    def creep_set_tc_wait_limit(self, rounds):
+        """try_wait rounds on each tensor-core tile's completion before its block gives up"""
+        self._check(self.L.mic_creep_set_tc_wait_limit(self.h, int(rounds)), "mic_creep_set_tc_wait_limit")
+
+    def creep_tc_stats(self):
+        t, d = ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self.L.mic_creep_tc_stats(self.h, ctypes.byref(t), ctypes.byref(d)), "mic_creep_tc_stats")
+        return {"tile_timeouts": t.value, "drain_timeouts": d.value}
 
     def synchronize(self):
         self._check(self.L.mic_synchronize(self.h), "mic_synchronize")

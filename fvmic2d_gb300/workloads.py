@@ -564,4 +564,8 @@ WORKLOADS = {
     "ice_creep_box": ice_creep_box,
     # 513 x 513 nodes, 4,194,304 markers
     "ice_creep_box_4m": lambda: ice_creep_box(nx_cells=512, ny_cells=512),
+    # 129 x 129 nodes, 262,144 markers with the ice box's per-marker distributions: the bounded
+    # sample the host-core baseline steps
+    "ice_creep_box_sample": lambda: ice_creep_box(nx_cells=128, ny_cells=128),
+    "vep_slab_box_sample": lambda: vep_slab_box(nx_cells=256, ny_cells=64),
 }

@@ -5,8 +5,7 @@
  * around the host Stokes and thermal solves -- with CUDA kernels for sm_103a.
  * Every entry point takes plain pointers and sizes; markers use the reference's
  * 216-byte record (mic_marker == fdcode.h Marker), nodal fields the NX*NY
- * global-vector layout ([j][i] = j*NX + i).  See INTEGRATION.md for the
- * reference-side binding.
+ * global-vector layout ([j][i] = j*NX + i).
  *
  * State model: a context owns one grid, the device copies of every nodal field
  * and up to `max_markers` markers kept on the device as columns.  Markers are
@@ -184,6 +183,13 @@ int mic_surrogate_infer(mic_ctx *ctx, const float *feat, int64_t n, int mode, fl
  * wait ran out (their markers took the exact solve) */
 int mic_creep_stats(mic_ctx *ctx, int64_t *markers, int64_t *iterations, int64_t *fallbacks, double *max_residual,
                     int64_t *tc_timeouts);
+/* the tensor-core inference's bounded completion wait: try_wait rounds per tile before a block
+ * gives up on the tensor cores (default 2^20; 0 gives up at once, every marker then takes the
+ * exact solve), and the last pass's counts of tiles that gave up and of blocks whose final
+ * drain before freeing tensor memory ran out as well (nonzero only if the tensor pipe never
+ * signalled) */
+int mic_creep_set_tc_wait_limit(mic_ctx *ctx, int rounds);
+int mic_creep_tc_stats(mic_ctx *ctx, int64_t *tile_timeouts, int64_t *drain_timeouts);
 
 /* ---- plumbing ---- */
 int mic_synchronize(mic_ctx *ctx);
@@ -193,6 +199,9 @@ int mic_get_status(mic_ctx *ctx, mic_status *status);
  * ((NX-1)*(NY-1)+2 entries; the last two bracket the out-of-domain markers) */
 int mic_debug_sorted_ids(mic_ctx *ctx, int32_t *ids);
 int mic_debug_cell_start(mic_ctx *ctx, int32_t *cell_start);
+/* num[k] / den[k] (host arrays) computed the way the kernels divide by a grid spacing: the
+ * correctly rounded reciprocal and one residual correction (the FMA-free build divides) */
+int mic_debug_div_sp(mic_ctx *ctx, const double *num, const double *den, int64_t n, double *quot);
 /* kernel launches issued by this context so far */
 int mic_launch_count(mic_ctx *ctx, int64_t *launches);
 /* per-launch CUDA-event timing on the context stream: enable with a record capacity (0 turns it
@@ -403,9 +412,10 @@ int mic_ensemble_get_stream(mic_ensemble *ens, void **stream);
  *   stream            cudaStream_t to run on (NULL: the legacy default stream)
  *   n_out             optional host pointer: markers outside the domain (synchronises stream)
  * Limits: n <= MIC_NOALLOC_MAX_MARKERS and (NX-1)*(NY-1) <= MIC_NOALLOC_MAX_CELLS, else
- * MIC_ERR_CAPACITY.  The first call on a device looks up the array's device address, so make
- * that first call before capturing a stream.  All calls share the one array: calls that overlap
- * on the GPU race and must be ordered by the caller. */
+ * MIC_ERR_CAPACITY.  The first call in a CUDA context (on each device, and again after a
+ * cudaDeviceReset) looks up the array's device address, so make that first call before
+ * capturing a stream.  All calls share the one array: calls that overlap on the GPU race and
+ * must be ordered by the caller. */
 #define MIC_NOALLOC_MAX_MARKERS 1048576
 #define MIC_NOALLOC_MAX_CELLS 1048576
 int mic_bin_sort_noalloc(const double *X, const double *Y, int64_t n, const double *x, const double *y, int NX,

@@ -10,7 +10,9 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
-REFERENCE_DIR = os.environ.get("FVMIC2D_REFERENCE_DIR", "/root/reference")
+# the fvmic2d source tree: FVMIC2D_REFERENCE_DIR, else a checkout named "reference" beside this
+# repository
+REFERENCE_DIR = os.environ.get("FVMIC2D_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def build_oracle(force=False):

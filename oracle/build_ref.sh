@@ -5,10 +5,14 @@
 # restatement (oracle/mic_oracle.c) and generates the golden vectors under
 # tests/golden/.  Nothing is copied out of the reference tree.
 #
-# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default: /root/reference)
+# usage: oracle/build_ref.sh REFERENCE_DIR   (the fvmic2d source tree)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-/root/reference}
+if [ $# -lt 1 ]; then
+  echo "usage: $0 REFERENCE_DIR" >&2
+  exit 2
+fi
+REF=$1
 OUT="$HERE/_ref"
 if [ ! -f "$REF/markerProjection.c" ]; then
   echo "reference sources not found under $REF; oracle/_ref not built" >&2

@@ -155,3 +155,57 @@ def test_law7_marker_pass_matches_oracle(trained, mode):
     assert st["markers"] == len(wl.markers) and st["tc_timeouts"] == 0
     assert st["fallbacks"] <= 0.01 * len(wl.markers)
     assert st["max_residual"] <= 2e-14
+
+
+def test_tensor_core_wait_that_runs_out_falls_back_to_exact(trained):
+    """The bounded wait on each tensor-core tile's completion, made to run out (a limit of zero
+    try_wait rounds): every block gives up on its first tile and counts it, drains the committed
+    MMA before freeing its tensor memory, and every non-linear marker takes the exact solve --
+    stresses bit for bit those of mode 0.  The context stays usable: with the default limit the
+    next solve uses the tensor cores again."""
+    G, _ = trained
+    edot, T, d, P = creep_samples(100000, 79)
+    G.creep_configure(mode=0, tol=2e-14, polish_iters=3, polish_tol=1e-7)
+    s0, _, _, _ = G.creep_solve(edot, T, d, P, mode=0)
+    G.creep_set_tc_wait_limit(0)
+    try:
+        s, _, res, fb = G.creep_solve(edot, T, d, P, mode=2)
+        st, tcs = G.creep_stats(), G.creep_tc_stats()
+    finally:
+        G.creep_set_tc_wait_limit(1 << 20)
+    assert st["tc_timeouts"] > 0 and tcs["tile_timeouts"] == st["tc_timeouts"]
+    assert tcs["drain_timeouts"] == 0
+    # the non-linear branch (s* >= 1 Pa) is where the network would have been used
+    nonlinear = (edot > 0) & (s0 >= 1.0)
+    assert nonlinear.any() and np.array_equal(fb == 1, nonlinear)
+    assert st["fallbacks"] == int(fb.sum())
+    assert np.array_equal(s.view(np.uint64), s0.view(np.uint64))
+    s2, _, _, fb2 = G.creep_solve(edot, T, d, P, mode=2)
+    assert G.creep_tc_stats() == {"tile_timeouts": 0, "drain_timeouts": 0}
+    assert fb2.mean() < 0.01
+    assert np.max(np.abs(s2 / s0 - 1.0)) <= 1e-6
+
+
+def test_tensor_core_wait_that_runs_out_in_the_marker_pass(trained):
+    """The same give-up inside checkPlasticYielding's tensor-core pass: viscosities bit for bit
+    those of the exact pass, tiles counted, and the context usable afterwards"""
+    wl = W.ice_creep_box(nx_cells=24, ny_cells=24, nm=3, seed=6)
+    A = gpu.MicProblem(wl)
+    B = gpu.MicProblem(wl)
+    for G in (A, B):
+        G.set_grain_size(wl.grain_size)
+        G.findMarkerCells()
+    B.creep_set_params(trained[0].creep_params())
+    A.creep_configure(mode=0, tol=2e-14, polish_iters=3, polish_tol=1e-7)
+    B.creep_configure(mode=2, tol=2e-14, polish_iters=3, polish_tol=1e-7)
+    B.creep_set_tc_wait_limit(0)
+    A.checkPlasticYielding(wl.dt)
+    B.checkPlasticYielding(wl.dt)
+    tcs = B.creep_tc_stats()
+    assert tcs["tile_timeouts"] > 0 and tcs["drain_timeouts"] == 0
+    assert np.array_equal(A.markers["eta"].view(np.uint64), B.markers["eta"].view(np.uint64))
+    B.creep_set_tc_wait_limit(1 << 20)
+    B.checkPlasticYielding(wl.dt)
+    assert B.creep_tc_stats()["tile_timeouts"] == 0
+    A.close()
+    B.close()

@@ -150,3 +150,41 @@ def test_plastic_members_match_members_stepped_alone(graph):
         assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
         for f in ("rho", "etaN", "etaS", "soxx", "soxy", "lastT", "kThermal", "dsxx"):
             assert np.array_equal(a.get_nodal(f), b.get_nodal(f)), f
+
+
+def test_member_stepped_or_tuned_between_replays():
+    """A member stepped on its own between captured-graph replays (its step swaps its column
+    buffers), or given new launch shapes, must not replay a stale graph: the next ensemble step
+    re-captures, and every member still matches the same member stepped alone, bit for bit"""
+    wls = _members(60)
+    A = _setup(wls)
+    B = _setup(wls)
+    E = gpu.MicEnsemble(A)
+    dts = np.array([wl.dt for wl in wls])
+
+    def both_ensemble():
+        E.step(dts, dts, subgrid_stress=1, graph=True)
+        for b, dt in zip(B, dts):
+            b.step(dt, dt, True)
+
+    for _ in range(3):  # direct step, capture, first replay
+        both_ensemble()
+    E.synchronize()
+    # one member alone: an odd number of buffer swaps relative to the graph's layout
+    A[2].step(dts[2], dts[2], True)
+    B[2].step(dts[2], dts[2], True)
+    for _ in range(3):
+        both_ensemble()
+    E.synchronize()
+    # new launch shapes on one member
+    t = A[1].tuning()
+    A[1].set_tuning({k: (256 if v != 256 else 128) for k, v in t.items()})
+    for _ in range(2):
+        both_ensemble()
+    E.synchronize()
+    for a, b in zip(A, B):
+        assert a.n == b.n
+        assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
+        for f in ("rho", "etaN", "etaS", "lastT"):
+            assert np.array_equal(a.get_nodal(f), b.get_nodal(f)), f
+    E.close()
