@@ -123,6 +123,7 @@ static void free_ctx(mic_ctx *ctx) {
   }
   for (int f = 0; f < MIC_NF_COUNT; ++f) cudaFree(ctx->nodal[f]);
   for (int f = 0; f < 6; ++f) cudaFree(ctx->node_scr[f]);
+  cudaFree(ctx->adv_coef);
   cudaFree(ctx->grid_buf);
   cudaFree(ctx->bits_buf);
   cudaFree(ctx->spacing_buf);

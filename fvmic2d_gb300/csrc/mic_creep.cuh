@@ -168,12 +168,16 @@ __device__ __forceinline__ double creep_stress_exact_u(const CreepCoef &k, doubl
   return s < 1.0 ? 1.0 : s;
 }
 
-// natural log of a positive normal double to FP32 accuracy: exponent from frexp, __logf of the
-// mantissa (no FP64 transcendental; also the range of every double, which FP32 lacks)
+// natural log of a positive normal double to FP32 accuracy, from its bit pattern: the exponent
+// field, and __logf of the top 23 mantissa bits as a float in [1, 2) -- integer work and the
+// FP32 pipe only (no FP64 instruction), over the whole double range, which FP32 lacks.  Zero
+// gives about -709 (a huge negative log) instead of -inf; the callers take minima, where that
+// acts the same.
 __device__ __forceinline__ float ln_f(double v) {
-  int e;
-  const double mant = frexp(v, &e);  // [0.5, 1)
-  return (float)e * 0.693147181f + __logf((float)mant);
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  const float mant = __int_as_float(0x3F800000 | (int)((b >> 29) & 0x7FFFFF));
+  return (float)e * 0.693147181f + __logf(mant);
 }
 
 #ifndef MIC_EXACT
@@ -188,51 +192,62 @@ __device__ __forceinline__ CreepTerms creep_terms(const CreepCoef &k, double ied
   return {k.C * 1e6 * iedot, k.G * iedot, k.B * iedot, k.D * iedot};
 }
 
-// one evaluation at p: the residual r - 1 (exact FP64), the three terms of r (diffusion, the
-// series of basal slip and grain-boundary sliding, dislocation), w = tg / (tg + tb), and p^5
+// One evaluation at p, without a division: with S = tg + tb (the series' two terms) and
+// N = (td + tl - 1) S + tg tb, the residual r - 1 is N / S, so |r - 1| <= tol is tested as
+// |N| <= tol S, exactly in FP64 (the cancelling products are one FMA: their rounding is 1e-16 of
+// tg tb / S <= 1).  The quotients the step needs come later, in FP32.
 struct CreepEval {
-  double res, td, tc, tl, w, p5;
+  double N, S, tg, tb, td, tl, p5;
 };
 __device__ __forceinline__ void creep_eval(const CreepTerms &q, double p, CreepEval &e) {
   const double p2 = p * p, p4 = p2 * p2, p8 = p4 * p4;
   const double p12 = p8 * p4;
-  const double tg = q.g * (p8 * p), tb = q.b * p12;
+  e.tg = q.g * (p8 * p);
+  e.tb = q.b * p12;
   e.p5 = p4 * p;
-  e.w = tg / (tg + tb);
   e.td = q.a * e.p5;
-  e.tc = tb * e.w;  // (1/tg + 1/tb)^-1
   e.tl = q.d * (p12 * p8);
-  e.res = (e.td + e.tc + e.tl) - 1.0;
+  e.S = e.tg + e.tb;
+  e.N = fma((e.td + e.tl) - 1.0, e.S, e.tg * e.tb);
 }
+__device__ __forceinline__ bool creep_converged(const CreepEval &e, double tol) { return fabs(e.N) <= tol * e.S; }
+// the residual r - 1 (to FP32 accuracy: reported, and used for the step far from the root)
+__device__ __forceinline__ double creep_residual(const CreepEval &e) { return e.N / e.S; }
 
 // Halley step in u = ln s for g(u) = ln r from one evaluation.  With r' and r'' the u-derivatives
-// of r (term slopes 1, mc = 1.8 + 0.6 w for the series, 4; the series' log has curvature
-// -0.36 w (1 - w)), g' = r'/r, g'' = r''/r - g'^2, and du = -2 g g' / (2 g'^2 - g g'').
-// Far from the root (|r - 1| >= 2^-16) it runs on the FP32 pipe: its rounding (about 1e-7 of
-// the step) only perturbs the next iterate.  Near the root, g, g' and the final quotient are
-// FP64 (the step then decides the last digits), the small Halley correction stays FP32.
+// of r = td + tc + tl (term slopes 1, mc = 1.8 + 0.6 w for the series tc = tb w, w = tg / S, and 4;
+// the series' log has curvature -0.36 w (1 - w)), g' = r'/r, g'' = r''/r - g'^2, and
+// du = -2 g g' / (2 g'^2 - g g'').  The quotients come from FP32 copies: their rounding (about
+// 1e-7 of the step) only perturbs the next iterate.  Near the root (|r - 1| < 2^-16) g and g' are
+// formed in FP64 from the exact N and S (the step then decides the last digits); the small
+// Halley correction stays FP32.  Returns du.
 __device__ __forceinline__ double creep_step(const CreepEval &e) {
-  const float td = (float)e.td, tc = (float)e.tc, tl = (float)e.tl, w = (float)e.w;
+  const float S = (float)e.S, tb = (float)e.tb, td = (float)e.td, tl = (float)e.tl;
+  const float iS = 1.0f / S;
+  const float w = (float)e.tg * iS;
+  const float tc = tb * w;
+  const float resf = (float)e.N * iS;
   const float mc = fmaf(0.6f, w, 1.8f);
   const float r1f = fmaf(tc, mc, fmaf(4.0f, tl, td));
   const float r2f = fmaf(tc, fmaf(mc, mc, -0.36f * w * (1.0f - w)), fmaf(16.0f, tl, td));
-  if (fabs(e.res) >= 0x1p-16) {
+  if (!(fabsf(resf) < 0x1p-16f)) {
     const float r = td + tc + tl;
-    if (!(r > 1e-30f && r < 1e30f)) {
+    if (!(r > 1e-30f && r < 1e30f && S < 1e30f)) {
       // terms beyond FP32 range (an iterate far from the root): a step of -g / 4, which the
       // slope bound g' <= 4 keeps on the root's side
-      return -0.25 * (double)ln_f(e.res + 1.0);
+      return -0.25 * (double)ln_f(fabs(creep_residual(e) + 1.0));
     }
     const float ir = 1.0f / r;
-    const float g = fabsf((float)e.res) < 0.5f ? log1pf((float)e.res) : __logf(r);
+    const float g = fabsf(resf) < 0.5f ? log1pf(resf) : __logf(r);
     const float g1 = r1f * ir, g2 = fmaf(-g1, g1, r2f * ir);
     const float den = fmaf(-g, g2, 2.0f * g1 * g1);
     // Halley where its correction is moderate, Newton otherwise
     return (double)(den > g1 * g1 ? -2.0f * g * g1 / den : -g / g1);
   }
-  const double t = e.res;
+  const double t = creep_residual(e);
   const double g = t * fma(t, fma(t, fma(t, -0.25, 1.0 / 3.0), -0.5), 1.0);  // ln(1 + t), |t| < 2^-16
-  const double r1 = fma(e.tc, fma(0.6, e.w, 1.8), fma(4.0, e.tl, e.td));
+  const double w64 = e.tg / e.S;
+  const double r1 = fma(e.tb * w64, fma(0.6, w64, 1.8), fma(4.0, e.tl, e.td));
   // r = 1 + t within 2^-16, so the correction g g'' / (2 g'^2) is formed with r = 1
   const float h = 1.0f - (float)g * (r2f - r1f * r1f) / (2.0f * r1f * r1f);
   return -(g * (1.0 + t)) / (r1 * (double)h);
@@ -255,15 +270,17 @@ __device__ __forceinline__ double creep_p_factor(double du) {
 
 // Steps from p until |r - 1| <= tol or maxit steps were taken; [plo, phi] brackets the root
 // (plo may be 0, phi infinite) and a step leaving it bisects in ln p instead.  Returns the
-// steps taken; res and p5 belong to the final p.
+// steps taken; conv, res and p5 belong to the final p (res to FP32 accuracy, at most tol in
+// magnitude when conv).
 __device__ __forceinline__ int creep_iterate(const CreepTerms &q, double &p, double plo, double phi, double tol,
-                                             int maxit, double &res, double &p5) {
+                                             int maxit, bool &conv, double &res, double &p5) {
   CreepEval e;
   int it = 0;
   for (;; ++it) {
     creep_eval(q, p, e);
-    if (fabs(e.res) <= tol || it >= maxit) break;
-    if (e.res > 0.0)
+    conv = creep_converged(e, tol);
+    if (conv || it >= maxit) break;
+    if (e.N > 0.0)
       phi = fmin(phi, p);
     else
       plo = fmax(plo, p);
@@ -271,7 +288,8 @@ __device__ __forceinline__ int creep_iterate(const CreepTerms &q, double &p, dou
     if (!(pn > plo && pn < phi)) pn = (plo > 0.0) ? sqrt(plo * phi) : phi * 0.67032004603563930;  // e^-0.4
     p = pn;
   }
-  res = e.res;
+  res = (double)((float)e.N / (float)e.S);
+  if (conv) res = copysign(fmin(fabs(res), tol), res);
   p5 = e.p5;
   return it;
 }
@@ -282,7 +300,8 @@ __device__ __forceinline__ double creep_solve_terms(const CreepTerms &q, double 
                                                     double *res_out) {
   const float lp = fminf(-0.2f * ln_f(q.a), -0.05f * ln_f(q.d));
   double p = (double)__expf(lp) * 1.0001, res, p5;
-  *iters = creep_iterate(q, p, 0.0, INFINITY, tol, maxit, res, p5);
+  bool conv;
+  *iters = creep_iterate(q, p, 0.0, INFINITY, tol, maxit, conv, res, p5);
   *res_out = res;
   const double s = 1e6 * p5;
   // the rate jumps at s = 1 Pa where the non-linear terms switch on; a root in the jump is 1 Pa
@@ -347,9 +366,12 @@ __device__ __forceinline__ float creep_features(const CreepCoef &k, double edot,
   return m;
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU and its derivative with the fast reciprocal (__fdividef: two MUFU ops and a multiply,
+// about 2 ulp) instead of the IEEE division sequence: 128 of these per marker at inference.  For
+// z below about -87 the denominator overflows and both return 0, the limit.
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
+  const float s = __fdividef(1.0f, 1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
 }
 
@@ -408,8 +430,9 @@ __device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, do
   const CreepTerms q = creep_terms(k, iedot);
   if (isfinite(lx0)) {
     double p = (double)__expf(0.2f * lx0), res, p5;
-    *iters = creep_iterate(q, p, 0.0, INFINITY, polish_tol, polish_iters, res, p5);
-    if (fabs(res) <= polish_tol) {
+    bool conv;
+    *iters = creep_iterate(q, p, 0.0, INFINITY, polish_tol, polish_iters, conv, res, p5);
+    if (conv) {
       *res_out = res;
       const double s = 1e6 * p5;
       return s < 1.0 ? 1.0 : s;

@@ -30,7 +30,9 @@ constexpr int kTile = 128;              // markers per block tile = MMA M = TMEM
 constexpr int kTmemCols = 64;           // FP32 accumulator columns (N)
 constexpr uint32_t kOpA = 128 * 64 * 2;  // bytes of one A operand (hi or lo)
 constexpr uint32_t kOpB = 64 * 64 * 2;   // bytes of one B operand
-constexpr int kNSmall = 4 * kH + 3 * kH + 3;  // W1, b1, b2, w3, b3, out_mu, out_sigma
+// small parameters in shared memory, neuron-major so that each neuron's are two 16-byte loads:
+// float4 {W1[k][0..3]}, float4 {b1[k], b2[k], w3[k], 0} for k < 64, then b3
+constexpr int kNSmall = 8 * kH + 4;
 
 struct Smem {  // offsets from a 1024-byte aligned base
   static constexpr uint32_t a_hi = 0, a_lo = kOpA, b_hi = 2 * kOpA, b_lo = 2 * kOpA + kOpB;
@@ -172,16 +174,12 @@ __device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float 
     *reinterpret_cast<uint4 *>(B.base + Smem::b_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
     *reinterpret_cast<uint4 *>(B.base + Smem::b_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
   }
-  float *sp = reinterpret_cast<float *>(B.base + Smem::small);
-  for (int q = t; q < kNSmall; q += kTile) {
-    float v;
-    if (q < 4 * kH) v = p[kOffW1 + q];
-    else if (q < 5 * kH) v = p[kOffB1 + q - 4 * kH];
-    else if (q < 6 * kH) v = p[kOffB2 + q - 5 * kH];
-    else if (q < 7 * kH) v = p[kOffW3 + q - 6 * kH];
-    else v = p[kOffB3 + q - 7 * kH];  // b3, out_mu, out_sigma
-    sp[q] = v;
+  float4 *sp4 = reinterpret_cast<float4 *>(B.base + Smem::small);
+  for (int k = t; k < kH; k += kTile) {
+    sp4[2 * k] = make_float4(p[kOffW1 + 4 * k], p[kOffW1 + 4 * k + 1], p[kOffW1 + 4 * k + 2], p[kOffW1 + 4 * k + 3]);
+    sp4[2 * k + 1] = make_float4(p[kOffB1 + k], p[kOffB2 + k], p[kOffW3 + k], 0.0f);
   }
+  if (t == 0) sp4[2 * kH] = make_float4(p[kOffB3], 0.0f, 0.0f, 0.0f);
   if (t < 32) tmem_alloc(B.sbase + Smem::taddr);
   if (t == 0) mbar_init(B.sbase + Smem::bar);
   fence_proxy_async();
@@ -197,7 +195,7 @@ __device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float 
 // the block gives up (the context's setting, default kWaitLimit).
 __device__ __forceinline__ float guess(Block &B, const float f[4], int wait_limit, unsigned long long *timeouts) {
   const int t = threadIdx.x;
-  const float *sp = reinterpret_cast<const float *>(B.base + Smem::small);
+  const float4 *sp4 = reinterpret_cast<const float4 *>(B.base + Smem::small);
   if (B.ok) {
     // layer 1 on the CUDA cores, row t of A as hi and lo BF16 pieces
 #pragma unroll
@@ -209,9 +207,8 @@ __device__ __forceinline__ float guess(Block &B, const float f[4], int wait_limi
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const int k = kg * 8 + 2 * e + u;
-          float z = sp[4 * kH + k];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) z = fmaf(sp[4 * k + i], f[i], z);
+          const float4 w = sp4[2 * k];
+          const float z = fmaf(w.w, f[3], fmaf(w.z, f[2], fmaf(w.y, f[1], fmaf(w.x, f[0], sp4[2 * k + 1].x))));
           h[u] = silu(z);
         }
         const float h0 = __bfloat162float(__float2bfloat16_rn(h[0])), h1 = __bfloat162float(__float2bfloat16_rn(h[1]));
@@ -251,15 +248,15 @@ __device__ __forceinline__ float guess(Block &B, const float f[4], int wait_limi
   fence_after_sync();
   // epilogue: row t of the accumulator (TMEM lanes 32w.. for warp w), bias, SiLU, output layer
   const uint32_t row = B.tmem + ((uint32_t)(t & ~31) << 16);
-  float y = sp[7 * kH];
+  float y = sp4[2 * kH].x;
 #pragma unroll
   for (int half = 0; half < 2; ++half) {
     float z[32];
     tmem_ld32(row + 32u * half, z);
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
-      const int n = 32 * half + i;
-      y = fmaf(sp[6 * kH + n], silu(z[i] + sp[5 * kH + n]), y);
+      const float4 q = sp4[2 * (32 * half + i) + 1];  // b1, b2, w3 of neuron n
+      y = fmaf(q.z, silu(z[i] + q.y), y);
     }
   }
   // the next tile's MMA may overwrite the accumulator only after every lane has read it

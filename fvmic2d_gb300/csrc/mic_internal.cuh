@@ -157,6 +157,7 @@ struct mic_ctx {
   // per-marker scratch
   double *scr0, *scr1, *scr2;
   double *node_scr[6];  // nodal scratch (NX*NY each)
+  void *adv_coef;       // per-cell bilinear coefficients of vx, vy, wxy for the advection (product build)
   double *red_buf;     // reduction partials
   int red_cap;
   mic::Status *d_status;

@@ -79,21 +79,7 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
                                              int &creep_active) {
   bool yielded = false;
   const double eta_old = c.eta[m], mu_old = c.mu[m];
-  double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
-  // visco-elastic forecast with the old viscosity and modulus (markers.c:1397-1402)
-  const double Xf = eta_old / (mu_old * dt + eta_old);
-#ifdef MIC_EXACT
-  const double fxx = s11 * Xf + 2 * eta_old * e11 * (1.0 - Xf);
-  const double fyy = s22 * Xf + 2 * eta_old * e22 * (1.0 - Xf);
-  const double fxy = s12 * Xf + 2 * eta_old * e12 * (1.0 - Xf);
-#else
-  const double ve = 2 * eta_old * (1.0 - Xf);  // shared by the three components
-  const double fxx = fma(s11, Xf, ve * e11);
-  const double fyy = fma(s22, Xf, ve * e22);
-  const double fxy = fma(s12, Xf, ve * e12);
-#endif
-  const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
   const int k = c.mat[m];
   double eta, mu;
   ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], lx_guess, 0, 0, 0.0, kc != nullptr, {}, kedot};
@@ -107,6 +93,21 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
   creep_active = M.hasEtaT[k] == 7;
   const int plast = M.hasPlasticity[k];
   if (plast) {
+    // visco-elastic forecast with the old viscosity and modulus (markers.c:1397-1402); only the
+    // yield test reads it (the rheology laws take no stress), so only plastic materials form it
+    double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+    const double Xf = eta_old / (mu_old * dt + eta_old);
+#ifdef MIC_EXACT
+    const double fxx = s11 * Xf + 2 * eta_old * e11 * (1.0 - Xf);
+    const double fyy = s22 * Xf + 2 * eta_old * e22 * (1.0 - Xf);
+    const double fxy = s12 * Xf + 2 * eta_old * e12 * (1.0 - Xf);
+#else
+    const double ve = 2 * eta_old * (1.0 - Xf);  // shared by the three components
+    const double fxx = fma(s11, Xf, ve * e11);
+    const double fyy = fma(s22, Xf, ve * e22);
+    const double fxy = fma(s12, Xf, ve * e12);
+#endif
+    const double sii = sqrt(0.5 * (fxx * fxx + fyy * fyy) + fxy * fxy);
     double sy;
     if (plast == 1) {
       sy = M.materialCohesion[k] + M.materialFriction[k] * c.p[m];
@@ -761,6 +762,77 @@ __global__ void k_subgridT_apply(Params P, SubTCols c, Geo g, const double *__re
   c.Tdot[m] = dtm / dt;
 }
 
+#ifndef MIC_EXACT
+// A nodal field's bilinear form on one cell in coefficient form, v = c0 + tx c1 + ty (c2 + tx c3)
+// (corners 00, 10, 01, 11 as in lerp2): three FMAs per evaluation instead of three subtractions
+// and three FMAs.  The advection evaluates eleven of these per marker on three fields; forming
+// the coefficients once per cell and step (a node kernel) moves the subtractions off the marker
+// loop.  32-byte records: one cell's form is one aligned sector.
+struct alignas(32) Bil4 {
+  double c0, c1, c2, c3;
+};
+__device__ __forceinline__ Bil4 bil_coef(double f00, double f10, double f01, double f11) {
+  Bil4 b;
+  b.c0 = f00;
+  b.c1 = f10 - f00;
+  b.c2 = f01 - f00;
+  b.c3 = (f11 - f01) - b.c1;
+  return b;
+}
+__device__ __forceinline__ double bil_eval(const Bil4 *__restrict__ cells, size_t k, double tx, double ty) {
+  const double2 lo = __ldg(reinterpret_cast<const double2 *>(cells + k));
+  const double2 hi = __ldg(reinterpret_cast<const double2 *>(cells + k) + 1);
+  return fma(ty, fma(tx, hi.y, hi.x), fma(tx, lo.y, lo.x));
+}
+
+// The cells the advection interpolates on (markers.c:1978-2029), with the boundary ghosts it
+// forms there: vx cells (NX-1 per row, rows vxY = -1 .. NY-2, the top ghost row from the top
+// boundary condition), vy cells (NX per row, columns vyX = -1 .. NX-2, the left ghost column from
+// the left boundary condition, rows 0 .. NY-2) and basic cells of the vorticity.
+__global__ void k_advect_coef(const double *__restrict__ vx, const double *__restrict__ vy,
+                              const double *__restrict__ wz, mic_bcinfo top, mic_bcinfo left, int NX, int NY,
+                              Bil4 *cvx, Bil4 *cvy, Bil4 *cwz) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < (int64_t)NY * (NX - 1)) {
+    const int row = (int)(k / (NX - 1)), i = (int)(k % (NX - 1));
+    const size_t r1 = (size_t)row * NX;
+    double vul, vur;
+    if (row == 0 && top.type[0] == 0) {
+      vul = 2.0 * top.value[0] - vx[r1 + i];
+      vur = 2.0 * top.value[0] - vx[r1 + i + 1];
+    } else if (row == 0) {
+      vul = vx[r1 + i];
+      vur = vx[r1 + i + 1];
+    } else {
+      vul = vx[r1 - NX + i];
+      vur = vx[r1 - NX + i + 1];
+    }
+    cvx[k] = bil_coef(vul, vur, vx[r1 + i], vx[r1 + i + 1]);
+  }
+  if (k < (int64_t)(NY - 1) * NX) {
+    const int j = (int)(k / NX), col = (int)(k % NX);
+    const size_t q0 = (size_t)j * NX, q1 = q0 + NX;
+    double wul, wll;
+    if (col == 0 && left.type[1] == 0) {
+      wul = 2.0 * left.value[1] - vy[q0];
+      wll = 2.0 * left.value[1] - vy[q1];
+    } else if (col == 0) {
+      wul = vy[q0];
+      wll = vy[q1];
+    } else {
+      wul = vy[q0 + col - 1];
+      wll = vy[q1 + col - 1];
+    }
+    cvy[k] = bil_coef(wul, vy[q0 + col], wll, vy[q1 + col]);
+  }
+  if (k < (int64_t)(NY - 1) * (NX - 1)) {
+    const int j = (int)(k / (NX - 1)), i = (int)(k % (NX - 1));
+    const size_t w0 = (size_t)j * NX + i;
+    cwz[k] = bil_coef(wz[w0], wz[w0 + 1], wz[w0 + NX], wz[w0 + NX + 1]);
+  }
+}
+#endif
+
 struct AdvectCols {
   const int *cellX, *cellY;
   double *X, *Y, *VX, *VY, *wxy, *sxx, *syy, *sxy, *Eii;
@@ -771,11 +843,22 @@ struct AdvectCols {
 // wz_known (product build): the marker's wxy column holds the vorticity k_strain_pressure of this
 // step interpolated at the marker (the first stage's value: same nodes, weights and order)
 // one in-domain marker m in stored cell (ci, cj); returns its rotated sxx
+// (product build: cv holds the per-cell coefficient forms of vx, vy, wz, k_advect_coef)
+struct AdvectCoef {
+  const void *cvx, *cvy, *cwz;
+};
 __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCols &c, const Geo &g,
                                                 const double *__restrict__ vx, const double *__restrict__ vy,
-                                                const double *__restrict__ wz, const mic_bcinfo &top,
-                                                const mic_bcinfo &left, double dt, int64_t m, int ci, int cj,
-                                                int wz_known) {
+                                                const double *__restrict__ wz, const AdvectCoef &cv,
+                                                const mic_bcinfo &top, const mic_bcinfo &left, double dt, int64_t m,
+                                                int ci, int cj, int wz_known) {
+#ifndef MIC_EXACT
+  const Bil4 *__restrict__ cvx = static_cast<const Bil4 *>(cv.cvx);
+  const Bil4 *__restrict__ cvy = static_cast<const Bil4 *>(cv.cvy);
+  const Bil4 *__restrict__ cwz = static_cast<const Bil4 *>(cv.cwz);
+#else
+  (void)cv;
+#endif
   const int NX = P.NX, NY = P.NY;
   const double X0 = c.X[m], Y0 = c.Y[m];
   double xcur = X0, ycur = Y0;
@@ -829,6 +912,7 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     const double tx = mdx;
     const double ty = (s == 0) ? g.gy1[m] : ay * P.iyc[vxY + 1];
 #endif
+#ifdef MIC_EXACT
     const size_t r1 = (size_t)(vxY + 1) * NX;
     double vul, vur;
     if (vxY == -1 && top.type[0] == 0) {
@@ -842,15 +926,15 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
       vur = vx[r1 - NX + vxX + 1];
     }
     const double vll = vx[r1 + vxX], vlr = vx[r1 + vxX + 1];
-#ifdef MIC_EXACT
     double t = vul * (1.0 - ax / hx) * (1.0 - ay / hy);
     t += vur * (ax / hx) * (1.0 - ay / hy);
     t += vll * (1.0 - ax / hx) * (ay / hy);
     t += vlr * (ax * ay) / hx / hy;
 #else
-    double t = lerp2(vul, vur, vll, vlr, tx, ty);
+    double t = bil_eval(cvx, (size_t)(vxY + 1) * (NX - 1) + vxX, tx, ty);
 #endif
     mvx[s] = t;
+#ifdef MIC_EXACT
     const size_t q0 = (size_t)vyY * NX, q1 = q0 + NX;
     const double wur = vy[q0 + vyX + 1], wlr = vy[q1 + vyX + 1];
     double wul, wll;
@@ -864,7 +948,6 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
       wul = vy[q0 + vyX];
       wll = vy[q1 + vyX];
     }
-#ifdef MIC_EXACT
     ax = xcur - P.xc[vyX + 1];
     ay = ycur - P.y[vyY];
     hx = P.xc[vyX + 2] - P.xc[vyX + 1];
@@ -874,11 +957,12 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     t += wll * (1.0 - ax / hx) * (ay / hy);
     t += wlr * (ax * ay) / hx / hy;
 #else
-    t = lerp2(wul, wur, wll, wlr, (s == 0) ? g.gx1[m] : (xcur - P.xc[vyX + 1]) * P.ixc[vyX + 1], mdy);
+    t = bil_eval(cvy, (size_t)vyY * NX + vyX + 1, (s == 0) ? g.gx1[m] : (xcur - P.xc[vyX + 1]) * P.ixc[vyX + 1],
+                 mdy);
 #endif
     mvy[s] = t;
-    const size_t w0 = (size_t)j * NX + i;
 #ifdef MIC_EXACT
+    const size_t w0 = (size_t)j * NX + i;
     const double mdx = div_sp(xcur - P.x[i], P.hx[i], P.ix[i]);
     const double mdy = div_sp(ycur - P.y[j], P.hy[j], P.iy[j]);
     t = (1.0 - mdx) * (1.0 - mdy) * wz[w0];
@@ -889,7 +973,7 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     if (s == 0)  // at the marker itself: the bilinear form of the stored weights
       t = wz_known ? c.wxy[m] : interp_w(wz, NX, i, j, load_w4(g.w0, m));
     else
-      t = lerp2(wz[w0], wz[w0 + 1], wz[w0 + NX], wz[w0 + NX + 1], mdx, mdy);
+      t = bil_eval(cwz, (size_t)j * (NX - 1) + i, mdx, mdy);
 #endif
     mwz[s] = t;
     if (s < 2) {
@@ -937,14 +1021,14 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
 template <bool MAXS>
 __global__ void __launch_bounds__(512, 2) k_advect(Params P, AdvectCols c, Geo g, const double *__restrict__ vx,
                                                    const double *__restrict__ vy, const double *__restrict__ wz,
-                                                   mic_bcinfo top, mic_bcinfo left, double dt, int64_t n,
-                                                   int wz_known, unsigned long long *maxs) {
+                                                   AdvectCoef cv, mic_bcinfo top, mic_bcinfo left, double dt,
+                                                   int64_t n, int wz_known, unsigned long long *maxs) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   long long b = 0;  // bits of 0.0
   if (m < n) {
     const int ci = c.cellX[m], cj = c.cellY[m];
     if (ci != -1) {
-      const double a = fabs(advect_marker(P, c, g, vx, vy, wz, top, left, dt, m, ci, cj, wz_known));
+      const double a = fabs(advect_marker(P, c, g, vx, vy, wz, cv, top, left, dt, m, ci, cj, wz_known));
       if (MAXS && a > 0.0) b = __double_as_longlong(a);
     }
   }
@@ -1428,16 +1512,33 @@ static int advect_launch(mic_ctx *ctx, double dt, bool wz_known, bool with_max =
     c.exx = ctx->f64[C_EXX];
     c.eyy = ctx->f64[C_EYY];
     c.exy = ctx->f64[C_EXY];
+    AdvectCoef cv = {nullptr, nullptr, nullptr};
+#ifndef MIC_EXACT
+    {
+      const int NX = ctx->P.NX, NY = ctx->P.NY;
+      const size_t nn = (size_t)NX * NY;
+      if (!ctx->adv_coef && cudaMalloc((void **)&ctx->adv_coef, 3 * nn * sizeof(Bil4)) != cudaSuccess) {
+        ctx->adv_coef = nullptr;
+        return MIC_ERR_NOMEM;
+      }
+      Bil4 *cb = static_cast<Bil4 *>(ctx->adv_coef);
+      cv = {cb, cb + nn, cb + 2 * nn};
+      MIC_KERNEL(ctx, "k_advect_coef");
+      k_advect_coef<<<grid_for((int64_t)nn), kBlock, 0, ctx->stream>>>(
+          ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
+          ctx->bcs.mechBCLeft, NX, NY, cb, cb + nn, cb + 2 * nn);
+    }
+#endif
     {
       MIC_KERNEL(ctx, "k_advect");
       const int B = tuned_block(ctx, TU_ADVECT);
       if (with_max)
         k_advect<true><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(
-            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY],
+            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY], cv,
             ctx->bcs.mechBCTop, ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0, d);
       else
         k_advect<false><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(
-            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY],
+            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY], cv,
             ctx->bcs.mechBCTop, ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0, nullptr);
     }
     MIC_CUDA_TRY(cudaGetLastError());
