@@ -850,6 +850,31 @@ __global__ void k_fill_i32(int *col, int v, int64_t n) {
   if (m < n) col[m] = v;
 }
 
+// resetMarker (markers.c:255-330) on a host array: the same values k_reset_markers gives the
+// device columns, for host code that owns a marker array before any context exists
+// (allocateMarkers resets its fresh array)
+extern "C" int mic_markers_reset_host(mic_marker *m, int64_t n) {
+  if (n < 0 || (n > 0 && !m)) return MIC_ERR_ARG;
+  for (int64_t k = 0; k < n; ++k) {
+    mic_marker &r = m[k];
+    r.X = -1.0;
+    r.Y = -1.0;
+    r.VX = r.VY = 0.0;
+    r.T = r.Tdot = 0.0;
+    r.s.T11 = r.s.T22 = r.s.T12 = 0.0;
+    r.eta = 0.0;
+    r.rho = r.rhodot = 0.0;
+    r.p = 0.0;
+    r.e.T11 = r.e.T22 = r.e.T12 = 0.0;
+    r.E.T11 = r.E.T22 = r.E.T12 = 0.0;
+    r.Eii = 0.0;
+    r.wxy = 0.0;
+    r.Mat = -1;
+    r.isYielding = 0;
+  }
+  return MIC_OK;
+}
+
 extern "C" int mic_reset_markers(mic_ctx *ctx) {
   if (!ctx) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);

@@ -61,6 +61,13 @@ __device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, i
 }
 #endif
 
+// limitViscosity (viscosity.c:90-104) on one viscosity
+__device__ __forceinline__ double limit_eta(double e, const mic_options &O) {
+  if (e > O.etamax) return O.etamax;
+  if (e < O.etamin) return O.etamin;
+  return e;
+}
+
 struct YieldCols {
   const int *cellX, *mat;
   const double *X, *Y, *T, *p, *Eii, *exx, *eyy, *exy, *grain;
@@ -76,7 +83,7 @@ template <bool CREEP = true>
 __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_materials &M, const mic_options &O,
                                              const CreepConfig &cfg, double dt, int64_t m, float lx_guess,
                                              const CreepCoef *kc, double kedot, Status *st, CreepIn &ci,
-                                             int &creep_active) {
+                                             int &creep_active, int limit) {
   bool yielded = false;
   const double eta_old = c.eta[m], mu_old = c.mu[m];
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
@@ -152,6 +159,7 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
     }
     eta = etanew;
   }
+  if (limit) eta = limit_eta(eta, O);  // limitViscosity fused (the step runs it right after)
   c.eta[m] = eta;
   c.mu[m] = mu;
   return yielded;
@@ -175,9 +183,10 @@ __device__ __forceinline__ bool creep_marker_features(const YieldCols &c, const 
 
 // checkPlasticYielding, one thread per marker.  MODE 0: exact creep solve; MODE 1: surrogate
 // guess on the CUDA cores (FP32), polish and fallback; MODE 2: no material uses law 7.
+// limit: limitViscosity fused in (every marker, out-of-domain ones included, viscosity.c:93-95)
 template <int MODE>
 __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig cfg, double dt, int64_t n,
-                        Status *st, CreepCounters *cc) {
+                        Status *st, CreepCounters *cc, int limit) {
   __shared__ int s_yield;
   __shared__ float w2s[MODE == 1 ? kH * kH : 1];
   if (threadIdx.x == 0) s_yield = 0;
@@ -193,8 +202,10 @@ __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig
     CreepCoef k;
     const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, edot, f, &mref);
     if (law7) lx = creep_guess_lx(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
-    if (yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, st, ci, creep_active))
+    if (yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, st, ci, creep_active, limit))
       s_yield = 1;
+  } else if (limit && m < n) {
+    c.eta[m] = limit_eta(c.eta[m], O);
   }
   if (MODE != 2) creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   __syncthreads();
@@ -205,7 +216,7 @@ __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig
 // blocks of 128 threads, one 128-marker tile per round (mic_creep_tc.cuh).
 __global__ void __launch_bounds__(tc::kTile) k_yield_tc(YieldCols c, mic_materials M, mic_options O,
                                                         CreepConfig cfg, double dt, int64_t n, Status *st,
-                                                        CreepCounters *cc) {
+                                                        CreepCounters *cc, int limit) {
   extern __shared__ unsigned char dyn[];
   __shared__ int s_yield;
   if (threadIdx.x == 0) s_yield = 0;
@@ -223,8 +234,9 @@ __global__ void __launch_bounds__(tc::kTile) k_yield_tc(YieldCols c, mic_materia
     int creep_active = 0;
     CreepIn ci = {};
     if (live && yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 ? &k : nullptr, edot, st,
-                             ci, creep_active))
+                             ci, creep_active, limit))
       s_yield = 1;
+    if (limit && !live && m < n) c.eta[m] = limit_eta(c.eta[m], O);
     creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   }
   tc::teardown(B, &cc->tc_drain_timeouts);
@@ -1198,7 +1210,8 @@ extern "C" int mic_max_abs_sxx(mic_ctx *ctx, double *v) {
   return run_max(ctx, C_SXX, 1, v);
 }
 
-static int yield_launch(mic_ctx *ctx, double dt) {
+// limit: limitViscosity (viscosity.c:90-104) fused into the pass, for callers that run it next
+static int yield_launch(mic_ctx *ctx, double dt, bool limit = false) {
   int e = mic_ensure_sorted(ctx);
   if (e) return e;
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->is_yielding, 0, sizeof(int), ctx->stream));
@@ -1211,21 +1224,21 @@ static int yield_launch(mic_ctx *ctx, double dt) {
     if (!law7) {
       MIC_KERNEL(ctx, "k_yield");
       k_yield<2><<<grid_for(ctx->n, tuned_block(ctx, TU_YIELD)), tuned_block(ctx, TU_YIELD), 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
-                                                               dt, ctx->n, ctx->d_status, ctx->d_creep);
+                                                               dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
     } else if (mode == 0) {
       MIC_KERNEL(ctx, "k_yield");
       k_yield<0><<<grid_for(ctx->n, tuned_block(ctx, TU_YIELD)), tuned_block(ctx, TU_YIELD), 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
-                                                               dt, ctx->n, ctx->d_status, ctx->d_creep);
+                                                               dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
     } else if (mode == 1) {
       MIC_KERNEL(ctx, "k_yield_surrogate_fp32");
       k_yield<1><<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
-                                                                 dt, ctx->n, ctx->d_status, ctx->d_creep);
+                                                                 dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
     } else {
       MIC_CUDA_TRY(cudaFuncSetAttribute(k_yield_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)tc::kDynSmem));
       MIC_KERNEL(ctx, "k_yield_tc");
       k_yield_tc<<<mic_creep_tc_blocks(ctx, ctx->n), tc::kTile, tc::kDynSmem, ctx->stream>>>(
-          yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep, dt, ctx->n, ctx->d_status, ctx->d_creep);
+          yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep, dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
     }
     MIC_CUDA_TRY(cudaGetLastError());
   }
@@ -1312,7 +1325,10 @@ extern "C" int mic_update_marker_strain_pressure(mic_ctx *ctx, double dt) {
 
 static int residual_launch(mic_ctx *ctx, int iter, double *res_dev, cudaStream_t st = nullptr) {
   const cudaStream_t s = st ? st : ctx->stream;
-  int e = mic_project_scalar(ctx, ctx->f64[C_SRR], -1, ctx->nodal[MIC_NF_SRR], s);
+  // binning first: a re-sort swaps the column buffers, so the srr column is taken after it
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  e = mic_project_scalar(ctx, ctx->f64[C_SRR], -1, ctx->nodal[MIC_NF_SRR], s);
   if (e) return e;
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
   const int nb = (int)grid_for(nn);
@@ -1343,6 +1359,19 @@ extern "C" int mic_update_global_strain_rate_residual(mic_ctx *ctx, int iter, do
   s /= (ctx->P.LX * ctx->P.LY);
   ctx->residuals[iter % 100] = s;
   if (residual) *residual = s;
+  return MIC_OK;
+}
+
+// getGlobalStrainRateResidual / setGlobalStrainRateResidual (residual.c, residual.h:2-3): the
+// stored residual of plasticity iteration iter (100 slots, as the reference's NRES)
+extern "C" int mic_get_strain_rate_residual(mic_ctx *ctx, int iter, double *value) {
+  if (!ctx || !value || iter < 0) return MIC_ERR_ARG;
+  *value = ctx->residuals[iter % 100];
+  return MIC_OK;
+}
+extern "C" int mic_set_strain_rate_residual(mic_ctx *ctx, int iter, double value) {
+  if (!ctx || iter < 0) return MIC_ERR_ARG;
+  ctx->residuals[iter % 100] = value;
   return MIC_OK;
 }
 
@@ -1591,14 +1620,14 @@ extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yieldin
   // The first projection (main:268) and the yield pass touch disjoint marker columns (rho, T,
   // materials against viscosity, modulus and stresses), and the first projection's viscosity and
   // stress fields are replaced by the second (main:303) before anything reads them: so it forms
-  // only rho, k, T and Cp, on the second stream, beside the yield pass and the viscosity limit.
+  // only rho, k, T and Cp, on the second stream, beside the yield pass (which applies the
+  // viscosity limit of main:297 to every marker as it stores the viscosities).
   if ((e = mic_ensure_geometry(ctx))) return e;
   MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
   MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
   if ((e = mic_project_all2_first(ctx, ctx->aux))) return e;
   MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
-  if ((e = yield_launch(ctx, dt_disp))) return e;
-  if ((e = mic_limit_viscosity(ctx))) return e;
+  if ((e = yield_launch(ctx, dt_disp, /*limit=*/true))) return e;  // limitViscosity fused in
   MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
   // the second projection: yielding and the limit changed viscosities and stresses only
   if ((e = mic_project_all2_viscous(ctx))) return e;

@@ -67,6 +67,9 @@ SIGNATURES = {
     "mic_debug_sorted_ids": (_I, [_P, _P]),
     "mic_debug_cell_start": (_I, [_P, _P]),
     "mic_debug_div_sp": (_I, [_P, _P, _P, _I64, _P]),
+    "mic_markers_reset_host": (_I, [_P, _I64]),
+    "mic_get_strain_rate_residual": (_I, [_P, _I, _DP]),
+    "mic_set_strain_rate_residual": (_I, [_P, _I, _D]),
     "mic_launch_count": (_I, [_P, _I64P]),
     "mic_profile_enable": (_I, [_P, _I]),
     "mic_profile_read": (_I, [_P, _I, _P, _DP, _I64P, _IP]),

@@ -118,6 +118,10 @@ int mic_update_marker_strain_pressure(mic_ctx *ctx, double dt);
 int mic_update_global_strain_rate_residual(mic_ctx *ctx, int iter, double *residual);
 /* checkConvergence (residual.c:53-69; residual.h:5) over the stored residuals */
 int mic_check_convergence(mic_ctx *ctx, double atol, double rtol, int iter, int *converged);
+/* getGlobalStrainRateResidual / setGlobalStrainRateResidual (residual.c; residual.h:2-3): the
+ * stored residual of iteration iter (100 slots) */
+int mic_get_strain_rate_residual(mic_ctx *ctx, int iter, double *value);
+int mic_set_strain_rate_residual(mic_ctx *ctx, int iter, double value);
 /* subgridStressChanges (subgridStressChanges.c:5-318; subgridStressChanges.h:1) */
 int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double diffusivity);
 /* updateMarkerStress (updateMarkerStress.c:5-163; updateMarkerStress.h:1) */
@@ -237,6 +241,9 @@ int mic_set_tuning(mic_ctx *ctx, const int *block, int count);
  * kinematic, thermal, stress, strain and density fields 0; mu, cellX, cellY, cpu and the
  * strain-rate residual untouched).  The marker count is unchanged. */
 int mic_reset_markers(mic_ctx *ctx);
+/* resetMarker's values on a host marker array (no device work): for host code that owns the array
+ * before a context exists (allocateMarkers, markers.c:15-27) */
+int mic_markers_reset_host(mic_marker *markers, int64_t n);
 /* current number of markers (MarkerSet.nMark) */
 int mic_marker_count(mic_ctx *ctx, int64_t *n);
 /* distributeMarkersUniformInDomain on one rank: NMX x NMY markers per basic cell of the

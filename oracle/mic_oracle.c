@@ -995,6 +995,17 @@ int orc_creep_stress(double edot, double T, double d, double P, double rtol, dou
   return ORC_OK;
 }
 
+/* orc_creep_stress over arrays (test access: large strided samples in one call) */
+int orc_creep_stress_batch(const double *edot, const double *T, const double *d, const double *P, int64_t n,
+                           double rtol, double *s_out, int *iters) {
+  for (int64_t m = 0; m < n; ++m) {
+    int it = 0;
+    orc_creep_stress(edot[m], T[m], d[m], P[m], rtol, &s_out[m], &it);
+    if (iters) iters[m] = it;
+  }
+  return ORC_OK;
+}
+
 /* ---- marker lifecycle -------------------------------------------------------------- */
 
 /* resetMarker (markers.c:255-330): the fields the reference zeroes; mu, cellX, cellY, cpu and

@@ -78,6 +78,8 @@ int64_t orc_sizeof(int which);
 void orc_set_grain(orc_ctx *c, const double *d, int64_t n);
 double orc_gk_strain_rate(double s, double T, double d, double P);
 int orc_creep_stress(double edot, double T, double d, double P, double rtol, double *s_out, int *iters);
+int orc_creep_stress_batch(const double *edot, const double *T, const double *d, const double *P, int64_t n,
+                           double rtol, double *s_out, int *iters);
 
 /* marker lifecycle: resetMarker (markers.c:255-330) and distributeMarkersUniformInDomain
  * (markers.c:342-400) with the stand-in's seeded erand48 stream */

@@ -55,6 +55,7 @@ def lib():
             "orc_set_grain": (None, [_P, _DP, _I64]),
             "orc_gk_strain_rate": (_D, [_D, _D, _D, _D]),
             "orc_creep_stress": (_I, [_D, _D, _D, _D, _D, _DP, _IP]),
+            "orc_creep_stress_batch": (_I, [_DP, _DP, _DP, _DP, _I64, _D, _DP, _P]),
             "orc_reset_markers": (None, [_P, _I64]),
             "orc_srand48_state": (ctypes.c_uint64, [ctypes.c_long]),
             "orc_nodal_stress_strain": (None, [_P, _D]),
@@ -268,13 +269,10 @@ def gk_strain_rate(s, T, d, P):
 
 
 def creep_stress(edot, T, d, P, rtol=1e-14):
-    """Stress at which the reference law's strain rate equals edot (oracle solve)."""
-    f = lib().orc_creep_stress
-    out, its = [], []
-    for a, b, c, e in np.broadcast(np.asarray(edot), np.asarray(T), np.asarray(d), np.asarray(P)):
-        sv = ctypes.c_double(0.0)
-        it = ctypes.c_int(0)
-        f(float(a), float(b), float(c), float(e), rtol, ctypes.byref(sv), ctypes.byref(it))
-        out.append(sv.value)
-        its.append(it.value)
-    return np.array(out), np.array(its)
+    """Stress at which the reference law's strain rate equals edot (oracle solve, one C call)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in np.broadcast_arrays(edot, T, d, P)]
+    n = len(arrs[0])
+    out = np.zeros(n)
+    its = np.zeros(n, dtype=np.int32)
+    lib().orc_creep_stress_batch(*[_dp(a) for a in arrs], n, rtol, _dp(out), its.ctypes.data)
+    return out, its

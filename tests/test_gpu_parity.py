@@ -429,3 +429,25 @@ def test_step_split_reports_max_temperature_and_yielding():
     B.advectMarkersRK(wl.dt_thermal)
     assert mx.value == B.maxAbsSxx() > 0.0
     assert not compare_markers(A.markers, B.markers)
+
+
+@pytest.mark.parametrize("exact_build", [False, True])
+def test_residual_of_markers_not_yet_binned(exact_build):
+    """updateGlobalStrainRateResidual called on markers just uploaded in the caller's order (the
+    binning it triggers re-sorts the columns): the residual of the sorted strain-rate residuals,
+    the same as from markers already binned, and the oracle's"""
+    wl = W.vep_slab_box(nx_cells=32, ny_cells=8, nm=4, seed=5)
+    G = gpu.MicProblem(wl, exact=exact_build)
+    O = oraclepy.OracleProblem(wl)
+    for P in (G, O):
+        P.findMarkerCells()
+        P.updateMarkerRho()
+        P.projectMarkersNodesAll2()
+        P.updateMarkerStrainPressure(wl.dt)
+    r_bin = G.updateGlobalStrainRateResidual(0)
+    r_o = O.updateGlobalStrainRateResidual(0)
+    G.upload_markers(G.markers)  # caller order, no binning yet
+    r_up = G.updateGlobalStrainRateResidual(1)
+    assert r_up == r_bin
+    ok, msg = close([r_up], [r_o], RTOL)
+    assert ok, msg
