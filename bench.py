@@ -76,14 +76,17 @@ KERNEL_BYTES = {
     "k_advect": (8 + 16 + 24 + 24 + 8 + 16 + 16 + 8 + 24 + 8, 24),
     # cellX, cellY, flags, 4 offsets, X, Y, eta, mu read; p, e3, wxy, srr written; 10 nodal read
     "k_strain_pressure": (8 + 4 + 32 + 16 + 16 + 8 + 24 + 8 + 8, 80),
-    # cellX, Mat, X, Y, T, p, Eii, e3, eta, mu, s3 read; eta, mu, s3 written
-    "k_yield": (8 + 16 + 8 + 8 + 8 + 24 + 16 + 24 + 16 + 24, 0),
-    # law-7 variants read the grain size as well
-    "k_yield_surrogate_fp32": (8 + 16 + 8 + 8 + 8 + 24 + 16 + 24 + 16 + 24 + 8, 0),
-    "k_yield_tc": (8 + 16 + 8 + 8 + 8 + 24 + 16 + 24 + 16 + 24 + 8, 0),
+    # plastic materials: cellX, Mat, T, p, Eii, e3, eta, mu, s3 read; eta, mu, s3 written
+    "k_yield": (4 + 4 + 8 + 8 + 8 + 24 + 16 + 24 + 40, 0),
     # all 29 marker columns read and written
     "k_reorder": (2 * (23 * 8 + 6 * 4) + 4, 0),
 }
+
+
+# The law-7 pass of the ice workload (no plastic yield: the visco-elastic forecast and stresses are
+# not read): cellX, Mat, T, p, e3, eta, mu and the grain factor read; eta, mu written
+KERNEL_BYTES_LAW7 = {k: (4 + 4 + 8 + 8 + 24 + 16 + 8 + 16, 0) for k in ("k_yield", "k_yield_tc",
+                                                                      "k_yield_surrogate_fp32")}
 
 
 # DRAM bytes per marker of one launch from an ncu capture (dram__bytes_read.sum +
@@ -92,13 +95,17 @@ KERNEL_BYTES = {
 # the 32 B/marker of stored offsets the first RK4 stage loads instead of forming them (bytes for
 # FP64 instructions); at the small size part of the written bytes is still in L2 when the kernel
 # ends.
-KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (127373312 + 32452608) / 1048576}
-# FP64 work per marker from the same capture (per-cycle DFMA / DADD / DMUL thread instructions x
-# elapsed cycles / markers: 67.9 / 60.9 / 32.9): flops with DFMA counted twice, and the FP64
-# arithmetic instructions (the three summed, 161.7).  The kernels of this path are bound by the
-# FP64 pipe, which issues 2 FP64 instructions per SM per clock on GB300, not by HBM.
-KERNEL_FP64_FLOPS_PER_MARKER = {"k_advect": 229.6}
-KERNEL_FP64_INST_PER_MARKER = {"k_advect": 161.7}
+# The advection and the law-7 passes from captures of the 4,194,304-marker ice box
+# (profiles/k_advect_ice_creep_box_4m_full.md, profiles/k_yield_creep_ice_creep_box_4m_full.md).
+KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (528.6e6 + 258.5e6) / 4194304, "k_yield_tc": (302.1e6 + 50.6e6) / 4194304,
+                             "k_yield": (302.2e6 + 48.7e6) / 4194304}
+# FP64 work per marker from the same captures (DFMA, DADD, DMUL thread instructions / markers):
+# flops with a DFMA counted twice, and the FP64 arithmetic instructions.  The kernels of this path
+# are bound by the FP64 pipe, which issues 2 FP64 instructions per SM per clock on GB300, not by
+# HBM.  (k_yield: the exact law-7 pass.)
+_FP64_WARP_INSTR = {"k_advect": (8.78e6, 7.86e6), "k_yield_tc": (10.37e6, 13.31e6), "k_yield": (22.00e6, 22.11e6)}
+KERNEL_FP64_FLOPS_PER_MARKER = {k: (2 * f + u) * 32 / 4194304 for k, (f, u) in _FP64_WARP_INSTR.items()}
+KERNEL_FP64_INST_PER_MARKER = {k: (f + u) * 32 / 4194304 for k, (f, u) in _FP64_WARP_INSTR.items()}
 FP64_PEAK_TFLOPS = 2 * 2 * 152 * 2.07e9 / 1e12  # 2 DFMA/SM/clk x 2 flops x 152 SMs x 2.07 GHz
 FP64_PEAK_GINST = 2 * 152 * 2.07  # FP64 instructions per second, in G
 
@@ -378,12 +385,17 @@ def timed_steps(G, wl, args, pg, label):
     return out, prof
 
 
-def roofline(prof, n, nodes, steps, hbm_peak, peak_src):
+def roofline(prof, n, nodes, steps, hbm_peak, peak_src, law7=False):
     """HBM roofline of the step's dominant kernel (live CUDA-event duration), with its FP64 issue
     rate where ncu measured its FP64 instructions per marker"""
     kern = sorted(prof.items(), key=lambda kv: -kv[1][0])
-    top_name, (top_ms, top_cnt) = kern[0]
-    per_marker, per_node = KERNEL_BYTES.get(top_name, (0, 0))
+    # a kernel on the second stream (the first projection's partial sums) overlaps the yield pass:
+    # its event span is not its own cost, so the dominant kernel is taken among the main stream's
+    main = [kv for kv in kern if not kv[0].startswith(("k_partials_basic<first>", "k_partials_centre<scalar>",
+                                                        "k_combine_scalar<-1>", "k_residual_weight"))]
+    top_name, (top_ms, top_cnt) = (main or kern)[0]
+    table = dict(KERNEL_BYTES, **(KERNEL_BYTES_LAW7 if law7 else {}))
+    per_marker, per_node = table.get(top_name, (0, 0))
     algo = per_marker * n + per_node * nodes
     dur = top_ms / max(top_cnt, 1)
     achieved = algo / (dur * 1e-3) / 1e9
@@ -391,10 +403,11 @@ def roofline(prof, n, nodes, steps, hbm_peak, peak_src):
     roof = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak,
             "traffic": (KERNEL_TRAFFIC_PER_MARKER[top_name] * n if top_name in KERNEL_TRAFFIC_PER_MARKER else None),
-            "traffic_note": "ncu dram bytes of a smaller capture of the same kernel, scaled by markers processed",
+            "traffic_note": "ncu dram bytes of the 4,194,304-marker capture of the same kernel, scaled by markers "
+                            "processed",
             "peak_source": peak_src, "algorithmic_bytes_per_launch": algo, "ms_per_launch": dur}
     fp64 = None
-    if top_name in KERNEL_FP64_INST_PER_MARKER:
+    if top_name in KERNEL_FP64_INST_PER_MARKER and (law7 or not top_name.startswith("k_yield")):
         ipm = KERNEL_FP64_INST_PER_MARKER[top_name]
         fpm = KERNEL_FP64_FLOPS_PER_MARKER[top_name]
         fp64 = {"kernel": top_name, "flops_per_marker": fpm, "achieved": fpm * n / (dur * 1e-3) / 1e12,
@@ -536,7 +549,7 @@ def measure_workload(args, name, local, pg, world, cpu=None, with_e2e=True, with
             G.creep_configure(mode=mode, tol=CREEP_TOL, maxit=CREEP_MAXIT, polish_iters=POLISH_ITERS,
                               polish_tol=POLISH_TOL)
         rec, prof = timed_steps(G, wl, args, pg, label)
-        roof, fp64, shares, per_step = roofline(prof, n, nodes, args.steps, hbm_peak, peak_src)
+        roof, fp64, shares, per_step = roofline(prof, n, nodes, args.steps, hbm_peak, peak_src, law7)
         rec.update({"roofline": roof, "fp64_roofline": fp64, "kernel_share": shares, "kernel_ms_per_step": per_step})
         if law7:
             st = G.creep_stats()
