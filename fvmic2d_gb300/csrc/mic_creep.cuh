@@ -53,10 +53,12 @@ constexpr double kGrainDefault = 1e-3;  // metres, until mic_markers_set_grain_s
 // viscosity.c:109-173: constants of the law at (T, grain argument g, P), with P clamped below at
 // 1 Pa.  The FMA-free parity build evaluates each Arrhenius factor as the reference writes it.
 // The product build factors exp((-Q + P V) / RT) = exp(-Q / RT) exp(P V / RT); the activation
-// energies 49, 60, 180 and 192 kJ/mol are whole kJ/mol, so their factors are integer powers of
-// c = exp(-1 kJ/mol / RT) by repeated squaring (relative error about Q/kJ ulp, below 5e-14),
-// and only c, the 59.4 kJ/mol volume diffusion and the pressure factor take an exp: three
-// exponentials instead of six (both temperature branches of a warp run) plus log2 and exp2.
+// energies 49, 59.4, 60, 180 and 192 kJ/mol are whole multiples of 0.2 kJ/mol, so their factors
+// are integer powers (245, 297, 300, 900, 960) of b = exp(-0.2 kJ/mol / RT) by repeated squaring
+// and shared partial products (22 multiplies; relative error at most about one ulp of b per unit
+// of the power, below 2.2e-13 for the largest, typically a quarter of that), and only b and the
+// pressure factor take an exp: two exponentials instead of six (both temperature branches of a
+// warp run) plus log2 and exp2.
 __device__ __forceinline__ CreepCoef creep_coef(double T, double g, double P) {
   const double R = 8.3144621;
   if (P < 1.0) P = 1.0;
@@ -76,13 +78,16 @@ __device__ __forceinline__ CreepCoef creep_coef(double T, double g, double P) {
   k.B = 5.5e7 * exp((-60.0e3 + P * V) / RT);
 #else
   const double iRT = 1.0 / RT;
-  const double c1 = exp(-1.0e3 * iRT);
-  const double c2 = c1 * c1, c4 = c2 * c2, c8 = c4 * c4, c16 = c8 * c8, c32 = c16 * c16, c64 = c32 * c32,
-               c128 = c64 * c64;
-  const double e49 = (c32 * c16) * c1, e60 = (c32 * c16) * (c8 * c4);
-  const double e180 = (c128 * c32) * (c16 * c4), e192 = c128 * c64;
+  const double b1 = exp(-200.0 * iRT);
+  const double b2 = b1 * b1, b4 = b2 * b2, b8 = b4 * b4, b16 = b8 * b8, b32 = b16 * b16, b64 = b32 * b32,
+               b128 = b64 * b64, b256 = b128 * b128, b512 = b256 * b256;
+  const double b296 = (b256 * b32) * b8;
+  const double e594 = b296 * b1, e60 = b296 * b4;                          // 59.4 and 60 kJ/mol
+  const double e49 = ((b128 * b64) * (b32 * b16)) * (b4 * b1);              // b^245
+  const double b896 = (b512 * b256) * b128;
+  const double e180 = b896 * b4, e192 = b896 * b64;                          // b^900, b^960
   const double eP = exp(P * V * iRT);
-  const double Dv = 9.10e-4 * exp(-59.4e3 * iRT);
+  const double Dv = 9.10e-4 * e594;
   const double Db = 5.8e-4 * e49;
   const double g2 = g * g, id = (g2 * g2) * g;  // 1/d
   k.C = 42.0 * Vm * iRT * id * id * (Dv + M_PI * delta * id * Db);
