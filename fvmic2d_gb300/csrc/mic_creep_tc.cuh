@@ -148,16 +148,9 @@ struct Block {
   int pending;          // a committed MMA whose completion was not observed
 };
 
-// All kTile threads: carve shared memory, stage W2 (hi/lo BF16) and the small parameters,
-// allocate TMEM (warp 0) and initialise the barrier (thread 0).
-__device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float *__restrict__ p) {
-  const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(dyn);
-  const uint32_t pad = (1024u - (s0 & 1023u)) & 1023u;
-  B.base = dyn + pad;
-  B.sbase = s0 + pad;
-  B.phase = 0;
-  B.ok = 1;
-  B.pending = 0;
+// All kTile threads: write W2 (hi/lo BF16, the B operand) and the small parameters of network p
+// into the block's shared memory (no fence, no barrier).
+__device__ __forceinline__ void stage_params(Block &B, const float *__restrict__ p) {
   const int t = threadIdx.x;
   // W2 rows n (outputs) x k (inputs), K-major core matrices; 64 x 8 groups of 8 elements
   for (int g = t; g < kH * 8; g += kTile) {
@@ -180,6 +173,20 @@ __device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float 
     sp4[2 * k + 1] = make_float4(p[kOffB1 + k], p[kOffB2 + k], p[kOffW3 + k], 0.0f);
   }
   if (t == 0) sp4[2 * kH] = make_float4(p[kOffB3], 0.0f, 0.0f, 0.0f);
+}
+
+// All kTile threads: carve shared memory, stage W2 (hi/lo BF16) and the small parameters,
+// allocate TMEM (warp 0) and initialise the barrier (thread 0).
+__device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float *__restrict__ p) {
+  const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(dyn);
+  const uint32_t pad = (1024u - (s0 & 1023u)) & 1023u;
+  B.base = dyn + pad;
+  B.sbase = s0 + pad;
+  B.phase = 0;
+  B.ok = 1;
+  B.pending = 0;
+  const int t = threadIdx.x;
+  stage_params(B, p);
   if (t < 32) tmem_alloc(B.sbase + Smem::taddr);
   if (t == 0) mbar_init(B.sbase + Smem::bar);
   fence_proxy_async();
@@ -187,6 +194,20 @@ __device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float 
   __syncthreads();
   fence_after_sync();
   B.tmem = *reinterpret_cast<volatile uint32_t *>(B.base + Smem::taddr);
+}
+
+// All kTile threads, block-uniform, between two guesses: replace the staged network by p (a batch
+// of ensemble members whose networks live in different buffers).  Every MMA of the block has
+// completed by then (guess returns after its completion wait), so the operands are free; a
+// block that gave up on the tensor path keeps what it has (an abandoned MMA may still read it,
+// and its markers take the exact solve anyway).
+__device__ __forceinline__ void restage(Block &B, const float *__restrict__ p) {
+  __syncthreads();  // every thread has finished the last epilogue's reads of the small parameters
+  if (B.ok) stage_params(B, p);
+  fence_proxy_async();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
 }
 
 // All kTile threads, block-uniform: network output y for this thread's features (NaN when the

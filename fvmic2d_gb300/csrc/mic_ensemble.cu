@@ -5,6 +5,18 @@
 // launches as mic_step without a residual read, so nothing waits on the host) and joins back.
 // Small members then overlap on the GPU instead of running one after another.
 //
+// Batched (the default): a step's marker passes run as one kernel per pass over all members
+// instead of one per member.  A step is cut into segments at its marker passes
+// (mic_step_segment); each segment's own launches (binning, projections, node kernels) are
+// issued on every member's stream, the members join the ensemble stream, one batched kernel per
+// pass walks the work table of (member, tile) pairs, and the members fork again.  The table (the
+// members' launch arguments and their tile offsets) is written on the host and copied into a
+// device buffer: once per captured graph (the graph reads it at every replay), or by an
+// asynchronous copy before each pass of a step run directly (two alternating buffers).  The
+// tile size, the persistent / one-tile-per-block grid and the block-to-tile schedule come from
+// mic_ensemble_set_schedule or mic_ensemble_autotune.  Per-member (batched off): each member's
+// whole step on its own stream, between one fork and one join.
+//
 // With graphs on, the fork / members / join sequence is captured once into CUDA graphs and each
 // later step is a single graph launch.  A step's launches read the marker columns from one
 // buffer of each double-buffered pair and leave them in the other (the binning's reorder), so
@@ -39,7 +51,23 @@ struct mic_ensemble {
   long long graph_kernels[2];  // kernel launches inside each graph
   long long launches;          // kernel launches issued through this ensemble
   std::vector<int> order;      // members in the order their steps are issued (and captured)
+  // batched marker passes
+  int batched;
+  mic::BatchShape shape[mic::BP_COUNT];
+  mic_batch *batch;
+  size_t table_cap;
+  // work tables: slot 0, 1 the captured graphs of either parity; 2, 3 steps run directly (in turn)
+  unsigned char *h_table[4], *d_table[4];
+  size_t table_used[4];
+  cudaEvent_t table_ev[2];  // end of the last direct step that used slot 2 + k
+  int table_ev_live[2];
+  int direct_next;
 };
+
+constexpr int kSlotDirect = 2;
+// default walk of a batched pass: tiles of 4 blocks' worth of markers, persistent grid, blocks
+// taking contiguous runs of tiles
+constexpr mic::BatchShape kDefaultShape = {4, 1, 1};
 
 namespace {
 
@@ -48,8 +76,84 @@ int fail(cudaError_t e) {
   return MIC_ERR_CUDA;
 }
 
+int ensure_tables(mic_ensemble *E) {
+  if (E->h_table[0]) return MIC_OK;
+  E->table_cap = mic_batch_table_bound(E->n);
+  for (int k = 0; k < 4; ++k) {
+    cudaError_t ce = cudaHostAlloc((void **)&E->h_table[k], E->table_cap, cudaHostAllocDefault);
+    if (ce == cudaSuccess) ce = cudaMalloc((void **)&E->d_table[k], E->table_cap);
+    if (ce != cudaSuccess) return fail(ce);
+  }
+  return MIC_OK;
+}
+
+cudaError_t join_members(mic_ensemble *E) {
+  cudaError_t ce = cudaSuccess;
+  for (int i = 0; i < E->n && ce == cudaSuccess; ++i) {
+    ce = cudaEventRecord(E->join[i], E->m[i]->stream);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(E->stream, E->join[i], 0);
+  }
+  return ce;
+}
+
+cudaError_t fork_members(mic_ensemble *E) {
+  cudaError_t ce = cudaEventRecord(E->fork, E->stream);
+  for (int i = 0; i < E->n && ce == cudaSuccess; ++i) ce = cudaStreamWaitEvent(E->m[i]->stream, E->fork, 0);
+  return ce;
+}
+
+// One step with batched marker passes; its work table goes to `slot` (a graph being captured,
+// or kSlotDirect: the next direct buffer, copied inside the step).
+int issue_batched(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub, int slot) {
+  int e = ensure_tables(E);
+  if (e) return e;
+  cudaError_t ce;
+  int ev = -1;
+  if (slot == kSlotDirect) {
+    ev = E->direct_next;
+    E->direct_next ^= 1;
+    slot = kSlotDirect + ev;
+    // the host buffer is rewritten below: the step that last copied out of it must be done
+    if (E->table_ev_live[ev] && (ce = cudaEventSynchronize(E->table_ev[ev])) != cudaSuccess) return fail(ce);
+  }
+  const bool copy = ev >= 0;
+  if ((ce = fork_members(E)) != cudaSuccess) return fail(ce);
+  size_t off = 0;
+  for (int seg = 0; seg < mic::kStepSegments && !e; ++seg) {
+    for (int k = 0; k < E->n && !e; ++k) {
+      const int i = E->order[k];
+      mic_ctx *c = E->m[i];
+#ifdef MIC_EXACT
+      const int wz_known = 0;
+#else
+      const int wz_known = c->n > 0;  // as mic_step
+#endif
+      const long long l0 = c->launches;
+      e = mic_step_segment(c, seg, dt_disp[i], dt_thermal[i], sub, wz_known, E->batch);
+      E->launches += c->launches - l0;
+    }
+    if (e || mic_batch_empty(E->batch)) continue;
+    if ((ce = join_members(E)) != cudaSuccess) {
+      e = fail(ce);
+      break;
+    }
+    e = mic_batch_launch(E->batch, E->shape, E->h_table[slot], E->d_table[slot], &off, E->table_cap, copy ? 1 : 0,
+                         E->stream, &E->launches);
+    if (!e && (ce = fork_members(E)) != cudaSuccess) e = fail(ce);
+  }
+  mic_batch_clear(E->batch);
+  E->table_used[slot] = off;
+  if ((ce = join_members(E)) != cudaSuccess && !e) e = fail(ce);
+  if (copy && !e) {
+    if ((ce = cudaEventRecord(E->table_ev[ev], E->stream)) != cudaSuccess) return fail(ce);
+    E->table_ev_live[ev] = 1;
+  }
+  return e;
+}
+
 // fork, every member's step, join: all asynchronous on the ensemble stream's timeline
-int issue(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub) {
+int issue(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub, int slot = kSlotDirect) {
+  if (E->batched) return issue_batched(E, dt_disp, dt_thermal, sub, slot);
   cudaError_t ce = cudaEventRecord(E->fork, E->stream);
   if (ce != cudaSuccess) return fail(ce);
   for (int k = 0; k < E->n; ++k) {
@@ -115,7 +219,7 @@ int capture(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, in
     cudaError_t ce = cudaStreamBeginCapture(E->stream, cudaStreamCaptureModeRelaxed);
     if (ce != cudaSuccess) return fail(ce);
     const long long l0 = E->launches;
-    int e = issue(E, dt_disp, dt_thermal, sub);
+    int e = issue(E, dt_disp, dt_thermal, sub, q);
     cudaGraph_t g = nullptr;
     ce = cudaStreamEndCapture(E->stream, &g);
     for (int i = 0; i < E->n; ++i) E->m[i]->prof_on = prof[i];
@@ -130,6 +234,14 @@ int capture(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, in
     ce = cudaGraphInstantiate(&E->exec[q], g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) {
+      if (q == 1) cudaGraphExecDestroy(E->exec[0]);
+      return fail(ce);
+    }
+    // the graph's batched kernels read the work table written while it was captured: copy it
+    // into the graph's own device buffer now (nothing in flight reads that buffer)
+    if (E->batched && E->table_used[q] > 0 &&
+        (ce = cudaMemcpy(E->d_table[q], E->h_table[q], E->table_used[q], cudaMemcpyHostToDevice)) != cudaSuccess) {
+      cudaGraphExecDestroy(E->exec[q]);
       if (q == 1) cudaGraphExecDestroy(E->exec[0]);
       return fail(ce);
     }
@@ -165,13 +277,18 @@ extern "C" int mic_ensemble_create(mic_ensemble **out, mic_ctx *const *members, 
   E->join.assign(n_members, nullptr);
   E->order.resize(n_members);
   for (int i = 0; i < n_members; ++i) E->order[i] = i;
+  E->batched = 1;
+  for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = kDefaultShape;
+  E->batch = mic_batch_new();
   cudaSetDevice(E->device);
-  bool ok = cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) == cudaSuccess &&
-            cudaEventCreateWithFlags(&E->fork, cudaEventDisableTiming) == cudaSuccess;
+  bool ok = E->batch && cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&E->fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&E->table_ev[0], cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&E->table_ev[1], cudaEventDisableTiming) == cudaSuccess;
   for (int i = 0; ok && i < n_members; ++i)
     ok = cudaEventCreateWithFlags(&E->join[i], cudaEventDisableTiming) == cudaSuccess;
   if (!ok) {
-    delete E;
+    mic_ensemble_destroy(E);
     return MIC_ERR_CUDA;
   }
   *out = E;
@@ -181,12 +298,19 @@ extern "C" int mic_ensemble_create(mic_ensemble **out, mic_ctx *const *members, 
 extern "C" int mic_ensemble_destroy(mic_ensemble *E) {
   if (!E) return MIC_ERR_ARG;
   cudaSetDevice(E->device);
-  cudaStreamSynchronize(E->stream);
+  if (E->stream) cudaStreamSynchronize(E->stream);
   drop_graphs(E);
   for (auto ev : E->join)
     if (ev) cudaEventDestroy(ev);
-  cudaEventDestroy(E->fork);
-  cudaStreamDestroy(E->stream);
+  if (E->fork) cudaEventDestroy(E->fork);
+  for (int k = 0; k < 2; ++k)
+    if (E->table_ev[k]) cudaEventDestroy(E->table_ev[k]);
+  for (int k = 0; k < 4; ++k) {
+    if (E->h_table[k]) cudaFreeHost(E->h_table[k]);
+    if (E->d_table[k]) cudaFree(E->d_table[k]);
+  }
+  if (E->stream) cudaStreamDestroy(E->stream);
+  mic_batch_free(E->batch);
   delete E;
   return MIC_OK;
 }
@@ -247,6 +371,30 @@ extern "C" int mic_ensemble_get_stream(mic_ensemble *E, void **stream) {
   return MIC_OK;
 }
 
+// How a step runs its marker passes: batched (1: one kernel per pass over all members; 0: each
+// member's own kernels on its stream), and for the batched kernels the tile size in blocks'
+// worth of markers, persistent grid or one block per tile, and contiguous runs of tiles per
+// block or round-robin.  The surrogate passes always walk contiguous runs on a persistent grid
+// (a block restages the network when its member changes).
+extern "C" int mic_ensemble_set_schedule(mic_ensemble *E, int batched, int tile_mult, int persistent, int chunked) {
+  if (!E || tile_mult < 1 || tile_mult > 64) return MIC_ERR_ARG;
+  cudaSetDevice(E->device);
+  drop_graphs(E);
+  E->batched = batched ? 1 : 0;
+  for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = {tile_mult, persistent ? 1 : 0, chunked ? 1 : 0};
+  return MIC_OK;
+}
+
+extern "C" int mic_ensemble_get_schedule(mic_ensemble *E, int *batched, int *tile_mult, int *persistent,
+                                         int *chunked) {
+  if (!E) return MIC_ERR_ARG;
+  if (batched) *batched = E->batched;
+  if (tile_mult) *tile_mult = E->shape[0].mult;
+  if (persistent) *persistent = E->shape[0].persistent;
+  if (chunked) *chunked = E->shape[0].chunked;
+  return MIC_OK;
+}
+
 // Launch shapes and the member schedule, measured on the ensemble's own members: each member's
 // kernels get their block sizes from mic_autotune (member by member), then the order in which
 // the members' steps are issued into the step (and its captured graphs) is chosen among: as
@@ -263,19 +411,37 @@ extern "C" int mic_ensemble_autotune(mic_ensemble *E, const double *dt_disp, con
   if (e) return e;
   std::vector<void *> saved(E->n, nullptr);
   for (int i = 0; i < E->n && !e; ++i) e = mic_state_save(E->m[i], &saved[i]);
-  std::vector<std::vector<int>> cand(3, E->order);
-  for (int i = 0; i < E->n; ++i) cand[0][i] = i;
-  cand[1] = cand[0];
-  std::stable_sort(cand[1].begin(), cand[1].end(), [&](int a, int b) { return E->m[a]->n > E->m[b]->n; });
-  cand[2] = cand[0];
-  std::stable_sort(cand[2].begin(), cand[2].end(), [&](int a, int b) { return E->m[a]->n < E->m[b]->n; });
+  std::vector<int> given(E->n), big(E->n), small(E->n);
+  for (int i = 0; i < E->n; ++i) given[i] = i;
+  big = given;
+  std::stable_sort(big.begin(), big.end(), [&](int a, int b) { return E->m[a]->n > E->m[b]->n; });
+  small = given;
+  std::stable_sort(small.begin(), small.end(), [&](int a, int b) { return E->m[a]->n < E->m[b]->n; });
+  struct Cand {
+    std::vector<int> order;
+    int batched;
+    mic::BatchShape shape;
+  };
+  // per-member steps in three issue orders, then batched passes over the table in two member
+  // orders and four walks (one block per tile; persistent round-robin; persistent contiguous
+  // runs of two tile sizes)
+  std::vector<Cand> cand;
+  for (const auto *o : {&given, &big, &small}) cand.push_back({*o, 0, kDefaultShape});
+  const mic::BatchShape walks[4] = {{1, 0, 0}, {4, 1, 0}, {4, 1, 1}, {16, 1, 1}};
+  for (const auto *o : {&given, &big})
+    for (const auto &w : walks) cand.push_back({*o, 1, w});
   const std::vector<int> before = E->order;
+  const int batched_before = E->batched;
+  mic::BatchShape shape_before[mic::BP_COUNT];
+  for (int p = 0; p < mic::BP_COUNT; ++p) shape_before[p] = E->shape[p];
   int best = -1;
   float best_ms = 0.f;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   if (!e && (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)) e = MIC_ERR_CUDA;
   for (int c = 0; c < (int)cand.size() && !e; ++c) {
-    E->order = cand[c];
+    E->order = cand[c].order;
+    E->batched = cand[c].batched;
+    for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = cand[c].shape;
     drop_graphs(E);
     for (int i = 0; i < E->n && !e; ++i) e = mic_state_restore(E->m[i], saved[i]);
     if (e) break;
@@ -298,7 +464,15 @@ extern "C" int mic_ensemble_autotune(mic_ensemble *E, const double *dt_disp, con
   if (t0) cudaEventDestroy(t0);
   if (t1) cudaEventDestroy(t1);
   drop_graphs(E);
-  E->order = (!e && best >= 0) ? cand[best] : before;
+  if (!e && best >= 0) {
+    E->order = cand[best].order;
+    E->batched = cand[best].batched;
+    for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = cand[best].shape;
+  } else {
+    E->order = before;
+    E->batched = batched_before;
+    for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = shape_before[p];
+  }
   int e2 = MIC_OK;
   for (int i = 0; i < E->n; ++i) {
     if (saved[i] && !e2) e2 = mic_state_restore(E->m[i], saved[i]);

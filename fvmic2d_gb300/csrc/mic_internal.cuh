@@ -158,6 +158,7 @@ struct mic_ctx {
   double *scr0, *scr1, *scr2;
   double *node_scr[6];  // nodal scratch (NX*NY each)
   void *adv_coef;       // per-cell bilinear coefficients of vx, vy, wxy for the advection (product build)
+  void *job_slots;      // one-job tables of the marker passes, one slot per pass (mic_job_slots_bytes)
   double *red_buf;     // reduction partials
   int red_cap;
   mic::Status *d_status;
@@ -231,6 +232,57 @@ int mic_mlp_infer_tc_launch(mic_ctx *ctx, const float *feat, int64_t n, float *y
 // tensor-core creep surrogate over a device batch (mic_creep_tc.cu)
 int mic_creep_surrogate_tc_launch(mic_ctx *ctx, const double *edot, const double *T, const double *d,
                                   const double *P, int64_t n, double *s, int *it, double *res, int *fb);
+
+// ---- one step in segments, and marker passes batched over many contexts (mic_marker_passes.cu)
+
+namespace mic {
+// The marker passes of a step a batch gathers: one batched kernel each.  The yield pass has one
+// per creep variant (no law-7 material, exact solve, FP32 surrogate, tensor-core surrogate).
+enum BatchPass {
+  BP_RHO = 0,
+  BP_YIELD_PLAIN,
+  BP_YIELD_EXACT,
+  BP_YIELD_FP32,
+  BP_YIELD_TC,
+  BP_STRAIN,
+  BP_SUBGRID,
+  BP_STRESS,
+  BP_SUBT,
+  BP_SUBT_APPLY,
+  BP_ADVECT,
+  BP_COUNT
+};
+// How a batched kernel walks its work table: tiles of `mult` x block-size markers, each inside
+// one member; one block per tile, or a persistent grid (SMs x resident blocks) whose blocks take
+// tiles round-robin or as one contiguous run each (chunked).
+struct BatchShape {
+  int mult, persistent, chunked;
+};
+constexpr int kStepSegments = 10;
+}  // namespace mic
+
+struct mic_batch;  // the marker-pass jobs of one segment, gathered over the members
+mic_batch *mic_batch_new();
+void mic_batch_free(mic_batch *b);
+bool mic_batch_empty(const mic_batch *b);
+void mic_batch_clear(mic_batch *b);
+// bytes of work table one ensemble step of n_members contexts needs at most
+size_t mic_batch_table_bound(int n_members);
+// bytes of a context's one-job tables (mic_ctx::job_slots)
+size_t mic_job_slots_bytes();
+// Segment seg (0 .. kStepSegments-1) of one step: the context's own launches up to and including
+// one marker pass, on its stream.  Segments 0 .. kStepSegments-1 in order are mic_step without its
+// residual read.  With b, the segment's marker pass joins the batch instead of being launched.
+// wz_known: the advection may take the marker vorticity of this step's strain-rate pass.
+int mic_step_segment(mic_ctx *ctx, int seg, double dt_disp, double dt_thermal, int subgrid_stress, int wz_known,
+                     mic_batch *b);
+// Launch every pass the batch holds on stream s, each as one kernel over its jobs (in the order
+// they were added) with its shape; the jobs and the tile table are written into host_table at
+// *off (advanced; cap bytes in all) and read by the kernels from the same offset of dev_table.
+// copy: enqueue the host-to-device copy of the written bytes on s first (else the caller copies
+// the table before the launches run).  *launches counts the kernels.  Empties the batch.
+int mic_batch_launch(mic_batch *b, const mic::BatchShape *shape, unsigned char *host_table, unsigned char *dev_table,
+                     size_t *off, size_t cap, int copy, cudaStream_t s, long long *launches);
 
 namespace mic {
 

@@ -8,6 +8,8 @@
 // transcendental (exp, sin, cos, tan) differs from the host libm in the last place.
 #include <cmath>
 #include <cstring>
+#include <new>
+#include <vector>
 
 #include "mic_creep.cuh"
 #include "mic_creep_tc.cuh"
@@ -22,14 +24,6 @@ namespace {
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 #ifndef MIC_EXACT  // product-build helpers
-// Bilinear value of corners (00, 10, 01, 11) at fractions (tx, ty) in lerp form: three
-// subtractions and three FMAs.
-__device__ __forceinline__ double lerp2(double f00, double f10, double f01, double f11, double tx, double ty) {
-  const double a = fma(tx, f10 - f00, f00);
-  const double b = fma(tx, f11 - f01, f01);
-  return fma(ty, b - a, a);
-}
-
 // cos, sin, sin 2t, cos 2t of the rotation angle t of markers.c:2158-2164.  Per-step rotations
 // are small: for |t| <= 2^-6 truncated Taylor series (to t^7 / t^8, remainder below 2^-60
 // relative) and the double-angle identities replace four transcendental calls; larger angles
@@ -181,19 +175,16 @@ __device__ __forceinline__ bool creep_marker_features(const YieldCols &c, const 
   return true;
 }
 
-// checkPlasticYielding, one thread per marker.  MODE 0: exact creep solve; MODE 1: surrogate
-// guess on the CUDA cores (FP32), polish and fallback; MODE 2: no material uses law 7.
-// limit: limitViscosity fused in (every marker, out-of-domain ones included, viscosity.c:93-95)
+// One marker of checkPlasticYielding (the solo kernels and their batched forms share it).
+// MODE 0: exact creep solve; MODE 1: surrogate guess on the CUDA cores (FP32, w2s: the hidden
+// layer's weights in shared memory), polish and fallback; MODE 2: no material uses law 7.
+// limit: limitViscosity fused in (every marker, out-of-domain ones included, viscosity.c:93-95).
+// Every thread of a warp calls it (the creep counters reduce over the warp).
 template <int MODE>
-__global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig cfg, double dt, int64_t n,
-                        Status *st, CreepCounters *cc, int limit) {
-  __shared__ int s_yield;
-  __shared__ float w2s[MODE == 1 ? kH * kH : 1];
-  if (threadIdx.x == 0) s_yield = 0;
-  if (MODE == 1)
-    for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = cfg.mlp[kOffW2 + q];
-  __syncthreads();
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ bool yield_one(const YieldCols &c, const mic_materials &M, const mic_options &O,
+                                          const CreepConfig &cfg, double dt, int64_t n, Status *st,
+                                          CreepCounters *cc, int limit, const float *w2s, int64_t m) {
+  bool yielded = false;
   int creep_active = 0;
   CreepIn ci = {};
   if (m < n && c.cellX[m] != -1) {
@@ -202,46 +193,35 @@ __global__ void k_yield(YieldCols c, mic_materials M, mic_options O, CreepConfig
     CreepCoef k;
     const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, edot, f, &mref);
     if (law7) lx = creep_guess_lx(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
-    if (yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, st, ci, creep_active, limit))
-      s_yield = 1;
+    yielded = yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, st, ci, creep_active, limit);
   } else if (limit && m < n) {
     c.eta[m] = limit_eta(c.eta[m], O);
   }
   if (MODE != 2) creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
-  __syncthreads();
-  if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
+  return yielded;
 }
 
-// checkPlasticYielding with the surrogate's hidden layer on the tensor cores: persistent
-// blocks of 128 threads, one 128-marker tile per round (mic_creep_tc.cuh).
-__global__ void __launch_bounds__(tc::kTile) k_yield_tc(YieldCols c, mic_materials M, mic_options O,
-                                                        CreepConfig cfg, double dt, int64_t n, Status *st,
-                                                        CreepCounters *cc, int limit) {
-  extern __shared__ unsigned char dyn[];
-  __shared__ int s_yield;
-  if (threadIdx.x == 0) s_yield = 0;
-  tc::Block B;
-  tc::setup(B, dyn, cfg.mlp);
-  const int64_t ntiles = (n + tc::kTile - 1) / tc::kTile;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t m = tile * tc::kTile + threadIdx.x;
-    const bool live = m < n && c.cellX[m] != -1;
-    float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
-    double edot = 0.0;
-    CreepCoef k;
-    const bool law7 = live && creep_marker_features(c, M, m, k, edot, f, &mref);
-    const float y = tc::guess(B, f, cfg.tc_wait_limit, &cc->tc_timeouts);
-    int creep_active = 0;
-    CreepIn ci = {};
-    if (live && yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 ? &k : nullptr, edot, st,
-                             ci, creep_active, limit))
-      s_yield = 1;
-    if (limit && !live && m < n) c.eta[m] = limit_eta(c.eta[m], O);
-    creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
-  }
-  tc::teardown(B, &cc->tc_drain_timeouts);
-  __syncthreads();
-  if (threadIdx.x == 0 && s_yield) atomicOr(&st->is_yielding, 1);
+// One 128-marker round of checkPlasticYielding with the surrogate's hidden layer on the tensor
+// cores (all kTile threads of the block, block-uniform; thread t takes marker m0 + t).  Returns
+// whether this thread's marker yielded.
+__device__ __forceinline__ bool yield_tc_round(tc::Block &B, const YieldCols &c, const mic_materials &M,
+                                               const mic_options &O, const CreepConfig &cfg, double dt, int64_t n,
+                                               Status *st, CreepCounters *cc, int limit, int64_t m) {
+  const bool live = m < n && c.cellX[m] != -1;
+  float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
+  double edot = 0.0;
+  CreepCoef k;
+  const bool law7 = live && creep_marker_features(c, M, m, k, edot, f, &mref);
+  const float y = tc::guess(B, f, cfg.tc_wait_limit, &cc->tc_timeouts);
+  int creep_active = 0;
+  CreepIn ci = {};
+  bool yielded = false;
+  if (live)
+    yielded = yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 ? &k : nullptr, edot, st, ci,
+                           creep_active, limit);
+  if (limit && !live && m < n) c.eta[m] = limit_eta(c.eta[m], O);
+  creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
+  return yielded;
 }
 
 // updateViscosity (viscosity.c:77-88): rheology from the current marker stress
@@ -275,30 +255,34 @@ __global__ void k_limit_viscosity(double *eta, double etamin, double etamax, int
 // density update inline in main_subduction.c:255-264
 // MAXT: also the maximum marker temperature of main:271-281 (in-domain markers, from 0; the bit
 // patterns of non-negative doubles order as the values), one atomic per block into *maxT
-template <bool MAXT>
-__global__ void k_update_rho(const int *cellX, const int *mat, const double *T, double *rho, double *rhodot,
-                             mic_materials M, int64_t n, unsigned long long *maxT) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// one marker; returns the bits of its temperature when it is in the domain and above 0, else 0
+__device__ __forceinline__ long long update_rho_one(const int *cellX, const int *mat, const double *T, double *rho,
+                                                    double *rhodot, const mic_materials &M, int64_t n, int64_t m) {
   long long b = 0;  // bits of 0.0
   if (m < n && cellX[m] != -1) {
     const int k = mat[m];
     const double t = T[m];
     rho[m] = -M.materialRho[k] * (M.materialAlpha[k] * t);
     rhodot[m] = 0.0;
-    if (MAXT && t > 0.0) b = __double_as_longlong(t);
+    if (t > 0.0) b = __double_as_longlong(t);
   }
-  if (MAXT) {
-    __shared__ long long wmax[32];
+  return b;
+}
+
+// block maximum of non-negative double bit patterns, one atomic into *dst when above 0 (every
+// thread of the block calls it; it may be called again right after)
+__device__ __forceinline__ void block_max_to(long long b, unsigned long long *dst) {
+  __shared__ long long wmax[32];
+  for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) wmax[warp] = b;
+  __syncthreads();
+  if (warp == 0) {
+    b = lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0;
     for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) wmax[warp] = b;
-    __syncthreads();
-    if (warp == 0) {
-      b = lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0;
-      for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
-      if (lane == 0 && b > 0) atomicMax(maxT, (unsigned long long)b);
-    }
+    if (lane == 0 && b > 0) atomicMax(dst, (unsigned long long)b);
   }
+  __syncthreads();
 }
 
 struct Geo {
@@ -336,8 +320,8 @@ struct StrainCols {
 };
 
 // updateMarkerStrainPressure (updateMarkerStrainPressure.c:131-306, non-TEXTURE branch)
-__global__ void k_strain_pressure(Params P, StrainCols c, Geo g, Nodal nd, double dt, int64_t n, Status *st) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// one marker (the marker-pass kernel k_batched runs it over a table of jobs)
+__device__ __forceinline__ void strain_pressure_one(Params P, StrainCols c, Geo g, Nodal nd, double dt, int64_t n, Status *st, int64_t m) {
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
@@ -457,10 +441,10 @@ struct SubgridCols {
 
 // subgridStressChanges, marker part (subgridStressChanges.c:79-221)
 // reuse (product build): dxx, dyy, dxy hold the nodal soxx, soyy, soxy interpolated at the
-// marker by k_strain_pressure of this step (same nodes, weights and order: the same values)
-__global__ void k_subgrid_stress_markers(Params P, SubgridCols c, Geo g, Nodal nd, double dt, double D,
-                                         int64_t n, int reuse) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// marker by the strain-rate pass of this step (same nodes, weights and order: the same values)
+// one marker (the marker-pass kernel k_batched runs it over a table of jobs)
+__device__ __forceinline__ void subgrid_stress_one(Params P, SubgridCols c, Geo g, Nodal nd, double dt, double D,
+                                         int64_t n, int reuse, int64_t m) {
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
@@ -673,8 +657,8 @@ struct StressCols {
 };
 
 // updateMarkerStress (updateMarkerStress.c:60-144)
-__global__ void k_update_marker_stress(Params P, StressCols c, Geo g, Nodal nd, int64_t n, Status *st) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// one marker (the marker-pass kernel k_batched runs it over a table of jobs)
+__device__ __forceinline__ void update_stress_one(Params P, StressCols c, Geo g, Nodal nd, int64_t n, Status *st, int64_t m) {
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
@@ -707,10 +691,10 @@ struct SubTCols {
 };
 
 // subgridTemperatureChanges, first marker loop (subgridTemperatureChanges.c:45-70)
-__global__ void k_subgridT_markers(Params P, SubTCols c, Geo g, const double *__restrict__ Tn,
+// one marker (the marker-pass kernel k_batched runs it over a table of jobs)
+__device__ __forceinline__ void subgridT_markers_one(Params P, SubTCols c, Geo g, const double *__restrict__ Tn,
                                    const double *__restrict__ rn, const double *__restrict__ cpn,
-                                   const double *__restrict__ kn, double rho0, double D, double dt, int64_t n) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+                                   const double *__restrict__ kn, double rho0, double D, double dt, int64_t n, int64_t m) {
   if (m >= n) return;
   const int i = c.cellX[m], j = c.cellY[m];
   if (i == -1) return;
@@ -756,8 +740,8 @@ __global__ void k_subgridT_nodes(const double *thisT, const double *lastT, const
 }
 
 // subgridTemperatureChanges, second marker loop (subgridTemperatureChanges.c:87-103)
-__global__ void k_subgridT_apply(Params P, SubTCols c, Geo g, const double *__restrict__ dT, double dt, int64_t n) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// one marker (the marker-pass kernel k_batched runs it over a table of jobs)
+__device__ __forceinline__ void subgridT_apply_one(Params P, SubTCols c, Geo g, const double *__restrict__ dT, double dt, int64_t n, int64_t m) {
   if (m >= n) return;
   const int i = c.cellX[m], j = c.cellY[m];
   if (i == -1) return;
@@ -776,7 +760,7 @@ __global__ void k_subgridT_apply(Params P, SubTCols c, Geo g, const double *__re
 
 #ifndef MIC_EXACT
 // A nodal field's bilinear form on one cell in coefficient form, v = c0 + tx c1 + ty (c2 + tx c3)
-// (corners 00, 10, 01, 11 as in lerp2): three FMAs per evaluation instead of three subtractions
+// (corners 00, 10, 01, 11): three FMAs per evaluation instead of three subtractions
 // and three FMAs.  The advection evaluates eleven of these per marker on three fields; forming
 // the coefficients once per cell and step (a node kernel) moves the subtractions off the marker
 // loop.  32-byte records: one cell's form is one aligned sector.
@@ -1028,34 +1012,21 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
   return nsxx;
 }
 
-// MAXS: also max |sxx| over the in-domain markers after the rotation (main_subduction.c:437-448,
-// from 0, bit patterns of non-negative doubles), one atomic per block into *maxs
-template <bool MAXS>
-__global__ void __launch_bounds__(512, 2) k_advect(Params P, AdvectCols c, Geo g, const double *__restrict__ vx,
-                                                   const double *__restrict__ vy, const double *__restrict__ wz,
-                                                   AdvectCoef cv, mic_bcinfo top, mic_bcinfo left, double dt,
-                                                   int64_t n, int wz_known, unsigned long long *maxs) {
-  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// one marker; returns the bits of |sxx| after the rotation for an in-domain marker, else 0
+__device__ __forceinline__ long long advect_one(const Params &P, const AdvectCols &c, const Geo &g,
+                                                const double *__restrict__ vx, const double *__restrict__ vy,
+                                                const double *__restrict__ wz, const AdvectCoef &cv,
+                                                const mic_bcinfo &top, const mic_bcinfo &left, double dt, int64_t n,
+                                                int wz_known, int64_t m) {
   long long b = 0;  // bits of 0.0
   if (m < n) {
     const int ci = c.cellX[m], cj = c.cellY[m];
     if (ci != -1) {
       const double a = fabs(advect_marker(P, c, g, vx, vy, wz, cv, top, left, dt, m, ci, cj, wz_known));
-      if (MAXS && a > 0.0) b = __double_as_longlong(a);
+      if (a > 0.0) b = __double_as_longlong(a);
     }
   }
-  if (MAXS) {
-    __shared__ long long wmax[32];
-    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) wmax[warp] = b;
-    __syncthreads();
-    if (warp == 0) {
-      b = lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0;
-      for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
-      if (lane == 0 && b > 0) atomicMax(maxs, (unsigned long long)b);
-    }
-  }
+  return b;
 }
 
 // max over in-domain markers of v (or |v|), starting from 0 (main_subduction.c:271-281, 437-448)
@@ -1165,32 +1136,452 @@ int run_max(mic_ctx *ctx, int col, int absval, double *out) {
   return MIC_OK;
 }
 
+// ---- marker-pass kernels over tables of jobs ---------------------------------------------
+//
+// A job is one context's launch of a marker pass (its columns, grid, settings).  Every marker
+// pass runs as one kernel over a table of jobs: a single job when a context steps alone, every
+// member's when an ensemble batches the pass.  Both launch the same kernel, so a member's markers
+// go through the same machine code either way and come out bit for bit the same (the product
+// build lets the compiler fuse multiplies and adds, and it may fuse the same source differently
+// in two different kernels).  Each job's markers are cut into tiles of a fixed number of markers
+// (a multiple of the block size); tile_start[j] is the first tile of job j (prefix sums, njobs + 1
+// entries), so the table orders the tiles job-major in the order the jobs were added.  A block
+// finds its tile's job by a binary search over tile_start, stages the job in shared memory and
+// runs the per-marker code on the tile's markers; per-job reductions (flags, maxima) close at the
+// end of each tile, since a tile never spans two jobs.
+
+struct RhoJob {
+  const int *cellX, *mat;
+  const double *T;
+  double *rho, *rhodot;
+  mic_materials M;
+  int64_t n;
+  unsigned long long *maxT;  // null: no maximum
+};
+struct YieldJob {
+  YieldCols c;
+  mic_materials M;
+  mic_options O;
+  CreepConfig cfg;
+  double dt;
+  int64_t n;
+  Status *st;
+  CreepCounters *cc;
+  int limit;
+};
+struct StrainJob {
+  Params P;
+  StrainCols c;
+  Geo g;
+  Nodal nd;
+  double dt;
+  int64_t n;
+  Status *st;
+};
+struct SubgridJob {
+  Params P;
+  SubgridCols c;
+  Geo g;
+  Nodal nd;
+  double dt, D;
+  int64_t n;
+  int reuse;
+};
+struct StressJob {
+  Params P;
+  StressCols c;
+  Geo g;
+  Nodal nd;
+  int64_t n;
+  Status *st;
+};
+struct SubTJob {
+  Params P;
+  SubTCols c;
+  Geo g;
+  const double *Tn, *rn, *cpn, *kn;
+  double rho0, D, dt;
+  int64_t n;
+};
+struct SubTApplyJob {
+  Params P;
+  SubTCols c;
+  Geo g;
+  const double *dT;
+  double dt;
+  int64_t n;
+};
+struct AdvectJob {
+  Params P;
+  AdvectCols c;
+  Geo g;
+  const double *vx, *vy, *wz;
+  AdvectCoef cv;
+  mic_bcinfo top, left;
+  double dt;
+  int64_t n;
+  int wz_known;
+  unsigned long long *maxs;  // null: no maximum
+};
+
+constexpr int kBatchBlock = 256;  // threads per block of ensemble-batched passes (tensor-core yield: tc::kTile)
+
+// the job of tile t: the last j with tile_start[j] <= t
+__device__ __forceinline__ int tile_job(const int *__restrict__ ts, int njobs, int t) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(ts + mid) <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// this block's tiles: [t, end) with stride step
+struct TileRange {
+  int t, end, step;
+};
+__device__ __forceinline__ TileRange tile_range(int ntiles, int chunked) {
+  TileRange r;
+  if (chunked) {
+    r.t = (int)((long long)blockIdx.x * ntiles / gridDim.x);
+    r.end = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
+    r.step = 1;
+  } else {
+    r.t = blockIdx.x;
+    r.end = ntiles;
+    r.step = gridDim.x;
+  }
+  return r;
+}
+
+// Per-pass operations of the generic batched kernel: Acc is a thread's per-tile partial result,
+// one() a marker, flush() closes a tile (every thread of the block calls it).
+struct NoAcc {};
+struct RhoOp {
+  static constexpr int kMaxRegs = 64;
+  using Job = RhoJob;
+  using Acc = long long;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &a) {
+    a = max(a, update_rho_one(J.cellX, J.mat, J.T, J.rho, J.rhodot, J.M, J.n, m));
+  }
+  static __device__ __forceinline__ void flush(const Job &J, Acc a) {
+    if (J.maxT) block_max_to(a, J.maxT);
+  }
+};
+template <int MODE>
+struct YieldOp {
+  static constexpr int kMaxRegs = 80;
+  using Job = YieldJob;
+  using Acc = int;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &a) {
+    if (yield_one<MODE>(J.c, J.M, J.O, J.cfg, J.dt, J.n, J.st, J.cc, J.limit, nullptr, m)) a = 1;
+  }
+  static __device__ __forceinline__ void flush(const Job &J, Acc a) {
+    if (__syncthreads_or(a) && threadIdx.x == 0) atomicOr(&J.st->is_yielding, 1);
+  }
+};
+struct StrainOp {
+  static constexpr int kMaxRegs = 80;
+  using Job = StrainJob;
+  using Acc = NoAcc;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
+    strain_pressure_one(J.P, J.c, J.g, J.nd, J.dt, J.n, J.st, m);
+  }
+  static __device__ __forceinline__ void flush(const Job &, Acc) {}
+};
+struct SubgridOp {
+  static constexpr int kMaxRegs = 80;
+  using Job = SubgridJob;
+  using Acc = NoAcc;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
+    subgrid_stress_one(J.P, J.c, J.g, J.nd, J.dt, J.D, J.n, J.reuse, m);
+  }
+  static __device__ __forceinline__ void flush(const Job &, Acc) {}
+};
+struct StressOp {
+  static constexpr int kMaxRegs = 64;
+  using Job = StressJob;
+  using Acc = NoAcc;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
+    update_stress_one(J.P, J.c, J.g, J.nd, J.n, J.st, m);
+  }
+  static __device__ __forceinline__ void flush(const Job &, Acc) {}
+};
+struct SubTOp {
+  static constexpr int kMaxRegs = 64;
+  using Job = SubTJob;
+  using Acc = NoAcc;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
+    subgridT_markers_one(J.P, J.c, J.g, J.Tn, J.rn, J.cpn, J.kn, J.rho0, J.D, J.dt, J.n, m);
+  }
+  static __device__ __forceinline__ void flush(const Job &, Acc) {}
+};
+struct SubTApplyOp {
+  static constexpr int kMaxRegs = 64;
+  using Job = SubTApplyJob;
+  using Acc = NoAcc;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
+    subgridT_apply_one(J.P, J.c, J.g, J.dT, J.dt, J.n, m);
+  }
+  static __device__ __forceinline__ void flush(const Job &, Acc) {}
+};
+struct AdvectOp {
+  static constexpr int kMaxRegs = 64;
+  using Job = AdvectJob;
+  using Acc = long long;
+  static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &a) {
+    a = max(a, advect_one(J.P, J.c, J.g, J.vx, J.vy, J.wz, J.cv, J.top, J.left, J.dt, J.n, J.wz_known, m));
+  }
+  static __device__ __forceinline__ void flush(const Job &J, Acc a) {
+    if (J.maxs) block_max_to(a, J.maxs);
+  }
+};
+
+// One marker pass over every job of a table (tile_markers a multiple of blockDim.x, so every
+// warp stays whole through the per-marker code and the tile's closing reduction).
+// Op::kMaxRegs caps the registers (the job's fields otherwise stay in registers across the tile
+// loop and halve the resident warps of the memory-bound passes); blocks of up to 512 threads.
+template <class Op>
+__global__ void __maxnreg__(Op::kMaxRegs) k_batched(const typename Op::Job *__restrict__ jobs,
+                                                         const int *__restrict__ ts, int njobs, int ntiles,
+                                                         int tile_markers, int chunked) {
+  using Job = typename Op::Job;
+  static_assert(sizeof(Job) % 8 == 0, "job records are whole 8-byte words");
+  __shared__ unsigned long long sj[sizeof(Job) / 8];
+  const Job &J = *reinterpret_cast<const Job *>(sj);
+  const TileRange r = tile_range(ntiles, chunked);
+  int cur = -1;
+  for (int t = r.t; t < r.end; t += r.step) {
+    const int j = tile_job(ts, njobs, t);
+    if (j != cur) {  // the tile's job into shared memory (block-uniform)
+      __syncthreads();
+      const unsigned long long *src = reinterpret_cast<const unsigned long long *>(jobs + j);
+      for (int w = threadIdx.x; w < (int)(sizeof(Job) / 8); w += blockDim.x) sj[w] = __ldg(src + w);
+      __syncthreads();
+      cur = j;
+    }
+    const int64_t base = (int64_t)(t - __ldg(ts + j)) * tile_markers;
+    typename Op::Acc a{};
+    for (int q = threadIdx.x; q < tile_markers; q += blockDim.x) Op::one(J, base + q, a);
+    Op::flush(J, a);
+  }
+}
+
+// checkPlasticYielding with the FP32 surrogate over a table: the hidden layer's weights are
+// staged in shared memory again whenever a tile's member uses another network buffer.
+__global__ void __launch_bounds__(512) k_yield_fp32_batched(const YieldJob *__restrict__ jobs,
+                                                                    const int *__restrict__ ts, int njobs,
+                                                                    int ntiles, int tile_markers, int chunked) {
+  __shared__ float w2s[kH * kH];
+  const float *staged = nullptr;
+  const TileRange r = tile_range(ntiles, chunked);
+  for (int t = r.t; t < r.end; t += r.step) {
+    const int j = tile_job(ts, njobs, t);
+    const YieldJob &J = jobs[j];
+    if (J.cfg.mlp != staged) {
+      staged = J.cfg.mlp;
+      __syncthreads();
+      for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = staged[kOffW2 + q];
+      __syncthreads();
+    }
+    const int64_t base = (int64_t)(t - __ldg(ts + j)) * tile_markers;
+    int a = 0;
+    for (int q = threadIdx.x; q < tile_markers; q += blockDim.x)
+      if (yield_one<1>(J.c, J.M, J.O, J.cfg, J.dt, J.n, J.st, J.cc, J.limit, w2s, base + q)) a = 1;
+    if (__syncthreads_or(a) && threadIdx.x == 0) atomicOr(&J.st->is_yielding, 1);
+  }
+}
+
+// checkPlasticYielding with the tensor-core surrogate over a table (blocks of tc::kTile threads,
+// tiles of multiples of tc::kTile markers).  The network is staged at the block's first tile
+// and again when a tile's member uses another network buffer.  A block that gives up on the
+// tensor path does so for the rest of its tiles (their markers take the exact solve); the drain
+// timeout, if any, is counted on the member whose round gave up.
+__global__ void __launch_bounds__(tc::kTile) k_yield_tc_batched(const YieldJob *__restrict__ jobs,
+                                                                const int *__restrict__ ts, int njobs, int ntiles,
+                                                                int tile_markers, int chunked) {
+  extern __shared__ unsigned char dyn[];
+  const TileRange r = tile_range(ntiles, chunked);
+  if (r.t >= r.end) return;  // block-uniform, before any TMEM is taken
+  tc::Block B;
+  const float *staged = jobs[tile_job(ts, njobs, r.t)].cfg.mlp;
+  tc::setup(B, dyn, staged);
+  CreepCounters *gave_up = nullptr;
+  for (int t = r.t; t < r.end; t += r.step) {
+    const int j = tile_job(ts, njobs, t);
+    const YieldJob &J = jobs[j];
+    if (J.cfg.mlp != staged) {
+      staged = J.cfg.mlp;
+      tc::restage(B, staged);
+    }
+    const int64_t base = (int64_t)(t - __ldg(ts + j)) * tile_markers;
+    int a = 0;
+    for (int q = 0; q < tile_markers; q += tc::kTile) {
+      const int pending = B.pending;
+      if (yield_tc_round(B, J.c, J.M, J.O, J.cfg, J.dt, J.n, J.st, J.cc, J.limit, base + q + threadIdx.x)) a = 1;
+      if (!pending && B.pending) gave_up = J.cc;
+    }
+    if (__syncthreads_or(a) && threadIdx.x == 0) atomicOr(&J.st->is_yielding, 1);
+  }
+  tc::teardown(B, gave_up ? &gave_up->tc_drain_timeouts : &jobs[0].cc->tc_drain_timeouts);
+}
+
+// a one-job table for a context stepping alone: the job (a kernel argument) and its tile offsets
+template <class Job>
+__global__ void k_put_job(const __grid_constant__ Job J, Job *dst, int *ts, int ntiles) {
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&J);
+  unsigned long long *d = reinterpret_cast<unsigned long long *>(dst);
+  for (int w = threadIdx.x; w < (int)(sizeof(Job) / 8); w += blockDim.x) d[w] = src[w];
+  if (threadIdx.x == 0) {
+    ts[0] = 0;
+    ts[1] = ntiles;
+  }
+}
+
+constexpr size_t kJobBytes[BP_COUNT] = {sizeof(RhoJob),    sizeof(YieldJob),  sizeof(YieldJob), sizeof(YieldJob),
+                                        sizeof(YieldJob),  sizeof(StrainJob), sizeof(SubgridJob), sizeof(StressJob),
+                                        sizeof(SubTJob),   sizeof(SubTApplyJob), sizeof(AdvectJob)};
+constexpr size_t max_job_bytes(int k = 0) {
+  return k == BP_COUNT ? 0 : (kJobBytes[k] > max_job_bytes(k + 1) ? kJobBytes[k] : max_job_bytes(k + 1));
+}
+// a context's one-job tables: per pass one slot, the job and then its two tile offsets
+constexpr size_t kJobSlotBytes = (max_job_bytes() + 16 + 255) / 256 * 256;
+constexpr size_t kTableAlign = 256;
+
+int batch_fail(cudaError_t e) { return mic_fail_cuda(nullptr, e); }
+
+// resident blocks per SM of pass p's kernel at `block` threads (cached per device and shape)
+int pass_occupancy(int dev, int pass, int block) {
+  static int cache[64][BP_COUNT][5];
+  const int bi = block / 128;
+  if (dev < 0 || dev >= 64 || bi < 1 || bi > 4 || block % 128) return 1;
+  int &c = cache[dev][pass][bi];
+  if (c > 0) return c;
+  int occ = 0;
+  cudaError_t e;
+  switch (pass) {
+    case BP_RHO: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<RhoOp>, block, 0); break;
+    case BP_YIELD_PLAIN: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<YieldOp<2>>, block, 0); break;
+    case BP_YIELD_EXACT: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<YieldOp<0>>, block, 0); break;
+    case BP_YIELD_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_yield_fp32_batched, block, 0); break;
+    case BP_YIELD_TC:
+      e = cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_yield_tc_batched, tc::kTile, tc::kDynSmem);
+      break;
+    case BP_STRAIN: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<StrainOp>, block, 0); break;
+    case BP_SUBGRID: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<SubgridOp>, block, 0); break;
+    case BP_STRESS: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<StressOp>, block, 0); break;
+    case BP_SUBT: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<SubTOp>, block, 0); break;
+    case BP_SUBT_APPLY: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<SubTApplyOp>, block, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<AdvectOp>, block, 0); break;
+  }
+  if (e != cudaSuccess || occ < 1) occ = 1;
+  c = occ;
+  return c;
+}
+
+template <class Op>
+void launch_generic(unsigned grid, int block, cudaStream_t s, const unsigned char *jobs, const int *ts, int nj,
+                    int ntiles, int tm, int chunked) {
+  k_batched<Op><<<grid, block, 0, s>>>(reinterpret_cast<const typename Op::Job *>(jobs), ts, nj, ntiles, tm, chunked);
+}
+
+// pass p's kernel over a job table in device memory (block: tc::kTile for the tensor-core yield)
+cudaError_t launch_pass(int pass, unsigned grid, int block, cudaStream_t s, const unsigned char *jobs, const int *ts,
+                        int nj, int ntiles, int tm, int chunked) {
+  switch (pass) {
+    case BP_RHO: launch_generic<RhoOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_YIELD_PLAIN: launch_generic<YieldOp<2>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_YIELD_EXACT: launch_generic<YieldOp<0>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_YIELD_FP32:
+      k_yield_fp32_batched<<<grid, block, 0, s>>>(reinterpret_cast<const YieldJob *>(jobs), ts, nj, ntiles, tm,
+                                                   chunked);
+      break;
+    case BP_YIELD_TC: {
+      const cudaError_t e =
+          cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem);
+      if (e != cudaSuccess) return e;
+      k_yield_tc_batched<<<grid, tc::kTile, tc::kDynSmem, s>>>(reinterpret_cast<const YieldJob *>(jobs), ts, nj,
+                                                                ntiles, tm, chunked);
+      break;
+    }
+    case BP_STRAIN: launch_generic<StrainOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_SUBGRID: launch_generic<SubgridOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_STRESS: launch_generic<StressOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_SUBT: launch_generic<SubTOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_SUBT_APPLY: launch_generic<SubTApplyOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    default: launch_generic<AdvectOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+  }
+  return cudaGetLastError();
+}
+
+// One context's marker pass: its job into the context's slot for the pass (a one-block kernel),
+// then the pass kernel over that one-job table -- tiles of one block, a persistent grid walking
+// them round-robin (the tensor-core yield: the context's persistent tensor-core grid).
+template <class Job>
+int solo_pass(mic_ctx *ctx, int pass, const Job &J, int block, const char *name) {
+  const bool tcp = pass == BP_YIELD_TC;
+  if (tcp) block = tc::kTile;
+  unsigned char *slot = static_cast<unsigned char *>(ctx->job_slots) + (size_t)pass * kJobSlotBytes;
+  int *ts = reinterpret_cast<int *>(slot + kJobSlotBytes - 16);
+  const int64_t nt = (J.n + block - 1) / block;
+  if (nt > 0x7fffffff) return MIC_ERR_ARG;
+  const int ntiles = (int)nt;
+  {
+    MIC_KERNEL(ctx, "k_put_job");
+    k_put_job<Job><<<1, 32, 0, ctx->stream>>>(J, reinterpret_cast<Job *>(slot), ts, ntiles);
+  }
+  MIC_CUDA_TRY(cudaGetLastError());
+  int64_t grid = ntiles;
+  if (tcp) {
+    grid = mic_creep_tc_blocks(ctx, J.n);
+  } else {
+    int sms = 0;
+    MIC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int64_t g = (int64_t)(sms > 0 ? sms : 1) * pass_occupancy(ctx->device, pass, block);
+    if (g < grid) grid = g;
+  }
+  if (grid < 1) grid = 1;
+  MIC_KERNEL(ctx, name);
+  MIC_CUDA_TRY(launch_pass(pass, (unsigned)grid, block, ctx->stream, slot, ts, 1, ntiles, block, 0));
+  return MIC_OK;
+}
+
 }  // namespace
 
 #define CHECK_CTX()                 \
   if (!ctx) return MIC_ERR_ARG;     \
   cudaSetDevice(ctx->device)
 
+struct mic_batch {
+  std::vector<unsigned char> jobs[BP_COUNT];  // job records of each pass, in the order added
+  std::vector<int64_t> n[BP_COUNT];           // markers of each job
+  template <class J>
+  int add(int pass, const J &job, int64_t markers) {
+    std::vector<unsigned char> &v = jobs[pass];
+    const size_t o = v.size();
+    v.resize(o + sizeof(J));
+    memcpy(v.data() + o, &job, sizeof(J));
+    n[pass].push_back(markers);
+    return MIC_OK;
+  }
+};
+
 // with_max: the step's maximum marker temperature into the reduction slot as well (run_max's)
-static int update_rho(mic_ctx *ctx, bool with_max) {
+static int update_rho(mic_ctx *ctx, bool with_max, mic_batch *b = nullptr) {
   int e = mic_ensure_sorted(ctx);
   if (e) return e;
   unsigned long long *d = reinterpret_cast<unsigned long long *>(ctx->red_buf + 8);
   if (with_max) MIC_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
   if (ctx->n == 0) return MIC_OK;
-  const int B = tuned_block(ctx, TU_UPDATE_RHO);
-  {
-    MIC_KERNEL(ctx, "k_update_rho");
-    if (with_max)
-      k_update_rho<true><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
-                                                                    ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n, d);
-    else
-      k_update_rho<false><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T],
-                                                                     ctx->f64[C_RHO], ctx->f64[C_RHODOT], ctx->mat, ctx->n,
-                                                                     nullptr);
-  }
-  MIC_CUDA_TRY(cudaGetLastError());
-  return MIC_OK;
+  const RhoJob J = {ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T], ctx->f64[C_RHO], ctx->f64[C_RHODOT],
+                    ctx->mat, ctx->n, with_max ? d : nullptr};
+  if (b) return b->add(BP_RHO, J, ctx->n);
+  return solo_pass(ctx, BP_RHO, J, tuned_block(ctx, TU_UPDATE_RHO), "k_update_rho");
 }
 
 extern "C" int mic_update_marker_rho(mic_ctx *ctx) {
@@ -1211,38 +1602,23 @@ extern "C" int mic_max_abs_sxx(mic_ctx *ctx, double *v) {
 }
 
 // limit: limitViscosity (viscosity.c:90-104) fused into the pass, for callers that run it next
-static int yield_launch(mic_ctx *ctx, double dt, bool limit = false) {
+static int yield_launch(mic_ctx *ctx, double dt, bool limit = false, mic_batch *b = nullptr) {
   int e = mic_ensure_sorted(ctx);
   if (e) return e;
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->is_yielding, 0, sizeof(int), ctx->stream));
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->bad_law, 0, sizeof(unsigned long long), ctx->stream));
   MIC_CUDA_TRY(cudaMemsetAsync(ctx->d_creep, 0, sizeof(CreepCounters), ctx->stream));
-  if (ctx->n > 0) {
-    const int mode = ctx->creep.mlp ? ctx->creep.mode : 0;
-    bool law7 = false;
-    for (int k = 0; k < MIC_MAXMAT; ++k) law7 = law7 || ctx->mat.hasEtaT[k] == 7;
-    if (!law7) {
-      MIC_KERNEL(ctx, "k_yield");
-      k_yield<2><<<grid_for(ctx->n, tuned_block(ctx, TU_YIELD)), tuned_block(ctx, TU_YIELD), 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
-                                                               dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
-    } else if (mode == 0) {
-      MIC_KERNEL(ctx, "k_yield");
-      k_yield<0><<<grid_for(ctx->n, tuned_block(ctx, TU_YIELD)), tuned_block(ctx, TU_YIELD), 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
-                                                               dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
-    } else if (mode == 1) {
-      MIC_KERNEL(ctx, "k_yield_surrogate_fp32");
-      k_yield<1><<<grid_for(ctx->n, 128), 128, 0, ctx->stream>>>(yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep,
-                                                                 dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
-    } else {
-      MIC_CUDA_TRY(cudaFuncSetAttribute(k_yield_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)tc::kDynSmem));
-      MIC_KERNEL(ctx, "k_yield_tc");
-      k_yield_tc<<<mic_creep_tc_blocks(ctx, ctx->n), tc::kTile, tc::kDynSmem, ctx->stream>>>(
-          yield_cols(ctx), ctx->mat, ctx->opt, ctx->creep, dt, ctx->n, ctx->d_status, ctx->d_creep, limit ? 1 : 0);
-    }
-    MIC_CUDA_TRY(cudaGetLastError());
-  }
-  return MIC_OK;
+  if (ctx->n == 0) return MIC_OK;
+  const int mode = ctx->creep.mlp ? ctx->creep.mode : 0;
+  bool law7 = false;
+  for (int k = 0; k < MIC_MAXMAT; ++k) law7 = law7 || ctx->mat.hasEtaT[k] == 7;
+  const YieldJob J = {yield_cols(ctx), ctx->mat,    ctx->opt,     ctx->creep,   dt,
+                      ctx->n,          ctx->d_status, ctx->d_creep, limit ? 1 : 0};
+  const int pass = !law7 ? BP_YIELD_PLAIN : mode == 0 ? BP_YIELD_EXACT : mode == 1 ? BP_YIELD_FP32 : BP_YIELD_TC;
+  if (b) return b->add(pass, J, ctx->n);
+  if (pass == BP_YIELD_PLAIN || pass == BP_YIELD_EXACT) return solo_pass(ctx, pass, J, tuned_block(ctx, TU_YIELD), "k_yield");
+  if (pass == BP_YIELD_FP32) return solo_pass(ctx, pass, J, kBatchBlock, "k_yield_surrogate_fp32");
+  return solo_pass(ctx, pass, J, tc::kTile, "k_yield_tc");
 }
 
 extern "C" int mic_check_plastic_yielding(mic_ctx *ctx, double dt, int *is_yielding, double elapsed_time) {
@@ -1285,7 +1661,7 @@ extern "C" int mic_limit_viscosity(mic_ctx *ctx) {
 }
 
 // keep: store the interpolated old stresses for a sub-grid stress pass that follows in this step
-static int strain_launch(mic_ctx *ctx, double dt, bool keep = false) {
+static int strain_launch(mic_ctx *ctx, double dt, bool keep = false, mic_batch *b = nullptr) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->nan_residual, 0, sizeof(unsigned long long), ctx->stream));
@@ -1306,13 +1682,9 @@ static int strain_launch(mic_ctx *ctx, double dt, bool keep = false) {
   c.kxy = keep ? ctx->scr0 : nullptr;
   c.kxx = keep ? ctx->scr1 : nullptr;
   c.kyy = keep ? ctx->scr2 : nullptr;
-  {
-    MIC_KERNEL(ctx, "k_strain_pressure");
-    k_strain_pressure<<<grid_for(ctx->n, tuned_block(ctx, TU_STRAIN)), tuned_block(ctx, TU_STRAIN), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n,
-                                                                    ctx->d_status);
-  }
-  MIC_CUDA_TRY(cudaGetLastError());
-  return MIC_OK;
+  const StrainJob J = {ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, ctx->n, ctx->d_status};
+  if (b) return b->add(BP_STRAIN, J, ctx->n);
+  return solo_pass(ctx, BP_STRAIN, J, tuned_block(ctx, TU_STRAIN), "k_strain_pressure");
 }
 
 extern "C" int mic_update_marker_strain_pressure(mic_ctx *ctx, double dt) {
@@ -1394,32 +1766,34 @@ extern "C" int mic_check_convergence(mic_ctx *ctx, double atol, double rtol, int
   return MIC_OK;
 }
 
-// reuse: k_strain_pressure of this step kept the interpolated old stresses in the scratch columns
-static int subgrid_launch(mic_ctx *ctx, double dt, double D, bool reuse) {
+// subgridStressChanges, marker part.  reuse: k_strain_pressure of this step kept the
+// interpolated old stresses in the scratch columns
+static int subgrid_markers(mic_ctx *ctx, double dt, double D, bool reuse, mic_batch *b = nullptr) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
-  if (ctx->n > 0) {
-    SubgridCols c;
-    c.cellX = ctx->i32[C_CELLX];
-    c.cellY = ctx->i32[C_CELLY];
-    c.X = ctx->f64[C_X];
-    c.Y = ctx->f64[C_Y];
-    c.eta = ctx->f64[C_ETA];
-    c.mu = ctx->f64[C_MU];
-    c.sxx = ctx->f64[C_SXX];
-    c.syy = ctx->f64[C_SYY];
-    c.sxy = ctx->f64[C_SXY];
-    c.dxy = ctx->scr0;
-    c.dxx = ctx->scr1;
-    c.dyy = ctx->scr2;
-    {
-      MIC_KERNEL(ctx, "k_subgrid_stress_markers");
-      const int B = tuned_block(ctx, TU_SUBGRID_STRESS);
-      k_subgrid_stress_markers<<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), dt,
-                                                                           D, ctx->n, reuse ? 1 : 0);
-    }
-    MIC_CUDA_TRY(cudaGetLastError());
-  }
+  if (ctx->n == 0) return MIC_OK;
+  SubgridCols c;
+  c.cellX = ctx->i32[C_CELLX];
+  c.cellY = ctx->i32[C_CELLY];
+  c.X = ctx->f64[C_X];
+  c.Y = ctx->f64[C_Y];
+  c.eta = ctx->f64[C_ETA];
+  c.mu = ctx->f64[C_MU];
+  c.sxx = ctx->f64[C_SXX];
+  c.syy = ctx->f64[C_SYY];
+  c.sxy = ctx->f64[C_SXY];
+  c.dxy = ctx->scr0;
+  c.dxx = ctx->scr1;
+  c.dyy = ctx->scr2;
+  const SubgridJob J = {ctx->P, c, geo_of(ctx), nodal_of(ctx), dt, D, ctx->n, reuse ? 1 : 0};
+  if (b) return b->add(BP_SUBGRID, J, ctx->n);
+  return solo_pass(ctx, BP_SUBGRID, J, tuned_block(ctx, TU_SUBGRID_STRESS), "k_subgrid_stress_markers");
+}
+
+// subgridStressChanges, node part: the nodal stress changes from the markers' ones
+static int subgrid_nodes(mic_ctx *ctx) {
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
   dim3 grid((ctx->P.NX + 127) / 128, ctx->P.NY);
 #ifdef MIC_EXACT
   {
@@ -1451,10 +1825,11 @@ static int subgrid_launch(mic_ctx *ctx, double dt, double D, bool reuse) {
 
 extern "C" int mic_subgrid_stress_changes(mic_ctx *ctx, double dt, double D) {
   CHECK_CTX();
-  return subgrid_launch(ctx, dt, D, false);
+  int e = subgrid_markers(ctx, dt, D, false);
+  return e ? e : subgrid_nodes(ctx);
 }
 
-static int stress_launch(mic_ctx *ctx) {
+static int stress_launch(mic_ctx *ctx, mic_batch *b = nullptr) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   MIC_CUDA_TRY(cudaMemsetAsync(&ctx->d_status->nan_dsxy, 0, sizeof(unsigned long long), ctx->stream));
@@ -1467,13 +1842,9 @@ static int stress_launch(mic_ctx *ctx) {
   c.sxx = ctx->f64[C_SXX];
   c.syy = ctx->f64[C_SYY];
   c.sxy = ctx->f64[C_SXY];
-  {
-    MIC_KERNEL(ctx, "k_update_marker_stress");
-    k_update_marker_stress<<<grid_for(ctx->n, tuned_block(ctx, TU_UPDATE_STRESS)), tuned_block(ctx, TU_UPDATE_STRESS), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), nodal_of(ctx), ctx->n,
-                                                                         ctx->d_status);
-  }
-  MIC_CUDA_TRY(cudaGetLastError());
-  return MIC_OK;
+  const StressJob J = {ctx->P, c, geo_of(ctx), nodal_of(ctx), ctx->n, ctx->d_status};
+  if (b) return b->add(BP_STRESS, J, ctx->n);
+  return solo_pass(ctx, BP_STRESS, J, tuned_block(ctx, TU_UPDATE_STRESS), "k_update_marker_stress");
 }
 
 extern "C" int mic_update_marker_stress(mic_ctx *ctx) {
@@ -1481,25 +1852,40 @@ extern "C" int mic_update_marker_stress(mic_ctx *ctx) {
   return stress_launch(ctx);
 }
 
-extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
-  CHECK_CTX();
-  int e = mic_ensure_geometry(ctx);
-  if (e) return e;
+static SubTCols subt_cols(mic_ctx *ctx) {
   SubTCols c;
   c.cellX = ctx->i32[C_CELLX];
   c.cellY = ctx->i32[C_CELLY];
   c.T = ctx->f64[C_T];
   c.Tdot = ctx->f64[C_TDOT];
   c.dTsub = ctx->scr0;
-  if (ctx->n > 0) {
-    {
-      MIC_KERNEL(ctx, "k_subgridT_markers");
-      k_subgridT_markers<<<grid_for(ctx->n, tuned_block(ctx, TU_SUBGRID_T)), tuned_block(ctx, TU_SUBGRID_T), 0, ctx->stream>>>(
-          ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_LASTT], ctx->nodal[MIC_NF_RHO], ctx->nodal[MIC_NF_CP],
-          ctx->nodal[MIC_NF_KTHERMAL], ctx->mat.materialRho[0], ctx->opt.subgridTemperatureDiffusivity, dt, ctx->n);
-    }
-    MIC_CUDA_TRY(cudaGetLastError());
-  }
+  return c;
+}
+
+// subgridTemperatureChanges in three parts: the markers' subgrid changes, their projection and
+// the nodal remainder, and its interpolation back to the markers
+static int subt_markers(mic_ctx *ctx, double dt, mic_batch *b = nullptr) {
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  if (ctx->n == 0) return MIC_OK;
+  const SubTJob J = {ctx->P,
+                     subt_cols(ctx),
+                     geo_of(ctx),
+                     ctx->nodal[MIC_NF_LASTT],
+                     ctx->nodal[MIC_NF_RHO],
+                     ctx->nodal[MIC_NF_CP],
+                     ctx->nodal[MIC_NF_KTHERMAL],
+                     ctx->mat.materialRho[0],
+                     ctx->opt.subgridTemperatureDiffusivity,
+                     dt,
+                     ctx->n};
+  if (b) return b->add(BP_SUBT, J, ctx->n);
+  return solo_pass(ctx, BP_SUBT, J, tuned_block(ctx, TU_SUBGRID_T), "k_subgridT_markers");
+}
+
+static int subt_nodes(mic_ctx *ctx) {
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
   if ((e = mic_project_scalar(ctx, ctx->scr0, 0, ctx->node_scr[0]))) return e;
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
   {
@@ -1508,19 +1894,27 @@ extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
                                                                ctx->node_scr[0], ctx->node_scr[1], nn);
   }
   MIC_CUDA_TRY(cudaGetLastError());
-  if (ctx->n > 0) {
-    {
-      MIC_KERNEL(ctx, "k_subgridT_apply");
-      k_subgridT_apply<<<grid_for(ctx->n, tuned_block(ctx, TU_SUBGRID_T_APPLY)), tuned_block(ctx, TU_SUBGRID_T_APPLY), 0, ctx->stream>>>(ctx->P, c, geo_of(ctx), ctx->node_scr[1], dt,
-                                                                     ctx->n);
-    }
-    MIC_CUDA_TRY(cudaGetLastError());
-  }
+  return MIC_OK;
+}
+
+static int subt_apply(mic_ctx *ctx, double dt, mic_batch *b = nullptr) {
+  int e = mic_ensure_geometry(ctx);
+  if (e) return e;
+  if (ctx->n == 0) return MIC_OK;
+  const SubTApplyJob J = {ctx->P, subt_cols(ctx), geo_of(ctx), ctx->node_scr[1], dt, ctx->n};
+  if (b) return b->add(BP_SUBT_APPLY, J, ctx->n);
+  return solo_pass(ctx, BP_SUBT_APPLY, J, tuned_block(ctx, TU_SUBGRID_T_APPLY), "k_subgridT_apply");
+}
+
+extern "C" int mic_subgrid_temperature_changes(mic_ctx *ctx, double dt) {
+  CHECK_CTX();
+  int e;
+  if ((e = subt_markers(ctx, dt)) || (e = subt_nodes(ctx)) || (e = subt_apply(ctx, dt))) return e;
   return MIC_OK;
 }
 
 // with_max: max |sxx| after the rotation into the reduction slot as well (run_max's)
-static int advect_launch(mic_ctx *ctx, double dt, bool wz_known, bool with_max = false) {
+static int advect_launch(mic_ctx *ctx, double dt, bool wz_known, bool with_max = false, mic_batch *b = nullptr) {
   int e = mic_ensure_geometry(ctx);
   if (e) return e;
   unsigned long long *d = reinterpret_cast<unsigned long long *>(ctx->red_buf + 8);
@@ -1557,20 +1951,25 @@ static int advect_launch(mic_ctx *ctx, double dt, bool wz_known, bool with_max =
           ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY], ctx->bcs.mechBCTop,
           ctx->bcs.mechBCLeft, NX, NY, cb, cb + nn, cb + 2 * nn);
     }
-#endif
-    {
-      MIC_KERNEL(ctx, "k_advect");
-      const int B = tuned_block(ctx, TU_ADVECT);
-      if (with_max)
-        k_advect<true><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(
-            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY], cv,
-            ctx->bcs.mechBCTop, ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0, d);
-      else
-        k_advect<false><<<grid_for(ctx->n, B), B, 0, ctx->stream>>>(
-            ctx->P, c, geo_of(ctx), ctx->nodal[MIC_NF_VX], ctx->nodal[MIC_NF_VY], ctx->nodal[MIC_NF_WXY], cv,
-            ctx->bcs.mechBCTop, ctx->bcs.mechBCLeft, dt, ctx->n, wz_known ? 1 : 0, nullptr);
-    }
     MIC_CUDA_TRY(cudaGetLastError());
+#endif
+    const AdvectJob J = {ctx->P,
+                         c,
+                         geo_of(ctx),
+                         ctx->nodal[MIC_NF_VX],
+                         ctx->nodal[MIC_NF_VY],
+                         ctx->nodal[MIC_NF_WXY],
+                         cv,
+                         ctx->bcs.mechBCTop,
+                         ctx->bcs.mechBCLeft,
+                         dt,
+                         ctx->n,
+                         wz_known ? 1 : 0,
+                         with_max ? d : nullptr};
+    if (b)
+      b->add(BP_ADVECT, J, ctx->n);
+    else if ((e = solo_pass(ctx, BP_ADVECT, J, tuned_block(ctx, TU_ADVECT), "k_advect")))
+      return e;
   }
   // positions moved: cells, order and geometry are stale until the next binning
   ctx->sorted = 0;
@@ -1602,50 +2001,10 @@ extern "C" int mic_project_nodal_field_to_markers(mic_ctx *ctx, int f, int off) 
 
 // ---- step drivers ------------------------------------------------------------------
 
-extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yielding, double *max_T) {
-  CHECK_CTX();
-  int e;
-  // findMarkerCells (main:243, 247, 252): positions do not change between the three calls on
-  // one rank without density control, so one binning gives all three results
-  if ((e = mic_bin_and_sort(ctx, nullptr))) return e;
-  // the density update also finds the maximum temperature (main:271-281; the projection between
-  // changes no marker temperature)
-  if ((e = update_rho(ctx, true))) return e;
-#ifdef MIC_EXACT
-  if ((e = mic_project_markers_nodes_all2(ctx))) return e;
-  if ((e = yield_launch(ctx, dt_disp))) return e;
-  if ((e = mic_limit_viscosity(ctx))) return e;
-  if ((e = mic_project_all2_viscous(ctx))) return e;
-#else
-  // The first projection (main:268) and the yield pass touch disjoint marker columns (rho, T,
-  // materials against viscosity, modulus and stresses), and the first projection's viscosity and
-  // stress fields are replaced by the second (main:303) before anything reads them: so it forms
-  // only rho, k, T and Cp, on the second stream, beside the yield pass (which applies the
-  // viscosity limit of main:297 to every marker as it stores the viscosities).
-  if ((e = mic_ensure_geometry(ctx))) return e;
-  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
-  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
-  if ((e = mic_project_all2_first(ctx, ctx->aux))) return e;
-  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
-  if ((e = yield_launch(ctx, dt_disp, /*limit=*/true))) return e;  // limitViscosity fused in
-  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
-  // the second projection: yielding and the limit changed viscosities and stresses only
-  if ((e = mic_project_all2_viscous(ctx))) return e;
-#endif
-  if (is_yielding || max_T) {
-    if ((e = read_status(ctx))) return e;
-    if (is_yielding) *is_yielding = ctx->h_status->is_yielding;
-    if (max_T) {
-      unsigned long long h = 0;
-      MIC_CUDA_TRY(cudaMemcpyAsync(&h, ctx->red_buf + 8, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
-      MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-      memcpy(max_T, &h, sizeof(double));
-    }
-  }
-  return MIC_OK;
-}
-
-extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_stress, double *residual) {
+// One segment of a step (declared in mic_internal.cuh): the stages of main_subduction.c's time
+// loop between one marker pass and the next, on the context's stream.
+int mic_step_segment(mic_ctx *ctx, int seg, double dt_disp, double dt_thermal, int subgrid_stress, int wz_known,
+                     mic_batch *b) {
   CHECK_CTX();
   int e;
   const bool sub = subgrid_stress && ctx->opt.subgridStressDiffusivity > 0.0;
@@ -1654,64 +2013,225 @@ extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_st
 #else
   const bool keep = sub && ctx->n > 0;
 #endif
-  if ((e = strain_launch(ctx, dt_disp, keep))) return e;
-  double *d = ctx->red_buf + 16;
+  switch (seg) {
+    case 0:
+      // findMarkerCells (main:243, 247, 252): positions do not change between the three calls on
+      // one rank without density control, so one binning gives all three results.  The density
+      // update also finds the maximum temperature (main:271-281; the projection between changes no
+      // marker temperature).
+      if ((e = mic_bin_and_sort(ctx, nullptr))) return e;
+      return update_rho(ctx, true, b);
+    case 1:
 #ifdef MIC_EXACT
-  if ((e = residual_launch(ctx, 0, d))) return e;
+      if ((e = mic_project_markers_nodes_all2(ctx))) return e;
+      return yield_launch(ctx, dt_disp, false, b);
 #else
-  // the residual (a cell-centre projection of srr and its area-weighted sum) shares no buffer with
-  // the sub-grid stress and stress-update passes: it runs on the second stream beside them
-  if ((e = mic_ensure_geometry(ctx))) return e;
-  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
-  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
-  if ((e = residual_launch(ctx, 0, d, ctx->aux))) return e;  // leaves the scratch columns alone
-  MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
+      // The first projection (main:268) and the yield pass touch disjoint marker columns (rho, T,
+      // materials against viscosity, modulus and stresses), and the first projection's viscosity
+      // and stress fields are replaced by the second (main:303) before anything reads them: so it
+      // forms only rho, k, T and Cp, on the second stream, beside the yield pass (which applies
+      // the viscosity limit of main:297 to every marker as it stores the viscosities).
+      if ((e = mic_ensure_geometry(ctx))) return e;
+      MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
+      MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
+      if ((e = mic_project_all2_first(ctx, ctx->aux))) return e;
+      MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
+      return yield_launch(ctx, dt_disp, /*limit=*/true, b);  // limitViscosity fused in
 #endif
-  if (sub && (e = subgrid_launch(ctx, dt_disp, ctx->opt.subgridStressDiffusivity, keep))) return e;
-  if ((e = stress_launch(ctx))) return e;
+    case 2:
+#ifdef MIC_EXACT
+      if ((e = mic_limit_viscosity(ctx))) return e;
+#else
+      MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
+#endif
+      // the second projection: yielding and the limit changed viscosities and stresses only
+      return mic_project_all2_viscous(ctx);
+    case 3:
+      return strain_launch(ctx, dt_disp, keep, b);
+    case 4:
+#ifdef MIC_EXACT
+      if ((e = residual_launch(ctx, 0, ctx->red_buf + 16))) return e;
+#else
+      // the residual (a cell-centre projection of srr and its area-weighted sum) shares no buffer
+      // with the sub-grid stress and stress-update passes: it runs on the second stream beside them
+      if ((e = mic_ensure_geometry(ctx))) return e;
+      MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[0], ctx->stream));
+      MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
+      if ((e = residual_launch(ctx, 0, ctx->red_buf + 16, ctx->aux))) return e;  // leaves the scratch columns alone
+      MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
+#endif
+      return sub ? subgrid_markers(ctx, dt_disp, ctx->opt.subgridStressDiffusivity, keep, b) : MIC_OK;
+    case 5:
+      if (sub && (e = subgrid_nodes(ctx))) return e;
+      return stress_launch(ctx, b);
+    case 6:
 #ifndef MIC_EXACT
-  MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
+      MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[1], 0));
 #endif
-  if (residual) {
-    double s = 0.0;
-    MIC_CUDA_TRY(cudaMemcpyAsync(&s, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    s /= (ctx->P.LX * ctx->P.LY);
-    ctx->residuals[0] = s;
-    *residual = s;
+      return MIC_OK;
+    case 7:
+      return subt_markers(ctx, dt_thermal, b);
+    case 8:
+      if ((e = subt_nodes(ctx))) return e;
+      return subt_apply(ctx, dt_thermal, b);
+    case 9:
+      // the advection also forms max |sxx| of the rotated stresses (main:437-448)
+      return advect_launch(ctx, dt_thermal, wz_known != 0, true, b);
+  }
+  return MIC_ERR_ARG;
+}
+
+// segments [s0, s1) of a step, each marker pass launched on the context's stream
+static int run_segments(mic_ctx *ctx, int s0, int s1, double dt_disp, double dt_thermal, int sub, int wz_known) {
+  for (int k = s0; k < s1; ++k) {
+    const int e = mic_step_segment(ctx, k, dt_disp, dt_thermal, sub, wz_known, nullptr);
+    if (e) return e;
   }
   return MIC_OK;
 }
 
-// wz_known: the marker vorticity is this step's k_strain_pressure value on the nodal wxy the
-// advection reads (true inside mic_step; a caller between the calls may replace nodal fields)
-static int post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx, bool wz_known) {
+static int read_max_slot(mic_ctx *ctx, double *out) {
+  unsigned long long h = 0;
+  MIC_CUDA_TRY(cudaMemcpyAsync(&h, ctx->red_buf + 8, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  memcpy(out, &h, sizeof(double));
+  return MIC_OK;
+}
+
+extern "C" int mic_step_pre_stokes(mic_ctx *ctx, double dt_disp, int *is_yielding, double *max_T) {
+  CHECK_CTX();
   int e;
-  if ((e = mic_subgrid_temperature_changes(ctx, dt_thermal))) return e;
-  // the advection also forms max |sxx| of the rotated stresses (main:437-448)
-  if ((e = advect_launch(ctx, dt_thermal, wz_known, true))) return e;
-  if (max_abs_sxx) {
-    unsigned long long h = 0;
-    MIC_CUDA_TRY(cudaMemcpyAsync(&h, ctx->red_buf + 8, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
-    MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    memcpy(max_abs_sxx, &h, sizeof(double));
+  if ((e = run_segments(ctx, 0, 3, dt_disp, 0.0, 0, 0))) return e;
+  if (is_yielding || max_T) {
+    if ((e = read_status(ctx))) return e;
+    if (is_yielding) *is_yielding = ctx->h_status->is_yielding;
+    if (max_T && (e = read_max_slot(ctx, max_T))) return e;
   }
   return MIC_OK;
+}
+
+static int read_residual(mic_ctx *ctx, double *residual) {
+  double s = 0.0;
+  MIC_CUDA_TRY(cudaMemcpyAsync(&s, ctx->red_buf + 16, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  s /= (ctx->P.LX * ctx->P.LY);
+  ctx->residuals[0] = s;
+  *residual = s;
+  return MIC_OK;
+}
+
+extern "C" int mic_step_post_stokes(mic_ctx *ctx, double dt_disp, int subgrid_stress, double *residual) {
+  CHECK_CTX();
+  int e;
+  if ((e = run_segments(ctx, 3, 7, dt_disp, 0.0, subgrid_stress, 0))) return e;
+  return residual ? read_residual(ctx, residual) : MIC_OK;
 }
 
 extern "C" int mic_step_post_thermal(mic_ctx *ctx, double dt_thermal, double *max_abs_sxx) {
   CHECK_CTX();
-  return post_thermal(ctx, dt_thermal, max_abs_sxx, false);
+  int e;
+  // the marker vorticity may be stale here: a caller between the calls may replace nodal fields
+  if ((e = run_segments(ctx, 7, kStepSegments, 0.0, dt_thermal, 0, 0))) return e;
+  return max_abs_sxx ? read_max_slot(ctx, max_abs_sxx) : MIC_OK;
 }
 
 extern "C" int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress, double *residual) {
   CHECK_CTX();
   int e;
-  if ((e = mic_step_pre_stokes(ctx, dt_disp, nullptr, nullptr))) return e;
-  if ((e = mic_step_post_stokes(ctx, dt_disp, subgrid_stress, residual))) return e;
+  if ((e = run_segments(ctx, 0, 7, dt_disp, dt_thermal, subgrid_stress, 0))) return e;
+  if (residual && (e = read_residual(ctx, residual))) return e;
 #ifdef MIC_EXACT
-  return post_thermal(ctx, dt_thermal, nullptr, false);
+  const int wz_known = 0;
 #else
-  return post_thermal(ctx, dt_thermal, nullptr, ctx->n > 0);
+  // the marker vorticity is this step's k_strain_pressure value on the nodal wxy the advection reads
+  const int wz_known = ctx->n > 0;
 #endif
+  return run_segments(ctx, 7, kStepSegments, dt_disp, dt_thermal, subgrid_stress, wz_known);
+}
+
+// ---- batches --------------------------------------------------------------------------
+
+mic_batch *mic_batch_new() { return new (std::nothrow) mic_batch(); }
+void mic_batch_free(mic_batch *b) { delete b; }
+void mic_batch_clear(mic_batch *b) {
+  for (int p = 0; p < BP_COUNT; ++p) {
+    b->jobs[p].clear();
+    b->n[p].clear();
+  }
+}
+bool mic_batch_empty(const mic_batch *b) {
+  for (int p = 0; p < BP_COUNT; ++p)
+    if (!b->n[p].empty()) return false;
+  return true;
+}
+
+
+size_t mic_job_slots_bytes() { return (size_t)BP_COUNT * kJobSlotBytes; }
+
+size_t mic_batch_table_bound(int n_members) {
+  size_t per = sizeof(RhoJob) + sizeof(YieldJob) + sizeof(StrainJob) + sizeof(SubgridJob) + sizeof(StressJob) +
+               sizeof(SubTJob) + sizeof(SubTApplyJob) + sizeof(AdvectJob);
+  return (size_t)n_members * per + (size_t)BP_COUNT * (kTableAlign + sizeof(int) * ((size_t)n_members + 1)) +
+         kTableAlign;
+}
+
+int mic_batch_launch(mic_batch *b, const BatchShape *shape, unsigned char *host_table, unsigned char *dev_table,
+                     size_t *off, size_t cap, int copy, cudaStream_t s, long long *launches) {
+  int dev = 0, nsm = 0;
+  cudaError_t ce;
+  if ((ce = cudaGetDevice(&dev)) != cudaSuccess) return batch_fail(ce);
+  if ((ce = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return batch_fail(ce);
+  int status = MIC_OK;
+  for (int p = 0; p < BP_COUNT && status == MIC_OK; ++p) {
+    const int nj = (int)b->n[p].size();
+    if (nj == 0) continue;
+    const bool tcp = p == BP_YIELD_TC;
+    const int block = tcp ? tc::kTile : kBatchBlock;
+    // a job switch restages the network in the surrogate passes: those walk contiguous runs
+    const bool restages = tcp || p == BP_YIELD_FP32;
+    const int persistent = restages ? 1 : shape[p].persistent;
+    const int chunked = restages ? 1 : shape[p].chunked;
+    const int mult = shape[p].mult < 1 ? 1 : (shape[p].mult > 64 ? 64 : shape[p].mult);
+    const int tm = block * mult;
+    std::vector<int> ts(nj + 1);
+    ts[0] = 0;
+    for (int j = 0; j < nj; ++j) {
+      const int64_t t = (b->n[p][j] + tm - 1) / tm;
+      if ((int64_t)ts[j] + t > 0x7fffffff) {
+        status = MIC_ERR_ARG;
+        break;
+      }
+      ts[j + 1] = ts[j] + (int)t;
+    }
+    if (status) break;
+    const int ntiles = ts[nj];
+    const size_t o = (*off + kTableAlign - 1) / kTableAlign * kTableAlign;
+    const size_t jb = b->jobs[p].size(), tb = sizeof(int) * (size_t)(nj + 1);
+    if (jb != (size_t)nj * kJobBytes[p] || o + jb + tb > cap) {
+      status = MIC_ERR_NOMEM;
+      break;
+    }
+    memcpy(host_table + o, b->jobs[p].data(), jb);
+    memcpy(host_table + o + jb, ts.data(), tb);
+    if (copy && (ce = cudaMemcpyAsync(dev_table + o, host_table + o, jb + tb, cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+      status = batch_fail(ce);
+      break;
+    }
+    *off = o + jb + tb;
+    const unsigned char *dj = dev_table + o;
+    const int *dts = reinterpret_cast<const int *>(dev_table + o + jb);
+    int64_t grid = ntiles;
+    if (persistent) {
+      const int64_t g = (int64_t)nsm * pass_occupancy(dev, p, block);
+      if (g < grid) grid = g;
+    }
+    if (grid < 1) grid = 1;
+    if ((ce = launch_pass(p, (unsigned)grid, block, s, dj, dts, nj, ntiles, tm, chunked)) != cudaSuccess) {
+      status = batch_fail(ce);
+      break;
+    }
+    if (launches) ++*launches;
+  }
+  mic_batch_clear(b);
+  return status;
 }

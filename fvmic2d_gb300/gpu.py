@@ -100,6 +100,8 @@ SIGNATURES = {
     "mic_ensemble_synchronize": (_I, [_P]),
     "mic_ensemble_launch_count": (_I, [_P, _I64P, _I64P]),
     "mic_ensemble_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
+    "mic_ensemble_set_schedule": (_I, [_P, _I, _I, _I, _I]),
+    "mic_ensemble_get_schedule": (_I, [_P, _IP, _IP, _IP, _IP]),
     "mic_check_marker_density": (_I, [_P, _P, _I64P, _I64P]),
     "mic_nodal_stress_strain": (_I, [_P, _D, _D]),
     "mic_project_markers_nodes_from_scalar": (_I, [_P, _DP, _I]),
@@ -677,6 +679,22 @@ class MicEnsemble:
         if code:
             raise MicError(code, "mic_ensemble_autotune")
         return list(out)
+
+    def set_schedule(self, batched=True, tile_mult=4, persistent=True, chunked=True):
+        """mic_ensemble_set_schedule: batched marker passes (one kernel per pass over all members)
+        or per-member kernels; tile size in blocks' worth of markers and the grid's walk."""
+        code = self.L.mic_ensemble_set_schedule(self.h, 1 if batched else 0, int(tile_mult), 1 if persistent else 0,
+                                                1 if chunked else 0)
+        if code:
+            raise MicError(code, "mic_ensemble_set_schedule")
+
+    def schedule(self):
+        v = [ctypes.c_int(0) for _ in range(4)]
+        code = self.L.mic_ensemble_get_schedule(self.h, *[ctypes.byref(x) for x in v])
+        if code:
+            raise MicError(code, "mic_ensemble_get_schedule")
+        return {"batched": bool(v[0].value), "tile_mult": v[1].value, "persistent": bool(v[2].value),
+                "chunked": bool(v[3].value)}
 
     def step(self, dt_disp=None, dt_thermal=None, subgrid_stress=1, graph=True):
         n = len(self.members)

@@ -62,12 +62,27 @@ def _setup(wls):
     return out
 
 
+# (batched, tile_mult, persistent, chunked): per-member kernels on member streams, and batched
+# marker passes with one block per tile, a persistent round-robin walk, and persistent
+# contiguous runs of two tile sizes
+SCHEDULES = {
+    "per_member": (False, 4, True, True),
+    "tile_per_block": (True, 1, False, False),
+    "round_robin": (True, 4, True, False),
+    "runs": (True, 4, True, True),
+    "runs16": (True, 16, True, True),
+}
+
+
+@pytest.mark.parametrize("schedule", list(SCHEDULES))
 @pytest.mark.parametrize("graph", [True, False])
-def test_ensemble_matches_members_stepped_alone(graph):
+def test_ensemble_matches_members_stepped_alone(graph, schedule):
     wls = _members(40)
     A = _setup(wls)
     B = _setup(wls)
     E = gpu.MicEnsemble(A)
+    E.set_schedule(*SCHEDULES[schedule])
+    assert E.schedule()["batched"] == SCHEDULES[schedule][0]
     dts = np.array([wl.dt for wl in wls])
 
     def compare():
@@ -96,7 +111,7 @@ def test_ensemble_matches_members_stepped_alone(graph):
     compare()
     launches, per_graph = E.launch_count()
     assert launches > 0
-    if graph:
+    if graph and not SCHEDULES[schedule][0]:
         assert per_graph >= 25 * len(A)
     E.close()
 
@@ -117,6 +132,8 @@ def test_ensemble_autotune_keeps_states_and_results():
     before = [_bytes(a.markers) for a in A]
     order = E.autotune(dts, dts, subgrid_stress=1, steps=1)
     assert sorted(order) == list(range(len(A)))
+    sch = E.schedule()
+    assert sch["tile_mult"] in (1, 4, 16)
     for a, m in zip(A, before):
         assert np.array_equal(_bytes(a.markers), m)
     for _ in range(3):
@@ -129,8 +146,9 @@ def test_ensemble_autotune_keeps_states_and_results():
         assert np.array_equal(a.get_nodal("lastT"), b.get_nodal("lastT"))
 
 
+@pytest.mark.parametrize("schedule", ["per_member", "runs"])
 @pytest.mark.parametrize("graph", [True, False])
-def test_plastic_members_match_members_stepped_alone(graph):
+def test_plastic_members_match_members_stepped_alone(graph, schedule):
     """Visco-elasto-plastic members (yielding, so the step's viscosity-only second projection
     and its first projection beside the yield pass on each member's second stream both matter),
     of different sizes, stepped together as captured graphs or on streams: each member's markers
@@ -140,6 +158,7 @@ def test_plastic_members_match_members_stepped_alone(graph):
     A = [gpu.MicProblem(wl) for wl in wls]
     B = [gpu.MicProblem(wl) for wl in wls]
     E = gpu.MicEnsemble(A)
+    E.set_schedule(*SCHEDULES[schedule])
     dts = np.array([wl.dt for wl in wls])
     for _ in range(3):
         E.step(dts, dts, subgrid_stress=1, graph=graph)
@@ -186,5 +205,59 @@ def test_member_stepped_or_tuned_between_replays():
         assert a.n == b.n
         assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
         for f in ("rho", "etaN", "etaS", "lastT"):
+            assert np.array_equal(a.get_nodal(f), b.get_nodal(f)), f
+    E.close()
+
+
+@pytest.mark.parametrize("schedule", ["runs", "round_robin", "tile_per_block"])
+@pytest.mark.parametrize("graph", [True, False])
+def test_creep_members_batched_match_members_stepped_alone(graph, schedule):
+    """Law-7 ice members with every yield variant in one batch -- exact creep solve, tensor-core
+    surrogate with two different networks, FP32 surrogate -- beside a member without law 7:
+    the batched yield kernels restage the network whenever a tile's member uses another one, and
+    every member's markers, nodal fields and creep counters are what stepping it alone gives,
+    bit for bit"""
+    specs = [(24, 24, 0), (32, 16, 2), (16, 40, 2), (40, 24, 1)]
+    wls = [W.ice_member(nx, ny, 900 + k) for k, (nx, ny, _) in enumerate(specs)]
+    conv = W.convection_member(16, 16, 4, 4, 1e5, 1e2, 77)
+
+    def build():
+        out = []
+        for wl in wls:
+            P = gpu.MicProblem(wl, capacity=wl.capacity)
+            gpu.initialize_markers(P, *wl.nm, seed=wl.seed)
+            P.set_grain_size(W.ice_grain_sizes(P.n, wl.seed))
+            out.append(P)
+        P = gpu.MicProblem(conv, capacity=conv.capacity)
+        gpu.initialize_markers(P, *conv.nm, seed=conv.seed)
+        out.append(P)
+        return out
+
+    A, B = build(), build()
+    A[1].creep_train(nsamples=1 << 16, batch=1024, steps=300, seed=3)
+    net = A[1].creep_params()
+    other = net.copy()
+    rng = np.random.default_rng(5)
+    other[:-16] *= (1.0 + 0.05 * rng.standard_normal(len(other) - 16)).astype(np.float32)
+    for k, (_, _, mode) in enumerate(specs):
+        for P in (A[k], B[k]):
+            P.creep_set_params(other if k == 2 else net)
+            P.creep_configure(mode=mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
+    E = gpu.MicEnsemble(A)
+    E.set_schedule(*SCHEDULES[schedule])
+    dts = np.array([wl.dt for wl in wls] + [conv.dt])
+    for _ in range(3):
+        E.step(dts, dts, subgrid_stress=1, graph=graph)
+        for b, dt in zip(B, dts):
+            b.step(dt, dt, True)
+        E.synchronize()
+        for k in range(len(specs)):
+            sa, sb = A[k].creep_stats(), B[k].creep_stats()
+            assert sa == sb, (k, sa, sb)
+            assert sa["markers"] > 0
+    for a, b in zip(A, B):
+        assert a.n == b.n
+        assert np.array_equal(_bytes(a.markers), _bytes(b.markers))
+        for f in ("rho", "etaN", "etaS", "soxx", "lastT"):
             assert np.array_equal(a.get_nodal(f), b.get_nodal(f)), f
     E.close()
