@@ -665,10 +665,35 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+ENSEMBLE_STEPS = 50  # the batching configurations' step count
+
+
+def _time_ensemble(E, es, dts, steps, graph):
+    """ms per ensemble step over `steps` steps (after three untimed ones), CUDA events on the
+    ensemble stream, and kernels launched per step"""
+    import torch
+
+    for _ in range(3):
+        E.step(dts, dts, 1, graph)
+    E.synchronize()
+    l0, _ = E.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(es)
+    for _ in range(steps):
+        E.step(dts, dts, 1, graph)
+    ev1.record(es)
+    ev1.synchronize()
+    l1, _ = E.launch_count()
+    return ev0.elapsed_time(ev1) / steps, (l1 - l0) / steps
+
+
 def ensemble_leg(args, local):
     """Ensemble of independent convection runs (64 members, mixed grids): the same steps issued
-    one member at a time (each step waiting for the host, as a plain loop over problems does),
-    concurrently on the members' streams, and as one captured CUDA graph per ensemble step."""
+    one member at a time (each step waiting for the host, as a plain loop over problems does);
+    per-member (every member's own kernels on its stream) and batched (one kernel per marker pass
+    over all members), each on streams and as one captured CUDA graph per ensemble step; then the
+    schedule mic_ensemble_autotune picks."""
     import numpy as np
     import torch
 
@@ -685,58 +710,42 @@ def ensemble_leg(args, local):
     E = gpu.MicEnsemble(members)
     es = torch.cuda.ExternalStream(E.stream(), device=local)
     dts = np.array([wl.dt for wl in wls])
-    steps = max(3, min(args.steps, 10))
+    steps = ENSEMBLE_STEPS
     out = {"workload": "convection_ensemble: 64 independent thermal-convection runs, square grids drawn from "
                        "{64^2,128^2,256^2,512^2} cells, 9/16/25 markers per cell, Ra log-uniform 1e4-1e7, viscosity "
                        "contrast log-uniform 1e1-1e5 (SplitMix64 seed 4); markers laid out on the device by "
                        "resetMarkers + distributeMarkersUniformInDomain",
            "members": len(members), "markers": int(n_total), "steps": steps}
     # one member at a time, host waiting on each (the residual read of mic_step)
+    seq_steps = max(3, min(args.steps, 10))
     for _ in range(2):
         for P, dt in zip(members, dts):
             P.step(dt, dt, True)
     t0 = time.perf_counter()
-    for _ in range(steps):
+    for _ in range(seq_steps):
         for P, dt in zip(members, dts):
             P.step(dt, dt, True)
-    ms = (time.perf_counter() - t0) * 1e3 / steps
-    out["sequential"] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms}
-    for label, graph in (("streams", False), ("graph", True)):
-        for _ in range(3):
-            E.step(dts, dts, 1, graph)
-        E.synchronize()
-        l0, _ = E.launch_count()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(es)
-        for _ in range(steps):
-            E.step(dts, dts, 1, graph)
-        ev1.record(es)
-        ev1.synchronize()
-        ms = ev0.elapsed_time(ev1) / steps
-        l1, per_graph = E.launch_count()
-        out[label] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
-                      "kernels_per_step": (l1 - l0) / steps}
-    out["speedup_graph_vs_sequential"] = out["graph"]["value"] / out["sequential"]["value"]
-    # members' launch shapes and the issue order of their steps from mic_ensemble_autotune (state
-    # restored by it), then the captured steps timed again
+    ms = (time.perf_counter() - t0) * 1e3 / seq_steps
+    out["sequential"] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
+                         "steps": seq_steps}
+    for mode, batched in (("per_member", False), ("batched", True)):
+        E.set_schedule(batched=batched)
+        for label, graph in (("streams", False), ("graph", True)):
+            ms, kps = _time_ensemble(E, es, dts, steps, graph)
+            out[mode + "_" + label] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
+                                       "kernels_per_step": kps}
+    out["speedup_batched_vs_per_member_graph"] = out["batched_graph"]["value"] / out["per_member_graph"]["value"]
+    out["speedup_graph_vs_sequential"] = out["batched_graph"]["value"] / out["sequential"]["value"]
+    # members' launch shapes, the member order and the batching schedule from mic_ensemble_autotune
+    # (state restored by it), then the captured steps timed again
     E.synchronize()
     t_tune = time.perf_counter()
     order = E.autotune(dts, dts, 1, steps=2)
     t_tune = time.perf_counter() - t_tune
     sizes = [members[i].n for i in order]
-    for _ in range(3):
-        E.step(dts, dts, 1, True)
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(es)
-    for _ in range(steps):
-        E.step(dts, dts, 1, True)
-    ev1.record(es)
-    ev1.synchronize()
-    ms = ev0.elapsed_time(ev1) / steps
+    ms, kps = _time_ensemble(E, es, dts, steps, True)
     out["graph_tuned"] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
-                          "tune_seconds": t_tune,
+                          "kernels_per_step": kps, "tune_seconds": t_tune, "schedule": E.schedule(),
                           "order": ("largest first" if sizes == sorted(sizes, reverse=True) else
                                     "smallest first" if sizes == sorted(sizes) else "as given"),
                           "member_blocks_k_advect": sorted(set(P.tuning()["k_advect"] for P in members))}
@@ -749,8 +758,9 @@ def ensemble_leg(args, local):
 def ice_ensemble_leg(args, local):
     """Mixed ensemble with the learned closure: 256 independent ice-creep VEP boxes (grids from
     128^2 to 1024 x 256 cells, 16 markers per cell, law 7 with per-marker grain sizes,
-    Drucker-Prager yield), stepped as captured graphs with the exact creep solve and with the
-    tensor-core surrogate (one network trained once, shared by all members)."""
+    Drucker-Prager yield), 50 captured-graph steps with the exact creep solve and with the
+    tensor-core surrogate (one network trained once, shared by all members), each per-member and
+    batched."""
     import torch
 
     from fvmic2d_gb300 import gpu
@@ -773,7 +783,7 @@ def ice_ensemble_leg(args, local):
     E = gpu.MicEnsemble(members)
     es = torch.cuda.ExternalStream(E.stream(), device=local)
     dts = [wl.dt for wl in wls]
-    steps = max(3, min(args.steps, 10))
+    steps = ENSEMBLE_STEPS
     out = {"workload": "ice_ensemble: 256 independent ice-creep VEP boxes (law 7, Drucker-Prager yield, "
                        "shear modulus 3.5 GPa), grids drawn from {128^2, 256x64, 128x256, 192^2, 1024x256} cells "
                        "(SplitMix64 seed 5), 16 markers per cell, per-marker log10 grain size ~ U[-4,-1] m",
@@ -781,25 +791,23 @@ def ice_ensemble_leg(args, local):
     for label, mode in (("plain", 0), ("surrogate_tc", 2)):
         for P in members:
             P.creep_configure(mode=mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
-        for _ in range(2):
-            E.step(dts, dts, 1, True)
-        E.synchronize()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(es)
-        for _ in range(steps):
-            E.step(dts, dts, 1, True)
-        ev1.record(es)
-        ev1.synchronize()
-        ms = ev0.elapsed_time(ev1) / steps
-        st = [P.creep_stats() for P in members]
-        mk = sum(x["markers"] for x in st)
-        out[label] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
-                      "newton_iters_per_marker": sum(x["iterations"] for x in st) / max(mk, 1),
-                      "fallbacks_per_step": sum(x["fallbacks"] for x in st),
-                      "max_residual": max(x["max_residual"] for x in st),
-                      "tc_timeouts": sum(x["tc_timeouts"] for x in st)}
-    out["speedup_surrogate_vs_plain"] = out["surrogate_tc"]["value"] / out["plain"]["value"]
+        for sched, batched in (("per_member", False), ("batched", True)):
+            E.set_schedule(batched=batched)
+            ms, kps = _time_ensemble(E, es, dts, steps, True)
+            st = [P.creep_stats() for P in members]
+            mk = sum(x["markers"] for x in st)
+            out[label + "_" + sched] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
+                                        "kernels_per_step": kps,
+                                        "newton_iters_per_marker": sum(x["iterations"] for x in st) / max(mk, 1),
+                                        "fallbacks_per_step": sum(x["fallbacks"] for x in st),
+                                        "max_residual": max(x["max_residual"] for x in st),
+                                        "tc_timeouts": sum(x["tc_timeouts"] for x in st)}
+    for sched in ("per_member", "batched"):
+        out["speedup_surrogate_vs_plain_" + sched] = (out["surrogate_tc_" + sched]["value"] /
+                                                      out["plain_" + sched]["value"])
+    for label in ("plain", "surrogate_tc"):
+        out["speedup_batched_vs_per_member_" + label] = (out[label + "_batched"]["value"] /
+                                                         out[label + "_per_member"]["value"])
     E.close()
     for P in members:
         P.close()

@@ -290,6 +290,15 @@ int ensure_mlp(mic_ctx *ctx) {
 
 size_t fwdbwd_smem() { return sizeof(float) * (kH * kH + 4 * kTB * kH + kTB * 4 + kTB); }
 
+// content key of a network's parameters (FNV-1a over their bytes, never 0): contexts whose keys
+// agree hold the same network, so a batch of their marker passes may read any one of the copies
+unsigned long long net_key(const float *p) {
+  const unsigned char *b = reinterpret_cast<const unsigned char *>(p);
+  unsigned long long h = 1469598103934665603ULL;
+  for (size_t i = 0; i < sizeof(float) * kNParams; ++i) h = (h ^ b[i]) * 1099511628211ULL;
+  return h ? h : 1ULL;
+}
+
 }  // namespace
 
 // grain sizes -> the grain argument the creep coefficients take (grain_arg), in place
@@ -362,6 +371,8 @@ extern "C" int mic_creep_set_mlp(mic_ctx *ctx, const float *params, int n) {
   if (e) return e;
   MIC_CUDA_TRY(cudaMemcpyAsync(ctx->mlp, params, sizeof(float) * kNParams, cudaMemcpyHostToDevice, ctx->stream));
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  ctx->mlp_key = net_key(params);
+  ctx->gen++;  // captured steps may read this network through another context's copy
   return MIC_OK;
 }
 
@@ -495,6 +506,7 @@ extern "C" int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int st
   cudaSetDevice(ctx->device);
   int e = ensure_mlp(ctx);
   if (e) return e;
+  ctx->mlp_key = 0;  // the network is rewritten below
   const int nblocks = batch / kTB;
   // features (4n), targets (n), sample order (n ints), partials, loss partials, Adam moments, losses
   const int64_t need = 6 * nsamples + (int64_t)nblocks * kNTrain + nblocks + 2 * (int64_t)kNTrain + steps + 16;
@@ -557,6 +569,11 @@ extern "C" int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int st
     for (int s = 0; s < steps; ++s) loss_hist[s] /= batch;
   }
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  {
+    std::vector<float> h(kNParams);
+    MIC_CUDA_TRY(cudaMemcpy(h.data(), ctx->mlp, sizeof(float) * kNParams, cudaMemcpyDeviceToHost));
+    ctx->mlp_key = net_key(h.data());
+  }
   ctx->creep.mlp = ctx->mlp;
   ctx->gen++;
   return MIC_OK;

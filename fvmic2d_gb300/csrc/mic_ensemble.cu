@@ -374,8 +374,8 @@ extern "C" int mic_ensemble_get_stream(mic_ensemble *E, void **stream) {
 // How a step runs its marker passes: batched (1: one kernel per pass over all members; 0: each
 // member's own kernels on its stream), and for the batched kernels the tile size in blocks'
 // worth of markers, persistent grid or one block per tile, and contiguous runs of tiles per
-// block or round-robin.  The surrogate passes always walk contiguous runs on a persistent grid
-// (a block restages the network when its member changes).
+// block or round-robin.  The surrogate passes always walk one-block tiles round-robin on a
+// persistent grid (a block stages the network again only when a tile reads another copy).
 extern "C" int mic_ensemble_set_schedule(mic_ensemble *E, int batched, int tile_mult, int persistent, int chunked) {
   if (!E || tile_mult < 1 || tile_mult > 64) return MIC_ERR_ARG;
   cudaSetDevice(E->device);

@@ -112,6 +112,7 @@ struct mic_ctx {
   mic::CreepConfig creep;
   mic::CreepCounters *d_creep;  // device counters of the last rheology pass
   float *mlp;                   // device surrogate parameters
+  unsigned long long mlp_key;   // content key of *mlp (0: not known)
   float *train_buf;             // training scratch (grown on demand)
   int64_t train_cap;
   int64_t n, cap;
@@ -158,7 +159,6 @@ struct mic_ctx {
   double *scr0, *scr1, *scr2;
   double *node_scr[6];  // nodal scratch (NX*NY each)
   void *adv_coef;       // per-cell bilinear coefficients of vx, vy, wxy for the advection (product build)
-  void *job_slots;      // one-job tables of the marker passes, one slot per pass (mic_job_slots_bytes)
   double *red_buf;     // reduction partials
   int red_cap;
   mic::Status *d_status;
@@ -268,8 +268,6 @@ bool mic_batch_empty(const mic_batch *b);
 void mic_batch_clear(mic_batch *b);
 // bytes of work table one ensemble step of n_members contexts needs at most
 size_t mic_batch_table_bound(int n_members);
-// bytes of a context's one-job tables (mic_ctx::job_slots)
-size_t mic_job_slots_bytes();
 // Segment seg (0 .. kStepSegments-1) of one step: the context's own launches up to and including
 // one marker pass, on its stream.  Segments 0 .. kStepSegments-1 in order are mic_step without its
 // residual read.  With b, the segment's marker pass joins the batch instead of being launched.

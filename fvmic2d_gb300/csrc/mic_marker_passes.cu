@@ -321,7 +321,8 @@ struct StrainCols {
 
 // updateMarkerStrainPressure (updateMarkerStrainPressure.c:131-306, non-TEXTURE branch)
 // one marker (the marker-pass kernel k_batched runs it over a table of jobs)
-__device__ __forceinline__ void strain_pressure_one(Params P, StrainCols c, Geo g, Nodal nd, double dt, int64_t n, Status *st, int64_t m) {
+__device__ __forceinline__ void strain_pressure_one(const Params &P, const StrainCols &c, const Geo &g,
+                                                    const Nodal &nd, double dt, int64_t n, Status *st, int64_t m) {
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
@@ -443,8 +444,9 @@ struct SubgridCols {
 // reuse (product build): dxx, dyy, dxy hold the nodal soxx, soyy, soxy interpolated at the
 // marker by the strain-rate pass of this step (same nodes, weights and order: the same values)
 // one marker (the marker-pass kernel k_batched runs it over a table of jobs)
-__device__ __forceinline__ void subgrid_stress_one(Params P, SubgridCols c, Geo g, Nodal nd, double dt, double D,
-                                         int64_t n, int reuse, int64_t m) {
+__device__ __forceinline__ void subgrid_stress_one(const Params &P, const SubgridCols &c, const Geo &g,
+                                                   const Nodal &nd, double dt, double D, int64_t n, int reuse,
+                                                   int64_t m) {
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
@@ -658,7 +660,8 @@ struct StressCols {
 
 // updateMarkerStress (updateMarkerStress.c:60-144)
 // one marker (the marker-pass kernel k_batched runs it over a table of jobs)
-__device__ __forceinline__ void update_stress_one(Params P, StressCols c, Geo g, Nodal nd, int64_t n, Status *st, int64_t m) {
+__device__ __forceinline__ void update_stress_one(const Params &P, const StressCols &c, const Geo &g, const Nodal &nd,
+                                                  int64_t n, Status *st, int64_t m) {
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
@@ -692,7 +695,7 @@ struct SubTCols {
 
 // subgridTemperatureChanges, first marker loop (subgridTemperatureChanges.c:45-70)
 // one marker (the marker-pass kernel k_batched runs it over a table of jobs)
-__device__ __forceinline__ void subgridT_markers_one(Params P, SubTCols c, Geo g, const double *__restrict__ Tn,
+__device__ __forceinline__ void subgridT_markers_one(const Params &P, const SubTCols &c, const Geo &g, const double *__restrict__ Tn,
                                    const double *__restrict__ rn, const double *__restrict__ cpn,
                                    const double *__restrict__ kn, double rho0, double D, double dt, int64_t n, int64_t m) {
   if (m >= n) return;
@@ -741,7 +744,7 @@ __global__ void k_subgridT_nodes(const double *thisT, const double *lastT, const
 
 // subgridTemperatureChanges, second marker loop (subgridTemperatureChanges.c:87-103)
 // one marker (the marker-pass kernel k_batched runs it over a table of jobs)
-__device__ __forceinline__ void subgridT_apply_one(Params P, SubTCols c, Geo g, const double *__restrict__ dT, double dt, int64_t n, int64_t m) {
+__device__ __forceinline__ void subgridT_apply_one(const Params &P, const SubTCols &c, const Geo &g, const double *__restrict__ dT, double dt, int64_t n, int64_t m) {
   if (m >= n) return;
   const int i = c.cellX[m], j = c.cellY[m];
   if (i == -1) return;
@@ -972,6 +975,7 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
       t = bil_eval(cwz, (size_t)j * (NX - 1) + i, mdx, mdy);
 #endif
     mwz[s] = t;
+#ifdef MIC_EXACT
     if (s < 2) {
       xcur = X0 + dt / 2 * mvx[s];
       ycur = Y0 + dt / 2 * mvy[s];
@@ -979,36 +983,59 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
       xcur = X0 + dt * mvx[s];
       ycur = Y0 + dt * mvy[s];
     }
+#else
+    // the product build's sums of products are written as FMAs (the same operations whichever
+    // kernel inlines this, and the fewest FP64 instructions)
+    if (s < 2) {
+      xcur = fma(0.5 * dt, mvx[s], X0);
+      ycur = fma(0.5 * dt, mvy[s], Y0);
+    } else if (s == 2) {
+      xcur = fma(dt, mvx[s], X0);
+      ycur = fma(dt, mvy[s], Y0);
+    }
+#endif
   }
 #ifdef MIC_EXACT
   const double VX = div6(mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]);
   const double VY = div6(mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]);
   const double w = div6(mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]);
-#else
-  const double inv6 = 0.16666666666666666;
-  const double VX = (mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]) * inv6;
-  const double VY = (mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]) * inv6;
-  const double w = (mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]) * inv6;
-#endif
   c.VX[m] = VX;
   c.VY[m] = VY;
   c.wxy[m] = w;
   c.X[m] = X0 + dt * VX;
   c.Y[m] = Y0 + dt * VY;
+#else
+  const double inv6 = 0.16666666666666666;
+  const double VX = (fma(2.0, mvx[2], fma(2.0, mvx[1], mvx[0])) + mvx[3]) * inv6;
+  const double VY = (fma(2.0, mvy[2], fma(2.0, mvy[1], mvy[0])) + mvy[3]) * inv6;
+  const double w = (fma(2.0, mwz[2], fma(2.0, mwz[1], mwz[0])) + mwz[3]) * inv6;
+  c.VX[m] = VX;
+  c.VY[m] = VY;
+  c.wxy[m] = w;
+  c.X[m] = fma(dt, VX, X0);
+  c.Y[m] = fma(dt, VY, Y0);
+#endif
   const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
   const double th = -w * dt;
 #ifdef MIC_EXACT
   const double ct = cos(th), st_ = sin(th), s2 = sin(2.0 * th), c2 = cos(2.0 * th);
-#else
-  double ct, st_, s2, c2;
-  small_angle_rotation(th, ct, st_, s2, c2);
-#endif
   const double nsxx = s11 * (ct * ct) + s22 * (st_ * st_) - s12 * s2;
   c.sxx[m] = nsxx;
   c.syy[m] = s11 * (st_ * st_) + s22 * (ct * ct) + s12 * s2;
   c.sxy[m] = 0.5 * (s11 - s22) * s2 + s12 * c2;
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   c.Eii[m] = c.Eii[m] + dt * sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
+#else
+  double ct, st_, s2, c2;
+  small_angle_rotation(th, ct, st_, s2, c2);
+  const double cc = ct * ct, ss = st_ * st_;
+  const double nsxx = fma(s11, cc, fma(s22, ss, -(s12 * s2)));
+  c.sxx[m] = nsxx;
+  c.syy[m] = fma(s11, ss, fma(s22, cc, s12 * s2));
+  c.sxy[m] = fma(0.5 * (s11 - s22), s2, s12 * c2);
+  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
+  c.Eii[m] = fma(dt, sqrt(fma(e12, e12, 0.5 * fma(e11, e11, e22 * e22))), c.Eii[m]);
+#endif
   return nsxx;
 }
 
@@ -1329,7 +1356,7 @@ struct SubTApplyOp {
   static __device__ __forceinline__ void flush(const Job &, Acc) {}
 };
 struct AdvectOp {
-  static constexpr int kMaxRegs = 64;
+  static constexpr int kMaxRegs = 80;
   using Job = AdvectJob;
   using Acc = long long;
   static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &a) {
@@ -1347,7 +1374,8 @@ struct AdvectOp {
 template <class Op>
 __global__ void __maxnreg__(Op::kMaxRegs) k_batched(const typename Op::Job *__restrict__ jobs,
                                                          const int *__restrict__ ts, int njobs, int ntiles,
-                                                         int tile_markers, int chunked) {
+                                                         int tile_markers, int chunked,
+                                                         const __grid_constant__ typename Op::Job one) {
   using Job = typename Op::Job;
   static_assert(sizeof(Job) % 8 == 0, "job records are whole 8-byte words");
   __shared__ unsigned long long sj[sizeof(Job) / 8];
@@ -1355,15 +1383,15 @@ __global__ void __maxnreg__(Op::kMaxRegs) k_batched(const typename Op::Job *__re
   const TileRange r = tile_range(ntiles, chunked);
   int cur = -1;
   for (int t = r.t; t < r.end; t += r.step) {
-    const int j = tile_job(ts, njobs, t);
+    const int j = jobs ? tile_job(ts, njobs, t) : 0;
     if (j != cur) {  // the tile's job into shared memory (block-uniform)
       __syncthreads();
-      const unsigned long long *src = reinterpret_cast<const unsigned long long *>(jobs + j);
-      for (int w = threadIdx.x; w < (int)(sizeof(Job) / 8); w += blockDim.x) sj[w] = __ldg(src + w);
+      const unsigned long long *src = reinterpret_cast<const unsigned long long *>(jobs ? jobs + j : &one);
+      for (int w = threadIdx.x; w < (int)(sizeof(Job) / 8); w += blockDim.x) sj[w] = src[w];
       __syncthreads();
       cur = j;
     }
-    const int64_t base = (int64_t)(t - __ldg(ts + j)) * tile_markers;
+    const int64_t base = (int64_t)(t - (jobs ? __ldg(ts + j) : 0)) * tile_markers;
     typename Op::Acc a{};
     for (int q = threadIdx.x; q < tile_markers; q += blockDim.x) Op::one(J, base + q, a);
     Op::flush(J, a);
@@ -1374,20 +1402,21 @@ __global__ void __maxnreg__(Op::kMaxRegs) k_batched(const typename Op::Job *__re
 // staged in shared memory again whenever a tile's member uses another network buffer.
 __global__ void __launch_bounds__(512) k_yield_fp32_batched(const YieldJob *__restrict__ jobs,
                                                                     const int *__restrict__ ts, int njobs,
-                                                                    int ntiles, int tile_markers, int chunked) {
+                                                                    int ntiles, int tile_markers, int chunked,
+                                                                    const __grid_constant__ YieldJob one) {
   __shared__ float w2s[kH * kH];
   const float *staged = nullptr;
   const TileRange r = tile_range(ntiles, chunked);
   for (int t = r.t; t < r.end; t += r.step) {
-    const int j = tile_job(ts, njobs, t);
-    const YieldJob &J = jobs[j];
+    const int j = jobs ? tile_job(ts, njobs, t) : 0;
+    const YieldJob &J = jobs ? jobs[j] : one;
     if (J.cfg.mlp != staged) {
       staged = J.cfg.mlp;
       __syncthreads();
       for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = staged[kOffW2 + q];
       __syncthreads();
     }
-    const int64_t base = (int64_t)(t - __ldg(ts + j)) * tile_markers;
+    const int64_t base = (int64_t)(t - (jobs ? __ldg(ts + j) : 0)) * tile_markers;
     int a = 0;
     for (int q = threadIdx.x; q < tile_markers; q += blockDim.x)
       if (yield_one<1>(J.c, J.M, J.O, J.cfg, J.dt, J.n, J.st, J.cc, J.limit, w2s, base + q)) a = 1;
@@ -1402,22 +1431,23 @@ __global__ void __launch_bounds__(512) k_yield_fp32_batched(const YieldJob *__re
 // timeout, if any, is counted on the member whose round gave up.
 __global__ void __launch_bounds__(tc::kTile) k_yield_tc_batched(const YieldJob *__restrict__ jobs,
                                                                 const int *__restrict__ ts, int njobs, int ntiles,
-                                                                int tile_markers, int chunked) {
+                                                                int tile_markers, int chunked,
+                                                                const __grid_constant__ YieldJob one) {
   extern __shared__ unsigned char dyn[];
   const TileRange r = tile_range(ntiles, chunked);
   if (r.t >= r.end) return;  // block-uniform, before any TMEM is taken
   tc::Block B;
-  const float *staged = jobs[tile_job(ts, njobs, r.t)].cfg.mlp;
+  const float *staged = jobs ? jobs[tile_job(ts, njobs, r.t)].cfg.mlp : one.cfg.mlp;
   tc::setup(B, dyn, staged);
   CreepCounters *gave_up = nullptr;
   for (int t = r.t; t < r.end; t += r.step) {
-    const int j = tile_job(ts, njobs, t);
-    const YieldJob &J = jobs[j];
+    const int j = jobs ? tile_job(ts, njobs, t) : 0;
+    const YieldJob &J = jobs ? jobs[j] : one;
     if (J.cfg.mlp != staged) {
       staged = J.cfg.mlp;
       tc::restage(B, staged);
     }
-    const int64_t base = (int64_t)(t - __ldg(ts + j)) * tile_markers;
+    const int64_t base = (int64_t)(t - (jobs ? __ldg(ts + j) : 0)) * tile_markers;
     int a = 0;
     for (int q = 0; q < tile_markers; q += tc::kTile) {
       const int pending = B.pending;
@@ -1426,29 +1456,12 @@ __global__ void __launch_bounds__(tc::kTile) k_yield_tc_batched(const YieldJob *
     }
     if (__syncthreads_or(a) && threadIdx.x == 0) atomicOr(&J.st->is_yielding, 1);
   }
-  tc::teardown(B, gave_up ? &gave_up->tc_drain_timeouts : &jobs[0].cc->tc_drain_timeouts);
-}
-
-// a one-job table for a context stepping alone: the job (a kernel argument) and its tile offsets
-template <class Job>
-__global__ void k_put_job(const __grid_constant__ Job J, Job *dst, int *ts, int ntiles) {
-  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&J);
-  unsigned long long *d = reinterpret_cast<unsigned long long *>(dst);
-  for (int w = threadIdx.x; w < (int)(sizeof(Job) / 8); w += blockDim.x) d[w] = src[w];
-  if (threadIdx.x == 0) {
-    ts[0] = 0;
-    ts[1] = ntiles;
-  }
+  tc::teardown(B, &(gave_up ? gave_up : (jobs ? jobs[0].cc : one.cc))->tc_drain_timeouts);
 }
 
 constexpr size_t kJobBytes[BP_COUNT] = {sizeof(RhoJob),    sizeof(YieldJob),  sizeof(YieldJob), sizeof(YieldJob),
                                         sizeof(YieldJob),  sizeof(StrainJob), sizeof(SubgridJob), sizeof(StressJob),
                                         sizeof(SubTJob),   sizeof(SubTApplyJob), sizeof(AdvectJob)};
-constexpr size_t max_job_bytes(int k = 0) {
-  return k == BP_COUNT ? 0 : (kJobBytes[k] > max_job_bytes(k + 1) ? kJobBytes[k] : max_job_bytes(k + 1));
-}
-// a context's one-job tables: per pass one slot, the job and then its two tile offsets
-constexpr size_t kJobSlotBytes = (max_job_bytes() + 16 + 255) / 256 * 256;
 constexpr size_t kTableAlign = 256;
 
 int batch_fail(cudaError_t e) { return mic_fail_cuda(nullptr, e); }
@@ -1484,73 +1497,66 @@ int pass_occupancy(int dev, int pass, int block) {
   return c;
 }
 
-template <class Op>
-void launch_generic(unsigned grid, int block, cudaStream_t s, const unsigned char *jobs, const int *ts, int nj,
-                    int ntiles, int tm, int chunked) {
-  k_batched<Op><<<grid, block, 0, s>>>(reinterpret_cast<const typename Op::Job *>(jobs), ts, nj, ntiles, tm, chunked);
+// pass p's kernel over a job table in device memory (jobs, ts), or over the single job `one`
+// passed as a kernel argument (jobs null).  block: tc::kTile for the tensor-core yield.
+template <class Job>
+const Job &job_arg(const void *one) {
+  static const Job zero{};
+  return one ? *static_cast<const Job *>(one) : zero;
 }
 
-// pass p's kernel over a job table in device memory (block: tc::kTile for the tensor-core yield)
+template <class Op>
+void launch_generic(unsigned grid, int block, cudaStream_t s, const unsigned char *jobs, const int *ts, int nj,
+                    int ntiles, int tm, int chunked, const void *one) {
+  using Job = typename Op::Job;
+  k_batched<Op><<<grid, block, 0, s>>>(reinterpret_cast<const Job *>(jobs), ts, nj, ntiles, tm, chunked,
+                                       job_arg<Job>(one));
+}
+
 cudaError_t launch_pass(int pass, unsigned grid, int block, cudaStream_t s, const unsigned char *jobs, const int *ts,
-                        int nj, int ntiles, int tm, int chunked) {
+                        int nj, int ntiles, int tm, int chunked, const void *one) {
   switch (pass) {
-    case BP_RHO: launch_generic<RhoOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
-    case BP_YIELD_PLAIN: launch_generic<YieldOp<2>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
-    case BP_YIELD_EXACT: launch_generic<YieldOp<0>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_RHO: launch_generic<RhoOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_YIELD_PLAIN: launch_generic<YieldOp<2>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_YIELD_EXACT: launch_generic<YieldOp<0>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
     case BP_YIELD_FP32:
       k_yield_fp32_batched<<<grid, block, 0, s>>>(reinterpret_cast<const YieldJob *>(jobs), ts, nj, ntiles, tm,
-                                                   chunked);
+                                                   chunked, job_arg<YieldJob>(one));
       break;
     case BP_YIELD_TC: {
       const cudaError_t e =
           cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem);
       if (e != cudaSuccess) return e;
       k_yield_tc_batched<<<grid, tc::kTile, tc::kDynSmem, s>>>(reinterpret_cast<const YieldJob *>(jobs), ts, nj,
-                                                                ntiles, tm, chunked);
+                                                                ntiles, tm, chunked, job_arg<YieldJob>(one));
       break;
     }
-    case BP_STRAIN: launch_generic<StrainOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
-    case BP_SUBGRID: launch_generic<SubgridOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
-    case BP_STRESS: launch_generic<StressOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
-    case BP_SUBT: launch_generic<SubTOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
-    case BP_SUBT_APPLY: launch_generic<SubTApplyOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
-    default: launch_generic<AdvectOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked); break;
+    case BP_STRAIN: launch_generic<StrainOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_SUBGRID: launch_generic<SubgridOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_STRESS: launch_generic<StressOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_SUBT: launch_generic<SubTOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_SUBT_APPLY: launch_generic<SubTApplyOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    default: launch_generic<AdvectOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
   }
   return cudaGetLastError();
 }
 
-// One context's marker pass: its job into the context's slot for the pass (a one-block kernel),
-// then the pass kernel over that one-job table -- tiles of one block, a persistent grid walking
-// them round-robin (the tensor-core yield: the context's persistent tensor-core grid).
+// One context's marker pass: the pass kernel with the context's job as its argument -- one block
+// per tile of one block's worth of markers (the tensor-core yield: the context's persistent
+// tensor-core grid, round-robin).
 template <class Job>
 int solo_pass(mic_ctx *ctx, int pass, const Job &J, int block, const char *name) {
   const bool tcp = pass == BP_YIELD_TC;
   if (tcp) block = tc::kTile;
-  unsigned char *slot = static_cast<unsigned char *>(ctx->job_slots) + (size_t)pass * kJobSlotBytes;
-  int *ts = reinterpret_cast<int *>(slot + kJobSlotBytes - 16);
   const int64_t nt = (J.n + block - 1) / block;
   if (nt > 0x7fffffff) return MIC_ERR_ARG;
   const int ntiles = (int)nt;
-  {
-    MIC_KERNEL(ctx, "k_put_job");
-    k_put_job<Job><<<1, 32, 0, ctx->stream>>>(J, reinterpret_cast<Job *>(slot), ts, ntiles);
-  }
-  MIC_CUDA_TRY(cudaGetLastError());
-  int64_t grid = ntiles;
-  if (tcp) {
-    grid = mic_creep_tc_blocks(ctx, J.n);
-  } else {
-    int sms = 0;
-    MIC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    const int64_t g = (int64_t)(sms > 0 ? sms : 1) * pass_occupancy(ctx->device, pass, block);
-    if (g < grid) grid = g;
-  }
+  int64_t grid = tcp ? mic_creep_tc_blocks(ctx, J.n) : ntiles;
   if (grid < 1) grid = 1;
   MIC_KERNEL(ctx, name);
-  MIC_CUDA_TRY(launch_pass(pass, (unsigned)grid, block, ctx->stream, slot, ts, 1, ntiles, block, 0));
+  MIC_CUDA_TRY(launch_pass(pass, (unsigned)grid, block, ctx->stream, nullptr, nullptr, 1, ntiles, block, 0, &J));
   return MIC_OK;
 }
-
 }  // namespace
 
 #define CHECK_CTX()                 \
@@ -1560,6 +1566,16 @@ int solo_pass(mic_ctx *ctx, int pass, const Job &J, int block, const char *name)
 struct mic_batch {
   std::vector<unsigned char> jobs[BP_COUNT];  // job records of each pass, in the order added
   std::vector<int64_t> n[BP_COUNT];           // markers of each job
+  // surrogate networks of the batch by content key: members holding the same network read one
+  // copy of it, so a block of the batched yield pass stages it once
+  std::vector<std::pair<unsigned long long, const float *>> nets;
+  const float *shared_net(unsigned long long key, const float *own) {
+    if (!key) return own;
+    for (const auto &kv : nets)
+      if (kv.first == key) return kv.second;
+    nets.push_back({key, own});
+    return own;
+  }
   template <class J>
   int add(int pass, const J &job, int64_t markers) {
     std::vector<unsigned char> &v = jobs[pass];
@@ -1612,10 +1628,13 @@ static int yield_launch(mic_ctx *ctx, double dt, bool limit = false, mic_batch *
   const int mode = ctx->creep.mlp ? ctx->creep.mode : 0;
   bool law7 = false;
   for (int k = 0; k < MIC_MAXMAT; ++k) law7 = law7 || ctx->mat.hasEtaT[k] == 7;
-  const YieldJob J = {yield_cols(ctx), ctx->mat,    ctx->opt,     ctx->creep,   dt,
-                      ctx->n,          ctx->d_status, ctx->d_creep, limit ? 1 : 0};
+  YieldJob J = {yield_cols(ctx), ctx->mat,    ctx->opt,     ctx->creep,   dt,
+                ctx->n,          ctx->d_status, ctx->d_creep, limit ? 1 : 0};
   const int pass = !law7 ? BP_YIELD_PLAIN : mode == 0 ? BP_YIELD_EXACT : mode == 1 ? BP_YIELD_FP32 : BP_YIELD_TC;
-  if (b) return b->add(pass, J, ctx->n);
+  if (b) {
+    if (pass == BP_YIELD_FP32 || pass == BP_YIELD_TC) J.cfg.mlp = b->shared_net(ctx->mlp_key, J.cfg.mlp);
+    return b->add(pass, J, ctx->n);
+  }
   if (pass == BP_YIELD_PLAIN || pass == BP_YIELD_EXACT) return solo_pass(ctx, pass, J, tuned_block(ctx, TU_YIELD), "k_yield");
   if (pass == BP_YIELD_FP32) return solo_pass(ctx, pass, J, kBatchBlock, "k_yield_surrogate_fp32");
   return solo_pass(ctx, pass, J, tc::kTile, "k_yield_tc");
@@ -2158,6 +2177,7 @@ void mic_batch_clear(mic_batch *b) {
     b->jobs[p].clear();
     b->n[p].clear();
   }
+  b->nets.clear();
 }
 bool mic_batch_empty(const mic_batch *b) {
   for (int p = 0; p < BP_COUNT; ++p)
@@ -2165,8 +2185,6 @@ bool mic_batch_empty(const mic_batch *b) {
   return true;
 }
 
-
-size_t mic_job_slots_bytes() { return (size_t)BP_COUNT * kJobSlotBytes; }
 
 size_t mic_batch_table_bound(int n_members) {
   size_t per = sizeof(RhoJob) + sizeof(YieldJob) + sizeof(StrainJob) + sizeof(SubgridJob) + sizeof(StressJob) +
@@ -2187,11 +2205,13 @@ int mic_batch_launch(mic_batch *b, const BatchShape *shape, unsigned char *host_
     if (nj == 0) continue;
     const bool tcp = p == BP_YIELD_TC;
     const int block = tcp ? tc::kTile : kBatchBlock;
-    // a job switch restages the network in the surrogate passes: those walk contiguous runs
-    const bool restages = tcp || p == BP_YIELD_FP32;
-    const int persistent = restages ? 1 : shape[p].persistent;
-    const int chunked = restages ? 1 : shape[p].chunked;
-    const int mult = shape[p].mult < 1 ? 1 : (shape[p].mult > 64 ? 64 : shape[p].mult);
+    // the surrogate passes stage the network per block (and again when a tile's job reads another
+    // copy): a persistent grid walking tiles of one block round-robin, as a context alone runs
+    // them, which also spreads the markers' uneven solve costs over the blocks
+    const bool surrogate = tcp || p == BP_YIELD_FP32;
+    const int persistent = surrogate ? 1 : shape[p].persistent;
+    const int chunked = surrogate ? 0 : shape[p].chunked;
+    const int mult = surrogate ? 1 : (shape[p].mult < 1 ? 1 : (shape[p].mult > 64 ? 64 : shape[p].mult));
     const int tm = block * mult;
     std::vector<int> ts(nj + 1);
     ts[0] = 0;
@@ -2226,7 +2246,7 @@ int mic_batch_launch(mic_batch *b, const BatchShape *shape, unsigned char *host_
       if (g < grid) grid = g;
     }
     if (grid < 1) grid = 1;
-    if ((ce = launch_pass(p, (unsigned)grid, block, s, dj, dts, nj, ntiles, tm, chunked)) != cudaSuccess) {
+    if ((ce = launch_pass(p, (unsigned)grid, block, s, dj, dts, nj, ntiles, tm, chunked, nullptr)) != cudaSuccess) {
       status = batch_fail(ce);
       break;
     }

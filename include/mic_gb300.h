@@ -402,7 +402,8 @@ int mic_ensemble_synchronize(mic_ensemble *ens);
  * of tile_mult (1..64) blocks' worth and run one block per tile (persistent 0) or a persistent
  * grid of SMs x resident blocks whose blocks take contiguous runs of tiles (chunked 1) or tiles
  * round-robin (chunked 0); tiles are ordered member by member in the issue order.  The surrogate
- * yield passes always use a persistent grid of contiguous runs.  Default: batched, 4, 1, 1. */
+ * yield passes always use a persistent grid walking one-block tiles round-robin (members whose
+ * networks are equal read one copy).  Default: batched, 4, 1, 1. */
 int mic_ensemble_set_schedule(mic_ensemble *ens, int batched, int tile_mult, int persistent, int chunked);
 int mic_ensemble_get_schedule(mic_ensemble *ens, int *batched, int *tile_mult, int *persistent, int *chunked);
 /* Launch shapes and member schedule measured on the ensemble (new): mic_autotune on every member,
