@@ -728,13 +728,16 @@ def ensemble_leg(args, local):
     ms = (time.perf_counter() - t0) * 1e3 / seq_steps
     out["sequential"] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
                          "steps": seq_steps}
-    for mode, batched in (("per_member", False), ("batched", True)):
-        E.set_schedule(batched=batched)
+    # per-member kernels; batched marker passes in the default four groups and in one group
+    for mode, groups in (("per_member", 0), ("batched", 4), ("batched_1group", 1)):
+        E.set_schedule(groups=groups, chunked=2)
         for label, graph in (("streams", False), ("graph", True)):
             ms, kps = _time_ensemble(E, es, dts, steps, graph)
             out[mode + "_" + label] = {"value": n_total / (ms * 1e-3), "unit": "markers/s", "ms_per_step": ms,
                                        "kernels_per_step": kps}
-    out["speedup_batched_vs_per_member_graph"] = out["batched_graph"]["value"] / out["per_member_graph"]["value"]
+    for mode in ("batched", "batched_1group"):
+        out["speedup_%s_vs_per_member_graph" % mode] = (out[mode + "_graph"]["value"] /
+                                                         out["per_member_graph"]["value"])
     out["speedup_graph_vs_sequential"] = out["batched_graph"]["value"] / out["sequential"]["value"]
     # members' launch shapes, the member order and the batching schedule from mic_ensemble_autotune
     # (state restored by it), then the captured steps timed again
@@ -760,7 +763,7 @@ def ice_ensemble_leg(args, local):
     128^2 to 1024 x 256 cells, 16 markers per cell, law 7 with per-marker grain sizes,
     Drucker-Prager yield), 50 captured-graph steps with the exact creep solve and with the
     tensor-core surrogate (one network trained once, shared by all members), each per-member and
-    batched."""
+    batched (four batch groups, the default, and one group)."""
     import torch
 
     from fvmic2d_gb300 import gpu
@@ -791,8 +794,8 @@ def ice_ensemble_leg(args, local):
     for label, mode in (("plain", 0), ("surrogate_tc", 2)):
         for P in members:
             P.creep_configure(mode=mode, tol=2e-14, maxit=60, polish_iters=3, polish_tol=1e-7)
-        for sched, batched in (("per_member", False), ("batched", True)):
-            E.set_schedule(batched=batched)
+        for sched, groups in (("per_member", 0), ("batched", 4), ("batched_1group", 1)):
+            E.set_schedule(groups=groups, chunked=2)
             ms, kps = _time_ensemble(E, es, dts, steps, True)
             st = [P.creep_stats() for P in members]
             mk = sum(x["markers"] for x in st)
@@ -802,12 +805,13 @@ def ice_ensemble_leg(args, local):
                                         "fallbacks_per_step": sum(x["fallbacks"] for x in st),
                                         "max_residual": max(x["max_residual"] for x in st),
                                         "tc_timeouts": sum(x["tc_timeouts"] for x in st)}
-    for sched in ("per_member", "batched"):
+    for sched in ("per_member", "batched", "batched_1group"):
         out["speedup_surrogate_vs_plain_" + sched] = (out["surrogate_tc_" + sched]["value"] /
                                                       out["plain_" + sched]["value"])
     for label in ("plain", "surrogate_tc"):
-        out["speedup_batched_vs_per_member_" + label] = (out[label + "_batched"]["value"] /
-                                                         out[label + "_per_member"]["value"])
+        for sched in ("batched", "batched_1group"):
+            out["speedup_%s_vs_per_member_%s" % (sched, label)] = (out[label + "_" + sched]["value"] /
+                                                                   out[label + "_per_member"]["value"])
     E.close()
     for P in members:
         P.close()

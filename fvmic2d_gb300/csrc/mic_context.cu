@@ -124,6 +124,7 @@ static void free_ctx(mic_ctx *ctx) {
   for (int f = 0; f < MIC_NF_COUNT; ++f) cudaFree(ctx->nodal[f]);
   for (int f = 0; f < 6; ++f) cudaFree(ctx->node_scr[f]);
   cudaFree(ctx->adv_coef);
+  cudaFree(ctx->tickets);
   cudaFree(ctx->grid_buf);
   cudaFree(ctx->bits_buf);
   cudaFree(ctx->spacing_buf);
@@ -348,6 +349,7 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
   ALLOC(ctx->red_buf, sizeof(double) * ctx->red_cap);
   ALLOC(ctx->d_creep, sizeof(CreepCounters));
   cudaMemset(ctx->d_creep, 0, sizeof(CreepCounters));
+  ALLOC(ctx->tickets, sizeof(unsigned int) * BP_COUNT);
   ALLOC(ctx->d_status, sizeof(Status));
   cudaMemset(ctx->d_status, 0, sizeof(Status));
   if (cudaHostAlloc((void **)&ctx->h_status, sizeof(Status), cudaHostAllocDefault) != cudaSuccess) {

@@ -5,16 +5,18 @@
 // launches as mic_step without a residual read, so nothing waits on the host) and joins back.
 // Small members then overlap on the GPU instead of running one after another.
 //
-// Batched (the default): a step's marker passes run as one kernel per pass over all members
+// Batched (the default): a step's marker passes run as one kernel per pass over many members
 // instead of one per member.  A step is cut into segments at its marker passes
 // (mic_step_segment); each segment's own launches (binning, projections, node kernels) are
-// issued on every member's stream, the members join the ensemble stream, one batched kernel per
-// pass walks the work table of (member, tile) pairs, and the members fork again.  The table (the
+// issued on every member's stream, the members join their batch group's stream, one batched
+// kernel per pass walks the group's work table of (member, tile) pairs, and the members fork
+// again.  With several groups (members dealt by marker count), one group's batched passes
+// overlap the other groups' member work, since a pass waits for its slowest member.  The table (the
 // members' launch arguments and their tile offsets) is written on the host and copied into a
 // device buffer: once per captured graph (the graph reads it at every replay), or by an
 // asynchronous copy before each pass of a step run directly (two alternating buffers).  The
 // tile size, the persistent / one-tile-per-block grid and the block-to-tile schedule come from
-// mic_ensemble_set_schedule or mic_ensemble_autotune.  Per-member (batched off): each member's
+// mic_ensemble_set_schedule or mic_ensemble_autotune.  Per-member (no groups): each member's
 // whole step on its own stream, between one fork and one join.
 //
 // With graphs on, the fork / members / join sequence is captured once into CUDA graphs and each
@@ -32,6 +34,8 @@
 #include <vector>
 
 #include "mic_internal.cuh"
+
+constexpr int kMaxGroups = 8;
 
 struct mic_ensemble {
   int device;
@@ -51,10 +55,13 @@ struct mic_ensemble {
   long long graph_kernels[2];  // kernel launches inside each graph
   long long launches;          // kernel launches issued through this ensemble
   std::vector<int> order;      // members in the order their steps are issued (and captured)
-  // batched marker passes
-  int batched;
+  // batched marker passes: `groups` batch groups (0: per-member steps), each with its own stream,
+  // fork event, completion event and batch; members are dealt to the groups by marker count
+  int groups;
   mic::BatchShape shape[mic::BP_COUNT];
-  mic_batch *batch;
+  cudaStream_t gstream[kMaxGroups];
+  cudaEvent_t gfork[kMaxGroups], gdone[kMaxGroups];
+  mic_batch *gbatch[kMaxGroups];
   size_t table_cap;
   // work tables: slot 0, 1 the captured graphs of either parity; 2, 3 steps run directly (in turn)
   unsigned char *h_table[4], *d_table[4];
@@ -66,8 +73,12 @@ struct mic_ensemble {
 
 constexpr int kSlotDirect = 2;
 // default walk of a batched pass: tiles of 4 blocks' worth of markers, persistent grid, blocks
-// taking contiguous runs of tiles
-constexpr mic::BatchShape kDefaultShape = {4, 1, 1};
+// taking the next tile from a shared counter
+constexpr mic::BatchShape kDefaultShape = {4, 1, 2};
+// default batch groups: a pass waits for its group's slowest member, and the tensor-core yield
+// pass fills every SM's registers, so a single group leaves the other streams' memory-bound work
+// no room beside it; four groups interleave their phases
+constexpr int kDefaultGroups = 4;
 
 namespace {
 
@@ -78,7 +89,9 @@ int fail(cudaError_t e) {
 
 int ensure_tables(mic_ensemble *E) {
   if (E->h_table[0]) return MIC_OK;
-  E->table_cap = mic_batch_table_bound(E->n);
+  // every group's table in its own region: at most the whole ensemble's bound plus one empty
+  // table's overhead per further group
+  E->table_cap = mic_batch_table_bound(E->n) + kMaxGroups * mic_batch_table_bound(0);
   for (int k = 0; k < 4; ++k) {
     cudaError_t ce = cudaHostAlloc((void **)&E->h_table[k], E->table_cap, cudaHostAllocDefault);
     if (ce == cudaSuccess) ce = cudaMalloc((void **)&E->d_table[k], E->table_cap);
@@ -87,23 +100,46 @@ int ensure_tables(mic_ensemble *E) {
   return MIC_OK;
 }
 
-cudaError_t join_members(mic_ensemble *E) {
+// members dealt to the batch groups: largest marker count first, each to the group with the
+// fewest markers so far (ties: the lower group); each group keeps the issue order
+std::vector<std::vector<int>> group_members(const mic_ensemble *E) {
+  const int G = E->groups < 1 ? 1 : (E->groups > E->n ? E->n : E->groups);
+  std::vector<int> by_size = E->order;
+  std::stable_sort(by_size.begin(), by_size.end(), [&](int a, int b) { return E->m[a]->n > E->m[b]->n; });
+  std::vector<int64_t> load(G, 0);
+  std::vector<int> group_of(E->n, 0);
+  for (int i : by_size) {
+    int g = 0;
+    for (int h = 1; h < G; ++h)
+      if (load[h] < load[g]) g = h;
+    group_of[i] = g;
+    load[g] += E->m[i]->n;
+  }
+  std::vector<std::vector<int>> out(G);
+  for (int i : E->order) out[group_of[i]].push_back(i);
+  return out;
+}
+
+cudaError_t join_group(mic_ensemble *E, const std::vector<int> &mem, cudaStream_t s) {
   cudaError_t ce = cudaSuccess;
-  for (int i = 0; i < E->n && ce == cudaSuccess; ++i) {
-    ce = cudaEventRecord(E->join[i], E->m[i]->stream);
-    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(E->stream, E->join[i], 0);
+  for (size_t k = 0; k < mem.size() && ce == cudaSuccess; ++k) {
+    ce = cudaEventRecord(E->join[mem[k]], E->m[mem[k]]->stream);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(s, E->join[mem[k]], 0);
   }
   return ce;
 }
 
-cudaError_t fork_members(mic_ensemble *E) {
-  cudaError_t ce = cudaEventRecord(E->fork, E->stream);
-  for (int i = 0; i < E->n && ce == cudaSuccess; ++i) ce = cudaStreamWaitEvent(E->m[i]->stream, E->fork, 0);
+cudaError_t fork_group(mic_ensemble *E, const std::vector<int> &mem, cudaStream_t s, cudaEvent_t ev) {
+  cudaError_t ce = cudaEventRecord(ev, s);
+  for (size_t k = 0; k < mem.size() && ce == cudaSuccess; ++k) ce = cudaStreamWaitEvent(E->m[mem[k]]->stream, ev, 0);
   return ce;
 }
 
-// One step with batched marker passes; its work table goes to `slot` (a graph being captured,
-// or kSlotDirect: the next direct buffer, copied inside the step).
+// One step with batched marker passes; its work tables go to `slot` (a graph being captured, or
+// kSlotDirect: the next direct buffer, copied inside the step), one region per group.  Every
+// group runs its own chain -- its members' segments on their streams, a join into the group
+// stream, the batched passes, a fork back -- beside the other groups; the ensemble stream forks
+// the groups at the start and joins them at the end.
 int issue_batched(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub, int slot) {
   int e = ensure_tables(E);
   if (e) return e;
@@ -117,33 +153,53 @@ int issue_batched(mic_ensemble *E, const double *dt_disp, const double *dt_therm
     if (E->table_ev_live[ev] && (ce = cudaEventSynchronize(E->table_ev[ev])) != cudaSuccess) return fail(ce);
   }
   const bool copy = ev >= 0;
-  if ((ce = fork_members(E)) != cudaSuccess) return fail(ce);
-  size_t off = 0;
-  for (int seg = 0; seg < mic::kStepSegments && !e; ++seg) {
-    for (int k = 0; k < E->n && !e; ++k) {
-      const int i = E->order[k];
-      mic_ctx *c = E->m[i];
-#ifdef MIC_EXACT
-      const int wz_known = 0;
-#else
-      const int wz_known = c->n > 0;  // as mic_step
-#endif
-      const long long l0 = c->launches;
-      e = mic_step_segment(c, seg, dt_disp[i], dt_thermal[i], sub, wz_known, E->batch);
-      E->launches += c->launches - l0;
-    }
-    if (e || mic_batch_empty(E->batch)) continue;
-    if ((ce = join_members(E)) != cudaSuccess) {
-      e = fail(ce);
-      break;
-    }
-    e = mic_batch_launch(E->batch, E->shape, E->h_table[slot], E->d_table[slot], &off, E->table_cap, copy ? 1 : 0,
-                         E->stream, &E->launches);
-    if (!e && (ce = fork_members(E)) != cudaSuccess) e = fail(ce);
+  const std::vector<std::vector<int>> gm = group_members(E);
+  const int G = (int)gm.size();
+  std::vector<size_t> off(G), end(G);
+  size_t base = 0;
+  for (int g = 0; g < G; ++g) {
+    off[g] = base;
+    base += mic_batch_table_bound((int)gm[g].size());
+    end[g] = base;
   }
-  mic_batch_clear(E->batch);
-  E->table_used[slot] = off;
-  if ((ce = join_members(E)) != cudaSuccess && !e) e = fail(ce);
+  if ((ce = cudaEventRecord(E->fork, E->stream)) != cudaSuccess) return fail(ce);
+  for (int g = 0; g < G && !e; ++g) {
+    if ((ce = cudaStreamWaitEvent(E->gstream[g], E->fork, 0)) != cudaSuccess ||
+        (ce = fork_group(E, gm[g], E->gstream[g], E->gfork[g])) != cudaSuccess)
+      e = fail(ce);
+  }
+  for (int seg = 0; seg < mic::kStepSegments && !e; ++seg) {
+    for (int g = 0; g < G && !e; ++g) {
+      for (size_t k = 0; k < gm[g].size() && !e; ++k) {
+        const int i = gm[g][k];
+        mic_ctx *c = E->m[i];
+#ifdef MIC_EXACT
+        const int wz_known = 0;
+#else
+        const int wz_known = c->n > 0;  // as mic_step
+#endif
+        const long long l0 = c->launches;
+        e = mic_step_segment(c, seg, dt_disp[i], dt_thermal[i], sub, wz_known, E->gbatch[g]);
+        E->launches += c->launches - l0;
+      }
+      if (e || mic_batch_empty(E->gbatch[g])) continue;
+      if ((ce = join_group(E, gm[g], E->gstream[g])) != cudaSuccess) {
+        e = fail(ce);
+        break;
+      }
+      // the group's region is sized for its members: the table cannot run into the next group's
+      e = mic_batch_launch(E->gbatch[g], E->shape, E->h_table[slot], E->d_table[slot], &off[g], end[g],
+                           copy ? 1 : 0, E->gstream[g], &E->launches);
+      if (!e && (ce = fork_group(E, gm[g], E->gstream[g], E->gfork[g])) != cudaSuccess) e = fail(ce);
+    }
+  }
+  for (int g = 0; g < G; ++g) {
+    mic_batch_clear(E->gbatch[g]);
+    if ((ce = join_group(E, gm[g], E->gstream[g])) != cudaSuccess && !e) e = fail(ce);
+    if ((ce = cudaEventRecord(E->gdone[g], E->gstream[g])) != cudaSuccess && !e) e = fail(ce);
+    if ((ce = cudaStreamWaitEvent(E->stream, E->gdone[g], 0)) != cudaSuccess && !e) e = fail(ce);
+  }
+  E->table_used[slot] = base;
   if (copy && !e) {
     if ((ce = cudaEventRecord(E->table_ev[ev], E->stream)) != cudaSuccess) return fail(ce);
     E->table_ev_live[ev] = 1;
@@ -153,7 +209,7 @@ int issue_batched(mic_ensemble *E, const double *dt_disp, const double *dt_therm
 
 // fork, every member's step, join: all asynchronous on the ensemble stream's timeline
 int issue(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, int sub, int slot = kSlotDirect) {
-  if (E->batched) return issue_batched(E, dt_disp, dt_thermal, sub, slot);
+  if (E->groups > 0) return issue_batched(E, dt_disp, dt_thermal, sub, slot);
   cudaError_t ce = cudaEventRecord(E->fork, E->stream);
   if (ce != cudaSuccess) return fail(ce);
   for (int k = 0; k < E->n; ++k) {
@@ -239,7 +295,7 @@ int capture(mic_ensemble *E, const double *dt_disp, const double *dt_thermal, in
     }
     // the graph's batched kernels read the work table written while it was captured: copy it
     // into the graph's own device buffer now (nothing in flight reads that buffer)
-    if (E->batched && E->table_used[q] > 0 &&
+    if (E->groups > 0 && E->table_used[q] > 0 &&
         (ce = cudaMemcpy(E->d_table[q], E->h_table[q], E->table_used[q], cudaMemcpyHostToDevice)) != cudaSuccess) {
       cudaGraphExecDestroy(E->exec[q]);
       if (q == 1) cudaGraphExecDestroy(E->exec[0]);
@@ -277,14 +333,18 @@ extern "C" int mic_ensemble_create(mic_ensemble **out, mic_ctx *const *members, 
   E->join.assign(n_members, nullptr);
   E->order.resize(n_members);
   for (int i = 0; i < n_members; ++i) E->order[i] = i;
-  E->batched = 1;
+  E->groups = kDefaultGroups;
   for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = kDefaultShape;
-  E->batch = mic_batch_new();
   cudaSetDevice(E->device);
-  bool ok = E->batch && cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) == cudaSuccess &&
+  bool ok = cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&E->fork, cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreateWithFlags(&E->table_ev[0], cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreateWithFlags(&E->table_ev[1], cudaEventDisableTiming) == cudaSuccess;
+  for (int g = 0; ok && g < kMaxGroups; ++g)
+    ok = (E->gbatch[g] = mic_batch_new()) != nullptr &&
+         cudaStreamCreateWithFlags(&E->gstream[g], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&E->gfork[g], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&E->gdone[g], cudaEventDisableTiming) == cudaSuccess;
   for (int i = 0; ok && i < n_members; ++i)
     ok = cudaEventCreateWithFlags(&E->join[i], cudaEventDisableTiming) == cudaSuccess;
   if (!ok) {
@@ -309,8 +369,13 @@ extern "C" int mic_ensemble_destroy(mic_ensemble *E) {
     if (E->h_table[k]) cudaFreeHost(E->h_table[k]);
     if (E->d_table[k]) cudaFree(E->d_table[k]);
   }
+  for (int g = 0; g < kMaxGroups; ++g) {
+    if (E->gstream[g]) cudaStreamDestroy(E->gstream[g]);
+    if (E->gfork[g]) cudaEventDestroy(E->gfork[g]);
+    if (E->gdone[g]) cudaEventDestroy(E->gdone[g]);
+    mic_batch_free(E->gbatch[g]);
+  }
   if (E->stream) cudaStreamDestroy(E->stream);
-  mic_batch_free(E->batch);
   delete E;
   return MIC_OK;
 }
@@ -371,24 +436,27 @@ extern "C" int mic_ensemble_get_stream(mic_ensemble *E, void **stream) {
   return MIC_OK;
 }
 
-// How a step runs its marker passes: batched (1: one kernel per pass over all members; 0: each
-// member's own kernels on its stream), and for the batched kernels the tile size in blocks'
-// worth of markers, persistent grid or one block per tile, and contiguous runs of tiles per
-// block or round-robin.  The surrogate passes always walk one-block tiles round-robin on a
-// persistent grid (a block stages the network again only when a tile reads another copy).
-extern "C" int mic_ensemble_set_schedule(mic_ensemble *E, int batched, int tile_mult, int persistent, int chunked) {
-  if (!E || tile_mult < 1 || tile_mult > 64) return MIC_ERR_ARG;
+// How a step runs its marker passes: `groups` batch groups (0: each member's own kernels on its
+// stream; 1..kMaxGroups: members dealt to that many groups by marker count, one kernel per pass
+// per group), and for the batched kernels the tile size in blocks' worth of markers, persistent
+// grid or one block per tile, and on a persistent grid the walk: tiles round-robin (chunked 0),
+// one contiguous run per block (1) or the next tile from a shared counter (2).  The surrogate
+// passes always take one-block tiles from a counter on a persistent grid (a block stages the
+// network again only when a tile reads another copy).
+extern "C" int mic_ensemble_set_schedule(mic_ensemble *E, int groups, int tile_mult, int persistent, int chunked) {
+  if (!E || groups < 0 || groups > kMaxGroups || tile_mult < 1 || tile_mult > 64 || chunked < 0 || chunked > 2)
+    return MIC_ERR_ARG;
   cudaSetDevice(E->device);
   drop_graphs(E);
-  E->batched = batched ? 1 : 0;
-  for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = {tile_mult, persistent ? 1 : 0, chunked ? 1 : 0};
+  E->groups = groups;
+  for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = {tile_mult, persistent ? 1 : 0, chunked};
   return MIC_OK;
 }
 
-extern "C" int mic_ensemble_get_schedule(mic_ensemble *E, int *batched, int *tile_mult, int *persistent,
+extern "C" int mic_ensemble_get_schedule(mic_ensemble *E, int *groups, int *tile_mult, int *persistent,
                                          int *chunked) {
   if (!E) return MIC_ERR_ARG;
-  if (batched) *batched = E->batched;
+  if (groups) *groups = E->groups;
   if (tile_mult) *tile_mult = E->shape[0].mult;
   if (persistent) *persistent = E->shape[0].persistent;
   if (chunked) *chunked = E->shape[0].chunked;
@@ -419,19 +487,20 @@ extern "C" int mic_ensemble_autotune(mic_ensemble *E, const double *dt_disp, con
   std::stable_sort(small.begin(), small.end(), [&](int a, int b) { return E->m[a]->n < E->m[b]->n; });
   struct Cand {
     std::vector<int> order;
-    int batched;
+    int groups;
     mic::BatchShape shape;
   };
-  // per-member steps in three issue orders, then batched passes over the table in two member
-  // orders and four walks (one block per tile; persistent round-robin; persistent contiguous
-  // runs of two tile sizes)
+  // per-member steps in three issue orders, then batched passes in 1, 2, 4 and 8 groups, each
+  // with three walks (one block per tile; persistent grids over tiles of four blocks' worth taken
+  // as contiguous runs or from a shared counter)
   std::vector<Cand> cand;
   for (const auto *o : {&given, &big, &small}) cand.push_back({*o, 0, kDefaultShape});
-  const mic::BatchShape walks[4] = {{1, 0, 0}, {4, 1, 0}, {4, 1, 1}, {16, 1, 1}};
-  for (const auto *o : {&given, &big})
-    for (const auto &w : walks) cand.push_back({*o, 1, w});
+  const mic::BatchShape walks[3] = {{1, 0, 0}, {4, 1, 1}, {4, 1, 2}};
+  for (int g = 1; g <= kMaxGroups; g *= 2)
+    if (g == 1 || g <= E->n)
+      for (const auto &w : walks) cand.push_back({given, g, w});
   const std::vector<int> before = E->order;
-  const int batched_before = E->batched;
+  const int groups_before = E->groups;
   mic::BatchShape shape_before[mic::BP_COUNT];
   for (int p = 0; p < mic::BP_COUNT; ++p) shape_before[p] = E->shape[p];
   int best = -1;
@@ -440,7 +509,7 @@ extern "C" int mic_ensemble_autotune(mic_ensemble *E, const double *dt_disp, con
   if (!e && (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess)) e = MIC_ERR_CUDA;
   for (int c = 0; c < (int)cand.size() && !e; ++c) {
     E->order = cand[c].order;
-    E->batched = cand[c].batched;
+    E->groups = cand[c].groups;
     for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = cand[c].shape;
     drop_graphs(E);
     for (int i = 0; i < E->n && !e; ++i) e = mic_state_restore(E->m[i], saved[i]);
@@ -466,11 +535,11 @@ extern "C" int mic_ensemble_autotune(mic_ensemble *E, const double *dt_disp, con
   drop_graphs(E);
   if (!e && best >= 0) {
     E->order = cand[best].order;
-    E->batched = cand[best].batched;
+    E->groups = cand[best].groups;
     for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = cand[best].shape;
   } else {
     E->order = before;
-    E->batched = batched_before;
+    E->groups = groups_before;
     for (int p = 0; p < mic::BP_COUNT; ++p) E->shape[p] = shape_before[p];
   }
   int e2 = MIC_OK;

@@ -159,6 +159,7 @@ struct mic_ctx {
   double *scr0, *scr1, *scr2;
   double *node_scr[6];  // nodal scratch (NX*NY each)
   void *adv_coef;       // per-cell bilinear coefficients of vx, vy, wxy for the advection (product build)
+  unsigned int *tickets;  // per marker pass: the tile counter of a dynamic walk (mic_batch_launch's walk 2)
   double *red_buf;     // reduction partials
   int red_cap;
   mic::Status *d_status;

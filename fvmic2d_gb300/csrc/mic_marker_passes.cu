@@ -1266,22 +1266,55 @@ __device__ __forceinline__ int tile_job(const int *__restrict__ ts, int njobs, i
   return lo;
 }
 
-// this block's tiles: [t, end) with stride step
-struct TileRange {
-  int t, end, step;
+// How a block walks the tiles (block-uniform): walk 0 round-robin (tiles blockIdx.x, + gridDim.x,
+// ...), 1 one contiguous run per block, 2 each block takes the next tile from a counter the grid
+// shares (*ticket, 0 at launch): blocks that start late (other streams' kernels holding SMs) or
+// meet costly markers take fewer tiles.
+struct TileWalk {
+  int first, end, step;
+  unsigned int *ticket;  // walk 2
 };
-__device__ __forceinline__ TileRange tile_range(int ntiles, int chunked) {
-  TileRange r;
-  if (chunked) {
-    r.t = (int)((long long)blockIdx.x * ntiles / gridDim.x);
-    r.end = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
-    r.step = 1;
+__device__ __forceinline__ TileWalk tile_walk(int ntiles, int walk, unsigned int *ticket) {
+  TileWalk w;
+  w.ticket = nullptr;
+  if (walk == 2 && ticket) {
+    w.first = 0;
+    w.end = ntiles;
+    w.step = 0;
+    w.ticket = ticket;
+  } else if (walk == 1) {
+    w.first = (int)((long long)blockIdx.x * ntiles / gridDim.x);
+    w.end = (int)((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
+    w.step = 1;
   } else {
-    r.t = blockIdx.x;
-    r.end = ntiles;
-    r.step = gridDim.x;
+    w.first = blockIdx.x;
+    w.end = ntiles;
+    w.step = gridDim.x;
   }
-  return r;
+  return w;
+}
+__device__ __forceinline__ int walk_fetch(unsigned int *ticket) {
+  __shared__ int s_next;
+  if (threadIdx.x == 0) s_next = (int)atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int t = s_next;
+  __syncthreads();  // every thread has read it before the next fetch overwrites it
+  return t;
+}
+__device__ __forceinline__ int walk_start(const TileWalk &w) { return w.ticket ? walk_fetch(w.ticket) : w.first; }
+__device__ __forceinline__ int walk_next(const TileWalk &w, int t) {
+  return w.ticket ? walk_fetch(w.ticket) : t + w.step;
+}
+
+// the block's job j (or the kernel-argument job when the table is null) into shared memory;
+// block-uniform, called between tiles
+template <class Job>
+__device__ __forceinline__ void stage_job(unsigned long long *sj, const Job *__restrict__ jobs, int j, const Job &one) {
+  static_assert(sizeof(Job) % 8 == 0, "job records are whole 8-byte words");
+  __syncthreads();
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(jobs ? jobs + j : &one);
+  for (int w = threadIdx.x; w < (int)(sizeof(Job) / 8); w += blockDim.x) sj[w] = src[w];
+  __syncthreads();
 }
 
 // Per-pass operations of the generic batched kernel: Acc is a thread's per-tile partial result,
@@ -1374,21 +1407,17 @@ struct AdvectOp {
 template <class Op>
 __global__ void __maxnreg__(Op::kMaxRegs) k_batched(const typename Op::Job *__restrict__ jobs,
                                                          const int *__restrict__ ts, int njobs, int ntiles,
-                                                         int tile_markers, int chunked,
+                                                         int tile_markers, int walk, unsigned int *ticket,
                                                          const __grid_constant__ typename Op::Job one) {
   using Job = typename Op::Job;
-  static_assert(sizeof(Job) % 8 == 0, "job records are whole 8-byte words");
   __shared__ unsigned long long sj[sizeof(Job) / 8];
   const Job &J = *reinterpret_cast<const Job *>(sj);
-  const TileRange r = tile_range(ntiles, chunked);
+  const TileWalk w = tile_walk(ntiles, walk, ticket);
   int cur = -1;
-  for (int t = r.t; t < r.end; t += r.step) {
+  for (int t = walk_start(w); t < w.end; t = walk_next(w, t)) {
     const int j = jobs ? tile_job(ts, njobs, t) : 0;
     if (j != cur) {  // the tile's job into shared memory (block-uniform)
-      __syncthreads();
-      const unsigned long long *src = reinterpret_cast<const unsigned long long *>(jobs ? jobs + j : &one);
-      for (int w = threadIdx.x; w < (int)(sizeof(Job) / 8); w += blockDim.x) sj[w] = src[w];
-      __syncthreads();
+      stage_job(sj, jobs, j, one);
       cur = j;
     }
     const int64_t base = (int64_t)(t - (jobs ? __ldg(ts + j) : 0)) * tile_markers;
@@ -1402,14 +1431,21 @@ __global__ void __maxnreg__(Op::kMaxRegs) k_batched(const typename Op::Job *__re
 // staged in shared memory again whenever a tile's member uses another network buffer.
 __global__ void __launch_bounds__(512) k_yield_fp32_batched(const YieldJob *__restrict__ jobs,
                                                                     const int *__restrict__ ts, int njobs,
-                                                                    int ntiles, int tile_markers, int chunked,
+                                                                    int ntiles, int tile_markers, int walk,
+                                                                    unsigned int *ticket,
                                                                     const __grid_constant__ YieldJob one) {
   __shared__ float w2s[kH * kH];
+  __shared__ unsigned long long sj[sizeof(YieldJob) / 8];
+  const YieldJob &J = *reinterpret_cast<const YieldJob *>(sj);
   const float *staged = nullptr;
-  const TileRange r = tile_range(ntiles, chunked);
-  for (int t = r.t; t < r.end; t += r.step) {
+  const TileWalk w = tile_walk(ntiles, walk, ticket);
+  int cur = -1;
+  for (int t = walk_start(w); t < w.end; t = walk_next(w, t)) {
     const int j = jobs ? tile_job(ts, njobs, t) : 0;
-    const YieldJob &J = jobs ? jobs[j] : one;
+    if (j != cur) {
+      stage_job(sj, jobs, j, one);
+      cur = j;
+    }
     if (J.cfg.mlp != staged) {
       staged = J.cfg.mlp;
       __syncthreads();
@@ -1426,23 +1462,31 @@ __global__ void __launch_bounds__(512) k_yield_fp32_batched(const YieldJob *__re
 
 // checkPlasticYielding with the tensor-core surrogate over a table (blocks of tc::kTile threads,
 // tiles of multiples of tc::kTile markers).  The network is staged at the block's first tile
-// and again when a tile's member uses another network buffer.  A block that gives up on the
+// and again when a tile's member reads another network buffer.  A block that gives up on the
 // tensor path does so for the rest of its tiles (their markers take the exact solve); the drain
 // timeout, if any, is counted on the member whose round gave up.
 __global__ void __launch_bounds__(tc::kTile) k_yield_tc_batched(const YieldJob *__restrict__ jobs,
                                                                 const int *__restrict__ ts, int njobs, int ntiles,
-                                                                int tile_markers, int chunked,
+                                                                int tile_markers, int walk, unsigned int *ticket,
                                                                 const __grid_constant__ YieldJob one) {
   extern __shared__ unsigned char dyn[];
-  const TileRange r = tile_range(ntiles, chunked);
-  if (r.t >= r.end) return;  // block-uniform, before any TMEM is taken
+  __shared__ unsigned long long sj[sizeof(YieldJob) / 8];
+  const YieldJob &J = *reinterpret_cast<const YieldJob *>(sj);
+  const TileWalk w = tile_walk(ntiles, walk, ticket);
+  int t = walk_start(w);
+  if (t >= w.end) return;  // block-uniform, before any TMEM is taken
   tc::Block B;
-  const float *staged = jobs ? jobs[tile_job(ts, njobs, r.t)].cfg.mlp : one.cfg.mlp;
+  int cur = jobs ? tile_job(ts, njobs, t) : 0;
+  stage_job(sj, jobs, cur, one);
+  const float *staged = J.cfg.mlp;
   tc::setup(B, dyn, staged);
   CreepCounters *gave_up = nullptr;
-  for (int t = r.t; t < r.end; t += r.step) {
+  for (; t < w.end; t = walk_next(w, t)) {
     const int j = jobs ? tile_job(ts, njobs, t) : 0;
-    const YieldJob &J = jobs ? jobs[j] : one;
+    if (j != cur) {
+      stage_job(sj, jobs, j, one);
+      cur = j;
+    }
     if (J.cfg.mlp != staged) {
       staged = J.cfg.mlp;
       tc::restage(B, staged);
@@ -1456,7 +1500,7 @@ __global__ void __launch_bounds__(tc::kTile) k_yield_tc_batched(const YieldJob *
     }
     if (__syncthreads_or(a) && threadIdx.x == 0) atomicOr(&J.st->is_yielding, 1);
   }
-  tc::teardown(B, &(gave_up ? gave_up : (jobs ? jobs[0].cc : one.cc))->tc_drain_timeouts);
+  tc::teardown(B, &(gave_up ? gave_up : J.cc)->tc_drain_timeouts);
 }
 
 constexpr size_t kJobBytes[BP_COUNT] = {sizeof(RhoJob),    sizeof(YieldJob),  sizeof(YieldJob), sizeof(YieldJob),
@@ -1465,6 +1509,17 @@ constexpr size_t kJobBytes[BP_COUNT] = {sizeof(RhoJob),    sizeof(YieldJob),  si
 constexpr size_t kTableAlign = 256;
 
 int batch_fail(cudaError_t e) { return mic_fail_cuda(nullptr, e); }
+
+// the tensor-core yield kernel's shared memory (51 KB a block): the largest carveout, so that four
+// blocks fit an SM -- the occupancy calculator otherwise assumes the default split and allows one
+cudaError_t tc_kernel_attributes() {
+  cudaError_t e =
+      cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+  return e;
+}
 
 // resident blocks per SM of pass p's kernel at `block` threads (cached per device and shape)
 int pass_occupancy(int dev, int pass, int block) {
@@ -1481,7 +1536,7 @@ int pass_occupancy(int dev, int pass, int block) {
     case BP_YIELD_EXACT: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched<YieldOp<0>>, block, 0); break;
     case BP_YIELD_FP32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_yield_fp32_batched, block, 0); break;
     case BP_YIELD_TC:
-      e = cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem);
+      e = tc_kernel_attributes();
       if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_yield_tc_batched, tc::kTile, tc::kDynSmem);
       break;
@@ -1505,45 +1560,54 @@ const Job &job_arg(const void *one) {
   return one ? *static_cast<const Job *>(one) : zero;
 }
 
+struct Walk {
+  int walk;
+  unsigned int *ticket;  // walk 2: zeroed on the stream before the launch
+};
+
 template <class Op>
 void launch_generic(unsigned grid, int block, cudaStream_t s, const unsigned char *jobs, const int *ts, int nj,
-                    int ntiles, int tm, int chunked, const void *one) {
+                    int ntiles, int tm, Walk wk, const void *one) {
   using Job = typename Op::Job;
-  k_batched<Op><<<grid, block, 0, s>>>(reinterpret_cast<const Job *>(jobs), ts, nj, ntiles, tm, chunked,
+  k_batched<Op><<<grid, block, 0, s>>>(reinterpret_cast<const Job *>(jobs), ts, nj, ntiles, tm, wk.walk, wk.ticket,
                                        job_arg<Job>(one));
 }
 
 cudaError_t launch_pass(int pass, unsigned grid, int block, cudaStream_t s, const unsigned char *jobs, const int *ts,
-                        int nj, int ntiles, int tm, int chunked, const void *one) {
+                        int nj, int ntiles, int tm, Walk wk, const void *one) {
+  if (wk.walk == 2) {
+    const cudaError_t e = wk.ticket ? cudaMemsetAsync(wk.ticket, 0, sizeof(unsigned int), s) : cudaErrorInvalidValue;
+    if (e != cudaSuccess) return e;
+  }
   switch (pass) {
-    case BP_RHO: launch_generic<RhoOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
-    case BP_YIELD_PLAIN: launch_generic<YieldOp<2>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
-    case BP_YIELD_EXACT: launch_generic<YieldOp<0>>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_RHO: launch_generic<RhoOp>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
+    case BP_YIELD_PLAIN: launch_generic<YieldOp<2>>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
+    case BP_YIELD_EXACT: launch_generic<YieldOp<0>>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
     case BP_YIELD_FP32:
       k_yield_fp32_batched<<<grid, block, 0, s>>>(reinterpret_cast<const YieldJob *>(jobs), ts, nj, ntiles, tm,
-                                                   chunked, job_arg<YieldJob>(one));
+                                                   wk.walk, wk.ticket, job_arg<YieldJob>(one));
       break;
     case BP_YIELD_TC: {
-      const cudaError_t e =
-          cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem);
+      const cudaError_t e = tc_kernel_attributes();
       if (e != cudaSuccess) return e;
       k_yield_tc_batched<<<grid, tc::kTile, tc::kDynSmem, s>>>(reinterpret_cast<const YieldJob *>(jobs), ts, nj,
-                                                                ntiles, tm, chunked, job_arg<YieldJob>(one));
+                                                                ntiles, tm, wk.walk, wk.ticket,
+                                                                job_arg<YieldJob>(one));
       break;
     }
-    case BP_STRAIN: launch_generic<StrainOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
-    case BP_SUBGRID: launch_generic<SubgridOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
-    case BP_STRESS: launch_generic<StressOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
-    case BP_SUBT: launch_generic<SubTOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
-    case BP_SUBT_APPLY: launch_generic<SubTApplyOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
-    default: launch_generic<AdvectOp>(grid, block, s, jobs, ts, nj, ntiles, tm, chunked, one); break;
+    case BP_STRAIN: launch_generic<StrainOp>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
+    case BP_SUBGRID: launch_generic<SubgridOp>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
+    case BP_STRESS: launch_generic<StressOp>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
+    case BP_SUBT: launch_generic<SubTOp>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
+    case BP_SUBT_APPLY: launch_generic<SubTApplyOp>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
+    default: launch_generic<AdvectOp>(grid, block, s, jobs, ts, nj, ntiles, tm, wk, one); break;
   }
   return cudaGetLastError();
 }
 
 // One context's marker pass: the pass kernel with the context's job as its argument -- one block
 // per tile of one block's worth of markers (the tensor-core yield: the context's persistent
-// tensor-core grid, round-robin).
+// tensor-core grid, each block taking the next tile from the context's counter for the pass).
 template <class Job>
 int solo_pass(mic_ctx *ctx, int pass, const Job &J, int block, const char *name) {
   const bool tcp = pass == BP_YIELD_TC;
@@ -1554,7 +1618,8 @@ int solo_pass(mic_ctx *ctx, int pass, const Job &J, int block, const char *name)
   int64_t grid = tcp ? mic_creep_tc_blocks(ctx, J.n) : ntiles;
   if (grid < 1) grid = 1;
   MIC_KERNEL(ctx, name);
-  MIC_CUDA_TRY(launch_pass(pass, (unsigned)grid, block, ctx->stream, nullptr, nullptr, 1, ntiles, block, 0, &J));
+  const Walk wk = tcp ? Walk{2, ctx->tickets + pass} : Walk{0, nullptr};
+  MIC_CUDA_TRY(launch_pass(pass, (unsigned)grid, block, ctx->stream, nullptr, nullptr, 1, ntiles, block, wk, &J));
   return MIC_OK;
 }
 }  // namespace
@@ -2189,7 +2254,7 @@ bool mic_batch_empty(const mic_batch *b) {
 size_t mic_batch_table_bound(int n_members) {
   size_t per = sizeof(RhoJob) + sizeof(YieldJob) + sizeof(StrainJob) + sizeof(SubgridJob) + sizeof(StressJob) +
                sizeof(SubTJob) + sizeof(SubTApplyJob) + sizeof(AdvectJob);
-  return (size_t)n_members * per + (size_t)BP_COUNT * (kTableAlign + sizeof(int) * ((size_t)n_members + 1)) +
+  return (size_t)n_members * per + (size_t)BP_COUNT * (kTableAlign + sizeof(int) * ((size_t)n_members + 2)) +
          kTableAlign;
 }
 
@@ -2210,11 +2275,10 @@ int mic_batch_launch(mic_batch *b, const BatchShape *shape, unsigned char *host_
     // them, which also spreads the markers' uneven solve costs over the blocks
     const bool surrogate = tcp || p == BP_YIELD_FP32;
     const int persistent = surrogate ? 1 : shape[p].persistent;
-    const int chunked = surrogate ? 0 : shape[p].chunked;
+    const int walk = surrogate ? 2 : (persistent ? shape[p].chunked : 0);
     const int mult = surrogate ? 1 : (shape[p].mult < 1 ? 1 : (shape[p].mult > 64 ? 64 : shape[p].mult));
     const int tm = block * mult;
-    std::vector<int> ts(nj + 1);
-    ts[0] = 0;
+    std::vector<int> ts(nj + 2, 0);  // tile offsets, then the walk's ticket (zeroed before the launch)
     for (int j = 0; j < nj; ++j) {
       const int64_t t = (b->n[p][j] + tm - 1) / tm;
       if ((int64_t)ts[j] + t > 0x7fffffff) {
@@ -2226,7 +2290,7 @@ int mic_batch_launch(mic_batch *b, const BatchShape *shape, unsigned char *host_
     if (status) break;
     const int ntiles = ts[nj];
     const size_t o = (*off + kTableAlign - 1) / kTableAlign * kTableAlign;
-    const size_t jb = b->jobs[p].size(), tb = sizeof(int) * (size_t)(nj + 1);
+    const size_t jb = b->jobs[p].size(), tb = sizeof(int) * (size_t)(nj + 2);  // tile offsets, then the ticket
     if (jb != (size_t)nj * kJobBytes[p] || o + jb + tb > cap) {
       status = MIC_ERR_NOMEM;
       break;
@@ -2240,13 +2304,15 @@ int mic_batch_launch(mic_batch *b, const BatchShape *shape, unsigned char *host_
     *off = o + jb + tb;
     const unsigned char *dj = dev_table + o;
     const int *dts = reinterpret_cast<const int *>(dev_table + o + jb);
+    unsigned int *ticket = reinterpret_cast<unsigned int *>(dev_table + o + jb) + nj + 1;
     int64_t grid = ntiles;
     if (persistent) {
       const int64_t g = (int64_t)nsm * pass_occupancy(dev, p, block);
       if (g < grid) grid = g;
     }
     if (grid < 1) grid = 1;
-    if ((ce = launch_pass(p, (unsigned)grid, block, s, dj, dts, nj, ntiles, tm, chunked, nullptr)) != cudaSuccess) {
+    if ((ce = launch_pass(p, (unsigned)grid, block, s, dj, dts, nj, ntiles, tm, Walk{walk, ticket}, nullptr)) !=
+        cudaSuccess) {
       status = batch_fail(ce);
       break;
     }

@@ -680,11 +680,12 @@ class MicEnsemble:
             raise MicError(code, "mic_ensemble_autotune")
         return list(out)
 
-    def set_schedule(self, batched=True, tile_mult=4, persistent=True, chunked=True):
-        """mic_ensemble_set_schedule: batched marker passes (one kernel per pass over all members)
-        or per-member kernels; tile size in blocks' worth of markers and the grid's walk."""
-        code = self.L.mic_ensemble_set_schedule(self.h, 1 if batched else 0, int(tile_mult), 1 if persistent else 0,
-                                                1 if chunked else 0)
+    def set_schedule(self, groups=4, tile_mult=4, persistent=True, chunked=2):
+        """mic_ensemble_set_schedule: groups 0 = per-member kernels on member streams; 1..8 = batch
+        groups, one kernel per marker pass per group; tile size in blocks' worth of markers and the
+        persistent grid's walk (chunked 0 round-robin, 1 contiguous runs, 2 shared counter)."""
+        code = self.L.mic_ensemble_set_schedule(self.h, int(groups), int(tile_mult), 1 if persistent else 0,
+                                                int(chunked))
         if code:
             raise MicError(code, "mic_ensemble_set_schedule")
 
@@ -693,8 +694,8 @@ class MicEnsemble:
         code = self.L.mic_ensemble_get_schedule(self.h, *[ctypes.byref(x) for x in v])
         if code:
             raise MicError(code, "mic_ensemble_get_schedule")
-        return {"batched": bool(v[0].value), "tile_mult": v[1].value, "persistent": bool(v[2].value),
-                "chunked": bool(v[3].value)}
+        return {"groups": v[0].value, "tile_mult": v[1].value, "persistent": bool(v[2].value),
+                "walk": ("round_robin", "runs", "counter")[v[3].value]}
 
     def step(self, dt_disp=None, dt_thermal=None, subgrid_stress=1, graph=True):
         n = len(self.members)

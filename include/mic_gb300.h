@@ -384,9 +384,9 @@ int mic_subduction_timestep_many(mic_ctx *const *ctxs, int n, const mic_timestep
  * iMonte option).  Independent problems, each a context with its own stream, stepped together:
  * one mic_ensemble_step is every member's mic_step (no residual read), with the same results as
  * each member stepped alone.  Batched (the default), each marker pass of the step is one kernel
- * over a work table of (member, tile) pairs for all members, and the members' other launches
- * (binning, projections, node kernels) run on their own streams between the passes; per-member,
- * each member's whole step runs on its stream and small members overlap on the GPU.  With
+ * over a work table of (member, tile) pairs for the members of a batch group, and the members'
+ * other launches (binning, projections, node kernels) run on their own streams between the
+ * passes; per-member, each member's whole step runs on its stream and small members overlap.  With
  * use_graph the whole ensemble step is captured as CUDA graphs on the first call and replayed as
  * one launch afterwards (re-captured when a member's settings, marker count or the time steps
  * change).  Asynchronous: mic_ensemble_synchronize waits; member streams are ordered after each
@@ -397,22 +397,24 @@ int mic_ensemble_destroy(mic_ensemble *ens);
 int mic_ensemble_step(mic_ensemble *ens, const double *dt_disp, const double *dt_thermal, int subgrid_stress,
                       int use_graph);
 int mic_ensemble_synchronize(mic_ensemble *ens);
-/* How a step runs its marker passes (new): batched 1 = one kernel per pass over all members, 0 =
- * each member's own kernels on its stream.  Batched kernels cut each member's markers into tiles
- * of tile_mult (1..64) blocks' worth and run one block per tile (persistent 0) or a persistent
- * grid of SMs x resident blocks whose blocks take contiguous runs of tiles (chunked 1) or tiles
- * round-robin (chunked 0); tiles are ordered member by member in the issue order.  The surrogate
- * yield passes always use a persistent grid walking one-block tiles round-robin (members whose
- * networks are equal read one copy).  Default: batched, 4, 1, 1. */
-int mic_ensemble_set_schedule(mic_ensemble *ens, int batched, int tile_mult, int persistent, int chunked);
-int mic_ensemble_get_schedule(mic_ensemble *ens, int *batched, int *tile_mult, int *persistent, int *chunked);
+/* How a step runs its marker passes (new): groups 0 = each member's own kernels on its stream;
+ * groups 1..8 = members dealt to that many batch groups by marker count (largest first, each to
+ * the group with the fewest markers), one kernel per marker pass per group over the group's
+ * (member, tile) table, the groups running beside one another.  Batched kernels cut each
+ * member's markers into tiles of tile_mult (1..64) blocks' worth and run one block per tile
+ * (persistent 0) or a persistent grid of SMs x resident blocks whose blocks take tiles
+ * round-robin (chunked 0), one contiguous run each (1) or the next tile from a counter the grid
+ * shares (2); tiles are ordered member by member in the issue order.  The surrogate yield passes
+ * always take one-block tiles from a counter on a persistent grid (members whose networks are
+ * equal read one copy).  Default: 4, 4, 1, 2. */
+int mic_ensemble_set_schedule(mic_ensemble *ens, int groups, int tile_mult, int persistent, int chunked);
+int mic_ensemble_get_schedule(mic_ensemble *ens, int *groups, int *tile_mult, int *persistent, int *chunked);
 /* Launch shapes and member schedule measured on the ensemble (new): mic_autotune on every member,
  * then the fastest captured step among per-member steps in three issue orders (as given, largest
- * first, smallest first) and batched passes in two member orders (as given, largest first) with
- * four walks (tile_mult, persistent, chunked = 1,0,0; 4,1,0; 4,1,1; 16,1,1), each timed over
- * 2 x steps graph replays from saved member states.  The winner becomes the ensemble's schedule
- * (mic_ensemble_get_schedule); every member's state is restored; order_out (n_members ints, may
- * be NULL) receives the member order. */
+ * first, smallest first) and batched passes in 1, 2, 4 and 8 groups with three walks (tile_mult,
+ * persistent, chunked = 1,0,0; 4,1,1; 4,1,2), each timed over 2 x steps graph replays from saved
+ * member states.  The winner becomes the ensemble's schedule (mic_ensemble_get_schedule); every
+ * member's state is restored; order_out (n_members ints, may be NULL) receives the member order. */
 int mic_ensemble_autotune(mic_ensemble *ens, const double *dt_disp, const double *dt_thermal, int subgrid_stress,
                           int steps, int *order_out);
 /* kernels issued through the ensemble so far, and kernels inside one captured step */

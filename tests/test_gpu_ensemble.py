@@ -62,15 +62,19 @@ def _setup(wls):
     return out
 
 
-# (batched, tile_mult, persistent, chunked): per-member kernels on member streams, and batched
-# marker passes with one block per tile, a persistent round-robin walk, and persistent
-# contiguous runs of two tile sizes
+# (groups, tile_mult, persistent, walk): per-member kernels on member streams, and batched
+# marker passes with one block per tile, a persistent round-robin walk, persistent contiguous
+# runs of two tile sizes, tiles taken from a shared counter, and the members dealt to two and
+# three batch groups
 SCHEDULES = {
-    "per_member": (False, 4, True, True),
-    "tile_per_block": (True, 1, False, False),
-    "round_robin": (True, 4, True, False),
-    "runs": (True, 4, True, True),
-    "runs16": (True, 16, True, True),
+    "per_member": (0, 4, True, True),
+    "tile_per_block": (1, 1, False, False),
+    "round_robin": (1, 4, True, False),
+    "runs": (1, 4, True, True),
+    "runs16": (1, 16, True, True),
+    "counter": (1, 4, True, 2),
+    "two_groups": (2, 4, True, True),
+    "three_groups": (3, 1, False, False),
 }
 
 
@@ -82,7 +86,7 @@ def test_ensemble_matches_members_stepped_alone(graph, schedule):
     B = _setup(wls)
     E = gpu.MicEnsemble(A)
     E.set_schedule(*SCHEDULES[schedule])
-    assert E.schedule()["batched"] == SCHEDULES[schedule][0]
+    assert E.schedule()["groups"] == SCHEDULES[schedule][0]
     dts = np.array([wl.dt for wl in wls])
 
     def compare():
@@ -111,7 +115,7 @@ def test_ensemble_matches_members_stepped_alone(graph, schedule):
     compare()
     launches, per_graph = E.launch_count()
     assert launches > 0
-    if graph and not SCHEDULES[schedule][0]:
+    if graph and SCHEDULES[schedule][0] == 0:
         assert per_graph >= 25 * len(A)
     E.close()
 
@@ -133,7 +137,7 @@ def test_ensemble_autotune_keeps_states_and_results():
     order = E.autotune(dts, dts, subgrid_stress=1, steps=1)
     assert sorted(order) == list(range(len(A)))
     sch = E.schedule()
-    assert sch["tile_mult"] in (1, 4, 16)
+    assert sch["tile_mult"] in (1, 4) and 0 <= sch["groups"] <= 8
     for a, m in zip(A, before):
         assert np.array_equal(_bytes(a.markers), m)
     for _ in range(3):
@@ -146,7 +150,7 @@ def test_ensemble_autotune_keeps_states_and_results():
         assert np.array_equal(a.get_nodal("lastT"), b.get_nodal("lastT"))
 
 
-@pytest.mark.parametrize("schedule", ["per_member", "runs"])
+@pytest.mark.parametrize("schedule", ["per_member", "runs", "two_groups"])
 @pytest.mark.parametrize("graph", [True, False])
 def test_plastic_members_match_members_stepped_alone(graph, schedule):
     """Visco-elasto-plastic members (yielding, so the step's viscosity-only second projection
@@ -209,7 +213,7 @@ def test_member_stepped_or_tuned_between_replays():
     E.close()
 
 
-@pytest.mark.parametrize("schedule", ["runs", "round_robin", "tile_per_block"])
+@pytest.mark.parametrize("schedule", ["runs", "round_robin", "tile_per_block", "two_groups"])
 @pytest.mark.parametrize("graph", [True, False])
 def test_creep_members_batched_match_members_stepped_alone(graph, schedule):
     """Law-7 ice members with every yield variant in one batch -- exact creep solve, tensor-core
