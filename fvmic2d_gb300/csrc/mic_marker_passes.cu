@@ -256,13 +256,15 @@ __global__ void k_limit_viscosity(double *eta, double etamin, double etamax, int
 // MAXT: also the maximum marker temperature of main:271-281 (in-domain markers, from 0; the bit
 // patterns of non-negative doubles order as the values), one atomic per block into *maxT
 // one marker; returns the bits of its temperature when it is in the domain and above 0, else 0
+// (rho0, alpha: the materials' materialRho and materialAlpha)
 __device__ __forceinline__ long long update_rho_one(const int *cellX, const int *mat, const double *T, double *rho,
-                                                    double *rhodot, const mic_materials &M, int64_t n, int64_t m) {
+                                                    double *rhodot, const double *rho0, const double *alpha,
+                                                    int64_t n, int64_t m) {
   long long b = 0;  // bits of 0.0
   if (m < n && cellX[m] != -1) {
     const int k = mat[m];
     const double t = T[m];
-    rho[m] = -M.materialRho[k] * (M.materialAlpha[k] * t);
+    rho[m] = -rho0[k] * (alpha[k] * t);
     rhodot[m] = 0.0;
     if (t > 0.0) b = __double_as_longlong(t);
   }
@@ -1181,7 +1183,7 @@ struct RhoJob {
   const int *cellX, *mat;
   const double *T;
   double *rho, *rhodot;
-  mic_materials M;
+  double rho0[MIC_MAXMAT], alpha[MIC_MAXMAT];  // the materials' materialRho, materialAlpha
   int64_t n;
   unsigned long long *maxT;  // null: no maximum
 };
@@ -1325,7 +1327,7 @@ struct RhoOp {
   using Job = RhoJob;
   using Acc = long long;
   static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &a) {
-    a = max(a, update_rho_one(J.cellX, J.mat, J.T, J.rho, J.rhodot, J.M, J.n, m));
+    a = max(a, update_rho_one(J.cellX, J.mat, J.T, J.rho, J.rhodot, J.rho0, J.alpha, J.n, m));
   }
   static __device__ __forceinline__ void flush(const Job &J, Acc a) {
     if (J.maxT) block_max_to(a, J.maxT);
@@ -1659,8 +1661,12 @@ static int update_rho(mic_ctx *ctx, bool with_max, mic_batch *b = nullptr) {
   unsigned long long *d = reinterpret_cast<unsigned long long *>(ctx->red_buf + 8);
   if (with_max) MIC_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
   if (ctx->n == 0) return MIC_OK;
-  const RhoJob J = {ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T], ctx->f64[C_RHO], ctx->f64[C_RHODOT],
-                    ctx->mat, ctx->n, with_max ? d : nullptr};
+  RhoJob J = {ctx->i32[C_CELLX], ctx->i32[C_MAT], ctx->f64[C_T], ctx->f64[C_RHO], ctx->f64[C_RHODOT], {}, {},
+              ctx->n, with_max ? d : nullptr};
+  for (int k = 0; k < MIC_MAXMAT; ++k) {
+    J.rho0[k] = ctx->mat.materialRho[k];
+    J.alpha[k] = ctx->mat.materialAlpha[k];
+  }
   if (b) return b->add(BP_RHO, J, ctx->n);
   return solo_pass(ctx, BP_RHO, J, tuned_block(ctx, TU_UPDATE_RHO), "k_update_rho");
 }
