@@ -5,9 +5,10 @@
 // (valid because every compared value is non-negative): the same answer as the reference's
 // bisection, with no FP64 instructions on a GPU whose FP64 rate is 1/60 of FP32.
 //
-// Sorting: key = 4*(cellY*(NX-1) + cellX) + 2*qy + qx, where (qx, qy) is the marker's quadrant
-// of its cell (X >= xc[cellX+1], Y >= yc[cellY+1]: the stagger test of findCellStag2D); out-of-
-// domain markers get key 4*(NX-1)*(NY-1).  Cells stay contiguous and inside a cell the markers
+// Sorting: key = 4*(cellY*NCX + cellX) + 2*qy + qx, where (qx, qy) is the marker's quadrant of
+// its cell (X >= xc[cellX+1], Y >= yc[cellY+1]: the stagger test of findCellStag2D) and NCX the
+// basic cells in x (NX - 1, or NX on a grid periodic in x: markers.c:49, 73); out-of-domain
+// markers get key 4*NCX*(NY-1).  Cells stay contiguous and inside a cell the markers
 // of each quadrant are contiguous, so every staggered (cell-centre) cell's markers are four
 // runs.  An LSD radix sort with 8-bit digits (stable by construction) orders (key, index) pairs:
 // per 4096-marker tile a digit histogram, one exclusive scan over the digit-major
@@ -54,12 +55,12 @@ __global__ void k_find_cells(Params P, const double *__restrict__ X, const doubl
     const long long blx = __double_as_longlong(P.LX), bly = __double_as_longlong(P.LY);
     // X >= 0 && Y >= 0 && X <= LX && Y <= LY; NaN fails every test
     const bool in = ux >= 0 && uy >= 0 && ux <= blx && uy <= bly;
-    int cx = -1, cy = -1, k = 4 * (P.NX - 1) * (P.NY - 1);
+    int cx = -1, cy = -1, k = 4 * P.NCX * (P.NY - 1);
     if (in) {
-      cx = bisect_bits(P.xbits, P.NX, ux);
+      cx = bisect_bits(P.xbits, P.NCX + 1, ux);  // lines 0..NCX (periodic: line NX = LX)
       cy = bisect_bits(P.ybits, P.NY, uy);
       const int qx = ux >= nonneg_bits(P.xc[cx + 1]), qy = uy >= nonneg_bits(P.yc[cy + 1]);
-      k = 4 * (cy * (P.NX - 1) + cx) + 2 * qy + qx;
+      k = 4 * (cy * P.NCX + cx) + 2 * qy + qx;
     } else {
       atomicAdd(&s_out, 1ULL);
     }

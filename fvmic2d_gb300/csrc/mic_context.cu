@@ -4,6 +4,8 @@
 #include <cstring>
 #include <new>
 
+#include <vector>
+
 #include "mic_internal.cuh"
 
 using namespace mic;
@@ -178,6 +180,109 @@ static void free_ctx(mic_ctx *ctx) {
   delete ctx;
 }
 
+// The grid tables on the host and the device from the gridlines kept in h_x (x[0..NX-1],
+// y[0..NY-1]): cell centres as getCellCenters (gridSpacing.c:150-157); periodic in x, the lines
+// and centres beyond the seam as makePeriodic (gridSpacing.c:159-168), x[NX] = LX and NX basic
+// cells in x instead of NX - 1.  Order-preserving bit images of the lines and centres (integer
+// compares for cell location and the advection's cell walk) and the spacings with their
+// reciprocals, every table with 2 ghost entries in front.
+static int grid_tables(mic_ctx *ctx, int periodic) {
+  const int NX = ctx->P.NX, NY = ctx->P.NY;
+  const double LX = ctx->P.LX, LY = ctx->P.LY;
+  const size_t nx4 = (size_t)NX + 4, ny4 = (size_t)NY + 4;
+  double *hx = ctx->h_x + 2, *hxc = ctx->h_x + nx4 + 2, *hy = ctx->h_x + 2 * nx4 + 2,
+         *hyc = ctx->h_x + 2 * nx4 + ny4 + 2;
+  for (int i = -2; i < 0; ++i) hx[i] = 0.0;
+  for (int i = NX; i < NX + 2; ++i) hx[i] = 0.0;
+  for (int i = -2; i < NX + 2; ++i) hxc[i] = 0.0;
+  for (int j = -2; j < NY + 2; ++j) hyc[j] = 0.0;
+  for (int i = 1; i < NX; ++i) hxc[i] = (hx[i - 1] + hx[i]) / 2.0;
+  hxc[0] = -hxc[1];
+  hxc[NX] = 2.0 * LX - hxc[NX - 1];
+  for (int j = 1; j < NY; ++j) hyc[j] = (hy[j - 1] + hy[j]) / 2.0;
+  hyc[0] = -hyc[1];
+  hyc[NY] = 2.0 * LY - hyc[NY - 1];
+  if (periodic) {
+    hx[NX] = LX;
+    hx[NX + 1] = LX + hx[1];
+    hx[-1] = hx[NX - 1] - LX;
+    hx[-2] = hx[NX - 2] - LX;
+    hxc[NX] = (LX + hx[NX - 1]) / 2.0;
+    hxc[NX + 1] = hxc[1] + LX;
+    hxc[0] = 0.0 - (LX - hxc[NX]);
+    hxc[-1] = 0.0 - (LX - hxc[NX - 1]);
+  }
+  ctx->h_xc = hxc;
+  ctx->h_y = hy;
+  ctx->h_yc = hyc;
+  ctx->P.xper = periodic ? 1 : 0;
+  ctx->P.NCX = periodic ? NX : NX - 1;
+  const int NCX = ctx->P.NCX;
+  if (cudaMemcpy(ctx->grid_buf, ctx->h_x, sizeof(double) * (2 * nx4 + 2 * ny4), cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return MIC_ERR_CUDA;
+  // ordered images (a -0.0 line counts as +0.0): lines 0..NCX in x (and -2, -1 beyond the seam),
+  // centres 0..NCX+1
+  auto ordered = [](double v) {
+    long long b;
+    memcpy(&b, &v, 8);
+    if (b == (long long)0x8000000000000000ULL) b = 0;
+    return b >= 0 ? b : (long long)(0x8000000000000000ULL) - b;
+  };
+  std::vector<long long> hb(2 * (nx4 + ny4), 0);
+  long long *bx = hb.data() + 2, *by = hb.data() + nx4 + 2, *bxc = hb.data() + nx4 + ny4 + 2,
+            *byc = hb.data() + 2 * nx4 + ny4 + 2;
+  for (int i = periodic ? -2 : 0; i <= (periodic ? NX + 1 : NX - 1); ++i) bx[i] = ordered(hx[i]);
+  for (int j = 0; j < NY; ++j) by[j] = ordered(hy[j]);
+  for (int i = periodic ? -1 : 0; i <= (periodic ? NX + 1 : NX); ++i) bxc[i] = ordered(hxc[i]);
+  for (int j = 0; j <= NY; ++j) byc[j] = ordered(hyc[j]);
+  if (cudaMemcpy(ctx->bits_buf, hb.data(), sizeof(long long) * hb.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return MIC_ERR_CUDA;
+  ctx->P.x = ctx->grid_buf + 2;
+  ctx->P.xc = ctx->grid_buf + nx4 + 2;
+  ctx->P.y = ctx->grid_buf + 2 * nx4 + 2;
+  ctx->P.yc = ctx->grid_buf + 2 * nx4 + ny4 + 2;
+  ctx->P.xbits = ctx->bits_buf + 2;
+  ctx->P.ybits = ctx->bits_buf + nx4 + 2;
+  ctx->P.xcbits = ctx->bits_buf + nx4 + ny4 + 2;
+  ctx->P.ycbits = ctx->bits_buf + 2 * nx4 + ny4 + 2;
+  // spacings h[i] = g[i+1] - g[i] and reciprocals: basic cells 0..NCX-1, centre cells 0..NCX
+  // (periodic: also cell -1 beyond the seam), y as before
+  std::vector<double> h(4 * nx4 + 4 * ny4, 0.0);
+  double *hx_ = h.data() + 2, *ix_ = h.data() + nx4 + 2, *hxc_ = h.data() + 2 * nx4 + 2,
+         *ixc_ = h.data() + 3 * nx4 + 2;
+  double *hy_ = h.data() + 4 * nx4 + 2, *iy_ = hy_ + ny4, *hyc_ = hy_ + 2 * ny4, *iyc_ = hy_ + 3 * ny4;
+  for (int i = periodic ? -1 : 0; i < NCX; ++i) {
+    hx_[i] = hx[i + 1] - hx[i];
+    ix_[i] = 1.0 / hx_[i];
+  }
+  for (int i = periodic ? -1 : 0; i <= NCX; ++i) {
+    hxc_[i] = hxc[i + 1] - hxc[i];
+    ixc_[i] = 1.0 / hxc_[i];
+  }
+  for (int j = 0; j + 1 < NY; ++j) {
+    hy_[j] = hy[j + 1] - hy[j];
+    iy_[j] = 1.0 / hy_[j];
+  }
+  for (int j = 0; j < NY; ++j) {
+    hyc_[j] = hyc[j + 1] - hyc[j];
+    iyc_[j] = 1.0 / hyc_[j];
+  }
+  if (cudaMemcpy(ctx->spacing_buf, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return MIC_ERR_CUDA;
+  const double *d = ctx->spacing_buf + 2;
+  ctx->P.hx = d;
+  ctx->P.ix = d + nx4;
+  ctx->P.hxc = d + 2 * nx4;
+  ctx->P.ixc = d + 3 * nx4;
+  ctx->P.hy = d + 4 * nx4;
+  ctx->P.iy = d + 4 * nx4 + ny4;
+  ctx->P.hyc = d + 4 * nx4 + 2 * ny4;
+  ctx->P.iyc = d + 4 * nx4 + 3 * ny4;
+  ctx->ncells = NCX * (NY - 1);
+  return MIC_OK;
+}
+
 #define ALLOC(ptr, bytes)                                                            \
   do {                                                                               \
     if (cudaMalloc((void **)&(ptr), (size_t)(bytes)) != cudaSuccess) {              \
@@ -219,95 +324,26 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
     free_ctx(ctx);
     return MIC_ERR_CUDA;
   }
-  // host grid copies with fvmic2d's ghost offset of 2; cell centres as in getCellCenters
+  // host grid copies with fvmic2d's ghost offset of 2 (the caller's gridlines; the rest of the
+  // tables follows from them, periodic or not: grid_tables)
   const size_t nx4 = (size_t)NX + 4, ny4 = (size_t)NY + 4;
-  ctx->h_x = (double *)malloc(sizeof(double) * (2 * nx4 + 2 * ny4));
+  ctx->h_x = (double *)calloc(2 * nx4 + 2 * ny4, sizeof(double));
   if (!ctx->h_x) {
     free_ctx(ctx);
     return MIC_ERR_NOMEM;
   }
-  for (size_t k = 0; k < 2 * nx4 + 2 * ny4; ++k) ctx->h_x[k] = 0.0;
-  double *hx = ctx->h_x + 2, *hxc = ctx->h_x + nx4 + 2, *hy = ctx->h_x + 2 * nx4 + 2,
-         *hyc = ctx->h_x + 2 * nx4 + ny4 + 2;
-  for (int i = 0; i < NX; ++i) hx[i] = x[i];
-  for (int j = 0; j < NY; ++j) hy[j] = y[j];
-  for (int i = 1; i < NX; ++i) hxc[i] = (hx[i - 1] + hx[i]) / 2.0;
-  hxc[0] = -hxc[1];
-  hxc[NX] = 2.0 * LX - hxc[NX - 1];
-  for (int j = 1; j < NY; ++j) hyc[j] = (hy[j - 1] + hy[j]) / 2.0;
-  hyc[0] = -hyc[1];
-  hyc[NY] = 2.0 * LY - hyc[NY - 1];
-  ctx->h_xc = hxc;
-  ctx->h_y = hy;
-  ctx->h_yc = hyc;
-  ALLOC(ctx->grid_buf, sizeof(double) * (2 * nx4 + 2 * ny4));
-  if (cudaMemcpy(ctx->grid_buf, ctx->h_x, sizeof(double) * (2 * nx4 + 2 * ny4), cudaMemcpyHostToDevice) !=
-      cudaSuccess) {
-    free_ctx(ctx);
-    return MIC_ERR_CUDA;
-  }
-  ALLOC(ctx->bits_buf, sizeof(long long) * 2 * (nx4 + ny4));
-  {
-    // raw bits of the (non-negative) grid lines; order-preserving images of the cell centres
-    auto ordered = [](double v) {
-      long long b;
-      memcpy(&b, &v, 8);
-      return b >= 0 ? b : (long long)(0x8000000000000000ULL) - b;
-    };
-    long long *hb = (long long *)calloc(2 * (nx4 + ny4), sizeof(long long));
-    for (int i = 0; i < NX; ++i) hb[i] = ordered(hx[i]);  // -0.0 -> bits of +0.0
-    for (int j = 0; j < NY; ++j) hb[nx4 + j] = ordered(hy[j]);
-    for (int i = 0; i <= NX; ++i) hb[nx4 + ny4 + i] = ordered(hxc[i]);
-    for (int j = 0; j <= NY; ++j) hb[2 * nx4 + ny4 + j] = ordered(hyc[j]);
-    cudaMemcpy(ctx->bits_buf, hb, sizeof(long long) * 2 * (nx4 + ny4), cudaMemcpyHostToDevice);
-    free(hb);
-  }
+  for (int i = 0; i < NX; ++i) ctx->h_x[2 + i] = x[i];
+  for (int j = 0; j < NY; ++j) ctx->h_x[2 * nx4 + 2 + j] = y[j];
   ctx->P.NX = NX;
   ctx->P.NY = NY;
   ctx->P.LX = LX;
   ctx->P.LY = LY;
-  ctx->P.x = ctx->grid_buf + 2;
-  ctx->P.xc = ctx->grid_buf + nx4 + 2;
-  ctx->P.y = ctx->grid_buf + 2 * nx4 + 2;
-  ctx->P.yc = ctx->grid_buf + 2 * nx4 + ny4 + 2;
-  ctx->P.xbits = ctx->bits_buf;
-  ctx->P.ybits = ctx->bits_buf + nx4;
-  ctx->P.xcbits = ctx->bits_buf + nx4 + ny4;
-  ctx->P.ycbits = ctx->bits_buf + 2 * nx4 + ny4;
-  {
-    // spacing tables: 8 arrays of nx4 / ny4 entries (hx, ix, hxc, ixc sized nx4; hy, iy, hyc, iyc ny4)
-    const size_t tot = 4 * nx4 + 4 * ny4;
-    ALLOC(ctx->spacing_buf, sizeof(double) * tot);
-    double *h = (double *)calloc(tot, sizeof(double));
-    double *hx_ = h, *ix_ = h + nx4, *hxc_ = h + 2 * nx4, *ixc_ = h + 3 * nx4;
-    double *hy_ = h + 4 * nx4, *iy_ = hy_ + ny4, *hyc_ = hy_ + 2 * ny4, *iyc_ = hy_ + 3 * ny4;
-    for (int i = 0; i + 1 < NX; ++i) {
-      hx_[i] = hx[i + 1] - hx[i];
-      ix_[i] = 1.0 / hx_[i];
-    }
-    for (int i = 0; i < NX; ++i) {
-      hxc_[i] = hxc[i + 1] - hxc[i];
-      ixc_[i] = 1.0 / hxc_[i];
-    }
-    for (int j = 0; j + 1 < NY; ++j) {
-      hy_[j] = hy[j + 1] - hy[j];
-      iy_[j] = 1.0 / hy_[j];
-    }
-    for (int j = 0; j < NY; ++j) {
-      hyc_[j] = hyc[j + 1] - hyc[j];
-      iyc_[j] = 1.0 / hyc_[j];
-    }
-    cudaMemcpy(ctx->spacing_buf, h, sizeof(double) * tot, cudaMemcpyHostToDevice);
-    free(h);
-    const double *d = ctx->spacing_buf;
-    ctx->P.hx = d;
-    ctx->P.ix = d + nx4;
-    ctx->P.hxc = d + 2 * nx4;
-    ctx->P.ixc = d + 3 * nx4;
-    ctx->P.hy = d + 4 * nx4;
-    ctx->P.iy = d + 4 * nx4 + ny4;
-    ctx->P.hyc = d + 4 * nx4 + 2 * ny4;
-    ctx->P.iyc = d + 4 * nx4 + 3 * ny4;
+  ALLOC(ctx->grid_buf, sizeof(double) * (2 * nx4 + 2 * ny4));
+  ALLOC(ctx->bits_buf, sizeof(long long) * 2 * (nx4 + ny4));
+  ALLOC(ctx->spacing_buf, sizeof(double) * (4 * nx4 + 4 * ny4));
+  if (grid_tables(ctx, 0) != MIC_OK) {
+    free_ctx(ctx);
+    return MIC_ERR_CUDA;
   }
   const int64_t cap = max_markers > 0 ? max_markers : 1;
   ctx->cap = cap;
@@ -327,15 +363,18 @@ extern "C" int mic_create(mic_ctx **out, int device, void *stream, int NX, int N
     cudaMemset(ctx->nodal[f], 0, sizeof(double) * nn);
   }
   for (int f = 0; f < 6; ++f) ALLOC(ctx->node_scr[f], sizeof(double) * nn);
-  ctx->ncells = (NX - 1) * (NY - 1);
+  // cell arrays sized for the periodic grid's NX x (NY-1) cells (one more column of cells), so
+  // that mic_set_bcs can switch periodicity without reallocating
+  const size_t max_cells = (size_t)NX * (NY - 1);
+  ctx->ncells = ctx->P.NCX * (NY - 1);
   ALLOC(ctx->key, sizeof(int) * cap);
   ALLOC(ctx->key_alt, sizeof(int) * cap);
   ALLOC(ctx->perm, sizeof(int) * cap);
   ALLOC(ctx->perm_alt, sizeof(int) * cap);
-  ALLOC(ctx->cell_start, sizeof(int) * ((size_t)ctx->ncells + 2));
-  ALLOC(ctx->quad_start, sizeof(int) * (4 * (size_t)ctx->ncells + 5));
-  ALLOC(ctx->part_b, sizeof(double) * 32 * (size_t)ctx->ncells);
-  ALLOC(ctx->part_c, sizeof(double) * 20 * nn);
+  ALLOC(ctx->cell_start, sizeof(int) * (max_cells + 2));
+  ALLOC(ctx->quad_start, sizeof(int) * (4 * max_cells + 5));
+  ALLOC(ctx->part_b, sizeof(double) * 32 * max_cells);
+  ALLOC(ctx->part_c, sizeof(double) * 20 * (size_t)(NX + 1) * NY);  // staggered cells: NX + 1 per row at most
   for (int g = 0; g < 4; ++g) ALLOC(ctx->geo[g], sizeof(double) * cap);
   ALLOC(ctx->geo_flags, sizeof(int) * cap);
 #ifndef MIC_EXACT
@@ -412,10 +451,28 @@ extern "C" int mic_get_bcs(mic_ctx *ctx, mic_bcs *bcs) {
   return MIC_OK;
 }
 
+// Boundary values.  A left or right vx type 2 makes the grid periodic in x, as the reference's
+// grid generators and nodal DMDAs do (gridGenerator.c:67-68, 97-98; nodalFields.c:11-19): the
+// caller's x holds the first NX of NX + 1 lines from 0 to LX, the cells, centres and tables are
+// rebuilt, and the markers are binned again.
 extern "C" int mic_set_bcs(mic_ctx *ctx, const mic_bcs *b) {
   if (!ctx || !b) return MIC_ERR_ARG;
+  const int periodic = b->mechBCLeft.type[0] == 2 || b->mechBCRight.type[0] == 2;
   if (b->mechBCTop.type[0] != 0 && b->mechBCTop.type[0] != 1) return MIC_ERR_BC;
-  if (b->mechBCLeft.type[1] != 0 && b->mechBCLeft.type[1] != 1) return MIC_ERR_BC;
+  // the left wall's vy ghost (markers.c:2014-2023) is read only on a non-periodic grid
+  if (!periodic && b->mechBCLeft.type[1] != 0 && b->mechBCLeft.type[1] != 1) return MIC_ERR_BC;
+  cudaSetDevice(ctx->device);
+  if (periodic != ctx->P.xper) {
+    // the seam line LX beyond the last line; the sort keys 4 (NX (NY-1)) + 4 fit an int
+    if (periodic && (ctx->P.NX < 4 || !(ctx->h_x[2 + ctx->P.NX - 1] < ctx->P.LX) ||
+                     4LL * ctx->P.NX * (ctx->P.NY - 1) + 4 >= 0x7FFFFFFFLL))
+      return MIC_ERR_ARG;
+    cudaError_t ce = cudaStreamSynchronize(ctx->stream);  // the tables are in use by queued work
+    if (ce != cudaSuccess) return mic_fail_cuda(ctx, ce);
+    const int e = grid_tables(ctx, periodic);
+    if (e) return e;
+    mic_invalidate_sort(ctx);
+  }
   ctx->bcs = *b;
   ctx->gen++;
   return MIC_OK;

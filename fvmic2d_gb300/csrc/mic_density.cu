@@ -646,6 +646,7 @@ extern "C" int mic_density_fill_rounds(mic_ctx *ctx, int *rounds) {
 
 extern "C" int mic_check_marker_density(mic_ctx *ctx, const mic_density_options *d, int64_t *n_added,
                                         int64_t *n_removed) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !d || d->NMX < 1 || d->NMY < 1) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   if (n_added) *n_added = 0;

@@ -194,6 +194,7 @@ __global__ void k_pressure_shift(Params P, double *p, const double *pm) {
 }  // namespace
 
 extern "C" int mic_nodal_stress_strain(mic_ctx *ctx, double dt, double gy) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx) return MIC_ERR_ARG;
   (void)gy;  // the reference's gravity argument is not read in this routine
   cudaSetDevice(ctx->device);
@@ -213,6 +214,7 @@ extern "C" int mic_nodal_stress_strain(mic_ctx *ctx, double dt, double gy) {
 }
 
 extern "C" int mic_limit_displacement_timestep(mic_ctx *ctx, double factor, double *dt) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !dt) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
@@ -247,6 +249,7 @@ extern "C" int mic_limit_displacement_timestep(mic_ctx *ctx, double factor, doub
 }
 
 extern "C" int mic_retrieve_solutions(mic_ctx *ctx, const double *S, double Kcont, int *foundnan) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || (!S && !ctx->solution)) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;
@@ -329,6 +332,7 @@ __global__ void k_vrms_final(Params P, const double *__restrict__ part, int npar
 }  // namespace
 
 extern "C" int mic_nusselt_number(mic_ctx *ctx, double bottom_T, double top_T, double *Nu) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !Nu) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   double *d = ctx->red_buf + 40;
@@ -343,6 +347,7 @@ extern "C" int mic_nusselt_number(mic_ctx *ctx, double bottom_T, double top_T, d
 }
 
 extern "C" int mic_rms_velocity(mic_ctx *ctx, double *vrms) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !vrms) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   constexpr int kParts = 64;

@@ -67,6 +67,8 @@ struct CreepCounters {
 
 struct Params {  // everything a kernel needs besides the marker columns; passed by value
   int NX, NY;
+  int NCX;   // basic cells in x: NX - 1, or NX on a grid periodic in x (line NX is line 0's image)
+  int xper;  // periodic in x: node column NX is column 0, NX + 1 is 1, -1 is NX - 1
   double LX, LY;
   const double *x, *y, *xc, *yc;  // point at index 0 (ghost entries at -2, -1 exist)
   const long long *xbits, *ybits; // bit patterns of x[0..NX-1], y[0..NY-1] for integer compares
@@ -383,23 +385,31 @@ __device__ __forceinline__ double div_sp(double num, double den, double inv) {
 // Running bilinear sum in the order 00, 01, 10, 11 of updateMarkerStrainPressure.c:152-158,
 // subgridStressChanges.c:97-102 and updateMarkerStress.c:84-93.
 // The same running sum with the weights given.
+// Node column i + 1 wraps to 0 at NX: only on a grid periodic in x does an interpolation cell
+// reach column NX (the seam's image of column 0); elsewhere i + 1 <= NX - 1.
+__device__ __forceinline__ int next_col(int i, int NX) { return (i + 1 == NX) ? 0 : i + 1; }
+// node column of a periodic local index in [-NX, 2 NX)
+__device__ __forceinline__ int wrap_col(int i, int NX) { return i < 0 ? i + NX : (i >= NX ? i - NX : i); }
+
 __device__ __forceinline__ double interp_w(const double *__restrict__ f, int NX, int i, int j, const W4 &w) {
-  const size_t k = (size_t)j * NX + i;
-  double s = w.w00 * __ldg(f + k);
-  s = fma(w.w01, __ldg(f + k + NX), s);
-  s = fma(w.w10, __ldg(f + k + 1), s);
-  s = fma(w.w11, __ldg(f + k + NX + 1), s);
+  const size_t r0 = (size_t)j * NX, r1 = r0 + NX;
+  const int i1 = next_col(i, NX);
+  double s = w.w00 * __ldg(f + r0 + i);
+  s = fma(w.w01, __ldg(f + r1 + i), s);
+  s = fma(w.w10, __ldg(f + r0 + i1), s);
+  s = fma(w.w11, __ldg(f + r1 + i1), s);
   return s;
 }
 
 __device__ __forceinline__ double interp_run(const double *__restrict__ f, int NX, int i, int j, double mdx,
                                              double mdy) {
-  const size_t k = (size_t)j * NX + i;
+  const size_t r0 = (size_t)j * NX, r1 = r0 + NX;
+  const int i1 = next_col(i, NX);
   double s = 0.0;
-  s += (1.0 - mdx) * (1.0 - mdy) * __ldg(f + k);
-  s += (1.0 - mdx) * mdy * __ldg(f + k + NX);
-  s += mdx * (1.0 - mdy) * __ldg(f + k + 1);
-  s += mdx * mdy * __ldg(f + k + NX + 1);
+  s += (1.0 - mdx) * (1.0 - mdy) * __ldg(f + r0 + i);
+  s += (1.0 - mdx) * mdy * __ldg(f + r1 + i);
+  s += mdx * (1.0 - mdy) * __ldg(f + r0 + i1);
+  s += mdx * mdy * __ldg(f + r1 + i1);
   return s;
 }
 

@@ -43,17 +43,23 @@ __device__ __forceinline__ void small_angle_rotation(double t, double &c, double
 
 #ifdef MIC_EXACT
 // Interpolation cell at cell centres (updateMarkerStrainPressure.c:137-150, updateMarkerStress.c:66-80,
-// subgridStressChanges.c:179-190): staggered cell clamped to the interior [1, NX-2] x [1, NY-2].
-// Where the clamp leaves the staggered cell unchanged the offsets are the projection geometry.
+// subgridStressChanges.c:179-190): staggered cell clamped to [1, cmax] x [1, NY-2].  Where the
+// clamp leaves the staggered cell unchanged the offsets are the projection geometry.
 __device__ __forceinline__ void centre_interp(const Params &P, int cx, int cy, int fl, double gx1, double gy1,
-                                              double x, double y, int &i, int &j, double &mdx, double &mdy) {
+                                              double x, double y, int cmax, int &i, int &j, double &mdx,
+                                              double &mdy) {
   const int sx = cx + (fl & 1), sy = cy + ((fl >> 1) & 1);
-  i = clampi(sx, 1, P.NX - 2);
+  i = clampi(sx, 1, cmax);
   j = clampi(sy, 1, P.NY - 2);
   mdx = (i == sx) ? gx1 : div_sp(x - P.xc[i], P.hxc[i], P.ixc[i]);
   mdy = (j == sy) ? gy1 : div_sp(y - P.yc[j], P.hyc[j], P.iyc[j]);
 }
 #endif
+
+// Largest staggered interpolation cell of updateMarkerStrainPressure and updateMarkerStress
+// (cellXMax: NX - 2, NX - 1 on a grid periodic in x; updateMarkerStrainPressure.c:137-147,
+// updateMarkerStress.c:66-77).  subgridStressChanges keeps NX - 2 either way (its lines 92, 187).
+__device__ __forceinline__ int centre_cmax(const Params &P) { return P.xper ? P.NX - 1 : P.NX - 2; }
 
 // limitViscosity (viscosity.c:90-104) on one viscosity
 __device__ __forceinline__ double limit_eta(double e, const mic_options &O) {
@@ -297,10 +303,11 @@ struct Geo {
 // Centre-cell weights of marker m: the stored ones, unless the interior clamp of centre_interp
 // moved the cell (then formed from the offsets, as centre_interp forms them).
 __device__ __forceinline__ W4 centre_w(const Params &P, const Geo &g, int64_t m, int cx, int cy,
-                                       const double *__restrict__ X, const double *__restrict__ Y, int &i, int &j) {
+                                       const double *__restrict__ X, const double *__restrict__ Y, int cmax, int &i,
+                                       int &j) {
   const int fl = g.flags[m];
   const int sx = cx + (fl & 1), sy = cy + ((fl >> 1) & 1);
-  i = clampi(sx, 1, P.NX - 2);
+  i = clampi(sx, 1, cmax);
   j = clampi(sy, 1, P.NY - 2);
   if (i == sx && j == sy) return load_w4(g.w1, m);
   const double mdx = (i == sx) ? g.gx1[m] : div_sp(X[m] - P.xc[i], P.hxc[i], P.ixc[i]);
@@ -333,7 +340,7 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
 #ifdef MIC_EXACT
   const double x = c.X[m], y = c.Y[m];
   double mdx, mdy;
-  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], x, y, i, j, mdx, mdy);
+  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], x, y, centre_cmax(P), i, j, mdx, mdy);
   c.p[m] = interp_run(nd.p, NX, i, j, mdx, mdy);
   const double mexx = interp_run(nd.exx, NX, i, j, mdx, mdy);
   const double msxx = interp_run(nd.soxx, NX, i, j, mdx, mdy);
@@ -346,7 +353,7 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
   const double msxy = interp_run(nd.soxy, NX, cx, cy, bx, by);
   const double mdsxy = interp_run(nd.dsxy, NX, cx, cy, bx, by);
 #else
-  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
+  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, centre_cmax(P), i, j);
   c.p[m] = interp_w(nd.p, NX, i, j, wc);
   const double mexx = interp_w(nd.exx, NX, i, j, wc);
   const double msxx = interp_w(nd.soxx, NX, i, j, wc);
@@ -460,18 +467,24 @@ __device__ __forceinline__ void subgrid_stress_one(const Params &P, const Subgri
 #endif
   if (sdif < -30.0) sdif = -30.0;
   sdif = 1.0 - exp(sdif);
+  // the basic cell clamped to [0, NX-2] (subgridStressChanges.c:91-92): only a marker in the
+  // last cell of a grid periodic in x moves, and its offset is formed again
+  const int bxc = min(cx, P.NX - 2);
+  const double bmdx = (bxc == cx) ? g.gx0[m] : div_sp(c.X[m] - P.x[bxc], P.hx[bxc], P.ix[bxc]);
 #ifdef MIC_EXACT
   (void)reuse;
-  double dsxy = interp_run(nd.soxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]) - c.sxy[m];
+  double dsxy = interp_run(nd.soxy, P.NX, bxc, cy, bmdx, g.gy0[m]) - c.sxy[m];
 #else
-  double dsxy = (reuse ? c.dxy[m] : interp_w(nd.soxy, P.NX, cx, cy, load_w4(g.w0, m))) - c.sxy[m];
+  double dsxy = (reuse ? c.dxy[m]
+                       : interp_w(nd.soxy, P.NX, bxc, cy, (bxc == cx) ? load_w4(g.w0, m) : make_w4(bmdx, g.gy0[m]))) -
+                c.sxy[m];
 #endif
   dsxy *= sdif;
   c.sxy[m] = c.sxy[m] + dsxy;
   int i, j;
 #ifdef MIC_EXACT
   double mdx, mdy;
-  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], i, j, mdx, mdy);
+  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], P.NX - 2, i, j, mdx, mdy);
   double dsxx = interp_run(nd.soxx, P.NX, i, j, mdx, mdy) - c.sxx[m];
   dsxx *= sdif;
   c.sxx[m] = c.sxx[m] + dsxx;
@@ -482,7 +495,7 @@ __device__ __forceinline__ void subgrid_stress_one(const Params &P, const Subgri
     msxx = c.dxx[m];
     msyy = c.dyy[m];
   } else {
-    const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
+    const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, P.NX - 2, i, j);
     msxx = interp_w(nd.soxx, P.NX, i, j, wc);
     msyy = interp_w(nd.soyy, P.NX, i, j, wc);
   }
@@ -499,8 +512,49 @@ __device__ __forceinline__ void subgrid_stress_one(const Params &P, const Subgri
 }
 
 #ifdef MIC_EXACT
+// sums of local column L of node row j (the node's own column, or its periodic image)
+__device__ __forceinline__ void subgrid_column(const Params &P, const int *__restrict__ cellX,
+                                               const double *__restrict__ gx0, const double *__restrict__ gy0,
+                                               const double *__restrict__ dxy, const double *__restrict__ dxx,
+                                               const double *__restrict__ dyy, const int *__restrict__ cs, int L,
+                                               int j, double &sxy, double &wxy, double &sxx, double &syy,
+                                               double &wn) {
+  const int NC = P.NCX;
+  const long long half = 0x3FE0000000000000LL;
+  const int cy0 = max(j - 1, 0), cy1 = min(j, P.NY - 2);
+  const int cx0 = max(L - 1, 0), cx1 = min(L, NC - 1);
+  if (cx0 <= cx1) {
+    for (int cy = cy0; cy <= cy1; ++cy) {
+      const int mb = cs[cy * NC + cx0], me = cs[cy * NC + cx1 + 1];
+      const int oy = j - cy;
+      for (int m = mb; m < me; ++m) {
+        const int ox = L - cellX[m];
+        const double mx = gx0[m], my = gy0[m];
+        const long long bx = nonneg_bits(mx), by = nonneg_bits(my);
+        const bool inx = ox ? (bx >= half) : (bx <= half);
+        const bool iny = oy ? (by >= half) : (by <= half);
+        if (inx && iny) {
+          const double w = (ox ? mx : (1.0 - mx)) * (oy ? my : (1.0 - my));
+          sxy = sxy + w * dxy[m];
+          wxy = wxy + w;
+        }
+      }
+    }
+  }
+  if (L >= 1 && L - 1 < NC && j >= 1) {
+    const int c = (j - 1) * NC + (L - 1);
+    for (int m = cs[c]; m < cs[c + 1]; ++m) {
+      const double w = (1.0 - fabs(0.5 - gx0[m])) * (1.0 - fabs(0.5 - gy0[m]));
+      sxx += w * dxx[m];
+      syy += w * dyy[m];
+      wn += w;
+    }
+  }
+}
+
 // subgridStressChanges, node part (134-175 quadrant scatter, 227-233 centre scatter, 258-286
-// divide and subtract) as a gather in marker order.
+// divide and subtract) as a gather in marker order.  Periodic in x, nodes 0 and 1 add their seam
+// image's sums after their own.
 __global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const int *__restrict__ cellX,
                                                               const double *__restrict__ gx0,
                                                               const double *__restrict__ gy0,
@@ -512,42 +566,16 @@ __global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const in
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= P.NX || j >= P.NY) return;
-  const int NC = P.NX - 1;
-  const long long half = 0x3FE0000000000000LL;
-  double sxy = 0.0, wxy = 0.0;
-  const int cy0 = max(j - 1, 0), cy1 = min(j, P.NY - 2);
-  const int cx0 = max(i - 1, 0), cx1 = min(i, P.NX - 2);
-  for (int cy = cy0; cy <= cy1; ++cy) {
-    const int mb = cs[cy * NC + cx0], me = cs[cy * NC + cx1 + 1];
-    const int oy = j - cy;
-    for (int m = mb; m < me; ++m) {
-      const int ox = i - cellX[m];
-      const double mx = gx0[m], my = gy0[m];
-      const long long bx = nonneg_bits(mx), by = nonneg_bits(my);
-      const bool inx = ox ? (bx >= half) : (bx <= half);
-      const bool iny = oy ? (by >= half) : (by <= half);
-      if (inx && iny) {
-        const double w = (ox ? mx : (1.0 - mx)) * (oy ? my : (1.0 - my));
-        sxy = sxy + w * dxy[m];
-        wxy = wxy + w;
-      }
-    }
-  }
-  double sxx = 0.0, syy = 0.0, wn = 0.0;
-  if (i >= 1 && j >= 1) {
-    const int c = (j - 1) * NC + (i - 1);
-    for (int m = cs[c]; m < cs[c + 1]; ++m) {
-      const double w = (1.0 - fabs(0.5 - gx0[m])) * (1.0 - fabs(0.5 - gy0[m]));
-      sxx += w * dxx[m];
-      syy += w * dyy[m];
-      wn += w;
-    }
-  }
+  double sxy = 0.0, wxy = 0.0, sxx = 0.0, syy = 0.0, wn = 0.0;
+  double sxy2 = 0.0, wxy2 = 0.0, sxx2 = 0.0, syy2 = 0.0, wn2 = 0.0;
+  subgrid_column(P, cellX, gx0, gy0, dxy, dxx, dyy, cs, i, j, sxy, wxy, sxx, syy, wn);
+  if (P.xper && i + P.NX <= P.NCX + 1)
+    subgrid_column(P, cellX, gx0, gy0, dxy, dxx, dyy, cs, i + P.NX, j, sxy2, wxy2, sxx2, syy2, wn2);
   const size_t q = (size_t)j * P.NX + i;
-  const double W = 0.0 + wxy, Wn = 0.0 + wn;
-  const double gxy = (W != 0.0) ? (0.0 + sxy) / W : 0.0;
-  const double gxx = (Wn != 0.0) ? (0.0 + sxx) / Wn : 0.0;
-  const double gyy = (Wn != 0.0) ? (0.0 + syy) / Wn : 0.0;
+  const double W = (0.0 + wxy) + wxy2, Wn = (0.0 + wn) + wn2;
+  const double gxy = (W != 0.0) ? ((0.0 + sxy) + sxy2) / W : 0.0;
+  const double gxx = (Wn != 0.0) ? ((0.0 + sxx) + sxx2) / Wn : 0.0;
+  const double gyy = (Wn != 0.0) ? ((0.0 + syy) + syy2) / Wn : 0.0;
   dsxx[q] = dsxx[q] + -1.0 * gxx;
   dsyy[q] = dsyy[q] + -1.0 * gyy;
   dsxy[q] = dsxy[q] + -1.0 * gxy;
@@ -571,7 +599,7 @@ __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double
                                                           const double *__restrict__ dyy,
                                                           const int *__restrict__ cs, double *__restrict__ part) {
   __shared__ double sloc[8][128];
-  const int ncells = (P.NX - 1) * (P.NY - 1);
+  const int ncells = P.NCX * (P.NY - 1);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   const int t = threadIdx.x;
@@ -623,24 +651,28 @@ __global__ void __launch_bounds__(128) k_subgrid_combine(Params P, const double 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= P.NX || j >= P.NY) return;
-  const int NC = P.NX - 1, ncells = NC * (P.NY - 1);
-  double sxy = 0.0, wxy = 0.0;
+  const int NC = P.NCX, ncells = NC * (P.NY - 1);
+  double sxy = 0.0, wxy = 0.0, sxx = 0.0, syy = 0.0, wn = 0.0;
+  // the node's own local column and, periodic in x, its seam image (nodes 0 and 1)
+  const int nL = (P.xper && i + P.NX <= NC + 1) ? 2 : 1;
+  for (int l = 0; l < nL; ++l) {
+    const int L = i + l * P.NX;
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int dx = r & 1, dy = r >> 1;
-    const int cx = i - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
-    if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
-      const size_t cc = (size_t)cy * NC + cx;
-      sxy += part[(size_t)(2 * k) * ncells + cc];
-      wxy += part[(size_t)(2 * k + 1) * ncells + cc];
+    for (int r = 0; r < 4; ++r) {
+      const int dx = r & 1, dy = r >> 1;
+      const int cx = L - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
+      if (cx >= 0 && cx < NC && cy >= 0 && cy <= P.NY - 2) {
+        const size_t cc = (size_t)cy * NC + cx;
+        sxy += part[(size_t)(2 * k) * ncells + cc];
+        wxy += part[(size_t)(2 * k + 1) * ncells + cc];
+      }
     }
-  }
-  double sxx = 0.0, syy = 0.0, wn = 0.0;
-  if (i >= 1 && j >= 1 && i <= P.NX - 1 && j <= P.NY - 1) {
-    const size_t cc = (size_t)(j - 1) * NC + (i - 1);
-    sxx = part[(size_t)8 * ncells + cc];
-    syy = part[(size_t)9 * ncells + cc];
-    wn = part[(size_t)10 * ncells + cc];
+    if (L >= 1 && j >= 1 && L - 1 < NC && j <= P.NY - 1) {
+      const size_t cc = (size_t)(j - 1) * NC + (L - 1);
+      sxx += part[(size_t)8 * ncells + cc];
+      syy += part[(size_t)9 * ncells + cc];
+      wn += part[(size_t)10 * ncells + cc];
+    }
   }
   const size_t q = (size_t)j * P.NX + i;
   const double W = 0.0 + wxy, Wn = 0.0 + wn;
@@ -670,11 +702,11 @@ __device__ __forceinline__ void update_stress_one(const Params &P, const StressC
   int i, j;
 #ifdef MIC_EXACT
   double mdx, mdy;
-  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], i, j, mdx, mdy);
+  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], centre_cmax(P), i, j, mdx, mdy);
   const double mdsxx = interp_run(nd.dsxx, P.NX, i, j, mdx, mdy);
   const double mdsyy = interp_run(nd.dsyy, P.NX, i, j, mdx, mdy);
 #else
-  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, i, j);
+  const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, centre_cmax(P), i, j);
   const double mdsxx = interp_w(nd.dsxx, P.NX, i, j, wc);
   const double mdsyy = interp_w(nd.dsyy, P.NX, i, j, wc);
 #endif
@@ -705,7 +737,8 @@ __device__ __forceinline__ void subgridT_markers_one(const Params &P, const SubT
   if (i == -1) return;
   const int NX = P.NX;
 #ifdef MIC_EXACT
-  const size_t k00 = (size_t)j * NX + i, k10 = k00 + 1, k01 = k00 + NX, k11 = k01 + 1;
+  // (node column i + 1 wraps to 0 across the seam of a grid periodic in x)
+  const size_t k00 = (size_t)j * NX + i, k10 = (size_t)j * NX + next_col(i, NX), k01 = k00 + NX, k11 = k10 + NX;
   const double mdx = g.gx0[m], mdy = g.gy0[m];
   const double dx = P.x[i + 1] - P.x[i], dy = P.y[j + 1] - P.y[j];
   const double Tm = Tn[k00] * (1.0 - mdx) * (1.0 - mdy) + Tn[k10] * mdx * (1.0 - mdy) +
@@ -751,10 +784,10 @@ __device__ __forceinline__ void subgridT_apply_one(const Params &P, const SubTCo
   const int i = c.cellX[m], j = c.cellY[m];
   if (i == -1) return;
 #ifdef MIC_EXACT
-  const size_t k00 = (size_t)j * P.NX + i;
+  const size_t k00 = (size_t)j * P.NX + i, k10 = (size_t)j * P.NX + next_col(i, P.NX);
   const double mdx = g.gx0[m], mdy = g.gy0[m];
   const double dtm = (dT[k00] * (1.0 - mdy) * (1.0 - mdx) + dT[k00 + P.NX] * mdy * (1.0 - mdx) +
-                      dT[k00 + 1] * (1.0 - mdy) * mdx + dT[k00 + P.NX + 1] * mdy * mdx) +
+                      dT[k10] * (1.0 - mdy) * mdx + dT[k10 + P.NX] * mdy * mdx) +
                      c.dTsub[m];
 #else
   const double dtm = interp_w(dT, P.NX, i, j, load_w4(g.w0, m)) + c.dTsub[m];
@@ -848,6 +881,9 @@ struct AdvectCols {
 struct AdvectCoef {
   const void *cvx, *cvy, *cwz;
 };
+__device__ __forceinline__ double advect_tail(const Params &P, const AdvectCols &c, double dt, int64_t m, double X0,
+                                              double Y0, const double *mvx, const double *mvy, const double *mwz);
+
 __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCols &c, const Geo &g,
                                                 const double *__restrict__ vx, const double *__restrict__ vy,
                                                 const double *__restrict__ wz, const AdvectCoef &cv,
@@ -997,6 +1033,14 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     }
 #endif
   }
+  return advect_tail(P, c, dt, m, X0, Y0, mvx, mvy, mwz);
+}
+
+// The RK4 average of the four stages, the new position (wrapped across the seam of a grid
+// periodic in x, markers.c:2225-2231), the stress rotation and the accumulated strain
+// (markers.c:2120-2223).  Returns the rotated sxx.
+__device__ __forceinline__ double advect_tail(const Params &P, const AdvectCols &c, double dt, int64_t m, double X0,
+                                              double Y0, const double *mvx, const double *mvy, const double *mwz) {
 #ifdef MIC_EXACT
   const double VX = div6(mvx[0] + 2 * mvx[1] + 2 * mvx[2] + mvx[3]);
   const double VY = div6(mvy[0] + 2 * mvy[1] + 2 * mvy[2] + mvy[3]);
@@ -1004,7 +1048,7 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
   c.VX[m] = VX;
   c.VY[m] = VY;
   c.wxy[m] = w;
-  c.X[m] = X0 + dt * VX;
+  double Xn = X0 + dt * VX;
   c.Y[m] = Y0 + dt * VY;
 #else
   const double inv6 = 0.16666666666666666;
@@ -1014,9 +1058,16 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
   c.VX[m] = VX;
   c.VY[m] = VY;
   c.wxy[m] = w;
-  c.X[m] = fma(dt, VX, X0);
+  double Xn = fma(dt, VX, X0);
   c.Y[m] = fma(dt, VY, Y0);
 #endif
+  if (P.xper) {
+    if (Xn > P.LX)
+      Xn -= P.LX;
+    else if (Xn < 0)
+      Xn += P.LX;
+  }
+  c.X[m] = Xn;
   const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
   const double th = -w * dt;
 #ifdef MIC_EXACT
@@ -1041,6 +1092,87 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
   return nsxx;
 }
 
+// advectMarkersRK on a grid periodic in x (markers.c:1907-1913, 1928-1944, 1961-1966, 2014-2023):
+// the cell walk runs over cells -1 .. NX-1 (line -1 and NX are the seam's images), the vx and vy
+// cells are not clamped in x, node columns wrap, and the left wall has no ghost values.  The
+// reference's own divisions, in both builds (periodic grids are small).
+__device__ double advect_marker_periodic(const Params &P, const AdvectCols &c, const double *__restrict__ vx,
+                                         const double *__restrict__ vy, const double *__restrict__ wz,
+                                         const mic_bcinfo &top, double dt, int64_t m, int ci, int cj) {
+  const int NX = P.NX, NY = P.NY;
+  const double X0 = c.X[m], Y0 = c.Y[m];
+  double xcur = X0, ycur = Y0;
+  double mvx[4], mvy[4], mwz[4];
+  for (int s = 0; s < 4; ++s) {
+    int i = ci, j = cj;
+    if (xcur > P.x[i + 1]) {
+      while (xcur > P.x[i + 1] && i < NX - 1) i++;
+    } else if (xcur < P.x[i]) {
+      while (xcur < P.x[i] && i > -1) i--;
+    }
+    if (ycur > P.y[j + 1]) {
+      while (ycur > P.y[j + 1] && j < NY - 2) j++;
+    } else if (ycur < P.y[j]) {
+      while (ycur < P.y[j] && j > 0) j--;
+    }
+    int vxX = i, vxY = j, vyX = i, vyY = j;
+    if (vxY > -1 && ycur < P.yc[vxY + 1]) vxY--;
+    if (vyX > -1 && xcur < P.xc[vyX + 1]) vyX--;
+    vxY = clampi(vxY, -1, NY - 2);
+    vyY = clampi(vyY, 0, NY - 2);
+    const int a0 = wrap_col(vxX, NX), a1 = wrap_col(vxX + 1, NX);
+    double deltaxm = xcur - P.x[vxX], deltaym = ycur - P.yc[vxY + 1];
+    double dx = P.x[vxX + 1] - P.x[vxX], dy = P.yc[vxY + 2] - P.yc[vxY + 1];
+    const size_t r1 = (size_t)(vxY + 1) * NX;
+    double vul, vur;
+    if (vxY == -1 && top.type[0] == 0) {
+      vul = 2.0 * top.value[0] - vx[r1 + a0];
+      vur = 2.0 * top.value[0] - vx[r1 + a1];
+    } else if (vxY == -1) {
+      vul = vx[r1 + a0];
+      vur = vx[r1 + a1];
+    } else {
+      vul = vx[r1 - NX + a0];
+      vur = vx[r1 - NX + a1];
+    }
+    const double vll = vx[r1 + a0], vlr = vx[r1 + a1];
+    double t = vul * (1.0 - deltaxm / dx) * (1.0 - deltaym / dy);
+    t += vur * (deltaxm / dx) * (1.0 - deltaym / dy);
+    t += vll * (1.0 - deltaxm / dx) * (deltaym / dy);
+    t += vlr * (deltaxm * deltaym) / dx / dy;
+    mvx[s] = t;
+    const int b0 = wrap_col(vyX, NX), b1 = wrap_col(vyX + 1, NX);
+    const size_t q0 = (size_t)vyY * NX, q1 = q0 + NX;
+    const double wul = vy[q0 + b0], wur = vy[q0 + b1], wll = vy[q1 + b0], wlr = vy[q1 + b1];
+    deltaxm = xcur - P.xc[vyX + 1];
+    deltaym = ycur - P.y[vyY];
+    dx = P.xc[vyX + 2] - P.xc[vyX + 1];
+    dy = P.y[vyY + 1] - P.y[vyY];
+    t = wul * (1.0 - deltaxm / dx) * (1.0 - deltaym / dy);
+    t += wur * (deltaxm / dx) * (1.0 - deltaym / dy);
+    t += wll * (1.0 - deltaxm / dx) * (deltaym / dy);
+    t += wlr * (deltaxm * deltaym) / dx / dy;
+    mvy[s] = t;
+    const int z0 = wrap_col(i, NX), z1 = wrap_col(i + 1, NX);
+    const double mdx = (xcur - P.x[i]) / (P.x[i + 1] - P.x[i]);
+    const double mdy = (ycur - P.y[j]) / (P.y[j + 1] - P.y[j]);
+    const size_t k0 = (size_t)j * NX, k1 = k0 + NX;
+    t = (1.0 - mdx) * (1.0 - mdy) * wz[k0 + z0];
+    t += (mdx) * (1.0 - mdy) * wz[k0 + z1];
+    t += (1.0 - mdx) * (mdy)*wz[k1 + z0];
+    t += (mdx) * (mdy)*wz[k1 + z1];
+    mwz[s] = t;
+    if (s < 2) {
+      xcur = X0 + dt / 2 * mvx[s];
+      ycur = Y0 + dt / 2 * mvy[s];
+    } else if (s == 2) {
+      xcur = X0 + dt * mvx[s];
+      ycur = Y0 + dt * mvy[s];
+    }
+  }
+  return advect_tail(P, c, dt, m, X0, Y0, mvx, mvy, mwz);
+}
+
 // one marker; returns the bits of |sxx| after the rotation for an in-domain marker, else 0
 __device__ __forceinline__ long long advect_one(const Params &P, const AdvectCols &c, const Geo &g,
                                                 const double *__restrict__ vx, const double *__restrict__ vy,
@@ -1051,7 +1183,8 @@ __device__ __forceinline__ long long advect_one(const Params &P, const AdvectCol
   if (m < n) {
     const int ci = c.cellX[m], cj = c.cellY[m];
     if (ci != -1) {
-      const double a = fabs(advect_marker(P, c, g, vx, vy, wz, cv, top, left, dt, m, ci, cj, wz_known));
+      const double a = fabs(P.xper ? advect_marker_periodic(P, c, vx, vy, wz, top, dt, m, ci, cj)
+                                   : advect_marker(P, c, g, vx, vy, wz, cv, top, left, dt, m, ci, cj, wz_known));
       if (a > 0.0) b = __double_as_longlong(a);
     }
   }
@@ -1085,9 +1218,10 @@ __global__ void k_nodal_to_markers(Params P, const int *cellX, const int *cellY,
   const int i = cellX[m], j = cellY[m];
   if (i == -1) return;
   const double mdx = g.gx0[m], mdy = g.gy0[m];
-  const size_t k = (size_t)j * P.NX + i;
-  dst[m] = f[k] * (1 - mdx) * (1 - mdy) + f[k + P.NX] * (1 - mdx) * mdy + f[k + 1] * (mdx) * (1 - mdy) +
-           f[k + P.NX + 1] * mdx * mdy;
+  const size_t r0 = (size_t)j * P.NX, r1 = r0 + P.NX;
+  const int i1 = next_col(i, P.NX);  // the seam image of column 0 on a grid periodic in x
+  dst[m] = f[r0 + i] * (1 - mdx) * (1 - mdy) + f[r1 + i] * (1 - mdx) * mdy + f[r0 + i1] * (mdx) * (1 - mdy) +
+           f[r1 + i1] * mdx * mdy;
 }
 
 Geo geo_of(mic_ctx *ctx) {
@@ -2027,7 +2161,7 @@ static int advect_launch(mic_ctx *ctx, double dt, bool wz_known, bool with_max =
     c.exy = ctx->f64[C_EXY];
     AdvectCoef cv = {nullptr, nullptr, nullptr};
 #ifndef MIC_EXACT
-    {
+    if (!ctx->P.xper) {  // (the periodic advection interpolates the nodes directly)
       const int NX = ctx->P.NX, NY = ctx->P.NY;
       const size_t nn = (size_t)NX * NY;
       if (!ctx->adv_coef && cudaMalloc((void **)&ctx->adv_coef, 3 * nn * sizeof(Bil4)) != cudaSuccess) {
@@ -2101,7 +2235,9 @@ int mic_step_segment(mic_ctx *ctx, int seg, double dt_disp, double dt_thermal, i
 #ifdef MIC_EXACT
   const bool keep = false;
 #else
-  const bool keep = sub && ctx->n > 0;
+  // (not on a grid periodic in x: there the sub-grid pass clamps the marker's cells differently
+  // from the strain-rate pass, subgridStressChanges.c:91-92, 186-187)
+  const bool keep = sub && ctx->n > 0 && !ctx->P.xper;
 #endif
   switch (seg) {
     case 0:

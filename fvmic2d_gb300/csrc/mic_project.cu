@@ -13,7 +13,15 @@
 //
 // Node index NX or NY (the ghost column/row of fvmic2d's ghosted DMDA) receives no
 // contribution (its ADD_VALUES would be dropped); a node whose weight sum is zero is
-// set to zero.
+// set to zero.  On a grid periodic in x the ghost columns are the periodic images: local column
+// NX adds into node column 0, NX + 1 into 1 and -1 into NX - 1, after the column's own sum (the
+// order of DMLocalToGlobal's ADD on a periodic DMDA).  A node kernel then gathers each of its
+// local columns L in {i, i + NX (, i - NX)} separately and adds them in that order.
+//
+// Staggered (cell-centre) cells sx run over [0, NCX] (NCX basic cells in x: NX - 1, or NX when
+// periodic) and are stored with a row stride of NX + 1.
+#include <climits>
+
 #include "mic_internal.cuh"
 
 using namespace mic;
@@ -39,68 +47,82 @@ struct MarkerView {
 };
 
 #ifdef MIC_EXACT  // the product build projects through per-cell partials (below)
-// One thread per node (i, j): basic-node sums (rho, etaS, k, T, Cp with ARITHMETIC weights;
-// soxy with the nearest-node ARITHMETIC_LOCAL weight) and cell-centre sums (etaN ARITHMETIC;
-// soxx, soyy ARITHMETIC_LOCAL) in the marker order of markerProjection.c:115-229.
-__global__ void __launch_bounds__(128) k_project_all2(Params P, MarkerView mv, const int *__restrict__ cs,
-                                                       mic_materials mat, All2Out o) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i >= P.NX || j >= P.NY) return;
-  const int NC = P.NX - 1;
-  double sRho = 0.0, sEtaS = 0.0, sK = 0.0, sT = 0.0, sCp = 0.0, w0 = 0.0, sSxy = 0.0, w3 = 0.0;
-  double sEtaN = 0.0, w1 = 0.0, sSxx = 0.0, sSyy = 0.0, w2 = 0.0;
+struct All2Sums {
+  double rho, etaS, k, T, Cp, w0, sxy, w3, etaN, w1, sxx, syy, w2;
+};
+
+// the sums of local column L (node column i, or its periodic image i + NX) of node row j, over
+// the markers of the cells that can touch it, in marker order
+__device__ __forceinline__ void all2_column(const Params &P, const MarkerView &mv, const int *__restrict__ cs,
+                                            const mic_materials &mat, int L, int j, All2Sums &S) {
+  const int NC = P.NCX;
   const int cy0 = max(j - 2, 0), cy1 = min(j, P.NY - 2);
-  const int cx0 = max(i - 2, 0), cx1 = min(i, P.NX - 2);
+  const int cx0 = max(L - 2, 0), cx1 = min(L, NC - 1);
+  if (cx0 > cx1) return;
   for (int cy = cy0; cy <= cy1; ++cy) {
     const int mb = cs[cy * NC + cx0], me = cs[cy * NC + cx1 + 1];
     for (int m = mb; m < me; ++m) {
       const int cx = mv.cellX[m];
       const int fl = mv.flags[m];
       // cell-centre node: staggered cell (sx, sy) = (cx + qx, cy + qy), corners sx..sx+1
-      const int ox = i - (cx + (fl & 1)), oy = j - (cy + ((fl >> 1) & 1));
+      const int ox = L - (cx + (fl & 1)), oy = j - (cy + ((fl >> 1) & 1));
       if ((unsigned)ox <= 1u && (unsigned)oy <= 1u) {
         const double mx = mv.gx1[m], my = mv.gy1[m];
         const double w = (ox ? mx : (1.0 - mx)) * (oy ? my : (1.0 - my));
-        sEtaN += w * mv.eta[m];
-        w1 += w;
+        S.etaN += w * mv.eta[m];
+        S.w1 += w;
         if (ox == ((fl >> 4) & 1) && oy == ((fl >> 5) & 1)) {
-          sSxx += w * mv.sxx[m];
-          sSyy += w * mv.syy[m];
-          w2 += w;
+          S.sxx += w * mv.sxx[m];
+          S.syy += w * mv.syy[m];
+          S.w2 += w;
         }
       }
       // basic node: cell (cx, cy) corners cx..cx+1
-      const int bx = i - cx, by = j - cy;
+      const int bx = L - cx, by = j - cy;
       if ((unsigned)bx <= 1u && (unsigned)by <= 1u) {
         const double mx = mv.gx0[m], my = mv.gy0[m];
         const double w = (bx ? mx : (1.0 - mx)) * (by ? my : (1.0 - my));
         const int k = mv.mat[m];
-        sRho += w * mv.rho[m];
-        sEtaS += w * mv.eta[m];
-        sK += w * mat.materialkThermal[k];
-        sT += w * mv.T[m];
-        sCp += w * mat.materialCp[k];
-        w0 += w;
+        S.rho += w * mv.rho[m];
+        S.etaS += w * mv.eta[m];
+        S.k += w * mat.materialkThermal[k];
+        S.T += w * mv.T[m];
+        S.Cp += w * mat.materialCp[k];
+        S.w0 += w;
         if (bx == ((fl >> 2) & 1) && by == ((fl >> 3) & 1)) {
-          sSxy += w * mv.sxy[m];
-          w3 += w;
+          S.sxy += w * mv.sxy[m];
+          S.w3 += w;
         }
       }
     }
   }
+}
+
+// One thread per node (i, j): basic-node sums (rho, etaS, k, T, Cp with ARITHMETIC weights;
+// soxy with the nearest-node ARITHMETIC_LOCAL weight) and cell-centre sums (etaN ARITHMETIC;
+// soxx, soyy ARITHMETIC_LOCAL) in the marker order of markerProjection.c:115-229.  Periodic in
+// x, nodes 0 and 1 add their seam image's sums (local columns NX, NX + 1) after their own.
+__global__ void __launch_bounds__(128) k_project_all2(Params P, MarkerView mv, const int *__restrict__ cs,
+                                                       mic_materials mat, All2Out o) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= P.NX || j >= P.NY) return;
+  All2Sums A = {}, B = {};
+  all2_column(P, mv, cs, mat, i, j, A);
+  if (P.xper && i + P.NX <= P.NCX + 1) all2_column(P, mv, cs, mat, i + P.NX, j, B);
+  // global = 0 + the column's local sum (+ the seam image's), then a guarded divide
+  const double W0 = (0.0 + A.w0) + B.w0, W1 = (0.0 + A.w1) + B.w1, W2 = (0.0 + A.w2) + B.w2,
+               W3 = (0.0 + A.w3) + B.w3;
   const size_t q = (size_t)j * P.NX + i;
-  // global = 0 + local sum (DMLocalToGlobal ADD into a zeroed vector), then a guarded divide
-  const double W0 = 0.0 + w0, W1 = 0.0 + w1, W2 = 0.0 + w2, W3 = 0.0 + w3;
-  o.rho[q] = (W0 != 0.0) ? (0.0 + sRho) / W0 : 0.0;
-  o.etaS[q] = (W0 != 0.0) ? (0.0 + sEtaS) / W0 : 0.0;
-  o.k[q] = (W0 != 0.0) ? (0.0 + sK) / W0 : 0.0;
-  o.lastT[q] = (W0 != 0.0) ? (0.0 + sT) / W0 : 0.0;
-  o.Cp[q] = (W0 != 0.0) ? (0.0 + sCp) / W0 : 0.0;
-  o.soxy[q] = (W3 != 0.0) ? (0.0 + sSxy) / W3 : 0.0;
-  o.etaN[q] = (W1 != 0.0) ? (0.0 + sEtaN) / W1 : 0.0;
-  o.soxx[q] = (W2 != 0.0) ? (0.0 + sSxx) / W2 : 0.0;
-  o.soyy[q] = (W2 != 0.0) ? (0.0 + sSyy) / W2 : 0.0;
+  o.rho[q] = (W0 != 0.0) ? ((0.0 + A.rho) + B.rho) / W0 : 0.0;
+  o.etaS[q] = (W0 != 0.0) ? ((0.0 + A.etaS) + B.etaS) / W0 : 0.0;
+  o.k[q] = (W0 != 0.0) ? ((0.0 + A.k) + B.k) / W0 : 0.0;
+  o.lastT[q] = (W0 != 0.0) ? ((0.0 + A.T) + B.T) / W0 : 0.0;
+  o.Cp[q] = (W0 != 0.0) ? ((0.0 + A.Cp) + B.Cp) / W0 : 0.0;
+  o.soxy[q] = (W3 != 0.0) ? ((0.0 + A.sxy) + B.sxy) / W3 : 0.0;
+  o.etaN[q] = (W1 != 0.0) ? ((0.0 + A.etaN) + B.etaN) / W1 : 0.0;
+  o.soxx[q] = (W2 != 0.0) ? ((0.0 + A.sxx) + B.sxx) / W2 : 0.0;
+  o.soyy[q] = (W2 != 0.0) ? ((0.0 + A.syy) + B.syy) / W2 : 0.0;
   o.rhodot[q] = 0.0;
   o.muS[q] = 1e99;
   o.muN[q] = 1e99;
@@ -111,31 +133,26 @@ __global__ void __launch_bounds__(128) k_project_all2(Params P, MarkerView mv, c
 // (projectMarkersNodesFromScalar, markers.c:1507-1594, and stagger (0,0)); STAG -1 ->
 // cell centres (stagger (-1,-1), e.g. the strain-rate residual of residual.c:20).
 template <int STAG>
-__global__ void __launch_bounds__(128) k_project_geo_arith(Params P, const double *__restrict__ v,
-                                                            const int *__restrict__ cellX,
-                                                            const double *__restrict__ gx,
-                                                            const double *__restrict__ gy,
-                                                            const int *__restrict__ flags,
-                                                            const int *__restrict__ cs, double *__restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i >= P.NX || j >= P.NY) return;
-  const int NC = P.NX - 1;
+__device__ __forceinline__ void geo_arith_column(const Params &P, const double *__restrict__ v,
+                                                 const int *__restrict__ cellX, const double *__restrict__ gx,
+                                                 const double *__restrict__ gy, const int *__restrict__ flags,
+                                                 const int *__restrict__ cs, int L, int j, double &s, double &w_) {
+  const int NC = P.NCX;
   const int R = (STAG == 0) ? 1 : 2;
-  double s = 0.0, w_ = 0.0;
   const int cy0 = max(j - R, 0), cy1 = min(j, P.NY - 2);
-  const int cx0 = max(i - R, 0), cx1 = min(i, P.NX - 2);
+  const int cx0 = max(L - R, 0), cx1 = min(L, NC - 1);
+  if (cx0 > cx1) return;
   for (int cy = cy0; cy <= cy1; ++cy) {
     const int mb = cs[cy * NC + cx0], me = cs[cy * NC + cx1 + 1];
     for (int m = mb; m < me; ++m) {
       const int cx = cellX[m];
       int ox, oy;
       if (STAG == 0) {
-        ox = i - cx;
+        ox = L - cx;
         oy = j - cy;
       } else {
         const int fl = flags[m];
-        ox = i - (cx + (fl & 1));
+        ox = L - (cx + (fl & 1));
         oy = j - (cy + ((fl >> 1) & 1));
       }
       if ((unsigned)ox <= 1u && (unsigned)oy <= 1u) {
@@ -146,26 +163,38 @@ __global__ void __launch_bounds__(128) k_project_geo_arith(Params P, const doubl
       }
     }
   }
-  const double W = 0.0 + w_;
-  out[(size_t)j * P.NX + i] = (W != 0.0) ? (0.0 + s) / W : 0.0;
 }
 
-// Generic projectMarkerFieldToNodes for any stagger in {-1,0,1}^2 and method, computing the
-// offsets from scratch (markerProjection.c:115-229).  Candidate cells cx in [i-2, i+1].
-__global__ void __launch_bounds__(128) k_project_generic(Params P, const double *__restrict__ X,
-                                                          const double *__restrict__ Y,
-                                                          const int *__restrict__ cellX,
-                                                          const double *__restrict__ v, const int *__restrict__ mat,
-                                                          const double *__restrict__ matprop_dev, int stagx,
-                                                          int stagy, int method, const int *__restrict__ cs,
-                                                          double *__restrict__ out) {
+template <int STAG>
+__global__ void __launch_bounds__(128) k_project_geo_arith(Params P, const double *__restrict__ v,
+                                                            const int *__restrict__ cellX,
+                                                            const double *__restrict__ gx,
+                                                            const double *__restrict__ gy,
+                                                            const int *__restrict__ flags,
+                                                            const int *__restrict__ cs, double *__restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= P.NX || j >= P.NY) return;
-  const int NC = P.NX - 1;
-  double s = 0.0, w_ = 0.0;
+  double s = 0.0, w_ = 0.0, s2 = 0.0, w2 = 0.0;
+  geo_arith_column<STAG>(P, v, cellX, gx, gy, flags, cs, i, j, s, w_);
+  if (P.xper && i + P.NX <= P.NCX + 1) geo_arith_column<STAG>(P, v, cellX, gx, gy, flags, cs, i + P.NX, j, s2, w2);
+  const double W = (0.0 + w_) + w2;
+  out[(size_t)j * P.NX + i] = (W != 0.0) ? ((0.0 + s) + s2) / W : 0.0;
+}
+
+// Generic projectMarkerFieldToNodes for any stagger in {-1,0,1}^2 and method, computing the
+// offsets from scratch (markerProjection.c:115-229): the sums of local column L of node row j,
+// over candidate cells cx in [L-2, L+1].
+__device__ __forceinline__ void generic_column(const Params &P, const double *__restrict__ X,
+                                               const double *__restrict__ Y, const int *__restrict__ cellX,
+                                               const double *__restrict__ v, const int *__restrict__ mat,
+                                               const double *__restrict__ matprop_dev, int stagx, int stagy,
+                                               int method, const int *__restrict__ cs, int L, int j, double &s,
+                                               double &w_) {
+  const int NC = P.NCX;
   const int cy0 = max(j - 2, 0), cy1 = min(j + 1, P.NY - 2);
-  const int cx0 = max(i - 2, 0), cx1 = min(i + 1, P.NX - 2);
+  const int cx0 = max(L - 2, 0), cx1 = min(L + 1, NC - 1);
+  if (cx0 > cx1) return;
   for (int cy = cy0; cy <= cy1; ++cy) {
     const int mb = cs[cy * NC + cx0], me = cs[cy * NC + cx1 + 1];
     for (int m = mb; m < me; ++m) {
@@ -182,7 +211,7 @@ __global__ void __launch_bounds__(128) k_project_generic(Params P, const double 
       } else if (stagy == -1) {
         if (y >= P.yc[cy + 1]) sy++;
       }
-      if (i - sx < 0 || i - sx > 1 || j - sy < 0 || j - sy > 1) continue;
+      if (L - sx < 0 || L - sx > 1 || j - sy < 0 || j - sy > 1) continue;
       double mdx, mdy;
       if (stagx == -1)
         mdx = (x - P.xc[sx]) / (P.xc[sx + 1] - P.xc[sx]);
@@ -197,7 +226,7 @@ __global__ void __launch_bounds__(128) k_project_generic(Params P, const double 
       else
         mdy = (y - P.yc[sy + 1]) / (P.yc[sy + 2] - P.yc[sy + 1]);
       const double val = matprop_dev ? matprop_dev[mat[m]] : v[m];
-      const int ox = i - sx, oy = j - sy;
+      const int ox = L - sx, oy = j - sy;
       if (method == MIC_ARITHMETIC) {
         const double w = (ox ? mdx : (1.0 - mdx)) * (oy ? mdy : (1.0 - mdy));
         s += w * val;
@@ -216,7 +245,27 @@ __global__ void __launch_bounds__(128) k_project_generic(Params P, const double 
       }
     }
   }
-  const double a = 0.0 + s, W = 0.0 + w_;
+}
+
+// One thread per node.  Periodic in x, node NX - 1 adds local column -1 (stagger +1 reaches it)
+// and nodes 0, 1 add columns NX, NX + 1 after their own.
+__global__ void __launch_bounds__(128) k_project_generic(Params P, const double *__restrict__ X,
+                                                          const double *__restrict__ Y,
+                                                          const int *__restrict__ cellX,
+                                                          const double *__restrict__ v, const int *__restrict__ mat,
+                                                          const double *__restrict__ matprop_dev, int stagx,
+                                                          int stagy, int method, const int *__restrict__ cs,
+                                                          double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= P.NX || j >= P.NY) return;
+  double s = 0.0, w_ = 0.0, s2 = 0.0, w2 = 0.0;
+  generic_column(P, X, Y, cellX, v, mat, matprop_dev, stagx, stagy, method, cs, i, j, s, w_);
+  if (P.xper) {
+    const int L = (i == P.NX - 1) ? -1 : (i + P.NX <= P.NCX + 1 ? i + P.NX : INT_MIN);
+    if (L != INT_MIN) generic_column(P, X, Y, cellX, v, mat, matprop_dev, stagx, stagy, method, cs, L, j, s2, w2);
+  }
+  const double a = (0.0 + s) + s2, W = (0.0 + w_) + w2;
   const size_t q = (size_t)j * P.NX + i;
   if (method == MIC_HARMONIC)
     out[q] = (a != 0.0) ? W / a : 0.0;
@@ -227,6 +276,9 @@ __global__ void __launch_bounds__(128) k_project_generic(Params P, const double 
 inline dim3 node_grid(const Params &P) { return dim3((P.NX + 127) / 128, P.NY); }
 
 #ifndef MIC_EXACT
+// staggered cells: NCX + 1 per row
+inline dim3 centre_grid(const Params &P) { return dim3((P.NCX + 1 + 127) / 128, P.NY); }
+
 // ---- product build: divergence-free projection through per-cell corner partials ------
 //
 // One thread per cell runs over the cell's markers, whose quadrant runs are contiguous
@@ -261,7 +313,7 @@ template <bool ALL2, bool VISC = false, bool FIRST = false>
 __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v, const int *__restrict__ qs,
                                                          mic_materials mat, double *__restrict__ part) {
   __shared__ double sloc[(ALL2 && !FIRST) ? 8 : 1][128];
-  const int ncells = (P.NX - 1) * (P.NY - 1);
+  const int ncells = P.NCX * (P.NY - 1);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   constexpr int NA = ALL2 ? 6 : 2;
@@ -328,10 +380,10 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
   }
 }
 
-// Staggered (cell-centre) cell s = (sx, sy), sx in [0, NX-1]: its markers are quadrant 3 of
+// Staggered (cell-centre) cell s = (sx, sy), sx in [0, NCX]: its markers are quadrant 3 of
 // basic cell (sx-1, sy-1), quadrant 2 of (sx, sy-1), quadrant 1 of (sx-1, sy) and quadrant 0 of
 // (sx, sy).  ALL2: etaN, weight per corner (8) + nearest-node sxx, syy, weight (12) = 20 sums;
-// !ALL2: scalar, weight per corner = 8.  part[acc * NX*NY + s].
+// !ALL2: scalar, weight per corner = 8.  part[acc * (NX+1)*NY + s], s = sy (NX+1) + sx.
 //
 // The four runs are walked as one sequence (run 0's markers, then run 1's, ...) by one loop,
 // for the same reason as in k_partials_basic; the nearest-centre sums use per-thread shared
@@ -342,10 +394,10 @@ __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v
   __shared__ double sloc[ALL2 ? 12 : 1][128];
   const int sx = blockIdx.x * blockDim.x + threadIdx.x;
   const int sy = blockIdx.y;
-  if (sx >= P.NX || sy >= P.NY) return;
-  const int NC = P.NX - 1;
+  if (sx > P.NCX || sy >= P.NY) return;
+  const int NC = P.NCX;
   const int t = threadIdx.x;
-  const size_t ns = (size_t)P.NX * P.NY, s = (size_t)sy * P.NX + sx;
+  const size_t ns = (size_t)(P.NX + 1) * P.NY, s = (size_t)sy * (P.NX + 1) + sx;
   double acc[4][2];
 #pragma unroll
   for (int k = 0; k < 4; ++k) acc[k][0] = acc[k][1] = 0.0;
@@ -361,7 +413,7 @@ __global__ void __launch_bounds__(128) k_partials_centre(Params P, PartialView v
     const int q = (1 - dx) + 2 * (1 - dy);      // ... contributes its quadrant q
     rb[r] = 0;
     rn[r] = 0;
-    if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
+    if (cx >= 0 && cx < NC && cy >= 0 && cy <= P.NY - 2) {
       const int qq = 4 * (cy * NC + cx) + q;
       rb[r] = qs[qq];
       rn[r] = qs[qq + 1] - qs[qq];
@@ -417,30 +469,35 @@ __global__ void __launch_bounds__(128) k_combine_all2(Params P, const double *__
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= P.NX || j >= P.NY) return;
-  const int NC = P.NX - 1, ncells = NC * (P.NY - 1);
-  const size_t ns = (size_t)P.NX * P.NY;
+  const int NC = P.NCX, ncells = NC * (P.NY - 1);
+  const size_t ns = (size_t)(P.NX + 1) * P.NY;
   double b[8] = {0, 0, 0, 0, 0, 0, 0, 0}, c[5] = {0, 0, 0, 0, 0};
+  // local columns of this node: its own and, periodic, the seam image i + NX (nodes 0 and 1)
+  const int nL = (P.xper && i + P.NX <= NC + 1) ? 2 : 1;
+  for (int l = 0; l < nL; ++l) {
+    const int L = i + l * P.NX;
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int dx = r & 1, dy = r >> 1;
-    const int cx = i - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
-    if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
-      const size_t cc = (size_t)cy * NC + cx;
+    for (int r = 0; r < 4; ++r) {
+      const int dx = r & 1, dy = r >> 1;
+      const int cx = L - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
+      if (cx >= 0 && cx < NC && cy >= 0 && cy <= P.NY - 2) {
+        const size_t cc = (size_t)cy * NC + cx;
 #pragma unroll
-      for (int f = 0; f < 6; ++f)
-        if ((!VISC || f == 1 || f == 5) && (!FIRST || f != 1)) b[f] += pb[(size_t)(k * 6 + f) * ncells + cc];
-      if (!FIRST) {
-        b[6] += pb[(size_t)(24 + 2 * k) * ncells + cc];
-        b[7] += pb[(size_t)(25 + 2 * k) * ncells + cc];
+        for (int f = 0; f < 6; ++f)
+          if ((!VISC || f == 1 || f == 5) && (!FIRST || f != 1)) b[f] += pb[(size_t)(k * 6 + f) * ncells + cc];
+        if (!FIRST) {
+          b[6] += pb[(size_t)(24 + 2 * k) * ncells + cc];
+          b[7] += pb[(size_t)(25 + 2 * k) * ncells + cc];
+        }
       }
-    }
-    if (!FIRST && cx >= 0 && cy >= 0) {  // staggered cells exist for sx in [0, NX-1]
-      const size_t ss = (size_t)cy * P.NX + cx;
-      c[0] += pc[(size_t)(2 * k) * ns + ss];
-      c[1] += pc[(size_t)(2 * k + 1) * ns + ss];
-      c[2] += pc[(size_t)(8 + 3 * k) * ns + ss];
-      c[3] += pc[(size_t)(9 + 3 * k) * ns + ss];
-      c[4] += pc[(size_t)(10 + 3 * k) * ns + ss];
+      if (!FIRST && cx >= 0 && cx <= NC && cy >= 0) {  // staggered cells exist for sx in [0, NCX]
+        const size_t ss = (size_t)cy * (P.NX + 1) + cx;
+        c[0] += pc[(size_t)(2 * k) * ns + ss];
+        c[1] += pc[(size_t)(2 * k + 1) * ns + ss];
+        c[2] += pc[(size_t)(8 + 3 * k) * ns + ss];
+        c[3] += pc[(size_t)(9 + 3 * k) * ns + ss];
+        c[4] += pc[(size_t)(10 + 3 * k) * ns + ss];
+      }
     }
   }
   const size_t q = (size_t)j * P.NX + i;
@@ -470,23 +527,27 @@ __global__ void __launch_bounds__(128) k_combine_scalar(Params P, const double *
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= P.NX || j >= P.NY) return;
-  const int NC = P.NX - 1, ncells = NC * (P.NY - 1);
-  const size_t ns = (size_t)P.NX * P.NY;
+  const int NC = P.NCX, ncells = NC * (P.NY - 1);
+  const size_t ns = (size_t)(P.NX + 1) * P.NY;
   double a = 0.0, w = 0.0;
+  const int nL = (P.xper && i + P.NX <= NC + 1) ? 2 : 1;
+  for (int l = 0; l < nL; ++l) {
+    const int L = i + l * P.NX;
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int dx = r & 1, dy = r >> 1;
-    const int cx = i - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
-    if (STAG == 0) {
-      if (cx >= 0 && cx <= P.NX - 2 && cy >= 0 && cy <= P.NY - 2) {
-        const size_t cc = (size_t)cy * NC + cx;
-        a += part[(size_t)(2 * k) * ncells + cc];
-        w += part[(size_t)(2 * k + 1) * ncells + cc];
+    for (int r = 0; r < 4; ++r) {
+      const int dx = r & 1, dy = r >> 1;
+      const int cx = L - 1 + dx, cy = j - 1 + dy, k = (1 - dx) + 2 * (1 - dy);
+      if (STAG == 0) {
+        if (cx >= 0 && cx < NC && cy >= 0 && cy <= P.NY - 2) {
+          const size_t cc = (size_t)cy * NC + cx;
+          a += part[(size_t)(2 * k) * ncells + cc];
+          w += part[(size_t)(2 * k + 1) * ncells + cc];
+        }
+      } else if (cx >= 0 && cx <= NC && cy >= 0) {
+        const size_t ss = (size_t)cy * (P.NX + 1) + cx;
+        a += part[(size_t)(2 * k) * ns + ss];
+        w += part[(size_t)(2 * k + 1) * ns + ss];
       }
-    } else if (cx >= 0 && cy >= 0) {
-      const size_t ss = (size_t)cy * P.NX + cx;
-      a += part[(size_t)(2 * k) * ns + ss];
-      w += part[(size_t)(2 * k + 1) * ns + ss];
     }
   }
   out[(size_t)j * P.NX + i] = guarded(a, w);
@@ -541,7 +602,7 @@ int mic_project_scalar(mic_ctx *ctx, const double *v, int stag, double *out, cud
     } else {
       {
         MIC_KERNEL_ON(ctx, "k_partials_centre<scalar>", s);
-        k_partials_centre<false><<<node_grid(ctx->P), 128, 0, s>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
+        k_partials_centre<false><<<centre_grid(ctx->P), 128, 0, s>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
       }
       {
         MIC_KERNEL_ON(ctx, "k_combine_scalar<-1>", s);
@@ -650,7 +711,7 @@ static int project_all2(mic_ctx *ctx, int mode, cudaStream_t st = nullptr) {
   MIC_CUDA_TRY(cudaStreamWaitEvent(ctx->aux, ctx->aux_ev[0], 0));
   {
     MIC_KERNEL_ON(ctx, "k_partials_centre", ctx->aux);
-    k_partials_centre<true><<<node_grid(ctx->P), 128, 0, ctx->aux>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
+    k_partials_centre<true><<<centre_grid(ctx->P), 128, 0, ctx->aux>>>(ctx->P, pv, ctx->quad_start, ctx->part_c);
   }
   MIC_CUDA_TRY(cudaEventRecord(ctx->aux_ev[1], ctx->aux));
   if (visc) {

@@ -555,6 +555,7 @@ extern "C" int mic_reset_nodal_fields(mic_ctx *ctx) {
 }
 
 extern "C" int mic_initial_conditions_van_keken(mic_ctx *ctx, const mic_subduction_options *o) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !o) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   if (ctx->n > 0) {
@@ -583,6 +584,7 @@ extern "C" int mic_initial_conditions_van_keken(mic_ctx *ctx, const mic_subducti
 
 extern "C" int mic_form_vep_system(mic_ctx *ctx, const mic_subduction_options *o, double dt, double *Kbond,
                                    double *Kcont) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !o) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   const int NX = ctx->P.NX, NY = ctx->P.NY;
@@ -625,6 +627,7 @@ extern "C" int mic_form_vep_system(mic_ctx *ctx, const mic_subduction_options *o
 }
 
 extern "C" int mic_enforce_thermal_bcs(mic_ctx *ctx, const mic_subduction_options *o) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !o) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   Scratch s;
@@ -640,6 +643,7 @@ extern "C" int mic_enforce_thermal_bcs(mic_ctx *ctx, const mic_subduction_option
 }
 
 extern "C" int mic_form_thermal_system(mic_ctx *ctx, const mic_subduction_options *o, double dt, int doSteady) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !o) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   const int64_t nn = (int64_t)ctx->P.NX * ctx->P.NY;

@@ -87,6 +87,7 @@ int thermal_solve(mic_ctx *ctx, const mic_timestep_options &o, double dt) {
 }  // namespace
 
 extern "C" int mic_adiabatic_heating(mic_ctx *ctx, double gy) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);
   int e = mic_ensure_sorted(ctx);
@@ -115,6 +116,7 @@ extern "C" int mic_adiabatic_heating(mic_ctx *ctx, double gy) {
 
 extern "C" int mic_subduction_timestep(mic_ctx *ctx, const mic_timestep_options *o, double elapsed_time,
                                        mic_timestep_report *rep) {
+  if (ctx && ctx->P.xper) return MIC_ERR_BC;  // grids periodic in x: the marker path only
   if (!ctx || !o || !rep) return MIC_ERR_ARG;
   if (ctx->red_cap < 64) return MIC_ERR_ARG;
   cudaSetDevice(ctx->device);

@@ -287,6 +287,107 @@ def vep_slab_box(nx_cells=1024, ny_cells=256, nm=4, seed=2):
     return Workload("vep_slab_box", g, m, mat, opt, _free_slip(), nodal, dt, dt, 20)
 
 
+def periodic_cell_centers(x, LX):
+    """getCellCenters then makePeriodic (gridSpacing.c:150-168) for NX lines of a periodic x:
+    xc[0..NX+1]."""
+    NX = len(x)
+    xc = np.empty(NX + 2)
+    xc[1:NX] = (x[:-1] + x[1:]) / 2.0
+    xc[NX] = (LX + x[NX - 1]) / 2.0
+    xc[NX + 1] = xc[1] + LX
+    xc[0] = 0.0 - (LX - xc[NX])
+    return xc
+
+
+def periodic_box(nx_cells=16, ny_cells=6, nm=4, seed=9):
+    """Visco-elasto-plastic box periodic in x (mechBCLeft/Right type 0 = 2: gridGenerator.c:67-68,
+    97-110; nodalFields.c:11-19): nx_cells uniform cells between x = 0 and LX (NX = nx_cells
+    lines, line NX = LX is line 0's image), y about 2x finer in the top 20 %, an Arrhenius mantle
+    with a Mohr-Coulomb band, and a periodic velocity field with a uniform drift, so markers
+    cross x = LX and x = 0 during advection.  Markers on a jittered lattice over [0, LX] x
+    [0, LY] plus markers on the periodic seam (X = 0, X = LX, the last cell's halves)."""
+    NX, NY = nx_cells, ny_cells + 1
+    LX, LY = 4.0e5, 1.0e5
+    x = spacing_uniform(0.0, LX, NX + 1)[:NX]
+    g = Grid(NX, NY, LX, LY, x, refined_top_y(LY, ny_cells))
+    g.xc = periodic_cell_centers(x, LX)[: NX + 1]
+    mdx, mdy = LX / (nm * NX), LY / (nm * ny_cells)
+    nk, nl = nm * NX, nm * ny_cells
+    u = splitmix64_uniform(seed, 2 * nk * nl)
+    k = np.repeat(np.arange(nk, dtype=np.float64), nl)
+    l = np.tile(np.arange(nl, dtype=np.float64), nk)
+    m = np.zeros(nk * nl + 8, dtype=MARKER_DTYPE)
+    m["X"][: nk * nl] = mdx * (0.5 + k) + (-mdx / 4.0 + (mdx / 2.0) * u[0::2])
+    m["Y"][: nk * nl] = mdy * (0.5 + l) + (-mdy / 4.0 + (mdy / 2.0) * u[1::2])
+    xcp = periodic_cell_centers(x, LX)
+    seam = [(0.0, 0.3 * LY), (LX, 0.4 * LY), (x[NX - 1], 0.5 * LY), (0.5 * (x[NX - 1] + xcp[NX]), 0.6 * LY),
+            (0.5 * (xcp[NX] + LX), 0.7 * LY), (0.5 * xcp[1], 0.2 * LY), (xcp[NX], 0.8 * LY), (LX * (1 - 1e-12), 0.1 * LY)]
+    for q, (xx, yy) in enumerate(seam):
+        m["X"][nk * nl + q], m["Y"][nk * nl + q] = xx, yy
+    m["cellX"] = -1
+    m["cellY"] = -1
+    X, Y = m["X"], m["Y"]
+    ur = splitmix64_uniform(seed + 1000, len(m))
+    band = (Y > 0.15 * LY) & (Y < 0.3 * LY)
+    m["Mat"] = np.where(band, 1, 0)
+    m["T"] = 273.0 + 1300.0 * np.minimum(1.0, Y / (0.4 * LY)) + 5.0 * (ur - 0.5)
+    mat = _materials(2)
+    for q, (eta, rho) in enumerate([(1e21, 3300.0), (1e23, 3400.0)]):
+        mat.materialEta[q] = eta
+        mat.materialRho[q] = rho
+        mat.materialkThermal[q] = 3.0
+        mat.materialCp[q] = 1250.0
+        mat.materialAlpha[q] = 3e-5
+        mat.materialMu[q] = 1e10
+        mat.Tref[q] = 1573.0
+    mat.hasEtaT[0] = 1
+    mat.QonR[0] = 2.0e4
+    mat.hasEtaT[1] = 0
+    mat.hasPlasticity[1] = 1
+    mat.materialCohesion[1] = 2e7
+    mat.materialFriction[1] = 0.6
+    opt = Options(etamin=1e19, etamax=1e23, fractionalEtamin=0.1, subgridStressDiffusivity=1.0,
+                  subgridTemperatureDiffusivity=1.0)
+    pi = np.pi
+    kx = 2.0 * pi / LX
+    u0, a = 3e-10, 2e-10
+    vx_fn = lambda x_, y_: u0 + a * np.sin(kx * x_) * np.cos(pi * y_ / LY)
+    vy_fn = lambda x_, y_: -a * (kx * LY / pi) * np.cos(kx * x_) * np.sin(pi * y_ / LY)
+    dvx = {"x": lambda x_, y_: a * kx * np.cos(kx * x_) * np.cos(pi * y_ / LY),
+           "y": lambda x_, y_: -a * (pi / LY) * np.sin(kx * x_) * np.sin(pi * y_ / LY)}
+    dvy = {"x": lambda x_, y_: a * (kx * kx * LY / pi) * np.sin(kx * x_) * np.sin(pi * y_ / LY),
+           "y": lambda x_, y_: -a * kx * np.cos(kx * x_) * np.cos(pi * y_ / LY)}
+    vx, vy, exx, eyy, exy, wxy = _velocity_fields(g, vx_fn, vy_fn, dvx, dvy)
+    m["mu"] = 1e10
+    m["eta"] = np.clip(_eta_law(mat, m), opt.etamin, opt.etamax)
+    m["exx"] = dvx["x"](X, Y)
+    m["eyy"] = dvy["y"](X, Y)
+    m["exy"] = 0.5 * (dvx["y"](X, Y) + dvy["x"](X, Y))
+    m["sxx"] = 2.0 * m["eta"] * m["exx"]
+    m["syy"] = 2.0 * m["eta"] * m["eyy"]
+    m["sxy"] = 2.0 * m["eta"] * m["exy"]
+    m["p"] = 3300.0 * 9.8 * Y
+    XCc, YCc = np.meshgrid(g.xc[:NX], g.yc[:NY], indexing="xy")
+    Xb, Yb = np.meshgrid(g.x, g.y, indexing="xy")
+    eta_ref = 1e21
+    nodal = {
+        "vx": vx, "vy": vy, "edotxx": exx, "edotyy": eyy, "edotxy": exy, "wxy": wxy,
+        "p": 3300.0 * 9.8 * YCc,
+        "soxx": 2.0 * eta_ref * exx, "soyy": 2.0 * eta_ref * eyy, "soxy": 2.0 * eta_ref * exy,
+        "thisT": 273.0 + 1300.0 * np.minimum(1.0, Yb / (0.4 * LY)) + 2.0 * np.sin(kx * Xb) * np.sin(pi * Yb / LY),
+    }
+    nodal["dsxx"] = 0.05 * nodal["soxx"]
+    nodal["dsyy"] = 0.05 * nodal["soyy"]
+    nodal["dsxy"] = 0.05 * nodal["soxy"]
+    bcs = _free_slip()
+    bcs.mechBCLeft.type[0] = 2
+    bcs.mechBCRight.type[0] = 2
+    vmax = float(np.max(np.abs(vx))) + float(np.max(np.abs(vy)))
+    dmin = min(LX / NX, float(np.min(np.diff(g.y))))
+    dt = 0.6 * dmin / vmax
+    return Workload("periodic_box", g, m, mat, opt, bcs, nodal, dt, dt, 4)
+
+
 def ice_creep_box(nx_cells=1024, ny_cells=1024, nm=4, seed=3):
     """Composite ice creep (material law 7): per-marker strain-rate invariant
     10^U[-18,-10] 1/s, T ~ U[100, 273] K, grain size 10^U[-4,-1] m, pressure U[0, 1e8] Pa;

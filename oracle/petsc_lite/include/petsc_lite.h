@@ -10,13 +10,17 @@
  * Semantics fixed here (they decide the reference's results on one rank):
  *  - The DMDA: NX x NY nodes, dof 1 (dof 3 for the Stokes solution, values interleaved per
  *    node), stencil width 2, DMDA_STENCIL_BOX, boundary
- *    DM_BOUNDARY_GHOSTED in x and y (fvmic2d nodalFields.c:19-20).  Periodic x
- *    is not modelled: the harness rejects it.
+ *    DM_BOUNDARY_GHOSTED in x and y (fvmic2d nodalFields.c:19-20), or in x
+ *    DM_BOUNDARY_PERIODIC (nodalFields.c:11-19; plite_DMDASetPeriodicX).
  *  - Global vectors hold NX*NY values, x fastest ([j][i]); local vectors hold
  *    (NX+4)*(NY+4) values with ghost offset 2 on every side.
  *  - DMGlobalToLocal(INSERT_VALUES) copies the interior and leaves ghost
  *    entries untouched; DMLocalToGlobal(ADD_VALUES) adds the interior and drops
  *    the ghost entries (they have no owner on a ghosted, non-periodic DMDA).
+ *    Periodic in x: DMGlobalToLocal also fills ghost columns -2, -1, NX, NX+1 of
+ *    every row with columns NX-2, NX-1, 0, 1, and DMLocalToGlobal(ADD_VALUES)
+ *    adds those ghost columns into their owners after the interior (in the
+ *    order -2, -1, NX, NX+1); ghost rows are handled as before.
  *  - VecPointwiseDivide(w,x,y) gives w[i] = x[i]/y[i] when y[i] != 0 and 0
  *    otherwise (the zero-divisor guard of current PETSc releases).
  *  - Fresh vectors (DMCreate*Vector, DMGet*Vector, VecDuplicate) are zeroed.
@@ -91,6 +95,7 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 /* DMDA / Vec (single rank) */
 PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da);
 PetscErrorCode plite_DMDACreateDOF(PetscInt NX, PetscInt NY, PetscInt dof, DM *da);
+void plite_DMDASetPeriodicX(DM da, int periodic);
 PetscErrorCode plite_DMDestroy(DM *da);
 PetscErrorCode DMDAGetCorners(DM, PetscInt *, PetscInt *, PetscInt *, PetscInt *, PetscInt *, PetscInt *);
 PetscErrorCode DMCreateGlobalVector(DM, Vec *);

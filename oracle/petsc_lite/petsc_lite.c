@@ -13,6 +13,7 @@ struct _p_ISLocalToGlobalMapping {
 struct _p_DM {
   PetscInt NX, NY;
   PetscInt dof;          /* values per node: 1, or 3 for the Stokes solution DMDA (vx, vy, p) */
+  int xperiodic;         /* DM_BOUNDARY_PERIODIC in x (nodalFields.c:11-19) */
   struct _p_ISLocalToGlobalMapping *ltog;  /* built on first request */
 };
 
@@ -35,6 +36,8 @@ PetscErrorCode plite_DMDACreate(PetscInt NX, PetscInt NY, DM *da) {
   (*da)->dof = 1;
   return 0;
 }
+
+void plite_DMDASetPeriodicX(DM da, int periodic) { da->xperiodic = periodic ? 1 : 0; }
 
 PetscErrorCode plite_DMDACreateDOF(PetscInt NX, PetscInt NY, PetscInt dof, DM *da) {
   PetscErrorCode e = plite_DMDACreate(NX, NY, da);
@@ -160,8 +163,17 @@ PetscErrorCode DMGlobalToLocalBegin(DM da, Vec g, InsertMode mode, Vec l) {
   (void)mode;
   if (g->is_local || !l->is_local) return 62;
   const PetscInt NX = da->NX, NY = da->NY, W = NX + 4;
-  for (PetscInt j = 0; j < NY; ++j)
-    memcpy(l->data + (size_t)(j + 2) * W + 2, g->data + (size_t)j * NX, (size_t)NX * sizeof(PetscScalar));
+  for (PetscInt j = 0; j < NY; ++j) {
+    PetscScalar *row = l->data + (size_t)(j + 2) * W + 2;
+    const PetscScalar *src = g->data + (size_t)j * NX;
+    memcpy(row, src, (size_t)NX * sizeof(PetscScalar));
+    if (da->xperiodic) {  /* ghost columns -2, -1, NX, NX+1 hold their periodic images */
+      row[-2] = src[NX - 2];
+      row[-1] = src[NX - 1];
+      row[NX] = src[0];
+      row[NX + 1] = src[1];
+    }
+  }
   return 0;
 }
 PetscErrorCode DMGlobalToLocalEnd(DM da, Vec g, InsertMode mode, Vec l) { (void)da; (void)g; (void)mode; (void)l; return 0; }
@@ -174,6 +186,12 @@ PetscErrorCode DMLocalToGlobalBegin(DM da, Vec l, InsertMode mode, Vec g) {
     PetscScalar *dst = g->data + (size_t)j * NX;
     if (mode == ADD_VALUES) {
       for (PetscInt i = 0; i < NX; ++i) dst[i] = dst[i] + src[i];
+      if (da->xperiodic) {  /* ghost columns add into their periodic owners, after the interior */
+        dst[NX - 2] = dst[NX - 2] + src[-2];
+        dst[NX - 1] = dst[NX - 1] + src[-1];
+        dst[0] = dst[0] + src[NX];
+        dst[1] = dst[1] + src[NX + 1];
+      }
     } else {
       memcpy(dst, src, (size_t)NX * sizeof(PetscScalar));
     }

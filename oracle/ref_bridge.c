@@ -126,6 +126,16 @@ refp *ref_create(int NX, int NY, double LX, double LY, const double *x, const do
   return p;
 }
 
+/* periodic x (gridGenerator.c:67-68, 82-84 and 97-110; nodalFields.c:11-19): the gridlines and
+ * cell centres through the reference's own makePeriodic (gridSpacing.c:159-168), both DMDAs
+ * periodic in x.  The caller's x holds NX uniform lines of the NX+1 from 0 to LX. */
+void ref_set_periodic_x(refp *p) {
+  p->grid.xperiodic = 1;
+  makePeriodic(p->grid.x, p->grid.xc, p->grid.LX, p->grid.NX);
+  plite_DMDASetPeriodicX(p->grid.da, 1);
+  plite_DMDASetPeriodicX(p->grid.vda, 1);
+}
+
 void ref_destroy(refp *p) {
   if (!p) return;
   for (int id = 0; id < MIC_NF_COUNT; ++id) VecDestroy(field_vec(p, id));
@@ -137,7 +147,7 @@ void ref_destroy(refp *p) {
 }
 
 void ref_get_grid(refp *p, double *xc, double *yc) {
-  for (int i = 0; i <= p->grid.NX; ++i) xc[i] = p->grid.xc[i];
+  for (int i = 0; i <= p->grid.NX; ++i) xc[i] = p->grid.xc[i];  /* periodic: xc[NX] from makePeriodic */
   for (int j = 0; j <= p->grid.NY; ++j) yc[j] = p->grid.yc[j];
 }
 

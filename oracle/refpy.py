@@ -35,6 +35,7 @@ def lib():
             "ref_get_grid": (None, [_P, _DP, _DP]),
             "ref_set_materials": (None, [_P, _P]),
             "ref_set_bcs": (None, [_P, _P]),
+            "ref_set_periodic_x": (None, [_P]),
             "ref_set_options": (None, [_P, _P]),
             "ref_set_markers": (None, [_P, _P, _I]),
             "ref_set_nodal": (_I, [_P, _I, _DP]),
@@ -108,6 +109,8 @@ class RefProblem:
         L.ref_set_materials(self.h, ctypes.byref(self.materials))
         L.ref_set_options(self.h, ctypes.byref(self.options))
         L.ref_set_bcs(self.h, ctypes.byref(self.bcs))
+        if self.bcs.mechBCLeft.type[0] == 2 or self.bcs.mechBCRight.type[0] == 2:
+            L.ref_set_periodic_x(self.h)  # nodalFields.c:11-19, gridGenerator.c:67-68
         self.markers = np.array(wl.markers if markers is None else markers, dtype=MARKER_DTYPE, copy=True)
         L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         for name, arr in wl.nodal.items():

@@ -406,6 +406,13 @@ def main():
     if sys.argv[1:] in ([], ["grid"]):
         np.savez_compressed(os.path.join(OUT, "grid_routines.npz"), **grid_table())
         print("wrote grid_routines")
+    if sys.argv[1:] in ([], ["periodic"]):
+        # the marker path on a grid periodic in x (gridGenerator.c:67-68), markers crossing the seam
+        wl = W.periodic_box(nx_cells=16, ny_cells=6, nm=3, seed=9)
+        rec = record(wl, steps=3)
+        rec.update(tables(wl))
+        np.savez_compressed(os.path.join(OUT, "periodic_box.npz"), **rec)
+        print("wrote periodic_box", len(wl.markers), "markers")
     if sys.argv[1:]:
         return
     cases = {
