@@ -97,13 +97,13 @@ KERNEL_BYTES_LAW7 = {k: (4 + 4 + 8 + 8 + 24 + 16 + 8 + 16, 0) for k in ("k_yield
 # ends.
 # The advection and the law-7 passes from captures of the 4,194,304-marker ice box
 # (profiles/k_advect_ice_creep_box_4m_full.md, profiles/k_yield_creep_ice_creep_box_4m_full.md).
-KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (528.6e6 + 258.5e6) / 4194304, "k_yield_tc": (302.1e6 + 50.6e6) / 4194304,
+KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (528.6e6 + 258.3e6) / 4194304, "k_yield_tc": (370.2e6 + 53.5e6) / 4194304,
                              "k_yield": (302.2e6 + 48.7e6) / 4194304}
 # FP64 work per marker from the same captures (DFMA, DADD, DMUL thread instructions / markers):
 # flops with a DFMA counted twice, and the FP64 arithmetic instructions.  The kernels of this path
 # are bound by the FP64 pipe, which issues 2 FP64 instructions per SM per clock on GB300, not by
 # HBM.  (k_yield: the exact law-7 pass.)
-_FP64_WARP_INSTR = {"k_advect": (8.78e6, 7.86e6), "k_yield_tc": (10.37e6, 13.31e6), "k_yield": (22.00e6, 22.11e6)}
+_FP64_WARP_INSTR = {"k_advect": (8.78e6, 7.86e6), "k_yield_tc": (7.15e6, 13.16e6), "k_yield": (22.00e6, 22.11e6)}
 KERNEL_FP64_FLOPS_PER_MARKER = {k: (2 * f + u) * 32 / 4194304 for k, (f, u) in _FP64_WARP_INSTR.items()}
 KERNEL_FP64_INST_PER_MARKER = {k: (f + u) * 32 / 4194304 for k, (f, u) in _FP64_WARP_INSTR.items()}
 FP64_PEAK_TFLOPS = 2 * 2 * 152 * 2.07e9 / 1e12  # 2 DFMA/SM/clk x 2 flops x 152 SMs x 2.07 GHz

@@ -35,7 +35,8 @@ enum {
   MIC_ERR_CELL = 4,       /* impossible cell index; markers.c:74-77 aborts */
   MIC_ERR_NAN = 5,        /* NaN strain-rate residual; updateMarkerStrainPressure.c:302-306 aborts */
   MIC_ERR_LAW = 6,        /* undefined viscosity law; viscosity.c:60-62 aborts */
-  MIC_ERR_BC = 7,         /* boundary type whose ghost values the path would read (periodic) */
+  MIC_ERR_BC = 7,         /* unsupported boundary type, or a routine outside the marker path on a grid
+                             periodic in x */
   MIC_ERR_CAPACITY = 8,   /* more markers than the context was created for; markers.c:771-774 aborts */
   MIC_ERR_NO_DEVICE = 9,  /* no CUDA device: there is no CPU fallback */
   MIC_ERR_DENSITY = 10,   /* density control: a quarter cell would get a non-positive number of
@@ -66,7 +67,13 @@ int mic_create(mic_ctx **out, int device, void *stream, int NX, int NY, double L
 int mic_destroy(mic_ctx *ctx);
 int mic_set_materials(mic_ctx *ctx, const mic_materials *materials);
 int mic_set_options(mic_ctx *ctx, const mic_options *options);
-/* BoundaryValues read by advectMarkersRK (markers.c:1986-2023); periodic walls are rejected */
+/* BoundaryValues read by advectMarkersRK (markers.c:1986-2023).  A left or right vx type 2 makes
+ * the grid periodic in x, as the reference's grid generators and nodal DMDAs do
+ * (gridGenerator.c:67-68, 97-110; nodalFields.c:11-19): x holds the first NX of NX + 1 uniform
+ * lines from 0 to LX (NX cells in x; line NX = LX is line 0's image), the marker path wraps node
+ * columns and marker positions across the seam (markers.c:2225-2231), and the routines outside
+ * the marker path (density control, grid routines, systems, time step) return MIC_ERR_BC.  Top
+ * vx type 0 or 1; on a non-periodic grid left vy type 0 or 1. */
 int mic_set_bcs(mic_ctx *ctx, const mic_bcs *bcs);
 int mic_get_bcs(mic_ctx *ctx, mic_bcs *bcs); /* the context's boundary conditions */
 int mic_get_grid_centres(mic_ctx *ctx, double *xc, double *yc); /* NX+1, NY+1 entries */

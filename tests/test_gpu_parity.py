@@ -309,12 +309,23 @@ def test_nan_strain_rate_residual_is_an_error():
     G.findMarkerCells()  # still usable
 
 
-def test_rejects_periodic_boundaries():
+def test_rejects_unsupported_boundaries():
+    """A top wall of type 2 (the reference's grids are never periodic in y) is refused with
+    MIC_ERR_BC; on a grid periodic in x the routines outside the marker path (here the density
+    control) return MIC_ERR_BC and leave the context usable"""
     wl = W.convection_box(ncell=8, nm=2)
     wl.bcs.mechBCTop.type[0] = 2
     with pytest.raises(gpu.MicError) as e:
         gpu.MicProblem(wl)
     assert e.value.code == 7
+    from fvmic2d_gb300.mic_types import DensityOptions
+
+    wp = W.periodic_box(nx_cells=16, ny_cells=6, nm=2, seed=5)
+    G = gpu.MicProblem(wp)
+    with pytest.raises(gpu.MicError) as e:
+        G.checkMarkerDensity(DensityOptions(NMX=4, NMY=4, minMarkers=1, maxMarkers=100))
+    assert e.value.code == 7
+    assert G.findMarkerCells() == 0
 
 
 # ---- full-size properties ----------------------------------------------------------------
