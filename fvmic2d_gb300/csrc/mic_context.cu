@@ -445,6 +445,22 @@ extern "C" int mic_set_options(mic_ctx *ctx, const mic_options *o) {
   return MIC_OK;
 }
 
+// The reference's compile-time JAUMANN switch (markers.c:2147-2164) as a context setting.
+extern "C" int mic_set_stress_rotation(mic_ctx *ctx, int rotation) {
+  if (!ctx || (rotation != MIC_ROTATION_EXACT && rotation != MIC_ROTATION_JAUMANN)) return MIC_ERR_ARG;
+  if (ctx->P.jaumann != (rotation == MIC_ROTATION_JAUMANN)) {
+    ctx->P.jaumann = rotation == MIC_ROTATION_JAUMANN;
+    ctx->gen++;
+  }
+  return MIC_OK;
+}
+
+extern "C" int mic_get_stress_rotation(mic_ctx *ctx, int *rotation) {
+  if (!ctx || !rotation) return MIC_ERR_ARG;
+  *rotation = ctx->P.jaumann ? MIC_ROTATION_JAUMANN : MIC_ROTATION_EXACT;
+  return MIC_OK;
+}
+
 extern "C" int mic_get_bcs(mic_ctx *ctx, mic_bcs *bcs) {
   if (!ctx || !bcs) return MIC_ERR_ARG;
   *bcs = ctx->bcs;

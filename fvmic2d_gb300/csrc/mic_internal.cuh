@@ -69,6 +69,8 @@ struct Params {  // everything a kernel needs besides the marker columns; passed
   int NX, NY;
   int NCX;   // basic cells in x: NX - 1, or NX on a grid periodic in x (line NX is line 0's image)
   int xper;  // periodic in x: node column NX is column 0, NX + 1 is 1, -1 is NX - 1
+  int jaumann;  // stress rotation of the advection: 1 the first-order Jaumann update (markers.c:2147-2156,
+                // the reference built with -DJAUMANN), 0 the exact rotation (2158-2164)
   double LX, LY;
   const double *x, *y, *xc, *yc;  // point at index 0 (ghost entries at -2, -1 exist)
   const long long *xbits, *ybits; // bit patterns of x[0..NX-1], y[0..NY-1] for integer compares

@@ -1069,23 +1069,42 @@ __device__ __forceinline__ double advect_tail(const Params &P, const AdvectCols 
   }
   c.X[m] = Xn;
   const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
-  const double th = -w * dt;
+  double nsxx;
+  if (P.jaumann) {
+    // first-order Jaumann terms with wxy1 = wxy dt (markers.c:2147-2156)
+    const double w1 = w * dt;
 #ifdef MIC_EXACT
-  const double ct = cos(th), st_ = sin(th), s2 = sin(2.0 * th), c2 = cos(2.0 * th);
-  const double nsxx = s11 * (ct * ct) + s22 * (st_ * st_) - s12 * s2;
-  c.sxx[m] = nsxx;
-  c.syy[m] = s11 * (st_ * st_) + s22 * (ct * ct) + s12 * s2;
-  c.sxy[m] = 0.5 * (s11 - s22) * s2 + s12 * c2;
+    nsxx = s11 + 2.0 * s12 * -w1;
+    c.syy[m] = s22 + 2.0 * s12 * w1;
+    c.sxy[m] = s12 + (s11 - s22) * w1;
+#else
+    nsxx = fma(2.0 * s12, -w1, s11);
+    c.syy[m] = fma(2.0 * s12, w1, s22);
+    c.sxy[m] = fma(s11 - s22, w1, s12);
+#endif
+    c.sxx[m] = nsxx;
+  } else {
+    const double th = -w * dt;
+#ifdef MIC_EXACT
+    const double ct = cos(th), st_ = sin(th), s2 = sin(2.0 * th), c2 = cos(2.0 * th);
+    nsxx = s11 * (ct * ct) + s22 * (st_ * st_) - s12 * s2;
+    c.sxx[m] = nsxx;
+    c.syy[m] = s11 * (st_ * st_) + s22 * (ct * ct) + s12 * s2;
+    c.sxy[m] = 0.5 * (s11 - s22) * s2 + s12 * c2;
+#else
+    double ct, st_, s2, c2;
+    small_angle_rotation(th, ct, st_, s2, c2);
+    const double cc = ct * ct, ss = st_ * st_;
+    nsxx = fma(s11, cc, fma(s22, ss, -(s12 * s2)));
+    c.sxx[m] = nsxx;
+    c.syy[m] = fma(s11, ss, fma(s22, cc, s12 * s2));
+    c.sxy[m] = fma(0.5 * (s11 - s22), s2, s12 * c2);
+#endif
+  }
+#ifdef MIC_EXACT
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   c.Eii[m] = c.Eii[m] + dt * sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
 #else
-  double ct, st_, s2, c2;
-  small_angle_rotation(th, ct, st_, s2, c2);
-  const double cc = ct * ct, ss = st_ * st_;
-  const double nsxx = fma(s11, cc, fma(s22, ss, -(s12 * s2)));
-  c.sxx[m] = nsxx;
-  c.syy[m] = fma(s11, ss, fma(s22, cc, s12 * s2));
-  c.sxy[m] = fma(0.5 * (s11 - s22), s2, s12 * c2);
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   c.Eii[m] = fma(dt, sqrt(fma(e12, e12, 0.5 * fma(e11, e11, e22 * e22))), c.Eii[m]);
 #endif

@@ -31,6 +31,8 @@ SIGNATURES = {
     "mic_set_options": (_I, [_P, _P]),
     "mic_set_bcs": (_I, [_P, _P]),
     "mic_get_bcs": (_I, [_P, _P]),
+    "mic_set_stress_rotation": (_I, [_P, _I]),
+    "mic_get_stress_rotation": (_I, [_P, _IP]),
     "mic_get_grid_centres": (_I, [_P, _DP, _DP]),
     "mic_markers_upload": (_I, [_P, _P, _I64]),
     "mic_markers_download": (_I, [_P, _P, _I64]),
@@ -138,6 +140,7 @@ _libs = {}
 
 NOALLOC_MAX_MARKERS = 1048576  # MIC_NOALLOC_MAX_MARKERS
 NOALLOC_MAX_CELLS = 1048576    # MIC_NOALLOC_MAX_CELLS
+MIC_ROTATION_EXACT, MIC_ROTATION_JAUMANN = 0, 1  # mic_set_stress_rotation
 
 
 class MicError(RuntimeError):
@@ -183,7 +186,8 @@ TUNE_KERNELS = ["k_advect", "k_strain_pressure", "k_yield", "k_subgrid_stress_ma
 class MicProblem:
     """A device context holding one grid, its nodal fields and a marker set."""
 
-    def __init__(self, wl, markers=None, exact=False, device=0, capacity=None, stream=None):
+    def __init__(self, wl, markers=None, exact=False, device=0, capacity=None, stream=None, jaumann=False):
+        """jaumann: advectMarkersRK's stress rotation as the reference built with -DJAUMANN"""
         self.L = L = load(exact)
         g = wl.grid
         self.wl = wl
@@ -198,6 +202,8 @@ class MicProblem:
         self._check(L.mic_set_materials(self.h, ctypes.byref(self.materials)), "mic_set_materials")
         self._check(L.mic_set_options(self.h, ctypes.byref(self.options)), "mic_set_options")
         self._check(L.mic_set_bcs(self.h, ctypes.byref(self.bcs)), "mic_set_bcs")
+        if jaumann:
+            self.set_stress_rotation(MIC_ROTATION_JAUMANN)
         self.upload_markers(mk)
         for name, arr in wl.nodal.items():
             self.set_nodal(name, arr)
@@ -205,6 +211,15 @@ class MicProblem:
     def _check(self, code, what):
         if code != 0:
             raise MicError(code, what)
+
+    def set_stress_rotation(self, rotation):
+        """MIC_ROTATION_EXACT (markers.c:2158-2164) or MIC_ROTATION_JAUMANN (2147-2156)"""
+        self._check(self.L.mic_set_stress_rotation(self.h, rotation), "mic_set_stress_rotation")
+
+    def stress_rotation(self):
+        r = ctypes.c_int(-1)
+        self._check(self.L.mic_get_stress_rotation(self.h, ctypes.byref(r)), "mic_get_stress_rotation")
+        return r.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -116,6 +116,10 @@ static int ensure_ctx(GridData *grid, MarkerSet *ms) {
   }
   g.ms = ms;
   g.where = ON_HOST;
+#ifdef JAUMANN
+  /* the application is built with the Jaumann stress rotation (markers.c:2147-2156) */
+  if ((e = mic_set_stress_rotation(g.ctx, MIC_ROTATION_JAUMANN))) return note(e);
+#endif
   return MIC_OK;
 }
 

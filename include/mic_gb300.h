@@ -76,6 +76,13 @@ int mic_set_options(mic_ctx *ctx, const mic_options *options);
  * vx type 0 or 1; on a non-periodic grid left vy type 0 or 1. */
 int mic_set_bcs(mic_ctx *ctx, const mic_bcs *bcs);
 int mic_get_bcs(mic_ctx *ctx, mic_bcs *bcs); /* the context's boundary conditions */
+/* The stress rotation of advectMarkersRK, the reference's compile-time JAUMANN switch as a
+ * context setting (new): MIC_ROTATION_EXACT (default) rotates the marker stresses through the
+ * angle -wxy dt (markers.c:2158-2164, the reference built without JAUMANN); MIC_ROTATION_JAUMANN
+ * adds the first-order Jaumann terms (markers.c:2147-2156, built with -DJAUMANN). */
+enum { MIC_ROTATION_EXACT = 0, MIC_ROTATION_JAUMANN = 1 };
+int mic_set_stress_rotation(mic_ctx *ctx, int rotation);
+int mic_get_stress_rotation(mic_ctx *ctx, int *rotation);
 int mic_get_grid_centres(mic_ctx *ctx, double *xc, double *yc); /* NX+1, NY+1 entries */
 
 /* ---- markers: host AoS records <-> device columns ---- */

@@ -36,5 +36,10 @@ done
 $CC $CFLAGS $INC -c "$HERE/petsc_lite/petsc_lite.c" -o "$OUT/petsc_lite.o"
 $CC $CFLAGS $INC -c "$HERE/ref_bridge.c" -o "$OUT/ref_bridge.o"
 $CC -shared -o "$OUT/libfvmic2d_ref.so" $OBJS "$OUT/petsc_lite.o" "$OUT/ref_bridge.o" -lm
+# the same library with the reference's compile-time JAUMANN switch (markers.c:2147-2156: the
+# first-order Jaumann stress rotation in advectMarkersRK instead of the exact rotation)
+$CC $CFLAGS -DJAUMANN $INC -c "$REF/markers.c" -o "$OUT/markers_jaumann.o"
+$CC -shared -o "$OUT/libfvmic2d_ref_jaumann.so" $(echo $OBJS | sed "s#$OUT/markers.o#$OUT/markers_jaumann.o#") \
+  "$OUT/petsc_lite.o" "$OUT/ref_bridge.o" -lm
 rm -f "$OUT"/*.o
-echo "built $OUT/libfvmic2d_ref.so"
+echo "built $OUT/libfvmic2d_ref.so $OUT/libfvmic2d_ref_jaumann.so"

@@ -31,6 +31,7 @@ struct orc_ctx {
   int64_t scratch_n;
   double residuals[100];   /* residual.c:9-10 ring of stored residuals */
   const mic_marker *mk_base; /* marker array of the current call (indexes the grain sizes) */
+  int jaumann;             /* stress rotation: the reference built with -DJAUMANN (markers.c:2147-2156) */
 };
 
 #define NODE(c, f, i, j) ((c)->nodal[f][(size_t)(j) * (size_t)(c)->NX + (size_t)(i)])
@@ -82,6 +83,7 @@ void orc_get_grid(const orc_ctx *c, double *xc, double *yc) {
 
 void orc_set_materials(orc_ctx *c, const mic_materials *m) { c->mat = *m; }
 void orc_set_options(orc_ctx *c, const mic_options *o) { c->opt = *o; }
+void orc_set_jaumann(orc_ctx *c, int on) { c->jaumann = on != 0; }
 
 int orc_set_bcs(orc_ctx *c, const mic_bcs *b) {
   /* markers.c:1986-2023 reads ghost velocities unless the top vx / left vy boundary is 0 or 1 */
@@ -736,7 +738,8 @@ int orc_subgrid_temperature_changes(orc_ctx *c, mic_marker *mk, int64_t n, doubl
 /* ------------------------------------------------------------------------- */
 /* advection                                                                  */
 
-/* advectMarkersRK (markers.c:1865-2250), non-periodic grid, non-JAUMANN stress rotation */
+/* advectMarkersRK (markers.c:1865-2250), non-periodic grid; the stress rotation of the default
+ * build or of -DJAUMANN (orc_set_jaumann) */
 int orc_advect_markers_rk(orc_ctx *c, mic_marker *mk, int64_t n, double dt) {
   const int NX = c->NX, NY = c->NY;
   const double *vx = c->nodal[MIC_NF_VX], *vy = c->nodal[MIC_NF_VY], *wz = c->nodal[MIC_NF_WXY];
@@ -841,12 +844,20 @@ int orc_advect_markers_rk(orc_ctx *c, mic_marker *mk, int64_t n, double dt) {
     p->wxy = (mwz[0] + 2 * mwz[1] + 2 * mwz[2] + mwz[3]) / 6.0;
     p->X += dt * p->VX;
     p->Y += dt * p->VY;
-    /* finite rotation of the stress tensor by -wxy dt (2158-2164) */
     const double s11 = p->s.T11, s22 = p->s.T22, s12 = p->s.T12;
-    const double th = -p->wxy * dt;
-    p->s.T11 = s11 * pow(cos(th), 2.0) + s22 * pow(sin(th), 2.0) - s12 * sin(2.0 * th);
-    p->s.T22 = s11 * pow(sin(th), 2.0) + s22 * pow(cos(th), 2.0) + s12 * sin(2.0 * th);
-    p->s.T12 = 0.5 * (s11 - s22) * sin(2.0 * th) + s12 * cos(2.0 * th);
+    if (c->jaumann) {
+      /* first-order Jaumann terms, wxy1 = wxy dt (2147-2156) */
+      const double w1 = p->wxy * dt;
+      p->s.T11 += 2.0 * s12 * -w1;
+      p->s.T22 += 2.0 * s12 * w1;
+      p->s.T12 += (s11 - s22) * w1;
+    } else {
+      /* finite rotation of the stress tensor by -wxy dt (2158-2164) */
+      const double th = -p->wxy * dt;
+      p->s.T11 = s11 * pow(cos(th), 2.0) + s22 * pow(sin(th), 2.0) - s12 * sin(2.0 * th);
+      p->s.T22 = s11 * pow(sin(th), 2.0) + s22 * pow(cos(th), 2.0) + s12 * sin(2.0 * th);
+      p->s.T12 = 0.5 * (s11 - s22) * sin(2.0 * th) + s12 * cos(2.0 * th);
+    }
     p->Eii += dt * sqrt(0.5 * (p->e.T11 * p->e.T11 + p->e.T22 * p->e.T22) + p->e.T12 * p->e.T12);
   }
 #undef VXN

@@ -39,6 +39,8 @@ void orc_destroy(orc_ctx *c);
 void orc_get_grid(const orc_ctx *c, double *xc, double *yc);
 void orc_set_materials(orc_ctx *c, const mic_materials *m);
 void orc_set_options(orc_ctx *c, const mic_options *o);
+/* advectMarkersRK's stress rotation as the reference compiled with -DJAUMANN (markers.c:2147-2156) */
+void orc_set_jaumann(orc_ctx *c, int on);
 int orc_set_bcs(orc_ctx *c, const mic_bcs *b);
 int orc_set_nodal(orc_ctx *c, int field, const double *v);
 int orc_get_nodal(const orc_ctx *c, int field, double *v);

@@ -31,6 +31,7 @@ def lib():
             "orc_get_grid": (None, [_P, _DP, _DP]),
             "orc_set_materials": (None, [_P, _P]),
             "orc_set_options": (None, [_P, _P]),
+            "orc_set_jaumann": (None, [_P, _I]),
             "orc_set_bcs": (_I, [_P, _P]),
             "orc_set_nodal": (_I, [_P, _I, _DP]),
             "orc_get_nodal": (_I, [_P, _I, _DP]),
@@ -83,7 +84,8 @@ def _dp(a):
 class OracleProblem:
     """Same surface as refpy.RefProblem, backed by the C restatement."""
 
-    def __init__(self, wl, markers=None):
+    def __init__(self, wl, markers=None, jaumann=False):
+        """jaumann: the stress rotation of the reference built with -DJAUMANN"""
         L = lib()
         g = wl.grid
         self.wl = wl
@@ -92,6 +94,7 @@ class OracleProblem:
         self.materials, self.options, self.bcs = wl.materials, wl.options, wl.bcs
         L.orc_set_materials(self.h, ctypes.byref(self.materials))
         L.orc_set_options(self.h, ctypes.byref(self.options))
+        L.orc_set_jaumann(self.h, 1 if jaumann else 0)
         if L.orc_set_bcs(self.h, ctypes.byref(self.bcs)) != 0:
             raise ValueError("boundary types other than 0/1 on the top-vx / left-vy walls are not supported")
         self.markers = np.array(wl.markers if markers is None else markers, dtype=MARKER_DTYPE, copy=True)

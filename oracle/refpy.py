@@ -11,24 +11,27 @@ from fvmic2d_gb300.mic_types import NF, MARKER_DTYPE, MARKER_F64_OFFSETS
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libfvmic2d_ref.so")
+# the same sources with markers.c compiled under -DJAUMANN (the Jaumann stress rotation of
+# advectMarkersRK, markers.c:2147-2156)
+LIB_PATH_JAUMANN = os.path.join(HERE, "_ref", "libfvmic2d_ref_jaumann.so")
 
-_lib = None
+_libs = {}
 _P = ctypes.c_void_p
 _D = ctypes.c_double
 _I = ctypes.c_int
 _DP = ctypes.POINTER(ctypes.c_double)
 
 
-def available():
-    return os.path.exists(LIB_PATH)
+def available(jaumann=False):
+    return os.path.exists(LIB_PATH_JAUMANN if jaumann else LIB_PATH)
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not available():
-            raise RuntimeError("oracle/_ref/libfvmic2d_ref.so missing: run oracle/build_ref.sh where the reference tree exists")
-        L = ctypes.CDLL(LIB_PATH)
+def lib(jaumann=False):
+    if jaumann not in _libs:
+        path = LIB_PATH_JAUMANN if jaumann else LIB_PATH
+        if not os.path.exists(path):
+            raise RuntimeError("%s missing: run oracle/build_ref.sh where the reference tree exists" % path)
+        L = ctypes.CDLL(path)
         sig = {
             "ref_create": (_P, [_I, _I, _D, _D, _DP, _DP]),
             "ref_destroy": (None, [_P]),
@@ -85,8 +88,8 @@ def lib():
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
-        _lib = L
-    return _lib
+        _libs[jaumann] = L
+    return _libs[jaumann]
 
 
 def _dp(a):
@@ -97,8 +100,9 @@ class RefProblem:
     """One reference problem: grid + nodal Vecs + material/option tables + a marker array
     that stays owned by this object (the reference functions mutate it in place)."""
 
-    def __init__(self, wl, markers=None):
-        L = lib()
+    def __init__(self, wl, markers=None, jaumann=False):
+        """jaumann: step with the reference built under -DJAUMANN"""
+        self.L = L = lib(jaumann)
         g = wl.grid
         self.wl = wl
         self.NX, self.NY = g.NX, g.NY
@@ -118,13 +122,13 @@ class RefProblem:
 
     def saveMarkersBinary(self, iMonte, iTime, elapsed_time):
         """writes output/Markers.<iMonte>.<iTime> under the current directory"""
-        L = lib()
+        L = self.L
         e = L.ref_saveMarkersBinary(self.h, self.markers.ctypes.data, len(self.markers), iMonte, iTime, elapsed_time)
         L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         return e
 
     def restartFromMarkers(self, iMonte, iTime, cap, maxMarkFactor=1.0):
-        L = lib()
+        L = self.L
         mk = np.zeros(cap, dtype=self.markers.dtype)
         t = ctypes.c_double(0.0)
         n = L.ref_restartFromMarkers(self.h, iMonte, iTime, maxMarkFactor, mk.ctypes.data, cap, ctypes.byref(t))
@@ -136,20 +140,20 @@ class RefProblem:
 
     def projectMarkersNodesFromScalar(self, values, nodal):
         v = np.ascontiguousarray(values, dtype=np.float64)
-        return lib().ref_projectMarkersNodesFromScalar(self.h, _dp(v), NF[nodal])
+        return self.L.ref_projectMarkersNodesFromScalar(self.h, _dp(v), NF[nodal])
 
     def nodalStressStrain(self, dt, gy=0.0):
-        return lib().ref_nodalStressStrain(self.h, dt, gy)
+        return self.L.ref_nodalStressStrain(self.h, dt, gy)
 
     def limitDisplacementTimestep(self, dt, factor):
-        return lib().ref_limitDisplacementTimestep(self.h, dt, factor)
+        return self.L.ref_limitDisplacementTimestep(self.h, dt, factor)
 
     def retrieveSolutions(self, S, Kcont):
         S = np.ascontiguousarray(S, dtype=np.float64)
-        return lib().ref_retrieveSolutions(self.h, _dp(S), Kcont)
+        return self.L.ref_retrieveSolutions(self.h, _dp(S), Kcont)
 
     def _system(self, which):
-        L = lib()
+        L = self.L
         nrows = ctypes.c_long(0)
         nnz = L.ref_system_nnz(which, ctypes.byref(nrows))
         rowptr = np.zeros(nrows.value + 1, dtype=np.int32)
@@ -164,44 +168,44 @@ class RefProblem:
         Kcont), the matrix as CSR with ascending columns, rows in the reference's ordering
         3 (j NX + i) + dof"""
         kb, kc = ctypes.c_double(0.0), ctypes.c_double(0.0)
-        e = lib().ref_formVEPSystem(self.h, ctypes.byref(sopt), dt, ctypes.byref(kb), ctypes.byref(kc))
+        e = self.L.ref_formVEPSystem(self.h, ctypes.byref(sopt), dt, ctypes.byref(kb), ctypes.byref(kc))
         if e:
             raise RuntimeError("formVEPSystem failed: %d" % e)
         return self._system(0) + (kb.value, kc.value)
 
     def adiabaticHeating(self, gy):
         """adiabaticHeating (adiabaticHeating.c:7) added to the heating field as main adds it"""
-        e = lib().ref_adiabaticHeating(self.h, gy)
+        e = self.L.ref_adiabaticHeating(self.h, gy)
         if e:
             raise RuntimeError("adiabaticHeating failed: %d" % e)
 
     def nusseltNumber(self, bottom, top):
-        return lib().ref_nusseltNumber(self.h, bottom, top)
+        return self.L.ref_nusseltNumber(self.h, bottom, top)
 
     def rmsVelocity(self):
-        return lib().ref_rmsVelocity(self.h)
+        return self.L.ref_rmsVelocity(self.h)
 
     def initialConditionsVanKeken(self, sopt):
         """initialConditionsVanKeken on this problem's markers; returns the BCs it sets"""
         from fvmic2d_gb300.mic_types import BCs
 
         b = BCs()
-        e = lib().ref_initialConditionsVanKeken(self.h, self.markers.ctypes.data, len(self.markers),
+        e = self.L.ref_initialConditionsVanKeken(self.h, self.markers.ctypes.data, len(self.markers),
                                                 ctypes.byref(sopt), ctypes.byref(b))
-        lib().ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
+        self.L.ref_set_markers(self.h, self.markers.ctypes.data, len(self.markers))
         if e:
             raise RuntimeError("initialConditionsVanKeken failed: %d" % e)
         return b
 
     def enforceThermalBCs1(self, sopt):
-        e = lib().ref_enforceThermalBCs1(self.h, ctypes.byref(sopt))
+        e = self.L.ref_enforceThermalBCs1(self.h, ctypes.byref(sopt))
         if e:
             raise RuntimeError("enforceThermalBCs1 failed: %d" % e)
 
     def formThermalSystem(self, sopt, dt, doSteady=0):
         """formThermalSystem (formThermalSystem.c:6) with the right-hand side starting as the
         heating field: (rowptr, cols, vals, rhs)"""
-        e = lib().ref_formThermalSystem(self.h, ctypes.byref(sopt), dt, doSteady)
+        e = self.L.ref_formThermalSystem(self.h, ctypes.byref(sopt), dt, doSteady)
         if e:
             raise RuntimeError("formThermalSystem failed: %d" % e)
         return self._system(1)
@@ -209,7 +213,7 @@ class RefProblem:
     def checkMarkerDensity(self, dopt, cap, seed=1):
         """The reference's checkMarkerDensity (PETSCRAND48 object seeded with srand48(seed)) on a
         copy of the markers grown to capacity cap; returns (markers[:n_new], 48-bit state)."""
-        L = lib()
+        L = self.L
         mk = np.zeros(cap, dtype=self.markers.dtype)
         mk[:len(self.markers)] = self.markers
         slab = np.array([dopt.slabAngle, dopt.slabAge, dopt.overridingPlateThickness, dopt.rootThickness,
@@ -227,7 +231,7 @@ class RefProblem:
 
     def distribute_uniform(self, NMX, NMY, cap=None):
         """The reference's resetMarkers + distributeMarkersUniformInDomain (seed 0)."""
-        L = lib()
+        L = self.L
         cap = cap or NMX * NMY * (self.wl.grid.NX - 1) * (self.wl.grid.NY - 1) + 16
         mk = np.zeros(cap, dtype=self.markers.dtype)
         L.ref_resetMarkers(self.h, mk.ctypes.data, cap)
@@ -237,7 +241,7 @@ class RefProblem:
 
     def close(self):
         if self.h:
-            lib().ref_destroy(self.h)
+            self.L.ref_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -249,33 +253,33 @@ class RefProblem:
     def grid_centres(self):
         xc = np.empty(self.NX + 1)
         yc = np.empty(self.NY + 1)
-        lib().ref_get_grid(self.h, _dp(xc), _dp(yc))
+        self.L.ref_get_grid(self.h, _dp(xc), _dp(yc))
         return xc, yc
 
     def set_nodal(self, name, arr):
         a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.NY, self.NX)
-        assert lib().ref_set_nodal(self.h, NF[name], _dp(a)) == 0
+        assert self.L.ref_set_nodal(self.h, NF[name], _dp(a)) == 0
 
     def get_nodal(self, name):
         a = np.empty((self.NY, self.NX))
-        assert lib().ref_get_nodal(self.h, NF[name], _dp(a)) == 0
+        assert self.L.ref_get_nodal(self.h, NF[name], _dp(a)) == 0
         return a
 
     # --- reference entry points -------------------------------------------------
     def findMarkerCells(self):
-        return lib().ref_findMarkerCells(self.h)
+        return self.L.ref_findMarkerCells(self.h)
 
     def updateMarkerRho(self):
-        lib().ref_updateMarkerRho(self.h)
+        self.L.ref_updateMarkerRho(self.h)
 
     def maxMarkerT(self):
-        return lib().ref_maxMarkerT(self.h)
+        return self.L.ref_maxMarkerT(self.h)
 
     def maxAbsSxx(self):
-        return lib().ref_maxAbsSxx(self.h)
+        return self.L.ref_maxAbsSxx(self.h)
 
     def projectMarkersNodesAll2(self):
-        return lib().ref_projectMarkersNodesAll2(self.h)
+        return self.L.ref_projectMarkersNodesAll2(self.h)
 
     def projectMarkerFieldToNodes(self, field, out, stagx, stagy, method, matprop=None):
         off = -1 if field is None else MARKER_F64_OFFSETS[field]
@@ -283,34 +287,34 @@ class RefProblem:
         if matprop is not None:
             self._mp = np.ascontiguousarray(matprop, dtype=np.float64)
             mp = _dp(self._mp)
-        return lib().ref_projectMarkerFieldToNodes(self.h, off, mp, NF[out], stagx, stagy, method)
+        return self.L.ref_projectMarkerFieldToNodes(self.h, off, mp, NF[out], stagx, stagy, method)
 
     def projectNodalFieldToMarkersS(self, nodal, field):
-        return lib().ref_projectNodalFieldToMarkersS(self.h, NF[nodal], MARKER_F64_OFFSETS[field])
+        return self.L.ref_projectNodalFieldToMarkersS(self.h, NF[nodal], MARKER_F64_OFFSETS[field])
 
     def checkPlasticYielding(self, dt, t=0.0):
-        return lib().ref_checkPlasticYielding(self.h, dt, t)
+        return self.L.ref_checkPlasticYielding(self.h, dt, t)
 
     def limitViscosity(self):
-        lib().ref_limitViscosity(self.h)
+        self.L.ref_limitViscosity(self.h)
 
     def updateMarkerStrainPressure(self, dt):
-        return lib().ref_updateMarkerStrainPressure(self.h, dt)
+        return self.L.ref_updateMarkerStrainPressure(self.h, dt)
 
     def updateGlobalStrainRateResidual(self, it=0):
-        return lib().ref_updateGlobalStrainRateResidual(self.h, it)
+        return self.L.ref_updateGlobalStrainRateResidual(self.h, it)
 
     def subgridStressChanges(self, dt, D):
-        return lib().ref_subgridStressChanges(self.h, dt, D)
+        return self.L.ref_subgridStressChanges(self.h, dt, D)
 
     def updateMarkerStress(self):
-        return lib().ref_updateMarkerStress(self.h)
+        return self.L.ref_updateMarkerStress(self.h)
 
     def subgridTemperatureChanges(self, dt):
-        return lib().ref_subgridTemperatureChanges(self.h, dt)
+        return self.L.ref_subgridTemperatureChanges(self.h, dt)
 
     def advectMarkersRK(self, dt):
-        return lib().ref_advectMarkersRK(self.h, dt)
+        return self.L.ref_advectMarkersRK(self.h, dt)
 
 
 def goldsby_kohlstedt(s, T, d, P):

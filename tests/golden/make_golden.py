@@ -88,11 +88,13 @@ def edge_case_workload():
     return wl
 
 
-def record(wl, steps=2):
-    """Run `steps` reference steps; store inputs and the state after every entry point."""
-    p = refpy.RefProblem(wl)
+def record(wl, steps=2, jaumann=False):
+    """Run `steps` reference steps; store inputs and the state after every entry point.
+    jaumann: the reference built with -DJAUMANN (advectMarkersRK's first-order stress rotation)."""
+    p = refpy.RefProblem(wl, jaumann=jaumann)
     out = {"x": wl.grid.x, "y": wl.grid.y, "LX": wl.grid.LX, "LY": wl.grid.LY,
-           "markers_in": wl.markers.copy(), "dt": wl.dt, "dt_thermal": wl.dt_thermal}
+           "markers_in": wl.markers.copy(), "dt": wl.dt, "dt_thermal": wl.dt_thermal,
+           "jaumann": np.int32(1 if jaumann else 0)}
     for name, arr in wl.nodal.items():
         out["nodal_in_" + name] = np.asarray(arr, dtype=np.float64)
     D = wl.options.subgridStressDiffusivity
@@ -413,6 +415,13 @@ def main():
         rec.update(tables(wl))
         np.savez_compressed(os.path.join(OUT, "periodic_box.npz"), **rec)
         print("wrote periodic_box", len(wl.markers), "markers")
+    if sys.argv[1:] in ([], ["jaumann"]):
+        # the same path with the reference's compile-time JAUMANN stress rotation (markers.c:2147-2156)
+        wl = W.vep_slab_box(nx_cells=16, ny_cells=4, nm=4, seed=12)
+        rec = record(wl, steps=2, jaumann=True)
+        rec.update(tables(wl))
+        np.savez_compressed(os.path.join(OUT, "vep_jaumann.npz"), **rec)
+        print("wrote vep_jaumann", len(wl.markers), "markers")
     if sys.argv[1:]:
         return
     cases = {

@@ -15,7 +15,7 @@ from fvmic2d_gb300 import gpu, workloads as W
 from fvmic2d_gb300.mic_types import MARKER_DTYPE, PROJECTED_FIELDS
 from oracle import oraclepy
 from tests.helpers import compare_markers, exact, close, RTOL
-from tests.test_oracle_pin import load_case, run_sequence, as_markers
+from tests.test_oracle_pin import load_case, run_sequence, as_markers, is_jaumann
 
 pytestmark = pytest.mark.gpu
 
@@ -224,10 +224,11 @@ def test_generic_projection_exact(stag, method):
 
 
 @pytest.mark.parametrize("exact_build", [False, True])
-@pytest.mark.parametrize("name", ["convection_box_8", "vep_slab_box_16x4", "edge_cases", "periodic_box"])
+@pytest.mark.parametrize("name", ["convection_box_8", "vep_slab_box_16x4", "edge_cases", "periodic_box",
+                                  "vep_jaumann"])
 def test_sequence_matches_reference_golden(name, exact_build):
     wl, z = load_case(name)
-    G = gpu.MicProblem(wl, exact=exact_build)
+    G = gpu.MicProblem(wl, exact=exact_build, jaumann=is_jaumann(z))
     fails = []
 
     def check(tag, P, nout=None, value=None):

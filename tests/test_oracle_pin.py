@@ -19,7 +19,7 @@ from oracle import oraclepy, refpy
 from tests.helpers import compare_markers, exact, same_fields
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["convection_box_8", "vep_slab_box_16x4", "edge_cases"]
+CASES = ["convection_box_8", "vep_slab_box_16x4", "edge_cases", "vep_jaumann"]
 
 
 def as_markers(a):
@@ -40,6 +40,11 @@ def load_case(name):
     wl = W.Workload(name, g, as_markers(z["markers_in"]), mat, opt, bcs, nodal,
                     float(z["dt"]), float(z["dt_thermal"]), 2)
     return wl, z
+
+
+def is_jaumann(z):
+    """fixture recorded with the reference built with -DJAUMANN"""
+    return "jaumann" in z.files and int(z["jaumann"]) == 1
 
 
 def run_sequence(P, wl, z, steps=2, check=None):
@@ -103,10 +108,22 @@ def golden_checker(z, fails):
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_matches_golden(name):
     wl, z = load_case(name)
-    P = oraclepy.OracleProblem(wl)
+    P = oraclepy.OracleProblem(wl, jaumann=is_jaumann(z))
     fails = []
     run_sequence(P, wl, z, check=golden_checker(z, fails))
     assert not fails, "\n".join(fails[:20])
+
+
+def test_jaumann_fixture_tells_the_rotations_apart():
+    """The -DJAUMANN fixture is not met by the default build's exact rotation: after the first
+    advection the stresses differ, so the golden test above checks the switch itself."""
+    wl, z = load_case("vep_jaumann")
+    assert is_jaumann(z)
+    P = oraclepy.OracleProblem(wl, jaumann=False)
+    fails = []
+    run_sequence(P, wl, z, steps=1, check=golden_checker(z, fails))
+    assert fails and all("after_advect" in f or "maxSxx" in f for f in fails), fails[:5]
+    assert any("sxx" in f for f in fails)
 
 
 def test_goldsby_kohlstedt_matches_golden():
