@@ -61,7 +61,11 @@ constexpr double kGrainDefault = 1e-3;  // metres, until mic_markers_set_grain_s
 // warp run) plus log2 and exp2.
 __device__ __forceinline__ CreepCoef creep_coef(double T, double g, double P) {
   const double R = 8.3144621;
+#ifdef MIC_EXACT
   if (P < 1.0) P = 1.0;
+#else
+  if (lt_pos(P, 1.0)) P = 1.0;  // the compares of this build by bit pattern (no FP64-pipe slot)
+#endif
   const double RT = R * T;
   const double b = 4.52e-10, Vm = 1.97e-5, delta = 2.0 * b;
   const double V = -13e-6;
@@ -90,9 +94,10 @@ __device__ __forceinline__ CreepCoef creep_coef(double T, double g, double P) {
   const double Dv = 9.10e-4 * e594;
   const double Db = 5.8e-4 * e49;
   const double g2 = g * g, id = (g2 * g2) * g;  // 1/d
-  k.C = 42.0 * Vm * iRT * id * id * (Dv + M_PI * delta * id * Db);
-  const double eg = (T < 255.0) ? 3.9e-3 * e49 : 3.0e26 * e192;
-  const double ed = (T < 258.0) ? 4.0e5 * e60 : 6.0e28 * e180;
+  k.C = 42.0 * Vm * iRT * id * id * fma(M_PI * delta * id, Db, Dv);
+  const bool cold_g = lt_pos(T, 255.0), cold_d = lt_pos(T, 258.0);
+  const double eg = (cold_g ? 3.9e-3 : 3.0e26) * (cold_g ? e49 : e192);
+  const double ed = (cold_d ? 4.0e5 : 6.0e28) * (cold_d ? e60 : e180);
   k.G = eg * eP * (id * g2);  // d^-1.4
   k.D = ed * eP;
   k.B = 5.5e7 * e60 * eP;
@@ -182,7 +187,7 @@ __device__ __forceinline__ float ln_f(double v) {
   const long long b = __double_as_longlong(v);
   const int e = (int)((b >> 52) & 0x7FF) - 1023;
   const float mant = __int_as_float(0x3F800000 | (int)((b >> 29) & 0x7FFFFF));
-  return (float)e * 0.693147181f + __logf(mant);
+  return fmaf((float)e, 0.693147181f, __logf(mant));
 }
 
 #ifndef MIC_EXACT
@@ -212,89 +217,106 @@ __device__ __forceinline__ void creep_eval(const CreepTerms &q, double p, CreepE
   e.p5 = p4 * p;
   e.td = q.a * e.p5;
   e.tl = q.d * (p12 * p8);
-  e.S = e.tg + e.tb;
-  e.N = fma((e.td + e.tl) - 1.0, e.S, e.tg * e.tb);
+  // explicit roundings where a product meets a sum: the solve is shared by several kernels and
+  // must not depend on how the compiler fuses it in each (the members of a batch and the
+  // fallback of the surrogate modes reproduce the exact solve bit for bit)
+  e.S = __dadd_rn(e.tg, e.tb);
+  e.N = fma(__dadd_rn(__dadd_rn(e.td, e.tl), -1.0), e.S, e.tg * e.tb);
 }
-__device__ __forceinline__ bool creep_converged(const CreepEval &e, double tol) { return fabs(e.N) <= tol * e.S; }
+// |r - 1| <= tol as |N| <= tol S, compared by bit pattern (S > 0)
+__device__ __forceinline__ bool creep_converged(const CreepEval &e, double tol) { return abs_le(e.N, tol * e.S); }
 // the residual r - 1 (to FP32 accuracy: reported, and used for the step far from the root)
 __device__ __forceinline__ double creep_residual(const CreepEval &e) { return e.N / e.S; }
 
-// Halley step in u = ln s for g(u) = ln r from one evaluation.  With r' and r'' the u-derivatives
-// of r = td + tc + tl (term slopes 1, mc = 1.8 + 0.6 w for the series tc = tb w, w = tg / S, and 4;
-// the series' log has curvature -0.36 w (1 - w)), g' = r'/r, g'' = r''/r - g'^2, and
-// du = -2 g g' / (2 g'^2 - g g'').  The quotients come from FP32 copies: their rounding (about
-// 1e-7 of the step) only perturbs the next iterate.  Near the root (|r - 1| < 2^-16) g and g' are
-// formed in FP64 from the exact N and S (the step then decides the last digits); the small
-// Halley correction stays FP32.  Returns du.
-__device__ __forceinline__ double creep_step(const CreepEval &e) {
-  const float S = (float)e.S, tb = (float)e.tb, td = (float)e.td, tl = (float)e.tl;
+// p exp(a) for a step a = 0.2 du formed in FP32: for |a| < 2^-5 as p + p d with d = exp(a) - 1
+// from its series in FP32 (truncation below 2^-30 of d) and one FMA, else p times an FP32
+// exponential.  The rounding of d (2^-24 of a step of at most 3 %) is below that of the FP32 step
+// itself; the float-to-double conversions go by bit pattern.
+__device__ __forceinline__ double creep_advance_f32(double p, float a) {
+  if (fabsf(a) < 0.03125f) {
+    const float d = a * fmaf(a, fmaf(a, fmaf(a, fmaf(a, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f), 0.5f), 1.0f);
+    return fma(p, f64_of(d), p);
+  }
+  return p * f64_of(__expf(fminf(fmaxf(a, -80.0f), 80.0f)));
+}
+
+// One step from an evaluation: p exp(0.2 du) for the Halley step du in u = ln s on
+// g(u) = ln r.  With r' and r'' the u-derivatives of r = td + tc + tl (term slopes 1,
+// mc = 1.8 + 0.6 w for the series tc = tb w, w = tg / S, and 4; the series' log has curvature
+// -0.36 w (1 - w)), g' = r'/r, g'' = r''/r - g'^2, and du = -2 g g' / (2 g'^2 - g g'').  The
+// quotients come from FP32 copies (by bit pattern; N, S and tg scaled by S's binary exponent, so
+// that the ratios N / S and tg / S stay in FP32 range however small the series' terms are): their
+// rounding, about 1e-7 of the step, only perturbs the next iterate.  With `fine` (a tolerance
+// FP32 steps cannot reach) and |r - 1| < 2^-16, g and g' are formed in FP64 from the exact N and
+// S and the step decides the last digits; the small Halley correction stays FP32.
+__device__ __forceinline__ double creep_advance(const CreepEval &e, double p, bool fine) {
+  const int k = exp2_of(e.S);
+  const float S = f32_trunc(e.S, k), tg = f32_trunc(e.tg, k), N = f32_trunc(e.N, k);
+  const float tb = f32_trunc(e.tb), td = f32_trunc(e.td), tl = f32_trunc(e.tl);
   const float iS = 1.0f / S;
-  const float w = (float)e.tg * iS;
+  const float w = tg * iS;
   const float tc = tb * w;
-  const float resf = (float)e.N * iS;
+  const float resf = N * iS;
   const float mc = fmaf(0.6f, w, 1.8f);
   const float r1f = fmaf(tc, mc, fmaf(4.0f, tl, td));
   const float r2f = fmaf(tc, fmaf(mc, mc, -0.36f * w * (1.0f - w)), fmaf(16.0f, tl, td));
-  if (!(fabsf(resf) < 0x1p-16f)) {
-    const float r = td + tc + tl;
-    if (!(r > 1e-30f && r < 1e30f && S < 1e30f)) {
+  if (!fine || !(fabsf(resf) < 0x1p-16f)) {
+    const float r = __fadd_rn(__fadd_rn(td, tc), tl);
+    if (!(r > 1e-30f && r < 1e30f && lt_pos(e.S, 1e30))) {
       // terms beyond FP32 range (an iterate far from the root): a step of -g / 4, which the
       // slope bound g' <= 4 keeps on the root's side
-      return -0.25 * (double)ln_f(fabs(creep_residual(e) + 1.0));
+      return creep_advance_f32(p, -0.05f * ln_f(fabs(creep_residual(e) + 1.0)));
     }
     const float ir = 1.0f / r;
     const float g = fabsf(resf) < 0.5f ? log1pf(resf) : __logf(r);
     const float g1 = r1f * ir, g2 = fmaf(-g1, g1, r2f * ir);
     const float den = fmaf(-g, g2, 2.0f * g1 * g1);
     // Halley where its correction is moderate, Newton otherwise
-    return (double)(den > g1 * g1 ? -2.0f * g * g1 / den : -g / g1);
+    const float du = den > g1 * g1 ? -2.0f * g * g1 / den : -g / g1;
+    return creep_advance_f32(p, 0.2f * du);
   }
-  const double t = creep_residual(e);
+  const double iS64 = 1.0 / e.S;
+  const double t = e.N * iS64;
   const double g = t * fma(t, fma(t, fma(t, -0.25, 1.0 / 3.0), -0.5), 1.0);  // ln(1 + t), |t| < 2^-16
-  const double w64 = e.tg / e.S;
+  const double w64 = e.tg * iS64;
   const double r1 = fma(e.tb * w64, fma(0.6, w64, 1.8), fma(4.0, e.tl, e.td));
   // r = 1 + t within 2^-16, so the correction g g'' / (2 g'^2) is formed with r = 1
-  const float h = 1.0f - (float)g * (r2f - r1f * r1f) / (2.0f * r1f * r1f);
-  return -(g * (1.0 + t)) / (r1 * (double)h);
-}
-
-// exp(0.2 du), the factor that moves p by a step du in u: Taylor polynomial in FP64 for
-// |0.2 du| < 2^-5 (truncation below 7e-15), else FP32 (large steps are far from the root)
-__device__ __forceinline__ double creep_p_factor(double du) {
-  const double a = 0.2 * du;
-  if (fabs(a) < 0.03125) {
-    double t = fma(a, 1.0 / 720.0, 1.0 / 120.0);
-    t = fma(a, t, 1.0 / 24.0);
-    t = fma(a, t, 1.0 / 6.0);
-    t = fma(a, t, 0.5);
-    t = fma(a, t, 1.0);
-    return fma(a, t, 1.0);
-  }
-  return (double)__expf((float)fmin(fmax(a, -80.0), 80.0));
+  const float h = 1.0f - f32_trunc(g) * fmaf(-r1f, r1f, r2f) / (2.0f * r1f * r1f);
+  const double a = -0.2 * (g * (1.0 + t)) / (r1 * f64_of(h));
+  // exp(a) - 1 for |a| < 2e-5 to its third power (truncation below 1e-21)
+  return fma(p, a * fma(a, fma(a, 1.0 / 6.0, 0.5), 1.0), p);
 }
 
 // Steps from p until |r - 1| <= tol or maxit steps were taken; [plo, phi] brackets the root
-// (plo may be 0, phi infinite) and a step leaving it bisects in ln p instead.  Returns the
-// steps taken; conv, res and p5 belong to the final p (res to FP32 accuracy, at most tol in
-// magnitude when conv).
+// (plo may be 0, phi infinite; compared by bit pattern, all non-negative) and a step leaving it
+// bisects in ln p instead.  Returns the steps taken; conv, res and p5 belong to the final p (res
+// to FP32 accuracy, at most tol in magnitude when conv).
 __device__ __forceinline__ int creep_iterate(const CreepTerms &q, double &p, double plo, double phi, double tol,
                                              int maxit, bool &conv, double &res, double &p5) {
+  const bool fine = tol < 1e-9;
+  long long blo = __double_as_longlong(plo), bhi = __double_as_longlong(phi);
   CreepEval e;
   int it = 0;
   for (;; ++it) {
     creep_eval(q, p, e);
     conv = creep_converged(e, tol);
     if (conv || it >= maxit) break;
-    if (e.N > 0.0)
-      phi = fmin(phi, p);
+    const long long bp = __double_as_longlong(p);
+    if (__double_as_longlong(e.N) > 0)
+      bhi = min(bhi, bp);
     else
-      plo = fmax(plo, p);
-    double pn = p * creep_p_factor(creep_step(e));
-    if (!(pn > plo && pn < phi)) pn = (plo > 0.0) ? sqrt(plo * phi) : phi * 0.67032004603563930;  // e^-0.4
+      blo = max(blo, bp);
+    double pn = creep_advance(e, p, fine);
+    const long long bn = __double_as_longlong(pn);
+    if (!(bn > blo && bn < bhi)) {
+      const double lo = __longlong_as_double(blo), hi = __longlong_as_double(bhi);
+      pn = (blo > 0) ? sqrt(lo * hi) : hi * 0.67032004603563930;  // e^-0.4
+    }
     p = pn;
   }
-  res = (double)((float)e.N / (float)e.S);
-  if (conv) res = copysign(fmin(fabs(res), tol), res);
+  const int k = exp2_of(e.S);
+  res = f64_of(f32_trunc(e.N, k) / f32_trunc(e.S, k));
+  if (conv && !abs_le(res, tol)) res = copysign(tol, res);
   p5 = e.p5;
   return it;
 }
@@ -304,13 +326,13 @@ __device__ __forceinline__ int creep_iterate(const CreepTerms &q, double &p, dou
 __device__ __forceinline__ double creep_solve_terms(const CreepTerms &q, double tol, int maxit, int *iters,
                                                     double *res_out) {
   const float lp = fminf(-0.2f * ln_f(q.a), -0.05f * ln_f(q.d));
-  double p = (double)__expf(lp) * 1.0001, res, p5;
+  double p = f64_of(__expf(lp) * 1.0001f), res, p5;
   bool conv;
   *iters = creep_iterate(q, p, 0.0, INFINITY, tol, maxit, conv, res, p5);
   *res_out = res;
   const double s = 1e6 * p5;
   // the rate jumps at s = 1 Pa where the non-linear terms switch on; a root in the jump is 1 Pa
-  return s < 1.0 ? 1.0 : s;
+  return lt_pos(s, 1.0) ? 1.0 : s;
 }
 #endif
 
@@ -323,8 +345,9 @@ __device__ __forceinline__ double creep_stress_exact(const CreepCoef &k, double 
 #else
   *iters = 0;
   *res_out = 0.0;
-  if (!(edot > 0.0)) return 0.0;
-  if (edot < k.C) return edot / k.C;  // linear diffusion branch, s = edot / C < 1 Pa (viscosity.c:130-133)
+  if (!gt_zero(edot)) return 0.0;
+  // linear diffusion branch, s = edot / C < 1 Pa (viscosity.c:130-133); edot, C > 0 compared by bits
+  if (__double_as_longlong(edot) < __double_as_longlong(k.C)) return edot / k.C;
   return creep_solve_terms(creep_terms(k, iedot), tol, maxit, iters, res_out);
 #endif
 }
@@ -411,8 +434,8 @@ __device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, do
   *iters = 0;
   *res_out = 0.0;
   *fb = 0;
-  if (!(edot > 0.0)) return 0.0;
 #ifdef MIC_EXACT
+  if (!(edot > 0.0)) return 0.0;
   (void)iedot;
   const double s_lin = edot / k.C;
   if (s_lin < 1.0) return s_lin;
@@ -431,16 +454,17 @@ __device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, do
   *iters += it2;
   return s;
 #else
-  if (edot < k.C) return edot / k.C;
+  if (!gt_zero(edot)) return 0.0;
+  if (__double_as_longlong(edot) < __double_as_longlong(k.C)) return edot / k.C;
   const CreepTerms q = creep_terms(k, iedot);
   if (isfinite(lx0)) {
-    double p = (double)__expf(0.2f * lx0), res, p5;
+    double p = f64_of(__expf(0.2f * lx0)), res, p5;
     bool conv;
     *iters = creep_iterate(q, p, 0.0, INFINITY, polish_tol, polish_iters, conv, res, p5);
     if (conv) {
       *res_out = res;
       const double s = 1e6 * p5;
-      return s < 1.0 ? 1.0 : s;
+      return lt_pos(s, 1.0) ? 1.0 : s;
     }
   }
   *fb = 1;

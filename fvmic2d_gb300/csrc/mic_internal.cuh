@@ -358,6 +358,56 @@ __device__ __forceinline__ bool nan_bits(long long b) {
   return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
 }
 
+// Conversions and compares by bit pattern.  On GB300 every conversion to or from FP64 and every
+// FP64 compare or min/max takes a slot of the FP64 pipe (2 per SM per clock), the bound of the
+// FP64-heavy marker passes; these forms use integer instructions only.
+
+// a < c for a positive finite constant c and any a; false for NaN (as the FP64 compare)
+__device__ __forceinline__ bool lt_pos(double a, double c) {
+  const long long b = __double_as_longlong(a);
+  return b < __double_as_longlong(c) && !nan_bits(b);
+}
+// a > 0, false for zero of either sign and for NaN (as the FP64 compare)
+__device__ __forceinline__ bool gt_zero(double a) {
+  const long long b = __double_as_longlong(a);
+  return b > 0 && b <= 0x7FF0000000000000LL;
+}
+// |a| <= c for c >= 0 (not NaN); false for a NaN a
+__device__ __forceinline__ bool abs_le(double a, double c) {
+  return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFLL) <= __double_as_longlong(c);
+}
+
+// FP32 copy of v scaled by 2^-k, from its bit pattern: the exponent re-biased and the mantissa
+// truncated to 23 bits (relative error below 2^-23, against 2^-24 for a rounding conversion);
+// signed zero below FP32's normal range, infinity above it, NaN for NaN.
+__device__ __forceinline__ float f32_trunc(double v, int k = 0) {
+  const long long b = __double_as_longlong(v);
+  const unsigned hi = (unsigned)((unsigned long long)b >> 32);
+  const unsigned s = hi & 0x80000000u;
+  const int eb = (int)((hi >> 20) & 0x7FFu);
+  const int e = eb - 896 - k;
+  unsigned r = s | ((unsigned)e << 23) | ((unsigned)((unsigned long long)b >> 29) & 0x7FFFFFu);
+  if (e <= 0 || eb == 0) r = s;
+  if (e >= 255 || eb == 0x7FF) r = s | (nan_bits(b) ? 0x7FC00000u : 0x7F800000u);
+  return __uint_as_float(r);
+}
+// binary exponent of a positive normal double (floor(log2 v))
+__device__ __forceinline__ int exp2_of(double v) {
+  return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF) - 1023;
+}
+// exact FP64 value of f from its bit pattern: normal floats, infinities and NaN; zero and the FP32
+// subnormals (below 1.2e-38) give signed zero
+__device__ __forceinline__ double f64_of(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long m = (unsigned long long)(u & 0x7FFFFFu) << 29;
+  unsigned long long r = s | ((unsigned long long)(e + 896u) << 52) | m;
+  if (e == 0) r = s;
+  if (e == 255) r = s | 0x7FF0000000000000ULL | m;
+  return __longlong_as_double((long long)r);
+}
+
 // a / 6 from the correctly rounded reciprocal, corrected by one residual step (Markstein)
 __device__ __forceinline__ double div6(double a) {
 #ifdef MIC_EXACT

@@ -63,8 +63,16 @@ __device__ __forceinline__ int centre_cmax(const Params &P) { return P.xper ? P.
 
 // limitViscosity (viscosity.c:90-104) on one viscosity
 __device__ __forceinline__ double limit_eta(double e, const mic_options &O) {
+#ifdef MIC_EXACT
   if (e > O.etamax) return O.etamax;
   if (e < O.etamin) return O.etamin;
+#else
+  // the same two compares on order-preserving integer keys (a NaN viscosity stays NaN)
+  if (nan_bits(__double_as_longlong(e))) return e;
+  const long long k = ordered_bits(e);
+  if (k > ordered_bits(O.etamax)) return O.etamax;
+  if (k < ordered_bits(O.etamin)) return O.etamin;
+#endif
   return e;
 }
 
@@ -82,14 +90,14 @@ struct YieldCols {
 template <bool CREEP = true>
 __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_materials &M, const mic_options &O,
                                              const CreepConfig &cfg, double dt, int64_t m, float lx_guess,
-                                             const CreepCoef *kc, double kedot, Status *st, CreepIn &ci,
-                                             int &creep_active, int limit) {
+                                             const CreepCoef *kc, double kedot, double kiedot, Status *st,
+                                             CreepIn &ci, int &creep_active, int limit) {
   bool yielded = false;
   const double eta_old = c.eta[m], mu_old = c.mu[m];
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   const int k = c.mat[m];
   double eta, mu;
-  ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], lx_guess, 0, 0, 0.0, kc != nullptr, {}, kedot};
+  ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], lx_guess, 0, 0, 0.0, kc != nullptr, {}, kedot, kiedot};
   if (kc) ci.k = *kc;
   if (!(CREEP ? rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)
               : rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu))) {
@@ -168,11 +176,16 @@ __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_mater
 // coefficients, strain-rate invariant and surrogate features of marker m when it follows law 7
 // (false otherwise); *mref receives the features' reference
 __device__ __forceinline__ bool creep_marker_features(const YieldCols &c, const mic_materials &M, int64_t m,
-                                                      CreepCoef &k, double &edot, float f[4], float *mref) {
+                                                      CreepCoef &k, double &edot, double &iedot, float f[4],
+                                                      float *mref) {
   if (M.hasEtaT[c.mat[m]] != 7) return false;
-  edot = strain_rate_invariant(c.exx[m], c.eyy[m], c.exy[m]);
+  strain_rate_and_inverse(c.exx[m], c.eyy[m], c.exy[m], edot, iedot);
   k = creep_coef(c.T[m], c.grain[m], c.p[m]);
+#ifdef MIC_EXACT
   if (!(edot > 0.0)) {
+#else
+  if (!gt_zero(edot)) {
+#endif
     *mref = 0.f;
     f[0] = f[1] = f[2] = f[3] = 0.f;
     return true;
@@ -195,11 +208,12 @@ __device__ __forceinline__ bool yield_one(const YieldCols &c, const mic_material
   CreepIn ci = {};
   if (m < n && c.cellX[m] != -1) {
     float lx = 0.f, f[4], mref;
-    double edot = 0.0;
+    double edot = 0.0, iedot = 0.0;
     CreepCoef k;
-    const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, edot, f, &mref);
+    const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, edot, iedot, f, &mref);
     if (law7) lx = creep_guess_lx(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
-    yielded = yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, st, ci, creep_active, limit);
+    yielded = yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, iedot, st, ci, creep_active,
+                                      limit);
   } else if (limit && m < n) {
     c.eta[m] = limit_eta(c.eta[m], O);
   }
@@ -215,16 +229,16 @@ __device__ __forceinline__ bool yield_tc_round(tc::Block &B, const YieldCols &c,
                                                Status *st, CreepCounters *cc, int limit, int64_t m) {
   const bool live = m < n && c.cellX[m] != -1;
   float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
-  double edot = 0.0;
+  double edot = 0.0, iedot = 0.0;
   CreepCoef k;
-  const bool law7 = live && creep_marker_features(c, M, m, k, edot, f, &mref);
+  const bool law7 = live && creep_marker_features(c, M, m, k, edot, iedot, f, &mref);
   const float y = tc::guess(B, f, cfg.tc_wait_limit, &cc->tc_timeouts);
   int creep_active = 0;
   CreepIn ci = {};
   bool yielded = false;
   if (live)
-    yielded = yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 ? &k : nullptr, edot, st, ci,
-                           creep_active, limit);
+    yielded = yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 ? &k : nullptr, edot, iedot,
+                           st, ci, creep_active, limit);
   if (limit && !live && m < n) c.eta[m] = limit_eta(c.eta[m], O);
   creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   return yielded;

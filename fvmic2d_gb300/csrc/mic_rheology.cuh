@@ -17,26 +17,51 @@ struct CreepIn {
   float lx_guess;
   int iters, fb;
   double res;
-  int have_k;    // k and edot below already evaluated for this marker
+  int have_k;    // k, edot and iedot below already evaluated for this marker
   CreepCoef k;
   double edot;   // strain-rate invariant sqrt(0.5 (e11^2 + e22^2) + e12^2)
+  double iedot;  // 1 / edot (product build)
 };
 
 __device__ __forceinline__ double strain_rate_invariant(double e11, double e22, double e12) {
   return sqrt(0.5 * (e11 * e11 + e22 * e22) + e12 * e12);
 }
 
+// The strain-rate invariant and its reciprocal.  The FMA-free parity build takes the square root
+// (and divides by edot where the reference does; iedot is unused there).  The product build takes
+// one reciprocal square root r of the invariant's square q, edot = q r and 1 / edot = r (at most
+// about 1.5 ulp from the correctly rounded square root), where a square root and a division
+// would each cost several FP64 instructions; q = 0 and q = +inf give edot = q.
+__device__ __forceinline__ void strain_rate_and_inverse(double e11, double e22, double e12, double &edot,
+                                                        double &iedot) {
+#ifdef MIC_EXACT
+  edot = strain_rate_invariant(e11, e22, e12);
+  iedot = 0.0;
+#else
+  const double q = fma(e12, e12, 0.5 * fma(e11, e11, e22 * e22));
+  const double r = rsqrt(q);
+  const long long b = __double_as_longlong(q);
+  edot = (b == 0 || b == 0x7FF0000000000000LL) ? q : q * r;
+  iedot = r;
+#endif
+}
+
 // Law 7 (new): composite ice creep, eta = s* / (2 edot_II) with s* the stress at which the
 // Goldsby-Kohlstedt strain rate (viscosity.c:106-179) equals the marker's strain-rate
 // invariant; at zero strain rate the law's diffusion viscosity 0.5 / C (viscosity.c:130-133).
 __device__ __forceinline__ double creep_viscosity(const CreepConfig &cfg, double T, CreepIn &ci) {
-  const double edot = ci.have_k ? ci.edot : strain_rate_invariant(ci.e11, ci.e22, ci.e12);
+  double edot, iedot;  // once per marker: the solve and the viscosity share them
+  if (ci.have_k) {
+    edot = ci.edot;
+    iedot = ci.iedot;
+  } else {
+    strain_rate_and_inverse(ci.e11, ci.e22, ci.e12, edot, iedot);
+  }
   const CreepCoef k = ci.have_k ? ci.k : creep_coef(T, ci.grain, ci.p);
-  if (!(edot > 0.0)) return 0.5 / k.C;
 #ifdef MIC_EXACT
-  const double iedot = 0.0;  // unused: the parity build divides as the reference does
+  if (!(edot > 0.0)) return 0.5 / k.C;
 #else
-  const double iedot = 1.0 / edot;  // once per marker: the solve and the viscosity share it
+  if (!gt_zero(edot)) return 0.5 / k.C;
 #endif
   const double s = (cfg.mode == 0) ? creep_stress_exact(k, edot, iedot, cfg.tol, cfg.maxit, &ci.iters, &ci.res)
                                    : creep_stress_from_guess(k, edot, iedot, ci.lx_guess, cfg.tol, cfg.maxit,
