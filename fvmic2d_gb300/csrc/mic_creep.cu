@@ -8,6 +8,7 @@
 // tensor memory; mic_creep_tc.cuh); the guess is then polished by FP64 Newton steps and any
 // marker still above the residual tolerance finishes with the exact solve in the same thread.
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(kTB) k_train_fwdbwd(const float *__restrict__ 
   float *fs = dz1s + kTB * kH;        // [128][4]
   float *dys = fs + kTB * 4;          // [128]
   const int t = threadIdx.x;
-  for (int q = t; q < kH * kH; q += kTB) w2s[q] = p[kOffW2 + q];
+  for (int q = t; q < kH * kH; q += kTB) w2s[q] = bf16_round(p[kOffW2 + q]);
   const int64_t b = (int64_t)blockIdx.x * kTB + t;
   const bool valid = b < nb;
   const int s = valid ? index[b] : 0;
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(128) k_creep_surrogate_batch_fp32(const double
                                                                      double *res_out, int *fb_out,
                                                                      CreepCounters *cc) {
   __shared__ float w2s[kH * kH];
-  for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = cfg.mlp[kOffW2 + q];
+  for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = bf16_round(cfg.mlp[kOffW2 + q]);
   __syncthreads();
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int it = 0, fb = 0, active = 0;
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(128) k_creep_surrogate_batch_fp32(const double
 __global__ void __launch_bounds__(128) k_mlp_infer_fp32(const float *__restrict__ feat, int64_t n,
                                                          const float *__restrict__ p, float *y_out) {
   __shared__ float w2s[kH * kH];
-  for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = p[kOffW2 + q];
+  for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = bf16_round(p[kOffW2 + q]);
   __syncthreads();
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
@@ -289,6 +290,18 @@ int ensure_mlp(mic_ctx *ctx) {
 }
 
 size_t fwdbwd_smem() { return sizeof(float) * (kH * kH + 4 * kTB * kH + kTB * 4 + kTB); }
+
+// W2 of a host copy of the parameters rounded to BF16 (round to nearest even, as
+// __float2bfloat16_rn; the weights are finite)
+void round_w2_bf16(float *p) {
+  for (int q = kOffW2; q < kOffB2; ++q) {
+    uint32_t u;
+    memcpy(&u, &p[q], sizeof(u));
+    if ((u & 0x7F800000u) == 0x7F800000u) continue;
+    u = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
+    memcpy(&p[q], &u, sizeof(u));
+  }
+}
 
 // content key of a network's parameters (FNV-1a over their bytes, never 0): contexts whose keys
 // agree hold the same network, so a batch of their marker passes may read any one of the copies
@@ -369,9 +382,11 @@ extern "C" int mic_creep_set_mlp(mic_ctx *ctx, const float *params, int n) {
   cudaSetDevice(ctx->device);
   int e = ensure_mlp(ctx);
   if (e) return e;
-  MIC_CUDA_TRY(cudaMemcpyAsync(ctx->mlp, params, sizeof(float) * kNParams, cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<float> h(params, params + kNParams);
+  round_w2_bf16(h.data());
+  MIC_CUDA_TRY(cudaMemcpyAsync(ctx->mlp, h.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice, ctx->stream));
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  ctx->mlp_key = net_key(params);
+  ctx->mlp_key = net_key(h.data());
   ctx->gen++;  // captured steps may read this network through another context's copy
   return MIC_OK;
 }
@@ -570,8 +585,11 @@ extern "C" int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int st
   }
   MIC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   {
+    // the trained FP32 master of W2 rounded to the BF16 values the forward passes used
     std::vector<float> h(kNParams);
     MIC_CUDA_TRY(cudaMemcpy(h.data(), ctx->mlp, sizeof(float) * kNParams, cudaMemcpyDeviceToHost));
+    round_w2_bf16(h.data());
+    MIC_CUDA_TRY(cudaMemcpy(ctx->mlp, h.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice));
     ctx->mlp_key = net_key(h.data());
   }
   ctx->creep.mlp = ctx->mlp;

@@ -25,6 +25,7 @@
 //   inside the loop.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "mic_internal.cuh"
@@ -379,6 +380,12 @@ constexpr int kOffNorm = kOffB3 + 1;     // out_mu, out_sigma
 constexpr int kNParams = kOffNorm + 2;   // 4547
 constexpr int kNTrain = kOffNorm;        // trained parameters (normalisation excluded)
 constexpr float kFeatClamp = 12.0f;
+
+// The hidden layer's weights W2 are BF16 values: every reader rounds them to BF16 (round to
+// nearest even) as it stages them, the tensor cores take them as one BF16 operand, and training
+// is quantization-aware (its forward and backward passes use the rounded weights, the update
+// goes to the FP32 master copy); the library rounds W2 when a network is set or trained.
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
 // features of (coefficients, edot > 0); returns the reference m (ln x units)
 __device__ __forceinline__ float creep_features(const CreepCoef &k, double edot, float f[4]) {

@@ -3,15 +3,15 @@
 //
 // Persistent blocks of 128 threads walk the batch in tiles of 128 samples; each block stages
 // the network once, holds 64 TMEM columns for its lifetime and frees them on exit.  At most
-// four blocks fit on an SM (about 51 KB of shared memory each), so the 512 TMEM columns of an
-// SM are never over-subscribed and an allocation never waits on another block.
+// tc::kBlocksPerSM = 5 blocks fit on an SM (about 44 KB of shared memory each), so the 512 TMEM
+// columns of an SM are never over-subscribed and an allocation never waits on another block.
 #include "mic_creep_tc.cuh"
 
 using namespace mic;
 
 namespace {
 
-__global__ void __launch_bounds__(tc::kTile) k_creep_surrogate_batch_tc(const double *__restrict__ edot,
+__global__ void __launch_bounds__(tc::kTile, tc::kBlocksPerSM) k_creep_surrogate_batch_tc(const double *__restrict__ edot,
                                                                          const double *__restrict__ T,
                                                                          const double *__restrict__ d,
                                                                          const double *__restrict__ P, int64_t n,
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(tc::kTile) k_creep_surrogate_batch_tc(const do
 }
 
 // network outputs for given features (n x 4, row-major) on the tensor-core path
-__global__ void __launch_bounds__(tc::kTile) k_mlp_infer_tc(const float *__restrict__ feat, int64_t n,
+__global__ void __launch_bounds__(tc::kTile, tc::kBlocksPerSM) k_mlp_infer_tc(const float *__restrict__ feat, int64_t n,
                                                              const float *__restrict__ p, float *y_out,
                                                              CreepCounters *cc) {
   extern __shared__ unsigned char dyn[];
@@ -83,7 +83,7 @@ int mic_creep_tc_blocks(mic_ctx *ctx, int64_t n) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   const int64_t tiles = (n + tc::kTile - 1) / tc::kTile;
-  const int64_t cap = 4 * (int64_t)(sms > 0 ? sms : 1);
+  const int64_t cap = tc::kBlocksPerSM * (int64_t)(sms > 0 ? sms : 1);
   return (int)(tiles < cap ? (tiles > 0 ? tiles : 1) : cap);
 }
 

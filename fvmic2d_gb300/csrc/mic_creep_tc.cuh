@@ -3,10 +3,13 @@
 //
 // Layer 1 (4 -> 64) and the SiLUs run on the CUDA cores in FP32.  The hidden layer
 // z2 = h1 W2^T (M = 128 markers, N = 64, K = 64) runs as tcgen05.mma kind::f16 with BF16
-// operands and an FP32 accumulator in tensor memory, in three products that recover FP32-level
-// accuracy from BF16 pieces: h1_hi W2_hi + h1_hi W2_lo + h1_lo W2_hi, where x_hi = bf16(x) and
-// x_lo = bf16(x - x_hi).  Thread t of the block owns marker row t: it writes that row of the A
-// operand, and reads row t of the accumulator back (TMEM lane t) with tcgen05.ld.
+// operands and an FP32 accumulator in tensor memory.  W2 is BF16 by construction (bf16_round);
+// the FP32 activations enter as two BF16 pieces, h1_hi W2 + h1_lo W2 with h1_hi = bf16(h1) and
+// h1_lo = bf16(h1 - h1_hi), so the layer is FP32-accurate in h1.  Thread t of the block owns
+// marker row t: it writes that row of the A operand, and reads row t of the accumulator back
+// (TMEM lane t) with tcgen05.ld.  Shared memory per block (42 KB) and at most 102 registers a
+// thread let kBlocksPerSM = 5 blocks share an SM; their TMEM (5 x 64 of 512 columns) never
+// makes an allocation wait.
 //
 // Shared-memory operand layout (no swizzle, K-major core matrices of 8 rows x 16 bytes):
 // element (row, k) of a 64-wide operand sits at (row/8)*1024 + (k/8)*128 + (row%8)*16 + (k%8)*2,
@@ -28,20 +31,25 @@ namespace tc {
 
 constexpr int kTile = 128;              // markers per block tile = MMA M = TMEM lanes
 constexpr int kTmemCols = 64;           // FP32 accumulator columns (N)
+constexpr int kBlocksPerSM = 5;         // resident blocks per SM (launch bounds, persistent grids)
 constexpr uint32_t kOpA = 128 * 64 * 2;  // bytes of one A operand (hi or lo)
 constexpr uint32_t kOpB = 64 * 64 * 2;   // bytes of one B operand
 // small parameters in shared memory, neuron-major so that each neuron's are two 16-byte loads:
 // float4 {W1[k][0..3]}, float4 {b1[k], b2[k], w3[k], 0} for k < 64, then b3
 constexpr int kNSmall = 8 * kH + 4;
 
-struct Smem {  // offsets from a 1024-byte aligned base
-  static constexpr uint32_t a_hi = 0, a_lo = kOpA, b_hi = 2 * kOpA, b_lo = 2 * kOpA + kOpB;
-  static constexpr uint32_t small = 2 * kOpA + 2 * kOpB;             // kNSmall floats
+struct Smem {  // offsets from a 128-byte aligned base (the no-swizzle operands need 16 bytes)
+  static constexpr uint32_t a_hi = 0, a_lo = kOpA, b = 2 * kOpA;
+  static constexpr uint32_t small = 2 * kOpA + kOpB;                 // kNSmall floats
   static constexpr uint32_t bar = small + ((kNSmall * 4 + 15) / 16) * 16;  // mbarrier (8 B)
   static constexpr uint32_t taddr = bar + 8;                          // TMEM address (4 B)
   static constexpr uint32_t bytes = taddr + 8;
 };
-constexpr size_t kDynSmem = Smem::bytes + 1024;  // + alignment slack
+constexpr uint32_t kAlign = 128;
+constexpr size_t kDynSmem = Smem::bytes + kAlign;  // + alignment slack
+// kBlocksPerSM blocks' dynamic and static shared memory (the job record, 1.4 KB) and the 1 KB the
+// hardware reserves per block, within the SM's 228 KB
+static_assert(kBlocksPerSM * (kDynSmem + 1536 + 1024) <= 228 * 1024, "tensor-core blocks do not fit an SM");
 
 // instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1),
 // both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
@@ -152,20 +160,14 @@ struct Block {
 // into the block's shared memory (no fence, no barrier).
 __device__ __forceinline__ void stage_params(Block &B, const float *__restrict__ p) {
   const int t = threadIdx.x;
-  // W2 rows n (outputs) x k (inputs), K-major core matrices; 64 x 8 groups of 8 elements
+  // W2 rows n (outputs) x k (inputs) as BF16, K-major core matrices; 64 x 8 groups of 8 elements
   for (int g = t; g < kH * 8; g += kTile) {
     const int n = g >> 3, kg = g & 7;
-    uint32_t hi[4], lo[4];
+    uint32_t w[4];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const float w0 = p[kOffW2 + n * kH + kg * 8 + 2 * e], w1 = p[kOffW2 + n * kH + kg * 8 + 2 * e + 1];
-      const float h0 = __bfloat162float(__float2bfloat16_rn(w0)), h1 = __bfloat162float(__float2bfloat16_rn(w1));
-      hi[e] = bf16_pair(h0, h1);
-      lo[e] = bf16_pair(w0 - h0, w1 - h1);
-    }
-    const uint32_t off = core_offset(n, kg * 8);
-    *reinterpret_cast<uint4 *>(B.base + Smem::b_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-    *reinterpret_cast<uint4 *>(B.base + Smem::b_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    for (int e = 0; e < 4; ++e)
+      w[e] = bf16_pair(p[kOffW2 + n * kH + kg * 8 + 2 * e], p[kOffW2 + n * kH + kg * 8 + 2 * e + 1]);
+    *reinterpret_cast<uint4 *>(B.base + Smem::b + core_offset(n, kg * 8)) = make_uint4(w[0], w[1], w[2], w[3]);
   }
   float4 *sp4 = reinterpret_cast<float4 *>(B.base + Smem::small);
   for (int k = t; k < kH; k += kTile) {
@@ -175,11 +177,11 @@ __device__ __forceinline__ void stage_params(Block &B, const float *__restrict__
   if (t == 0) sp4[2 * kH] = make_float4(p[kOffB3], 0.0f, 0.0f, 0.0f);
 }
 
-// All kTile threads: carve shared memory, stage W2 (hi/lo BF16) and the small parameters,
-// allocate TMEM (warp 0) and initialise the barrier (thread 0).
+// All kTile threads: carve shared memory, stage W2 (BF16) and the small parameters, allocate
+// TMEM (warp 0) and initialise the barrier (thread 0).
 __device__ __forceinline__ void setup(Block &B, unsigned char *dyn, const float *__restrict__ p) {
   const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(dyn);
-  const uint32_t pad = (1024u - (s0 & 1023u)) & 1023u;
+  const uint32_t pad = (kAlign - (s0 & (kAlign - 1))) & (kAlign - 1);
   B.base = dyn + pad;
   B.sbase = s0 + pad;
   B.phase = 0;
@@ -247,14 +249,12 @@ __device__ __forceinline__ float guess(Block &B, const float f[4], int wait_limi
   fence_after_sync();
   if (!B.ok) return __int_as_float(0x7fc00000);
   if (t == 0) {
-    const uint32_t ahi = B.sbase + Smem::a_hi, alo = B.sbase + Smem::a_lo;
-    const uint32_t bhi = B.sbase + Smem::b_hi, blo = B.sbase + Smem::b_lo;
+    const uint32_t ahi = B.sbase + Smem::a_hi, alo = B.sbase + Smem::a_lo, bw = B.sbase + Smem::b;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const uint32_t o = 256u * j;
-      mma_bf16(B.tmem, smem_desc(ahi + o), smem_desc(bhi + o), j > 0 ? 1u : 0u);
-      mma_bf16(B.tmem, smem_desc(ahi + o), smem_desc(blo + o), 1u);
-      mma_bf16(B.tmem, smem_desc(alo + o), smem_desc(bhi + o), 1u);
+      mma_bf16(B.tmem, smem_desc(ahi + o), smem_desc(bw + o), j > 0 ? 1u : 0u);
+      mma_bf16(B.tmem, smem_desc(alo + o), smem_desc(bw + o), 1u);
     }
     mma_commit(B.sbase + Smem::bar);
   }

@@ -1618,7 +1618,7 @@ __global__ void __launch_bounds__(512) k_yield_fp32_batched(const YieldJob *__re
     if (J.cfg.mlp != staged) {
       staged = J.cfg.mlp;
       __syncthreads();
-      for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = staged[kOffW2 + q];
+      for (int q = threadIdx.x; q < kH * kH; q += blockDim.x) w2s[q] = bf16_round(staged[kOffW2 + q]);
       __syncthreads();
     }
     const int64_t base = (int64_t)(t - (jobs ? __ldg(ts + j) : 0)) * tile_markers;
@@ -1634,7 +1634,7 @@ __global__ void __launch_bounds__(512) k_yield_fp32_batched(const YieldJob *__re
 // and again when a tile's member reads another network buffer.  A block that gives up on the
 // tensor path does so for the rest of its tiles (their markers take the exact solve); the drain
 // timeout, if any, is counted on the member whose round gave up.
-__global__ void __launch_bounds__(tc::kTile) k_yield_tc_batched(const YieldJob *__restrict__ jobs,
+__global__ void __launch_bounds__(tc::kTile, tc::kBlocksPerSM) k_yield_tc_batched(const YieldJob *__restrict__ jobs,
                                                                 const int *__restrict__ ts, int njobs, int ntiles,
                                                                 int tile_markers, int walk, unsigned int *ticket,
                                                                 const __grid_constant__ YieldJob one) {
@@ -1679,8 +1679,8 @@ constexpr size_t kTableAlign = 256;
 
 int batch_fail(cudaError_t e) { return mic_fail_cuda(nullptr, e); }
 
-// the tensor-core yield kernel's shared memory (51 KB a block): the largest carveout, so that four
-// blocks fit an SM -- the occupancy calculator otherwise assumes the default split and allows one
+// the tensor-core yield kernel's shared memory (44 KB a block): the largest carveout, so that
+// tc::kBlocksPerSM blocks fit an SM -- the occupancy calculator otherwise assumes the default split
 cudaError_t tc_kernel_attributes() {
   cudaError_t e =
       cudaFuncSetAttribute(k_yield_tc_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kDynSmem);

@@ -49,7 +49,8 @@ def test_training_gradient_matches_fp64_oracle(ctx):
     X = rng.uniform(-1, 1, (512, 4)).astype(np.float32)
     t = rng.normal(5.0, 1.5, 512).astype(np.float32)
     g, loss = G.creep_grad(p, X, t)
-    loss_o, g_o = M.loss_and_grad(p.astype(np.float64), X.astype(np.float64), t.astype(np.float64))
+    # quantization-aware: the library's forward and backward use W2 rounded to BF16
+    loss_o, g_o = M.loss_and_grad(p.astype(np.float64), X.astype(np.float64), t.astype(np.float64), w2_bf16=True)
     assert abs(loss - loss_o) <= 1e-4 * loss_o
     assert np.linalg.norm(g - g_o) <= 1e-4 * np.linalg.norm(g_o)
     # every parameter block individually
@@ -72,14 +73,15 @@ def _random_params(seed):
 
 @pytest.mark.parametrize("n", [1, 127, 1000, 128 * 4 * 152 * 2 + 7])
 def test_tensor_core_network_matches_fp64_forward(ctx, n):
-    """The tcgen05 path (split-BF16 hidden layer, FP32 accumulation in tensor memory) against the
-    FP64 NumPy forward pass and the FP32 CUDA-core path; ragged tile counts and more tiles than
+    """The tcgen05 path (BF16 W2, activations as two BF16 pieces, FP32 accumulation in tensor
+    memory) against the FP64 NumPy forward pass of the same network (W2 rounded to BF16, as the
+    library holds it) and the FP32 CUDA-core path; ragged tile counts and more tiles than
     persistent blocks."""
     G, _ = ctx
     p = _random_params(n)
     G.creep_set_params(p)
     X = np.random.default_rng(n + 1).uniform(-1, 1, (n, 4)).astype(np.float32)
-    y64, (_, h1, z2, h2) = M.forward(p.astype(np.float64), X.astype(np.float64))
+    y64, (_, h1, z2, h2) = M.forward(p.astype(np.float64), X.astype(np.float64), w2_bf16=True)
     # error scale: magnitude of the terms summed in the hidden and output layers
     scale = 1.0 + np.abs(h2) @ np.abs(p[M.OFF_W3:M.OFF_B3].astype(np.float64))
     y1 = G.creep_infer(X, mode=1)
