@@ -42,7 +42,11 @@ WORKLOAD_DESC = {
                       "tensor cores with FP32 accumulation, FP64 polish to |rate/edot - 1| <= 1e-7, exact fallback; FP64"),
     "vep_slab_box": ("vep_slab_box: 1025x257 staggered grid (2x refined top 20%), 16 markers/cell, "
                      "4,194,304 markers, two materials, Mohr-Coulomb yield, FP64"),
+    "convection_box": ("convection_box: unit-square thermal convection, viscosity exp(-ln(1000) T), free slip, "
+                       "T0 = 1 - y + 0.01 cos(pi x) sin(pi y), 64x64 cells (65x65 nodes), 16 jittered markers/cell, "
+                       "65,536 markers, 10 steps, FP64"),
 }
+CONVECTION_STEPS = 10  # the convection configuration's step count
 # the bounded sample of each workload that the host-core baseline steps: the same generator and
 # per-marker distributions on a smaller grid
 CPU_SAMPLE = {"ice_creep_box": "ice_creep_box_sample", "vep_slab_box": "vep_slab_box_sample",
@@ -119,6 +123,7 @@ def parse():
     ap.add_argument("--workload", default="ice_creep_box")
     ap.add_argument("--no-legs", action="store_true", help="main workload only (no VEP, ensemble, systems legs)")
     ap.add_argument("--no-vep", action="store_true", help="skip the visco-elasto-plastic box leg")
+    ap.add_argument("--no-convection", action="store_true", help="skip the 64x64 convection box leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble legs")
     ap.add_argument("--no-systems", action="store_true", help="skip the linear-systems / whole-time-step leg")
     ap.add_argument("--only-systems", action="store_true",
@@ -297,10 +302,13 @@ def sum_over_ranks(pg, v):
 
 
 def base_config(wl, name, world):
+    state = len(wl.markers) * 208
+    l2 = ("inputs larger than L2 (marker state %.2f GB per replica)" % (state / 1e9) if state > 129e6 else
+          "inputs smaller than L2 (marker state %.1f MB): L2-resident between steps, no flush" % (state / 1e6))
     return {"workload": WORKLOAD_DESC.get(name, name),
             "markers_per_replica": int(len(wl.markers)), "nodes": [wl.grid.NX, wl.grid.NY],
             "parallelism": "replicas x%d (independent problems, no collective)" % world,
-            "l2": "inputs larger than L2 (marker state %.2f GB per replica)" % (len(wl.markers) * 208 / 1e9),
+            "l2": l2,
             "timed": "bin+sort, rho, project x2, max T, yield (law-7 stress solve), limit, strain/pressure, residual, "
                      "subgrid stress, stress update, subgrid T, RK4 advection, max |sxx|; host solves excluded"}
 
@@ -605,7 +613,7 @@ def run_ours(args):
             torch.cuda.set_device(local)
             print(json.dumps({"systems": systems_leg(args, local)}), flush=True)
         return
-    cpu = cpu_vep = None
+    cpu = cpu_vep = cpu_conv = None
     legs = not args.no_legs
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # bounded samples: one step per replica on all host cores, and on one core, spawned before
@@ -617,8 +625,16 @@ def run_ours(args):
                "sample": cpu_sample_text(args.workload, cores, 1, rate1, ms1), "value_1core": rate1}
         if legs and not args.no_vep and args.workload != "vep_slab_box":
             rate, ms = cpu_throughput(cpu_sample("vep_slab_box"), cores, 1, 0)
+            rate1, ms1 = cpu_throughput(cpu_sample("vep_slab_box"), 1, 1, 0)
             cpu_vep = {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
-                       "sample": cpu_sample_text("vep_slab_box", cores, 1)}
+                       "sample": cpu_sample_text("vep_slab_box", cores, 1, rate1, ms1), "value_1core": rate1}
+        if legs and not args.no_convection:
+            # the whole configuration (65,536 markers, 10 steps) on the host cores
+            rate, ms = cpu_throughput("convection_box", cores, CONVECTION_STEPS, 0)
+            rate1, ms1 = cpu_throughput("convection_box", 1, CONVECTION_STEPS, 0)
+            cpu_conv = {"value": rate, "unit": "markers/s", "cores": cores, "kind": "port",
+                        "sample": cpu_sample_text("convection_box", cores, CONVECTION_STEPS, rate1, ms1),
+                        "value_1core": rate1}
     import torch
 
     torch.cuda.set_device(local)
@@ -657,6 +673,12 @@ def run_ours(args):
         vep, vhead = measure_workload(args, "vep_slab_box", local, None, 1, cpu=cpu_vep, with_density=False)
         vep["plain"].pop("launch_tuning", None)
         line["vep_slab_box"] = vep
+    if legs and not args.no_convection:
+        cargs = argparse.Namespace(**vars(args))
+        cargs.steps, cargs.warmup = CONVECTION_STEPS, max(3, min(args.warmup, CONVECTION_STEPS))
+        conv, _ = measure_workload(cargs, "convection_box", local, None, 1, cpu=cpu_conv, with_density=False)
+        conv["plain"].pop("launch_tuning", None)
+        line["convection_box"] = conv
     if legs and not args.no_ensemble:
         line["ensemble"] = ensemble_leg(args, local)
         line["ice_ensemble"] = ice_ensemble_leg(args, local)
