@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(MAXT) k_band_panel(double *band, int64_t n, in
     long long bv = -1;
     int bi = INT_MAX;
     if (own && tid >= jj && tid <= rmax) {
-      const long long a = __double_as_longlong(row[jj]) & 0x7fffffffffffffffLL;
+      const long long a = dbits(row[jj]) & 0x7fffffffffffffffLL;
       if (a <= 0x7ff0000000000000LL) {
         bv = a;
         bi = tid;

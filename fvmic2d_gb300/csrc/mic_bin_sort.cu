@@ -48,11 +48,11 @@ __global__ void k_find_cells(Params P, const double *__restrict__ X, const doubl
   __syncthreads();
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m < n) {
-    const long long bx = __double_as_longlong(X[m]);
-    const long long by = __double_as_longlong(Y[m]);
+    const long long bx = dbits(X[m]);
+    const long long by = dbits(Y[m]);
     const long long ux = (bx == (long long)0x8000000000000000ULL) ? 0LL : bx;
     const long long uy = (by == (long long)0x8000000000000000ULL) ? 0LL : by;
-    const long long blx = __double_as_longlong(P.LX), bly = __double_as_longlong(P.LY);
+    const long long blx = dbits(P.LX), bly = dbits(P.LY);
     // X >= 0 && Y >= 0 && X <= LX && Y <= LY; NaN fails every test
     const bool in = ux >= 0 && uy >= 0 && ux <= blx && uy <= bly;
     int cx = -1, cy = -1, k = 4 * P.NCX * (P.NY - 1);
@@ -535,7 +535,7 @@ __global__ void k_find_cells_grid(const double *__restrict__ X, const double *__
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m < n) {
     const long long ux = nonneg_bits(X[m]), uy = nonneg_bits(Y[m]);
-    const bool in = ux >= 0 && uy >= 0 && ux <= __double_as_longlong(LX) && uy <= __double_as_longlong(LY);
+    const bool in = ux >= 0 && uy >= 0 && ux <= dbits(LX) && uy <= dbits(LY);
     int cx = -1, cy = -1, k = 4 * (NX - 1) * (NY - 1);
     if (in) {
       int lo = 0, hi = NX - 1;

@@ -185,7 +185,7 @@ __device__ __forceinline__ double creep_stress_exact_u(const CreepCoef &k, doubl
 // gives about -709 (a huge negative log) instead of -inf; the callers take minima, where that
 // acts the same.
 __device__ __forceinline__ float ln_f(double v) {
-  const long long b = __double_as_longlong(v);
+  const long long b = dbits(v);
   const int e = (int)((b >> 52) & 0x7FF) - 1023;
   const float mant = __int_as_float(0x3F800000 | (int)((b >> 29) & 0x7FFFFF));
   return fmaf((float)e, 0.693147181f, __logf(mant));
@@ -295,20 +295,20 @@ __device__ __forceinline__ double creep_advance(const CreepEval &e, double p, bo
 __device__ __forceinline__ int creep_iterate(const CreepTerms &q, double &p, double plo, double phi, double tol,
                                              int maxit, bool &conv, double &res, double &p5) {
   const bool fine = tol < 1e-9;
-  long long blo = __double_as_longlong(plo), bhi = __double_as_longlong(phi);
+  long long blo = dbits(plo), bhi = dbits(phi);
   CreepEval e;
   int it = 0;
   for (;; ++it) {
     creep_eval(q, p, e);
     conv = creep_converged(e, tol);
     if (conv || it >= maxit) break;
-    const long long bp = __double_as_longlong(p);
-    if (__double_as_longlong(e.N) > 0)
+    const long long bp = dbits(p);
+    if (dbits(e.N) > 0)
       bhi = min(bhi, bp);
     else
       blo = max(blo, bp);
     double pn = creep_advance(e, p, fine);
-    const long long bn = __double_as_longlong(pn);
+    const long long bn = dbits(pn);
     if (!(bn > blo && bn < bhi)) {
       const double lo = __longlong_as_double(blo), hi = __longlong_as_double(bhi);
       pn = (blo > 0) ? sqrt(lo * hi) : hi * 0.67032004603563930;  // e^-0.4
@@ -348,7 +348,7 @@ __device__ __forceinline__ double creep_stress_exact(const CreepCoef &k, double 
   *res_out = 0.0;
   if (!gt_zero(edot)) return 0.0;
   // linear diffusion branch, s = edot / C < 1 Pa (viscosity.c:130-133); edot, C > 0 compared by bits
-  if (__double_as_longlong(edot) < __double_as_longlong(k.C)) return edot / k.C;
+  if (dbits(edot) < dbits(k.C)) return edot / k.C;
   return creep_solve_terms(creep_terms(k, iedot), tol, maxit, iters, res_out);
 #endif
 }
@@ -462,7 +462,7 @@ __device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, do
   return s;
 #else
   if (!gt_zero(edot)) return 0.0;
-  if (__double_as_longlong(edot) < __double_as_longlong(k.C)) return edot / k.C;
+  if (dbits(edot) < dbits(k.C)) return edot / k.C;
   const CreepTerms q = creep_terms(k, iedot);
   if (isfinite(lx0)) {
     double p = f64_of(__expf(0.2f * lx0)), res, p5;

@@ -139,7 +139,7 @@ __global__ void k_limit_dt(Params P, GridFields g, double factor, unsigned long 
   const int ix = (int)(k % NX), jy = (int)(k / NX);
   long long best = LLONG_MAX;
   auto take = [&](double c) {
-    if (!nan_bits(__double_as_longlong(c))) best = min(best, ordered_bits(c));
+    if (!nan_bits(dbits(c))) best = min(best, ordered_bits(c));
   };
   double dx, dy;
   if (ix == 0) dx = P.x[1] - P.x[0];
@@ -159,7 +159,7 @@ __global__ void k_limit_dt(Params P, GridFields g, double factor, unsigned long 
   const double rd = g.rhodot[k];
   if (rd != 0.0) take(fabs(D(M(0.01, g.rho[k]), rd)));
   if (best != LLONG_MAX) atomicMin(reinterpret_cast<long long *>(mins), best);
-  if (!nan_bits(__double_as_longlong(rd))) {
+  if (!nan_bits(dbits(rd))) {
     atomicMax(maxr, (unsigned long long)nonneg_bits(fabs(rd)));
     *nonnan = 1;
   }

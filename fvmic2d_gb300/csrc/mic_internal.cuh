@@ -342,14 +342,24 @@ __device__ __forceinline__ void store_w4(double *w, int64_t m, const W4 &v) {
   reinterpret_cast<double2 *>(w + 4 * m)[1] = make_double2(v.w01, v.w11);
 }
 
+// The bit pattern of v through an opaque 64-bit move.  The integer tests and conversions built on
+// it stay integer instructions: on a double computed in registers the compiler otherwise may turn
+// a test of its bits back into FP64 instructions (measured: an FP64 add per test), which take
+// slots of the FP64 pipe these tests exist to spare.
+__device__ __forceinline__ long long dbits(double v) {
+  long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(v));
+  return b;
+}
+
 __device__ __forceinline__ long long nonneg_bits(double v) {
-  long long b = __double_as_longlong(v);
+  long long b = dbits(v);
   return (b == (long long)0x8000000000000000ULL) ? 0LL : b;
 }
 
 // Order-preserving map of any non-NaN double to a signed integer key.
 __device__ __forceinline__ long long ordered_bits(double v) {
-  long long b = __double_as_longlong(v);
+  long long b = dbits(v);
   return b >= 0 ? b : (long long)(0x8000000000000000ULL) - b;
 }
 
@@ -364,24 +374,24 @@ __device__ __forceinline__ bool nan_bits(long long b) {
 
 // a < c for a positive finite constant c and any a; false for NaN (as the FP64 compare)
 __device__ __forceinline__ bool lt_pos(double a, double c) {
-  const long long b = __double_as_longlong(a);
-  return b < __double_as_longlong(c) && !nan_bits(b);
+  const long long b = dbits(a);
+  return b < dbits(c) && !nan_bits(b);
 }
 // a > 0, false for zero of either sign and for NaN (as the FP64 compare)
 __device__ __forceinline__ bool gt_zero(double a) {
-  const long long b = __double_as_longlong(a);
+  const long long b = dbits(a);
   return b > 0 && b <= 0x7FF0000000000000LL;
 }
 // |a| <= c for c >= 0 (not NaN); false for a NaN a
 __device__ __forceinline__ bool abs_le(double a, double c) {
-  return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFLL) <= __double_as_longlong(c);
+  return (dbits(a) & 0x7FFFFFFFFFFFFFFFLL) <= dbits(c);
 }
 
 // FP32 copy of v scaled by 2^-k, from its bit pattern: the exponent re-biased and the mantissa
 // truncated to 23 bits (relative error below 2^-23, against 2^-24 for a rounding conversion);
 // signed zero below FP32's normal range, infinity above it, NaN for NaN.
 __device__ __forceinline__ float f32_trunc(double v, int k = 0) {
-  const long long b = __double_as_longlong(v);
+  const long long b = dbits(v);
   const unsigned hi = (unsigned)((unsigned long long)b >> 32);
   const unsigned s = hi & 0x80000000u;
   const int eb = (int)((hi >> 20) & 0x7FFu);
@@ -393,7 +403,7 @@ __device__ __forceinline__ float f32_trunc(double v, int k = 0) {
 }
 // binary exponent of a positive normal double (floor(log2 v))
 __device__ __forceinline__ int exp2_of(double v) {
-  return (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF) - 1023;
+  return (int)(((unsigned long long)dbits(v) >> 52) & 0x7FF) - 1023;
 }
 // exact FP64 value of f from its bit pattern: normal floats, infinities and NaN; zero and the FP32
 // subnormals (below 1.2e-38) give signed zero

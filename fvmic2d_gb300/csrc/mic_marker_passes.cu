@@ -13,6 +13,7 @@
 
 #include "mic_creep.cuh"
 #include "mic_creep_tc.cuh"
+#include "mic_df.cuh"
 #include "mic_internal.cuh"
 #include "mic_rheology.cuh"
 
@@ -68,7 +69,7 @@ __device__ __forceinline__ double limit_eta(double e, const mic_options &O) {
   if (e < O.etamin) return O.etamin;
 #else
   // the same two compares on order-preserving integer keys (a NaN viscosity stays NaN)
-  if (nan_bits(__double_as_longlong(e))) return e;
+  if (nan_bits(dbits(e))) return e;
   const long long k = ordered_bits(e);
   if (k > ordered_bits(O.etamax)) return O.etamax;
   if (k < ordered_bits(O.etamin)) return O.etamin;
@@ -286,7 +287,7 @@ __device__ __forceinline__ long long update_rho_one(const int *cellX, const int 
     const double t = T[m];
     rho[m] = -rho0[k] * (alpha[k] * t);
     rhodot[m] = 0.0;
-    if (t > 0.0) b = __double_as_longlong(t);
+    if (t > 0.0) b = dbits(t);
   }
   return b;
 }
@@ -390,7 +391,7 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
   // three components (within a few ulp of the reference's quotients)
   const double dtmu = dt * mu, den = eta * dtmu;
   double ie, idm;
-  const unsigned ex = (unsigned)(__double_as_longlong(den) >> 52) & 0x7ffu;  // den >= 0
+  const unsigned ex = (unsigned)(dbits(den) >> 52) & 0x7ffu;  // den >= 0
   if (ex > 64u && ex < 1984u) {  // far from under- and overflow (an integer test)
     const double inv = 0.5 / den;
     ie = dtmu * inv;
@@ -827,10 +828,23 @@ __device__ __forceinline__ Bil4 bil_coef(double f00, double f10, double f01, dou
   b.c3 = (f11 - f01) - b.c1;
   return b;
 }
-__device__ __forceinline__ double bil_eval(const Bil4 *__restrict__ cells, size_t k, double tx, double ty) {
-  const double2 lo = __ldg(reinterpret_cast<const double2 *>(cells + k));
-  const double2 hi = __ldg(reinterpret_cast<const double2 *>(cells + k) + 1);
-  return fma(ty, fma(tx, hi.y, hi.x), fma(tx, lo.y, lo.x));
+// The advection's records hold the four coefficients as double-floats (hi, lo for c0 .. c3; the
+// same 32 bytes): its marker loop evaluates them on the FP32 pipe (mic_df.cuh).
+struct alignas(32) BilDF {
+  float c0h, c0l, c1h, c1l, c2h, c2l, c3h, c3l;
+};
+__device__ __forceinline__ BilDF bil_coef_df(double f00, double f10, double f01, double f11) {
+  const Bil4 b = bil_coef(f00, f10, f01, f11);
+  const df c0 = df_of(b.c0), c1 = df_of(b.c1), c2 = df_of(b.c2), c3 = df_of(b.c3);
+  return {c0.hi, c0.lo, c1.hi, c1.lo, c2.hi, c2.lo, c3.hi, c3.lo};
+}
+// c0 + tx c1 + ty (c2 + tx c3) in double-float arithmetic (two 16-byte loads, no FP64 instruction)
+__device__ __forceinline__ df bil_eval_df(const BilDF *__restrict__ cells, size_t k, const df &tx, const df &ty) {
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(cells + k));
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(cells + k) + 1);
+  const df lower = df_fma(tx, df{a.z, a.w}, df{a.x, a.y});
+  const df upper = df_fma(tx, df{b.z, b.w}, df{b.x, b.y});
+  return df_fma(ty, upper, lower);
 }
 
 // The cells the advection interpolates on (markers.c:1978-2029), with the boundary ghosts it
@@ -839,7 +853,7 @@ __device__ __forceinline__ double bil_eval(const Bil4 *__restrict__ cells, size_
 // the left boundary condition, rows 0 .. NY-2) and basic cells of the vorticity.
 __global__ void k_advect_coef(const double *__restrict__ vx, const double *__restrict__ vy,
                               const double *__restrict__ wz, mic_bcinfo top, mic_bcinfo left, int NX, int NY,
-                              Bil4 *cvx, Bil4 *cvy, Bil4 *cwz) {
+                              BilDF *cvx, BilDF *cvy, BilDF *cwz) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k < (int64_t)NY * (NX - 1)) {
     const int row = (int)(k / (NX - 1)), i = (int)(k % (NX - 1));
@@ -855,7 +869,7 @@ __global__ void k_advect_coef(const double *__restrict__ vx, const double *__res
       vul = vx[r1 - NX + i];
       vur = vx[r1 - NX + i + 1];
     }
-    cvx[k] = bil_coef(vul, vur, vx[r1 + i], vx[r1 + i + 1]);
+    cvx[k] = bil_coef_df(vul, vur, vx[r1 + i], vx[r1 + i + 1]);
   }
   if (k < (int64_t)(NY - 1) * NX) {
     const int j = (int)(k / NX), col = (int)(k % NX);
@@ -871,12 +885,12 @@ __global__ void k_advect_coef(const double *__restrict__ vx, const double *__res
       wul = vy[q0 + col - 1];
       wll = vy[q1 + col - 1];
     }
-    cvy[k] = bil_coef(wul, vy[q0 + col], wll, vy[q1 + col]);
+    cvy[k] = bil_coef_df(wul, vy[q0 + col], wll, vy[q1 + col]);
   }
   if (k < (int64_t)(NY - 1) * (NX - 1)) {
     const int j = (int)(k / (NX - 1)), i = (int)(k % (NX - 1));
     const size_t w0 = (size_t)j * NX + i;
-    cwz[k] = bil_coef(wz[w0], wz[w0 + 1], wz[w0 + NX], wz[w0 + NX + 1]);
+    cwz[k] = bil_coef_df(wz[w0], wz[w0 + 1], wz[w0 + NX], wz[w0 + NX + 1]);
   }
 }
 #endif
@@ -897,6 +911,10 @@ struct AdvectCoef {
 };
 __device__ __forceinline__ double advect_tail(const Params &P, const AdvectCols &c, double dt, int64_t m, double X0,
                                               double Y0, const double *mvx, const double *mvy, const double *mwz);
+#ifndef MIC_EXACT
+__device__ __forceinline__ double advect_tail_df(const Params &P, const AdvectCols &c, double dt, int64_t m, double X0,
+                                                 double Y0, const df *mvx, const df *mvy, const df *mwz);
+#endif
 
 __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCols &c, const Geo &g,
                                                 const double *__restrict__ vx, const double *__restrict__ vy,
@@ -904,23 +922,29 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
                                                 const mic_bcinfo &top, const mic_bcinfo &left, double dt, int64_t m,
                                                 int ci, int cj, int wz_known) {
 #ifndef MIC_EXACT
-  const Bil4 *__restrict__ cvx = static_cast<const Bil4 *>(cv.cvx);
-  const Bil4 *__restrict__ cvy = static_cast<const Bil4 *>(cv.cvy);
-  const Bil4 *__restrict__ cwz = static_cast<const Bil4 *>(cv.cwz);
+  const BilDF *__restrict__ cvx = static_cast<const BilDF *>(cv.cvx);
+  const BilDF *__restrict__ cvy = static_cast<const BilDF *>(cv.cvy);
+  const BilDF *__restrict__ cwz = static_cast<const BilDF *>(cv.cwz);
 #else
   (void)cv;
 #endif
   const int NX = P.NX, NY = P.NY;
   const double X0 = c.X[m], Y0 = c.Y[m];
   double xcur = X0, ycur = Y0;
+#ifdef MIC_EXACT
   double mvx[4], mvy[4], mwz[4];
+#else
+  // the stage values as double-floats (mic_df.cuh), and the half and full time steps
+  df mvx[4], mvy[4], mwz[4];
+  const df fdt = df_of(dt), hdt = df_scale(fdt, 0.5f);
+#endif
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     // cell walk from the stored cell (markers.c:1928-1944) and the staggered-cell tests, all on
     // order-preserving integer images of the coordinates: same decisions as the FP64 compares
     // (a NaN coordinate compares false everywhere, as in the reference), none on the FP64 pipe
     const long long bx = ordered_bits(xcur), by = ordered_bits(ycur);
-    const bool okx = !nan_bits(__double_as_longlong(xcur)), oky = !nan_bits(__double_as_longlong(ycur));
+    const bool okx = !nan_bits(dbits(xcur)), oky = !nan_bits(dbits(ycur));
     int i = ci, j = cj;
     if (okx) {
       if (bx > P.xbits[i + 1]) {
@@ -943,27 +967,11 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     vyX = clampi(vyX, -1, NX - 2);
     vxY = clampi(vxY, -1, NY - 2);
     vyY = clampi(vyY, 0, NY - 2);
-#ifndef MIC_EXACT
-    // vx sits on the basic x lines and vy on the basic y lines: with vxX == i and vyY == j (the
-    // walk keeps i, j inside the clamps) their fractions there are the basic cell's mdx, mdy
-    // fractions here only weight interpolations (every cell decision above is on integer images),
-    // so one multiply by the tabulated reciprocal, within an ulp of the quotient, stands in for it.
-    // The first stage samples at the marker itself, in its stored cell: its fractions are the
-    // binning geometry's (basic cell; the vx cell's y and the vy cell's x fractions are those of
-    // the cell-centre cell, whose stagger tests are the same).
-    const double mdx = (s == 0) ? g.gx0[m] : (xcur - P.x[i]) * P.ix[i];
-    const double mdy = (s == 0) ? g.gy0[m] : (ycur - P.y[j]) * P.iy[j];
-#endif
-    double ay = ycur - P.yc[vxY + 1];
 #ifdef MIC_EXACT
+    double ay = ycur - P.yc[vxY + 1];
     double ax = xcur - P.x[vxX];
     double hx = P.x[vxX + 1] - P.x[vxX];
     double hy = P.yc[vxY + 2] - P.yc[vxY + 1];
-#else
-    const double tx = mdx;
-    const double ty = (s == 0) ? g.gy1[m] : ay * P.iyc[vxY + 1];
-#endif
-#ifdef MIC_EXACT
     const size_t r1 = (size_t)(vxY + 1) * NX;
     double vul, vur;
     if (vxY == -1 && top.type[0] == 0) {
@@ -981,11 +989,7 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     t += vur * (ax / hx) * (1.0 - ay / hy);
     t += vll * (1.0 - ax / hx) * (ay / hy);
     t += vlr * (ax * ay) / hx / hy;
-#else
-    double t = bil_eval(cvx, (size_t)(vxY + 1) * (NX - 1) + vxX, tx, ty);
-#endif
     mvx[s] = t;
-#ifdef MIC_EXACT
     const size_t q0 = (size_t)vyY * NX, q1 = q0 + NX;
     const double wur = vy[q0 + vyX + 1], wlr = vy[q1 + vyX + 1];
     double wul, wll;
@@ -1007,12 +1011,7 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     t += wur * (ax / hx) * (1.0 - ay / hy);
     t += wll * (1.0 - ax / hx) * (ay / hy);
     t += wlr * (ax * ay) / hx / hy;
-#else
-    t = bil_eval(cvy, (size_t)vyY * NX + vyX + 1, (s == 0) ? g.gx1[m] : (xcur - P.xc[vyX + 1]) * P.ixc[vyX + 1],
-                 mdy);
-#endif
     mvy[s] = t;
-#ifdef MIC_EXACT
     const size_t w0 = (size_t)j * NX + i;
     const double mdx = div_sp(xcur - P.x[i], P.hx[i], P.ix[i]);
     const double mdy = div_sp(ycur - P.y[j], P.hy[j], P.iy[j]);
@@ -1020,14 +1019,7 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     t += (mdx) * (1.0 - mdy) * wz[w0 + 1];
     t += (1.0 - mdx) * (mdy)*wz[w0 + NX];
     t += (mdx) * (mdy)*wz[w0 + NX + 1];
-#else
-    if (s == 0)  // at the marker itself: the bilinear form of the stored weights
-      t = wz_known ? c.wxy[m] : interp_w(wz, NX, i, j, load_w4(g.w0, m));
-    else
-      t = bil_eval(cwz, (size_t)j * (NX - 1) + i, mdx, mdy);
-#endif
     mwz[s] = t;
-#ifdef MIC_EXACT
     if (s < 2) {
       xcur = X0 + dt / 2 * mvx[s];
       ycur = Y0 + dt / 2 * mvy[s];
@@ -1036,18 +1028,45 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
       ycur = Y0 + dt * mvy[s];
     }
 #else
-    // the product build's sums of products are written as FMAs (the same operations whichever
-    // kernel inlines this, and the fewest FP64 instructions)
-    if (s < 2) {
-      xcur = fma(0.5 * dt, mvx[s], X0);
-      ycur = fma(0.5 * dt, mvy[s], Y0);
-    } else if (s == 2) {
-      xcur = fma(dt, mvx[s], X0);
-      ycur = fma(dt, mvy[s], Y0);
+    // Fractions in the cells (they only weight interpolations: every cell decision above is on
+    // integer images): the offset from the cell's line in FP64 (exact or within an ulp of the
+    // offset), times the tabulated reciprocal spacing in double-float arithmetic.  vx sits on the
+    // basic x lines and vy on the basic y lines: with vxX == i and vyY == j (the walk keeps i, j
+    // inside the clamps) their fractions there are the basic cell's.  The first stage samples at
+    // the marker itself, in its stored cell: its fractions are the binning geometry's (basic cell;
+    // the vx cell's y and the vy cell's x fractions are those of the cell-centre cell, whose
+    // stagger tests are the same).
+    df fx, fy, fty, ftx;
+    if (s == 0) {
+      fx = df_of(g.gx0[m]);
+      fy = df_of(g.gy0[m]);
+      fty = df_of(g.gy1[m]);
+      ftx = df_of(g.gx1[m]);
+    } else {
+      fx = df_mul(df_of(xcur - P.x[i]), df_of(P.ix[i]));
+      fy = df_mul(df_of(ycur - P.y[j]), df_of(P.iy[j]));
+      fty = df_mul(df_of(ycur - P.yc[vxY + 1]), df_of(P.iyc[vxY + 1]));
+      ftx = df_mul(df_of(xcur - P.xc[vyX + 1]), df_of(P.ixc[vyX + 1]));
+    }
+    mvx[s] = bil_eval_df(cvx, (size_t)(vxY + 1) * (NX - 1) + vxX, fx, fty);
+    mvy[s] = bil_eval_df(cvy, (size_t)vyY * NX + vyX + 1, ftx, fy);
+    if (s == 0)  // at the marker itself: the bilinear form of the stored weights
+      mwz[s] = df_of(wz_known ? c.wxy[m] : interp_w(wz, NX, i, j, load_w4(g.w0, m)));
+    else
+      mwz[s] = bil_eval_df(cwz, (size_t)j * (NX - 1) + i, fx, fy);
+    // the next stage's position: the displacement in double-float, added to the FP64 start
+    if (s < 3) {
+      const df h = (s < 2) ? hdt : fdt;
+      xcur = X0 + df_to_f64(df_mul(h, mvx[s]));
+      ycur = Y0 + df_to_f64(df_mul(h, mvy[s]));
     }
 #endif
   }
+#ifdef MIC_EXACT
   return advect_tail(P, c, dt, m, X0, Y0, mvx, mvy, mwz);
+#else
+  return advect_tail_df(P, c, dt, m, X0, Y0, mvx, mvy, mwz);
+#endif
 }
 
 // The RK4 average of the four stages, the new position (wrapped across the seam of a grid
@@ -1124,6 +1143,71 @@ __device__ __forceinline__ double advect_tail(const Params &P, const AdvectCols 
 #endif
   return nsxx;
 }
+
+#ifndef MIC_EXACT
+// sin^2 t and sin 2t of the rotation angle t of markers.c:2158-2164.  For |t| <= 2^-6 (an
+// integer test) their Taylor series to t^8 (truncation below 1e-18 relative); sincos beyond.
+__device__ __forceinline__ void rotation_terms(double t, double &ss, double &s2) {
+  if (abs_le(t, 0.015625)) {
+    const double t2 = t * t, u = 2.0 * t, u2 = 4.0 * t2;
+    ss = t2 * fma(t2, fma(t2, fma(t2, -1.0 / 315.0, 2.0 / 45.0), -1.0 / 3.0), 1.0);
+    s2 = u * fma(u2, fma(u2, fma(u2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), 1.0);
+  } else {
+    double sn, cs;
+    sincos(t, &sn, &cs);
+    ss = sn * sn;
+    s2 = 2.0 * sn * cs;
+  }
+}
+
+// The product build's tail of the advection on a grid not periodic in x: the RK4 averages of the
+// double-float stage values (each entering FP64 once), the new position, the stress rotation and
+// the accumulated strain (markers.c:2120-2223).  The exact rotation s' = R s R^T is written as
+// its change: with d = s22 - s11, sxx' = sxx + (d sin^2 t - sxy sin 2t), syy' = syy minus the same,
+// sxy' = sxy - (2 sxy sin^2 t + d sin 2t / 2) (cos^2 + sin^2 = 1), the changes formed in
+// double-float arithmetic, so only the additions to the stresses are FP64.  Returns the rotated
+// sxx.
+__device__ __forceinline__ double advect_tail_df(const Params &P, const AdvectCols &c, double dt, int64_t m, double X0,
+                                                 double Y0, const df *mvx, const df *mvy, const df *mwz) {
+  const df k6 = df_of(1.0 / 6.0);
+  const df vxa = df_mul(df_add(df_add(mvx[0], mvx[3]), df_scale(df_add(mvx[1], mvx[2]), 2.0f)), k6);
+  const df vya = df_mul(df_add(df_add(mvy[0], mvy[3]), df_scale(df_add(mvy[1], mvy[2]), 2.0f)), k6);
+  const df wa = df_mul(df_add(df_add(mwz[0], mwz[3]), df_scale(df_add(mwz[1], mwz[2]), 2.0f)), k6);
+  const double VX = df_to_f64(vxa), VY = df_to_f64(vya), w = df_to_f64(wa);
+  c.VX[m] = VX;
+  c.VY[m] = VY;
+  c.wxy[m] = w;
+  c.X[m] = fma(dt, VX, X0);
+  c.Y[m] = fma(dt, VY, Y0);
+  const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+  double nsxx;
+  if (P.jaumann) {
+    // first-order Jaumann terms with wxy1 = wxy dt (markers.c:2147-2156)
+    const double w1 = w * dt;
+    nsxx = fma(2.0 * s12, -w1, s11);
+    c.syy[m] = fma(2.0 * s12, w1, s22);
+    c.sxy[m] = fma(s11 - s22, w1, s12);
+    c.sxx[m] = nsxx;
+  } else {
+    double ss, s2;
+    rotation_terms(-w * dt, ss, s2);
+    const df d = df_of(s22 - s11), a = df_of(s12), dss = df_of(ss), ds2 = df_of(s2);
+    const double c11 = df_to_f64(df_fma(d, dss, df_neg(df_mul(a, ds2))));
+    const double c12 = df_to_f64(df_fma(df_scale(a, 2.0f), dss, df_scale(df_mul(d, ds2), 0.5f)));
+    nsxx = s11 + c11;
+    c.sxx[m] = nsxx;
+    c.syy[m] = s22 - c11;
+    c.sxy[m] = s12 - c12;
+  }
+  // accumulated strain: the invariant's square root as q / sqrt(q) by one reciprocal square root
+  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
+  const double q = fma(e12, e12, 0.5 * fma(e11, e11, e22 * e22));
+  const long long qb = dbits(q);
+  const double rq = (qb == 0 || qb == 0x7FF0000000000000LL) ? q : q * rsqrt(q);
+  c.Eii[m] = fma(dt, rq, c.Eii[m]);
+  return nsxx;
+}
+#endif
 
 // advectMarkersRK on a grid periodic in x (markers.c:1907-1913, 1928-1944, 1961-1966, 2014-2023):
 // the cell walk runs over cells -1 .. NX-1 (line -1 and NX are the seam's images), the vx and vy
@@ -1218,7 +1302,7 @@ __device__ __forceinline__ long long advect_one(const Params &P, const AdvectCol
     if (ci != -1) {
       const double a = fabs(P.xper ? advect_marker_periodic(P, c, vx, vy, wz, top, dt, m, ci, cj)
                                    : advect_marker(P, c, g, vx, vy, wz, cv, top, left, dt, m, ci, cj, wz_known));
-      if (a > 0.0) b = __double_as_longlong(a);
+      if (a > 0.0) b = dbits(a);
     }
   }
   return b;
@@ -1232,7 +1316,7 @@ __global__ void k_max(const int *cellX, const double *v, int absval, int64_t n, 
   if (m < n && cellX[m] != -1) {
     double x = v[m];
     if (absval) x = fabs(x);
-    if (x > 0.0) b = __double_as_longlong(x);
+    if (x > 0.0) b = dbits(x);
   }
   sh[threadIdx.x] = b;
   __syncthreads();
@@ -2197,11 +2281,11 @@ static int advect_launch(mic_ctx *ctx, double dt, bool wz_known, bool with_max =
     if (!ctx->P.xper) {  // (the periodic advection interpolates the nodes directly)
       const int NX = ctx->P.NX, NY = ctx->P.NY;
       const size_t nn = (size_t)NX * NY;
-      if (!ctx->adv_coef && cudaMalloc((void **)&ctx->adv_coef, 3 * nn * sizeof(Bil4)) != cudaSuccess) {
+      if (!ctx->adv_coef && cudaMalloc((void **)&ctx->adv_coef, 3 * nn * sizeof(BilDF)) != cudaSuccess) {
         ctx->adv_coef = nullptr;
         return MIC_ERR_NOMEM;
       }
-      Bil4 *cb = static_cast<Bil4 *>(ctx->adv_coef);
+      BilDF *cb = static_cast<BilDF *>(ctx->adv_coef);
       cv = {cb, cb + nn, cb + 2 * nn};
       MIC_KERNEL(ctx, "k_advect_coef");
       k_advect_coef<<<grid_for((int64_t)nn), kBlock, 0, ctx->stream>>>(

@@ -40,7 +40,7 @@ __device__ __forceinline__ void strain_rate_and_inverse(double e11, double e22, 
 #else
   const double q = fma(e12, e12, 0.5 * fma(e11, e11, e22 * e22));
   const double r = rsqrt(q);
-  const long long b = __double_as_longlong(q);
+  const long long b = dbits(q);
   edot = (b == 0 || b == 0x7FF0000000000000LL) ? q : q * r;
   iedot = r;
 #endif
