@@ -225,8 +225,24 @@ __global__ void __launch_bounds__(128) k_creep_surrogate_batch_fp32(const double
   int it = 0, fb = 0, active = 0;
   double res = 0.0;
   if (m < n) {
-    const double e = edot[m];
-    const CreepCoef k = creep_coef(T[m], grain_arg(d[m]), P[m]);
+    const double e = edot[m], g = grain_arg(d[m]);
+#ifndef MIC_EXACT
+    if (!(cfg.polish_tol < kCoarseTol)) {  // the polish in double-float arithmetic
+      CreepTermsDF q;
+      const bool q_ok = e > 0.0 && creep_terms_df(T[m], g, P[m], 1.0 / e, q);
+      float lx0 = 0.f;
+      if (q_ok && !(q.a.hi > 1e6f)) {  // the network is consulted on the non-linear branch only
+        float f[4];
+        const float mref = creep_features_df(q, f);
+        lx0 = creep_guess_lx(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
+      }
+      s_out[m] = e > 0.0 ? creep_stress_coarse(q, q_ok, T[m], g, P[m], e, 1.0 / e, lx0, cfg.tol, cfg.maxit,
+                                               cfg.polish_iters, cfg.polish_tol, &it, &res, &fb)
+                         : 0.0;
+    } else
+#endif
+    {
+    const CreepCoef k = creep_coef(T[m], g, P[m]);
     float lx0 = 0.f;
     if (e > 0.0 && e / k.C >= 1.0) {  // the network is consulted on the non-linear branch only
       float f[4];
@@ -235,6 +251,7 @@ __global__ void __launch_bounds__(128) k_creep_surrogate_batch_fp32(const double
     }
     s_out[m] = creep_stress_from_guess(k, e, lx0, cfg.tol, cfg.maxit, cfg.polish_iters, cfg.polish_tol, &it, &res,
                                        &fb);
+    }
     if (it_out) it_out[m] = it;
     if (res_out) res_out[m] = res;
     if (fb_out) fb_out[m] = fb;

@@ -28,6 +28,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "mic_df.cuh"
 #include "mic_internal.cuh"
 
 namespace mic {
@@ -37,6 +38,12 @@ struct CreepCoef {
   double G;     // GBS:         rate = G x^1.8
   double B;     // basal slip:  rate = B x^2.4
   double D;     // dislocation: rate = D x^4
+};
+
+// the law's terms q = (C 1e6, G, B, D) / edot as double-floats (product build, the surrogate's
+// coarse polish: creep_terms_df)
+struct CreepTermsDF {
+  df a, g, b, d;
 };
 
 // The per-marker grain column holds what creep_coef takes: the grain size d in the FMA-free
@@ -335,6 +342,140 @@ __device__ __forceinline__ double creep_solve_terms(const CreepTerms &q, double 
   // the rate jumps at s = 1 Pa where the non-linear terms switch on; a root in the jump is 1 Pa
   return lt_pos(s, 1.0) ? 1.0 : s;
 }
+
+// ---- product build, surrogate polish at a coarse tolerance: double-float arithmetic --------
+//
+// The surrogate's polish stops at |rate/edot - 1| <= polish_tol (1e-7 by default: the stress is
+// then within 1e-7 of the root).  For polish tolerances from kCoarseTol up, the law's terms and
+// the polish run in double-float arithmetic on the FP32 pipe (mic_df.cuh), with no FP64
+// instruction: the terms to a relative 1e-11 (which moves the root by no more than that, a
+// hundredth of the smallest such tolerance) and the residual r - 1 to 1e-13.  A marker the
+// polish does not bring below the tolerance, or whose terms leave FP32's range, takes the exact
+// FP64 solve (its coefficients recomputed in FP64).
+constexpr double kCoarseTol = 1e-9;
+
+// q from (T, grain argument g, P, 1 / edot).  Each Arrhenius factor is one exponential of its
+// whole exponent -- the log of its prefactor (the law's constants folded in), the binary
+// exponent ke of 1/edot = m 2^ke (as ke ln 2) and (P V - Q) / RT -- so that every factor lies in
+// FP32's range; the grain powers and m multiply after.  Logs of the prefactors in 60-digit
+// arithmetic: ln(9.1e-4 42 Vm 1e6), ln(5.8e-4 42 Vm 1e6 pi delta) (viscosity.c:113-121), ln Ag,
+// ln Ad, ln 5.5e7 of both temperature branches (viscosity.c:138-162); R and V as double-floats.
+// Returns false when an exponent or a term leaves FP32's range.
+__device__ __forceinline__ bool creep_terms_df(double T, double g, double P, double iedot, CreepTermsDF &q) {
+  if (lt_pos(P, 1.0)) P = 1.0;
+  const df iRT = df_rcp(df_mul(df_of(T), df{8.314461708068848f, 3.9193113821056613e-07f}));
+  const df PV = df_mul(df_of(P), df{-1.2999999853491317e-05f, -1.4650868680136236e-13f});
+  const df gd = df_of(g), g2 = df_mul(gd, gd), id = df_mul(df_mul(g2, g2), gd);  // 1/d = g^5
+  const long long eb = dbits(iedot);
+  const int ke = (int)((eb >> 52) & 0x7FF) - 1023;
+  const df m = df_of(__longlong_as_double((eb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL));
+  const df kl = df_mul(df{(float)ke, 0.0f}, kLn2);
+  const bool cold_g = lt_pos(T, 255.0), cold_d = lt_pos(T, 258.0);
+  const df x0 = df_add(df_add(df{-0.28377771377563477f, 9.349567342553655e-09f}, kl),
+                       df_mul(df{-59400.0f, 0.0f}, iRT));  // Dv (59.4 kJ/mol)
+  const df x1 = df_add(df_add(df{-20.41365623474121f, 1.6465773455820454e-07f}, kl),
+                       df_mul(df{-49000.0f, 0.0f}, iRT));  // Db (49 kJ/mol), with pi delta
+  const df x2 = df_add(df_add(cold_g ? df{-5.546778678894043f, -4.695249344877084e-08f}
+                                     : df{60.965824127197266f, 5.793160084976989e-07f},
+                              kl),
+                       df_mul(df_add(PV, df{cold_g ? -49000.0f : -192000.0f, 0.0f}), iRT));  // GBS
+  const df x3 = df_add(df_add(cold_d ? df{12.899219512939453f, 3.1315067872128566e-07f}
+                                     : df{66.26414489746094f, -2.824399643941433e-06f},
+                              kl),
+                       df_mul(df_add(PV, df{cold_d ? -60000.0f : -180000.0f, 0.0f}), iRT));  // dislocation
+  const df x4 = df_add(df_add(df{17.822843551635742f, 1.915609999514345e-07f}, kl),
+                       df_mul(df_add(PV, df{-60000.0f, 0.0f}), iRT));  // basal slip
+  const bool ok = fabsf(x0.hi) <= 80.0f && fabsf(x1.hi) <= 80.0f && fabsf(x2.hi) <= 80.0f &&
+                  fabsf(x3.hi) <= 80.0f && fabsf(x4.hi) <= 80.0f;
+  q.a = df_mul(df_mul(iRT, df_mul(id, id)), df_mul(m, df_fma(id, df_exp(x1), df_exp(x0))));
+  q.g = df_mul(df_mul(df_exp(x2), df_mul(id, g2)), m);  // d^-1.4 = g^7
+  q.d = df_mul(df_exp(x3), m);
+  q.b = df_mul(df_exp(x4), m);
+  return ok && fabsf(q.a.hi) < 1e37f && fabsf(q.g.hi) < 1e37f && fabsf(q.d.hi) < 1e37f && fabsf(q.b.hi) < 1e37f;
+}
+
+// One evaluation at p: the residual r - 1 = td + tc + tl - 1 with the series term
+// tc = tg (tb / (tg + tb)) (one double-float division; no product of the two terms, which could
+// leave FP32's range), and FP32 copies of the terms for the step.
+struct CreepEvalDF {
+  df res, p5;
+  float S, tg, tb, td, tl;
+};
+__device__ __forceinline__ void creep_eval_df(const CreepTermsDF &q, const df &p, CreepEvalDF &e) {
+  const df p2 = df_mul(p, p), p4 = df_mul(p2, p2), p8 = df_mul(p4, p4), p12 = df_mul(p8, p4);
+  const df tg = df_mul(q.g, df_mul(p8, p)), tb = df_mul(q.b, p12);
+  e.p5 = df_mul(p4, p);
+  const df td = df_mul(q.a, e.p5), tl = df_mul(q.d, df_mul(p12, p8));
+  const df S = df_add(tg, tb);
+  const df tc = S.hi > 0.0f ? df_mul(tg, df_div(tb, S)) : df{0.0f, 0.0f};
+  e.res = df_add(df_add(td, tl), df_add(tc, df{-1.0f, 0.0f}));
+  e.S = S.hi;
+  e.tg = tg.hi;
+  e.tb = tb.hi;
+  e.td = td.hi;
+  e.tl = tl.hi;
+}
+
+// The Halley step of creep_advance (FP32 branch) from an evaluation: returns a = 0.2 du, the
+// exponent of the factor on p
+__device__ __forceinline__ float creep_step_df(const CreepEvalDF &e) {
+  const float w = e.S > 0.0f ? e.tg / e.S : 0.0f;
+  const float tc = e.tb * w;
+  const float resf = e.res.hi;
+  const float mc = fmaf(0.6f, w, 1.8f);
+  const float r1f = fmaf(tc, mc, fmaf(4.0f, e.tl, e.td));
+  const float r2f = fmaf(tc, fmaf(mc, mc, -0.36f * w * (1.0f - w)), fmaf(16.0f, e.tl, e.td));
+  const float r = __fadd_rn(__fadd_rn(e.td, tc), e.tl);
+  if (!(r > 1e-30f && r < 1e30f)) {
+    // terms beyond FP32 range (an iterate far from the root): a step of -g / 4, which the slope
+    // bound g' <= 4 keeps on the root's side
+    return -0.05f * __logf(fmaxf(fabsf(resf + 1.0f), 1e-30f));
+  }
+  const float ir = 1.0f / r;
+  const float g = fabsf(resf) < 0.5f ? log1pf(resf) : __logf(r);
+  const float g1 = r1f * ir, g2 = fmaf(-g1, g1, r2f * ir);
+  const float den = fmaf(-g, g2, 2.0f * g1 * g1);
+  // Halley where its correction is moderate, Newton otherwise
+  return 0.2f * (den > g1 * g1 ? -2.0f * g * g1 / den : -g / g1);
+}
+
+// p exp(a): p + p d with d = exp(a) - 1 from its series in FP32 for |a| < 2^-5, else p times an
+// FP32 exponential
+__device__ __forceinline__ df creep_advance_df(const df &p, float a) {
+  if (fabsf(a) < 0.03125f) {
+    const float d = a * fmaf(a, fmaf(a, fmaf(a, fmaf(a, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f), 0.5f), 1.0f);
+    return df_fma(p, df{d, 0.0f}, p);
+  }
+  return df_mul(p, df{__expf(fminf(fmaxf(a, -80.0f), 80.0f)), 0.0f});
+}
+
+// Polish steps from p until |r - 1| <= tolf or maxit steps were taken, with creep_iterate's
+// bracket and bisection (the bracket compared as double-floats: a last step below an FP32 ulp of
+// p must not read as leaving it).  Returns the steps taken; res (FP32) and p5 belong to the
+// final p.
+__device__ __forceinline__ int creep_iterate_df(const CreepTermsDF &q, df &p, float tolf, int maxit, bool &conv,
+                                                float &res, df &p5) {
+  df plo = {0.0f, 0.0f}, phi = {INFINITY, 0.0f};
+  CreepEvalDF e;
+  int it = 0;
+  for (;; ++it) {
+    creep_eval_df(q, p, e);
+    conv = fabsf(e.res.hi) <= tolf;
+    if (conv || it >= maxit) break;
+    if (e.res.hi > 0.0f) {
+      if (df_lt(p, phi)) phi = p;
+    } else if (df_lt(plo, p)) {
+      plo = p;
+    }
+    df pn = creep_advance_df(p, creep_step_df(e));
+    if (!(df_lt(plo, pn) && df_lt(pn, phi)))
+      pn = df{plo.hi > 0.0f ? sqrtf(plo.hi * phi.hi) : phi.hi * 0.67032004603563930f, 0.0f};
+    p = pn;
+  }
+  res = e.res.hi;
+  p5 = e.p5;
+  return it;
+}
 #endif
 
 // Exact stress at strain rate edot (law 7) given 1 / edot: returns s*, iterations in *iters.
@@ -400,6 +541,22 @@ __device__ __forceinline__ float creep_features(const CreepCoef &k, double edot,
   for (int i = 0; i < 4; ++i) f[i] = fminf(fmaxf(x[i] - m, -kFeatClamp), kFeatClamp) * (1.0f / kFeatClamp);
   return m;
 }
+
+#ifndef MIC_EXACT
+// the same features from double-float terms q: ln x_lin = -ln q.a, ln x_g = -ln q.g / 1.8,
+// ln x_b = -ln q.b / 2.4, ln x_d = -ln q.d / 4 (FP32 logs of the high parts)
+__device__ __forceinline__ float creep_features_df(const CreepTermsDF &q, float f[4]) {
+  const float xl = -__logf(q.a.hi);
+  const float xg = -__logf(q.g.hi) * (1.0f / 1.8f);
+  const float xb = -__logf(q.b.hi) * (1.0f / 2.4f);
+  const float xd = -__logf(q.d.hi) * 0.25f;
+  const float m = fminf(fminf(xl, xd), fmaxf(xg, xb));
+  const float x[4] = {xl, xg, xb, xd};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) f[i] = fminf(fmaxf(x[i] - m, -kFeatClamp), kFeatClamp) * (1.0f / kFeatClamp);
+  return m;
+}
+#endif
 
 // SiLU and its derivative with the fast reciprocal (__fdividef: two MUFU ops and a multiply,
 // about 2 ulp) instead of the IEEE division sequence: 128 of these per marker at inference.  For
@@ -487,6 +644,42 @@ __device__ __forceinline__ double creep_stress_from_guess(const CreepCoef &k, do
   return creep_stress_from_guess(k, edot, edot > 0.0 ? 1.0 / edot : 0.0, lx0, tol, maxit, polish_iters, polish_tol,
                                  iters, res_out, fb);
 }
+
+#ifndef MIC_EXACT
+// Stress from a surrogate guess lx0 = ln(s / 1e6) at a coarse polish tolerance (from kCoarseTol):
+// the polish in double-float arithmetic on the terms q (q_ok: creep_terms_df succeeded).  A marker
+// on or within 1e-6 of the linear-diffusion branch (edot < C, i.e. q.a > 1e6) is decided and
+// evaluated in FP64 exactly as the exact solve does it (s = edot / C); one whose terms are out of
+// range or whose polish does not reach the tolerance takes the exact FP64 solve (*fb = 1).
+// edot > 0.
+__device__ __forceinline__ double creep_stress_coarse(const CreepTermsDF &q, bool q_ok, double T, double g, double P,
+                                                      double edot, double iedot, float lx0, double tol, int maxit,
+                                                      int polish_iters, double polish_tol, int *iters,
+                                                      double *res_out, int *fb) {
+  *iters = 0;
+  *res_out = 0.0;
+  *fb = 0;
+  if (q_ok && !(q.a.hi > 0.999999e6f) && isfinite(lx0)) {
+    const float tolf = f32_trunc(polish_tol);  // at most polish_tol
+    df p = {__expf(0.2f * lx0), 0.0f}, p5;
+    float res;
+    bool conv;
+    *iters = creep_iterate_df(q, p, tolf, polish_iters, conv, res, p5);
+    if (conv) {
+      *res_out = f64_of(res);
+      const double s = 1e6 * df_to_f64(p5);
+      return lt_pos(s, 1.0) ? 1.0 : s;
+    }
+  }
+  const CreepCoef k = creep_coef(T, g, P);
+  if (dbits(edot) < dbits(k.C)) return edot / k.C;  // linear diffusion branch (viscosity.c:130-133)
+  *fb = 1;
+  int it2;
+  const double s = creep_solve_terms(creep_terms(k, iedot), tol, maxit, &it2, res_out);
+  *iters += it2;
+  return s;
+}
+#endif
 
 // per-warp reduction of the creep counters into the device totals (all lanes of the warp)
 __device__ __forceinline__ void creep_count(CreepCounters *cc, int active, int iters, double res, int fallback) {

@@ -22,23 +22,50 @@ __global__ void __launch_bounds__(tc::kTile, tc::kBlocksPerSM) k_creep_surrogate
   tc::Block B;
   tc::setup(B, dyn, cfg.mlp);
   const int64_t ntiles = (n + tc::kTile - 1) / tc::kTile;
+#ifndef MIC_EXACT
+  const bool coarse = !(cfg.polish_tol < kCoarseTol);  // the polish in double-float arithmetic
+#else
+  const bool coarse = false;
+#endif
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t m = tile * tc::kTile + threadIdx.x;
     const bool valid = m < n;
-    double e = 0.0;
+    double e = 0.0, g = 1.0;
     float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
     CreepCoef k = {1.0, 1.0, 1.0, 1.0};
+    CreepTermsDF q;
+    bool q_ok = false;
     if (valid) {
       e = edot[m];
-      k = creep_coef(T[m], grain_arg(d[m]), P[m]);
-      if (e > 0.0) mref = creep_features(k, e, f);
+      g = grain_arg(d[m]);
+#ifndef MIC_EXACT
+      if (coarse) {
+        q_ok = e > 0.0 && creep_terms_df(T[m], g, P[m], 1.0 / e, q);
+        if (q_ok) mref = creep_features_df(q, f);
+      } else
+#endif
+      {
+        k = creep_coef(T[m], g, P[m]);
+        if (e > 0.0) mref = creep_features(k, e, f);
+      }
     }
     const float y = tc::guess(B, f, cfg.tc_wait_limit, &cc->tc_timeouts);
     int it = 0, fb = 0;
     double res = 0.0;
     if (valid) {
-      const double s = creep_stress_from_guess(k, e, creep_guess_lx(cfg.mlp, y, mref), cfg.tol, cfg.maxit,
-                                               cfg.polish_iters, cfg.polish_tol, &it, &res, &fb);
+      const float lx = creep_guess_lx(cfg.mlp, y, mref);
+#ifndef MIC_EXACT
+      const double s =
+          !coarse ? creep_stress_from_guess(k, e, lx, cfg.tol, cfg.maxit, cfg.polish_iters, cfg.polish_tol, &it,
+                                            &res, &fb)
+          : e > 0.0 ? creep_stress_coarse(q, q_ok, T[m], g, P[m], e, 1.0 / e, lx, cfg.tol, cfg.maxit,
+                                          cfg.polish_iters, cfg.polish_tol, &it, &res, &fb)
+                    : 0.0;
+#else
+      (void)q_ok;
+      const double s =
+          creep_stress_from_guess(k, e, lx, cfg.tol, cfg.maxit, cfg.polish_iters, cfg.polish_tol, &it, &res, &fb);
+#endif
       s_out[m] = s;
       if (it_out) it_out[m] = it;
       if (res_out) res_out[m] = res;

@@ -80,4 +80,64 @@ __device__ __forceinline__ df df_fma(const df &a, const df &b, const df &c) {
   return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(e, c.lo)));
 }
 
+// a < b for normalised double-floats (|lo| at most half an ulp of hi): lexicographic on (hi, lo)
+__device__ __forceinline__ bool df_lt(const df &a, const df &b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+
+// a / b: the FP32 quotient and one correction from the double-float remainder a - b q
+__device__ __forceinline__ df df_div(const df &a, const df &b) {
+  const float q = __fdiv_rn(a.hi, b.hi);
+  const df r = df_fma(b, df{-q, 0.0f}, a);
+  return fast_two_sum(q, __fdiv_rn(r.hi, b.hi));
+}
+// 1 / a: the FP32 reciprocal and one Newton step, y + y (1 - a y)
+__device__ __forceinline__ df df_rcp(const df &a) {
+  const float y = __frcp_rn(a.hi);
+  const df e = df_fma(a, df{-y, 0.0f}, df{1.0f, 0.0f});
+  return df_fma(df{y, 0.0f}, e, df{y, 0.0f});
+}
+
+// 2^(j/16) for j = 0 .. 15 as double-floats (hi, lo), from 60-digit arithmetic
+__device__ const float2 kExp2Sixteenths[16] = {
+    {1.0f, 0.0f},
+    {1.0442737340927124f, 4.8334701574503924e-08f},
+    {1.0905077457427979f, -1.3077539939843064e-08f},
+    {1.1387885808944702f, 5.386222312608879e-08f},
+    {1.1892070770263672f, 3.797635272917432e-08f},
+    {1.2418577671051025f, 4.496838101886169e-08f},
+    {1.2968395948410034f, -4.018999533172973e-08f},
+    {1.3542555570602417f, -1.0123349269974824e-08f},
+    {1.4142135381698608f, 2.4203234971764687e-08f},
+    {1.4768261909484863f, -4.500898853621038e-08f},
+    {1.5422108173370361f, 8.070904833346049e-09f},
+    {1.610490322113037f, 9.836217174097328e-09f},
+    {1.6817928552627563f, -2.4755326677450284e-08f},
+    {1.7562521696090698f, -9.235770370707996e-09f},
+    {1.8340080976486206f, -1.1239277952768134e-08f},
+    {1.9152065515518188f, 9.845328108326612e-09f}};
+// ln 2 / 16 and ln 2 as double-floats
+#define kLn2Over16 (df{0.043321698904037476f, -1.1904088825787085e-10f})
+#define kLn2 (df{0.6931471824645996f, -1.9046542121259336e-09f})
+
+// exp(x) for x in about [-87, 88] (the result in FP32's normal range), relative error near 1e-11
+// (Tang's table-driven method): x = k ln2/16 + r with k = round(16 x / ln 2) and |r| <= ln2/32,
+// exp(x) = 2^(k div 16) 2^((k mod 16) / 16) exp(r), 2^(j/16) from the table and exp(r) = 1 + r + t
+// with the tail t = r^2 (1/2 + r/6 + r^2/24 + r^3/120 + r^4/720) in FP32 (|t| < 2.4e-4: its
+// rounding is below 2e-11, the truncation below 1e-15).
+__device__ __forceinline__ df df_exp(const df &x) {
+  // (callers keep x in range; the clamp only keeps the exponent arithmetic below valid)
+  const float kf = fminf(fmaxf(rintf(__fmul_rn(x.hi, 23.083120346069336f)), -2016.0f), 2016.0f);
+  const df r = df_fma(df{-kf, 0.0f}, kLn2Over16, x);
+  const float h = r.hi;
+  const float t = __fmul_rn(
+      __fmul_rn(h, h),
+      __fmaf_rn(h, __fmaf_rn(h, __fmaf_rn(h, __fmaf_rn(h, 1.0f / 720.0f, 1.0f / 120.0f), 1.0f / 24.0f), 1.0f / 6.0f),
+                0.5f));
+  const df one_r = two_sum(1.0f, r.hi);
+  const df e = fast_two_sum(one_r.hi, __fadd_rn(one_r.lo, __fadd_rn(r.lo, t)));
+  const int k = (int)kf;
+  const float2 tb = __ldg(&kExp2Sixteenths[k & 15]);
+  const float p2 = __int_as_float(((k >> 4) + 127) << 23);  // 2^(k div 16), k div 16 in [-126, 126]
+  return df_scale(df_mul(e, df{tb.x, tb.y}), p2);
+}
+
 }  // namespace mic

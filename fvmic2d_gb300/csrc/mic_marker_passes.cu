@@ -92,13 +92,14 @@ template <bool CREEP = true>
 __device__ __forceinline__ bool yield_marker(const YieldCols &c, const mic_materials &M, const mic_options &O,
                                              const CreepConfig &cfg, double dt, int64_t m, float lx_guess,
                                              const CreepCoef *kc, double kedot, double kiedot, Status *st,
-                                             CreepIn &ci, int &creep_active, int limit) {
+                                             CreepIn &ci, int &creep_active, int limit,
+                                             const CreepTermsDF *qdf = nullptr, int q_ok = 0) {
   bool yielded = false;
   const double eta_old = c.eta[m], mu_old = c.mu[m];
   const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   const int k = c.mat[m];
   double eta, mu;
-  ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], lx_guess, 0, 0, 0.0, kc != nullptr, {}, kedot, kiedot};
+  ci = CreepIn{e11, e22, e12, c.grain[m], c.p[m], lx_guess, 0, 0, 0.0, kc != nullptr, {}, kedot, kiedot, qdf, q_ok};
   if (kc) ci.k = *kc;
   if (!(CREEP ? rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu, &cfg, &ci)
               : rheology(M, O, k, c.T[m], c.X[m], c.Y[m], eta, mu))) {
@@ -195,6 +196,25 @@ __device__ __forceinline__ bool creep_marker_features(const YieldCols &c, const 
   return true;
 }
 
+#ifndef MIC_EXACT
+// creep_marker_features for the surrogate's coarse polish: the law's terms in double-float
+// arithmetic (q_ok false when they leave FP32's range: the marker then takes the FP64 solve)
+__device__ __forceinline__ bool creep_marker_features_df(const YieldCols &c, const mic_materials &M, int64_t m,
+                                                         CreepTermsDF &q, int &q_ok, double &edot, double &iedot,
+                                                         float f[4], float *mref) {
+  if (M.hasEtaT[c.mat[m]] != 7) return false;
+  strain_rate_and_inverse(c.exx[m], c.eyy[m], c.exy[m], edot, iedot);
+  q_ok = gt_zero(edot) && creep_terms_df(c.T[m], c.grain[m], c.p[m], iedot, q);
+  if (!q_ok) {
+    *mref = 0.f;
+    f[0] = f[1] = f[2] = f[3] = 0.f;
+    return true;
+  }
+  *mref = creep_features_df(q, f);
+  return true;
+}
+#endif
+
 // One marker of checkPlasticYielding (the solo kernels and their batched forms share it).
 // MODE 0: exact creep solve; MODE 1: surrogate guess on the CUDA cores (FP32, w2s: the hidden
 // layer's weights in shared memory), polish and fallback; MODE 2: no material uses law 7.
@@ -211,10 +231,21 @@ __device__ __forceinline__ bool yield_one(const YieldCols &c, const mic_material
     float lx = 0.f, f[4], mref;
     double edot = 0.0, iedot = 0.0;
     CreepCoef k;
+#ifndef MIC_EXACT
+    CreepTermsDF q;
+    int q_ok = 0;
+    const bool coarse = MODE == 1 && !(cfg.polish_tol < kCoarseTol);  // uniform over the pass
+    const bool law7 = MODE == 1 && (coarse ? creep_marker_features_df(c, M, m, q, q_ok, edot, iedot, f, &mref)
+                                           : creep_marker_features(c, M, m, k, edot, iedot, f, &mref));
+#else
+    const bool coarse = false;
+    const CreepTermsDF q{};
+    const int q_ok = 0;
     const bool law7 = MODE == 1 && creep_marker_features(c, M, m, k, edot, iedot, f, &mref);
+#endif
     if (law7) lx = creep_guess_lx(cfg.mlp, mlp_forward(cfg.mlp, w2s, f), mref);
-    yielded = yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 ? &k : nullptr, edot, iedot, st, ci, creep_active,
-                                      limit);
+    yielded = yield_marker<MODE != 2>(c, M, O, cfg, dt, m, lx, law7 && !coarse ? &k : nullptr, edot, iedot, st, ci,
+                                      creep_active, limit, law7 && coarse ? &q : nullptr, q_ok);
   } else if (limit && m < n) {
     c.eta[m] = limit_eta(c.eta[m], O);
   }
@@ -232,14 +263,25 @@ __device__ __forceinline__ bool yield_tc_round(tc::Block &B, const YieldCols &c,
   float f[4] = {0.f, 0.f, 0.f, 0.f}, mref = 0.f;
   double edot = 0.0, iedot = 0.0;
   CreepCoef k;
+#ifndef MIC_EXACT
+  CreepTermsDF q;
+  int q_ok = 0;
+  const bool coarse = !(cfg.polish_tol < kCoarseTol);  // uniform over the pass
+  const bool law7 = live && (coarse ? creep_marker_features_df(c, M, m, q, q_ok, edot, iedot, f, &mref)
+                                    : creep_marker_features(c, M, m, k, edot, iedot, f, &mref));
+#else
+  const bool coarse = false;
+  const CreepTermsDF q{};
+  const int q_ok = 0;
   const bool law7 = live && creep_marker_features(c, M, m, k, edot, iedot, f, &mref);
+#endif
   const float y = tc::guess(B, f, cfg.tc_wait_limit, &cc->tc_timeouts);
   int creep_active = 0;
   CreepIn ci = {};
   bool yielded = false;
   if (live)
-    yielded = yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 ? &k : nullptr, edot, iedot,
-                           st, ci, creep_active, limit);
+    yielded = yield_marker(c, M, O, cfg, dt, m, creep_guess_lx(cfg.mlp, y, mref), law7 && !coarse ? &k : nullptr,
+                           edot, iedot, st, ci, creep_active, limit, law7 && coarse ? &q : nullptr, q_ok);
   if (limit && !live && m < n) c.eta[m] = limit_eta(c.eta[m], O);
   creep_count(cc, creep_active, ci.iters, ci.res, ci.fb);
   return yielded;

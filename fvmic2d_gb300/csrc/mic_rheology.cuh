@@ -21,6 +21,10 @@ struct CreepIn {
   CreepCoef k;
   double edot;   // strain-rate invariant sqrt(0.5 (e11^2 + e22^2) + e12^2)
   double iedot;  // 1 / edot (product build)
+  // product build, surrogate at a coarse polish tolerance: the law's terms in double-float
+  // arithmetic (then k is not evaluated) and whether they are in range
+  const CreepTermsDF *qdf;
+  int q_ok;
 };
 
 __device__ __forceinline__ double strain_rate_invariant(double e11, double e22, double e12) {
@@ -51,6 +55,15 @@ __device__ __forceinline__ void strain_rate_and_inverse(double e11, double e22, 
 // invariant; at zero strain rate the law's diffusion viscosity 0.5 / C (viscosity.c:130-133).
 __device__ __forceinline__ double creep_viscosity(const CreepConfig &cfg, double T, CreepIn &ci) {
   double edot, iedot;  // once per marker: the solve and the viscosity share them
+#ifndef MIC_EXACT
+  if (ci.qdf) {  // the surrogate's coarse polish in double-float arithmetic (mic_creep.cuh)
+    if (!gt_zero(ci.edot)) return 0.5 / creep_coef(T, ci.grain, ci.p).C;
+    const double s = creep_stress_coarse(*ci.qdf, ci.q_ok != 0, T, ci.grain, ci.p, ci.edot, ci.iedot, ci.lx_guess,
+                                         cfg.tol, cfg.maxit, cfg.polish_iters, cfg.polish_tol, &ci.iters, &ci.res,
+                                         &ci.fb);
+    return s * (0.5 * ci.iedot);
+  }
+#endif
   if (ci.have_k) {
     edot = ci.edot;
     iedot = ci.iedot;
