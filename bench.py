@@ -94,22 +94,23 @@ KERNEL_BYTES_LAW7 = {k: (4 + 4 + 8 + 8 + 24 + 16 + 8 + 16, 0) for k in ("k_yield
 
 
 # DRAM bytes per marker of one launch from an ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum) of the 1,048,576-marker box, scaled to a full launch by markers
-# processed (profiles/k_advect_vep_slab_box_1m_full.md).  Reads are the algorithmic reads plus
-# the 32 B/marker of stored offsets the first RK4 stage loads instead of forming them (bytes for
-# FP64 instructions); at the small size part of the written bytes is still in L2 when the kernel
-# ends.
-# The advection and the law-7 passes from captures of the 4,194,304-marker ice box
-# (profiles/k_advect_ice_creep_box_4m_full.md, profiles/k_yield_creep_ice_creep_box_4m_full.md).
-KERNEL_TRAFFIC_PER_MARKER = {"k_advect": (528.6e6 + 258.3e6) / 4194304, "k_yield_tc": (370.2e6 + 53.5e6) / 4194304,
-                             "k_yield": (302.2e6 + 48.7e6) / 4194304}
-# FP64 work per marker from the same captures (DFMA, DADD, DMUL thread instructions / markers):
-# flops with a DFMA counted twice, and the FP64 arithmetic instructions.  The kernels of this path
-# are bound by the FP64 pipe, which issues 2 FP64 instructions per SM per clock on GB300, not by
-# HBM.  (k_yield: the exact law-7 pass.)
-_FP64_WARP_INSTR = {"k_advect": (8.78e6, 7.86e6), "k_yield_tc": (7.15e6, 13.16e6), "k_yield": (22.00e6, 22.11e6)}
-KERNEL_FP64_FLOPS_PER_MARKER = {k: (2 * f + u) * 32 / 4194304 for k, (f, u) in _FP64_WARP_INSTR.items()}
-KERNEL_FP64_INST_PER_MARKER = {k: (f + u) * 32 / 4194304 for k, (f, u) in _FP64_WARP_INSTR.items()}
+# dram__bytes_write.sum) of the 4,194,304-marker ice box (the first step of each mode), scaled to a
+# full launch by markers processed (profiles/fp64_mix_ice_creep_box_4m.md).  The advection reads
+# the algorithmic bytes plus the 32 B/marker of stored offsets its first RK4 stage loads instead
+# of forming them.
+KERNEL_TRAFFIC_PER_MARKER = {"k_advect": 791.1e6 / 4194304, "k_yield_tc": 423.9e6 / 4194304,
+                             "k_yield": 421.5e6 / 4194304}
+# FP64 work per marker from the same captures (DFMA and DADD + DMUL thread instructions per
+# marker): flops with a DFMA counted twice, and the FP64 arithmetic instructions.  The exact law-7
+# pass (k_yield) is bound by the FP64 pipe, which issues 2 FP64 instructions per SM per clock on
+# GB300; the advection mostly, with its interpolations in double-float arithmetic on the FP32
+# pipe; the tensor-core surrogate pass runs its polish in double-float arithmetic and is bound by
+# instruction issue (KERNEL_INST_PER_MARKER: every thread instruction, all pipes).
+_FP64_PER_MARKER = {"k_advect": (14.0, 45.0), "k_yield_tc": (5.0, 10.0), "k_yield": (65.7, 130.6)}
+KERNEL_FP64_FLOPS_PER_MARKER = {k: 2 * f + u for k, (f, u) in _FP64_PER_MARKER.items()}
+KERNEL_FP64_INST_PER_MARKER = {k: f + u for k, (f, u) in _FP64_PER_MARKER.items()}
+KERNEL_INST_PER_MARKER = {"k_advect": 3005.0, "k_yield_tc": 4008.0, "k_yield": 2885.0}
+ISSUE_PEAK_GINST = 4 * 32 * 152 * 2.07  # thread instructions per second, in G (4 warp issues/SM/clk)
 FP64_PEAK_TFLOPS = 2 * 2 * 152 * 2.07e9 / 1e12  # 2 DFMA/SM/clk x 2 flops x 152 SMs x 2.07 GHz
 FP64_PEAK_GINST = 2 * 152 * 2.07  # FP64 instructions per second, in G
 
@@ -421,8 +422,14 @@ def roofline(prof, n, nodes, steps, hbm_peak, peak_src, law7=False):
         fp64 = {"kernel": top_name, "flops_per_marker": fpm, "achieved": fpm * n / (dur * 1e-3) / 1e12,
                 "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": fpm * n / (dur * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
                 "inst_per_marker": ipm, "issue_frac": ipm * n / (dur * 1e-3) / 1e9 / FP64_PEAK_GINST,
-                "note": "the bound that applies: FP64 pipe, 2 FP64 instructions/SM/clk; flops and instructions per "
-                        "marker from ncu; issue_frac = FP64 instructions issued / peak"}
+                "note": "FP64 pipe, 2 FP64 instructions/SM/clk; flops and instructions per marker from ncu; "
+                        "issue_frac = FP64 instructions issued / peak"}
+        if top_name in KERNEL_INST_PER_MARKER:
+            ins = KERNEL_INST_PER_MARKER[top_name]
+            fp64["all_inst_per_marker"] = ins
+            fp64["all_issue_frac"] = ins * n / (dur * 1e-3) / 1e9 / ISSUE_PEAK_GINST
+            fp64["all_issue_note"] = ("every thread instruction (all pipes) from ncu against 4 warp instructions "
+                                      "per SM per clock: the bound of a pass whose FP64 work moved to the FP32 pipe")
     shares = {k: round(v[0] / prof_total, 4) for k, v in kern[:12]}
     per_step = {k: round(v[0] / steps, 4) for k, v in kern[:12]}
     return roof, fp64, shares, per_step
