@@ -114,6 +114,24 @@ __device__ const float2 kExp2Sixteenths[16] = {
     {1.7562521696090698f, -9.235770370707996e-09f},
     {1.8340080976486206f, -1.1239277952768134e-08f},
     {1.9152065515518188f, 9.845328108326612e-09f}};
+// interp_w (mic_internal.cuh) in double-float arithmetic: sum_k w_k f_k over the cell's four
+// nodes in the same order, the weights given as double-floats, the node values split on load
+__device__ __forceinline__ df interp_w_df(const double *__restrict__ f, int NX, int i, int j, const df w[4]) {
+  const size_t r0 = (size_t)j * NX, r1 = r0 + NX;
+  const int i1 = next_col(i, NX);
+  df s = df_mul(w[0], df_of(__ldg(f + r0 + i)));
+  s = df_fma(w[1], df_of(__ldg(f + r1 + i)), s);
+  s = df_fma(w[2], df_of(__ldg(f + r0 + i1)), s);
+  return df_fma(w[3], df_of(__ldg(f + r1 + i1)), s);
+}
+// the four corner weights of a W4 (w00, w01, w10, w11: interp_w's order) as double-floats
+__device__ __forceinline__ void w4_df(const W4 &w, df out[4]) {
+  out[0] = df_of(w.w00);
+  out[1] = df_of(w.w01);
+  out[2] = df_of(w.w10);
+  out[3] = df_of(w.w11);
+}
+
 // ln 2 / 16 and ln 2 as double-floats
 #define kLn2Over16 (df{0.043321698904037476f, -1.1904088825787085e-10f})
 #define kLn2 (df{0.6931471824645996f, -1.9046542121259336e-09f})

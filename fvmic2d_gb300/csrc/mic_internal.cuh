@@ -316,6 +316,16 @@ inline unsigned grid_for(int64_t n, int block) {
   int64_t g = (n + block - 1) / block;
   return (unsigned)(g < 1 ? 1 : g);
 }
+// streaming multiprocessors of the context's device (cached per device ordinal)
+inline int sm_count(const mic_ctx *ctx) {
+  static int cache[64];
+  const int d = ctx->device;
+  if (d >= 0 && d < 64 && cache[d] > 0) return cache[d];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d) != cudaSuccess || n < 1) n = 1;
+  if (d >= 0 && d < 64) cache[d] = n;
+  return n;
+}
 
 // Bit pattern of a non-negative double, canonicalising -0.0 to +0.0, so that for
 // non-negative finite values a >= b  <=>  bits(a) >= bits(b) as signed integers.

@@ -410,15 +410,23 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
   const double msxy = interp_run(nd.soxy, NX, cx, cy, bx, by);
   const double mdsxy = interp_run(nd.dsxy, NX, cx, cy, bx, by);
 #else
+  // values that later enter a difference stay FP64: the strain-rate residual's (e11 - exx,
+  // e12 - exy, with their sources) and the old stresses the sub-grid stress pass subtracts the
+  // marker's from; pressure, dsyy and the vorticity in double-float arithmetic on the FP32 pipe
+  // (mic_df.cuh)
   const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, centre_cmax(P), i, j);
-  c.p[m] = interp_w(nd.p, NX, i, j, wc);
+  df wcd[4];
+  w4_df(wc, wcd);
+  c.p[m] = df_to_f64(interp_w_df(nd.p, NX, i, j, wcd));
   const double mexx = interp_w(nd.exx, NX, i, j, wc);
   const double msxx = interp_w(nd.soxx, NX, i, j, wc);
   const double msyy = interp_w(nd.soyy, NX, i, j, wc);
   const double mdsxx = interp_w(nd.dsxx, NX, i, j, wc);
-  const double mdsyy = interp_w(nd.dsyy, NX, i, j, wc);
+  const df mdsyy = interp_w_df(nd.dsyy, NX, i, j, wcd);
   const W4 wb = load_w4(g.w0, m);
-  c.wxy[m] = interp_w(nd.wxy, NX, cx, cy, wb);
+  df wbd[4];
+  w4_df(wb, wbd);
+  c.wxy[m] = df_to_f64(interp_w_df(nd.wxy, NX, cx, cy, wbd));
   const double mexy = interp_w(nd.exy, NX, cx, cy, wb);
   const double msxy = interp_w(nd.soxy, NX, cx, cy, wb);
   const double mdsxy = interp_w(nd.dsxy, NX, cx, cy, wb);
@@ -443,7 +451,7 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
     idm = 0.5 / dtmu;
   }
   const double e11 = fma(mdsxx, idm, msxx * ie);
-  const double e22 = fma(mdsyy, idm, msyy * ie);
+  const double e22 = df_to_f64(df_fma(mdsyy, df_of(idm), df_mul(df_of(msyy), df_of(ie))));
   const double e12 = fma(mdsxy, idm, msxy * ie);
 #endif
   c.exx[m] = e11;
@@ -648,6 +656,7 @@ __global__ void __launch_bounds__(128) k_subgrid_stress_nodes(Params P, const in
 // and divides.  Sums run in marker order within a cell; the cross-cell order differs from the
 // reference's single loop (rounding at the last place), and is fixed, so runs reproduce.
 // part[acc * ncells + cell]: corner k sxy at 2k, weight at 2k+1; centre sxx, syy, weight at 8..10.
+constexpr int kSubgridBlocksPerSM = 4;
 __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double *__restrict__ gx0,
                                                           const double *__restrict__ gy0,
                                                           const double *__restrict__ wb,
@@ -657,9 +666,11 @@ __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double
                                                           const int *__restrict__ cs, double *__restrict__ part) {
   __shared__ double sloc[8][128];
   const int ncells = P.NCX * (P.NY - 1);
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
   const int t = threadIdx.x;
+  // a persistent grid (kSubgridBlocksPerSM blocks of 128 per SM) walking the cells: each thread
+  // streams its cell's markers from six columns, and with more warps per SM their sectors no
+  // longer fit L1 (measured: 4.3 times the algorithmic DRAM bytes at the default occupancy)
+  for (int c = blockIdx.x * blockDim.x + t; c < ncells; c += gridDim.x * blockDim.x) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) sloc[k][t] = 0.0;
   const long long half = 0x3FE0000000000000LL;
@@ -698,6 +709,7 @@ __global__ void __launch_bounds__(128) k_subgrid_partials(Params P, const double
   part[(size_t)8 * ncells + c] = sxx;
   part[(size_t)9 * ncells + c] = syy;
   part[(size_t)10 * ncells + c] = wn;
+  }
 }
 
 // Node (i, j): dsxy sums of cells (i-1,j-1) corner 3, (i,j-1) corner 2, (i-1,j) corner 1, (i,j)
@@ -809,19 +821,26 @@ __device__ __forceinline__ void subgridT_markers_one(const Params &P, const SubT
 #else
   // the stored corner weights, shared by the four fields (the reference multiplies each value
   // by both factors in turn; the products agree to rounding)
+  // T enters as the difference Tm - T: FP64; density, heat capacity and conductivity only form
+  // the exponent, in double-float arithmetic on the FP32 pipe (mic_df.cuh)
   const W4 w = load_w4(g.w0, m);
   const double Tm = interp_w(Tn, NX, i, j, w);
-  const double rhom = rho0 + interp_w(rn, NX, i, j, w);
-  const double cpm = interp_w(cpn, NX, i, j, w);
-  const double km = interp_w(kn, NX, i, j, w);
+  df wd[4];
+  w4_df(w, wd);
+  const df rhom = df_add(df_of(rho0), interp_w_df(rn, NX, i, j, wd));
+  const df cpm = interp_w_df(cpn, NX, i, j, wd);
+  const df km = interp_w_df(kn, NX, i, j, wd);
 #endif
 #ifdef MIC_EXACT
   const double tdiff = cpm * rhom / km / (2.0 / (dx * dx) + 2.0 / (dy * dy));
   c.dTsub[m] = (Tm - c.T[m]) * (1.0 - exp(-D * dt / tdiff));
 #else
-  // -D dt / tdiff with 1/dx^2, 1/dy^2 from the reciprocal tables: one division
-  const double ixx = P.ix[i], iyy = P.iy[j];
-  const double arg = -D * dt * km * (2.0 * (ixx * ixx + iyy * iyy)) / (cpm * rhom);
+  // -D dt / tdiff = -D dt km 2 (1/dx^2 + 1/dy^2) / (cp rho), 1/dx and 1/dy from the reciprocal
+  // tables; one FP64 add brings it back for the exponential
+  const df ixx = df_of(P.ix[i]), iyy = df_of(P.iy[j]);
+  const df h2 = df_scale(df_fma(ixx, ixx, df_mul(iyy, iyy)), 2.0f);
+  const df num = df_mul(df_mul(df_neg(df_mul(df_of(D), df_of(dt))), km), h2);
+  const double arg = df_to_f64(df_div(num, df_mul(cpm, rhom)));
   c.dTsub[m] = (Tm - c.T[m]) * (1.0 - exp(arg));
 #endif
 }
@@ -1092,10 +1111,13 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     }
     mvx[s] = bil_eval_df(cvx, (size_t)(vxY + 1) * (NX - 1) + vxX, fx, fty);
     mvy[s] = bil_eval_df(cvy, (size_t)vyY * NX + vyX + 1, ftx, fy);
-    if (s == 0)  // at the marker itself: the bilinear form of the stored weights
-      mwz[s] = df_of(wz_known ? c.wxy[m] : interp_w(wz, NX, i, j, load_w4(g.w0, m)));
-    else
+    if (s == 0) {  // at the marker itself: the stored weights' form, as the strain pass forms it
+      df wbd[4];
+      if (!wz_known) w4_df(load_w4(g.w0, m), wbd);
+      mwz[s] = df_of(wz_known ? c.wxy[m] : df_to_f64(interp_w_df(wz, NX, i, j, wbd)));
+    } else {
       mwz[s] = bil_eval_df(cwz, (size_t)j * (NX - 1) + i, fx, fy);
+    }
     // the next stage's position: the displacement in double-float, added to the FP64 start
     if (s < 3) {
       const df h = (s < 2) ? hdt : fdt;
@@ -2189,7 +2211,8 @@ static int subgrid_nodes(mic_ctx *ctx) {
 #else
   if (ctx->n > 0) {
     MIC_KERNEL(ctx, "k_subgrid_partials");
-    k_subgrid_partials<<<grid_for(ctx->ncells, 128), 128, 0, ctx->stream>>>(
+    const int64_t full = grid_for(ctx->ncells, 128), cap = (int64_t)kSubgridBlocksPerSM * sm_count(ctx);
+    k_subgrid_partials<<<(unsigned)(full < cap ? full : cap), 128, 0, ctx->stream>>>(
         ctx->P, ctx->geo[0], ctx->geo[1], ctx->wgt[0], ctx->scr0, ctx->scr1, ctx->scr2, ctx->cell_start,
         ctx->part_b);
   } else {
