@@ -110,7 +110,7 @@ int mic_creep_tc_blocks(mic_ctx *ctx, int64_t n) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   const int64_t tiles = (n + tc::kTile - 1) / tc::kTile;
-  const int64_t cap = tc::kBlocksPerSM * (int64_t)(sms > 0 ? sms : 1);
+  const int64_t cap = tc::kGridBlocksPerSM * (int64_t)(sms > 0 ? sms : 1);
   return (int)(tiles < cap ? (tiles > 0 ? tiles : 1) : cap);
 }
 

@@ -31,7 +31,10 @@ namespace tc {
 
 constexpr int kTile = 128;              // markers per block tile = MMA M = TMEM lanes
 constexpr int kTmemCols = 64;           // FP32 accumulator columns (N)
-constexpr int kBlocksPerSM = 5;         // resident blocks per SM (launch bounds, persistent grids)
+constexpr int kBlocksPerSM = 5;         // blocks that fit an SM (launch bounds: at most 102 registers)
+// blocks per SM of the persistent grids (all that fit: leaving one SM slot to the first
+// projection's partial sums on the second stream measured slower)
+constexpr int kGridBlocksPerSM = 5;
 constexpr uint32_t kOpA = 128 * 64 * 2;  // bytes of one A operand (hi or lo)
 constexpr uint32_t kOpB = 64 * 64 * 2;   // bytes of one B operand
 // small parameters in shared memory, neuron-major so that each neuron's are two 16-byte loads:

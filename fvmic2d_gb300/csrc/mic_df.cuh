@@ -39,6 +39,19 @@ __device__ __forceinline__ df df_of(double v) {
   r.lo = b < 0 ? -lo : lo;
   return r;
 }
+// the split of v 2^-k, an exact scaling by the exponent (for values whose squares would leave
+// FP32's range); zero and FP64 subnormals give zero
+__device__ __forceinline__ df df_of_scaled(double v, int k) {
+  const long long b = dbits(v);
+  const int eb = (int)((b >> 52) & 0x7FF);
+  const int e = eb - 1023 - k;
+  df r;
+  r.hi = eb == 0 ? 0.0f : f32_trunc(v, k);
+  const float m = __fmul_rn((float)(unsigned)(b & 0x1FFFFFFFLL), 0x1p-52f);
+  float lo = (eb != 0 && e >= -126 && e <= 127) ? __fmul_rn(m, __int_as_float((e + 127) << 23)) : 0.0f;
+  r.lo = b < 0 ? -lo : lo;
+  return r;
+}
 __device__ __forceinline__ df df_of(float v) { return {v, 0.0f}; }
 
 // hi + lo as a double: the halves are exact doubles (bit-pattern conversions), one FP64 addition
@@ -114,6 +127,31 @@ __device__ const float2 kExp2Sixteenths[16] = {
     {1.7562521696090698f, -9.235770370707996e-09f},
     {1.8340080976486206f, -1.1239277952768134e-08f},
     {1.9152065515518188f, 9.845328108326612e-09f}};
+// sqrt(a) for a >= 0 in FP32's normal range: the FP32 square root and one Newton correction
+// from the double-float remainder, s + (a - s^2) / (2 s)
+__device__ __forceinline__ df df_sqrt(const df &a) {
+  if (!(a.hi > 0.0f)) return df{0.0f, 0.0f};
+  const float s = __fsqrt_rn(a.hi);
+  const df r = df_fma(df{-s, 0.0f}, df{s, 0.0f}, a);
+  return fast_two_sum(s, __fdiv_rn(r.hi, 2.0f * s));
+}
+
+// sqrt(x^2 + y^2) (q = 0.5: sqrt(0.5 x^2 + 0.5 y^2 + z^2) with z given) for FP64 inputs of any
+// magnitude: scaled by the largest one's binary exponent before the double-float squares, the
+// result scaled back exactly
+__device__ __forceinline__ double df_norm(double x, double y, double z, bool half_xy) {
+  const int ex = exp2_of(fabs(x)), ey = exp2_of(fabs(y)), ez = exp2_of(fabs(z));
+  const int k = max(ex, max(ey, ez));
+  if (k < -1000 || k > 1000) return half_xy ? sqrt(0.5 * (x * x + y * y) + z * z) : sqrt(x * x + y * y + z * z);
+  const df xs = df_of_scaled(x, k), ys = df_of_scaled(y, k), zs = df_of_scaled(z, k);
+  df q = df_fma(xs, xs, df_mul(ys, ys));
+  if (half_xy) q = df_scale(q, 0.5f);
+  q = df_fma(zs, zs, q);
+  const double r = df_to_f64(df_sqrt(q));
+  // times 2^k, exactly: r is in [2^-1, 2^1] or zero
+  return __longlong_as_double(dbits(r) == 0 ? 0LL : dbits(r) + ((long long)k << 52));
+}
+
 // interp_w (mic_internal.cuh) in double-float arithmetic: sum_k w_k f_k over the cell's four
 // nodes in the same order, the weights given as double-floats, the node values split on load
 __device__ __forceinline__ df interp_w_df(const double *__restrict__ f, int NX, int i, int j, const df w[4]) {

@@ -465,7 +465,12 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
   }
 #endif
   const double a = e11 - mexx, b = e12 - mexy;
+#ifdef MIC_EXACT
   const double r = sqrt(a * a + b * b);  // pow(., 2.0) of the reference: the correctly rounded square
+#else
+  // the differences in FP64, their magnitude in double-float arithmetic (scaled)
+  const double r = df_norm(a, b, 0.0, false);
+#endif
   c.srr[m] = r;
   if (isnan(r)) atomicAdd(&st->nan_residual, 1ULL);
 }
@@ -1112,9 +1117,13 @@ __device__ __forceinline__ double advect_marker(const Params &P, const AdvectCol
     mvx[s] = bil_eval_df(cvx, (size_t)(vxY + 1) * (NX - 1) + vxX, fx, fty);
     mvy[s] = bil_eval_df(cvy, (size_t)vyY * NX + vyX + 1, ftx, fy);
     if (s == 0) {  // at the marker itself: the stored weights' form, as the strain pass forms it
-      df wbd[4];
-      if (!wz_known) w4_df(load_w4(g.w0, m), wbd);
-      mwz[s] = df_of(wz_known ? c.wxy[m] : df_to_f64(interp_w_df(wz, NX, i, j, wbd)));
+      if (wz_known) {
+        mwz[s] = df_of(c.wxy[m]);
+      } else {
+        df wbd[4];
+        w4_df(load_w4(g.w0, m), wbd);
+        mwz[s] = df_of(df_to_f64(interp_w_df(wz, NX, i, j, wbd)));
+      }
     } else {
       mwz[s] = bil_eval_df(cwz, (size_t)j * (NX - 1) + i, fx, fy);
     }
@@ -1253,6 +1262,8 @@ __device__ __forceinline__ double advect_tail_df(const Params &P, const AdvectCo
     c.sxy[m] = fma(s11 - s22, w1, s12);
     c.sxx[m] = nsxx;
   } else {
+    // (sin^2 t and sin 2t in FP64: forming them in double-float arithmetic as well measured slower,
+    // the pass then being bound by instruction issue)
     double ss, s2;
     rotation_terms(-w * dt, ss, s2);
     const df d = df_of(s22 - s11), a = df_of(s12), dss = df_of(ss), ds2 = df_of(s2);
@@ -2631,7 +2642,8 @@ int mic_batch_launch(mic_batch *b, const BatchShape *shape, unsigned char *host_
     unsigned int *ticket = reinterpret_cast<unsigned int *>(dev_table + o + jb) + nj + 1;
     int64_t grid = ntiles;
     if (persistent) {
-      const int64_t g = (int64_t)nsm * pass_occupancy(dev, p, block);
+      const int occ = pass_occupancy(dev, p, block);
+      const int64_t g = (int64_t)nsm * (tcp && occ > tc::kGridBlocksPerSM ? tc::kGridBlocksPerSM : occ);
       if (g < grid) grid = g;
     }
     if (grid < 1) grid = 1;
