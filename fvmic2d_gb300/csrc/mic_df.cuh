@@ -27,11 +27,15 @@ struct df {
 // v split into hi (its top 24 significant bits, truncated: f32_trunc) and lo (the remaining 29
 // mantissa bits rounded to 24): hi + lo = v within a relative 2^-48.  Integer work and one
 // integer-to-float conversion, no FP64 instruction.  Infinities and NaN give hi = v, lo = 0.
+// With sat, finite values beyond FP32's range saturate to +-FLT_MAX (instead of infinity), so
+// that a zero weight on such a value (a node an interpolation does not use) still contributes
+// zero, as in FP64, not 0 x inf = NaN.
+template <bool SAT = false>
 __device__ __forceinline__ df df_of(double v) {
   const long long b = dbits(v);
   const int e = (int)((b >> 52) & 0x7FF) - 1023;  // v = 1.m 2^e
   df r;
-  r.hi = f32_trunc(v);
+  r.hi = (SAT && e >= 128 && e < 1024) ? (b < 0 ? -3.402823466e38f : 3.402823466e38f) : f32_trunc(v);
   // the low 29 mantissa bits are worth 2^(e - 52) each: (m 2^-52) 2^e, exact scaling down to FP32's
   // subnormal range, where it rounds gradually
   const float m = __fmul_rn((float)(unsigned)(b & 0x1FFFFFFFLL), 0x1p-52f);
@@ -157,10 +161,10 @@ __device__ __forceinline__ double df_norm(double x, double y, double z, bool hal
 __device__ __forceinline__ df interp_w_df(const double *__restrict__ f, int NX, int i, int j, const df w[4]) {
   const size_t r0 = (size_t)j * NX, r1 = r0 + NX;
   const int i1 = next_col(i, NX);
-  df s = df_mul(w[0], df_of(__ldg(f + r0 + i)));
-  s = df_fma(w[1], df_of(__ldg(f + r1 + i)), s);
-  s = df_fma(w[2], df_of(__ldg(f + r0 + i1)), s);
-  return df_fma(w[3], df_of(__ldg(f + r1 + i1)), s);
+  df s = df_mul(w[0], df_of<true>(__ldg(f + r0 + i)));
+  s = df_fma(w[1], df_of<true>(__ldg(f + r1 + i)), s);
+  s = df_fma(w[2], df_of<true>(__ldg(f + r0 + i1)), s);
+  return df_fma(w[3], df_of<true>(__ldg(f + r1 + i1)), s);
 }
 // the four corner weights of a W4 (w00, w01, w10, w11: interp_w's order) as double-floats
 __device__ __forceinline__ void w4_df(const W4 &w, df out[4]) {

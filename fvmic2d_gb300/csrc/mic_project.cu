@@ -22,6 +22,7 @@
 // periodic) and are stored with a row stride of NX + 1.
 #include <climits>
 
+#include "mic_df.cuh"
 #include "mic_internal.cuh"
 
 using namespace mic;
@@ -318,11 +319,18 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
   if (c >= ncells) return;
   constexpr int NA = ALL2 ? 6 : 2;
   const int t = threadIdx.x;
+  // ALL2: rho (0), k (2) and Cp (4) sums in double-float arithmetic (slot f of accd); etaS (1,
+  // whose own pass measured slower in double-float), T (3) and the weights (5), which later enter
+  // differences (T against marker T in the sub-grid temperature pass), and the scalar
+  // projections in FP64 (acc)
   double acc[4][NA];
+  df accd[4][ALL2 ? 5 : 1];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
 #pragma unroll
     for (int f = 0; f < NA; ++f) acc[k][f] = 0.0;
+#pragma unroll
+    for (int f = 0; f < (ALL2 ? 5 : 1); ++f) accd[k][f] = df{0.0f, 0.0f};
   }
   if (ALL2 && !FIRST) {
 #pragma unroll
@@ -337,17 +345,19 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
 #pragma unroll
       for (int k = 0; k < 4; ++k) acc[k][1] = fma(w[k], e, acc[k][1]);
     } else if (ALL2) {
-      const double r = v.rho[m], tt = v.T[m];
+      const double tt = v.T[m];
+      const df r = df_of(v.rho[m]);
       const double e = FIRST ? 0.0 : v.eta[m];
       const int mt = v.mat[m];
-      const double kk = mat.materialkThermal[mt], cp = mat.materialCp[mt];
+      const df kk = df_of(mat.materialkThermal[mt]), cp = df_of(mat.materialCp[mt]);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        acc[k][0] = fma(w[k], r, acc[k][0]);
+        const df wk = df_of(w[k]);
+        accd[k][0] = df_fma(wk, r, accd[k][0]);
         if (!FIRST) acc[k][1] = fma(w[k], e, acc[k][1]);
-        acc[k][2] = fma(w[k], kk, acc[k][2]);
+        accd[k][2] = df_fma(wk, kk, accd[k][2]);
         acc[k][3] = fma(w[k], tt, acc[k][3]);
-        acc[k][4] = fma(w[k], cp, acc[k][4]);
+        accd[k][4] = df_fma(wk, cp, accd[k][4]);
         acc[k][5] += w[k];
       }
     }
@@ -372,7 +382,9 @@ __global__ void __launch_bounds__(128) k_partials_basic(Params P, PartialView v,
   for (int k = 0; k < 4; ++k) {
 #pragma unroll
     for (int f = 0; f < NA; ++f)
-      if ((!VISC || f == 1) && (!FIRST || f != 1)) part[(size_t)(k * NA + f) * ncells + c] = acc[k][f];
+      if ((!VISC || f == 1) && (!FIRST || f != 1))
+        part[(size_t)(k * NA + f) * ncells + c] =
+            (ALL2 && (f == 0 || f == 2 || f == 4)) ? df_to_f64(accd[k][f]) : acc[k][f];
     if (ALL2 && !FIRST) {
       part[(size_t)(24 + 2 * k) * ncells + c] = sloc[2 * k][t];
       part[(size_t)(25 + 2 * k) * ncells + c] = sloc[2 * k + 1][t];
