@@ -532,10 +532,16 @@ __device__ __forceinline__ void subgrid_stress_one(const Params &P, const Subgri
 #ifdef MIC_EXACT
   const double sdm = c.eta[m] / c.mu[m];
   double sdif = -D * dt / sdm;
-#else
-  double sdif = -D * dt * c.mu[m] / c.eta[m];
-#endif
   if (sdif < -30.0) sdif = -30.0;
+#else
+  // the exponent -D dt mu / eta in double-float arithmetic (one FP64 add to bring it back); the
+  // exponential and 1 - exp stay FP64, as the reference forms them
+  double sdif = df_to_f64(df_div(df_mul(df_neg(df_mul(df_of(D), df_of(dt))), df_of(c.mu[m])), df_of(c.eta[m])));
+  {
+    const long long sb = dbits(sdif);  // sdif < -30 as an integer test (NaN stays NaN)
+    if (sb < 0 && (sb & 0x7FFFFFFFFFFFFFFFLL) > dbits(30.0) && !nan_bits(sb)) sdif = -30.0;
+  }
+#endif
   sdif = 1.0 - exp(sdif);
   // the basic cell clamped to [0, NX-2] (subgridStressChanges.c:91-92): only a marker in the
   // last cell of a grid periodic in x moves, and its offset is formed again
@@ -780,6 +786,8 @@ __device__ __forceinline__ void update_stress_one(const Params &P, const StressC
   const double mdsxx = interp_run(nd.dsxx, P.NX, i, j, mdx, mdy);
   const double mdsyy = interp_run(nd.dsyy, P.NX, i, j, mdx, mdy);
 #else
+  // (FP64 interpolations: this pass does little FP64 work, and in double-float arithmetic it
+  // measured slower, bound by its loads' latency)
   const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, centre_cmax(P), i, j);
   const double mdsxx = interp_w(nd.dsxx, P.NX, i, j, wc);
   const double mdsyy = interp_w(nd.dsyy, P.NX, i, j, wc);
