@@ -165,17 +165,24 @@ int mic_step(mic_ctx *ctx, double dt_disp, double dt_thermal, int subgrid_stress
  * 106-179, stress -> strain rate).  Law 7 inverts it per marker: the viscosity is s* / (2 edot_II)
  * where s* is the stress at which the law's strain rate equals the marker's strain-rate
  * invariant (grain size from mic_markers_set_grain_size, pressure and temperature from the
- * marker).  mode 0 solves exactly (FP64 Newton to |rate/edot - 1| <= tol); modes 1 and 2 start
- * from the trained surrogate (4 -> 64 -> 64 -> 1 MLP; mode 1 on the CUDA cores in FP32, mode 2
- * with the hidden layer on the tensor cores in split BF16 with FP32 accumulation), take up to
- * polish_iters FP64 Newton steps and finish with the exact solve for markers still above
- * polish_tol.  With polish_tol = tol the surrogate modes converge to the same root as mode 0. */
+ * marker).  mode 0 solves exactly (FP64 Newton to |rate/edot - 1| <= tol).  Modes 1 and 2 start
+ * from the trained surrogate, a 4 -> 64 -> 64 -> 1 MLP whose hidden-layer weights are BF16:
+ * mode 1 on the CUDA cores in FP32; mode 2 with the hidden layer on the tensor cores, BF16
+ * weights against the FP32 activations as two BF16 pieces, FP32 accumulation.  They take up to
+ * polish_iters Halley steps and finish with the exact solve for markers still above polish_tol.
+ * For polish_tol >= 1e-9 the polish runs in double-float arithmetic on the FP32 pipe, with the
+ * law's terms to a relative 1e-11; below 1e-9 it runs in FP64.  With polish_tol = tol the
+ * surrogate modes converge to the same root as mode 0. */
 int mic_creep_configure(mic_ctx *ctx, int mode, double tol, int maxit, int polish_iters, double polish_tol);
 int mic_markers_set_grain_size(mic_ctx *ctx, const double *grain_size, int64_t n); /* caller order */
 int mic_creep_param_count(void);
+/* the network's parameters (mic_creep_param_count floats); set_mlp rounds the hidden layer's
+ * weights W2 to BF16 (round to nearest even), so get_mlp returns them rounded */
 int mic_creep_set_mlp(mic_ctx *ctx, const float *params, int n);
 int mic_creep_get_mlp(mic_ctx *ctx, float *params, int n);
-/* train the surrogate on the GPU from nsamples exact solves (Adam, cosine decay, batch % 128 == 0) */
+/* train the surrogate on the GPU from nsamples exact solves (Adam, cosine decay, batch % 128 == 0);
+ * quantization-aware: forward and backward passes use W2 rounded to BF16, the trained W2 is
+ * rounded at the end */
 int mic_creep_train(mic_ctx *ctx, int64_t nsamples, int batch, int steps, float lr, unsigned long long seed,
                     float *loss_history);
 /* mean-squared-loss gradient of the training kernels at params over n samples (n % 128 == 0) */
