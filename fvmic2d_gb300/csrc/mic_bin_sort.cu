@@ -221,29 +221,27 @@ struct GatherCols {
 // The gather of every column into the sorted order.  GEO: also the projection geometry of each
 // marker, from the position and cell just gathered: this kernel is bound by HBM and the
 // geometry by the FP64 pipe, so together they cost little more than the gather alone.
+// Every load comes before the first store.  The compiler cannot tell the column buffers apart,
+// so a load written after a store could not issue before it: interleaved, each thread would
+// wait out one memory latency per column (30 in a row) and the gather would be bound by latency.
+// The geometry's grid-line loads come before the stores for the same reason.
 template <bool GEO>
 __global__ void k_reorder(GatherCols g, const int *__restrict__ perm, int64_t n, Params P, GeoOut go) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int p = perm[k];
-  double x = 0.0, y = 0.0;
-  int cx = -1, cy = -1;
+  double vf[C_F64_COUNT];
+  int vi[C_I32_COUNT];
+#pragma unroll
+  for (int c = 0; c < C_F64_COUNT; ++c) vf[c] = (c < g.nf) ? __ldg(g.src_f[c] + p) : 0.0;
+#pragma unroll
+  for (int c = 0; c < C_I32_COUNT; ++c) vi[c] = __ldg(g.src_i[c] + p);
+  if (GEO) geometry_marker(P, vf[C_X], vf[C_Y], vi[C_CELLX], vi[C_CELLY], go, k);
 #pragma unroll
   for (int c = 0; c < C_F64_COUNT; ++c)
-    if (c < g.nf) {
-      const double v = g.src_f[c][p];
-      g.dst_f[c][k] = v;
-      if (c == C_X) x = v;
-      if (c == C_Y) y = v;
-    }
+    if (c < g.nf) g.dst_f[c][k] = vf[c];
 #pragma unroll
-  for (int c = 0; c < C_I32_COUNT; ++c) {
-    const int v = g.src_i[c][p];
-    g.dst_i[c][k] = v;
-    if (c == C_CELLX) cx = v;
-    if (c == C_CELLY) cy = v;
-  }
-  if (GEO) geometry_marker(P, x, y, cx, cy, go, k);
+  for (int c = 0; c < C_I32_COUNT; ++c) g.dst_i[c][k] = vi[c];
 }
 
 // perm[k] = device slot of caller marker k (k < n); slots from n on stay in place

@@ -392,6 +392,8 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
   if (m >= n) return;
   const int cx = c.cellX[m], cy = c.cellY[m];
   if (cx == -1) return;
+  // loaded ahead of the stores below (the compiler cannot tell the columns apart)
+  const double eta = c.eta[m], mu = c.mu[m];
   int i, j;
   const int NX = P.NX;
 #ifdef MIC_EXACT
@@ -431,7 +433,6 @@ __device__ __forceinline__ void strain_pressure_one(const Params &P, const Strai
   const double msxy = interp_w(nd.soxy, NX, cx, cy, wb);
   const double mdsxy = interp_w(nd.dsxy, NX, cx, cy, wb);
 #endif
-  const double eta = c.eta[m], mu = c.mu[m];
 #ifdef MIC_EXACT
   const double e11 = msxx / 2.0 / eta + mdsxx / 2.0 / dt / mu;
   const double e22 = msyy / 2.0 / eta + mdsyy / 2.0 / dt / mu;
@@ -533,7 +534,34 @@ __device__ __forceinline__ void subgrid_stress_one(const Params &P, const Subgri
   const double sdm = c.eta[m] / c.mu[m];
   double sdif = -D * dt / sdm;
   if (sdif < -30.0) sdif = -30.0;
+  sdif = 1.0 - exp(sdif);
+  // the basic cell clamped to [0, NX-2] (subgridStressChanges.c:91-92): only a marker in the
+  // last cell of a grid periodic in x moves, and its offset is formed again
+  const int bxc = min(cx, P.NX - 2);
+  const double bmdx = (bxc == cx) ? g.gx0[m] : div_sp(c.X[m] - P.x[bxc], P.hx[bxc], P.ix[bxc]);
+  (void)reuse;
+  double dsxy = interp_run(nd.soxy, P.NX, bxc, cy, bmdx, g.gy0[m]) - c.sxy[m];
+  dsxy *= sdif;
+  c.sxy[m] = c.sxy[m] + dsxy;
+  int i, j;
+  double mdx, mdy;
+  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], P.NX - 2, i, j, mdx, mdy);
+  double dsxx = interp_run(nd.soxx, P.NX, i, j, mdx, mdy) - c.sxx[m];
+  dsxx *= sdif;
+  c.sxx[m] = c.sxx[m] + dsxx;
+  double dsyy = interp_run(nd.soyy, P.NX, i, j, mdx, mdy) - c.syy[m];
+  dsyy *= sdif;
+  c.syy[m] = c.syy[m] + dsyy;
 #else
+  // every marker load before the first store: the compiler cannot tell the columns apart, and a
+  // load after a store would wait for it to issue
+  const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+  double mxy = 0.0, mxx = 0.0, myy = 0.0;
+  if (reuse) {
+    mxy = c.dxy[m];
+    mxx = c.dxx[m];
+    myy = c.dyy[m];
+  }
   // the exponent -D dt mu / eta in double-float arithmetic (one FP64 add to bring it back); the
   // exponential and 1 - exp stay FP64, as the reference forms them
   double sdif = df_to_f64(df_div(df_mul(df_neg(df_mul(df_of(D), df_of(dt))), df_of(c.mu[m])), df_of(c.eta[m])));
@@ -541,47 +569,23 @@ __device__ __forceinline__ void subgrid_stress_one(const Params &P, const Subgri
     const long long sb = dbits(sdif);  // sdif < -30 as an integer test (NaN stays NaN)
     if (sb < 0 && (sb & 0x7FFFFFFFFFFFFFFFLL) > dbits(30.0) && !nan_bits(sb)) sdif = -30.0;
   }
-#endif
   sdif = 1.0 - exp(sdif);
-  // the basic cell clamped to [0, NX-2] (subgridStressChanges.c:91-92): only a marker in the
-  // last cell of a grid periodic in x moves, and its offset is formed again
-  const int bxc = min(cx, P.NX - 2);
-  const double bmdx = (bxc == cx) ? g.gx0[m] : div_sp(c.X[m] - P.x[bxc], P.hx[bxc], P.ix[bxc]);
-#ifdef MIC_EXACT
-  (void)reuse;
-  double dsxy = interp_run(nd.soxy, P.NX, bxc, cy, bmdx, g.gy0[m]) - c.sxy[m];
-#else
-  double dsxy = (reuse ? c.dxy[m]
-                       : interp_w(nd.soxy, P.NX, bxc, cy, (bxc == cx) ? load_w4(g.w0, m) : make_w4(bmdx, g.gy0[m]))) -
-                c.sxy[m];
-#endif
-  dsxy *= sdif;
-  c.sxy[m] = c.sxy[m] + dsxy;
-  int i, j;
-#ifdef MIC_EXACT
-  double mdx, mdy;
-  centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], P.NX - 2, i, j, mdx, mdy);
-  double dsxx = interp_run(nd.soxx, P.NX, i, j, mdx, mdy) - c.sxx[m];
-  dsxx *= sdif;
-  c.sxx[m] = c.sxx[m] + dsxx;
-  double dsyy = interp_run(nd.soyy, P.NX, i, j, mdx, mdy) - c.syy[m];
-#else
-  double msxx, msyy;
-  if (reuse) {
-    msxx = c.dxx[m];
-    msyy = c.dyy[m];
-  } else {
+  if (!reuse) {
+    // the basic cell clamped to [0, NX-2] (subgridStressChanges.c:91-92): only a marker in the
+    // last cell of a grid periodic in x moves, and its offset is formed again
+    const int bxc = min(cx, P.NX - 2);
+    mxy = interp_w(nd.soxy, P.NX, bxc, cy,
+                   (bxc == cx) ? load_w4(g.w0, m) : make_w4(div_sp(c.X[m] - P.x[bxc], P.hx[bxc], P.ix[bxc]), g.gy0[m]));
+    int i, j;
     const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, P.NX - 2, i, j);
-    msxx = interp_w(nd.soxx, P.NX, i, j, wc);
-    msyy = interp_w(nd.soyy, P.NX, i, j, wc);
+    mxx = interp_w(nd.soxx, P.NX, i, j, wc);
+    myy = interp_w(nd.soyy, P.NX, i, j, wc);
   }
-  double dsxx = msxx - c.sxx[m];
-  dsxx *= sdif;
-  c.sxx[m] = c.sxx[m] + dsxx;
-  double dsyy = msyy - c.syy[m];
+  const double dsxy = (mxy - s12) * sdif, dsxx = (mxx - s11) * sdif, dsyy = (myy - s22) * sdif;
+  c.sxy[m] = s12 + dsxy;
+  c.sxx[m] = s11 + dsxx;
+  c.syy[m] = s22 + dsyy;
 #endif
-  dsyy *= sdif;
-  c.syy[m] = c.syy[m] + dsyy;
   c.dxy[m] = dsxy;
   c.dxx[m] = dsxx;
   c.dyy[m] = dsyy;
@@ -785,21 +789,24 @@ __device__ __forceinline__ void update_stress_one(const Params &P, const StressC
   centre_interp(P, cx, cy, g.flags[m], g.gx1[m], g.gy1[m], c.X[m], c.Y[m], centre_cmax(P), i, j, mdx, mdy);
   const double mdsxx = interp_run(nd.dsxx, P.NX, i, j, mdx, mdy);
   const double mdsyy = interp_run(nd.dsyy, P.NX, i, j, mdx, mdy);
+  c.sxx[m] = c.sxx[m] + mdsxx;
+  c.syy[m] = c.syy[m] + mdsyy;
+  const double mdsxy = interp_run(nd.dsxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]);
+  c.sxy[m] = c.sxy[m] + mdsxy;
 #else
   // (FP64 interpolations: this pass does little FP64 work, and in double-float arithmetic it
-  // measured slower, bound by its loads' latency)
+  // measured slower, bound by its loads' latency.)  Every load before the first store: the
+  // compiler cannot tell the columns apart, and a load after a store would wait for it to issue.
+  const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+  const W4 wb = load_w4(g.w0, m);
   const W4 wc = centre_w(P, g, m, cx, cy, c.X, c.Y, centre_cmax(P), i, j);
   const double mdsxx = interp_w(nd.dsxx, P.NX, i, j, wc);
   const double mdsyy = interp_w(nd.dsyy, P.NX, i, j, wc);
+  const double mdsxy = interp_w(nd.dsxy, P.NX, cx, cy, wb);
+  c.sxx[m] = s11 + mdsxx;
+  c.syy[m] = s22 + mdsyy;
+  c.sxy[m] = s12 + mdsxy;
 #endif
-  c.sxx[m] = c.sxx[m] + mdsxx;
-  c.syy[m] = c.syy[m] + mdsyy;
-#ifdef MIC_EXACT
-  const double mdsxy = interp_run(nd.dsxy, P.NX, cx, cy, g.gx0[m], g.gy0[m]);
-#else
-  const double mdsxy = interp_w(nd.dsxy, P.NX, cx, cy, load_w4(g.w0, m));
-#endif
-  c.sxy[m] = c.sxy[m] + mdsxy;
   if (isnan(mdsxy)) atomicAdd(&st->nan_dsxy, 1ULL);
 }
 
@@ -1250,6 +1257,10 @@ __device__ __forceinline__ void rotation_terms(double t, double &ss, double &s2)
 // sxx.
 __device__ __forceinline__ double advect_tail_df(const Params &P, const AdvectCols &c, double dt, int64_t m, double X0,
                                                  double Y0, const df *mvx, const df *mvy, const df *mwz) {
+  // the marker's stresses and strain rates are loaded before the first store: the compiler
+  // cannot tell the columns apart, and a load after a store would wait for it to issue
+  const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
+  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m], E0 = c.Eii[m];
   const df k6 = df_of(1.0 / 6.0);
   const df vxa = df_mul(df_add(df_add(mvx[0], mvx[3]), df_scale(df_add(mvx[1], mvx[2]), 2.0f)), k6);
   const df vya = df_mul(df_add(df_add(mvy[0], mvy[3]), df_scale(df_add(mvy[1], mvy[2]), 2.0f)), k6);
@@ -1260,7 +1271,6 @@ __device__ __forceinline__ double advect_tail_df(const Params &P, const AdvectCo
   c.wxy[m] = w;
   c.X[m] = fma(dt, VX, X0);
   c.Y[m] = fma(dt, VY, Y0);
-  const double s11 = c.sxx[m], s22 = c.syy[m], s12 = c.sxy[m];
   double nsxx;
   if (P.jaumann) {
     // first-order Jaumann terms with wxy1 = wxy dt (markers.c:2147-2156)
@@ -1283,11 +1293,10 @@ __device__ __forceinline__ double advect_tail_df(const Params &P, const AdvectCo
     c.sxy[m] = s12 - c12;
   }
   // accumulated strain: the invariant's square root as q / sqrt(q) by one reciprocal square root
-  const double e11 = c.exx[m], e22 = c.eyy[m], e12 = c.exy[m];
   const double q = fma(e12, e12, 0.5 * fma(e11, e11, e22 * e22));
   const long long qb = dbits(q);
   const double rq = (qb == 0 || qb == 0x7FF0000000000000LL) ? q : q * rsqrt(q);
-  c.Eii[m] = fma(dt, rq, c.Eii[m]);
+  c.Eii[m] = fma(dt, rq, E0);
   return nsxx;
 }
 #endif
@@ -1680,7 +1689,7 @@ struct YieldOp {
   }
 };
 struct StrainOp {
-  static constexpr int kMaxRegs = 80;
+  static constexpr int kMaxRegs = 64;
   using Job = StrainJob;
   using Acc = NoAcc;
   static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
@@ -1689,7 +1698,7 @@ struct StrainOp {
   static __device__ __forceinline__ void flush(const Job &, Acc) {}
 };
 struct SubgridOp {
-  static constexpr int kMaxRegs = 80;
+  static constexpr int kMaxRegs = 64;
   using Job = SubgridJob;
   using Acc = NoAcc;
   static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
@@ -1698,7 +1707,7 @@ struct SubgridOp {
   static __device__ __forceinline__ void flush(const Job &, Acc) {}
 };
 struct StressOp {
-  static constexpr int kMaxRegs = 64;
+  static constexpr int kMaxRegs = 48;
   using Job = StressJob;
   using Acc = NoAcc;
   static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &) {
@@ -1725,7 +1734,7 @@ struct SubTApplyOp {
   static __device__ __forceinline__ void flush(const Job &, Acc) {}
 };
 struct AdvectOp {
-  static constexpr int kMaxRegs = 80;
+  static constexpr int kMaxRegs = 64;
   using Job = AdvectJob;
   using Acc = long long;
   static __device__ __forceinline__ void one(const Job &J, int64_t m, Acc &a) {
@@ -1740,6 +1749,10 @@ struct AdvectOp {
 // warp stays whole through the per-marker code and the tile's closing reduction).
 // Op::kMaxRegs caps the registers (the job's fields otherwise stay in registers across the tile
 // loop and halve the resident warps of the memory-bound passes); blocks of up to 512 threads.
+// The caps were measured per pass on the 4,194,304-marker ice box: these passes wait mostly on
+// loads, and the resident warps a lower cap buys outweigh the spills it costs (the advection at
+// 64 registers spills about 0.5 KB per thread to L1 and runs 6% faster than at 80; at 48 its
+// spills grow to 1.3 KB and it is slower again).
 template <class Op>
 __global__ void __maxnreg__(Op::kMaxRegs) k_batched(const typename Op::Job *__restrict__ jobs,
                                                          const int *__restrict__ ts, int njobs, int ntiles,
