@@ -98,7 +98,7 @@ KERNEL_BYTES_LAW7 = {k: (4 + 4 + 8 + 8 + 24 + 16 + 8 + 16, 0) for k in ("k_yield
 # full launch by markers processed (profiles/fp64_mix_ice_creep_box_4m.md).  The advection reads
 # the algorithmic bytes plus the 32 B/marker of stored offsets its first RK4 stage loads instead
 # of forming them.
-KERNEL_TRAFFIC_PER_MARKER = {"k_advect": 791.1e6 / 4194304, "k_yield_tc": 423.9e6 / 4194304,
+KERNEL_TRAFFIC_PER_MARKER = {"k_advect": 792.6e6 / 4194304, "k_yield_tc": 424.5e6 / 4194304,
                              "k_yield": 421.5e6 / 4194304}
 # FP64 work per marker from the same captures (DFMA and DADD + DMUL thread instructions per
 # marker): flops with a DFMA counted twice, and the FP64 arithmetic instructions.  The exact law-7
@@ -109,7 +109,7 @@ KERNEL_TRAFFIC_PER_MARKER = {"k_advect": 791.1e6 / 4194304, "k_yield_tc": 423.9e
 _FP64_PER_MARKER = {"k_advect": (14.0, 45.0), "k_yield_tc": (5.0, 10.0), "k_yield": (65.7, 130.6)}
 KERNEL_FP64_FLOPS_PER_MARKER = {k: 2 * f + u for k, (f, u) in _FP64_PER_MARKER.items()}
 KERNEL_FP64_INST_PER_MARKER = {k: f + u for k, (f, u) in _FP64_PER_MARKER.items()}
-KERNEL_INST_PER_MARKER = {"k_advect": 3005.0, "k_yield_tc": 4008.0, "k_yield": 2885.0}
+KERNEL_INST_PER_MARKER = {"k_advect": 3070.0, "k_yield_tc": 4066.0, "k_yield": 2885.0}
 ISSUE_PEAK_GINST = 4 * 32 * 152 * 2.07  # thread instructions per second, in G (4 warp issues/SM/clk)
 FP64_PEAK_TFLOPS = 2 * 2 * 152 * 2.07e9 / 1e12  # 2 DFMA/SM/clk x 2 flops x 152 SMs x 2.07 GHz
 FP64_PEAK_GINST = 2 * 152 * 2.07  # FP64 instructions per second, in G
