@@ -194,11 +194,42 @@ __global__ void k_radix_scatter(const int *__restrict__ key_in, const int *__res
 __global__ void k_cell_start(const int *__restrict__ skey, int64_t n, int ncells, int *__restrict__ cs,
                              int *__restrict__ qs) {
   // one thread per (cell, quadrant) key q in [0, 4 ncells + 4]: the run of key q starts at the
-  // first sorted position whose key is >= q (n when there is none), found by binary search, so
-  // empty stretches of cells cost nothing extra.  cs[c] = qs[4c].
+  // first sorted position whose key is >= q (n when there is none), so empty stretches of cells
+  // cost nothing extra.  cs[c] = qs[4c].  The search starts at the position q would have with
+  // markers spread evenly over the keys and gallops outwards (steps 1, 2, 4, ...) until it
+  // brackets the answer, then bisects the bracket: a few loads, near those of the neighbouring
+  // threads, where a bisection of the whole array takes log2 n.  Invariant of the final
+  // bisection: every position below lo holds a key < q, and hi is n or holds a key >= q.
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (q > 4LL * ncells + 4) return;
+  const int64_t qmax = 4LL * ncells + 4;
+  if (q > qmax) return;
   int64_t lo = 0, hi = n;
+  if (n > 0) {
+    const int64_t g = q * n / (qmax + 1);  // in [0, n)
+    if (skey[g] < q) {
+      lo = g + 1;
+      for (int64_t step = 1;; step <<= 1) {
+        const int64_t p = g + step;
+        if (p >= n) break;  // hi stays n
+        if (skey[p] >= q) {
+          hi = p;
+          break;
+        }
+        lo = p + 1;
+      }
+    } else {
+      hi = g;
+      for (int64_t step = 1;; step <<= 1) {
+        const int64_t p = g - step;
+        if (p < 0) break;  // lo stays 0
+        if (skey[p] < q) {
+          lo = p + 1;
+          break;
+        }
+        hi = p;
+      }
+    }
+  }
   while (lo < hi) {
     const int64_t mid = (lo + hi) >> 1;
     if (skey[mid] < q)
