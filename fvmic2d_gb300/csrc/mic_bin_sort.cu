@@ -40,6 +40,23 @@ __device__ __forceinline__ int bisect_bits(const long long *__restrict__ g, int 
   return lo;
 }
 
+// The same index from a hint, the marker's cell before this binning: most markers stay in it or
+// move to a neighbour, whose intervals g[h] <= v < g[h+1] (the last index takes every v >= g[n-2])
+// are tested first; otherwise, or for a hint out of [0, n-2], the bisection.  The tested interval
+// characterises the largest i with g[i] <= v, so the result is the bisection's for any hint.
+__device__ __forceinline__ int locate_bits(const long long *__restrict__ g, int n, long long v, int hint) {
+  if (hint >= 0 && hint <= n - 2) {
+    if (__ldg(g + hint) <= v) {
+      if (hint == n - 2 || v < __ldg(g + hint + 1)) return hint;
+      // v >= g[hint + 1]
+      if (hint + 1 == n - 2 || v < __ldg(g + hint + 2)) return hint + 1;
+    } else if (hint >= 1 && __ldg(g + hint - 1) <= v) {
+      return hint - 1;  // g[hint - 1] <= v < g[hint]
+    }
+  }
+  return bisect_bits(g, n, v);
+}
+
 __global__ void k_find_cells(Params P, const double *__restrict__ X, const double *__restrict__ Y,
                              int *__restrict__ cellX, int *__restrict__ cellY, int *__restrict__ cpu,
                              int *__restrict__ key, int64_t n, Status *st) {
@@ -55,10 +72,11 @@ __global__ void k_find_cells(Params P, const double *__restrict__ X, const doubl
     const long long blx = dbits(P.LX), bly = dbits(P.LY);
     // X >= 0 && Y >= 0 && X <= LX && Y <= LY; NaN fails every test
     const bool in = ux >= 0 && uy >= 0 && ux <= blx && uy <= bly;
+    const int hx = cellX[m], hy = cellY[m];  // the cell before this binning (any value)
     int cx = -1, cy = -1, k = 4 * P.NCX * (P.NY - 1);
     if (in) {
-      cx = bisect_bits(P.xbits, P.NCX + 1, ux);  // lines 0..NCX (periodic: line NX = LX)
-      cy = bisect_bits(P.ybits, P.NY, uy);
+      cx = locate_bits(P.xbits, P.NCX + 1, ux, hx);  // lines 0..NCX (periodic: line NX = LX)
+      cy = locate_bits(P.ybits, P.NY, uy, hy);
       const int qx = ux >= nonneg_bits(P.xc[cx + 1]), qy = uy >= nonneg_bits(P.yc[cy + 1]);
       k = 4 * (cy * P.NCX + cx) + 2 * qy + qx;
     } else {
